@@ -1,0 +1,239 @@
+"""ctypes access to the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+the CPU legs of bench.py, never by the product package.  PARITY UNPINNED:
+the oracle restates the reference Fortran, which cannot be compiled here and
+ships no outputs to compare against.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+ORC_LEX = 0
+ORC_ZEBRA = 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+class MG(C.Structure):
+    _fields_ = [
+        ("nr", C.c_int), ("np", C.c_int), ("ld", C.c_int), ("nlev", C.c_int),
+        ("n1", C.c_int * 7), ("n3", C.c_int * 7),
+        ("hr", C.c_double * 7), ("hp", C.c_double * 7),
+        ("hhr", C.c_double * 7), ("hhp", C.c_double * 7),
+        ("v", _dp * 7), ("f", _dp * 7),
+        ("psic", _dp), ("psif", _dp), ("rc", _dp), ("rf", _dp), ("tempa", _dp),
+        ("tolcon", C.c_double), ("sor", C.c_double),
+        ("maxsweeps", C.c_int), ("mode", C.c_int), ("zero_scratch", C.c_int),
+        ("mgen", C.c_long),
+        ("scratch_v", _dp), ("scratch_f", _dp),
+        ("last_sweeps", C.c_int), ("last_resmax", C.c_double),
+    ]
+
+
+_PRB_FIELDS = ["An", "A", "Ap", "Bn", "B", "Bp", "Cn", "C", "Cp", "thn", "th", "thp",
+               "uel", "vel", "wel", "uelp", "velp", "welp", "urh", "vrh"]
+
+
+class PRB(C.Structure):
+    _fields_ = ([("nr", C.c_int), ("np", C.c_int), ("ld", C.c_int)] +
+                [(n, C.c_double) for n in ("dt", "dr", "dp", "Ra", "Pr", "r0", "rmax", "xx")] +
+                [(n, _dp) for n in _PRB_FIELDS] +
+                [("clamp_count", C.c_long)])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        for nm in ("orc_tdma", "orc_ptdma"):
+            getattr(L, nm).argtypes = [_dp] * 5 + [C.c_int]
+        L.orc_pdma.argtypes = [_dp] * 7 + [C.c_int]
+        L.orc_mg_init.argtypes = [C.POINTER(MG), C.c_int, C.c_int, C.c_double, C.c_double]
+        L.orc_mg_init.restype = C.c_int
+        L.orc_mg_free.argtypes = [C.POINTER(MG)]
+        L.orc_poisson.argtypes = [C.POINTER(MG), C.c_int, _dp, _dp, _dp, C.c_int, _ip]
+        L.orc_poisson.restype = C.c_int
+        L.orc_relax.argtypes = [C.POINTER(MG), C.c_int, C.c_int, C.c_int, _ip]
+        L.orc_corser.argtypes = [C.POINTER(MG), C.c_int]
+        L.orc_finer.argtypes = [C.POINTER(MG), C.c_int]
+        L.orc_prb_alloc.argtypes = [C.POINTER(PRB), C.c_int, C.c_int, C.c_int]
+        L.orc_prb_alloc.restype = C.c_int
+        L.orc_prb_free.argtypes = [C.POINTER(PRB)]
+        for nm in ("orc_cvorticity1", "orc_cvorticity", "orc_temperature1", "orc_temperature",
+                   "orc_update", "orc_rhsv", "orc_rhsu"):
+            getattr(L, nm).argtypes = [C.POINTER(PRB)]
+        L.orc_heat.argtypes = [C.POINTER(PRB), _dp, _dp]
+        L.orc_prb_step.argtypes = [C.POINTER(PRB), C.POINTER(MG), C.POINTER(MG), C.c_int, _dp, _ip]
+        L.orc_prb_step.restype = C.c_int
+        L.orc_prb_initial.argtypes = [C.POINTER(PRB), C.c_int, C.c_ulonglong, C.c_double]
+        L.orc_batch_solve.argtypes = [C.c_int, _ip, C.POINTER(C.c_longlong), _dp, _dp, C.c_int,
+                                      C.c_int, C.c_double, C.c_int, C.c_int, _ip, _dp]
+        L.orc_batch_solve.restype = C.c_int
+        for nm in ("orc_rb_sweep64",):
+            getattr(L, nm).argtypes = [C.c_int, _dp, _dp]
+        L.orc_residual64.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.orc_restrict64.argtypes = [C.c_int, _dp, _dp]
+        L.orc_prolong_add64.argtypes = [C.c_int, _dp, _dp]
+        L.orc_resnorm64.argtypes = [C.c_int, _dp, _dp]
+        L.orc_resnorm64.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"] or a.flags["F_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32
+    return a.ctypes.data_as(_ip)
+
+
+# --------------------------------------------------------------------------
+# banded solvers (copies made, the C routines destroy their inputs)
+# --------------------------------------------------------------------------
+def tdma(a, b, c, r):
+    a, b, c, r = (np.array(x, dtype=np.float64) for x in (a, b, c, r))
+    y = np.zeros_like(r)
+    lib().orc_tdma(ptr(a), ptr(b), ptr(c), ptr(y), ptr(r), len(r))
+    return y
+
+
+def ptdma(a, b, c, r):
+    a, b, c, r = (np.array(x, dtype=np.float64) for x in (a, b, c, r))
+    y = np.zeros_like(r)
+    lib().orc_ptdma(ptr(a), ptr(b), ptr(c), ptr(y), ptr(r), len(r))
+    return y
+
+
+def pdma(a, b, c, d, e, r):
+    a, b, c, d, e, r = (np.array(x, dtype=np.float64) for x in (a, b, c, d, e, r))
+    x = np.zeros_like(r)
+    lib().orc_pdma(ptr(a), ptr(b), ptr(c), ptr(d), ptr(e), ptr(r), ptr(x), len(r))
+    return x
+
+
+# --------------------------------------------------------------------------
+# PRB state
+# --------------------------------------------------------------------------
+class OraclePRB:
+    """The PRB physical state plus the two multigrid contexts (v and u)."""
+
+    def __init__(self, nr, np_, dt, Ra, Pr, r0=0.5, rmax=1.0, xx=3.0, mode=ORC_LEX,
+                 tolcon=2e-6, maxsweeps=500, sor=1.2):
+        L = lib()
+        self.s = PRB()
+        assert L.orc_prb_alloc(C.byref(self.s), nr, np_, nr + 2) == 0
+        s = self.s
+        s.dt, s.Ra, s.Pr, s.r0, s.rmax, s.xx = dt, Ra, Pr, r0, rmax, xx
+        s.dr = (rmax - r0) / nr
+        s.dp = xx / np_
+        self.mgv, self.mgu = MG(), MG()
+        for mg in (self.mgv, self.mgu):
+            st = L.orc_mg_init(C.byref(mg), nr, np_, s.dr, s.dp)
+            if st != 0:
+                raise ValueError("invalid multigrid size nr=%d np=%d" % (nr, np_))
+            mg.mode = mode
+            mg.tolcon = tolcon
+            mg.maxsweeps = maxsweeps
+            mg.sor = sor
+        self.kt = 0
+
+    @property
+    def nr(self):
+        return self.s.nr
+
+    @property
+    def np(self):
+        return self.s.np
+
+    def field(self, name) -> np.ndarray:
+        """A (ld, np+1) Fortran-ordered view of a state field (i fastest)."""
+        p = getattr(self.s, name)
+        n = self.s.ld * (self.s.np + 1)
+        flat = np.ctypeslib.as_array(p, shape=(n,))
+        return flat.reshape((self.s.np + 1, self.s.ld)).T
+
+    def initial(self, kind=1, seed=0, amp=1e-3):
+        lib().orc_prb_initial(C.byref(self.s), kind, seed, amp)
+        self.kt = 0
+
+    def step(self):
+        self.kt += 1
+        nu = np.zeros(2)
+        sw = np.zeros(2, dtype=np.int32)
+        st = lib().orc_prb_step(C.byref(self.s), C.byref(self.mgv), C.byref(self.mgu), self.kt,
+                                ptr(nu), iptr(sw))
+        return st, nu, sw
+
+    def close(self):
+        if self.s.C:
+            lib().orc_prb_free(C.byref(self.s))
+            lib().orc_mg_free(C.byref(self.mgv))
+            lib().orc_mg_free(C.byref(self.mgu))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def poisson(which, psi, psip, rhs, nr, np_, dr, dp, mode=ORC_LEX, tolcon=2e-6, maxsweeps=500):
+    """Run one orc_poisson call on (nr+2, np+1) Fortran-ordered arrays; returns
+    (status, sweeps).  psi and psip are updated in place."""
+    L = lib()
+    mg = MG()
+    assert L.orc_mg_init(C.byref(mg), nr, np_, dr, dp) == 0
+    mg.mode, mg.tolcon, mg.maxsweeps = mode, tolcon, maxsweeps
+    sw = C.c_int(0)
+    for a in (psi, psip, rhs):
+        assert a.flags["F_CONTIGUOUS"] and a.shape[0] == nr + 2
+    st = L.orc_poisson(C.byref(mg), which, ptr(psi), ptr(psip), ptr(rhs), nr + 2, C.byref(sw))
+    L.orc_mg_free(C.byref(mg))
+    return st, sw.value
+
+
+# --------------------------------------------------------------------------
+# batched Poisson
+# --------------------------------------------------------------------------
+def batch_offsets(sizes):
+    sizes = np.asarray(sizes, dtype=np.int32)
+    off = np.zeros(len(sizes), dtype=np.int64)
+    if len(sizes) > 1:
+        off[1:] = np.cumsum(sizes.astype(np.int64) ** 2)[:-1]
+    total = int(np.sum(sizes.astype(np.int64) ** 2))
+    return sizes, off, total
+
+
+def batch_solve(sizes, f, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, precision=0):
+    sizes, off, total = batch_offsets(sizes)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    assert f.size == total
+    psi = np.zeros(total)
+    cyc = np.zeros(len(sizes), dtype=np.int32)
+    rr = np.zeros(len(sizes))
+    st = lib().orc_batch_solve(len(sizes), iptr(sizes), off.ctypes.data_as(C.POINTER(C.c_longlong)),
+                               ptr(f), ptr(psi), nu1, nu2, rtol, max_cycles, precision,
+                               iptr(cyc), ptr(rr))
+    return st, psi, cyc, rr

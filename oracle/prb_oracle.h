@@ -1,0 +1,120 @@
+/*
+ * CPU oracle for the 2D periodic Rayleigh-Benard hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker used by tests/,
+ * __graft_entry__.smoke() and the cpu_baseline / reference legs of bench.py.
+ * Nothing in the product (codesthesis_dir_gb300/) links or calls it.
+ *
+ * It is a plain-C restatement of the Fortran 77 routines of
+ * monashubuntudir_velvor2dperiodicrbconvdir/velvor2dperiodicrbconv.f
+ * ("PRB" below), double precision throughout, evaluated in the
+ * reference's left-to-right operation order, compiled with
+ * -ffp-contract=off so that no multiply-add is fused.
+ *
+ * PARITY UNPINNED: the reference ships no tests, no golden vectors and no
+ * stored outputs, and no Fortran compiler exists where this was written, so
+ * the restatement is checked only by its own invariants (dense-solve
+ * agreement of the banded solvers, manufactured solutions, conduction
+ * Nusselt number 1, periodic-seam identities) and by golden fixtures it
+ * generated itself.
+ *
+ * Array convention: every field is the reference's (0:kr,1,0:kp) array,
+ * stored column-major, element (i,k) at index i + ld*k, 0 <= i <= ld-1,
+ * 0 <= k <= np.  ld is the declared leading dimension (kr+1 in the
+ * reference, 291 for kr=290); the oracle's own state uses ld = nr+2.
+ */
+#ifndef PRB_ORACLE_H
+#define PRB_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Smoother orderings of the multigrid line relaxation. */
+#define ORC_LEX   0   /* k = 1..n3 in order: the reference schedule (PRB:2113-2191) */
+#define ORC_ZEBRA 1   /* odd k lines, then even k lines: the GPU-parallel schedule */
+
+/* Status codes, shared with the GPU library. */
+#define ORC_OK        0
+#define ORC_MAXSWEEPS 1   /* the reference STOPs here (PRB:1843) */
+#define ORC_NAN       2
+#define ORC_INVALID   5
+
+/* Banded solvers, 1-based semantics of PRB:3046-3164 on 0-based arrays.
+ * Inputs are destroyed exactly as in the reference. */
+void orc_tdma(double *a, double *b, double *c, double *y, double *r, int n);
+void orc_ptdma(double *a, double *b, double *c, double *y, double *r, int n);
+void orc_pdma(double *a, double *b, double *c, double *d, double *e,
+              double *r, double *x, int n);
+
+/* Multigrid state (COMMON /backup/, /arrays/, /step/, /ints/ of PRB). */
+typedef struct {
+    int nr, np, ld, nlev;
+    int n1[7], n3[7];
+    double hr[7], hp[7], hhr[7], hhp[7];
+    double *v[7], *f[7];                 /* packed per-level storage */
+    double *psic, *psif, *rc, *rf, *tempa;
+    double tolcon;                       /* 2e-6 in PRB:2086 */
+    double sor;                          /* 1.2 in PRB:1850 */
+    int maxsweeps;                       /* 500 in PRB:1843 */
+    int mode;                            /* ORC_LEX or ORC_ZEBRA */
+    int zero_scratch;                    /* 1: zero v,f of mgen doubles per call (PRB:1822-1825) */
+    long mgen;                           /* size zeroed when zero_scratch */
+    double *scratch_v, *scratch_f;       /* the mgen-sized buffers when zero_scratch */
+    int last_sweeps;
+    double last_resmax;
+} orc_mg_t;
+
+int  orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp);
+void orc_mg_free(orc_mg_t *mg);
+/* which = 2: poisson2/relax2 (cell-centred v, pentadiagonal r-lines)
+ * which = 3: poisson3/relax3 (face u, tridiagonal r-lines)
+ * psi, psip, rhs use leading dimension ld_io.  Returns a status code;
+ * *sweeps receives the number of outer sweeps taken. */
+int  orc_poisson(orc_mg_t *mg, int which, double *psi, double *psip,
+                 const double *rhs, int ld_io, int *sweeps);
+
+/* Individual multigrid building blocks (exposed for unit tests). */
+void orc_relax(orc_mg_t *mg, int which, int nrel, int klev, int *nconv);
+void orc_corser(orc_mg_t *mg, int klev);
+void orc_finer(orc_mg_t *mg, int klev);
+
+/* Physical state of PRB (COMMON /sol1/ /sol2/ /sol3/ /num/ /val/ /radius/). */
+typedef struct {
+    int nr, np, ld;
+    double dt, dr, dp, Ra, Pr, r0, rmax, xx;
+    double *An, *A, *Ap, *Bn, *B, *Bp, *Cn, *C, *Cp;
+    double *thn, *th, *thp;
+    double *uel, *vel, *wel, *uelp, *velp, *welp;
+    double *urh, *vrh;
+    long clamp_count;                    /* "WARNING! Temp damped" count */
+} orc_prb_t;
+
+int  orc_prb_alloc(orc_prb_t *s, int nr, int np, int ld);
+void orc_prb_free(orc_prb_t *s);
+
+void orc_cvorticity1(orc_prb_t *s);
+void orc_cvorticity(orc_prb_t *s);
+void orc_temperature1(orc_prb_t *s);
+void orc_temperature(orc_prb_t *s);
+void orc_heat(const orc_prb_t *s, double *trans1, double *trans2);
+void orc_update(orc_prb_t *s);
+void orc_rhsv(orc_prb_t *s);
+void orc_rhsu(orc_prb_t *s);
+
+/* One time step of the PRB main loop (PRB:341-388 for kt=1, PRB:363-388
+ * otherwise).  nu[0], nu[1] receive httrans, httrans2; sweeps[0], sweeps[1]
+ * the outer sweep counts of the v and u solves.  Returns a status code. */
+int  orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt,
+                  double *nu, int *sweeps);
+
+/* Initial conditions.  kind 0: the reference's own deterministic profile
+ * (PRB:137-186).  kind 1: linear conduction plus seeded uniform noise of
+ * amplitude amp drawn from splitmix64(seed), periodic duplicate k=np equal
+ * to k=0.  Both set Ap..thp, uelp, velp as PRB:316-331 does. */
+void orc_prb_initial(orc_prb_t *s, int kind, unsigned long long seed, double amp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
