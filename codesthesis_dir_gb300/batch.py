@@ -1,0 +1,61 @@
+"""Batched Dirichlet Poisson solve (gb_batch_*): many independent
+nabla^2 psi = f problems on n x n vertex grids (n = 2^m + 1) of uneven size.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import lib as _L
+
+
+def offsets(sizes):
+    sizes = np.asarray(sizes, dtype=np.int64)
+    off = np.zeros(len(sizes), dtype=np.int64)
+    if len(sizes) > 1:
+        off[1:] = np.cumsum(sizes ** 2)[:-1]
+    return off, int(np.sum(sizes ** 2))
+
+
+class BatchPoisson:
+    def __init__(self, sizes, precision=_L.BATCH_FP64, nu1=2, nu2=2, rtol=1e-10, max_cycles=100):
+        L = _L.load()
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        self.offsets, self.total = offsets(self.sizes)
+        h = C.c_void_p()
+        _L.check(L.gb_batch_create(len(self.sizes), self.sizes.ctypes.data_as(C.POINTER(C.c_int)), precision,
+                                   nu1, nu2, rtol, max_cycles, C.byref(h)), "gb_batch_create")
+        self._h = h
+        self.nprob = len(self.sizes)
+
+    def solve_device(self, d_f: int, d_psi: int, stream: int = 0):
+        """d_f, d_psi: device addresses of packed float64 arrays."""
+        cyc = np.zeros(self.nprob, dtype=np.int32)
+        rr = np.zeros(self.nprob)
+        st = _L.load().gb_batch_solve_device(self._h, d_f, d_psi, cyc.ctypes.data, rr.ctypes.data, stream or None)
+        return st, cyc, rr
+
+    def solve_host(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        assert f.size == self.total
+        psi = np.zeros(self.total)
+        cyc = np.zeros(self.nprob, dtype=np.int32)
+        rr = np.zeros(self.nprob)
+        st = _L.load().gb_batch_solve_host(self._h, f.ctypes.data, psi.ctypes.data, cyc.ctypes.data,
+                                           rr.ctypes.data)
+        return st, psi, cyc, rr
+
+    def last_launches(self):
+        return int(_L.load().gb_batch_last_launches(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _L.load().gb_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

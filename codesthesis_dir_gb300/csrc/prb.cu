@@ -1,0 +1,738 @@
+// 2D periodic Rayleigh-Benard hot path on the device: compact-scheme
+// Dufort-Frankel transport of vorticity and temperature, wall boundary
+// conditions, Poisson right-hand sides, Nusselt integrals and the
+// velocity-component multigrid solves of
+// monashubuntudir_velvor2dperiodicrbconvdir/velvor2dperiodicrbconv.f (PRB).
+//
+// Numerics: every expression keeps the reference's operation order and this
+// translation unit is compiled with -fmad=false, so results are bit-identical
+// to the reference algorithm (and to the C oracle) for the same inputs.
+//
+// Layout: each field is a column-major (0:ld-1, 0:np) array, ld = nr+2, all
+// twenty fields of one instance in one allocation.  For the grids these
+// drivers use (nr <= 512, np <= 2048) an instance is at most ~170 MB and the
+// working set of a step stays in the 126 MB L2 for nr*np up to ~1.5e6.
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "banded.cuh"
+#include "gbcommon.cuh"
+#include "prb_internal.cuh"
+
+// ---------------------------------------------------------------------------
+// Matrix factors of the compact-derivative line solves (one thread).
+// ---------------------------------------------------------------------------
+__global__ void k_transport_factors(int nr, int np, double *fac_r1, double *fac_x,
+                                    double *fac_rT, double *work)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int nmax = (nr > np ? nr : np) + 2;
+    double *a = work, *b = work + nmax, *c = work + 2 * nmax;
+    // (1,4,1) on nr-1 rows: Cr and thr of Cvorticity (PRB:812-829, 855-879)
+    for (int j = 0; j < nr - 1; ++j) { a[j] = 1.0; b[j] = 4.0; c[j] = 1.0; }
+    factor_tdma(a, b, c, nr - 1, fac_r1);
+    // periodic (1,4,1) on np+1 rows: Ch, thh (PRB:834-850, 884-896, 1271-1289)
+    for (int j = 0; j < np + 1; ++j) { a[j] = 1.0; b[j] = 4.0; c[j] = 1.0; }
+    factor_ptdma(a, b, c, np + 1, fac_x);
+    // thr of temperature on nr rows with the wall rows of PRB:1249-1258
+    for (int j = 0; j < nr; ++j) { a[j] = 1.0; b[j] = 4.0; c[j] = 1.0; }
+    b[0] = 1.0; c[0] = 2.0;
+    a[nr - 1] = 2.0; b[nr - 1] = 1.0;
+    factor_tdma(a, b, c, nr, fac_rT);
+}
+
+// REAL*4 literals 2./3. and 1./6. of PRB:865-872, as the doubles they widen to.
+#define F23 ((double)(2.0f / 3.0f))
+#define F16 ((double)(1.0f / 6.0f))
+
+// Cr (tdma along r) -> A and thr at C points (tdma along r) -> An, one thread
+// per column k.  PRB:810-830 and PRB:854-880.
+__global__ void k_cvort_deriv_r(PrbDev d)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > d.np || *d.abort) return;
+    const int ld = d.ld, nr = d.nr, np = d.np;
+    const double dri = d.dri;
+    const double *C = d.f[GB_F_C], *th = d.f[GB_F_th];
+    auto rhsC = [&](int j) -> double {
+        const int i = j + 1;
+        if (i == 1)
+            return 3.0 * (C[GIX(2, k, ld)] - C[GIX(0, k, ld)]) * dri -
+                   (-1.5 * C[GIX(0, k, ld)] + 2.0 * C[GIX(1, k, ld)] - 0.5 * C[GIX(2, k, ld)]) * dri;
+        if (i == nr - 1)
+            return 3.0 * (C[GIX(nr, k, ld)] - C[GIX(nr - 2, k, ld)]) * dri -
+                   (0.5 * C[GIX(nr - 2, k, ld)] - 2.0 * C[GIX(nr - 1, k, ld)] + 1.5 * C[GIX(nr, k, ld)]) * dri;
+        return 3.0 * (C[GIX(i + 1, k, ld)] - C[GIX(i - 1, k, ld)]) * dri;
+    };
+    apply_tdma_rhs(d.fac_r1, nr - 1, d.f[GB_F_A] + GIX(1, k, ld), 1, rhsC);
+    const int ka = (k == np) ? 1 : k + 1;
+    auto rhsT = [&](int j) -> double {
+        const int i = j + 1;
+        if (i == 1)
+            return 1.5 * (th[GIX(2, k, ld)] + th[GIX(2, ka, ld)] - th[GIX(1, k, ld)] - th[GIX(1, ka, ld)]) * dri -
+                   (-F23 * (th[GIX(0, k, ld)] + th[GIX(0, ka, ld)]) + 0.5 * (th[GIX(1, k, ld)] + th[GIX(1, ka, ld)]) +
+                    F16 * (th[GIX(2, k, ld)] + th[GIX(2, ka, ld)])) * dri;
+        if (i == nr - 1)
+            return 1.5 * (th[GIX(nr, k, ld)] + th[GIX(nr, ka, ld)] - th[GIX(nr - 1, k, ld)] - th[GIX(nr - 1, ka, ld)]) * dri -
+                   (-F16 * (th[GIX(nr - 1, k, ld)] + th[GIX(nr - 1, ka, ld)]) - 0.5 * (th[GIX(nr, k, ld)] + th[GIX(nr, ka, ld)]) +
+                    F23 * (th[GIX(nr + 1, k, ld)] + th[GIX(nr + 1, ka, ld)])) * dri;
+        return 1.5 * (th[GIX(i + 1, k, ld)] + th[GIX(i + 1, ka, ld)] - th[GIX(i, k, ld)] - th[GIX(i, ka, ld)]) * dri;
+    };
+    apply_tdma_rhs(d.fac_r1, nr - 1, d.f[GB_F_An] + GIX(1, k, ld), 1, rhsT);
+}
+
+// Ch (periodic tdma along x) -> B and thh at C points -> Bn, one thread per
+// row i = 1..nr-1.  PRB:833-851 and PRB:882-897.
+__global__ void k_cvort_deriv_x(PrbDev d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > d.nr - 1 || *d.abort) return;
+    const int ld = d.ld, np = d.np;
+    const double dpi = d.dpi;
+    const double *C = d.f[GB_F_C], *th = d.f[GB_F_th];
+    auto rhsC = [&](int k) -> double {
+        if (k == np || k == 0) return 3.0 * (C[GIX(i, 1, ld)] - C[GIX(i, np - 1, ld)]) * dpi;
+        return 3.0 * (C[GIX(i, k + 1, ld)] - C[GIX(i, k - 1, ld)]) * dpi;
+    };
+    apply_ptdma_rhs(d.fac_x, np + 1, d.f[GB_F_B] + GIX(i, 0, ld), ld, rhsC);
+    auto rhsT = [&](int k) -> double {
+        const int ka = (k == np) ? 1 : k + 1;
+        return 1.5 * (th[GIX(i + 1, ka, ld)] + th[GIX(i, ka, ld)] - th[GIX(i + 1, k, ld)] - th[GIX(i, k, ld)]) * dpi;
+    };
+    apply_ptdma_rhs(d.fac_x, np + 1, d.f[GB_F_Bn] + GIX(i, 0, ld), ld, rhsT);
+}
+
+// Vorticity update, PRB:706-776 (first) / PRB:900-982 (leapfrog).
+__global__ void k_cvort_update(PrbDev d, int first)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nrow = d.nr - 1;
+    if (t >= nrow * (d.np + 1) || *d.abort) return;
+    const int i = t % nrow + 1, k = t / nrow;
+    const int ld = d.ld, np = d.np;
+    const double dri = d.dri, dpi = d.dpi, Ptl = d.Pr, dt = d.dt, Ra = d.Ra;
+    const double *C = d.f[GB_F_C], *Cp = d.f[GB_F_Cp];
+    const double *uel = d.f[GB_F_uel], *vel = d.f[GB_F_vel];
+    const int ip = i + 1;
+    int km = k - 1, ka = k + 1;
+    if (k == 0) km = np - 1;
+    if (k == np) ka = 1;
+    const double ri = 1.0;
+    const double u = (uel[GIX(i, ka, ld)] + uel[GIX(i, k, ld)]) * 0.5;
+    const double v = (vel[GIX(i, k, ld)] + vel[GIX(ip, k, ld)]) * 0.5;
+    const double Chha = (C[GIX(i, ka, ld)] + C[GIX(i, km, ld)]) * (dpi * dpi);
+    const double Ch = d.f[GB_F_B][GIX(i, k, ld)];
+    const double Crra = (C[GIX(i - 1, k, ld)] + C[GIX(i + 1, k, ld)]) * (dri * dri);
+    const double cnr = -1.0 * (dri * dri);
+    const double Cr = d.f[GB_F_A][GIX(i, k, ld)];
+    const double thh = d.f[GB_F_Bn][GIX(i, k, ld)];
+    const double cnh = (-1.0 * (dpi * dpi)) * (ri * ri);
+    double RHS1, cf1;
+    if (first) {
+        RHS1 = Crra + Chha * (ri * ri) + C[GIX(i, k, ld)] / (Ptl * dt);
+        cf1 = 1.0 / (Ptl * dt) - cnr - cnh;
+    } else {
+        RHS1 = Crra + Chha * (ri * ri) + 0.5 * C[GIX(i, k, ld)] / (Ptl * dt);
+        cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
+    }
+    const double ULT = (u * Cr + v * Ch * ri) / Ptl;
+    const double RHS2 = -Ra * thh;
+    const double cf2 = cnr + cnh;
+    const double cn = (cf2 * Cp[GIX(i, k, ld)] - ULT - RHS2 + RHS1) / cf1;
+    d.f[GB_F_Cn][GIX(i, k, ld)] = cn;
+    if (!first) d.f[GB_F_Ap][GIX(i, k, ld)] = cn;
+}
+
+// Robert filter X += 0.02 (Xn - 2X + Xp) on rows 1..imax (PRB:1041-1045,
+// PRB:1435-1440).
+__global__ void k_robert(PrbDev d, int fx, int fxn, int fxp, int imax)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= imax * (d.np + 1) || *d.abort) return;
+    const int i = t % imax + 1, k = t / imax;
+    const size_t c = GIX(i, k, d.ld);
+    double *X = d.f[fx];
+    X[c] = X[c] + 0.02 * (d.f[fxn][c] - 2.0 * X[c] + d.f[fxp][c]);
+}
+
+// thr (tdma along r, third-order wall rows) -> A, one thread per column k
+// (PRB:1244-1268).
+__global__ void k_temp_deriv_r(PrbDev d)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > d.np || *d.abort) return;
+    const int ld = d.ld, nr = d.nr;
+    const double dri = d.dri;
+    const double *th = d.f[GB_F_th];
+    auto rhs = [&](int j) -> double {
+        const int i = j + 1;
+        if (i == 1)
+            return dri * (0.533333333 * th[GIX(0, k, ld)] - 3.6 * th[GIX(1, k, ld)] +
+                          2.966666667 * th[GIX(2, k, ld)] + 0.1 * th[GIX(4, k, ld)]);
+        if (i == nr)
+            return dri * (-0.1 * th[GIX(nr - 3, k, ld)] - 2.966666667 * th[GIX(nr - 1, k, ld)] +
+                          3.6 * th[GIX(nr, k, ld)] - 0.533333333 * th[GIX(nr + 1, k, ld)]);
+        return 3.0 * (th[GIX(i + 1, k, ld)] - th[GIX(i - 1, k, ld)]) * dri;
+    };
+    apply_tdma_rhs(d.fac_rT, nr, d.f[GB_F_A] + GIX(1, k, ld), 1, rhs);
+}
+
+// thh (periodic tdma along x) -> B, one thread per row i = 1..nr (PRB:1271-1289).
+__global__ void k_temp_deriv_x(PrbDev d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > d.nr || *d.abort) return;
+    const int ld = d.ld, np = d.np;
+    const double dpi = d.dpi;
+    const double *th = d.f[GB_F_th];
+    auto rhs = [&](int k) -> double {
+        if (k == np || k == 0) return 3.0 * (th[GIX(i, 1, ld)] - th[GIX(i, np - 1, ld)]) * dpi;
+        return 3.0 * (th[GIX(i, k + 1, ld)] - th[GIX(i, k - 1, ld)]) * dpi;
+    };
+    apply_ptdma_rhs(d.fac_x, np + 1, d.f[GB_F_B] + GIX(i, 0, ld), ld, rhs);
+}
+
+// Temperature update, PRB:1142-1207 (first) / PRB:1292-1377 (Dufort-Frankel).
+__global__ void k_temp_update(PrbDev d, int first)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nr = d.nr;
+    if (t >= nr * (d.np + 1) || *d.abort) return;
+    const int i = t % nr + 1, k = t / nr;
+    const int ld = d.ld, np = d.np;
+    const double dri = d.dri, dpi = d.dpi, dt = d.dt;
+    const double *th = d.f[GB_F_th], *thp = d.f[GB_F_thp];
+    const double *uel = d.f[GB_F_uel], *vel = d.f[GB_F_vel];
+    const int im = i - 1;
+    int km = k - 1, ka = k + 1;
+    if (k == 0) km = np - 1;
+    if (k == np) ka = 1;
+    const double ri = 1.0;
+    const double u = (uel[GIX(i, k, ld)] + uel[GIX(im, k, ld)]) * 0.5;
+    const double v = (vel[GIX(i, k, ld)] + vel[GIX(i, km, ld)]) * 0.5;
+    double thrra, cnr;
+    const double thr = d.f[GB_F_A][GIX(i, k, ld)];
+    if (i == 1) {
+        thrra = (3.2 * th[GIX(i - 1, k, ld)] + 2.0 * th[GIX(i + 1, k, ld)] - 0.2 * th[GIX(i + 2, k, ld)]) * (dri * dri);
+        cnr = -2.5 * (dri * dri) + 0.5 * dri * ri;
+    } else if (i == nr) {
+        thrra = (3.2 * th[GIX(i + 1, k, ld)] + 2.0 * th[GIX(i - 1, k, ld)] - 0.2 * th[GIX(i - 2, k, ld)]) * (dri * dri);
+        cnr = -2.5 * (dri * dri) - 0.5 * dri * ri;
+    } else {
+        thrra = (th[GIX(i - 1, k, ld)] + th[GIX(i + 1, k, ld)]) * (dri * dri);
+        cnr = -1.0 * (dri * dri);
+    }
+    const double thhha = (th[GIX(i, ka, ld)] + th[GIX(i, km, ld)]) * (dpi * dpi);
+    const double thh = d.f[GB_F_B][GIX(i, k, ld)];
+    const double cnp = -(1.0 * (dpi * dpi)) * (ri * ri);
+    double RHS1, cf1;
+    if (first) {
+        RHS1 = thrra + thhha * (ri * ri) + th[GIX(i, k, ld)] / dt;
+        cf1 = 1.0 / dt - cnr - cnp;
+    } else {
+        RHS1 = thrra + thhha * (ri * ri) + 0.5 * thp[GIX(i, k, ld)] / dt;
+        cf1 = 0.5 / dt - cnr - cnp;
+    }
+    const double ULT = u * thr + v * thh * ri;
+    const double cf2 = cnr + cnp;
+    const double tn = (cf2 * thp[GIX(i, k, ld)] - ULT + RHS1) / cf1;
+    d.f[GB_F_thn][GIX(i, k, ld)] = tn;
+    if (!first) d.f[GB_F_Ap][GIX(i, k, ld)] = tn;
+}
+
+// Wall heat fluxes, PRB:1452-1500.  The per-column five-point derivatives are
+// formed in parallel; one thread then sums them in the reference's order.
+__global__ void k_heat(PrbDev d)
+{
+    extern __shared__ double sh[];
+    if (*d.abort) return;
+    const int ld = d.ld, nr = d.nr, np = d.np;
+    const double dri = d.dri, dp = d.dp;
+    const double *th = d.f[GB_F_th];
+    double *P0 = sh, *P1 = sh + (np + 1);
+    for (int k = threadIdx.x; k <= np; k += blockDim.x) {
+        P0[k] = 0.5 * dp * (-3.35238095 * th[GIX(0, k, ld)] + 4.375 * th[GIX(1, k, ld)] -
+                            1.45833333 * th[GIX(2, k, ld)] + 0.525 * th[GIX(3, k, ld)] -
+                            0.08928571 * th[GIX(4, k, ld)]) * dri;
+        P1[k] = 0.5 * dp * (-3.35238095 * th[GIX(nr + 1, k, ld)] + 4.375 * th[GIX(nr, k, ld)] -
+                            1.45833333 * th[GIX(nr - 1, k, ld)] + 0.525 * th[GIX(nr - 2, k, ld)] -
+                            0.08928571 * th[GIX(nr - 3, k, ld)]) * dri;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t1 = 0.0, t2 = 0.0;
+        for (int k = 1; k <= np; ++k) {
+            const int ka = (k == np) ? 1 : k + 1;
+            t1 = t1 + P0[k] + P0[ka];
+            t2 = t2 + P1[k] + P1[ka];
+        }
+        d.heat[0] = t1;
+        d.heat[1] = t2;
+    }
+}
+
+// rhsv (PRB:1629-1676) and rhsu (PRB:1679-1721) in one pass.
+__global__ void k_rhs(PrbDev d, int do_v, int do_u)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nr = d.nr, np = d.np, ld = d.ld;
+    if (t >= nr * (np + 1) || *d.abort) return;
+    const int i = t % nr + 1, k = t / nr;
+    const double *Cn = d.f[GB_F_Cn];
+    if (do_v) {
+        const double Cr = (Cn[GIX(i, k, ld)] - Cn[GIX(i - 1, k, ld)]) / d.dr;
+        double v;
+        if (i == 1) v = Cn[GIX(1, k, ld)] / d.dr;
+        else if (i == nr) v = -Cn[GIX(nr - 1, k, ld)] / d.dr;
+        else v = Cr;
+        d.f[GB_F_vrh][GIX(i, k, ld)] = v;
+    }
+    if (do_u && i <= nr - 1) {
+        const int km = (k == 0) ? np - 1 : k - 1;
+        const double Ch = (Cn[GIX(i, k, ld)] - Cn[GIX(i, km, ld)]) / d.dp;
+        d.f[GB_F_urh][GIX(i, k, ld)] = -Ch / 1.0;
+    }
+}
+
+// update, PRB:1557-1626.  Each thread owns one (i,k) of rows 0..nr+1; the
+// wall values it writes are only read back by the same thread.
+__global__ void k_update(PrbDev d)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nr = d.nr, np = d.np, ld = d.ld;
+    if (t >= (nr + 2) * (np + 1) || *d.abort) return;
+    const int i = t % (nr + 2), k = t / (nr + 2);
+    double *const *f = d.f;
+    const double dr = d.dr;
+    const size_t c = GIX(i, k, ld);
+    if (i == 0) {
+        f[GB_F_Bn][c] = -(3.0 * f[GB_F_wel][GIX(1, k, ld)] - f[GB_F_wel][GIX(2, k, ld)] / 3.0) / dr;
+        f[GB_F_Cn][c] = (3.0 * f[GB_F_vel][GIX(1, k, ld)] - f[GB_F_vel][GIX(2, k, ld)] / 3.0) / dr;
+        f[GB_F_thn][c] = 0.0;
+    } else if (i == nr) {
+        f[GB_F_Bn][c] = -(f[GB_F_wel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_wel][GIX(nr, k, ld)]) / dr;
+        f[GB_F_Cn][c] = (f[GB_F_vel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_vel][GIX(nr, k, ld)]) / dr;
+    } else if (i == nr + 1) {
+        f[GB_F_thn][c] = 1.0;
+    }
+    f[GB_F_Cp][c] = f[GB_F_C][c];
+    f[GB_F_C][c] = f[GB_F_Cn][c];
+    f[GB_F_thp][c] = f[GB_F_th][c];
+    double tn = f[GB_F_thn][c];
+    unsigned long long clamped = 0;
+    if (tn > 1.0) { tn = 0.99; clamped++; }
+    if (tn < 0.0) { tn = 0.01; clamped++; }
+    f[GB_F_thn][c] = tn;
+    f[GB_F_th][c] = tn;
+    if (clamped) atomicAdd(d.clamps, clamped);
+}
+
+// Per-step bookkeeping for graph-replayed steps: copies the step's Nusselt
+// numbers and sweep counts into the history slot given by *d.step_index.
+__global__ void k_record(PrbDev d, double rmr0, double xx)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int s = *d.step_index;
+    if (s < d.hist_cap) {
+        d.nu_hist[2 * s + 0] = d.heat[0] * rmr0 / xx;   // PRB:386-388
+        d.nu_hist[2 * s + 1] = d.heat[1] * rmr0 / xx;
+        d.sweep_hist[2 * s + 0] = d.mg_status[1];
+        d.sweep_hist[2 * s + 1] = d.mg_status[3];
+    }
+    if (!*d.abort) *d.step_index = s + 1;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static const int TPB = 256;
+
+int prb_launch_cvorticity(gb_prb *h, int first, cudaStream_t s)
+{
+    PrbDev &d = h->dev;
+    k_cvort_deriv_r<<<gb_ceil_div(d.np + 1, 64), 64, 0, s>>>(d);
+    k_cvort_deriv_x<<<gb_ceil_div(d.nr - 1, 64), 64, 0, s>>>(d);
+    k_cvort_update<<<gb_ceil_div((size_t)(d.nr - 1) * (d.np + 1), TPB), TPB, 0, s>>>(d, first);
+    if (!first)
+        k_robert<<<gb_ceil_div((size_t)(d.nr - 1) * (d.np + 1), TPB), TPB, 0, s>>>(d, GB_F_C, GB_F_Cn, GB_F_Cp, d.nr - 1);
+    h->launches += first ? 3 : 4;
+    return GB_OK;
+}
+
+int prb_launch_temperature(gb_prb *h, int first, cudaStream_t s)
+{
+    PrbDev &d = h->dev;
+    k_temp_deriv_r<<<gb_ceil_div(d.np + 1, 64), 64, 0, s>>>(d);
+    k_temp_deriv_x<<<gb_ceil_div(d.nr, 64), 64, 0, s>>>(d);
+    k_temp_update<<<gb_ceil_div((size_t)d.nr * (d.np + 1), TPB), TPB, 0, s>>>(d, first);
+    if (!first)
+        k_robert<<<gb_ceil_div((size_t)d.nr * (d.np + 1), TPB), TPB, 0, s>>>(d, GB_F_th, GB_F_thn, GB_F_thp, d.nr);
+    h->launches += first ? 3 : 4;
+    return GB_OK;
+}
+
+int prb_launch_heat(gb_prb *h, cudaStream_t s)
+{
+    PrbDev &d = h->dev;
+    k_heat<<<1, 256, 2 * (d.np + 1) * sizeof(double), s>>>(d);
+    h->launches += 1;
+    return GB_OK;
+}
+
+int prb_launch_rhs(gb_prb *h, int do_v, int do_u, cudaStream_t s)
+{
+    PrbDev &d = h->dev;
+    k_rhs<<<gb_ceil_div((size_t)d.nr * (d.np + 1), TPB), TPB, 0, s>>>(d, do_v, do_u);
+    h->launches += 1;
+    return GB_OK;
+}
+
+int prb_launch_update(gb_prb *h, cudaStream_t s)
+{
+    PrbDev &d = h->dev;
+    k_update<<<gb_ceil_div((size_t)(d.nr + 2) * (d.np + 1), TPB), TPB, 0, s>>>(d);
+    h->launches += 1;
+    return GB_OK;
+}
+
+int prb_launch_record(gb_prb *h, cudaStream_t s)
+{
+    k_record<<<1, 32, 0, s>>>(h->dev, h->p.rmax - h->p.r0, h->p.xx);
+    h->launches += 1;
+    return GB_OK;
+}
+
+extern "C" void gb_prb_default_params(gb_prb_params *p, int nr, int np)
+{
+    memset(p, 0, sizeof(*p));
+    p->nr = nr;
+    p->np = np;
+    p->dt = 1e-7;
+    p->r0 = 0.5;
+    p->rmax = 1.0;
+    p->xx = 3.0;
+    p->Ra = 1e7;
+    p->Pr = 0.71;
+    p->tolcon = 2e-6;
+    p->sor = 1.2;
+    p->maxsweeps = 500;
+    p->smoother = GB_SMOOTHER_LEX;
+}
+
+// Level count of poissoninit (PRB:1744-1767).
+int prb_mg_levels(int nr)
+{
+    int nlev = 0, itest = nr, itest2 = nr;
+    for (int i = 2; i <= 8; ++i) {
+        itest = itest / 2;
+        if (itest * 2 - itest2 == 0) {
+            if (itest2 >= 4) nlev = nlev + 1;
+            itest2 = itest;
+        } else {
+            break;
+        }
+    }
+    if (nlev >= 5) nlev = 4;
+    return nlev;
+}
+
+int prb_refresh_scalars(gb_prb *h)
+{
+    PrbDev &d = h->dev;
+    d.dt = h->p.dt;
+    d.Ra = h->p.Ra;
+    d.Pr = h->p.Pr;
+    d.dr = h->dr_set != 0.0 ? h->dr_set : (h->p.rmax - h->p.r0) / (double)h->p.nr;
+    d.dp = h->dp_set != 0.0 ? h->dp_set : h->p.xx / (double)h->p.np;
+    d.dri = 1.0 / d.dr;
+    d.dpi = 1.0 / d.dp;
+    return GB_OK;
+}
+
+// dr, dp: grid spacings to use verbatim (the Fortran caller's /num/ values),
+// or 0 to derive them as the reference main program does (PRB:127-133).
+int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out, int *nlev_out)
+{
+    if (!p || !out) { gb_set_error("gb_prb_create: null argument"); return GB_ERR_INVALID; }
+    *out = nullptr;
+    const int nr = p->nr, np = p->np;
+    const int nlev = prb_mg_levels(nr);
+    if (nlev_out) *nlev_out = nlev;
+    if (nr < 4 || np < 4 || (np & 1) || nlev < 1 || nr > 8192 || np > 65536) {
+        gb_set_error("gb_prb_create: unsupported grid nr=%d np=%d (need even nr >= 4 with >= 1 multigrid level, even np >= 4)", nr, np);
+        return GB_ERR_INVALID;
+    }
+    gb_prb *h = new gb_prb();
+    h->p = *p;
+    h->nlev = nlev;
+    PrbDev &d = h->dev;
+    d.nr = nr;
+    d.np = np;
+    d.ld = nr + 2;
+    h->fsz = (size_t)d.ld * (size_t)(np + 1);
+    h->dr_set = dr;
+    h->dp_set = dp;
+    prb_refresh_scalars(h);
+    cudaError_t e = cudaMalloc(&h->fields, sizeof(double) * h->fsz * GB_F_COUNT);
+    if (e != cudaSuccess) { gb_set_error("gb_prb_create: %s", cudaGetErrorString(e)); delete h; return GB_ERR_ALLOC; }
+    cudaMemset(h->fields, 0, sizeof(double) * h->fsz * GB_F_COUNT);
+    for (int f = 0; f < GB_F_COUNT; ++f) d.f[f] = h->fields + (size_t)f * h->fsz;
+    // factors + small device state
+    const size_t nfac = 3 * (size_t)nr + (6 * (size_t)(np + 1) + 3) + 3 * (size_t)nr + 3 * ((size_t)(nr > np ? nr : np) + 2);
+    e = cudaMalloc(&h->factors, sizeof(double) * nfac);
+    if (e != cudaSuccess) { gb_prb_destroy(h); gb_set_error("gb_prb_create: factor alloc"); return GB_ERR_ALLOC; }
+    double *fr1 = h->factors;
+    double *fx = fr1 + 3 * (size_t)nr;
+    double *frT = fx + 6 * (size_t)(np + 1) + 3;
+    double *work = frT + 3 * (size_t)nr;
+    d.fac_r1 = fr1;
+    d.fac_x = fx;
+    d.fac_rT = frT;
+    k_transport_factors<<<1, 1>>>(nr, np, fr1, fx, frT, work);
+    e = cudaMalloc(&h->small, 4096);
+    if (e != cudaSuccess) { gb_prb_destroy(h); gb_set_error("gb_prb_create: small alloc"); return GB_ERR_ALLOC; }
+    cudaMemset(h->small, 0, 4096);
+    char *sm = (char *)h->small;
+    d.heat = (double *)(sm + 0);
+    d.clamps = (unsigned long long *)(sm + 64);
+    d.abort = (int *)(sm + 128);
+    d.step_index = (int *)(sm + 192);
+    d.mg_status = (int *)(sm + 256);  // [status_v, sweeps_v, status_u, sweeps_u]
+    d.mg_resmax = (double *)(sm + 320);
+    d.nu_hist = nullptr;
+    d.sweep_hist = nullptr;
+    d.hist_cap = 0;
+    int st = prb_mg_create(h);
+    if (st != GB_OK) { gb_prb_destroy(h); return st; }
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { gb_prb_destroy(h); gb_set_error("gb_prb_create: stream"); return GB_ERR_CUDA; }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { gb_set_error("gb_prb_create: %s", cudaGetErrorString(e)); gb_prb_destroy(h); return GB_ERR_CUDA; }
+    *out = h;
+    return GB_OK;
+}
+
+extern "C" int gb_prb_create(const gb_prb_params *p, gb_prb **out, int *nlev_out)
+{
+    return gb_prb_create_ex(p, 0.0, 0.0, out, nlev_out);
+}
+
+extern "C" int gb_prb_destroy(gb_prb *h)
+{
+    if (!h) return GB_OK;
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph_exec1) cudaGraphExecDestroy(h->graph_exec1);
+    prb_mg_destroy(h);
+    cudaFree(h->fields);
+    cudaFree(h->factors);
+    cudaFree(h->small);
+    cudaFree(h->hist);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GB_OK;
+}
+
+extern "C" int gb_prb_set_field(gb_prb *h, int field, const double *host, int ld)
+{
+    if (!h || !host || field < 0 || field >= GB_F_COUNT || ld < h->dev.nr + 2) {
+        gb_set_error("gb_prb_set_field: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    GB_CUDA_TRY(cudaMemcpy2DAsync(h->dev.f[field], sizeof(double) * h->dev.ld, host, sizeof(double) * (size_t)ld,
+                                  sizeof(double) * (h->dev.nr + 2), h->dev.np + 1, cudaMemcpyHostToDevice, h->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_prb_get_field(gb_prb *h, int field, double *host, int ld)
+{
+    if (!h || !host || field < 0 || field >= GB_F_COUNT || ld < h->dev.nr + 2) {
+        gb_set_error("gb_prb_get_field: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    GB_CUDA_TRY(cudaMemcpy2DAsync(host, sizeof(double) * (size_t)ld, h->dev.f[field], sizeof(double) * h->dev.ld,
+                                  sizeof(double) * (h->dev.nr + 2), h->dev.np + 1, cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_prb_field_device_ptr(gb_prb *h, int field, double **dev, int *ld)
+{
+    if (!h || field < 0 || field >= GB_F_COUNT) { gb_set_error("gb_prb_field_device_ptr: invalid argument"); return GB_ERR_INVALID; }
+    if (dev) *dev = h->dev.f[field];
+    if (ld) *ld = h->dev.ld;
+    return GB_OK;
+}
+
+// Clears the step-abort flag so that an earlier failed solve does not make
+// the kernels of an individual routine call skip their work.
+static void prb_begin(gb_prb *h)
+{
+    prb_refresh_scalars(h);
+    cudaMemsetAsync(h->dev.abort, 0, sizeof(int), h->stream);
+}
+
+static int prb_sync(gb_prb *h, const char *what)
+{
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { gb_set_error("%s: %s", what, cudaGetErrorString(e)); return GB_ERR_CUDA; }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { gb_set_error("%s: %s", what, cudaGetErrorString(e)); return GB_ERR_CUDA; }
+    return GB_OK;
+}
+
+extern "C" int gb_prb_cvorticity(gb_prb *h, int first)
+{
+    if (!h) return GB_ERR_INVALID;
+    prb_begin(h);
+    prb_launch_cvorticity(h, first, h->stream);
+    return prb_sync(h, "gb_prb_cvorticity");
+}
+
+extern "C" int gb_prb_temperature(gb_prb *h, int first)
+{
+    if (!h) return GB_ERR_INVALID;
+    prb_begin(h);
+    prb_launch_temperature(h, first, h->stream);
+    return prb_sync(h, "gb_prb_temperature");
+}
+
+extern "C" int gb_prb_heat(gb_prb *h, double *trans1, double *trans2)
+{
+    if (!h) return GB_ERR_INVALID;
+    prb_begin(h);
+    prb_launch_heat(h, h->stream);
+    double t[2];
+    GB_CUDA_TRY(cudaMemcpyAsync(t, h->dev.heat, sizeof(t), cudaMemcpyDeviceToHost, h->stream));
+    int st = prb_sync(h, "gb_prb_heat");
+    if (st != GB_OK) return st;
+    if (trans1) *trans1 = t[0];
+    if (trans2) *trans2 = t[1];
+    return GB_OK;
+}
+
+extern "C" int gb_prb_rhsv(gb_prb *h)
+{
+    if (!h) return GB_ERR_INVALID;
+    prb_begin(h);
+    prb_launch_rhs(h, 1, 0, h->stream);
+    return prb_sync(h, "gb_prb_rhsv");
+}
+
+extern "C" int gb_prb_rhsu(gb_prb *h)
+{
+    if (!h) return GB_ERR_INVALID;
+    prb_begin(h);
+    prb_launch_rhs(h, 0, 1, h->stream);
+    return prb_sync(h, "gb_prb_rhsu");
+}
+
+extern "C" int gb_prb_update(gb_prb *h, long long *clamps)
+{
+    if (!h) return GB_ERR_INVALID;
+    prb_begin(h);
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.clamps, 0, sizeof(unsigned long long), h->stream));
+    prb_launch_update(h, h->stream);
+    unsigned long long c = 0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&c, h->dev.clamps, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    int st = prb_sync(h, "gb_prb_update");
+    if (clamps) *clamps = (long long)c;
+    return st;
+}
+
+extern "C" int gb_prb_poisson(gb_prb *h, int which, int *sweeps)
+{
+    if (!h || (which != 2 && which != 3)) { gb_set_error("gb_prb_poisson: which must be 2 or 3"); return GB_ERR_INVALID; }
+    prb_begin(h);
+    prb_launch_mg(h, which == 2 ? 1 : 0, which == 3 ? 1 : 0, h->stream);
+    int stat[4];
+    GB_CUDA_TRY(cudaMemcpyAsync(stat, h->dev.mg_status, sizeof(stat), cudaMemcpyDeviceToHost, h->stream));
+    int st = prb_sync(h, "gb_prb_poisson");
+    if (st != GB_OK) return st;
+    const int o = (which == 2) ? 0 : 2;
+    if (sweeps) *sweeps = stat[o + 1];
+    return stat[o];
+}
+
+// One step's launches on stream s (v and u solves in one multigrid launch).
+static void prb_enqueue_step(gb_prb *h, int first, cudaStream_t s)
+{
+    prb_launch_cvorticity(h, first, s);
+    prb_launch_temperature(h, first, s);
+    prb_launch_heat(h, s);
+    prb_launch_rhs(h, 1, 1, s);
+    prb_launch_mg(h, 1, 1, s);
+    prb_launch_update(h, s);
+    prb_launch_record(h, s);
+}
+
+static int prb_build_graph(gb_prb *h, int first, cudaGraphExec_t *exec)
+{
+    cudaGraph_t g;
+    GB_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long l0 = h->launches;
+    prb_enqueue_step(h, first, h->stream);
+    h->launches_per_step = h->launches - l0;
+    h->launches = l0;
+    GB_CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+    GB_CUDA_TRY(cudaGraphInstantiate(exec, g, 0));
+    cudaGraphDestroy(g);
+    return GB_OK;
+}
+
+extern "C" int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *sweeps)
+{
+    if (!h || nsteps < 0 || kt0 < 1) { gb_set_error("gb_prb_step: invalid argument"); return GB_ERR_INVALID; }
+    if (nsteps == 0) return GB_OK;
+    prb_refresh_scalars(h);
+    PrbDev &d = h->dev;
+    if (h->hist_cap < nsteps) {
+        cudaFree(h->hist);
+        h->hist = nullptr;
+        GB_CUDA_TRY(cudaMalloc(&h->hist, (sizeof(double) * 2 + sizeof(int) * 2) * (size_t)nsteps));
+        h->hist_cap = nsteps;
+        if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+        if (h->graph_exec1) { cudaGraphExecDestroy(h->graph_exec1); h->graph_exec1 = nullptr; }
+    }
+    d.nu_hist = (double *)h->hist;
+    d.sweep_hist = (int *)((double *)h->hist + 2 * (size_t)h->hist_cap);
+    d.hist_cap = h->hist_cap;
+    // scalars are baked into the graph: rebuild when they change
+    if (memcmp(&h->graph_scalars, &h->p, sizeof(gb_prb_params)) != 0) {
+        if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+        if (h->graph_exec1) { cudaGraphExecDestroy(h->graph_exec1); h->graph_exec1 = nullptr; }
+        h->graph_scalars = h->p;
+    }
+    GB_CUDA_TRY(cudaMemsetAsync(d.abort, 0, sizeof(int), h->stream));
+    GB_CUDA_TRY(cudaMemsetAsync(d.step_index, 0, sizeof(int), h->stream));
+    GB_CUDA_TRY(cudaMemsetAsync(d.clamps, 0, sizeof(unsigned long long), h->stream));
+    int st;
+    for (int s = 0; s < nsteps; ++s) {
+        const int first = (kt0 + s == 1);
+        cudaGraphExec_t *ex = first ? &h->graph_exec1 : &h->graph_exec;
+        if (!*ex && (st = prb_build_graph(h, first, ex)) != GB_OK) return st;
+        GB_CUDA_TRY(cudaGraphLaunch(*ex, h->stream));
+        h->launches += h->launches_per_step;
+    }
+    int info[2];
+    GB_CUDA_TRY(cudaMemcpyAsync(info, d.step_index, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(info + 1, d.abort, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double> nuh(2 * (size_t)nsteps);
+    std::vector<int> swh(2 * (size_t)nsteps);
+    GB_CUDA_TRY(cudaMemcpyAsync(nuh.data(), d.nu_hist, sizeof(double) * 2 * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(swh.data(), d.sweep_hist, sizeof(int) * 2 * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    int stat[4];
+    GB_CUDA_TRY(cudaMemcpyAsync(stat, d.mg_status, sizeof(stat), cudaMemcpyDeviceToHost, h->stream));
+    st = prb_sync(h, "gb_prb_step");
+    if (st != GB_OK) return st;
+    if (nu) memcpy(nu, nuh.data(), sizeof(double) * 2 * nsteps);
+    if (sweeps) memcpy(sweeps, swh.data(), sizeof(int) * 2 * nsteps);
+    h->steps_done = info[0];
+    if (info[1]) {
+        gb_set_error("gb_prb_step: multigrid failed at step %d (status v=%d u=%d)", kt0 + info[0], stat[0], stat[2]);
+        return stat[0] != GB_OK ? stat[0] : stat[2];
+    }
+    return GB_OK;
+}

@@ -1,0 +1,75 @@
+// Internal state of a device-resident 2D periodic Rayleigh-Benard instance.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "gbcommon.cuh"
+
+#define PRB_MAXLEV 7
+
+// One multigrid level of one equation (COMMON /step/, /ints/ of
+// velvor2dperiodicrbconv.f:1810-1814, plus the packed v/f slots).
+struct MgLevel {
+    int n1, n3;
+    double hhri, hhpi;   // 1/hr^2, 1/hp^2 of the level
+    const double *fac;   // factored line matrix (pdma for v, tdma for u)
+    double *v, *f;       // packed (n1+1)*(n3+1) solution / right-hand side
+};
+
+// Device description of one Poisson solve (poisson2 or poisson3).
+struct MgEq {
+    int which;           // 2: v (cell centred, pentadiagonal), 3: u (face, tridiagonal)
+    int nr, np, ld, nlev, mode, maxsweeps;
+    double tolcon, sor;
+    MgLevel lev[PRB_MAXLEV];
+    double *psic, *psif, *rc, *rf, *tempa;   // COMMON /arrays/ (per equation)
+    double *psi, *psip;                      // solution and previous level (in/out)
+    const double *rhs;
+    int *status;         // [0] status, [1] sweeps
+    double *resmax;      // last level-1 residual max norm
+    int *abort;          // set on failure: later kernels of a step skip their work
+};
+
+struct PrbDev {
+    int nr, np, ld;
+    double dt, Ra, Pr, dr, dp, dri, dpi;
+    double *f[GB_F_COUNT];
+    const double *fac_r1, *fac_x, *fac_rT;
+    double *heat;
+    unsigned long long *clamps;
+    int *abort, *step_index, *mg_status;
+    double *mg_resmax;
+    double *nu_hist;
+    int *sweep_hist;
+    int hist_cap;
+};
+
+struct gb_prb {
+    gb_prb_params p;
+    int nlev;
+    size_t fsz;
+    double dr_set = 0.0, dp_set = 0.0;  // verbatim spacings of a Fortran caller, 0 = derived
+    PrbDev dev;
+    double *fields = nullptr;
+    double *factors = nullptr;
+    void *small = nullptr;
+    void *hist = nullptr;
+    int hist_cap = 0;
+    // multigrid
+    MgEq eq_host[2];          // [0] v (which 2), [1] u (which 3)
+    MgEq *eq_dev = nullptr;   // device copy, 2 entries
+    double *mg_pool = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph_exec = nullptr, graph_exec1 = nullptr;
+    gb_prb_params graph_scalars;
+    long long launches = 0, launches_per_step = 0;
+    int steps_done = 0;
+};
+
+int prb_mg_levels(int nr);
+int prb_mg_create(gb_prb *h);
+void prb_mg_destroy(gb_prb *h);
+int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s);
+int prb_refresh_scalars(gb_prb *h);

@@ -1,0 +1,131 @@
+"""ctypes binding of the CUDA library libgb300conv.so (the C ABI declared in
+include/gb300_convection.h).
+
+The library is the only compute path: there is no CPU fallback.  Loading
+fails with an exception when the shared object is missing or was not built
+for this machine, and every call that returns a status other than GB_OK
+raises GBError carrying the library's own error text.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgb300conv.so")
+
+GB_OK = 0
+GB_MAXSWEEPS = 1
+GB_NAN = 2
+GB_TIMEOUT = 3
+GB_ERR_ALLOC = 4
+GB_ERR_INVALID = 5
+GB_ERR_CUDA = 6
+
+STATUS_NAMES = {0: "GB_OK", 1: "GB_MAXSWEEPS", 2: "GB_NAN", 3: "GB_TIMEOUT", 4: "GB_ERR_ALLOC",
+                5: "GB_ERR_INVALID", 6: "GB_ERR_CUDA"}
+
+FIELDS = ["An", "A", "Ap", "Bn", "B", "Bp", "Cn", "C", "Cp", "thn", "th", "thp",
+          "uel", "vel", "wel", "uelp", "velp", "welp", "urh", "vrh"]
+FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
+
+SMOOTHER_LEX = 0
+SMOOTHER_ZEBRA = 1
+BATCH_FP64 = 0
+BATCH_MIXED = 1
+
+
+class GBError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__("%s: %s (%s)" % (what, STATUS_NAMES.get(status, status), last_error()))
+        self.status = status
+
+
+class PrbParams(C.Structure):
+    _fields_ = [("nr", C.c_int), ("np", C.c_int),
+                ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
+                ("Ra", C.c_double), ("Pr", C.c_double), ("tolcon", C.c_double), ("sor", C.c_double),
+                ("maxsweeps", C.c_int), ("smoother", C.c_int)]
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+_lib = None
+
+# (name, restype, argtypes) of every exported entry point of the C ABI.
+SIGNATURES = [
+    ("gb_last_error", C.c_char_p, []),
+    ("gb_version", C.c_char_p, []),
+    ("gb_prb_default_params", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
+    ("gb_prb_create", C.c_int, [C.POINTER(PrbParams), C.POINTER(_vp), _ip]),
+    ("gb_prb_destroy", C.c_int, [_vp]),
+    ("gb_prb_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
+    ("gb_prb_get_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
+    ("gb_prb_field_device_ptr", C.c_int, [_vp, C.c_int, C.POINTER(_vp), _ip]),
+    ("gb_prb_cvorticity", C.c_int, [_vp, C.c_int]),
+    ("gb_prb_temperature", C.c_int, [_vp, C.c_int]),
+    ("gb_prb_heat", C.c_int, [_vp, _dp, _dp]),
+    ("gb_prb_rhsv", C.c_int, [_vp]),
+    ("gb_prb_rhsu", C.c_int, [_vp]),
+    ("gb_prb_poisson", C.c_int, [_vp, C.c_int, _ip]),
+    ("gb_prb_update", C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    ("gb_prb_step", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    ("gb_prb_bind_bounds", None, [C.c_int, C.c_int]),
+    ("gb_prb_bind_smoother", None, [C.c_int]),
+    ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),
+    ("gb_prb_bind_common", None, [_vp, _vp, _vp, _vp, _vp]),
+    ("gb_prb_last_status", C.c_int, []),
+    ("gb_prb_last_sweeps", C.c_int, []),
+    ("poissoninit_", None, [_ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    ("poisson2_", None, [_vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    ("poisson3_", None, [_vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    ("cvorticity1_", None, []),
+    ("cvorticity_", None, []),
+    ("temperature1_", None, []),
+    ("temperature_", None, []),
+    ("heat_", None, [_dp, _dp]),
+    ("update_", None, []),
+    ("rhsv_", None, [_vp]),
+    ("rhsu_", None, [_vp]),
+    ("gb_tdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
+    ("gb_ptdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
+    ("gb_pdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
+    ("gb_batch_create", C.c_int, [C.c_int, _ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(_vp)]),
+    ("gb_batch_destroy", C.c_int, [_vp]),
+    ("gb_batch_total_points", C.c_longlong, [_vp]),
+    ("gb_batch_solve_device", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    ("gb_batch_solve_host", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("gb_batch_last_launches", C.c_longlong, [_vp]),
+]
+
+
+def load(path: str = LIB_PATH):
+    """Loads the library (once).  Raises if it is missing: there is no
+    fallback implementation."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libgb300conv.so not found at %s; run __graft_entry__.build() "
+                           "(nvcc, sm_103a) first" % path)
+    L = C.CDLL(path, mode=C.RTLD_GLOBAL)
+    for name, res, args in SIGNATURES:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    if _lib is None:
+        return ""
+    s = _lib.gb_last_error()
+    return s.decode() if s else ""
+
+
+def check(status: int, what: str):
+    if status != GB_OK:
+        raise GBError(status, what)
+    return status

@@ -1,0 +1,118 @@
+"""Host-side mirror of the 2D periodic Rayleigh-Benard driver's subroutines
+(monashubuntudir_velvor2dperiodicrbconvdir/velvor2dperiodicrbconv.f).
+
+`PRB` owns one device-resident instance (gb_prb_create) and exposes the
+reference's routines under their reference names, with the reference's
+argument meaning: cvorticity1/cvorticity (PRB:584, 786), temperature1/
+temperature (PRB:1056, 1220), heat (PRB:1452), rhsv/rhsu (PRB:1629, 1679),
+poisson2/poisson3 (PRB:1796, 1930), update (PRB:1557).  Fields move in and
+out as Fortran-ordered (ld, np+1) float64 arrays with ld >= nr+2.
+
+Error behaviour: where the reference STOPs after 500 multigrid sweeps
+(PRB:1843), poisson2/poisson3 raise GBError with status GB_MAXSWEEPS.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import lib as _L
+
+
+class PRB:
+    def __init__(self, nr, np_, dt=1e-7, r0=0.5, rmax=1.0, xx=3.0, Ra=1e7, Pr=0.71,
+                 tolcon=2e-6, sor=1.2, maxsweeps=500, smoother=_L.SMOOTHER_LEX):
+        L = _L.load()
+        p = _L.PrbParams()
+        L.gb_prb_default_params(C.byref(p), nr, np_)
+        p.dt, p.r0, p.rmax, p.xx, p.Ra, p.Pr = dt, r0, rmax, xx, Ra, Pr
+        p.tolcon, p.sor, p.maxsweeps, p.smoother = tolcon, sor, maxsweeps, smoother
+        self.params = p
+        h = C.c_void_p()
+        nlev = C.c_int(0)
+        _L.check(L.gb_prb_create(C.byref(p), C.byref(h), C.byref(nlev)), "gb_prb_create")
+        self._h = h
+        self.nlev = nlev.value
+        self.nr, self.np = nr, np_
+        self.ld = nr + 2
+        self.kt = 0
+
+    # -- fields ------------------------------------------------------------
+    def set(self, name, arr):
+        a = np.asfortranarray(arr, dtype=np.float64)
+        assert a.shape[0] >= self.nr + 2 and a.shape[1] >= self.np + 1, a.shape
+        _L.check(_L.load().gb_prb_set_field(self._h, _L.FIELD_ID[name], a.ctypes.data, a.shape[0]),
+                 "set_field " + name)
+
+    def get(self, name, ld=None):
+        ld = ld or self.ld
+        a = np.zeros((ld, self.np + 1), order="F")
+        _L.check(_L.load().gb_prb_get_field(self._h, _L.FIELD_ID[name], a.ctypes.data, ld), "get_field " + name)
+        return a
+
+    def device_ptr(self, name):
+        p = C.c_void_p()
+        ld = C.c_int()
+        _L.check(_L.load().gb_prb_field_device_ptr(self._h, _L.FIELD_ID[name], C.byref(p), C.byref(ld)), "ptr")
+        return p.value, ld.value
+
+    # -- the reference routines ---------------------------------------------
+    def cvorticity1(self):
+        _L.check(_L.load().gb_prb_cvorticity(self._h, 1), "cvorticity1")
+
+    def cvorticity(self):
+        _L.check(_L.load().gb_prb_cvorticity(self._h, 0), "cvorticity")
+
+    def temperature1(self):
+        _L.check(_L.load().gb_prb_temperature(self._h, 1), "temperature1")
+
+    def temperature(self):
+        _L.check(_L.load().gb_prb_temperature(self._h, 0), "temperature")
+
+    def heat(self):
+        t1, t2 = C.c_double(), C.c_double()
+        _L.check(_L.load().gb_prb_heat(self._h, C.byref(t1), C.byref(t2)), "heat")
+        return t1.value, t2.value
+
+    def rhsv(self):
+        _L.check(_L.load().gb_prb_rhsv(self._h), "rhsv")
+
+    def rhsu(self):
+        _L.check(_L.load().gb_prb_rhsu(self._h), "rhsu")
+
+    def poisson2(self):
+        sw = C.c_int()
+        _L.check(_L.load().gb_prb_poisson(self._h, 2, C.byref(sw)), "poisson2")
+        return sw.value
+
+    def poisson3(self):
+        sw = C.c_int()
+        _L.check(_L.load().gb_prb_poisson(self._h, 3, C.byref(sw)), "poisson3")
+        return sw.value
+
+    def update(self):
+        c = C.c_longlong()
+        _L.check(_L.load().gb_prb_update(self._h, C.byref(c)), "update")
+        return c.value
+
+    def step(self, nsteps=1):
+        """nsteps steps of the main loop from a CUDA graph; returns
+        (nu[nsteps,2], sweeps[nsteps,2])."""
+        nu = np.zeros((nsteps, 2))
+        sw = np.zeros((nsteps, 2), dtype=np.int32)
+        st = _L.load().gb_prb_step(self._h, self.kt + 1, nsteps, nu.ctypes.data, sw.ctypes.data)
+        _L.check(st, "step")
+        self.kt += nsteps
+        return nu, sw
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _L.load().gb_prb_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,214 @@
+/*
+ * gb300_convection.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * time-step hot path of the rotating-annulus / Rayleigh-Benard convection
+ * codes (martin-king/codesthesis_dir, Fortran 77).
+ *
+ * Library: codesthesis_dir_gb300/_build/libgb300conv.so
+ *
+ * Three layers, all plain C types (pointers, sizes, status codes):
+ *
+ *  1. gfortran-compatible drop-in symbols (lower case, trailing underscore,
+ *     every argument by reference) for the subroutines of
+ *     monashubuntudir_velvor2dperiodicrbconvdir/velvor2dperiodicrbconv.f
+ *     (abbreviated PRB below).  They read and write the caller's COMMON
+ *     blocks /sol1/ /sol2/ /sol3/ /num/ /val/ /radius/ exactly as the
+ *     Fortran routines they replace, and run the work on the GPU.
+ *
+ *  2. A context API (gb_prb_*) that keeps every field resident on the
+ *     device between calls and steps; the drop-in symbols are thin wrappers
+ *     over one process-wide context.
+ *
+ *  3. The batched Poisson solver (gb_batch_*) and batched banded line
+ *     solvers (gb_*_batch).
+ *
+ * Status codes: every entry point that can fail returns (or stores) one of
+ * GB_OK ... GB_ERR_*; no entry point exits the process (the reference STOPs
+ * after 500 multigrid sweeps, PRB:1843; here that is GB_MAXSWEEPS).
+ * gb_last_error() gives a one-line description of the last failure on the
+ * calling thread.
+ */
+#ifndef GB300_CONVECTION_H
+#define GB300_CONVECTION_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define GB_OK            0
+#define GB_MAXSWEEPS     1  /* multigrid hit its sweep limit (PRB:1843 STOPs there) */
+#define GB_NAN           2  /* a NaN residual was seen */
+#define GB_TIMEOUT       3  /* a bounded device-side wait gave up */
+#define GB_ERR_ALLOC     4  /* device or host allocation failed */
+#define GB_ERR_INVALID   5  /* invalid argument or grid size */
+#define GB_ERR_CUDA      6  /* CUDA runtime error (see gb_last_error) */
+
+const char *gb_last_error(void);
+/* Library build string: version, target architecture, build flags. */
+const char *gb_version(void);
+
+/* ---------------------------------------------------------------- fields */
+/* Field identifiers, in the order of the reference COMMON blocks
+ * /sol1/ An,A,Ap,Bn,B,Bp,Cn,C,Cp  /sol2/ thn,th,thp
+ * /sol3/ uel,vel,wel,uelp,velp,welp (PRB:69-71), plus the two Poisson
+ * right-hand sides urh, vrh of the main program (PRB:60). */
+enum gb_prb_field {
+    GB_F_An = 0, GB_F_A, GB_F_Ap, GB_F_Bn, GB_F_B, GB_F_Bp, GB_F_Cn, GB_F_C, GB_F_Cp,
+    GB_F_thn, GB_F_th, GB_F_thp,
+    GB_F_uel, GB_F_vel, GB_F_wel, GB_F_uelp, GB_F_velp, GB_F_welp,
+    GB_F_urh, GB_F_vrh,
+    GB_F_COUNT
+};
+
+/* Smoother orderings of the multigrid line relaxation. */
+#define GB_SMOOTHER_LEX   0  /* k = 1..n3 in order: the reference schedule (PRB:2113-2191) */
+#define GB_SMOOTHER_ZEBRA 1  /* odd k lines, then even k lines (all lines of a colour in parallel) */
+
+/* Parameters of one 2D periodic Rayleigh-Benard instance.  Defaults that
+ * reproduce the reference: tolcon 2e-6 (PRB:2086), sor 1.2 (PRB:1850),
+ * maxsweeps 500 (PRB:1843), xx 3 (PRB:132), smoother LEX. */
+typedef struct gb_prb_params {
+    int nr;          /* intervals in r (wall-normal), even, >= 4 */
+    int np;          /* intervals in the periodic direction, even, >= 4 */
+    double dt, r0, rmax, xx;
+    double Ra, Pr;   /* Rayleigh and Prandtl numbers (COMMON /val/ Ra, Ptl) */
+    double tolcon;   /* absolute max-norm residual tolerance of the level-1 relax */
+    double sor;      /* over-relaxation factor of the whole-cycle change */
+    int maxsweeps;   /* outer multigrid sweep limit */
+    int smoother;    /* GB_SMOOTHER_LEX or GB_SMOOTHER_ZEBRA */
+} gb_prb_params;
+
+/* Fills *p with the reference defaults for an nr x np grid
+ * (dt 1e-7, r0 0.5, rmax 1, xx 3, Ra 1e7, Pr 0.71: the PRB input deck). */
+void gb_prb_default_params(gb_prb_params *p, int nr, int np);
+
+typedef struct gb_prb gb_prb;
+
+/* Creates a device-resident instance on the current CUDA device; every
+ * field starts at zero.  Replaces poissoninit (PRB:1724) plus the COMMON
+ * storage of the fields.  nlev_out (may be NULL) receives the multigrid
+ * level count, computed as poissoninit does (halvings of nr, capped at 4). */
+int gb_prb_create(const gb_prb_params *p, gb_prb **out, int *nlev_out);
+int gb_prb_destroy(gb_prb *h);
+
+/* Host <-> device copies of one field.  host is a column-major
+ * (0:ld-1, 0:np) array with leading dimension ld >= nr+2 (ld = kr+1 = 291
+ * for the reference's COMMON arrays); rows 0..nr+1 and columns 0..np move. */
+int gb_prb_set_field(gb_prb *h, int field, const double *host, int ld);
+int gb_prb_get_field(gb_prb *h, int field, double *host, int ld);
+/* Device pointer and leading dimension of a field (for zero-copy callers). */
+int gb_prb_field_device_ptr(gb_prb *h, int field, double **dev, int *ld);
+
+/* One routine each, on the device-resident fields (replacing PRB:584-1721):
+ *   first != 0: Cvorticity1 / temperature1 (forward first step),
+ *   first == 0: Cvorticity / temperature (leapfrog + Robert filter). */
+int gb_prb_cvorticity(gb_prb *h, int first);        /* PRB:584-778, PRB:786-1048 */
+int gb_prb_temperature(gb_prb *h, int first);       /* PRB:1056-1212, PRB:1220-1443 */
+int gb_prb_heat(gb_prb *h, double *trans1, double *trans2); /* PRB:1452-1500 */
+int gb_prb_rhsv(gb_prb *h);                         /* PRB:1629-1676 */
+int gb_prb_rhsu(gb_prb *h);                         /* PRB:1679-1721 */
+/* which = 2: poisson2 on vel/velp/vrh (PRB:1796-1927);
+ * which = 3: poisson3 on uel/uelp/urh (PRB:1930-2059).
+ * Returns GB_OK, GB_MAXSWEEPS or GB_NAN; *sweeps gets the sweep count. */
+int gb_prb_poisson(gb_prb *h, int which, int *sweeps);
+/* update (PRB:1557-1626); *clamps (may be NULL) gets the number of
+ * temperatures clamped, each of which the reference reports with
+ * 'WARNING! Temp damped'. */
+int gb_prb_update(gb_prb *h, long long *clamps);
+
+/* nsteps steps of the main loop (PRB:341-388 for kt == 1, PRB:363-388
+ * after), kt0 the index of the first.  nu (2*nsteps, may be NULL) receives
+ * httrans, httrans2 per step (Nu = trans*(rmax-r0)/xx, PRB:386-388);
+ * sweeps (2*nsteps, may be NULL) the v and u sweep counts.  The steps run
+ * from a CUDA graph; the v and u solves run concurrently (the reference's
+ * OpenMP sections, PRB:370-380). */
+int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *sweeps);
+
+/* ------------------------------------------- gfortran-compatible drop-in */
+/* These read/write the caller's COMMON blocks (declared by the Fortran main
+ * program; the library carries weak definitions of the reference's sizes,
+ * kr = 290, kp = 1610).  Other PARAMETER bounds: call gb_prb_bind_bounds
+ * (or set GB300_PRB_KR / GB300_PRB_KP) before poissoninit_. */
+void gb_prb_bind_bounds(int kr, int kp);
+/* The smoother used by the drop-in symbols (default LEX, the reference's). */
+void gb_prb_bind_smoother(int smoother);
+/* Tolerance and sweep limit of the drop-in solves (default 2e-6, 500:
+ * PRB:2086, PRB:1843). */
+void gb_prb_bind_tolerance(double tolcon, int maxsweeps);
+/* Explicit COMMON storage for callers that are not a Fortran main program:
+ * sol1 = 9 arrays An..Cp, sol2 = thn,th,thp, sol3 = uel..welp, each
+ * (kr+1)*(kp+1) doubles; num = {double dt,dr,dz,dp; int nr,nz,np};
+ * val = {Ra, Re, Ptl, Gr}.  Pass NULLs to return to the weak symbols. */
+void gb_prb_bind_common(double *sol1, double *sol2, double *sol3, void *num, double *val);
+
+void poissoninit_(int *nr, int *nz, int *np, double *dr, double *dz, double *dp,
+                  int *nlev);                                   /* PRB:1724 */
+void poisson2_(double *psi, double *psip, double *rhs, int *nr, int *nz, int *np,
+               double *dr, double *dz, double *dp, int *nlev);  /* PRB:1796 */
+void poisson3_(double *psi, double *psip, double *rhs, int *nr, int *nz, int *np,
+               double *dr, double *dz, double *dp, int *nlev);  /* PRB:1930 */
+void cvorticity1_(void);                                        /* PRB:584 */
+void cvorticity_(void);                                         /* PRB:786 */
+void temperature1_(void);                                       /* PRB:1056 */
+void temperature_(void);                                        /* PRB:1220 */
+void heat_(double *trans1, double *trans2);                     /* PRB:1452 */
+void update_(void);                                             /* PRB:1557 */
+void rhsv_(double *vrh);                                        /* PRB:1629 */
+void rhsu_(double *urh);                                        /* PRB:1679 */
+/* Status and sweep count of the last drop-in call on this process. */
+int gb_prb_last_status(void);
+int gb_prb_last_sweeps(void);
+
+/* ------------------------------------------------ batched banded solvers */
+/* nlines independent systems with the same n; line l's element j sits at
+ * base + l*line_stride + j*elem_stride in each array.  Device pointers.
+ * The matrices may differ per line.  Inputs are preserved (unlike the
+ * reference, whose solvers overwrite them).
+ *   tdma:  PRB:3046-3064 (a sub, b diag, c super)
+ *   ptdma: PRB:3066-3116 (periodic: a(1) couples to x(n), c(n) to x(1))
+ *   pdma:  PRB:3118-3164 (a 2nd sub, b sub, c diag, d super, e 2nd super) */
+int gb_tdma_batch(const double *a, const double *b, const double *c, const double *r,
+                  double *y, int n, int nlines, long long line_stride, long long elem_stride,
+                  void *stream);
+int gb_ptdma_batch(const double *a, const double *b, const double *c, const double *r,
+                   double *y, int n, int nlines, long long line_stride, long long elem_stride,
+                   void *stream);
+int gb_pdma_batch(const double *a, const double *b, const double *c, const double *d,
+                  const double *e, const double *r, double *x, int n, int nlines,
+                  long long line_stride, long long elem_stride, void *stream);
+
+/* ------------------------------------------------- batched Poisson solve */
+/* Many independent Dirichlet problems nabla^2 psi = f on n x n vertex grids
+ * (n = 2^m + 1, 3 <= n <= 8193) of the unit square, psi = 0 on the boundary;
+ * V(nu1,nu2) red-black Gauss-Seidel cycles with full-weighting restriction
+ * and bilinear prolongation (the transfer operators of rotann2.f:755-854)
+ * until ||f - A psi||_2 <= rtol ||f||_2.  Problem p occupies n[p]^2
+ * doubles, row-major, starting at offset sum_{q<p} n[q]^2. */
+#define GB_BATCH_FP64  0   /* plain FP64 V-cycles */
+#define GB_BATCH_MIXED 1   /* FP32 inner V-cycle inside FP64 defect correction */
+
+typedef struct gb_batch gb_batch;
+
+int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
+                    int max_cycles, gb_batch **out);
+int gb_batch_destroy(gb_batch *b);
+/* Total doubles of the packed f / psi arrays. */
+long long gb_batch_total_points(const gb_batch *b);
+/* Device-resident solve: d_f, d_psi device pointers (packed).  cycles and
+ * relres (host, nprob each, may be NULL) receive per-problem V-cycle counts
+ * and final relative residuals.  Returns GB_OK or GB_MAXSWEEPS. */
+int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_psi, int *cycles,
+                          double *relres, void *stream);
+/* Host-buffer solve (copies in and out inside the call). */
+int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi, int *cycles,
+                        double *relres);
+/* Number of kernel launches the last solve issued. */
+long long gb_batch_last_launches(const gb_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GB300_CONVECTION_H */

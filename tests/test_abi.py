@@ -1,0 +1,68 @@
+"""The C-ABI library builds (nvcc cross-compiles without a GPU), loads, and
+exports every entry point include/gb300_convection.h declares; the Python
+binding's signature table covers the same set.  No compute call is made."""
+import os
+import re
+import subprocess
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gb300_convection.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", "", src)
+    src = "\n".join(l for l in src.splitlines() if not l.strip().startswith("#"))
+    names = set()
+    for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(([^;{}]*)\)\s*;", src):
+        name = m.group(1)
+        if name in ("sizeof",):
+            continue
+        names.add(name)
+    return names
+
+
+def test_header_declares_the_dropin_symbols():
+    names = declared_functions()
+    for sym in ("poissoninit_", "poisson2_", "poisson3_", "cvorticity1_", "cvorticity_", "temperature1_",
+                "temperature_", "heat_", "update_", "rhsv_", "rhsu_"):
+        assert sym in names, sym
+
+
+def test_library_exports_every_declared_symbol(gblib):
+    from codesthesis_dir_gb300 import lib
+    out = subprocess.run(["nm", "-D", "--defined-only", lib.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    missing = sorted(declared_functions() - exported)
+    assert not missing, missing
+
+
+def test_binding_table_matches_header(gblib):
+    from codesthesis_dir_gb300 import lib
+    bound = {n for n, _, _ in lib.SIGNATURES}
+    assert declared_functions() == bound, declared_functions() ^ bound
+
+
+def test_library_reports_version_without_gpu(gblib):
+    v = gblib.gb_version().decode()
+    assert "sm_103a" in v
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    import importlib
+
+    from codesthesis_dir_gb300 import lib
+    mod = importlib.reload(lib)
+    try:
+        mod._lib = None
+        try:
+            mod.load(str(tmp_path / "nope.so"))
+        except RuntimeError as e:
+            assert "not found" in str(e)
+        else:
+            raise AssertionError("load() of a missing library must raise")
+    finally:
+        mod._lib = None
+        mod.load()

@@ -1,0 +1,92 @@
+"""The gfortran-compatible drop-in symbols (poissoninit_, cvorticity1_, ...,
+update_) driven the way the Fortran main program drives them (PRB:341-388),
+with COMMON blocks laid out as gfortran lays them out, against the oracle.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from prb_helpers import STATE_FIELDS
+
+pytestmark = pytest.mark.gpu
+
+
+class Num(C.Structure):  # COMMON /num/ dt,dr,dz,dp,nr,nz,np
+    _fields_ = [("dt", C.c_double), ("dr", C.c_double), ("dz", C.c_double), ("dp", C.c_double),
+                ("nr", C.c_int), ("nz", C.c_int), ("np", C.c_int)]
+
+
+SOL1 = ["An", "A", "Ap", "Bn", "B", "Bp", "Cn", "C", "Cp"]
+SOL2 = ["thn", "th", "thp"]
+SOL3 = ["uel", "vel", "wel", "uelp", "velp", "welp"]
+
+
+@pytest.mark.parametrize("kr,kp", [(20, 40), (290, 1610)], ids=["small-bounds", "reference-bounds"])
+def test_dropin_main_loop(oracle, gblib, kr, kp):
+    L = gblib
+    nr, np_ = 16, 32
+    dt, Ra, Pr, r0, rmax, xx = 1e-4, 1e5, 0.71, 0.5, 1.0, 3.0
+    o = oracle.OraclePRB(nr, np_, dt, Ra, Pr, r0=r0, rmax=rmax, xx=xx)
+    o.initial(0, 0, 0.0)  # the reference's own initial profile (PRB:137-186)
+    S = (kr + 1) * (kp + 1)
+    sol1 = np.zeros(9 * S)
+    sol2 = np.zeros(3 * S)
+    sol3 = np.zeros(6 * S)
+    vrh = np.zeros(S)
+    urh = np.zeros(S)
+
+    def view(block, idx):
+        return block[idx * S:(idx + 1) * S].reshape((kp + 1, kr + 1)).T
+
+    for blk, names in ((sol1, SOL1), (sol2, SOL2), (sol3, SOL3)):
+        for i, nm in enumerate(names):
+            view(blk, i)[: nr + 2, : np_ + 1] = np.array(o.field(nm))
+    num = Num(dt, o.s.dr, 0.0, o.s.dp, nr, 1, np_)
+    val = np.array([Ra, 0.0, Pr, 0.0])
+    L.gb_prb_bind_bounds(kr, kp)
+    L.gb_prb_bind_tolerance(2e-6, 500)
+    L.gb_prb_bind_smoother(0)
+    L.gb_prb_bind_common(sol1.ctypes.data, sol2.ctypes.data, sol3.ctypes.data, C.addressof(num), val.ctypes.data)
+    try:
+        nrc, nzc, npc = C.c_int(nr), C.c_int(1), C.c_int(np_)
+        drc, dzc, dpc = C.c_double(o.s.dr), C.c_double(0.0), C.c_double(o.s.dp)
+        nlev = C.c_int(0)
+        L.poissoninit_(C.byref(nrc), C.byref(nzc), C.byref(npc), C.byref(drc), C.byref(dzc), C.byref(dpc),
+                       C.byref(nlev))
+        assert nlev.value == o.mgv.nlev
+        vel, velp = view(sol3, 1), view(sol3, 4)
+        uel, uelp = view(sol3, 0), view(sol3, 3)
+        # the three arrays are views into the COMMON storage: pass raw addresses
+        a_vel = sol3.ctypes.data + 1 * S * 8
+        a_velp = sol3.ctypes.data + 4 * S * 8
+        a_uel = sol3.ctypes.data + 0 * S * 8
+        a_uelp = sol3.ctypes.data + 3 * S * 8
+        for kt in range(1, 5):
+            st, nu, sw = o.step()
+            assert st == 0
+            (L.cvorticity1_ if kt == 1 else L.cvorticity_)()
+            (L.temperature1_ if kt == 1 else L.temperature_)()
+            t1, t2 = C.c_double(), C.c_double()
+            L.heat_(C.byref(t1), C.byref(t2))
+            L.rhsv_(vrh.ctypes.data)
+            L.poisson2_(a_vel, a_velp, vrh.ctypes.data, C.byref(nrc), C.byref(nzc), C.byref(npc), C.byref(drc),
+                        C.byref(dzc), C.byref(dpc), C.byref(nlev))
+            assert L.gb_prb_last_status() == 0
+            assert L.gb_prb_last_sweeps() == sw[0]
+            L.rhsu_(urh.ctypes.data)
+            L.poisson3_(a_uel, a_uelp, urh.ctypes.data, C.byref(nrc), C.byref(nzc), C.byref(npc), C.byref(drc),
+                        C.byref(dzc), C.byref(dpc), C.byref(nlev))
+            assert L.gb_prb_last_status() == 0
+            assert L.gb_prb_last_sweeps() == sw[1]
+            L.update_()
+            assert L.gb_prb_last_status() == 0
+            assert t1.value * (rmax - r0) / xx == nu[0]
+            for blk, names in ((sol1, SOL1), (sol2, SOL2), (sol3, SOL3)):
+                for i, nm in enumerate(names):
+                    np.testing.assert_array_equal(view(blk, i)[: nr + 2, : np_ + 1], np.array(o.field(nm)),
+                                                  err_msg="%s kt=%d" % (nm, kt))
+        del vel, velp, uel, uelp
+    finally:
+        L.gb_prb_bind_common(None, None, None, None, None)
+        L.gb_prb_bind_bounds(290, 1610)
