@@ -1,0 +1,389 @@
+"""Benchmark of the batched Poisson workload: 256 independent Dirichlet
+problems nabla^2 psi = -omega on n x n vertex grids, n drawn uniformly from
+{65, 129, 257, 513} (seed 0), omega a seeded zero-mean unit-variance Gaussian
+random field with squared-exponential correlation length 0.05 of the domain
+(synthetic: FFT-filtered white noise), solved by V(2,2) red-black cycles to
+relative residual 1e-10.
+
+One step = one solve of the whole batch.  value = cell-updates/s (interior
+points x V-cycles / second) of the FP32-inner / FP64-defect-correction path,
+with inputs resident in HBM; the plain FP64 path is timed the same way and
+reported beside it; e2e repeats the mixed solve through the C ABI's host-
+buffer entry point (gb_batch_solve_host) with pinned host arrays, so the
+host->device copy of f and the device->host copy of psi are inside the
+timed region.
+
+--impl reference times the CPU restatement of the same algorithm (oracle/,
+OpenMP over problems, all host threads) on a bounded sample of problems.
+Under torchrun each rank solves its own batch of 256 problems (weak scaling,
+no collective on the data path); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZES = (65, 129, 257, 513)
+NPROB = 256
+CORR = 0.05
+RTOL = 1e-10
+METRIC = "cell-updates/s (batched Poisson, V(2,2) to rel. residual 1e-10)"
+
+
+def workload_sizes(seed=0, nprob=NPROB):
+    return np.random.default_rng(seed).choice(SIZES, size=nprob).astype(np.int32)
+
+
+def grf(rng, n, corr=CORR):
+    """Zero-mean, unit-variance Gaussian random field on an n x n grid with
+    squared-exponential covariance of correlation length corr (FFT filtering
+    of white noise), boundary zeroed."""
+    w = rng.standard_normal((n, n))
+    k = np.fft.fftfreq(n, d=1.0 / (n - 1))
+    kx, ky = np.meshgrid(k, k, indexing="ij")
+    filt = np.exp(-((2 * np.pi) ** 2) * (kx ** 2 + ky ** 2) * corr ** 2 / 4.0)
+    g = np.real(np.fft.ifft2(np.fft.fft2(w) * filt))
+    g = (g - g.mean()) / g.std()
+    g[0, :] = g[-1, :] = g[:, 0] = g[:, -1] = 0.0
+    return g
+
+
+def workload_rhs(sizes, seed):
+    rng = np.random.default_rng(1000 + seed)
+    return np.concatenate([-grf(rng, int(n)).ravel() for n in sizes])
+
+
+def interior(sizes):
+    s = np.asarray(sizes, dtype=np.int64)
+    return (s - 2) ** 2
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while
+    the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                mhz.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_reference(sizes_all, seed, budget_s=20.0, threads=None):
+    """The oracle (CPU restatement, OpenMP over problems) on a bounded
+    sample of the workload: problems are added until about budget_s of work
+    is measured.  Returns (cell-updates/s, sample description, threads,
+    per-problem psi for the sample, sample sizes, sample rhs)."""
+    from oracle import oracle as O
+    O.build()
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    # one of each size first, then the workload's own order
+    order = []
+    for n in SIZES:
+        order.append(int(np.nonzero(sizes_all == n)[0][0]))
+    order += [i for i in range(len(sizes_all)) if i not in order]
+    done_cu, done_t, used = 0.0, 0.0, []
+    psi_s, f_s = [], []
+    rng_f = workload_rhs(sizes_all, seed)
+    offs = np.concatenate([[0], np.cumsum(sizes_all.astype(np.int64) ** 2)])
+    i = 0
+    while i < len(order) and done_t < budget_s:
+        chunk = order[i:i + max(threads, 4)]
+        i += len(chunk)
+        sz = [int(sizes_all[j]) for j in chunk]
+        f = np.concatenate([rng_f[offs[j]:offs[j + 1]] for j in chunk])
+        t0 = time.perf_counter()
+        st, psi, cyc, rr = O.batch_solve(sz, f, precision=0, rtol=RTOL)
+        dt = time.perf_counter() - t0
+        done_t += dt
+        done_cu += float(np.sum(interior(sz) * cyc))
+        used += chunk
+        psi_s.append(psi)
+        f_s.append(f)
+    sample = "%d of the %d problems (sizes %s), FP64 oracle, %d OpenMP threads, %.1f s" % (
+        len(used), len(sizes_all), sorted(set(int(sizes_all[j]) for j in used)), threads, done_t)
+    return done_cu / done_t, sample, threads, used, np.concatenate(psi_s)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    sizes = workload_sizes(0)
+    vals = []
+    threads = os.cpu_count()
+    sample = ""
+    for s in range(args.warmup + args.steps):
+        v, sample, threads, _, _ = cpu_reference(sizes, 0, budget_s=max(2.0, args.ref_budget), threads=threads)
+        if s >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batched Poisson: 256 problems, n in {65,129,257,513}, V(2,2) RB-GS, rtol 1e-10",
+                   "nprob": NPROB, "sizes": list(SIZES), "rtol": RTOL},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="time only the mixed solve (for profiler launch lists); prints no JSON line")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from codesthesis_dir_gb300 import lib
+    from codesthesis_dir_gb300.batch import BatchPoisson
+    lib.load()
+
+    sizes = workload_sizes(0)
+    f_host = workload_rhs(sizes, rank)
+    total = int(np.sum(sizes.astype(np.int64) ** 2))
+    cu_per_cycle = interior(sizes)
+    d_f = torch.from_numpy(f_host).cuda()
+    d_psi = torch.zeros(total, dtype=torch.float64, device="cuda")
+    d_psi64 = torch.zeros(total, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(solver, d_out, steps, warmup):
+        for _ in range(warmup):
+            st, cyc, rr = solver.solve_device(d_f.data_ptr(), d_out.data_ptr(), sh)
+            assert st == 0, lib.last_error()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cu, launches = 0.0, 0
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        for _ in range(steps):
+            st, cyc, rr = solver.solve_device(d_f.data_ptr(), d_out.data_ptr(), sh)
+            assert st == 0, lib.last_error()
+            cu += float(np.sum(cu_per_cycle * cyc))
+            launches += solver.last_launches()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms, cu], dtype=torch.float64, device="cuda")
+            mx = t.clone()
+            dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+            dist.all_reduce(t, op=dist.ReduceOp.SUM)
+            ms, cu = float(mx[0]), float(t[1])
+        return ms, cu, cyc, rr, launches
+
+    mixed = BatchPoisson(sizes, precision=lib.BATCH_MIXED, rtol=RTOL)
+    if args.mixed_only:
+        ms, cu, cyc, rr, launches = timed(mixed, d_psi, args.steps, args.warmup)
+        if rank == 0:
+            print("mixed-only: %.3f ms/step, %.4g cell-updates/s, cycles %s, launches %d" % (
+                ms / max(1, args.steps), cu / (ms / 1e3) if ms > 0 else 0.0, np.bincount(cyc), launches))
+        return 0
+    fp64 = BatchPoisson(sizes, precision=lib.BATCH_FP64, rtol=RTOL)
+
+    # plain FP64 arm
+    ms64, cu64, cyc64, rr64, _ = timed(fp64, d_psi64, args.steps, args.warmup)
+    # mixed arm (headline), clocks sampled during it, smoothing kernel profiled
+    L = lib.load()
+    L.gb_batch_profile(mixed._h, 1)
+    timed(mixed, d_psi, 0, args.warmup)
+    L.gb_batch_profile_read(mixed._h, None, None, None, 1)
+    with ClockSampler(local) as clk:
+        ms, cu, cyc, rr, launches = timed(mixed, d_psi, args.steps, 0)
+    import ctypes as C
+    pms, pl, pb = C.c_double(), C.c_longlong(), C.c_double()
+    L.gb_batch_profile_read(mixed._h, C.byref(pms), C.byref(pl), C.byref(pb), 1)
+    L.gb_batch_profile(mixed._h, 0)
+
+    # accuracy of the mixed path against the FP64 path (bit-identical to the FP64 oracle)
+    a, b = d_psi.cpu().numpy(), d_psi64.cpu().numpy()
+    field_err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    # e2e: host buffers (pinned), copies inside the timed region, through the C ABI
+    h_f = torch.from_numpy(f_host).pin_memory()
+    h_psi = torch.zeros(total, dtype=torch.float64).pin_memory()
+    cycp = np.zeros(len(sizes), dtype=np.int32)
+    rrp = np.zeros(len(sizes))
+    for _ in range(1):
+        L.gb_batch_solve_host(mixed._h, h_f.data_ptr(), h_psi.data_ptr(), cycp.ctypes.data, rrp.ctypes.data)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_cu = 0.0
+    for _ in range(args.steps):
+        st = L.gb_batch_solve_host(mixed._h, h_f.data_ptr(), h_psi.data_ptr(), cycp.ctypes.data, rrp.ctypes.data)
+        assert st == 0, lib.last_error()
+        e2e_cu += float(np.sum(cu_per_cycle * cycp))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s, e2e_cu], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        e2e_s, e2e_cu = float(mx[0]), float(t[1])
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = measured_peaks()
+    achieved = (pb.value / (pms.value / 1e3)) / 1e9 if pms.value > 0 else None
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "batch_smooth_fp32_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        if pl.value > 0:
+            traffic = tj.get("bytes_per_launch_full_scale")
+    line = {
+        "metric": METRIC,
+        "value": cu / (ms / 1e3),
+        "unit": "cell-updates/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer",
+        "data": "synthetic",
+        "config": {"workload": "batched Poisson: 256 problems, n in {65,129,257,513}, V(2,2) RB-GS, rtol 1e-10",
+                   "nprob": NPROB, "points": total, "interior_points": int(np.sum(cu_per_cycle)),
+                   "rtol": RTOL, "l2": "inputs larger than L2 (f and psi 2 x %.0f MB)" % (total * 8 / 1e6),
+                   "parallelism": "replicas x%d" % ws},
+        "fp64": {"value": cu64 / (ms64 / 1e3), "ms_per_step": ms64 / args.steps,
+                 "cycles_mean": float(np.mean(cyc64)), "relres_max": float(np.max(rr64))},
+        "mixed": {"cycles_mean": float(np.mean(cyc)), "relres_max": float(np.max(rr)),
+                  "field_rel_l2_vs_fp64": field_err, "speedup_vs_fp64": (cu / ms) / (cu64 / ms64)},
+        "e2e": {"value": e2e_cu / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": total * 8,
+                "d2h_bytes_per_step": total * 8},
+        "roofline": {"bound": "hbm", "kernel": "k_rb_half<float> (finest level, red or black half-sweep)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "peak_kind": peak_kind, "launches": pl.value,
+                     "avg_launch_ms": (pms.value / pl.value) if pl.value else None},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        v, sample, threads, used, psi_ref = cpu_reference(sizes, rank, budget_s=args.ref_budget)
+        offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+        got = np.concatenate([a[offs[j]:offs[j + 1]] for j in used])
+        line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                                "sample": sample}
+        line["mixed"]["field_rel_l2_vs_fp64_oracle_sample"] = float(np.linalg.norm(got - psi_ref) /
+                                                                     np.linalg.norm(psi_ref))
+    print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

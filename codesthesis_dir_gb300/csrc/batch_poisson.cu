@@ -388,6 +388,14 @@ struct gb_batch {
     const double *graph_f = nullptr;
     double *graph_psi = nullptr;
     long long launches = 0, launches_per_cycle = 0;
+    // optional per-launch timing of the finest-level smoothing kernel
+    int profile = 0, graph_profile = -1, graph_ev = 0;
+    std::vector<cudaEvent_t> ev;
+    int ev_used = 0;
+    double prof_ms = 0.0, prof_bytes = 0.0;
+    long long prof_launches = 0;
+    std::vector<int> h_active;
+    double level0_points_all = 0.0;
 };
 
 static int levels_of(int n, int *nl)
@@ -585,6 +593,7 @@ extern "C" int gb_batch_destroy(gb_batch *b)
 {
     if (!b) return GB_OK;
     if (b->cycle_graph) cudaGraphExecDestroy(b->cycle_graph);
+    for (auto &e : b->ev) cudaEventDestroy(e);
     cudaFree(b->pool);
     cudaFree(b->d_int);
     cudaFree(b->d_dbl);
@@ -598,6 +607,16 @@ extern "C" int gb_batch_destroy(gb_batch *b)
 
 extern "C" long long gb_batch_total_points(const gb_batch *b) { return b ? b->total : 0; }
 extern "C" long long gb_batch_last_launches(const gb_batch *b) { return b ? b->launches : 0; }
+
+// Records a timing event: as an event node of the graph while the stream is
+// being captured, as a plain record otherwise.
+static void prof_record(cudaEvent_t e, cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    if (cs == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else cudaEventRecord(e, s);
+}
 
 // The kernels of one V-cycle (descent over the global levels, the local
 // coarse solves, ascent), for element type T.
@@ -613,8 +632,12 @@ static void enqueue_vcycle(gb_batch *b, cudaStream_t s)
         if (cnt == 0) continue;
         const BlkEntry *t = tb + b->tbl_off[l];
         for (int it = 0; it < b->nu1; ++it) {
-            k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, 0);
-            k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, 1);
+            for (int color = 0; color < 2; ++color) {
+                const bool ev = b->profile && l == 0 && b->ev_used + 2 <= (int)b->ev.size();
+                if (ev) prof_record(b->ev[b->ev_used], s);
+                k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, color);
+                if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
+            }
             nl += 2;
         }
         k_residual<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l);
@@ -631,8 +654,12 @@ static void enqueue_vcycle(gb_batch *b, cudaStream_t s)
         k_prolong_add<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l);
         nl += 1;
         for (int it = 0; it < b->nu2; ++it) {
-            k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, 0);
-            k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, 1);
+            for (int color = 0; color < 2; ++color) {
+                const bool ev = b->profile && l == 0 && b->ev_used + 2 <= (int)b->ev.size();
+                if (ev) prof_record(b->ev[b->ev_used], s);
+                k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, color);
+                if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
+            }
             nl += 2;
         }
     }
@@ -658,6 +685,58 @@ static void enqueue_iteration(gb_batch *b, int first, cudaStream_t s)
         b->launches += 1;
     }
     cudaMemcpyAsync(b->h_pinned, D.num_active, sizeof(int), cudaMemcpyDeviceToHost, s);
+}
+
+// After an iteration has completed: adds the recorded smoothing-launch times
+// and the algorithmic bytes of the problems that took part (1.5 words per
+// interior point per half-sweep: psi read, f read, psi written, each for
+// half of the points plus the neighbours' half).
+static void batch_profile_collect(gb_batch *b, cudaStream_t s)
+{
+    if (!b->profile || b->ev_used == 0) return;
+    b->h_active.resize(b->nprob);
+    cudaMemcpyAsync(b->h_active.data(), b->dev.active, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    double pts = 0.0;
+    for (int p = 0; p < b->nprob; ++p)
+        if (b->h_active[p] && b->dloc[p] > 0) pts += (double)(b->n[p] - 2) * (double)(b->n[p] - 2);
+    const double esz = b->precision == GB_BATCH_FP64 ? 8.0 : 4.0;
+    for (int i = 0; i + 1 < b->ev_used; i += 2) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]) == cudaSuccess) {
+            b->prof_ms += ms;
+            b->prof_launches += 1;
+            b->prof_bytes += 1.5 * esz * pts;
+        } else {
+            cudaGetLastError();  // timing is advisory: never let it fail a solve
+        }
+    }
+}
+
+extern "C" int gb_batch_profile(gb_batch *b, int enable)
+{
+    if (!b) return GB_ERR_INVALID;
+    if (enable && b->ev.empty()) {
+        const int need = 2 * 2 * (b->nu1 + b->nu2) + 4;
+        b->ev.resize(need);
+        for (auto &e : b->ev) GB_CUDA_TRY(cudaEventCreate(&e));
+    }
+    b->profile = enable ? 1 : 0;
+    return GB_OK;
+}
+
+extern "C" int gb_batch_profile_read(gb_batch *b, double *ms, long long *launches, double *alg_bytes, int reset)
+{
+    if (!b) return GB_ERR_INVALID;
+    if (ms) *ms = b->prof_ms;
+    if (launches) *launches = b->prof_launches;
+    if (alg_bytes) *alg_bytes = b->prof_bytes;
+    if (reset) {
+        b->prof_ms = 0.0;
+        b->prof_bytes = 0.0;
+        b->prof_launches = 0;
+    }
+    return GB_OK;
 }
 
 static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStream_t s)
@@ -697,14 +776,17 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
     GB_CUDA_TRY(cudaMemsetAsync(D.cycles, 0, sizeof(int) * b->nprob, s));
     GB_CUDA_TRY(cudaMemsetAsync(D.failed, 0, sizeof(int) * b->nprob, s));
     // first iteration eagerly (records ||f||); later ones from a CUDA graph
+    b->ev_used = 0;
     enqueue_iteration(b, 1, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
-    if (!b->cycle_graph || b->graph_f != d_f || b->graph_psi != d_psi) {
+    batch_profile_collect(b, s);
+    if (!b->cycle_graph || b->graph_f != d_f || b->graph_psi != d_psi || b->graph_profile != b->profile) {
         if (b->cycle_graph) cudaGraphExecDestroy(b->cycle_graph);
         b->cycle_graph = nullptr;
         cudaStream_t cs = b->stream;
         cudaGraph_t g;
         const long long l0 = b->launches;
+        b->ev_used = 0;
         GB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         enqueue_iteration(b, 0, cs);
         GB_CUDA_TRY(cudaStreamEndCapture(cs, &g));
@@ -714,11 +796,15 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
         cudaGraphDestroy(g);
         b->graph_f = d_f;
         b->graph_psi = d_psi;
+        b->graph_profile = b->profile;
+        b->graph_ev = b->ev_used;
     }
     for (int it = 0; it <= b->max_cycles + 1 && *b->h_pinned > 0; ++it) {
         GB_CUDA_TRY(cudaGraphLaunch(b->cycle_graph, s));
         b->launches += b->launches_per_cycle;
         GB_CUDA_TRY(cudaStreamSynchronize(s));
+        b->ev_used = b->graph_ev;
+        batch_profile_collect(b, s);
     }
     std::vector<int> fl(b->nprob);
     GB_CUDA_TRY(cudaMemcpyAsync(fl.data(), D.failed, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s));

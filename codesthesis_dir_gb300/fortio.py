@@ -1,0 +1,99 @@
+"""Fortran file formats of the PRB driver: unformatted sequential records
+(the restart/output files of velvor2dperiodicrbconv.f:253-312 and :500-549),
+the ASCII dump of readoutput.f (format 1(1x,e16.8)) and the Nusselt history
+(format 14(1x,e16.8), velvor2dperiodicrbconv.f:551-560).
+
+gfortran frames every unformatted sequential record with a 4-byte
+little-endian length before and after the payload; records here are far
+below the 2 GiB at which gfortran splits them into sub-records.
+"""
+from __future__ import annotations
+
+import struct
+
+import numpy as np
+
+# Rows written per field (PRB:503-542): A, vel, wel, th use i = 0..nr+1; B, C, uel use i = 0..nr.
+RESTART_ROWS = {"A": 2, "B": 1, "C": 1, "uel": 1, "vel": 2, "wel": 2, "th": 2}
+RESTART_ORDER = ["A", "B", "C", "uel", "vel", "wel", "th"]
+
+
+def write_record(fh, payload: bytes):
+    n = len(payload)
+    if n >= 2 ** 31:
+        raise ValueError("record too large for a single gfortran record")
+    fh.write(struct.pack("<i", n))
+    fh.write(payload)
+    fh.write(struct.pack("<i", n))
+
+
+def read_record(fh) -> bytes:
+    head = fh.read(4)
+    if len(head) < 4:
+        raise EOFError("end of unformatted file")
+    (n,) = struct.unpack("<i", head)
+    if n < 0:
+        raise ValueError("sub-record files are not supported")
+    data = fh.read(n)
+    (tail,) = struct.unpack("<i", fh.read(4))
+    if tail != n or len(data) != n:
+        raise ValueError("corrupt record framing (%d vs %d)" % (n, tail))
+    return data
+
+
+def write_field(path, arr, nrows, np_):
+    """arr: (ld, >= np+1) Fortran-ordered field; writes rows 0..nrows-1 of
+    columns 0..np as one record, i fastest (the implied-do of PRB:503)."""
+    a = np.asarray(arr)[:nrows, : np_ + 1]
+    with open(path, "wb") as fh:
+        write_record(fh, np.asfortranarray(a).ravel(order="F").astype("<f8").tobytes())
+
+
+def read_field(path, nrows, np_, ld=None):
+    with open(path, "rb") as fh:
+        rec = read_record(fh)
+    v = np.frombuffer(rec, dtype="<f8")
+    if v.size != nrows * (np_ + 1):
+        raise ValueError("%s holds %d values, expected %d x %d" % (path, v.size, nrows, np_ + 1))
+    out = np.zeros((ld or nrows, np_ + 1), order="F")
+    out[:nrows, :] = v.reshape((np_ + 1, nrows)).T
+    return out
+
+
+def fortran_e(x: float, w: int = 16, d: int = 8) -> str:
+    """Fortran Ew.d edit descriptor (mantissa in [0.1, 1), two-digit
+    exponent for |exp| < 100, three digits with no 'E' above)."""
+    if x == 0.0:
+        s = "0." + "0" * d + "E+00"
+        return s.rjust(w)
+    sign = "-" if x < 0 else ""
+    m, e = ("%.*e" % (d - 1, abs(x))).split("e")
+    e = int(e) + 1
+    digits = m.replace(".", "")
+    if len(digits) > d:
+        digits = digits[:d]
+    if abs(e) < 100:
+        ex = "E%+03d" % e
+    else:
+        ex = "%+04d" % e
+    s = "%s0.%s%s" % (sign, digits, ex)
+    return s.rjust(w)
+
+
+def write_dump(path, values):
+    """readoutput.f's ASCII dump: one value per line, format (1x,e16.8)."""
+    with open(path, "w") as fh:
+        for v in np.ravel(values, order="F"):
+            fh.write(" " + fortran_e(float(v)) + "\n")
+
+
+def write_nu_history(path, dt, httrans, ssumc=None, ssums=None):
+    """Nusselt history of PRB:551-560: (i-1)*dt, httrans(i), then six
+    cos/sin Fourier integrals per line (zeros: the reference computes them in
+    a routine that is commented out, so it writes the zero-initialised
+    COMMON /grals/)."""
+    n = len(httrans)
+    with open(path, "w") as fh:
+        for i in range(n):
+            vals = [i * dt, httrans[i]] + [0.0] * 12
+            fh.write("".join(" " + fortran_e(v) for v in vals) + "\n")

@@ -207,6 +207,12 @@ int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi, int *cycl
                         double *relres);
 /* Number of kernel launches the last solve issued. */
 long long gb_batch_last_launches(const gb_batch *b);
+/* Times every launch of the finest-level smoothing kernel with CUDA events
+ * on the solve's stream during later solves (enable = 0 stops). */
+int gb_batch_profile(gb_batch *b, int enable);
+/* Accumulated smoothing-launch time (ms), launch count and algorithmic
+ * bytes (1.5 words per interior point per half-sweep); reset != 0 clears. */
+int gb_batch_profile_read(gb_batch *b, double *ms, long long *launches, double *alg_bytes, int reset);
 
 #ifdef __cplusplus
 }

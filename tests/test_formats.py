@@ -1,0 +1,79 @@
+"""Input decks, unformatted restart records and ASCII dumps (CPU only)."""
+import io
+import os
+
+import numpy as np
+
+from codesthesis_dir_gb300 import deck, fortio
+
+# The layout of the reference's PRB deck (velvor2dperiodicrbconv.f:78-120):
+# eight file names, dt, nr, np, nts, "r0,rmax,zmax" on one line, Ra, Re, Gr,
+# Pr, pert, amp, nval, the restart answer, then "more iterations" blocks.
+DECK = """a.dat
+b.dat
+c.dat
+u.dat
+v.dat
+w.dat
+t.dat
+nu.dat
+1.d-7
+96
+336
+50000
+0.5d0,1.0d0,0.1d0
+1.d7
+0d0
+0.d0
+0.71d0
+0.d0
+1.d0
+3
+no
+yes
+40000
+no
+"""
+
+
+def test_parse_prb_deck():
+    d = deck.parse_prb_deck(DECK)
+    assert d.fnames[0] == "a.dat" and d.fnames[7] == "nu.dat"
+    assert d.dt == 1e-7 and d.nr == 96 and d.np == 336 and d.nts == 50000
+    assert (d.r0, d.rmax, d.zmax) == (0.5, 1.0, 0.1)
+    assert d.Ra == 1e7 and d.Pr == 0.71 and d.nval == 3
+    assert d.restart is None and d.more == [40000]
+
+
+def test_parse_restart_deck():
+    text = DECK.replace("3\nno\nyes\n40000\nno\n", "3\nyes\n" + "".join("r%d.dat\n" % i for i in range(7)) + "no\n")
+    d = deck.parse_prb_deck(text)
+    assert d.restart == ["r%d.dat" % i for i in range(7)] and d.more == []
+
+
+def test_list_directed_continuation():
+    r = deck.ListDirected("1.5d0\n2.5d0, 3\n")
+    assert [deck.fortran_float(t) for t in r.read(3)] == [1.5, 2.5, 3.0]
+
+
+def test_unformatted_roundtrip(tmp_path):
+    nr, np_ = 6, 8
+    a = np.asfortranarray(np.random.default_rng(0).standard_normal((nr + 2, np_ + 1)))
+    p = tmp_path / "x.dat"
+    fortio.write_field(str(p), a, nr + 2, np_)
+    raw = p.read_bytes()
+    n = (nr + 2) * (np_ + 1) * 8
+    assert len(raw) == n + 8
+    assert int.from_bytes(raw[:4], "little") == n and int.from_bytes(raw[-4:], "little") == n
+    # i fastest inside the record (the implied-do of velvor2dperiodicrbconv.f:503)
+    assert np.frombuffer(raw[4:12], "<f8")[0] == a[0, 0] and np.frombuffer(raw[12:20], "<f8")[0] == a[1, 0]
+    b = fortio.read_field(str(p), nr + 2, np_)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_fortran_e_format():
+    assert fortio.fortran_e(0.5) == "  0.50000000E+00"
+    assert fortio.fortran_e(-1.0) == " -0.10000000E+01"
+    assert fortio.fortran_e(1.23456789e-5) == "  0.12345679E-04"
+    assert fortio.fortran_e(0.0) == "  0.00000000E+00"
+    assert len(fortio.fortran_e(3.0e120)) == 16
