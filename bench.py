@@ -94,7 +94,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -208,7 +208,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-budget", type=float, default=20.0)
@@ -362,7 +362,7 @@ def main():
                   "field_rel_l2_vs_fp64": field_err, "speedup_vs_fp64": (cu / ms) / (cu64 / ms64)},
         "e2e": {"value": e2e_cu / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": total * 8,
                 "d2h_bytes_per_step": total * 8},
-        "roofline": {"bound": "hbm", "kernel": "k_rb_half<float> (finest level, red or black half-sweep)",
+        "roofline": {"bound": "hbm", "kernel": "k_smooth<float,2> (finest level, two red-black sweeps per launch)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_kind": peak_kind, "launches": pl.value,

@@ -26,16 +26,15 @@
 
 #define BP_MAXL 16
 #define LOCAL_N 65
-#define PTS_PER_BLOCK 1024   // interior points per block of the level tables
 #define BP_THREADS 256
 
 template <class T> __device__ __forceinline__ T fmaT(T a, T b, T c);
 template <> __device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
 template <> __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
-struct BlkEntry {
-    int p;       // problem
-    int start;   // first interior point (row-major over the (n-2)^2 interior)
+struct TileEntry {
+    int p;            // problem
+    short tx, ty;     // tile index (origin tx*TX, ty*TY in grid points)
 };
 
 struct BatchDev {
@@ -43,118 +42,241 @@ struct BatchDev {
     const int *n_of;          // [p*BP_MAXL + l] level sizes (0 past the last level)
     const int *nlev;          // [p]
     const int *dloc;          // [p] first level solved locally
-    void *const *x;           // [p*BP_MAXL + l] solution / correction of level l (T*)
+    void *const *x;           // [(slot*nprob + p)*BP_MAXL + l] the two buffers of level l's solution (T*)
     void *const *f;           // right-hand side of level l (T*)
-    void *const *r;           // residual scratch of level l (T*)
+    void *const *r;           // unused
     int *active;              // [p]
     int *cycles;              // [p]
     int *failed;              // [p]
     double *fnorm, *relres;   // [p]
     double *partial;          // per level-0 block
     const int *p_blk0, *p_nblk0;  // level-0 table range of each problem
+    double *const *psi;       // [p] the caller's FP64 solution of level 0
     int *num_active;
     int max_cycles;
     double rtol;
 };
 
-template <class T> __device__ __forceinline__ T *XP(const BatchDev &B, int p, int l) { return (T *)B.x[p * BP_MAXL + l]; }
+template <class T> __device__ __forceinline__ T *XS(const BatchDev &B, int p, int l, int slot)
+{
+    return (T *)B.x[((size_t)slot * B.nprob + p) * BP_MAXL + l];
+}
 template <class T> __device__ __forceinline__ T *FP(const BatchDev &B, int p, int l) { return (T *)B.f[p * BP_MAXL + l]; }
 template <class T> __device__ __forceinline__ T *RP(const BatchDev &B, int p, int l) { return (T *)B.r[p * BP_MAXL + l]; }
 
 // ---------------------------------------------------------------------------
-// Level-synchronous kernels (one table entry per block)
+// Level-synchronous tile kernels (one table entry per block)
+//
+// A fine tile is TX x TY grid points with origin (tx*TX, ty*TY); a block
+// stages the tile plus a halo of H = 2*NU points in shared memory and runs
+// NU red-black sweeps there: sweep s updates red on ring H-1-2s and black
+// on ring H-2-2s, so after NU sweeps the tile itself is exact.  Points on
+// the Dirichlet boundary or outside the grid are never updated.
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(BP_THREADS) k_rb_half(BatchDev B, const BlkEntry *tbl, int l, int color)
-{
-    const BlkEntry e = tbl[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL + l], m = n - 2;
-    T *x = XP<T>(B, e.p, l);
-    const T *f = FP<T>(B, e.p, l);
-    const T h = (T)1 / (T)(n - 1), h2 = h * h;
-    const int end = min(e.start + PTS_PER_BLOCK, m * m);
-    for (int q = e.start + threadIdx.x; q < end; q += blockDim.x) {
-        const int j = q / m + 1, i = q - (j - 1) * m + 1;
-        if (((i + j) & 1) != color) continue;
-        const size_t c = (size_t)j * n + i;
-        const T s = (x[c - 1] + x[c + 1]) + (x[c - n] + x[c + n]);
-        x[c] = fmaT<T>(-h2, f[c], s) * (T)0.25;
-    }
-}
+#define TX 128
+#define TY 32
+#define CX 64    // coarse tile of the restriction kernel (fine 128 x 32)
+#define CY 16
+#define TILE_THREADS 256
 
+// One red (color 0) or black (color 1) phase on ring rho around the tile.
+// The smem array has origin (ox, oy) in grid coordinates and row stride SX.
 template <class T>
-__global__ void __launch_bounds__(BP_THREADS) k_residual(BatchDev B, const BlkEntry *tbl, int l)
+__device__ __forceinline__ void tile_phase(T *sx, const T *sf, int SX, int ox, int oy, int x0, int y0, int n,
+                                           T h2, int rho, int color)
 {
-    const BlkEntry e = tbl[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL + l], m = n - 2;
-    const T *x = XP<T>(B, e.p, l);
-    const T *f = FP<T>(B, e.p, l);
-    T *r = RP<T>(B, e.p, l);
-    const T h = (T)1 / (T)(n - 1), ih2 = (T)1 / (h * h);
-    const int end = min(e.start + PTS_PER_BLOCK, m * m);
-    for (int q = e.start + threadIdx.x; q < end; q += blockDim.x) {
-        const int j = q / m + 1, i = q - (j - 1) * m + 1;
-        const size_t c = (size_t)j * n + i;
-        const T s = (x[c - 1] + x[c + 1]) + (x[c - n] + x[c + n]);
-        const T lap = fmaT<T>((T)-4, x[c], s);
-        r[c] = fmaT<T>(-ih2, lap, f[c]);
-    }
-}
-
-// Full weighting onto the coarse interior (rotann2.f:773-785 summation
-// order); the coarse solution is zeroed.  tbl is the table of level l+1.
-template <class T>
-__global__ void __launch_bounds__(BP_THREADS) k_restrict(BatchDev B, const BlkEntry *tbl, int l)
-{
-    const BlkEntry e = tbl[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1], mc = nc - 2;
-    const T *r = RP<T>(B, e.p, l);
-    T *fc = FP<T>(B, e.p, l + 1);
-    T *xc = XP<T>(B, e.p, l + 1);
-    const int end = min(e.start + PTS_PER_BLOCK, mc * mc);
-    for (int q = e.start + threadIdx.x; q < end; q += blockDim.x) {
-        const int j = q / mc + 1, i = q - (j - 1) * mc + 1;
-        const size_t c = (size_t)(2 * j) * n + (size_t)(2 * i);
-        T t = r[c];
-        t = t * (T)2 + r[c + 1] + r[c - 1];
-        t = t + r[c + n] + r[c - n];
-        t = t * (T)2 + r[c + 1 + n] + r[c - 1 - n];
-        t = t + r[c + 1 - n] + r[c - 1 + n];
-        fc[(size_t)j * nc + i] = t * (T)0.0625;
-        xc[(size_t)j * nc + i] = (T)0;
-    }
-}
-
-// Bilinear prolongation of level l+1 added into level l (rotann2.f:821-858).
-template <class T>
-__global__ void __launch_bounds__(BP_THREADS) k_prolong_add(BatchDev B, const BlkEntry *tbl, int l)
-{
-    const BlkEntry e = tbl[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1], m = n - 2;
-    T *x = XP<T>(B, e.p, l);
-    const T *ec = XP<T>(B, e.p, l + 1);
-    const int end = min(e.start + PTS_PER_BLOCK, m * m);
-    for (int q = e.start + threadIdx.x; q < end; q += blockDim.x) {
-        const int j = q / m + 1, i = q - (j - 1) * m + 1;
-        const T *ep = ec + (size_t)(j / 2) * nc + (i / 2);
-        T v;
-        if ((i & 1) == 0) {
-            if ((j & 1) == 0) v = ep[0];
-            else v = (ep[0] + ep[nc]) * (T)0.5;
-        } else {
-            if ((j & 1) == 0) v = (ep[0] + ep[1]) * (T)0.5;
-            else {
-                T t = ep[0] + ep[nc + 1];
-                t = t + ep[nc] + ep[1];
-                v = t * (T)0.25;
-            }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int gxa = max(x0 - rho, 1), gxb = min(x0 + TX + rho, n - 1);
+    const int gya = max(y0 - rho, 1), gyb = min(y0 + TY + rho, n - 1);
+    for (int gy = gya + warp; gy < gyb; gy += nw) {
+        const int base = (gy - oy) * SX - ox;
+        const int first = gxa + ((gxa + gy + color) & 1);
+        for (int gx = first + 2 * lane; gx < gxb; gx += 64) {
+            const int c = base + gx;
+            const T s = (sx[c - 1] + sx[c + 1]) + (sx[c - SX] + sx[c + SX]);
+            sx[c] = fmaT<T>(-h2, sf[c], s) * (T)0.25;
         }
-        const size_t c = (size_t)j * n + i;
-        x[c] = x[c] + v;
+    }
+    __syncthreads();
+}
+
+template <class T>
+__device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int SX, int ox, int oy, int x0, int y0, int n,
+                                            int nu, int H)
+{
+    const T h = (T)1 / (T)(n - 1), h2 = h * h;
+    for (int s = 0; s < nu; ++s) {
+        tile_phase<T>(sx, sf, SX, ox, oy, x0, y0, n, h2, H - 1 - 2 * s, 0);
+        tile_phase<T>(sx, sf, SX, ox, oy, x0, y0, n, h2, H - 2 - 2 * s, 1);
+    }
+}
+
+// Stores the tile's interior points into x, or (psi != nullptr) adds them to
+// the FP64 solution instead: the last level-0 kernel of an inner cycle
+// applies the defect correction psi += e point by point.
+template <class T>
+__device__ __forceinline__ void tile_store(const T *sx, int SX, int ox, int oy, int x0, int y0, int n, T *x,
+                                           double *psi)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int gxa = max(x0, 1), gxb = min(x0 + TX, n - 1);
+    const int gya = max(y0, 1), gyb = min(y0 + TY, n - 1);
+    for (int gy = gya + warp; gy < gyb; gy += nw)
+        for (int gx = gxa + lane; gx < gxb; gx += 32) {
+            const size_t g = (size_t)gy * n + gx;
+            const T v = sx[(gy - oy) * SX + gx - ox];
+            if (psi) psi[g] = psi[g] + (double)v;
+            else x[g] = v;
+        }
+}
+
+// NU smoothing sweeps of level l from buffer src into buffer dst (never the
+// same buffer: blocks read their neighbours' tiles as halo).  zero_init: the
+// level's current solution is zero (the correction of a coarse level, or the
+// FP32 correction of the defect-correction loop) and is not read.  correct:
+// add the result to the FP64 solution instead of storing it (level 0).
+template <class T, int NU>
+__global__ void __launch_bounds__(TILE_THREADS) k_smooth(BatchDev B, const TileEntry *tiles, int l, int zero_init,
+                                                         int src, int dst, int correct)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
+    T *sx = (T *)smem_raw, *sf = sx + SX * SY;
+    const TileEntry e = tiles[blockIdx.x];
+    if (!B.active[e.p]) return;
+    const int n = B.n_of[e.p * BP_MAXL + l];
+    const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
+    const T *x = XS<T>(B, e.p, l, src);
+    const T *f = FP<T>(B, e.p, l);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = warp; r < SY; r += nw) {
+        const int gy = oy + r;
+        const bool rowin = gy >= 0 && gy < n;
+        for (int c = lane; c < SX; c += 32) {
+            const int gx = ox + c;
+            T v = (T)0, fv = (T)0;
+            if (rowin && gx >= 0 && gx < n) {
+                const size_t g = (size_t)gy * n + gx;
+                fv = f[g];
+                if (!zero_init) v = x[g];
+            }
+            sx[r * SX + c] = v;
+            sf[r * SX + c] = fv;
+        }
+    }
+    __syncthreads();
+    tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
+    tile_store<T>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), correct ? B.psi[e.p] : nullptr);
+}
+
+// Bilinear prolongation of level l+1 (buffer csrc) added into level l
+// (buffer src) over the tile and its halo (rotann2.f:821-858), then NU
+// post-smoothing sweeps, stored into buffer dst (or added to psi: correct).
+template <class T, int NU>
+__global__ void __launch_bounds__(TILE_THREADS) k_prolong_smooth(BatchDev B, const TileEntry *tiles, int l, int src,
+                                                                 int csrc, int dst, int correct)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
+    T *sx = (T *)smem_raw, *sf = sx + SX * SY;
+    const TileEntry e = tiles[blockIdx.x];
+    if (!B.active[e.p]) return;
+    const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1];
+    const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
+    const T *x = XS<T>(B, e.p, l, src);
+    const T *f = FP<T>(B, e.p, l);
+    const T *ec = XS<T>(B, e.p, l + 1, csrc);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = warp; r < SY; r += nw) {
+        const int gy = oy + r;
+        const bool rowin = gy >= 0 && gy < n;
+        for (int c = lane; c < SX; c += 32) {
+            const int gx = ox + c;
+            T v = (T)0, fv = (T)0;
+            if (rowin && gx >= 0 && gx < n) {
+                const size_t g = (size_t)gy * n + gx;
+                v = x[g];
+                if (NU > 0) fv = f[g];
+                if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
+                    const T *ep = ec + (size_t)(gy / 2) * nc + (gx / 2);
+                    T p;
+                    if ((gx & 1) == 0) {
+                        if ((gy & 1) == 0) p = ep[0];
+                        else p = (ep[0] + ep[nc]) * (T)0.5;
+                    } else {
+                        if ((gy & 1) == 0) p = (ep[0] + ep[1]) * (T)0.5;
+                        else {
+                            T t = ep[0] + ep[nc + 1];
+                            t = t + ep[nc] + ep[1];
+                            p = t * (T)0.25;
+                        }
+                    }
+                    v = v + p;
+                }
+            }
+            sx[r * SX + c] = v;
+            if (NU > 0) sf[r * SX + c] = fv;
+        }
+    }
+    __syncthreads();
+    if (NU > 0) tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
+    tile_store<T>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), correct ? B.psi[e.p] : nullptr);
+}
+
+// Residual of level l and its full weighting onto level l+1 (rotann2.f:
+// 773-785 summation order) for one CX x CY tile of coarse points.
+template <class T>
+__global__ void __launch_bounds__(TILE_THREADS) k_resid_restrict(BatchDev B, const TileEntry *ctiles, int l, int src)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int FW = 2 * CX + 1, FH = 2 * CY + 1, XW = FW + 2, XH = FH + 2;
+    T *sx = (T *)smem_raw, *sr = sx + XW * XH;
+    const TileEntry e = ctiles[blockIdx.x];
+    if (!B.active[e.p]) return;
+    const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1];
+    const int X0 = e.tx * CX, Y0 = e.ty * CY;
+    const int rx = 2 * X0 - 1, ry = 2 * Y0 - 1;     // residual region origin
+    const T *x = XS<T>(B, e.p, l, src);
+    const T *f = FP<T>(B, e.p, l);
+    T *fc = FP<T>(B, e.p, l + 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = warp; r < XH; r += nw) {
+        const int gy = ry - 1 + r;
+        const bool rowin = gy >= 0 && gy < n;
+        for (int c = lane; c < XW; c += 32) {
+            const int gx = rx - 1 + c;
+            sx[r * XW + c] = (rowin && gx >= 0 && gx < n) ? x[(size_t)gy * n + gx] : (T)0;
+        }
+    }
+    __syncthreads();
+    const T h = (T)1 / (T)(n - 1), ih2 = (T)1 / (h * h);
+    for (int r = warp; r < FH; r += nw) {
+        const int gy = ry + r;
+        for (int c = lane; c < FW; c += 32) {
+            const int gx = rx + c;
+            T rv = (T)0;
+            if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
+                const int q = (r + 1) * XW + (c + 1);
+                const T s = (sx[q - 1] + sx[q + 1]) + (sx[q - XW] + sx[q + XW]);
+                const T lap = fmaT<T>((T)-4, sx[q], s);
+                rv = fmaT<T>(-ih2, lap, f[(size_t)gy * n + gx]);
+            }
+            sr[r * FW + c] = rv;
+        }
+    }
+    __syncthreads();
+    const int Ia = max(X0, 1), Ib = min(X0 + CX, nc - 1);
+    const int Ja = max(Y0, 1), Jb = min(Y0 + CY, nc - 1);
+    for (int J = Ja + warp; J < Jb; J += nw) {
+        for (int I = Ia + lane; I < Ib; I += 32) {
+            const int q = (2 * (J - Y0) + 1) * FW + (2 * (I - X0) + 1);
+            T t = sr[q];
+            t = t * (T)2 + sr[q + 1] + sr[q - 1];
+            t = t + sr[q + FW] + sr[q - FW];
+            t = t * (T)2 + sr[q + 1 + FW] + sr[q - 1 - FW];
+            t = t + sr[q + 1 - FW] + sr[q - 1 + FW];
+            fc[(size_t)J * nc + I] = t * (T)0.0625;
+        }
     }
 }
 
@@ -176,7 +298,7 @@ __device__ void loc_rb_half(T *x, const T *f, int n, T h2, int color)
 }
 
 template <class T>
-__global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1, int nu2)
+__global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1, int nu2, int zero_level0)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = (T *)smem_raw;
@@ -195,9 +317,15 @@ __global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1
     for (int q = threadIdx.x; q < tot; q += blockDim.x) { X[q] = (T)0; F[q] = (T)0; R[q] = (T)0; }
     __syncthreads();
     {
+        // the level's solution is a correction that starts at zero unless this
+        // is the finest level of a plain FP64 solve
+        const bool zero = d0 > 0 || zero_level0;
         const int n = B.n_of[p * BP_MAXL + d0];
-        const T *gx = XP<T>(B, p, d0), *gf = FP<T>(B, p, d0);
-        for (int q = threadIdx.x; q < n * n; q += blockDim.x) { X[q] = gx[q]; F[q] = gf[q]; }
+        const T *gx = XS<T>(B, p, d0, 0), *gf = FP<T>(B, p, d0);
+        for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+            if (!zero) X[q] = gx[q];
+            F[q] = gf[q];
+        }
     }
     __syncthreads();
     // descent
@@ -264,9 +392,16 @@ __global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1
         for (int s = 0; s < nu2; ++s) { loc_rb_half(x, f, n, h2, 0); loc_rb_half(x, f, n, h2, 1); }
     }
     {
+        // the local levels end in buffer 0; a mixed solve local from level 0
+        // applies its correction to the FP64 solution directly
         const int n = B.n_of[p * BP_MAXL + d0];
-        T *gx = XP<T>(B, p, d0);
-        for (int q = threadIdx.x; q < n * n; q += blockDim.x) gx[q] = X[q];
+        if (d0 == 0 && zero_level0) {
+            double *psi = B.psi[p];
+            for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = psi[q] + (double)X[q];
+        } else {
+            T *gx = XS<T>(B, p, d0, 0);
+            for (int q = threadIdx.x; q < n * n; q += blockDim.x) gx[q] = X[q];
+        }
     }
 }
 
@@ -285,64 +420,91 @@ __device__ __forceinline__ double blk_sum(double v, double *s_red)
     return r;
 }
 
-// FP64 residual of level 0 (psi, f user arrays); mode 0: norm only (plain),
-// mode 1: also store the residual as the FP32 right-hand side of the inner
-// cycle and zero the FP32 correction (mixed).
-__global__ void __launch_bounds__(BP_THREADS) k_outer_residual(BatchDev B, const BlkEntry *tbl, const double *const *psi_p,
-                                                               const double *const *f_p, int mode)
+// FP64 outer pass over one TX x TY tile of level 0 (psi, f: the caller's
+// arrays): the residual r = f - A psi, its squared norm (block partial) and,
+// when store_r, r rounded to FP32 as the inner cycle's right-hand side.
+// psi is only read here, so neighbouring tiles may overlap freely.
+__global__ void __launch_bounds__(TILE_THREADS) k_outer(BatchDev B, const TileEntry *tiles, const double *const *f_p,
+                                                        int store_r)
 {
+    __shared__ double sp[(TY + 2) * (TX + 2)];
     __shared__ double s_red[32];
-    const BlkEntry e = tbl[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL], m = n - 2;
-    const double *x = psi_p[e.p], *f = f_p[e.p];
-    const double h = 1.0 / (double)(n - 1), ih2 = 1.0 / (h * h);
-    float *f32 = mode ? FP<float>(B, e.p, 0) : nullptr;
-    float *x32 = mode ? XP<float>(B, e.p, 0) : nullptr;
-    double acc = 0.0;
-    const int end = min(e.start + PTS_PER_BLOCK, m * m);
-    for (int q = e.start + threadIdx.x; q < end; q += blockDim.x) {
-        const int j = q / m + 1, i = q - (j - 1) * m + 1;
-        const size_t c = (size_t)j * n + i;
-        const double s = (x[c - 1] + x[c + 1]) + (x[c - n] + x[c + n]);
-        const double lap = __fma_rn(-4.0, x[c], s);
-        const double r = __fma_rn(-ih2, lap, f[c]);
-        acc = __fma_rn(r, r, acc);
-        if (mode) {
-            f32[c] = (float)r;
-            x32[c] = 0.0f;
+    constexpr int SX = TX + 2, SY = TY + 2;
+    const TileEntry e = tiles[blockIdx.x];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (!B.active[e.p]) {
+        if (threadIdx.x == 0) B.partial[blockIdx.x] = 0.0;
+        return;
+    }
+    const int n = B.n_of[e.p * BP_MAXL];
+    const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - 1, oy = y0 - 1;
+    const double *psi = B.psi[e.p];
+    const double *f = f_p[e.p];
+    for (int r = warp; r < SY; r += nw) {
+        const int gy = oy + r;
+        const bool rowin = gy >= 0 && gy < n;
+        for (int c = lane; c < SX; c += 32) {
+            const int gx = ox + c;
+            sp[r * SX + c] = (rowin && gx >= 0 && gx < n) ? psi[(size_t)gy * n + gx] : 0.0;
         }
     }
-    const double tot = blk_sum(acc, s_red);
-    if (threadIdx.x == 0) B.partial[blockIdx.x] = tot;
-}
-
-// psi += (double) e over the interior (mixed mode).
-__global__ void __launch_bounds__(BP_THREADS) k_correct(BatchDev B, const BlkEntry *tbl, double *const *psi_p)
-{
-    const BlkEntry e = tbl[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL], m = n - 2;
-    double *x = psi_p[e.p];
-    const float *ev = XP<float>(B, e.p, 0);
-    const int end = min(e.start + PTS_PER_BLOCK, m * m);
-    for (int q = e.start + threadIdx.x; q < end; q += blockDim.x) {
-        const int j = q / m + 1, i = q - (j - 1) * m + 1;
-        const size_t c = (size_t)j * n + i;
-        x[c] = x[c] + (double)ev[c];
+    __syncthreads();
+    const double h = 1.0 / (double)(n - 1), ih2 = 1.0 / (h * h);
+    float *f32 = store_r ? FP<float>(B, e.p, 0) : nullptr;
+    double acc = 0.0;
+    const int gxa = max(x0, 1), gxb = min(x0 + TX, n - 1);
+    const int gya = max(y0, 1), gyb = min(y0 + TY, n - 1);
+    for (int gy = gya + warp; gy < gyb; gy += nw) {
+        for (int gx = gxa + lane; gx < gxb; gx += 32) {
+            const int q = (gy - oy) * SX + gx - ox;
+            const size_t g = (size_t)gy * n + gx;
+            const double s = (sp[q - 1] + sp[q + 1]) + (sp[q - SX] + sp[q + SX]);
+            const double lap = __fma_rn(-4.0, sp[q], s);
+            const double r = __fma_rn(-ih2, lap, f[g]);
+            acc = __fma_rn(r, r, acc);
+            if (store_r) f32[g] = (float)r;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_red[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t += s_red[w];
+        B.partial[blockIdx.x] = t;
     }
 }
 
-// One thread per problem: sums the block partials in order, decides whether
-// the problem keeps cycling.  first != 0 records ||f|| (psi = 0).
+// Copies buffer 1 of level 0 into the caller's psi (plain FP64 cycles whose
+// level-0 kernels leave the result in the internal buffer).
+__global__ void __launch_bounds__(TILE_THREADS) k_copy_back(BatchDev B, const TileEntry *tiles)
+{
+    const TileEntry e = tiles[blockIdx.x];
+    if (!B.active[e.p]) return;
+    const int n = B.n_of[e.p * BP_MAXL];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const double *src = XS<double>(B, e.p, 0, 1);
+    double *dst = B.psi[e.p];
+    const int x0 = e.tx * TX, y0 = e.ty * TY;
+    const int gxa = max(x0, 1), gxb = min(x0 + TX, n - 1);
+    const int gya = max(y0, 1), gyb = min(y0 + TY, n - 1);
+    for (int gy = gya + warp; gy < gyb; gy += nw)
+        for (int gx = gxa + lane; gx < gxb; gx += 32) dst[(size_t)gy * n + gx] = src[(size_t)gy * n + gx];
+}
+
+// One warp per problem: sums the problem's tile partials in a fixed order
+// and decides whether it keeps cycling.  first != 0 records ||f|| (psi = 0).
 __global__ void k_finalize(BatchDev B, int first)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (p >= B.nprob) return;
     if (!B.active[p]) return;
     double s = 0.0;
     const int b0 = B.p_blk0[p], nb = B.p_nblk0[p];
-    for (int b = 0; b < nb; ++b) s += B.partial[b0 + b];
+    for (int b = lane; b < nb; b += 32) s += B.partial[b0 + b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane != 0) return;
     const double rn = sqrt(s);
     if (first) B.fnorm[p] = rn;
     const double fn = B.fnorm[p];
@@ -366,36 +528,32 @@ struct gb_batch {
     double rtol = 1e-10;
     std::vector<int> n, L, dloc;
     long long total = 0;
-    std::vector<long long> off0;      // level-0 offsets in the packed user arrays
-    int maxdepth_global = 0;          // levels 0..maxdepth_global-1 have global work
-    // device
-    void *pool = nullptr;             // T levels (T = double or float)
+    std::vector<long long> off0;        // level-0 offsets in the packed user arrays
+    int maxdepth_global = 0;            // levels 0..maxdepth_global-1 have tile work
+    void *pool = nullptr;               // per-level x, f (T = double or float)
     size_t pool_bytes = 0;
-    int *d_int = nullptr;             // n_of, nlev, dloc, active, cycles, failed, p_blk0, p_nblk0, num_active
-    double *d_dbl = nullptr;          // fnorm, relres, partial
-    void **d_ptrs = nullptr;          // x, f, r tables + psi/f level-0 pointer tables
-    BlkEntry *d_tbl = nullptr;
-    std::vector<int> tbl_off, tbl_cnt;    // per level: smoothing table segment
-    std::vector<int> rtbl_off, rtbl_cnt;  // per level: restriction-target table segment
-    int tbl0_off = 0, tbl0_cnt = 0;     // level-0 table over all problems (norms)
+    int *d_int = nullptr;
+    double *d_dbl = nullptr;
+    void **d_ptrs = nullptr;
+    TileEntry *d_tiles = nullptr;
+    std::vector<int> ft_off, ft_cnt;    // per level: fine tiles (problems with l < dloc)
+    std::vector<int> ct_off, ct_cnt;    // per level l >= 1: coarse tiles of l (problems with l <= dloc)
+    int ot_off = 0, ot_cnt = 0;         // level-0 tiles of every problem (outer pass)
     BatchDev dev;
     double **d_psi_tab = nullptr, **d_f_tab = nullptr;
-    std::vector<void *> hx, hf, hr;     // host copies of the pointer tables
+    std::vector<void *> hx, hf;
     size_t local_smem = 0;
     int *h_pinned = nullptr;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t cycle_graph = nullptr;
-    const double *graph_f = nullptr;
-    double *graph_psi = nullptr;
     long long launches = 0, launches_per_cycle = 0;
-    // optional per-launch timing of the finest-level smoothing kernel
+    // optional per-launch timing of the finest-level pre-smoothing kernel
     int profile = 0, graph_profile = -1, graph_ev = 0;
     std::vector<cudaEvent_t> ev;
     int ev_used = 0;
     double prof_ms = 0.0, prof_bytes = 0.0;
     long long prof_launches = 0;
     std::vector<int> h_active;
-    double level0_points_all = 0.0;
 };
 
 static int levels_of(int n, int *nl)
@@ -409,12 +567,30 @@ static int levels_of(int n, int *nl)
     return L;
 }
 
+template <class T, int NU> static size_t smem_smooth() { return 2 * sizeof(T) * (TX + 4 * NU) * (TY + 4 * NU); }
+template <class T> static size_t smem_restrict() { return sizeof(T) * ((2 * CX + 3) * (2 * CY + 3) + (2 * CX + 1) * (2 * CY + 1)); }
+
+template <class T> static cudaError_t set_smem_attrs(size_t local)
+{
+    cudaError_t e;
+#define SA(k, sz) if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sz))) != cudaSuccess) return e
+    SA((k_smooth<T, 1>), (smem_smooth<T, 1>()));
+    SA((k_smooth<T, 2>), (smem_smooth<T, 2>()));
+    SA((k_prolong_smooth<T, 0>), (smem_smooth<T, 0>()));
+    SA((k_prolong_smooth<T, 1>), (smem_smooth<T, 1>()));
+    SA((k_prolong_smooth<T, 2>), (smem_smooth<T, 2>()));
+    SA((k_resid_restrict<T>), (smem_restrict<T>()));
+    SA((k_local_vcycle<T>), (local));
+#undef SA
+    return cudaSuccess;
+}
+
 extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
                                int max_cycles, gb_batch **out)
 {
-    if (!out || !n || nprob <= 0 || (precision != GB_BATCH_FP64 && precision != GB_BATCH_MIXED) || nu1 < 0 ||
-        nu2 < 0 || max_cycles < 0) {
-        gb_set_error("gb_batch_create: invalid argument");
+    if (!out || !n || nprob <= 0 || (precision != GB_BATCH_FP64 && precision != GB_BATCH_MIXED) || nu1 < 1 ||
+        nu1 > 8 || nu2 < 0 || nu2 > 8 || max_cycles < 0 || !(rtol >= 0.0)) {
+        gb_set_error("gb_batch_create: invalid argument (need nprob > 0, 1 <= nu1 <= 8, 0 <= nu2 <= 8)");
         return GB_ERR_INVALID;
     }
     *out = nullptr;
@@ -450,56 +626,52 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
         maxd = std::max(maxd, d);
         for (int l = 0; l < L; ++l) {
             nof[(size_t)p * BP_MAXL + l] = nl[l];
+            // x buffers 0 and 1 plus f; the plain solve's level 0 uses the
+            // caller's psi and f, with one internal FP64 buffer beside psi
             const size_t sz = (size_t)nl[l] * nl[l];
-            // plain: levels >= 1 need x, f; all levels need r.  mixed: every level x, f, r.
-            pool_elems += (precision == GB_BATCH_FP64 && l == 0) ? sz : 3 * sz;
+            if (precision == GB_BATCH_FP64 && l == 0) pool_elems += sz;
+            else pool_elems += 3 * sz;
         }
         b->off0[p] = tot;
         tot += (long long)np_ * np_;
     }
     b->total = tot;
     b->maxdepth_global = maxd;
-    // local-solve shared memory: x, f, r of levels dloc..L-1
     size_t smax = 0;
     for (int p = 0; p < nprob; ++p) {
-        size_t s = 0;
-        for (int l = b->dloc[p]; l < b->L[p]; ++l) s += (size_t)nof[(size_t)p * BP_MAXL + l] * nof[(size_t)p * BP_MAXL + l];
-        smax = std::max(smax, 3 * s * esz);
+        size_t sz = 0;
+        for (int l = b->dloc[p]; l < b->L[p]; ++l) sz += (size_t)nof[(size_t)p * BP_MAXL + l] * nof[(size_t)p * BP_MAXL + l];
+        smax = std::max(smax, 3 * sz * esz);
     }
     b->local_smem = smax;
-    // block tables: smoothing tables per level l (problems with l < dloc),
-    // restriction-target tables per level l >= 1 (problems with l <= dloc),
-    // and the level-0 table over all problems (norms, defect correction)
-    std::vector<BlkEntry> tbl;
-    b->tbl_off.assign(BP_MAXL, 0);
-    b->tbl_cnt.assign(BP_MAXL, 0);
-    b->rtbl_off.assign(BP_MAXL, 0);
-    b->rtbl_cnt.assign(BP_MAXL, 0);
+    // tile tables
+    std::vector<TileEntry> tiles;
+    b->ft_off.assign(BP_MAXL + 1, 0);
+    b->ft_cnt.assign(BP_MAXL + 1, 0);
+    b->ct_off.assign(BP_MAXL + 1, 0);
+    b->ct_cnt.assign(BP_MAXL + 1, 0);
     std::vector<int> pb0(nprob), pnb0(nprob);
+    auto add_tiles = [&](int p, int nn, int tw, int th) {
+        for (int ty = 0; ty * th < nn - 1; ++ty)
+            for (int tx = 0; tx * tw < nn - 1; ++tx) tiles.push_back({p, (short)tx, (short)ty});
+    };
     for (int l = 0; l < BP_MAXL; ++l) {
-        b->tbl_off[l] = (int)tbl.size();
-        for (int p = 0; p < nprob; ++p) {
-            if (l >= b->dloc[p]) continue;
-            const int m = nof[(size_t)p * BP_MAXL + l] - 2;
-            for (int s0 = 0; s0 < m * m; s0 += PTS_PER_BLOCK) tbl.push_back({p, s0});
-        }
-        b->tbl_cnt[l] = (int)tbl.size() - b->tbl_off[l];
-        b->rtbl_off[l] = (int)tbl.size();
-        for (int p = 0; p < nprob; ++p) {
-            if (l < 1 || l > b->dloc[p]) continue;
-            const int m = nof[(size_t)p * BP_MAXL + l] - 2;
-            for (int s0 = 0; s0 < m * m; s0 += PTS_PER_BLOCK) tbl.push_back({p, s0});
-        }
-        b->rtbl_cnt[l] = (int)tbl.size() - b->rtbl_off[l];
+        b->ft_off[l] = (int)tiles.size();
+        for (int p = 0; p < nprob; ++p)
+            if (l < b->dloc[p]) add_tiles(p, nof[(size_t)p * BP_MAXL + l], TX, TY);
+        b->ft_cnt[l] = (int)tiles.size() - b->ft_off[l];
+        b->ct_off[l] = (int)tiles.size();
+        for (int p = 0; p < nprob; ++p)
+            if (l >= 1 && l <= b->dloc[p]) add_tiles(p, nof[(size_t)p * BP_MAXL + l], CX, CY);
+        b->ct_cnt[l] = (int)tiles.size() - b->ct_off[l];
     }
-    b->tbl0_off = (int)tbl.size();
+    b->ot_off = (int)tiles.size();
     for (int p = 0; p < nprob; ++p) {
-        const int m = n[p] - 2;
-        pb0[p] = (int)tbl.size() - b->tbl0_off;
-        for (int s = 0; s < m * m; s += PTS_PER_BLOCK) tbl.push_back({p, s});
-        pnb0[p] = (int)tbl.size() - b->tbl0_off - pb0[p];
+        pb0[p] = (int)tiles.size() - b->ot_off;
+        add_tiles(p, n[p], TX, TY);
+        pnb0[p] = (int)tiles.size() - b->ot_off - pb0[p];
     }
-    b->tbl0_cnt = (int)tbl.size() - b->tbl0_off;
+    b->ot_cnt = (int)tiles.size() - b->ot_off;
 
 #define BTRY(x)                                                                 \
     do {                                                                        \
@@ -510,31 +682,34 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
             return GB_ERR_ALLOC;                                                \
         }                                                                       \
     } while (0)
-    b->pool_bytes = pool_elems * esz;
+    b->pool_bytes = std::max<size_t>(pool_elems * esz, 16);
     BTRY(cudaMalloc(&b->pool, b->pool_bytes));
     BTRY(cudaMemset(b->pool, 0, b->pool_bytes));
-    const size_t nint = (size_t)nprob * BP_MAXL + 2 * (size_t)nprob + 3 * (size_t)nprob + 2 * (size_t)nprob + 1;
+    const size_t nint = (size_t)nprob * BP_MAXL + 7 * (size_t)nprob + 1;
     BTRY(cudaMalloc(&b->d_int, sizeof(int) * nint));
-    const size_t ndbl = 2 * (size_t)nprob + (size_t)b->tbl0_cnt;
-    BTRY(cudaMalloc(&b->d_dbl, sizeof(double) * ndbl));
-    BTRY(cudaMalloc(&b->d_ptrs, sizeof(void *) * (3 * (size_t)nprob * BP_MAXL + 2 * (size_t)nprob)));
-    BTRY(cudaMalloc(&b->d_tbl, sizeof(BlkEntry) * std::max<size_t>(1, tbl.size())));
+    BTRY(cudaMemset(b->d_int, 0, sizeof(int) * nint));
+    BTRY(cudaMalloc(&b->d_dbl, sizeof(double) * (2 * (size_t)nprob + (size_t)b->ot_cnt)));
+    // pointer tables: x (two buffers per level), f (one per level), psi and f of level 0
+    const size_t nptr = 2 * (size_t)nprob * BP_MAXL + (size_t)nprob * BP_MAXL + 2 * (size_t)nprob;
+    BTRY(cudaMalloc(&b->d_ptrs, sizeof(void *) * nptr));
+    BTRY(cudaMalloc(&b->d_tiles, sizeof(TileEntry) * tiles.size()));
     BTRY(cudaMallocHost(&b->h_pinned, sizeof(int) * 16));
     BTRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-    // pointer tables
-    b->hx.assign((size_t)nprob * BP_MAXL, nullptr);
+    b->hx.assign(2 * (size_t)nprob * BP_MAXL, nullptr);
     b->hf.assign((size_t)nprob * BP_MAXL, nullptr);
-    b->hr.assign((size_t)nprob * BP_MAXL, nullptr);
     char *base = (char *)b->pool;
     for (int p = 0; p < nprob; ++p) {
         for (int l = 0; l < b->L[p]; ++l) {
             const size_t sz = (size_t)nof[(size_t)p * BP_MAXL + l] * nof[(size_t)p * BP_MAXL + l] * esz;
             const size_t k = (size_t)p * BP_MAXL + l;
-            if (!(precision == GB_BATCH_FP64 && l == 0)) {
-                b->hx[k] = base; base += sz;
-                b->hf[k] = base; base += sz;
+            const size_t k1 = ((size_t)nprob + p) * BP_MAXL + l;
+            if (precision == GB_BATCH_FP64 && l == 0) {
+                b->hx[k1] = base; base += sz;
+                continue;
             }
-            b->hr[k] = base; base += sz;
+            b->hx[k] = base; base += sz;
+            b->hx[k1] = base; base += sz;
+            b->hf[k] = base; base += sz;
         }
     }
     int *di = b->d_int;
@@ -552,13 +727,18 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     BTRY(cudaMemcpy(d_dloc, b->dloc.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice));
     BTRY(cudaMemcpy(d_pb0, pb0.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice));
     BTRY(cudaMemcpy(d_pnb0, pnb0.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice));
-    if (!tbl.empty()) BTRY(cudaMemcpy(b->d_tbl, tbl.data(), sizeof(BlkEntry) * tbl.size(), cudaMemcpyHostToDevice));
+    BTRY(cudaMemcpy(b->d_tiles, tiles.data(), sizeof(TileEntry) * tiles.size(), cudaMemcpyHostToDevice));
     void **dp = b->d_ptrs;
     BTRY(cudaMemcpy(dp, b->hx.data(), sizeof(void *) * b->hx.size(), cudaMemcpyHostToDevice));
     BTRY(cudaMemcpy(dp + b->hx.size(), b->hf.data(), sizeof(void *) * b->hf.size(), cudaMemcpyHostToDevice));
-    BTRY(cudaMemcpy(dp + 2 * b->hx.size(), b->hr.data(), sizeof(void *) * b->hr.size(), cudaMemcpyHostToDevice));
-    b->d_psi_tab = (double **)(dp + 3 * b->hx.size());
-    b->d_f_tab = (double **)(dp + 3 * b->hx.size() + nprob);
+    // table layout: x (2 buffers), f, then the caller's psi and f per problem
+    b->d_psi_tab = (double **)(dp + b->hx.size() + b->hf.size());
+    b->d_f_tab = (double **)(dp + b->hx.size() + b->hf.size() + nprob);
+    if (b->hx.size() + b->hf.size() + 2 * (size_t)nprob != nptr) {
+        gb_set_error("gb_batch_create: pointer table layout mismatch");
+        gb_batch_destroy(b);
+        return GB_ERR_INVALID;
+    }
     BatchDev &D = b->dev;
     D.nprob = nprob;
     D.n_of = d_nof;
@@ -566,7 +746,8 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     D.dloc = d_dloc;
     D.x = dp;
     D.f = dp + b->hx.size();
-    D.r = dp + 2 * b->hx.size();
+    D.r = nullptr;
+    D.psi = b->d_psi_tab;
     D.active = d_active;
     D.cycles = d_cycles;
     D.failed = d_failed;
@@ -578,12 +759,8 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     D.num_active = d_numact;
     D.max_cycles = max_cycles;
     D.rtol = rtol;
-    if (b->local_smem > 48 * 1024) {
-        if (precision == GB_BATCH_FP64)
-            BTRY(cudaFuncSetAttribute(k_local_vcycle<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->local_smem));
-        else
-            BTRY(cudaFuncSetAttribute(k_local_vcycle<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->local_smem));
-    }
+    if (precision == GB_BATCH_FP64) BTRY(set_smem_attrs<double>(b->local_smem));
+    else BTRY(set_smem_attrs<float>(b->local_smem));
 #undef BTRY
     *out = b;
     return GB_OK;
@@ -598,7 +775,7 @@ extern "C" int gb_batch_destroy(gb_batch *b)
     cudaFree(b->d_int);
     cudaFree(b->d_dbl);
     cudaFree(b->d_ptrs);
-    cudaFree(b->d_tbl);
+    cudaFree(b->d_tiles);
     if (b->h_pinned) cudaFreeHost(b->h_pinned);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -618,79 +795,114 @@ static void prof_record(cudaEvent_t e, cudaStream_t s)
     else cudaEventRecord(e, s);
 }
 
-// The kernels of one V-cycle (descent over the global levels, the local
-// coarse solves, ascent), for element type T.
+// Launch plan of one level: how many sweeps each smoothing launch does
+// (two per launch in FP32, one in FP64, whose pipe is the bottleneck and
+// would pay for the wider halo's redundant updates).
+template <class T> static int sweeps_per_launch(int nu) { return (sizeof(T) == 4 && nu >= 2) ? 2 : 1; }
+template <class T> static int launches_for(int nu)
+{
+    int k = 0;
+    while (nu > 0) { nu -= sweeps_per_launch<T>(nu); ++k; }
+    return k;
+}
+
+template <class T>
+static void launch_smooth(gb_batch *b, int l, int k, int zero_init, int src, int dst, int correct, cudaStream_t s,
+                          bool timed)
+{
+    const int cnt = b->ft_cnt[l];
+    const TileEntry *t = b->d_tiles + b->ft_off[l];
+    const bool ev = timed && b->profile && b->ev_used + 2 <= (int)b->ev.size();
+    if (ev) prof_record(b->ev[b->ev_used], s);
+    if (k == 2) k_smooth<T, 2><<<cnt, TILE_THREADS, smem_smooth<T, 2>(), s>>>(b->dev, t, l, zero_init, src, dst, correct);
+    else k_smooth<T, 1><<<cnt, TILE_THREADS, smem_smooth<T, 1>(), s>>>(b->dev, t, l, zero_init, src, dst, correct);
+    if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
+    b->launches += 1;
+}
+
+// The kernels of one V-cycle: pre-smoothing, residual + restriction on each
+// tile level, the local coarse cycles, then prolongation + post-smoothing.
+// Tile kernels read one buffer of a level and write the other; the plan
+// below picks the buffers so that every coarse level ends in buffer 0 (where
+// the local kernel also leaves its levels) and the plain solve's level 0
+// ends in the caller's psi (buffer 0).
 template <class T>
 static void enqueue_vcycle(gb_batch *b, cudaStream_t s)
 {
-    BatchDev &D = b->dev;
-    const BlkEntry *tb = b->d_tbl;
-    long long &nl = b->launches;
-    // descent: level l is global for problems with dloc > l
+    const bool mixed = b->precision == GB_BATCH_MIXED;
+    int cur[BP_MAXL] = {0};
+    const int k1 = launches_for<T>(b->nu1);
+    const int pro = std::min(b->nu2, sizeof(T) == 4 ? 2 : 1);  // sweeps fused into the prolongation
+    const int k2 = launches_for<T>(b->nu2 - pro);
     for (int l = 0; l < b->maxdepth_global; ++l) {
-        const int cnt = b->tbl_cnt[l];
-        if (cnt == 0) continue;
-        const BlkEntry *t = tb + b->tbl_off[l];
-        for (int it = 0; it < b->nu1; ++it) {
-            for (int color = 0; color < 2; ++color) {
-                const bool ev = b->profile && l == 0 && b->ev_used + 2 <= (int)b->ev.size();
-                if (ev) prof_record(b->ev[b->ev_used], s);
-                k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, color);
-                if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
-            }
-            nl += 2;
+        if (b->ft_cnt[l] == 0) continue;
+        const bool zero = mixed || l > 0;
+        const int writes = k1 + 1 + k2;
+        int dst = zero ? ((writes - 1) & 1) : 1, src = 0;
+        int nu = b->nu1;
+        for (int i = 0; i < k1; ++i) {
+            const int k = sweeps_per_launch<T>(nu);
+            launch_smooth<T>(b, l, k, (zero && i == 0) ? 1 : 0, src, dst, 0, s, l == 0);
+            nu -= k;
+            src = dst;
+            dst = 1 - dst;
         }
-        k_residual<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l);
-        const int cntc = b->rtbl_cnt[l + 1];
-        k_restrict<T><<<cntc, BP_THREADS, 0, s>>>(D, tb + b->rtbl_off[l + 1], l);
-        nl += 2;
+        cur[l] = src;
+        k_resid_restrict<T><<<b->ct_cnt[l + 1], TILE_THREADS, smem_restrict<T>(), s>>>(
+            b->dev, b->d_tiles + b->ct_off[l + 1], l, cur[l]);
+        b->launches += 1;
     }
-    k_local_vcycle<T><<<b->nprob, BP_THREADS, b->local_smem, s>>>(D, b->nu1, b->nu2);
-    nl += 1;
+    k_local_vcycle<T><<<b->nprob, BP_THREADS, b->local_smem, s>>>(b->dev, b->nu1, b->nu2, mixed ? 1 : 0);
+    b->launches += 1;
     for (int l = b->maxdepth_global - 1; l >= 0; --l) {
-        const int cnt = b->tbl_cnt[l];
+        const int cnt = b->ft_cnt[l];
         if (cnt == 0) continue;
-        const BlkEntry *t = tb + b->tbl_off[l];
-        k_prolong_add<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l);
-        nl += 1;
-        for (int it = 0; it < b->nu2; ++it) {
-            for (int color = 0; color < 2; ++color) {
-                const bool ev = b->profile && l == 0 && b->ev_used + 2 <= (int)b->ev.size();
-                if (ev) prof_record(b->ev[b->ev_used], s);
-                k_rb_half<T><<<cnt, BP_THREADS, 0, s>>>(D, t, l, color);
-                if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
-            }
-            nl += 2;
+        const TileEntry *t = b->d_tiles + b->ft_off[l];
+        const int correct_last = (mixed && l == 0) ? 1 : 0;
+        int src = cur[l], dst = 1 - cur[l];
+        const int corr = (k2 == 0) ? correct_last : 0;
+        if (pro == 2) k_prolong_smooth<T, 2><<<cnt, TILE_THREADS, smem_smooth<T, 2>(), s>>>(b->dev, t, l, src, 0, dst, corr);
+        else if (pro == 1) k_prolong_smooth<T, 1><<<cnt, TILE_THREADS, smem_smooth<T, 1>(), s>>>(b->dev, t, l, src, 0, dst, corr);
+        else k_prolong_smooth<T, 0><<<cnt, TILE_THREADS, smem_smooth<T, 0>(), s>>>(b->dev, t, l, src, 0, dst, corr);
+        b->launches += 1;
+        src = dst;
+        dst = 1 - dst;
+        int nu = b->nu2 - pro;
+        for (int i = 0; i < k2; ++i) {
+            const int k = sweeps_per_launch<T>(nu);
+            launch_smooth<T>(b, l, k, 0, src, dst, (i == k2 - 1) ? correct_last : 0, s, false);
+            nu -= k;
+            src = dst;
+            dst = 1 - dst;
+        }
+        cur[l] = src;
+        if (!mixed && l == 0 && cur[0] != 0) {
+            k_copy_back<<<cnt, TILE_THREADS, 0, s>>>(b->dev, t);
+            b->launches += 1;
         }
     }
 }
 
-// One outer iteration: residual norm (and, mixed, the FP32 right-hand side),
-// convergence bookkeeping, one V-cycle, and (mixed) the FP64 correction.
+// One outer iteration: the FP64 residual norm of level 0 (mixed: also its
+// FP32 copy as the inner right-hand side), convergence bookkeeping, one
+// V-cycle (mixed: its last level-0 kernel adds the correction to psi).
 static void enqueue_iteration(gb_batch *b, int first, cudaStream_t s)
 {
     BatchDev &D = b->dev;
-    const BlkEntry *t0 = b->d_tbl + b->tbl0_off;
+    const TileEntry *t0 = b->d_tiles + b->ot_off;
     cudaMemsetAsync(D.num_active, 0, sizeof(int), s);
-    const int mode = b->precision == GB_BATCH_MIXED ? 1 : 0;
-    k_outer_residual<<<b->tbl0_cnt, BP_THREADS, 0, s>>>(D, t0, (const double *const *)b->d_psi_tab,
-                                                         (const double *const *)b->d_f_tab, mode);
-    k_finalize<<<gb_ceil_div(b->nprob, 128), 128, 0, s>>>(D, first);
+    const bool mixed = b->precision == GB_BATCH_MIXED;
+    k_outer<<<b->ot_cnt, TILE_THREADS, 0, s>>>(D, t0, (const double *const *)b->d_f_tab, mixed ? 1 : 0);
+    k_finalize<<<gb_ceil_div(b->nprob, 4), 128, 0, s>>>(D, first);
     b->launches += 2;
-    if (b->precision == GB_BATCH_FP64) {
-        enqueue_vcycle<double>(b, s);
-    } else {
-        enqueue_vcycle<float>(b, s);
-        k_correct<<<b->tbl0_cnt, BP_THREADS, 0, s>>>(D, t0, b->d_psi_tab);
-        b->launches += 1;
-    }
+    if (mixed) enqueue_vcycle<float>(b, s);
+    else enqueue_vcycle<double>(b, s);
     cudaMemcpyAsync(b->h_pinned, D.num_active, sizeof(int), cudaMemcpyDeviceToHost, s);
 }
 
-// After an iteration has completed: adds the recorded smoothing-launch times
-// and the algorithmic bytes of the problems that took part (1.5 words per
-// interior point per half-sweep: psi read, f read, psi written, each for
-// half of the points plus the neighbours' half).
+// After an iteration has completed: adds the recorded pre-smoothing launch
+// times and the algorithmic bytes of the problems that took part (per sweep
+// and interior point: psi read, f read, psi written, one word each).
 static void batch_profile_collect(gb_batch *b, cudaStream_t s)
 {
     if (!b->profile || b->ev_used == 0) return;
@@ -701,12 +913,13 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
     for (int p = 0; p < b->nprob; ++p)
         if (b->h_active[p] && b->dloc[p] > 0) pts += (double)(b->n[p] - 2) * (double)(b->n[p] - 2);
     const double esz = b->precision == GB_BATCH_FP64 ? 8.0 : 4.0;
+    const int per_launch_sweeps = (b->precision == GB_BATCH_MIXED && b->nu1 >= 2) ? 2 : 1;  // first pre-smoothing launch
     for (int i = 0; i + 1 < b->ev_used; i += 2) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]) == cudaSuccess) {
             b->prof_ms += ms;
             b->prof_launches += 1;
-            b->prof_bytes += 1.5 * esz * pts;
+            b->prof_bytes += 3.0 * esz * per_launch_sweeps * pts;
         } else {
             cudaGetLastError();  // timing is advisory: never let it fail a solve
         }
@@ -717,8 +930,7 @@ extern "C" int gb_batch_profile(gb_batch *b, int enable)
 {
     if (!b) return GB_ERR_INVALID;
     if (enable && b->ev.empty()) {
-        const int need = 2 * 2 * (b->nu1 + b->nu2) + 4;
-        b->ev.resize(need);
+        b->ev.resize(2 * (b->nu1 + 1));
         for (auto &e : b->ev) GB_CUDA_TRY(cudaEventCreate(&e));
     }
     b->profile = enable ? 1 : 0;
@@ -751,13 +963,16 @@ static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStre
     if (b->precision == GB_BATCH_FP64) {
         // level-0 x and f of the plain cycle are the caller's arrays
         for (int p = 0; p < b->nprob; ++p) {
-            b->hx[(size_t)p * BP_MAXL] = d_psi + b->off0[p];
+            b->hx[(size_t)p * BP_MAXL] = d_psi + b->off0[p];            // buffer 0 of level 0
             b->hf[(size_t)p * BP_MAXL] = (void *)(d_f + b->off0[p]);
         }
         GB_CUDA_TRY(cudaMemcpyAsync(b->d_ptrs, b->hx.data(), sizeof(void *) * b->hx.size(), cudaMemcpyHostToDevice, s));
         GB_CUDA_TRY(cudaMemcpyAsync(b->d_ptrs + b->hx.size(), b->hf.data(), sizeof(void *) * b->hf.size(),
                                     cudaMemcpyHostToDevice, s));
     }
+    // the pointer tables live in pageable host vectors: complete the copies
+    // before those vectors can change
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
     return GB_OK;
 }
 
@@ -780,7 +995,7 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
     enqueue_iteration(b, 1, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     batch_profile_collect(b, s);
-    if (!b->cycle_graph || b->graph_f != d_f || b->graph_psi != d_psi || b->graph_profile != b->profile) {
+    if (!b->cycle_graph || b->graph_profile != b->profile) {
         if (b->cycle_graph) cudaGraphExecDestroy(b->cycle_graph);
         b->cycle_graph = nullptr;
         cudaStream_t cs = b->stream;
@@ -794,8 +1009,6 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
         b->launches = l0;
         GB_CUDA_TRY(cudaGraphInstantiate(&b->cycle_graph, g, 0));
         cudaGraphDestroy(g);
-        b->graph_f = d_f;
-        b->graph_psi = d_psi;
         b->graph_profile = b->profile;
         b->graph_ev = b->ev_used;
     }

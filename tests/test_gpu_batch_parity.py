@@ -43,7 +43,7 @@ def independent_relres(sizes, f, psi):
     return np.array(out)
 
 
-SMALL = [3, 5, 9, 17, 33, 65, 129, 257, 65, 129, 3, 33]
+SMALL = [3, 5, 9, 17, 33, 65, 129, 257, 65, 129, 3, 33, 513]
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
