@@ -19,7 +19,7 @@ def offsets(sizes):
 
 
 class BatchPoisson:
-    def __init__(self, sizes, precision=_L.BATCH_FP64, nu1=2, nu2=2, rtol=1e-10, max_cycles=100):
+    def __init__(self, sizes, precision=_L.BATCH_FP64, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, inner=1):
         L = _L.load()
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
         self.offsets, self.total = offsets(self.sizes)
@@ -28,6 +28,8 @@ class BatchPoisson:
                                    nu1, nu2, rtol, max_cycles, C.byref(h)), "gb_batch_create")
         self._h = h
         self.nprob = len(self.sizes)
+        if inner != 1:
+            _L.check(L.gb_batch_set_inner_cycles(h, inner), "gb_batch_set_inner_cycles")
 
     def solve_device(self, d_f: int, d_psi: int, stream: int = 0):
         """d_f, d_psi: device addresses of packed float64 arrays."""

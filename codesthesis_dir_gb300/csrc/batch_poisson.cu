@@ -54,6 +54,7 @@ struct BatchDev {
     double *const *psi;       // [p] the caller's FP64 solution of level 0
     int *num_active;
     int max_cycles;
+    int inner;                // V-cycles per outer iteration (defect correction)
     double rtol;
 };
 
@@ -114,7 +115,7 @@ __device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int SX, int ox, 
 // Stores the tile's interior points into x, or (psi != nullptr) adds them to
 // the FP64 solution instead: the last level-0 kernel of an inner cycle
 // applies the defect correction psi += e point by point.
-template <class T>
+template <class T, bool CORRECT>
 __device__ __forceinline__ void tile_store(const T *sx, int SX, int ox, int oy, int x0, int y0, int n, T *x,
                                            double *psi)
 {
@@ -125,7 +126,7 @@ __device__ __forceinline__ void tile_store(const T *sx, int SX, int ox, int oy, 
         for (int gx = gxa + lane; gx < gxb; gx += 32) {
             const size_t g = (size_t)gy * n + gx;
             const T v = sx[(gy - oy) * SX + gx - ox];
-            if (psi) psi[g] = psi[g] + (double)v;
+            if (CORRECT) psi[g] = psi[g] + (double)v;
             else x[g] = v;
         }
 }
@@ -135,9 +136,9 @@ __device__ __forceinline__ void tile_store(const T *sx, int SX, int ox, int oy, 
 // level's current solution is zero (the correction of a coarse level, or the
 // FP32 correction of the defect-correction loop) and is not read.  correct:
 // add the result to the FP64 solution instead of storing it (level 0).
-template <class T, int NU>
+template <class T, int NU, bool CORR>
 __global__ void __launch_bounds__(TILE_THREADS) k_smooth(BatchDev B, const TileEntry *tiles, int l, int zero_init,
-                                                         int src, int dst, int correct)
+                                                         int src, int dst)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
@@ -148,33 +149,30 @@ __global__ void __launch_bounds__(TILE_THREADS) k_smooth(BatchDev B, const TileE
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
     const T *x = XS<T>(B, e.p, l, src);
     const T *f = FP<T>(B, e.p, l);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int r = warp; r < SY; r += nw) {
-        const int gy = oy + r;
-        const bool rowin = gy >= 0 && gy < n;
-        for (int c = lane; c < SX; c += 32) {
-            const int gx = ox + c;
-            T v = (T)0, fv = (T)0;
-            if (rowin && gx >= 0 && gx < n) {
-                const size_t g = (size_t)gy * n + gx;
-                fv = f[g];
-                if (!zero_init) v = x[g];
-            }
-            sx[r * SX + c] = v;
-            sf[r * SX + c] = fv;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
+        const int r = i / SX, c = i - r * SX;
+        const int gy = oy + r, gx = ox + c;
+        T v = (T)0, fv = (T)0;
+        if (gy >= 0 && gy < n && gx >= 0 && gx < n) {
+            const size_t g = (size_t)gy * n + gx;
+            fv = f[g];
+            if (!zero_init) v = x[g];
         }
+        sx[i] = v;
+        sf[i] = fv;
     }
     __syncthreads();
     tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
-    tile_store<T>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), correct ? B.psi[e.p] : nullptr);
+    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr);
 }
 
 // Bilinear prolongation of level l+1 (buffer csrc) added into level l
 // (buffer src) over the tile and its halo (rotann2.f:821-858), then NU
 // post-smoothing sweeps, stored into buffer dst (or added to psi: correct).
-template <class T, int NU>
+template <class T, int NU, bool CORR>
 __global__ void __launch_bounds__(TILE_THREADS) k_prolong_smooth(BatchDev B, const TileEntry *tiles, int l, int src,
-                                                                 int csrc, int dst, int correct)
+                                                                 int csrc, int dst)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
@@ -186,14 +184,13 @@ __global__ void __launch_bounds__(TILE_THREADS) k_prolong_smooth(BatchDev B, con
     const T *x = XS<T>(B, e.p, l, src);
     const T *f = FP<T>(B, e.p, l);
     const T *ec = XS<T>(B, e.p, l + 1, csrc);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int r = warp; r < SY; r += nw) {
-        const int gy = oy + r;
-        const bool rowin = gy >= 0 && gy < n;
-        for (int c = lane; c < SX; c += 32) {
-            const int gx = ox + c;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
+        const int r = i / SX, c = i - r * SX;
+        const int gy = oy + r, gx = ox + c;
+        {
             T v = (T)0, fv = (T)0;
-            if (rowin && gx >= 0 && gx < n) {
+            if (gy >= 0 && gy < n && gx >= 0 && gx < n) {
                 const size_t g = (size_t)gy * n + gx;
                 v = x[g];
                 if (NU > 0) fv = f[g];
@@ -214,13 +211,13 @@ __global__ void __launch_bounds__(TILE_THREADS) k_prolong_smooth(BatchDev B, con
                     v = v + p;
                 }
             }
-            sx[r * SX + c] = v;
-            if (NU > 0) sf[r * SX + c] = fv;
+            sx[i] = v;
+            if (NU > 0) sf[i] = fv;
         }
     }
     __syncthreads();
     if (NU > 0) tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
-    tile_store<T>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), correct ? B.psi[e.p] : nullptr);
+    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr);
 }
 
 // Residual of level l and its full weighting onto level l+1 (rotann2.f:
@@ -240,13 +237,11 @@ __global__ void __launch_bounds__(TILE_THREADS) k_resid_restrict(BatchDev B, con
     const T *f = FP<T>(B, e.p, l);
     T *fc = FP<T>(B, e.p, l + 1);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int r = warp; r < XH; r += nw) {
-        const int gy = ry - 1 + r;
-        const bool rowin = gy >= 0 && gy < n;
-        for (int c = lane; c < XW; c += 32) {
-            const int gx = rx - 1 + c;
-            sx[r * XW + c] = (rowin && gx >= 0 && gx < n) ? x[(size_t)gy * n + gx] : (T)0;
-        }
+#pragma unroll 4
+    for (int i = threadIdx.x; i < XW * XH; i += TILE_THREADS) {
+        const int r = i / XW, c = i - r * XW;
+        const int gy = ry - 1 + r, gx = rx - 1 + c;
+        sx[i] = (gy >= 0 && gy < n && gx >= 0 && gx < n) ? x[(size_t)gy * n + gx] : (T)0;
     }
     __syncthreads();
     const T h = (T)1 / (T)(n - 1), ih2 = (T)1 / (h * h);
@@ -298,7 +293,8 @@ __device__ void loc_rb_half(T *x, const T *f, int n, T h2, int color)
 }
 
 template <class T>
-__global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1, int nu2, int zero_level0)
+__global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1, int nu2, int zero_level0,
+                                                               int correct_level0)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = (T *)smem_raw;
@@ -395,7 +391,7 @@ __global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1
         // the local levels end in buffer 0; a mixed solve local from level 0
         // applies its correction to the FP64 solution directly
         const int n = B.n_of[p * BP_MAXL + d0];
-        if (d0 == 0 && zero_level0) {
+        if (d0 == 0 && correct_level0) {
             double *psi = B.psi[p];
             for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = psi[q] + (double)X[q];
         } else {
@@ -515,7 +511,7 @@ __global__ void k_finalize(BatchDev B, int first)
         B.active[p] = 0;
         B.failed[p] = 1;
     } else {
-        B.cycles[p] += 1;
+        B.cycles[p] += B.inner;
         atomicAdd(B.num_active, 1);
     }
 }
@@ -525,6 +521,8 @@ __global__ void k_finalize(BatchDev B, int first)
 // ---------------------------------------------------------------------------
 struct gb_batch {
     int nprob = 0, precision = 0, nu1 = 2, nu2 = 2, max_cycles = 100;
+    int inner = 1;                      // V-cycles per outer iteration (mixed)
+    int cur0 = 0;                       // level-0 buffer holding the correction between inner cycles
     double rtol = 1e-10;
     std::vector<int> n, L, dloc;
     long long total = 0;
@@ -574,11 +572,16 @@ template <class T> static cudaError_t set_smem_attrs(size_t local)
 {
     cudaError_t e;
 #define SA(k, sz) if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sz))) != cudaSuccess) return e
-    SA((k_smooth<T, 1>), (smem_smooth<T, 1>()));
-    SA((k_smooth<T, 2>), (smem_smooth<T, 2>()));
-    SA((k_prolong_smooth<T, 0>), (smem_smooth<T, 0>()));
-    SA((k_prolong_smooth<T, 1>), (smem_smooth<T, 1>()));
-    SA((k_prolong_smooth<T, 2>), (smem_smooth<T, 2>()));
+    SA((k_smooth<T, 1, false>), (smem_smooth<T, 1>()));
+    SA((k_smooth<T, 2, false>), (smem_smooth<T, 2>()));
+    SA((k_smooth<T, 1, true>), (smem_smooth<T, 1>()));
+    SA((k_smooth<T, 2, true>), (smem_smooth<T, 2>()));
+    SA((k_prolong_smooth<T, 0, false>), (smem_smooth<T, 0>()));
+    SA((k_prolong_smooth<T, 1, false>), (smem_smooth<T, 1>()));
+    SA((k_prolong_smooth<T, 2, false>), (smem_smooth<T, 2>()));
+    SA((k_prolong_smooth<T, 0, true>), (smem_smooth<T, 0>()));
+    SA((k_prolong_smooth<T, 1, true>), (smem_smooth<T, 1>()));
+    SA((k_prolong_smooth<T, 2, true>), (smem_smooth<T, 2>()));
     SA((k_resid_restrict<T>), (smem_restrict<T>()));
     SA((k_local_vcycle<T>), (local));
 #undef SA
@@ -758,6 +761,7 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     D.p_nblk0 = d_pnb0;
     D.num_active = d_numact;
     D.max_cycles = max_cycles;
+    D.inner = 1;
     D.rtol = rtol;
     if (precision == GB_BATCH_FP64) BTRY(set_smem_attrs<double>(b->local_smem));
     else BTRY(set_smem_attrs<float>(b->local_smem));
@@ -783,6 +787,21 @@ extern "C" int gb_batch_destroy(gb_batch *b)
 }
 
 extern "C" long long gb_batch_total_points(const gb_batch *b) { return b ? b->total : 0; }
+
+extern "C" int gb_batch_set_inner_cycles(gb_batch *b, int inner)
+{
+    if (!b || inner < 1 || inner > 16 || (b->precision == GB_BATCH_FP64 && inner != 1)) {
+        gb_set_error("gb_batch_set_inner_cycles: need 1 <= inner <= 16 (and 1 for the plain FP64 solve)");
+        return GB_ERR_INVALID;
+    }
+    if (inner != b->inner && b->cycle_graph) {
+        cudaGraphExecDestroy(b->cycle_graph);
+        b->cycle_graph = nullptr;
+    }
+    b->inner = inner;
+    b->dev.inner = inner;
+    return GB_OK;
+}
 extern "C" long long gb_batch_last_launches(const gb_batch *b) { return b ? b->launches : 0; }
 
 // Records a timing event: as an event node of the graph while the stream is
@@ -813,21 +832,40 @@ static void launch_smooth(gb_batch *b, int l, int k, int zero_init, int src, int
     const int cnt = b->ft_cnt[l];
     const TileEntry *t = b->d_tiles + b->ft_off[l];
     const bool ev = timed && b->profile && b->ev_used + 2 <= (int)b->ev.size();
+    const size_t sm = k == 2 ? smem_smooth<T, 2>() : smem_smooth<T, 1>();
     if (ev) prof_record(b->ev[b->ev_used], s);
-    if (k == 2) k_smooth<T, 2><<<cnt, TILE_THREADS, smem_smooth<T, 2>(), s>>>(b->dev, t, l, zero_init, src, dst, correct);
-    else k_smooth<T, 1><<<cnt, TILE_THREADS, smem_smooth<T, 1>(), s>>>(b->dev, t, l, zero_init, src, dst, correct);
+    if (k == 2 && correct) k_smooth<T, 2, true><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
+    else if (k == 2) k_smooth<T, 2, false><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
+    else if (correct) k_smooth<T, 1, true><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
+    else k_smooth<T, 1, false><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
     if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
+    b->launches += 1;
+}
+
+template <class T>
+static void launch_prolong(gb_batch *b, int l, int nu, int src, int dst, int correct, cudaStream_t s)
+{
+    const int cnt = b->ft_cnt[l];
+    const TileEntry *t = b->d_tiles + b->ft_off[l];
+#define PL(NU, C) k_prolong_smooth<T, NU, C><<<cnt, TILE_THREADS, smem_smooth<T, NU>(), s>>>(b->dev, t, l, src, 0, dst)
+    if (nu == 2) { if (correct) PL(2, true); else PL(2, false); }
+    else if (nu == 1) { if (correct) PL(1, true); else PL(1, false); }
+    else { if (correct) PL(0, true); else PL(0, false); }
+#undef PL
     b->launches += 1;
 }
 
 // The kernels of one V-cycle: pre-smoothing, residual + restriction on each
 // tile level, the local coarse cycles, then prolongation + post-smoothing.
 // Tile kernels read one buffer of a level and write the other; the plan
-// below picks the buffers so that every coarse level ends in buffer 0 (where
-// the local kernel also leaves its levels) and the plain solve's level 0
-// ends in the caller's psi (buffer 0).
+// picks the buffers so that every coarse level ends in buffer 0 (where the
+// local kernel also leaves its levels) and the plain solve's level 0 ends in
+// the caller's psi (buffer 0).  Mixed: zero0 = the level-0 correction starts
+// at zero (first inner cycle of an outer iteration), corr0 = the last
+// level-0 kernel adds the correction to psi (last inner cycle); between
+// inner cycles the correction waits in level-0 buffer b->cur0.
 template <class T>
-static void enqueue_vcycle(gb_batch *b, cudaStream_t s)
+static void enqueue_vcycle(gb_batch *b, cudaStream_t s, bool zero0, bool corr0)
 {
     const bool mixed = b->precision == GB_BATCH_MIXED;
     int cur[BP_MAXL] = {0};
@@ -836,9 +874,12 @@ static void enqueue_vcycle(gb_batch *b, cudaStream_t s)
     const int k2 = launches_for<T>(b->nu2 - pro);
     for (int l = 0; l < b->maxdepth_global; ++l) {
         if (b->ft_cnt[l] == 0) continue;
-        const bool zero = mixed || l > 0;
+        const bool zero = l > 0 || (mixed && zero0);
         const int writes = k1 + 1 + k2;
-        int dst = zero ? ((writes - 1) & 1) : 1, src = 0;
+        int src, dst;
+        if (zero) { dst = (writes - 1) & 1; src = 1 - dst; }
+        else if (mixed) { src = b->cur0; dst = 1 - src; }   // level 0, later inner cycle
+        else { src = 0; dst = 1; }                          // level 0 of the plain solve: psi
         int nu = b->nu1;
         for (int i = 0; i < k1; ++i) {
             const int k = sweeps_per_launch<T>(nu);
@@ -852,19 +893,14 @@ static void enqueue_vcycle(gb_batch *b, cudaStream_t s)
             b->dev, b->d_tiles + b->ct_off[l + 1], l, cur[l]);
         b->launches += 1;
     }
-    k_local_vcycle<T><<<b->nprob, BP_THREADS, b->local_smem, s>>>(b->dev, b->nu1, b->nu2, mixed ? 1 : 0);
+    k_local_vcycle<T><<<b->nprob, BP_THREADS, b->local_smem, s>>>(b->dev, b->nu1, b->nu2, (mixed && zero0) ? 1 : 0,
+                                                                 (mixed && corr0) ? 1 : 0);
     b->launches += 1;
     for (int l = b->maxdepth_global - 1; l >= 0; --l) {
-        const int cnt = b->ft_cnt[l];
-        if (cnt == 0) continue;
-        const TileEntry *t = b->d_tiles + b->ft_off[l];
-        const int correct_last = (mixed && l == 0) ? 1 : 0;
+        if (b->ft_cnt[l] == 0) continue;
+        const int correct_last = (mixed && l == 0 && corr0) ? 1 : 0;
         int src = cur[l], dst = 1 - cur[l];
-        const int corr = (k2 == 0) ? correct_last : 0;
-        if (pro == 2) k_prolong_smooth<T, 2><<<cnt, TILE_THREADS, smem_smooth<T, 2>(), s>>>(b->dev, t, l, src, 0, dst, corr);
-        else if (pro == 1) k_prolong_smooth<T, 1><<<cnt, TILE_THREADS, smem_smooth<T, 1>(), s>>>(b->dev, t, l, src, 0, dst, corr);
-        else k_prolong_smooth<T, 0><<<cnt, TILE_THREADS, smem_smooth<T, 0>(), s>>>(b->dev, t, l, src, 0, dst, corr);
-        b->launches += 1;
+        launch_prolong<T>(b, l, pro, src, dst, k2 == 0 ? correct_last : 0, s);
         src = dst;
         dst = 1 - dst;
         int nu = b->nu2 - pro;
@@ -877,15 +913,17 @@ static void enqueue_vcycle(gb_batch *b, cudaStream_t s)
         }
         cur[l] = src;
         if (!mixed && l == 0 && cur[0] != 0) {
-            k_copy_back<<<cnt, TILE_THREADS, 0, s>>>(b->dev, t);
+            k_copy_back<<<b->ft_cnt[0], TILE_THREADS, 0, s>>>(b->dev, b->d_tiles + b->ft_off[0]);
             b->launches += 1;
         }
     }
+    if (mixed) b->cur0 = cur[0];
 }
 
 // One outer iteration: the FP64 residual norm of level 0 (mixed: also its
-// FP32 copy as the inner right-hand side), convergence bookkeeping, one
-// V-cycle (mixed: its last level-0 kernel adds the correction to psi).
+// FP32 copy as the inner right-hand side), convergence bookkeeping, then
+// b->inner V-cycles (mixed: the last one's final level-0 kernel adds the
+// correction to psi).
 static void enqueue_iteration(gb_batch *b, int first, cudaStream_t s)
 {
     BatchDev &D = b->dev;
@@ -895,8 +933,12 @@ static void enqueue_iteration(gb_batch *b, int first, cudaStream_t s)
     k_outer<<<b->ot_cnt, TILE_THREADS, 0, s>>>(D, t0, (const double *const *)b->d_f_tab, mixed ? 1 : 0);
     k_finalize<<<gb_ceil_div(b->nprob, 4), 128, 0, s>>>(D, first);
     b->launches += 2;
-    if (mixed) enqueue_vcycle<float>(b, s);
-    else enqueue_vcycle<double>(b, s);
+    if (mixed) {
+        b->cur0 = 0;
+        for (int k = 0; k < b->inner; ++k) enqueue_vcycle<float>(b, s, k == 0, k == b->inner - 1);
+    } else {
+        enqueue_vcycle<double>(b, s, false, false);
+    }
     cudaMemcpyAsync(b->h_pinned, D.num_active, sizeof(int), cudaMemcpyDeviceToHost, s);
 }
 

@@ -94,6 +94,7 @@ SIGNATURES = [
     ("gb_batch_create", C.c_int, [C.c_int, _ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(_vp)]),
     ("gb_batch_destroy", C.c_int, [_vp]),
     ("gb_batch_total_points", C.c_longlong, [_vp]),
+    ("gb_batch_set_inner_cycles", C.c_int, [_vp, C.c_int]),
     ("gb_batch_solve_device", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("gb_batch_solve_host", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     ("gb_batch_last_launches", C.c_longlong, [_vp]),

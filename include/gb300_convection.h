@@ -195,6 +195,11 @@ typedef struct gb_batch gb_batch;
 int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
                     int max_cycles, gb_batch **out);
 int gb_batch_destroy(gb_batch *b);
+/* Mixed solves only: V-cycles per outer (FP64 defect-correction)
+ * iteration, 1..16 (default 1).  With k > 1 the FP64 residual, its norm
+ * and the FP64 update run once per k inner cycles, and convergence is
+ * tested every k cycles. */
+int gb_batch_set_inner_cycles(gb_batch *b, int inner);
 /* Total doubles of the packed f / psi arrays. */
 long long gb_batch_total_points(const gb_batch *b);
 /* Device-resident solve: d_f, d_psi device pointers (packed).  cycles and

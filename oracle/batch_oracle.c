@@ -158,7 +158,7 @@ static int levels_of(int n, int *nl)
 }
 
 static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, double rtol,
-                     int max_cycles, int precision, int *cycles_out, double *relres_out)
+                     int max_cycles, int precision, int inner, int *cycles_out, double *relres_out)
 {
     int nl[32];
     int L = levels_of(n, nl);
@@ -210,16 +210,16 @@ static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, doub
             rn = sqrt(s);
             if (rn <= rtol * fn) break;
             if (cycles >= max_cycles) { status = 1; break; }
-            /* FP32 inner V-cycle on A e = r, e0 = 0 */
+            /* inner FP32 V-cycles on A e = r, e0 = 0 */
             for (size_t c = 0; c < nn; ++c) F[0][c] = (float)r64[c];
             memset(P[0], 0, sizeof(float) * nn);
-            vcycle_32(L, nl, P, F, R, nu1, nu2, 0);
+            for (int k = 0; k < inner; ++k) vcycle_32(L, nl, P, F, R, nu1, nu2, 0);
             for (int j = 1; j <= n - 2; ++j)
                 for (int i = 1; i <= n - 2; ++i) {
                     size_t c = (size_t)j * n + i;
                     psi[c] = psi[c] + (double)P[0][c];
                 }
-            ++cycles;
+            cycles += inner;
         }
         free(pool);
     }
@@ -231,13 +231,14 @@ static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, doub
 
 int orc_batch_solve(int nprob, const int *n, const long long *offset, const double *f,
                     double *psi, int nu1, int nu2, double rtol, int max_cycles,
-                    int precision, int *cycles, double *relres)
+                    int precision, int inner, int *cycles, double *relres)
 {
+    if (inner < 1) inner = 1;
     int status = 0;
 #pragma omp parallel for schedule(dynamic, 1) reduction(| : status)
     for (int p = 0; p < nprob; ++p) {
         status |= solve_one(n[p], f + offset[p], psi + offset[p], nu1, nu2, rtol, max_cycles,
-                            precision, &cycles[p], &relres[p]);
+                            precision, inner, &cycles[p], &relres[p]);
     }
     return status;
 }

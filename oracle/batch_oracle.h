@@ -29,11 +29,12 @@ extern "C" {
 
 /* Solve every problem.  psi is overwritten (initial guess zero).  cycles[p]
  * receives the V-cycles taken, relres[p] the final ||f - A psi||_2/||f||_2.
+ * inner: FP32 V-cycles per FP64 defect-correction step (mixed only).
  * Returns 0, or 1 if any problem hit max_cycles. Uses OpenMP threads over
  * problems when built with -fopenmp. */
 int orc_batch_solve(int nprob, const int *n, const long long *offset,
                     const double *f, double *psi, int nu1, int nu2,
-                    double rtol, int max_cycles, int precision,
+                    double rtol, int max_cycles, int precision, int inner,
                     int *cycles, double *relres);
 
 /* Building blocks on one grid, exposed for unit tests. */

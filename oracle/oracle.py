@@ -86,7 +86,7 @@ def lib():
         L.orc_prb_step.restype = C.c_int
         L.orc_prb_initial.argtypes = [C.POINTER(PRB), C.c_int, C.c_ulonglong, C.c_double]
         L.orc_batch_solve.argtypes = [C.c_int, _ip, C.POINTER(C.c_longlong), _dp, _dp, C.c_int,
-                                      C.c_int, C.c_double, C.c_int, C.c_int, _ip, _dp]
+                                      C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _ip, _dp]
         L.orc_batch_solve.restype = C.c_int
         for nm in ("orc_rb_sweep64",):
             getattr(L, nm).argtypes = [C.c_int, _dp, _dp]
@@ -226,7 +226,7 @@ def batch_offsets(sizes):
     return sizes, off, total
 
 
-def batch_solve(sizes, f, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, precision=0):
+def batch_solve(sizes, f, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, precision=0, inner=1):
     sizes, off, total = batch_offsets(sizes)
     f = np.ascontiguousarray(f, dtype=np.float64)
     assert f.size == total
@@ -234,6 +234,6 @@ def batch_solve(sizes, f, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, precision=0)
     cyc = np.zeros(len(sizes), dtype=np.int32)
     rr = np.zeros(len(sizes))
     st = lib().orc_batch_solve(len(sizes), iptr(sizes), off.ctypes.data_as(C.POINTER(C.c_longlong)),
-                               ptr(f), ptr(psi), nu1, nu2, rtol, max_cycles, precision,
+                               ptr(f), ptr(psi), nu1, nu2, rtol, max_cycles, precision, inner,
                                iptr(cyc), ptr(rr))
     return st, psi, cyc, rr

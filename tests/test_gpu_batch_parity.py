@@ -46,12 +46,13 @@ def independent_relres(sizes, f, psi):
 SMALL = [3, 5, 9, 17, 33, 65, 129, 257, 65, 129, 3, 33, 513]
 
 
-@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
-def test_batch_matches_oracle(oracle, gblib, precision):
+@pytest.mark.parametrize("precision,inner", [(0, 1), (1, 1), (1, 2), (1, 3)],
+                         ids=["fp64", "mixed", "mixed-inner2", "mixed-inner3"])
+def test_batch_matches_oracle(oracle, gblib, precision, inner):
     from codesthesis_dir_gb300.batch import BatchPoisson
     f = make_batch(SMALL, 7)
-    st_o, psi_o, cyc_o, rr_o = oracle.batch_solve(SMALL, f, precision=precision)
-    bp = BatchPoisson(SMALL, precision=precision)
+    st_o, psi_o, cyc_o, rr_o = oracle.batch_solve(SMALL, f, precision=precision, inner=inner)
+    bp = BatchPoisson(SMALL, precision=precision, inner=inner)
     st, psi, cyc, rr = bp.solve_host(f)
     assert st == 0 and st_o == 0
     np.testing.assert_array_equal(cyc, cyc_o)
