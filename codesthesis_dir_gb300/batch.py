@@ -19,7 +19,8 @@ def offsets(sizes):
 
 
 class BatchPoisson:
-    def __init__(self, sizes, precision=_L.BATCH_FP64, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, inner=1):
+    def __init__(self, sizes, precision=_L.BATCH_FP64, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, inner=1,
+                 exec_mode=None):
         L = _L.load()
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
         self.offsets, self.total = offsets(self.sizes)
@@ -30,6 +31,8 @@ class BatchPoisson:
         self.nprob = len(self.sizes)
         if inner != 1:
             _L.check(L.gb_batch_set_inner_cycles(h, inner), "gb_batch_set_inner_cycles")
+        if exec_mode is not None:
+            _L.check(L.gb_batch_set_exec(h, exec_mode), "gb_batch_set_exec")
 
     def solve_device(self, d_f: int, d_psi: int, stream: int = 0):
         """d_f, d_psi: device addresses of packed float64 arrays."""

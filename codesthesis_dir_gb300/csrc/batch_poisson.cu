@@ -32,6 +32,42 @@ template <class T> __device__ __forceinline__ T fmaT(T a, T b, T c);
 template <> __device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
 template <> __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
+// Conversions between float and double on the integer pipe.  GB300 issues
+// FP64 instructions (conversions included) at about 1/64 of the FP32 rate,
+// and the defect-correction loop converts every point twice per outer
+// iteration.  Both functions round exactly as the hardware conversions
+// (round to nearest even; float -> double is exact); values outside the
+// normal float range take the hardware path.
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int hi = (unsigned int)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    if (e >= 897 && e <= 1150) {
+        const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+        unsigned int r = (hi & 0x80000000u) | ((unsigned int)(e - 896) << 23) | (unsigned int)(m >> 29);
+        const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull);
+        r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float(r);
+    }
+    return __double2float_rn(x);
+}
+
+__device__ __forceinline__ double f2d(float v)
+{
+    const unsigned int u = __float_as_uint(v);
+    const unsigned int e = (u >> 23) & 0xffu;
+    if (e != 0u && e != 255u)
+        return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                                ((unsigned long long)(e + 896u) << 52) |
+                                                ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+    if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(u & 0x80000000u) << 32));
+    return (double)v;
+}
+
+__device__ __forceinline__ double to_double(float v) { return f2d(v); }
+__device__ __forceinline__ double to_double(double v) { return v; }
+
 struct TileEntry {
     int p;            // problem
     short tx, ty;     // tile index (origin tx*TX, ty*TY in grid points)
@@ -66,19 +102,23 @@ template <class T> __device__ __forceinline__ T *FP(const BatchDev &B, int p, in
 template <class T> __device__ __forceinline__ T *RP(const BatchDev &B, int p, int l) { return (T *)B.r[p * BP_MAXL + l]; }
 
 // ---------------------------------------------------------------------------
-// Level-synchronous tile kernels (one table entry per block)
+// Tile operations
 //
-// A fine tile is TX x TY grid points with origin (tx*TX, ty*TY); a block
-// stages the tile plus a halo of H = 2*NU points in shared memory and runs
-// NU red-black sweeps there: sweep s updates red on ring H-1-2s and black
-// on ring H-2-2s, so after NU sweeps the tile itself is exact.  Points on
-// the Dirichlet boundary or outside the grid are never updated.
+// A fine tile is TX x TY grid points with origin (tx*TX, ty*TY); the block
+// stages the tile plus a halo of H points in shared memory and runs NU
+// red-black sweeps there: sweep s updates red on ring H-1-2s and black on
+// ring H-2-2s, so after NU sweeps the tile plus ring H-2*NU is exact.
+// Points on the Dirichlet boundary or outside the grid are never updated.
+// Every operation reads one buffer of a level and writes another (or a
+// different array), because neighbouring tiles read each other's points as
+// halo while they run.  Each operation ends with a block barrier so that a
+// block may run the next operation in the same shared memory.
 // ---------------------------------------------------------------------------
 #define TX 128
 #define TY 32
-#define CX 64    // coarse tile of the restriction kernel (fine 128 x 32)
-#define CY 16
 #define TILE_THREADS 256
+#define ST_R (TY / 8)    // rows a thread stores: TILE_THREADS / 32 warps step through TY rows
+#define ST_C (TX / 32)   // columns a thread stores
 
 // One red (color 0) or black (color 1) phase on ring rho around the tile.
 // The smem array has origin (ox, oy) in grid coordinates and row stride SX.
@@ -112,43 +152,49 @@ __device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int SX, int ox, 
     }
 }
 
-// Stores the tile's interior points into x, or (psi != nullptr) adds them to
-// the FP64 solution instead: the last level-0 kernel of an inner cycle
-// applies the defect correction psi += e point by point.
+// psi values of the points this thread stores (fixed assignment: row
+// warp + 8*rr, column lane + 32*cc of the tile), fetched before the sweeps
+// so that the defect correction's read of psi does not wait at the store.
+__device__ __forceinline__ void psi_prefetch(const double *psi, int x0, int y0, int n, double (&pv)[ST_R * ST_C])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int rr = 0; rr < ST_R; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < ST_C; ++cc) {
+            const int gy = y0 + warp + 8 * rr, gx = x0 + lane + 32 * cc;
+            const bool in = gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2;
+            pv[rr * ST_C + cc] = in ? psi[(size_t)gy * n + gx] : 0.0;
+        }
+}
+
+// Stores the tile's interior points into x, or (CORRECT) adds them to the
+// FP64 solution: the last level-0 operation of an inner cycle applies the
+// defect correction psi += e point by point.
 template <class T, bool CORRECT>
 __device__ __forceinline__ void tile_store(const T *sx, int SX, int ox, int oy, int x0, int y0, int n, T *x,
-                                           double *psi)
+                                           double *psi, const double (&pv)[ST_R * ST_C])
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int gxa = max(x0, 1), gxb = min(x0 + TX, n - 1);
-    const int gya = max(y0, 1), gyb = min(y0 + TY, n - 1);
-    for (int gy = gya + warp; gy < gyb; gy += nw)
-        for (int gx = gxa + lane; gx < gxb; gx += 32) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int rr = 0; rr < ST_R; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < ST_C; ++cc) {
+            const int gy = y0 + warp + 8 * rr, gx = x0 + lane + 32 * cc;
+            if (gx < 1 || gx > n - 2 || gy < 1 || gy > n - 2) continue;
             const size_t g = (size_t)gy * n + gx;
             const T v = sx[(gy - oy) * SX + gx - ox];
-            if (CORRECT) psi[g] = psi[g] + (double)v;
+            if (CORRECT) psi[g] = pv[rr * ST_C + cc] + to_double(v);
             else x[g] = v;
         }
 }
 
-// NU smoothing sweeps of level l from buffer src into buffer dst (never the
-// same buffer: blocks read their neighbours' tiles as halo).  zero_init: the
-// level's current solution is zero (the correction of a coarse level, or the
-// FP32 correction of the defect-correction loop) and is not read.  correct:
-// add the result to the FP64 solution instead of storing it (level 0).
-template <class T, int NU, bool CORR>
-__global__ void __launch_bounds__(TILE_THREADS) k_smooth(BatchDev B, const TileEntry *tiles, int l, int zero_init,
-                                                         int src, int dst)
+// Loads x (or zeros) and f over the tile plus an H halo.
+template <class T, int H>
+__device__ __forceinline__ void tile_load(T *sx, T *sf, const T *x, const T *f, int ox, int oy, int n,
+                                          bool zero_x, bool load_f)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
-    T *sx = (T *)smem_raw, *sf = sx + SX * SY;
-    const TileEntry e = tiles[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL + l];
-    const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
-    const T *x = XS<T>(B, e.p, l, src);
-    const T *f = FP<T>(B, e.p, l);
+    constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
 #pragma unroll 4
     for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
         const int r = i / SX, c = i - r * SX;
@@ -156,127 +202,124 @@ __global__ void __launch_bounds__(TILE_THREADS) k_smooth(BatchDev B, const TileE
         T v = (T)0, fv = (T)0;
         if (gy >= 0 && gy < n && gx >= 0 && gx < n) {
             const size_t g = (size_t)gy * n + gx;
-            fv = f[g];
-            if (!zero_init) v = x[g];
+            if (load_f) fv = f[g];
+            if (!zero_x) v = x[g];
         }
         sx[i] = v;
-        sf[i] = fv;
+        if (load_f) sf[i] = fv;
     }
-    __syncthreads();
-    tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
-    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr);
 }
 
-// Bilinear prolongation of level l+1 (buffer csrc) added into level l
-// (buffer src) over the tile and its halo (rotann2.f:821-858), then NU
-// post-smoothing sweeps, stored into buffer dst (or added to psi: correct).
-template <class T, int NU, bool CORR>
-__global__ void __launch_bounds__(TILE_THREADS) k_prolong_smooth(BatchDev B, const TileEntry *tiles, int l, int src,
-                                                                 int csrc, int dst)
+// NU smoothing sweeps of level l from buffer src into buffer dst.
+// zero_init: the level's current solution is zero (a coarse-level
+// correction, or the FP32 correction of the defect-correction loop) and is
+// not read.  RESTRICT: also form the residual on the tile plus one ring and
+// its full weighting (rotann2.f:773-785 summation order) onto the coarse
+// points of the tile, which the halo of 2*NU + 2 makes exact.
+template <class T, int NU, bool CORR, bool RESTRICT>
+__device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, int src, int dst,
+                          unsigned char *smem)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int H = 2 * NU + (RESTRICT ? 2 : 0), SX = TX + 2 * H, SY = TY + 2 * H;
+    T *sx = (T *)smem, *sf = sx + SX * SY;
+    const int n = B.n_of[e.p * BP_MAXL + l];
+    const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
+    double pv[ST_R * ST_C];
+    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
+    tile_load<T, H>(sx, sf, XS<T>(B, e.p, l, src), FP<T>(B, e.p, l), ox, oy, n, zero_init != 0, true);
+    __syncthreads();
+    tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
+    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
+    if (RESTRICT) {
+        // residual on the tile plus one ring, in place of f
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        const T h = (T)1 / (T)(n - 1), ih2 = (T)1 / (h * h);
+        for (int gy = y0 - 1 + warp; gy <= y0 + TY; gy += nw) {
+            for (int gx = x0 - 1 + lane; gx <= x0 + TX; gx += 32) {
+                const int q = (gy - oy) * SX + gx - ox;
+                T rv = (T)0;
+                if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
+                    const T s = (sx[q - 1] + sx[q + 1]) + (sx[q - SX] + sx[q + SX]);
+                    const T lap = fmaT<T>((T)-4, sx[q], s);
+                    rv = fmaT<T>(-ih2, lap, sf[q]);
+                }
+                sf[q] = rv;
+            }
+        }
+        __syncthreads();
+        const int nc = B.n_of[e.p * BP_MAXL + l + 1];
+        T *fc = FP<T>(B, e.p, l + 1);
+        const int Ia = max(x0 / 2, 1), Ib = min(x0 / 2 + TX / 2, nc - 1);
+        const int Ja = max(y0 / 2, 1), Jb = min(y0 / 2 + TY / 2, nc - 1);
+        for (int J = Ja + warp; J < Jb; J += nw) {
+            for (int I = Ia + lane; I < Ib; I += 32) {
+                const int q = (2 * J - oy) * SX + 2 * I - ox;
+                T t = sf[q];
+                t = t * (T)2 + sf[q + 1] + sf[q - 1];
+                t = t + sf[q + SX] + sf[q - SX];
+                t = t * (T)2 + sf[q + 1 + SX] + sf[q - 1 - SX];
+                t = t + sf[q + 1 - SX] + sf[q - 1 + SX];
+                fc[(size_t)J * nc + I] = t * (T)0.0625;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Bilinear prolongation of level l+1 (buffer 0) added into level l (buffer
+// src) over the tile and its halo (rotann2.f:821-858), then NU
+// post-smoothing sweeps, stored into buffer dst (or added to psi: CORR).
+template <class T, int NU, bool CORR>
+__device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int dst, unsigned char *smem)
+{
     constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
-    T *sx = (T *)smem_raw, *sf = sx + SX * SY;
-    const TileEntry e = tiles[blockIdx.x];
-    if (!B.active[e.p]) return;
+    T *sx = (T *)smem, *sf = sx + SX * SY;
     const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1];
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
+    double pv[ST_R * ST_C];
+    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
     const T *x = XS<T>(B, e.p, l, src);
     const T *f = FP<T>(B, e.p, l);
-    const T *ec = XS<T>(B, e.p, l + 1, csrc);
+    const T *ec = XS<T>(B, e.p, l + 1, 0);
 #pragma unroll 4
     for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
         const int r = i / SX, c = i - r * SX;
         const int gy = oy + r, gx = ox + c;
-        {
-            T v = (T)0, fv = (T)0;
-            if (gy >= 0 && gy < n && gx >= 0 && gx < n) {
-                const size_t g = (size_t)gy * n + gx;
-                v = x[g];
-                if (NU > 0) fv = f[g];
-                if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
-                    const T *ep = ec + (size_t)(gy / 2) * nc + (gx / 2);
-                    T p;
-                    if ((gx & 1) == 0) {
-                        if ((gy & 1) == 0) p = ep[0];
-                        else p = (ep[0] + ep[nc]) * (T)0.5;
-                    } else {
-                        if ((gy & 1) == 0) p = (ep[0] + ep[1]) * (T)0.5;
-                        else {
-                            T t = ep[0] + ep[nc + 1];
-                            t = t + ep[nc] + ep[1];
-                            p = t * (T)0.25;
-                        }
+        T v = (T)0, fv = (T)0;
+        if (gy >= 0 && gy < n && gx >= 0 && gx < n) {
+            const size_t g = (size_t)gy * n + gx;
+            v = x[g];
+            if (NU > 0) fv = f[g];
+            if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
+                const T *ep = ec + (size_t)(gy / 2) * nc + (gx / 2);
+                T pr;
+                if ((gx & 1) == 0) {
+                    if ((gy & 1) == 0) pr = ep[0];
+                    else pr = (ep[0] + ep[nc]) * (T)0.5;
+                } else {
+                    if ((gy & 1) == 0) pr = (ep[0] + ep[1]) * (T)0.5;
+                    else {
+                        T t = ep[0] + ep[nc + 1];
+                        t = t + ep[nc] + ep[1];
+                        pr = t * (T)0.25;
                     }
-                    v = v + p;
                 }
+                v = v + pr;
             }
-            sx[i] = v;
-            if (NU > 0) sf[i] = fv;
         }
+        sx[i] = v;
+        if (NU > 0) sf[i] = fv;
     }
     __syncthreads();
     if (NU > 0) tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
-    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr);
-}
-
-// Residual of level l and its full weighting onto level l+1 (rotann2.f:
-// 773-785 summation order) for one CX x CY tile of coarse points.
-template <class T>
-__global__ void __launch_bounds__(TILE_THREADS) k_resid_restrict(BatchDev B, const TileEntry *ctiles, int l, int src)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int FW = 2 * CX + 1, FH = 2 * CY + 1, XW = FW + 2, XH = FH + 2;
-    T *sx = (T *)smem_raw, *sr = sx + XW * XH;
-    const TileEntry e = ctiles[blockIdx.x];
-    if (!B.active[e.p]) return;
-    const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1];
-    const int X0 = e.tx * CX, Y0 = e.ty * CY;
-    const int rx = 2 * X0 - 1, ry = 2 * Y0 - 1;     // residual region origin
-    const T *x = XS<T>(B, e.p, l, src);
-    const T *f = FP<T>(B, e.p, l);
-    T *fc = FP<T>(B, e.p, l + 1);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll 4
-    for (int i = threadIdx.x; i < XW * XH; i += TILE_THREADS) {
-        const int r = i / XW, c = i - r * XW;
-        const int gy = ry - 1 + r, gx = rx - 1 + c;
-        sx[i] = (gy >= 0 && gy < n && gx >= 0 && gx < n) ? x[(size_t)gy * n + gx] : (T)0;
-    }
+    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     __syncthreads();
-    const T h = (T)1 / (T)(n - 1), ih2 = (T)1 / (h * h);
-    for (int r = warp; r < FH; r += nw) {
-        const int gy = ry + r;
-        for (int c = lane; c < FW; c += 32) {
-            const int gx = rx + c;
-            T rv = (T)0;
-            if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
-                const int q = (r + 1) * XW + (c + 1);
-                const T s = (sx[q - 1] + sx[q + 1]) + (sx[q - XW] + sx[q + XW]);
-                const T lap = fmaT<T>((T)-4, sx[q], s);
-                rv = fmaT<T>(-ih2, lap, f[(size_t)gy * n + gx]);
-            }
-            sr[r * FW + c] = rv;
-        }
-    }
-    __syncthreads();
-    const int Ia = max(X0, 1), Ib = min(X0 + CX, nc - 1);
-    const int Ja = max(Y0, 1), Jb = min(Y0 + CY, nc - 1);
-    for (int J = Ja + warp; J < Jb; J += nw) {
-        for (int I = Ia + lane; I < Ib; I += 32) {
-            const int q = (2 * (J - Y0) + 1) * FW + (2 * (I - X0) + 1);
-            T t = sr[q];
-            t = t * (T)2 + sr[q + 1] + sr[q - 1];
-            t = t + sr[q + FW] + sr[q - FW];
-            t = t * (T)2 + sr[q + 1 + FW] + sr[q - 1 - FW];
-            t = t + sr[q + 1 - FW] + sr[q - 1 + FW];
-            fc[(size_t)J * nc + I] = t * (T)0.0625;
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
-// Coarse levels of one problem in shared memory (one block per problem).
+// Coarse levels of one problem in shared memory (one block per problem):
+// the V-cycle below level dloc, solution and right-hand side of every level
+// resident, residuals formed inside the restriction.
 // ---------------------------------------------------------------------------
 template <class T>
 __device__ void loc_rb_half(T *x, const T *f, int n, T h2, int color)
@@ -293,13 +336,21 @@ __device__ void loc_rb_half(T *x, const T *f, int n, T h2, int color)
 }
 
 template <class T>
-__global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1, int nu2, int zero_level0,
-                                                               int correct_level0)
+__device__ __forceinline__ T loc_residual(const T *x, const T *f, int n, int c, T ih2)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *sm = (T *)smem_raw;
-    const int p = blockIdx.x;
-    if (!B.active[p]) return;
+    const T s = (x[c - 1] + x[c + 1]) + (x[c - n] + x[c + n]);
+    const T lap = fmaT<T>((T)-4, x[c], s);
+    return fmaT<T>(-ih2, lap, f[c]);
+}
+
+// zero0: the level-dloc solution starts at zero (a coarse correction, or the
+// first inner cycle of a mixed solve); corr0 (dloc == 0 only): add the
+// result to the FP64 solution instead of storing it.
+template <class T>
+__device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_level0, int correct_level0,
+                         unsigned char *smem)
+{
+    T *sm = (T *)smem;
     const int L = B.nlev[p], d0 = B.dloc[p];
     int off[BP_MAXL];
     int tot = 0;
@@ -308,13 +359,10 @@ __global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1
         const int n = B.n_of[p * BP_MAXL + l];
         tot += n * n;
     }
-    T *X = sm, *F = sm + tot, *R = sm + 2 * tot;
-    // load level d0 (x and f), zero everything else
-    for (int q = threadIdx.x; q < tot; q += blockDim.x) { X[q] = (T)0; F[q] = (T)0; R[q] = (T)0; }
+    T *X = sm, *F = sm + tot;
+    for (int q = threadIdx.x; q < tot; q += blockDim.x) { X[q] = (T)0; F[q] = (T)0; }
     __syncthreads();
     {
-        // the level's solution is a correction that starts at zero unless this
-        // is the finest level of a plain FP64 solve
         const bool zero = d0 > 0 || zero_level0;
         const int n = B.n_of[p * BP_MAXL + d0];
         const T *gx = XS<T>(B, p, d0, 0), *gf = FP<T>(B, p, d0);
@@ -324,43 +372,30 @@ __global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1
         }
     }
     __syncthreads();
-    // descent
     for (int l = d0; l < L - 1; ++l) {
         const int n = B.n_of[p * BP_MAXL + l], nc = B.n_of[p * BP_MAXL + l + 1];
-        T *x = X + off[l], *f = F + off[l], *r = R + off[l];
+        T *x = X + off[l], *f = F + off[l];
         const T h = (T)1 / (T)(n - 1), h2 = h * h, ih2 = (T)1 / h2;
         for (int s = 0; s < nu1; ++s) { loc_rb_half(x, f, n, h2, 0); loc_rb_half(x, f, n, h2, 1); }
-        const int m = n - 2;
-        for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
-            const int j = q / m + 1, i = q - (j - 1) * m + 1;
-            const int c = j * n + i;
-            const T s = (x[c - 1] + x[c + 1]) + (x[c - n] + x[c + n]);
-            const T lap = fmaT<T>((T)-4, x[c], s);
-            r[c] = fmaT<T>(-ih2, lap, f[c]);
-        }
-        __syncthreads();
-        T *fc = F + off[l + 1], *xc = X + off[l + 1];
+        T *fc = F + off[l + 1];
         const int mc = nc - 2;
         for (int q = threadIdx.x; q < mc * mc; q += blockDim.x) {
             const int j = q / mc + 1, i = q - (j - 1) * mc + 1;
             const int c = (2 * j) * n + 2 * i;
-            T t = r[c];
-            t = t * (T)2 + r[c + 1] + r[c - 1];
-            t = t + r[c + n] + r[c - n];
-            t = t * (T)2 + r[c + 1 + n] + r[c - 1 - n];
-            t = t + r[c + 1 - n] + r[c - 1 + n];
+            T t = loc_residual(x, f, n, c, ih2);
+            t = t * (T)2 + loc_residual(x, f, n, c + 1, ih2) + loc_residual(x, f, n, c - 1, ih2);
+            t = t + loc_residual(x, f, n, c + n, ih2) + loc_residual(x, f, n, c - n, ih2);
+            t = t * (T)2 + loc_residual(x, f, n, c + 1 + n, ih2) + loc_residual(x, f, n, c - 1 - n, ih2);
+            t = t + loc_residual(x, f, n, c + 1 - n, ih2) + loc_residual(x, f, n, c - 1 + n, ih2);
             fc[j * nc + i] = t * (T)0.0625;
-            xc[j * nc + i] = (T)0;
         }
         __syncthreads();
     }
-    // coarsest: one red update solves the single interior point
     {
         const int n = B.n_of[p * BP_MAXL + L - 1];
         const T h = (T)1 / (T)(n - 1);
         loc_rb_half(X + off[L - 1], F + off[L - 1], n, h * h, 0);
     }
-    // ascent
     for (int l = L - 2; l >= d0; --l) {
         const int n = B.n_of[p * BP_MAXL + l], nc = B.n_of[p * BP_MAXL + l + 1], m = n - 2;
         T *x = X + off[l], *f = F + off[l];
@@ -388,61 +423,45 @@ __global__ void __launch_bounds__(BP_THREADS) k_local_vcycle(BatchDev B, int nu1
         for (int s = 0; s < nu2; ++s) { loc_rb_half(x, f, n, h2, 0); loc_rb_half(x, f, n, h2, 1); }
     }
     {
-        // the local levels end in buffer 0; a mixed solve local from level 0
-        // applies its correction to the FP64 solution directly
         const int n = B.n_of[p * BP_MAXL + d0];
         if (d0 == 0 && correct_level0) {
             double *psi = B.psi[p];
-            for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = psi[q] + (double)X[q];
+            for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = psi[q] + to_double(X[q]);
         } else {
             T *gx = XS<T>(B, p, d0, 0);
             for (int q = threadIdx.x; q < n * n; q += blockDim.x) gx[q] = X[q];
         }
     }
-}
-
-// ---------------------------------------------------------------------------
-// Norms, defect correction and convergence bookkeeping
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double blk_sum(double v, double *s_red)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) s_red[warp] = v;
     __syncthreads();
-    double r = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < nw; ++w) r += s_red[w];
-    return r;
 }
 
-// FP64 outer pass over one TX x TY tile of level 0 (psi, f: the caller's
-// arrays): the residual r = f - A psi, its squared norm (block partial) and,
+// ---------------------------------------------------------------------------
+// FP64 outer pass, convergence bookkeeping
+// ---------------------------------------------------------------------------
+// One TX x TY tile of level 0 (psi, f: the caller's arrays): the FP64
+// residual r = f - A psi, its squared norm (the tile's partial sum) and,
 // when store_r, r rounded to FP32 as the inner cycle's right-hand side.
 // psi is only read here, so neighbouring tiles may overlap freely.
-__global__ void __launch_bounds__(TILE_THREADS) k_outer(BatchDev B, const TileEntry *tiles, const double *const *f_p,
-                                                        int store_r)
+__device__ void op_outer(const BatchDev &B, TileEntry e, int item, const double *const *f_p, int store_r,
+                         unsigned char *smem)
 {
-    __shared__ double sp[(TY + 2) * (TX + 2)];
-    __shared__ double s_red[32];
     constexpr int SX = TX + 2, SY = TY + 2;
-    const TileEntry e = tiles[blockIdx.x];
+    double *sp = (double *)smem;
+    double *s_red = sp + SX * SY;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (!B.active[e.p]) {
-        if (threadIdx.x == 0) B.partial[blockIdx.x] = 0.0;
+        if (threadIdx.x == 0) B.partial[item] = 0.0;
         return;
     }
     const int n = B.n_of[e.p * BP_MAXL];
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - 1, oy = y0 - 1;
     const double *psi = B.psi[e.p];
     const double *f = f_p[e.p];
-    for (int r = warp; r < SY; r += nw) {
-        const int gy = oy + r;
-        const bool rowin = gy >= 0 && gy < n;
-        for (int c = lane; c < SX; c += 32) {
-            const int gx = ox + c;
-            sp[r * SX + c] = (rowin && gx >= 0 && gx < n) ? psi[(size_t)gy * n + gx] : 0.0;
-        }
+#pragma unroll 4
+    for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
+        const int r = i / SX, c = i - r * SX;
+        const int gy = oy + r, gx = ox + c;
+        sp[i] = (gy >= 0 && gy < n && gx >= 0 && gx < n) ? psi[(size_t)gy * n + gx] : 0.0;
     }
     __syncthreads();
     const double h = 1.0 / (double)(n - 1), ih2 = 1.0 / (h * h);
@@ -458,7 +477,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_outer(BatchDev B, const TileEn
             const double lap = __fma_rn(-4.0, sp[q], s);
             const double r = __fma_rn(-ih2, lap, f[g]);
             acc = __fma_rn(r, r, acc);
-            if (store_r) f32[g] = (float)r;
+            if (store_r) f32[g] = d2f_rn(r);
         }
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -467,16 +486,15 @@ __global__ void __launch_bounds__(TILE_THREADS) k_outer(BatchDev B, const TileEn
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int w = 0; w < nw; ++w) t += s_red[w];
-        B.partial[blockIdx.x] = t;
+        B.partial[item] = t;
     }
+    __syncthreads();
 }
 
 // Copies buffer 1 of level 0 into the caller's psi (plain FP64 cycles whose
-// level-0 kernels leave the result in the internal buffer).
-__global__ void __launch_bounds__(TILE_THREADS) k_copy_back(BatchDev B, const TileEntry *tiles)
+// level-0 operations leave the result in the internal buffer).
+__device__ void op_copyback(const BatchDev &B, TileEntry e)
 {
-    const TileEntry e = tiles[blockIdx.x];
-    if (!B.active[e.p]) return;
     const int n = B.n_of[e.p * BP_MAXL];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const double *src = XS<double>(B, e.p, 0, 1);
@@ -490,11 +508,9 @@ __global__ void __launch_bounds__(TILE_THREADS) k_copy_back(BatchDev B, const Ti
 
 // One warp per problem: sums the problem's tile partials in a fixed order
 // and decides whether it keeps cycling.  first != 0 records ||f|| (psi = 0).
-__global__ void k_finalize(BatchDev B, int first)
+__device__ void op_finalize(const BatchDev &B, int p, int first)
 {
     const int lane = threadIdx.x & 31;
-    const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (p >= B.nprob) return;
     if (!B.active[p]) return;
     double s = 0.0;
     const int b0 = B.p_blk0[p], nb = B.p_nblk0[p];
@@ -517,25 +533,184 @@ __global__ void k_finalize(BatchDev B, int first)
 }
 
 // ---------------------------------------------------------------------------
+// Operation list.  One outer iteration is a fixed sequence of operations;
+// the host builds it once and either launches one kernel per operation
+// (captured in a CUDA graph) or hands the whole list to the persistent
+// kernel, which runs every operation of every iteration in one launch with
+// grid-wide barriers between them.
+// ---------------------------------------------------------------------------
+enum OpKind { OP_SMOOTH = 0, OP_SMOOTH_R = 1, OP_PROLONG = 2, OP_LOCAL = 3, OP_OUTER = 4, OP_FINALIZE = 5,
+              OP_COPYBACK = 6 };
+
+struct Op {
+    int kind, l, nu, zero, src, dst, corr;
+    int off, cnt;     // work items: tiles [off, off+cnt) of the tile table, or problems / warps
+    int aux;          // OP_LOCAL: zero0 | corr0 << 1; OP_OUTER: store_r; OP_FINALIZE: first
+};
+
+// Runs work item `item` of op on this block.
+template <class T>
+__device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *tiles, const double *const *f_p,
+                                         const Op &op, int item, int nu1, int nu2, unsigned char *smem)
+{
+    switch (op.kind) {
+    case OP_SMOOTH: {
+        const TileEntry e = tiles[op.off + item];
+        if (!B.active[e.p]) return;
+        if (op.nu == 2) {
+            if (op.corr) op_smooth<T, 2, true, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
+            else op_smooth<T, 2, false, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
+        } else {
+            if (op.corr) op_smooth<T, 1, true, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
+            else op_smooth<T, 1, false, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
+        }
+        return;
+    }
+    case OP_SMOOTH_R: {
+        const TileEntry e = tiles[op.off + item];
+        if (!B.active[e.p]) return;
+        if (op.nu == 2) op_smooth<T, 2, false, true>(B, e, op.l, op.zero, op.src, op.dst, smem);
+        else op_smooth<T, 1, false, true>(B, e, op.l, op.zero, op.src, op.dst, smem);
+        return;
+    }
+    case OP_PROLONG: {
+        const TileEntry e = tiles[op.off + item];
+        if (!B.active[e.p]) return;
+        if (op.nu == 2) {
+            if (op.corr) op_prolong<T, 2, true>(B, e, op.l, op.src, op.dst, smem);
+            else op_prolong<T, 2, false>(B, e, op.l, op.src, op.dst, smem);
+        } else if (op.nu == 1) {
+            if (op.corr) op_prolong<T, 1, true>(B, e, op.l, op.src, op.dst, smem);
+            else op_prolong<T, 1, false>(B, e, op.l, op.src, op.dst, smem);
+        } else {
+            if (op.corr) op_prolong<T, 0, true>(B, e, op.l, op.src, op.dst, smem);
+            else op_prolong<T, 0, false>(B, e, op.l, op.src, op.dst, smem);
+        }
+        return;
+    }
+    case OP_LOCAL:
+        if (!B.active[item]) return;
+        op_local<T>(B, item, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, smem);
+        return;
+    case OP_OUTER:
+        op_outer(B, tiles[op.off + item], item, f_p, op.aux, smem);
+        return;
+    case OP_COPYBACK: {
+        const TileEntry e = tiles[op.off + item];
+        if (B.active[e.p]) op_copyback(B, e);
+        return;
+    }
+    default:
+        return;
+    }
+}
+
+// One kernel launch per operation (graph path).
+template <class T, int KIND, int NU, bool CORR>
+__global__ void __launch_bounds__(TILE_THREADS) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
+                                                     Op op, int nu1, int nu2)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (KIND == OP_FINALIZE) {
+        const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        if (p < B.nprob) op_finalize(B, p, op.aux);
+        return;
+    }
+    Op o = op;
+    o.kind = KIND;
+    o.nu = NU;
+    o.corr = CORR ? 1 : 0;
+    run_item<T>(B, tiles, f_p, o, blockIdx.x, nu1, nu2, smem_raw);
+}
+
+// Grid-wide barrier of the persistent kernel.  Every wait is bounded: a
+// block that waits longer than `limit` polls sets the error flag and every
+// block leaves the kernel at its next barrier, so a lost block cannot hang
+// the GPU.
+struct GridSync {
+    unsigned *count;
+    unsigned *gen;
+    int *err;
+    long long limit;
+};
+
+__device__ __forceinline__ bool grid_sync(const GridSync &gs)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = gs.gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(gs.count, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(gs.count, 0u);
+            __threadfence();
+            atomicAdd(gs.gen, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == g) {
+                if (++it > gs.limit || *(volatile int *)gs.err) {
+                    atomicExch(gs.err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)gs.err == 0;
+}
+
+// The whole solve in one launch: the first iteration's operations, then
+// further iterations until every problem has converged (or hit the cycle
+// limit).  Must be launched cooperatively (all blocks resident).
+template <class T>
+__global__ void __launch_bounds__(TILE_THREADS, 3) k_persistent(BatchDev B, const TileEntry *tiles,
+                                                             const double *const *f_p, const Op *ops0, int n0,
+                                                             const Op *ops, int nops, int nu1, int nu2,
+                                                             int max_iter, GridSync gs)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warps_total = gridDim.x * (blockDim.x >> 5);
+    const int gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    for (int it = 0; it <= max_iter; ++it) {
+        const Op *list = it == 0 ? ops0 : ops;
+        const int cnt_ops = it == 0 ? n0 : nops;
+        for (int k = 0; k < cnt_ops; ++k) {
+            const Op op = list[k];
+            if (op.kind == OP_OUTER && blockIdx.x == 0 && threadIdx.x == 0) *B.num_active = 0;
+            if (op.kind == OP_FINALIZE) {
+                for (int p = gwarp; p < B.nprob; p += warps_total) op_finalize(B, p, op.aux);
+            } else {
+                for (int item = blockIdx.x; item < op.cnt; item += gridDim.x)
+                    run_item<T>(B, tiles, f_p, op, item, nu1, nu2, smem_raw);
+            }
+            if (!grid_sync(gs)) return;
+            if (op.kind == OP_FINALIZE && *(volatile int *)B.num_active == 0) return;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 struct gb_batch {
     int nprob = 0, precision = 0, nu1 = 2, nu2 = 2, max_cycles = 100;
     int inner = 1;                      // V-cycles per outer iteration (mixed)
-    int cur0 = 0;                       // level-0 buffer holding the correction between inner cycles
+    int exec = GB_BATCH_EXEC_GRAPH;
     double rtol = 1e-10;
     std::vector<int> n, L, dloc;
     long long total = 0;
     std::vector<long long> off0;        // level-0 offsets in the packed user arrays
     int maxdepth_global = 0;            // levels 0..maxdepth_global-1 have tile work
-    void *pool = nullptr;               // per-level x, f (T = double or float)
+    void *pool = nullptr;               // per-level x (two buffers), f (T = double or float)
     size_t pool_bytes = 0;
     int *d_int = nullptr;
     double *d_dbl = nullptr;
     void **d_ptrs = nullptr;
     TileEntry *d_tiles = nullptr;
-    std::vector<int> ft_off, ft_cnt;    // per level: fine tiles (problems with l < dloc)
-    std::vector<int> ct_off, ct_cnt;    // per level l >= 1: coarse tiles of l (problems with l <= dloc)
+    std::vector<int> ft_off, ft_cnt;    // per level: tiles of problems with l < dloc
     int ot_off = 0, ot_cnt = 0;         // level-0 tiles of every problem (outer pass)
     BatchDev dev;
     double **d_psi_tab = nullptr, **d_f_tab = nullptr;
@@ -543,9 +718,18 @@ struct gb_batch {
     size_t local_smem = 0;
     int *h_pinned = nullptr;
     cudaStream_t stream = nullptr;
+    // operation lists (first iteration, later iterations) and their device copies
+    std::vector<Op> ops0, ops;
+    Op *d_ops = nullptr;
+    int plan_inner = -1;
+    // persistent launch
+    unsigned *d_sync = nullptr;         // count, gen, err
+    int pgrid = 0;
+    size_t psmem = 0;
+    // graph path
     cudaGraphExec_t cycle_graph = nullptr;
     long long launches = 0, launches_per_cycle = 0;
-    // optional per-launch timing of the finest-level pre-smoothing kernel
+    // profiling
     int profile = 0, graph_profile = -1, graph_ev = 0;
     std::vector<cudaEvent_t> ev;
     int ev_used = 0;
@@ -565,27 +749,207 @@ static int levels_of(int n, int *nl)
     return L;
 }
 
-template <class T, int NU> static size_t smem_smooth() { return 2 * sizeof(T) * (TX + 4 * NU) * (TY + 4 * NU); }
-template <class T> static size_t smem_restrict() { return sizeof(T) * ((2 * CX + 3) * (2 * CY + 3) + (2 * CX + 1) * (2 * CY + 1)); }
+template <class T> static size_t smem_tile(int H) { return 2 * sizeof(T) * (size_t)(TX + 2 * H) * (TY + 2 * H); }
+static size_t smem_outer() { return sizeof(double) * ((size_t)(TX + 2) * (TY + 2) + 32); }
 
-template <class T> static cudaError_t set_smem_attrs(size_t local)
+template <class T> static size_t smem_of(const gb_batch *b, const Op &op)
+{
+    switch (op.kind) {
+    case OP_SMOOTH: return smem_tile<T>(2 * op.nu);
+    case OP_SMOOTH_R: return smem_tile<T>(2 * op.nu + 2);
+    case OP_PROLONG: return smem_tile<T>(2 * op.nu);
+    case OP_LOCAL: return b->local_smem;
+    case OP_OUTER: return smem_outer();
+    default: return 0;
+    }
+}
+
+// Sweeps fused into one smoothing operation: two in FP32; one in FP64,
+// whose pipe is the bottleneck and would pay for the wider halo's
+// redundant updates.
+template <class T> static int sweeps_per_op(int nu) { return (sizeof(T) == 4 && nu >= 2) ? 2 : 1; }
+template <class T> static int ops_for(int nu)
+{
+    int k = 0;
+    while (nu > 0) { nu -= sweeps_per_op<T>(nu); ++k; }
+    return k;
+}
+
+// Operations of one V-cycle.  Tile operations read one buffer of a level
+// and write the other; the plan picks the buffers so that every coarse level
+// ends in buffer 0 (where the local operation also leaves its levels) and
+// the plain solve's level 0 ends in the caller's psi (buffer 0).  Mixed:
+// zero0 = the level-0 correction starts at zero (first inner cycle),
+// corr0 = the last level-0 operation adds the correction to psi (last inner
+// cycle); between inner cycles the correction waits in level-0 buffer *cur0.
+template <class T>
+static void plan_vcycle(gb_batch *b, std::vector<Op> &v, bool zero0, bool corr0, int *cur0)
+{
+    const bool mixed = b->precision == GB_BATCH_MIXED;
+    int cur[BP_MAXL] = {0};
+    const int k1 = ops_for<T>(b->nu1);
+    const int pro = std::min(b->nu2, sizeof(T) == 4 ? 2 : 1);  // sweeps fused into the prolongation
+    const int k2 = ops_for<T>(b->nu2 - pro);
+    for (int l = 0; l < b->maxdepth_global; ++l) {
+        if (b->ft_cnt[l] == 0) continue;
+        const bool zero = l > 0 || (mixed && zero0);
+        const int writes = k1 + 1 + k2;
+        int src, dst;
+        if (zero) { dst = (writes - 1) & 1; src = 1 - dst; }
+        else if (mixed) { src = *cur0; dst = 1 - src; }    // level 0, later inner cycle
+        else { src = 0; dst = 1; }                         // level 0 of the plain solve: psi
+        int nu = b->nu1;
+        for (int i = 0; i < k1; ++i) {
+            const int k = sweeps_per_op<T>(nu);
+            Op o{};
+            o.kind = (i == k1 - 1) ? OP_SMOOTH_R : OP_SMOOTH;
+            o.l = l; o.nu = k; o.zero = (zero && i == 0) ? 1 : 0; o.src = src; o.dst = dst; o.corr = 0;
+            o.off = b->ft_off[l]; o.cnt = b->ft_cnt[l];
+            v.push_back(o);
+            nu -= k;
+            src = dst;
+            dst = 1 - dst;
+        }
+        cur[l] = src;
+    }
+    {
+        Op o{};
+        o.kind = OP_LOCAL;
+        o.cnt = b->nprob;
+        o.aux = ((mixed && zero0) ? 1 : 0) | ((mixed && corr0) ? 2 : 0);
+        v.push_back(o);
+    }
+    for (int l = b->maxdepth_global - 1; l >= 0; --l) {
+        if (b->ft_cnt[l] == 0) continue;
+        const int correct_last = (mixed && l == 0 && corr0) ? 1 : 0;
+        int src = cur[l], dst = 1 - cur[l];
+        Op o{};
+        o.kind = OP_PROLONG; o.l = l; o.nu = pro; o.src = src; o.dst = dst;
+        o.corr = k2 == 0 ? correct_last : 0;
+        o.off = b->ft_off[l]; o.cnt = b->ft_cnt[l];
+        v.push_back(o);
+        src = dst;
+        dst = 1 - dst;
+        int nu = b->nu2 - pro;
+        for (int i = 0; i < k2; ++i) {
+            const int k = sweeps_per_op<T>(nu);
+            Op q{};
+            q.kind = OP_SMOOTH; q.l = l; q.nu = k; q.zero = 0; q.src = src; q.dst = dst;
+            q.corr = (i == k2 - 1) ? correct_last : 0;
+            q.off = b->ft_off[l]; q.cnt = b->ft_cnt[l];
+            v.push_back(q);
+            nu -= k;
+            src = dst;
+            dst = 1 - dst;
+        }
+        cur[l] = src;
+        if (!mixed && l == 0 && cur[0] != 0) {
+            Op c{};
+            c.kind = OP_COPYBACK; c.off = b->ft_off[0]; c.cnt = b->ft_cnt[0];
+            v.push_back(c);
+        }
+    }
+    if (mixed) *cur0 = cur[0];
+}
+
+// One outer iteration: the FP64 residual norm of level 0 (mixed: also its
+// FP32 copy as the inner right-hand side), convergence bookkeeping, then
+// b->inner V-cycles (mixed: the last one's final level-0 operation adds the
+// correction to psi).
+template <class T>
+static void plan_iteration(gb_batch *b, std::vector<Op> &v, int first)
+{
+    v.clear();
+    const bool mixed = b->precision == GB_BATCH_MIXED;
+    Op o{};
+    o.kind = OP_OUTER; o.off = b->ot_off; o.cnt = b->ot_cnt; o.aux = mixed ? 1 : 0;
+    v.push_back(o);
+    Op f{};
+    f.kind = OP_FINALIZE; f.cnt = b->nprob; f.aux = first;
+    v.push_back(f);
+    int cur0 = 0;
+    const int inner = mixed ? b->inner : 1;
+    for (int k = 0; k < inner; ++k) plan_vcycle<T>(b, v, k == 0, k == inner - 1, &cur0);
+}
+
+static void build_plans(gb_batch *b)
+{
+    if (b->precision == GB_BATCH_MIXED) {
+        plan_iteration<float>(b, b->ops0, 1);
+        plan_iteration<float>(b, b->ops, 0);
+    } else {
+        plan_iteration<double>(b, b->ops0, 1);
+        plan_iteration<double>(b, b->ops, 0);
+    }
+    b->plan_inner = b->inner;
+}
+
+template <class T> static cudaError_t set_smem_attrs(size_t local, size_t persistent)
 {
     cudaError_t e;
 #define SA(k, sz) if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sz))) != cudaSuccess) return e
-    SA((k_smooth<T, 1, false>), (smem_smooth<T, 1>()));
-    SA((k_smooth<T, 2, false>), (smem_smooth<T, 2>()));
-    SA((k_smooth<T, 1, true>), (smem_smooth<T, 1>()));
-    SA((k_smooth<T, 2, true>), (smem_smooth<T, 2>()));
-    SA((k_prolong_smooth<T, 0, false>), (smem_smooth<T, 0>()));
-    SA((k_prolong_smooth<T, 1, false>), (smem_smooth<T, 1>()));
-    SA((k_prolong_smooth<T, 2, false>), (smem_smooth<T, 2>()));
-    SA((k_prolong_smooth<T, 0, true>), (smem_smooth<T, 0>()));
-    SA((k_prolong_smooth<T, 1, true>), (smem_smooth<T, 1>()));
-    SA((k_prolong_smooth<T, 2, true>), (smem_smooth<T, 2>()));
-    SA((k_resid_restrict<T>), (smem_restrict<T>()));
-    SA((k_local_vcycle<T>), (local));
+    SA((k_op<T, OP_SMOOTH, 1, false>), smem_tile<T>(2));
+    SA((k_op<T, OP_SMOOTH, 2, false>), smem_tile<T>(4));
+    SA((k_op<T, OP_SMOOTH, 1, true>), smem_tile<T>(2));
+    SA((k_op<T, OP_SMOOTH, 2, true>), smem_tile<T>(4));
+    SA((k_op<T, OP_SMOOTH_R, 1, false>), smem_tile<T>(4));
+    SA((k_op<T, OP_SMOOTH_R, 2, false>), smem_tile<T>(6));
+    SA((k_op<T, OP_PROLONG, 0, false>), smem_tile<T>(0));
+    SA((k_op<T, OP_PROLONG, 1, false>), smem_tile<T>(2));
+    SA((k_op<T, OP_PROLONG, 2, false>), smem_tile<T>(4));
+    SA((k_op<T, OP_PROLONG, 0, true>), smem_tile<T>(0));
+    SA((k_op<T, OP_PROLONG, 1, true>), smem_tile<T>(2));
+    SA((k_op<T, OP_PROLONG, 2, true>), smem_tile<T>(4));
+    SA((k_op<T, OP_LOCAL, 0, false>), local);
+    SA((k_persistent<T>), persistent);
 #undef SA
     return cudaSuccess;
+}
+
+// Launches one operation as its own kernel (graph path).
+template <class T>
+static void launch_op(gb_batch *b, const Op &op, cudaStream_t s)
+{
+    const BatchDev &D = b->dev;
+    const TileEntry *t = b->d_tiles;
+    const double *const *fp = (const double *const *)b->d_f_tab;
+    const size_t sm = smem_of<T>(b, op);
+    const int g = op.cnt;
+    if (g <= 0) return;
+    const int n1 = b->nu1, n2 = b->nu2;
+    switch (op.kind) {
+    case OP_SMOOTH:
+        if (op.nu == 2 && op.corr) k_op<T, OP_SMOOTH, 2, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else if (op.nu == 2) k_op<T, OP_SMOOTH, 2, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else if (op.corr) k_op<T, OP_SMOOTH, 1, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else k_op<T, OP_SMOOTH, 1, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        break;
+    case OP_SMOOTH_R:
+        if (op.nu == 2) k_op<T, OP_SMOOTH_R, 2, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else k_op<T, OP_SMOOTH_R, 1, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        break;
+    case OP_PROLONG:
+        if (op.nu == 2 && op.corr) k_op<T, OP_PROLONG, 2, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else if (op.nu == 2) k_op<T, OP_PROLONG, 2, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else if (op.nu == 1 && op.corr) k_op<T, OP_PROLONG, 1, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else if (op.nu == 1) k_op<T, OP_PROLONG, 1, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else if (op.corr) k_op<T, OP_PROLONG, 0, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        else k_op<T, OP_PROLONG, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        break;
+    case OP_LOCAL:
+        k_op<T, OP_LOCAL, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        break;
+    case OP_OUTER:
+        k_op<T, OP_OUTER, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        break;
+    case OP_FINALIZE:
+        k_op<T, OP_FINALIZE, 0, false><<<gb_ceil_div(b->nprob, TILE_THREADS / 32), TILE_THREADS, 0, s>>>(D, t, fp, op, n1, n2);
+        break;
+    case OP_COPYBACK:
+        k_op<T, OP_COPYBACK, 0, false><<<g, TILE_THREADS, 0, s>>>(D, t, fp, op, n1, n2);
+        break;
+    }
+    b->launches += 1;
 }
 
 extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
@@ -644,34 +1008,28 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     for (int p = 0; p < nprob; ++p) {
         size_t sz = 0;
         for (int l = b->dloc[p]; l < b->L[p]; ++l) sz += (size_t)nof[(size_t)p * BP_MAXL + l] * nof[(size_t)p * BP_MAXL + l];
-        smax = std::max(smax, 3 * sz * esz);
+        smax = std::max(smax, 2 * sz * esz);
     }
     b->local_smem = smax;
     // tile tables
     std::vector<TileEntry> tiles;
     b->ft_off.assign(BP_MAXL + 1, 0);
     b->ft_cnt.assign(BP_MAXL + 1, 0);
-    b->ct_off.assign(BP_MAXL + 1, 0);
-    b->ct_cnt.assign(BP_MAXL + 1, 0);
     std::vector<int> pb0(nprob), pnb0(nprob);
-    auto add_tiles = [&](int p, int nn, int tw, int th) {
-        for (int ty = 0; ty * th < nn - 1; ++ty)
-            for (int tx = 0; tx * tw < nn - 1; ++tx) tiles.push_back({p, (short)tx, (short)ty});
+    auto add_tiles = [&](int p, int nn) {
+        for (int ty = 0; ty * TY < nn - 1; ++ty)
+            for (int tx = 0; tx * TX < nn - 1; ++tx) tiles.push_back({p, (short)tx, (short)ty});
     };
     for (int l = 0; l < BP_MAXL; ++l) {
         b->ft_off[l] = (int)tiles.size();
         for (int p = 0; p < nprob; ++p)
-            if (l < b->dloc[p]) add_tiles(p, nof[(size_t)p * BP_MAXL + l], TX, TY);
+            if (l < b->dloc[p]) add_tiles(p, nof[(size_t)p * BP_MAXL + l]);
         b->ft_cnt[l] = (int)tiles.size() - b->ft_off[l];
-        b->ct_off[l] = (int)tiles.size();
-        for (int p = 0; p < nprob; ++p)
-            if (l >= 1 && l <= b->dloc[p]) add_tiles(p, nof[(size_t)p * BP_MAXL + l], CX, CY);
-        b->ct_cnt[l] = (int)tiles.size() - b->ct_off[l];
     }
     b->ot_off = (int)tiles.size();
     for (int p = 0; p < nprob; ++p) {
         pb0[p] = (int)tiles.size() - b->ot_off;
-        add_tiles(p, n[p], TX, TY);
+        add_tiles(p, n[p]);
         pnb0[p] = (int)tiles.size() - b->ot_off - pb0[p];
     }
     b->ot_cnt = (int)tiles.size() - b->ot_off;
@@ -696,6 +1054,8 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     const size_t nptr = 2 * (size_t)nprob * BP_MAXL + (size_t)nprob * BP_MAXL + 2 * (size_t)nprob;
     BTRY(cudaMalloc(&b->d_ptrs, sizeof(void *) * nptr));
     BTRY(cudaMalloc(&b->d_tiles, sizeof(TileEntry) * tiles.size()));
+    BTRY(cudaMalloc(&b->d_sync, sizeof(unsigned) * 4));
+    BTRY(cudaMemset(b->d_sync, 0, sizeof(unsigned) * 4));
     BTRY(cudaMallocHost(&b->h_pinned, sizeof(int) * 16));
     BTRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     b->hx.assign(2 * (size_t)nprob * BP_MAXL, nullptr);
@@ -734,7 +1094,6 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     void **dp = b->d_ptrs;
     BTRY(cudaMemcpy(dp, b->hx.data(), sizeof(void *) * b->hx.size(), cudaMemcpyHostToDevice));
     BTRY(cudaMemcpy(dp + b->hx.size(), b->hf.data(), sizeof(void *) * b->hf.size(), cudaMemcpyHostToDevice));
-    // table layout: x (2 buffers), f, then the caller's psi and f per problem
     b->d_psi_tab = (double **)(dp + b->hx.size() + b->hf.size());
     b->d_f_tab = (double **)(dp + b->hx.size() + b->hf.size() + nprob);
     if (b->hx.size() + b->hf.size() + 2 * (size_t)nprob != nptr) {
@@ -763,8 +1122,25 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     D.max_cycles = max_cycles;
     D.inner = 1;
     D.rtol = rtol;
-    if (precision == GB_BATCH_FP64) BTRY(set_smem_attrs<double>(b->local_smem));
-    else BTRY(set_smem_attrs<float>(b->local_smem));
+    // persistent launch: shared memory of the largest operation, grid of
+    // every block that can be resident at once
+    build_plans(b);
+    size_t ps = 0;
+    for (const Op &o : b->ops)
+        ps = std::max(ps, precision == GB_BATCH_FP64 ? smem_of<double>(b, o) : smem_of<float>(b, o));
+    b->psmem = ps;
+    if (precision == GB_BATCH_FP64) BTRY(set_smem_attrs<double>(b->local_smem, b->psmem));
+    else BTRY(set_smem_attrs<float>(b->local_smem, b->psmem));
+    int dev = 0, nsm = 0, per = 0, coop = 0;
+    BTRY(cudaGetDevice(&dev));
+    BTRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    BTRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (precision == GB_BATCH_FP64) BTRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persistent<double>, TILE_THREADS, b->psmem));
+    else BTRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persistent<float>, TILE_THREADS, b->psmem));
+    b->pgrid = nsm * per;
+    if (!coop) b->pgrid = 0;
+    const size_t nops_max = 4 * (b->ops.size() + 8);
+    BTRY(cudaMalloc(&b->d_ops, sizeof(Op) * nops_max));
 #undef BTRY
     *out = b;
     return GB_OK;
@@ -780,6 +1156,8 @@ extern "C" int gb_batch_destroy(gb_batch *b)
     cudaFree(b->d_dbl);
     cudaFree(b->d_ptrs);
     cudaFree(b->d_tiles);
+    cudaFree(b->d_ops);
+    cudaFree(b->d_sync);
     if (b->h_pinned) cudaFreeHost(b->h_pinned);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -787,6 +1165,7 @@ extern "C" int gb_batch_destroy(gb_batch *b)
 }
 
 extern "C" long long gb_batch_total_points(const gb_batch *b) { return b ? b->total : 0; }
+extern "C" long long gb_batch_last_launches(const gb_batch *b) { return b ? b->launches : 0; }
 
 extern "C" int gb_batch_set_inner_cycles(gb_batch *b, int inner)
 {
@@ -800,9 +1179,27 @@ extern "C" int gb_batch_set_inner_cycles(gb_batch *b, int inner)
     }
     b->inner = inner;
     b->dev.inner = inner;
+    build_plans(b);
+    if (4 * (b->ops.size() + 8) < b->ops0.size() + b->ops.size()) {
+        gb_set_error("gb_batch_set_inner_cycles: operation list too long");
+        return GB_ERR_INVALID;
+    }
     return GB_OK;
 }
-extern "C" long long gb_batch_last_launches(const gb_batch *b) { return b ? b->launches : 0; }
+
+extern "C" int gb_batch_set_exec(gb_batch *b, int mode)
+{
+    if (!b || (mode != GB_BATCH_EXEC_GRAPH && mode != GB_BATCH_EXEC_PERSISTENT)) {
+        gb_set_error("gb_batch_set_exec: mode must be GB_BATCH_EXEC_GRAPH or GB_BATCH_EXEC_PERSISTENT");
+        return GB_ERR_INVALID;
+    }
+    if (mode == GB_BATCH_EXEC_PERSISTENT && b->pgrid <= 0) {
+        gb_set_error("gb_batch_set_exec: cooperative launch unavailable on this device");
+        return GB_ERR_INVALID;
+    }
+    b->exec = mode;
+    return GB_OK;
+}
 
 // Records a timing event: as an event node of the graph while the stream is
 // being captured, as a plain record otherwise.
@@ -814,137 +1211,32 @@ static void prof_record(cudaEvent_t e, cudaStream_t s)
     else cudaEventRecord(e, s);
 }
 
-// Launch plan of one level: how many sweeps each smoothing launch does
-// (two per launch in FP32, one in FP64, whose pipe is the bottleneck and
-// would pay for the wider halo's redundant updates).
-template <class T> static int sweeps_per_launch(int nu) { return (sizeof(T) == 4 && nu >= 2) ? 2 : 1; }
-template <class T> static int launches_for(int nu)
+// Graph path: the operations of one iteration, each its own kernel; the
+// finest-level pre-smoothing operation (the largest FP32 kernel) is
+// bracketed by timing events when profiling.
+static void enqueue_iteration(gb_batch *b, const std::vector<Op> &v, cudaStream_t s)
 {
-    int k = 0;
-    while (nu > 0) { nu -= sweeps_per_launch<T>(nu); ++k; }
-    return k;
-}
-
-template <class T>
-static void launch_smooth(gb_batch *b, int l, int k, int zero_init, int src, int dst, int correct, cudaStream_t s,
-                          bool timed)
-{
-    const int cnt = b->ft_cnt[l];
-    const TileEntry *t = b->d_tiles + b->ft_off[l];
-    const bool ev = timed && b->profile && b->ev_used + 2 <= (int)b->ev.size();
-    const size_t sm = k == 2 ? smem_smooth<T, 2>() : smem_smooth<T, 1>();
-    if (ev) prof_record(b->ev[b->ev_used], s);
-    if (k == 2 && correct) k_smooth<T, 2, true><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
-    else if (k == 2) k_smooth<T, 2, false><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
-    else if (correct) k_smooth<T, 1, true><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
-    else k_smooth<T, 1, false><<<cnt, TILE_THREADS, sm, s>>>(b->dev, t, l, zero_init, src, dst);
-    if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
-    b->launches += 1;
-}
-
-template <class T>
-static void launch_prolong(gb_batch *b, int l, int nu, int src, int dst, int correct, cudaStream_t s)
-{
-    const int cnt = b->ft_cnt[l];
-    const TileEntry *t = b->d_tiles + b->ft_off[l];
-#define PL(NU, C) k_prolong_smooth<T, NU, C><<<cnt, TILE_THREADS, smem_smooth<T, NU>(), s>>>(b->dev, t, l, src, 0, dst)
-    if (nu == 2) { if (correct) PL(2, true); else PL(2, false); }
-    else if (nu == 1) { if (correct) PL(1, true); else PL(1, false); }
-    else { if (correct) PL(0, true); else PL(0, false); }
-#undef PL
-    b->launches += 1;
-}
-
-// The kernels of one V-cycle: pre-smoothing, residual + restriction on each
-// tile level, the local coarse cycles, then prolongation + post-smoothing.
-// Tile kernels read one buffer of a level and write the other; the plan
-// picks the buffers so that every coarse level ends in buffer 0 (where the
-// local kernel also leaves its levels) and the plain solve's level 0 ends in
-// the caller's psi (buffer 0).  Mixed: zero0 = the level-0 correction starts
-// at zero (first inner cycle of an outer iteration), corr0 = the last
-// level-0 kernel adds the correction to psi (last inner cycle); between
-// inner cycles the correction waits in level-0 buffer b->cur0.
-template <class T>
-static void enqueue_vcycle(gb_batch *b, cudaStream_t s, bool zero0, bool corr0)
-{
-    const bool mixed = b->precision == GB_BATCH_MIXED;
-    int cur[BP_MAXL] = {0};
-    const int k1 = launches_for<T>(b->nu1);
-    const int pro = std::min(b->nu2, sizeof(T) == 4 ? 2 : 1);  // sweeps fused into the prolongation
-    const int k2 = launches_for<T>(b->nu2 - pro);
-    for (int l = 0; l < b->maxdepth_global; ++l) {
-        if (b->ft_cnt[l] == 0) continue;
-        const bool zero = l > 0 || (mixed && zero0);
-        const int writes = k1 + 1 + k2;
-        int src, dst;
-        if (zero) { dst = (writes - 1) & 1; src = 1 - dst; }
-        else if (mixed) { src = b->cur0; dst = 1 - src; }   // level 0, later inner cycle
-        else { src = 0; dst = 1; }                          // level 0 of the plain solve: psi
-        int nu = b->nu1;
-        for (int i = 0; i < k1; ++i) {
-            const int k = sweeps_per_launch<T>(nu);
-            launch_smooth<T>(b, l, k, (zero && i == 0) ? 1 : 0, src, dst, 0, s, l == 0);
-            nu -= k;
-            src = dst;
-            dst = 1 - dst;
-        }
-        cur[l] = src;
-        k_resid_restrict<T><<<b->ct_cnt[l + 1], TILE_THREADS, smem_restrict<T>(), s>>>(
-            b->dev, b->d_tiles + b->ct_off[l + 1], l, cur[l]);
-        b->launches += 1;
+    cudaMemsetAsync(b->dev.num_active, 0, sizeof(int), s);
+    for (const Op &op : v) {
+        const bool ev = b->profile && op.kind == OP_SMOOTH_R && op.l == 0 && b->ev_used + 2 <= (int)b->ev.size();
+        if (ev) prof_record(b->ev[b->ev_used], s);
+        if (b->precision == GB_BATCH_MIXED) launch_op<float>(b, op, s);
+        else launch_op<double>(b, op, s);
+        if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
     }
-    k_local_vcycle<T><<<b->nprob, BP_THREADS, b->local_smem, s>>>(b->dev, b->nu1, b->nu2, (mixed && zero0) ? 1 : 0,
-                                                                 (mixed && corr0) ? 1 : 0);
-    b->launches += 1;
-    for (int l = b->maxdepth_global - 1; l >= 0; --l) {
-        if (b->ft_cnt[l] == 0) continue;
-        const int correct_last = (mixed && l == 0 && corr0) ? 1 : 0;
-        int src = cur[l], dst = 1 - cur[l];
-        launch_prolong<T>(b, l, pro, src, dst, k2 == 0 ? correct_last : 0, s);
-        src = dst;
-        dst = 1 - dst;
-        int nu = b->nu2 - pro;
-        for (int i = 0; i < k2; ++i) {
-            const int k = sweeps_per_launch<T>(nu);
-            launch_smooth<T>(b, l, k, 0, src, dst, (i == k2 - 1) ? correct_last : 0, s, false);
-            nu -= k;
-            src = dst;
-            dst = 1 - dst;
-        }
-        cur[l] = src;
-        if (!mixed && l == 0 && cur[0] != 0) {
-            k_copy_back<<<b->ft_cnt[0], TILE_THREADS, 0, s>>>(b->dev, b->d_tiles + b->ft_off[0]);
-            b->launches += 1;
-        }
-    }
-    if (mixed) b->cur0 = cur[0];
+    cudaMemcpyAsync(b->h_pinned, b->dev.num_active, sizeof(int), cudaMemcpyDeviceToHost, s);
 }
 
-// One outer iteration: the FP64 residual norm of level 0 (mixed: also its
-// FP32 copy as the inner right-hand side), convergence bookkeeping, then
-// b->inner V-cycles (mixed: the last one's final level-0 kernel adds the
-// correction to psi).
-static void enqueue_iteration(gb_batch *b, int first, cudaStream_t s)
-{
-    BatchDev &D = b->dev;
-    const TileEntry *t0 = b->d_tiles + b->ot_off;
-    cudaMemsetAsync(D.num_active, 0, sizeof(int), s);
-    const bool mixed = b->precision == GB_BATCH_MIXED;
-    k_outer<<<b->ot_cnt, TILE_THREADS, 0, s>>>(D, t0, (const double *const *)b->d_f_tab, mixed ? 1 : 0);
-    k_finalize<<<gb_ceil_div(b->nprob, 4), 128, 0, s>>>(D, first);
-    b->launches += 2;
-    if (mixed) {
-        b->cur0 = 0;
-        for (int k = 0; k < b->inner; ++k) enqueue_vcycle<float>(b, s, k == 0, k == b->inner - 1);
-    } else {
-        enqueue_vcycle<double>(b, s, false, false);
-    }
-    cudaMemcpyAsync(b->h_pinned, D.num_active, sizeof(int), cudaMemcpyDeviceToHost, s);
-}
+// Algorithmic bytes of one V-cycle per interior point (24.7 words: four
+// sweeps of 3 words, residual 3, restriction 1.25, prolongation 2.25, all
+// levels x 4/3) at the inner precision, and of one FP64 outer step (read psi
+// and f, write the FP32 residual; read e, read and write psi).
+static double cycle_bytes(const gb_batch *b) { return 24.7 * (b->precision == GB_BATCH_FP64 ? 8.0 : 4.0); }
+static double outer_bytes(const gb_batch *b) { return b->precision == GB_BATCH_FP64 ? 16.0 : 40.0; }
 
-// After an iteration has completed: adds the recorded pre-smoothing launch
-// times and the algorithmic bytes of the problems that took part (per sweep
-// and interior point: psi read, f read, psi written, one word each).
+// Graph path, after an iteration: adds the recorded pre-smoothing times and
+// that operation's algorithmic bytes (per fused sweep and point: psi read,
+// f read, psi written; plus 3 words of residual and 1.25 of restriction).
 static void batch_profile_collect(gb_batch *b, cudaStream_t s)
 {
     if (!b->profile || b->ev_used == 0) return;
@@ -955,13 +1247,13 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
     for (int p = 0; p < b->nprob; ++p)
         if (b->h_active[p] && b->dloc[p] > 0) pts += (double)(b->n[p] - 2) * (double)(b->n[p] - 2);
     const double esz = b->precision == GB_BATCH_FP64 ? 8.0 : 4.0;
-    const int per_launch_sweeps = (b->precision == GB_BATCH_MIXED && b->nu1 >= 2) ? 2 : 1;  // first pre-smoothing launch
+    const int sweeps = (b->precision == GB_BATCH_MIXED && b->nu1 >= 2) ? 2 : 1;
     for (int i = 0; i + 1 < b->ev_used; i += 2) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]) == cudaSuccess) {
             b->prof_ms += ms;
             b->prof_launches += 1;
-            b->prof_bytes += 3.0 * esz * per_launch_sweeps * pts;
+            b->prof_bytes += (3.0 * sweeps + 3.0 + 1.25) * esz * pts;
         } else {
             cudaGetLastError();  // timing is advisory: never let it fail a solve
         }
@@ -972,7 +1264,7 @@ extern "C" int gb_batch_profile(gb_batch *b, int enable)
 {
     if (!b) return GB_ERR_INVALID;
     if (enable && b->ev.empty()) {
-        b->ev.resize(2 * (b->nu1 + 1));
+        b->ev.resize(2 * (b->inner + 2));
         for (auto &e : b->ev) GB_CUDA_TRY(cudaEventCreate(&e));
     }
     b->profile = enable ? 1 : 0;
@@ -1003,9 +1295,9 @@ static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStre
     GB_CUDA_TRY(cudaMemcpyAsync(b->d_f_tab, pf.data(), sizeof(void *) * b->nprob, cudaMemcpyHostToDevice, s));
     GB_CUDA_TRY(cudaMemcpyAsync(b->d_psi_tab, pp.data(), sizeof(void *) * b->nprob, cudaMemcpyHostToDevice, s));
     if (b->precision == GB_BATCH_FP64) {
-        // level-0 x and f of the plain cycle are the caller's arrays
+        // level-0 x (buffer 0) and f of the plain cycle are the caller's arrays
         for (int p = 0; p < b->nprob; ++p) {
-            b->hx[(size_t)p * BP_MAXL] = d_psi + b->off0[p];            // buffer 0 of level 0
+            b->hx[(size_t)p * BP_MAXL] = d_psi + b->off0[p];
             b->hf[(size_t)p * BP_MAXL] = (void *)(d_f + b->off0[p]);
         }
         GB_CUDA_TRY(cudaMemcpyAsync(b->d_ptrs, b->hx.data(), sizeof(void *) * b->hx.size(), cudaMemcpyHostToDevice, s));
@@ -1018,23 +1310,10 @@ static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStre
     return GB_OK;
 }
 
-extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_psi, int *cycles, double *relres,
-                                     void *stream)
+static int solve_graph(gb_batch *b, cudaStream_t s)
 {
-    if (!b || !d_f || !d_psi) { gb_set_error("gb_batch_solve_device: null argument"); return GB_ERR_INVALID; }
-    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
-    BatchDev &D = b->dev;
-    b->launches = 0;
-    int st = batch_bind_io(b, d_f, d_psi, s);
-    if (st != GB_OK) return st;
-    GB_CUDA_TRY(cudaMemsetAsync(d_psi, 0, sizeof(double) * (size_t)b->total, s));
-    std::vector<int> ones(b->nprob, 1);
-    GB_CUDA_TRY(cudaMemcpyAsync(D.active, ones.data(), sizeof(int) * b->nprob, cudaMemcpyHostToDevice, s));
-    GB_CUDA_TRY(cudaMemsetAsync(D.cycles, 0, sizeof(int) * b->nprob, s));
-    GB_CUDA_TRY(cudaMemsetAsync(D.failed, 0, sizeof(int) * b->nprob, s));
-    // first iteration eagerly (records ||f||); later ones from a CUDA graph
     b->ev_used = 0;
-    enqueue_iteration(b, 1, s);
+    enqueue_iteration(b, b->ops0, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     batch_profile_collect(b, s);
     if (!b->cycle_graph || b->graph_profile != b->profile) {
@@ -1045,7 +1324,7 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
         const long long l0 = b->launches;
         b->ev_used = 0;
         GB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        enqueue_iteration(b, 0, cs);
+        enqueue_iteration(b, b->ops, cs);
         GB_CUDA_TRY(cudaStreamEndCapture(cs, &g));
         b->launches_per_cycle = b->launches - l0;
         b->launches = l0;
@@ -1061,6 +1340,89 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
         b->ev_used = b->graph_ev;
         batch_profile_collect(b, s);
     }
+    return GB_OK;
+}
+
+static int solve_persistent(gb_batch *b, cudaStream_t s)
+{
+    const int n0 = (int)b->ops0.size(), n1 = (int)b->ops.size();
+    GB_CUDA_TRY(cudaMemcpyAsync(b->d_ops, b->ops0.data(), sizeof(Op) * n0, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(b->d_ops + n0, b->ops.data(), sizeof(Op) * n1, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(cudaMemsetAsync(b->d_sync, 0, sizeof(unsigned) * 4, s));
+    GridSync gs;
+    gs.count = b->d_sync;
+    gs.gen = b->d_sync + 1;
+    gs.err = (int *)(b->d_sync + 2);
+    gs.limit = 1LL << 24;   // ~1-2 s of polling at 64 ns per poll
+    const Op *ops0 = b->d_ops, *ops = b->d_ops + n0;
+    const TileEntry *tiles = b->d_tiles;
+    const double *const *fp = (const double *const *)b->d_f_tab;
+    int nu1 = b->nu1, nu2 = b->nu2;
+    int max_iter = b->max_cycles / std::max(1, b->inner) + 2;
+    BatchDev D = b->dev;
+    void *args[] = {&D, &tiles, &fp, &ops0, (void *)&n0, &ops, (void *)&n1, &nu1, &nu2, &max_iter, &gs};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (b->profile && b->ev.size() >= 2) {
+        e0 = b->ev[0];
+        e1 = b->ev[1];
+        cudaEventRecord(e0, s);
+    }
+    cudaError_t err;
+    if (b->precision == GB_BATCH_FP64)
+        err = cudaLaunchCooperativeKernel((void *)k_persistent<double>, b->pgrid, TILE_THREADS, args, b->psmem, s);
+    else
+        err = cudaLaunchCooperativeKernel((void *)k_persistent<float>, b->pgrid, TILE_THREADS, args, b->psmem, s);
+    if (err != cudaSuccess) {
+        gb_set_error("persistent launch (%d blocks, %zu B shared): %s", b->pgrid, b->psmem, cudaGetErrorString(err));
+        return GB_ERR_CUDA;
+    }
+    b->launches += 1;
+    if (e1) cudaEventRecord(e1, s);
+    unsigned sync[4];
+    GB_CUDA_TRY(cudaMemcpyAsync(sync, b->d_sync, sizeof(sync), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (sync[2]) {
+        gb_set_error("persistent solve: a grid barrier wait timed out");
+        return GB_TIMEOUT;
+    }
+    if (e1) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) {
+            std::vector<int> cyc(b->nprob);
+            cudaMemcpy(cyc.data(), b->dev.cycles, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost);
+            double bytes = 0.0;
+            for (int p = 0; p < b->nprob; ++p) {
+                const double pts = (double)(b->n[p] - 2) * (double)(b->n[p] - 2);
+                const int outer = cyc[p] / std::max(1, b->inner) + 1;
+                bytes += pts * (cyc[p] * cycle_bytes(b) + outer * outer_bytes(b));
+            }
+            b->prof_ms += ms;
+            b->prof_launches += 1;
+            b->prof_bytes += bytes;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    return GB_OK;
+}
+
+extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_psi, int *cycles, double *relres,
+                                     void *stream)
+{
+    if (!b || !d_f || !d_psi) { gb_set_error("gb_batch_solve_device: null argument"); return GB_ERR_INVALID; }
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    BatchDev &D = b->dev;
+    b->launches = 0;
+    if (b->plan_inner != b->inner) build_plans(b);
+    int st = batch_bind_io(b, d_f, d_psi, s);
+    if (st != GB_OK) return st;
+    GB_CUDA_TRY(cudaMemsetAsync(d_psi, 0, sizeof(double) * (size_t)b->total, s));
+    std::vector<int> ones(b->nprob, 1);
+    GB_CUDA_TRY(cudaMemcpyAsync(D.active, ones.data(), sizeof(int) * b->nprob, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(cudaMemsetAsync(D.cycles, 0, sizeof(int) * b->nprob, s));
+    GB_CUDA_TRY(cudaMemsetAsync(D.failed, 0, sizeof(int) * b->nprob, s));
+    st = b->exec == GB_BATCH_EXEC_PERSISTENT ? solve_persistent(b, s) : solve_graph(b, s);
+    if (st != GB_OK) return st;
     std::vector<int> fl(b->nprob);
     GB_CUDA_TRY(cudaMemcpyAsync(fl.data(), D.failed, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s));
     if (cycles) GB_CUDA_TRY(cudaMemcpyAsync(cycles, D.cycles, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s));

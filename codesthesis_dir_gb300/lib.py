@@ -33,6 +33,8 @@ SMOOTHER_LEX = 0
 SMOOTHER_ZEBRA = 1
 BATCH_FP64 = 0
 BATCH_MIXED = 1
+BATCH_EXEC_GRAPH = 0
+BATCH_EXEC_PERSISTENT = 1
 
 
 class GBError(RuntimeError):
@@ -95,6 +97,7 @@ SIGNATURES = [
     ("gb_batch_destroy", C.c_int, [_vp]),
     ("gb_batch_total_points", C.c_longlong, [_vp]),
     ("gb_batch_set_inner_cycles", C.c_int, [_vp, C.c_int]),
+    ("gb_batch_set_exec", C.c_int, [_vp, C.c_int]),
     ("gb_batch_solve_device", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("gb_batch_solve_host", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     ("gb_batch_last_launches", C.c_longlong, [_vp]),

@@ -200,6 +200,15 @@ int gb_batch_destroy(gb_batch *b);
  * and the FP64 update run once per k inner cycles, and convergence is
  * tested every k cycles. */
 int gb_batch_set_inner_cycles(gb_batch *b, int inner);
+/* How a solve is executed.  GRAPH (the default): one kernel per level
+ * operation, one CUDA graph per outer iteration.  PERSISTENT (devices with
+ * cooperative launch): one launch runs every level of every cycle of every
+ * problem until all have converged, with bounded grid-wide barriers between
+ * the level operations (a barrier that waits too long ends the solve with
+ * GB_TIMEOUT).  Both run the same operations and give identical results. */
+#define GB_BATCH_EXEC_GRAPH      0
+#define GB_BATCH_EXEC_PERSISTENT 1
+int gb_batch_set_exec(gb_batch *b, int mode);
 /* Total doubles of the packed f / psi arrays. */
 long long gb_batch_total_points(const gb_batch *b);
 /* Device-resident solve: d_f, d_psi device pointers (packed).  cycles and

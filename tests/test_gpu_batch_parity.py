@@ -46,13 +46,14 @@ def independent_relres(sizes, f, psi):
 SMALL = [3, 5, 9, 17, 33, 65, 129, 257, 65, 129, 3, 33, 513]
 
 
+@pytest.mark.parametrize("exec_mode", [0, 1], ids=["graph", "persistent"])
 @pytest.mark.parametrize("precision,inner", [(0, 1), (1, 1), (1, 2), (1, 3)],
                          ids=["fp64", "mixed", "mixed-inner2", "mixed-inner3"])
-def test_batch_matches_oracle(oracle, gblib, precision, inner):
+def test_batch_matches_oracle(oracle, gblib, precision, inner, exec_mode):
     from codesthesis_dir_gb300.batch import BatchPoisson
     f = make_batch(SMALL, 7)
     st_o, psi_o, cyc_o, rr_o = oracle.batch_solve(SMALL, f, precision=precision, inner=inner)
-    bp = BatchPoisson(SMALL, precision=precision, inner=inner)
+    bp = BatchPoisson(SMALL, precision=precision, inner=inner, exec_mode=exec_mode)
     st, psi, cyc, rr = bp.solve_host(f)
     assert st == 0 and st_o == 0
     np.testing.assert_array_equal(cyc, cyc_o)
@@ -90,9 +91,25 @@ def test_batch_edge_cases(oracle, gblib):
     np.testing.assert_array_equal(cyc1, cyc2)
 
 
-def test_batch_max_cycles_status(gblib):
+@pytest.mark.parametrize("exec_mode", [0, 1], ids=["graph", "persistent"])
+def test_batch_max_cycles_status(gblib, exec_mode):
     from codesthesis_dir_gb300.batch import BatchPoisson
     sizes = [129, 65]
     f = make_batch(sizes, 2)
-    st, psi, cyc, rr = BatchPoisson(sizes, precision=0, max_cycles=2, rtol=1e-14).solve_host(f)
+    st, psi, cyc, rr = BatchPoisson(sizes, precision=0, max_cycles=2, rtol=1e-14, exec_mode=exec_mode).solve_host(f)
     assert st == 1 and np.all(cyc == 2)
+
+
+def test_graph_and_persistent_agree_on_workload_sizes(gblib):
+    """The two execution modes run the same operations: identical results on
+    a batch with every size of the benchmark workload."""
+    from codesthesis_dir_gb300.batch import BatchPoisson
+    sizes = [513, 65, 257, 129, 513, 129, 65, 257, 3, 17]
+    f = make_batch(sizes, 21)
+    out = []
+    for mode in (0, 1):
+        st, psi, cyc, rr = BatchPoisson(sizes, precision=1, inner=3, exec_mode=mode).solve_host(f)
+        assert st == 0
+        out.append((psi, cyc))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
