@@ -3,6 +3,8 @@
 // per line, matrices allowed to differ per line.  Each line is eliminated
 // with the reference's operations in the reference's order (-fmad=false), on
 // copies in a scratch buffer, so the caller's inputs survive.
+#include <mutex>
+
 #include "gbcommon.cuh"
 
 struct LineView {
@@ -159,5 +161,70 @@ extern "C" int gb_pdma_batch(const double *a, const double *b, const double *c, 
     GB_CUDA_TRY(cudaFreeAsync(scr, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// gb_pdma_batch_noalloc: the pentadiagonal batch without any allocation.
+//
+// The per-line work copies live in one file-scope device array of
+// GB_PDMA_NOALLOC_MAX_DOUBLES doubles (4 MiB) that every GPU which loads the
+// library holds until the process exits.  Host code may not pass the
+// array's name to a kernel (on the host it is only a stand-in for the
+// device symbol), so its device address is looked up once per device, with
+// that device current, and cached.  The kernel writes every scratch element
+// it reads, so nothing needs clearing between calls; calls that overlap on
+// the GPU share the array and race.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_pdma_noalloc_scratch[GB_PDMA_NOALLOC_MAX_DOUBLES];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_addr[128];
+static bool g_noalloc_ready[128];
+
+static int noalloc_scratch(double **out)
+{
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) {
+        gb_set_error("gb_pdma_batch_noalloc: device ordinal %d out of range", dev);
+        return GB_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ready[dev]) {
+        void *addr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&addr, g_pdma_noalloc_scratch);
+        if (e != cudaSuccess) {
+            gb_set_error("gb_pdma_batch_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            return GB_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = (double *)addr;
+        g_noalloc_ready[dev] = true;
+    }
+    *out = g_noalloc_addr[dev];
+    return GB_OK;
+}
+
+extern "C" int gb_pdma_batch_noalloc(const double *a, const double *b, const double *c, const double *d,
+                                     const double *e, const double *r, double *x, int n, int nlines,
+                                     long long ls, long long es, void *stream)
+{
+    int st = check(n, 2, nlines, "gb_pdma_batch_noalloc");
+    if (st != GB_OK || nlines == 0) return st;
+    const unsigned long long need = 5ull * (unsigned long long)n * (unsigned long long)nlines;
+    if (need > (unsigned long long)GB_PDMA_NOALLOC_MAX_DOUBLES) {
+        gb_set_error("gb_pdma_batch_noalloc: 5*n*nlines = %llu doubles exceeds the fixed scratch of %u doubles "
+                     "(n=%d, nlines=%d); use gb_pdma_batch or split the lines",
+                     need, (unsigned)GB_PDMA_NOALLOC_MAX_DOUBLES, n, nlines);
+        return GB_ERR_INVALID;
+    }
+    double *scr = nullptr;
+    st = noalloc_scratch(&scr);
+    if (st != GB_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_pdma_batch<<<gb_ceil_div(nlines, 128), 128, 0, s>>>({a, ls, es}, {b, ls, es}, {c, ls, es}, {d, ls, es}, {e, ls, es},
+                                                          {r, ls, es}, x, ls, es, n, nlines, scr);
+    GB_CUDA_TRY(cudaGetLastError());
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
     return GB_OK;
 }

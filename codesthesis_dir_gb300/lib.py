@@ -93,6 +93,8 @@ SIGNATURES = [
     ("gb_tdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
     ("gb_ptdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
     ("gb_pdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
+    ("gb_pdma_batch_noalloc", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong,
+                                       C.c_longlong, _vp]),
     ("gb_batch_create", C.c_int, [C.c_int, _ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(_vp)]),
     ("gb_batch_destroy", C.c_int, [_vp]),
     ("gb_batch_total_points", C.c_longlong, [_vp]),

@@ -180,6 +180,25 @@ int gb_pdma_batch(const double *a, const double *b, const double *c, const doubl
                   const double *e, const double *r, double *x, int n, int nlines,
                   long long line_stride, long long elem_stride, void *stream);
 
+/* The same pentadiagonal batch without any allocation, for callers that
+ * cannot allocate device memory when they call: a Fortran driver whose
+ * storage is all static (COMMON blocks sized by PARAMETER at compile time)
+ * and which has no way to handle an allocation failure in the middle of a
+ * time step, or a program that has handed the device to its own memory
+ * pool or budget (a server admitting work against a fixed device-memory
+ * budget) and must not let the CUDA runtime grow its own pool.  No
+ * counterpart in the reference (its pdma works on arrays the caller owns).
+ * Limit: 5*n*nlines <= GB_PDMA_NOALLOC_MAX_DOUBLES (4 MiB of scratch that
+ * every GPU loading the library holds until exit); larger requests return
+ * GB_ERR_INVALID without launching.  The first call on each device looks up
+ * the scratch array's device address (make that first call before any
+ * stream capture).  All calls share the scratch: calls that overlap on the
+ * GPU race.  Results are identical to gb_pdma_batch. */
+#define GB_PDMA_NOALLOC_MAX_DOUBLES 524288u
+int gb_pdma_batch_noalloc(const double *a, const double *b, const double *c, const double *d,
+                          const double *e, const double *r, double *x, int n, int nlines,
+                          long long line_stride, long long elem_stride, void *stream);
+
 /* ------------------------------------------------- batched Poisson solve */
 /* Many independent Dirichlet problems nabla^2 psi = f on n x n vertex grids
  * (n = 2^m + 1, 3 <= n <= 8193) of the unit square, psi = 0 on the boundary;
