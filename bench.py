@@ -294,8 +294,31 @@ def main():
         ms, cu, cyc, rr, launches = timed(mixed, d_psi, args.steps, 0)
     import ctypes as C
     pms, pl, pb = C.c_double(), C.c_longlong(), C.c_double()
-    L.gb_batch_profile_read(mixed._h, C.byref(pms), C.byref(pl), C.byref(pb), 1)
+    L.gb_batch_profile_read(mixed._h, C.byref(pms), C.byref(pl), C.byref(pb), 0)
+    kinds = {}
+    for kname, kid in (("down_finest", 1), ("up_finest", 2), ("outer_fp64", 4)):
+        kms, kl, kb = C.c_double(), C.c_longlong(), C.c_double()
+        L.gb_batch_profile_read_kind(mixed._h, kid, C.byref(kms), C.byref(kl), C.byref(kb))
+        if kl.value:
+            kinds[kname] = {"launches": kl.value, "avg_ms": kms.value / kl.value,
+                            "alg_bytes_per_launch": kb.value / kl.value,
+                            "achieved_GBs": kb.value / (kms.value / 1e3) / 1e9 if kms.value > 0 else None}
+    L.gb_batch_profile_read(mixed._h, None, None, None, 1)
     L.gb_batch_profile(mixed._h, 0)
+    r64, r32 = C.c_double(), C.c_double()
+    L.gb_measure_issue_rates(C.byref(r64), C.byref(r32))
+    fp64_pipe = None
+    if "outer_fp64" in kinds:
+        # 3 adds + 3 fused multiply-adds of FP64 per interior point (the float
+        # conversion runs on the integer pipe)
+        k = kinds["outer_fp64"]
+        pts_per_launch = k["alg_bytes_per_launch"] / 20.0
+        ach = 6.0 * pts_per_launch / (k["avg_ms"] / 1e3)
+        fp64_pipe = {"kernel": "k_op<float,OP_OUTER> (FP64 residual, norm and FP32 copy)",
+                     "achieved_instr_per_s": ach, "peak_instr_per_s": r64.value,
+                     "frac": ach / r64.value if r64.value > 0 else None,
+                     "peak_kind": "measured (FP64 FMA issue probe, gb_measure_issue_rates)",
+                     "fp32_fma_instr_per_s": r32.value}
 
     # the same mixed solve as one persistent launch per solve
     pers = BatchPoisson(sizes, precision=lib.BATCH_MIXED, rtol=RTOL, inner=args.inner,
@@ -382,6 +405,8 @@ def main():
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_kind": peak_kind, "launches": pl.value,
                      "avg_launch_ms": (pms.value / pl.value) if pl.value else None},
+        "fp64_pipe": fp64_pipe,
+        "kernels_mixed_graph": kinds,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

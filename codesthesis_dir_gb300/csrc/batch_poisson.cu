@@ -729,12 +729,15 @@ struct gb_batch {
     // graph path
     cudaGraphExec_t cycle_graph = nullptr;
     long long launches = 0, launches_per_cycle = 0;
-    // profiling
+    // profiling: CUDA events around every level-0 operation and outer pass
     int profile = 0, graph_profile = -1, graph_ev = 0;
     std::vector<cudaEvent_t> ev;
+    std::vector<int> ev_kind;           // operation kind of each recorded event pair
     int ev_used = 0;
-    double prof_ms = 0.0, prof_bytes = 0.0;
+    double prof_ms = 0.0, prof_bytes = 0.0;   // persistent launches / the finest-level OP_SMOOTH_R
     long long prof_launches = 0;
+    double kind_ms[8] = {0}, kind_bytes[8] = {0};
+    long long kind_launches[8] = {0};
     std::vector<int> h_active;
 };
 
@@ -1218,11 +1221,16 @@ static void enqueue_iteration(gb_batch *b, const std::vector<Op> &v, cudaStream_
 {
     cudaMemsetAsync(b->dev.num_active, 0, sizeof(int), s);
     for (const Op &op : v) {
-        const bool ev = b->profile && op.kind == OP_SMOOTH_R && op.l == 0 && b->ev_used + 2 <= (int)b->ev.size();
+        const bool timed = (op.l == 0 && op.kind != OP_FINALIZE && op.kind != OP_LOCAL) || op.kind == OP_OUTER;
+        const bool ev = b->profile && timed && b->ev_used + 2 <= (int)b->ev.size();
         if (ev) prof_record(b->ev[b->ev_used], s);
         if (b->precision == GB_BATCH_MIXED) launch_op<float>(b, op, s);
         else launch_op<double>(b, op, s);
-        if (ev) { prof_record(b->ev[b->ev_used + 1], s); b->ev_used += 2; }
+        if (ev) {
+            prof_record(b->ev[b->ev_used + 1], s);
+            b->ev_kind[b->ev_used / 2] = op.kind;
+            b->ev_used += 2;
+        }
     }
     cudaMemcpyAsync(b->h_pinned, b->dev.num_active, sizeof(int), cudaMemcpyDeviceToHost, s);
 }
@@ -1234,28 +1242,54 @@ static void enqueue_iteration(gb_batch *b, const std::vector<Op> &v, cudaStream_
 static double cycle_bytes(const gb_batch *b) { return 24.7 * (b->precision == GB_BATCH_FP64 ? 8.0 : 4.0); }
 static double outer_bytes(const gb_batch *b) { return b->precision == GB_BATCH_FP64 ? 16.0 : 40.0; }
 
-// Graph path, after an iteration: adds the recorded pre-smoothing times and
-// that operation's algorithmic bytes (per fused sweep and point: psi read,
-// f read, psi written; plus 3 words of residual and 1.25 of restriction).
+// Graph path, after an iteration: adds the recorded times per operation kind
+// and each operation's algorithmic bytes for the problems that took part.
+// Per interior point (words of the inner precision unless noted):
+//   OP_SMOOTH_R  sweeps x 3 (psi read, f read, psi written) + residual 3 +
+//                restriction 1.25;
+//   OP_PROLONG   prolongation 2.25 + sweeps x 3 (+ 16 B of psi when it
+//                applies the correction);
+//   OP_SMOOTH    sweeps x 3;
+//   OP_OUTER     FP64 psi and f read (16 B) + FP32 residual written (4 B).
 static void batch_profile_collect(gb_batch *b, cudaStream_t s)
 {
     if (!b->profile || b->ev_used == 0) return;
     b->h_active.resize(b->nprob);
     cudaMemcpyAsync(b->h_active.data(), b->dev.active, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
-    double pts = 0.0;
-    for (int p = 0; p < b->nprob; ++p)
-        if (b->h_active[p] && b->dloc[p] > 0) pts += (double)(b->n[p] - 2) * (double)(b->n[p] - 2);
+    double pts_tile = 0.0, pts_all = 0.0;
+    for (int p = 0; p < b->nprob; ++p) {
+        if (!b->h_active[p]) continue;
+        const double pts = (double)(b->n[p] - 2) * (double)(b->n[p] - 2);
+        pts_all += pts;
+        if (b->dloc[p] > 0) pts_tile += pts;
+    }
     const double esz = b->precision == GB_BATCH_FP64 ? 8.0 : 4.0;
-    const int sweeps = (b->precision == GB_BATCH_MIXED && b->nu1 >= 2) ? 2 : 1;
+    const bool mixed = b->precision == GB_BATCH_MIXED;
+    const int pre = (mixed && b->nu1 >= 2) ? 2 : 1;
+    const int post = std::min(b->nu2, mixed ? 2 : 1);
     for (int i = 0; i + 1 < b->ev_used; i += 2) {
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]) == cudaSuccess) {
+        if (cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]) != cudaSuccess) {
+            cudaGetLastError();  // timing is advisory: never let it fail a solve
+            continue;
+        }
+        const int k = b->ev_kind[i / 2];
+        double bytes = 0.0;
+        switch (k) {
+        case OP_SMOOTH_R: bytes = (3.0 * pre + 3.0 + 1.25) * esz * pts_tile; break;
+        case OP_PROLONG: bytes = ((2.25 + 3.0 * post) * esz + (mixed ? 16.0 : 0.0)) * pts_tile; break;
+        case OP_SMOOTH: bytes = 3.0 * esz * pts_tile; break;
+        case OP_OUTER: bytes = 20.0 * pts_all; break;
+        default: break;
+        }
+        b->kind_ms[k] += ms;
+        b->kind_bytes[k] += bytes;
+        b->kind_launches[k] += 1;
+        if (k == OP_SMOOTH_R) {
             b->prof_ms += ms;
             b->prof_launches += 1;
-            b->prof_bytes += (3.0 * sweeps + 3.0 + 1.25) * esz * pts;
-        } else {
-            cudaGetLastError();  // timing is advisory: never let it fail a solve
+            b->prof_bytes += bytes;
         }
     }
 }
@@ -1264,7 +1298,8 @@ extern "C" int gb_batch_profile(gb_batch *b, int enable)
 {
     if (!b) return GB_ERR_INVALID;
     if (enable && b->ev.empty()) {
-        b->ev.resize(2 * (b->inner + 2));
+        b->ev.resize(2 * (4 * b->inner + 8));
+        b->ev_kind.assign(b->ev.size() / 2, 0);
         for (auto &e : b->ev) GB_CUDA_TRY(cudaEventCreate(&e));
     }
     b->profile = enable ? 1 : 0;
@@ -1281,7 +1316,21 @@ extern "C" int gb_batch_profile_read(gb_batch *b, double *ms, long long *launche
         b->prof_ms = 0.0;
         b->prof_bytes = 0.0;
         b->prof_launches = 0;
+        for (int k = 0; k < 8; ++k) {
+            b->kind_ms[k] = 0.0;
+            b->kind_bytes[k] = 0.0;
+            b->kind_launches[k] = 0;
+        }
     }
+    return GB_OK;
+}
+
+extern "C" int gb_batch_profile_read_kind(gb_batch *b, int kind, double *ms, long long *launches, double *alg_bytes)
+{
+    if (!b || kind < 0 || kind >= 8) return GB_ERR_INVALID;
+    if (ms) *ms = b->kind_ms[kind];
+    if (launches) *launches = b->kind_launches[kind];
+    if (alg_bytes) *alg_bytes = b->kind_bytes[kind];
     return GB_OK;
 }
 

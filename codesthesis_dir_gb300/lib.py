@@ -105,6 +105,8 @@ SIGNATURES = [
     ("gb_batch_last_launches", C.c_longlong, [_vp]),
     ("gb_batch_profile", C.c_int, [_vp, C.c_int]),
     ("gb_batch_profile_read", C.c_int, [_vp, _dp, C.POINTER(C.c_longlong), _dp, C.c_int]),
+    ("gb_batch_profile_read_kind", C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp]),
+    ("gb_measure_issue_rates", C.c_int, [_dp, _dp]),
 ]
 
 

@@ -129,7 +129,7 @@ int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *sweeps);
 
 /* ------------------------------------------- gfortran-compatible drop-in */
 /* These read/write the caller's COMMON blocks (declared by the Fortran main
- * program; the library carries weak definitions of the reference's sizes,
+ * program; the library carries weak references of the reference's sizes,
  * kr = 290, kp = 1610).  Other PARAMETER bounds: call gb_prb_bind_bounds
  * (or set GB300_PRB_KR / GB300_PRB_KP) before poissoninit_. */
 void gb_prb_bind_bounds(int kr, int kp);
@@ -243,9 +243,25 @@ long long gb_batch_last_launches(const gb_batch *b);
 /* Times every launch of the finest-level smoothing kernel with CUDA events
  * on the solve's stream during later solves (enable = 0 stops). */
 int gb_batch_profile(gb_batch *b, int enable);
-/* Accumulated smoothing-launch time (ms), launch count and algorithmic
- * bytes (1.5 words per interior point per half-sweep); reset != 0 clears. */
+/* Accumulated time (ms), launch count and algorithmic bytes of the
+ * finest-level down operation (sweeps + residual + restriction; in
+ * persistent mode: of the whole-solve launches); reset != 0 clears all
+ * profile counters. */
 int gb_batch_profile_read(gb_batch *b, double *ms, long long *launches, double *alg_bytes, int reset);
+/* The same per operation kind (graph mode): 0 smoothing, 1 smoothing +
+ * residual + restriction, 2 prolongation + smoothing, 4 FP64 outer pass;
+ * finest level only, except the outer pass. */
+#define GB_BATCH_OP_SMOOTH   0
+#define GB_BATCH_OP_DOWN     1
+#define GB_BATCH_OP_UP       2
+#define GB_BATCH_OP_OUTER    4
+int gb_batch_profile_read_kind(gb_batch *b, int kind, double *ms, long long *launches, double *alg_bytes);
+
+/* ------------------------------------------------------ device probes */
+/* Issue rates of FP64 and FP32 fused multiply-adds on the current device
+ * (instructions per second, every SM busy); the FP64 figure is the peak the
+ * FP64-bound kernels are measured against. */
+int gb_measure_issue_rates(double *fp64_fma_per_s, double *fp32_fma_per_s);
 
 #ifdef __cplusplus
 }
