@@ -12,6 +12,7 @@
 // twenty fields of one instance in one allocation.  For the grids these
 // drivers use (nr <= 512, np <= 2048) an instance is at most ~170 MB and the
 // working set of a step stays in the 126 MB L2 for nr*np up to ~1.5e6.
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -104,7 +105,9 @@ __global__ void k_cvort_deriv_x(PrbDev d)
     apply_ptdma_rhs(d.fac_x, np + 1, d.f[GB_F_Bn] + GIX(i, 0, ld), ld, rhsT);
 }
 
-// Vorticity update, PRB:706-776 (first) / PRB:900-982 (leapfrog).
+// Vorticity update, PRB:706-776 (first) / PRB:900-982 (leapfrog).  Annulus
+// (velvor2dnewsch3.4.f:710-786 / :911-993): radius r = r0 + i dr, the Cra/r
+// term, 0.5*Cp in the leapfrog RHS1 and the rotational buoyancy in RHS2.
 __global__ void k_cvort_update(PrbDev d, int first)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -119,7 +122,7 @@ __global__ void k_cvort_update(PrbDev d, int first)
     int km = k - 1, ka = k + 1;
     if (k == 0) km = np - 1;
     if (k == np) ka = 1;
-    const double ri = 1.0;
+    const double ri = d.polar ? 1.0 / (d.r0 + (double)i * d.dr) : 1.0;
     const double u = (uel[GIX(i, ka, ld)] + uel[GIX(i, k, ld)]) * 0.5;
     const double v = (vel[GIX(i, k, ld)] + vel[GIX(ip, k, ld)]) * 0.5;
     const double Chha = (C[GIX(i, ka, ld)] + C[GIX(i, km, ld)]) * (dpi * dpi);
@@ -129,32 +132,47 @@ __global__ void k_cvort_update(PrbDev d, int first)
     const double Cr = d.f[GB_F_A][GIX(i, k, ld)];
     const double thh = d.f[GB_F_Bn][GIX(i, k, ld)];
     const double cnh = (-1.0 * (dpi * dpi)) * (ri * ri);
-    double RHS1, cf1;
-    if (first) {
-        RHS1 = Crra + Chha * (ri * ri) + C[GIX(i, k, ld)] / (Ptl * dt);
-        cf1 = 1.0 / (Ptl * dt) - cnr - cnh;
+    double RHS1, RHS2, cf1;
+    if (d.polar) {
+        const double Cra = (C[GIX(i + 1, k, ld)] - C[GIX(i - 1, k, ld)]) * 0.5 * dri;
+        const double thr = d.f[GB_F_An][GIX(i, k, ld)];
+        if (first) {
+            RHS1 = Crra + Cra * ri + Chha * (ri * ri) + C[GIX(i, k, ld)] / (Ptl * dt);
+            cf1 = 1.0 / (Ptl * dt) - cnr - cnh;
+        } else {
+            RHS1 = Crra + Cra * ri + Chha * (ri * ri) + 0.5 * Cp[GIX(i, k, ld)] / (Ptl * dt);
+            cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
+        }
+        RHS2 = -Ra * thh + 2.0 * Ra * (-thr * u - thh * v * ri) / d.Re / Ptl;
     } else {
-        RHS1 = Crra + Chha * (ri * ri) + 0.5 * C[GIX(i, k, ld)] / (Ptl * dt);
-        cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
+        if (first) {
+            RHS1 = Crra + Chha * (ri * ri) + C[GIX(i, k, ld)] / (Ptl * dt);
+            cf1 = 1.0 / (Ptl * dt) - cnr - cnh;
+        } else {
+            RHS1 = Crra + Chha * (ri * ri) + 0.5 * C[GIX(i, k, ld)] / (Ptl * dt);
+            cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
+        }
+        RHS2 = -Ra * thh;
     }
     const double ULT = (u * Cr + v * Ch * ri) / Ptl;
-    const double RHS2 = -Ra * thh;
     const double cf2 = cnr + cnh;
     const double cn = (cf2 * Cp[GIX(i, k, ld)] - ULT - RHS2 + RHS1) / cf1;
     d.f[GB_F_Cn][GIX(i, k, ld)] = cn;
     if (!first) d.f[GB_F_Ap][GIX(i, k, ld)] = cn;
 }
 
-// Robert filter X += 0.02 (Xn - 2X + Xp) on rows 1..imax (PRB:1041-1045,
-// PRB:1435-1440).
+// Robert filter X += gamma (Xn - 2X + Xp) on rows 1..imax, gamma = 0.02
+// (PRB:1041-1045, PRB:1435-1440) or 0.05 in the annulus
+// (velvor2dnewsch3.4.f:1055, :1454).
 __global__ void k_robert(PrbDev d, int fx, int fxn, int fxp, int imax)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= imax * (d.np + 1) || *d.abort) return;
     const int i = t % imax + 1, k = t / imax;
     const size_t c = GIX(i, k, d.ld);
+    const double gamma = d.polar ? 0.05 : 0.02;
     double *X = d.f[fx];
-    X[c] = X[c] + 0.02 * (d.f[fxn][c] - 2.0 * X[c] + d.f[fxp][c]);
+    X[c] = X[c] + gamma * (d.f[fxn][c] - 2.0 * X[c] + d.f[fxp][c]);
 }
 
 // thr (tdma along r, third-order wall rows) -> A, one thread per column k
@@ -195,6 +213,8 @@ __global__ void k_temp_deriv_x(PrbDev d)
 }
 
 // Temperature update, PRB:1142-1207 (first) / PRB:1292-1377 (Dufort-Frankel).
+// Annulus (velvor2dnewsch3.4.f:1140-1223 / :1308-1393): cell-centre radius
+// r = r0 + (i-1/2) dr and the thra/r term.
 __global__ void k_temp_update(PrbDev d, int first)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,26 +229,37 @@ __global__ void k_temp_update(PrbDev d, int first)
     int km = k - 1, ka = k + 1;
     if (k == 0) km = np - 1;
     if (k == np) ka = 1;
-    const double ri = 1.0;
+    const double ri = d.polar ? 1.0 / (d.r0 + ((double)i - 0.5) * d.dr) : 1.0;
     const double u = (uel[GIX(i, k, ld)] + uel[GIX(im, k, ld)]) * 0.5;
     const double v = (vel[GIX(i, k, ld)] + vel[GIX(i, km, ld)]) * 0.5;
-    double thrra, cnr;
+    double thrra, thra, cnr;
     const double thr = d.f[GB_F_A][GIX(i, k, ld)];
     if (i == 1) {
         thrra = (3.2 * th[GIX(i - 1, k, ld)] + 2.0 * th[GIX(i + 1, k, ld)] - 0.2 * th[GIX(i + 2, k, ld)]) * (dri * dri);
+        thra = (-4.0 * th[GIX(i - 1, k, ld)] / 3.0 + th[GIX(i + 1, k, ld)] / 3.0) * dri;
         cnr = -2.5 * (dri * dri) + 0.5 * dri * ri;
     } else if (i == nr) {
         thrra = (3.2 * th[GIX(i + 1, k, ld)] + 2.0 * th[GIX(i - 1, k, ld)] - 0.2 * th[GIX(i - 2, k, ld)]) * (dri * dri);
+        thra = (-th[GIX(i - 1, k, ld)] / 3.0 + 4.0 * th[GIX(i + 1, k, ld)] / 3.0) * dri;
         cnr = -2.5 * (dri * dri) - 0.5 * dri * ri;
     } else {
         thrra = (th[GIX(i - 1, k, ld)] + th[GIX(i + 1, k, ld)]) * (dri * dri);
+        thra = (th[GIX(i + 1, k, ld)] - th[GIX(i - 1, k, ld)]) * 0.5 * dri;
         cnr = -1.0 * (dri * dri);
     }
     const double thhha = (th[GIX(i, ka, ld)] + th[GIX(i, km, ld)]) * (dpi * dpi);
     const double thh = d.f[GB_F_B][GIX(i, k, ld)];
     const double cnp = -(1.0 * (dpi * dpi)) * (ri * ri);
     double RHS1, cf1;
-    if (first) {
+    if (d.polar) {
+        if (first) {
+            RHS1 = thrra + thra * ri + thhha * (ri * ri) + th[GIX(i, k, ld)] / dt;
+            cf1 = 1.0 / dt - cnr - cnp;
+        } else {
+            RHS1 = thrra + thra * ri + thhha * (ri * ri) + 0.5 * thp[GIX(i, k, ld)] / dt;
+            cf1 = 0.5 / dt - cnr - cnp;
+        }
+    } else if (first) {
         RHS1 = thrra + thhha * (ri * ri) + th[GIX(i, k, ld)] / dt;
         cf1 = 1.0 / dt - cnr - cnp;
     } else {
@@ -273,7 +304,9 @@ __global__ void k_heat(PrbDev d)
     }
 }
 
-// rhsv (PRB:1629-1676) and rhsu (PRB:1679-1721) in one pass.
+// rhsv (PRB:1629-1676) and rhsu (PRB:1679-1721) in one pass; the annulus
+// adds the Cn/r terms of velvor2dnewsch3.4.f:1666-1686 and divides the u
+// source by the face radius (:1714-1730).
 __global__ void k_rhs(PrbDev d, int do_v, int do_u)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -284,15 +317,21 @@ __global__ void k_rhs(PrbDev d, int do_v, int do_u)
     if (do_v) {
         const double Cr = (Cn[GIX(i, k, ld)] - Cn[GIX(i - 1, k, ld)]) / d.dr;
         double v;
-        if (i == 1) v = Cn[GIX(1, k, ld)] / d.dr;
+        if (d.polar) {
+            const double r = d.r0 + ((double)i - 0.5) * d.dr;
+            if (i == 1) v = Cn[GIX(1, k, ld)] / d.dr + Cn[GIX(1, k, ld)] / r;
+            else if (i == nr) v = -Cn[GIX(nr - 1, k, ld)] / d.dr + Cn[GIX(nr - 1, k, ld)] / r;
+            else v = Cr + (Cn[GIX(i, k, ld)] + Cn[GIX(i - 1, k, ld)]) / r;
+        } else if (i == 1) v = Cn[GIX(1, k, ld)] / d.dr;
         else if (i == nr) v = -Cn[GIX(nr - 1, k, ld)] / d.dr;
         else v = Cr;
         d.f[GB_F_vrh][GIX(i, k, ld)] = v;
     }
     if (do_u && i <= nr - 1) {
         const int km = (k == 0) ? np - 1 : k - 1;
+        const double r = d.polar ? d.r0 + (double)i * d.dr : 1.0;
         const double Ch = (Cn[GIX(i, k, ld)] - Cn[GIX(i, km, ld)]) / d.dp;
-        d.f[GB_F_urh][GIX(i, k, ld)] = -Ch / 1.0;
+        d.f[GB_F_urh][GIX(i, k, ld)] = -Ch / r;
     }
 }
 
@@ -331,13 +370,16 @@ __global__ void k_update(PrbDev d)
 
 // Per-step bookkeeping for graph-replayed steps: copies the step's Nusselt
 // numbers and sweep counts into the history slot given by *d.step_index.
-__global__ void k_record(PrbDev d, double rmr0, double xx)
+// Nu = heat * c / div: c = rmax - r0, div = xx in PRB (PRB:386-388);
+// c = -r0 ln(r0/rmax) (inner) and -rmax ln(r0/rmax) (outer), div = 2 pi in
+// the annulus (velvor2dnewsch3.4.f:386-387).
+__global__ void k_record(PrbDev d, double c1, double c2, double div)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int s = *d.step_index;
     if (s < d.hist_cap) {
-        d.nu_hist[2 * s + 0] = d.heat[0] * rmr0 / xx;   // PRB:386-388
-        d.nu_hist[2 * s + 1] = d.heat[1] * rmr0 / xx;
+        d.nu_hist[2 * s + 0] = d.heat[0] * c1 / div;
+        d.nu_hist[2 * s + 1] = d.heat[1] * c2 / div;
         d.sweep_hist[2 * s + 0] = d.mg_status[1];
         d.sweep_hist[2 * s + 1] = d.mg_status[3];
     }
@@ -399,7 +441,14 @@ int prb_launch_update(gb_prb *h, cudaStream_t s)
 
 int prb_launch_record(gb_prb *h, cudaStream_t s)
 {
-    k_record<<<1, 32, 0, s>>>(h->dev, h->p.rmax - h->p.r0, h->p.xx);
+    double c1 = h->p.rmax - h->p.r0, c2 = c1, div = h->p.xx;
+    if (h->p.variant == GB_PRB_ANNULUS) {
+        const double L = log(h->p.r0 / h->p.rmax);
+        c1 = -h->p.r0 * L;
+        c2 = -h->p.rmax * L;
+        div = 2.0 * acos(-1.0);
+    }
+    k_record<<<1, 32, 0, s>>>(h->dev, c1, c2, div);
     h->launches += 1;
     return GB_OK;
 }
@@ -419,10 +468,28 @@ extern "C" void gb_prb_default_params(gb_prb_params *p, int nr, int np)
     p->sor = 1.2;
     p->maxsweeps = 500;
     p->smoother = GB_SMOOTHER_LEX;
+    p->variant = GB_PRB_LAYER;
+    p->Re = 0.0;
 }
 
-// Level count of poissoninit (PRB:1744-1767).
-int prb_mg_levels(int nr)
+extern "C" void gb_prb_default_params_annulus(gb_prb_params *p, int nr, int np)
+{
+    gb_prb_default_params(p, nr, np);
+    p->variant = GB_PRB_ANNULUS;
+    p->dt = 2e-8;
+    p->r0 = 0.5;
+    p->rmax = 1.0;
+    p->xx = 2.0 * acos(-1.0);
+    p->Ra = 8e8;
+    p->Re = 1.06148e5;
+    p->Pr = 0.71;
+    p->tolcon = 10e-6;
+    p->maxsweeps = 10000;
+}
+
+// Level count of poissoninit (PRB:1744-1767; the annulus caps at 5,
+// velvor2dnewsch3.4.f:1778).
+int prb_mg_levels(int nr, int variant)
 {
     int nlev = 0, itest = nr, itest2 = nr;
     for (int i = 2; i <= 8; ++i) {
@@ -434,7 +501,11 @@ int prb_mg_levels(int nr)
             break;
         }
     }
-    if (nlev >= 5) nlev = 4;
+    if (variant == GB_PRB_ANNULUS) {
+        if (nlev > 5) nlev = 5;
+    } else if (nlev >= 5) {
+        nlev = 4;
+    }
     return nlev;
 }
 
@@ -444,8 +515,13 @@ int prb_refresh_scalars(gb_prb *h)
     d.dt = h->p.dt;
     d.Ra = h->p.Ra;
     d.Pr = h->p.Pr;
+    d.polar = h->p.variant == GB_PRB_ANNULUS;
+    d.r0 = h->p.r0;
+    d.Re = h->p.Re;
     d.dr = h->dr_set != 0.0 ? h->dr_set : (h->p.rmax - h->p.r0) / (double)h->p.nr;
-    d.dp = h->dp_set != 0.0 ? h->dp_set : h->p.xx / (double)h->p.np;
+    if (h->dp_set != 0.0) d.dp = h->dp_set;
+    else if (d.polar) d.dp = 2.0 * acos(-1.0) / (double)h->p.np;   // velvor2dnewsch3.4.f:124
+    else d.dp = h->p.xx / (double)h->p.np;
     d.dri = 1.0 / d.dr;
     d.dpi = 1.0 / d.dp;
     return GB_OK;
@@ -458,8 +534,16 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     if (!p || !out) { gb_set_error("gb_prb_create: null argument"); return GB_ERR_INVALID; }
     *out = nullptr;
     const int nr = p->nr, np = p->np;
-    const int nlev = prb_mg_levels(nr);
+    const int nlev = prb_mg_levels(nr, p->variant);
     if (nlev_out) *nlev_out = nlev;
+    if (p->variant != GB_PRB_LAYER && p->variant != GB_PRB_ANNULUS) {
+        gb_set_error("gb_prb_create: unknown variant %d", p->variant);
+        return GB_ERR_INVALID;
+    }
+    if (p->variant == GB_PRB_ANNULUS && !(p->r0 > 0.0 && p->rmax > p->r0 && p->Re != 0.0)) {
+        gb_set_error("gb_prb_create: the annulus needs 0 < r0 < rmax and Re != 0 (r0=%g rmax=%g Re=%g)", p->r0, p->rmax, p->Re);
+        return GB_ERR_INVALID;
+    }
     if (nr < 4 || np < 4 || (np & 1) || nlev < 1 || nr > 8192 || np > 65536) {
         gb_set_error("gb_prb_create: unsupported grid nr=%d np=%d (need even nr >= 4 with >= 1 multigrid level, even np >= 4)", nr, np);
         return GB_ERR_INVALID;

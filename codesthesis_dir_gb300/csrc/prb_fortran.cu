@@ -10,10 +10,17 @@
 // the arrays the Fortran routine would have left.
 //
 // COMMON blocks are found through weak references to the gfortran symbols
-// sol1_, sol2_, sol3_, num_, val_ (defined by the Fortran main program), or
-// through gb_prb_bind_common for callers that are not Fortran.  Array bounds
-// are the reference's PARAMETER values kr = 290, kp = 1610 unless
-// gb_prb_bind_bounds or GB300_PRB_KR / GB300_PRB_KP say otherwise.
+// sol1_, sol2_, sol3_, num_, val_, radius_ (defined by the Fortran main
+// program), or through gb_prb_bind_common / gb_prb_bind_radius for callers
+// that are not Fortran.  Array bounds are the reference's PARAMETER values
+// kr = 290, kp = 1610 unless gb_prb_bind_bounds or GB300_PRB_KR /
+// GB300_PRB_KP say otherwise.
+//
+// The same symbols serve the rotating-annulus driver
+// (iarchomedir_groke_storage_users_mpking_rotannconvvelvorplane_continueddir/
+// velvor2dnewsch3.4.f, same subroutine names and COMMON blocks) once
+// gb_prb_bind_variant(GB_PRB_ANNULUS) or GB300_PRB_VARIANT=annulus selects
+// it; its solves then default to tolcon 1e-5 and 10000 sweeps.
 #include <stdlib.h>
 #include <string.h>
 
@@ -28,6 +35,7 @@ extern char sol2_[] __attribute__((weak));
 extern char sol3_[] __attribute__((weak));
 extern char num_[] __attribute__((weak));
 extern char val_[] __attribute__((weak));
+extern char radius_[] __attribute__((weak));
 }
 
 int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out, int *nlev_out);
@@ -47,11 +55,14 @@ struct DropIn {
     gb_prb *ctx = nullptr;
     int kr = 290, kp = 1610;
     int smoother = GB_SMOOTHER_LEX;
+    int variant = GB_PRB_LAYER;
+    bool tol_bound = false;   // gb_prb_bind_tolerance called: keep its values
     double tolcon = 2e-6;
     int maxsweeps = 500;
     double *sol1 = nullptr, *sol2 = nullptr, *sol3 = nullptr;
     NumBlock *num = nullptr;
     ValBlock *val = nullptr;
+    double *radius = nullptr;   // COMMON /radius/ r0, rmax
     int last_status = GB_OK, last_sweeps = 0;
     bool env_read = false;
 };
@@ -63,6 +74,8 @@ DropIn &g()
         d.env_read = true;
         if (const char *s = getenv("GB300_PRB_KR")) d.kr = atoi(s);
         if (const char *s = getenv("GB300_PRB_KP")) d.kp = atoi(s);
+        if (const char *s = getenv("GB300_PRB_VARIANT"))
+            if (strcmp(s, "annulus") == 0 || strcmp(s, "1") == 0) d.variant = GB_PRB_ANNULUS;
     }
     return d;
 }
@@ -72,6 +85,7 @@ double *sol2p() { return g().sol2 ? g().sol2 : (double *)sol2_; }
 double *sol3p() { return g().sol3 ? g().sol3 : (double *)sol3_; }
 NumBlock *nump() { return g().num ? g().num : (NumBlock *)num_; }
 ValBlock *valp() { return g().val ? g().val : (ValBlock *)val_; }
+double *radiusp() { return g().radius ? g().radius : (double *)radius_; }
 
 // Host address of field f inside the COMMON blocks.
 double *common_field(int f)
@@ -98,14 +112,37 @@ int ensure(int nr, int np, double dr, double dp)
         gb_set_error("grid nr=%d np=%d exceeds the COMMON bounds kr=%d kp=%d", nr, np, d.kr, d.kp);
         return GB_ERR_INVALID;
     }
-    if (d.ctx && d.ctx->p.nr == nr && d.ctx->p.np == np && d.ctx->dev.dr == dr && d.ctx->dev.dp == dp) return GB_OK;
+    const bool ann = d.variant == GB_PRB_ANNULUS;
+    double r0 = 0.5, rmax = 1.0, Re = 1.0;
+    if (ann) {
+        // the annulus multigrid coefficients depend on r0 (COMMON /radius/)
+        if (!radiusp()) {
+            gb_set_error("the annulus needs COMMON /radius/ r0,rmax (radius_ or gb_prb_bind_radius)");
+            return GB_ERR_INVALID;
+        }
+        r0 = radiusp()[0];
+        rmax = radiusp()[1];
+        if (valp() && valp()->Re != 0.0) Re = valp()->Re;
+    }
+    if (d.ctx && d.ctx->p.nr == nr && d.ctx->p.np == np && d.ctx->dev.dr == dr && d.ctx->dev.dp == dp &&
+        d.ctx->p.variant == d.variant && (!ann || (d.ctx->p.r0 == r0 && d.ctx->p.rmax == rmax)))
+        return GB_OK;
     if (d.ctx) gb_prb_destroy(d.ctx);
     d.ctx = nullptr;
     gb_prb_params p;
-    gb_prb_default_params(&p, nr, np);
+    if (ann) {
+        gb_prb_default_params_annulus(&p, nr, np);
+        p.r0 = r0;
+        p.rmax = rmax;
+        p.Re = Re;
+    } else {
+        gb_prb_default_params(&p, nr, np);
+    }
     p.smoother = d.smoother;
-    p.tolcon = d.tolcon;
-    p.maxsweeps = d.maxsweeps;
+    if (d.tol_bound) {
+        p.tolcon = d.tolcon;
+        p.maxsweeps = d.maxsweeps;
+    }
     return gb_prb_create_ex(&p, dr, dp, &d.ctx, nullptr);
 }
 
@@ -122,6 +159,11 @@ int ensure_from_common()
     h->p.dt = n->dt;
     h->p.Ra = valp()->Ra;
     h->p.Pr = valp()->Ptl;
+    if (h->p.variant == GB_PRB_ANNULUS) {
+        h->p.Re = valp()->Re;
+        h->p.r0 = radiusp()[0];
+        h->p.rmax = radiusp()[1];
+    }
     return GB_OK;
 }
 
@@ -213,6 +255,7 @@ void gb_prb_bind_smoother(int smoother)
 void gb_prb_bind_tolerance(double tolcon, int maxsweeps)
 {
     std::lock_guard<std::mutex> lk(g().mu);
+    g().tol_bound = true;
     g().tolcon = tolcon;
     g().maxsweeps = maxsweeps;
     if (g().ctx) {
@@ -231,6 +274,18 @@ void gb_prb_bind_common(double *sol1, double *sol2, double *sol3, void *num, dou
     g().val = (ValBlock *)val;
 }
 
+void gb_prb_bind_variant(int variant)
+{
+    std::lock_guard<std::mutex> lk(g().mu);
+    g().variant = variant == GB_PRB_ANNULUS ? GB_PRB_ANNULUS : GB_PRB_LAYER;
+}
+
+void gb_prb_bind_radius(double *radius)
+{
+    std::lock_guard<std::mutex> lk(g().mu);
+    g().radius = radius;
+}
+
 int gb_prb_last_status(void) { return g().last_status; }
 int gb_prb_last_sweeps(void) { return g().last_sweeps; }
 
@@ -239,7 +294,7 @@ void poissoninit_(int *nr, int *nz, int *np, double *dr, double *dz, double *dp,
     (void)nz;
     (void)dz;
     std::lock_guard<std::mutex> lk(g().mu);
-    *nlev = prb_mg_levels(*nr);
+    *nlev = prb_mg_levels(*nr, g().variant);
     int st = ensure(*nr, *np, *dr, *dp);
     fail(st);
 }

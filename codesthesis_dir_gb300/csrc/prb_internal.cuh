@@ -13,15 +13,21 @@
 // velvor2dperiodicrbconv.f:1810-1814, plus the packed v/f slots).
 struct MgLevel {
     int n1, n3;
+    double hr;           // radial spacing of the level
     double hhri, hhpi;   // 1/hr^2, 1/hp^2 of the level
+    double hri;          // 1/hr
     const double *fac;   // factored line matrix (pdma for v, tdma for u)
     double *v, *f;       // packed (n1+1)*(n3+1) solution / right-hand side
+    double *rvi, *rvq;   // annulus: 1/r and 1/r^2 of row i (n1+2 entries)
 };
 
 // Device description of one Poisson solve (poisson2 or poisson3).
 struct MgEq {
     int which;           // 2: v (cell centred, pentadiagonal), 3: u (face, tridiagonal)
     int nr, np, ld, nlev, mode, maxsweeps;
+    int polar;           // annulus operator, three relaxations per visit, seam residual kept
+    int stop_on_max;     // the sweep limit fails the step (PRB's STOP) or only is reported
+    double r0;
     double tolcon, sor;
     MgLevel lev[PRB_MAXLEV];
     double *psic, *psif, *rc, *rf, *tempa;   // COMMON /arrays/ (per equation)
@@ -34,7 +40,9 @@ struct MgEq {
 
 struct PrbDev {
     int nr, np, ld;
+    int polar;           // GB_PRB_ANNULUS
     double dt, Ra, Pr, dr, dp, dri, dpi;
+    double r0, Re;
     double *f[GB_F_COUNT];
     const double *fac_r1, *fac_x, *fac_rT;
     double *heat;
@@ -68,7 +76,7 @@ struct gb_prb {
     int steps_done = 0;
 };
 
-int prb_mg_levels(int nr);
+int prb_mg_levels(int nr, int variant);
 int prb_mg_create(gb_prb *h);
 void prb_mg_destroy(gb_prb *h);
 int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s);

@@ -16,6 +16,14 @@
 // bit-identical to the reference algorithm and ZEBRA results to the same
 // algorithm under zebra ordering.
 //
+// The rotating-annulus variant (E.polar; relax2/relax3/corser of
+// velvor2dnewsch3.4.f:2071-2716) uses the same kernel: its line matrices
+// depend on the radius of row i but not on the line k, so they are still
+// factored once per level; the line right-hand sides and residuals gain the
+// polar terms, every level visit runs three relaxations (:2134, :2410), and
+// the coarse right-hand side of seam line n3c keeps the fine residual stored
+// there because that corser does not clear it (:2696-2704).
+//
 // Storage differs from the reference only in scratch that no output depends
 // on: the right-hand sides are read from the packed per-level arrays instead
 // of being unpacked into rf, and the prolongation reads the coarse solution
@@ -56,9 +64,13 @@ __device__ __forceinline__ void mg_line(const MgEq &E, const MgLevel &L, int k)
     const double *f = L.f;
     const double hhpi = L.hhpi;
     const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
+    const bool polar = E.polar;
+    const double *rvq = L.rvq;
     auto rhs = [&](int j) -> double {
         const int i = j + 1;
-        return -(psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi + f[(size_t)k * (n1 + 1) + i];
+        double t = -(psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi;
+        if (polar) t = t * rvq[i];
+        return t + f[(size_t)k * (n1 + 1) + i];
     };
     const int nrow = (E.which == 2) ? n1 : n1 - 1;
     if (E.which == 2) apply_pdma_rhs(L.fac, n1, psif + GIX(1, k, ld), 1, rhs);
@@ -67,25 +79,31 @@ __device__ __forceinline__ void mg_line(const MgEq &E, const MgLevel &L, int k)
         for (int i = 1; i <= nrow; ++i) psif[GIX(i, 0, ld)] = psif[GIX(i, k, ld)];
 }
 
-// relax2 / relax3 with nrel = 1: line sweep, residual into rc, max norm,
-// pack psif into v.  Returns the level's residual max norm (NaNs ignored as
-// in the reference's comparison); *nan_out (uniform over the block) is set
-// when a NaN residual appears.
+// relax2 / relax3: line sweeps (one with nrel = 1; three in the annulus),
+// then the residual into rc, its max norm, and psif packed into v.  Only
+// the last sweep's residual is formed: the reference recomputes rc and
+// resmax after every sweep and keeps the last.  Returns the level's
+// residual max norm (NaNs ignored as in the reference's comparison);
+// *nan_out (uniform over the block) is set when a NaN residual appears.
 __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
 {
     const MgLevel &L = E.lev[klev];
     const int ld = E.ld, n1 = L.n1, n3 = L.n3;
-    const double hhri = L.hhri, hhpi = L.hhpi;
+    const double hhri = L.hhri, hhpi = L.hhpi, hri = L.hri;
+    const double *rvi = L.rvi, *rvq = L.rvq;
     double *psif = E.psif, *rc = E.rc;
     const double *f = L.f;
-    if (E.mode == GB_SMOOTHER_LEX) {
-        if (threadIdx.x == 0)
-            for (int k = 1; k <= n3; ++k) mg_line(E, L, k);
-        __syncthreads();
-    } else {
-        for (int parity = 1; parity >= 0; --parity) {
-            for (int t = threadIdx.x; t < n3 / 2; t += blockDim.x) mg_line(E, L, 2 * t + 2 - parity);
+    const int nrel = E.polar ? 3 : 1;
+    for (int irel = 0; irel < nrel; ++irel) {
+        if (E.mode == GB_SMOOTHER_LEX) {
+            if (threadIdx.x == 0)
+                for (int k = 1; k <= n3; ++k) mg_line(E, L, k);
             __syncthreads();
+        } else {
+            for (int parity = 1; parity >= 0; --parity) {
+                for (int t = threadIdx.x; t < n3 / 2; t += blockDim.x) mg_line(E, L, 2 * t + 2 - parity);
+                __syncthreads();
+            }
         }
     }
     // residual, PRB:2306-2357 (v) and PRB:2553-2587 (u)
@@ -97,7 +115,29 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
         const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
         const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
         double temp;
-        if (E.which == 2) {
+        if (E.polar && E.which == 2) {
+            // velvor2dnewsch3.4.f:2300-2346
+            temp = (psif[GIX(i, ka, ld)] - 2.0 * psif[GIX(i, k, ld)] + psif[GIX(i, km, ld)]) * hhpi * rvq[i] +
+                   psif[GIX(i, k, ld)] * rvq[i];
+            if (i == 1)
+                temp = temp + (-2.0 * psif[GIX(i, k, ld)] + 5.0 / 3.0 * psif[GIX(i + 1, k, ld)] -
+                               0.2 * psif[GIX(i + 2, k, ld)]) * hhri +
+                       4.0 / 3.0 * psif[GIX(i + 1, k, ld)] * hri * rvi[i];
+            else if (i == n1)
+                temp = temp + (-2.0 * psif[GIX(i, k, ld)] + 5.0 / 3.0 * psif[GIX(i - 1, k, ld)] -
+                               0.2 * psif[GIX(i - 2, k, ld)]) * hhri -
+                       4.0 / 3.0 * psif[GIX(i - 1, k, ld)] * hri * rvi[i];
+            else
+                temp = temp + (psif[GIX(i - 1, k, ld)] - 2.0 * psif[GIX(i, k, ld)] + psif[GIX(i + 1, k, ld)]) * hhri +
+                       1.5 * (psif[GIX(i + 1, k, ld)] - psif[GIX(i - 1, k, ld)]) * hri * rvi[i];
+        } else if (E.polar) {
+            // velvor2dnewsch3.4.f:2546-2579
+            temp = (psif[GIX(i + 1, k, ld)] + psif[GIX(i - 1, k, ld)]) * hhri +
+                   1.5 * (psif[GIX(i + 1, k, ld)] - psif[GIX(i - 1, k, ld)]) * hri * rvi[i] +
+                   psif[GIX(i, k, ld)] * rvq[i] +
+                   (psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi * rvq[i] -
+                   psif[GIX(i, k, ld)] * (2.0 * hhri + 2.0 * hhpi * rvq[i]);
+        } else if (E.which == 2) {
             temp = (psif[GIX(i, ka, ld)] - 2.0 * psif[GIX(i, k, ld)] + psif[GIX(i, km, ld)]) * hhpi;
             if (i == 1)
                 temp = temp + (-2.0 * psif[GIX(i, k, ld)] + 5.0 / 3.0 * psif[GIX(i + 1, k, ld)] -
@@ -177,6 +217,8 @@ __device__ void mg_corser(const MgEq &E, int klev)
             t = t + rf[GIX(iim, kkp, ld)];
             t = t + rf[GIX(iim, kkm, ld)];
             t = t * 0.015625;
+        } else if (E.polar && i >= 1 && i <= n1c - 1) {
+            t = rf[GIX(i, k, ld)];   // seam lines k = 0, n3c keep rc (k = 0 is never written)
         }
         fc[idx] = t;
     }
@@ -302,25 +344,50 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
         E.status[0] = status;
         E.status[1] = sweeps;
         *E.resmax = res1;
-        if (status != GB_OK) *E.abort = 1;
+        if (status == GB_NAN || (status == GB_MAXSWEEPS && E.stop_on_max)) *E.abort = 1;
     }
 }
 
 // Factored line matrices of every level (one thread), the coefficients of
-// relax2 (PRB:2128-2156) and relax3 (PRB:2421-2436).
+// relax2 (PRB:2128-2156) and relax3 (PRB:2421-2436); for the annulus those
+// of velvor2dnewsch3.4.f:2104-2131 and :2401-2408 with the per-row 1/r and
+// 1/r^2 they use.
 __global__ void k_mg_factors(MgEq eq, double *work)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     for (int l = 1; l <= eq.nlev; ++l) {
         const MgLevel &L = eq.lev[l];
         const int n1 = L.n1;
-        const double hhri = L.hhri, hhpi = L.hhpi;
+        const double hhri = L.hhri, hhpi = L.hhpi, hri = L.hri;
         double *a = work, *b = a + n1 + 2, *c = b + n1 + 2, *d = c + n1 + 2, *e = d + n1 + 2, *w = e + n1 + 2;
         double *fac = (double *)L.fac;
+        double *rvi = L.rvi, *rvq = L.rvq;
+        for (int i = 0; i <= n1 + 1; ++i) { rvi[i] = 1.0; rvq[i] = 1.0; }
         if (eq.which == 2) {
             for (int i = 1; i <= n1; ++i) {
                 const int j = i - 1;
-                if (i == 1) {
+                if (eq.polar) {
+                    const double rval = eq.r0 + ((double)i - 0.5) * L.hr;
+                    rvi[i] = 1.0 / rval;
+                    rvq[i] = rvi[i] * rvi[i];
+                    if (i == 1) {
+                        a[j] = 0.0; b[j] = 0.0;
+                        c[j] = -2.0 * hhri - 2.0 * hhpi * rvq[i] + rvq[i];
+                        d[j] = 5.0 / 3.0 * hhri + 4.0 / 3.0 * hri * rvi[i];
+                        e[j] = -0.2 * hhri;
+                    } else if (i == n1) {
+                        a[j] = -0.2 * hhri;
+                        b[j] = 5.0 / 3.0 * hhri - 4.0 / 3.0 * hri * rvi[i];
+                        c[j] = -2.0 * hhri - 2.0 * hhpi * rvq[i] + rvq[i];
+                        d[j] = 0.0; e[j] = 0.0;
+                    } else {
+                        a[j] = 0.0;
+                        b[j] = hhri - 1.5 * hri * rvi[i];
+                        c[j] = -(2.0 * hhri + 2.0 * hhpi * rvq[i]) + rvq[i];
+                        d[j] = hhri + 1.5 * hri * rvi[i];
+                        e[j] = 0.0;
+                    }
+                } else if (i == 1) {
                     a[j] = 0.0; b[j] = 0.0;
                     c[j] = -2.0 * hhri - 2.0 * hhpi;
                     d[j] = 5.0 / 3.0 * hhri;
@@ -339,9 +406,19 @@ __global__ void k_mg_factors(MgEq eq, double *work)
             factor_pdma(a, b, c, d, e, n1, fac, w);
         } else {
             for (int j = 0; j < n1 - 1; ++j) {
-                a[j] = hhri;
-                b[j] = -(2.0 * hhri + 2.0 * hhpi);
-                c[j] = hhri;
+                const int i = j + 1;
+                if (eq.polar) {
+                    const double rval = (double)i * L.hr + eq.r0;
+                    rvi[i] = 1.0 / rval;
+                    rvq[i] = rvi[i] * rvi[i];
+                    a[j] = hhri - 1.5 * hri * rvi[i];
+                    b[j] = -(2.0 * hhri - rvq[i] + 2.0 * hhpi * rvq[i]);
+                    c[j] = hhri + 1.5 * hri * rvi[i];
+                } else {
+                    a[j] = hhri;
+                    b[j] = -(2.0 * hhri + 2.0 * hhpi);
+                    c[j] = hhri;
+                }
             }
             factor_tdma(a, b, c, n1 - 1, fac);
         }
@@ -362,7 +439,7 @@ int prb_mg_create(gb_prb *h)
     size_t per_eq = 2 * (size_t)ld * (np + 1);
     for (int l = 1; l <= nlev; ++l) {
         const int n1 = nr * 2 / (1 << l), n3 = np * 2 / (1 << l);
-        per_eq += 2 * (size_t)(n1 + 1) * (n3 + 1) + 5 * (size_t)(n1 + 2) + 1;
+        per_eq += 2 * (size_t)(n1 + 1) * (n3 + 1) + 5 * (size_t)(n1 + 2) + 1 + 2 * (size_t)(n1 + 2);
     }
     const size_t work = 8 * (size_t)(nr + 2);
     cudaError_t e = cudaMalloc(&h->mg_pool, sizeof(double) * (2 * per_eq + work));
@@ -375,6 +452,9 @@ int prb_mg_create(gb_prb *h)
         E.which = q == 0 ? 2 : 3;
         E.nr = nr; E.np = np; E.ld = ld; E.nlev = nlev;
         E.mode = p.smoother; E.maxsweeps = p.maxsweeps; E.tolcon = p.tolcon; E.sor = p.sor;
+        E.polar = p.variant == GB_PRB_ANNULUS;
+        E.stop_on_max = !E.polar;
+        E.r0 = p.r0;
         double *base = h->mg_pool + q * per_eq;
         E.psif = base; base += (size_t)ld * (np + 1);
         E.rc = base; base += (size_t)ld * (np + 1);
@@ -385,12 +465,16 @@ int prb_mg_create(gb_prb *h)
             L.n3 = np * 2 / (1 << l);
             const double hr = dr * (double)(1 << l) * 0.5;
             const double hp = dp * (double)(1 << l) * 0.5;
+            L.hr = hr;
             L.hhri = 1.0 / (hr * hr);
             L.hhpi = 1.0 / (hp * hp);
+            L.hri = 1.0 / hr;
             const size_t sz = (size_t)(L.n1 + 1) * (L.n3 + 1);
             L.v = base; base += sz;
             L.f = base; base += sz;
             L.fac = base; base += 5 * (size_t)(L.n1 + 2) + 1;
+            L.rvi = base; base += (size_t)(L.n1 + 2);
+            L.rvq = base; base += (size_t)(L.n1 + 2);
         }
         E.psi = h->dev.f[q == 0 ? GB_F_vel : GB_F_uel];
         E.psip = h->dev.f[q == 0 ? GB_F_velp : GB_F_uelp];

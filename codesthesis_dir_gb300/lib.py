@@ -31,6 +31,8 @@ FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
 SMOOTHER_LEX = 0
 SMOOTHER_ZEBRA = 1
+PRB_LAYER = 0
+PRB_ANNULUS = 1
 BATCH_FP64 = 0
 BATCH_MIXED = 1
 BATCH_EXEC_GRAPH = 0
@@ -47,7 +49,7 @@ class PrbParams(C.Structure):
     _fields_ = [("nr", C.c_int), ("np", C.c_int),
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
                 ("Ra", C.c_double), ("Pr", C.c_double), ("tolcon", C.c_double), ("sor", C.c_double),
-                ("maxsweeps", C.c_int), ("smoother", C.c_int)]
+                ("maxsweeps", C.c_int), ("smoother", C.c_int), ("variant", C.c_int), ("Re", C.c_double)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -60,6 +62,7 @@ SIGNATURES = [
     ("gb_last_error", C.c_char_p, []),
     ("gb_version", C.c_char_p, []),
     ("gb_prb_default_params", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
+    ("gb_prb_default_params_annulus", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
     ("gb_prb_create", C.c_int, [C.POINTER(PrbParams), C.POINTER(_vp), _ip]),
     ("gb_prb_destroy", C.c_int, [_vp]),
     ("gb_prb_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
@@ -77,6 +80,8 @@ SIGNATURES = [
     ("gb_prb_bind_smoother", None, [C.c_int]),
     ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),
     ("gb_prb_bind_common", None, [_vp, _vp, _vp, _vp, _vp]),
+    ("gb_prb_bind_variant", None, [C.c_int]),
+    ("gb_prb_bind_radius", None, [_vp]),
     ("gb_prb_last_status", C.c_int, []),
     ("gb_prb_last_sweeps", C.c_int, []),
     ("poissoninit_", None, [_ip, _ip, _ip, _dp, _dp, _dp, _ip]),

@@ -8,8 +8,15 @@ temperature (PRB:1056, 1220), heat (PRB:1452), rhsv/rhsu (PRB:1629, 1679),
 poisson2/poisson3 (PRB:1796, 1930), update (PRB:1557).  Fields move in and
 out as Fortran-ordered (ld, np+1) float64 arrays with ld >= nr+2.
 
+variant=PRB_ANNULUS gives the rotating-annulus (r, phi) plane driver
+(iarchomedir_groke_storage_users_mpking_rotannconvvelvorplane_continueddir/
+velvor2dnewsch3.4.f), whose routines have the same names; tolcon and
+maxsweeps then default to its 1e-5 and 10000.
+
 Error behaviour: where the reference STOPs after 500 multigrid sweeps
-(PRB:1843), poisson2/poisson3 raise GBError with status GB_MAXSWEEPS.
+(PRB:1843), poisson2/poisson3 raise GBError with status GB_MAXSWEEPS.  The
+annulus driver does not stop (velvor2dnewsch3.4.f:1853): its solves return
+the sweep limit with psi untouched and step() carries on.
 """
 from __future__ import annotations
 
@@ -22,12 +29,21 @@ from . import lib as _L
 
 class PRB:
     def __init__(self, nr, np_, dt=1e-7, r0=0.5, rmax=1.0, xx=3.0, Ra=1e7, Pr=0.71,
-                 tolcon=2e-6, sor=1.2, maxsweeps=500, smoother=_L.SMOOTHER_LEX):
+                 tolcon=None, sor=1.2, maxsweeps=None, smoother=_L.SMOOTHER_LEX,
+                 variant=_L.PRB_LAYER, Re=0.0):
         L = _L.load()
         p = _L.PrbParams()
-        L.gb_prb_default_params(C.byref(p), nr, np_)
+        if variant == _L.PRB_ANNULUS:
+            L.gb_prb_default_params_annulus(C.byref(p), nr, np_)
+        else:
+            L.gb_prb_default_params(C.byref(p), nr, np_)
         p.dt, p.r0, p.rmax, p.xx, p.Ra, p.Pr = dt, r0, rmax, xx, Ra, Pr
-        p.tolcon, p.sor, p.maxsweeps, p.smoother = tolcon, sor, maxsweeps, smoother
+        p.sor, p.smoother, p.Re = sor, smoother, Re
+        if tolcon is not None:
+            p.tolcon = tolcon
+        if maxsweeps is not None:
+            p.maxsweeps = maxsweeps
+        self.variant = variant
         self.params = p
         h = C.c_void_p()
         nlev = C.c_int(0)
@@ -81,15 +97,18 @@ class PRB:
     def rhsu(self):
         _L.check(_L.load().gb_prb_rhsu(self._h), "rhsu")
 
-    def poisson2(self):
+    def _poisson(self, which):
         sw = C.c_int()
-        _L.check(_L.load().gb_prb_poisson(self._h, 2, C.byref(sw)), "poisson2")
+        st = _L.load().gb_prb_poisson(self._h, which, C.byref(sw))
+        if not (st == _L.GB_MAXSWEEPS and self.variant == _L.PRB_ANNULUS):
+            _L.check(st, "poisson%d" % which)
         return sw.value
 
+    def poisson2(self):
+        return self._poisson(2)
+
     def poisson3(self):
-        sw = C.c_int()
-        _L.check(_L.load().gb_prb_poisson(self._h, 3, C.byref(sw)), "poisson3")
-        return sw.value
+        return self._poisson(3)
 
     def update(self):
         c = C.c_longlong()

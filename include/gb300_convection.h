@@ -79,18 +79,42 @@ typedef struct gb_prb_params {
     double sor;      /* over-relaxation factor of the whole-cycle change */
     int maxsweeps;   /* outer multigrid sweep limit */
     int smoother;    /* GB_SMOOTHER_LEX or GB_SMOOTHER_ZEBRA */
+    int variant;     /* GB_PRB_LAYER or GB_PRB_ANNULUS */
+    double Re;       /* rotational Reynolds number (COMMON /val/ Re; annulus only) */
 } gb_prb_params;
+
+/* Geometry and physics of an instance.
+ *   GB_PRB_LAYER:   the periodic plane layer of velvor2dperiodicrbconv.f
+ *                   (x period xx, dp = xx/np, Nu = trans*(rmax-r0)/xx).
+ *   GB_PRB_ANNULUS: the (r, phi) plane of the rotating annulus,
+ *                   iarchomedir_groke_storage_users_mpking_rotannconvvelvorplane_continueddir/
+ *                   velvor2dnewsch3.4.f: dp = 2 pi/np, polar terms in the
+ *                   transport (:710-993, :1140-1393), in rhsv/rhsu
+ *                   (:1666-1730) and in relax2/relax3 (:2071-2596), Robert
+ *                   filter 0.05, rotational buoyancy 2 Ra (-thr u - thh v/r)/Re/Ptl
+ *                   (:779), up to 5 multigrid levels (:1778), three
+ *                   relaxations per level visit (:2134, :2410), no reset of
+ *                   the coarse seam residual in corser (:2696-2704), no STOP
+ *                   after the sweep limit (:1853), Nu = -r0 ln(r0/rmax)
+ *                   trans1/(2 pi) (:386-387). */
+#define GB_PRB_LAYER   0
+#define GB_PRB_ANNULUS 1
 
 /* Fills *p with the reference defaults for an nr x np grid
  * (dt 1e-7, r0 0.5, rmax 1, xx 3, Ra 1e7, Pr 0.71: the PRB input deck). */
 void gb_prb_default_params(gb_prb_params *p, int nr, int np);
+/* The annulus defaults (velvor2dnewsch3.4.f with its input.s: dt 2e-8,
+ * r0 0.5, rmax 1, Ra 8e8, Re 1.06148e5, Pr 0.71; tolcon 1e-5 (:2093),
+ * sweep limit 10000 (:1829)). */
+void gb_prb_default_params_annulus(gb_prb_params *p, int nr, int np);
 
 typedef struct gb_prb gb_prb;
 
 /* Creates a device-resident instance on the current CUDA device; every
  * field starts at zero.  Replaces poissoninit (PRB:1724) plus the COMMON
  * storage of the fields.  nlev_out (may be NULL) receives the multigrid
- * level count, computed as poissoninit does (halvings of nr, capped at 4). */
+ * level count, computed as poissoninit does (halvings of nr, capped at 4;
+ * at 5 for the annulus). */
 int gb_prb_create(const gb_prb_params *p, gb_prb **out, int *nlev_out);
 int gb_prb_destroy(gb_prb *h);
 
@@ -136,8 +160,14 @@ void gb_prb_bind_bounds(int kr, int kp);
 /* The smoother used by the drop-in symbols (default LEX, the reference's). */
 void gb_prb_bind_smoother(int smoother);
 /* Tolerance and sweep limit of the drop-in solves (default 2e-6, 500:
- * PRB:2086, PRB:1843). */
+ * PRB:2086, PRB:1843; for the annulus 1e-5, 10000). */
 void gb_prb_bind_tolerance(double tolcon, int maxsweeps);
+/* Which driver the drop-in symbols serve: GB_PRB_LAYER (default) or
+ * GB_PRB_ANNULUS (also selected by GB300_PRB_VARIANT=annulus).  The annulus
+ * routines read r0 from COMMON /radius/ r0,rmax (weak reference radius_, or
+ * gb_prb_bind_radius) and Re from /val/. */
+void gb_prb_bind_variant(int variant);
+void gb_prb_bind_radius(double *radius);
 /* Explicit COMMON storage for callers that are not a Fortran main program:
  * sol1 = 9 arrays An..Cp, sol2 = thn,th,thp, sol3 = uel..welp, each
  * (kr+1)*(kp+1) doubles; num = {double dt,dr,dz,dp; int nr,nz,np};

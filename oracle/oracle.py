@@ -8,6 +8,7 @@ ships no outputs to compare against.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -18,6 +19,8 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 ORC_LEX = 0
 ORC_ZEBRA = 1
+ORC_PRB = 0
+ORC_ANNULUS = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -41,6 +44,7 @@ class MG(C.Structure):
         ("mgen", C.c_long),
         ("scratch_v", _dp), ("scratch_f", _dp),
         ("last_sweeps", C.c_int), ("last_resmax", C.c_double),
+        ("variant", C.c_int), ("r0", C.c_double),
     ]
 
 
@@ -52,7 +56,7 @@ class PRB(C.Structure):
     _fields_ = ([("nr", C.c_int), ("np", C.c_int), ("ld", C.c_int)] +
                 [(n, C.c_double) for n in ("dt", "dr", "dp", "Ra", "Pr", "r0", "rmax", "xx")] +
                 [(n, _dp) for n in _PRB_FIELDS] +
-                [("clamp_count", C.c_long)])
+                [("clamp_count", C.c_long), ("variant", C.c_int), ("Re", C.c_double)])
 
 
 _lib = None
@@ -69,6 +73,9 @@ def lib():
         L.orc_pdma.argtypes = [_dp] * 7 + [C.c_int]
         L.orc_mg_init.argtypes = [C.POINTER(MG), C.c_int, C.c_int, C.c_double, C.c_double]
         L.orc_mg_init.restype = C.c_int
+        L.orc_mg_init_variant.argtypes = [C.POINTER(MG), C.c_int, C.c_int, C.c_double, C.c_double,
+                                          C.c_int, C.c_double]
+        L.orc_mg_init_variant.restype = C.c_int
         L.orc_mg_free.argtypes = [C.POINTER(MG)]
         L.orc_poisson.argtypes = [C.POINTER(MG), C.c_int, _dp, _dp, _dp, C.c_int, _ip]
         L.orc_poisson.restype = C.c_int
@@ -137,25 +144,32 @@ def pdma(a, b, c, d, e, r):
 # PRB state
 # --------------------------------------------------------------------------
 class OraclePRB:
-    """The PRB physical state plus the two multigrid contexts (v and u)."""
+    """The PRB physical state plus the two multigrid contexts (v and u).
+
+    variant ORC_PRB is the periodic plane layer (dp = xx/np); ORC_ANNULUS the
+    rotating annulus (dp = 2 pi/np, rotational Reynolds number Re).  tolcon
+    and maxsweeps default to each driver's own values."""
 
     def __init__(self, nr, np_, dt, Ra, Pr, r0=0.5, rmax=1.0, xx=3.0, mode=ORC_LEX,
-                 tolcon=2e-6, maxsweeps=500, sor=1.2):
+                 tolcon=None, maxsweeps=None, sor=1.2, variant=ORC_PRB, Re=0.0):
         L = lib()
         self.s = PRB()
         assert L.orc_prb_alloc(C.byref(self.s), nr, np_, nr + 2) == 0
         s = self.s
         s.dt, s.Ra, s.Pr, s.r0, s.rmax, s.xx = dt, Ra, Pr, r0, rmax, xx
+        s.variant, s.Re = variant, Re
         s.dr = (rmax - r0) / nr
-        s.dp = xx / np_
+        s.dp = 2.0 * math.acos(-1.0) / np_ if variant == ORC_ANNULUS else xx / np_
         self.mgv, self.mgu = MG(), MG()
         for mg in (self.mgv, self.mgu):
-            st = L.orc_mg_init(C.byref(mg), nr, np_, s.dr, s.dp)
+            st = L.orc_mg_init_variant(C.byref(mg), nr, np_, s.dr, s.dp, variant, r0)
             if st != 0:
                 raise ValueError("invalid multigrid size nr=%d np=%d" % (nr, np_))
             mg.mode = mode
-            mg.tolcon = tolcon
-            mg.maxsweeps = maxsweeps
+            if tolcon is not None:
+                mg.tolcon = tolcon
+            if maxsweeps is not None:
+                mg.maxsweeps = maxsweeps
             mg.sor = sor
         self.kt = 0
 
@@ -199,13 +213,18 @@ class OraclePRB:
             pass
 
 
-def poisson(which, psi, psip, rhs, nr, np_, dr, dp, mode=ORC_LEX, tolcon=2e-6, maxsweeps=500):
+def poisson(which, psi, psip, rhs, nr, np_, dr, dp, mode=ORC_LEX, tolcon=None, maxsweeps=None,
+            variant=ORC_PRB, r0=0.0):
     """Run one orc_poisson call on (nr+2, np+1) Fortran-ordered arrays; returns
     (status, sweeps).  psi and psip are updated in place."""
     L = lib()
     mg = MG()
-    assert L.orc_mg_init(C.byref(mg), nr, np_, dr, dp) == 0
-    mg.mode, mg.tolcon, mg.maxsweeps = mode, tolcon, maxsweeps
+    assert L.orc_mg_init_variant(C.byref(mg), nr, np_, dr, dp, variant, r0) == 0
+    mg.mode = mode
+    if tolcon is not None:
+        mg.tolcon = tolcon
+    if maxsweeps is not None:
+        mg.maxsweeps = maxsweeps
     sw = C.c_int(0)
     for a in (psi, psip, rhs):
         assert a.flags["F_CONTIGUOUS"] and a.shape[0] == nr + 2

@@ -105,6 +105,15 @@ void orc_pdma(double *a, double *b, double *c, double *d, double *e,
  * at 4; np only follows (n3 = np*2/2^l, integer division). */
 int orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp)
 {
+    return orc_mg_init_variant(mg, nr, np, dr, dp, ORC_PRB, 0.0);
+}
+
+/* The annulus driver's poissoninit (velvor2dnewsch3.4.f:1736-1806) differs
+ * only in the cap of 5 levels (:1778); its relax2/relax3 set tolcon = 10e-6
+ * (:2093, :2389) and its poisson2/poisson3 run up to nvs = 10000 sweeps and
+ * then return without a STOP (:1829, :1960). */
+int orc_mg_init_variant(orc_mg_t *mg, int nr, int np, double dr, double dp, int variant, double r0)
+{
     memset(mg, 0, sizeof(*mg));
     int nlev = 0, itest = nr, itest2 = nr;
     for (int i = 2; i <= 8; ++i) {
@@ -116,7 +125,11 @@ int orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp)
             break;
         }
     }
-    if (nlev >= 5) nlev = 4;
+    if (variant == ORC_ANNULUS) {
+        if (nlev > 5) nlev = 5;
+    } else if (nlev >= 5) {
+        nlev = 4;
+    }
     if (nlev < 1 || np < 4) return ORC_INVALID;
     mg->nr = nr;
     mg->np = np;
@@ -145,6 +158,13 @@ int orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp)
     mg->mode = ORC_LEX;
     mg->zero_scratch = 0;
     mg->mgen = 650000;
+    mg->variant = variant;
+    mg->r0 = r0;
+    if (variant == ORC_ANNULUS) {
+        mg->tolcon = 10.0e-6;
+        mg->maxsweeps = 10000;
+        mg->mgen = 2000000;
+    }
     return ORC_OK;
 }
 
@@ -176,16 +196,16 @@ static void trans2(const orc_mg_t *mg, const double *a1, double *a2, int l)
             a2[IX(i, k)] = a1[(size_t)k * (n1 + 1) + i];
 }
 
-/* Line k of the cell-centred (v) relaxation, PRB:2113-2191. */
+/* Line k of the cell-centred (v) relaxation, PRB:2113-2191 (annulus:
+ * velvor2dnewsch3.4.f:2140-2182).  rvq[i] = 1/r^2 of row i (1 in PRB). */
 static void relax2_line(orc_mg_t *mg, int klev, int k, const double *ca,
                         const double *cb, const double *cc, const double *cd,
-                        const double *ce, double hhpi, double *wa, double *wb,
-                        double *wc, double *wd, double *we, double *wr, double *ws)
+                        const double *ce, const double *rvq, double hhpi, double *wa,
+                        double *wb, double *wc, double *wd, double *we, double *wr, double *ws)
 {
     const int ld = mg->ld, n1 = mg->n1[klev], n3 = mg->n3[klev];
     double *psif = mg->psif;
     const double *rf = mg->rf;
-    const double rvalisq = 1.0;
     int ka = k + 1, km = k - 1;
     if (k == n3) ka = 1;
     for (int i = 1; i <= n1; ++i) {
@@ -194,7 +214,7 @@ static void relax2_line(orc_mg_t *mg, int klev, int k, const double *ca,
         wc[i - 1] = cc[i];
         wd[i - 1] = cd[i];
         we[i - 1] = ce[i];
-        wr[i - 1] = -(psif[IX(i, ka)] + psif[IX(i, km)]) * hhpi * rvalisq + rf[IX(i, k)];
+        wr[i - 1] = -(psif[IX(i, ka)] + psif[IX(i, km)]) * hhpi * rvq[i] + rf[IX(i, k)];
     }
     orc_pdma(wa, wb, wc, wd, we, wr, ws, n1);
     for (int i = 1; i <= n1; ++i) {
@@ -203,21 +223,22 @@ static void relax2_line(orc_mg_t *mg, int klev, int k, const double *ca,
     }
 }
 
-/* Line k of the face (u) relaxation, PRB:2414-2460. */
-static void relax3_line(orc_mg_t *mg, int klev, int k, double hhri, double hhpi,
+/* Line k of the face (u) relaxation, PRB:2414-2460 (annulus:
+ * velvor2dnewsch3.4.f:2415-2452). */
+static void relax3_line(orc_mg_t *mg, int klev, int k, const double *ca,
+                        const double *cb, const double *cc, const double *rvq, double hhpi,
                         double *wa, double *wb, double *wc, double *wr, double *ws)
 {
     const int ld = mg->ld, n1 = mg->n1[klev], n3 = mg->n3[klev];
     double *psif = mg->psif;
     const double *rf = mg->rf;
-    const double rvalisq = 1.0;
     int ka = k + 1, km = k - 1;
     if (k == n3) ka = 1;
     for (int i = 1; i <= n1 - 1; ++i) {
-        wa[i - 1] = hhri;
-        wb[i - 1] = -(2.0 * hhri + 2.0 * hhpi * rvalisq);
-        wc[i - 1] = hhri;
-        wr[i - 1] = -(psif[IX(i, ka)] + psif[IX(i, km)]) * hhpi * rvalisq + rf[IX(i, k)];
+        wa[i - 1] = ca[i];
+        wb[i - 1] = cb[i];
+        wc[i - 1] = cc[i];
+        wr[i - 1] = -(psif[IX(i, ka)] + psif[IX(i, km)]) * hhpi * rvq[i] + rf[IX(i, k)];
     }
     orc_tdma(wa, wb, wc, ws, wr, n1 - 1);
     for (int i = 1; i <= n1 - 1; ++i) {
@@ -228,44 +249,94 @@ static void relax3_line(orc_mg_t *mg, int klev, int k, double hhri, double hhpi,
 
 /* relax2 (PRB:2063-2371) for which == 2, relax3 (PRB:2374-2600) for which == 3.
  * nconv is set when klev == 1 and the max-norm residual is below tolcon.
- * A NaN residual sets mg->last_resmax to NaN (the reference's max ignores it). */
+ * A NaN residual sets mg->last_resmax to NaN (the reference's max ignores it).
+ *
+ * ORC_ANNULUS follows relax2/relax3 of velvor2dnewsch3.4.f:2071-2596: the
+ * polar operator d2/dr2 + (1/r) d/dr + (1/r^2) d2/dphi2 with the extra 1/r^2
+ * diagonal term of the staggered velocity components, radii r = r0 +
+ * (i-1/2) hr (v) and r = i hr + r0 (u) of the level, and three relaxations
+ * per call whatever nrel says (:2134, :2410). */
 void orc_relax(orc_mg_t *mg, int which, int nrel, int klev, int *nconv)
 {
     const int ld = mg->ld, n1 = mg->n1[klev], n3 = mg->n3[klev];
+    const int polar = (mg->variant == ORC_ANNULUS);
     double *psif = mg->psif, *rc = mg->rc, *rf = mg->rf;
-    const double rvalisq = 1.0;
     *nconv = 0;
     trans2(mg, mg->f[klev], rf, klev);
     const double hhri = 1.0 / mg->hhr[klev];
+    const double hri = 1.0 / mg->hr[klev];
     const double hhpi = 1.0 / mg->hhp[klev];
+    if (polar) nrel = 3;
 
     const int nmax = n1 + 2;
-    double *buf = (double *)malloc(sizeof(double) * (size_t)nmax * 12);
+    double *buf = (double *)malloc(sizeof(double) * (size_t)nmax * 14);
     double *ca = buf, *cb = ca + nmax, *cc = cb + nmax, *cd = cc + nmax, *ce = cd + nmax;
     double *wa = ce + nmax, *wb = wa + nmax, *wc = wb + nmax, *wd = wc + nmax;
     double *we = wd + nmax, *wr = we + nmax, *ws = wr + nmax;
+    double *rvi = ws + nmax, *rvq = rvi + nmax;
 
+    for (int i = 0; i < nmax; ++i) { rvi[i] = 1.0; rvq[i] = 1.0; }
     if (which == 2) {
-        /* coefficients, PRB:2128-2156 (computed at k == 1, reused for every line) */
+        /* coefficients, PRB:2128-2156 (computed at k == 1, reused for every
+         * line); annulus velvor2dnewsch3.4.f:2104-2131 */
         for (int i = 1; i <= n1; ++i) {
-            if (i == 1) {
+            if (polar) {
+                const double rval = mg->r0 + ((double)i - 0.5) * mg->hr[klev];
+                rvi[i] = 1.0 / rval;
+                rvq[i] = rvi[i] * rvi[i];
+                if (i == 1) {
+                    ca[i] = 0.0;
+                    cb[i] = 0.0;
+                    cc[i] = -2.0 * hhri - 2.0 * hhpi * rvq[i] + rvq[i];
+                    cd[i] = 5.0 / 3.0 * hhri + 4.0 / 3.0 * hri * rvi[i];
+                    ce[i] = -0.2 * hhri;
+                } else if (i == n1) {
+                    ca[i] = -0.2 * hhri;
+                    cb[i] = 5.0 / 3.0 * hhri - 4.0 / 3.0 * hri * rvi[i];
+                    cc[i] = -2.0 * hhri - 2.0 * hhpi * rvq[i] + rvq[i];
+                    cd[i] = 0.0;
+                    ce[i] = 0.0;
+                } else {
+                    ca[i] = 0.0;
+                    cb[i] = hhri - 1.5 * hri * rvi[i];
+                    cc[i] = -(2.0 * hhri + 2.0 * hhpi * rvq[i]) + rvq[i];
+                    cd[i] = hhri + 1.5 * hri * rvi[i];
+                    ce[i] = 0.0;
+                }
+            } else if (i == 1) {
                 ca[i] = 0.0;
                 cb[i] = 0.0;
-                cc[i] = -2.0 * hhri - 2.0 * hhpi * rvalisq;
+                cc[i] = -2.0 * hhri - 2.0 * hhpi * rvq[i];
                 cd[i] = 5.0 / 3.0 * hhri;
                 ce[i] = -0.2 * hhri;
             } else if (i == n1) {
                 ca[i] = -0.2 * hhri;
                 cb[i] = 5.0 / 3.0 * hhri;
-                cc[i] = -2.0 * hhri - 2.0 * hhpi * rvalisq;
+                cc[i] = -2.0 * hhri - 2.0 * hhpi * rvq[i];
                 cd[i] = 0.0;
                 ce[i] = 0.0;
             } else {
                 ca[i] = 0.0;
                 cb[i] = hhri;
-                cc[i] = -(2.0 * hhri + 2.0 * hhpi * rvalisq);
+                cc[i] = -(2.0 * hhri + 2.0 * hhpi * rvq[i]);
                 cd[i] = hhri;
                 ce[i] = 0.0;
+            }
+        }
+    } else {
+        /* PRB:2421-2436; annulus velvor2dnewsch3.4.f:2401-2408 */
+        for (int i = 1; i <= n1 - 1; ++i) {
+            if (polar) {
+                const double rval = (double)i * mg->hr[klev] + mg->r0;
+                rvi[i] = 1.0 / rval;
+                rvq[i] = rvi[i] * rvi[i];
+                ca[i] = hhri - 1.5 * hri * rvi[i];
+                cb[i] = -(2.0 * hhri - rvq[i] + 2.0 * hhpi * rvq[i]);
+                cc[i] = hhri + 1.5 * hri * rvi[i];
+            } else {
+                ca[i] = hhri;
+                cb[i] = -(2.0 * hhri + 2.0 * hhpi * rvq[i]);
+                cc[i] = hhri;
             }
         }
     }
@@ -275,34 +346,52 @@ void orc_relax(orc_mg_t *mg, int which, int nrel, int klev, int *nconv)
     for (int irel = 1; irel <= nrel; ++irel) {
         if (mg->mode == ORC_LEX) {
             for (int k = 1; k <= n3; ++k) {
-                if (which == 2) relax2_line(mg, klev, k, ca, cb, cc, cd, ce, hhpi, wa, wb, wc, wd, we, wr, ws);
-                else relax3_line(mg, klev, k, hhri, hhpi, wa, wb, wc, wr, ws);
+                if (which == 2) relax2_line(mg, klev, k, ca, cb, cc, cd, ce, rvq, hhpi, wa, wb, wc, wd, we, wr, ws);
+                else relax3_line(mg, klev, k, ca, cb, cc, rvq, hhpi, wa, wb, wc, wr, ws);
             }
         } else {
             for (int parity = 1; parity >= 0; --parity) {
                 for (int k = 1; k <= n3; ++k) {
                     if ((k & 1) != parity) continue;
-                    if (which == 2) relax2_line(mg, klev, k, ca, cb, cc, cd, ce, hhpi, wa, wb, wc, wd, we, wr, ws);
-                    else relax3_line(mg, klev, k, hhri, hhpi, wa, wb, wc, wr, ws);
+                    if (which == 2) relax2_line(mg, klev, k, ca, cb, cc, cd, ce, rvq, hhpi, wa, wb, wc, wd, we, wr, ws);
+                    else relax3_line(mg, klev, k, ca, cb, cc, rvq, hhpi, wa, wb, wc, wr, ws);
                 }
             }
         }
-        /* residual and its max norm, PRB:2306-2357 / PRB:2553-2587 */
+        /* residual and its max norm, PRB:2306-2357 / PRB:2553-2587
+         * (annulus velvor2dnewsch3.4.f:2300-2346 / :2546-2579) */
         resmax = 0.0;
         for (int k = 1; k <= n3; ++k) {
             int ka = k + 1, km = k - 1;
             if (k == n3) ka = 1;
             if (which == 2) {
                 for (int i = 1; i <= n1; ++i) {
-                    double temp = (psif[IX(i, ka)] - 2.0 * psif[IX(i, k)] + psif[IX(i, km)]) * hhpi * rvalisq;
-                    if (i == 1)
-                        temp = temp + (-2.0 * psif[IX(i, k)] + 5.0 / 3.0 * psif[IX(i + 1, k)] -
-                                       0.2 * psif[IX(i + 2, k)]) * hhri;
-                    else if (i == n1)
-                        temp = temp + (-2.0 * psif[IX(i, k)] + 5.0 / 3.0 * psif[IX(i - 1, k)] -
-                                       0.2 * psif[IX(i - 2, k)]) * hhri;
-                    else
-                        temp = temp + (psif[IX(i - 1, k)] - 2.0 * psif[IX(i, k)] + psif[IX(i + 1, k)]) * hhri;
+                    double temp;
+                    if (polar) {
+                        temp = (psif[IX(i, ka)] - 2.0 * psif[IX(i, k)] + psif[IX(i, km)]) * hhpi * rvq[i] +
+                               psif[IX(i, k)] * rvq[i];
+                        if (i == 1)
+                            temp = temp + (-2.0 * psif[IX(i, k)] + 5.0 / 3.0 * psif[IX(i + 1, k)] -
+                                           0.2 * psif[IX(i + 2, k)]) * hhri +
+                                   4.0 / 3.0 * psif[IX(i + 1, k)] * hri * rvi[i];
+                        else if (i == n1)
+                            temp = temp + (-2.0 * psif[IX(i, k)] + 5.0 / 3.0 * psif[IX(i - 1, k)] -
+                                           0.2 * psif[IX(i - 2, k)]) * hhri -
+                                   4.0 / 3.0 * psif[IX(i - 1, k)] * hri * rvi[i];
+                        else
+                            temp = temp + (psif[IX(i - 1, k)] - 2.0 * psif[IX(i, k)] + psif[IX(i + 1, k)]) * hhri +
+                                   1.5 * (psif[IX(i + 1, k)] - psif[IX(i - 1, k)]) * hri * rvi[i];
+                    } else {
+                        temp = (psif[IX(i, ka)] - 2.0 * psif[IX(i, k)] + psif[IX(i, km)]) * hhpi * rvq[i];
+                        if (i == 1)
+                            temp = temp + (-2.0 * psif[IX(i, k)] + 5.0 / 3.0 * psif[IX(i + 1, k)] -
+                                           0.2 * psif[IX(i + 2, k)]) * hhri;
+                        else if (i == n1)
+                            temp = temp + (-2.0 * psif[IX(i, k)] + 5.0 / 3.0 * psif[IX(i - 1, k)] -
+                                           0.2 * psif[IX(i - 2, k)]) * hhri;
+                        else
+                            temp = temp + (psif[IX(i - 1, k)] - 2.0 * psif[IX(i, k)] + psif[IX(i + 1, k)]) * hhri;
+                    }
                     temp = rf[IX(i, k)] - temp;
                     rc[IX(i, k)] = temp;
                     temp = fabs(temp);
@@ -311,9 +400,17 @@ void orc_relax(orc_mg_t *mg, int which, int nrel, int klev, int *nconv)
                 }
             } else {
                 for (int i = 1; i <= n1 - 1; ++i) {
-                    double temp = (psif[IX(i + 1, k)] + psif[IX(i - 1, k)]) * hhri +
-                                  (psif[IX(i, ka)] + psif[IX(i, km)]) * hhpi * rvalisq -
-                                  psif[IX(i, k)] * (2.0 * hhri + 2.0 * hhpi * rvalisq);
+                    double temp;
+                    if (polar)
+                        temp = (psif[IX(i + 1, k)] + psif[IX(i - 1, k)]) * hhri +
+                               1.5 * (psif[IX(i + 1, k)] - psif[IX(i - 1, k)]) * hri * rvi[i] +
+                               psif[IX(i, k)] * rvq[i] +
+                               (psif[IX(i, ka)] + psif[IX(i, km)]) * hhpi * rvq[i] -
+                               psif[IX(i, k)] * (2.0 * hhri + 2.0 * hhpi * rvq[i]);
+                    else
+                        temp = (psif[IX(i + 1, k)] + psif[IX(i - 1, k)]) * hhri +
+                               (psif[IX(i, ka)] + psif[IX(i, km)]) * hhpi * rvq[i] -
+                               psif[IX(i, k)] * (2.0 * hhri + 2.0 * hhpi * rvq[i]);
                     temp = rf[IX(i, k)] - temp;
                     rc[IX(i, k)] = temp;
                     temp = fabs(temp);
@@ -389,8 +486,13 @@ void orc_corser(orc_mg_t *mg, int klev)
         psif[IX(n1c, k)] = 0.0;
     }
     for (int i = 0; i <= n1c; ++i) {
-        rc[IX(i, 0)] = 0.0;
-        rc[IX(i, n3c)] = 0.0;
+        /* The annulus corser (velvor2dnewsch3.4.f:2696-2704) leaves rc on the
+         * seam lines k = 0 and k = n3c alone, so the coarse right-hand side of
+         * line n3c keeps the fine residual stored there. */
+        if (mg->variant != ORC_ANNULUS) {
+            rc[IX(i, 0)] = 0.0;
+            rc[IX(i, n3c)] = 0.0;
+        }
         psic[IX(i, 0)] = 0.0;
         psic[IX(i, n3c)] = 0.0;
         psif[IX(i, 0)] = 0.0;
@@ -632,12 +734,18 @@ static void cvort_derivatives(orc_prb_t *s, double *wa, double *wb, double *wc,
 
 /* Dufort-Frankel / leapfrog vorticity update, PRB:900-982 (first == 0) and
  * the forward first step, PRB:706-776 (first == 1).  The leapfrog RHS1 uses
- * C, not Cp (PRB:971), as the reference does. */
+ * C, not Cp (PRB:971), as the reference does.
+ *
+ * ORC_ANNULUS (velvor2dnewsch3.4.f:710-786, :911-993): radius r = r0 + i dr
+ * of the C points, the (1/r) dC/dr term Cra*ri in RHS1, 0.5*Cp (not C) in
+ * the leapfrog RHS1, and the rotational buoyancy term
+ * 2 Ra (-thr u - thh v / r) / Re / Ptl in RHS2. */
 static void cvort_update(orc_prb_t *s, int first)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
+    const int polar = (s->variant == ORC_ANNULUS);
     const double dri = 1.0 / s->dr, dpi = 1.0 / s->dp;
-    const double Ptl = s->Pr, dt = s->dt, Ra = s->Ra;
+    const double Ptl = s->Pr, dt = s->dt, Ra = s->Ra, Re = s->Re;
     const double *C = s->C, *Cp = s->Cp, *uel = s->uel, *vel = s->vel;
     for (int i = 1; i <= nr - 1; ++i) {
         for (int k = 0; k <= np; ++k) {
@@ -645,32 +753,49 @@ static void cvort_update(orc_prb_t *s, int first)
             int km = k - 1, ka = k + 1;
             if (k == 0) km = np - 1;
             if (k == np) ka = 1;
-            const double r = 1.0, ri = 1.0 / r;
+            const double r = polar ? s->r0 + (double)i * s->dr : 1.0, ri = 1.0 / r;
             const double u = (uel[IX(i, ka)] + uel[IX(i, k)]) * 0.5;
             const double v = (vel[IX(i, k)] + vel[IX(ip, k)]) * 0.5;
+            const double thr = s->An[IX(i, k)];
             const double Chha = (C[IX(i, ka)] + C[IX(i, km)]) * (dpi * dpi);
             const double Ch = s->B[IX(i, k)];
             const double Crra = (C[IX(i - 1, k)] + C[IX(i + 1, k)]) * (dri * dri);
             const double cnr = -1.0 * (dri * dri);
+            const double Cra = (C[IX(i + 1, k)] - C[IX(i - 1, k)]) * 0.5 * dri;
             const double Cr = s->A[IX(i, k)];
             const double thh = s->Bn[IX(i, k)];
             const double cnh = (-1.0 * (dpi * dpi)) * (ri * ri);
-            double RHS1, cf1;
-            if (first) {
-                RHS1 = Crra + Chha * (ri * ri) + C[IX(i, k)] / (Ptl * dt);
-                cf1 = 1.0 / (Ptl * dt) - cnr - cnh;
+            double RHS1, RHS2, cf1;
+            if (polar) {
+                if (first) {
+                    RHS1 = Crra + Cra * ri + Chha * (ri * ri) + C[IX(i, k)] / (Ptl * dt);
+                    cf1 = 1.0 / (Ptl * dt) - cnr - cnh;
+                } else {
+                    RHS1 = Crra + Cra * ri + Chha * (ri * ri) + 0.5 * Cp[IX(i, k)] / (Ptl * dt);
+                    cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
+                }
+                RHS2 = -Ra * thh + 2.0 * Ra * (-thr * u - thh * v * ri) / Re / Ptl;
             } else {
-                RHS1 = Crra + Chha * (ri * ri) + 0.5 * C[IX(i, k)] / (Ptl * dt);
-                cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
+                if (first) {
+                    RHS1 = Crra + Chha * (ri * ri) + C[IX(i, k)] / (Ptl * dt);
+                    cf1 = 1.0 / (Ptl * dt) - cnr - cnh;
+                } else {
+                    RHS1 = Crra + Chha * (ri * ri) + 0.5 * C[IX(i, k)] / (Ptl * dt);
+                    cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
+                }
+                RHS2 = -Ra * thh;
             }
             const double ULT = (u * Cr + v * Ch * ri) / Ptl;
-            const double RHS2 = -Ra * thh;
             const double cf2 = cnr + cnh;
             s->Cn[IX(i, k)] = (cf2 * Cp[IX(i, k)] - ULT - RHS2 + RHS1) / cf1;
             if (!first) s->Ap[IX(i, k)] = s->Cn[IX(i, k)];
         }
     }
 }
+
+/* Robert filter coefficient: 0.02 in PRB (PRB:1041-1045), 0.05 in the
+ * annulus driver (velvor2dnewsch3.4.f:1055, :1454). */
+static double robert(const orc_prb_t *s) { return s->variant == ORC_ANNULUS ? 0.05 : 0.02; }
 
 static void *wbuf(int n, double **wa, double **wb, double **wc, double **wr, double **ws)
 {
@@ -700,7 +825,7 @@ void orc_cvorticity(orc_prb_t *s)
     cvort_update(s, 0);
     for (int i = 1; i <= nr - 1; ++i)
         for (int k = 0; k <= np; ++k)
-            s->C[IX(i, k)] = s->C[IX(i, k)] + 0.02 * (s->Cn[IX(i, k)] - 2.0 * s->C[IX(i, k)] + s->Cp[IX(i, k)]);
+            s->C[IX(i, k)] = s->C[IX(i, k)] + robert(s) * (s->Cn[IX(i, k)] - 2.0 * s->C[IX(i, k)] + s->Cp[IX(i, k)]);
     free(b);
 }
 
@@ -745,10 +870,13 @@ static void temp_derivatives(orc_prb_t *s, double *wa, double *wb, double *wc,
 }
 
 /* Temperature update, PRB:1292-1377 (first == 1, forward step) and
- * PRB:1292-1377 of `temperature` (first == 0, Dufort-Frankel). */
+ * PRB:1292-1377 of `temperature` (first == 0, Dufort-Frankel).
+ * ORC_ANNULUS (velvor2dnewsch3.4.f:1140-1223, :1308-1393): cell-centre
+ * radius r = r0 + (i-1/2) dr and the (1/r) dT/dr term thra*ri in RHS1. */
 static void temp_update(orc_prb_t *s, int first)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
+    const int polar = (s->variant == ORC_ANNULUS);
     const double dri = 1.0 / s->dr, dpi = 1.0 / s->dp, dt = s->dt;
     const double *th = s->th, *thp = s->thp, *uel = s->uel, *vel = s->vel;
     for (int i = 1; i <= nr; ++i) {
@@ -757,26 +885,37 @@ static void temp_update(orc_prb_t *s, int first)
             int km = k - 1, ka = k + 1;
             if (k == 0) km = np - 1;
             if (k == np) ka = 1;
-            const double r = 1.0, ri = 1.0 / r;
+            const double r = polar ? s->r0 + ((double)i - 0.5) * s->dr : 1.0, ri = 1.0 / r;
             const double u = (uel[IX(i, k)] + uel[IX(im, k)]) * 0.5;
             const double v = (vel[IX(i, k)] + vel[IX(i, km)]) * 0.5;
-            double thrra, cnr;
+            double thrra, thra, cnr;
             const double thr = s->A[IX(i, k)];
             if (i == 1) {
                 thrra = (3.2 * th[IX(i - 1, k)] + 2.0 * th[IX(i + 1, k)] - 0.2 * th[IX(i + 2, k)]) * (dri * dri);
+                thra = (-4.0 * th[IX(i - 1, k)] / 3.0 + th[IX(i + 1, k)] / 3.0) * dri;
                 cnr = -2.5 * (dri * dri) + 0.5 * dri * ri;
             } else if (i == nr) {
                 thrra = (3.2 * th[IX(i + 1, k)] + 2.0 * th[IX(i - 1, k)] - 0.2 * th[IX(i - 2, k)]) * (dri * dri);
+                thra = (-th[IX(i - 1, k)] / 3.0 + 4.0 * th[IX(i + 1, k)] / 3.0) * dri;
                 cnr = -2.5 * (dri * dri) - 0.5 * dri * ri;
             } else {
                 thrra = (th[IX(i - 1, k)] + th[IX(i + 1, k)]) * (dri * dri);
+                thra = (th[IX(i + 1, k)] - th[IX(i - 1, k)]) * 0.5 * dri;
                 cnr = -1.0 * (dri * dri);
             }
             const double thhha = (th[IX(i, ka)] + th[IX(i, km)]) * (dpi * dpi);
             const double thh = s->B[IX(i, k)];
             const double cnp = -(1.0 * (dpi * dpi)) * (ri * ri);
             double RHS1, cf1;
-            if (first) {
+            if (polar) {
+                if (first) {
+                    RHS1 = thrra + thra * ri + thhha * (ri * ri) + th[IX(i, k)] / dt;
+                    cf1 = 1.0 / dt - cnr - cnp;
+                } else {
+                    RHS1 = thrra + thra * ri + thhha * (ri * ri) + 0.5 * thp[IX(i, k)] / dt;
+                    cf1 = 0.5 / dt - cnr - cnp;
+                }
+            } else if (first) {
                 RHS1 = thrra + thhha * (ri * ri) + th[IX(i, k)] / dt;
                 cf1 = 1.0 / dt - cnr - cnp;
             } else {
@@ -811,7 +950,7 @@ void orc_temperature(orc_prb_t *s)
     temp_update(s, 0);
     for (int i = 1; i <= nr; ++i)
         for (int k = 0; k <= np; ++k)
-            s->th[IX(i, k)] = s->th[IX(i, k)] + 0.02 * (s->thn[IX(i, k)] - 2.0 * s->th[IX(i, k)] + s->thp[IX(i, k)]);
+            s->th[IX(i, k)] = s->th[IX(i, k)] + robert(s) * (s->thn[IX(i, k)] - 2.0 * s->th[IX(i, k)] + s->thp[IX(i, k)]);
     free(b);
 }
 
@@ -870,36 +1009,53 @@ void orc_update(orc_prb_t *s)
 }
 
 /* rhsv, PRB:1629-1676: v-equation source dCn/dr on i = 1..nr with the
- * one-sided rows of the reference at i = 1 and i = nr. */
+ * one-sided rows of the reference at i = 1 and i = nr.  ORC_ANNULUS
+ * (velvor2dnewsch3.4.f:1666-1686) adds the polar terms Cn/r at the
+ * cell-centre radius r = r0 + (i-1/2) dr. */
 void orc_rhsv(orc_prb_t *s)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
     const double dr = s->dr;
+    const int polar = (s->variant == ORC_ANNULUS);
     for (int i = 1; i <= nr; ++i) {
         for (int k = 0; k <= np; ++k) {
             const double Cr = (s->Cn[IX(i, k)] - s->Cn[IX(i - 1, k)]) / dr;
-            if (i == 1) s->vrh[IX(i, k)] = s->Cn[IX(1, k)] / dr;
+            if (polar) {
+                const double r = s->r0 + ((double)i - 0.5) * dr;
+                if (i == 1) s->vrh[IX(i, k)] = s->Cn[IX(1, k)] / dr + s->Cn[IX(1, k)] / r;
+                else if (i == nr) s->vrh[IX(i, k)] = -s->Cn[IX(nr - 1, k)] / dr + s->Cn[IX(nr - 1, k)] / r;
+                else s->vrh[IX(i, k)] = Cr + (s->Cn[IX(i, k)] + s->Cn[IX(i - 1, k)]) / r;
+            } else if (i == 1) s->vrh[IX(i, k)] = s->Cn[IX(1, k)] / dr;
             else if (i == nr) s->vrh[IX(i, k)] = -s->Cn[IX(nr - 1, k)] / dr;
             else s->vrh[IX(i, k)] = Cr;
         }
     }
 }
 
-/* rhsu, PRB:1679-1721: u-equation source -dCn/dx on i = 1..nr-1. */
+/* rhsu, PRB:1679-1721: u-equation source -dCn/dx / r on i = 1..nr-1, with
+ * r = 1 in PRB and the face radius r = r0 + i dr in the annulus
+ * (velvor2dnewsch3.4.f:1710-1730). */
 void orc_rhsu(orc_prb_t *s)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
-    const double dp = s->dp;
+    const int polar = (s->variant == ORC_ANNULUS);
     for (int i = 1; i <= nr - 1; ++i) {
         for (int k = 0; k <= np; ++k) {
             int km = k - 1;
             if (k == 0) km = np - 1;
-            const double r = 1.0;
+            const double r = polar ? s->r0 + (double)i * s->dr : 1.0;
             const double Ch = (s->Cn[IX(i, k)] - s->Cn[IX(i, km)]) / s->dp;
-            (void)dp;
             s->urh[IX(i, k)] = -Ch / r;
         }
     }
+}
+
+/* The annulus solves never stop the run: after nvs sweeps poisson2 and
+ * poisson3 return with psi untouched and the step goes on
+ * (velvor2dnewsch3.4.f:1853-1936, :1984-2068). */
+static int solve_failed(const orc_prb_t *s, int st)
+{
+    return st != ORC_OK && !(s->variant == ORC_ANNULUS && st == ORC_MAXSWEEPS);
 }
 
 int orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double *nu, int *sweeps)
@@ -916,14 +1072,21 @@ int orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double *nu,
     orc_heat(s, &t1, &t2);
     orc_rhsv(s);
     st = orc_poisson(mgv, 2, s->vel, s->velp, s->vrh, s->ld, &sv);
-    if (st != ORC_OK) { if (sweeps) { sweeps[0] = sv; sweeps[1] = 0; } return st; }
+    if (solve_failed(s, st)) { if (sweeps) { sweeps[0] = sv; sweeps[1] = 0; } return st; }
     orc_rhsu(s);
     st = orc_poisson(mgu, 3, s->uel, s->uelp, s->urh, s->ld, &su);
-    if (st != ORC_OK) { if (sweeps) { sweeps[0] = sv; sweeps[1] = su; } return st; }
+    if (solve_failed(s, st)) { if (sweeps) { sweeps[0] = sv; sweeps[1] = su; } return st; }
     orc_update(s);
     if (nu) {
-        nu[0] = t1 * (s->rmax - s->r0) / s->xx;
-        nu[1] = t2 * (s->rmax - s->r0) / s->xx;
+        if (s->variant == ORC_ANNULUS) {
+            /* httrans, httrans2 of velvor2dnewsch3.4.f:386-387 */
+            const double pi = acos(-1.0), L = log(s->r0 / s->rmax);
+            nu[0] = -s->r0 * L * t1 / (2.0 * pi);
+            nu[1] = -s->rmax * L * t2 / (2.0 * pi);
+        } else {
+            nu[0] = t1 * (s->rmax - s->r0) / s->xx;
+            nu[1] = t2 * (s->rmax - s->r0) / s->xx;
+        }
     }
     if (sweeps) { sweeps[0] = sv; sweeps[1] = su; }
     return ORC_OK;
@@ -952,7 +1115,21 @@ void orc_prb_initial(orc_prb_t *s, int kind, unsigned long long seed, double amp
             s->An[IX(i, k)] = s->Bn[IX(i, k)] = s->Cn[IX(i, k)] = 0.0;
             s->A[IX(i, k)] = s->B[IX(i, k)] = s->C[IX(i, k)] = 0.0;
             s->uel[IX(i, k)] = s->vel[IX(i, k)] = s->wel[IX(i, k)] = 0.0;
-            if (kind == 0) {
+            if (kind == 0 && s->variant == ORC_ANNULUS) {
+                /* velvor2dnewsch3.4.f:130-178: conduction profile 1 - ln r / ln r0
+                 * with walls 0 and 1 and the ripple 0.7 T (r-rmax)/rmax (2 randno - 1),
+                 * randno = 1/2 + sin(2 pi k/150)/2.  The blobs of :185-220 have
+                 * amplitude -0.0 and leave T unchanged. */
+                const double pi = acos(-1.0);
+                double t = 1.0 - log(r) / log(r0);
+                if (i == 0) t = 0.0;
+                else if (i == nr + 1) t = 1.0;
+                else {
+                    double randno = 0.5 + 0.5 * sin((double)k / 150.0 * 2.0 * pi);
+                    t = t + (r - rmax) / rmax * ((randno * 2.0) - 1.0) * 0.7 * t;
+                }
+                s->th[IX(i, k)] = t;
+            } else if (kind == 0) {
                 /* PRB:156-186: T = 2(r-r0) plus a deterministic sine ripple whose
                  * 0.01 is a REAL*4 literal.  The Gaussian blobs of PRB:193-227 have
                  * amplitude -0.0 and leave T unchanged. */
@@ -977,7 +1154,8 @@ void orc_prb_initial(orc_prb_t *s, int kind, unsigned long long seed, double amp
                 else if (k == np) t = s->th[IX(i, 0)];
                 else {
                     double u = (double)(splitmix64(&st) >> 11) * (1.0 / 9007199254740992.0);
-                    t = (r - r0) / (rmax - r0) + amp * (2.0 * u - 1.0);
+                    if (s->variant == ORC_ANNULUS) t = 1.0 - log(r) / log(r0) + amp * (2.0 * u - 1.0);
+                    else t = (r - r0) / (rmax - r0) + amp * (2.0 * u - 1.0);
                 }
                 s->th[IX(i, k)] = t;
             }

@@ -63,9 +63,19 @@ typedef struct {
     double *scratch_v, *scratch_f;       /* the mgen-sized buffers when zero_scratch */
     int last_sweeps;
     double last_resmax;
+    /* variant ORC_PRB (velvor2dperiodicrbconv.f) or ORC_ANNULUS (the polar
+     * (r,phi) plane of velvor2dnewsch3.4.f): polar coefficients, three
+     * relaxations per call, no reset of the coarse seam of rc, level cap 5 */
+    int variant;
+    double r0;
 } orc_mg_t;
 
+#define ORC_PRB     0
+#define ORC_ANNULUS 1
+
 int  orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp);
+/* Same with the variant and inner radius of the annulus driver. */
+int  orc_mg_init_variant(orc_mg_t *mg, int nr, int np, double dr, double dp, int variant, double r0);
 void orc_mg_free(orc_mg_t *mg);
 /* which = 2: poisson2/relax2 (cell-centred v, pentadiagonal r-lines)
  * which = 3: poisson3/relax3 (face u, tridiagonal r-lines)
@@ -88,6 +98,8 @@ typedef struct {
     double *uel, *vel, *wel, *uelp, *velp, *welp;
     double *urh, *vrh;
     long clamp_count;                    /* "WARNING! Temp damped" count */
+    int variant;                         /* ORC_PRB or ORC_ANNULUS */
+    double Re;                           /* rotational Reynolds number (annulus) */
 } orc_prb_t;
 
 int  orc_prb_alloc(orc_prb_t *s, int nr, int np, int ld);
@@ -109,7 +121,8 @@ int  orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt,
                   double *nu, int *sweeps);
 
 /* Initial conditions.  kind 0: the reference's own deterministic profile
- * (PRB:137-186).  kind 1: linear conduction plus seeded uniform noise of
+ * (PRB:137-186; for ORC_ANNULUS the conduction profile 1 - ln r / ln r0
+ * with the sine ripple of velvor2dnewsch3.4.f:131-150).  kind 1: linear conduction plus seeded uniform noise of
  * amplitude amp drawn from splitmix64(seed), periodic duplicate k=np equal
  * to k=0.  Both set Ap..thp, uelp, velp as PRB:316-331 does. */
 void orc_prb_initial(orc_prb_t *s, int kind, unsigned long long seed, double amp);

@@ -1,8 +1,11 @@
 """The gfortran-compatible drop-in symbols (poissoninit_, cvorticity1_, ...,
 update_) driven the way the Fortran main program drives them (PRB:341-388),
 with COMMON blocks laid out as gfortran lays them out, against the oracle.
+The same symbols serve the rotating-annulus driver (velvor2dnewsch3.4.f,
+main loop :341-387) once gb_prb_bind_variant selects it.
 """
 import ctypes as C
+import math
 
 import numpy as np
 import pytest
@@ -22,13 +25,17 @@ SOL2 = ["thn", "th", "thp"]
 SOL3 = ["uel", "vel", "wel", "uelp", "velp", "welp"]
 
 
-@pytest.mark.parametrize("kr,kp", [(20, 40), (290, 1610)], ids=["small-bounds", "reference-bounds"])
-def test_dropin_main_loop(oracle, gblib, kr, kp):
+@pytest.mark.parametrize("kr,kp,variant", [(20, 40, 0), (290, 1610, 0), (20, 40, 1), (420, 3600, 1)],
+                         ids=["small-bounds", "reference-bounds", "annulus-small-bounds", "annulus-reference-bounds"])
+def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
     L = gblib
     nr, np_ = 16, 32
-    dt, Ra, Pr, r0, rmax, xx = 1e-4, 1e5, 0.71, 0.5, 1.0, 3.0
-    o = oracle.OraclePRB(nr, np_, dt, Ra, Pr, r0=r0, rmax=rmax, xx=xx)
-    o.initial(0, 0, 0.0)  # the reference's own initial profile (PRB:137-186)
+    dt, Ra, Pr, r0, rmax, xx, Re = 1e-4, 1e5, 0.71, 0.5, 1.0, 3.0, 1e4
+    if variant:
+        dt, Ra = 1e-6, 1e6
+    tol, maxsw = (10e-6, 10000) if variant else (2e-6, 500)
+    o = oracle.OraclePRB(nr, np_, dt, Ra, Pr, r0=r0, rmax=rmax, xx=xx, variant=variant, Re=Re)
+    o.initial(0, 0, 0.0)  # the reference's own initial profile (PRB:137-186, annulus :130-178)
     S = (kr + 1) * (kp + 1)
     sol1 = np.zeros(9 * S)
     sol2 = np.zeros(3 * S)
@@ -43,10 +50,13 @@ def test_dropin_main_loop(oracle, gblib, kr, kp):
         for i, nm in enumerate(names):
             view(blk, i)[: nr + 2, : np_ + 1] = np.array(o.field(nm))
     num = Num(dt, o.s.dr, 0.0, o.s.dp, nr, 1, np_)
-    val = np.array([Ra, 0.0, Pr, 0.0])
+    val = np.array([Ra, Re if variant else 0.0, Pr, 0.0])
+    radius = np.array([r0, rmax])
     L.gb_prb_bind_bounds(kr, kp)
-    L.gb_prb_bind_tolerance(2e-6, 500)
+    L.gb_prb_bind_tolerance(tol, maxsw)
     L.gb_prb_bind_smoother(0)
+    L.gb_prb_bind_variant(variant)
+    L.gb_prb_bind_radius(radius.ctypes.data)
     L.gb_prb_bind_common(sol1.ctypes.data, sol2.ctypes.data, sol3.ctypes.data, C.addressof(num), val.ctypes.data)
     try:
         nrc, nzc, npc = C.c_int(nr), C.c_int(1), C.c_int(np_)
@@ -81,7 +91,10 @@ def test_dropin_main_loop(oracle, gblib, kr, kp):
             assert L.gb_prb_last_sweeps() == sw[1]
             L.update_()
             assert L.gb_prb_last_status() == 0
-            assert t1.value * (rmax - r0) / xx == nu[0]
+            if variant:
+                assert -r0 * math.log(r0 / rmax) * t1.value / (2.0 * math.acos(-1.0)) == nu[0]
+            else:
+                assert t1.value * (rmax - r0) / xx == nu[0]
             for blk, names in ((sol1, SOL1), (sol2, SOL2), (sol3, SOL3)):
                 for i, nm in enumerate(names):
                     np.testing.assert_array_equal(view(blk, i)[: nr + 2, : np_ + 1], np.array(o.field(nm)),
@@ -89,4 +102,7 @@ def test_dropin_main_loop(oracle, gblib, kr, kp):
         del vel, velp, uel, uelp
     finally:
         L.gb_prb_bind_common(None, None, None, None, None)
+        L.gb_prb_bind_radius(None)
+        L.gb_prb_bind_variant(0)
+        L.gb_prb_bind_tolerance(2e-6, 500)
         L.gb_prb_bind_bounds(290, 1610)
