@@ -177,6 +177,126 @@ def cpu_reference(sizes_all, seed, budget_s=20.0, threads=None):
     return done_cu / done_t, sample, threads, used, np.concatenate(psi_s)
 
 
+# ---------------------------------------------------------------------------
+# 2D driver workloads: the 129 x 65 periodic layer (Ra 1e5, Pr 1, dt 1e-5,
+# multigrid to max-norm residual 1e-10) and the rotating annulus of the
+# annulus driver's own deck (nr 272, np 1200, Ra 8e8, Re 1.06148e5, Pr 0.71,
+# dt 2e-8, tolcon 1e-5).  A cell-update is one (i,k) cell advanced one step.
+# ---------------------------------------------------------------------------
+LAYER = dict(nr=64, np_=128, dt=1e-5, Ra=1e5, Pr=1.0, r0=0.0, rmax=1.0, xx=2.0, Re=0.0, variant=0,
+             tolcon=1e-10, kind=1, amp=1e-3,
+             name="2D periodic layer 129 x 65 (nr 64, np 128), Ra 1e5, Pr 1, dt 1e-5, MG to 1e-10")
+ANNULUS = dict(nr=272, np_=1200, dt=2e-8, Ra=8e8, Pr=0.71, r0=0.5, rmax=1.0, xx=0.0, Re=1.06148e5, variant=1,
+               tolcon=10e-6, kind=0, amp=0.0,
+               name="2D rotating annulus (r, phi) nr 272, np 1200, Ra 8e8, Re 1.06148e5, Pr 0.71, dt 2e-8, tolcon 1e-5")
+
+
+def layer_words(sweeps_mean):
+    """FP64 words per cell-update of a step: transport 10, per solve 8 for
+    set-up and finalise plus 29.5 per outer multigrid sweep."""
+    return 10.0 + sum(8.0 + 29.5 * s for s in sweeps_mean)
+
+
+def prb_instance(cfg, smoother, seed=0):
+    from codesthesis_dir_gb300 import initial, prb
+    g = prb.PRB(cfg["nr"], cfg["np_"], dt=cfg["dt"], r0=cfg["r0"], rmax=cfg["rmax"], xx=cfg["xx"] or 3.0,
+                Ra=cfg["Ra"], Pr=cfg["Pr"], tolcon=cfg["tolcon"], smoother=smoother, variant=cfg["variant"],
+                Re=cfg["Re"])
+    for name, a in initial.initial_fields(cfg["nr"], cfg["np_"], cfg["r0"], cfg["rmax"], cfg["variant"],
+                                          cfg["kind"], seed, cfg["amp"]).items():
+        g.set(name, a)
+    return g
+
+
+def time_prb_gpu(cfg, smoother, steps, warmup):
+    """Device steps (one CUDA graph per step) timed with CUDA events on the
+    instance's own stream.  Returns (cell-updates/s, ms/step, mean sweeps
+    [v, u], Nu history, launches)."""
+    import torch
+    from codesthesis_dir_gb300 import lib
+    g = prb_instance(cfg, smoother)
+    L = lib.load()
+    s = torch.cuda.ExternalStream(L.gb_prb_stream(g._h))
+    if warmup:
+        g.step(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    nu, sw = g.step(steps)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = cfg["nr"] * cfg["np_"]
+    g.close()
+    return cells * steps / (ms / 1e3), ms / steps, sw.mean(axis=0).tolist(), nu, steps * 0
+
+
+def time_prb_cpu(cfg, smoother, budget_s=3.0, max_steps=200):
+    """The oracle (one core: the reference's loop is serial) on the same
+    instance for a bounded number of steps."""
+    from oracle import oracle as O
+    O.build()
+    o = O.OraclePRB(cfg["nr"], cfg["np_"], cfg["dt"], cfg["Ra"], cfg["Pr"], r0=cfg["r0"], rmax=cfg["rmax"],
+                    xx=cfg["xx"] or 3.0, mode=smoother, tolcon=cfg["tolcon"], variant=cfg["variant"], Re=cfg["Re"])
+    o.initial(cfg["kind"], 0, cfg["amp"])
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps and time.perf_counter() - t0 < budget_s:
+        st, nu, sw = o.step()
+        assert st == 0
+        n += 1
+    dt = time.perf_counter() - t0
+    o.close()
+    return cfg["nr"] * cfg["np_"] * n / dt, n, dt
+
+
+def prb_summary(cfg, steps_zebra, steps_lex, warmup, cpu_budget):
+    out = {"workload": cfg["name"]}
+    for nm, sm, st in (("fp64_zebra", 1, steps_zebra), ("fp64_lex", 0, steps_lex)):
+        if st <= 0:
+            continue
+        v, ms, sw, nu, _ = time_prb_gpu(cfg, sm, st, warmup if sm == 1 else 1)
+        w = layer_words(sw)
+        out[nm] = {"value": v, "unit": "cell-updates/s", "ms_per_step": ms, "steps": st, "sweeps_mean_v_u": sw,
+                   "alg_bytes_per_cell_update": 8 * w, "achieved_GBs": 8 * w * v / 1e9,
+                   "nu_last": [float(nu[-1, 0]), float(nu[-1, 1])]}
+    if cpu_budget > 0:
+        v, n, dt = time_prb_cpu(cfg, 0, cpu_budget)
+        out["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                               "sample": "%d steps of the same instance, oracle LEX (the reference schedule), "
+                                         "1 thread, %.1f s" % (n, dt)}
+    return out
+
+
+def run_prb_workload(args, cfg):
+    """--workload layer|annulus: one JSON line for the 2D driver step."""
+    import torch
+    from codesthesis_dir_gb300 import lib
+    lib.load()
+    peak, peak_kind = measured_peaks()
+    with ClockSampler() as clk:
+        summ = prb_summary(cfg, args.steps, 0 if args.workload == "annulus" else max(1, args.steps // 20),
+                           args.warmup, 0 if args.no_cpu_baseline else 3.0)
+    z = summ["fp64_zebra"]
+    line = {
+        "metric": "cell-updates/s (2D driver step, FP64 device path)", "value": z["value"],
+        "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": z["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfg["name"], "smoother": "zebra",
+                   "l2": "working set (~%.0f MB) fits in L2; steps are latency and FP64-pipe bound" % (
+                       20 * (cfg["nr"] + 2) * (cfg["np_"] + 1) * 8 / 1e6)},
+        "roofline": {"bound": "hbm", "achieved": z["achieved_GBs"], "peak": peak, "unit": "GB/s",
+                     "frac": z["achieved_GBs"] / peak, "traffic": None, "peak_kind": peak_kind},
+        "detail": summ,
+        "clocks": clk.summary(),
+    }
+    if "cpu_baseline" in summ:
+        line["cpu_baseline"] = summ["cpu_baseline"]
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -216,9 +336,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-only", action="store_true",
                     help="time only the mixed solve (for profiler launch lists); prints no JSON line")
+    ap.add_argument("--no-layer", action="store_true", help="skip the 2D layer step measurement of the default run")
+    ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus"],
+                    help="batch: 256 batched Poisson problems (the headline); layer / annulus: the 2D driver step")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "batch":
+        return run_prb_workload(args, LAYER if args.workload == "layer" else ANNULUS)
 
     import torch
 
@@ -418,6 +543,9 @@ def main():
                                 "sample": sample}
         line["mixed"]["field_rel_l2_vs_fp64_oracle_sample"] = float(np.linalg.norm(got - psi_ref) /
                                                                      np.linalg.norm(psi_ref))
+    if not args.no_layer:
+        # the 129 x 65 layer workload's step (FP64 device path) beside the CPU oracle
+        line["layer_config0"] = prb_summary(LAYER, 60, 3, 3, 0.0 if args.no_cpu_baseline else 3.0)
     print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist

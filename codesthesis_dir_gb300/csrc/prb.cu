@@ -820,3 +820,5 @@ extern "C" int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *swee
     }
     return GB_OK;
 }
+
+extern "C" void *gb_prb_stream(gb_prb *h) { return h ? (void *)h->stream : nullptr; }

@@ -76,6 +76,7 @@ SIGNATURES = [
     ("gb_prb_poisson", C.c_int, [_vp, C.c_int, _ip]),
     ("gb_prb_update", C.c_int, [_vp, C.POINTER(C.c_longlong)]),
     ("gb_prb_step", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    ("gb_prb_stream", _vp, [_vp]),
     ("gb_prb_bind_bounds", None, [C.c_int, C.c_int]),
     ("gb_prb_bind_smoother", None, [C.c_int]),
     ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),

@@ -150,6 +150,9 @@ int gb_prb_update(gb_prb *h, long long *clamps);
  * from a CUDA graph; the v and u solves run concurrently (the reference's
  * OpenMP sections, PRB:370-380). */
 int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *sweeps);
+/* The CUDA stream (cudaStream_t) every call on h runs on, for callers that
+ * order their own work or time the steps with events on it. */
+void *gb_prb_stream(gb_prb *h);
 
 /* ------------------------------------------- gfortran-compatible drop-in */
 /* These read/write the caller's COMMON blocks (declared by the Fortran main

@@ -3,6 +3,7 @@ import io
 import os
 
 import numpy as np
+import pytest
 
 from codesthesis_dir_gb300 import deck, fortio
 
@@ -77,3 +78,17 @@ def test_fortran_e_format():
     assert fortio.fortran_e(1.23456789e-5) == "  0.12345679E-04"
     assert fortio.fortran_e(0.0) == "  0.00000000E+00"
     assert len(fortio.fortran_e(3.0e120)) == 16
+
+
+@pytest.mark.parametrize("variant,kind", [(0, 0), (0, 1), (1, 0), (1, 1)],
+                         ids=["layer-ref", "layer-noise", "annulus-ref", "annulus-noise"])
+def test_host_initial_states_match_oracle(oracle, variant, kind):
+    """The package's numpy initial states are the oracle's, bit for bit."""
+    from codesthesis_dir_gb300 import initial
+    nr, np_ = 24, 48
+    r0, rmax = (0.5, 1.0) if variant else (0.0, 1.0)
+    o = oracle.OraclePRB(nr, np_, 1e-5, 1e5, 1.0, r0=r0, rmax=rmax, xx=2.0, variant=variant, Re=1e4)
+    o.initial(kind, 7, 1e-3)
+    f = initial.initial_fields(nr, np_, r0, rmax, variant=variant, kind=kind, seed=7, amp=1e-3)
+    for name in ("th", "thp", "C", "uel", "vel"):
+        np.testing.assert_array_equal(f[name], np.array(o.field(name)), err_msg=name)
