@@ -208,17 +208,18 @@ def prb_instance(cfg, smoother, seed=0):
     return g
 
 
-def time_prb_gpu(cfg, smoother, steps, warmup):
+def time_prb_gpu(cfg, smoother, steps, warmup, precision=0):
     """Device steps (one CUDA graph per step) timed with CUDA events on the
     instance's own stream.  Returns (cell-updates/s, ms/step, mean sweeps
-    [v, u], Nu history, launches)."""
+    [v, u], Nu history of all warm-up and timed steps, final fields)."""
     import torch
     from codesthesis_dir_gb300 import lib
-    g = prb_instance(cfg, smoother)
+    g = prb_instance(cfg, smoother) if precision == 0 else _prb_mixed_instance(cfg, smoother)
     L = lib.load()
     s = torch.cuda.ExternalStream(L.gb_prb_stream(g._h))
+    nu_w = np.zeros((0, 2))
     if warmup:
-        g.step(warmup)
+        nu_w, _ = g.step(warmup)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
@@ -227,8 +228,20 @@ def time_prb_gpu(cfg, smoother, steps, warmup):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     cells = cfg["nr"] * cfg["np_"]
+    fields = {n: g.get(n) for n in ("vel", "uel", "C", "th")}
     g.close()
-    return cells * steps / (ms / 1e3), ms / steps, sw.mean(axis=0).tolist(), nu, steps * 0
+    return cells * steps / (ms / 1e3), ms / steps, sw.mean(axis=0).tolist(), np.concatenate([nu_w, nu]), fields
+
+
+def _prb_mixed_instance(cfg, smoother):
+    from codesthesis_dir_gb300 import initial, prb
+    g = prb.PRB(cfg["nr"], cfg["np_"], dt=cfg["dt"], r0=cfg["r0"], rmax=cfg["rmax"], xx=cfg["xx"] or 3.0,
+                Ra=cfg["Ra"], Pr=cfg["Pr"], tolcon=cfg["tolcon"], smoother=smoother, variant=cfg["variant"],
+                Re=cfg["Re"], precision=1)
+    for name, a in initial.initial_fields(cfg["nr"], cfg["np_"], cfg["r0"], cfg["rmax"], cfg["variant"],
+                                          cfg["kind"], 0, cfg["amp"]).items():
+        g.set(name, a)
+    return g
 
 
 def time_prb_cpu(cfg, smoother, budget_s=3.0, max_steps=200):
@@ -251,15 +264,32 @@ def time_prb_cpu(cfg, smoother, budget_s=3.0, max_steps=200):
 
 
 def prb_summary(cfg, steps_zebra, steps_lex, warmup, cpu_budget):
+    """FP64 device steps (zebra and the reference's lexicographic order),
+    the mixed-precision steps with their error against the FP64 run (which
+    is bit-identical to the FP64 oracle), and the CPU oracle."""
     out = {"workload": cfg["name"]}
-    for nm, sm, st in (("fp64_zebra", 1, steps_zebra), ("fp64_lex", 0, steps_lex)):
+    runs = {}
+    for nm, sm, st, prec in (("fp64_zebra", 1, steps_zebra, 0), ("mixed_zebra", 1, steps_zebra, 1),
+                             ("fp64_lex", 0, steps_lex, 0)):
         if st <= 0:
             continue
-        v, ms, sw, nu, _ = time_prb_gpu(cfg, sm, st, warmup if sm == 1 else 1)
-        w = layer_words(sw)
-        out[nm] = {"value": v, "unit": "cell-updates/s", "ms_per_step": ms, "steps": st, "sweeps_mean_v_u": sw,
-                   "alg_bytes_per_cell_update": 8 * w, "achieved_GBs": 8 * w * v / 1e9,
+        v, ms, sw, nu, fields = time_prb_gpu(cfg, sm, st, warmup if sm == 1 else 1, prec)
+        runs[nm] = (nu, fields)
+        w = layer_words(sw) if prec == 0 else None
+        out[nm] = {"value": v, "unit": "cell-updates/s", "ms_per_step": ms, "steps": st,
+                   "sweeps_mean_v_u" if prec == 0 else "fp32_cycles_mean_v_u": sw,
                    "nu_last": [float(nu[-1, 0]), float(nu[-1, 1])]}
+        if w is not None:
+            out[nm].update({"alg_bytes_per_cell_update": 8 * w, "achieved_GBs": 8 * w * v / 1e9})
+    if "mixed_zebra" in runs and "fp64_zebra" in runs:
+        nu_m, f_m = runs["mixed_zebra"]
+        nu_d, f_d = runs["fp64_zebra"]
+        m = out["mixed_zebra"]
+        m["speedup_vs_fp64"] = m["value"] / out["fp64_zebra"]["value"]
+        m["nu_rel_err_vs_fp64"] = float(np.max(np.abs(nu_m - nu_d) / np.abs(nu_d)))
+        m["field_rel_l2_vs_fp64"] = {n: float(np.linalg.norm(f_m[n] - f_d[n]) / max(np.linalg.norm(f_d[n]), 1e-300))
+                                     for n in f_d}
+        m["after_steps"] = int(nu_d.shape[0])
     if cpu_budget > 0:
         v, n, dt = time_prb_cpu(cfg, 0, cpu_budget)
         out["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
@@ -278,11 +308,12 @@ def run_prb_workload(args, cfg):
         summ = prb_summary(cfg, args.steps, 0 if args.workload == "annulus" else max(1, args.steps // 20),
                            args.warmup, 0 if args.no_cpu_baseline else 3.0)
     z = summ["fp64_zebra"]
+    mx = summ["mixed_zebra"]
     line = {
-        "metric": "cell-updates/s (2D driver step, FP64 device path)", "value": z["value"],
-        "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": z["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
+        "metric": "cell-updates/s (2D driver step, mixed-precision velocity solves; FP64 path beside)",
+        "value": mx["value"], "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer", "data": "synthetic",
         "config": {"workload": cfg["name"], "smoother": "zebra",
                    "l2": "working set (~%.0f MB) fits in L2; steps are latency and FP64-pipe bound" % (
                        20 * (cfg["nr"] + 2) * (cfg["np_"] + 1) * 8 / 1e6)},

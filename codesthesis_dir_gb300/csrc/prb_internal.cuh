@@ -19,6 +19,10 @@ struct MgLevel {
     const double *fac;   // factored line matrix (pdma for v, tdma for u)
     double *v, *f;       // packed (n1+1)*(n3+1) solution / right-hand side
     double *rvi, *rvq;   // annulus: 1/r and 1/r^2 of row i (n1+2 entries)
+    // mixed precision: the FP32 correction cycle's storage
+    float *v32, *f32;    // packed correction / right-hand side
+    float *fac32;        // factors with the pivots stored as reciprocals
+    float *rvi32, *rvq32;
 };
 
 // Device description of one Poisson solve (poisson2 or poisson3).
@@ -31,6 +35,7 @@ struct MgEq {
     double tolcon, sor;
     MgLevel lev[PRB_MAXLEV];
     double *psic, *psif, *rc, *rf, *tempa;   // COMMON /arrays/ (per equation)
+    float *psif32, *rc32;                    // mixed precision: FP32 correction and residual
     double *psi, *psip;                      // solution and previous level (in/out)
     const double *rhs;
     int *status;         // [0] status, [1] sweeps

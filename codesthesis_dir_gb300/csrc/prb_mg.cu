@@ -30,6 +30,7 @@
 // straight from its packed slot (the reference stages both through psic/rf/
 // tempa).  Every value the solution depends on is formed by the same
 // arithmetic on the same operands.
+#include <stdint.h>
 #include <string.h>
 
 #include "banded.cuh"
@@ -53,6 +54,55 @@ __device__ __forceinline__ double blk_max(double v, double *s_red)
     const double r = s_red[32];
     __syncthreads();
     return r;
+}
+
+// The level operator applied at (i, k) (the part of relax2/relax3's
+// residual before it is subtracted from f): PRB:2306-2357 (v),
+// PRB:2553-2587 (u), and the annulus forms of velvor2dnewsch3.4.f:2300-2346
+// and :2546-2579.  Instantiated for double (bit-identical to the reference)
+// and for float (the mixed-precision correction cycle).
+template <class T>
+__device__ __forceinline__ T mg_apply_op(const T *psif, int ld, int i, int k, int ka, int km, int which, int polar,
+                                         int n1, T hhri, T hhpi, T hri, const T *rvi, const T *rvq)
+{
+    const T two = T(2.0), c53 = T(5.0 / 3.0), c02 = T(0.2), c15 = T(1.5), c43 = T(4.0 / 3.0);
+    T temp;
+    if (polar && which == 2) {
+        temp = (psif[GIX(i, ka, ld)] - two * psif[GIX(i, k, ld)] + psif[GIX(i, km, ld)]) * hhpi * rvq[i] +
+               psif[GIX(i, k, ld)] * rvq[i];
+        if (i == 1)
+            temp = temp + (-two * psif[GIX(i, k, ld)] + c53 * psif[GIX(i + 1, k, ld)] -
+                           c02 * psif[GIX(i + 2, k, ld)]) * hhri +
+                   c43 * psif[GIX(i + 1, k, ld)] * hri * rvi[i];
+        else if (i == n1)
+            temp = temp + (-two * psif[GIX(i, k, ld)] + c53 * psif[GIX(i - 1, k, ld)] -
+                           c02 * psif[GIX(i - 2, k, ld)]) * hhri -
+                   c43 * psif[GIX(i - 1, k, ld)] * hri * rvi[i];
+        else
+            temp = temp + (psif[GIX(i - 1, k, ld)] - two * psif[GIX(i, k, ld)] + psif[GIX(i + 1, k, ld)]) * hhri +
+                   c15 * (psif[GIX(i + 1, k, ld)] - psif[GIX(i - 1, k, ld)]) * hri * rvi[i];
+    } else if (polar) {
+        temp = (psif[GIX(i + 1, k, ld)] + psif[GIX(i - 1, k, ld)]) * hhri +
+               c15 * (psif[GIX(i + 1, k, ld)] - psif[GIX(i - 1, k, ld)]) * hri * rvi[i] +
+               psif[GIX(i, k, ld)] * rvq[i] +
+               (psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi * rvq[i] -
+               psif[GIX(i, k, ld)] * (two * hhri + two * hhpi * rvq[i]);
+    } else if (which == 2) {
+        temp = (psif[GIX(i, ka, ld)] - two * psif[GIX(i, k, ld)] + psif[GIX(i, km, ld)]) * hhpi;
+        if (i == 1)
+            temp = temp + (-two * psif[GIX(i, k, ld)] + c53 * psif[GIX(i + 1, k, ld)] -
+                           c02 * psif[GIX(i + 2, k, ld)]) * hhri;
+        else if (i == n1)
+            temp = temp + (-two * psif[GIX(i, k, ld)] + c53 * psif[GIX(i - 1, k, ld)] -
+                           c02 * psif[GIX(i - 2, k, ld)]) * hhri;
+        else
+            temp = temp + (psif[GIX(i - 1, k, ld)] - two * psif[GIX(i, k, ld)] + psif[GIX(i + 1, k, ld)]) * hhri;
+    } else {
+        temp = (psif[GIX(i + 1, k, ld)] + psif[GIX(i - 1, k, ld)]) * hhri +
+               (psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi -
+               psif[GIX(i, k, ld)] * (two * hhri + two * hhpi);
+    }
+    return temp;
 }
 
 // One line k of relax2 (pentadiagonal, rows i = 1..n1, PRB:2113-2191) or
@@ -114,44 +164,7 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
         const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
         const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
-        double temp;
-        if (E.polar && E.which == 2) {
-            // velvor2dnewsch3.4.f:2300-2346
-            temp = (psif[GIX(i, ka, ld)] - 2.0 * psif[GIX(i, k, ld)] + psif[GIX(i, km, ld)]) * hhpi * rvq[i] +
-                   psif[GIX(i, k, ld)] * rvq[i];
-            if (i == 1)
-                temp = temp + (-2.0 * psif[GIX(i, k, ld)] + 5.0 / 3.0 * psif[GIX(i + 1, k, ld)] -
-                               0.2 * psif[GIX(i + 2, k, ld)]) * hhri +
-                       4.0 / 3.0 * psif[GIX(i + 1, k, ld)] * hri * rvi[i];
-            else if (i == n1)
-                temp = temp + (-2.0 * psif[GIX(i, k, ld)] + 5.0 / 3.0 * psif[GIX(i - 1, k, ld)] -
-                               0.2 * psif[GIX(i - 2, k, ld)]) * hhri -
-                       4.0 / 3.0 * psif[GIX(i - 1, k, ld)] * hri * rvi[i];
-            else
-                temp = temp + (psif[GIX(i - 1, k, ld)] - 2.0 * psif[GIX(i, k, ld)] + psif[GIX(i + 1, k, ld)]) * hhri +
-                       1.5 * (psif[GIX(i + 1, k, ld)] - psif[GIX(i - 1, k, ld)]) * hri * rvi[i];
-        } else if (E.polar) {
-            // velvor2dnewsch3.4.f:2546-2579
-            temp = (psif[GIX(i + 1, k, ld)] + psif[GIX(i - 1, k, ld)]) * hhri +
-                   1.5 * (psif[GIX(i + 1, k, ld)] - psif[GIX(i - 1, k, ld)]) * hri * rvi[i] +
-                   psif[GIX(i, k, ld)] * rvq[i] +
-                   (psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi * rvq[i] -
-                   psif[GIX(i, k, ld)] * (2.0 * hhri + 2.0 * hhpi * rvq[i]);
-        } else if (E.which == 2) {
-            temp = (psif[GIX(i, ka, ld)] - 2.0 * psif[GIX(i, k, ld)] + psif[GIX(i, km, ld)]) * hhpi;
-            if (i == 1)
-                temp = temp + (-2.0 * psif[GIX(i, k, ld)] + 5.0 / 3.0 * psif[GIX(i + 1, k, ld)] -
-                               0.2 * psif[GIX(i + 2, k, ld)]) * hhri;
-            else if (i == n1)
-                temp = temp + (-2.0 * psif[GIX(i, k, ld)] + 5.0 / 3.0 * psif[GIX(i - 1, k, ld)] -
-                               0.2 * psif[GIX(i - 2, k, ld)]) * hhri;
-            else
-                temp = temp + (psif[GIX(i - 1, k, ld)] - 2.0 * psif[GIX(i, k, ld)] + psif[GIX(i + 1, k, ld)]) * hhri;
-        } else {
-            temp = (psif[GIX(i + 1, k, ld)] + psif[GIX(i - 1, k, ld)]) * hhri +
-                   (psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi -
-                   psif[GIX(i, k, ld)] * (2.0 * hhri + 2.0 * hhpi);
-        }
+        double temp = mg_apply_op<double>(psif, ld, i, k, ka, km, E.which, E.polar, n1, hhri, hhpi, hri, rvi, rvq);
         temp = f[(size_t)k * (n1 + 1) + i] - temp;
         rc[GIX(i, k, ld)] = temp;
         temp = fabs(temp);
@@ -348,6 +361,308 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision (GB_PRB_MIXED): FP64 defect correction around the
+// reference's sweep schedule run in FP32 on the correction equation A e = r.
+// A dependent FP32 operation costs a few cycles where an FP64 one costs tens
+// (and an FP64 division hundreds) on this part, and the line eliminations
+// are dependent chains, so the inner cycle runs an order of magnitude faster.
+// The FP32 line solves multiply by stored reciprocal pivots.
+// ---------------------------------------------------------------------------
+template <class Rhs>
+__device__ __forceinline__ void apply_pdma32(const float *fac, int n, float *x, Rhs rhs)
+{
+    const float *icdiv = fac, *bk1 = fac + n, *aa = fac + 2 * n, *dn = fac + 3 * n, *en = fac + 4 * n;
+    const float icN = fac[5 * n];
+    float rk = rhs(0), rk1 = rhs(1);
+    for (int k = 0; k <= n - 2; ++k) {
+        rk = rk * icdiv[k];
+        x[k] = rk;
+        rk1 = rk1 - bk1[k] * rk;
+        float rk2 = 0.f;
+        if (k != n - 2) rk2 = rhs(k + 2) - aa[k + 2] * rk;
+        rk = rk1;
+        rk1 = rk2;
+    }
+    float x1 = rk * icN;
+    x[n - 1] = x1;
+    float x0 = x[n - 2] - dn[n - 2] * x1;
+    x[n - 2] = x0;
+    for (int j = n - 3; j >= 0; --j) {
+        const float xj = x[j] - dn[j] * x0 - en[j] * x1;
+        x[j] = xj;
+        x1 = x0;
+        x0 = xj;
+    }
+}
+
+template <class Rhs>
+__device__ __forceinline__ void apply_tdma32(const float *fac, int n, float *x, Rhs rhs)
+{
+    const float *fact = fac, *ibp = fac + n, *c = fac + 2 * n;
+    float prev = rhs(0);
+    x[0] = prev;
+    for (int j = 1; j < n; ++j) {
+        const float rj = rhs(j) - fact[j] * prev;
+        x[j] = rj;
+        prev = rj;
+    }
+    float y = prev * ibp[n - 1];
+    x[n - 1] = y;
+    for (int j = n - 2; j >= 0; --j) {
+        y = (x[j] - c[j] * y) * ibp[j];
+        x[j] = y;
+    }
+}
+
+__device__ __forceinline__ void mg_line32(const MgEq &E, const MgLevel &L, int k)
+{
+    const int ld = E.ld, n1 = L.n1, n3 = L.n3;
+    float *psif = E.psif32;
+    const float *f = L.f32, *rvq = L.rvq32;
+    const float hhpi = (float)L.hhpi;
+    const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
+    const int polar = E.polar;
+    auto rhs = [&](int j) -> float {
+        const int i = j + 1;
+        float t = -(psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi;
+        if (polar) t = t * rvq[i];
+        return t + f[(size_t)k * (n1 + 1) + i];
+    };
+    const int nrow = (E.which == 2) ? n1 : n1 - 1;
+    if (E.which == 2) apply_pdma32(L.fac32, n1, psif + GIX(1, k, ld), rhs);
+    else apply_tdma32(L.fac32, n1 - 1, psif + GIX(1, k, ld), rhs);
+    if (k == n3)
+        for (int i = 1; i <= nrow; ++i) psif[GIX(i, 0, ld)] = psif[GIX(i, k, ld)];
+}
+
+// relax2/relax3 of the correction cycle: line sweeps, residual into rc32,
+// psif32 packed into v32.
+__device__ void mg_relax32(const MgEq &E, int klev)
+{
+    const MgLevel &L = E.lev[klev];
+    const int ld = E.ld, n1 = L.n1, n3 = L.n3;
+    const float hhri = (float)L.hhri, hhpi = (float)L.hhpi, hri = (float)L.hri;
+    float *psif = E.psif32, *rc = E.rc32;
+    const int nrel = E.polar ? 3 : 1;
+    for (int irel = 0; irel < nrel; ++irel) {
+        if (E.mode == GB_SMOOTHER_LEX) {
+            if (threadIdx.x == 0)
+                for (int k = 1; k <= n3; ++k) mg_line32(E, L, k);
+            __syncthreads();
+        } else {
+            for (int parity = 1; parity >= 0; --parity) {
+                for (int t = threadIdx.x; t < n3 / 2; t += blockDim.x) mg_line32(E, L, 2 * t + 2 - parity);
+                __syncthreads();
+            }
+        }
+    }
+    const int nrow = (E.which == 2) ? n1 : n1 - 1;
+    const int tot = nrow * n3;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
+        const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
+        const float a = mg_apply_op<float>(psif, ld, i, k, ka, km, E.which, E.polar, n1, hhri, hhpi, hri, L.rvi32,
+                                           L.rvq32);
+        rc[GIX(i, k, ld)] = L.f32[(size_t)k * (n1 + 1) + i] - a;
+    }
+    __syncthreads();
+    const int tp = (n1 + 1) * (n3 + 1);
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int k = idx / (n1 + 1), i = idx - k * (n1 + 1);
+        L.v32[idx] = psif[GIX(i, k, ld)];
+    }
+    __syncthreads();
+}
+
+__device__ void mg_corser32(const MgEq &E, int klev)
+{
+    const int ld = E.ld;
+    const int n1c = E.lev[klev + 1].n1, n3c = E.lev[klev + 1].n3;
+    const float *rf = E.rc32;
+    float *psif = E.psif32, *fc = E.lev[klev + 1].f32;
+    const int tot = (n1c + 1) * (n3c + 1);
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int k = idx / (n1c + 1), i = idx - k * (n1c + 1);
+        psif[GIX(i, k, ld)] = 0.f;
+        float t = 0.f;
+        if (i >= 1 && i <= n1c - 1 && k >= 1 && k <= n3c - 1) {
+            const int ii = i + i, kk = k + k;
+            // full weighting: 1/4 centre, 1/8 edges, 1/16 corners
+            t = 0.25f * rf[GIX(ii, kk, ld)] +
+                0.125f * (rf[GIX(ii + 1, kk, ld)] + rf[GIX(ii - 1, kk, ld)] + rf[GIX(ii, kk + 1, ld)] +
+                          rf[GIX(ii, kk - 1, ld)]) +
+                0.0625f * (rf[GIX(ii + 1, kk + 1, ld)] + rf[GIX(ii + 1, kk - 1, ld)] + rf[GIX(ii - 1, kk + 1, ld)] +
+                           rf[GIX(ii - 1, kk - 1, ld)]);
+        } else if (E.polar && i >= 1 && i <= n1c - 1 && k == n3c) {
+            t = rf[GIX(i, k, ld)];
+        }
+        fc[idx] = t;
+    }
+    __syncthreads();
+}
+
+__device__ void mg_finer32(const MgEq &E, int klev)
+{
+    const int ld = E.ld;
+    const int n1c = E.lev[klev].n1;
+    const int n1f = E.lev[klev - 1].n1, n3f = E.lev[klev - 1].n3;
+    const float *vc = E.lev[klev].v32, *vf = E.lev[klev - 1].v32;
+    float *psif = E.psif32;
+    const int tot = (n1f + 1) * (n3f + 1);
+#define PC(ii, kk) vc[(size_t)(kk) * (n1c + 1) + (ii)]
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int k = idx / (n1f + 1), i = idx - k * (n1f + 1);
+        const int i1 = i / 2, k1 = k / 2;
+        float p;
+        if (i1 * 2 == i) {
+            if (k1 * 2 == k) p = PC(i1, k1);
+            else p = (PC(i1, k1) + PC(i1, k1 + 1)) * 0.5f;
+        } else {
+            if (k1 * 2 == k) p = (PC(i1, k1) + PC(i1 + 1, k1)) * 0.5f;
+            else p = (PC(i1, k1) + PC(i1 + 1, k1) + PC(i1, k1 + 1) + PC(i1 + 1, k1 + 1)) * 0.25f;
+        }
+        psif[GIX(i, k, ld)] = p + vf[idx];
+    }
+#undef PC
+    __syncthreads();
+}
+
+// One FP32 cycle of the reference's sweep schedule (relax on the finest
+// level, the FMG-flavoured down and up legs of PRB:1869-1893) on A e = r
+// from e = 0.
+__device__ void mg_cycle32(const MgEq &E)
+{
+    const int nlev = E.nlev;
+    mg_relax32(E, 1);
+    if (nlev > 1) {
+        for (int l = 1; l <= nlev - 1; ++l) {
+            mg_corser32(E, l);
+            mg_relax32(E, l + 1);
+        }
+        for (int ifmg = 0; ifmg <= nlev - 2; ++ifmg) {
+            for (int l = nlev; l >= nlev - ifmg; --l) {
+                mg_finer32(E, l);
+                mg_relax32(E, l - 1);
+            }
+            for (int l = nlev - ifmg - 1; l <= nlev - 1; ++l) {
+                mg_corser32(E, l);
+                mg_relax32(E, l + 1);
+            }
+        }
+        for (int l = nlev; l >= 2; --l) {
+            mg_finer32(E, l);
+            mg_relax32(E, l - 1);
+        }
+    }
+}
+
+// poisson2 / poisson3 in mixed precision.  psif holds the FP64 iterate.
+__global__ void __launch_bounds__(MG_THREADS) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
+{
+    __shared__ double s_red[33];
+    const MgEq &E = eqs[first_eq + blockIdx.x];
+    const MgLevel &L1 = E.lev[1];
+    const int ld = E.ld, np = E.np;
+    const int imax = (E.which == 2) ? E.nr + 1 : E.nr;
+    const int n1 = L1.n1, n3 = L1.n3;
+    double *psif = E.psif, *psi = E.psi, *psip = E.psip;
+    const int rows = imax + 1, tot = rows * (np + 1);
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int k = idx / rows, i = idx - k * rows;
+        const size_t c = GIX(i, k, ld);
+        psif[c] = 2.0 * psi[c] - psip[c];
+        if (i <= n1) L1.f[(size_t)k * (n1 + 1) + i] = E.rhs[c];
+    }
+    __syncthreads();
+    const int nrow = (E.which == 2) ? n1 : n1 - 1;
+    int status = GB_MAXSWEEPS, cycles = 0;
+    double res = 0.0;
+    for (int it = 0;; ++it) {
+        // FP64 residual of the iterate; its FP32 copy is the cycle's right-hand side
+        double m = 0.0;
+        int nan = 0;
+        for (int idx = threadIdx.x; idx < nrow * n3; idx += blockDim.x) {
+            const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
+            const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
+            const double a = mg_apply_op<double>(psif, ld, i, k, ka, km, E.which, E.polar, n1, L1.hhri, L1.hhpi,
+                                                 L1.hri, L1.rvi, L1.rvq);
+            const double r = L1.f[(size_t)k * (n1 + 1) + i] - a;
+            L1.f32[(size_t)k * (n1 + 1) + i] = (float)r;
+            const double ar = fabs(r);
+            if (ar != ar) nan = 1;
+            if (ar > m) m = ar;
+        }
+        nan = __syncthreads_or(nan);
+        res = blk_max(m, s_red);
+        if (nan) { status = GB_NAN; break; }
+        if (res < E.tolcon) { status = GB_OK; break; }
+        if (it == E.maxsweeps) break;
+        // e = 0 on the finest level, then one FP32 cycle
+        for (int idx = threadIdx.x; idx < (n1 + 2) * (n3 + 1); idx += blockDim.x) {
+            const int k = idx / (n1 + 2), i = idx - k * (n1 + 2);
+            E.psif32[GIX(i, k, ld)] = 0.f;
+        }
+        __syncthreads();
+        mg_cycle32(E);
+        const double w = (it == 0) ? 1.0 : E.sor;
+        for (int idx = threadIdx.x; idx < nrow * (n3 + 1); idx += blockDim.x) {
+            const int k = idx / nrow, i = idx - k * nrow + 1;
+            psif[GIX(i, k, ld)] += w * (double)E.psif32[GIX(i, k, ld)];
+        }
+        __syncthreads();
+        cycles = it + 1;
+    }
+    if (status == GB_OK) {
+        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            const int k = idx / rows, i = idx - k * rows;
+            const size_t c = GIX(i, k, ld);
+            psip[c] = psi[c];
+            psi[c] = (i == 0 || i == imax) ? 0.0 : psif[c];
+        }
+    }
+    if (threadIdx.x == 0) {
+        E.status[0] = status;
+        E.status[1] = cycles;
+        *E.resmax = res;
+        if (status == GB_NAN || (status == GB_MAXSWEEPS && E.stop_on_max)) *E.abort = 1;
+    }
+}
+
+// FP32 copies of the factors (pivots as reciprocals) and radii.
+__global__ void k_mg_factors32(MgEq eq)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int l = 1; l <= eq.nlev; ++l) {
+        const MgLevel &L = eq.lev[l];
+        const int n1 = L.n1;
+        float *f32 = L.fac32;
+        const double *f = L.fac;
+        if (eq.which == 2) {
+            const int n = n1;
+            for (int j = 0; j < n; ++j) {
+                f32[j] = (float)(1.0 / f[j]);                     // cdiv
+                f32[n + j] = (float)f[n + j];                     // bk1
+                f32[2 * n + j] = (float)f[2 * n + j];             // a
+                f32[3 * n + j] = (float)f[3 * n + j];             // d
+                f32[4 * n + j] = (float)f[4 * n + j];             // e
+            }
+            f32[5 * n] = (float)(1.0 / f[5 * n]);
+        } else {
+            const int n = n1 - 1;
+            for (int j = 0; j < n; ++j) {
+                f32[j] = (float)f[j];                             // fact
+                f32[n + j] = (float)(1.0 / f[n + j]);             // bp
+                f32[2 * n + j] = (float)f[2 * n + j];             // c
+            }
+        }
+        for (int i = 0; i <= n1 + 1; ++i) {
+            L.rvi32[i] = (float)L.rvi[i];
+            L.rvq32[i] = (float)L.rvq[i];
+        }
+    }
+}
+
 // Factored line matrices of every level (one thread), the coefficients of
 // relax2 (PRB:2128-2156) and relax3 (PRB:2421-2436); for the annulus those
 // of velvor2dnewsch3.4.f:2104-2131 and :2401-2408 with the per-row 1/r and
@@ -436,10 +751,12 @@ int prb_mg_create(gb_prb *h)
         return GB_ERR_INVALID;
     }
     // pool: per equation psif, rc (full) + per level v, f + factors; plus work
-    size_t per_eq = 2 * (size_t)ld * (np + 1);
+    size_t per_eq = 2 * (size_t)ld * (np + 1) + (size_t)ld * (np + 1) + 8;   // psif, rc; psif32 + rc32
     for (int l = 1; l <= nlev; ++l) {
         const int n1 = nr * 2 / (1 << l), n3 = np * 2 / (1 << l);
         per_eq += 2 * (size_t)(n1 + 1) * (n3 + 1) + 5 * (size_t)(n1 + 2) + 1 + 2 * (size_t)(n1 + 2);
+        // FP32: v32, f32, fac32, rvi32, rvq32 (counted in doubles, rounded up)
+        per_eq += ((2 * (size_t)(n1 + 1) * (n3 + 1) + 5 * (size_t)(n1 + 2) + 1 + 2 * (size_t)(n1 + 2)) + 1) / 2 + 4;
     }
     const size_t work = 8 * (size_t)(nr + 2);
     cudaError_t e = cudaMalloc(&h->mg_pool, sizeof(double) * (2 * per_eq + work));
@@ -459,6 +776,10 @@ int prb_mg_create(gb_prb *h)
         E.psif = base; base += (size_t)ld * (np + 1);
         E.rc = base; base += (size_t)ld * (np + 1);
         E.psic = E.rf = E.tempa = nullptr;
+        float *fbase = (float *)base;
+        E.psif32 = fbase; fbase += (size_t)ld * (np + 1);
+        E.rc32 = fbase; fbase += (size_t)ld * (np + 1);
+        base = (double *)(((uintptr_t)fbase + 15) & ~(uintptr_t)15);
         for (int l = 1; l <= nlev; ++l) {
             MgLevel &L = E.lev[l];
             L.n1 = nr * 2 / (1 << l);
@@ -475,6 +796,13 @@ int prb_mg_create(gb_prb *h)
             L.fac = base; base += 5 * (size_t)(L.n1 + 2) + 1;
             L.rvi = base; base += (size_t)(L.n1 + 2);
             L.rvq = base; base += (size_t)(L.n1 + 2);
+            float *fb = (float *)base;
+            L.v32 = fb; fb += sz;
+            L.f32 = fb; fb += sz;
+            L.fac32 = fb; fb += 5 * (size_t)(L.n1 + 2) + 1;
+            L.rvi32 = fb; fb += (size_t)(L.n1 + 2);
+            L.rvq32 = fb; fb += (size_t)(L.n1 + 2);
+            base = (double *)(((uintptr_t)fb + 15) & ~(uintptr_t)15);
         }
         E.psi = h->dev.f[q == 0 ? GB_F_vel : GB_F_uel];
         E.psip = h->dev.f[q == 0 ? GB_F_velp : GB_F_uelp];
@@ -483,6 +811,7 @@ int prb_mg_create(gb_prb *h)
         E.resmax = h->dev.mg_resmax + q;
         E.abort = h->dev.abort;
         k_mg_factors<<<1, 1>>>(E, wk);
+        k_mg_factors32<<<1, 1>>>(E);
     }
     e = cudaMalloc(&h->eq_dev, sizeof(MgEq) * 2);
     if (e != cudaSuccess) { gb_set_error("multigrid descriptors: %s", cudaGetErrorString(e)); return GB_ERR_ALLOC; }
@@ -514,7 +843,8 @@ int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s)
     const int first = do_v ? 0 : 1;
     const int n = (do_v ? 1 : 0) + (do_u ? 1 : 0);
     if (n == 0) return GB_OK;
-    k_mg_solve<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
+    if (h->p.precision == GB_PRB_MIXED) k_mg_solve_mixed<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
+    else k_mg_solve<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
     h->launches += 1;
     return GB_OK;
 }

@@ -33,6 +33,8 @@ SMOOTHER_LEX = 0
 SMOOTHER_ZEBRA = 1
 PRB_LAYER = 0
 PRB_ANNULUS = 1
+PRB_FP64 = 0
+PRB_MIXED = 1
 BATCH_FP64 = 0
 BATCH_MIXED = 1
 BATCH_EXEC_GRAPH = 0
@@ -49,7 +51,8 @@ class PrbParams(C.Structure):
     _fields_ = [("nr", C.c_int), ("np", C.c_int),
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
                 ("Ra", C.c_double), ("Pr", C.c_double), ("tolcon", C.c_double), ("sor", C.c_double),
-                ("maxsweeps", C.c_int), ("smoother", C.c_int), ("variant", C.c_int), ("Re", C.c_double)]
+                ("maxsweeps", C.c_int), ("smoother", C.c_int), ("variant", C.c_int), ("Re", C.c_double),
+                ("precision", C.c_int)]
 
 
 _dp = C.POINTER(C.c_double)

@@ -30,7 +30,7 @@ from . import lib as _L
 class PRB:
     def __init__(self, nr, np_, dt=1e-7, r0=0.5, rmax=1.0, xx=3.0, Ra=1e7, Pr=0.71,
                  tolcon=None, sor=1.2, maxsweeps=None, smoother=_L.SMOOTHER_LEX,
-                 variant=_L.PRB_LAYER, Re=0.0):
+                 variant=_L.PRB_LAYER, Re=0.0, precision=_L.PRB_FP64):
         L = _L.load()
         p = _L.PrbParams()
         if variant == _L.PRB_ANNULUS:
@@ -38,7 +38,7 @@ class PRB:
         else:
             L.gb_prb_default_params(C.byref(p), nr, np_)
         p.dt, p.r0, p.rmax, p.xx, p.Ra, p.Pr = dt, r0, rmax, xx, Ra, Pr
-        p.sor, p.smoother, p.Re = sor, smoother, Re
+        p.sor, p.smoother, p.Re, p.precision = sor, smoother, Re, precision
         if tolcon is not None:
             p.tolcon = tolcon
         if maxsweeps is not None:

@@ -81,7 +81,22 @@ typedef struct gb_prb_params {
     int smoother;    /* GB_SMOOTHER_LEX or GB_SMOOTHER_ZEBRA */
     int variant;     /* GB_PRB_LAYER or GB_PRB_ANNULUS */
     double Re;       /* rotational Reynolds number (COMMON /val/ Re; annulus only) */
+    int precision;   /* GB_PRB_FP64 (bit-exact) or GB_PRB_MIXED (FP32 cycles inside FP64 defect correction) */
 } gb_prb_params;
+
+/* Precision of the velocity multigrid solves.
+ *   GB_PRB_FP64:  the reference algorithm in FP64, bit-identical to it.
+ *   GB_PRB_MIXED: FP64 defect correction: each outer iteration forms the
+ *                 FP64 residual r = rhs - A psi on the finest level, stops
+ *                 when its max norm is below tolcon, and otherwise runs the
+ *                 reference's multigrid sweep schedule in FP32 on A e = r
+ *                 from e = 0 and updates psi += w e in FP64 (w = 1 on the
+ *                 first iteration, then the reference's over-relaxation
+ *                 1.2).  The sweep count reported is the number of FP32
+ *                 cycles.  Transport, Nusselt integrals and boundary
+ *                 conditions stay FP64. */
+#define GB_PRB_FP64  0
+#define GB_PRB_MIXED 1
 
 /* Geometry and physics of an instance.
  *   GB_PRB_LAYER:   the periodic plane layer of velvor2dperiodicrbconv.f
