@@ -436,6 +436,103 @@ __device__ __forceinline__ void mg_line32(const MgEq &E, const MgLevel &L, int k
         for (int i = 1; i <= nrow; ++i) psif[GIX(i, 0, ld)] = psif[GIX(i, k, ld)];
 }
 
+// Shared memory of the mixed-precision kernel: the level's FP32 factors,
+// then a buffer of lines stored [row][line] with an odd pitch, so that
+// lanes walking rows (staging) and threads walking their own line
+// (elimination) both hit distinct banks.
+#define MG32_FAC_FLOATS 8192                  // >= 5 n1 + 1 for n1 <= 1600
+#define MG32_LINE_FLOATS 24576                // 96 KB of lines
+#define MG32_SMEM_BYTES ((MG32_FAC_FLOATS + MG32_LINE_FLOATS) * 4)
+
+__device__ __forceinline__ void pdma32_smem(const float *fac, int n, float *x, int pitch)
+{
+    const float *icdiv = fac, *bk1 = fac + n, *aa = fac + 2 * n, *dn = fac + 3 * n, *en = fac + 4 * n;
+    float rk = x[0], rk1 = x[pitch];
+    for (int k = 0; k <= n - 2; ++k) {
+        const float xr = (k + 2 < n) ? x[(k + 2) * pitch] : 0.f;
+        rk = rk * icdiv[k];
+        x[k * pitch] = rk;
+        rk1 = rk1 - bk1[k] * rk;
+        const float rk2 = (k != n - 2) ? xr - aa[k + 2] * rk : 0.f;
+        rk = rk1;
+        rk1 = rk2;
+    }
+    float x1 = rk * fac[5 * n];
+    x[(n - 1) * pitch] = x1;
+    float x0 = x[(n - 2) * pitch] - dn[n - 2] * x1;
+    x[(n - 2) * pitch] = x0;
+    for (int j = n - 3; j >= 0; --j) {
+        const float xj = x[j * pitch] - dn[j] * x0 - en[j] * x1;
+        x[j * pitch] = xj;
+        x1 = x0;
+        x0 = xj;
+    }
+}
+
+__device__ __forceinline__ void tdma32_smem(const float *fac, int n, float *x, int pitch)
+{
+    const float *fact = fac, *ibp = fac + n, *c = fac + 2 * n;
+    float prev = x[0];
+    for (int j = 1; j < n; ++j) {
+        prev = x[j * pitch] - fact[j] * prev;
+        x[j * pitch] = prev;
+    }
+    float y = prev * ibp[n - 1];
+    x[(n - 1) * pitch] = y;
+    for (int j = n - 2; j >= 0; --j) {
+        y = (x[j * pitch] - c[j] * y) * ibp[j];
+        x[j * pitch] = y;
+    }
+}
+
+// One colour (lines k = 2t + 2 - parity) of the zebra line sweep of the
+// correction cycle, in batches of lines staged in shared memory: right-hand
+// sides in (coalesced along rows), one thread per line eliminates, solutions
+// out.
+__device__ void mg_colour32_smem(const MgEq &E, const MgLevel &L, int parity)
+{
+    extern __shared__ float s_mg32[];
+    float *sfac = s_mg32, *sline = s_mg32 + MG32_FAC_FLOATS;
+    const int ld = E.ld, n1 = L.n1, n3 = L.n3;
+    const int nrow = (E.which == 2) ? n1 : n1 - 1;
+    const int nfac = (E.which == 2) ? 5 * n1 + 1 : 3 * (n1 - 1);
+    for (int j = threadIdx.x; j < nfac; j += blockDim.x) sfac[j] = L.fac32[j];
+    float *psif = E.psif32;
+    const float *f = L.f32, *rvq = L.rvq32;
+    const float hhpi = (float)L.hhpi;
+    const int nlines = n3 / 2;
+    int B = MG32_LINE_FLOATS / nrow - 1;
+    if (B > nlines) B = nlines;
+    for (int b0 = 0; b0 < nlines; b0 += B) {
+        const int nb = (nlines - b0 < B) ? nlines - b0 : B;
+        const int pitch = nb | 1;
+        for (int j = threadIdx.x >> 5; j < nb; j += blockDim.x >> 5) {
+            const int k = 2 * (b0 + j) + 2 - parity;
+            const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
+            for (int i = 1 + (threadIdx.x & 31); i <= nrow; i += 32) {
+                float r = -(psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi;
+                if (E.polar) r = r * rvq[i];
+                sline[(i - 1) * pitch + j] = r + f[(size_t)k * (n1 + 1) + i];
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+            if (E.which == 2) pdma32_smem(sfac, n1, sline + j, pitch);
+            else tdma32_smem(sfac, n1 - 1, sline + j, pitch);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x >> 5; j < nb; j += blockDim.x >> 5) {
+            const int k = 2 * (b0 + j) + 2 - parity;
+            for (int i = 1 + (threadIdx.x & 31); i <= nrow; i += 32) {
+                const float v = sline[(i - 1) * pitch + j];
+                psif[GIX(i, k, ld)] = v;
+                if (k == n3) psif[GIX(i, 0, ld)] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // relax2/relax3 of the correction cycle: line sweeps, residual into rc32,
 // psif32 packed into v32.
 __device__ void mg_relax32(const MgEq &E, int klev)
@@ -451,16 +548,13 @@ __device__ void mg_relax32(const MgEq &E, int klev)
                 for (int k = 1; k <= n3; ++k) mg_line32(E, L, k);
             __syncthreads();
         } else {
-            for (int parity = 1; parity >= 0; --parity) {
-                for (int t = threadIdx.x; t < n3 / 2; t += blockDim.x) mg_line32(E, L, 2 * t + 2 - parity);
-                __syncthreads();
-            }
+            for (int parity = 1; parity >= 0; --parity) mg_colour32_smem(E, L, parity);
         }
     }
     const int nrow = (E.which == 2) ? n1 : n1 - 1;
     const int tot = nrow * n3;
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-        const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
+    for (int k = 1 + (threadIdx.x >> 5); k <= n3; k += blockDim.x >> 5)
+        for (int i = 1 + (threadIdx.x & 31); i <= nrow; i += 32) {
         const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
         const float a = mg_apply_op<float>(psif, ld, i, k, ka, km, E.which, E.polar, n1, hhri, hhpi, hri, L.rvi32,
                                            L.rvq32);
@@ -468,8 +562,9 @@ __device__ void mg_relax32(const MgEq &E, int klev)
     }
     __syncthreads();
     const int tp = (n1 + 1) * (n3 + 1);
-    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
-        const int k = idx / (n1 + 1), i = idx - k * (n1 + 1);
+    for (int k = threadIdx.x >> 5; k < (tp) / ((n1 + 1)); k += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i < (n1 + 1); i += 32) {
+            const int idx = k * (n1 + 1) + i;
         L.v32[idx] = psif[GIX(i, k, ld)];
     }
     __syncthreads();
@@ -482,8 +577,9 @@ __device__ void mg_corser32(const MgEq &E, int klev)
     const float *rf = E.rc32;
     float *psif = E.psif32, *fc = E.lev[klev + 1].f32;
     const int tot = (n1c + 1) * (n3c + 1);
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-        const int k = idx / (n1c + 1), i = idx - k * (n1c + 1);
+    for (int k = threadIdx.x >> 5; k < (tot) / ((n1c + 1)); k += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i < (n1c + 1); i += 32) {
+            const int idx = k * (n1c + 1) + i;
         psif[GIX(i, k, ld)] = 0.f;
         float t = 0.f;
         if (i >= 1 && i <= n1c - 1 && k >= 1 && k <= n3c - 1) {
@@ -511,8 +607,9 @@ __device__ void mg_finer32(const MgEq &E, int klev)
     float *psif = E.psif32;
     const int tot = (n1f + 1) * (n3f + 1);
 #define PC(ii, kk) vc[(size_t)(kk) * (n1c + 1) + (ii)]
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-        const int k = idx / (n1f + 1), i = idx - k * (n1f + 1);
+    for (int k = threadIdx.x >> 5; k < (tot) / ((n1f + 1)); k += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i < (n1f + 1); i += 32) {
+            const int idx = k * (n1f + 1) + i;
         const int i1 = i / 2, k1 = k / 2;
         float p;
         if (i1 * 2 == i) {
@@ -568,8 +665,9 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve_mixed(const MgEq *eqs, 
     const int n1 = L1.n1, n3 = L1.n3;
     double *psif = E.psif, *psi = E.psi, *psip = E.psip;
     const int rows = imax + 1, tot = rows * (np + 1);
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-        const int k = idx / rows, i = idx - k * rows;
+    for (int k = threadIdx.x >> 5; k < (tot) / (rows); k += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i < rows; i += 32) {
+            const int idx = k * rows + i;
         const size_t c = GIX(i, k, ld);
         psif[c] = 2.0 * psi[c] - psip[c];
         if (i <= n1) L1.f[(size_t)k * (n1 + 1) + i] = E.rhs[c];
@@ -582,6 +680,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve_mixed(const MgEq *eqs, 
         // FP64 residual of the iterate; its FP32 copy is the cycle's right-hand side
         double m = 0.0;
         int nan = 0;
+        // packed 1D mapping: partly filled warps cost a full FP64 issue slot
         for (int idx = threadIdx.x; idx < nrow * n3; idx += blockDim.x) {
             const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
             const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
@@ -599,8 +698,9 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve_mixed(const MgEq *eqs, 
         if (res < E.tolcon) { status = GB_OK; break; }
         if (it == E.maxsweeps) break;
         // e = 0 on the finest level, then one FP32 cycle
-        for (int idx = threadIdx.x; idx < (n1 + 2) * (n3 + 1); idx += blockDim.x) {
-            const int k = idx / (n1 + 2), i = idx - k * (n1 + 2);
+        for (int k = threadIdx.x >> 5; k < (n3 + 1); k += blockDim.x >> 5)
+            for (int i = threadIdx.x & 31; i < (n1 + 2); i += 32) {
+                const int idx = k * (n1 + 2) + i;
             E.psif32[GIX(i, k, ld)] = 0.f;
         }
         __syncthreads();
@@ -614,8 +714,9 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve_mixed(const MgEq *eqs, 
         cycles = it + 1;
     }
     if (status == GB_OK) {
-        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-            const int k = idx / rows, i = idx - k * rows;
+        for (int k = threadIdx.x >> 5; k < (tot) / (rows); k += blockDim.x >> 5)
+            for (int i = threadIdx.x & 31; i < rows; i += 32) {
+                const int idx = k * rows + i;
             const size_t c = GIX(i, k, ld);
             psip[c] = psi[c];
             psi[c] = (i == 0 || i == imax) ? 0.0 : psif[c];
@@ -746,6 +847,10 @@ int prb_mg_create(gb_prb *h)
     const int nr = p.nr, np = p.np, nlev = h->nlev;
     const int ld = h->dev.ld;
     const double dr = h->dev.dr, dp = h->dev.dp;
+    if (5 * nr + 1 > MG32_FAC_FLOATS || 2 * nr > MG32_LINE_FLOATS) {
+        gb_set_error("nr=%d exceeds the multigrid kernel's shared-memory line buffers", nr);
+        return GB_ERR_INVALID;
+    }
     if (np % (1 << nlev) != 0) {
         gb_set_error("np=%d must be divisible by 2^nlev=%d so that every multigrid level has an even number of lines", np, 1 << nlev);
         return GB_ERR_INVALID;
@@ -813,6 +918,8 @@ int prb_mg_create(gb_prb *h)
         k_mg_factors<<<1, 1>>>(E, wk);
         k_mg_factors32<<<1, 1>>>(E);
     }
+    e = cudaFuncSetAttribute(k_mg_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, MG32_SMEM_BYTES);
+    if (e != cudaSuccess) { gb_set_error("multigrid shared memory: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
     e = cudaMalloc(&h->eq_dev, sizeof(MgEq) * 2);
     if (e != cudaSuccess) { gb_set_error("multigrid descriptors: %s", cudaGetErrorString(e)); return GB_ERR_ALLOC; }
     cudaMemcpy(h->eq_dev, h->eq_host, sizeof(MgEq) * 2, cudaMemcpyHostToDevice);
@@ -843,7 +950,7 @@ int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s)
     const int first = do_v ? 0 : 1;
     const int n = (do_v ? 1 : 0) + (do_u ? 1 : 0);
     if (n == 0) return GB_OK;
-    if (h->p.precision == GB_PRB_MIXED) k_mg_solve_mixed<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
+    if (h->p.precision == GB_PRB_MIXED) k_mg_solve_mixed<<<n, MG_THREADS, MG32_SMEM_BYTES, s>>>(h->eq_dev, first);
     else k_mg_solve<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
     h->launches += 1;
     return GB_OK;
