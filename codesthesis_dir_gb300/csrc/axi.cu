@@ -1,0 +1,880 @@
+// Axisymmetric rotating annulus in the (r, z) meridional plane (rotann2.f,
+// "AXI") on the device: Dufort-Frankel vorticity, swirl-velocity and
+// temperature updates with the Arakawa Jacobian, Thom wall vorticity, the
+// inner-wall heat flux, and the streamfunction multigrid.
+//
+// Numerics: every expression keeps the reference's operation order and the
+// translation unit is compiled with -fmad=false, so the FP64 path is
+// bit-identical to the reference algorithm (and to the C oracle).
+//
+// Layout: each field is a column-major (0:ld-1, 0:nz) array with ld = nr+1,
+// the ten fields of an instance in one allocation.  The multigrid keeps the
+// full-size psif and rc arrays, per level the packed v / f slots, the
+// factored r-line matrix (one per level: its coefficients vary with r only)
+// and one factored z-line matrix per r-row (its diagonal holds -1/r^2).
+//
+// The multigrid solve is one persistent block: the sweep loop, every level
+// and the convergence test run in one launch.  LEX orders the lines as the
+// reference does (rows j = 1..n2-1, then columns i = 1..n1-1, rotann2.f:
+// 698-725) and one thread marches them; ZEBRA solves odd lines, then even
+// lines, one thread per line.
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "banded.cuh"
+#include "gbcommon.cuh"
+
+#define AXI_THREADS 512
+#define AXI_MAXLEV 8
+#define AX(i, j) ((size_t)(i) + (size_t)ld * (size_t)(j))
+
+struct AxiLevel {
+    int n1, n2, lf;           // sizes; lf = 2^l / 2 scales i into rval
+    double hr, hz, hhr, hhz;
+    double *v, *f;            // packed (n1+1)*(n2+1)
+    double *fac_r;            // r-line factors, 3 (n1-1)
+    double *fac_z;            // z-line factors, 3 (n2-1) for each i = 1..n1-1
+};
+
+struct AxiDev {
+    int nr, nz, ld, nlev, mode, maxsweeps, nrel;
+    double dt, dr, dz, r0, rmax, zmax, Ra, Re, Ptl;
+    double cf1, cf2, cf3, cf4, tolcon;
+    double *f[GB_A_COUNT];
+    double *rval;             // rotann2.f:626: rval(i) = i hr(1) + r0
+    double *psif, *rc;
+    AxiLevel lev[AXI_MAXLEV];
+    double *heat;
+    unsigned long long *errmax;   // bit patterns of the step's max |x - x_p|, x = omega, v, T
+    int *abort;               // 1: a solve failed; 2: the run reached the steady state
+    int *status;              // [0] poisson status, [1] sweeps
+    int *step_index;
+    double *nu_hist;
+    int *sweep_hist;
+    int hist_cap;
+    double nu_c, nu_d;        // httrans = trans * nu_c / nu_d
+};
+
+// ---------------------------------------------------------------------------
+// Transport
+// ---------------------------------------------------------------------------
+
+// arakawa, rotann2.f:432-459, at one interior point.
+__device__ __forceinline__ double arakawa_at(const double *psi, const double *th, int ld, int i, int j, double hx,
+                                             double hy)
+{
+    const int ip = i + 1, im = i - 1;
+    const double a = (psi[AX(ip, j)] - psi[AX(im, j)]) * (th[AX(i, j + 1)] - th[AX(i, j - 1)]) -
+                     (psi[AX(i, j + 1)] - psi[AX(i, j - 1)]) * (th[AX(ip, j)] - th[AX(im, j)]) +
+                     psi[AX(ip, j)] * (th[AX(ip, j + 1)] - th[AX(ip, j - 1)]) -
+                     psi[AX(im, j)] * (th[AX(im, j + 1)] - th[AX(im, j - 1)]) -
+                     psi[AX(i, j + 1)] * (th[AX(ip, j + 1)] - th[AX(im, j + 1)]) +
+                     psi[AX(i, j - 1)] * (th[AX(ip, j - 1)] - th[AX(im, j - 1)]) +
+                     th[AX(i, j + 1)] * (psi[AX(ip, j + 1)] - psi[AX(im, j + 1)]) -
+                     th[AX(i, j - 1)] * (psi[AX(ip, j - 1)] - psi[AX(im, j - 1)]) -
+                     th[AX(ip, j)] * (psi[AX(ip, j + 1)] - psi[AX(ip, j - 1)]) +
+                     th[AX(im, j)] * (psi[AX(im, j + 1)] - psi[AX(im, j - 1)]);
+    return a / (12.0 * hx * hy);
+}
+
+// vorticity (rotann2.f:268-316, what & 1) and velocity (rotann2.f:324-370,
+// what & 2) on the interior, one thread per point.
+__global__ void k_axi_vort_vel(AxiDev d, int what)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ni = d.nr - 1, nj = d.nz - 1;
+    if (t >= ni * nj || *d.abort) return;
+    const int i = t % ni + 1, j = t / ni + 1;
+    const int ld = d.ld;
+    const int ip = i + 1, im = i - 1, jp = j + 1, jm = j - 1;
+    const double dr = d.dr, dz = d.dz, Ptl = d.Ptl;
+    const double *phi = d.f[GB_A_phi], *omeg = d.f[GB_A_omeg], *vel = d.f[GB_A_vel], *theta = d.f[GB_A_theta];
+    const double RRP = d.Ra / d.Re / Ptl;
+    const double r = d.r0 + (double)i * dr;
+    const double A = d.cf1 + 1.0 / (2.0 * (r * r));
+    const double AA = d.cf2 - 1.0 / (2.0 * (r * r));
+    if (what & 1) {
+        const double arak = arakawa_at(phi, omeg, ld, i, j, dr, dz);
+        const double B = (1.0 / (2.0 * Ptl * r * dz)) *
+                         (phi[AX(i, j)] * (omeg[AX(i, jp)] - omeg[AX(i, jm)]) +
+                          omeg[AX(i, j)] * (phi[AX(i, jp)] - phi[AX(i, jm)]));
+        const double C = (1.0 / (Ptl * r * dz)) * vel[AX(i, j)] * (vel[AX(i, jp)] - vel[AX(i, jm)]);
+        const double D = d.Re * (vel[AX(i, jp)] - vel[AX(i, jm)]) / dz;
+        const double E = r * d.Ra * (theta[AX(i, jp)] - theta[AX(i, jm)]) / (2.0 * dz);
+        const double EE = RRP * vel[AX(i, j)] * (theta[AX(i, jp)] - theta[AX(i, jm)]) / dz +
+                          RRP * theta[AX(i, j)] * (vel[AX(i, jp)] - vel[AX(i, jm)]) / dz;
+        const double F = (omeg[AX(ip, j)] + omeg[AX(im, j)]) / (dr * dr);
+        const double G = (1.0 / (2.0 * r * dr)) * (omeg[AX(ip, j)] - omeg[AX(im, j)]);
+        const double H = (omeg[AX(i, jp)] + omeg[AX(i, jm)]) / (dz * dz);
+        d.f[GB_A_omegn][AX(i, j)] =
+            (AA * d.f[GB_A_omegp][AX(i, j)] + arak / Ptl + B + C + D - E - EE + F + G + H) / A;
+    }
+    if (what & 2) {
+        const double arak = arakawa_at(phi, vel, ld, i, j, dr, dz);
+        const double B = (1.0 / (2.0 * Ptl * r * dz)) *
+                         (vel[AX(i, j)] * (phi[AX(i, jp)] - phi[AX(i, jm)]) -
+                          phi[AX(i, j)] * (vel[AX(i, jp)] - vel[AX(i, jm)]));
+        const double C = d.Re * (phi[AX(i, jp)] - phi[AX(i, jm)]) / dz;
+        const double CC = -RRP * theta[AX(i, j)] * (phi[AX(i, jp)] - phi[AX(i, jm)]) / dz;
+        const double D = (vel[AX(ip, j)] + vel[AX(im, j)]) / (dr * dr);
+        const double E = (1.0 / (2.0 * r * dr)) * (vel[AX(ip, j)] - vel[AX(im, j)]);
+        const double F = (vel[AX(i, jp)] + vel[AX(i, jm)]) / (dz * dz);
+        d.f[GB_A_veln][AX(i, j)] = (AA * d.f[GB_A_velp][AX(i, j)] + arak / Ptl - B - C - CC + D + E + F) / A;
+    }
+}
+
+// temperature, rotann2.f:379-424: rows j = 0 and nz mirror their neighbour
+// and take no Jacobian.
+__global__ void k_axi_temperature(AxiDev d)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ni = d.nr - 1, nj = d.nz + 1;
+    if (t >= ni * nj || *d.abort) return;
+    const int i = t % ni + 1, j = t / ni;
+    const int ld = d.ld, nz = d.nz;
+    const double dr = d.dr, dz = d.dz;
+    const double *phi = d.f[GB_A_phi], *theta = d.f[GB_A_theta];
+    const int ip = i + 1, im = i - 1;
+    int jp = j + 1, jm = j - 1;
+    double arak;
+    if (j == 0) {
+        jm = jp;
+        arak = 0.0;
+    } else if (j == nz) {
+        jp = jm;
+        arak = 0.0;
+    } else {
+        arak = arakawa_at(phi, theta, ld, i, j, dr, dz);
+    }
+    const double r = d.r0 + (double)i * dr;
+    const double B = (1.0 / (2.0 * r * dz)) * phi[AX(i, j)] * (theta[AX(i, jp)] - theta[AX(i, jm)]);
+    const double C = (theta[AX(ip, j)] + theta[AX(im, j)]) / (dr * dr);
+    const double D = (1.0 / (2.0 * r * dr)) * (theta[AX(ip, j)] - theta[AX(im, j)]);
+    const double E = (theta[AX(i, jp)] + theta[AX(i, jm)]) / (dz * dz);
+    d.f[GB_A_thetan][AX(i, j)] = (d.cf4 * d.f[GB_A_thetap][AX(i, j)] + arak + B + C + D + E) / d.cf3;
+}
+
+// update, rotann2.f:497-539, one thread per point: Thom wall vorticity (the
+// r-walls written last own the corners), v = 0 on the walls, T = 0 / 1 on
+// the inner / outer wall, then the time levels rotate.  The steady-state
+// test's maxima of |x - x_p| (rotann2.f:162-180) are gathered here.
+__global__ void k_axi_update(AxiDev d)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nr = d.nr, nz = d.nz, ld = d.ld;
+    if (*d.abort) return;   // uniform over the grid
+    const bool live = t < (nr + 1) * (nz + 1);
+    double e[3] = {0.0, 0.0, 0.0};
+    if (live) {
+        const int i = t % (nr + 1), j = t / (nr + 1);
+        const size_t c = AX(i, j);
+        double *const *f = d.f;
+        const double *phi = f[GB_A_phi];
+        double on = f[GB_A_omegn][c], vn = f[GB_A_veln][c], tn = f[GB_A_thetan][c];
+        if (i == 0) {
+            on = 2.0 * phi[AX(1, j)] / (d.dr * d.dr);
+            vn = 0.0;
+            tn = 0.0;
+        } else if (i == nr) {
+            on = 2.0 * phi[AX(nr - 1, j)] / (d.dr * d.dr);
+            vn = 0.0;
+            tn = 1.0;
+        } else if (j == 0) {
+            on = 2.0 * phi[AX(i, 1)] / (d.dz * d.dz);
+            vn = 0.0;
+        } else if (j == nz) {
+            on = 2.0 * phi[AX(i, nz - 1)] / (d.dz * d.dz);
+            vn = 0.0;
+        }
+        f[GB_A_omegn][c] = on;
+        f[GB_A_veln][c] = vn;
+        f[GB_A_thetan][c] = tn;
+        const double o = f[GB_A_omeg][c], v = f[GB_A_vel][c], th = f[GB_A_theta][c];
+        f[GB_A_omegp][c] = o;
+        f[GB_A_omeg][c] = on;
+        f[GB_A_velp][c] = v;
+        f[GB_A_vel][c] = vn;
+        f[GB_A_thetap][c] = th;
+        f[GB_A_theta][c] = tn;
+        e[0] = fabs(on - o);
+        e[1] = fabs(vn - v);
+        e[2] = fabs(tn - th);
+    }
+    // non-negative doubles order like their bit patterns: warp maximum, then
+    // one atomic per warp
+    for (int q = 0; q < 3; ++q) {
+        unsigned long long m = (unsigned long long)__double_as_longlong(e[q]);
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_down_sync(0xffffffffu, m, o);
+            m = w > m ? w : m;
+        }
+        if ((threadIdx.x & 31) == 0) atomicMax(&d.errmax[q], m);
+    }
+}
+
+// heat, rotann2.f:468-487: the per-row terms in parallel, summed by one
+// thread in the reference's order.
+__global__ void k_axi_heat(AxiDev d)
+{
+    extern __shared__ double sh[];
+    if (*d.abort == 1) return;
+    const int ld = d.ld, nz = d.nz;
+    const double dr = d.dr, dz = d.dz;
+    const double *th = d.f[GB_A_theta];
+    for (int j = threadIdx.x; j <= nz; j += blockDim.x) {
+        const double div = (j == 0 || j == nz) ? 24.0 * dr : 12.0 * dr;
+        sh[j] = dz * (-25.0 * th[AX(0, j)] + 48.0 * th[AX(1, j)] - 36.0 * th[AX(2, j)] + 16.0 * th[AX(3, j)] -
+                      3.0 * th[AX(4, j)]) / div;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double trans = sh[0];
+        trans = trans + sh[nz];
+        for (int j = 1; j <= nz - 1; ++j) trans = trans + sh[j];
+        d.heat[0] = trans;
+    }
+}
+
+// Per-step bookkeeping: Nu and sweeps into the history, the steady-state
+// test (REAL*4 threshold 1e-6, rotann2.f:191) and its reset.
+__global__ void k_axi_record(AxiDev d)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (*d.abort) return;
+    const int s = *d.step_index;
+    if (s < d.hist_cap) {
+        d.nu_hist[s] = d.heat[0] * d.nu_c / d.nu_d;
+        d.sweep_hist[s] = d.status[1];
+    }
+    *d.step_index = s + 1;
+    const double tol = (double)1e-6f;
+    const double e1 = __longlong_as_double((long long)d.errmax[0]), e2 = __longlong_as_double((long long)d.errmax[1]),
+                 e3 = __longlong_as_double((long long)d.errmax[2]);
+    if (e1 < tol && e2 < tol && e3 < tol) *d.abort = 2;
+    d.errmax[0] = d.errmax[1] = d.errmax[2] = 0ull;
+}
+
+// ---------------------------------------------------------------------------
+// Streamfunction multigrid (rotann2.f:543-854)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double axi_blk_max(double v, double *s_red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = (lane < nw) ? s_red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+        if (lane == 0) s_red[32] = v;
+    }
+    __syncthreads();
+    const double r = s_red[32];
+    __syncthreads();
+    return r;
+}
+
+// r-line j of relax (rotann2.f:698-710).
+__device__ __forceinline__ void axi_rline(const AxiDev &d, const AxiLevel &L, int j)
+{
+    const int ld = d.ld, n1 = L.n1;
+    double *psif = d.psif;
+    const double *f = L.f;
+    const double hhz = L.hhz;
+    auto rhs = [&](int q) -> double {
+        const int i = q + 1;
+        return -(psif[AX(i, j + 1)] + psif[AX(i, j - 1)]) / hhz + f[(size_t)j * (n1 + 1) + i];
+    };
+    apply_tdma_rhs(L.fac_r, n1 - 1, psif + AX(1, j), 1, rhs);
+}
+
+// z-line i of relax (rotann2.f:712-725).
+__device__ __forceinline__ void axi_zline(const AxiDev &d, const AxiLevel &L, int i)
+{
+    const int ld = d.ld, n1 = L.n1, n2 = L.n2;
+    double *psif = d.psif;
+    const double *f = L.f;
+    const double hhr = L.hhr, hr = L.hr, rv = d.rval[i * L.lf];
+    auto rhs = [&](int q) -> double {
+        const int j = q + 1;
+        return -(psif[AX(i + 1, j)] + psif[AX(i - 1, j)]) / hhr + f[(size_t)j * (n1 + 1) + i] -
+               (psif[AX(i + 1, j)] - psif[AX(i - 1, j)]) * 0.5 / rv / hr;
+    };
+    apply_tdma_rhs(L.fac_z + (size_t)(i - 1) * 3 * (n2 - 1), n2 - 1, psif + AX(i, 1), ld, rhs);
+}
+
+// relax (rotann2.f:668-753): psif from v, nrel sweeps of r-lines then
+// z-lines with the residual after each, psif back into v.  Returns the last
+// residual max norm; *nan_out is set (block-uniform) on a NaN residual.
+__device__ double axi_relax(const AxiDev &d, int klev, double *s_red, int *nan_out)
+{
+    const AxiLevel &L = d.lev[klev];
+    const int ld = d.ld, n1 = L.n1, n2 = L.n2;
+    const double hhr = L.hhr, hhz = L.hhz, hr = L.hr;
+    double *psif = d.psif, *rc = d.rc;
+    const int tp = (n1 + 1) * (n2 + 1);
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        psif[AX(i, j)] = L.v[idx];
+    }
+    __syncthreads();
+    const double drdz = 2.0 * (1.0 / hhr + 1.0 / hhz);
+    double m = 0.0;
+    int nan = 0;
+    for (int irel = 0; irel < d.nrel; ++irel) {
+        if (d.mode == GB_SMOOTHER_LEX) {
+            if (threadIdx.x == 0)
+                for (int j = 1; j <= n2 - 1; ++j) axi_rline(d, L, j);
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int i = 1; i <= n1 - 1; ++i) axi_zline(d, L, i);
+            __syncthreads();
+        } else {
+            for (int par = 1; par >= 0; --par) {
+                for (int t = threadIdx.x; 2 * t + 2 - par <= n2 - 1; t += blockDim.x) axi_rline(d, L, 2 * t + 2 - par);
+                __syncthreads();
+            }
+            for (int par = 1; par >= 0; --par) {
+                for (int t = threadIdx.x; 2 * t + 2 - par <= n1 - 1; t += blockDim.x) axi_zline(d, L, 2 * t + 2 - par);
+                __syncthreads();
+            }
+        }
+        m = 0.0;
+        nan = 0;
+        const int ni = n1 - 1, tot = ni * (n2 - 1);
+        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            const int j = idx / ni + 1, i = idx - (j - 1) * ni + 1;
+            const double rv = d.rval[i * L.lf];
+            double temp = (psif[AX(i + 1, j)] + psif[AX(i - 1, j)]) / hhr +
+                          (psif[AX(i + 1, j)] - psif[AX(i - 1, j)]) * 0.5 / hr / rv -
+                          psif[AX(i, j)] / (rv * rv) + (psif[AX(i, j + 1)] + psif[AX(i, j - 1)]) / hhz -
+                          psif[AX(i, j)] * drdz;
+            temp = L.f[(size_t)j * (n1 + 1) + i] - temp;
+            rc[AX(i, j)] = temp;
+            temp = fabs(temp);
+            if (temp != temp) nan = 1;
+            if (temp > m) m = temp;
+        }
+        nan = __syncthreads_or(nan);
+        m = axi_blk_max(m, s_red);
+    }
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        L.v[idx] = psif[AX(i, j)];
+    }
+    __syncthreads();
+    *nan_out = nan;
+    return m;
+}
+
+// corser (rotann2.f:755-801): the nine-point restriction of rc into the
+// packed coarse right-hand side; the rows and columns the reference clears
+// (i = 0, n1c and j = 0, n1c: n1 of the coarse level in both directions)
+// are zero, and the coarse solution slot is cleared.
+__device__ void axi_corser(const AxiDev &d, int klev)
+{
+    const int ld = d.ld;
+    const int n1c = d.lev[klev + 1].n1, n2c = d.lev[klev + 1].n2;
+    const double *rf = d.rc;
+    double *fc = d.lev[klev + 1].f, *vc = d.lev[klev + 1].v;
+    const int tot = (n1c + 1) * (n2c + 1);
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1c + 1), i = idx - j * (n1c + 1);
+        double temp = 0.0;
+        if (i >= 1 && i <= n1c - 1 && j >= 1 && j <= n2c - 1 && j != n1c) {
+            const int ii = i + i, jj = j + j;
+            temp = rf[AX(ii, jj)];
+            temp = temp * 2.0 + rf[AX(ii + 1, jj)] + rf[AX(ii - 1, jj)];
+            temp = temp + rf[AX(ii, jj + 1)] + rf[AX(ii, jj - 1)];
+            temp = temp * 2.0 + rf[AX(ii + 1, jj + 1)] + rf[AX(ii - 1, jj - 1)];
+            temp = temp + rf[AX(ii + 1, jj - 1)] + rf[AX(ii - 1, jj + 1)];
+            temp = temp / 16.0;
+        }
+        fc[idx] = temp;
+        vc[idx] = 0.0;
+    }
+    __syncthreads();
+}
+
+// finer (rotann2.f:803-854): bilinear prolongation of the coarse solution
+// plus the saved fine solution into psif, the coarse slot cleared, psif
+// packed into the fine slot.
+__device__ void axi_finer(const AxiDev &d, int klev)
+{
+    const int ld = d.ld;
+    const int n1c = d.lev[klev].n1;
+    const int n1f = d.lev[klev - 1].n1, n2f = d.lev[klev - 1].n2;
+    const double *vc = d.lev[klev].v;
+    double *vf = d.lev[klev - 1].v, *psif = d.psif;
+    const int tot = (n1f + 1) * (n2f + 1);
+#define PC(ii, jj) vc[(size_t)(jj) * (n1c + 1) + (ii)]
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1f + 1), i = idx - j * (n1f + 1);
+        const int i1 = i / 2, j1 = j / 2;
+        double p;
+        if (i1 * 2 == i) {
+            if (j1 * 2 == j) p = PC(i1, j1);
+            else p = (PC(i1, j1) + PC(i1, j1 + 1)) * 0.5;
+        } else {
+            if (j1 * 2 == j) {
+                p = (PC(i1, j1) + PC(i1 + 1, j1)) * 0.5;
+            } else {
+                double temp = PC(i1, j1) + PC(i1 + 1, j1 + 1);
+                temp = temp + PC(i1, j1 + 1) + PC(i1 + 1, j1);
+                p = temp * 0.25;
+            }
+        }
+        psif[AX(i, j)] = p + vf[idx];
+    }
+#undef PC
+    __syncthreads();
+    const int tc = (n1c + 1) * (d.lev[klev].n2 + 1);
+    for (int idx = threadIdx.x; idx < tc; idx += blockDim.x) d.lev[klev].v[idx] = 0.0;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1f + 1), i = idx - j * (n1f + 1);
+        vf[idx] = psif[AX(i, j)];
+    }
+    __syncthreads();
+}
+
+// poisson (rotann2.f:598-666): phi from omegn.
+__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve(AxiDev d)
+{
+    __shared__ double s_red[33];
+    if (*d.abort) return;
+    const int ld = d.ld, nlev = d.nlev;
+    const AxiLevel &L1 = d.lev[1];
+    const int n1 = L1.n1, n2 = L1.n2;
+    double *psi = d.f[GB_A_phi];
+    const double *rhs = d.f[GB_A_omegn];
+    const int tp = (n1 + 1) * (n2 + 1);
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        L1.f[idx] = rhs[AX(i, j)];
+        L1.v[idx] = psi[AX(i, j)];
+        d.rc[AX(i, j)] = 0.0;
+    }
+    __syncthreads();
+    int status = GB_MAXSWEEPS, sweeps = d.maxsweeps, nan1 = 0, nn = 0;
+    double res1 = 0.0;
+    for (int sweep = 1; sweep <= d.maxsweeps; ++sweep) {
+        if (sweep == 1 || nlev == 1) res1 = axi_relax(d, 1, s_red, &nan1);
+        if (nlev > 1) {
+            for (int l = 1; l <= nlev - 1; ++l) {
+                axi_corser(d, l);
+                axi_relax(d, l + 1, s_red, &nn);
+            }
+            for (int l = nlev; l >= 2; --l) {
+                axi_finer(d, l);
+                const double r = axi_relax(d, l - 1, s_red, &nn);
+                if (l - 1 == 1) { res1 = r; nan1 = nn; }
+            }
+        }
+        if (nan1) { status = GB_NAN; sweeps = sweep; break; }
+        if (res1 < d.tolcon) {
+            for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+                const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+                psi[AX(i, j)] = d.psif[AX(i, j)];
+            }
+            status = GB_OK;
+            sweeps = sweep;
+            break;
+        }
+    }
+    if (threadIdx.x == 0) {
+        d.status[0] = status;
+        d.status[1] = sweeps;
+        if (status == GB_NAN) *d.abort = 1;
+    }
+}
+
+// rval and the factored line matrices of every level (one thread): the
+// coefficients relax forms for each line (rotann2.f:698-721).
+__global__ void k_axi_factors(AxiDev d, double *work)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int i = 0; i <= d.lev[1].n1; ++i) d.rval[i] = (double)i * d.lev[1].hr + d.r0;
+    for (int l = 1; l <= d.nlev; ++l) {
+        const AxiLevel &L = d.lev[l];
+        const int n1 = L.n1, n2 = L.n2;
+        const double hhr = L.hhr, hhz = L.hhz, hr = L.hr;
+        const int nmax = (n1 > n2 ? n1 : n2) + 2;
+        double *a = work, *b = a + nmax, *c = b + nmax;
+        for (int i = 1; i <= n1 - 1; ++i) {
+            const double rv = d.rval[i * L.lf];
+            a[i - 1] = 1.0 / hhr - 0.5 / hr / rv;
+            c[i - 1] = 1.0 / hhr + 0.5 / hr / rv;
+            b[i - 1] = -2.0 / hhr - 2.0 / hhz - 1.0 / (rv * rv);
+        }
+        if (n1 - 1 >= 1) factor_tdma(a, b, c, n1 - 1, L.fac_r);
+        for (int i = 1; i <= n1 - 1; ++i) {
+            const double rv = d.rval[i * L.lf];
+            for (int j = 1; j <= n2 - 1; ++j) {
+                a[j - 1] = 1.0 / hhz;
+                c[j - 1] = 1.0 / hhz;
+                b[j - 1] = -2.0 / hhr - 2.0 / hhz - 1.0 / (rv * rv);
+            }
+            if (n2 - 1 >= 1) factor_tdma(a, b, c, n2 - 1, L.fac_z + (size_t)(i - 1) * 3 * (n2 - 1));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct gb_axi {
+    gb_axi_params p;
+    AxiDev dev;
+    double *fields = nullptr, *pool = nullptr;
+    void *small = nullptr, *hist = nullptr;
+    int hist_cap = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    gb_axi_params graph_params;
+};
+
+static int axi_levels(int nr, int nz)
+{
+    int nlev = 0, it = nr, it2 = nr, jt = nz, jt2 = nz;
+    for (int i = 2; i <= 8; ++i) {
+        it = it / 2;
+        jt = jt / 2;
+        if (it * 2 - it2 == 0 && jt * 2 - jt2 == 0) {
+            nlev = nlev + 1;
+            it2 = it;
+            jt2 = jt;
+        } else {
+            break;
+        }
+    }
+    if (nlev > 6) nlev = 6;
+    return nlev;
+}
+
+extern "C" void gb_axi_default_params(gb_axi_params *p, int nr, int nz)
+{
+    memset(p, 0, sizeof(*p));
+    p->nr = nr;
+    p->nz = nz;
+    p->dt = 1e-5;
+    p->r0 = 0.5;
+    p->rmax = 1.0;
+    p->zmax = 0.5;
+    p->Ra = 1e5;
+    p->Re = 1e2;
+    p->Pr = 1.0;
+    p->tolcon = 1.0e-6;
+    p->maxsweeps = 10000;
+    p->nrel = 2;
+    p->smoother = GB_SMOOTHER_LEX;
+    p->precision = GB_PRB_FP64;
+}
+
+static void axi_scalars(gb_axi *h)
+{
+    AxiDev &d = h->dev;
+    const gb_axi_params &p = h->p;
+    d.dt = p.dt;
+    d.r0 = p.r0;
+    d.rmax = p.rmax;
+    d.zmax = p.zmax;
+    d.Ra = p.Ra;
+    d.Re = p.Re;
+    d.Ptl = p.Pr;
+    d.dr = (p.rmax - p.r0) / (double)p.nr;
+    d.dz = p.zmax / (double)p.nz;
+    const double dr = d.dr, dz = d.dz, Ptl = p.Pr, dt = p.dt;
+    d.cf1 = 1.0 / (2.0 * Ptl * dt) + 1.0 / (dr * dr) + 1.0 / (dz * dz);
+    d.cf2 = 1.0 / (2.0 * Ptl * dt) - 1.0 / (dr * dr) - 1.0 / (dz * dz);
+    d.cf3 = 1.0 / (2.0 * dt) + 1.0 / (dr * dr) + 1.0 / (dz * dz);
+    d.cf4 = 1.0 / (2.0 * dt) - 1.0 / (dr * dr) - 1.0 / (dz * dz);
+    d.tolcon = p.tolcon;
+    d.maxsweeps = p.maxsweeps;
+    d.nrel = p.nrel;
+    d.mode = p.smoother;
+    d.nu_c = -p.r0 * log(p.r0 / p.rmax);
+    d.nu_d = p.zmax * p.rmax;
+}
+
+extern "C" int gb_axi_destroy(gb_axi *h)
+{
+    if (!h) return GB_OK;
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    cudaFree(h->fields);
+    cudaFree(h->pool);
+    cudaFree(h->small);
+    cudaFree(h->hist);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GB_OK;
+}
+
+extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out)
+{
+    if (!p || !out) { gb_set_error("gb_axi_create: null argument"); return GB_ERR_INVALID; }
+    *out = nullptr;
+    const int nr = p->nr, nz = p->nz;
+    const int nlev = axi_levels(nr, nz);
+    if (nlev_out) *nlev_out = nlev;
+    if (nr < 4 || nz < 4 || nlev < 1 || nr > 8192 || nz > 8192 || !(p->r0 > 0.0 && p->rmax > p->r0) ||
+        !(p->zmax > 0.0) || p->nrel < 1 || p->maxsweeps < 1 || p->Re == 0.0) {
+        gb_set_error("gb_axi_create: unsupported parameters (nr=%d nz=%d need both even with >= 1 multigrid level; "
+                     "0 < r0 < rmax, zmax > 0, Re != 0)", nr, nz);
+        return GB_ERR_INVALID;
+    }
+    if (p->precision != GB_PRB_FP64) {
+        gb_set_error("gb_axi_create: precision %d is not available for this geometry", p->precision);
+        return GB_ERR_INVALID;
+    }
+    gb_axi *h = new gb_axi();
+    h->p = *p;
+    AxiDev &d = h->dev;
+    memset(&d, 0, sizeof(d));
+    d.nr = nr;
+    d.nz = nz;
+    d.ld = nr + 1;
+    d.nlev = nlev;
+    axi_scalars(h);
+    const size_t fsz = (size_t)d.ld * (size_t)(nz + 1);
+    cudaError_t e = cudaMalloc(&h->fields, sizeof(double) * fsz * GB_A_COUNT);
+    if (e != cudaSuccess) { gb_set_error("gb_axi_create: %s", cudaGetErrorString(e)); delete h; return GB_ERR_ALLOC; }
+    cudaMemset(h->fields, 0, sizeof(double) * fsz * GB_A_COUNT);
+    for (int q = 0; q < GB_A_COUNT; ++q) d.f[q] = h->fields + (size_t)q * fsz;
+    // pool: rval, psif, rc, then per level v, f, fac_r, fac_z; work for the factors
+    size_t need = (size_t)(nr + 2) + 2 * fsz;
+    for (int l = 1; l <= nlev; ++l) {
+        const size_t n1 = (size_t)nr * 2 / ((size_t)1 << l), n2 = (size_t)nz * 2 / ((size_t)1 << l);
+        need += 2 * (n1 + 1) * (n2 + 1) + 3 * n1 + n1 * 3 * (n2 + 1);
+    }
+    const size_t work = 3 * (size_t)((nr > nz ? nr : nz) + 2);
+    e = cudaMalloc(&h->pool, sizeof(double) * (need + work));
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: multigrid pool"); return GB_ERR_ALLOC; }
+    cudaMemset(h->pool, 0, sizeof(double) * (need + work));
+    double *b = h->pool;
+    d.rval = b; b += nr + 2;
+    d.psif = b; b += fsz;
+    d.rc = b; b += fsz;
+    for (int l = 1; l <= nlev; ++l) {
+        AxiLevel &L = d.lev[l];
+        L.n1 = nr * 2 / (1 << l);
+        L.n2 = nz * 2 / (1 << l);
+        L.lf = (1 << l) / 2;
+        L.hr = d.dr * (double)(1 << l) / 2.0;
+        L.hz = d.dz * (double)(1 << l) / 2.0;
+        L.hhr = L.hr * L.hr;
+        L.hhz = L.hz * L.hz;
+        const size_t sz = (size_t)(L.n1 + 1) * (L.n2 + 1);
+        L.v = b; b += sz;
+        L.f = b; b += sz;
+        L.fac_r = b; b += 3 * (size_t)L.n1;
+        L.fac_z = b; b += (size_t)L.n1 * 3 * (size_t)(L.n2 + 1);
+    }
+    double *wk = h->pool + need;
+    e = cudaMalloc(&h->small, 4096);
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: state"); return GB_ERR_ALLOC; }
+    cudaMemset(h->small, 0, 4096);
+    char *sm = (char *)h->small;
+    d.heat = (double *)(sm + 0);
+    d.errmax = (unsigned long long *)(sm + 64);
+    d.abort = (int *)(sm + 128);
+    d.status = (int *)(sm + 192);
+    d.step_index = (int *)(sm + 256);
+    k_axi_factors<<<1, 1>>>(d, wk);
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: stream"); return GB_ERR_CUDA; }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { gb_set_error("gb_axi_create: %s", cudaGetErrorString(e)); gb_axi_destroy(h); return GB_ERR_CUDA; }
+    *out = h;
+    return GB_OK;
+}
+
+extern "C" int gb_axi_set_field(gb_axi *h, int field, const double *host, int ld)
+{
+    if (!h || !host || field < 0 || field >= GB_A_COUNT || ld < h->dev.nr + 1) {
+        gb_set_error("gb_axi_set_field: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    GB_CUDA_TRY(cudaMemcpy2DAsync(h->dev.f[field], sizeof(double) * h->dev.ld, host, sizeof(double) * (size_t)ld,
+                                  sizeof(double) * (h->dev.nr + 1), h->dev.nz + 1, cudaMemcpyHostToDevice, h->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_axi_get_field(gb_axi *h, int field, double *host, int ld)
+{
+    if (!h || !host || field < 0 || field >= GB_A_COUNT || ld < h->dev.nr + 1) {
+        gb_set_error("gb_axi_get_field: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    GB_CUDA_TRY(cudaMemcpy2DAsync(host, sizeof(double) * (size_t)ld, h->dev.f[field], sizeof(double) * h->dev.ld,
+                                  sizeof(double) * (h->dev.nr + 1), h->dev.nz + 1, cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GB_OK;
+}
+
+extern "C" void *gb_axi_stream(gb_axi *h) { return h ? (void *)h->stream : nullptr; }
+
+static const int AXI_TPB = 256;
+
+static void axi_launch_vort_vel(gb_axi *h, int what, cudaStream_t s)
+{
+    const int n = (h->dev.nr - 1) * (h->dev.nz - 1);
+    k_axi_vort_vel<<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev, what);
+}
+
+static void axi_launch_temperature(gb_axi *h, cudaStream_t s)
+{
+    const int n = (h->dev.nr - 1) * (h->dev.nz + 1);
+    k_axi_temperature<<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
+}
+
+static void axi_launch_update(gb_axi *h, cudaStream_t s)
+{
+    const int n = (h->dev.nr + 1) * (h->dev.nz + 1);
+    k_axi_update<<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
+}
+
+static void axi_launch_heat(gb_axi *h, cudaStream_t s)
+{
+    k_axi_heat<<<1, 256, sizeof(double) * (h->dev.nz + 1), s>>>(h->dev);
+}
+
+static void axi_launch_mg(gb_axi *h, cudaStream_t s) { k_axi_mg_solve<<<1, AXI_THREADS, 0, s>>>(h->dev); }
+
+static int axi_sync(gb_axi *h, const char *what)
+{
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) { gb_set_error("%s: %s", what, cudaGetErrorString(e)); return GB_ERR_CUDA; }
+    return GB_OK;
+}
+
+static void axi_begin(gb_axi *h)
+{
+    axi_scalars(h);
+    cudaMemsetAsync(h->dev.abort, 0, sizeof(int), h->stream);
+}
+
+extern "C" int gb_axi_vorticity(gb_axi *h)
+{
+    if (!h) return GB_ERR_INVALID;
+    axi_begin(h);
+    axi_launch_vort_vel(h, 1, h->stream);
+    return axi_sync(h, "gb_axi_vorticity");
+}
+
+extern "C" int gb_axi_velocity(gb_axi *h)
+{
+    if (!h) return GB_ERR_INVALID;
+    axi_begin(h);
+    axi_launch_vort_vel(h, 2, h->stream);
+    return axi_sync(h, "gb_axi_velocity");
+}
+
+extern "C" int gb_axi_temperature(gb_axi *h)
+{
+    if (!h) return GB_ERR_INVALID;
+    axi_begin(h);
+    axi_launch_temperature(h, h->stream);
+    return axi_sync(h, "gb_axi_temperature");
+}
+
+extern "C" int gb_axi_poisson(gb_axi *h, int *sweeps)
+{
+    if (!h) return GB_ERR_INVALID;
+    axi_begin(h);
+    axi_launch_mg(h, h->stream);
+    int st[2] = {0, 0};
+    GB_CUDA_TRY(cudaMemcpyAsync(st, h->dev.status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    int r = axi_sync(h, "gb_axi_poisson");
+    if (r != GB_OK) return r;
+    if (sweeps) *sweeps = st[1];
+    return st[0];
+}
+
+extern "C" int gb_axi_update(gb_axi *h)
+{
+    if (!h) return GB_ERR_INVALID;
+    axi_begin(h);
+    axi_launch_update(h, h->stream);
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.errmax, 0, 3 * sizeof(unsigned long long), h->stream));
+    return axi_sync(h, "gb_axi_update");
+}
+
+extern "C" int gb_axi_heat(gb_axi *h, double *trans)
+{
+    if (!h) return GB_ERR_INVALID;
+    axi_begin(h);
+    axi_launch_heat(h, h->stream);
+    double t = 0.0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&t, h->dev.heat, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    int r = axi_sync(h, "gb_axi_heat");
+    if (trans) *trans = t;
+    return r;
+}
+
+static int axi_build_graph(gb_axi *h)
+{
+    cudaGraph_t g;
+    GB_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    axi_launch_vort_vel(h, 3, h->stream);
+    axi_launch_temperature(h, h->stream);
+    axi_launch_mg(h, h->stream);
+    axi_launch_update(h, h->stream);
+    axi_launch_heat(h, h->stream);
+    k_axi_record<<<1, 32, 0, h->stream>>>(h->dev);
+    GB_CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+    GB_CUDA_TRY(cudaGraphInstantiate(&h->graph, g, 0));
+    cudaGraphDestroy(g);
+    return GB_OK;
+}
+
+extern "C" int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done)
+{
+    if (!h || nsteps < 0) { gb_set_error("gb_axi_step: invalid argument"); return GB_ERR_INVALID; }
+    if (steps_done) *steps_done = 0;
+    if (nsteps == 0) return GB_OK;
+    AxiDev &d = h->dev;
+    if (h->hist_cap < nsteps) {
+        cudaFree(h->hist);
+        h->hist = nullptr;
+        GB_CUDA_TRY(cudaMalloc(&h->hist, (sizeof(double) + sizeof(int)) * (size_t)nsteps));
+        h->hist_cap = nsteps;
+        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    }
+    d.nu_hist = (double *)h->hist;
+    d.sweep_hist = (int *)((double *)h->hist + h->hist_cap);
+    d.hist_cap = h->hist_cap;
+    if (memcmp(&h->graph_params, &h->p, sizeof(gb_axi_params)) != 0) {
+        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+        h->graph_params = h->p;
+        axi_scalars(h);
+    }
+    GB_CUDA_TRY(cudaMemsetAsync(d.abort, 0, sizeof(int), h->stream));
+    GB_CUDA_TRY(cudaMemsetAsync(d.step_index, 0, sizeof(int), h->stream));
+    GB_CUDA_TRY(cudaMemsetAsync(d.errmax, 0, 3 * sizeof(unsigned long long), h->stream));
+    int st;
+    if (!h->graph && (st = axi_build_graph(h)) != GB_OK) return st;
+    for (int s = 0; s < nsteps; ++s) GB_CUDA_TRY(cudaGraphLaunch(h->graph, h->stream));
+    int info[2] = {0, 0}, stat[2] = {0, 0};
+    GB_CUDA_TRY(cudaMemcpyAsync(&info[0], d.step_index, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(&info[1], d.abort, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(stat, d.status, sizeof(stat), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double> nuh(nsteps);
+    std::vector<int> swh(nsteps);
+    GB_CUDA_TRY(cudaMemcpyAsync(nuh.data(), d.nu_hist, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(swh.data(), d.sweep_hist, sizeof(int) * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    st = axi_sync(h, "gb_axi_step");
+    if (st != GB_OK) return st;
+    if (nu) memcpy(nu, nuh.data(), sizeof(double) * nsteps);
+    if (sweeps) memcpy(sweeps, swh.data(), sizeof(int) * nsteps);
+    if (steps_done) *steps_done = info[0];
+    if (info[1] == 1) {
+        gb_set_error("gb_axi_step: multigrid failed at step %d (status %d)", info[0] + 1, stat[0]);
+        return stat[0];
+    }
+    return GB_OK;
+}

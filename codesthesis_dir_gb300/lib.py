@@ -47,6 +47,17 @@ class GBError(RuntimeError):
         self.status = status
 
 
+AXI_FIELDS = ["phi", "omegn", "omeg", "omegp", "veln", "vel", "velp", "thetan", "theta", "thetap"]
+AXI_FIELD_ID = {n: i for i, n in enumerate(AXI_FIELDS)}
+
+
+class AxiParams(C.Structure):
+    _fields_ = [("nr", C.c_int), ("nz", C.c_int),
+                ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("zmax", C.c_double),
+                ("Ra", C.c_double), ("Re", C.c_double), ("Pr", C.c_double), ("tolcon", C.c_double),
+                ("maxsweeps", C.c_int), ("nrel", C.c_int), ("smoother", C.c_int), ("precision", C.c_int)]
+
+
 class PrbParams(C.Structure):
     _fields_ = [("nr", C.c_int), ("np", C.c_int),
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
@@ -80,6 +91,19 @@ SIGNATURES = [
     ("gb_prb_update", C.c_int, [_vp, C.POINTER(C.c_longlong)]),
     ("gb_prb_step", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     ("gb_prb_stream", _vp, [_vp]),
+    ("gb_axi_default_params", None, [C.POINTER(AxiParams), C.c_int, C.c_int]),
+    ("gb_axi_create", C.c_int, [C.POINTER(AxiParams), C.POINTER(_vp), _ip]),
+    ("gb_axi_destroy", C.c_int, [_vp]),
+    ("gb_axi_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
+    ("gb_axi_get_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
+    ("gb_axi_vorticity", C.c_int, [_vp]),
+    ("gb_axi_velocity", C.c_int, [_vp]),
+    ("gb_axi_temperature", C.c_int, [_vp]),
+    ("gb_axi_poisson", C.c_int, [_vp, _ip]),
+    ("gb_axi_update", C.c_int, [_vp]),
+    ("gb_axi_heat", C.c_int, [_vp, _dp]),
+    ("gb_axi_step", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
+    ("gb_axi_stream", _vp, [_vp]),
     ("gb_prb_bind_bounds", None, [C.c_int, C.c_int]),
     ("gb_prb_bind_smoother", None, [C.c_int]),
     ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),

@@ -210,6 +210,60 @@ void rhsu_(double *urh);                                        /* PRB:1679 */
 int gb_prb_last_status(void);
 int gb_prb_last_sweeps(void);
 
+/* ------------------------------------- axisymmetric annulus (rotann2.f) */
+/* The (r, z) meridional-plane rotating annulus of rotann2.f ("AXI"):
+ * vorticity omega, streamfunction phi, swirl velocity v and temperature
+ * theta on a vertex grid (0:nr, 0:nz), Dufort-Frankel transport with the
+ * Arakawa Jacobian (:268-459), Thom wall vorticity (:497-539), inner-wall
+ * heat flux (:468-487), and the streamfunction multigrid (:543-854:
+ * alternating r-line / z-line Gauss-Seidel, nine-point restriction,
+ * bilinear prolongation, plain V-cycle with nrel = 2, tolcon 1e-6, no STOP
+ * after nvs = 10000 sweeps).  Fields are column-major (0:ld-1, 0:nz) with
+ * ld >= nr+1 (the reference's ld is nrmax+1 = 129). */
+enum gb_axi_field {
+    GB_A_phi = 0, GB_A_omegn, GB_A_omeg, GB_A_omegp, GB_A_veln, GB_A_vel, GB_A_velp,
+    GB_A_thetan, GB_A_theta, GB_A_thetap, GB_A_COUNT
+};
+
+typedef struct gb_axi_params {
+    int nr, nz;          /* intervals in r and z (both even) */
+    double dt, r0, rmax, zmax;
+    double Ra, Re, Pr;   /* COMMON /val/ Ra, Re, Ptl */
+    double tolcon;       /* max-norm residual tolerance (1e-6, rotann2.f:689) */
+    int maxsweeps;       /* nvs (10000, rotann2.f:617) */
+    int nrel;            /* relaxations per level visit (2, rotann2.f:618-619) */
+    int smoother;        /* GB_SMOOTHER_LEX (the reference's order) or GB_SMOOTHER_ZEBRA */
+    int precision;       /* GB_PRB_FP64 or GB_PRB_MIXED (FP32 V-cycles in FP64 defect correction) */
+} gb_axi_params;
+
+typedef struct gb_axi gb_axi;
+
+/* Defaults of rotann2.f for an nr x nz grid (tolcon, nvs, nrel; LEX, FP64). */
+void gb_axi_default_params(gb_axi_params *p, int nr, int nz);
+/* Replaces poissoninit (rotann2.f:543) plus the COMMON storage; nlev_out
+ * (may be NULL) receives the level count (halvings while nr and nz stay
+ * even, capped at 6). */
+int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out);
+int gb_axi_destroy(gb_axi *h);
+int gb_axi_set_field(gb_axi *h, int field, const double *host, int ld);
+int gb_axi_get_field(gb_axi *h, int field, double *host, int ld);
+int gb_axi_vorticity(gb_axi *h);                     /* rotann2.f:268-316 */
+int gb_axi_velocity(gb_axi *h);                      /* rotann2.f:324-370 */
+int gb_axi_temperature(gb_axi *h);                   /* rotann2.f:379-424 */
+/* poisson(phi, omegn) (rotann2.f:598-666): GB_OK, or GB_MAXSWEEPS with phi
+ * untouched (the reference returns silently there). */
+int gb_axi_poisson(gb_axi *h, int *sweeps);
+int gb_axi_update(gb_axi *h);                        /* rotann2.f:497-539 */
+int gb_axi_heat(gb_axi *h, double *trans);           /* rotann2.f:468-487 */
+/* nsteps steps of the main loop (rotann2.f:147-194), one CUDA graph per
+ * step.  nu (nsteps, may be NULL) receives httrans = -r0 ln(r0/rmax) trans /
+ * (zmax rmax) per step, sweeps (nsteps) the multigrid sweep counts.  The
+ * reference stops when max |omega - omega_p|, |v - v_p| and |T - T_p| are
+ * all below the REAL*4 1e-6 (:191); the steps stop there too, and
+ * *steps_done (may be NULL) receives the number of steps taken. */
+int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done);
+void *gb_axi_stream(gb_axi *h);
+
 /* ------------------------------------------------ batched banded solvers */
 /* nlines independent systems with the same n; line l's element j sits at
  * base + l*line_stride + j*elem_stride in each array.  Device pointers.

@@ -59,6 +59,22 @@ class PRB(C.Structure):
                 [("clamp_count", C.c_long), ("variant", C.c_int), ("Re", C.c_double)])
 
 
+_AXI_FIELDS = ["phi", "omegn", "omeg", "omegp", "veln", "vel", "velp", "thetan", "theta", "thetap"]
+
+
+class AXI(C.Structure):
+    _fields_ = ([("nr", C.c_int), ("nz", C.c_int), ("ld", C.c_int)] +
+                [(n, C.c_double) for n in ("dt", "dr", "dz", "r0", "rmax", "zmax", "Ra", "Re", "Ptl",
+                                           "cf1", "cf2", "cf3", "cf4")] +
+                [(n, _dp) for n in _AXI_FIELDS] +
+                [("nlev", C.c_int), ("n1", C.c_int * 8), ("n2", C.c_int * 8),
+                 ("hr", C.c_double * 8), ("hz", C.c_double * 8), ("hhr", C.c_double * 8), ("hhz", C.c_double * 8),
+                 ("rval", _dp), ("v", _dp * 8), ("f", _dp * 8),
+                 ("psic", _dp), ("psif", _dp), ("rc", _dp), ("rf", _dp), ("tempa", _dp),
+                 ("tolcon", C.c_double), ("nrel", C.c_int), ("maxsweeps", C.c_int), ("mode", C.c_int),
+                 ("last_sweeps", C.c_int), ("last_resmax", C.c_double)])
+
+
 _lib = None
 
 
@@ -92,6 +108,21 @@ def lib():
         L.orc_prb_step.argtypes = [C.POINTER(PRB), C.POINTER(MG), C.POINTER(MG), C.c_int, _dp, _ip]
         L.orc_prb_step.restype = C.c_int
         L.orc_prb_initial.argtypes = [C.POINTER(PRB), C.c_int, C.c_ulonglong, C.c_double]
+        L.orc_axi_init.argtypes = [C.POINTER(AXI), C.c_int, C.c_int] + [C.c_double] * 7
+        L.orc_axi_init.restype = C.c_int
+        L.orc_axi_free.argtypes = [C.POINTER(AXI)]
+        L.orc_axi_initial.argtypes = [C.POINTER(AXI), C.c_int, C.c_ulonglong, C.c_double]
+        for nm in ("orc_axi_vorticity", "orc_axi_velocity", "orc_axi_temperature", "orc_axi_update"):
+            getattr(L, nm).argtypes = [C.POINTER(AXI)]
+        L.orc_axi_heat.argtypes = [C.POINTER(AXI)]
+        L.orc_axi_heat.restype = C.c_double
+        L.orc_axi_poisson.argtypes = [C.POINTER(AXI), _dp, _dp, _ip]
+        L.orc_axi_poisson.restype = C.c_int
+        L.orc_axi_step.argtypes = [C.POINTER(AXI), _dp, _ip, _ip]
+        L.orc_axi_step.restype = C.c_int
+        L.orc_axi_relax.argtypes = [C.POINTER(AXI), C.c_int, C.c_int, _ip]
+        L.orc_axi_corser.argtypes = [C.POINTER(AXI), C.c_int]
+        L.orc_axi_finer.argtypes = [C.POINTER(AXI), C.c_int]
         L.orc_batch_solve.argtypes = [C.c_int, _ip, C.POINTER(C.c_longlong), _dp, _dp, C.c_int,
                                       C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _ip, _dp]
         L.orc_batch_solve.restype = C.c_int
@@ -205,6 +236,46 @@ class OraclePRB:
             lib().orc_prb_free(C.byref(self.s))
             lib().orc_mg_free(C.byref(self.mgv))
             lib().orc_mg_free(C.byref(self.mgu))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OracleAXI:
+    """The axisymmetric annulus state of rotann2.f with its multigrid."""
+
+    def __init__(self, nr, nz, dt, r0, rmax, zmax, Ra, Re, Pr, mode=ORC_LEX, tolcon=None, maxsweeps=None):
+        L = lib()
+        self.s = AXI()
+        if L.orc_axi_init(C.byref(self.s), nr, nz, dt, r0, rmax, zmax, Ra, Re, Pr) != 0:
+            raise ValueError("invalid AXI size nr=%d nz=%d" % (nr, nz))
+        self.s.mode = mode
+        if tolcon is not None:
+            self.s.tolcon = tolcon
+        if maxsweeps is not None:
+            self.s.maxsweeps = maxsweeps
+
+    def field(self, name) -> np.ndarray:
+        p = getattr(self.s, name)
+        n = self.s.ld * (self.s.nz + 1)
+        return np.ctypeslib.as_array(p, shape=(n,)).reshape((self.s.nz + 1, self.s.ld)).T
+
+    def initial(self, kind=1, seed=0, amp=1e-3):
+        lib().orc_axi_initial(C.byref(self.s), kind, seed, amp)
+
+    def step(self):
+        nu = C.c_double()
+        sw = C.c_int()
+        conv = C.c_int()
+        st = lib().orc_axi_step(C.byref(self.s), C.byref(nu), C.byref(sw), C.byref(conv))
+        return st, nu.value, sw.value, bool(conv.value)
+
+    def close(self):
+        if self.s.phi:
+            lib().orc_axi_free(C.byref(self.s))
 
     def __del__(self):
         try:
