@@ -37,6 +37,8 @@ struct AxiLevel {
     double *v, *f;            // packed (n1+1)*(n2+1)
     double *fac_r;            // r-line factors, 3 (n1-1)
     double *fac_z;            // z-line factors, 3 (n2-1) for each i = 1..n1-1
+    // mixed precision: FP32 correction cycle (pivots stored as reciprocals)
+    float *v32, *f32, *fac_r32, *fac_z32;
 };
 
 struct AxiDev {
@@ -46,6 +48,7 @@ struct AxiDev {
     double *f[GB_A_COUNT];
     double *rval;             // rotann2.f:626: rval(i) = i hr(1) + r0
     double *psif, *rc;
+    float *psif32, *rc32, *rval32;
     AxiLevel lev[AXI_MAXLEV];
     double *heat;
     unsigned long long *errmax;   // bit patterns of the step's max |x - x_p|, x = omega, v, T
@@ -491,6 +494,281 @@ __global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve(AxiDev d)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision: FP64 defect correction around one FP32 V-cycle of the
+// reference's schedule (relax on the finest level, down, up) on A e = r from
+// e = 0; psi += e in FP64 (AXI has no over-relaxation).  Zebra colours stage
+// their lines in shared memory ([row][line], odd pitch) for the elimination.
+// ---------------------------------------------------------------------------
+#define AX32_LINE_FLOATS 24576
+#define AX32_SMEM_BYTES (AX32_LINE_FLOATS * 4)
+
+__device__ __forceinline__ void tdma32_pitch(const float *fac, int n, float *x, int pitch)
+{
+    const float *fact = fac, *ibp = fac + n, *c = fac + 2 * n;
+    float prev = x[0];
+    for (int j = 1; j < n; ++j) {
+        prev = x[j * pitch] - fact[j] * prev;
+        x[j * pitch] = prev;
+    }
+    float y = prev * ibp[n - 1];
+    x[(n - 1) * pitch] = y;
+    for (int j = n - 2; j >= 0; --j) {
+        y = (x[j * pitch] - c[j] * y) * ibp[j];
+        x[j * pitch] = y;
+    }
+}
+
+// right-hand side of r-line j (dir 0) or z-line i (dir 1) at row q+1
+__device__ __forceinline__ float axi_rhs32(const AxiDev &d, const AxiLevel &L, int dir, int line, int q)
+{
+    const int ld = d.ld, n1 = L.n1;
+    const float *psif = d.psif32;
+    if (dir == 0) {
+        const int i = q + 1, j = line;
+        return -(psif[AX(i, j + 1)] + psif[AX(i, j - 1)]) / (float)L.hhz + L.f32[(size_t)j * (n1 + 1) + i];
+    }
+    const int i = line, j = q + 1;
+    const float rv = d.rval32[i * L.lf];
+    return -(psif[AX(i + 1, j)] + psif[AX(i - 1, j)]) / (float)L.hhr + L.f32[(size_t)j * (n1 + 1) + i] -
+           (psif[AX(i + 1, j)] - psif[AX(i - 1, j)]) * 0.5f / rv / (float)L.hr;
+}
+
+// one colour of zebra lines in direction dir, staged in shared memory
+__device__ void axi_colour32(const AxiDev &d, const AxiLevel &L, int dir, int parity)
+{
+    extern __shared__ float s_ax32[];
+    const int ld = d.ld;
+    const int nlen = dir == 0 ? L.n1 - 1 : L.n2 - 1;       // rows of a line
+    const int nl_all = dir == 0 ? L.n2 - 1 : L.n1 - 1;     // lines 1..nl_all
+    const int nlines = (nl_all + parity) / 2;              // lines 2t + 2 - parity
+    int B = AX32_LINE_FLOATS / nlen - 1;
+    if (B > nlines) B = nlines;
+    for (int b0 = 0; b0 < nlines; b0 += B) {
+        const int nb = (nlines - b0 < B) ? nlines - b0 : B;
+        const int pitch = nb | 1;
+        for (int t = threadIdx.x >> 5; t < nb; t += blockDim.x >> 5) {
+            const int line = 2 * (b0 + t) + 2 - parity;
+            for (int q = threadIdx.x & 31; q < nlen; q += 32) s_ax32[q * pitch + t] = axi_rhs32(d, L, dir, line, q);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+            const int line = 2 * (b0 + t) + 2 - parity;
+            const float *fac = dir == 0 ? L.fac_r32 : L.fac_z32 + (size_t)(line - 1) * 3 * nlen;
+            tdma32_pitch(fac, nlen, s_ax32 + t, pitch);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x >> 5; t < nb; t += blockDim.x >> 5) {
+            const int line = 2 * (b0 + t) + 2 - parity;
+            for (int q = threadIdx.x & 31; q < nlen; q += 32) {
+                const float v = s_ax32[q * pitch + t];
+                if (dir == 0) d.psif32[AX(q + 1, line)] = v;
+                else d.psif32[AX(line, q + 1)] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// one line of the lexicographic order, marched by one thread
+__device__ void axi_line32_lex(const AxiDev &d, const AxiLevel &L, int dir, int line)
+{
+    const int ld = d.ld;
+    const int nlen = dir == 0 ? L.n1 - 1 : L.n2 - 1;
+    const float *fac = dir == 0 ? L.fac_r32 : L.fac_z32 + (size_t)(line - 1) * 3 * nlen;
+    float *x = dir == 0 ? d.psif32 + AX(1, line) : d.psif32 + AX(line, 1);
+    const int stride = dir == 0 ? 1 : ld;
+    const float *fact = fac, *ibp = fac + nlen, *c = fac + 2 * nlen;
+    float prev = axi_rhs32(d, L, dir, line, 0);
+    x[0] = prev;
+    for (int q = 1; q < nlen; ++q) {
+        prev = axi_rhs32(d, L, dir, line, q) - fact[q] * prev;
+        x[(size_t)q * stride] = prev;
+    }
+    float y = prev * ibp[nlen - 1];
+    x[(size_t)(nlen - 1) * stride] = y;
+    for (int q = nlen - 2; q >= 0; --q) {
+        y = (x[(size_t)q * stride] - c[q] * y) * ibp[q];
+        x[(size_t)q * stride] = y;
+    }
+}
+
+__device__ void axi_relax32(const AxiDev &d, int klev)
+{
+    const AxiLevel &L = d.lev[klev];
+    const int ld = d.ld, n1 = L.n1, n2 = L.n2;
+    for (int j = threadIdx.x >> 5; j <= n2; j += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i <= n1; i += 32) d.psif32[AX(i, j)] = L.v32[(size_t)j * (n1 + 1) + i];
+    __syncthreads();
+    const float hhr = (float)L.hhr, hhz = (float)L.hhz, hr = (float)L.hr;
+    const float drdz = 2.0f * (1.0f / hhr + 1.0f / hhz);
+    for (int irel = 0; irel < d.nrel; ++irel) {
+        if (d.mode == GB_SMOOTHER_LEX) {
+            if (threadIdx.x == 0)
+                for (int j = 1; j <= n2 - 1; ++j) axi_line32_lex(d, L, 0, j);
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int i = 1; i <= n1 - 1; ++i) axi_line32_lex(d, L, 1, i);
+            __syncthreads();
+        } else {
+            for (int par = 1; par >= 0; --par) axi_colour32(d, L, 0, par);
+            for (int par = 1; par >= 0; --par) axi_colour32(d, L, 1, par);
+        }
+    }
+    const float *psif = d.psif32;
+    for (int j = 1 + (threadIdx.x >> 5); j <= n2 - 1; j += blockDim.x >> 5)
+        for (int i = 1 + (threadIdx.x & 31); i <= n1 - 1; i += 32) {
+            const float rv = d.rval32[i * L.lf];
+            const float a = (psif[AX(i + 1, j)] + psif[AX(i - 1, j)]) / hhr +
+                            (psif[AX(i + 1, j)] - psif[AX(i - 1, j)]) * 0.5f / hr / rv - psif[AX(i, j)] / (rv * rv) +
+                            (psif[AX(i, j + 1)] + psif[AX(i, j - 1)]) / hhz - psif[AX(i, j)] * drdz;
+            d.rc32[AX(i, j)] = L.f32[(size_t)j * (n1 + 1) + i] - a;
+        }
+    for (int j = threadIdx.x >> 5; j <= n2; j += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i <= n1; i += 32) L.v32[(size_t)j * (n1 + 1) + i] = psif[AX(i, j)];
+    __syncthreads();
+}
+
+__device__ void axi_corser32(const AxiDev &d, int klev)
+{
+    const int ld = d.ld;
+    const int n1c = d.lev[klev + 1].n1, n2c = d.lev[klev + 1].n2;
+    const float *rf = d.rc32;
+    float *fc = d.lev[klev + 1].f32, *vc = d.lev[klev + 1].v32;
+    for (int j = threadIdx.x >> 5; j <= n2c; j += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i <= n1c; i += 32) {
+            float t = 0.f;
+            if (i >= 1 && i <= n1c - 1 && j >= 1 && j <= n2c - 1 && j != n1c) {
+                const int ii = i + i, jj = j + j;
+                t = 0.25f * rf[AX(ii, jj)] +
+                    0.125f * (rf[AX(ii + 1, jj)] + rf[AX(ii - 1, jj)] + rf[AX(ii, jj + 1)] + rf[AX(ii, jj - 1)]) +
+                    0.0625f * (rf[AX(ii + 1, jj + 1)] + rf[AX(ii - 1, jj - 1)] + rf[AX(ii + 1, jj - 1)] +
+                               rf[AX(ii - 1, jj + 1)]);
+            }
+            fc[(size_t)j * (n1c + 1) + i] = t;
+            vc[(size_t)j * (n1c + 1) + i] = 0.f;
+        }
+    __syncthreads();
+}
+
+__device__ void axi_finer32(const AxiDev &d, int klev)
+{
+    const int ld = d.ld;
+    const int n1c = d.lev[klev].n1, n2c = d.lev[klev].n2;
+    const int n1f = d.lev[klev - 1].n1, n2f = d.lev[klev - 1].n2;
+    const float *vc = d.lev[klev].v32;
+    float *vf = d.lev[klev - 1].v32, *psif = d.psif32;
+#define PC32(ii, jj) vc[(size_t)(jj) * (n1c + 1) + (ii)]
+    for (int j = threadIdx.x >> 5; j <= n2f; j += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i <= n1f; i += 32) {
+            const int i1 = i / 2, j1 = j / 2;
+            float p;
+            if (i1 * 2 == i) p = (j1 * 2 == j) ? PC32(i1, j1) : (PC32(i1, j1) + PC32(i1, j1 + 1)) * 0.5f;
+            else if (j1 * 2 == j) p = (PC32(i1, j1) + PC32(i1 + 1, j1)) * 0.5f;
+            else p = (PC32(i1, j1) + PC32(i1 + 1, j1 + 1) + PC32(i1, j1 + 1) + PC32(i1 + 1, j1)) * 0.25f;
+            psif[AX(i, j)] = p + vf[(size_t)j * (n1f + 1) + i];
+        }
+#undef PC32
+    __syncthreads();
+    for (int q = threadIdx.x; q < (n1c + 1) * (n2c + 1); q += blockDim.x) d.lev[klev].v32[q] = 0.f;
+    for (int j = threadIdx.x >> 5; j <= n2f; j += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i <= n1f; i += 32) vf[(size_t)j * (n1f + 1) + i] = psif[AX(i, j)];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve_mixed(AxiDev d)
+{
+    __shared__ double s_red[33];
+    if (*d.abort) return;
+    const int ld = d.ld, nlev = d.nlev;
+    const AxiLevel &L1 = d.lev[1];
+    const int n1 = L1.n1, n2 = L1.n2;
+    double *psi = d.f[GB_A_phi], *psif = d.psif;
+    const double *rhs = d.f[GB_A_omegn];
+    for (int idx = threadIdx.x; idx < (n1 + 1) * (n2 + 1); idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        L1.f[idx] = rhs[AX(i, j)];
+        psif[AX(i, j)] = psi[AX(i, j)];
+    }
+    __syncthreads();
+    const double hhr = L1.hhr, hhz = L1.hhz, hr = L1.hr;
+    const double drdz = 2.0 * (1.0 / hhr + 1.0 / hhz);
+    const int ni = n1 - 1, tot = ni * (n2 - 1);
+    int status = GB_MAXSWEEPS, cycles = 0;
+    for (int it = 0;; ++it) {
+        // FP64 residual of the iterate (the relax residual, rotann2.f:727-741)
+        double m = 0.0;
+        int nan = 0;
+        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            const int j = idx / ni + 1, i = idx - (j - 1) * ni + 1;
+            const double rv = d.rval[i];
+            double temp = (psif[AX(i + 1, j)] + psif[AX(i - 1, j)]) / hhr +
+                          (psif[AX(i + 1, j)] - psif[AX(i - 1, j)]) * 0.5 / hr / rv - psif[AX(i, j)] / (rv * rv) +
+                          (psif[AX(i, j + 1)] + psif[AX(i, j - 1)]) / hhz - psif[AX(i, j)] * drdz;
+            temp = L1.f[(size_t)j * (n1 + 1) + i] - temp;
+            L1.f32[(size_t)j * (n1 + 1) + i] = (float)temp;
+            temp = fabs(temp);
+            if (temp != temp) nan = 1;
+            if (temp > m) m = temp;
+        }
+        nan = __syncthreads_or(nan);
+        const double res = axi_blk_max(m, s_red);
+        if (nan) { status = GB_NAN; break; }
+        if (res < d.tolcon) { status = GB_OK; break; }
+        if (it == d.maxsweeps) break;
+        for (int q = threadIdx.x; q < (n1 + 1) * (n2 + 1); q += blockDim.x) L1.v32[q] = 0.f;
+        __syncthreads();
+        axi_relax32(d, 1);
+        if (nlev > 1) {
+            for (int l = 1; l <= nlev - 1; ++l) {
+                axi_corser32(d, l);
+                axi_relax32(d, l + 1);
+            }
+            for (int l = nlev; l >= 2; --l) {
+                axi_finer32(d, l);
+                axi_relax32(d, l - 1);
+            }
+        }
+        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            const int j = idx / ni + 1, i = idx - (j - 1) * ni + 1;
+            psif[AX(i, j)] += (double)L1.v32[(size_t)j * (n1 + 1) + i];
+        }
+        __syncthreads();
+        cycles = it + 1;
+    }
+    if (status == GB_OK)
+        for (int idx = threadIdx.x; idx < (n1 + 1) * (n2 + 1); idx += blockDim.x) {
+            const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+            psi[AX(i, j)] = psif[AX(i, j)];
+        }
+    if (threadIdx.x == 0) {
+        d.status[0] = status;
+        d.status[1] = cycles;
+        if (status == GB_NAN) *d.abort = 1;
+    }
+}
+
+// FP32 copies of rval and the factors (pivots as reciprocals).
+__global__ void k_axi_factors32(AxiDev d)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int i = 0; i <= d.lev[1].n1; ++i) d.rval32[i] = (float)d.rval[i];
+    for (int l = 1; l <= d.nlev; ++l) {
+        const AxiLevel &L = d.lev[l];
+        auto conv = [](const double *f, float *g, int n) {
+            for (int j = 0; j < n; ++j) {
+                g[j] = (float)f[j];
+                g[n + j] = (float)(1.0 / f[n + j]);
+                g[2 * n + j] = (float)f[2 * n + j];
+            }
+        };
+        if (L.n1 - 1 >= 1) conv(L.fac_r, L.fac_r32, L.n1 - 1);
+        if (L.n2 - 1 >= 1)
+            for (int i = 1; i <= L.n1 - 1; ++i)
+                conv(L.fac_z + (size_t)(i - 1) * 3 * (L.n2 - 1), L.fac_z32 + (size_t)(i - 1) * 3 * (L.n2 - 1), L.n2 - 1);
+    }
+}
+
 // rval and the factored line matrices of every level (one thread): the
 // coefficients relax forms for each line (rotann2.f:698-721).
 __global__ void k_axi_factors(AxiDev d, double *work)
@@ -625,8 +903,12 @@ extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out
                      "0 < r0 < rmax, zmax > 0, Re != 0)", nr, nz);
         return GB_ERR_INVALID;
     }
-    if (p->precision != GB_PRB_FP64) {
-        gb_set_error("gb_axi_create: precision %d is not available for this geometry", p->precision);
+    if (p->precision != GB_PRB_FP64 && p->precision != GB_PRB_MIXED) {
+        gb_set_error("gb_axi_create: unknown precision %d", p->precision);
+        return GB_ERR_INVALID;
+    }
+    if (2 * (nr > nz ? nr : nz) > AX32_LINE_FLOATS) {
+        gb_set_error("gb_axi_create: nr=%d nz=%d exceed the shared-memory line buffer", nr, nz);
         return GB_ERR_INVALID;
     }
     gb_axi *h = new gb_axi();
@@ -644,10 +926,11 @@ extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out
     cudaMemset(h->fields, 0, sizeof(double) * fsz * GB_A_COUNT);
     for (int q = 0; q < GB_A_COUNT; ++q) d.f[q] = h->fields + (size_t)q * fsz;
     // pool: rval, psif, rc, then per level v, f, fac_r, fac_z; work for the factors
-    size_t need = (size_t)(nr + 2) + 2 * fsz;
+    size_t need = (size_t)(nr + 2) + 2 * fsz + fsz + (size_t)(nr + 2) / 2 + 8;   // + psif32, rc32, rval32
     for (int l = 1; l <= nlev; ++l) {
         const size_t n1 = (size_t)nr * 2 / ((size_t)1 << l), n2 = (size_t)nz * 2 / ((size_t)1 << l);
-        need += 2 * (n1 + 1) * (n2 + 1) + 3 * n1 + n1 * 3 * (n2 + 1);
+        const size_t lv = 2 * (n1 + 1) * (n2 + 1) + 3 * n1 + n1 * 3 * (n2 + 1);
+        need += lv + (lv + 1) / 2 + 4;   // FP64 slots, then their FP32 copies
     }
     const size_t work = 3 * (size_t)((nr > nz ? nr : nz) + 2);
     e = cudaMalloc(&h->pool, sizeof(double) * (need + work));
@@ -657,6 +940,13 @@ extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out
     d.rval = b; b += nr + 2;
     d.psif = b; b += fsz;
     d.rc = b; b += fsz;
+    {
+        float *fb = (float *)b;
+        d.psif32 = fb; fb += fsz;
+        d.rc32 = fb; fb += fsz;
+        d.rval32 = fb; fb += nr + 2;
+        b = (double *)(((uintptr_t)fb + 15) & ~(uintptr_t)15);
+    }
     for (int l = 1; l <= nlev; ++l) {
         AxiLevel &L = d.lev[l];
         L.n1 = nr * 2 / (1 << l);
@@ -671,6 +961,17 @@ extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out
         L.f = b; b += sz;
         L.fac_r = b; b += 3 * (size_t)L.n1;
         L.fac_z = b; b += (size_t)L.n1 * 3 * (size_t)(L.n2 + 1);
+        float *fb = (float *)b;
+        L.v32 = fb; fb += sz;
+        L.f32 = fb; fb += sz;
+        L.fac_r32 = fb; fb += 3 * (size_t)L.n1;
+        L.fac_z32 = fb; fb += (size_t)L.n1 * 3 * (size_t)(L.n2 + 1);
+        b = (double *)(((uintptr_t)fb + 15) & ~(uintptr_t)15);
+    }
+    if ((size_t)(b - h->pool) > need) {
+        gb_axi_destroy(h);
+        gb_set_error("gb_axi_create: multigrid pool layout overflow");
+        return GB_ERR_CUDA;
     }
     double *wk = h->pool + need;
     e = cudaMalloc(&h->small, 4096);
@@ -683,6 +984,9 @@ extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out
     d.status = (int *)(sm + 192);
     d.step_index = (int *)(sm + 256);
     k_axi_factors<<<1, 1>>>(d, wk);
+    k_axi_factors32<<<1, 1>>>(d);
+    e = cudaFuncSetAttribute(k_axi_mg_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, AX32_SMEM_BYTES);
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: stream"); return GB_ERR_CUDA; }
     e = cudaDeviceSynchronize();
@@ -742,7 +1046,11 @@ static void axi_launch_heat(gb_axi *h, cudaStream_t s)
     k_axi_heat<<<1, 256, sizeof(double) * (h->dev.nz + 1), s>>>(h->dev);
 }
 
-static void axi_launch_mg(gb_axi *h, cudaStream_t s) { k_axi_mg_solve<<<1, AXI_THREADS, 0, s>>>(h->dev); }
+static void axi_launch_mg(gb_axi *h, cudaStream_t s)
+{
+    if (h->p.precision == GB_PRB_MIXED) k_axi_mg_solve_mixed<<<1, AXI_THREADS, AX32_SMEM_BYTES, s>>>(h->dev);
+    else k_axi_mg_solve<<<1, AXI_THREADS, 0, s>>>(h->dev);
+}
 
 static int axi_sync(gb_axi *h, const char *what)
 {
