@@ -328,6 +328,124 @@ def run_prb_workload(args, cfg):
     return 0
 
 
+# The axisymmetric annulus workload (rotann2.f physics): 257 x 257 vertices
+# (nr = nz = 256), radius ratio 0.5 and height = gap (r0 0.5, rmax 1, zmax
+# 0.5), Ra 1e8, Ta 1e5 as the rotational Reynolds number Re = sqrt(Ta)/2
+# (Ta = 4 Omega^2 d^4 / nu^2, Re = Omega d^2 / nu), Pr 1, dt 2e-7, the
+# conduction profile plus seeded noise of amplitude 1e-4; uniform grid.
+AXIWL = dict(nr=256, nz=256, dt=2e-7, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e8, Re=(1e5 ** 0.5) / 2.0, Pr=1.0,
+             tolcon=1e-6, amp=1e-4,
+             name="axisymmetric annulus 257 x 257 (nr = nz = 256), Ra 1e8, Ta 1e5 (Re 158.1), Pr 1, dt 2e-7, "
+                  "MG tolcon 1e-6, uniform grid")
+
+
+def axi_initial(cfg, seed=0):
+    """Conduction profile plus seeded noise (splitmix64 in j-major order over
+    rows i = 1..nr-1), as the oracle's kind-1 start."""
+    from codesthesis_dir_gb300 import initial
+    nr, nz = cfg["nr"], cfg["nz"]
+    dr = (cfg["rmax"] - cfg["r0"]) / nr
+    r = cfg["r0"] + np.arange(nr + 1) * dr
+    import math
+    base = np.array([1.0 - math.log(float(x) / cfg["rmax"]) / math.log(cfg["r0"] / cfg["rmax"]) for x in r])
+    u = (initial._splitmix64(seed, (nr - 1) * (nz + 1)) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    u = u.reshape(nz + 1, nr - 1).T
+    th = np.asfortranarray(np.repeat(base[:, None], nz + 1, axis=1))
+    th[1:nr, :] = base[1:nr, None] + cfg["amp"] * (2.0 * u - 1.0)
+    zero = np.zeros_like(th)
+    return {"theta": th, "thetap": th.copy(), "phi": zero, "omeg": zero, "omegp": zero, "vel": zero,
+            "velp": zero, "omegn": zero, "veln": zero, "thetan": zero}
+
+
+def time_axi_gpu(cfg, smoother, steps, warmup, precision=0):
+    import torch
+    from codesthesis_dir_gb300 import axi
+    g = axi.AXI(cfg["nr"], cfg["nz"], dt=cfg["dt"], r0=cfg["r0"], rmax=cfg["rmax"], zmax=cfg["zmax"], Ra=cfg["Ra"],
+                Re=cfg["Re"], Pr=cfg["Pr"], tolcon=cfg["tolcon"], smoother=smoother, precision=precision)
+    for n, a in axi_initial(cfg).items():
+        g.set(n, a)
+    s = torch.cuda.ExternalStream(g.stream())
+    nu_w = np.zeros(0)
+    if warmup:
+        nu_w, _ = g.step(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    nu, sw = g.step(steps)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    done = len(nu)
+    fields = {n: g.get(n) for n in ("phi", "omeg", "vel", "theta")}
+    g.close()
+    cells = (cfg["nr"] + 1) * (cfg["nz"] + 1)
+    return cells * done / (ms / 1e3), ms / max(done, 1), float(np.mean(sw)) if done else 0.0, \
+        np.concatenate([nu_w, nu]), fields
+
+
+def axi_summary(cfg, steps, steps_lex, warmup, cpu_budget):
+    out = {"workload": cfg["name"]}
+    runs = {}
+    for nm, sm, st, prec in (("fp64_zebra", 1, steps, 0), ("mixed_zebra", 1, steps, 1), ("fp64_lex", 0, steps_lex, 0)):
+        if st <= 0:
+            continue
+        v, ms, sw, nu, fields = time_axi_gpu(cfg, sm, st, warmup if sm == 1 else 1, prec)
+        runs[nm] = (nu, fields)
+        out[nm] = {"value": v, "unit": "cell-updates/s", "ms_per_step": ms, "steps": st,
+                   ("sweeps_mean" if prec == 0 else "fp32_cycles_mean"): sw, "nu_last": float(nu[-1])}
+    if "mixed_zebra" in runs and "fp64_zebra" in runs:
+        nu_m, f_m = runs["mixed_zebra"]
+        nu_d, f_d = runs["fp64_zebra"]
+        m = out["mixed_zebra"]
+        m["speedup_vs_fp64"] = m["value"] / out["fp64_zebra"]["value"]
+        m["nu_rel_err_vs_fp64"] = float(np.max(np.abs(nu_m - nu_d) / np.abs(nu_d)))
+        m["field_rel_l2_vs_fp64"] = {n: float(np.linalg.norm(f_m[n] - f_d[n]) / max(np.linalg.norm(f_d[n]), 1e-300))
+                                     for n in f_d}
+    if cpu_budget > 0:
+        from oracle import oracle as O
+        O.build()
+        o = O.OracleAXI(cfg["nr"], cfg["nz"], cfg["dt"], cfg["r0"], cfg["rmax"], cfg["zmax"], cfg["Ra"], cfg["Re"],
+                        cfg["Pr"], mode=0, tolcon=cfg["tolcon"])
+        o.initial(1, 0, cfg["amp"])
+        t0 = time.perf_counter()
+        n = 0
+        while n < 200 and time.perf_counter() - t0 < cpu_budget:
+            o.step()
+            n += 1
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": (cfg["nr"] + 1) * (cfg["nz"] + 1) * n / dt, "unit": "cell-updates/s",
+                               "cores": 1, "kind": "port",
+                               "sample": "%d steps of the same instance, oracle LEX (the reference's line order), "
+                                         "1 thread, %.1f s" % (n, dt)}
+    return out
+
+
+def run_axi_workload(args):
+    from codesthesis_dir_gb300 import lib
+    lib.load()
+    peak, peak_kind = measured_peaks()
+    with ClockSampler() as clk:
+        summ = axi_summary(AXIWL, args.steps, max(1, args.steps // 20), args.warmup,
+                           0 if args.no_cpu_baseline else 5.0)
+    mx, z = summ["mixed_zebra"], summ["fp64_zebra"]
+    line = {
+        "metric": "cell-updates/s (axisymmetric annulus step, mixed-precision streamfunction solve; FP64 beside)",
+        "value": mx["value"], "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer", "data": "synthetic",
+        "config": {"workload": AXIWL["name"], "smoother": "zebra",
+                   "l2": "working set (~6 MB) fits in L2; the step is latency and FP64-pipe bound"},
+        "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "note": "one-block multigrid on a 257 x 257 grid: chain-latency bound, see detail"},
+        "detail": summ, "clocks": clk.summary(),
+    }
+    if "cpu_baseline" in summ:
+        line["cpu_baseline"] = summ["cpu_baseline"]
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -368,11 +486,13 @@ def main():
     ap.add_argument("--mixed-only", action="store_true",
                     help="time only the mixed solve (for profiler launch lists); prints no JSON line")
     ap.add_argument("--no-layer", action="store_true", help="skip the 2D layer step measurement of the default run")
-    ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus"],
+    ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus", "axi"],
                     help="batch: 256 batched Poisson problems (the headline); layer / annulus: the 2D driver step")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "axi":
+        return run_axi_workload(args)
     if args.workload != "batch":
         return run_prb_workload(args, LAYER if args.workload == "layer" else ANNULUS)
 
