@@ -340,21 +340,9 @@ AXIWL = dict(nr=256, nz=256, dt=2e-7, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e8, Re=(1e
 
 
 def axi_initial(cfg, seed=0):
-    """Conduction profile plus seeded noise (splitmix64 in j-major order over
-    rows i = 1..nr-1), as the oracle's kind-1 start."""
-    from codesthesis_dir_gb300 import initial
-    nr, nz = cfg["nr"], cfg["nz"]
-    dr = (cfg["rmax"] - cfg["r0"]) / nr
-    r = cfg["r0"] + np.arange(nr + 1) * dr
-    import math
-    base = np.array([1.0 - math.log(float(x) / cfg["rmax"]) / math.log(cfg["r0"] / cfg["rmax"]) for x in r])
-    u = (initial._splitmix64(seed, (nr - 1) * (nz + 1)) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
-    u = u.reshape(nz + 1, nr - 1).T
-    th = np.asfortranarray(np.repeat(base[:, None], nz + 1, axis=1))
-    th[1:nr, :] = base[1:nr, None] + cfg["amp"] * (2.0 * u - 1.0)
-    zero = np.zeros_like(th)
-    return {"theta": th, "thetap": th.copy(), "phi": zero, "omeg": zero, "omegp": zero, "vel": zero,
-            "velp": zero, "omegn": zero, "veln": zero, "thetan": zero}
+    """Conduction profile plus seeded noise, the oracle's kind-1 start."""
+    from codesthesis_dir_gb300 import serve
+    return serve.axi_initial(cfg["nr"], cfg["nz"], cfg["r0"], cfg["rmax"], seed, cfg["amp"])
 
 
 def time_axi_gpu(cfg, smoother, steps, warmup, precision=0):
@@ -446,6 +434,50 @@ def run_axi_workload(args):
     return 0
 
 
+def run_serve_workload(args):
+    """--workload serve: the parameter sweep served by the continuous-batching
+    loop, FP64 and mixed precision on the same arrivals.  The sweep is a
+    bounded sample of the 512-request one: --requests requests with steps
+    drawn from --serve-steps instead of 500-5000; the four grids, the Ra, Pr
+    and Ta distributions and the Poisson arrivals at 50/s are as stated."""
+    from codesthesis_dir_gb300 import lib, serve
+    lib.load()
+    lo, hi = (int(x) for x in args.serve_steps.split(","))
+    reqs = serve.sweep_requests(n=args.requests, rate=50.0, seed=0, steps=(lo, hi))
+    out, res_by = {}, {}
+    with ClockSampler() as clk:
+        for name, prec in (("fp64", lib.PRB_FP64), ("mixed", lib.PRB_MIXED)):
+            srv = serve.Server(budget_bytes=120e9, max_active=args.max_active, chunk=16, precision=prec)
+            res = srv.run(reqs)
+            res_by[name] = res
+            out[name] = serve.summarize(reqs, res)
+            out[name]["peak_active"] = srv.peak_active
+            out[name]["peak_device_bytes_estimate"] = srv.peak_bytes
+    errs = []
+    for a, b in zip(res_by["fp64"], res_by["mixed"]):
+        if a.status == 0 and b.status == 0 and len(a.nu) and len(b.nu) == len(a.nu):
+            errs.append(float(np.max(np.abs(b.nu - a.nu) / np.maximum(np.abs(a.nu), 1e-300))))
+    m, f = out["mixed"], out["fp64"]
+    line = {
+        "metric": "served solves/s and p50/p99 time to solution (parameter sweep, mixed precision; FP64 beside)",
+        "value": m["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": len(reqs), "warmup": 0,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer", "data": "synthetic",
+        "config": {"workload": "served sweep: %d requests (layer or annulus), grids 65x33..513x257, Ra 1e4-1e8, "
+                               "Pr {0.7,1,7}, Ta 1-1e6, %d-%d steps, Poisson arrivals 50/s, 120 GB budget" % (
+                                   len(reqs), lo, hi),
+                   "max_active": args.max_active, "chunk_steps": 16},
+        "served": out,
+        "mixed_vs_fp64": {"solves_per_s_ratio": m["solves_per_s"] / f["solves_per_s"],
+                          "cell_updates_ratio": m["cell_updates_per_s"] / f["cell_updates_per_s"],
+                          "p50_ratio": f["tts_p50_s"] / m["tts_p50_s"], "p99_ratio": f["tts_p99_s"] / m["tts_p99_s"],
+                          "nu_max_rel_err": max(errs) if errs else None, "requests_compared": len(errs)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -486,13 +518,18 @@ def main():
     ap.add_argument("--mixed-only", action="store_true",
                     help="time only the mixed solve (for profiler launch lists); prints no JSON line")
     ap.add_argument("--no-layer", action="store_true", help="skip the 2D layer step measurement of the default run")
-    ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus", "axi"],
+    ap.add_argument("--requests", type=int, default=96, help="serve workload: number of requests")
+    ap.add_argument("--serve-steps", default="20,200", help="serve workload: step range lo,hi")
+    ap.add_argument("--max-active", type=int, default=128, help="serve workload: active slots")
+    ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus", "axi", "serve"],
                     help="batch: 256 batched Poisson problems (the headline); layer / annulus: the 2D driver step")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "axi":
         return run_axi_workload(args)
+    if args.workload == "serve":
+        return run_serve_workload(args)
     if args.workload != "batch":
         return run_prb_workload(args, LAYER if args.workload == "layer" else ANNULUS)
 

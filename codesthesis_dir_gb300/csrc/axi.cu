@@ -1140,17 +1140,17 @@ static int axi_build_graph(gb_axi *h)
     return GB_OK;
 }
 
-extern "C" int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done)
+// Asynchronous stepping (as for the 2D drivers).
+extern "C" int gb_axi_run_begin(gb_axi *h, int nsteps_total)
 {
-    if (!h || nsteps < 0) { gb_set_error("gb_axi_step: invalid argument"); return GB_ERR_INVALID; }
-    if (steps_done) *steps_done = 0;
-    if (nsteps == 0) return GB_OK;
+    if (!h || nsteps_total < 0) { gb_set_error("gb_axi_run_begin: invalid argument"); return GB_ERR_INVALID; }
     AxiDev &d = h->dev;
-    if (h->hist_cap < nsteps) {
+    const int cap = nsteps_total > 0 ? nsteps_total : 1;
+    if (h->hist_cap < cap) {
         cudaFree(h->hist);
         h->hist = nullptr;
-        GB_CUDA_TRY(cudaMalloc(&h->hist, (sizeof(double) + sizeof(int)) * (size_t)nsteps));
-        h->hist_cap = nsteps;
+        GB_CUDA_TRY(cudaMalloc(&h->hist, (sizeof(double) + sizeof(int)) * (size_t)cap));
+        h->hist_cap = cap;
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     }
     d.nu_hist = (double *)h->hist;
@@ -1164,18 +1164,43 @@ extern "C" int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *
     GB_CUDA_TRY(cudaMemsetAsync(d.abort, 0, sizeof(int), h->stream));
     GB_CUDA_TRY(cudaMemsetAsync(d.step_index, 0, sizeof(int), h->stream));
     GB_CUDA_TRY(cudaMemsetAsync(d.errmax, 0, 3 * sizeof(unsigned long long), h->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_axi_run_enqueue(gb_axi *h, int nsteps)
+{
+    if (!h || nsteps < 0) { gb_set_error("gb_axi_run_enqueue: invalid argument"); return GB_ERR_INVALID; }
     int st;
     if (!h->graph && (st = axi_build_graph(h)) != GB_OK) return st;
     for (int s = 0; s < nsteps; ++s) GB_CUDA_TRY(cudaGraphLaunch(h->graph, h->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_axi_run_query(gb_axi *h)
+{
+    if (!h) return -GB_ERR_INVALID;
+    const cudaError_t e = cudaStreamQuery(h->stream);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) { cudaGetLastError(); return 0; }
+    gb_set_error("gb_axi_run_query: %s", cudaGetErrorString(e));
+    return -GB_ERR_CUDA;
+}
+
+extern "C" int gb_axi_run_end(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done)
+{
+    if (!h || nsteps < 0 || nsteps > h->hist_cap) { gb_set_error("gb_axi_run_end: invalid argument"); return GB_ERR_INVALID; }
+    AxiDev &d = h->dev;
     int info[2] = {0, 0}, stat[2] = {0, 0};
     GB_CUDA_TRY(cudaMemcpyAsync(&info[0], d.step_index, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     GB_CUDA_TRY(cudaMemcpyAsync(&info[1], d.abort, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     GB_CUDA_TRY(cudaMemcpyAsync(stat, d.status, sizeof(stat), cudaMemcpyDeviceToHost, h->stream));
-    std::vector<double> nuh(nsteps);
-    std::vector<int> swh(nsteps);
-    GB_CUDA_TRY(cudaMemcpyAsync(nuh.data(), d.nu_hist, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, h->stream));
-    GB_CUDA_TRY(cudaMemcpyAsync(swh.data(), d.sweep_hist, sizeof(int) * nsteps, cudaMemcpyDeviceToHost, h->stream));
-    st = axi_sync(h, "gb_axi_step");
+    std::vector<double> nuh((size_t)nsteps + 1);
+    std::vector<int> swh((size_t)nsteps + 1);
+    if (nsteps > 0) {
+        GB_CUDA_TRY(cudaMemcpyAsync(nuh.data(), d.nu_hist, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, h->stream));
+        GB_CUDA_TRY(cudaMemcpyAsync(swh.data(), d.sweep_hist, sizeof(int) * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    }
+    int st = axi_sync(h, "gb_axi_run_end");
     if (st != GB_OK) return st;
     if (nu) memcpy(nu, nuh.data(), sizeof(double) * nsteps);
     if (sweeps) memcpy(sweeps, swh.data(), sizeof(int) * nsteps);
@@ -1185,4 +1210,15 @@ extern "C" int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *
         return stat[0];
     }
     return GB_OK;
+}
+
+extern "C" int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done)
+{
+    if (!h || nsteps < 0) { gb_set_error("gb_axi_step: invalid argument"); return GB_ERR_INVALID; }
+    if (steps_done) *steps_done = 0;
+    if (nsteps == 0) return GB_OK;
+    int st = gb_axi_run_begin(h, nsteps);
+    if (st == GB_OK) st = gb_axi_run_enqueue(h, nsteps);
+    if (st != GB_OK) return st;
+    return gb_axi_run_end(h, nsteps, nu, sweeps, steps_done);
 }

@@ -766,24 +766,27 @@ static int prb_build_graph(gb_prb *h, int first, cudaGraphExec_t *exec)
     return GB_OK;
 }
 
-extern "C" int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *sweeps)
+// Asynchronous stepping: run_begin sizes the history and resets the step
+// counters, run_enqueue queues graph launches on the instance's stream
+// without waiting, run_query polls it, run_end waits and collects.
+extern "C" int gb_prb_run_begin(gb_prb *h, int nsteps_total)
 {
-    if (!h || nsteps < 0 || kt0 < 1) { gb_set_error("gb_prb_step: invalid argument"); return GB_ERR_INVALID; }
-    if (nsteps == 0) return GB_OK;
+    if (!h || nsteps_total < 0) { gb_set_error("gb_prb_run_begin: invalid argument"); return GB_ERR_INVALID; }
     prb_refresh_scalars(h);
     PrbDev &d = h->dev;
-    if (h->hist_cap < nsteps) {
+    const int cap = nsteps_total > 0 ? nsteps_total : 1;
+    if (h->hist_cap < cap) {
         cudaFree(h->hist);
         h->hist = nullptr;
-        GB_CUDA_TRY(cudaMalloc(&h->hist, (sizeof(double) * 2 + sizeof(int) * 2) * (size_t)nsteps));
-        h->hist_cap = nsteps;
+        GB_CUDA_TRY(cudaMalloc(&h->hist, (sizeof(double) * 2 + sizeof(int) * 2) * (size_t)cap));
+        h->hist_cap = cap;
         if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
         if (h->graph_exec1) { cudaGraphExecDestroy(h->graph_exec1); h->graph_exec1 = nullptr; }
     }
     d.nu_hist = (double *)h->hist;
     d.sweep_hist = (int *)((double *)h->hist + 2 * (size_t)h->hist_cap);
     d.hist_cap = h->hist_cap;
-    // scalars are baked into the graph: rebuild when they change
+    // scalars are baked into the graphs: rebuild when they change
     if (memcmp(&h->graph_scalars, &h->p, sizeof(gb_prb_params)) != 0) {
         if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
         if (h->graph_exec1) { cudaGraphExecDestroy(h->graph_exec1); h->graph_exec1 = nullptr; }
@@ -792,6 +795,12 @@ extern "C" int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *swee
     GB_CUDA_TRY(cudaMemsetAsync(d.abort, 0, sizeof(int), h->stream));
     GB_CUDA_TRY(cudaMemsetAsync(d.step_index, 0, sizeof(int), h->stream));
     GB_CUDA_TRY(cudaMemsetAsync(d.clamps, 0, sizeof(unsigned long long), h->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_prb_run_enqueue(gb_prb *h, int kt0, int nsteps)
+{
+    if (!h || nsteps < 0 || kt0 < 1) { gb_set_error("gb_prb_run_enqueue: invalid argument"); return GB_ERR_INVALID; }
     int st;
     for (int s = 0; s < nsteps; ++s) {
         const int first = (kt0 + s == 1);
@@ -800,25 +809,54 @@ extern "C" int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *swee
         GB_CUDA_TRY(cudaGraphLaunch(*ex, h->stream));
         h->launches += h->launches_per_step;
     }
-    int info[2];
+    return GB_OK;
+}
+
+extern "C" int gb_prb_run_query(gb_prb *h)
+{
+    if (!h) return -GB_ERR_INVALID;
+    const cudaError_t e = cudaStreamQuery(h->stream);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) { cudaGetLastError(); return 0; }
+    gb_set_error("gb_prb_run_query: %s", cudaGetErrorString(e));
+    return -GB_ERR_CUDA;
+}
+
+extern "C" int gb_prb_run_end(gb_prb *h, int nsteps, double *nu, int *sweeps, int *steps_done)
+{
+    if (!h || nsteps < 0 || nsteps > h->hist_cap) { gb_set_error("gb_prb_run_end: invalid argument"); return GB_ERR_INVALID; }
+    PrbDev &d = h->dev;
+    int info[2] = {0, 0}, stat[4] = {0, 0, 0, 0};
     GB_CUDA_TRY(cudaMemcpyAsync(info, d.step_index, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     GB_CUDA_TRY(cudaMemcpyAsync(info + 1, d.abort, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    std::vector<double> nuh(2 * (size_t)nsteps);
-    std::vector<int> swh(2 * (size_t)nsteps);
-    GB_CUDA_TRY(cudaMemcpyAsync(nuh.data(), d.nu_hist, sizeof(double) * 2 * nsteps, cudaMemcpyDeviceToHost, h->stream));
-    GB_CUDA_TRY(cudaMemcpyAsync(swh.data(), d.sweep_hist, sizeof(int) * 2 * nsteps, cudaMemcpyDeviceToHost, h->stream));
-    int stat[4];
     GB_CUDA_TRY(cudaMemcpyAsync(stat, d.mg_status, sizeof(stat), cudaMemcpyDeviceToHost, h->stream));
-    st = prb_sync(h, "gb_prb_step");
+    std::vector<double> nuh(2 * (size_t)nsteps + 1);
+    std::vector<int> swh(2 * (size_t)nsteps + 1);
+    if (nsteps > 0) {
+        GB_CUDA_TRY(cudaMemcpyAsync(nuh.data(), d.nu_hist, sizeof(double) * 2 * nsteps, cudaMemcpyDeviceToHost, h->stream));
+        GB_CUDA_TRY(cudaMemcpyAsync(swh.data(), d.sweep_hist, sizeof(int) * 2 * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    }
+    int st = prb_sync(h, "gb_prb_run_end");
     if (st != GB_OK) return st;
     if (nu) memcpy(nu, nuh.data(), sizeof(double) * 2 * nsteps);
     if (sweeps) memcpy(sweeps, swh.data(), sizeof(int) * 2 * nsteps);
     h->steps_done = info[0];
+    if (steps_done) *steps_done = info[0];
     if (info[1]) {
-        gb_set_error("gb_prb_step: multigrid failed at step %d (status v=%d u=%d)", kt0 + info[0], stat[0], stat[2]);
+        gb_set_error("gb_prb_step: multigrid failed at step %d (status v=%d u=%d)", info[0] + 1, stat[0], stat[2]);
         return stat[0] != GB_OK ? stat[0] : stat[2];
     }
     return GB_OK;
+}
+
+extern "C" int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *sweeps)
+{
+    if (!h || nsteps < 0 || kt0 < 1) { gb_set_error("gb_prb_step: invalid argument"); return GB_ERR_INVALID; }
+    if (nsteps == 0) return GB_OK;
+    int st = gb_prb_run_begin(h, nsteps);
+    if (st == GB_OK) st = gb_prb_run_enqueue(h, kt0, nsteps);
+    if (st != GB_OK) return st;
+    return gb_prb_run_end(h, nsteps, nu, sweeps, nullptr);
 }
 
 extern "C" void *gb_prb_stream(gb_prb *h) { return h ? (void *)h->stream : nullptr; }

@@ -91,6 +91,10 @@ SIGNATURES = [
     ("gb_prb_update", C.c_int, [_vp, C.POINTER(C.c_longlong)]),
     ("gb_prb_step", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     ("gb_prb_stream", _vp, [_vp]),
+    ("gb_prb_run_begin", C.c_int, [_vp, C.c_int]),
+    ("gb_prb_run_enqueue", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("gb_prb_run_query", C.c_int, [_vp]),
+    ("gb_prb_run_end", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
     ("gb_axi_default_params", None, [C.POINTER(AxiParams), C.c_int, C.c_int]),
     ("gb_axi_create", C.c_int, [C.POINTER(AxiParams), C.POINTER(_vp), _ip]),
     ("gb_axi_destroy", C.c_int, [_vp]),
@@ -104,6 +108,10 @@ SIGNATURES = [
     ("gb_axi_heat", C.c_int, [_vp, _dp]),
     ("gb_axi_step", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
     ("gb_axi_stream", _vp, [_vp]),
+    ("gb_axi_run_begin", C.c_int, [_vp, C.c_int]),
+    ("gb_axi_run_enqueue", C.c_int, [_vp, C.c_int]),
+    ("gb_axi_run_query", C.c_int, [_vp]),
+    ("gb_axi_run_end", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
     ("gb_prb_bind_bounds", None, [C.c_int, C.c_int]),
     ("gb_prb_bind_smoother", None, [C.c_int]),
     ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),

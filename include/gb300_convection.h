@@ -168,6 +168,19 @@ int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *sweeps);
 /* The CUDA stream (cudaStream_t) every call on h runs on, for callers that
  * order their own work or time the steps with events on it. */
 void *gb_prb_stream(gb_prb *h);
+/* Asynchronous stepping for callers that keep many instances in flight
+ * (the served loop): run_begin sizes the per-step history for up to
+ * nsteps_total steps and resets the counters; run_enqueue queues nsteps
+ * graph-replayed steps (kt0: index of the first, 1 = the forward step) on
+ * the instance's stream and returns at once; run_query returns 1 when the
+ * queued steps are done, 0 while they run (a negative status on an error);
+ * run_end waits and copies the history of the first nsteps steps (as
+ * gb_prb_step does) and the number of steps completed.  gb_prb_step is
+ * run_begin + run_enqueue + run_end. */
+int gb_prb_run_begin(gb_prb *h, int nsteps_total);
+int gb_prb_run_enqueue(gb_prb *h, int kt0, int nsteps);
+int gb_prb_run_query(gb_prb *h);
+int gb_prb_run_end(gb_prb *h, int nsteps, double *nu, int *sweeps, int *steps_done);
 
 /* ------------------------------------------- gfortran-compatible drop-in */
 /* These read/write the caller's COMMON blocks (declared by the Fortran main
@@ -263,6 +276,11 @@ int gb_axi_heat(gb_axi *h, double *trans);           /* rotann2.f:468-487 */
  * *steps_done (may be NULL) receives the number of steps taken. */
 int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done);
 void *gb_axi_stream(gb_axi *h);
+/* Asynchronous stepping, as gb_prb_run_* (nu and sweeps: one per step). */
+int gb_axi_run_begin(gb_axi *h, int nsteps_total);
+int gb_axi_run_enqueue(gb_axi *h, int nsteps);
+int gb_axi_run_query(gb_axi *h);
+int gb_axi_run_end(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done);
 
 /* ------------------------------------------------ batched banded solvers */
 /* nlines independent systems with the same n; line l's element j sits at
