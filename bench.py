@@ -333,10 +333,13 @@ def run_prb_workload(args, cfg):
 # 0.5), Ra 1e8, Ta 1e5 as the rotational Reynolds number Re = sqrt(Ta)/2
 # (Ta = 4 Omega^2 d^4 / nu^2, Re = Omega d^2 / nu), Pr 1, dt 2e-7, the
 # conduction profile plus seeded noise of amplitude 1e-4; uniform grid.
+# The multigrid tolerance is 1e-9 (the reference's relax uses 1e-6): the
+# field comparison of the mixed and FP64 paths is only as close as the
+# tolerance the two solves stop at.
 AXIWL = dict(nr=256, nz=256, dt=2e-7, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e8, Re=(1e5 ** 0.5) / 2.0, Pr=1.0,
-             tolcon=1e-6, amp=1e-4,
+             tolcon=1e-9, amp=1e-4,
              name="axisymmetric annulus 257 x 257 (nr = nz = 256), Ra 1e8, Ta 1e5 (Re 158.1), Pr 1, dt 2e-7, "
-                  "MG tolcon 1e-6, uniform grid")
+                  "MG tolcon 1e-9, uniform grid")
 
 
 def axi_initial(cfg, seed=0):
