@@ -75,6 +75,24 @@ class AXI(C.Structure):
                  ("last_sweeps", C.c_int), ("last_resmax", C.c_double)])
 
 
+R3D_FIELDS = ["An", "A", "Ap", "Bn", "B", "Bp", "Cn", "C", "Cp", "thn", "th", "thp",
+              "uel", "vel", "wel", "uelp", "velp", "welp", "urh", "vrh", "wrh"]
+R3D_MAXLEV = 8
+
+
+class R3D(C.Structure):
+    _fields_ = ([(n, C.c_int) for n in ("nr", "nz", "np", "ni", "nj", "nk")] +
+                [(n, C.c_double) for n in ("dt", "r0", "rmax", "zmax", "Ra", "Re", "Gr", "Ptl",
+                                           "dr", "dz", "dp", "pi")] +
+                [(n, _dp) for n in R3D_FIELDS] +
+                [("nlev", C.c_int)] +
+                [(n, C.c_int * R3D_MAXLEV) for n in ("n1", "n2", "n3")] +
+                [(n, C.c_double * R3D_MAXLEV) for n in ("hr", "hz", "hp", "hhr", "hhz", "hhp")] +
+                [(n, _dp * R3D_MAXLEV) for n in ("v", "f", "res")] +
+                [("tolcon", C.c_double), ("sor", C.c_double), ("nrel", C.c_int), ("maxsweeps", C.c_int),
+                 ("mode", C.c_int), ("last_resmax", C.c_double), ("last_sweeps", C.c_int)])
+
+
 _lib = None
 
 
@@ -133,6 +151,21 @@ def lib():
         L.orc_prolong_add64.argtypes = [C.c_int, _dp, _dp]
         L.orc_resnorm64.argtypes = [C.c_int, _dp, _dp]
         L.orc_resnorm64.restype = C.c_double
+        L.orc_r3d_init.argtypes = [C.POINTER(R3D), C.c_int, C.c_int, C.c_int] + [C.c_double] * 8
+        L.orc_r3d_init.restype = C.c_int
+        L.orc_r3d_free.argtypes = [C.POINTER(R3D)]
+        L.orc_r3d_initial.argtypes = [C.POINTER(R3D), C.c_int, C.c_double]
+        for nm in ("avorticity", "bvorticity", "cvorticity", "temperature", "update", "rhsw", "rhsv", "rhsu"):
+            getattr(L, "orc_r3d_" + nm).argtypes = [C.POINTER(R3D)]
+        L.orc_r3d_heat.argtypes = [C.POINTER(R3D)]
+        L.orc_r3d_heat.restype = C.c_double
+        L.orc_r3d_poisson.argtypes = [C.POINTER(R3D), C.c_int, _ip]
+        L.orc_r3d_poisson.restype = C.c_int
+        L.orc_r3d_relax.argtypes = [C.POINTER(R3D), C.c_int, C.c_int, C.c_int, _ip]
+        L.orc_r3d_corser.argtypes = [C.POINTER(R3D), C.c_int]
+        L.orc_r3d_finer.argtypes = [C.POINTER(R3D), C.c_int]
+        L.orc_r3d_step.argtypes = [C.POINTER(R3D), _dp, _ip]
+        L.orc_r3d_step.restype = C.c_int
         _lib = L
     return _lib
 
@@ -276,6 +309,68 @@ class OracleAXI:
     def close(self):
         if self.s.phi:
             lib().orc_axi_free(C.byref(self.s))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OracleR3D:
+    """The 3D rotating annulus state of rot3dmg.f with its multigrid.
+
+    Fields are (nr+2, nz+2, np+1) Fortran-ordered views (i fastest)."""
+
+    def __init__(self, nr, nz, np_, dt, r0, rmax, zmax, Ra, Re, Pr, Gr=0.0, mode=ORC_LEX, tolcon=None,
+                 maxsweeps=None):
+        L = lib()
+        self.s = R3D()
+        if L.orc_r3d_init(C.byref(self.s), nr, nz, np_, dt, r0, rmax, zmax, Ra, Re, Gr, Pr) != 0:
+            L.orc_r3d_free(C.byref(self.s))
+            raise ValueError("invalid R3D size nr=%d nz=%d np=%d" % (nr, nz, np_))
+        self.s.mode = mode
+        if tolcon is not None:
+            self.s.tolcon = tolcon
+        if maxsweeps is not None:
+            self.s.maxsweeps = maxsweeps
+
+    @property
+    def shape(self):
+        return (self.s.ni, self.s.nj, self.s.nk)
+
+    def field(self, name) -> np.ndarray:
+        p = getattr(self.s, name)
+        ni, nj, nk = self.shape
+        return np.ctypeslib.as_array(p, shape=(ni * nj * nk,)).reshape((nk, nj, ni)).T
+
+    def level(self, which, l) -> np.ndarray:
+        """v, f or res of multigrid level l (1-based) as an (n1+1, n2+1, n3+1) view."""
+        n1, n2, n3 = self.s.n1[l], self.s.n2[l], self.s.n3[l]
+        p = getattr(self.s, which)[l]
+        n = (n1 + 1) * (n2 + 1) * (n3 + 1)
+        return np.ctypeslib.as_array(p, shape=(n,)).reshape((n3 + 1, n2 + 1, n1 + 1)).T
+
+    def initial(self, nval=3, amp=1e-3):
+        lib().orc_r3d_initial(C.byref(self.s), nval, amp)
+
+    def call(self, name):
+        return getattr(lib(), "orc_r3d_" + name)(C.byref(self.s))
+
+    def poisson(self, which):
+        sw = C.c_int()
+        st = lib().orc_r3d_poisson(C.byref(self.s), which, C.byref(sw))
+        return st, sw.value
+
+    def step(self):
+        nu = C.c_double()
+        sw = np.zeros(3, dtype=np.int32)
+        st = lib().orc_r3d_step(C.byref(self.s), C.byref(nu), iptr(sw))
+        return st, nu.value, sw
+
+    def close(self):
+        if self.s.th:
+            lib().orc_r3d_free(C.byref(self.s))
 
     def __del__(self):
         try:
