@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "gbcommon.cuh"
+#include "gridsync.cuh"
 
 #define BP_MAXL 16
 #define LOCAL_N 65
@@ -621,45 +622,6 @@ __global__ void __launch_bounds__(TILE_THREADS) k_op(BatchDev B, const TileEntry
     o.nu = NU;
     o.corr = CORR ? 1 : 0;
     run_item<T>(B, tiles, f_p, o, blockIdx.x, nu1, nu2, smem_raw);
-}
-
-// Grid-wide barrier of the persistent kernel.  Every wait is bounded: a
-// block that waits longer than `limit` polls sets the error flag and every
-// block leaves the kernel at its next barrier, so a lost block cannot hang
-// the GPU.
-struct GridSync {
-    unsigned *count;
-    unsigned *gen;
-    int *err;
-    long long limit;
-};
-
-__device__ __forceinline__ bool grid_sync(const GridSync &gs)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *vgen = gs.gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(gs.count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(gs.count, 0u);
-            __threadfence();
-            atomicAdd(gs.gen, 1u);
-        } else {
-            long long it = 0;
-            while (*vgen == g) {
-                if (++it > gs.limit || *(volatile int *)gs.err) {
-                    atomicExch(gs.err, 1);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return *(volatile int *)gs.err == 0;
 }
 
 // The whole solve in one launch: the first iteration's operations, then

@@ -1,0 +1,1815 @@
+// 3D rotating annulus of rot3dmg.f on sm_103a: the Dufort-Frankel transport
+// of the vorticity components A, B, C and the temperature, the wall
+// vorticities, the right-hand sides of the three velocity Poisson equations,
+// and their multigrid solves, FP64, bit-identical to the oracle (every
+// expression in the reference's order, -fmad=false, IEEE division).
+//
+// Layout: every field is a (0:nr+1, 0:nz+1, 0:np) column-major array in HBM
+// (i fastest), the reference's COMMON arrays cut to the run's size.  Each
+// multigrid level holds its correction v, right-hand side f and residual
+// res as (0:n1, 0:n2, 0:n3) arrays.
+//
+// Multigrid: one persistent cooperative launch per Poisson solve runs the
+// whole sweep loop of poisson1/2/3.  A relaxation pass in one direction is
+// a sequence of phases of independent lines separated by bounded grid
+// barriers; each thread solves whole lines in place.  The line matrices
+// depend only on the level and the line's radius, so the banded solvers'
+// matrix eliminations are done once at creation (k_r3d_factors) and a line
+// solve only carries its right-hand side through the recorded multipliers:
+// the same operations, in the same order, as the reference's tdma, ptdma
+// and pdma (rot3dmg.f:2570-2689).  Phases: GB_SMOOTHER_LEX runs the
+// reference's sequential order as anti-diagonal wavefronts (a line reads
+// the new values of the lines before it in the reference's order and the old
+// values of those after it, and every such neighbour sits on an earlier or
+// a later anti-diagonal), GB_SMOOTHER_ZEBRA the two-colour order with the
+// one-sided boundary rows last.
+#include "gbcommon.cuh"
+#include "gridsync.cuh"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#define R3_MAXLEV 8
+#define R3_THREADS 256
+
+struct R3Lev {
+    int n1, n2, n3, L1, L2;
+    double hr, hz, hp, hhr, hhz, hhp;
+    double *v, *f, *res;
+    double *rvc, *rvv;          // r0 + (i - 1/2) hr and i hr + r0, i = 0..n1+1
+    double *fac[4][3];          // [component][direction] factor tables
+    int *lines[4][3];           // packed p | q << 16, phase by phase
+    int *poff[4][3];            // phase offsets (nphase + 1)
+    int nphase[4][3];
+};
+
+struct R3Dev {
+    int nr, nz, np, ni, nj, nk, nlev;
+    double dt, r0, rmax, zmax, Ra, Re, Gr, Ptl, dr, dz, dp;
+    double nu_num, nu_den;      // -r0 ln(r0/rmax) and zmax 2 pi (host libm)
+    double tolcon, sor;
+    int nrel, maxsweeps;
+    double *fld[GB_R_COUNT];
+    R3Lev lev[R3_MAXLEV];
+    unsigned long long *resmax; // two slots, bit patterns of non-negative doubles
+    int *nanflag;               // two slots
+    int *abort;                 // nonzero: a solve failed, later kernels return
+    int *steps_done;
+    double *trans;              // per-k heat flux sums (np + 1)
+    double *hist_nu;
+    int *hist_sw;
+    int *solve_status, *solve_sweeps;
+    GridSync gs;
+};
+
+#define FX(a, i, j, k) ((a)[(size_t)(i) + (size_t)ni * ((size_t)(j) + (size_t)nj * (size_t)(k))])
+
+// ---------------------------------------------------------------------------
+// Transport (rot3dmg.f:341-873): one thread per point
+// ---------------------------------------------------------------------------
+
+__global__ void k_r3d_avort(R3Dev d)
+{
+    if (*(volatile int *)d.abort) return;
+    const int nr = d.nr, nz = d.nz, np = d.np, ni = d.ni, nj = d.nj;
+    const long long total = (long long)nr * (nz - 1) * (np + 1);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % nr);
+    const long long rest = t / nr;
+    const int j = 1 + (int)(rest % (nz - 1));
+    const int k = (int)(rest / (nz - 1));
+    const double dr = d.dr, dz = d.dz, dp = d.dp, dt = d.dt, Ptl = d.Ptl;
+    const double Ra = d.Ra, Re = d.Re, Gr = d.Gr;
+    const double *A = d.fld[GB_R_A], *Ap = d.fld[GB_R_Ap], *B = d.fld[GB_R_B], *C = d.fld[GB_R_C];
+    const double *th = d.fld[GB_R_th];
+    const double *uel = d.fld[GB_R_uel], *vel = d.fld[GB_R_vel], *wel = d.fld[GB_R_wel];
+    double *An = d.fld[GB_R_An];
+    const int im = i - 1, jp = j + 1;
+    const int km = k == 0 ? np - 1 : k - 1;
+    const int ka = k == np ? 1 : k + 1;
+    const double r = d.r0 + ((double)i - 0.5) * dr;
+    const double u = (FX(uel, i, j, k) + FX(uel, i, jp, k) + FX(uel, i, j, ka) + FX(uel, i, jp, ka) +
+                      FX(uel, im, j, k) + FX(uel, im, jp, k) + FX(uel, im, j, ka) + FX(uel, im, jp, ka)) *
+                     0.125;
+    const double v = (FX(vel, i, jp, k) + FX(vel, i, j, k)) * 0.5;
+    const double w = (FX(wel, i, j, ka) + FX(wel, i, j, k)) * 0.5;
+    const double tem = (FX(th, i, j, k) + FX(th, i, j, ka) + FX(th, i, jp, k) + FX(th, i, jp, ka)) * 0.25;
+    const double BB = (FX(B, i, j, k) + FX(B, im, j, k) + FX(B, i, j, ka) + FX(B, im, j, ka)) * 0.25;
+    const double CC = (FX(C, i, j, k) + FX(C, i, jp, k) + FX(C, im, j, k) + FX(C, im, jp, k)) * 0.25;
+    double Arra, Ara, Ar, cnr;
+    if (i == 1) {
+        Arra = (3.2 * FX(A, i - 1, j, k) + 2.0 * FX(A, i + 1, j, k) - 0.2 * FX(A, i + 2, j, k)) / (dr * dr);
+        Ara = (-4.0 * FX(A, i - 1, j, k) / 3.0 + FX(A, i + 1, j, k) / 3.0) / dr;
+        Ar = (-4.0 * FX(A, i - 1, j, k) / 3.0 + FX(A, i, j, k) + FX(A, i + 1, j, k) / 3.0) / dr;
+        cnr = -2.5 / (dr * dr) + 0.5 / dr / r;
+    } else if (i == nr) {
+        Arra = (3.2 * FX(A, i + 1, j, k) + 2.0 * FX(A, i - 1, j, k) - 0.2 * FX(A, i - 2, j, k)) / (dr * dr);
+        Ara = (-FX(A, i - 1, j, k) / 3.0 + 4.0 * FX(A, i + 1, j, k) / 3.0) / dr;
+        // the inner-wall formula again (rot3dmg.f:390)
+        Ar = (-4.0 * FX(A, i - 1, j, k) / 3.0 + FX(A, i, j, k) + FX(A, i + 1, j, k) / 3.0) / dr;
+        cnr = -2.5 / (dr * dr) - 0.5 / dr / r;
+    } else {
+        Arra = (FX(A, i - 1, j, k) + FX(A, i + 1, j, k)) / (dr * dr);
+        Ara = (FX(A, i + 1, j, k) - FX(A, i - 1, j, k)) * 0.5 / dr;
+        Ar = Ara;
+        cnr = -1.0 / (dr * dr);
+        const double Pe = fabs(u * dr / Ptl);
+        if (Pe > 2.0) {
+            if (u > 0.0) Ar = (FX(A, i, j, k) - FX(A, i - 1, j, k)) / dr;
+            else if (u < 0.0) Ar = (FX(A, i + 1, j, k) - FX(A, i, j, k)) / dr;
+        }
+    }
+    const double uelr = ((FX(uel, i, j, k) + FX(uel, i, jp, k) + FX(uel, i, j, ka) + FX(uel, i, jp, ka)) * 0.25 -
+                         (FX(uel, im, j, k) + FX(uel, im, jp, k) + FX(uel, im, j, ka) + FX(uel, im, jp, ka)) * 0.25) /
+                        dr;
+    const double Azza = (FX(A, i, j - 1, k) + FX(A, i, j + 1, k)) / (dz * dz);
+    double Az = (FX(A, i, j + 1, k) - FX(A, i, j - 1, k)) * 0.5 / dz;
+    {
+        const double Pe = fabs(w * dz / Ptl);
+        if (Pe > 2.0) {
+            if (w > 0.0) Az = (FX(A, i, j, k) - FX(A, i, j - 1, k)) / dz;
+            else if (w < 0.0) Az = (FX(A, i, j + 1, k) - FX(A, i, j, k)) / dz;
+        }
+    }
+    const double uelz = ((FX(uel, i, jp, k) + FX(uel, i, jp, ka) + FX(uel, im, jp, k) + FX(uel, im, jp, ka)) * 0.25 -
+                         (FX(uel, i, j, k) + FX(uel, i, j, ka) + FX(uel, im, j, k) + FX(uel, im, j, ka)) * 0.25) /
+                        dz;
+    const double thz = (FX(th, i, jp, k) + FX(th, i, jp, ka) - FX(th, i, j, k) - FX(th, i, j, ka)) * 0.5 / dz;
+    const double thh = (FX(th, i, j, ka) + FX(th, i, jp, ka) - FX(th, i, j, k) - FX(th, i, jp, k)) * 0.5 / dp;
+    const double Ahha = (FX(A, i, j, ka) + FX(A, i, j, km)) / (dp * dp);
+    double Ah = (FX(A, i, j, ka) - FX(A, i, j, km)) * 0.5 / dp;
+    {
+        const double Pe = fabs(v * dp * r / Ptl);
+        if (Pe > 2.0) {
+            if (v > 0.0) Ah = (FX(A, i, j, k) - FX(A, i, j, km)) / dp;
+            else if (v < 0.0) Ah = (FX(A, i, j, ka) - FX(A, i, j, k)) / dp;
+        }
+    }
+    const double Bh = (FX(B, i, j, ka) + FX(B, im, j, ka) - FX(B, i, j, k) - FX(B, im, j, k)) * 0.5 / dp;
+    const double uelh = ((FX(uel, i, j, ka) + FX(uel, i, jp, ka) + FX(uel, im, j, ka) + FX(uel, im, jp, ka)) * 0.25 -
+                         (FX(uel, i, j, k) + FX(uel, i, jp, k) + FX(uel, im, j, k) + FX(uel, im, jp, k)) * 0.25) /
+                        dp;
+    const double cnz = -1.0 / (dz * dz);
+    const double cnh = -1.0 / (dp * dp) / (r * r);
+    const double RHS1 = Arra + Ara / r + Ahha / (r * r) + Azza - 2.0 * Bh / (r * r) + FX(A, i, j, k) / (Ptl * dt);
+    const double ULT = (u * Ar + v * Ah / r + w * Az - uelh * BB / r - uelz * CC) / Ptl;
+    const double RHS2 = -2.0 * Re * uelz + 2.0 * Ra * (tem * uelz + thz * u) / Re / Ptl - Gr * Ptl / r * thh;
+    const double cf1 = 1.0 / (Ptl * dt) - uelr / (2.0 * Ptl) + 1.0 / (2.0 * (r * r)) - cnr - cnz - cnh;
+    const double cf2 = uelr / (2.0 * Ptl) - 1.0 / (2.0 * (r * r)) + cnr + cnz + cnh;
+    FX(An, i, j, k) = (cf2 * FX(Ap, i, j, k) - ULT - RHS2 + RHS1) / cf1;
+}
+
+__global__ void k_r3d_bvort(R3Dev d)
+{
+    if (*(volatile int *)d.abort) return;
+    const int nr = d.nr, nz = d.nz, np = d.np, ni = d.ni, nj = d.nj;
+    const long long total = (long long)(nr - 1) * (nz - 1) * (np + 1);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % (nr - 1));
+    const long long rest = t / (nr - 1);
+    const int j = 1 + (int)(rest % (nz - 1));
+    const int k = (int)(rest / (nz - 1));
+    const double dr = d.dr, dz = d.dz, dp = d.dp, dt = d.dt, Ptl = d.Ptl;
+    const double Ra = d.Ra, Re = d.Re, Gr = d.Gr;
+    const double *A = d.fld[GB_R_A], *B = d.fld[GB_R_B], *Bp = d.fld[GB_R_Bp], *C = d.fld[GB_R_C];
+    const double *th = d.fld[GB_R_th];
+    const double *uel = d.fld[GB_R_uel], *vel = d.fld[GB_R_vel], *wel = d.fld[GB_R_wel];
+    double *Bn = d.fld[GB_R_Bn];
+    const int ip = i + 1, jp = j + 1;
+    const int km = k == 0 ? np - 1 : k - 1;
+    const int ka = k == np ? 1 : k + 1;
+    const double r = d.r0 + (double)i * dr;
+    const double u = (FX(uel, i, j, k) + FX(uel, i, jp, k)) * 0.5;
+    const double v = (FX(vel, i, j, km) + FX(vel, i, jp, km) + FX(vel, i, j, k) + FX(vel, i, jp, k) +
+                      FX(vel, ip, j, km) + FX(vel, ip, jp, km) + FX(vel, ip, j, k) + FX(vel, ip, jp, k)) *
+                     0.125;
+    const double w = (FX(wel, i, j, k) + FX(wel, ip, j, k)) * 0.5;
+    const double tem = (FX(th, i, jp, k) + FX(th, ip, jp, k) + FX(th, i, j, k) + FX(th, ip, j, k)) * 0.25;
+    const double AA = (FX(A, i, j, k) + FX(A, ip, j, k) + FX(A, i, j, km) + FX(A, ip, j, km)) * 0.25;
+    const double CC = (FX(C, i, j, k) + FX(C, i, jp, k) + FX(C, i, j, km) + FX(C, i, jp, km)) * 0.25;
+    const double Brra = (FX(B, i - 1, j, k) + FX(B, i + 1, j, k)) / (dr * dr);
+    const double Bra = (FX(B, i + 1, j, k) - FX(B, i - 1, j, k)) * 0.5 / dr;
+    double Br = Bra;
+    {
+        const double Pe = fabs(u * dr / Ptl);
+        if (Pe > 2.0) {
+            if (u > 0.0) Br = (FX(B, i, j, k) - FX(B, i - 1, j, k)) / dr;
+            else if (u < 0.0) Br = (FX(B, i + 1, j, k) - FX(B, i, j, k)) / dr;
+        }
+    }
+    const double velr = ((FX(vel, ip, j, km) + FX(vel, ip, jp, km) + FX(vel, ip, j, k) + FX(vel, ip, jp, k)) * 0.25 -
+                         (FX(vel, i, j, km) + FX(vel, i, jp, km) + FX(vel, i, j, k) + FX(vel, i, jp, k)) * 0.25) /
+                        dr;
+    const double Bzza = (FX(B, i, j - 1, k) + FX(B, i, j + 1, k)) / (dz * dz);
+    double Bz = (FX(B, i, j + 1, k) - FX(B, i, j - 1, k)) * 0.5 / dz;
+    {
+        const double Pe = fabs(w * dz / Ptl);
+        if (Pe > 2.0) {
+            if (w > 0.0) Bz = (FX(B, i, j, k) - FX(B, i, j - 1, k)) / dz;
+            else if (w < 0.0) Bz = (FX(B, i, j + 1, k) - FX(B, i, j, k)) / dz;
+        }
+    }
+    const double velz = ((FX(vel, i, jp, km) + FX(vel, ip, jp, km) + FX(vel, i, jp, k) + FX(vel, ip, jp, k)) * 0.25 -
+                         (FX(vel, i, j, km) + FX(vel, ip, j, km) + FX(vel, i, j, k) + FX(vel, ip, j, k)) * 0.25) /
+                        dz;
+    const double thz = (FX(th, i, jp, k) + FX(th, ip, jp, k) - FX(th, i, j, k) - FX(th, ip, j, k)) * 0.5 / dz;
+    const double thr = (FX(th, ip, jp, k) + FX(th, ip, j, k) - FX(th, i, jp, k) - FX(th, i, j, k)) * 0.5 / dr;
+    const double Bhha = (FX(B, i, j, ka) + FX(B, i, j, km)) / (dp * dp);
+    double Bh = (FX(B, i, j, ka) - FX(B, i, j, km)) * 0.5 / dp;
+    {
+        const double Pe = fabs(v * dp * r / Ptl);
+        if (Pe > 2.0) {
+            if (v > 0.0) Bh = (FX(B, i, j, k) - FX(B, i, j, km)) / dp;
+            else if (v < 0.0) Bh = (FX(B, i, j, ka) - FX(B, i, j, k)) / dp;
+        }
+    }
+    const double Ah = (FX(A, i, j, k) + FX(A, ip, j, k) - FX(A, i, j, km) - FX(A, ip, j, km)) * 0.5 / dp;
+    const double velh = ((FX(vel, i, j, k) + FX(vel, ip, j, k) + FX(vel, i, jp, k) + FX(vel, ip, jp, k)) * 0.25 -
+                         (FX(vel, i, j, km) + FX(vel, ip, j, km) + FX(vel, i, jp, km) + FX(vel, ip, jp, km)) * 0.25) /
+                        dp;
+    const double cnr = -1.0 / (dr * dr);
+    const double cnz = -1.0 / (dz * dz);
+    const double cnh = -1.0 / (dp * dp) / (r * r);
+    const double RHS1 = Brra + Bra / r + Bhha / (r * r) + Bzza + 2.0 * Ah / (r * r) + FX(B, i, j, k) / (Ptl * dt);
+    const double ULT = (u * Br + v * Bh / r + w * Bz - (velr - v / r) * AA - velz * CC) / Ptl;
+    const double RHS2 = -2.0 * Re * velz + r * Ra * thz + 2.0 * Ra * (tem * velz + thz * v) / Re / Ptl + Gr * Ptl * thr;
+    const double cf1 = 1.0 / (Ptl * dt) - (u / r + velh / r) / (2.0 * Ptl) + 1.0 / (2.0 * (r * r)) - cnr - cnz - cnh;
+    const double cf2 = (u / r + velh / r) / (2.0 * Ptl) - 1.0 / (2.0 * (r * r)) + cnr + cnz + cnh;
+    FX(Bn, i, j, k) = (cf2 * FX(Bp, i, j, k) - ULT - RHS2 + RHS1) / cf1;
+}
+
+__global__ void k_r3d_cvort(R3Dev d)
+{
+    if (*(volatile int *)d.abort) return;
+    const int nr = d.nr, nz = d.nz, np = d.np, ni = d.ni, nj = d.nj;
+    const long long total = (long long)(nr - 1) * nz * (np + 1);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % (nr - 1));
+    const long long rest = t / (nr - 1);
+    const int j = 1 + (int)(rest % nz);
+    const int k = (int)(rest / nz);
+    const double dr = d.dr, dz = d.dz, dp = d.dp, dt = d.dt, Ptl = d.Ptl;
+    const double Ra = d.Ra, Re = d.Re;
+    const double *A = d.fld[GB_R_A], *B = d.fld[GB_R_B], *C = d.fld[GB_R_C], *Cp = d.fld[GB_R_Cp];
+    const double *th = d.fld[GB_R_th];
+    const double *uel = d.fld[GB_R_uel], *vel = d.fld[GB_R_vel], *wel = d.fld[GB_R_wel];
+    double *Cn = d.fld[GB_R_Cn];
+    const int ip = i + 1, jm = j - 1;
+    const int km = k == 0 ? np - 1 : k - 1;
+    const int ka = k == np ? 1 : k + 1;
+    const double r = d.r0 + (double)i * dr;
+    const double u = (FX(uel, i, j, ka) + FX(uel, i, j, k)) * 0.5;
+    const double v = (FX(vel, i, j, k) + FX(vel, ip, j, k)) * 0.5;
+    const double w = (FX(wel, i, j, k) + FX(wel, ip, j, k) + FX(wel, i, j, ka) + FX(wel, ip, j, ka) +
+                      FX(wel, i, jm, k) + FX(wel, ip, jm, k) + FX(wel, i, jm, ka) + FX(wel, ip, jm, ka)) *
+                     0.125;
+    const double AA = (FX(A, i, j, k) + FX(A, i, jm, k) + FX(A, ip, j, k) + FX(A, ip, jm, k)) * 0.25;
+    const double BB = (FX(B, i, j, k) + FX(B, i, jm, k) + FX(B, i, j, ka) + FX(B, i, jm, ka)) * 0.25;
+    const double tem = (FX(th, i, j, k) + FX(th, ip, j, k) + FX(th, ip, j, ka) + FX(th, i, j, ka)) * 0.25;
+    const double Crra = (FX(C, i - 1, j, k) + FX(C, i + 1, j, k)) / (dr * dr);
+    const double Cra = (FX(C, i + 1, j, k) - FX(C, i - 1, j, k)) * 0.5 / dr;
+    double Cr = Cra;
+    {
+        const double Pe = fabs(u * dr / Ptl);
+        if (Pe > 2.0) {
+            if (u > 0.0) Cr = (FX(C, i, j, k) - FX(C, i - 1, j, k)) / dr;
+            else if (u < 0.0) Cr = (FX(C, i + 1, j, k) - FX(C, i, j, k)) / dr;
+        }
+    }
+    const double welr = ((FX(wel, ip, j, k) + FX(wel, ip, j, ka) + FX(wel, ip, jm, k) + FX(wel, ip, jm, ka)) * 0.25 -
+                         (FX(wel, i, j, k) + FX(wel, i, j, ka) + FX(wel, i, jm, k) + FX(wel, i, jm, ka)) * 0.25) /
+                        dr;
+    const double thr = (FX(th, ip, j, k) + FX(th, ip, j, ka) - FX(th, i, j, k) - FX(th, i, j, ka)) * 0.5 / dr;
+    double Czza, Cz, cnz;
+    if (j == 1) {
+        Czza = (3.2 * FX(C, i, j - 1, k) + 2.0 * FX(C, i, j + 1, k) - 0.2 * FX(C, i, j + 2, k)) / (dz * dz);
+        Cz = (-4.0 * FX(C, i, j - 1, k) / 3.0 + FX(C, i, j, k) + FX(C, i, j + 1, k) / 3.0) / dz;
+        cnz = -2.5 / (dz * dz);
+    } else if (j == nz) {
+        Czza = (3.2 * FX(C, i, j + 1, k) + 2.0 * FX(C, i, j - 1, k) - 0.2 * FX(C, i, j - 2, k)) / (dz * dz);
+        Cz = (-FX(C, i, j - 1, k) / 3.0 - FX(C, i, j, k) + 4.0 * FX(C, i, j + 1, k) / 3.0) / dz;
+        cnz = -2.5 / (dz * dz);
+    } else {
+        Czza = (FX(C, i, j - 1, k) + FX(C, i, j + 1, k)) / (dz * dz);
+        Cz = (FX(C, i, j + 1, k) - FX(C, i, j - 1, k)) * 0.5 / dz;
+        const double Pe = fabs(w * dz / Ptl);
+        if (Pe > 2.0) {
+            if (w > 0.0) Cz = (FX(C, i, j, k) - FX(C, i, j - 1, k)) / dz;
+            else if (w < 0.0) Cz = (FX(C, i, j + 1, k) - FX(C, i, j, k)) / dz;
+        }
+        cnz = -1.0 / (dz * dz);
+    }
+    const double welz = ((FX(wel, i, j, k) + FX(wel, ip, j, k) + FX(wel, i, j, ka) + FX(wel, ip, j, ka)) * 0.25 -
+                         (FX(wel, i, jm, k) + FX(wel, ip, jm, k) + FX(wel, i, jm, ka) + FX(wel, ip, jm, ka)) * 0.25) /
+                        dz;
+    const double Chha = (FX(C, i, j, ka) + FX(C, i, j, km)) / (dp * dp);
+    double Ch = (FX(C, i, j, ka) - FX(C, i, j, km)) * 0.5 / dp;
+    {
+        const double Pe = fabs(v * dp * r / Ptl);
+        if (Pe > 2.0) {
+            if (v > 0.0) Ch = (FX(C, i, j, k) - FX(C, i, j, km)) / dp;
+            else if (v < 0.0) Ch = (FX(C, i, j, ka) - FX(C, i, j, k)) / dp;
+        }
+    }
+    const double welh = ((FX(wel, i, j, ka) + FX(wel, ip, j, ka) + FX(wel, i, jm, ka) + FX(wel, ip, jm, ka)) * 0.25 -
+                         (FX(wel, i, j, k) + FX(wel, ip, j, k) + FX(wel, i, jm, k) + FX(wel, ip, jm, k)) * 0.25) /
+                        dp;
+    const double thh = (FX(th, i, j, ka) + FX(th, ip, j, ka) - FX(th, i, j, k) - FX(th, ip, j, k)) * 0.5 / dp;
+    const double cnr = -1.0 / (dr * dr);
+    const double cnh = -1.0 / (dp * dp) / (r * r);
+    const double RHS1 = Crra + Cra / r + Chha / (r * r) + Czza + FX(C, i, j, k) / (Ptl * dt);
+    const double ULT = (u * Cr + v * Ch / r + w * Cz - welr * AA - welh * BB / r) / Ptl;
+    const double RHS2 = -2.0 * Re * welz - Ra * thh + 2.0 * Ra * (tem * welz - thr * u - thh * v / r) / Re / Ptl;
+    const double cf1 = 1.0 / (Ptl * dt) - welz / (2.0 * Ptl) - cnr - cnz - cnh;
+    const double cf2 = welz / (2.0 * Ptl) + cnr + cnz + cnh;
+    FX(Cn, i, j, k) = (cf2 * FX(Cp, i, j, k) - ULT - RHS2 + RHS1) / cf1;
+}
+
+__global__ void k_r3d_temp(R3Dev d)
+{
+    if (*(volatile int *)d.abort) return;
+    const int nr = d.nr, nz = d.nz, np = d.np, ni = d.ni, nj = d.nj;
+    const long long total = (long long)nr * (nz + 2) * (np + 1);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % nr);
+    const long long rest = t / nr;
+    const int j = (int)(rest % (nz + 2));
+    const int k = (int)(rest / (nz + 2));
+    const double dr = d.dr, dz = d.dz, dp = d.dp, dt = d.dt, Ptl = d.Ptl;
+    const double *th = d.fld[GB_R_th], *thp = d.fld[GB_R_thp];
+    const double *uel = d.fld[GB_R_uel], *vel = d.fld[GB_R_vel], *wel = d.fld[GB_R_wel];
+    double *thn = d.fld[GB_R_thn];
+    const int im = i - 1, jm = j - 1;
+    const int km = k == 0 ? np - 1 : k - 1;
+    const int ka = k == np ? 1 : k + 1;
+    const double r = d.r0 + ((double)i - 0.5) * dr;
+    double u, v, w;
+    if (j == 0 || j == nz + 1) {
+        u = 0.0;
+        v = 0.0;
+        w = 0.0;
+    } else {
+        u = (FX(uel, i, j, k) + FX(uel, im, j, k)) * 0.5;
+        v = (FX(vel, i, j, k) + FX(vel, i, j, km)) * 0.5;
+        w = (FX(wel, i, j, k) + FX(wel, i, jm, k)) * 0.5;
+    }
+    double thrra, thra, thr, cnr;
+    if (i == 1) {
+        thrra = (3.2 * FX(th, i - 1, j, k) + 2.0 * FX(th, i + 1, j, k) - 0.2 * FX(th, i + 2, j, k)) / (dr * dr);
+        thra = (-4.0 * FX(th, i - 1, j, k) / 3.0 + FX(th, i + 1, j, k) / 3.0) / dr;
+        thr = (-4.0 * FX(th, i - 1, j, k) / 3.0 + FX(th, i, j, k) + FX(th, i + 1, j, k) / 3.0) / dr;
+        cnr = -2.5 / (dr * dr) + 0.5 / dr / r;
+    } else if (i == nr) {
+        thrra = (3.2 * FX(th, i + 1, j, k) + 2.0 * FX(th, i - 1, j, k) - 0.2 * FX(th, i - 2, j, k)) / (dr * dr);
+        thra = (-FX(th, i - 1, j, k) / 3.0 + 4.0 * FX(th, i + 1, j, k) / 3.0) / dr;
+        thr = (-FX(th, i - 1, j, k) / 3.0 - FX(th, i, j, k) + 4.0 * FX(th, i + 1, j, k) / 3.0) / dr;
+        cnr = -2.5 / (dr * dr) - 0.5 / dr / r;
+    } else {
+        thrra = (FX(th, i - 1, j, k) + FX(th, i + 1, j, k)) / (dr * dr);
+        thra = (FX(th, i + 1, j, k) - FX(th, i - 1, j, k)) * 0.5 / dr;
+        thr = thra;
+        const double Pe = fabs(u * dr / Ptl);
+        if (Pe > 2.0) {
+            if (u > 0.0) thr = (FX(th, i, j, k) - FX(th, i - 1, j, k)) / dr;
+            else if (u < 0.0) thr = (FX(th, i + 1, j, k) - FX(th, i, j, k)) / dr;
+        }
+        cnr = -1.0 / (dr * dr);
+    }
+    double thzza, thz, cnz;
+    if (j == 1) {
+        thzza = (3.2 * FX(th, i, j - 1, k) + 2.0 * FX(th, i, j + 1, k) - 0.2 * FX(th, i, j + 2, k)) / (dz * dz);
+        thz = (-4.0 * FX(th, i, j - 1, k) / 3.0 + FX(th, i, j, k) + FX(th, i, j + 1, k) / 3.0) / dz;
+        cnz = -2.5 / (dz * dz);
+    } else if (j == nz) {
+        thzza = (3.2 * FX(th, i, j + 1, k) + 2.0 * FX(th, i, j - 1, k) - 0.2 * FX(th, i, j - 2, k)) / (dz * dz);
+        thz = (-FX(th, i, j - 1, k) / 3.0 - FX(th, i, j, k) + 4.0 * FX(th, i, j + 1, k) / 3.0) / dz;
+        cnz = -2.5 / (dz * dz);
+    } else if (j == 0) {
+        thzza = 8.0 * FX(th, i, j + 1, k) / (dz * dz);
+        thz = 0.0;
+        cnz = -4.0 / (dz * dz);
+    } else if (j == nz + 1) {
+        thzza = 8.0 * FX(th, i, j - 1, k) / (dz * dz);
+        thz = 0.0;
+        cnz = -4.0 / (dz * dz);
+    } else {
+        thzza = (FX(th, i, j - 1, k) + FX(th, i, j + 1, k)) / (dz * dz);
+        thz = (FX(th, i, j + 1, k) - FX(th, i, j - 1, k)) * 0.5 / dz;
+        const double Pe = fabs(w * dz / Ptl);
+        if (Pe > 2.0) {
+            if (w > 0.0) thz = (FX(th, i, j, k) - FX(th, i, j - 1, k)) / dz;
+            else if (w < 0.0) thz = (FX(th, i, j + 1, k) - FX(th, i, j, k)) / dz;
+        }
+        cnz = -1.0 / (dz * dz);
+    }
+    const double thhha = (FX(th, i, j, ka) + FX(th, i, j, km)) / (dp * dp);
+    double thh = (FX(th, i, j, ka) - FX(th, i, j, km)) * 0.5 / dp;
+    {
+        const double Pe = fabs(v * dp * r / Ptl);
+        if (Pe > 2.0) {
+            if (v > 0.0) thh = (FX(th, i, j, k) - FX(th, i, j, km)) / dp;
+            else if (v < 0.0) thh = (FX(th, i, j, ka) - FX(th, i, j, k)) / dp;
+        }
+    }
+    const double cnp = -1.0 / (dp * dp) / (r * r);
+    const double RHS1 = thrra + thra / r + thhha / (r * r) + thzza + FX(th, i, j, k) / dt;
+    const double ULT = u * thr + v * thh / r + w * thz;
+    const double cf1 = 1.0 / dt - cnr - cnz - cnp;
+    const double cf2 = cnr + cnz + cnp;
+    FX(thn, i, j, k) = (cf2 * FX(thp, i, j, k) - ULT + RHS1) / cf1;
+}
+
+// heat (rot3dmg.f:882-909): one thread per k sums its z column in the
+// reference's order; k_r3d_heat_sum adds the columns k = 1..np in order.
+__global__ void k_r3d_heat_k(R3Dev d)
+{
+    if (*(volatile int *)d.abort) return;
+    const int k = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > d.np) return;
+    const int ni = d.ni, nj = d.nj, nz = d.nz;
+    const double dr = d.dr, dz = d.dz;
+    const double *th = d.fld[GB_R_th];
+#define HT(j, k) ((-184.0 * FX(th, 0, j, k) + 225.0 * FX(th, 1, j, k) - 50.0 * FX(th, 2, j, k) + 9.0 * FX(th, 3, j, k)))
+    double trans = dz * HT(0, k) / (240.0 * dr);
+    trans = trans + dz * HT(1, k) / (80.0 * dr);
+    trans = trans + dz * HT(nz, k) / (80.0 * dr);
+    trans = trans + dz * HT(nz + 1, k) / (240.0 * dr);
+    for (int j = 2; j <= nz - 1; ++j) trans = trans + dz * HT(j, k) / (60.0 * dr);
+#undef HT
+    d.trans[k] = trans;
+}
+
+__global__ void k_r3d_heat_sum(R3Dev d, int step)
+{
+    if (*(volatile int *)d.abort) return;
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double trans1 = 0.0;
+    for (int k = 1; k <= d.np; ++k) trans1 = trans1 + d.trans[k] * d.dp;
+    d.trans[0] = trans1;
+    if (step >= 0) d.hist_nu[step] = d.nu_num * trans1 / d.nu_den;
+}
+
+// rhsw / rhsv / rhsu (rot3dmg.f:1026-1150)
+template <int COMP>
+__global__ void k_r3d_rhs(R3Dev d)
+{
+    if (*(volatile int *)d.abort) return;
+    const int nr = d.nr, nz = d.nz, np = d.np, ni = d.ni, nj = d.nj;
+    const int I = COMP == 3 ? nr - 1 : nr, J = COMP == 1 ? nz - 1 : nz;
+    const long long total = (long long)I * J * (np + 1);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % I);
+    const long long rest = t / I;
+    const int j = 1 + (int)(rest % J);
+    const int k = (int)(rest / J);
+    const double dr = d.dr, dz = d.dz, dp = d.dp;
+    const double *An = d.fld[GB_R_An], *Bn = d.fld[GB_R_Bn], *Cn = d.fld[GB_R_Cn], *wel = d.fld[GB_R_wel];
+    const int km = k == 0 ? np - 1 : k - 1;
+    if (COMP == 1) {
+        const double r = d.r0 + ((double)i - 0.5) * dr;
+        const double Ah = (FX(An, i, j, k) - FX(An, i, j, km)) / dp;
+        double w;
+        if (i == 1) w = Ah / r - FX(Bn, 1, j, k) / dr - 0.5 * FX(Bn, 1, j, k) / r;
+        else if (i == nr) w = Ah / r + FX(Bn, nr - 1, j, k) / dr - 0.5 * FX(Bn, nr - 1, j, k) / r;
+        else {
+            const double Br = (FX(Bn, i, j, k) - FX(Bn, i - 1, j, k)) / dr;
+            w = Ah / r - Br - 0.5 * (FX(Bn, i, j, k) + FX(Bn, i - 1, j, k)) / r;
+        }
+        FX(d.fld[GB_R_wrh], i, j, k) = w;
+    } else if (COMP == 2) {
+        const double r = d.r0 + ((double)i - 0.5) * dr;
+        double v;
+        if (i == 1) v = FX(Cn, 1, j, k) / dr + FX(Cn, 1, j, k) / r;
+        else if (i == nr) v = -FX(Cn, nr - 1, j, k) / dr + FX(Cn, nr - 1, j, k) / r;
+        else {
+            const double Cr = (FX(Cn, i, j, k) - FX(Cn, i - 1, j, k)) / dr;
+            v = Cr + (FX(Cn, i, j, k) + FX(Cn, i - 1, j, k)) / r;
+        }
+        if (j == 1) v = v - FX(An, i, 1, k) / dz;
+        else if (j == nz) v = v + FX(An, i, nz - 1, k) / dz;
+        else {
+            const double Az = (FX(An, i, j, k) - FX(An, i, j - 1, k)) / dz;
+            v = v - Az;
+        }
+        FX(d.fld[GB_R_vrh], i, j, k) = v;
+    } else {
+        const double r = d.r0 + (double)i * dr;
+        const double welz =
+            0.5 * (FX(wel, i, j, k) + FX(wel, i + 1, j, k) - FX(wel, i, j - 1, k) - FX(wel, i + 1, j - 1, k)) / dz;
+        const double Ch = (FX(Cn, i, j, k) - FX(Cn, i, j, km)) / dp;
+        double u;
+        if (j == 1) u = FX(Bn, i, 1, k) / dz - Ch / r - 2.0 * welz / r;
+        else if (j == nz) u = -FX(Bn, i, nz - 1, k) / dz - Ch / r - 2.0 * welz / r;
+        else {
+            const double Bz = (FX(Bn, i, j, k) - FX(Bn, i, j - 1, k)) / dz;
+            u = Bz - Ch / r - 2.0 * welz / r;
+        }
+        FX(d.fld[GB_R_urh], i, j, k) = u;
+    }
+}
+
+// update (rot3dmg.f:964-1023): each thread sets the wall values of its own
+// point (they depend on the velocities only) and moves its time levels.
+__global__ void k_r3d_update(R3Dev d, int step)
+{
+    if (*(volatile int *)d.abort) return;
+    const int nr = d.nr, nz = d.nz, ni = d.ni, nj = d.nj;
+    const long long total = (long long)ni * nj * d.nk;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0 && step >= 0) atomicAdd(d.steps_done, 1);
+    if (t >= total) return;
+    const int i = (int)(t % ni);
+    const long long rest = t / ni;
+    const int j = (int)(rest % nj);
+    const int k = (int)(rest / nj);
+    const double dr = d.dr, dz = d.dz;
+    const double *uel = d.fld[GB_R_uel], *vel = d.fld[GB_R_vel], *wel = d.fld[GB_R_wel];
+    double *An = d.fld[GB_R_An], *Bn = d.fld[GB_R_Bn], *Cn = d.fld[GB_R_Cn], *thn = d.fld[GB_R_thn];
+    if (i >= 1 && i <= nr) {
+        if (j == 0) FX(An, i, 0, k) = -(3.0 * FX(vel, i, 1, k) - FX(vel, i, 2, k) / 3.0) / dz;
+        else if (j == nz) FX(An, i, nz, k) = -(FX(vel, i, nz - 1, k) / 3.0 - 3.0 * FX(vel, i, nz, k)) / dz;
+    }
+    if (i >= 1 && i <= nr - 1) {
+        if (j == 0) FX(Bn, i, 0, k) = (3.0 * FX(uel, i, 1, k) - FX(uel, i, 2, k) / 3.0) / dz;
+        else if (j == nz) FX(Bn, i, nz, k) = (-3.0 * FX(uel, i, nz, k) + FX(uel, i, nz - 1, k) / 3.0) / dz;
+    }
+    if (j >= 1 && j <= nz - 1) {
+        if (i == 0) FX(Bn, 0, j, k) = -(3.0 * FX(wel, 1, j, k) - FX(wel, 2, j, k) / 3.0) / dr;
+        else if (i == nr) FX(Bn, nr, j, k) = -(FX(wel, nr - 1, j, k) / 3.0 - 3.0 * FX(wel, nr, j, k)) / dr;
+    }
+    if (j >= 1 && j <= nz) {
+        if (i == 0) FX(Cn, 0, j, k) = (3.0 * FX(vel, 1, j, k) - FX(vel, 2, j, k) / 3.0) / dr;
+        else if (i == nr) FX(Cn, nr, j, k) = (FX(vel, nr - 1, j, k) / 3.0 - 3.0 * FX(vel, nr, j, k)) / dr;
+    }
+    if (i == 0) FX(thn, 0, j, k) = 0.0;
+    else if (i == nr + 1) FX(thn, nr + 1, j, k) = 1.0;
+    const size_t p = (size_t)t;
+    d.fld[GB_R_Ap][p] = d.fld[GB_R_A][p];
+    d.fld[GB_R_A][p] = An[p];
+    d.fld[GB_R_Bp][p] = d.fld[GB_R_B][p];
+    d.fld[GB_R_B][p] = Bn[p];
+    d.fld[GB_R_Cp][p] = d.fld[GB_R_C][p];
+    d.fld[GB_R_C][p] = Cn[p];
+    d.fld[GB_R_thp][p] = d.fld[GB_R_th][p];
+    d.fld[GB_R_th][p] = thn[p];
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid line relaxation (rot3dmg.f:1543-2173)
+// ---------------------------------------------------------------------------
+
+// Solver of each (component, direction): 0 pdma, 1 tdma, 2 ptdma.
+__host__ __device__ __forceinline__ int r3_kind(int comp, int dir)
+{
+    if (dir == 2) return 2;
+    if (dir == 0) return comp == 3 ? 1 : 0;
+    return comp == 1 ? 1 : 0;
+}
+__host__ __device__ __forceinline__ int r3_len(int comp, int dir, int n1, int n2, int n3)
+{
+    if (dir == 0) return comp == 3 ? n1 - 1 : n1;
+    if (dir == 1) return comp == 1 ? n2 - 1 : n2;
+    return n3;
+}
+__host__ __device__ __forceinline__ int r3_tabsize(int kind, int n)
+{
+    return kind == 0 ? 5 * n : kind == 1 ? 3 * n : 6 * n;
+}
+__host__ __device__ __forceinline__ int r3_imax(int comp, int n1) { return comp == 3 ? n1 - 1 : n1; }
+__host__ __device__ __forceinline__ int r3_jmax(int comp, int n2) { return comp == 1 ? n2 - 1 : n2; }
+
+// Matrix row e (0-based) of a line of component comp in direction dir on
+// level L (ti: the line's i for z- and phi-lines), as the reference builds
+// it: relax1 :1576-1598, :1614-1643, :1652-1683; relax2 :1776-1799,
+// :1830-1878, :1890-1926; relax3 :2022-2026, :2060-2081, :2094-2120.
+__device__ void r3_coef(const R3Lev &L, int comp, int dir, int ti, int e, double &a, double &b, double &c, double &dd,
+                        double &ee)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const double hr = L.hr, hhr = L.hhr, hhz = L.hhz, hhp = L.hhp;
+    dd = 0.0;
+    ee = 0.0;
+    if (dir == 0) {
+        const int i = e + 1;
+        if (comp == 1) {
+            const double rval = L.rvc[i];
+            if (i == 1) {
+                a = 0.0;
+                b = 0.0;
+                c = -2.0 / hhr - 1.0 / hr / rval * 0.5 - 2.0 / hhz - 2.0 / hhp / (rval * rval);
+                dd = 5.0 / hhr / 3.0 + 1.0 / hr / rval * 0.5;
+                ee = -0.2 / hhr;
+            } else if (i == n1) {
+                a = -0.2 / hhr;
+                b = 5.0 / hhr / 3.0 - 1.0 / hr / rval * 0.5;
+                c = -2.0 / hhr + 1.0 / hr / rval * 0.5 - 2.0 / hhz - 2.0 / hhp / (rval * rval);
+            } else {
+                a = 0.0;
+                b = 1.0 / hhr - 0.5 / hr / rval;
+                c = -(2.0 / hhr + 2.0 / hhz + 2.0 / hhp / (rval * rval));
+                dd = 1.0 / hhr + 0.5 / hr / rval;
+            }
+        } else if (comp == 2) {
+            const double rval = L.rvc[i];
+            const double rq = rval * rval;
+            if (i == 1) {
+                a = 0.0;
+                b = 0.0;
+                c = -2.0 / hhr - 2.0 / hhp / rq + 1.0 / rq;
+                dd = 5.0 / 3.0 / hhr + 4.0 / 3.0 / hr / rval;
+                ee = -0.2 / hhr;
+            } else if (i == n1) {
+                a = -0.2 / hhr;
+                b = 5.0 / 3.0 / hhr - 4.0 / 3.0 / hr / rval;
+                c = -2.0 / hhr - 2.0 / hhp / rq + 1.0 / rq;
+            } else {
+                a = 0.0;
+                b = 1.0 / hhr - 1.5 / hr / rval;
+                c = -(2.0 / hhr + 2.0 / hhp / rq) + 1.0 / rq;
+                dd = 1.0 / hhr + 1.5 / hr / rval;
+            }
+            c = c - 2.0 / hhz;
+        } else {
+            const double rval = L.rvv[i];
+            const double rq = rval * rval;
+            a = 1.0 / hhr - 1.5 / hr / rval;
+            b = -(2.0 / hhr - 1.0 / rq + 2.0 / hhp / rq);
+            c = 1.0 / hhr + 1.5 / hr / rval;
+            b = b - 2.0 / hhz;
+        }
+    } else if (dir == 1) {
+        const int i = ti, j = e + 1;
+        if (comp == 1) {
+            const double rval = L.rvc[i];
+            a = 1.0 / hhz;
+            b = -(2.0 / hhz + 2.0 / hhp / (rval * rval));
+            c = 1.0 / hhz;
+            if (i == 1) b = b - 2.0 / hhr - 1.0 / hr / rval * 0.5;
+            else if (i == n1) b = b - 2.0 / hhr + 1.0 / hr / rval * 0.5;
+            else b = b - 2.0 / hhr;
+        } else if (comp == 2) {
+            const double rval = L.rvc[i];
+            const double rq = rval * rval;
+            if (j == 1) {
+                a = 0.0;
+                b = 0.0;
+                c = -2.0 / hhz - 2.0 / hhp / rq + 1.0 / rq;
+                dd = 5.0 / 3.0 / hhz;
+                ee = -0.2 / hhz;
+            } else if (j == n2) {
+                a = -0.2 / hhz;
+                b = 5.0 / 3.0 / hhz;
+                c = -2.0 / hhz - 2.0 / hhp / rq + 1.0 / rq;
+            } else {
+                a = 0.0;
+                b = 1.0 / hhz;
+                c = -(2.0 / hhz + 2.0 / hhp / rq) + 1.0 / rq;
+                dd = 1.0 / hhz;
+            }
+            c = c - 2.0 / hhr;
+        } else {
+            const double rval = L.rvv[i];
+            const double rq = rval * rval;
+            if (j == 1) {
+                a = 0.0;
+                b = 0.0;
+                c = -2.0 / hhz - 2.0 / hhr + 1.0 / rq - 2.0 / hhp / rq;
+                dd = 5.0 / hhz / 3.0;
+                ee = -0.2 / hhz;
+            } else if (j == n2) {
+                a = -0.2 / hhz;
+                b = 5.0 / hhz / 3.0;
+                c = -2.0 / hhz - 2.0 / hhr + 1.0 / rq - 2.0 / hhp / rq;
+            } else {
+                a = 0.0;
+                b = 1.0 / hhz;
+                c = -(2.0 / hhz + 2.0 / hhr + 2.0 / hhp / rq) + 1.0 / rq;
+                dd = 1.0 / hhz;
+            }
+        }
+    } else {
+        const int i = ti;
+        if (comp == 1) {
+            const double rval = L.rvc[i];
+            a = 1.0 / hhp / (rval * rval);
+            b = -(2.0 / hhz + 2.0 / hhp / (rval * rval));
+            c = 1.0 / hhp / (rval * rval);
+            if (i == 1) b = b - 2.0 / hhr - 1.0 / hr / rval * 0.5;
+            else if (i == n1) b = b - 2.0 / hhr + 1.0 / hr / rval * 0.5;
+            else b = b - 2.0 / hhr;
+        } else if (comp == 2) {
+            const double rval = L.rvc[i];
+            const double rq = rval * rval;
+            a = 1.0 / hhp / rq;
+            c = 1.0 / hhp / rq;
+            b = -(2.0 / hhp / rq) + 1.0 / rq;
+            b = b - 2.0 / hhr;
+            b = b - 2.0 / hhz;
+        } else {
+            const double rval = L.rvv[i];
+            const double rq = rval * rval;
+            a = 1.0 / hhp / rq;
+            b = -(2.0 / hhr - 1.0 / rq + 2.0 / hhp / rq);
+            c = 1.0 / hhp / rq;
+            b = b - 2.0 / hhz;
+        }
+    }
+}
+
+struct FacJob {
+    int lev, comp, dir, ti;
+    double *tab;
+};
+
+// Runs the matrix half of the reference's eliminations once per line class
+// and records what the right-hand-side half needs (one thread per class).
+//   pdma  [C | B | A | D | E]: divisor c(k) at step k, b(k) as used at step
+//         k-1, a(k), the normalised d(k), e(k); C(n) is the last divisor.
+//   tdma  [F | B | C]: multipliers a(j)/b(j-1), eliminated diagonal, c.
+//   ptdma [A | B | C | F1 | F2 | F3]: eliminated a (fill-in column), b, c;
+//         multipliers of row j and of row n at step j; the last multiplier.
+__global__ void k_r3d_factors(const __grid_constant__ R3Dev d, const FacJob *jobs, int njobs)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= njobs) return;
+    const FacJob J = jobs[q];
+    const R3Lev &L = d.lev[J.lev];
+    const int kind = r3_kind(J.comp, J.dir);
+    const int n = r3_len(J.comp, J.dir, L.n1, L.n2, L.n3);
+    double *T = J.tab;
+    if (kind == 0) {
+        double *Cc = T, *Bb = T + n, *Aa = T + 2 * n, *Dd = T + 3 * n, *Ee = T + 4 * n;
+        for (int e = 0; e < n; ++e) r3_coef(L, J.comp, J.dir, J.ti, e, Aa[e], Bb[e], Cc[e], Dd[e], Ee[e]);
+        for (int k = 0; k <= n - 2; ++k) {
+            const double ck = Cc[k];
+            Dd[k] = Dd[k] / ck;
+            Ee[k] = Ee[k] / ck;
+            Cc[k + 1] = Cc[k + 1] - Bb[k + 1] * Dd[k];
+            if (k != n - 2) Dd[k + 1] = Dd[k + 1] - Bb[k + 1] * Ee[k];
+            if (k != n - 2) {
+                Bb[k + 2] = Bb[k + 2] - Aa[k + 2] * Dd[k];
+                Cc[k + 2] = Cc[k + 2] - Aa[k + 2] * Ee[k];
+            }
+        }
+    } else if (kind == 1) {
+        double *F = T, *Bb = T + n, *Cc = T + 2 * n;
+        double dummy_d, dummy_e;
+        for (int e = 0; e < n; ++e) r3_coef(L, J.comp, J.dir, J.ti, e, F[e], Bb[e], Cc[e], dummy_d, dummy_e);
+        F[0] = 0.0;
+        for (int j = 1; j < n; ++j) {
+            const double fact = F[j] / Bb[j - 1];
+            Bb[j] = Bb[j] - fact * Cc[j - 1];
+            F[j] = fact;
+        }
+    } else {
+        double *a = T, *b = T + n, *c = T + 2 * n, *F1 = T + 3 * n, *F2 = T + 4 * n, *F3 = T + 5 * n;
+        double dummy_d, dummy_e;
+        for (int e = 0; e < n; ++e) {
+            r3_coef(L, J.comp, J.dir, J.ti, e, a[e], b[e], c[e], dummy_d, dummy_e);
+            F1[e] = 0.0;
+            F2[e] = 0.0;
+        }
+        const int N = n - 1;
+        double fact;
+        for (int j = 1; j <= n - 3; ++j) {
+            fact = a[j] / b[j - 1];
+            b[j] = b[j] - fact * c[j - 1];
+            a[j] = -fact * a[j - 1];
+            F1[j] = fact;
+            fact = c[N] / b[j - 1];
+            c[N] = -fact * c[j - 1];
+            b[N] = b[N] - fact * a[j - 1];
+            F2[j] = fact;
+        }
+        fact = a[n - 2] / b[n - 3];
+        b[n - 2] = b[n - 2] - fact * c[n - 3];
+        c[n - 2] = c[n - 2] - fact * a[n - 3];
+        F1[n - 2] = fact;
+        fact = c[N] / b[n - 3];
+        a[N] = a[N] - fact * c[n - 3];
+        b[N] = b[N] - fact * a[n - 3];
+        F2[n - 2] = fact;
+        fact = a[N] / b[n - 2];
+        b[N] = b[N] - fact * c[n - 2];
+        F3[0] = fact;
+    }
+}
+
+static const double F02 = (double)0.2f;   // REAL*4 literal 0.2 (rot3dmg.f:1626, 1800, 2029, 2106 ...)
+
+#define PV(i, j, k) v[(size_t)(i) + (size_t)L1 * ((size_t)(j) + (size_t)L2 * (size_t)(k))]
+#define RF(i, j, k) f[(size_t)(i) + (size_t)L1 * ((size_t)(j) + (size_t)L2 * (size_t)(k))]
+
+// Right-hand side of row e of line (p, q): relax1 :1599-1601, :1616-1640,
+// :1655-1681; relax2 :1798-1816, :1858-1876, :1891-1922; relax3 :2027-2041,
+// :2082-2085, :2096-2118.
+template <int COMP>
+__device__ __forceinline__ double r3_rhs(const R3Lev &L, int dir, int p, int q, int e)
+{
+    const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
+    const double hr = L.hr, hhr = L.hhr, hhz = L.hhz, hhp = L.hhp;
+    const double *v = L.v, *f = L.f;
+    if (dir == 0) {
+        const int i = e + 1, j = p, k = q;
+        const int ka = k == n3 ? 1 : k + 1, km = k - 1;
+        if (COMP == 1) {
+            const double rval = L.rvc[i];
+            return -(PV(i, j + 1, k) + PV(i, j - 1, k)) / hhz - (PV(i, j, ka) + PV(i, j, km)) / hhp / (rval * rval) +
+                   RF(i, j, k);
+        } else if (COMP == 2) {
+            const double rval = L.rvc[i];
+            const double rq = rval * rval;
+            if (j == 1)
+                return -(5.0 / 3.0 * PV(i, j + 1, k) - F02 * PV(i, j + 2, k)) / hhz -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+            if (j == n2)
+                return -(5.0 / 3.0 * PV(i, j - 1, k) - F02 * PV(i, j - 2, k)) / hhz -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+            return -(PV(i, j - 1, k) + PV(i, j + 1, k)) / hhz - (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+        } else {
+            const double rval = L.rvv[i];
+            const double rq = rval * rval;
+            if (j == 1)
+                return -(5.0 * PV(i, j + 1, k) / 3.0 - F02 * PV(i, j + 2, k)) / hhz -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+            if (j == n2)
+                return -(5.0 * PV(i, j - 1, k) / 3.0 - F02 * PV(i, j - 2, k)) / hhz -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+            return -(PV(i, j - 1, k) + PV(i, j + 1, k)) / hhz - (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+        }
+    } else if (dir == 1) {
+        const int i = p, j = e + 1, k = q;
+        const int ka = k == n3 ? 1 : k + 1, km = k - 1;
+        if (COMP == 1) {
+            const double rval = L.rvc[i];
+            if (i == 1)
+                return -(5.0 * PV(i + 1, j, k) / 3.0 - F02 * PV(i + 2, j, k)) / hhr - 1.0 * PV(i + 1, j, k) / hr / rval * 0.5 -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / (rval * rval) + RF(i, j, k);
+            if (i == n1)
+                return -(5.0 * PV(i - 1, j, k) / 3.0 - F02 * PV(i - 2, j, k)) / hhr + 1.0 * PV(i - 1, j, k) / hr / rval * 0.5 -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / (rval * rval) + RF(i, j, k);
+            return -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 0.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval -
+                   (PV(i, j, ka) + PV(i, j, km)) / hhp / (rval * rval) + RF(i, j, k);
+        } else if (COMP == 2) {
+            const double rval = L.rvc[i];
+            const double rq = rval * rval;
+            if (i == 1)
+                return -(5.0 / 3.0 * PV(i + 1, j, k) - 0.2 * PV(i + 2, j, k)) / hhr - 4.0 / 3.0 * PV(i + 1, j, k) / hr / rval -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+            if (i == n1)
+                return -(5.0 / 3.0 * PV(i - 1, j, k) - 0.2 * PV(i - 2, j, k)) / hhr + 4.0 / 3.0 * PV(i - 1, j, k) / hr / rval -
+                       (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+            return -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval -
+                   (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+        } else {
+            const double rval = L.rvv[i];
+            const double rq = rval * rval;
+            return -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval -
+                   (PV(i, j, ka) + PV(i, j, km)) / hhp / rq + RF(i, j, k);
+        }
+    } else {
+        const int i = p, j = q, k = e + 1;
+        if (COMP == 1) {
+            const double rval = L.rvc[i];
+            if (i == 1)
+                return -(5.0 * PV(i + 1, j, k) / 3.0 - F02 * PV(i + 2, j, k)) / hhr - PV(i + 1, j, k) / hr / rval * 0.5 -
+                       (PV(i, j + 1, k) + PV(i, j - 1, k)) / hhz + RF(i, j, k);
+            if (i == n1)
+                return -(5.0 * PV(i - 1, j, k) / 3.0 - F02 * PV(i - 2, j, k)) / hhr + PV(i - 1, j, k) / hr / rval * 0.5 -
+                       (PV(i, j + 1, k) + PV(i, j - 1, k)) / hhz + RF(i, j, k);
+            return -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 0.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval -
+                   (PV(i, j + 1, k) + PV(i, j - 1, k)) / hhz + RF(i, j, k);
+        } else if (COMP == 2) {
+            const double rval = L.rvc[i];
+            double rr;
+            if (i == 1)
+                rr = -(5.0 / 3.0 * PV(i + 1, j, k) - 0.2 * PV(i + 2, j, k)) / hhr - 4.0 / 3.0 * PV(i + 1, j, k) / hr / rval;
+            else if (i == n1)
+                rr = -(5.0 / 3.0 * PV(i - 1, j, k) - 0.2 * PV(i - 2, j, k)) / hhr + 4.0 / 3.0 * PV(i - 1, j, k) / hr / rval;
+            else
+                rr = -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval;
+            if (j == 1) return rr - (5.0 / 3.0 * PV(i, j + 1, k) - 0.2 * PV(i, j + 2, k)) / hhz + RF(i, j, k);
+            if (j == n2) return rr - (5.0 / 3.0 * PV(i, j - 1, k) - 0.2 * PV(i, j - 2, k)) / hhz + RF(i, j, k);
+            return rr - (PV(i, j - 1, k) + PV(i, j + 1, k)) / hhz + RF(i, j, k);
+        } else {
+            const double rval = L.rvv[i];
+            if (j == 1)
+                return -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval -
+                       (5.0 * PV(i, j + 1, k) / 3.0 - F02 * PV(i, j + 2, k)) / hhz + RF(i, j, k);
+            if (j == n2)
+                return -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval -
+                       (5.0 * PV(i, j - 1, k) / 3.0 - F02 * PV(i, j - 2, k)) / hhz + RF(i, j, k);
+            return -(PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr - 1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval -
+                   (PV(i, j + 1, k) + PV(i, j - 1, k)) / hhz + RF(i, j, k);
+        }
+    }
+}
+
+// Solves line (p, q) of direction dir in place: the right-hand side is
+// formed row by row as the forward elimination needs it, the eliminated
+// values are kept in the line's own storage (no line reads its own old
+// values), and back-substitution overwrites them with the solution.  Lines
+// along r and z on plane k = n3 also write plane 0.
+template <int COMP>
+__device__ void r3_line(const R3Lev &L, int dir, int p, int q)
+{
+    const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
+    const int kind = r3_kind(COMP, dir);
+    const int n = r3_len(COMP, dir, n1, n2, n3);
+    double *v = L.v;
+    size_t base;
+    long long step;
+    if (dir == 0) {
+        base = (size_t)1 + (size_t)L1 * ((size_t)p + (size_t)L2 * (size_t)q);
+        step = 1;
+    } else if (dir == 1) {
+        base = (size_t)p + (size_t)L1 * ((size_t)1 + (size_t)L2 * (size_t)q);
+        step = L1;
+    } else {
+        base = (size_t)p + (size_t)L1 * ((size_t)q + (size_t)L2);
+        step = (long long)L1 * L2;
+    }
+    const long long plane = (long long)L1 * L2 * n3;
+    const bool seam = dir != 2 && q == n3;
+    const double *T = L.fac[COMP][dir];
+    if (dir != 0) T += (size_t)(p - 1) * r3_tabsize(kind, n);
+#define MEM(e) v[base + (size_t)((long long)(e) * step)]
+#define PUT(e, x)                                                  \
+    do {                                                           \
+        const double _x = (x);                                     \
+        MEM(e) = _x;                                               \
+        if (seam) v[base + (size_t)((long long)(e) * step) - plane] = _x; \
+    } while (0)
+    if (kind == 0) {
+        const double *Cc = T, *Bb = T + n, *Aa = T + 2 * n, *Dd = T + 3 * n, *Ee = T + 4 * n;
+        double r0 = r3_rhs<COMP>(L, dir, p, q, 0), r1 = r3_rhs<COMP>(L, dir, p, q, 1);
+        for (int k = 0; k <= n - 2; ++k) {
+            const double rk = r0 / Cc[k];
+            MEM(k) = rk;
+            const double rk1 = r1 - Bb[k + 1] * rk;
+            double rk2 = 0.0;
+            if (k != n - 2) rk2 = r3_rhs<COMP>(L, dir, p, q, k + 2) - Aa[k + 2] * rk;
+            r0 = rk1;
+            r1 = rk2;
+        }
+        double x1 = r0 / Cc[n - 1];
+        PUT(n - 1, x1);
+        double x0 = MEM(n - 2) - Dd[n - 2] * x1;
+        PUT(n - 2, x0);
+        double x2 = x1;
+        x1 = x0;
+        for (int j = n - 3; j >= 0; --j) {
+            const double x = MEM(j) - Dd[j] * x1 - Ee[j] * x2;
+            PUT(j, x);
+            x2 = x1;
+            x1 = x;
+        }
+    } else if (kind == 1) {
+        const double *F = T, *Bb = T + n, *Cc = T + 2 * n;
+        double rprev = r3_rhs<COMP>(L, dir, p, q, 0);
+        MEM(0) = rprev;
+        for (int j = 1; j < n; ++j) {
+            const double rj = r3_rhs<COMP>(L, dir, p, q, j) - F[j] * rprev;
+            MEM(j) = rj;
+            rprev = rj;
+        }
+        double y = rprev / Bb[n - 1];
+        PUT(n - 1, y);
+        for (int j = n - 2; j >= 0; --j) {
+            y = (MEM(j) - Cc[j] * y) / Bb[j];
+            PUT(j, y);
+        }
+    } else {
+        const double *Aa = T, *Bb = T + n, *Cc = T + 2 * n, *F1 = T + 3 * n, *F2 = T + 4 * n, *F3 = T + 5 * n;
+        const int N = n - 1;
+        double rN = r3_rhs<COMP>(L, dir, p, q, N);
+        double rprev = r3_rhs<COMP>(L, dir, p, q, 0);
+        MEM(0) = rprev;
+        for (int j = 1; j <= n - 3; ++j) {
+            const double rj = r3_rhs<COMP>(L, dir, p, q, j) - F1[j] * rprev;
+            rN = rN - F2[j] * rprev;
+            MEM(j) = rj;
+            rprev = rj;
+        }
+        const double rn2 = r3_rhs<COMP>(L, dir, p, q, n - 2) - F1[n - 2] * rprev;
+        rN = rN - F2[n - 2] * rprev;
+        MEM(n - 2) = rn2;
+        rN = rN - F3[0] * rn2;
+        const double yN = rN / Bb[N];
+        MEM(N) = yN;
+        double y = (rn2 - Cc[n - 2] * yN) / Bb[n - 2];
+        MEM(n - 2) = y;
+        for (int j = n - 3; j >= 0; --j) {
+            y = (MEM(j) - Cc[j] * y - Aa[j] * yN) / Bb[j];
+            MEM(j) = y;
+        }
+        v[base - (size_t)step] = yN;   // plane 0 = plane n3
+    }
+#undef MEM
+#undef PUT
+}
+
+// Residual rc = rf - A psif at the level's unknowns (relax1 :1688-1720,
+// relax2 :1935-1977, relax3 :2129-2160), one point per call.
+template <int COMP>
+__device__ __forceinline__ double r3_resid(const R3Lev &L, int i, int j, int k)
+{
+    const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
+    const double hr = L.hr, hhr = L.hhr, hhz = L.hhz, hhp = L.hhp;
+    const double *v = L.v, *f = L.f;
+    const int ka = k == n3 ? 1 : k + 1, km = k - 1;
+    double temp;
+    if (COMP == 1) {
+        const double rval = L.rvc[i];
+        temp = (PV(i, j + 1, k) + PV(i, j - 1, k)) / hhz + (PV(i, j, ka) + PV(i, j, km)) / hhp / (rval * rval) -
+               PV(i, j, k) * (2.0 / hhz + 2.0 / hhp / (rval * rval));
+        if (i == 1)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 * PV(i + 1, j, k) / 3.0 - 0.2 * PV(i + 2, j, k)) / hhr +
+                   0.5 * (-PV(i, j, k) + PV(i + 1, j, k)) / hr / rval;
+        else if (i == n1)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 * PV(i - 1, j, k) / 3.0 - 0.2 * PV(i - 2, j, k)) / hhr +
+                   0.5 * (PV(i, j, k) - PV(i - 1, j, k)) / hr / rval;
+        else
+            temp = temp + (PV(i - 1, j, k) - 2.0 * PV(i, j, k) + PV(i + 1, j, k)) / hhr +
+                   0.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval;
+    } else if (COMP == 2) {
+        const double rval = L.rvc[i];
+        const double rq = rval * rval;
+        temp = (PV(i, j, ka) - 2.0 * PV(i, j, k) + PV(i, j, km)) / hhp / rq + PV(i, j, k) / rq;
+        if (i == 1)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 / 3.0 * PV(i + 1, j, k) - 0.2 * PV(i + 2, j, k)) / hhr +
+                   4.0 / 3.0 * PV(i + 1, j, k) / hr / rval;
+        else if (i == n1)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 / 3.0 * PV(i - 1, j, k) - 0.2 * PV(i - 2, j, k)) / hhr -
+                   4.0 / 3.0 * PV(i - 1, j, k) / hr / rval;
+        else
+            temp = temp + (PV(i - 1, j, k) - 2.0 * PV(i, j, k) + PV(i + 1, j, k)) / hhr +
+                   1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval;
+        if (j == 1)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 / 3.0 * PV(i, j + 1, k) - 0.2 * PV(i, j + 2, k)) / hhz;
+        else if (j == n2)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 / 3.0 * PV(i, j - 1, k) - 0.2 * PV(i, j - 2, k)) / hhz;
+        else
+            temp = temp + (PV(i, j + 1, k) - 2.0 * PV(i, j, k) + PV(i, j - 1, k)) / hhz;
+    } else {
+        const double rval = L.rvv[i];
+        const double rq = rval * rval;
+        temp = (PV(i + 1, j, k) + PV(i - 1, j, k)) / hhr + 1.5 * (PV(i + 1, j, k) - PV(i - 1, j, k)) / hr / rval +
+               PV(i, j, k) / rq + (PV(i, j, ka) + PV(i, j, km)) / hhp / rq - PV(i, j, k) * (2.0 / hhr + 2.0 / hhp / rq);
+        if (j == 1)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 * PV(i, j + 1, k) / 3.0 - 0.2 * PV(i, j + 2, k)) / hhz;
+        else if (j == n2)
+            temp = temp + (-2.0 * PV(i, j, k) + 5.0 * PV(i, j - 1, k) / 3.0 - 0.2 * PV(i, j - 2, k)) / hhz;
+        else
+            temp = temp + (PV(i, j + 1, k) - 2.0 * PV(i, j, k) + PV(i, j - 1, k)) / hhz;
+    }
+    return RF(i, j, k) - temp;
+}
+
+#undef PV
+#undef RF
+
+struct SolveCtx {
+    int m;              // residual evaluations so far (selects the max slot)
+};
+
+// One relaxation call relax<COMP>(nrel, klev); returns false when a grid
+// barrier timed out.
+template <int COMP>
+__device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx)
+{
+    const R3Lev &L = d.lev[klev];
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const int im = r3_imax(COMP, L.n1), jm = r3_jmax(COMP, L.n2), n3 = L.n3;
+    for (int irel = 1; irel <= d.nrel; ++irel) {
+        for (int dir = 0; dir < 3; ++dir) {
+            const int *lines = L.lines[COMP][dir];
+            const int *off = L.poff[COMP][dir];
+            for (int ph = 0; ph < L.nphase[COMP][dir]; ++ph) {
+                const int a = off[ph], b = off[ph + 1];
+                for (long long t = a + gt; t < b; t += T) {
+                    const int pk = lines[t];
+                    r3_line<COMP>(L, dir, pk & 0xffff, pk >> 16);
+                }
+                if (!grid_sync(d.gs)) return false;
+            }
+        }
+        // residual and its max norm into slot m & 1; the other slot is
+        // cleared for the next evaluation (nobody reads it before then)
+        const int slot = cx.m & 1;
+        if (gt == 0) {
+            d.resmax[slot ^ 1] = 0ull;
+            d.nanflag[slot ^ 1] = 0;
+        }
+        const long long npts = (long long)im * jm * n3;
+        double lmax = 0.0;
+        int lnan = 0;
+        for (long long t = gt; t < npts; t += T) {
+            const int i = 1 + (int)(t % im);
+            const long long rest = t / im;
+            const int j = 1 + (int)(rest % jm);
+            const int k = 1 + (int)(rest / jm);
+            const double r = r3_resid<COMP>(L, i, j, k);
+            L.res[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = r;
+            const double a = fabs(r);
+            if (a != a) lnan = 1;
+            if (a > lmax) lmax = a;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+            lnan |= __shfl_xor_sync(0xffffffffu, lnan, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if (lmax > 0.0) atomicMax(&d.resmax[slot], (unsigned long long)__double_as_longlong(lmax));
+            if (lnan) atomicOr(&d.nanflag[slot], 1);
+        }
+        cx.m++;
+        if (!grid_sync(d.gs)) return false;
+    }
+    return true;
+}
+
+// corser (rot3dmg.f:2176-2265): coarse right-hand side and zero correction.
+__device__ void r3_corser(const R3Dev &d, int klev)
+{
+    const R3Lev &F = d.lev[klev], &Cl = d.lev[klev + 1];
+    const int n1c = Cl.n1, n2c = Cl.n2, n3c = Cl.n3;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long npts = (long long)Cl.L1 * Cl.L2 * (n3c + 1);
+    const double *rf = F.res;
+    const size_t F1 = (size_t)F.L1, F2 = (size_t)F.L2;
+#define R(i, j, k) rf[(size_t)(i) + F1 * ((size_t)(j) + F2 * (size_t)(k))]
+    for (long long t = gt; t < npts; t += T) {
+        const int i = (int)(t % Cl.L1);
+        const long long rest = t / Cl.L1;
+        const int j = (int)(rest % Cl.L2);
+        const int k = (int)(rest / Cl.L2);
+        double val;
+        if (i == 0 || i == n1c || j == 0 || j == n2c) {
+            val = 0.0;
+        } else if (k == 0 || k == n3c) {
+            val = R(i, j, k);
+        } else {
+            const int ii = i + i, jj = j + j, kk = k + k;
+            const int iip = ii + 1, iim = ii - 1, jjp = jj + 1, jjm = jj - 1, kkp = kk + 1, kkm = kk - 1;
+            double temp = R(ii, jj, kk);
+            temp = temp + temp + R(iip, jj, kk) + R(iim, jj, kk) + R(ii, jjp, kk) + R(ii, jjm, kk) + R(ii, jj, kkp) +
+                   R(ii, jj, kkm);
+            temp = temp + temp + R(iip, jjp, kk) + R(iip, jjm, kk) + R(iim, jjp, kk) + R(iim, jjm, kk) + R(iip, jj, kkp) +
+                   R(iip, jj, kkm) + R(iim, jj, kkp) + R(iim, jj, kkm) + R(ii, jjp, kkp) + R(ii, jjp, kkm) +
+                   R(ii, jjm, kkp) + R(ii, jjm, kkm);
+            temp = temp + temp + R(iip, jjp, kkp) + R(iip, jjp, kkm) + R(iip, jjm, kkp) + R(iip, jjm, kkm) +
+                   R(iim, jjm, kkp) + R(iim, jjm, kkm) + R(iim, jjp, kkp) + R(iim, jjp, kkm);
+            val = temp * 0.015625;
+        }
+        Cl.f[t] = val;
+        Cl.v[t] = 0.0;
+    }
+#undef R
+}
+
+// finer (rot3dmg.f:2268-2344): trilinear prolongation added to the fine
+// level.  The coarse correction is cleared by the next corser.
+__device__ void r3_finer(const R3Dev &d, int klev)
+{
+    const R3Lev &Cl = d.lev[klev], &F = d.lev[klev - 1];
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long npts = (long long)F.L1 * F.L2 * (F.n3 + 1);
+    const double *pc = Cl.v;
+    const size_t C1 = (size_t)Cl.L1, C2 = (size_t)Cl.L2;
+#define PC(i, j, k) pc[(size_t)(i) + C1 * ((size_t)(j) + C2 * (size_t)(k))]
+    for (long long t = gt; t < npts; t += T) {
+        const int i = (int)(t % F.L1);
+        const long long rest = t / F.L1;
+        const int j = (int)(rest % F.L2);
+        const int k = (int)(rest / F.L2);
+        const int i1 = i / 2, j1 = j / 2, k1 = k / 2;
+        const bool ie = i1 * 2 == i, je = j1 * 2 == j, ke = k1 * 2 == k;
+        double p;
+        if (ie) {
+            if (je) {
+                if (ke) p = PC(i1, j1, k1);
+                else p = (PC(i1, j1, k1) + PC(i1, j1, k1 + 1)) * 0.5;
+            } else {
+                if (ke) p = (PC(i1, j1, k1) + PC(i1, j1 + 1, k1)) * 0.5;
+                else p = (PC(i1, j1, k1) + PC(i1, j1 + 1, k1) + PC(i1, j1, k1 + 1) + PC(i1, j1 + 1, k1 + 1)) * 0.25;
+            }
+        } else {
+            if (je) {
+                if (ke) p = (PC(i1, j1, k1) + PC(i1 + 1, j1, k1)) * 0.5;
+                else p = (PC(i1, j1, k1) + PC(i1 + 1, j1, k1) + PC(i1, j1, k1 + 1) + PC(i1 + 1, j1, k1 + 1)) * 0.25;
+            } else {
+                if (ke)
+                    p = (PC(i1, j1, k1) + PC(i1 + 1, j1, k1) + PC(i1, j1 + 1, k1) + PC(i1 + 1, j1 + 1, k1)) * 0.25;
+                else
+                    p = (PC(i1, j1, k1) + PC(i1 + 1, j1, k1) + PC(i1, j1 + 1, k1) + PC(i1 + 1, j1 + 1, k1) +
+                         PC(i1, j1, k1 + 1) + PC(i1 + 1, j1, k1 + 1) + PC(i1, j1 + 1, k1 + 1) +
+                         PC(i1 + 1, j1 + 1, k1 + 1)) *
+                        0.125;
+            }
+        }
+        F.v[t] = p + F.v[t];
+    }
+#undef PC
+}
+
+// poisson1/2/3 (rot3dmg.f:1216-1540) in one cooperative launch.
+template <int COMP>
+__global__ void __launch_bounds__(R3_THREADS) k_r3d_solve(const __grid_constant__ R3Dev d, int step)
+{
+    if (*(volatile int *)d.abort) return;
+    const int ni = d.ni, nj = d.nj;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    double *psi = d.fld[COMP == 1 ? GB_R_wel : COMP == 2 ? GB_R_vel : GB_R_uel];
+    double *psip = d.fld[COMP == 1 ? GB_R_welp : COMP == 2 ? GB_R_velp : GB_R_uelp];
+    const double *rhs = d.fld[COMP == 1 ? GB_R_wrh : COMP == 2 ? GB_R_vrh : GB_R_urh];
+    const R3Lev &L = d.lev[1];
+    const long long n1p = L.L1, n2p = L.L2;
+    const long long nlvl = n1p * n2p * (L.n3 + 1);
+    for (long long t = gt; t < nlvl; t += T) {
+        const int i = (int)(t % n1p);
+        const long long rest = t / n1p;
+        const int j = (int)(rest % n2p);
+        const int k = (int)(rest / n2p);
+        L.f[t] = FX(rhs, i, j, k);
+        L.v[t] = 2.0 * FX(psi, i, j, k) - FX(psip, i, j, k);
+    }
+    if (!grid_sync(d.gs)) return;
+    SolveCtx cx;
+    cx.m = 0;
+    int status = GB_MAXSWEEPS, sweeps = d.maxsweeps;
+    const int nlev = d.nlev;
+    for (int sweep = 1; sweep <= d.maxsweeps; ++sweep) {
+        if (sweep != 1) {
+            for (long long t = gt; t < nlvl; t += T) {
+                const int i = (int)(t % n1p);
+                const long long rest = t / n1p;
+                const int j = (int)(rest % n2p);
+                const int k = (int)(rest / n2p);
+                const double pp = FX(psip, i, j, k);
+                const double nv = pp + d.sor * (L.v[t] - pp);
+                L.v[t] = nv;
+                FX(psip, i, j, k) = nv;
+            }
+            if (!grid_sync(d.gs)) return;
+        }
+        if (sweep == 1 || nlev == 1) {
+            if (!r3_relax<COMP>(d, 1, cx)) return;
+            for (long long t = gt; t < nlvl; t += T) {
+                const int i = (int)(t % n1p);
+                const long long rest = t / n1p;
+                const int j = (int)(rest % n2p);
+                const int k = (int)(rest / n2p);
+                FX(psip, i, j, k) = L.v[t];
+            }
+            if (!grid_sync(d.gs)) return;
+        }
+        if (nlev > 1) {
+            for (int l = 1; l <= nlev - 1; ++l) {
+                r3_corser(d, l);
+                if (!grid_sync(d.gs)) return;
+                if (!r3_relax<COMP>(d, l + 1, cx)) return;
+            }
+            for (int l = nlev; l >= 2; --l) {
+                r3_finer(d, l);
+                if (!grid_sync(d.gs)) return;
+                if (!r3_relax<COMP>(d, l - 1, cx)) return;
+            }
+        }
+        const int slot = (cx.m - 1) & 1;
+        const double resmax = __longlong_as_double((long long)*(volatile unsigned long long *)&d.resmax[slot]);
+        if (*(volatile int *)&d.nanflag[slot]) {
+            status = GB_NAN;
+            sweeps = sweep;
+            break;
+        }
+        if (resmax < d.tolcon) {
+            status = GB_OK;
+            sweeps = sweep;
+            break;
+        }
+    }
+    if (status == GB_OK) {
+        const int imax = COMP == 3 ? d.nr : d.nr + 1;
+        const int jmax = COMP == 1 ? d.nz : d.nz + 1;
+        const int ii1 = COMP == 3 ? d.nr - 1 : d.nr;
+        const int jj1 = COMP == 1 ? d.nz - 1 : d.nz;
+        const long long npts = (long long)(imax + 1) * (jmax + 1) * (d.np + 1);
+        for (long long t = gt; t < npts; t += T) {
+            const int i = (int)(t % (imax + 1));
+            const long long rest = t / (imax + 1);
+            const int j = (int)(rest % (jmax + 1));
+            const int k = (int)(rest / (jmax + 1));
+            const double old = FX(psi, i, j, k);
+            FX(psip, i, j, k) = old;
+            const bool inner = i >= 1 && i <= ii1 && j >= 1 && j <= jj1;
+            FX(psi, i, j, k) = inner ? L.v[(size_t)i + (size_t)n1p * ((size_t)j + (size_t)n2p * (size_t)k)] : 0.0;
+        }
+    }
+    if (gt == 0) {
+        *d.solve_status = status;
+        *d.solve_sweeps = sweeps;
+        if (step >= 0) d.hist_sw[3 * step + COMP - 1] = sweeps;
+        if (status != GB_OK) atomicExch(d.abort, status);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct gb_r3d {
+    gb_r3d_params p;
+    R3Dev dev;
+    double *fields = nullptr, *pool = nullptr;
+    int *itab = nullptr;
+    void *small = nullptr;
+    double *hist_nu = nullptr;
+    int *hist_sw = nullptr;
+    int hist_cap = 0;
+    unsigned *sync = nullptr;
+    int grid = 0;
+    cudaStream_t stream = nullptr;
+};
+
+static int r3_levels(int nr, int nz)
+{
+    int nlev = 0, itest = nr, itest2 = nr, jtest = nz, jtest2 = nz;
+    for (int i = 2; i <= 8; ++i) {
+        itest /= 2;
+        jtest /= 2;
+        if (itest * 2 - itest2 == 0 && jtest * 2 - jtest2 == 0) {
+            if (itest2 >= 4 && jtest2 >= 4) nlev++;
+            itest2 = itest;
+            jtest2 = jtest;
+        } else {
+            break;
+        }
+    }
+    if (nlev > 4) nlev = 4;
+    return nlev < 1 ? 1 : nlev;
+}
+
+extern "C" void gb_r3d_default_params(gb_r3d_params *p, int nr, int nz, int np)
+{
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->nr = nr;
+    p->nz = nz;
+    p->np = np;
+    p->dt = 1e-5;
+    p->r0 = 0.5;
+    p->rmax = 1.0;
+    p->zmax = 0.5;
+    p->Ra = 1e6;
+    p->Re = 500.0;
+    p->Gr = 0.0;
+    p->Pr = 7.0;
+    p->tolcon = 1e-5;
+    p->sor = 1.2;
+    p->maxsweeps = 500;
+    p->nrel = 2;
+    p->smoother = GB_SMOOTHER_LEX;
+    p->precision = GB_PRB_FP64;
+}
+
+extern "C" int gb_r3d_destroy(gb_r3d *h)
+{
+    if (!h) return GB_OK;
+    cudaFree(h->fields);
+    cudaFree(h->pool);
+    cudaFree(h->itab);
+    cudaFree(h->small);
+    cudaFree(h->hist_nu);
+    cudaFree(h->hist_sw);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GB_OK;
+}
+
+// Phase lists of one (level, component, direction), as packed (p, q).
+static void r3_phases(int mode, int comp, int dir, int n1, int n2, int n3, std::vector<int> &lines, std::vector<int> &off)
+{
+    const int im = r3_imax(comp, n1), jm = r3_jmax(comp, n2);
+    int P, Q, p_os, q_os;
+    if (dir == 0) {
+        P = jm;
+        Q = n3;
+        p_os = comp != 1;
+        q_os = 0;
+    } else if (dir == 1) {
+        P = im;
+        Q = n3;
+        p_os = comp != 3;
+        q_os = 0;
+    } else {
+        P = im;
+        Q = jm;
+        p_os = comp != 3;
+        q_os = comp != 1;
+    }
+    off.clear();
+    lines.clear();
+    off.push_back(0);
+    if (mode == GB_SMOOTHER_LEX) {
+        for (int dsum = 2; dsum <= P + Q; ++dsum) {
+            for (int p = std::max(1, dsum - Q); p <= std::min(P, dsum - 1); ++p) lines.push_back(p | ((dsum - p) << 16));
+            off.push_back((int)lines.size());
+        }
+    } else {
+        for (int colour = 0; colour < 2; ++colour)
+            for (int cls = 0; cls < 3; ++cls) {
+                const size_t before = lines.size();
+                for (int q = 1; q <= Q; ++q)
+                    for (int p = 1; p <= P; ++p) {
+                        const int c = (p_os && (p == 1 || p == P)) + (q_os && (q == 1 || q == Q));
+                        if (((p + q) & 1) == colour && c == cls) lines.push_back(p | (q << 16));
+                    }
+                if (lines.size() != before) off.push_back((int)lines.size());
+            }
+    }
+}
+
+extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out)
+{
+    if (!p || !out) { gb_set_error("gb_r3d_create: null argument"); return GB_ERR_INVALID; }
+    *out = nullptr;
+    const int nr = p->nr, nz = p->nz, np = p->np;
+    const int nlev = r3_levels(nr, nz);
+    if (nlev_out) *nlev_out = nlev;
+    if (nr < 4 || nz < 4 || np < 4 || nr > 4096 || nz > 4096 || np > 16384 || np % (1 << nlev) != 0 ||
+        np / (1 << (nlev - 1)) < 4 || !(p->r0 > 0.0 && p->rmax > p->r0) || !(p->zmax > 0.0) || !(p->dt > 0.0) ||
+        p->Pr == 0.0 || p->Re == 0.0 || p->nrel < 1 || p->maxsweeps < 1) {
+        gb_set_error("gb_r3d_create: unsupported parameters (nr=%d nz=%d np=%d: nr, nz >= 4, np a multiple of 2^%d "
+                     "with >= 4 phi intervals on the coarsest level; 0 < r0 < rmax, zmax, dt > 0, Pr, Re != 0)",
+                     nr, nz, np, nlev);
+        return GB_ERR_INVALID;
+    }
+    if (p->smoother != GB_SMOOTHER_LEX && p->smoother != GB_SMOOTHER_ZEBRA) {
+        gb_set_error("gb_r3d_create: unknown smoother %d", p->smoother);
+        return GB_ERR_INVALID;
+    }
+    if (p->precision != GB_PRB_FP64) {
+        gb_set_error("gb_r3d_create: precision %d not available for the 3D annulus", p->precision);
+        return GB_ERR_INVALID;
+    }
+    gb_r3d *h = new gb_r3d();
+    h->p = *p;
+    R3Dev &d = h->dev;
+    memset(&d, 0, sizeof(d));
+    d.nr = nr;
+    d.nz = nz;
+    d.np = np;
+    d.ni = nr + 2;
+    d.nj = nz + 2;
+    d.nk = np + 1;
+    d.nlev = nlev;
+    d.dt = p->dt;
+    d.r0 = p->r0;
+    d.rmax = p->rmax;
+    d.zmax = p->zmax;
+    d.Ra = p->Ra;
+    d.Re = p->Re;
+    d.Gr = p->Gr;
+    d.Ptl = p->Pr;
+    const double pi = acos(-1.0);
+    d.dr = (p->rmax - p->r0) / (double)nr;
+    d.dz = p->zmax / (double)nz;
+    d.dp = 2.0 * pi / (double)np;
+    d.nu_num = -p->r0 * log(p->r0 / p->rmax);
+    d.nu_den = p->zmax * 2.0 * pi;
+    d.tolcon = p->tolcon;
+    d.sor = p->sor;
+    d.nrel = p->nrel;
+    d.maxsweeps = p->maxsweeps;
+    const size_t fsz = (size_t)d.ni * d.nj * d.nk;
+    cudaError_t e = cudaMalloc(&h->fields, sizeof(double) * fsz * GB_R_COUNT);
+    if (e != cudaSuccess) { gb_set_error("gb_r3d_create: fields: %s", cudaGetErrorString(e)); delete h; return GB_ERR_ALLOC; }
+    cudaMemset(h->fields, 0, sizeof(double) * fsz * GB_R_COUNT);
+    for (int q = 0; q < GB_R_COUNT; ++q) d.fld[q] = h->fields + (size_t)q * fsz;
+
+    // multigrid pool: per level v, f, res, rvc, rvv and the factor tables
+    std::vector<FacJob> jobs;
+    size_t need = 0;
+    std::vector<size_t> fac_off;   // per (level, comp, dir) start, filled below
+    for (int l = 1; l <= nlev; ++l) {
+        const int n1 = nr >> (l - 1), n2 = nz >> (l - 1), n3 = np >> (l - 1);
+        need += 3 * (size_t)(n1 + 1) * (n2 + 1) * (n3 + 1) + 2 * (size_t)(n1 + 2);
+        for (int comp = 1; comp <= 3; ++comp)
+            for (int dir = 0; dir < 3; ++dir) {
+                const int n = r3_len(comp, dir, n1, n2, n3);
+                const int inst = dir == 0 ? 1 : r3_imax(comp, n1);
+                need += (size_t)inst * r3_tabsize(r3_kind(comp, dir), n);
+            }
+    }
+    e = cudaMalloc(&h->pool, sizeof(double) * need);
+    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: multigrid pool"); return GB_ERR_ALLOC; }
+    cudaMemset(h->pool, 0, sizeof(double) * need);
+    double *b = h->pool;
+    std::vector<int> itab;
+    struct TabRef { int l, comp, dir; size_t lines, off; int nphase; };
+    std::vector<TabRef> refs;
+    std::vector<double> rv_host;
+    for (int l = 1; l <= nlev; ++l) {
+        R3Lev &L = d.lev[l];
+        L.n1 = nr >> (l - 1);
+        L.n2 = nz >> (l - 1);
+        L.n3 = np >> (l - 1);
+        L.L1 = L.n1 + 1;
+        L.L2 = L.n2 + 1;
+        const int p2 = 1 << l;
+        L.hr = d.dr * (double)p2 * 0.5;
+        L.hz = d.dz * (double)p2 * 0.5;
+        L.hp = d.dp * (double)p2 * 0.5;
+        L.hhr = L.hr * L.hr;
+        L.hhz = L.hz * L.hz;
+        L.hhp = L.hp * L.hp;
+        const size_t sz = (size_t)L.L1 * L.L2 * (L.n3 + 1);
+        L.v = b; b += sz;
+        L.f = b; b += sz;
+        L.res = b; b += sz;
+        L.rvc = b; b += L.n1 + 2;
+        L.rvv = b; b += L.n1 + 2;
+        rv_host.assign(2 * (size_t)(L.n1 + 2), 0.0);
+        for (int i = 0; i <= L.n1 + 1; ++i) {
+            rv_host[i] = d.r0 + ((double)i - 0.5) * L.hr;
+            rv_host[L.n1 + 2 + i] = (double)i * L.hr + d.r0;
+        }
+        cudaMemcpy(L.rvc, rv_host.data(), sizeof(double) * rv_host.size(), cudaMemcpyHostToDevice);
+        for (int comp = 1; comp <= 3; ++comp)
+            for (int dir = 0; dir < 3; ++dir) {
+                const int kind = r3_kind(comp, dir);
+                const int n = r3_len(comp, dir, L.n1, L.n2, L.n3);
+                const int inst = dir == 0 ? 1 : r3_imax(comp, L.n1);
+                L.fac[comp][dir] = b;
+                for (int q = 0; q < inst; ++q) jobs.push_back({l, comp, dir, dir == 0 ? 0 : q + 1, b + (size_t)q * r3_tabsize(kind, n)});
+                b += (size_t)inst * r3_tabsize(kind, n);
+                std::vector<int> lines, off;
+                r3_phases(p->smoother, comp, dir, L.n1, L.n2, L.n3, lines, off);
+                TabRef tr;
+                tr.l = l;
+                tr.comp = comp;
+                tr.dir = dir;
+                tr.lines = itab.size();
+                itab.insert(itab.end(), lines.begin(), lines.end());
+                tr.off = itab.size();
+                itab.insert(itab.end(), off.begin(), off.end());
+                tr.nphase = (int)off.size() - 1;
+                refs.push_back(tr);
+            }
+    }
+    if ((size_t)(b - h->pool) != need) {
+        gb_r3d_destroy(h);
+        gb_set_error("gb_r3d_create: multigrid pool layout mismatch");
+        return GB_ERR_CUDA;
+    }
+    e = cudaMalloc(&h->itab, sizeof(int) * itab.size());
+    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: phase tables"); return GB_ERR_ALLOC; }
+    cudaMemcpy(h->itab, itab.data(), sizeof(int) * itab.size(), cudaMemcpyHostToDevice);
+    for (const TabRef &tr : refs) {
+        R3Lev &L = d.lev[tr.l];
+        L.lines[tr.comp][tr.dir] = h->itab + tr.lines;
+        L.poff[tr.comp][tr.dir] = h->itab + tr.off;
+        L.nphase[tr.comp][tr.dir] = tr.nphase;
+    }
+    // small state
+    e = cudaMalloc(&h->small, 4096 + sizeof(double) * (size_t)(np + 2));
+    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: state"); return GB_ERR_ALLOC; }
+    cudaMemset(h->small, 0, 4096 + sizeof(double) * (size_t)(np + 2));
+    char *sm = (char *)h->small;
+    d.resmax = (unsigned long long *)(sm + 0);
+    d.nanflag = (int *)(sm + 64);
+    d.abort = (int *)(sm + 128);
+    d.steps_done = (int *)(sm + 192);
+    d.solve_status = (int *)(sm + 256);
+    d.solve_sweeps = (int *)(sm + 320);
+    h->sync = (unsigned *)(sm + 384);
+    d.trans = (double *)(sm + 4096);
+    d.gs.count = h->sync;
+    d.gs.gen = h->sync + 1;
+    d.gs.err = (int *)(h->sync + 2);
+    d.gs.limit = 1LL << 24;
+    // factor tables
+    FacJob *djobs = nullptr;
+    e = cudaMalloc(&djobs, sizeof(FacJob) * jobs.size());
+    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: factor jobs"); return GB_ERR_ALLOC; }
+    cudaMemcpy(djobs, jobs.data(), sizeof(FacJob) * jobs.size(), cudaMemcpyHostToDevice);
+    k_r3d_factors<<<gb_ceil_div(jobs.size(), 64), 64>>>(d, djobs, (int)jobs.size());
+    e = cudaDeviceSynchronize();
+    cudaFree(djobs);
+    if (e != cudaSuccess) { gb_set_error("gb_r3d_create: factors: %s", cudaGetErrorString(e)); gb_r3d_destroy(h); return GB_ERR_CUDA; }
+    // cooperative grid: every block resident
+    int dev = 0, sms = 0, coop = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    int worst = 1 << 30;
+    const void *kerns[3] = {(const void *)k_r3d_solve<1>, (const void *)k_r3d_solve<2>, (const void *)k_r3d_solve<3>};
+    for (int q = 0; q < 3; ++q) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[q], R3_THREADS, 0);
+        worst = std::min(worst, per_sm);
+    }
+    if (!coop || worst < 1) {
+        gb_r3d_destroy(h);
+        gb_set_error("gb_r3d_create: cooperative launch unavailable (coop=%d, blocks/SM=%d)", coop, worst);
+        return GB_ERR_CUDA;
+    }
+    h->grid = sms * std::min(worst, 2);
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: stream"); return GB_ERR_CUDA; }
+    *out = h;
+    return GB_OK;
+}
+
+extern "C" void *gb_r3d_stream(gb_r3d *h) { return h ? (void *)h->stream : nullptr; }
+
+static int r3_io(gb_r3d *h, int field, double *host, int ld1, int ld2, bool to_dev)
+{
+    if (!h || !host || field < 0 || field >= GB_R_COUNT || ld1 < h->dev.ni || ld2 < h->dev.nj) {
+        gb_set_error("gb_r3d_%s_field: invalid argument", to_dev ? "set" : "get");
+        return GB_ERR_INVALID;
+    }
+    const R3Dev &d = h->dev;
+    cudaMemcpy3DParms m;
+    memset(&m, 0, sizeof(m));
+    cudaPitchedPtr hp = make_cudaPitchedPtr(host, sizeof(double) * (size_t)ld1, (size_t)d.ni, (size_t)ld2);
+    cudaPitchedPtr dp = make_cudaPitchedPtr(d.fld[field], sizeof(double) * (size_t)d.ni, (size_t)d.ni, (size_t)d.nj);
+    m.srcPtr = to_dev ? hp : dp;
+    m.dstPtr = to_dev ? dp : hp;
+    m.extent = make_cudaExtent(sizeof(double) * (size_t)d.ni, (size_t)d.nj, (size_t)d.nk);
+    m.kind = to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    GB_CUDA_TRY(cudaMemcpy3DAsync(&m, h->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_r3d_set_field(gb_r3d *h, int field, const double *host, int ld1, int ld2)
+{
+    return r3_io(h, field, (double *)host, ld1, ld2, true);
+}
+
+extern "C" int gb_r3d_get_field(gb_r3d *h, int field, double *host, int ld1, int ld2)
+{
+    return r3_io(h, field, host, ld1, ld2, false);
+}
+
+static const int R3_TPB = 256;
+
+static void r3_launch_transport(gb_r3d *h, int what, int step, cudaStream_t s)
+{
+    const R3Dev &d = h->dev;
+    const long long nr = d.nr, nz = d.nz, npp = d.np + 1;
+    switch (what) {
+    case 0: k_r3d_avort<<<gb_ceil_div(nr * (nz - 1) * npp, R3_TPB), R3_TPB, 0, s>>>(d); break;
+    case 1: k_r3d_bvort<<<gb_ceil_div((nr - 1) * (nz - 1) * npp, R3_TPB), R3_TPB, 0, s>>>(d); break;
+    case 2: k_r3d_cvort<<<gb_ceil_div((nr - 1) * nz * npp, R3_TPB), R3_TPB, 0, s>>>(d); break;
+    case 3: k_r3d_temp<<<gb_ceil_div(nr * (nz + 2) * npp, R3_TPB), R3_TPB, 0, s>>>(d); break;
+    case 4:
+        k_r3d_heat_k<<<gb_ceil_div(d.np, 128), 128, 0, s>>>(d);
+        k_r3d_heat_sum<<<1, 32, 0, s>>>(d, step);
+        break;
+    case 5: k_r3d_rhs<1><<<gb_ceil_div(nr * (nz - 1) * npp, R3_TPB), R3_TPB, 0, s>>>(d); break;
+    case 6: k_r3d_rhs<2><<<gb_ceil_div(nr * nz * npp, R3_TPB), R3_TPB, 0, s>>>(d); break;
+    case 7: k_r3d_rhs<3><<<gb_ceil_div((nr - 1) * nz * npp, R3_TPB), R3_TPB, 0, s>>>(d); break;
+    case 8: k_r3d_update<<<gb_ceil_div((long long)d.ni * d.nj * d.nk, R3_TPB), R3_TPB, 0, s>>>(d, step); break;
+    }
+}
+
+static int r3_launch_solve(gb_r3d *h, int comp, int step, cudaStream_t s)
+{
+    GB_CUDA_TRY(cudaMemsetAsync(h->sync, 0, sizeof(unsigned) * 4, s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.resmax, 0, sizeof(unsigned long long) * 2, s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.nanflag, 0, sizeof(int) * 2, s));
+    R3Dev D = h->dev;
+    void *args[] = {&D, &step};
+    const void *k = comp == 1 ? (const void *)k_r3d_solve<1> : comp == 2 ? (const void *)k_r3d_solve<2>
+                                                                        : (const void *)k_r3d_solve<3>;
+    cudaError_t e = cudaLaunchCooperativeKernel(k, h->grid, R3_THREADS, args, 0, s);
+    if (e != cudaSuccess) {
+        gb_set_error("gb_r3d: cooperative solve launch (%d blocks): %s", h->grid, cudaGetErrorString(e));
+        return GB_ERR_CUDA;
+    }
+    return GB_OK;
+}
+
+static int r3_sync(gb_r3d *h, const char *what)
+{
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { gb_set_error("%s: %s", what, cudaGetErrorString(e)); return GB_ERR_CUDA; }
+    int err = 0;
+    GB_CUDA_TRY(cudaMemcpy(&err, h->sync + 2, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) { gb_set_error("%s: a grid barrier wait timed out", what); return GB_TIMEOUT; }
+    return GB_OK;
+}
+
+static void r3_clear_abort(gb_r3d *h) { cudaMemsetAsync(h->dev.abort, 0, sizeof(int), h->stream); }
+
+#define R3_ROUTINE(name, what)                                  \
+    extern "C" int gb_r3d_##name(gb_r3d *h)                     \
+    {                                                           \
+        if (!h) return GB_ERR_INVALID;                          \
+        r3_clear_abort(h);                                      \
+        r3_launch_transport(h, what, -1, h->stream);            \
+        return r3_sync(h, "gb_r3d_" #name);                     \
+    }
+R3_ROUTINE(avorticity, 0)
+R3_ROUTINE(bvorticity, 1)
+R3_ROUTINE(cvorticity, 2)
+R3_ROUTINE(temperature, 3)
+R3_ROUTINE(rhsw, 5)
+R3_ROUTINE(rhsv, 6)
+R3_ROUTINE(rhsu, 7)
+R3_ROUTINE(update, 8)
+#undef R3_ROUTINE
+
+extern "C" int gb_r3d_heat(gb_r3d *h, double *trans1)
+{
+    if (!h) return GB_ERR_INVALID;
+    r3_clear_abort(h);
+    r3_launch_transport(h, 4, -1, h->stream);
+    int st = r3_sync(h, "gb_r3d_heat");
+    if (st != GB_OK) return st;
+    if (trans1) GB_CUDA_TRY(cudaMemcpy(trans1, h->dev.trans, sizeof(double), cudaMemcpyDeviceToHost));
+    return GB_OK;
+}
+
+extern "C" int gb_r3d_poisson(gb_r3d *h, int which, int *sweeps)
+{
+    if (!h || which < 1 || which > 3) { gb_set_error("gb_r3d_poisson: invalid argument"); return GB_ERR_INVALID; }
+    r3_clear_abort(h);
+    int st = r3_launch_solve(h, which, -1, h->stream);
+    if (st != GB_OK) return st;
+    st = r3_sync(h, "gb_r3d_poisson");
+    if (st != GB_OK) return st;
+    int out[2] = {0, 0};
+    GB_CUDA_TRY(cudaMemcpy(&out[0], h->dev.solve_status, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CUDA_TRY(cudaMemcpy(&out[1], h->dev.solve_sweeps, sizeof(int), cudaMemcpyDeviceToHost));
+    if (sweeps) *sweeps = out[1];
+    return out[0];
+}
+
+extern "C" int gb_r3d_step(gb_r3d *h, int nsteps, double *nu, int *sweeps, int *steps_done)
+{
+    if (!h || nsteps < 0) { gb_set_error("gb_r3d_step: invalid argument"); return GB_ERR_INVALID; }
+    if (steps_done) *steps_done = 0;
+    if (nsteps == 0) return GB_OK;
+    if (nsteps > h->hist_cap) {
+        cudaFree(h->hist_nu);
+        cudaFree(h->hist_sw);
+        h->hist_nu = nullptr;
+        h->hist_sw = nullptr;
+        h->hist_cap = 0;
+        GB_CUDA_TRY(cudaMalloc(&h->hist_nu, sizeof(double) * (size_t)nsteps));
+        GB_CUDA_TRY(cudaMalloc(&h->hist_sw, sizeof(int) * 3 * (size_t)nsteps));
+        h->hist_cap = nsteps;
+    }
+    h->dev.hist_nu = h->hist_nu;
+    h->dev.hist_sw = h->hist_sw;
+    cudaStream_t s = h->stream;
+    GB_CUDA_TRY(cudaMemsetAsync(h->hist_sw, 0, sizeof(int) * 3 * (size_t)nsteps, s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.steps_done, 0, sizeof(int), s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.abort, 0, sizeof(int), s));
+    for (int step = 0; step < nsteps; ++step) {
+        r3_launch_transport(h, 0, step, s);
+        r3_launch_transport(h, 1, step, s);
+        r3_launch_transport(h, 2, step, s);
+        r3_launch_transport(h, 3, step, s);
+        r3_launch_transport(h, 4, step, s);
+        r3_launch_transport(h, 5, step, s);
+        int st = r3_launch_solve(h, 1, step, s);
+        if (st == GB_OK) {
+            r3_launch_transport(h, 6, step, s);
+            st = r3_launch_solve(h, 2, step, s);
+        }
+        if (st == GB_OK) {
+            r3_launch_transport(h, 7, step, s);
+            st = r3_launch_solve(h, 3, step, s);
+        }
+        if (st != GB_OK) return st;
+        r3_launch_transport(h, 8, step, s);
+    }
+    int st = r3_sync(h, "gb_r3d_step");
+    if (st != GB_OK) return st;
+    int done = 0, ab = 0;
+    GB_CUDA_TRY(cudaMemcpy(&done, h->dev.steps_done, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CUDA_TRY(cudaMemcpy(&ab, h->dev.abort, sizeof(int), cudaMemcpyDeviceToHost));
+    if (steps_done) *steps_done = done;
+    if (nu && done > 0) GB_CUDA_TRY(cudaMemcpy(nu, h->hist_nu, sizeof(double) * (size_t)done, cudaMemcpyDeviceToHost));
+    if (sweeps) {
+        const int n = std::min(nsteps, done + 1);
+        GB_CUDA_TRY(cudaMemcpy(sweeps, h->hist_sw, sizeof(int) * 3 * (size_t)n, cudaMemcpyDeviceToHost));
+    }
+    return ab ? ab : GB_OK;
+}

@@ -58,6 +58,19 @@ class AxiParams(C.Structure):
                 ("maxsweeps", C.c_int), ("nrel", C.c_int), ("smoother", C.c_int), ("precision", C.c_int)]
 
 
+R3D_FIELDS = ["An", "A", "Ap", "Bn", "B", "Bp", "Cn", "C", "Cp", "thn", "th", "thp",
+              "uel", "vel", "wel", "uelp", "velp", "welp", "urh", "vrh", "wrh"]
+R3D_FIELD_ID = {n: i for i, n in enumerate(R3D_FIELDS)}
+
+
+class R3dParams(C.Structure):
+    _fields_ = [("nr", C.c_int), ("nz", C.c_int), ("np", C.c_int),
+                ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("zmax", C.c_double),
+                ("Ra", C.c_double), ("Re", C.c_double), ("Gr", C.c_double), ("Pr", C.c_double),
+                ("tolcon", C.c_double), ("sor", C.c_double), ("maxsweeps", C.c_int), ("nrel", C.c_int),
+                ("smoother", C.c_int), ("precision", C.c_int)]
+
+
 class PrbParams(C.Structure):
     _fields_ = [("nr", C.c_int), ("np", C.c_int),
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
@@ -112,6 +125,23 @@ SIGNATURES = [
     ("gb_axi_run_enqueue", C.c_int, [_vp, C.c_int]),
     ("gb_axi_run_query", C.c_int, [_vp]),
     ("gb_axi_run_end", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
+    ("gb_r3d_default_params", None, [C.POINTER(R3dParams), C.c_int, C.c_int, C.c_int]),
+    ("gb_r3d_create", C.c_int, [C.POINTER(R3dParams), C.POINTER(_vp), _ip]),
+    ("gb_r3d_destroy", C.c_int, [_vp]),
+    ("gb_r3d_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int]),
+    ("gb_r3d_get_field", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int]),
+    ("gb_r3d_avorticity", C.c_int, [_vp]),
+    ("gb_r3d_bvorticity", C.c_int, [_vp]),
+    ("gb_r3d_cvorticity", C.c_int, [_vp]),
+    ("gb_r3d_temperature", C.c_int, [_vp]),
+    ("gb_r3d_heat", C.c_int, [_vp, _dp]),
+    ("gb_r3d_rhsw", C.c_int, [_vp]),
+    ("gb_r3d_rhsv", C.c_int, [_vp]),
+    ("gb_r3d_rhsu", C.c_int, [_vp]),
+    ("gb_r3d_poisson", C.c_int, [_vp, C.c_int, _ip]),
+    ("gb_r3d_update", C.c_int, [_vp]),
+    ("gb_r3d_step", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
+    ("gb_r3d_stream", _vp, [_vp]),
     ("gb_prb_bind_bounds", None, [C.c_int, C.c_int]),
     ("gb_prb_bind_smoother", None, [C.c_int]),
     ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),

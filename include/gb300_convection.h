@@ -282,6 +282,70 @@ int gb_axi_run_enqueue(gb_axi *h, int nsteps);
 int gb_axi_run_query(gb_axi *h);
 int gb_axi_run_end(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done);
 
+/* ---------------------------------------- 3D rotating annulus (rot3dmg.f) */
+/* The 3D rotating annulus of rot3dmg.f ("R3D"): vorticity components A, B,
+ * C and temperature by Dufort-Frankel with hybrid upwinding (:341-873), the
+ * inner-wall heat flux (:882-909), wall vorticities and temperatures
+ * (:964-1023), the right-hand sides (:1026-1150) and multigrid solves
+ * (:1153-2344) of the three velocity components: r-, z- and phi-line
+ * Gauss-Seidel per sweep, 27-point full weighting, trilinear prolongation,
+ * plain V-cycle with nrel = 2, SOR 1.2, tolcon 1e-5, STOP beyond 500
+ * sweeps.  Every field is a column-major (0:ld1-1, 0:ld2-1, 0:np) array,
+ * ld1 >= nr+2 and ld2 >= nz+2 (the reference's are kr+1 = 34 and kz+1 =
+ * 34, rot3dmg.f:23); element (i, j, k) at i + ld1*(j + ld2*k). */
+enum gb_r3d_field {
+    GB_R_An = 0, GB_R_A, GB_R_Ap, GB_R_Bn, GB_R_B, GB_R_Bp, GB_R_Cn, GB_R_C, GB_R_Cp,
+    GB_R_thn, GB_R_th, GB_R_thp, GB_R_uel, GB_R_vel, GB_R_wel, GB_R_uelp, GB_R_velp, GB_R_welp,
+    GB_R_urh, GB_R_vrh, GB_R_wrh, GB_R_COUNT
+};
+
+typedef struct gb_r3d_params {
+    int nr, nz, np;           /* intervals in r, z and phi */
+    double dt, r0, rmax, zmax;
+    double Ra, Re, Gr, Pr;    /* COMMON /val/ Ra, Re, Ptl, Gr (rot3dmg.f:38) */
+    double tolcon;            /* max-norm residual tolerance (1e-5, rot3dmg.f:1562) */
+    double sor;               /* over-relaxation between sweeps (1.2, rot3dmg.f:1263) */
+    int maxsweeps;            /* the reference STOPs beyond 500 sweeps (rot3dmg.f:1259) */
+    int nrel;                 /* relaxations per level visit (2, rot3dmg.f:1237-1238) */
+    int smoother;             /* GB_SMOOTHER_LEX: the reference's line order, run as wavefronts of
+                                 independent lines; GB_SMOOTHER_ZEBRA: two colours of lines, the
+                                 lines on one-sided boundary rows last within a colour */
+    int precision;            /* GB_PRB_FP64 or GB_PRB_MIXED (FP32 V-cycles in FP64 defect correction) */
+} gb_r3d_params;
+
+typedef struct gb_r3d gb_r3d;
+
+/* Defaults of rot3dmg.f for an nr x nz x np grid (LEX, FP64). */
+void gb_r3d_default_params(gb_r3d_params *p, int nr, int nz, int np);
+/* Replaces poissoninit (rot3dmg.f:1153-1213) plus the COMMON storage;
+ * nlev_out (may be NULL) receives the level count (halvings while nr and
+ * nz halve exactly and both are >= 4, capped at 4).  np must be a multiple
+ * of 2^nlev with at least 4 phi intervals on the coarsest level. */
+int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out);
+int gb_r3d_destroy(gb_r3d *h);
+int gb_r3d_set_field(gb_r3d *h, int field, const double *host, int ld1, int ld2);
+int gb_r3d_get_field(gb_r3d *h, int field, double *host, int ld1, int ld2);
+int gb_r3d_avorticity(gb_r3d *h);     /* rot3dmg.f:341-469 */
+int gb_r3d_bvorticity(gb_r3d *h);     /* rot3dmg.f:477-593 */
+int gb_r3d_cvorticity(gb_r3d *h);     /* rot3dmg.f:601-728 */
+int gb_r3d_temperature(gb_r3d *h);    /* rot3dmg.f:736-873 */
+int gb_r3d_heat(gb_r3d *h, double *trans1);   /* rot3dmg.f:882-909 */
+int gb_r3d_rhsw(gb_r3d *h);           /* rot3dmg.f:1026-1060 */
+int gb_r3d_rhsv(gb_r3d *h);           /* rot3dmg.f:1063-1104 */
+int gb_r3d_rhsu(gb_r3d *h);           /* rot3dmg.f:1107-1150 */
+/* poisson1 (which = 1: wel, welp, wrh), poisson2 (2: vel), poisson3 (3: uel),
+ * rot3dmg.f:1216-1540: GB_OK, GB_MAXSWEEPS (the reference STOPs), GB_NAN or
+ * GB_TIMEOUT; *sweeps (may be NULL) receives the sweep count. */
+int gb_r3d_poisson(gb_r3d *h, int which, int *sweeps);
+int gb_r3d_update(gb_r3d *h);         /* rot3dmg.f:964-1023 */
+/* nsteps steps of the main loop (rot3dmg.f:241-253).  nu (nsteps, may be
+ * NULL) receives httrans = -r0 ln(r0/rmax) trans1 / (zmax 2 pi) per step
+ * (:255), sweeps (3*nsteps, may be NULL) the w, v and u sweep counts.  A
+ * failing solve ends the run (the reference STOPs); *steps_done (may be
+ * NULL) receives the steps completed and the return value the status. */
+int gb_r3d_step(gb_r3d *h, int nsteps, double *nu, int *sweeps, int *steps_done);
+void *gb_r3d_stream(gb_r3d *h);
+
 /* ------------------------------------------------ batched banded solvers */
 /* nlines independent systems with the same n; line l's element j sits at
  * base + l*line_stride + j*elem_stride in each array.  Device pointers.
