@@ -914,13 +914,12 @@ __device__ __forceinline__ double r3_rhs(const R3Lev &L, int dir, int p, int q, 
     }
 }
 
-// Solves line (p, q) of direction dir in place: the right-hand side is
-// formed row by row as the forward elimination needs it, the eliminated
-// values are kept in the line's own storage (no line reads its own old
-// values), and back-substitution overwrites them with the solution.  Lines
-// along r and z on plane k = n3 also write plane 0.
+// Solves line (p, q) of direction dir whose right-hand side s[0..n-1] a
+// block formed beforehand in shared memory: the elimination runs in s and
+// the solution goes to the level's correction v.  Lines along r and z on
+// plane k = n3 also write plane 0; phi-lines write plane 0 from plane n3.
 template <int COMP>
-__device__ void r3_line(const R3Lev &L, int dir, int p, int q)
+__device__ void r3_line(const R3Lev &L, int dir, int p, int q, double *s)
 {
     const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
     const int kind = r3_kind(COMP, dir);
@@ -942,80 +941,114 @@ __device__ void r3_line(const R3Lev &L, int dir, int p, int q)
     const bool seam = dir != 2 && q == n3;
     const double *T = L.fac[COMP][dir];
     if (dir != 0) T += (size_t)(p - 1) * r3_tabsize(kind, n);
-#define MEM(e) v[base + (size_t)((long long)(e) * step)]
-#define PUT(e, x)                                                  \
-    do {                                                           \
-        const double _x = (x);                                     \
-        MEM(e) = _x;                                               \
-        if (seam) v[base + (size_t)((long long)(e) * step) - plane] = _x; \
+#define PUT(e, x)                                                                     \
+    do {                                                                              \
+        const double _x = (x);                                                        \
+        v[base + (size_t)((long long)(e) * step)] = _x;                               \
+        if (seam) v[base + (size_t)((long long)(e) * step) - plane] = _x;             \
     } while (0)
     if (kind == 0) {
         const double *Cc = T, *Bb = T + n, *Aa = T + 2 * n, *Dd = T + 3 * n, *Ee = T + 4 * n;
-        double r0 = r3_rhs<COMP>(L, dir, p, q, 0), r1 = r3_rhs<COMP>(L, dir, p, q, 1);
+        double r0 = s[0], r1 = s[1];
+#pragma unroll 4
         for (int k = 0; k <= n - 2; ++k) {
             const double rk = r0 / Cc[k];
-            MEM(k) = rk;
+            s[k] = rk;
             const double rk1 = r1 - Bb[k + 1] * rk;
             double rk2 = 0.0;
-            if (k != n - 2) rk2 = r3_rhs<COMP>(L, dir, p, q, k + 2) - Aa[k + 2] * rk;
+            if (k != n - 2) rk2 = s[k + 2] - Aa[k + 2] * rk;
             r0 = rk1;
             r1 = rk2;
         }
         double x1 = r0 / Cc[n - 1];
         PUT(n - 1, x1);
-        double x0 = MEM(n - 2) - Dd[n - 2] * x1;
+        double x0 = s[n - 2] - Dd[n - 2] * x1;
         PUT(n - 2, x0);
         double x2 = x1;
         x1 = x0;
+#pragma unroll 4
         for (int j = n - 3; j >= 0; --j) {
-            const double x = MEM(j) - Dd[j] * x1 - Ee[j] * x2;
+            const double x = s[j] - Dd[j] * x1 - Ee[j] * x2;
             PUT(j, x);
             x2 = x1;
             x1 = x;
         }
     } else if (kind == 1) {
         const double *F = T, *Bb = T + n, *Cc = T + 2 * n;
-        double rprev = r3_rhs<COMP>(L, dir, p, q, 0);
-        MEM(0) = rprev;
+        double rprev = s[0];
+#pragma unroll 4
         for (int j = 1; j < n; ++j) {
-            const double rj = r3_rhs<COMP>(L, dir, p, q, j) - F[j] * rprev;
-            MEM(j) = rj;
+            const double rj = s[j] - F[j] * rprev;
+            s[j] = rj;
             rprev = rj;
         }
         double y = rprev / Bb[n - 1];
         PUT(n - 1, y);
+#pragma unroll 4
         for (int j = n - 2; j >= 0; --j) {
-            y = (MEM(j) - Cc[j] * y) / Bb[j];
+            y = (s[j] - Cc[j] * y) / Bb[j];
             PUT(j, y);
         }
     } else {
         const double *Aa = T, *Bb = T + n, *Cc = T + 2 * n, *F1 = T + 3 * n, *F2 = T + 4 * n, *F3 = T + 5 * n;
         const int N = n - 1;
-        double rN = r3_rhs<COMP>(L, dir, p, q, N);
-        double rprev = r3_rhs<COMP>(L, dir, p, q, 0);
-        MEM(0) = rprev;
+        double rN = s[N];
+        double rprev = s[0];
+#pragma unroll 4
         for (int j = 1; j <= n - 3; ++j) {
-            const double rj = r3_rhs<COMP>(L, dir, p, q, j) - F1[j] * rprev;
+            const double rj = s[j] - F1[j] * rprev;
             rN = rN - F2[j] * rprev;
-            MEM(j) = rj;
+            s[j] = rj;
             rprev = rj;
         }
-        const double rn2 = r3_rhs<COMP>(L, dir, p, q, n - 2) - F1[n - 2] * rprev;
+        const double rn2 = s[n - 2] - F1[n - 2] * rprev;
         rN = rN - F2[n - 2] * rprev;
-        MEM(n - 2) = rn2;
         rN = rN - F3[0] * rn2;
         const double yN = rN / Bb[N];
-        MEM(N) = yN;
+        PUT(N, yN);
         double y = (rn2 - Cc[n - 2] * yN) / Bb[n - 2];
-        MEM(n - 2) = y;
+        PUT(n - 2, y);
+#pragma unroll 4
         for (int j = n - 3; j >= 0; --j) {
-            y = (MEM(j) - Cc[j] * y - Aa[j] * yN) / Bb[j];
-            MEM(j) = y;
+            y = (s[j] - Cc[j] * y - Aa[j] * yN) / Bb[j];
+            PUT(j, y);
         }
         v[base - (size_t)step] = yN;   // plane 0 = plane n3
     }
-#undef MEM
 #undef PUT
+}
+
+// Shared memory of a solve block: right-hand sides of up to R3_SMEM_DOUBLES
+// line elements (each line padded to an odd pitch against bank conflicts).
+#define R3_SMEM_DOUBLES 6144
+
+// One phase of independent lines [a, b) of the list: each block takes a
+// contiguous share, forms the right-hand sides of a chunk of its lines with
+// all its threads (every element independently, so the loads and divisions
+// overlap), then one thread per line runs the elimination.
+template <int COMP>
+__device__ void r3_phase(const R3Lev &L, int dir, const int *lines, int a, int b, double *sm)
+{
+    const int n = r3_len(COMP, dir, L.n1, L.n2, L.n3);
+    const int pitch = n | 1;
+    const int per = (b - a + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int my0 = a + (int)blockIdx.x * per;
+    const int my1 = min(b, my0 + per);
+    const int chunk = max(1, min((int)blockDim.x, R3_SMEM_DOUBLES / pitch));
+    for (int c0 = my0; c0 < my1; c0 += chunk) {
+        const int nl = min(chunk, my1 - c0);
+        for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+            const int li = t / n, e = t - li * n;
+            const int pk = lines[c0 + li];
+            sm[li * pitch + e] = r3_rhs<COMP>(L, dir, pk & 0xffff, pk >> 16, e);
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < nl) {
+            const int pk = lines[c0 + threadIdx.x];
+            r3_line<COMP>(L, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
+        }
+        __syncthreads();
+    }
 }
 
 // Residual rc = rf - A psif at the level's unknowns (relax1 :1688-1720,
@@ -1085,7 +1118,7 @@ struct SolveCtx {
 // One relaxation call relax<COMP>(nrel, klev); returns false when a grid
 // barrier timed out.
 template <int COMP>
-__device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx)
+__device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx, double *sm)
 {
     const R3Lev &L = d.lev[klev];
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1096,11 +1129,7 @@ __device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx)
             const int *lines = L.lines[COMP][dir];
             const int *off = L.poff[COMP][dir];
             for (int ph = 0; ph < L.nphase[COMP][dir]; ++ph) {
-                const int a = off[ph], b = off[ph + 1];
-                for (long long t = a + gt; t < b; t += T) {
-                    const int pk = lines[t];
-                    r3_line<COMP>(L, dir, pk & 0xffff, pk >> 16);
-                }
+                r3_phase<COMP>(L, dir, lines, off[ph], off[ph + 1], sm);
                 if (!grid_sync(d.gs)) return false;
             }
         }
@@ -1227,8 +1256,9 @@ __device__ void r3_finer(const R3Dev &d, int klev)
 
 // poisson1/2/3 (rot3dmg.f:1216-1540) in one cooperative launch.
 template <int COMP>
-__global__ void __launch_bounds__(R3_THREADS) k_r3d_solve(const __grid_constant__ R3Dev d, int step)
+__global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_constant__ R3Dev d, int step)
 {
+    __shared__ double sm[R3_SMEM_DOUBLES];
     if (*(volatile int *)d.abort) return;
     const int ni = d.ni, nj = d.nj;
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1267,7 +1297,7 @@ __global__ void __launch_bounds__(R3_THREADS) k_r3d_solve(const __grid_constant_
             if (!grid_sync(d.gs)) return;
         }
         if (sweep == 1 || nlev == 1) {
-            if (!r3_relax<COMP>(d, 1, cx)) return;
+            if (!r3_relax<COMP>(d, 1, cx, sm)) return;
             for (long long t = gt; t < nlvl; t += T) {
                 const int i = (int)(t % n1p);
                 const long long rest = t / n1p;
@@ -1281,12 +1311,12 @@ __global__ void __launch_bounds__(R3_THREADS) k_r3d_solve(const __grid_constant_
             for (int l = 1; l <= nlev - 1; ++l) {
                 r3_corser(d, l);
                 if (!grid_sync(d.gs)) return;
-                if (!r3_relax<COMP>(d, l + 1, cx)) return;
+                if (!r3_relax<COMP>(d, l + 1, cx, sm)) return;
             }
             for (int l = nlev; l >= 2; --l) {
                 r3_finer(d, l);
                 if (!grid_sync(d.gs)) return;
-                if (!r3_relax<COMP>(d, l - 1, cx)) return;
+                if (!r3_relax<COMP>(d, l - 1, cx, sm)) return;
             }
         }
         const int slot = (cx.m - 1) & 1;

@@ -6,6 +6,11 @@ device instance is loaded with.
 * ``annulus_reference``: velvor2dnewsch3.4.f:130-178, T = 1 - ln r / ln r0
   with the ripple 0.7 T (r - rmax)/rmax (2 randno - 1), randno =
   1/2 + sin(2 pi k/150)/2.
+* ``r3d_reference``: rot3dmg.f:103-131, the 3D annulus at rest with
+  T = 1 - ln r / ln r0 + amp (rmax - r)(r - r0) cos(nval phi) and the point
+  (nr/4, nz/4, np/2) halved; ``r3d_initial_fields`` adds the previous time
+  level (rot3dmg.f:220-230) and, with noise > 0, seeded uniform noise on
+  the interior temperature (splitmix64, i fastest, then j, then k).
 * ``conduction_noise``: the conduction profile of either geometry plus
   seeded uniform noise of amplitude amp, drawn from splitmix64 (Steele, Lea
   and Flood, 2014) in k-major, i-minor order over the interior rows, the
@@ -96,4 +101,38 @@ def initial_fields(nr, np_, r0, rmax, variant=_L.PRB_LAYER, kind=1, seed=0, amp=
     else:
         f["th"] = conduction_noise(nr, np_, r0, rmax, dr, seed, amp, variant)
     f["thp"] = f["th"].copy()
+    return f
+
+
+def r3d_reference(nr, nz, np_, r0, rmax, nval=3, amp=1e-3):
+    """T of rot3dmg.f:103-131 as a Fortran-ordered (nr+2, nz+2, np+1) array."""
+    dr = (rmax - r0) / float(nr)
+    r = _radii(nr, r0, rmax, dr)
+    lr0 = math.log(r0)
+    at1 = math.atan(1.0)
+    trad = np.array([1.0 - math.log(float(x)) / lr0 for x in r])
+    ramp = np.array([amp * (rmax - float(x)) * (float(x) - r0) for x in r])
+    cosk = np.array([math.cos(float(nval) * (8.0 * at1 * float(k) / float(np_))) for k in range(np_ + 1)])
+    th = np.asfortranarray(np.broadcast_to((trad[:, None] + ramp[:, None] * cosk[None, :])[:, None, :],
+                                           (nr + 2, nz + 2, np_ + 1)).copy())
+    i, j, k = nr // 4, nz // 4, np_ // 2
+    th[i, j, k] = th[i, j, k] - 0.5 * th[i, j, k]
+    return np.asfortranarray(th)
+
+
+def r3d_initial_fields(nr, nz, np_, r0, rmax, nval=3, amp=1e-3, noise=0.0, seed=0):
+    """Every field of a fresh 3D-annulus instance: velocities and vorticities
+    zero (the fluid in solid-body rotation with the frame), T from
+    r3d_reference plus optional seeded noise, previous levels equal to the
+    current ones."""
+    zero = np.zeros((nr + 2, nz + 2, np_ + 1), order="F")
+    f = {n: zero.copy() for n in _L.R3D_FIELDS}
+    th = r3d_reference(nr, nz, np_, r0, rmax, nval, amp)
+    if noise > 0.0:
+        n = nr * nz * np_
+        u = (_splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+        th[1:nr + 1, 1:nz + 1, 0:np_] += noise * (2.0 * u.reshape(np_, nz, nr).T - 1.0)
+        th[:, :, np_] = th[:, :, 0]
+    f["th"] = th
+    f["thp"] = th.copy()
     return f
