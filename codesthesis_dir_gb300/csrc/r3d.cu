@@ -45,6 +45,11 @@ struct R3Lev {
     int *lines[4][3];           // packed p | q << 16, phase by phase
     int *poff[4][3];            // phase offsets (nphase + 1)
     int nphase[4][3];
+    // FP32 inner cycles (GB_PRB_MIXED)
+    float *v32, *f32, *res32;
+    float *irc, *irv, *iqc, *iqv;   // 1/r and 1/r^2 at cell centres and faces, i = 0..n1+1
+    float ihr, ihhr, ihhz, ihhp;
+    float *fac32[4][3];         // the factor tables with reciprocal pivots
 };
 
 struct R3Dev {
@@ -1358,6 +1363,462 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
 }
 
 // ---------------------------------------------------------------------------
+// Mixed precision (GB_PRB_MIXED): FP32 V-cycles on the residual equation
+// inside an FP64 defect correction.  The FP32 operator is the reference's
+// operator with every division by a level constant or a radius replaced by
+// a multiplication with its reciprocal; pivots of the factor tables are
+// stored as reciprocals.
+// ---------------------------------------------------------------------------
+
+// FP32 copies of the factor tables (one thread per line class).
+__global__ void k_r3d_factors32(const __grid_constant__ R3Dev d, const FacJob *jobs, int njobs, float *const *dst)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= njobs) return;
+    const FacJob J = jobs[q];
+    const R3Lev &L = d.lev[J.lev];
+    const int kind = r3_kind(J.comp, J.dir);
+    const int n = r3_len(J.comp, J.dir, L.n1, L.n2, L.n3);
+    const double *T = J.tab;
+    float *o = dst[q];
+    const int m = r3_tabsize(kind, n);
+    for (int t = 0; t < m; ++t) o[t] = (float)T[t];
+    if (kind == 0)
+        for (int t = 0; t < n; ++t) o[t] = (float)(1.0 / T[t]);            // divisors c(k)
+    else
+        for (int t = 0; t < n; ++t) o[n + t] = (float)(1.0 / T[n + t]);    // eliminated diagonal b
+}
+
+#define PV(i, j, k) v[(size_t)(i) + (size_t)L1 * ((size_t)(j) + (size_t)L2 * (size_t)(k))]
+#define RF(i, j, k) f[(size_t)(i) + (size_t)L1 * ((size_t)(j) + (size_t)L2 * (size_t)(k))]
+
+template <int COMP>
+__device__ __forceinline__ float r3_rhs32(const R3Lev &L, int dir, int p, int q, int e)
+{
+    const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
+    const float ihr = L.ihr, ihhr = L.ihhr, ihhz = L.ihhz, ihhp = L.ihhp;
+    const float c53 = 5.0f / 3.0f, c43 = 4.0f / 3.0f;
+    const float *v = L.v32, *f = L.f32;
+    if (dir == 0) {
+        const int i = e + 1, j = p, k = q;
+        const int ka = k == n3 ? 1 : k + 1, km = k - 1;
+        const float iq = COMP == 3 ? L.iqv[i] : L.iqc[i];
+        const float ph = (PV(i, j, ka) + PV(i, j, km)) * ihhp * iq;
+        float zz;
+        if (COMP == 1) zz = (PV(i, j + 1, k) + PV(i, j - 1, k)) * ihhz;
+        else if (j == 1) zz = (c53 * PV(i, j + 1, k) - 0.2f * PV(i, j + 2, k)) * ihhz;
+        else if (j == n2) zz = (c53 * PV(i, j - 1, k) - 0.2f * PV(i, j - 2, k)) * ihhz;
+        else zz = (PV(i, j - 1, k) + PV(i, j + 1, k)) * ihhz;
+        return RF(i, j, k) - zz - ph;
+    } else if (dir == 1) {
+        const int i = p, j = e + 1, k = q;
+        const int ka = k == n3 ? 1 : k + 1, km = k - 1;
+        const float iq = COMP == 3 ? L.iqv[i] : L.iqc[i];
+        const float ir = COMP == 3 ? L.irv[i] : L.irc[i];
+        const float ph = (PV(i, j, ka) + PV(i, j, km)) * ihhp * iq;
+        float rr;
+        if (COMP == 1) {
+            if (i == 1) rr = -(c53 * PV(i + 1, j, k) - 0.2f * PV(i + 2, j, k)) * ihhr - 0.5f * PV(i + 1, j, k) * ihr * ir;
+            else if (i == n1) rr = -(c53 * PV(i - 1, j, k) - 0.2f * PV(i - 2, j, k)) * ihhr + 0.5f * PV(i - 1, j, k) * ihr * ir;
+            else rr = -(PV(i + 1, j, k) + PV(i - 1, j, k)) * ihhr - 0.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        } else if (COMP == 2) {
+            if (i == 1) rr = -(c53 * PV(i + 1, j, k) - 0.2f * PV(i + 2, j, k)) * ihhr - c43 * PV(i + 1, j, k) * ihr * ir;
+            else if (i == n1) rr = -(c53 * PV(i - 1, j, k) - 0.2f * PV(i - 2, j, k)) * ihhr + c43 * PV(i - 1, j, k) * ihr * ir;
+            else rr = -(PV(i + 1, j, k) + PV(i - 1, j, k)) * ihhr - 1.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        } else {
+            rr = -(PV(i + 1, j, k) + PV(i - 1, j, k)) * ihhr - 1.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        }
+        return rr - ph + RF(i, j, k);
+    } else {
+        const int i = p, j = q, k = e + 1;
+        const float ir = COMP == 3 ? L.irv[i] : L.irc[i];
+        float rr;
+        if (COMP == 1) {
+            if (i == 1) rr = -(c53 * PV(i + 1, j, k) - 0.2f * PV(i + 2, j, k)) * ihhr - 0.5f * PV(i + 1, j, k) * ihr * ir;
+            else if (i == n1) rr = -(c53 * PV(i - 1, j, k) - 0.2f * PV(i - 2, j, k)) * ihhr + 0.5f * PV(i - 1, j, k) * ihr * ir;
+            else rr = -(PV(i + 1, j, k) + PV(i - 1, j, k)) * ihhr - 0.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        } else if (COMP == 2) {
+            if (i == 1) rr = -(c53 * PV(i + 1, j, k) - 0.2f * PV(i + 2, j, k)) * ihhr - c43 * PV(i + 1, j, k) * ihr * ir;
+            else if (i == n1) rr = -(c53 * PV(i - 1, j, k) - 0.2f * PV(i - 2, j, k)) * ihhr + c43 * PV(i - 1, j, k) * ihr * ir;
+            else rr = -(PV(i + 1, j, k) + PV(i - 1, j, k)) * ihhr - 1.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        } else {
+            rr = -(PV(i + 1, j, k) + PV(i - 1, j, k)) * ihhr - 1.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        }
+        float zz;
+        if (COMP == 1) zz = (PV(i, j + 1, k) + PV(i, j - 1, k)) * ihhz;
+        else if (j == 1) zz = (c53 * PV(i, j + 1, k) - 0.2f * PV(i, j + 2, k)) * ihhz;
+        else if (j == n2) zz = (c53 * PV(i, j - 1, k) - 0.2f * PV(i, j - 2, k)) * ihhz;
+        else zz = (PV(i, j - 1, k) + PV(i, j + 1, k)) * ihhz;
+        return rr - zz + RF(i, j, k);
+    }
+}
+
+// FP32 residual (only where a restriction follows).
+template <int COMP>
+__device__ __forceinline__ float r3_resid32(const R3Lev &L, int i, int j, int k)
+{
+    const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
+    const float ihr = L.ihr, ihhr = L.ihhr, ihhz = L.ihhz, ihhp = L.ihhp;
+    const float c53 = 5.0f / 3.0f, c43 = 4.0f / 3.0f;
+    const float *v = L.v32, *f = L.f32;
+    const int ka = k == n3 ? 1 : k + 1, km = k - 1;
+    const float p0 = PV(i, j, k);
+    const float iq = COMP == 3 ? L.iqv[i] : L.iqc[i];
+    const float ir = COMP == 3 ? L.irv[i] : L.irc[i];
+    float t = (PV(i, j, ka) - 2.0f * p0 + PV(i, j, km)) * ihhp * iq;
+    if (COMP == 1) {
+        t += (PV(i, j + 1, k) - 2.0f * p0 + PV(i, j - 1, k)) * ihhz;
+        if (i == 1) t += (-2.0f * p0 + c53 * PV(i + 1, j, k) - 0.2f * PV(i + 2, j, k)) * ihhr + 0.5f * (PV(i + 1, j, k) - p0) * ihr * ir;
+        else if (i == n1) t += (-2.0f * p0 + c53 * PV(i - 1, j, k) - 0.2f * PV(i - 2, j, k)) * ihhr + 0.5f * (p0 - PV(i - 1, j, k)) * ihr * ir;
+        else t += (PV(i - 1, j, k) - 2.0f * p0 + PV(i + 1, j, k)) * ihhr + 0.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+    } else {
+        t += p0 * iq;
+        if (COMP == 2) {
+            if (i == 1) t += (-2.0f * p0 + c53 * PV(i + 1, j, k) - 0.2f * PV(i + 2, j, k)) * ihhr + c43 * PV(i + 1, j, k) * ihr * ir;
+            else if (i == n1) t += (-2.0f * p0 + c53 * PV(i - 1, j, k) - 0.2f * PV(i - 2, j, k)) * ihhr - c43 * PV(i - 1, j, k) * ihr * ir;
+            else t += (PV(i - 1, j, k) - 2.0f * p0 + PV(i + 1, j, k)) * ihhr + 1.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        } else {
+            t += (PV(i - 1, j, k) - 2.0f * p0 + PV(i + 1, j, k)) * ihhr + 1.5f * (PV(i + 1, j, k) - PV(i - 1, j, k)) * ihr * ir;
+        }
+        if (j == 1) t += (-2.0f * p0 + c53 * PV(i, j + 1, k) - 0.2f * PV(i, j + 2, k)) * ihhz;
+        else if (j == n2) t += (-2.0f * p0 + c53 * PV(i, j - 1, k) - 0.2f * PV(i, j - 2, k)) * ihhz;
+        else t += (PV(i, j + 1, k) - 2.0f * p0 + PV(i, j - 1, k)) * ihhz;
+    }
+    return RF(i, j, k) - t;
+}
+
+#undef PV
+#undef RF
+
+template <int COMP>
+__device__ void r3_line32(const R3Lev &L, int dir, int p, int q, float *s)
+{
+    const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
+    const int kind = r3_kind(COMP, dir);
+    const int n = r3_len(COMP, dir, n1, n2, n3);
+    float *v = L.v32;
+    size_t base;
+    long long step;
+    if (dir == 0) {
+        base = (size_t)1 + (size_t)L1 * ((size_t)p + (size_t)L2 * (size_t)q);
+        step = 1;
+    } else if (dir == 1) {
+        base = (size_t)p + (size_t)L1 * ((size_t)1 + (size_t)L2 * (size_t)q);
+        step = L1;
+    } else {
+        base = (size_t)p + (size_t)L1 * ((size_t)q + (size_t)L2);
+        step = (long long)L1 * L2;
+    }
+    const long long plane = (long long)L1 * L2 * n3;
+    const bool seam = dir != 2 && q == n3;
+    const float *T = L.fac32[COMP][dir];
+    if (dir != 0) T += (size_t)(p - 1) * r3_tabsize(kind, n);
+#define PUT(e, x)                                                                     \
+    do {                                                                              \
+        const float _x = (x);                                                         \
+        v[base + (size_t)((long long)(e) * step)] = _x;                               \
+        if (seam) v[base + (size_t)((long long)(e) * step) - plane] = _x;             \
+    } while (0)
+    if (kind == 0) {
+        const float *Ci = T, *Bb = T + n, *Aa = T + 2 * n, *Dd = T + 3 * n, *Ee = T + 4 * n;
+        float r0 = s[0], r1 = s[1];
+        for (int k = 0; k <= n - 2; ++k) {
+            const float rk = r0 * Ci[k];
+            s[k] = rk;
+            const float rk1 = __fmaf_rn(-Bb[k + 1], rk, r1);
+            float rk2 = 0.f;
+            if (k != n - 2) rk2 = __fmaf_rn(-Aa[k + 2], rk, s[k + 2]);
+            r0 = rk1;
+            r1 = rk2;
+        }
+        float x1 = r0 * Ci[n - 1];
+        PUT(n - 1, x1);
+        float x0 = __fmaf_rn(-Dd[n - 2], x1, s[n - 2]);
+        PUT(n - 2, x0);
+        float x2 = x1;
+        x1 = x0;
+        for (int j = n - 3; j >= 0; --j) {
+            const float x = __fmaf_rn(-Ee[j], x2, __fmaf_rn(-Dd[j], x1, s[j]));
+            PUT(j, x);
+            x2 = x1;
+            x1 = x;
+        }
+    } else if (kind == 1) {
+        const float *F = T, *Bi = T + n, *Cc = T + 2 * n;
+        float rprev = s[0];
+        for (int j = 1; j < n; ++j) {
+            const float rj = __fmaf_rn(-F[j], rprev, s[j]);
+            s[j] = rj;
+            rprev = rj;
+        }
+        float y = rprev * Bi[n - 1];
+        PUT(n - 1, y);
+        for (int j = n - 2; j >= 0; --j) {
+            y = __fmaf_rn(-Cc[j], y, s[j]) * Bi[j];
+            PUT(j, y);
+        }
+    } else {
+        const float *Aa = T, *Bi = T + n, *Cc = T + 2 * n, *F1 = T + 3 * n, *F2 = T + 4 * n, *F3 = T + 5 * n;
+        const int N = n - 1;
+        float rN = s[N];
+        float rprev = s[0];
+        for (int j = 1; j <= n - 3; ++j) {
+            const float rj = __fmaf_rn(-F1[j], rprev, s[j]);
+            rN = __fmaf_rn(-F2[j], rprev, rN);
+            s[j] = rj;
+            rprev = rj;
+        }
+        const float rn2 = __fmaf_rn(-F1[n - 2], rprev, s[n - 2]);
+        rN = __fmaf_rn(-F2[n - 2], rprev, rN);
+        rN = __fmaf_rn(-F3[0], rn2, rN);
+        const float yN = rN * Bi[N];
+        PUT(N, yN);
+        float y = __fmaf_rn(-Cc[n - 2], yN, rn2) * Bi[n - 2];
+        PUT(n - 2, y);
+        for (int j = n - 3; j >= 0; --j) {
+            y = __fmaf_rn(-Aa[j], yN, __fmaf_rn(-Cc[j], y, s[j])) * Bi[j];
+            PUT(j, y);
+        }
+        v[base - (size_t)step] = yN;
+    }
+#undef PUT
+}
+
+template <int COMP>
+__device__ void r3_phase32(const R3Lev &L, int dir, const int *lines, int a, int b, float *sm)
+{
+    const int n = r3_len(COMP, dir, L.n1, L.n2, L.n3);
+    const int pitch = n | 1;
+    const int per = (b - a + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int my0 = a + (int)blockIdx.x * per;
+    const int my1 = min(b, my0 + per);
+    const int chunk = max(1, min((int)blockDim.x, (2 * R3_SMEM_DOUBLES) / pitch));
+    for (int c0 = my0; c0 < my1; c0 += chunk) {
+        const int nl = min(chunk, my1 - c0);
+        for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+            const int li = t / n, e = t - li * n;
+            const int pk = lines[c0 + li];
+            sm[li * pitch + e] = r3_rhs32<COMP>(L, dir, pk & 0xffff, pk >> 16, e);
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < nl) {
+            const int pk = lines[c0 + threadIdx.x];
+            r3_line32<COMP>(L, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
+        }
+        __syncthreads();
+    }
+}
+
+// relax in FP32; the residual only when a restriction follows.
+template <int COMP>
+__device__ bool r3_relax32(const R3Dev &d, int klev, bool residual, float *sm)
+{
+    const R3Lev &L = d.lev[klev];
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const int im = r3_imax(COMP, L.n1), jm = r3_jmax(COMP, L.n2), n3 = L.n3;
+    for (int irel = 1; irel <= d.nrel; ++irel)
+        for (int dir = 0; dir < 3; ++dir) {
+            const int *lines = L.lines[COMP][dir];
+            const int *off = L.poff[COMP][dir];
+            for (int ph = 0; ph < L.nphase[COMP][dir]; ++ph) {
+                r3_phase32<COMP>(L, dir, lines, off[ph], off[ph + 1], sm);
+                if (!grid_sync(d.gs)) return false;
+            }
+        }
+    if (residual) {
+        const long long npts = (long long)im * jm * n3;
+        for (long long t = gt; t < npts; t += T) {
+            const int i = 1 + (int)(t % im);
+            const long long rest = t / im;
+            const int j = 1 + (int)(rest % jm);
+            const int k = 1 + (int)(rest / jm);
+            L.res32[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = r3_resid32<COMP>(L, i, j, k);
+        }
+        if (!grid_sync(d.gs)) return false;
+    }
+    return true;
+}
+
+__device__ void r3_corser32(const R3Dev &d, int klev)
+{
+    const R3Lev &F = d.lev[klev], &Cl = d.lev[klev + 1];
+    const int n1c = Cl.n1, n2c = Cl.n2, n3c = Cl.n3;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long npts = (long long)Cl.L1 * Cl.L2 * (n3c + 1);
+    const float *rf = F.res32;
+    const size_t F1 = (size_t)F.L1, F2 = (size_t)F.L2;
+#define R(i, j, k) rf[(size_t)(i) + F1 * ((size_t)(j) + F2 * (size_t)(k))]
+    for (long long t = gt; t < npts; t += T) {
+        const int i = (int)(t % Cl.L1);
+        const long long rest = t / Cl.L1;
+        const int j = (int)(rest % Cl.L2);
+        const int k = (int)(rest / Cl.L2);
+        float val;
+        if (i == 0 || i == n1c || j == 0 || j == n2c) {
+            val = 0.f;
+        } else if (k == 0 || k == n3c) {
+            val = k == 0 ? 0.f : R(i, j, k);
+        } else {
+            const int ii = i + i, jj = j + j, kk = k + k;
+            float c = 0.f;
+#pragma unroll
+            for (int dk = -1; dk <= 1; ++dk)
+#pragma unroll
+                for (int dj = -1; dj <= 1; ++dj)
+#pragma unroll
+                    for (int di = -1; di <= 1; ++di) {
+                        const float w = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) * (dk ? 0.5f : 1.f);
+                        c = __fmaf_rn(w, R(ii + di, jj + dj, kk + dk), c);
+                    }
+            val = c * 0.125f;
+        }
+        Cl.f32[t] = val;
+        Cl.v32[t] = 0.f;
+    }
+#undef R
+}
+
+__device__ void r3_finer32(const R3Dev &d, int klev)
+{
+    const R3Lev &Cl = d.lev[klev], &F = d.lev[klev - 1];
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long npts = (long long)F.L1 * F.L2 * (F.n3 + 1);
+    const float *pc = Cl.v32;
+    const size_t C1 = (size_t)Cl.L1, C2 = (size_t)Cl.L2;
+#define PC(i, j, k) pc[(size_t)(i) + C1 * ((size_t)(j) + C2 * (size_t)(k))]
+    for (long long t = gt; t < npts; t += T) {
+        const int i = (int)(t % F.L1);
+        const long long rest = t / F.L1;
+        const int j = (int)(rest % F.L2);
+        const int k = (int)(rest / F.L2);
+        const int i1 = i >> 1, j1 = j >> 1, k1 = k >> 1;
+        const int i2 = i1 + (i & 1), j2 = j1 + (j & 1), k2 = k1 + (k & 1);
+        const float p = 0.125f * (PC(i1, j1, k1) + PC(i2, j1, k1) + PC(i1, j2, k1) + PC(i2, j2, k1) + PC(i1, j1, k2) +
+                                  PC(i2, j1, k2) + PC(i1, j2, k2) + PC(i2, j2, k2));
+        F.v32[t] += p;
+    }
+#undef PC
+}
+
+// poisson1/2/3 in mixed precision: the FP64 iterate lives in level 1's v,
+// the FP64 right-hand side in level 1's f.
+template <int COMP>
+__global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_constant__ R3Dev d, int step)
+{
+    __shared__ float sm[2 * R3_SMEM_DOUBLES];
+    if (*(volatile int *)d.abort) return;
+    const int ni = d.ni, nj = d.nj;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long T = (long long)gridDim.x * blockDim.x;
+    double *psi = d.fld[COMP == 1 ? GB_R_wel : COMP == 2 ? GB_R_vel : GB_R_uel];
+    double *psip = d.fld[COMP == 1 ? GB_R_welp : COMP == 2 ? GB_R_velp : GB_R_uelp];
+    const double *rhs = d.fld[COMP == 1 ? GB_R_wrh : COMP == 2 ? GB_R_vrh : GB_R_urh];
+    const R3Lev &L = d.lev[1];
+    const long long n1p = L.L1, n2p = L.L2;
+    const long long nlvl = n1p * n2p * (L.n3 + 1);
+    for (long long t = gt; t < nlvl; t += T) {
+        const int i = (int)(t % n1p);
+        const long long rest = t / n1p;
+        const int j = (int)(rest % n2p);
+        const int k = (int)(rest / n2p);
+        L.f[t] = FX(rhs, i, j, k);
+        L.v[t] = 2.0 * FX(psi, i, j, k) - FX(psip, i, j, k);
+        L.f32[t] = 0.f;
+    }
+    if (!grid_sync(d.gs)) return;
+    const int im = r3_imax(COMP, L.n1), jm = r3_jmax(COMP, L.n2), n3 = L.n3;
+    const long long nunk = (long long)im * jm * n3;
+    int status = GB_MAXSWEEPS, cycles = d.maxsweeps, m = 0;
+    const int nlev = d.nlev;
+    for (int it = 0;; ++it) {
+        // FP64 residual of the iterate, its FP32 copy the cycle's right-hand side
+        const int slot = m & 1;
+        if (gt == 0) {
+            d.resmax[slot ^ 1] = 0ull;
+            d.nanflag[slot ^ 1] = 0;
+        }
+        double lmax = 0.0;
+        int lnan = 0;
+        for (long long t = gt; t < nunk; t += T) {
+            const int i = 1 + (int)(t % im);
+            const long long rest = t / im;
+            const int j = 1 + (int)(rest % jm);
+            const int k = 1 + (int)(rest / jm);
+            const double r = r3_resid<COMP>(L, i, j, k);
+            L.f32[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = (float)r;
+            const double a = fabs(r);
+            if (a != a) lnan = 1;
+            if (a > lmax) lmax = a;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+            lnan |= __shfl_xor_sync(0xffffffffu, lnan, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if (lmax > 0.0) atomicMax(&d.resmax[slot], (unsigned long long)__double_as_longlong(lmax));
+            if (lnan) atomicOr(&d.nanflag[slot], 1);
+        }
+        ++m;
+        if (!grid_sync(d.gs)) return;
+        const double res = __longlong_as_double((long long)*(volatile unsigned long long *)&d.resmax[slot]);
+        if (*(volatile int *)&d.nanflag[slot]) {
+            status = GB_NAN;
+            cycles = it;
+            break;
+        }
+        if (res < d.tolcon) {
+            status = GB_OK;
+            cycles = it;
+            break;
+        }
+        if (it == d.maxsweeps) break;
+        // e = 0, one FP32 cycle: relax on level 1, descent, ascent
+        for (long long t = gt; t < nlvl; t += T) L.v32[t] = 0.f;
+        if (!grid_sync(d.gs)) return;
+        if (!r3_relax32<COMP>(d, 1, nlev > 1, sm)) return;
+        for (int l = 1; l <= nlev - 1; ++l) {
+            r3_corser32(d, l);
+            if (!grid_sync(d.gs)) return;
+            if (!r3_relax32<COMP>(d, l + 1, l + 1 < nlev, sm)) return;
+        }
+        for (int l = nlev; l >= 2; --l) {
+            r3_finer32(d, l);
+            if (!grid_sync(d.gs)) return;
+            if (!r3_relax32<COMP>(d, l - 1, false, sm)) return;
+        }
+        const double w = it == 0 ? 1.0 : d.sor;
+        for (long long t = gt; t < nlvl; t += T) L.v[t] += w * (double)L.v32[t];
+        if (!grid_sync(d.gs)) return;
+    }
+    if (status == GB_OK) {
+        const int imax = COMP == 3 ? d.nr : d.nr + 1;
+        const int jmax = COMP == 1 ? d.nz : d.nz + 1;
+        const int ii1 = COMP == 3 ? d.nr - 1 : d.nr;
+        const int jj1 = COMP == 1 ? d.nz - 1 : d.nz;
+        const long long npts = (long long)(imax + 1) * (jmax + 1) * (d.np + 1);
+        for (long long t = gt; t < npts; t += T) {
+            const int i = (int)(t % (imax + 1));
+            const long long rest = t / (imax + 1);
+            const int j = (int)(rest % (jmax + 1));
+            const int k = (int)(rest / (jmax + 1));
+            const double old = FX(psi, i, j, k);
+            FX(psip, i, j, k) = old;
+            const bool inner = i >= 1 && i <= ii1 && j >= 1 && j <= jj1;
+            FX(psi, i, j, k) = inner ? L.v[(size_t)i + (size_t)n1p * ((size_t)j + (size_t)n2p * (size_t)k)] : 0.0;
+        }
+    }
+    if (gt == 0) {
+        *d.solve_status = status;
+        *d.solve_sweeps = cycles;
+        if (step >= 0) d.hist_sw[3 * step + COMP - 1] = cycles;
+        if (status != GB_OK) atomicExch(d.abort, status);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 struct gb_r3d {
@@ -1491,8 +1952,8 @@ extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out
         gb_set_error("gb_r3d_create: unknown smoother %d", p->smoother);
         return GB_ERR_INVALID;
     }
-    if (p->precision != GB_PRB_FP64) {
-        gb_set_error("gb_r3d_create: precision %d not available for the 3D annulus", p->precision);
+    if (p->precision != GB_PRB_FP64 && p->precision != GB_PRB_MIXED) {
+        gb_set_error("gb_r3d_create: unknown precision %d", p->precision);
         return GB_ERR_INVALID;
     }
     gb_r3d *h = new gb_r3d();
@@ -1537,12 +1998,15 @@ extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out
     for (int l = 1; l <= nlev; ++l) {
         const int n1 = nr >> (l - 1), n2 = nz >> (l - 1), n3 = np >> (l - 1);
         need += 3 * (size_t)(n1 + 1) * (n2 + 1) * (n3 + 1) + 2 * (size_t)(n1 + 2);
+        size_t f32 = 3 * (size_t)(n1 + 1) * (n2 + 1) * (n3 + 1) + 4 * (size_t)(n1 + 2);
         for (int comp = 1; comp <= 3; ++comp)
             for (int dir = 0; dir < 3; ++dir) {
                 const int n = r3_len(comp, dir, n1, n2, n3);
                 const int inst = dir == 0 ? 1 : r3_imax(comp, n1);
                 need += (size_t)inst * r3_tabsize(r3_kind(comp, dir), n);
+                f32 += (size_t)inst * r3_tabsize(r3_kind(comp, dir), n);
             }
+        need += (f32 + 1) / 2 + 2;
     }
     e = cudaMalloc(&h->pool, sizeof(double) * need);
     if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: multigrid pool"); return GB_ERR_ALLOC; }
@@ -1599,8 +2063,40 @@ extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out
                 tr.nphase = (int)off.size() - 1;
                 refs.push_back(tr);
             }
+        // FP32 storage of the level
+        {
+            float *fb = (float *)b;
+            L.v32 = fb; fb += sz;
+            L.f32 = fb; fb += sz;
+            L.res32 = fb; fb += sz;
+            L.irc = fb; fb += L.n1 + 2;
+            L.irv = fb; fb += L.n1 + 2;
+            L.iqc = fb; fb += L.n1 + 2;
+            L.iqv = fb; fb += L.n1 + 2;
+            std::vector<float> rr(4 * (size_t)(L.n1 + 2));
+            for (int i = 0; i <= L.n1 + 1; ++i) {
+                const double rc = rv_host[i], rv = rv_host[L.n1 + 2 + i];
+                rr[i] = (float)(1.0 / rc);
+                rr[L.n1 + 2 + i] = (float)(1.0 / rv);
+                rr[2 * (L.n1 + 2) + i] = (float)(1.0 / (rc * rc));
+                rr[3 * (L.n1 + 2) + i] = (float)(1.0 / (rv * rv));
+            }
+            cudaMemcpy(L.irc, rr.data(), sizeof(float) * rr.size(), cudaMemcpyHostToDevice);
+            L.ihr = (float)(1.0 / L.hr);
+            L.ihhr = (float)(1.0 / L.hhr);
+            L.ihhz = (float)(1.0 / L.hhz);
+            L.ihhp = (float)(1.0 / L.hhp);
+            for (int comp = 1; comp <= 3; ++comp)
+                for (int dir = 0; dir < 3; ++dir) {
+                    const int n = r3_len(comp, dir, L.n1, L.n2, L.n3);
+                    const int inst = dir == 0 ? 1 : r3_imax(comp, L.n1);
+                    L.fac32[comp][dir] = fb;
+                    fb += (size_t)inst * r3_tabsize(r3_kind(comp, dir), n);
+                }
+            b = (double *)(((uintptr_t)fb + 15) & ~(uintptr_t)15);
+        }
     }
-    if ((size_t)(b - h->pool) != need) {
+    if ((size_t)(b - h->pool) > need) {
         gb_r3d_destroy(h);
         gb_set_error("gb_r3d_create: multigrid pool layout mismatch");
         return GB_ERR_CUDA;
@@ -1637,6 +2133,23 @@ extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out
     if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: factor jobs"); return GB_ERR_ALLOC; }
     cudaMemcpy(djobs, jobs.data(), sizeof(FacJob) * jobs.size(), cudaMemcpyHostToDevice);
     k_r3d_factors<<<gb_ceil_div(jobs.size(), 64), 64>>>(d, djobs, (int)jobs.size());
+    {
+        // FP32 tables: the same job list, destinations in the FP32 pool
+        std::vector<float *> dst(jobs.size());
+        for (size_t q = 0; q < jobs.size(); ++q) {
+            const FacJob &J = jobs[q];
+            const R3Lev &L = d.lev[J.lev];
+            dst[q] = L.fac32[J.comp][J.dir] + (J.tab - L.fac[J.comp][J.dir]);
+        }
+        float **ddst = nullptr;
+        e = cudaMalloc(&ddst, sizeof(float *) * dst.size());
+        if (e == cudaSuccess) {
+            cudaMemcpy(ddst, dst.data(), sizeof(float *) * dst.size(), cudaMemcpyHostToDevice);
+            k_r3d_factors32<<<gb_ceil_div(jobs.size(), 64), 64>>>(d, djobs, (int)jobs.size(), ddst);
+            cudaDeviceSynchronize();
+            cudaFree(ddst);
+        }
+    }
     e = cudaDeviceSynchronize();
     cudaFree(djobs);
     if (e != cudaSuccess) { gb_set_error("gb_r3d_create: factors: %s", cudaGetErrorString(e)); gb_r3d_destroy(h); return GB_ERR_CUDA; }
@@ -1646,8 +2159,10 @@ extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     int worst = 1 << 30;
-    const void *kerns[3] = {(const void *)k_r3d_solve<1>, (const void *)k_r3d_solve<2>, (const void *)k_r3d_solve<3>};
-    for (int q = 0; q < 3; ++q) {
+    const void *kerns[6] = {(const void *)k_r3d_solve<1>, (const void *)k_r3d_solve<2>, (const void *)k_r3d_solve<3>,
+                            (const void *)k_r3d_solve_mixed<1>, (const void *)k_r3d_solve_mixed<2>,
+                            (const void *)k_r3d_solve_mixed<3>};
+    for (int q = 0; q < 6; ++q) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[q], R3_THREADS, 0);
         worst = std::min(worst, per_sm);
     }
@@ -1724,8 +2239,10 @@ static int r3_launch_solve(gb_r3d *h, int comp, int step, cudaStream_t s)
     GB_CUDA_TRY(cudaMemsetAsync(h->dev.nanflag, 0, sizeof(int) * 2, s));
     R3Dev D = h->dev;
     void *args[] = {&D, &step};
-    const void *k = comp == 1 ? (const void *)k_r3d_solve<1> : comp == 2 ? (const void *)k_r3d_solve<2>
-                                                                        : (const void *)k_r3d_solve<3>;
+    const bool mixed = h->p.precision == GB_PRB_MIXED;
+    const void *k = comp == 1   ? (mixed ? (const void *)k_r3d_solve_mixed<1> : (const void *)k_r3d_solve<1>)
+                    : comp == 2 ? (mixed ? (const void *)k_r3d_solve_mixed<2> : (const void *)k_r3d_solve<2>)
+                                : (mixed ? (const void *)k_r3d_solve_mixed<3> : (const void *)k_r3d_solve<3>);
     cudaError_t e = cudaLaunchCooperativeKernel(k, h->grid, R3_THREADS, args, 0, s);
     if (e != cudaSuccess) {
         gb_set_error("gb_r3d: cooperative solve launch (%d blocks): %s", h->grid, cudaGetErrorString(e));
