@@ -437,6 +437,112 @@ def run_axi_workload(args):
     return 0
 
 
+R3DWL = dict(nr=64, nz=64, np=128, dt=4e-6, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e6, Re=500.0, Pr=7.0, Gr=0.0, nval=3,
+             amp=1e-3,
+             name="3D rotating annulus 128 (phi, periodic) x 65 x 65 (nr = nz = 64, np = 128), radius ratio 0.5, "
+                  "height/gap 1, Ra 1e6, Ta 1e6 (Re 500), Pr 7, dt 4e-6, MG tolcon 1e-5, mode-3 start amp 1e-3")
+
+
+def time_r3d_gpu(cfg, smoother, steps, warmup, precision=0):
+    import torch
+    from codesthesis_dir_gb300 import initial, r3d
+    g = r3d.R3D(cfg["nr"], cfg["nz"], cfg["np"], dt=cfg["dt"], r0=cfg["r0"], rmax=cfg["rmax"], zmax=cfg["zmax"],
+                Ra=cfg["Ra"], Re=cfg["Re"], Pr=cfg["Pr"], Gr=cfg["Gr"], smoother=smoother, precision=precision)
+    f0 = initial.r3d_initial_fields(cfg["nr"], cfg["nz"], cfg["np"], cfg["r0"], cfg["rmax"], cfg["nval"], cfg["amp"])
+    for n, a in f0.items():
+        g.set(n, a)
+    s = torch.cuda.ExternalStream(g.stream())
+    nu_w = np.zeros(0)
+    if warmup:
+        nu_w, _ = g.step(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    nu, sw = g.step(steps)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    done = len(nu)
+    fields = {n: g.get(n) for n in ("uel", "vel", "wel", "A", "B", "C", "th")}
+    g.close()
+    cells = cfg["nr"] * cfg["nz"] * cfg["np"]
+    return cells * done / (ms / 1e3), ms / max(done, 1), sw.sum(axis=1).mean() if done else 0.0, \
+        np.concatenate([nu_w, nu]), fields
+
+
+def r3d_summary(cfg, steps, steps_fp64, warmup, cpu_budget):
+    """Mixed over `steps` steps (the throughput figure); mixed and FP64 two-colour
+    over the same `steps_fp64` steps from the same start (speed-up and the
+    accuracy of the mixed path against FP64); one step in the reference's
+    line order; a bounded CPU sample of the oracle."""
+    out = {"workload": cfg["name"]}
+    runs = {}
+    for nm, sm, st, wu, prec in (("mixed_zebra", 1, steps, warmup, 1), ("mixed_zebra_short", 1, steps_fp64, 0, 1),
+                                 ("fp64_zebra", 1, steps_fp64, 0, 0), ("fp64_lex", 0, 1, 0, 0)):
+        if st <= 0:
+            continue
+        v, ms, sw, nu, fields = time_r3d_gpu(cfg, sm, st, wu, prec)
+        runs[nm] = (nu, fields)
+        out[nm] = {"value": v, "unit": "cell-updates/s", "ms_per_step": ms, "steps": st, "warmup": wu,
+                   ("sweeps_per_step" if prec == 0 else "fp32_cycles_per_step"): float(sw),
+                   "nu_last": float(nu[-1])}
+    if "mixed_zebra_short" in runs and "fp64_zebra" in runs:
+        nu_m, f_m = runs["mixed_zebra_short"]
+        nu_d, f_d = runs["fp64_zebra"]
+        m = out["mixed_zebra"]
+        m["speedup_vs_fp64_zebra"] = out["mixed_zebra_short"]["value"] / out["fp64_zebra"]["value"]
+        m["speedup_vs_fp64_lex"] = m["value"] / out["fp64_lex"]["value"] if "fp64_lex" in out else None
+        m["nu_rel_err_vs_fp64"] = float(np.max(np.abs(nu_m - nu_d) / np.abs(nu_d)))
+        m["field_rel_l2_vs_fp64"] = {n: float(np.linalg.norm(f_m[n] - f_d[n]) / max(np.linalg.norm(f_d[n]), 1e-300))
+                                     for n in f_d}
+        m["compared_after_steps"] = steps_fp64
+    if cpu_budget > 0:
+        from oracle import oracle as O
+        O.build()
+        o = O.OracleR3D(cfg["nr"], cfg["nz"], cfg["np"], cfg["dt"], cfg["r0"], cfg["rmax"], cfg["zmax"], cfg["Ra"],
+                        cfg["Re"], cfg["Pr"], Gr=cfg["Gr"], mode=0)
+        o.initial(cfg["nval"], cfg["amp"])
+        t0 = time.perf_counter()
+        n = 0
+        while n < 200 and (n == 0 or time.perf_counter() - t0 < cpu_budget):
+            o.step()
+            n += 1
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": cfg["nr"] * cfg["nz"] * cfg["np"] * n / dt, "unit": "cell-updates/s",
+                               "cores": 1, "kind": "port",
+                               "sample": "%d step(s) of the same instance from the same start, oracle in the "
+                                         "reference's line order, 1 thread, %.1f s" % (n, dt)}
+    return out
+
+
+def run_r3d_workload(args):
+    from codesthesis_dir_gb300 import lib
+    lib.load()
+    if args.mixed_only:
+        v, ms, sw, nu, _ = time_r3d_gpu(R3DWL, 1, args.steps, args.warmup, 1)
+        print("r3d mixed: %.4g cell-updates/s, %.1f ms/step, %.1f FP32 cycles/step" % (v, ms, sw))
+        return 0
+    with ClockSampler() as clk:
+        summ = r3d_summary(R3DWL, args.steps, args.r3d_fp64_steps, args.warmup, 0 if args.no_cpu_baseline else 30.0)
+    mx = summ["mixed_zebra"]
+    line = {
+        "metric": "cell-updates/s (3D rotating annulus step, mixed-precision velocity solves; FP64 beside)",
+        "value": mx["value"], "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer", "data": "synthetic",
+        "config": {"workload": R3DWL["name"], "smoother": "zebra",
+                   "l2": "working set (~120 MB) fits in L2; the solves are phase-latency bound"},
+        "roofline": {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
+                     "note": "each relaxation phase costs the elimination chain of its longest line plus one grid "
+                             "barrier; HBM and the FP64 pipe are far from busy"},
+        "detail": summ, "clocks": clk.summary(),
+    }
+    if "cpu_baseline" in summ:
+        line["cpu_baseline"] = summ["cpu_baseline"]
+    print(json.dumps(line))
+    return 0
+
+
 def run_serve_workload(args):
     """--workload serve: the parameter sweep served by the continuous-batching
     loop, FP64 and mixed precision on the same arrivals.  The sweep is a
@@ -524,7 +630,8 @@ def main():
     ap.add_argument("--requests", type=int, default=96, help="serve workload: number of requests")
     ap.add_argument("--serve-steps", default="20,200", help="serve workload: step range lo,hi")
     ap.add_argument("--max-active", type=int, default=128, help="serve workload: active slots")
-    ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus", "axi", "serve"],
+    ap.add_argument("--r3d-fp64-steps", type=int, default=10, help="r3d workload: FP64 comparison steps")
+    ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus", "axi", "serve", "r3d"],
                     help="batch: 256 batched Poisson problems (the headline); layer / annulus: the 2D driver step")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -533,6 +640,8 @@ def main():
         return run_axi_workload(args)
     if args.workload == "serve":
         return run_serve_workload(args)
+    if args.workload == "r3d":
+        return run_r3d_workload(args)
     if args.workload != "batch":
         return run_prb_workload(args, LAYER if args.workload == "layer" else ANNULUS)
 
