@@ -1,7 +1,10 @@
 """Builds the in-tree CUDA library (sm_103a) with nvcc.
 
 Every .cu file under csrc/ is compiled in parallel to an object file and
-linked into codesthesis_dir_gb300/_build/libgb300conv.so.  Files whose
+linked into codesthesis_dir_gb300/_build/libgb300conv.so.  The 3D annulus's
+gfortran drop-in symbols (csrc_dropin/r3d_fortran.cpp, host code over the
+context API) go into their own libgb300r3d.so, linked against it, because
+their names clash with the 2D drivers' drop-ins.  Files whose
 numerics must match the reference operation for operation are compiled with
 -fmad=false (no contraction of multiply-add) and place fused multiply-adds
 explicitly where they want them; host code is compiled with
@@ -20,6 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgb300conv.so")
+DROPIN_SRC = os.path.join(HERE, "csrc_dropin", "r3d_fortran.cpp")
+R3D_LIB = os.path.join(OUT, "libgb300r3d.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -64,8 +69,26 @@ def needs_build() -> bool:
     return any(os.path.getmtime(f) > t for f in _sources() + _headers())
 
 
+def _build_dropin(force: bool) -> str:
+    deps = [DROPIN_SRC, LIB] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    if not force and os.path.exists(R3D_LIB) and os.path.getmtime(R3D_LIB) >= max(os.path.getmtime(f) for f in deps):
+        return R3D_LIB
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler found for the drop-in library")
+    tmp = R3D_LIB + ".tmp"
+    cmd = [cxx, "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", INCLUDE, DROPIN_SRC,
+           "-L", OUT, "-lgb300conv", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("drop-in build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+    os.replace(tmp, R3D_LIB)
+    return R3D_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and not needs_build():
+        _build_dropin(False)
         return LIB
     os.makedirs(OUT, exist_ok=True)
     srcs = _sources()
@@ -77,6 +100,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
     os.replace(tmp, LIB)
+    _build_dropin(True)
     return LIB
 
 

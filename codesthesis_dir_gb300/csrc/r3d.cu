@@ -1933,7 +1933,25 @@ static void r3_phases(int mode, int comp, int dir, int n1, int n2, int n3, std::
     }
 }
 
+static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out, int *nlev_out);
+
 extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out)
+{
+    return r3_create(p, nullptr, out, nlev_out);
+}
+
+extern "C" int gb_r3d_create_spacing(const gb_r3d_params *p, double dr, double dz, double dp, gb_r3d **out,
+                                     int *nlev_out)
+{
+    if (!(dr > 0.0 && dz > 0.0 && dp > 0.0)) {
+        gb_set_error("gb_r3d_create_spacing: spacings must be positive");
+        return GB_ERR_INVALID;
+    }
+    const double sp[3] = {dr, dz, dp};
+    return r3_create(p, sp, out, nlev_out);
+}
+
+static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out, int *nlev_out)
 {
     if (!p || !out) { gb_set_error("gb_r3d_create: null argument"); return GB_ERR_INVALID; }
     *out = nullptr;
@@ -1976,9 +1994,9 @@ extern "C" int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out
     d.Gr = p->Gr;
     d.Ptl = p->Pr;
     const double pi = acos(-1.0);
-    d.dr = (p->rmax - p->r0) / (double)nr;
-    d.dz = p->zmax / (double)nz;
-    d.dp = 2.0 * pi / (double)np;
+    d.dr = spacing ? spacing[0] : (p->rmax - p->r0) / (double)nr;
+    d.dz = spacing ? spacing[1] : p->zmax / (double)nz;
+    d.dp = spacing ? spacing[2] : 2.0 * pi / (double)np;
     d.nu_num = -p->r0 * log(p->r0 / p->rmax);
     d.nu_den = p->zmax * 2.0 * pi;
     d.tolcon = p->tolcon;

@@ -127,6 +127,8 @@ SIGNATURES = [
     ("gb_axi_run_end", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
     ("gb_r3d_default_params", None, [C.POINTER(R3dParams), C.c_int, C.c_int, C.c_int]),
     ("gb_r3d_create", C.c_int, [C.POINTER(R3dParams), C.POINTER(_vp), _ip]),
+    ("gb_r3d_create_spacing", C.c_int, [C.POINTER(R3dParams), C.c_double, C.c_double, C.c_double,
+                                        C.POINTER(_vp), _ip]),
     ("gb_r3d_destroy", C.c_int, [_vp]),
     ("gb_r3d_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int]),
     ("gb_r3d_get_field", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int]),
@@ -179,6 +181,51 @@ SIGNATURES = [
     ("gb_batch_profile_read_kind", C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp]),
     ("gb_measure_issue_rates", C.c_int, [_dp, _dp]),
 ]
+
+
+R3D_DROPIN_PATH = os.path.join(HERE, "_build", "libgb300r3d.so")
+# (name, restype, argtypes) of libgb300r3d.so (include/gb300_r3d_fortran.h).
+R3D_DROPIN_SIGNATURES = [
+    ("poissoninit_", None, [_ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    ("poisson1_", None, [_vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    ("poisson2_", None, [_vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    ("poisson3_", None, [_vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    ("avorticity_", None, []),
+    ("bvorticity_", None, []),
+    ("cvorticity_", None, []),
+    ("temperature_", None, []),
+    ("heat_", None, [_dp]),
+    ("update_", None, []),
+    ("rhsw_", None, [_vp]),
+    ("rhsv_", None, [_vp]),
+    ("rhsu_", None, [_vp]),
+    ("gb_r3d_bind_bounds", None, [C.c_int, C.c_int, C.c_int]),
+    ("gb_r3d_bind_common", None, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    ("gb_r3d_bind_smoother", None, [C.c_int]),
+    ("gb_r3d_bind_precision", None, [C.c_int]),
+    ("gb_r3d_bind_tolerance", None, [C.c_double, C.c_int]),
+    ("gb_r3d_last_status", C.c_int, []),
+    ("gb_r3d_last_sweeps", C.c_int, []),
+]
+_r3d_dropin = None
+
+
+def load_r3d_dropin(path: str = R3D_DROPIN_PATH):
+    """Loads the rot3dmg.f drop-in library (its own handle: its symbols share
+    names with the 2D drop-ins of the main library)."""
+    global _r3d_dropin
+    if _r3d_dropin is not None:
+        return _r3d_dropin
+    load()
+    if not os.path.exists(path):
+        raise RuntimeError("libgb300r3d.so not found at %s; run __graft_entry__.build() first" % path)
+    L = C.CDLL(path, mode=C.RTLD_LOCAL)
+    for name, res, args in R3D_DROPIN_SIGNATURES:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _r3d_dropin = L
+    return L
 
 
 def load(path: str = LIB_PATH):

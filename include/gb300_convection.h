@@ -205,6 +205,10 @@ void gb_prb_bind_radius(double *radius);
  * val = {Ra, Re, Ptl, Gr}.  Pass NULLs to return to the weak symbols. */
 void gb_prb_bind_common(double *sol1, double *sol2, double *sol3, void *num, double *val);
 
+/* The 2D drivers' Fortran names; a translation unit that defines the 3D
+ * annulus's drop-ins (include/gb300_r3d_fortran.h, same names with other
+ * arguments) defines GB300_NO_PRB_DROPIN before including this header. */
+#ifndef GB300_NO_PRB_DROPIN
 void poissoninit_(int *nr, int *nz, int *np, double *dr, double *dz, double *dp,
                   int *nlev);                                   /* PRB:1724 */
 void poisson2_(double *psi, double *psip, double *rhs, int *nr, int *nz, int *np,
@@ -219,6 +223,7 @@ void heat_(double *trans1, double *trans2);                     /* PRB:1452 */
 void update_(void);                                             /* PRB:1557 */
 void rhsv_(double *vrh);                                        /* PRB:1629 */
 void rhsu_(double *urh);                                        /* PRB:1679 */
+#endif
 /* Status and sweep count of the last drop-in call on this process. */
 int gb_prb_last_status(void);
 int gb_prb_last_sweeps(void);
@@ -322,6 +327,10 @@ void gb_r3d_default_params(gb_r3d_params *p, int nr, int nz, int np);
  * nz halve exactly and both are >= 4, capped at 4).  np must be a multiple
  * of 2^nlev with at least 4 phi intervals on the coarsest level. */
 int gb_r3d_create(const gb_r3d_params *p, gb_r3d **out, int *nlev_out);
+/* As gb_r3d_create with the grid spacings given: a Fortran driver's own
+ * dr, dz, dp from COMMON /num/ (rot3dmg.f:93-95), so that no spacing is
+ * recomputed from r0, rmax, zmax (the routines never see zmax). */
+int gb_r3d_create_spacing(const gb_r3d_params *p, double dr, double dz, double dp, gb_r3d **out, int *nlev_out);
 int gb_r3d_destroy(gb_r3d *h);
 int gb_r3d_set_field(gb_r3d *h, int field, const double *host, int ld1, int ld2);
 int gb_r3d_get_field(gb_r3d *h, int field, double *host, int ld1, int ld2);

@@ -9,8 +9,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "gb300_convection.h")
 
 
-def declared_functions():
-    src = open(HEADER).read()
+R3D_HEADER = os.path.join(ROOT, "include", "gb300_r3d_fortran.h")
+
+
+def declared_functions(header=HEADER):
+    src = open(header).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     src = re.sub(r"//[^\n]*", "", src)
     src = "\n".join(l for l in src.splitlines() if not l.strip().startswith("#"))
@@ -66,3 +69,17 @@ def test_missing_library_fails_loudly(tmp_path):
     finally:
         mod._lib = None
         mod.load()
+
+
+def test_r3d_dropin_exports_its_header():
+    """libgb300r3d.so (the rot3dmg.f drop-ins) exports every symbol its header
+    declares, and the binding table covers the same set."""
+    from codesthesis_dir_gb300 import _build, lib
+    _build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", lib.R3D_DROPIN_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    declared = declared_functions(R3D_HEADER)
+    assert {"avorticity_", "bvorticity_", "poisson1_", "rhsw_", "heat_", "update_"} <= declared
+    assert not sorted(declared - exported), sorted(declared - exported)
+    assert declared == {n for n, _, _ in lib.R3D_DROPIN_SIGNATURES}
