@@ -1,7 +1,11 @@
 """Fortran file formats of the PRB driver: unformatted sequential records
 (the restart/output files of velvor2dperiodicrbconv.f:253-312 and :500-549),
 the ASCII dump of readoutput.f (format 1(1x,e16.8)) and the Nusselt history
-(format 14(1x,e16.8), velvor2dperiodicrbconv.f:551-560).
+(format 14(1x,e16.8), velvor2dperiodicrbconv.f:551-560); and those of the 3D
+annulus driver: per field a header record nr,nz,np (default INTEGERs), a
+header record rmax,r0,zmax,zmin and the field's own (i, j) extent over
+k = 0..np (rot3dmg.f:157-216, 262-319), and the Nusselt history in format
+2(1x,e16.8) (rot3dmg.f:321-326).
 
 gfortran frames every unformatted sequential record with a 4-byte
 little-endian length before and after the payload; records here are far
@@ -97,3 +101,45 @@ def write_nu_history(path, dt, httrans, ssumc=None, ssums=None):
         for i in range(n):
             vals = [i * dt, httrans[i]] + [0.0] * 12
             fh.write("".join(" " + fortran_e(v) for v in vals) + "\n")
+
+
+# (i, j) extents of the 3D fields in their files (rot3dmg.f:265-310): the last
+# i and j index written, given nr and nz.
+R3D_ORDER = ["A", "B", "C", "uel", "vel", "wel", "th"]
+
+
+def r3d_extent(name, nr, nz):
+    return {"A": (nr + 1, nz), "B": (nr, nz), "C": (nr, nz + 1), "uel": (nr, nz + 1), "vel": (nr + 1, nz + 1),
+            "wel": (nr + 1, nz), "th": (nr + 1, nz + 1)}[name]
+
+
+def write_r3d_field(path, arr, name, nr, nz, np_, rmax, r0, zmax, zmin=0.0):
+    """arr: a (>= nr+2, >= nz+2, >= np+1) Fortran-ordered field."""
+    im, jm = r3d_extent(name, nr, nz)
+    a = np.asarray(arr)[: im + 1, : jm + 1, : np_ + 1]
+    with open(path, "wb") as fh:
+        write_record(fh, struct.pack("<3i", nr, nz, np_))
+        write_record(fh, struct.pack("<4d", rmax, r0, zmax, zmin))
+        write_record(fh, np.asfortranarray(a).ravel(order="F").astype("<f8").tobytes())
+
+
+def read_r3d_field(path, name):
+    """Returns ((nr, nz, np), (rmax, r0, zmax, zmin), field) with the field as
+    a (nr+2, nz+2, np+1) Fortran-ordered array, zero outside its extent."""
+    with open(path, "rb") as fh:
+        nr, nz, np_ = struct.unpack("<3i", read_record(fh))
+        geom = struct.unpack("<4d", read_record(fh))
+        v = np.frombuffer(read_record(fh), dtype="<f8")
+    im, jm = r3d_extent(name, nr, nz)
+    if v.size != (im + 1) * (jm + 1) * (np_ + 1):
+        raise ValueError("%s holds %d values, expected %d x %d x %d" % (path, v.size, im + 1, jm + 1, np_ + 1))
+    out = np.zeros((nr + 2, nz + 2, np_ + 1), order="F")
+    out[: im + 1, : jm + 1, :] = v.reshape((np_ + 1, jm + 1, im + 1)).T
+    return (nr, nz, np_), geom, out
+
+
+def write_r3d_nu_history(path, dt, httrans):
+    """rot3dmg.f:321-326: (i-1)*dt, httrans(i) per line, format 2(1x,e16.8)."""
+    with open(path, "w") as fh:
+        for i, h in enumerate(httrans):
+            fh.write(" " + fortran_e(i * dt) + " " + fortran_e(float(h)) + "\n")

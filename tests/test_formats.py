@@ -92,3 +92,65 @@ def test_host_initial_states_match_oracle(oracle, variant, kind):
     f = initial.initial_fields(nr, np_, r0, rmax, variant=variant, kind=kind, seed=7, amp=1e-3)
     for name in ("th", "thp", "C", "uel", "vel"):
         np.testing.assert_array_equal(f[name], np.array(o.field(name)), err_msg=name)
+
+
+R3D_DECK = """a.dat
+b.dat
+c.dat
+u.dat
+v.dat
+w.dat
+t.dat
+nu.dat
+1.d-5
+8
+8
+16
+3
+0.5, 1.0, 0.5
+1.d5
+100.
+0.
+0.7
+0.
+5.d-2
+3
+no
+y
+2
+n
+"""
+
+
+def test_r3d_deck():
+    d = deck.parse_r3d_deck(R3D_DECK)
+    assert d.fnames == ["a.dat", "b.dat", "c.dat", "u.dat", "v.dat", "w.dat", "t.dat", "nu.dat"]
+    assert (d.nr, d.nz, d.np, d.nts) == (8, 8, 16, 3)
+    assert (d.r0, d.rmax, d.zmax) == (0.5, 1.0, 0.5)
+    assert (d.Ra, d.Re, d.Gr, d.Pr, d.amp, d.nval) == (1e5, 100.0, 0.0, 0.7, 5e-2, 3)
+    assert d.restart is None and d.more == [2] and d.total_steps == 5
+
+
+def test_r3d_field_records(tmp_path):
+    import struct
+    nr, nz, np_ = 6, 4, 8
+    rng = np.random.default_rng(2)
+    for name in fortio.R3D_ORDER:
+        a = np.asfortranarray(rng.standard_normal((nr + 2, nz + 2, np_ + 1)))
+        p = tmp_path / (name + ".dat")
+        fortio.write_r3d_field(str(p), a, name, nr, nz, np_, 1.0, 0.5, 0.5)
+        raw = p.read_bytes()
+        assert struct.unpack("<i", raw[:4])[0] == 12 and struct.unpack("<3i", raw[4:16]) == (nr, nz, np_)
+        assert struct.unpack("<i", raw[20:24])[0] == 32
+        dims, geom, b = fortio.read_r3d_field(str(p), name)
+        assert dims == (nr, nz, np_) and geom == (1.0, 0.5, 0.5, 0.0)
+        im, jm = fortio.r3d_extent(name, nr, nz)
+        np.testing.assert_array_equal(b[:im + 1, :jm + 1], a[:im + 1, :jm + 1])
+        assert np.all(b[im + 1:] == 0) and np.all(b[:, jm + 1:] == 0)
+
+
+def test_r3d_nu_history(tmp_path):
+    p = tmp_path / "nu.dat"
+    fortio.write_r3d_nu_history(str(p), 1e-5, [1.0, 0.5])
+    # (1x,e16.8) twice: one blank, then a 16-wide field with two leading blanks
+    assert p.read_text().splitlines() == ["   0.00000000E+00   0.10000000E+01", "   0.10000000E-04   0.50000000E+00"]

@@ -42,3 +42,44 @@ def test_driver_matches_oracle(oracle, gblib, tmp_path):
     np.testing.assert_array_equal(c, np.array(o.field("C"))[:17])
     lines = open(tmp_path / "nu.dat").read().splitlines()
     assert len(lines) == nts + more and len(lines[0].split()) == 14
+
+
+def test_r3d_driver_matches_oracle_and_restarts(oracle, gblib, tmp_path):
+    """The deck-driven 3D annulus main program (rot3dmg.f): two blocks of steps
+    (3 + 2) against the oracle; the field files it writes restart a second
+    run of 2 steps, which matches the oracle restarted the reference's way
+    (previous time level = current, rot3dmg.f:220-230)."""
+    from codesthesis_dir_gb300 import driver_r3d, fortio
+    from test_formats import R3D_DECK
+    g, ht = driver_r3d.run(R3D_DECK, outdir=str(tmp_path), log=lambda *a: None)
+    o = oracle.OracleR3D(8, 8, 16, 1e-5, 0.5, 1.0, 0.5, 1e5, 100.0, 0.7)
+    o.initial(3, 5e-2)
+    want = []
+    for _ in range(5):
+        st, nu, sw = o.step()
+        assert st == 0
+        want.append(nu)
+    np.testing.assert_array_equal(ht, np.array(want))
+    for name in ("A", "B", "C", "th", "uel", "vel", "wel"):
+        np.testing.assert_array_equal(g.get(name), np.array(o.field(name)), err_msg=name)
+    lines = open(tmp_path / "nu.dat").read().splitlines()
+    assert len(lines) == 5 and len(lines[0].split()) == 2
+    g.close()
+    # restart from the written files
+    deck2 = R3D_DECK.replace("no\ny\n2\nn\n", "yes\na.dat\nb.dat\nc.dat\nu.dat\nv.dat\nw.dat\nt.dat\nn\n")
+    deck2 = deck2.replace("\n3\n0.5, 1.0", "\n2\n0.5, 1.0")
+    deck2 = deck2.replace("a.dat\nb.dat\nc.dat\nu.dat\nv.dat\nw.dat\nt.dat\nnu.dat\n",
+                          "a2.dat\nb2.dat\nc2.dat\nu2.dat\nv2.dat\nw2.dat\nt2.dat\nno\n", 1)
+    g2, ht2 = driver_r3d.run(deck2, outdir=str(tmp_path), log=lambda *a: None)
+    for a, b in (("Ap", "A"), ("Bp", "B"), ("Cp", "C"), ("thp", "th"), ("uelp", "uel"), ("velp", "vel"),
+                 ("welp", "wel")):
+        o.field(a)[...] = np.array(o.field(b))
+    want2 = []
+    for _ in range(2):
+        st, nu, sw = o.step()
+        want2.append(nu)
+    np.testing.assert_array_equal(ht2, np.array(want2))
+    for name in ("A", "B", "C", "th", "uel", "vel", "wel"):
+        np.testing.assert_array_equal(g2.get(name), np.array(o.field(name)), err_msg=name)
+    _, _, t2 = fortio.read_r3d_field(str(tmp_path / "t2.dat"), "th")
+    np.testing.assert_array_equal(t2, np.array(o.field("th")))
