@@ -1,0 +1,508 @@
+// Stretched-grid streamfunction multigrid of rcsc.f on sm_103a, FP64,
+// bit-identical to the oracle (-fmad=false, IEEE division, the reference's
+// order): psi_rr + psi_r / r - psi / r^2 + psi_zz with grid.f's per-level
+// finite-difference weights, pentadiagonal r-line and z-line Gauss-Seidel,
+// nine-point restriction, bilinear prolongation, plain V-cycle (rcsc.f:
+// 1118-1444).
+//
+// One persistent block per solve (the AXI solver's structure).  Every
+// r-line has its own matrix (the z weights of its row shift the diagonal)
+// and every z-line its own (the r weights and -1/r^2 of its column), so the
+// matrix halves of all line eliminations are done once at creation
+// (factor_pdma, one thread per line) and a sweep only carries right-hand
+// sides through them.  Line orders: the reference's (r-lines j = 1..n2-1 in
+// order, then z-lines i = 1..n1-1, on one thread: each line needs the one
+// before it) or four colours (index mod 4 = 1, 2, 3, 0: a line reads the
+// lines one and two away, never one of its colour), each colour's lines in
+// parallel.
+#include "gbcommon.cuh"
+#include "banded.cuh"
+
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#define STR_THREADS 512
+#define STR_MAXLEV 8
+
+struct StrLevel {
+    int n1, n2;
+    double *r, *cr, *crr, *czz;
+    double *v, *f;            // packed (n1+1)*(n2+1)
+    double *fac_r, *fac_z;    // per r-line j (5(n1-1)+1 each), per z-line i (5(n2-1)+1 each)
+};
+
+struct StrDev {
+    int nlev, ld, nrel, maxsweeps, mode;
+    double tolcon;
+    double *psif, *rc;        // ld x ld, ld = max(n1, n2) + 1
+    double *io_psi, *io_rhs;  // level-1 (n1+1) x (n2+1) staging of the caller's arrays
+    StrLevel lev[STR_MAXLEV];
+    int *status;              // [0] status, [1] sweeps
+};
+
+#define PS(i, j) d.psif[(size_t)(i) + (size_t)d.ld * (size_t)(j)]
+#define CR(i, k) L.cr[3 * ((i) - 1) + (k) - 1]
+#define CRR(i, k) L.crr[4 * ((i) - 1) + (k) - 1]
+#define CZZ(j, k) L.czz[4 * ((j) - 1) + (k) - 1]
+
+// Matrix of r-line j (rcsc.f:1228-1252) or z-line i (rcsc.f:1265-1285).
+__device__ void str_line_matrix(const StrLevel &L, int dir, int line, double *a, double *b, double *c, double *dd,
+                                double *e)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    if (dir == 0) {
+        const int j = line;
+        for (int i = 1; i <= n1 - 1; ++i) {
+            const int q = i - 1;
+            const double r = L.r[i];
+            if (i <= n1 / 2) {
+                a[q] = 0.0;
+                b[q] = CRR(i, 1) + CR(i, 1) / r;
+                c[q] = CRR(i, 2) + CR(i, 2) / r - 1.0 / (r * r);
+                dd[q] = CRR(i, 3) + CR(i, 3) / r;
+                e[q] = CRR(i, 4);
+            } else {
+                a[q] = CRR(i, 1);
+                b[q] = CRR(i, 2) + CR(i, 1) / r;
+                c[q] = CRR(i, 3) + CR(i, 2) / r - 1.0 / (r * r);
+                dd[q] = CRR(i, 4) + CR(i, 3) / r;
+                e[q] = 0.0;
+            }
+            if (j <= n2 / 2) c[q] = c[q] + CZZ(j, 2);
+            else c[q] = c[q] + CZZ(j, 3);
+        }
+    } else {
+        const int i = line;
+        const double r = L.r[i];
+        for (int j = 1; j <= n2 - 1; ++j) {
+            const int q = j - 1;
+            if (j <= n2 / 2) {
+                a[q] = 0.0;
+                b[q] = CZZ(j, 1);
+                c[q] = CZZ(j, 2) - 1.0 / (r * r);
+                dd[q] = CZZ(j, 3);
+                e[q] = CZZ(j, 4);
+            } else {
+                a[q] = CZZ(j, 1);
+                b[q] = CZZ(j, 2);
+                c[q] = CZZ(j, 3) - 1.0 / (r * r);
+                dd[q] = CZZ(j, 4);
+                e[q] = 0.0;
+            }
+            if (i <= n1 / 2) c[q] = c[q] + CRR(i, 2) + CR(i, 2) / r;
+            else c[q] = c[q] + CRR(i, 3) + CR(i, 2) / r;
+        }
+    }
+}
+
+struct StrJob {
+    int lev, dir, line;
+};
+
+__global__ void k_str_factors(const __grid_constant__ StrDev d, const StrJob *jobs, int njobs, double *work, int wstride)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= njobs) return;
+    const StrJob J = jobs[q];
+    const StrLevel &L = d.lev[J.lev];
+    const int n = J.dir == 0 ? L.n1 - 1 : L.n2 - 1;
+    double *w = work + (size_t)q * wstride;
+    double *a = w, *b = w + n, *c = w + 2 * n, *dd = w + 3 * n, *e = w + 4 * n, *scratch = w + 5 * n;
+    str_line_matrix(L, J.dir, J.line, a, b, c, dd, e);
+    double *fac = J.dir == 0 ? L.fac_r + (size_t)(J.line - 1) * (5 * n + 1) : L.fac_z + (size_t)(J.line - 1) * (5 * n + 1);
+    factor_pdma(a, b, c, dd, e, n, fac, scratch);
+}
+
+// r-line j: right-hand side of row i (rcsc.f:1246-1252)
+__device__ __forceinline__ void str_rline(const StrDev &d, const StrLevel &L, int j)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const double *f = L.f;
+    auto rhs = [&](int q) -> double {
+        const int i = q + 1;
+        if (j <= n2 / 2)
+            return -(CZZ(j, 1) * PS(i, j - 1) + CZZ(j, 3) * PS(i, j + 1) + CZZ(j, 4) * PS(i, j + 2)) +
+                   f[(size_t)i + (size_t)(n1 + 1) * j];
+        return -(CZZ(j, 1) * PS(i, j - 2) + CZZ(j, 2) * PS(i, j - 1) + CZZ(j, 4) * PS(i, j + 1)) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    };
+    const int n = n1 - 1;
+    apply_pdma_rhs(L.fac_r + (size_t)(j - 1) * (5 * n + 1), n, &PS(1, j), 1, rhs);
+}
+
+// z-line i: right-hand side of row j (rcsc.f:1279-1290)
+__device__ __forceinline__ void str_zline(const StrDev &d, const StrLevel &L, int i)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const double *f = L.f;
+    const double r = L.r[i];
+    auto rhs = [&](int q) -> double {
+        const int j = q + 1;
+        if (i <= n1 / 2)
+            return -(CRR(i, 1) * PS(i - 1, j) + CRR(i, 3) * PS(i + 1, j) + CRR(i, 4) * PS(i + 2, j) +
+                     (CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j)) / r) +
+                   f[(size_t)i + (size_t)(n1 + 1) * j];
+        return -(CRR(i, 1) * PS(i - 2, j) + CRR(i, 2) * PS(i - 1, j) + CRR(i, 4) * PS(i + 1, j) +
+                 (CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j)) / r) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    };
+    const int n = n2 - 1;
+    apply_pdma_rhs(L.fac_z + (size_t)(i - 1) * (5 * n + 1), n, &PS(i, 1), d.ld, rhs);
+}
+
+__device__ __forceinline__ double str_blk_max(double v, double *s_red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = (lane < nw) ? s_red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+        if (lane == 0) s_red[32] = v;
+    }
+    __syncthreads();
+    const double r = s_red[32];
+    __syncthreads();
+    return r;
+}
+
+// relax (rcsc.f:1197-1341); returns the last residual max norm.
+__device__ double str_relax(const StrDev &d, int klev, double *s_red, int *nan_out)
+{
+    const StrLevel &L = d.lev[klev];
+    const int n1 = L.n1, n2 = L.n2;
+    const int tp = (n1 + 1) * (n2 + 1);
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        PS(i, j) = L.v[idx];
+    }
+    __syncthreads();
+    double m = 0.0;
+    int nan = 0;
+    for (int irel = 0; irel < d.nrel; ++irel) {
+        if (d.mode == GB_SMOOTHER_LEX) {
+            if (threadIdx.x == 0) {
+                for (int j = 1; j <= n2 - 1; ++j) str_rline(d, L, j);
+                for (int i = 1; i <= n1 - 1; ++i) str_zline(d, L, i);
+            }
+            __syncthreads();
+        } else {
+            for (int c = 1; c <= 4; ++c) {
+                const int first = (c & 3) == 0 ? 4 : (c & 3);
+                for (int j = first + 4 * threadIdx.x; j <= n2 - 1; j += 4 * blockDim.x) str_rline(d, L, j);
+                __syncthreads();
+            }
+            for (int c = 1; c <= 4; ++c) {
+                const int first = (c & 3) == 0 ? 4 : (c & 3);
+                for (int i = first + 4 * threadIdx.x; i <= n1 - 1; i += 4 * blockDim.x) str_zline(d, L, i);
+                __syncthreads();
+            }
+        }
+        m = 0.0;
+        nan = 0;
+        const int ni = n1 - 1, tot = ni * (n2 - 1);
+        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            const int j = idx / ni + 1, i = idx - (j - 1) * ni + 1;
+            const double r = L.r[i];
+            double temp;
+            if (i <= n1 / 2)
+                temp = CRR(i, 1) * PS(i - 1, j) + CRR(i, 2) * PS(i, j) + CRR(i, 3) * PS(i + 1, j) +
+                       CRR(i, 4) * PS(i + 2, j) + (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r -
+                       PS(i, j) / (r * r);
+            else
+                temp = CRR(i, 1) * PS(i - 2, j) + CRR(i, 2) * PS(i - 1, j) + CRR(i, 3) * PS(i, j) +
+                       CRR(i, 4) * PS(i + 1, j) + (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r -
+                       PS(i, j) / (r * r);
+            if (j <= n2 / 2)
+                temp = temp + CZZ(j, 1) * PS(i, j - 1) + CZZ(j, 2) * PS(i, j) + CZZ(j, 3) * PS(i, j + 1) +
+                       CZZ(j, 4) * PS(i, j + 2);
+            else
+                temp = temp + CZZ(j, 1) * PS(i, j - 2) + CZZ(j, 2) * PS(i, j - 1) + CZZ(j, 3) * PS(i, j) +
+                       CZZ(j, 4) * PS(i, j + 1);
+            temp = L.f[(size_t)i + (size_t)(n1 + 1) * j] - temp;
+            d.rc[(size_t)i + (size_t)d.ld * j] = temp;
+            temp = fabs(temp);
+            if (temp != temp) nan = 1;
+            if (temp > m) m = temp;
+        }
+        nan = __syncthreads_or(nan);
+        m = str_blk_max(m, s_red);
+    }
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        L.v[idx] = PS(i, j);
+    }
+    __syncthreads();
+    *nan_out = nan;
+    return m;
+}
+
+// corser (rcsc.f:1343-1390): restriction of rc into the packed coarse
+// right-hand side; rows and columns 0 and n1c of the coarse level (n1 for
+// both directions) are zero, as are the boundary rows the restriction does
+// not reach (never read by the coarse relax); the coarse correction is zero.
+__device__ void str_corser(const StrDev &d, int klev)
+{
+    const int ld = d.ld;
+    const int n1c = d.lev[klev + 1].n1, n2c = d.lev[klev + 1].n2;
+    const double *rf = d.rc;
+    double *fc = d.lev[klev + 1].f, *vc = d.lev[klev + 1].v;
+    const int tot = (n1c + 1) * (n2c + 1);
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1c + 1), i = idx - j * (n1c + 1);
+        double temp = 0.0;
+        if (i >= 1 && i <= n1c - 1 && j >= 1 && j <= n2c - 1 && j != n1c) {
+            const int ii = i + i, jj = j + j;
+            temp = rf[(size_t)ii + (size_t)ld * jj];
+            temp = temp * 2.0 + rf[(size_t)(ii + 1) + (size_t)ld * jj] + rf[(size_t)(ii - 1) + (size_t)ld * jj];
+            temp = temp + rf[(size_t)ii + (size_t)ld * (jj + 1)] + rf[(size_t)ii + (size_t)ld * (jj - 1)];
+            temp = temp * 2.0 + rf[(size_t)(ii + 1) + (size_t)ld * (jj + 1)] + rf[(size_t)(ii - 1) + (size_t)ld * (jj - 1)];
+            temp = temp + rf[(size_t)(ii + 1) + (size_t)ld * (jj - 1)] + rf[(size_t)(ii - 1) + (size_t)ld * (jj + 1)];
+            temp = temp / 16.0;
+        }
+        fc[idx] = temp;
+        vc[idx] = 0.0;
+    }
+    __syncthreads();
+}
+
+// finer (rcsc.f:1392-1444)
+__device__ void str_finer(const StrDev &d, int klev)
+{
+    const int n1c = d.lev[klev].n1;
+    const int n1f = d.lev[klev - 1].n1, n2f = d.lev[klev - 1].n2;
+    const double *vc = d.lev[klev].v;
+    double *vf = d.lev[klev - 1].v;
+    const int tot = (n1f + 1) * (n2f + 1);
+#define PC(ii, jj) vc[(size_t)(jj) * (n1c + 1) + (ii)]
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1f + 1), i = idx - j * (n1f + 1);
+        const int i1 = i / 2, j1 = j / 2;
+        double p;
+        if (i1 * 2 == i) {
+            if (j1 * 2 == j) p = PC(i1, j1);
+            else p = (PC(i1, j1) + PC(i1, j1 + 1)) * 0.5;
+        } else {
+            if (j1 * 2 == j) {
+                p = (PC(i1, j1) + PC(i1 + 1, j1)) * 0.5;
+            } else {
+                double temp = PC(i1, j1) + PC(i1 + 1, j1 + 1);
+                temp = temp + PC(i1, j1 + 1) + PC(i1 + 1, j1);
+                p = temp * 0.25;
+            }
+        }
+        PS(i, j) = p + vf[idx];
+    }
+#undef PC
+    __syncthreads();
+    const int tc = (n1c + 1) * (d.lev[klev].n2 + 1);
+    for (int idx = threadIdx.x; idx < tc; idx += blockDim.x) d.lev[klev].v[idx] = 0.0;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1f + 1), i = idx - j * (n1f + 1);
+        vf[idx] = PS(i, j);
+    }
+    __syncthreads();
+}
+
+// poisson(psi, rhs, nlev, vel) (rcsc.f:1118-1195) on the staged arrays.
+__global__ void __launch_bounds__(STR_THREADS) k_str_solve(const __grid_constant__ StrDev d)
+{
+    __shared__ double s_red[33];
+    const int nlev = d.nlev;
+    const StrLevel &L1 = d.lev[1];
+    const int n1 = L1.n1, n2 = L1.n2;
+    const int tp = (n1 + 1) * (n2 + 1);
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        L1.f[idx] = d.io_rhs[idx];
+        L1.v[idx] = d.io_psi[idx];
+    }
+    for (int idx = threadIdx.x; idx < d.ld * d.ld; idx += blockDim.x) d.rc[idx] = 0.0;
+    __syncthreads();
+    int status = GB_MAXSWEEPS, sweeps = d.maxsweeps, nan1 = 0, nn = 0;
+    double res1 = 0.0;
+    for (int sweep = 1; sweep <= d.maxsweeps; ++sweep) {
+        if (sweep == 1 || nlev == 1) res1 = str_relax(d, 1, s_red, &nan1);
+        if (nlev > 1) {
+            for (int l = 1; l <= nlev - 1; ++l) {
+                str_corser(d, l);
+                str_relax(d, l + 1, s_red, &nn);
+            }
+            for (int l = nlev; l >= 2; --l) {
+                str_finer(d, l);
+                const double r = str_relax(d, l - 1, s_red, &nn);
+                if (l - 1 == 1) {
+                    res1 = r;
+                    nan1 = nn;
+                }
+            }
+        }
+        if (nan1) {
+            status = GB_NAN;
+            sweeps = sweep;
+            break;
+        }
+        if (res1 < d.tolcon) {
+            for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+                const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+                d.io_psi[idx] = PS(i, j);
+            }
+            status = GB_OK;
+            sweeps = sweep;
+            break;
+        }
+    }
+    if (threadIdx.x == 0) {
+        d.status[0] = status;
+        d.status[1] = sweeps;
+    }
+}
+
+#undef PS
+#undef CR
+#undef CRR
+#undef CZZ
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct gb_str {
+    StrDev dev;
+    double *pool = nullptr;
+    int *status = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+extern "C" int gb_str_destroy(gb_str *h)
+{
+    if (!h) return GB_OK;
+    cudaFree(h->pool);
+    cudaFree(h->status);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GB_OK;
+}
+
+extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, int maxsweeps, int nrel, int smoother,
+                             gb_str **out)
+{
+    if (!out || !lv || nlev < 1 || nlev >= STR_MAXLEV || maxsweeps < 1 || nrel < 1 ||
+        (smoother != GB_SMOOTHER_LEX && smoother != GB_SMOOTHER_ZEBRA)) {
+        gb_set_error("gb_str_create: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    *out = nullptr;
+    const int n1 = lv[0].n1, n2 = lv[0].n2;
+    if (n1 < 4 || n2 < 4 || n1 > 8192 || n2 > 8192) {
+        gb_set_error("gb_str_create: level-1 grid %d x %d unsupported", n1, n2);
+        return GB_ERR_INVALID;
+    }
+    for (int l = 0; l < nlev; ++l) {
+        if (lv[l].n1 != (n1 >> l) || lv[l].n2 != (n2 >> l) || (l && (lv[l - 1].n1 & 1 || lv[l - 1].n2 & 1)) ||
+            lv[l].n1 < 4 || lv[l].n2 < 4 || !lv[l].r || !lv[l].cr || !lv[l].crr || !lv[l].czz) {
+            gb_set_error("gb_str_create: level %d must be %d x %d (halvings of level 1, >= 4) with all tables", l + 1,
+                         n1 >> l, n2 >> l);
+            return GB_ERR_INVALID;
+        }
+    }
+    gb_str *h = new gb_str();
+    StrDev &d = h->dev;
+    memset(&d, 0, sizeof(d));
+    d.nlev = nlev;
+    d.ld = std::max(n1, n2) + 1;
+    d.nrel = nrel;
+    d.maxsweeps = maxsweeps;
+    d.mode = smoother;
+    d.tolcon = tolcon;
+    size_t need = 2 * (size_t)d.ld * d.ld + 2 * (size_t)(n1 + 1) * (n2 + 1);
+    for (int l = 0; l < nlev; ++l) {
+        const size_t a = lv[l].n1, b = lv[l].n2;
+        need += (a + 1) + 3 * (a - 1) + 4 * (a - 1) + 4 * (b - 1) + 2 * (a + 1) * (b + 1);
+        need += (b - 1) * (5 * (a - 1) + 1) + (a - 1) * (5 * (b - 1) + 1);
+    }
+    cudaError_t e = cudaMalloc(&h->pool, sizeof(double) * need);
+    if (e != cudaSuccess) { delete h; gb_set_error("gb_str_create: %s", cudaGetErrorString(e)); return GB_ERR_ALLOC; }
+    cudaMemset(h->pool, 0, sizeof(double) * need);
+    double *b = h->pool;
+    d.psif = b; b += (size_t)d.ld * d.ld;
+    d.rc = b; b += (size_t)d.ld * d.ld;
+    d.io_psi = b; b += (size_t)(n1 + 1) * (n2 + 1);
+    d.io_rhs = b; b += (size_t)(n1 + 1) * (n2 + 1);
+    std::vector<StrJob> jobs;
+    int wmax = 0;
+    for (int l = 0; l < nlev; ++l) {
+        StrLevel &L = d.lev[l + 1];
+        const int a = lv[l].n1, bb = lv[l].n2;
+        L.n1 = a;
+        L.n2 = bb;
+        L.r = b; b += a + 1;
+        L.cr = b; b += 3 * (size_t)(a - 1);
+        L.crr = b; b += 4 * (size_t)(a - 1);
+        L.czz = b; b += 4 * (size_t)(bb - 1);
+        L.v = b; b += (size_t)(a + 1) * (bb + 1);
+        L.f = b; b += (size_t)(a + 1) * (bb + 1);
+        L.fac_r = b; b += (size_t)(bb - 1) * (5 * (a - 1) + 1);
+        L.fac_z = b; b += (size_t)(a - 1) * (5 * (bb - 1) + 1);
+        cudaMemcpy(L.r, lv[l].r, sizeof(double) * (a + 1), cudaMemcpyHostToDevice);
+        cudaMemcpy(L.cr, lv[l].cr, sizeof(double) * 3 * (a - 1), cudaMemcpyHostToDevice);
+        cudaMemcpy(L.crr, lv[l].crr, sizeof(double) * 4 * (a - 1), cudaMemcpyHostToDevice);
+        cudaMemcpy(L.czz, lv[l].czz, sizeof(double) * 4 * (bb - 1), cudaMemcpyHostToDevice);
+        for (int j = 1; j <= bb - 1; ++j) jobs.push_back({l + 1, 0, j});
+        for (int i = 1; i <= a - 1; ++i) jobs.push_back({l + 1, 1, i});
+        wmax = std::max(wmax, std::max(a, bb));
+    }
+    if ((size_t)(b - h->pool) != need) {
+        gb_str_destroy(h);
+        gb_set_error("gb_str_create: pool layout mismatch");
+        return GB_ERR_CUDA;
+    }
+    const int wstride = 7 * wmax;
+    StrJob *djobs = nullptr;
+    double *work = nullptr;
+    e = cudaMalloc(&djobs, sizeof(StrJob) * jobs.size());
+    if (e == cudaSuccess) e = cudaMalloc(&work, sizeof(double) * (size_t)wstride * jobs.size());
+    if (e != cudaSuccess) {
+        cudaFree(djobs);
+        gb_str_destroy(h);
+        gb_set_error("gb_str_create: factor scratch");
+        return GB_ERR_ALLOC;
+    }
+    cudaMemcpy(djobs, jobs.data(), sizeof(StrJob) * jobs.size(), cudaMemcpyHostToDevice);
+    k_str_factors<<<gb_ceil_div(jobs.size(), 64), 64>>>(d, djobs, (int)jobs.size(), work, wstride);
+    e = cudaDeviceSynchronize();
+    cudaFree(djobs);
+    cudaFree(work);
+    if (e != cudaSuccess) { gb_set_error("gb_str_create: factors: %s", cudaGetErrorString(e)); gb_str_destroy(h); return GB_ERR_CUDA; }
+    e = cudaMalloc(&h->status, 64);
+    if (e != cudaSuccess) { gb_str_destroy(h); gb_set_error("gb_str_create: status"); return GB_ERR_ALLOC; }
+    d.status = h->status;
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { gb_str_destroy(h); gb_set_error("gb_str_create: stream"); return GB_ERR_CUDA; }
+    *out = h;
+    return GB_OK;
+}
+
+extern "C" int gb_str_poisson(gb_str *h, double *psi, const double *rhs, int ld, int *sweeps)
+{
+    if (!h || !psi || !rhs) { gb_set_error("gb_str_poisson: null argument"); return GB_ERR_INVALID; }
+    const StrDev &d = h->dev;
+    const int n1 = d.lev[1].n1, n2 = d.lev[1].n2;
+    if (ld < n1 + 1) { gb_set_error("gb_str_poisson: ld %d < n1+1", ld); return GB_ERR_INVALID; }
+    const size_t row = sizeof(double) * (size_t)(n1 + 1);
+    GB_CUDA_TRY(cudaMemcpy2DAsync(d.io_psi, row, psi, sizeof(double) * (size_t)ld, row, n2 + 1, cudaMemcpyHostToDevice,
+                                  h->stream));
+    GB_CUDA_TRY(cudaMemcpy2DAsync(d.io_rhs, row, rhs, sizeof(double) * (size_t)ld, row, n2 + 1, cudaMemcpyHostToDevice,
+                                  h->stream));
+    k_str_solve<<<1, STR_THREADS, 0, h->stream>>>(d);
+    GB_CUDA_TRY(cudaGetLastError());
+    int st[2] = {0, 0};
+    GB_CUDA_TRY(cudaMemcpyAsync(st, d.status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (st[0] == GB_OK)
+        GB_CUDA_TRY(cudaMemcpy2D(psi, sizeof(double) * (size_t)ld, d.io_psi, row, row, n2 + 1, cudaMemcpyDeviceToHost));
+    if (sweeps) *sweeps = st[1];
+    return st[0];
+}

@@ -71,6 +71,11 @@ class R3dParams(C.Structure):
                 ("smoother", C.c_int), ("precision", C.c_int)]
 
 
+class StrLevel(C.Structure):
+    _fields_ = [("n1", C.c_int), ("n2", C.c_int), ("r", C.c_void_p), ("cr", C.c_void_p), ("crr", C.c_void_p),
+                ("czz", C.c_void_p)]
+
+
 class PrbParams(C.Structure):
     _fields_ = [("nr", C.c_int), ("np", C.c_int),
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
@@ -163,6 +168,10 @@ SIGNATURES = [
     ("update_", None, []),
     ("rhsv_", None, [_vp]),
     ("rhsu_", None, [_vp]),
+    ("gb_str_create", C.c_int, [C.c_int, C.POINTER(StrLevel), C.c_double, C.c_int, C.c_int, C.c_int,
+                                C.POINTER(_vp)]),
+    ("gb_str_poisson", C.c_int, [_vp, _vp, _vp, C.c_int, _ip]),
+    ("gb_str_destroy", C.c_int, [_vp]),
     ("gb_tdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
     ("gb_ptdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
     ("gb_pdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),

@@ -355,6 +355,36 @@ int gb_r3d_update(gb_r3d *h);         /* rot3dmg.f:964-1023 */
 int gb_r3d_step(gb_r3d *h, int nsteps, double *nu, int *sweeps, int *steps_done);
 void *gb_r3d_stream(gb_r3d *h);
 
+/* ------------------------- stretched-grid streamfunction solve (rcsc.f) */
+/* The multigrid of rcsc.f:1118-1444 on a non-uniform (r, z) grid: operator
+ * psi_rr + psi_r / r - psi / r^2 + psi_zz with the per-level finite-
+ * difference weights of grid.f (rcsc.f reads them from grid.f's file,
+ * :82-97), pentadiagonal r-line and z-line Gauss-Seidel (tolcon 1e-6,
+ * nrel 2), nine-point restriction that clears rows and columns 0 and n1 of
+ * the coarse level in both directions, bilinear prolongation, plain V-cycle
+ * from psi itself with no over-relaxation, no STOP after nvs = 10000
+ * sweeps.  Level l (0-based here) is (n1 >> l) x (n2 >> l). */
+typedef struct gb_str_level {
+    int n1, n2;
+    const double *r;     /* r(0..n1) of the level */
+    const double *cr;    /* first-derivative weights of rows i = 1..n1-1 on (i-1, i, i+1): [3*(i-1) + k] */
+    const double *crr;   /* second-derivative weights on (i-1..i+2) for i <= n1/2, else (i-2..i+1): [4*(i-1) + k] */
+    const double *czz;   /* the same in z for rows j = 1..n2-1: [4*(j-1) + k] */
+} gb_str_level;
+
+typedef struct gb_str gb_str;
+
+/* smoother: GB_SMOOTHER_LEX (the reference's line order, one thread) or
+ * GB_SMOOTHER_ZEBRA (four colours of lines, index mod 4 = 1, 2, 3, 0; a line
+ * reads the lines one and two away, so no line reads one of its colour). */
+int gb_str_create(int nlev, const gb_str_level *levels, double tolcon, int maxsweeps, int nrel, int smoother,
+                  gb_str **out);
+/* poisson(psi, rhs) on host arrays (0:ld-1, 0:n2), ld >= n1+1: GB_OK (psi
+ * updated), GB_MAXSWEEPS (psi untouched: the reference returns silently) or
+ * GB_NAN; *sweeps (may be NULL) the sweep count. */
+int gb_str_poisson(gb_str *h, double *psi, const double *rhs, int ld, int *sweeps);
+int gb_str_destroy(gb_str *h);
+
 /* ------------------------------------------------ batched banded solvers */
 /* nlines independent systems with the same n; line l's element j sits at
  * base + l*line_stride + j*elem_stride in each array.  Device pointers.

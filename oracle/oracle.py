@@ -93,6 +93,22 @@ class R3D(C.Structure):
                  ("mode", C.c_int), ("last_resmax", C.c_double), ("last_sweeps", C.c_int)])
 
 
+STR_MAXLEV = 8
+
+
+class STRGrid(C.Structure):
+    _fields_ = [("nlev", C.c_int), ("n1", C.c_int * STR_MAXLEV), ("n2", C.c_int * STR_MAXLEV)] + \
+               [(n, _dp * STR_MAXLEV) for n in ("hr", "hz", "r", "z", "cr", "crr", "cz", "czz")] + \
+               [(n, C.c_double * 3) for n in ("cr0", "crn", "cz0", "czn")]
+
+
+class STRMG(C.Structure):
+    _fields_ = [("g", C.c_void_p), ("nlev", C.c_int), ("ld", C.c_int),
+                ("v", _dp * STR_MAXLEV), ("f", _dp * STR_MAXLEV), ("psif", _dp), ("rc", _dp),
+                ("tolcon", C.c_double), ("nrel", C.c_int), ("maxsweeps", C.c_int), ("mode", C.c_int),
+                ("last_resmax", C.c_double)]
+
+
 _lib = None
 
 
@@ -166,6 +182,20 @@ def lib():
         L.orc_r3d_finer.argtypes = [C.POINTER(R3D), C.c_int]
         L.orc_r3d_step.argtypes = [C.POINTER(R3D), _dp, _ip]
         L.orc_r3d_step.restype = C.c_int
+        L.orc_str_spacing_gef.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, _dp]
+        L.orc_str_spacing_gef.restype = C.c_int
+        L.orc_str_levels.argtypes = [C.POINTER(STRGrid), C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_double, C.c_int]
+        L.orc_str_levels.restype = C.c_int
+        L.orc_str_grid_free.argtypes = [C.POINTER(STRGrid)]
+        L.orc_str_fdif.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
+        L.orc_str_fdif.restype = C.c_int
+        L.orc_str_coefficients.argtypes = [C.POINTER(STRGrid)]
+        L.orc_str_coefficients.restype = C.c_int
+        L.orc_str_mg_init.argtypes = [C.POINTER(STRMG), C.POINTER(STRGrid), C.c_int]
+        L.orc_str_mg_init.restype = C.c_int
+        L.orc_str_mg_free.argtypes = [C.POINTER(STRMG)]
+        L.orc_str_poisson.argtypes = [C.POINTER(STRMG), _dp, _dp, _ip]
+        L.orc_str_poisson.restype = C.c_int
         _lib = L
     return _lib
 
@@ -371,6 +401,75 @@ class OracleR3D:
     def close(self):
         if self.s.th:
             lib().orc_r3d_free(C.byref(self.s))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def str_spacing_gef(n, lo, hi, dist, gef, d1):
+    """grid.f's wall-clustered spacings (1-based array of n+1, index 0 unused)."""
+    h = np.zeros(n + 1)
+    if lib().orc_str_spacing_gef(n, lo, hi, dist, gef, d1, ptr(h)) != 0:
+        raise ValueError("grid.f would STOP for these GEF parameters")
+    return h
+
+
+def str_fdif(nx, nref, k, x):
+    """Weights w[d, p] of point x[k-nref+1+p] for derivative d (grid.f fdif)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    w = np.zeros(nx * nx)
+    assert lib().orc_str_fdif(nx, nref, k, ptr(x), ptr(w)) == 0
+    return w.reshape(nx, nx)
+
+
+class OracleSTR:
+    """grid.f's levels and coefficient tables for level-1 spacings hr1, hz1
+    (1-based, index 0 unused) and rcsc.f's multigrid on them."""
+
+    def __init__(self, hr1, hz1, r0, zmin=0.0, mode=ORC_LEX, tolcon=None, maxsweeps=None, maxlev=0):
+        L = lib()
+        self.hr1 = np.ascontiguousarray(hr1, dtype=np.float64)
+        self.hz1 = np.ascontiguousarray(hz1, dtype=np.float64)
+        n1, n2 = len(self.hr1) - 1, len(self.hz1) - 1
+        self.g = STRGrid()
+        if L.orc_str_levels(C.byref(self.g), n1, n2, ptr(self.hr1), ptr(self.hz1), r0, zmin, maxlev) < 1:
+            raise ValueError("no multigrid level for %d x %d" % (n1, n2))
+        if L.orc_str_coefficients(C.byref(self.g)) != 0:
+            raise ValueError("singular Taylor matrix")
+        self.m = STRMG()
+        assert L.orc_str_mg_init(C.byref(self.m), C.byref(self.g), 0) == 0
+        self.m.mode = mode
+        if tolcon is not None:
+            self.m.tolcon = tolcon
+        if maxsweeps is not None:
+            self.m.maxsweeps = maxsweeps
+        self.n1, self.n2 = n1, n2
+
+    @property
+    def nlev(self):
+        return self.g.nlev
+
+    def table(self, name, l):
+        n1, n2 = self.g.n1[l], self.g.n2[l]
+        size = {"r": n1 + 1, "z": n2 + 1, "hr": n1 + 1, "hz": n2 + 1, "cr": 3 * (n1 - 1), "crr": 4 * (n1 - 1),
+                "cz": 3 * (n2 - 1), "czz": 4 * (n2 - 1)}[name]
+        return np.ctypeslib.as_array(getattr(self.g, name)[l], shape=(size,)).copy()
+
+    def poisson(self, psi, rhs):
+        """psi, rhs: (n1+1, n2+1) arrays; returns (status, sweeps, psi)."""
+        p = np.asfortranarray(psi, dtype=np.float64).copy(order="F")
+        f = np.asfortranarray(rhs, dtype=np.float64)
+        sw = C.c_int()
+        st = lib().orc_str_poisson(C.byref(self.m), ptr(p), ptr(f), C.byref(sw))
+        return st, sw.value, p
+
+    def close(self):
+        if self.m.psif:
+            lib().orc_str_mg_free(C.byref(self.m))
+            lib().orc_str_grid_free(C.byref(self.g))
 
     def __del__(self):
         try:
