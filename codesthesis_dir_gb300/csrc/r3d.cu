@@ -35,18 +35,24 @@
 
 #define R3_MAXLEV 8
 #define R3_THREADS 256
+#define R3_SYNC_STRIDE 32           // unsigneds between the components' barriers
+
+// Work arrays of one level of one component's solve (the w and v solves
+// of a step run concurrently, each on its own arrays).
+struct R3Work {
+    double *v, *f, *res;
+    float *v32, *f32, *res32;
+};
 
 struct R3Lev {
     int n1, n2, n3, L1, L2;
     double hr, hz, hp, hhr, hhz, hhp;
-    double *v, *f, *res;
     double *rvc, *rvv;          // r0 + (i - 1/2) hr and i hr + r0, i = 0..n1+1
     double *fac[4][3];          // [component][direction] factor tables
     int *lines[4][3];           // packed p | q << 16, phase by phase
     int *poff[4][3];            // phase offsets (nphase + 1)
     int nphase[4][3];
     // FP32 inner cycles (GB_PRB_MIXED)
-    float *v32, *f32, *res32;
     float *irc, *irv, *iqc, *iqv;   // 1/r and 1/r^2 at cell centres and faces, i = 0..n1+1
     float ihr, ihhr, ihhz, ihhp;
     float *fac32[4][3];         // the factor tables with reciprocal pivots
@@ -60,15 +66,16 @@ struct R3Dev {
     int nrel, maxsweeps;
     double *fld[GB_R_COUNT];
     R3Lev lev[R3_MAXLEV];
-    unsigned long long *resmax; // two slots, bit patterns of non-negative doubles
-    int *nanflag;               // two slots
+    R3Work work[4][R3_MAXLEV];  // [component 1..3][level]
+    unsigned long long *resmax; // two slots per component, bit patterns of non-negative doubles
+    int *nanflag;               // two slots per component
     int *abort;                 // nonzero: a solve failed, later kernels return
     int *steps_done;
     double *trans;              // per-k heat flux sums (np + 1)
     double *hist_nu;
     int *hist_sw;
-    int *solve_status, *solve_sweeps;
-    GridSync gs;
+    int *solve_status, *solve_sweeps;   // per component
+    GridSync gs[4];             // per component (the w and v solves run concurrently)
 };
 
 #define FX(a, i, j, k) ((a)[(size_t)(i) + (size_t)ni * ((size_t)(j) + (size_t)nj * (size_t)(k))])
@@ -818,11 +825,11 @@ static const double F02 = (double)0.2f;   // REAL*4 literal 0.2 (rot3dmg.f:1626,
 // :1655-1681; relax2 :1798-1816, :1858-1876, :1891-1922; relax3 :2027-2041,
 // :2082-2085, :2096-2118.
 template <int COMP>
-__device__ __forceinline__ double r3_rhs(const R3Lev &L, int dir, int p, int q, int e)
+__device__ __forceinline__ double r3_rhs(const R3Lev &L, const R3Work &W, int dir, int p, int q, int e)
 {
     const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
     const double hr = L.hr, hhr = L.hhr, hhz = L.hhz, hhp = L.hhp;
-    const double *v = L.v, *f = L.f;
+    const double *v = W.v, *f = W.f;
     if (dir == 0) {
         const int i = e + 1, j = p, k = q;
         const int ka = k == n3 ? 1 : k + 1, km = k - 1;
@@ -924,12 +931,12 @@ __device__ __forceinline__ double r3_rhs(const R3Lev &L, int dir, int p, int q, 
 // the solution goes to the level's correction v.  Lines along r and z on
 // plane k = n3 also write plane 0; phi-lines write plane 0 from plane n3.
 template <int COMP>
-__device__ void r3_line(const R3Lev &L, int dir, int p, int q, double *s)
+__device__ void r3_line(const R3Lev &L, const R3Work &W, int dir, int p, int q, double *s)
 {
     const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
     const int kind = r3_kind(COMP, dir);
     const int n = r3_len(COMP, dir, n1, n2, n3);
-    double *v = L.v;
+    double *v = W.v;
     size_t base;
     long long step;
     if (dir == 0) {
@@ -1032,7 +1039,7 @@ __device__ void r3_line(const R3Lev &L, int dir, int p, int q, double *s)
 // all its threads (every element independently, so the loads and divisions
 // overlap), then one thread per line runs the elimination.
 template <int COMP>
-__device__ void r3_phase(const R3Lev &L, int dir, const int *lines, int a, int b, double *sm)
+__device__ void r3_phase(const R3Lev &L, const R3Work &W, int dir, const int *lines, int a, int b, double *sm)
 {
     const int n = r3_len(COMP, dir, L.n1, L.n2, L.n3);
     const int pitch = n | 1;
@@ -1045,12 +1052,12 @@ __device__ void r3_phase(const R3Lev &L, int dir, const int *lines, int a, int b
         for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
             const int li = t / n, e = t - li * n;
             const int pk = lines[c0 + li];
-            sm[li * pitch + e] = r3_rhs<COMP>(L, dir, pk & 0xffff, pk >> 16, e);
+            sm[li * pitch + e] = r3_rhs<COMP>(L, W, dir, pk & 0xffff, pk >> 16, e);
         }
         __syncthreads();
         if ((int)threadIdx.x < nl) {
             const int pk = lines[c0 + threadIdx.x];
-            r3_line<COMP>(L, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
+            r3_line<COMP>(L, W, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
         }
         __syncthreads();
     }
@@ -1059,11 +1066,11 @@ __device__ void r3_phase(const R3Lev &L, int dir, const int *lines, int a, int b
 // Residual rc = rf - A psif at the level's unknowns (relax1 :1688-1720,
 // relax2 :1935-1977, relax3 :2129-2160), one point per call.
 template <int COMP>
-__device__ __forceinline__ double r3_resid(const R3Lev &L, int i, int j, int k)
+__device__ __forceinline__ double r3_resid(const R3Lev &L, const R3Work &W, int i, int j, int k)
 {
     const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
     const double hr = L.hr, hhr = L.hhr, hhz = L.hhz, hhp = L.hhp;
-    const double *v = L.v, *f = L.f;
+    const double *v = W.v, *f = W.f;
     const int ka = k == n3 ? 1 : k + 1, km = k - 1;
     double temp;
     if (COMP == 1) {
@@ -1126,6 +1133,10 @@ template <int COMP>
 __device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx, double *sm)
 {
     const R3Lev &L = d.lev[klev];
+    const R3Work &W = d.work[COMP][klev];
+    const GridSync &gs = d.gs[COMP];
+    unsigned long long *resmax = d.resmax + 2 * COMP;
+    int *nanflag = d.nanflag + 2 * COMP;
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long T = (long long)gridDim.x * blockDim.x;
     const int im = r3_imax(COMP, L.n1), jm = r3_jmax(COMP, L.n2), n3 = L.n3;
@@ -1134,16 +1145,16 @@ __device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx, double *sm)
             const int *lines = L.lines[COMP][dir];
             const int *off = L.poff[COMP][dir];
             for (int ph = 0; ph < L.nphase[COMP][dir]; ++ph) {
-                r3_phase<COMP>(L, dir, lines, off[ph], off[ph + 1], sm);
-                if (!grid_sync(d.gs)) return false;
+                r3_phase<COMP>(L, W, dir, lines, off[ph], off[ph + 1], sm);
+                if (!grid_sync(gs)) return false;
             }
         }
         // residual and its max norm into slot m & 1; the other slot is
         // cleared for the next evaluation (nobody reads it before then)
         const int slot = cx.m & 1;
         if (gt == 0) {
-            d.resmax[slot ^ 1] = 0ull;
-            d.nanflag[slot ^ 1] = 0;
+            resmax[slot ^ 1] = 0ull;
+            nanflag[slot ^ 1] = 0;
         }
         const long long npts = (long long)im * jm * n3;
         double lmax = 0.0;
@@ -1153,8 +1164,8 @@ __device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx, double *sm)
             const long long rest = t / im;
             const int j = 1 + (int)(rest % jm);
             const int k = 1 + (int)(rest / jm);
-            const double r = r3_resid<COMP>(L, i, j, k);
-            L.res[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = r;
+            const double r = r3_resid<COMP>(L, W, i, j, k);
+            W.res[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = r;
             const double a = fabs(r);
             if (a != a) lnan = 1;
             if (a > lmax) lmax = a;
@@ -1164,24 +1175,25 @@ __device__ bool r3_relax(const R3Dev &d, int klev, SolveCtx &cx, double *sm)
             lnan |= __shfl_xor_sync(0xffffffffu, lnan, o);
         }
         if ((threadIdx.x & 31) == 0) {
-            if (lmax > 0.0) atomicMax(&d.resmax[slot], (unsigned long long)__double_as_longlong(lmax));
-            if (lnan) atomicOr(&d.nanflag[slot], 1);
+            if (lmax > 0.0) atomicMax(&resmax[slot], (unsigned long long)__double_as_longlong(lmax));
+            if (lnan) atomicOr(&nanflag[slot], 1);
         }
         cx.m++;
-        if (!grid_sync(d.gs)) return false;
+        if (!grid_sync(gs)) return false;
     }
     return true;
 }
 
 // corser (rot3dmg.f:2176-2265): coarse right-hand side and zero correction.
-__device__ void r3_corser(const R3Dev &d, int klev)
+__device__ void r3_corser(const R3Dev &d, int comp, int klev)
 {
     const R3Lev &F = d.lev[klev], &Cl = d.lev[klev + 1];
+    const R3Work &FW = d.work[comp][klev], &CW = d.work[comp][klev + 1];
     const int n1c = Cl.n1, n2c = Cl.n2, n3c = Cl.n3;
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long T = (long long)gridDim.x * blockDim.x;
     const long long npts = (long long)Cl.L1 * Cl.L2 * (n3c + 1);
-    const double *rf = F.res;
+    const double *rf = FW.res;
     const size_t F1 = (size_t)F.L1, F2 = (size_t)F.L2;
 #define R(i, j, k) rf[(size_t)(i) + F1 * ((size_t)(j) + F2 * (size_t)(k))]
     for (long long t = gt; t < npts; t += T) {
@@ -1207,21 +1219,22 @@ __device__ void r3_corser(const R3Dev &d, int klev)
                    R(iim, jjm, kkp) + R(iim, jjm, kkm) + R(iim, jjp, kkp) + R(iim, jjp, kkm);
             val = temp * 0.015625;
         }
-        Cl.f[t] = val;
-        Cl.v[t] = 0.0;
+        CW.f[t] = val;
+        CW.v[t] = 0.0;
     }
 #undef R
 }
 
 // finer (rot3dmg.f:2268-2344): trilinear prolongation added to the fine
 // level.  The coarse correction is cleared by the next corser.
-__device__ void r3_finer(const R3Dev &d, int klev)
+__device__ void r3_finer(const R3Dev &d, int comp, int klev)
 {
     const R3Lev &Cl = d.lev[klev], &F = d.lev[klev - 1];
+    const R3Work &CW = d.work[comp][klev], &FW = d.work[comp][klev - 1];
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long T = (long long)gridDim.x * blockDim.x;
     const long long npts = (long long)F.L1 * F.L2 * (F.n3 + 1);
-    const double *pc = Cl.v;
+    const double *pc = CW.v;
     const size_t C1 = (size_t)Cl.L1, C2 = (size_t)Cl.L2;
 #define PC(i, j, k) pc[(size_t)(i) + C1 * ((size_t)(j) + C2 * (size_t)(k))]
     for (long long t = gt; t < npts; t += T) {
@@ -1254,7 +1267,7 @@ __device__ void r3_finer(const R3Dev &d, int klev)
                         0.125;
             }
         }
-        F.v[t] = p + F.v[t];
+        FW.v[t] = p + FW.v[t];
     }
 #undef PC
 }
@@ -1272,6 +1285,8 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
     double *psip = d.fld[COMP == 1 ? GB_R_welp : COMP == 2 ? GB_R_velp : GB_R_uelp];
     const double *rhs = d.fld[COMP == 1 ? GB_R_wrh : COMP == 2 ? GB_R_vrh : GB_R_urh];
     const R3Lev &L = d.lev[1];
+    const R3Work &W = d.work[COMP][1];
+    const GridSync &gs = d.gs[COMP];
     const long long n1p = L.L1, n2p = L.L2;
     const long long nlvl = n1p * n2p * (L.n3 + 1);
     for (long long t = gt; t < nlvl; t += T) {
@@ -1279,10 +1294,10 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
         const long long rest = t / n1p;
         const int j = (int)(rest % n2p);
         const int k = (int)(rest / n2p);
-        L.f[t] = FX(rhs, i, j, k);
-        L.v[t] = 2.0 * FX(psi, i, j, k) - FX(psip, i, j, k);
+        W.f[t] = FX(rhs, i, j, k);
+        W.v[t] = 2.0 * FX(psi, i, j, k) - FX(psip, i, j, k);
     }
-    if (!grid_sync(d.gs)) return;
+    if (!grid_sync(gs)) return;
     SolveCtx cx;
     cx.m = 0;
     int status = GB_MAXSWEEPS, sweeps = d.maxsweeps;
@@ -1295,11 +1310,11 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
                 const int j = (int)(rest % n2p);
                 const int k = (int)(rest / n2p);
                 const double pp = FX(psip, i, j, k);
-                const double nv = pp + d.sor * (L.v[t] - pp);
-                L.v[t] = nv;
+                const double nv = pp + d.sor * (W.v[t] - pp);
+                W.v[t] = nv;
                 FX(psip, i, j, k) = nv;
             }
-            if (!grid_sync(d.gs)) return;
+            if (!grid_sync(gs)) return;
         }
         if (sweep == 1 || nlev == 1) {
             if (!r3_relax<COMP>(d, 1, cx, sm)) return;
@@ -1308,25 +1323,26 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
                 const long long rest = t / n1p;
                 const int j = (int)(rest % n2p);
                 const int k = (int)(rest / n2p);
-                FX(psip, i, j, k) = L.v[t];
+                FX(psip, i, j, k) = W.v[t];
             }
-            if (!grid_sync(d.gs)) return;
+            if (!grid_sync(gs)) return;
         }
         if (nlev > 1) {
             for (int l = 1; l <= nlev - 1; ++l) {
-                r3_corser(d, l);
-                if (!grid_sync(d.gs)) return;
+                r3_corser(d, COMP, l);
+                if (!grid_sync(gs)) return;
                 if (!r3_relax<COMP>(d, l + 1, cx, sm)) return;
             }
             for (int l = nlev; l >= 2; --l) {
-                r3_finer(d, l);
-                if (!grid_sync(d.gs)) return;
+                r3_finer(d, COMP, l);
+                if (!grid_sync(gs)) return;
                 if (!r3_relax<COMP>(d, l - 1, cx, sm)) return;
             }
         }
         const int slot = (cx.m - 1) & 1;
-        const double resmax = __longlong_as_double((long long)*(volatile unsigned long long *)&d.resmax[slot]);
-        if (*(volatile int *)&d.nanflag[slot]) {
+        const double resmax =
+            __longlong_as_double((long long)*(volatile unsigned long long *)&d.resmax[2 * COMP + slot]);
+        if (*(volatile int *)&d.nanflag[2 * COMP + slot]) {
             status = GB_NAN;
             sweeps = sweep;
             break;
@@ -1351,12 +1367,12 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
             const double old = FX(psi, i, j, k);
             FX(psip, i, j, k) = old;
             const bool inner = i >= 1 && i <= ii1 && j >= 1 && j <= jj1;
-            FX(psi, i, j, k) = inner ? L.v[(size_t)i + (size_t)n1p * ((size_t)j + (size_t)n2p * (size_t)k)] : 0.0;
+            FX(psi, i, j, k) = inner ? W.v[(size_t)i + (size_t)n1p * ((size_t)j + (size_t)n2p * (size_t)k)] : 0.0;
         }
     }
     if (gt == 0) {
-        *d.solve_status = status;
-        *d.solve_sweeps = sweeps;
+        d.solve_status[COMP] = status;
+        d.solve_sweeps[COMP] = sweeps;
         if (step >= 0) d.hist_sw[3 * step + COMP - 1] = sweeps;
         if (status != GB_OK) atomicExch(d.abort, status);
     }
@@ -1393,12 +1409,12 @@ __global__ void k_r3d_factors32(const __grid_constant__ R3Dev d, const FacJob *j
 #define RF(i, j, k) f[(size_t)(i) + (size_t)L1 * ((size_t)(j) + (size_t)L2 * (size_t)(k))]
 
 template <int COMP>
-__device__ __forceinline__ float r3_rhs32(const R3Lev &L, int dir, int p, int q, int e)
+__device__ __forceinline__ float r3_rhs32(const R3Lev &L, const R3Work &W, int dir, int p, int q, int e)
 {
     const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
     const float ihr = L.ihr, ihhr = L.ihhr, ihhz = L.ihhz, ihhp = L.ihhp;
     const float c53 = 5.0f / 3.0f, c43 = 4.0f / 3.0f;
-    const float *v = L.v32, *f = L.f32;
+    const float *v = W.v32, *f = W.f32;
     if (dir == 0) {
         const int i = e + 1, j = p, k = q;
         const int ka = k == n3 ? 1 : k + 1, km = k - 1;
@@ -1455,12 +1471,12 @@ __device__ __forceinline__ float r3_rhs32(const R3Lev &L, int dir, int p, int q,
 
 // FP32 residual (only where a restriction follows).
 template <int COMP>
-__device__ __forceinline__ float r3_resid32(const R3Lev &L, int i, int j, int k)
+__device__ __forceinline__ float r3_resid32(const R3Lev &L, const R3Work &W, int i, int j, int k)
 {
     const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
     const float ihr = L.ihr, ihhr = L.ihhr, ihhz = L.ihhz, ihhp = L.ihhp;
     const float c53 = 5.0f / 3.0f, c43 = 4.0f / 3.0f;
-    const float *v = L.v32, *f = L.f32;
+    const float *v = W.v32, *f = W.f32;
     const int ka = k == n3 ? 1 : k + 1, km = k - 1;
     const float p0 = PV(i, j, k);
     const float iq = COMP == 3 ? L.iqv[i] : L.iqc[i];
@@ -1491,12 +1507,12 @@ __device__ __forceinline__ float r3_resid32(const R3Lev &L, int i, int j, int k)
 #undef RF
 
 template <int COMP>
-__device__ void r3_line32(const R3Lev &L, int dir, int p, int q, float *s)
+__device__ void r3_line32(const R3Lev &L, const R3Work &W, int dir, int p, int q, float *s)
 {
     const int n1 = L.n1, n2 = L.n2, n3 = L.n3, L1 = L.L1, L2 = L.L2;
     const int kind = r3_kind(COMP, dir);
     const int n = r3_len(COMP, dir, n1, n2, n3);
-    float *v = L.v32;
+    float *v = W.v32;
     size_t base;
     long long step;
     if (dir == 0) {
@@ -1585,7 +1601,7 @@ __device__ void r3_line32(const R3Lev &L, int dir, int p, int q, float *s)
 }
 
 template <int COMP>
-__device__ void r3_phase32(const R3Lev &L, int dir, const int *lines, int a, int b, float *sm)
+__device__ void r3_phase32(const R3Lev &L, const R3Work &W, int dir, const int *lines, int a, int b, float *sm)
 {
     const int n = r3_len(COMP, dir, L.n1, L.n2, L.n3);
     const int pitch = n | 1;
@@ -1598,12 +1614,12 @@ __device__ void r3_phase32(const R3Lev &L, int dir, const int *lines, int a, int
         for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
             const int li = t / n, e = t - li * n;
             const int pk = lines[c0 + li];
-            sm[li * pitch + e] = r3_rhs32<COMP>(L, dir, pk & 0xffff, pk >> 16, e);
+            sm[li * pitch + e] = r3_rhs32<COMP>(L, W, dir, pk & 0xffff, pk >> 16, e);
         }
         __syncthreads();
         if ((int)threadIdx.x < nl) {
             const int pk = lines[c0 + threadIdx.x];
-            r3_line32<COMP>(L, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
+            r3_line32<COMP>(L, W, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
         }
         __syncthreads();
     }
@@ -1614,6 +1630,8 @@ template <int COMP>
 __device__ bool r3_relax32(const R3Dev &d, int klev, bool residual, float *sm)
 {
     const R3Lev &L = d.lev[klev];
+    const R3Work &W = d.work[COMP][klev];
+    const GridSync &gs = d.gs[COMP];
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long T = (long long)gridDim.x * blockDim.x;
     const int im = r3_imax(COMP, L.n1), jm = r3_jmax(COMP, L.n2), n3 = L.n3;
@@ -1622,8 +1640,8 @@ __device__ bool r3_relax32(const R3Dev &d, int klev, bool residual, float *sm)
             const int *lines = L.lines[COMP][dir];
             const int *off = L.poff[COMP][dir];
             for (int ph = 0; ph < L.nphase[COMP][dir]; ++ph) {
-                r3_phase32<COMP>(L, dir, lines, off[ph], off[ph + 1], sm);
-                if (!grid_sync(d.gs)) return false;
+                r3_phase32<COMP>(L, W, dir, lines, off[ph], off[ph + 1], sm);
+                if (!grid_sync(gs)) return false;
             }
         }
     if (residual) {
@@ -1633,21 +1651,22 @@ __device__ bool r3_relax32(const R3Dev &d, int klev, bool residual, float *sm)
             const long long rest = t / im;
             const int j = 1 + (int)(rest % jm);
             const int k = 1 + (int)(rest / jm);
-            L.res32[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = r3_resid32<COMP>(L, i, j, k);
+            W.res32[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = r3_resid32<COMP>(L, W, i, j, k);
         }
-        if (!grid_sync(d.gs)) return false;
+        if (!grid_sync(gs)) return false;
     }
     return true;
 }
 
-__device__ void r3_corser32(const R3Dev &d, int klev)
+__device__ void r3_corser32(const R3Dev &d, int comp, int klev)
 {
     const R3Lev &F = d.lev[klev], &Cl = d.lev[klev + 1];
+    const R3Work &WF = d.work[comp][klev], &WC = d.work[comp][klev + 1];
     const int n1c = Cl.n1, n2c = Cl.n2, n3c = Cl.n3;
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long T = (long long)gridDim.x * blockDim.x;
     const long long npts = (long long)Cl.L1 * Cl.L2 * (n3c + 1);
-    const float *rf = F.res32;
+    const float *rf = WF.res32;
     const size_t F1 = (size_t)F.L1, F2 = (size_t)F.L2;
 #define R(i, j, k) rf[(size_t)(i) + F1 * ((size_t)(j) + F2 * (size_t)(k))]
     for (long long t = gt; t < npts; t += T) {
@@ -1674,19 +1693,20 @@ __device__ void r3_corser32(const R3Dev &d, int klev)
                     }
             val = c * 0.125f;
         }
-        Cl.f32[t] = val;
-        Cl.v32[t] = 0.f;
+        WC.f32[t] = val;
+        WC.v32[t] = 0.f;
     }
 #undef R
 }
 
-__device__ void r3_finer32(const R3Dev &d, int klev)
+__device__ void r3_finer32(const R3Dev &d, int comp, int klev)
 {
     const R3Lev &Cl = d.lev[klev], &F = d.lev[klev - 1];
+    const R3Work &WC = d.work[comp][klev], &WF = d.work[comp][klev - 1];
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long T = (long long)gridDim.x * blockDim.x;
     const long long npts = (long long)F.L1 * F.L2 * (F.n3 + 1);
-    const float *pc = Cl.v32;
+    const float *pc = WC.v32;
     const size_t C1 = (size_t)Cl.L1, C2 = (size_t)Cl.L2;
 #define PC(i, j, k) pc[(size_t)(i) + C1 * ((size_t)(j) + C2 * (size_t)(k))]
     for (long long t = gt; t < npts; t += T) {
@@ -1698,7 +1718,7 @@ __device__ void r3_finer32(const R3Dev &d, int klev)
         const int i2 = i1 + (i & 1), j2 = j1 + (j & 1), k2 = k1 + (k & 1);
         const float p = 0.125f * (PC(i1, j1, k1) + PC(i2, j1, k1) + PC(i1, j2, k1) + PC(i2, j2, k1) + PC(i1, j1, k2) +
                                   PC(i2, j1, k2) + PC(i1, j2, k2) + PC(i2, j2, k2));
-        F.v32[t] += p;
+        WF.v32[t] += p;
     }
 #undef PC
 }
@@ -1717,6 +1737,8 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
     double *psip = d.fld[COMP == 1 ? GB_R_welp : COMP == 2 ? GB_R_velp : GB_R_uelp];
     const double *rhs = d.fld[COMP == 1 ? GB_R_wrh : COMP == 2 ? GB_R_vrh : GB_R_urh];
     const R3Lev &L = d.lev[1];
+    const R3Work &W = d.work[COMP][1];
+    const GridSync &gs = d.gs[COMP];
     const long long n1p = L.L1, n2p = L.L2;
     const long long nlvl = n1p * n2p * (L.n3 + 1);
     for (long long t = gt; t < nlvl; t += T) {
@@ -1724,11 +1746,11 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
         const long long rest = t / n1p;
         const int j = (int)(rest % n2p);
         const int k = (int)(rest / n2p);
-        L.f[t] = FX(rhs, i, j, k);
-        L.v[t] = 2.0 * FX(psi, i, j, k) - FX(psip, i, j, k);
-        L.f32[t] = 0.f;
+        W.f[t] = FX(rhs, i, j, k);
+        W.v[t] = 2.0 * FX(psi, i, j, k) - FX(psip, i, j, k);
+        W.f32[t] = 0.f;
     }
-    if (!grid_sync(d.gs)) return;
+    if (!grid_sync(gs)) return;
     const int im = r3_imax(COMP, L.n1), jm = r3_jmax(COMP, L.n2), n3 = L.n3;
     const long long nunk = (long long)im * jm * n3;
     int status = GB_MAXSWEEPS, cycles = d.maxsweeps, m = 0;
@@ -1737,8 +1759,8 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
         // FP64 residual of the iterate, its FP32 copy the cycle's right-hand side
         const int slot = m & 1;
         if (gt == 0) {
-            d.resmax[slot ^ 1] = 0ull;
-            d.nanflag[slot ^ 1] = 0;
+            d.resmax[2 * COMP + (slot ^ 1)] = 0ull;
+            d.nanflag[2 * COMP + (slot ^ 1)] = 0;
         }
         double lmax = 0.0;
         int lnan = 0;
@@ -1747,8 +1769,8 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
             const long long rest = t / im;
             const int j = 1 + (int)(rest % jm);
             const int k = 1 + (int)(rest / jm);
-            const double r = r3_resid<COMP>(L, i, j, k);
-            L.f32[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = (float)r;
+            const double r = r3_resid<COMP>(L, W, i, j, k);
+            W.f32[(size_t)i + (size_t)L.L1 * ((size_t)j + (size_t)L.L2 * (size_t)k)] = (float)r;
             const double a = fabs(r);
             if (a != a) lnan = 1;
             if (a > lmax) lmax = a;
@@ -1758,13 +1780,13 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
             lnan |= __shfl_xor_sync(0xffffffffu, lnan, o);
         }
         if ((threadIdx.x & 31) == 0) {
-            if (lmax > 0.0) atomicMax(&d.resmax[slot], (unsigned long long)__double_as_longlong(lmax));
-            if (lnan) atomicOr(&d.nanflag[slot], 1);
+            if (lmax > 0.0) atomicMax(&d.resmax[2 * COMP + slot], (unsigned long long)__double_as_longlong(lmax));
+            if (lnan) atomicOr(&d.nanflag[2 * COMP + slot], 1);
         }
         ++m;
-        if (!grid_sync(d.gs)) return;
-        const double res = __longlong_as_double((long long)*(volatile unsigned long long *)&d.resmax[slot]);
-        if (*(volatile int *)&d.nanflag[slot]) {
+        if (!grid_sync(gs)) return;
+        const double res = __longlong_as_double((long long)*(volatile unsigned long long *)&d.resmax[2 * COMP + slot]);
+        if (*(volatile int *)&d.nanflag[2 * COMP + slot]) {
             status = GB_NAN;
             cycles = it;
             break;
@@ -1776,22 +1798,22 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
         }
         if (it == d.maxsweeps) break;
         // e = 0, one FP32 cycle: relax on level 1, descent, ascent
-        for (long long t = gt; t < nlvl; t += T) L.v32[t] = 0.f;
-        if (!grid_sync(d.gs)) return;
+        for (long long t = gt; t < nlvl; t += T) W.v32[t] = 0.f;
+        if (!grid_sync(gs)) return;
         if (!r3_relax32<COMP>(d, 1, nlev > 1, sm)) return;
         for (int l = 1; l <= nlev - 1; ++l) {
-            r3_corser32(d, l);
-            if (!grid_sync(d.gs)) return;
+            r3_corser32(d, COMP, l);
+            if (!grid_sync(gs)) return;
             if (!r3_relax32<COMP>(d, l + 1, l + 1 < nlev, sm)) return;
         }
         for (int l = nlev; l >= 2; --l) {
-            r3_finer32(d, l);
-            if (!grid_sync(d.gs)) return;
+            r3_finer32(d, COMP, l);
+            if (!grid_sync(gs)) return;
             if (!r3_relax32<COMP>(d, l - 1, false, sm)) return;
         }
         const double w = it == 0 ? 1.0 : d.sor;
-        for (long long t = gt; t < nlvl; t += T) L.v[t] += w * (double)L.v32[t];
-        if (!grid_sync(d.gs)) return;
+        for (long long t = gt; t < nlvl; t += T) W.v[t] += w * (double)W.v32[t];
+        if (!grid_sync(gs)) return;
     }
     if (status == GB_OK) {
         const int imax = COMP == 3 ? d.nr : d.nr + 1;
@@ -1807,12 +1829,12 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
             const double old = FX(psi, i, j, k);
             FX(psip, i, j, k) = old;
             const bool inner = i >= 1 && i <= ii1 && j >= 1 && j <= jj1;
-            FX(psi, i, j, k) = inner ? L.v[(size_t)i + (size_t)n1p * ((size_t)j + (size_t)n2p * (size_t)k)] : 0.0;
+            FX(psi, i, j, k) = inner ? W.v[(size_t)i + (size_t)n1p * ((size_t)j + (size_t)n2p * (size_t)k)] : 0.0;
         }
     }
     if (gt == 0) {
-        *d.solve_status = status;
-        *d.solve_sweeps = cycles;
+        d.solve_status[COMP] = status;
+        d.solve_sweeps[COMP] = cycles;
         if (step >= 0) d.hist_sw[3 * step + COMP - 1] = cycles;
         if (status != GB_OK) atomicExch(d.abort, status);
     }
@@ -1824,7 +1846,7 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
 struct gb_r3d {
     gb_r3d_params p;
     R3Dev dev;
-    double *fields = nullptr, *pool = nullptr;
+    double *fields = nullptr, *pool = nullptr, *work = nullptr;
     int *itab = nullptr;
     void *small = nullptr;
     double *hist_nu = nullptr;
@@ -1832,7 +1854,8 @@ struct gb_r3d {
     int hist_cap = 0;
     unsigned *sync = nullptr;
     int grid = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr, side = nullptr;   // side: the v solve, beside the w solve
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 static int r3_levels(int nr, int nz)
@@ -1881,11 +1904,15 @@ extern "C" int gb_r3d_destroy(gb_r3d *h)
     if (!h) return GB_OK;
     cudaFree(h->fields);
     cudaFree(h->pool);
+    cudaFree(h->work);
     cudaFree(h->itab);
     cudaFree(h->small);
     cudaFree(h->hist_nu);
     cudaFree(h->hist_sw);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->side) cudaStreamDestroy(h->side);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
     return GB_OK;
 }
@@ -2009,14 +2036,17 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     cudaMemset(h->fields, 0, sizeof(double) * fsz * GB_R_COUNT);
     for (int q = 0; q < GB_R_COUNT; ++q) d.fld[q] = h->fields + (size_t)q * fsz;
 
-    // multigrid pool: per level v, f, res, rvc, rvv and the factor tables
+    // multigrid pool: per level rvc, rvv and the factor tables (shared by the
+    // components); the work pool: per component and level v, f, res and their
+    // FP32 twins
     std::vector<FacJob> jobs;
-    size_t need = 0;
-    std::vector<size_t> fac_off;   // per (level, comp, dir) start, filled below
+    size_t need = 0, wneed = 0;
     for (int l = 1; l <= nlev; ++l) {
         const int n1 = nr >> (l - 1), n2 = nz >> (l - 1), n3 = np >> (l - 1);
-        need += 3 * (size_t)(n1 + 1) * (n2 + 1) * (n3 + 1) + 2 * (size_t)(n1 + 2);
-        size_t f32 = 3 * (size_t)(n1 + 1) * (n2 + 1) * (n3 + 1) + 4 * (size_t)(n1 + 2);
+        const size_t sz = (size_t)(n1 + 1) * (n2 + 1) * (n3 + 1);
+        wneed += 3 * (3 * sz + (3 * sz + 1) / 2 + 2);
+        need += 2 * (size_t)(n1 + 2);
+        size_t f32 = 4 * (size_t)(n1 + 2);
         for (int comp = 1; comp <= 3; ++comp)
             for (int dir = 0; dir < 3; ++dir) {
                 const int n = r3_len(comp, dir, n1, n2, n3);
@@ -2029,7 +2059,10 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     e = cudaMalloc(&h->pool, sizeof(double) * need);
     if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: multigrid pool"); return GB_ERR_ALLOC; }
     cudaMemset(h->pool, 0, sizeof(double) * need);
-    double *b = h->pool;
+    e = cudaMalloc(&h->work, sizeof(double) * wneed);
+    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: multigrid work arrays"); return GB_ERR_ALLOC; }
+    cudaMemset(h->work, 0, sizeof(double) * wneed);
+    double *b = h->pool, *wb = h->work;
     std::vector<int> itab;
     struct TabRef { int l, comp, dir; size_t lines, off; int nphase; };
     std::vector<TabRef> refs;
@@ -2049,9 +2082,17 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
         L.hhz = L.hz * L.hz;
         L.hhp = L.hp * L.hp;
         const size_t sz = (size_t)L.L1 * L.L2 * (L.n3 + 1);
-        L.v = b; b += sz;
-        L.f = b; b += sz;
-        L.res = b; b += sz;
+        for (int comp = 1; comp <= 3; ++comp) {
+            R3Work &W = d.work[comp][l];
+            W.v = wb; wb += sz;
+            W.f = wb; wb += sz;
+            W.res = wb; wb += sz;
+            float *fw = (float *)wb;
+            W.v32 = fw; fw += sz;
+            W.f32 = fw; fw += sz;
+            W.res32 = fw; fw += sz;
+            wb = (double *)(((uintptr_t)fw + 15) & ~(uintptr_t)15);
+        }
         L.rvc = b; b += L.n1 + 2;
         L.rvv = b; b += L.n1 + 2;
         rv_host.assign(2 * (size_t)(L.n1 + 2), 0.0);
@@ -2084,9 +2125,6 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
         // FP32 storage of the level
         {
             float *fb = (float *)b;
-            L.v32 = fb; fb += sz;
-            L.f32 = fb; fb += sz;
-            L.res32 = fb; fb += sz;
             L.irc = fb; fb += L.n1 + 2;
             L.irv = fb; fb += L.n1 + 2;
             L.iqc = fb; fb += L.n1 + 2;
@@ -2114,7 +2152,7 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
             b = (double *)(((uintptr_t)fb + 15) & ~(uintptr_t)15);
         }
     }
-    if ((size_t)(b - h->pool) > need) {
+    if ((size_t)(b - h->pool) > need || (size_t)(wb - h->work) > wneed) {
         gb_r3d_destroy(h);
         gb_set_error("gb_r3d_create: multigrid pool layout mismatch");
         return GB_ERR_CUDA;
@@ -2133,18 +2171,20 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: state"); return GB_ERR_ALLOC; }
     cudaMemset(h->small, 0, 4096 + sizeof(double) * (size_t)(np + 2));
     char *sm = (char *)h->small;
-    d.resmax = (unsigned long long *)(sm + 0);
-    d.nanflag = (int *)(sm + 64);
+    d.resmax = (unsigned long long *)(sm + 0);    // 8 slots
+    d.nanflag = (int *)(sm + 64);                 // 8 slots
     d.abort = (int *)(sm + 128);
     d.steps_done = (int *)(sm + 192);
-    d.solve_status = (int *)(sm + 256);
-    d.solve_sweeps = (int *)(sm + 320);
-    h->sync = (unsigned *)(sm + 384);
+    d.solve_status = (int *)(sm + 256);           // 4 slots
+    d.solve_sweeps = (int *)(sm + 320);           // 4 slots
+    h->sync = (unsigned *)(sm + 512);             // 4 barriers, 128 bytes apart
     d.trans = (double *)(sm + 4096);
-    d.gs.count = h->sync;
-    d.gs.gen = h->sync + 1;
-    d.gs.err = (int *)(h->sync + 2);
-    d.gs.limit = 1LL << 24;
+    for (int c = 0; c < 4; ++c) {
+        d.gs[c].count = h->sync + R3_SYNC_STRIDE * c;
+        d.gs[c].gen = h->sync + R3_SYNC_STRIDE * c + 1;
+        d.gs[c].err = (int *)(h->sync + R3_SYNC_STRIDE * c + 2);
+        d.gs[c].limit = 1LL << 24;
+    }
     // factor tables
     FacJob *djobs = nullptr;
     e = cudaMalloc(&djobs, sizeof(FacJob) * jobs.size());
@@ -2191,7 +2231,10 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     }
     h->grid = sms * std::min(worst, 2);
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: stream"); return GB_ERR_CUDA; }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: streams"); return GB_ERR_CUDA; }
     *out = h;
     return GB_OK;
 }
@@ -2250,20 +2293,24 @@ static void r3_launch_transport(gb_r3d *h, int what, int step, cudaStream_t s)
     }
 }
 
-static int r3_launch_solve(gb_r3d *h, int comp, int step, cudaStream_t s)
+// One component's solve on `grid` blocks (at most h->grid, all resident).
+// The w and v solves of a step run side by side on half the blocks each:
+// their blocks together never exceed the resident capacity, and each waits
+// only at its own barrier.
+static int r3_launch_solve(gb_r3d *h, int comp, int step, cudaStream_t s, int grid)
 {
-    GB_CUDA_TRY(cudaMemsetAsync(h->sync, 0, sizeof(unsigned) * 4, s));
-    GB_CUDA_TRY(cudaMemsetAsync(h->dev.resmax, 0, sizeof(unsigned long long) * 2, s));
-    GB_CUDA_TRY(cudaMemsetAsync(h->dev.nanflag, 0, sizeof(int) * 2, s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->sync + R3_SYNC_STRIDE * comp, 0, sizeof(unsigned) * 4, s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.resmax + 2 * comp, 0, sizeof(unsigned long long) * 2, s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->dev.nanflag + 2 * comp, 0, sizeof(int) * 2, s));
     R3Dev D = h->dev;
     void *args[] = {&D, &step};
     const bool mixed = h->p.precision == GB_PRB_MIXED;
     const void *k = comp == 1   ? (mixed ? (const void *)k_r3d_solve_mixed<1> : (const void *)k_r3d_solve<1>)
                     : comp == 2 ? (mixed ? (const void *)k_r3d_solve_mixed<2> : (const void *)k_r3d_solve<2>)
                                 : (mixed ? (const void *)k_r3d_solve_mixed<3> : (const void *)k_r3d_solve<3>);
-    cudaError_t e = cudaLaunchCooperativeKernel(k, h->grid, R3_THREADS, args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel(k, grid, R3_THREADS, args, 0, s);
     if (e != cudaSuccess) {
-        gb_set_error("gb_r3d: cooperative solve launch (%d blocks): %s", h->grid, cudaGetErrorString(e));
+        gb_set_error("gb_r3d: cooperative solve launch (%d blocks): %s", grid, cudaGetErrorString(e));
         return GB_ERR_CUDA;
     }
     return GB_OK;
@@ -2271,11 +2318,16 @@ static int r3_launch_solve(gb_r3d *h, int comp, int step, cudaStream_t s)
 
 static int r3_sync(gb_r3d *h, const char *what)
 {
-    cudaError_t e = cudaStreamSynchronize(h->stream);
+    cudaError_t e = cudaStreamSynchronize(h->side);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) { gb_set_error("%s: %s", what, cudaGetErrorString(e)); return GB_ERR_CUDA; }
-    int err = 0;
-    GB_CUDA_TRY(cudaMemcpy(&err, h->sync + 2, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) { gb_set_error("%s: a grid barrier wait timed out", what); return GB_TIMEOUT; }
+    unsigned sy[4 * R3_SYNC_STRIDE];
+    GB_CUDA_TRY(cudaMemcpy(sy, h->sync, sizeof(sy), cudaMemcpyDeviceToHost));
+    for (int c = 1; c <= 3; ++c)
+        if (sy[R3_SYNC_STRIDE * c + 2]) {
+            gb_set_error("%s: a grid barrier wait timed out (component %d)", what, c);
+            return GB_TIMEOUT;
+        }
     return GB_OK;
 }
 
@@ -2314,13 +2366,13 @@ extern "C" int gb_r3d_poisson(gb_r3d *h, int which, int *sweeps)
 {
     if (!h || which < 1 || which > 3) { gb_set_error("gb_r3d_poisson: invalid argument"); return GB_ERR_INVALID; }
     r3_clear_abort(h);
-    int st = r3_launch_solve(h, which, -1, h->stream);
+    int st = r3_launch_solve(h, which, -1, h->stream, h->grid);
     if (st != GB_OK) return st;
     st = r3_sync(h, "gb_r3d_poisson");
     if (st != GB_OK) return st;
     int out[2] = {0, 0};
-    GB_CUDA_TRY(cudaMemcpy(&out[0], h->dev.solve_status, sizeof(int), cudaMemcpyDeviceToHost));
-    GB_CUDA_TRY(cudaMemcpy(&out[1], h->dev.solve_sweeps, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CUDA_TRY(cudaMemcpy(&out[0], h->dev.solve_status + which, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CUDA_TRY(cudaMemcpy(&out[1], h->dev.solve_sweeps + which, sizeof(int), cudaMemcpyDeviceToHost));
     if (sweeps) *sweeps = out[1];
     return out[0];
 }
@@ -2353,14 +2405,21 @@ extern "C" int gb_r3d_step(gb_r3d *h, int nsteps, double *nu, int *sweeps, int *
         r3_launch_transport(h, 3, step, s);
         r3_launch_transport(h, 4, step, s);
         r3_launch_transport(h, 5, step, s);
-        int st = r3_launch_solve(h, 1, step, s);
+        // rhsv reads An and Cn only, and the w and v solves touch disjoint
+        // fields: the v solve runs beside the w solve, on the side stream
+        GB_CUDA_TRY(cudaEventRecord(h->ev_fork, s));
+        GB_CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+        const int half = std::max(1, h->grid / 2);
+        int st = r3_launch_solve(h, 1, step, s, half);
         if (st == GB_OK) {
-            r3_launch_transport(h, 6, step, s);
-            st = r3_launch_solve(h, 2, step, s);
+            r3_launch_transport(h, 6, step, h->side);
+            st = r3_launch_solve(h, 2, step, h->side, h->grid - half);
         }
         if (st == GB_OK) {
+            GB_CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
+            GB_CUDA_TRY(cudaStreamWaitEvent(s, h->ev_join, 0));
             r3_launch_transport(h, 7, step, s);
-            st = r3_launch_solve(h, 3, step, s);
+            st = r3_launch_solve(h, 3, step, s, h->grid);
         }
         if (st != GB_OK) return st;
         r3_launch_transport(h, 8, step, s);
