@@ -337,35 +337,82 @@ __global__ void k_rhs(PrbDev d, int do_v, int do_u)
 
 // update, PRB:1557-1626.  Each thread owns one (i,k) of rows 0..nr+1; the
 // wall values it writes are only read back by the same thread.
+// Warp maximum of the CFL candidates (non-negative, never NaN), one atomic
+// per warp into the step's history slot (zeroed when the run began).
+__device__ __forceinline__ void prb_cfl_reduce(const PrbDev &d, double cu, double cv)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        cu = fmax(cu, __shfl_xor_sync(0xffffffffu, cu, o));
+        cv = fmax(cv, __shfl_xor_sync(0xffffffffu, cv, o));
+    }
+    const int s = *d.step_index;
+    if ((threadIdx.x & 31) == 0 && s < d.hist_cap) {
+        if (cu > 0.0) atomicMax(&d.cfl_hist[2 * s + 0], (unsigned long long)__double_as_longlong(cu));
+        if (cv > 0.0) atomicMax(&d.cfl_hist[2 * s + 1], (unsigned long long)__double_as_longlong(cv));
+    }
+}
+
+//
+// DIAG: the time loop's diagnostics of the step, fused (PRB:404-459,
+// velvor2dnewsch3.4.f:404-459): at kt >= 2 the running means
+// m = (1/(kt-1)) m (kt-2) + (1/(kt-1)) x of T^2, T, u^2, v^2 at every point,
+// and the step's CFL maxima max |u dt/dr| (rows 1..nr) and max |v dt/(r dp)|
+// (rows 1..nr-1; r = 1 in the layer, r0 + (i - 1/2) dr in the annulus) into
+// the step's history slot.  A NaN never wins the reference's comparison.
+template <bool DIAG>
 __global__ void k_update(PrbDev d)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nr = d.nr, np = d.np, ld = d.ld;
-    if (t >= (nr + 2) * (np + 1) || *d.abort) return;
-    const int i = t % (nr + 2), k = t / (nr + 2);
-    double *const *f = d.f;
-    const double dr = d.dr;
-    const size_t c = GIX(i, k, ld);
-    if (i == 0) {
-        f[GB_F_Bn][c] = -(3.0 * f[GB_F_wel][GIX(1, k, ld)] - f[GB_F_wel][GIX(2, k, ld)] / 3.0) / dr;
-        f[GB_F_Cn][c] = (3.0 * f[GB_F_vel][GIX(1, k, ld)] - f[GB_F_vel][GIX(2, k, ld)] / 3.0) / dr;
-        f[GB_F_thn][c] = 0.0;
-    } else if (i == nr) {
-        f[GB_F_Bn][c] = -(f[GB_F_wel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_wel][GIX(nr, k, ld)]) / dr;
-        f[GB_F_Cn][c] = (f[GB_F_vel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_vel][GIX(nr, k, ld)]) / dr;
-    } else if (i == nr + 1) {
-        f[GB_F_thn][c] = 1.0;
+    if (*d.abort) return;   // uniform across the grid
+    double cu = 0.0, cv = 0.0;
+    if (t < (nr + 2) * (np + 1)) {
+        const int i = t % (nr + 2), k = t / (nr + 2);
+        double *const *f = d.f;
+        const double dr = d.dr;
+        const size_t c = GIX(i, k, ld);
+        if (i == 0) {
+            f[GB_F_Bn][c] = -(3.0 * f[GB_F_wel][GIX(1, k, ld)] - f[GB_F_wel][GIX(2, k, ld)] / 3.0) / dr;
+            f[GB_F_Cn][c] = (3.0 * f[GB_F_vel][GIX(1, k, ld)] - f[GB_F_vel][GIX(2, k, ld)] / 3.0) / dr;
+            f[GB_F_thn][c] = 0.0;
+        } else if (i == nr) {
+            f[GB_F_Bn][c] = -(f[GB_F_wel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_wel][GIX(nr, k, ld)]) / dr;
+            f[GB_F_Cn][c] = (f[GB_F_vel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_vel][GIX(nr, k, ld)]) / dr;
+        } else if (i == nr + 1) {
+            f[GB_F_thn][c] = 1.0;
+        }
+        f[GB_F_Cp][c] = f[GB_F_C][c];
+        f[GB_F_C][c] = f[GB_F_Cn][c];
+        f[GB_F_thp][c] = f[GB_F_th][c];
+        double tn = f[GB_F_thn][c];
+        unsigned long long clamped = 0;
+        if (tn > 1.0) { tn = 0.99; clamped++; }
+        if (tn < 0.0) { tn = 0.01; clamped++; }
+        f[GB_F_thn][c] = tn;
+        f[GB_F_th][c] = tn;
+        if (clamped) atomicAdd(d.clamps, clamped);
+        const int kt = DIAG ? *d.diag_kt : 0;
+        if (DIAG && kt >= 2) {
+            const size_t n = (size_t)ld * (size_t)(np + 1);
+            double *mT2 = d.diag, *mT = d.diag + n, *mU2 = d.diag + 2 * n, *mV2 = d.diag + 3 * n;
+            const double tkti = 1.0 / (double)(kt - 1), w = (double)(kt - 2);
+            const double u = f[GB_F_uel][c], v = f[GB_F_vel][c];
+            mT2[c] = tkti * mT2[c] * w + tkti * (tn * tn);
+            mT[c] = tkti * mT[c] * w + tkti * tn;
+            mU2[c] = tkti * mU2[c] * w + tkti * (u * u);
+            mV2[c] = tkti * mV2[c] * w + tkti * (v * v);
+            if (i >= 1 && i <= nr) {
+                const double x = fabs(u * d.dt / d.dr);
+                if (x > cu) cu = x;
+            }
+            if (i >= 1 && i <= nr - 1) {
+                const double r = d.polar ? d.r0 + ((double)i - 0.5) * dr : 1.0;
+                const double x = fabs(v * d.dt / (r * d.dp));
+                if (x > cv) cv = x;
+            }
+        }
     }
-    f[GB_F_Cp][c] = f[GB_F_C][c];
-    f[GB_F_C][c] = f[GB_F_Cn][c];
-    f[GB_F_thp][c] = f[GB_F_th][c];
-    double tn = f[GB_F_thn][c];
-    unsigned long long clamped = 0;
-    if (tn > 1.0) { tn = 0.99; clamped++; }
-    if (tn < 0.0) { tn = 0.01; clamped++; }
-    f[GB_F_thn][c] = tn;
-    f[GB_F_th][c] = tn;
-    if (clamped) atomicAdd(d.clamps, clamped);
+    if (DIAG) prb_cfl_reduce(d, cu, cv);   // every lane of every warp
 }
 
 // Per-step bookkeeping for graph-replayed steps: copies the step's Nusselt
@@ -383,7 +430,38 @@ __global__ void k_record(PrbDev d, double c1, double c2, double div)
         d.sweep_hist[2 * s + 0] = d.mg_status[1];
         d.sweep_hist[2 * s + 1] = d.mg_status[3];
     }
-    if (!*d.abort) *d.step_index = s + 1;
+    if (!*d.abort) {
+        *d.step_index = s + 1;
+        if (d.diag_kt) *d.diag_kt += 1;
+    }
+}
+
+__global__ void k_prb_set_kt(int *kt, int value) { *kt = value; }
+
+// Zonal means of the running means, one thread per row i = 0..nr+1, summed
+// over k = 0..np in order (PRB:474-493): out[3 i + 0] the zonal-mean time
+// variance of T, out[3 i + 1..2] the zonal rms of u and v.  The reference
+// evaluates **0.5d0 through libm's pow; sqrt here (correctly rounded; the two
+// agree to an ulp).
+__global__ void k_prb_zonal(PrbDev d, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > d.nr + 1) return;
+    const int ld = d.ld, np = d.np;
+    const size_t n = (size_t)ld * (size_t)(np + 1);
+    const double *mT2 = d.diag, *mT = d.diag + n, *mU2 = d.diag + 2 * n, *mV2 = d.diag + 3 * n;
+    double a = 0.0, b = 0.0, cu = 0.0, cv = 0.0;
+    for (int k = 0; k <= np; ++k) {
+        const size_t c = GIX(i, k, ld);
+        a = a + mT2[c];
+        b = b + mT[c] * mT[c];
+        cu = cu + mU2[c];
+        cv = cv + mV2[c];
+    }
+    const double m = (double)(np + 1);
+    out[3 * i + 0] = (a - b) / m;
+    out[3 * i + 1] = sqrt(cu / m);
+    out[3 * i + 2] = sqrt(cv / m);
 }
 
 // ---------------------------------------------------------------------------
@@ -431,10 +509,13 @@ int prb_launch_rhs(gb_prb *h, int do_v, int do_u, cudaStream_t s)
     return GB_OK;
 }
 
-int prb_launch_update(gb_prb *h, cudaStream_t s)
+int prb_launch_update(gb_prb *h, cudaStream_t s, bool diag)
 {
     PrbDev &d = h->dev;
-    k_update<<<gb_ceil_div((size_t)(d.nr + 2) * (d.np + 1), TPB), TPB, 0, s>>>(d);
+    if (diag && d.diag)
+        k_update<true><<<gb_ceil_div((size_t)(d.nr + 2) * (d.np + 1), TPB), TPB, 0, s>>>(d);
+    else
+        k_update<false><<<gb_ceil_div((size_t)(d.nr + 2) * (d.np + 1), TPB), TPB, 0, s>>>(d);
     h->launches += 1;
     return GB_OK;
 }
@@ -613,6 +694,7 @@ extern "C" int gb_prb_destroy(gb_prb *h)
     cudaFree(h->factors);
     cudaFree(h->small);
     cudaFree(h->hist);
+    cudaFree(h->diag_buf);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return GB_OK;
@@ -718,7 +800,7 @@ extern "C" int gb_prb_update(gb_prb *h, long long *clamps)
     if (!h) return GB_ERR_INVALID;
     prb_begin(h);
     GB_CUDA_TRY(cudaMemsetAsync(h->dev.clamps, 0, sizeof(unsigned long long), h->stream));
-    prb_launch_update(h, h->stream);
+    prb_launch_update(h, h->stream, false);
     unsigned long long c = 0;
     GB_CUDA_TRY(cudaMemcpyAsync(&c, h->dev.clamps, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
     int st = prb_sync(h, "gb_prb_update");
@@ -748,7 +830,7 @@ static void prb_enqueue_step(gb_prb *h, int first, cudaStream_t s)
     prb_launch_heat(h, s);
     prb_launch_rhs(h, 1, 1, s);
     prb_launch_mg(h, 1, 1, s);
-    prb_launch_update(h, s);
+    prb_launch_update(h, s, true);
     prb_launch_record(h, s);
 }
 
@@ -765,6 +847,8 @@ static int prb_build_graph(gb_prb *h, int first, cudaGraphExec_t *exec)
     cudaGraphDestroy(g);
     return GB_OK;
 }
+
+static int prb_diag_alloc(gb_prb *h, int cap);
 
 // Asynchronous stepping: run_begin sizes the history and resets the step
 // counters, run_enqueue queues graph launches on the instance's stream
@@ -786,6 +870,13 @@ extern "C" int gb_prb_run_begin(gb_prb *h, int nsteps_total)
     d.nu_hist = (double *)h->hist;
     d.sweep_hist = (int *)((double *)h->hist + 2 * (size_t)h->hist_cap);
     d.hist_cap = h->hist_cap;
+    if (h->diag_buf) {
+        if (h->diag_cap < h->hist_cap) {
+            int st = prb_diag_alloc(h, h->hist_cap);
+            if (st != GB_OK) return st;
+        }
+        GB_CUDA_TRY(cudaMemsetAsync(d.cfl_hist, 0, sizeof(unsigned long long) * 2 * (size_t)h->hist_cap, h->stream));
+    }
     // scalars are baked into the graphs: rebuild when they change
     if (memcmp(&h->graph_scalars, &h->p, sizeof(gb_prb_params)) != 0) {
         if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
@@ -802,6 +893,10 @@ extern "C" int gb_prb_run_enqueue(gb_prb *h, int kt0, int nsteps)
 {
     if (!h || nsteps < 0 || kt0 < 1) { gb_set_error("gb_prb_run_enqueue: invalid argument"); return GB_ERR_INVALID; }
     int st;
+    if (h->dev.diag && nsteps > 0) {
+        k_prb_set_kt<<<1, 1, 0, h->stream>>>(h->dev.diag_kt, kt0);
+        h->launches += 1;
+    }
     for (int s = 0; s < nsteps; ++s) {
         const int first = (kt0 + s == 1);
         cudaGraphExec_t *ex = first ? &h->graph_exec1 : &h->graph_exec;
@@ -860,3 +955,103 @@ extern "C" int gb_prb_step(gb_prb *h, int kt0, int nsteps, double *nu, int *swee
 }
 
 extern "C" void *gb_prb_stream(gb_prb *h) { return h ? (void *)h->stream : nullptr; }
+
+// ---------------------------------------------------------------------------
+// Time-loop diagnostics (PRB:404-493)
+// ---------------------------------------------------------------------------
+static void prb_drop_graphs(gb_prb *h)
+{
+    if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+    if (h->graph_exec1) { cudaGraphExecDestroy(h->graph_exec1); h->graph_exec1 = nullptr; }
+}
+
+// (Re)allocates the diagnostics buffer for `cap` history slots; the running
+// means start at zero (as weln, welp and vrms do; Bp's initial value is
+// multiplied by zero at the block's first step).
+static int prb_diag_alloc(gb_prb *h, int cap)
+{
+    PrbDev &d = h->dev;
+    const size_t n = h->fsz;
+    const size_t bytes = sizeof(double) * 4 * n + 64 + sizeof(unsigned long long) * 2 * (size_t)cap;
+    double *buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, bytes);
+    if (e != cudaSuccess) { gb_set_error("gb_prb_diag_enable: %s", cudaGetErrorString(e)); return GB_ERR_ALLOC; }
+    cudaMemsetAsync(buf, 0, bytes, h->stream);
+    if (h->diag_buf) {
+        // keep the running means across a history resize
+        cudaMemcpyAsync(buf, h->diag_buf, sizeof(double) * 4 * n + 64, cudaMemcpyDeviceToDevice, h->stream);
+        cudaStreamSynchronize(h->stream);
+        cudaFree(h->diag_buf);
+    }
+    h->diag_buf = buf;
+    h->diag_cap = cap;
+    d.diag = buf;
+    d.diag_kt = (int *)(buf + 4 * n);
+    d.cfl_hist = (unsigned long long *)(buf + 4 * n + 8);
+    prb_drop_graphs(h);
+    return GB_OK;
+}
+
+extern "C" int gb_prb_diag_enable(gb_prb *h, int on)
+{
+    if (!h) { gb_set_error("gb_prb_diag_enable: null handle"); return GB_ERR_INVALID; }
+    PrbDev &d = h->dev;
+    if (!on) {
+        if (h->diag_buf) {
+            GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+            cudaFree(h->diag_buf);
+        }
+        h->diag_buf = nullptr;
+        h->diag_cap = 0;
+        d.diag = nullptr;
+        d.diag_kt = nullptr;
+        d.cfl_hist = nullptr;
+        prb_drop_graphs(h);
+        return GB_OK;
+    }
+    if (h->diag_buf) {
+        // a fresh start: clear the running means
+        GB_CUDA_TRY(cudaMemsetAsync(h->diag_buf, 0, sizeof(double) * 4 * h->fsz, h->stream));
+        return prb_sync(h, "gb_prb_diag_enable");
+    }
+    int st = prb_diag_alloc(h, h->hist_cap > 0 ? h->hist_cap : 1);
+    if (st != GB_OK) return st;
+    return prb_sync(h, "gb_prb_diag_enable");
+}
+
+extern "C" int gb_prb_diag_zonal(gb_prb *h, double *out)
+{
+    if (!h || !out || !h->dev.diag) { gb_set_error("gb_prb_diag_zonal: diagnostics not enabled"); return GB_ERR_INVALID; }
+    const int rows = h->dev.nr + 2;
+    double *dout = nullptr;
+    GB_CUDA_TRY(cudaMallocAsync(&dout, sizeof(double) * 3 * (size_t)rows, h->stream));
+    k_prb_zonal<<<gb_ceil_div(rows, 64), 64, 0, h->stream>>>(h->dev, dout);
+    GB_CUDA_TRY(cudaMemcpyAsync(out, dout, sizeof(double) * 3 * (size_t)rows, cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA_TRY(cudaFreeAsync(dout, h->stream));
+    return prb_sync(h, "gb_prb_diag_zonal");
+}
+
+extern "C" int gb_prb_diag_mean(gb_prb *h, int q, double *host, int ld)
+{
+    if (!h || !host || q < 0 || q > 3 || !h->dev.diag || ld < h->dev.ld) {
+        gb_set_error("gb_prb_diag_mean: invalid argument or diagnostics not enabled");
+        return GB_ERR_INVALID;
+    }
+    const PrbDev &d = h->dev;
+    GB_CUDA_TRY(cudaMemcpy2DAsync(host, sizeof(double) * (size_t)ld, d.diag + (size_t)q * h->fsz,
+                                  sizeof(double) * (size_t)d.ld, sizeof(double) * (size_t)d.ld, (size_t)d.np + 1,
+                                  cudaMemcpyDeviceToHost, h->stream));
+    return prb_sync(h, "gb_prb_diag_mean");
+}
+
+extern "C" int gb_prb_diag_cfl(gb_prb *h, int nsteps, double *cfl)
+{
+    if (!h || nsteps < 0 || !h->dev.diag || nsteps > h->hist_cap) {
+        gb_set_error("gb_prb_diag_cfl: invalid argument or diagnostics not enabled");
+        return GB_ERR_INVALID;
+    }
+    if (nsteps == 0) return GB_OK;
+    GB_CUDA_TRY(cudaMemcpyAsync(cfl, h->dev.cfl_hist, sizeof(double) * 2 * (size_t)nsteps, cudaMemcpyDeviceToHost,
+                                h->stream));
+    return prb_sync(h, "gb_prb_diag_cfl");
+}

@@ -57,6 +57,12 @@ struct PrbDev {
     double *nu_hist;
     int *sweep_hist;
     int hist_cap;
+    // time-loop diagnostics (PRB:404-459), null when off: running means of
+    // T^2, T, u^2, v^2 (four (ld, np+1) arrays), the kt of the step in
+    // flight, per-step CFL maxima (2 per history slot, bit patterns)
+    double *diag;
+    int *diag_kt;
+    unsigned long long *cfl_hist;
 };
 
 struct gb_prb {
@@ -78,6 +84,8 @@ struct gb_prb {
     cudaGraphExec_t graph_exec = nullptr, graph_exec1 = nullptr;
     gb_prb_params graph_scalars;
     long long launches = 0, launches_per_step = 0;
+    double *diag_buf = nullptr;   // 4 running means + kt + CFL history (hist_cap slots)
+    int diag_cap = 0;
     int steps_done = 0;
 };
 

@@ -8,7 +8,9 @@ Usage:  python -m codesthesis_dir_gb300.driver < input.s  [--xx 3] [--smoother l
 Block structure as in the reference: the first block runs steps kt = 1..nts
 (kt = 1 is the forward step); every "more iterations" block runs kt = 2..nts
 and advances the step counter ntot by nts, so httrans(ntot+1) of each later
-block stays zero (PRB:357-571).
+block stays zero (PRB:357-571).  The time loop's diagnostics run on the
+device: zmtmtempvar.dat is written after every block (PRB:474-493) and the
+CFL maxima are logged as the reference prints them (PRB:390-459).
 """
 from __future__ import annotations
 
@@ -60,25 +62,41 @@ def run(deck_text, xx=3.0, smoother=_L.SMOOTHER_LEX, outdir=".", tolcon=2e-6, lo
     fields["thp"], fields["uelp"], fields["velp"] = fields["th"].copy(), fields["uel"].copy(), fields["vel"].copy()
     for n, a in fields.items():
         g.set(n, a)
+    g.diagnostics(True)
     httrans, httrans2 = [], []
     ntot = 0
     blocks = [d.nts] + list(d.more)
     for b, nts in enumerate(blocks):
         if b == 0:
             nu, sw = g.step(nts)
-            g.kt = 0
+            kt0 = 1
             httrans += list(nu[:, 0])
             httrans2 += list(nu[:, 1])
         else:
             httrans += [0.0]
             httrans2 += [0.0]
+            kt0 = 2
+            nu = np.zeros((0, 2))
             if nts >= 2:
-                nu = np.zeros((nts - 1, 2))
-                sw = np.zeros((nts - 1, 2), dtype=np.int32)
-                _L.check(_L.load().gb_prb_step(g._h, 2, nts - 1, nu.ctypes.data, sw.ctypes.data), "step")
+                g.new_block()
+                nu, sw = g.step(nts - 1)
                 httrans += list(nu[:, 0])
                 httrans2 += list(nu[:, 1])
+        # the time loop's prints (PRB:390-395, 432-434, 456-458): every 50th
+        # step the Nusselt numbers and the CFL maxima of the step before
+        cfl = g.cfl(len(nu))
+        for s_ in range(len(nu)):
+            kt = kt0 + s_
+            if kt >= 2 and cfl[s_, 0] > 1.0:
+                log("WARNING! CFLU EXCEEDED!")
+            if kt >= 2 and cfl[s_, 1] > 1.0:
+                log("WARNING! CFLV EXCEEDED!")
+            if kt % 50 == 0:
+                log("%r %r %d" % (nu[s_, 0], nu[s_, 1], ntot + kt))
+                log("CFLMAXU= %r" % cfl[s_ - 1, 0])   # kt >= 50: s_ >= 48
+                log("CFLMAXV= %r" % cfl[s_ - 1, 1])
         ntot += nts
+        fortio.write_zmtm(os.path.join(outdir, "zmtmtempvar.dat"), g.zonal())
         log("block %d: %d steps, Nu = %.8f %.8f" % (b + 1, ntot, httrans[-1], httrans2[-1]))
         # restart / output files (PRB:500-549) and the Nusselt history (PRB:551-560)
         for name, fn in zip(fortio.RESTART_ORDER, d.fnames[:7]):

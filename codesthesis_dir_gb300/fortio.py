@@ -103,6 +103,28 @@ def write_nu_history(path, dt, httrans, ssumc=None, ssums=None):
             fh.write("".join(" " + fortran_e(v) for v in vals) + "\n")
 
 
+def write_zmtm(path, rows):
+    """zmtmtempvar.dat of PRB:474-493: per row i = 0..nr+1 the zonal-mean
+    time variance of T and the zonal rms of u and v, format 3(1x,e16.8)."""
+    with open(path, "w") as fh:
+        for r in np.asarray(rows).reshape(-1, 3):
+            fh.write("".join(" " + fortran_e(float(v)) for v in r) + "\n")
+
+
+def fortran_real(tok: str) -> float:
+    """A value printed by an E edit descriptor, including the form without
+    the letter E that a three-digit exponent takes (0.2+121)."""
+    t = tok.strip()
+    k = max(t.rfind("+"), t.rfind("-"))
+    if k > 0 and t[k - 1] not in "eEdD":
+        t = t[:k] + "E" + t[k:]
+    return float(t.replace("D", "E").replace("d", "E"))
+
+
+def read_zmtm(path):
+    return np.array([[fortran_real(x) for x in ln.split()] for ln in open(path) if ln.strip()])
+
+
 # (i, j) extents of the 3D fields in their files (rot3dmg.f:265-310): the last
 # i and j index written, given nr and nz.
 R3D_ORDER = ["A", "B", "C", "uel", "vel", "wel", "th"]

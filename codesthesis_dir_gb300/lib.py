@@ -113,6 +113,10 @@ SIGNATURES = [
     ("gb_prb_run_enqueue", C.c_int, [_vp, C.c_int, C.c_int]),
     ("gb_prb_run_query", C.c_int, [_vp]),
     ("gb_prb_run_end", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
+    ("gb_prb_diag_enable", C.c_int, [_vp, C.c_int]),
+    ("gb_prb_diag_zonal", C.c_int, [_vp, _vp]),
+    ("gb_prb_diag_mean", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
+    ("gb_prb_diag_cfl", C.c_int, [_vp, C.c_int, _vp]),
     ("gb_axi_default_params", None, [C.POINTER(AxiParams), C.c_int, C.c_int]),
     ("gb_axi_create", C.c_int, [C.POINTER(AxiParams), C.POINTER(_vp), _ip]),
     ("gb_axi_destroy", C.c_int, [_vp]),

@@ -125,6 +125,35 @@ class PRB:
         self.kt += nsteps
         return nu, sw
 
+    def new_block(self):
+        """A "more iterations" block of the main program: its steps run as
+        kt = 2, 3, ... again (PRB:357-571)."""
+        self.kt = 1
+
+    # -- time-loop diagnostics (PRB:404-493) ----------------------------------
+    def diagnostics(self, on=True):
+        """Running means of T^2, T, u^2, v^2 and per-step CFL maxima, updated
+        on the device by every step with kt >= 2."""
+        _L.check(_L.load().gb_prb_diag_enable(self._h, 1 if on else 0), "diag_enable")
+
+    def zonal(self):
+        """(nr+2, 3): the rows of zmtmtempvar.dat (T variance, u rms, v rms)."""
+        out = np.zeros(3 * (self.nr + 2))
+        _L.check(_L.load().gb_prb_diag_zonal(self._h, out.ctypes.data), "diag_zonal")
+        return out.reshape(-1, 3)
+
+    def running_mean(self, q):
+        """Running mean q (0: T^2, 1: T, 2: u^2, 3: v^2), (ld, np+1)."""
+        a = np.zeros((self.ld, self.np + 1), order="F")
+        _L.check(_L.load().gb_prb_diag_mean(self._h, q, a.ctypes.data, self.ld), "diag_mean")
+        return a
+
+    def cfl(self, nsteps):
+        """(nsteps, 2): the u and v CFL maxima of each step of the last run."""
+        out = np.zeros((nsteps, 2))
+        _L.check(_L.load().gb_prb_diag_cfl(self._h, nsteps, out.ctypes.data), "diag_cfl")
+        return out
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             _L.load().gb_prb_destroy(self._h)

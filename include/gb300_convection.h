@@ -182,6 +182,31 @@ int gb_prb_run_enqueue(gb_prb *h, int kt0, int nsteps);
 int gb_prb_run_query(gb_prb *h);
 int gb_prb_run_end(gb_prb *h, int nsteps, double *nu, int *sweeps, int *steps_done);
 
+/* Time-loop diagnostics on the device (PRB:404-493; velvor2dnewsch3.4.f:
+ * 404-493 for the annulus), fused into the step's update kernel so the step
+ * reads nothing back.  Enabled, every graph-replayed step with kt >= 2
+ * updates the running means of T^2, T, u^2 and v^2 over the block's steps
+ * 2..kt (m = (1/(kt-1)) m (kt-2) + (1/(kt-1)) x; the reference keeps them
+ * in weln, welp, Bp and vrms, PRB:408-416), and records the step's CFL
+ * maxima max |u dt/dr| over rows 1..nr and max |v dt/(r dp)| over rows
+ * 1..nr-1, r = 1 in the layer and r0 + (i - 1/2) dr in the annulus
+ * (PRB:420-459).  A run that starts again at kt0 = 2 (a "more iterations"
+ * block) starts the means again, as the reference's factor (kt-2) does.
+ *
+ * diag_enable: on != 0 allocates and zeroes the running means (again, when
+ * already on); 0 frees them.  Graphs are rebuilt on the next run.
+ * diag_zonal: out[3 i + c], i = 0..nr+1: the rows of zmtmtempvar.dat
+ * (PRB:474-493): zonal-mean time variance of T, zonal rms of u, of v (sqrt;
+ * the reference's **0.5d0 goes through libm pow and agrees to an ulp).
+ * diag_mean: running mean q (0: T^2, 1: T, 2: u^2, 3: v^2) into host
+ * (ld, np+1) column-major.
+ * diag_cfl: cfl[2 s + 0..1], the u and v CFL maxima of step s of the last
+ * run (0, 0 for a kt = 1 step and for steps that did not run). */
+int gb_prb_diag_enable(gb_prb *h, int on);
+int gb_prb_diag_zonal(gb_prb *h, double *out);
+int gb_prb_diag_mean(gb_prb *h, int q, double *host, int ld);
+int gb_prb_diag_cfl(gb_prb *h, int nsteps, double *cfl);
+
 /* ------------------------------------------- gfortran-compatible drop-in */
 /* These read/write the caller's COMMON blocks (declared by the Fortran main
  * program; the library carries weak references of the reference's sizes,

@@ -142,6 +142,9 @@ def lib():
         L.orc_prb_step.argtypes = [C.POINTER(PRB), C.POINTER(MG), C.POINTER(MG), C.c_int, _dp, _ip]
         L.orc_prb_step.restype = C.c_int
         L.orc_prb_initial.argtypes = [C.POINTER(PRB), C.c_int, C.c_ulonglong, C.c_double]
+        L.orc_prb_diag_accum.argtypes = [C.POINTER(PRB), C.c_int, _dp, _dp, _dp, _dp]
+        L.orc_prb_cfl.argtypes = [C.POINTER(PRB), _dp, _dp]
+        L.orc_prb_zmtm.argtypes = [C.POINTER(PRB), _dp, _dp, _dp, _dp, _dp]
         L.orc_axi_init.argtypes = [C.POINTER(AXI), C.c_int, C.c_int] + [C.c_double] * 7
         L.orc_axi_init.restype = C.c_int
         L.orc_axi_free.argtypes = [C.POINTER(AXI)]
@@ -266,6 +269,30 @@ class OraclePRB:
                 mg.maxsweeps = maxsweeps
             mg.sor = sor
         self.kt = 0
+        self.diag = None
+        self.cfl_hist = []
+
+    def enable_diagnostics(self):
+        """Running means (T^2, T, u^2, v^2) and per-step CFL maxima of
+        PRB:404-459, updated by every later step with kt >= 2; a step with
+        kt = 1 records CFL maxima (0, 0)."""
+        n = self.s.ld * (self.s.np + 1)
+        self.diag = [np.zeros(n) for _ in range(4)]
+        self.cfl_hist = []
+
+    def new_block(self):
+        """A "more iterations" block: its steps run as kt = 2, 3, ... again."""
+        self.kt = 1
+
+    def zmtm(self) -> np.ndarray:
+        """(nr+2, 3): the rows of zmtmtempvar.dat (PRB:474-493)."""
+        out = np.zeros(3 * (self.s.nr + 2))
+        lib().orc_prb_zmtm(C.byref(self.s), *[ptr(a) for a in self.diag], ptr(out))
+        return out.reshape(-1, 3)
+
+    def running_mean(self, q) -> np.ndarray:
+        """Running mean q (0: T^2, 1: T, 2: u^2, 3: v^2) as a (ld, np+1) view."""
+        return self.diag[q].reshape((self.s.np + 1, self.s.ld)).T
 
     @property
     def nr(self):
@@ -292,6 +319,12 @@ class OraclePRB:
         sw = np.zeros(2, dtype=np.int32)
         st = lib().orc_prb_step(C.byref(self.s), C.byref(self.mgv), C.byref(self.mgu), self.kt,
                                 ptr(nu), iptr(sw))
+        if self.diag is not None and st == 0:
+            cu, cv = C.c_double(0.0), C.c_double(0.0)
+            if self.kt >= 2:
+                lib().orc_prb_diag_accum(C.byref(self.s), self.kt, *[ptr(a) for a in self.diag])
+                lib().orc_prb_cfl(C.byref(self.s), C.byref(cu), C.byref(cv))
+            self.cfl_hist.append((cu.value, cv.value))
         return st, nu, sw
 
     def close(self):

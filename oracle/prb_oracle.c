@@ -1092,6 +1092,68 @@ int orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double *nu,
     return ORC_OK;
 }
 
+/* Running means of the zonal-mean time-mean diagnostics (PRB:404-416).  The
+ * reference keeps them in borrowed arrays (weln, welp, Bp, vrms); x**2.d0 is
+ * x*x. */
+void orc_prb_diag_accum(const orc_prb_t *s, int kt, double *msqT, double *mT, double *msqU, double *msqV)
+{
+    if (kt < 2) return;
+    const int ld = s->ld;
+    const double tkti = 1.0 / (double)(kt - 1);
+    const double w = (double)(kt - 2);
+    for (int i = 0; i <= s->nr + 1; ++i)
+        for (int k = 0; k <= s->np; ++k) {
+            const size_t c = (size_t)i + (size_t)ld * (size_t)k;
+            const double th = s->th[c], u = s->uel[c], v = s->vel[c];
+            msqT[c] = tkti * msqT[c] * w + tkti * (th * th);
+            mT[c] = tkti * mT[c] * w + tkti * th;
+            msqU[c] = tkti * msqU[c] * w + tkti * (u * u);
+            msqV[c] = tkti * msqV[c] * w + tkti * (v * v);
+        }
+}
+
+/* CFL scans (PRB:420-459; the annulus radius of velvor2dnewsch3.4.f:437-445). */
+void orc_prb_cfl(const orc_prb_t *s, double *cflu, double *cflv)
+{
+    const int ld = s->ld;
+    double mu = 0.0, mv = 0.0;
+    for (int i = 1; i <= s->nr; ++i)
+        for (int k = 0; k <= s->np; ++k) {
+            const double cfl = fabs(s->uel[(size_t)i + (size_t)ld * (size_t)k] * s->dt / s->dr);
+            if (cfl > mu) mu = cfl;
+        }
+    for (int i = 1; i <= s->nr - 1; ++i) {
+        const double r = s->variant == ORC_ANNULUS ? s->r0 + ((double)i - 0.5) * s->dr : 1.0;
+        for (int k = 0; k <= s->np; ++k) {
+            const double cfl = fabs(s->vel[(size_t)i + (size_t)ld * (size_t)k] * s->dt / (r * s->dp));
+            if (cfl > mv) mv = cfl;
+        }
+    }
+    *cflu = mu;
+    *cflv = mv;
+}
+
+/* Zonal means written to zmtmtempvar.dat (PRB:474-493). */
+void orc_prb_zmtm(const orc_prb_t *s, const double *msqT, const double *mT, const double *msqU,
+                  const double *msqV, double *out)
+{
+    const int ld = s->ld;
+    const double n = (double)(s->np + 1);
+    for (int i = 0; i <= s->nr + 1; ++i) {
+        double a = 0.0, b = 0.0, cu = 0.0, cv = 0.0;
+        for (int k = 0; k <= s->np; ++k) {
+            const size_t c = (size_t)i + (size_t)ld * (size_t)k;
+            a = a + msqT[c];
+            b = b + mT[c] * mT[c];
+            cu = cu + msqU[c];
+            cv = cv + msqV[c];
+        }
+        out[3 * i + 0] = (a - b) / n;
+        out[3 * i + 1] = pow(cu / n, 0.5);
+        out[3 * i + 2] = pow(cv / n, 0.5);
+    }
+}
+
 /* splitmix64 (Steele, Lea, Flood 2014), used for the seeded noise. */
 static unsigned long long splitmix64(unsigned long long *state)
 {

@@ -120,6 +120,27 @@ void orc_rhsu(orc_prb_t *s);
 int  orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt,
                   double *nu, int *sweeps);
 
+/* Diagnostics of the time loop.  Arrays are (ld, np+1) column-major like the
+ * fields.
+ *
+ * orc_prb_diag_accum, PRB:404-416 (velvor2dnewsch3.4.f:404-416 alike): at step
+ * kt >= 2 the running means over the block's steps 2..kt of T^2, T, u^2 and
+ * v^2, m = (1/(kt-1)) m (kt-2) + (1/(kt-1)) x, rows 0..nr+1, k = 0..np.
+ *
+ * orc_prb_cfl, PRB:420-459: max |u dt / dr| over i = 1..nr and
+ * max |v dt / (r dp)| over i = 1..nr-1 (r = 1 in PRB, r0 + (i - 1/2) dr in
+ * the annulus, velvor2dnewsch3.4.f:437-445); NaN entries never win a
+ * comparison.
+ *
+ * orc_prb_zmtm, PRB:474-493: per row i = 0..nr+1, the zonal means
+ * (sum msqT - sum mT^2) / (np+1), (sum msqU / (np+1))**0.5 and
+ * (sum msqV / (np+1))**0.5 (libm pow, as the compiled Fortran evaluates
+ * **0.5d0), summed over k = 0..np in order; out[3 i + c]. */
+void orc_prb_diag_accum(const orc_prb_t *s, int kt, double *msqT, double *mT, double *msqU, double *msqV);
+void orc_prb_cfl(const orc_prb_t *s, double *cflu, double *cflv);
+void orc_prb_zmtm(const orc_prb_t *s, const double *msqT, const double *mT, const double *msqU,
+                  const double *msqV, double *out);
+
 /* Initial conditions.  kind 0: the reference's own deterministic profile
  * (PRB:137-186; for ORC_ANNULUS the conduction profile 1 - ln r / ln r0
  * with the sine ripple of velvor2dnewsch3.4.f:131-150).  kind 1: linear conduction plus seeded uniform noise of

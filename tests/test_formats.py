@@ -154,3 +154,15 @@ def test_r3d_nu_history(tmp_path):
     fortio.write_r3d_nu_history(str(p), 1e-5, [1.0, 0.5])
     # (1x,e16.8) twice: one blank, then a 16-wide field with two leading blanks
     assert p.read_text().splitlines() == ["   0.00000000E+00   0.10000000E+01", "   0.10000000E-04   0.50000000E+00"]
+
+
+def test_zmtm_file(tmp_path):
+    """zmtmtempvar.dat (PRB:474-493, format 202 = 3(1x,e16.8)): one line of
+    three e16.8 fields per row, read back to the printed precision."""
+    rows = np.array([[3.62685898e-06, 12.8889259, 6.08776334], [0.0, -1.5e-17, 2.0e120]])
+    p = tmp_path / "zmtmtempvar.dat"
+    fortio.write_zmtm(str(p), rows)
+    lines = open(p).read().splitlines()
+    assert lines[0] == "   0.36268590E-05   0.12888926E+02   0.60877633E+01"
+    assert lines[1] == "   0.00000000E+00  -0.15000000E-16   0.20000000+121"
+    np.testing.assert_allclose(fortio.read_zmtm(str(p))[0], rows[0], rtol=5.1e-8)

@@ -22,6 +22,7 @@ def test_driver_matches_oracle(oracle, gblib, tmp_path):
     g, ht, ht2 = driver.run(small_deck(nts, more), xx=3.0, outdir=str(tmp_path), log=lambda *a: None)
     o = oracle.OraclePRB(16, 48, 1e-5, 1e7, 0.71, r0=0.5, rmax=1.0, xx=3.0)
     o.initial(0, 0, 0.0)
+    o.enable_diagnostics()
     np.testing.assert_array_equal(np.array(o.field("th")), driver.reference_initial(16, 48, 0.5, 1.0, 0.5 / 16))
     want = []
     for _ in range(nts):
@@ -42,6 +43,10 @@ def test_driver_matches_oracle(oracle, gblib, tmp_path):
     np.testing.assert_array_equal(c, np.array(o.field("C"))[:17])
     lines = open(tmp_path / "nu.dat").read().splitlines()
     assert len(lines) == nts + more and len(lines[0].split()) == 14
+    # zmtmtempvar.dat of the last block (PRB:474-493), e16.8 rounding
+    z = fortio.read_zmtm(str(tmp_path / "zmtmtempvar.dat"))
+    assert z.shape == (18, 3)
+    np.testing.assert_allclose(z, o.zmtm(), rtol=5.1e-8, atol=1e-300)
 
 
 def test_r3d_driver_matches_oracle_and_restarts(oracle, gblib, tmp_path):
