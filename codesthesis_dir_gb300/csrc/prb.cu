@@ -108,6 +108,7 @@ __global__ void k_cvort_deriv_x(PrbDev d)
 // Vorticity update, PRB:706-776 (first) / PRB:900-982 (leapfrog).  Annulus
 // (velvor2dnewsch3.4.f:710-786 / :911-993): radius r = r0 + i dr, the Cra/r
 // term, 0.5*Cp in the leapfrog RHS1 and the rotational buoyancy in RHS2.
+// Oblique gravity (mpkoks.f): RHS2 = -Ra thr 0.707106781 with thr = An.
 __global__ void k_cvort_update(PrbDev d, int first)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -152,7 +153,8 @@ __global__ void k_cvort_update(PrbDev d, int first)
             RHS1 = Crra + Chha * (ri * ri) + 0.5 * C[GIX(i, k, ld)] / (Ptl * dt);
             cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
         }
-        RHS2 = -Ra * thh;
+        // mpkoks.f:769-770, :974-975: gravity along the diagonal, REAL*4 0.707106781
+        RHS2 = d.oblique ? -Ra * d.f[GB_F_An][GIX(i, k, ld)] * (double)0.707106781f : -Ra * thh;
     }
     const double ULT = (u * Cr + v * Ch * ri) / Ptl;
     const double cf2 = cnr + cnh;
@@ -597,6 +599,7 @@ int prb_refresh_scalars(gb_prb *h)
     d.Ra = h->p.Ra;
     d.Pr = h->p.Pr;
     d.polar = h->p.variant == GB_PRB_ANNULUS;
+    d.oblique = h->p.variant == GB_PRB_OBLIQUE;
     d.r0 = h->p.r0;
     d.Re = h->p.Re;
     d.dr = h->dr_set != 0.0 ? h->dr_set : (h->p.rmax - h->p.r0) / (double)h->p.nr;
@@ -617,7 +620,7 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     const int nr = p->nr, np = p->np;
     const int nlev = prb_mg_levels(nr, p->variant);
     if (nlev_out) *nlev_out = nlev;
-    if (p->variant != GB_PRB_LAYER && p->variant != GB_PRB_ANNULUS) {
+    if (p->variant != GB_PRB_LAYER && p->variant != GB_PRB_ANNULUS && p->variant != GB_PRB_OBLIQUE) {
         gb_set_error("gb_prb_create: unknown variant %d", p->variant);
         return GB_ERR_INVALID;
     }

@@ -20,7 +20,9 @@
 // (iarchomedir_groke_storage_users_mpking_rotannconvvelvorplane_continueddir/
 // velvor2dnewsch3.4.f, same subroutine names and COMMON blocks) once
 // gb_prb_bind_variant(GB_PRB_ANNULUS) or GB300_PRB_VARIANT=annulus selects
-// it; its solves then default to tolcon 1e-5 and 10000 sweeps.
+// it; its solves then default to tolcon 1e-5 and 10000 sweeps.  mpkoks.f
+// (the layer with oblique gravity, same names) is GB_PRB_OBLIQUE or
+// GB300_PRB_VARIANT=oblique.
 #include <stdlib.h>
 #include <string.h>
 
@@ -75,7 +77,10 @@ DropIn &g()
         if (const char *s = getenv("GB300_PRB_KR")) d.kr = atoi(s);
         if (const char *s = getenv("GB300_PRB_KP")) d.kp = atoi(s);
         if (const char *s = getenv("GB300_PRB_VARIANT"))
+        {
             if (strcmp(s, "annulus") == 0 || strcmp(s, "1") == 0) d.variant = GB_PRB_ANNULUS;
+            if (strcmp(s, "oblique") == 0 || strcmp(s, "2") == 0) d.variant = GB_PRB_OBLIQUE;
+        }
     }
     return d;
 }
@@ -137,6 +142,7 @@ int ensure(int nr, int np, double dr, double dp)
         p.Re = Re;
     } else {
         gb_prb_default_params(&p, nr, np);
+        p.variant = d.variant;   // GB_PRB_LAYER or GB_PRB_OBLIQUE
     }
     p.smoother = d.smoother;
     if (d.tol_bound) {
@@ -277,7 +283,7 @@ void gb_prb_bind_common(double *sol1, double *sol2, double *sol3, void *num, dou
 void gb_prb_bind_variant(int variant)
 {
     std::lock_guard<std::mutex> lk(g().mu);
-    g().variant = variant == GB_PRB_ANNULUS ? GB_PRB_ANNULUS : GB_PRB_LAYER;
+    g().variant = (variant == GB_PRB_ANNULUS || variant == GB_PRB_OBLIQUE) ? variant : GB_PRB_LAYER;
 }
 
 void gb_prb_bind_radius(double *radius)

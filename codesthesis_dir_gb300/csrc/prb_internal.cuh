@@ -46,6 +46,7 @@ struct MgEq {
 struct PrbDev {
     int nr, np, ld;
     int polar;           // GB_PRB_ANNULUS
+    int oblique;         // GB_PRB_OBLIQUE
     double dt, Ra, Pr, dr, dp, dri, dpi;
     double r0, Re;
     double *f[GB_F_COUNT];

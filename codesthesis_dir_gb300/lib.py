@@ -33,6 +33,7 @@ SMOOTHER_LEX = 0
 SMOOTHER_ZEBRA = 1
 PRB_LAYER = 0
 PRB_ANNULUS = 1
+PRB_OBLIQUE = 2   # mpkoks.f: the layer with gravity along the diagonal
 PRB_FP64 = 0
 PRB_MIXED = 1
 BATCH_FP64 = 0

@@ -38,7 +38,7 @@ class PRB:
         else:
             L.gb_prb_default_params(C.byref(p), nr, np_)
         p.dt, p.r0, p.rmax, p.xx, p.Ra, p.Pr = dt, r0, rmax, xx, Ra, Pr
-        p.sor, p.smoother, p.Re, p.precision = sor, smoother, Re, precision
+        p.sor, p.smoother, p.Re, p.precision, p.variant = sor, smoother, Re, precision, variant
         if tolcon is not None:
             p.tolcon = tolcon
         if maxsweeps is not None:

@@ -79,7 +79,7 @@ typedef struct gb_prb_params {
     double sor;      /* over-relaxation factor of the whole-cycle change */
     int maxsweeps;   /* outer multigrid sweep limit */
     int smoother;    /* GB_SMOOTHER_LEX or GB_SMOOTHER_ZEBRA */
-    int variant;     /* GB_PRB_LAYER or GB_PRB_ANNULUS */
+    int variant;     /* GB_PRB_LAYER, GB_PRB_ANNULUS or GB_PRB_OBLIQUE */
     double Re;       /* rotational Reynolds number (COMMON /val/ Re; annulus only) */
     int precision;   /* GB_PRB_FP64 (bit-exact) or GB_PRB_MIXED (FP32 cycles inside FP64 defect correction) */
 } gb_prb_params;
@@ -111,9 +111,15 @@ typedef struct gb_prb_params {
  *                   relaxations per level visit (:2134, :2410), no reset of
  *                   the coarse seam residual in corser (:2696-2704), no STOP
  *                   after the sweep limit (:1853), Nu = -r0 ln(r0/rmax)
- *                   trans1/(2 pi) (:386-387). */
+ *                   trans1/(2 pi) (:386-387).
+ *   GB_PRB_OBLIQUE: the layer with gravity along the diagonal,
+ *                   monashubuntudir_velvor2dperiodicrbconvdir/mpkoks.f: the
+ *                   buoyancy term of both vorticity updates is
+ *                   RHS2 = -Ra thr 0.707106781 (REAL*4 literal; :769-770,
+ *                   :974-975) instead of -Ra thh; all else is the layer's. */
 #define GB_PRB_LAYER   0
 #define GB_PRB_ANNULUS 1
+#define GB_PRB_OBLIQUE 2
 
 /* Fills *p with the reference defaults for an nr x np grid
  * (dt 1e-7, r0 0.5, rmax 1, xx 3, Ra 1e7, Pr 0.71: the PRB input deck). */

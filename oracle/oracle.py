@@ -21,6 +21,7 @@ ORC_LEX = 0
 ORC_ZEBRA = 1
 ORC_PRB = 0
 ORC_ANNULUS = 1
+ORC_OBLIQUE = 2   # mpkoks.f: the layer with gravity along the diagonal
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

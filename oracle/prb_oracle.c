@@ -739,7 +739,11 @@ static void cvort_derivatives(orc_prb_t *s, double *wa, double *wb, double *wc,
  * ORC_ANNULUS (velvor2dnewsch3.4.f:710-786, :911-993): radius r = r0 + i dr
  * of the C points, the (1/r) dC/dr term Cra*ri in RHS1, 0.5*Cp (not C) in
  * the leapfrog RHS1, and the rotational buoyancy term
- * 2 Ra (-thr u - thh v / r) / Re / Ptl in RHS2. */
+ * 2 Ra (-thr u - thh v / r) / Re / Ptl in RHS2.
+ *
+ * ORC_OBLIQUE (mpkoks.f:769-770, :974-975): the layer with the buoyancy of
+ * gravity along the diagonal, RHS2 = -Ra thr 0.707106781 (a REAL*4
+ * literal). */
 static void cvort_update(orc_prb_t *s, int first)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
@@ -783,7 +787,7 @@ static void cvort_update(orc_prb_t *s, int first)
                     RHS1 = Crra + Chha * (ri * ri) + 0.5 * C[IX(i, k)] / (Ptl * dt);
                     cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
                 }
-                RHS2 = -Ra * thh;
+                RHS2 = s->variant == ORC_OBLIQUE ? -Ra * thr * (double)0.707106781f : -Ra * thh;
             }
             const double ULT = (u * Cr + v * Ch * ri) / Ptl;
             const double cf2 = cnr + cnh;

@@ -72,6 +72,7 @@ typedef struct {
 
 #define ORC_PRB     0
 #define ORC_ANNULUS 1
+#define ORC_OBLIQUE 2   /* the layer with gravity at 45 degrees (mpkoks.f:769-770, :974-975) */
 
 int  orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp);
 /* Same with the variant and inner radius of the annulus driver. */
