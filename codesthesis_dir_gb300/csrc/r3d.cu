@@ -76,6 +76,13 @@ struct R3Dev {
     int *hist_sw;
     int *solve_status, *solve_sweeps;   // per component
     GridSync gs[4];             // per component (the w and v solves run concurrently)
+    // rot3dmghor.f (GB_R3D_HORIZONTAL): gravity across the axis, both walls'
+    // heat flux, the inner wall hot, plain V-cycles
+    int horizontal;
+    const double *sinth, *costh;        // libm sin, cos of 6.283185307/np k, k = 0..np
+    double nu2_num;                     // nz/6 rmax ln(r0/rmax); nu_num is nz/6 r0 ln(r0/rmax) there
+    double *trans2;                     // outer-wall per-k sums (np + 1)
+    double *hist_nu2;
 };
 
 #define FX(a, i, j, k) ((a)[(size_t)(i) + (size_t)ni * ((size_t)(j) + (size_t)nj * (size_t)(k))])
@@ -170,7 +177,8 @@ __global__ void k_r3d_avort(R3Dev d)
     const double cnh = -1.0 / (dp * dp) / (r * r);
     const double RHS1 = Arra + Ara / r + Ahha / (r * r) + Azza - 2.0 * Bh / (r * r) + FX(A, i, j, k) / (Ptl * dt);
     const double ULT = (u * Ar + v * Ah / r + w * Az - uelh * BB / r - uelz * CC) / Ptl;
-    const double RHS2 = -2.0 * Re * uelz + 2.0 * Ra * (tem * uelz + thz * u) / Re / Ptl - Gr * Ptl / r * thh;
+    const double RHS2 = d.horizontal ? d.sinth[k] * Gr * Ptl * thz   // rot3dmghor.f:479
+                                     : -2.0 * Re * uelz + 2.0 * Ra * (tem * uelz + thz * u) / Re / Ptl - Gr * Ptl / r * thh;
     const double cf1 = 1.0 / (Ptl * dt) - uelr / (2.0 * Ptl) + 1.0 / (2.0 * (r * r)) - cnr - cnz - cnh;
     const double cf2 = uelr / (2.0 * Ptl) - 1.0 / (2.0 * (r * r)) + cnr + cnz + cnh;
     FX(An, i, j, k) = (cf2 * FX(Ap, i, j, k) - ULT - RHS2 + RHS1) / cf1;
@@ -250,7 +258,9 @@ __global__ void k_r3d_bvort(R3Dev d)
     const double cnh = -1.0 / (dp * dp) / (r * r);
     const double RHS1 = Brra + Bra / r + Bhha / (r * r) + Bzza + 2.0 * Ah / (r * r) + FX(B, i, j, k) / (Ptl * dt);
     const double ULT = (u * Br + v * Bh / r + w * Bz - (velr - v / r) * AA - velz * CC) / Ptl;
-    const double RHS2 = -2.0 * Re * velz + r * Ra * thz + 2.0 * Ra * (tem * velz + thz * v) / Re / Ptl + Gr * Ptl * thr;
+    const double RHS2 = d.horizontal ? d.costh[k] * Gr * Ptl * thz   // rot3dmghor.f:606
+                                     : -2.0 * Re * velz + r * Ra * thz + 2.0 * Ra * (tem * velz + thz * v) / Re / Ptl +
+                                           Gr * Ptl * thr;
     const double cf1 = 1.0 / (Ptl * dt) - (u / r + velh / r) / (2.0 * Ptl) + 1.0 / (2.0 * (r * r)) - cnr - cnz - cnh;
     const double cf2 = (u / r + velh / r) / (2.0 * Ptl) - 1.0 / (2.0 * (r * r)) + cnr + cnz + cnh;
     FX(Bn, i, j, k) = (cf2 * FX(Bp, i, j, k) - ULT - RHS2 + RHS1) / cf1;
@@ -338,7 +348,9 @@ __global__ void k_r3d_cvort(R3Dev d)
     const double cnh = -1.0 / (dp * dp) / (r * r);
     const double RHS1 = Crra + Cra / r + Chha / (r * r) + Czza + FX(C, i, j, k) / (Ptl * dt);
     const double ULT = (u * Cr + v * Ch / r + w * Cz - welr * AA - welh * BB / r) / Ptl;
-    const double RHS2 = -2.0 * Re * welz - Ra * thh + 2.0 * Ra * (tem * welz - thr * u - thh * v / r) / Re / Ptl;
+    const double RHS2 =
+        d.horizontal ? -(1.0 / r * d.Gr * Ptl * d.costh[k] * thh) - d.Gr * Ptl * d.sinth[k] * thr   // rot3dmghor.f:749
+                     : -2.0 * Re * welz - Ra * thh + 2.0 * Ra * (tem * welz - thr * u - thh * v / r) / Re / Ptl;
     const double cf1 = 1.0 / (Ptl * dt) - welz / (2.0 * Ptl) - cnr - cnz - cnh;
     const double cf2 = welz / (2.0 * Ptl) + cnr + cnz + cnh;
     FX(Cn, i, j, k) = (cf2 * FX(Cp, i, j, k) - ULT - RHS2 + RHS1) / cf1;
@@ -450,6 +462,24 @@ __global__ void k_r3d_heat_k(R3Dev d)
     const double dr = d.dr, dz = d.dz;
     const double *th = d.fld[GB_R_th];
 #define HT(j, k) ((-184.0 * FX(th, 0, j, k) + 225.0 * FX(th, 1, j, k) - 50.0 * FX(th, 2, j, k) + 9.0 * FX(th, 3, j, k)))
+    if (d.horizontal) {
+        // rot3dmghor.f:913-945: both cylinders over j = nz/2-3 .. nz/2+3
+        const int nr = d.nr, nza = nz / 2 - 3, nzb = nz / 2 + 3;
+#define HB(j, k) ((184.0 * FX(th, nr + 1, j, k) - 225.0 * FX(th, nr, j, k) + 50.0 * FX(th, nr - 1, j, k) - \
+                   9.0 * FX(th, nr - 2, j, k)))
+        double ta = dz * HT(nza, k) / (120.0 * dr);
+        double tb = dz * HB(nza, k) / (120.0 * dr);
+        ta = ta + dz * HT(nzb, k) / (120.0 * dr);
+        tb = tb + dz * HB(nzb, k) / (120.0 * dr);
+        for (int j = nza + 1; j <= nzb - 1; ++j) {
+            ta = ta + dz * HT(j, k) / (60.0 * dr);
+            tb = tb + dz * HB(j, k) / (60.0 * dr);
+        }
+#undef HB
+        d.trans[k] = ta;
+        d.trans2[k] = tb;
+        return;
+    }
     double trans = dz * HT(0, k) / (240.0 * dr);
     trans = trans + dz * HT(1, k) / (80.0 * dr);
     trans = trans + dz * HT(nz, k) / (80.0 * dr);
@@ -463,10 +493,16 @@ __global__ void k_r3d_heat_sum(R3Dev d, int step)
 {
     if (*(volatile int *)d.abort) return;
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    double trans1 = 0.0;
+    double trans1 = 0.0, trans2 = 0.0;
     for (int k = 1; k <= d.np; ++k) trans1 = trans1 + d.trans[k] * d.dp;
+    if (d.horizontal)
+        for (int k = 1; k <= d.np; ++k) trans2 = trans2 + d.trans2[k] * d.dp;
     d.trans[0] = trans1;
-    if (step >= 0) d.hist_nu[step] = d.nu_num * trans1 / d.nu_den;
+    d.trans2[0] = trans2;
+    if (step >= 0) {
+        d.hist_nu[step] = d.nu_num * trans1 / d.nu_den;
+        d.hist_nu2[step] = d.horizontal ? d.nu2_num * trans2 / d.nu_den : 0.0;
+    }
 }
 
 // rhsw / rhsv / rhsu (rot3dmg.f:1026-1150)
@@ -562,8 +598,9 @@ __global__ void k_r3d_update(R3Dev d, int step)
         if (i == 0) FX(Cn, 0, j, k) = (3.0 * FX(vel, 1, j, k) - FX(vel, 2, j, k) / 3.0) / dr;
         else if (i == nr) FX(Cn, nr, j, k) = (FX(vel, nr - 1, j, k) / 3.0 - 3.0 * FX(vel, nr, j, k)) / dr;
     }
-    if (i == 0) FX(thn, 0, j, k) = 0.0;
-    else if (i == nr + 1) FX(thn, nr + 1, j, k) = 1.0;
+    // wall temperatures: inner 0, outer 1 (the horizontal annulus: inner 1, outer 0)
+    if (i == 0) FX(thn, 0, j, k) = d.horizontal ? 1.0 : 0.0;
+    else if (i == nr + 1) FX(thn, nr + 1, j, k) = d.horizontal ? 0.0 : 1.0;
     const size_t p = (size_t)t;
     d.fld[GB_R_Ap][p] = d.fld[GB_R_A][p];
     d.fld[GB_R_A][p] = An[p];
@@ -1303,7 +1340,7 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
     int status = GB_MAXSWEEPS, sweeps = d.maxsweeps;
     const int nlev = d.nlev;
     for (int sweep = 1; sweep <= d.maxsweeps; ++sweep) {
-        if (sweep != 1) {
+        if (sweep != 1 && !d.horizontal) {
             for (long long t = gt; t < nlvl; t += T) {
                 const int i = (int)(t % n1p);
                 const long long rest = t / n1p;
@@ -1318,14 +1355,16 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve(const __grid_consta
         }
         if (sweep == 1 || nlev == 1) {
             if (!r3_relax<COMP>(d, 1, cx, sm)) return;
-            for (long long t = gt; t < nlvl; t += T) {
-                const int i = (int)(t % n1p);
-                const long long rest = t / n1p;
-                const int j = (int)(rest % n2p);
-                const int k = (int)(rest / n2p);
-                FX(psip, i, j, k) = W.v[t];
+            if (!d.horizontal) {
+                for (long long t = gt; t < nlvl; t += T) {
+                    const int i = (int)(t % n1p);
+                    const long long rest = t / n1p;
+                    const int j = (int)(rest % n2p);
+                    const int k = (int)(rest / n2p);
+                    FX(psip, i, j, k) = W.v[t];
+                }
+                if (!grid_sync(gs)) return;
             }
-            if (!grid_sync(gs)) return;
         }
         if (nlev > 1) {
             for (int l = 1; l <= nlev - 1; ++l) {
@@ -1811,7 +1850,7 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
             if (!grid_sync(gs)) return;
             if (!r3_relax32<COMP>(d, l - 1, false, sm)) return;
         }
-        const double w = it == 0 ? 1.0 : d.sor;
+        const double w = (it == 0 || d.horizontal) ? 1.0 : d.sor;
         for (long long t = gt; t < nlvl; t += T) W.v[t] += w * (double)W.v32[t];
         if (!grid_sync(gs)) return;
     }
@@ -1846,7 +1885,7 @@ __global__ void __launch_bounds__(R3_THREADS, 2) k_r3d_solve_mixed(const __grid_
 struct gb_r3d {
     gb_r3d_params p;
     R3Dev dev;
-    double *fields = nullptr, *pool = nullptr, *work = nullptr;
+    double *fields = nullptr, *pool = nullptr, *work = nullptr, *tables = nullptr;
     int *itab = nullptr;
     void *small = nullptr;
     double *hist_nu = nullptr;
@@ -1905,6 +1944,7 @@ extern "C" int gb_r3d_destroy(gb_r3d *h)
     cudaFree(h->fields);
     cudaFree(h->pool);
     cudaFree(h->work);
+    cudaFree(h->tables);
     cudaFree(h->itab);
     cudaFree(h->small);
     cudaFree(h->hist_nu);
@@ -1987,9 +2027,10 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     if (nlev_out) *nlev_out = nlev;
     if (nr < 4 || nz < 4 || np < 4 || nr > 4096 || nz > 4096 || np > 16384 || np % (1 << nlev) != 0 ||
         np / (1 << (nlev - 1)) < 4 || !(p->r0 > 0.0 && p->rmax > p->r0) || !(p->zmax > 0.0) || !(p->dt > 0.0) ||
-        p->Pr == 0.0 || p->Re == 0.0 || p->nrel < 1 || p->maxsweeps < 1) {
+        p->Pr == 0.0 || (p->Re == 0.0 && p->variant != GB_R3D_HORIZONTAL) || p->nrel < 1 || p->maxsweeps < 1) {
         gb_set_error("gb_r3d_create: unsupported parameters (nr=%d nz=%d np=%d: nr, nz >= 4, np a multiple of 2^%d "
-                     "with >= 4 phi intervals on the coarsest level; 0 < r0 < rmax, zmax, dt > 0, Pr, Re != 0)",
+                     "with >= 4 phi intervals on the coarsest level; 0 < r0 < rmax, zmax, dt > 0, Pr != 0, Re != 0 "
+                     "unless horizontal)",
                      nr, nz, np, nlev);
         return GB_ERR_INVALID;
     }
@@ -1999,6 +2040,14 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     }
     if (p->precision != GB_PRB_FP64 && p->precision != GB_PRB_MIXED) {
         gb_set_error("gb_r3d_create: unknown precision %d", p->precision);
+        return GB_ERR_INVALID;
+    }
+    if (p->variant != GB_R3D_VERTICAL && p->variant != GB_R3D_HORIZONTAL) {
+        gb_set_error("gb_r3d_create: unknown variant %d", p->variant);
+        return GB_ERR_INVALID;
+    }
+    if (p->variant == GB_R3D_HORIZONTAL && nz < 6) {
+        gb_set_error("gb_r3d_create: the horizontal annulus's heat band j = nz/2-3..nz/2+3 needs nz >= 6 (nz=%d)", nz);
         return GB_ERR_INVALID;
     }
     gb_r3d *h = new gb_r3d();
@@ -2026,6 +2075,12 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     d.dp = spacing ? spacing[2] : 2.0 * pi / (double)np;
     d.nu_num = -p->r0 * log(p->r0 / p->rmax);
     d.nu_den = p->zmax * 2.0 * pi;
+    d.horizontal = p->variant == GB_R3D_HORIZONTAL;
+    if (d.horizontal) {
+        // httrans1, httrans2 of rot3dmghor.f:264-267, host libm as the Fortran runtime
+        d.nu_num = (double)nz / 6.0 * p->r0 * log(p->r0 / p->rmax);
+        d.nu2_num = (double)nz / 6.0 * p->rmax * log(p->r0 / p->rmax);
+    }
     d.tolcon = p->tolcon;
     d.sor = p->sor;
     d.nrel = p->nrel;
@@ -2166,10 +2221,25 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
         L.poff[tr.comp][tr.dir] = h->itab + tr.off;
         L.nphase[tr.comp][tr.dir] = tr.nphase;
     }
+    // sin and cos of theta = 6.283185307/np k (rot3dmghor.f:373-378), host libm
+    {
+        std::vector<double> tab(2 * (size_t)(np + 1), 0.0);
+        if (d.horizontal)
+            for (int k = 0; k <= np; ++k) {
+                const double theta = 6.283185307 / (double)np * (double)k;
+                tab[k] = sin(theta);
+                tab[np + 1 + k] = cos(theta);
+            }
+        e = cudaMalloc(&h->tables, sizeof(double) * tab.size());
+        if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: tables"); return GB_ERR_ALLOC; }
+        cudaMemcpy(h->tables, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice);
+        d.sinth = h->tables;
+        d.costh = h->tables + np + 1;
+    }
     // small state
-    e = cudaMalloc(&h->small, 4096 + sizeof(double) * (size_t)(np + 2));
+    e = cudaMalloc(&h->small, 4096 + 2 * sizeof(double) * (size_t)(np + 2));
     if (e != cudaSuccess) { gb_r3d_destroy(h); gb_set_error("gb_r3d_create: state"); return GB_ERR_ALLOC; }
-    cudaMemset(h->small, 0, 4096 + sizeof(double) * (size_t)(np + 2));
+    cudaMemset(h->small, 0, 4096 + 2 * sizeof(double) * (size_t)(np + 2));
     char *sm = (char *)h->small;
     d.resmax = (unsigned long long *)(sm + 0);    // 8 slots
     d.nanflag = (int *)(sm + 64);                 // 8 slots
@@ -2179,6 +2249,7 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
     d.solve_sweeps = (int *)(sm + 320);           // 4 slots
     h->sync = (unsigned *)(sm + 512);             // 4 barriers, 128 bytes apart
     d.trans = (double *)(sm + 4096);
+    d.trans2 = d.trans + (np + 2);
     for (int c = 0; c < 4; ++c) {
         d.gs[c].count = h->sync + R3_SYNC_STRIDE * c;
         d.gs[c].gen = h->sync + R3_SYNC_STRIDE * c + 1;
@@ -2362,6 +2433,29 @@ extern "C" int gb_r3d_heat(gb_r3d *h, double *trans1)
     return GB_OK;
 }
 
+extern "C" int gb_r3d_heat2(gb_r3d *h, double *trans1, double *trans2)
+{
+    if (!h) return GB_ERR_INVALID;
+    r3_clear_abort(h);
+    r3_launch_transport(h, 4, -1, h->stream);
+    int st = r3_sync(h, "gb_r3d_heat2");
+    if (st != GB_OK) return st;
+    if (trans1) GB_CUDA_TRY(cudaMemcpy(trans1, h->dev.trans, sizeof(double), cudaMemcpyDeviceToHost));
+    if (trans2) GB_CUDA_TRY(cudaMemcpy(trans2, h->dev.trans2, sizeof(double), cudaMemcpyDeviceToHost));
+    return GB_OK;
+}
+
+extern "C" int gb_r3d_nu2(gb_r3d *h, int nsteps, double *nu2)
+{
+    if (!h || nsteps < 0 || nsteps > h->hist_cap || (nsteps > 0 && !nu2)) {
+        gb_set_error("gb_r3d_nu2: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    if (nsteps > 0)
+        GB_CUDA_TRY(cudaMemcpy(nu2, h->hist_nu + h->hist_cap, sizeof(double) * (size_t)nsteps, cudaMemcpyDeviceToHost));
+    return GB_OK;
+}
+
 extern "C" int gb_r3d_poisson(gb_r3d *h, int which, int *sweeps)
 {
     if (!h || which < 1 || which > 3) { gb_set_error("gb_r3d_poisson: invalid argument"); return GB_ERR_INVALID; }
@@ -2388,14 +2482,16 @@ extern "C" int gb_r3d_step(gb_r3d *h, int nsteps, double *nu, int *sweeps, int *
         h->hist_nu = nullptr;
         h->hist_sw = nullptr;
         h->hist_cap = 0;
-        GB_CUDA_TRY(cudaMalloc(&h->hist_nu, sizeof(double) * (size_t)nsteps));
+        GB_CUDA_TRY(cudaMalloc(&h->hist_nu, 2 * sizeof(double) * (size_t)nsteps));
         GB_CUDA_TRY(cudaMalloc(&h->hist_sw, sizeof(int) * 3 * (size_t)nsteps));
         h->hist_cap = nsteps;
     }
     h->dev.hist_nu = h->hist_nu;
+    h->dev.hist_nu2 = h->hist_nu + h->hist_cap;
     h->dev.hist_sw = h->hist_sw;
     cudaStream_t s = h->stream;
     GB_CUDA_TRY(cudaMemsetAsync(h->hist_sw, 0, sizeof(int) * 3 * (size_t)nsteps, s));
+    GB_CUDA_TRY(cudaMemsetAsync(h->hist_nu, 0, 2 * sizeof(double) * (size_t)h->hist_cap, s));
     GB_CUDA_TRY(cudaMemsetAsync(h->dev.steps_done, 0, sizeof(int), s));
     GB_CUDA_TRY(cudaMemsetAsync(h->dev.abort, 0, sizeof(int), s));
     for (int step = 0; step < nsteps; ++step) {

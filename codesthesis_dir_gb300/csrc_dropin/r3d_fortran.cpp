@@ -47,6 +47,7 @@ struct DropIn {
     double cur_dr = 0, cur_dz = 0, cur_dp = 0;
     int kr = 33, kz = 33, kp = 160;
     int smoother = GB_SMOOTHER_LEX, precision = GB_PRB_FP64;
+    int variant = GB_R3D_VERTICAL;
     bool tol_bound = false;
     double tolcon = 1e-5;
     int maxsweeps = 500;
@@ -65,6 +66,8 @@ DropIn &g()
         if (const char *s = getenv("GB300_R3D_KR")) d.kr = atoi(s);
         if (const char *s = getenv("GB300_R3D_KZ")) d.kz = atoi(s);
         if (const char *s = getenv("GB300_R3D_KP")) d.kp = atoi(s);
+        if (const char *s = getenv("GB300_R3D_VARIANT"))
+            if (strcmp(s, "horizontal") == 0 || strcmp(s, "1") == 0) d.variant = GB_R3D_HORIZONTAL;
     }
     return d;
 }
@@ -119,6 +122,8 @@ int ensure(int nr, int nz, int np, double dr, double dz, double dp)
     p.Pr = valp()->Ptl;
     p.smoother = d.smoother;
     p.precision = d.precision;
+    p.variant = d.variant;
+    if (d.variant == GB_R3D_HORIZONTAL) p.tolcon = 1e-6;   // rot3dmghor.f:1599, :1798, :2051
     if (d.tol_bound) {
         p.tolcon = d.tolcon;
         p.maxsweeps = d.maxsweeps;
@@ -265,6 +270,12 @@ void gb_r3d_bind_smoother(int smoother)
     g().smoother = smoother;
 }
 
+void gb_r3d_bind_variant(int variant)
+{
+    std::lock_guard<std::mutex> lk(g().mu);
+    g().variant = variant == GB_R3D_HORIZONTAL ? GB_R3D_HORIZONTAL : GB_R3D_VERTICAL;
+}
+
 void gb_r3d_bind_precision(int precision)
 {
     std::lock_guard<std::mutex> lk(g().mu);
@@ -330,12 +341,15 @@ void temperature_(void)
     transport(gb_r3d_temperature, GB_R_thn, {GB_R_th, GB_R_thp, GB_R_uel, GB_R_vel, GB_R_wel});
 }
 
-void heat_(double *trans1)
+// rot3dmg.f calls heat(trans1); rot3dmghor.f calls heat(trans1, trans2),
+// and only the horizontal variant reads the second argument.
+void heat_(double *trans1, double *trans2)
 {
     std::lock_guard<std::mutex> lk(g().mu);
     int st = ensure_from_common();
     if (st == GB_OK) st = up({GB_R_th});
-    if (st == GB_OK) st = gb_r3d_heat(g().ctx, trans1);
+    if (st == GB_OK)
+        st = g().variant == GB_R3D_HORIZONTAL ? gb_r3d_heat2(g().ctx, trans1, trans2) : gb_r3d_heat(g().ctx, trans1);
     fail(st);
 }
 

@@ -5,6 +5,11 @@ time loop through the device-resident context, and writes the reference's
 output files (fields with their header records, the Nusselt history).
 
 Usage:  python -m codesthesis_dir_gb300.driver_r3d < input  [--smoother lex|zebra] [--precision fp64|mixed]
+                                                           [--horizontal]
+
+--horizontal runs rot3dmghor.f (the same deck): the annulus with its axis
+horizontal, its own start (inner cylinder hot, the point (nr/2, nz/2,
+np/2) halved) and the three-column Nusselt history of both cylinders.
 
 Every block of the reference's loop runs kt = 1..nts and appends httrans for
 each step (rot3dmg.f:237-268); the files are written once, after the last
@@ -26,10 +31,10 @@ from .deck import parse_r3d_deck
 from .r3d import R3D
 
 
-def run(deck_text, smoother=_L.SMOOTHER_LEX, precision=_L.PRB_FP64, outdir=".", log=print):
+def run(deck_text, smoother=_L.SMOOTHER_LEX, precision=_L.PRB_FP64, outdir=".", log=print, horizontal=False):
     d = parse_r3d_deck(deck_text)
     nr, nz, np_, r0, rmax, zmax = d.nr, d.nz, d.np, d.r0, d.rmax, d.zmax
-    fields = initial.r3d_initial_fields(nr, nz, np_, r0, rmax, d.nval, d.amp)
+    fields = initial.r3d_initial_fields(nr, nz, np_, r0, rmax, d.nval, d.amp, horizontal=horizontal)
     zmin = 0.0
     if d.restart:
         for name, fn in zip(fortio.R3D_ORDER, d.restart):
@@ -43,18 +48,21 @@ def run(deck_text, smoother=_L.SMOOTHER_LEX, precision=_L.PRB_FP64, outdir=".", 
                      ("welp", "wel")):
             fields[a] = fields[b].copy()
     g = R3D(nr, nz, np_, dt=d.dt, r0=r0, rmax=rmax, zmax=zmax, Ra=d.Ra, Re=d.Re, Pr=d.Pr, Gr=d.Gr,
-            smoother=smoother, precision=precision)
+            smoother=smoother, precision=precision,
+            variant=_L.R3D_HORIZONTAL if horizontal else _L.R3D_VERTICAL)
     for n, a in fields.items():
         g.set(n, a)
-    httrans = []
+    httrans, httrans2 = [], []
     for b, nts in enumerate([d.nts] + list(d.more)):
         nu, sw = g.step(nts)
         httrans += list(nu)
+        httrans2 += list(g.nu2)
         log("block %d: %d steps, Nu = %.8f, sweeps (w v u) %s" % (b + 1, len(httrans), httrans[-1], list(sw[-1])))
     for name, fn in zip(fortio.R3D_ORDER, d.fnames[:7]):
         fortio.write_r3d_field(os.path.join(outdir, fn), g.get(name), name, nr, nz, np_, rmax, r0, zmax, zmin)
     if d.fnames[7] != "no":
-        fortio.write_r3d_nu_history(os.path.join(outdir, d.fnames[7]), d.dt, httrans)
+        fortio.write_r3d_nu_history(os.path.join(outdir, d.fnames[7]), d.dt, httrans,
+                                    httrans2 if horizontal else None)
     return g, np.array(httrans)
 
 
@@ -63,9 +71,11 @@ def main(argv=None):
     ap.add_argument("--smoother", default="lex", choices=["lex", "zebra"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--outdir", default=".")
+    ap.add_argument("--horizontal", action="store_true", help="rot3dmghor.f: the annulus with its axis horizontal")
     a = ap.parse_args(argv)
     run(sys.stdin.read(), smoother=_L.SMOOTHER_LEX if a.smoother == "lex" else _L.SMOOTHER_ZEBRA,
-        precision=_L.PRB_FP64 if a.precision == "fp64" else _L.PRB_MIXED, outdir=a.outdir)
+        precision=_L.PRB_FP64 if a.precision == "fp64" else _L.PRB_MIXED, outdir=a.outdir,
+        horizontal=a.horizontal)
 
 
 if __name__ == "__main__":

@@ -160,8 +160,11 @@ def read_r3d_field(path, name):
     return (nr, nz, np_), geom, out
 
 
-def write_r3d_nu_history(path, dt, httrans):
-    """rot3dmg.f:321-326: (i-1)*dt, httrans(i) per line, format 2(1x,e16.8)."""
+def write_r3d_nu_history(path, dt, httrans, httrans2=None):
+    """rot3dmg.f:321-326: (i-1)*dt, httrans(i) per line, format 2(1x,e16.8);
+    with httrans2, rot3dmghor.f:334-343: (i-1)*dt, httrans1(i), httrans2(i),
+    format 3(1x,e16.8)."""
     with open(path, "w") as fh:
         for i, h in enumerate(httrans):
-            fh.write(" " + fortran_e(i * dt) + " " + fortran_e(float(h)) + "\n")
+            vals = [i * dt, float(h)] + ([float(httrans2[i])] if httrans2 is not None else [])
+            fh.write("".join(" " + fortran_e(v) for v in vals) + "\n")

@@ -104,30 +104,35 @@ def initial_fields(nr, np_, r0, rmax, variant=_L.PRB_LAYER, kind=1, seed=0, amp=
     return f
 
 
-def r3d_reference(nr, nz, np_, r0, rmax, nval=3, amp=1e-3):
-    """T of rot3dmg.f:103-131 as a Fortran-ordered (nr+2, nz+2, np+1) array."""
+def r3d_reference(nr, nz, np_, r0, rmax, nval=3, amp=1e-3, horizontal=False):
+    """T of rot3dmg.f:103-131 as a Fortran-ordered (nr+2, nz+2, np+1) array;
+    horizontal: rot3dmghor.f:107-141 (T = ln r / ln r0 + ..., the inner
+    cylinder hot, the point (nr/2, nz/2, np/2) halved)."""
     dr = (rmax - r0) / float(nr)
     r = _radii(nr, r0, rmax, dr)
     lr0 = math.log(r0)
     at1 = math.atan(1.0)
-    trad = np.array([1.0 - math.log(float(x)) / lr0 for x in r])
+    if horizontal:
+        trad = np.array([math.log(float(x)) / lr0 for x in r])
+    else:
+        trad = np.array([1.0 - math.log(float(x)) / lr0 for x in r])
     ramp = np.array([amp * (rmax - float(x)) * (float(x) - r0) for x in r])
     cosk = np.array([math.cos(float(nval) * (8.0 * at1 * float(k) / float(np_))) for k in range(np_ + 1)])
     th = np.asfortranarray(np.broadcast_to((trad[:, None] + ramp[:, None] * cosk[None, :])[:, None, :],
                                            (nr + 2, nz + 2, np_ + 1)).copy())
-    i, j, k = nr // 4, nz // 4, np_ // 2
+    i, j, k = (nr // 2, nz // 2, np_ // 2) if horizontal else (nr // 4, nz // 4, np_ // 2)
     th[i, j, k] = th[i, j, k] - 0.5 * th[i, j, k]
     return np.asfortranarray(th)
 
 
-def r3d_initial_fields(nr, nz, np_, r0, rmax, nval=3, amp=1e-3, noise=0.0, seed=0):
+def r3d_initial_fields(nr, nz, np_, r0, rmax, nval=3, amp=1e-3, noise=0.0, seed=0, horizontal=False):
     """Every field of a fresh 3D-annulus instance: velocities and vorticities
     zero (the fluid in solid-body rotation with the frame), T from
     r3d_reference plus optional seeded noise, previous levels equal to the
     current ones."""
     zero = np.zeros((nr + 2, nz + 2, np_ + 1), order="F")
     f = {n: zero.copy() for n in _L.R3D_FIELDS}
-    th = r3d_reference(nr, nz, np_, r0, rmax, nval, amp)
+    th = r3d_reference(nr, nz, np_, r0, rmax, nval, amp, horizontal)
     if noise > 0.0:
         n = nr * nz * np_
         u = (_splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)

@@ -69,7 +69,11 @@ class R3dParams(C.Structure):
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("zmax", C.c_double),
                 ("Ra", C.c_double), ("Re", C.c_double), ("Gr", C.c_double), ("Pr", C.c_double),
                 ("tolcon", C.c_double), ("sor", C.c_double), ("maxsweeps", C.c_int), ("nrel", C.c_int),
-                ("smoother", C.c_int), ("precision", C.c_int)]
+                ("smoother", C.c_int), ("precision", C.c_int), ("variant", C.c_int)]
+
+
+R3D_VERTICAL = 0
+R3D_HORIZONTAL = 1   # rot3dmghor.f
 
 
 class StrLevel(C.Structure):
@@ -147,6 +151,8 @@ SIGNATURES = [
     ("gb_r3d_cvorticity", C.c_int, [_vp]),
     ("gb_r3d_temperature", C.c_int, [_vp]),
     ("gb_r3d_heat", C.c_int, [_vp, _dp]),
+    ("gb_r3d_heat2", C.c_int, [_vp, _dp, _dp]),
+    ("gb_r3d_nu2", C.c_int, [_vp, C.c_int, _vp]),
     ("gb_r3d_rhsw", C.c_int, [_vp]),
     ("gb_r3d_rhsv", C.c_int, [_vp]),
     ("gb_r3d_rhsu", C.c_int, [_vp]),
@@ -208,7 +214,7 @@ R3D_DROPIN_SIGNATURES = [
     ("bvorticity_", None, []),
     ("cvorticity_", None, []),
     ("temperature_", None, []),
-    ("heat_", None, [_dp]),
+    ("heat_", None, [_dp, _dp]),
     ("update_", None, []),
     ("rhsw_", None, [_vp]),
     ("rhsv_", None, [_vp]),
@@ -217,6 +223,7 @@ R3D_DROPIN_SIGNATURES = [
     ("gb_r3d_bind_common", None, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("gb_r3d_bind_smoother", None, [C.c_int]),
     ("gb_r3d_bind_precision", None, [C.c_int]),
+    ("gb_r3d_bind_variant", None, [C.c_int]),
     ("gb_r3d_bind_tolerance", None, [C.c_double, C.c_int]),
     ("gb_r3d_last_status", C.c_int, []),
     ("gb_r3d_last_sweeps", C.c_int, []),

@@ -7,6 +7,11 @@ rhsw / rhsv / rhsu (:1026-1150), poisson1/2/3 (:1216-1540), update (:964);
 `step` runs the main loop (:241-255).  Fields move as Fortran-ordered
 (ld1, ld2, np+1) float64 arrays with ld1 >= nr+2 and ld2 >= nz+2.
 
+variant=R3D_HORIZONTAL gives rot3dmghor.f, the annulus with its axis
+horizontal (gravity Gr Ptl across the axis, both cylinders' heat flux,
+the inner cylinder hot, plain V-cycles, tolcon 1e-6 by default); `heat2`
+and the `nu2` of `step` are its outer-cylinder quantities.
+
 Error behaviour: the reference STOPs when a solve passes 500 sweeps;
 `poisson1/2/3` and `step` raise GBError with GB_MAXSWEEPS there (and on a
 NaN residual), `step` after recording the steps completed.
@@ -23,12 +28,15 @@ from . import lib as _L
 class R3D:
     def __init__(self, nr, nz, np_, dt=1e-5, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e6, Re=500.0, Pr=7.0, Gr=0.0,
                  tolcon=None, maxsweeps=None, nrel=None, sor=None, smoother=_L.SMOOTHER_LEX,
-                 precision=_L.PRB_FP64):
+                 precision=_L.PRB_FP64, variant=_L.R3D_VERTICAL):
         L = _L.load()
         p = _L.R3dParams()
         L.gb_r3d_default_params(C.byref(p), nr, nz, np_)
         p.dt, p.r0, p.rmax, p.zmax, p.Ra, p.Re, p.Pr, p.Gr = dt, r0, rmax, zmax, Ra, Re, Pr, Gr
-        p.smoother, p.precision = smoother, precision
+        p.smoother, p.precision, p.variant = smoother, precision, variant
+        if variant == _L.R3D_HORIZONTAL:
+            p.tolcon = 1e-6   # rot3dmghor.f:1599, :1798, :2051
+        self.variant = variant
         for name, val in (("tolcon", tolcon), ("maxsweeps", maxsweeps), ("nrel", nrel), ("sor", sor)):
             if val is not None:
                 setattr(p, name, val)
@@ -86,6 +94,12 @@ class R3D:
         _L.check(_L.load().gb_r3d_heat(self._h, C.byref(t)), "heat")
         return t.value
 
+    def heat2(self):
+        """heat(trans1, trans2) of rot3dmghor.f:913-945."""
+        t1, t2 = C.c_double(), C.c_double()
+        _L.check(_L.load().gb_r3d_heat2(self._h, C.byref(t1), C.byref(t2)), "heat2")
+        return t1.value, t2.value
+
     def poisson(self, which):
         """poisson1 (which=1, w), poisson2 (2, v), poisson3 (3, u); returns the sweep count."""
         sw = C.c_int()
@@ -109,6 +123,9 @@ class R3D:
         st = _L.load().gb_r3d_step(self._h, nsteps, nu.ctypes.data, sw.ctypes.data, C.byref(done))
         self.steps_done = done.value
         self.last_sweeps = sw[:min(nsteps, done.value + 1)]
+        nu2 = np.zeros(nsteps)
+        _L.load().gb_r3d_nu2(self._h, nsteps, nu2.ctypes.data)
+        self.nu2 = nu2[:done.value]
         _L.check(st, "step")
         return nu[:done.value], sw[:done.value]
 

@@ -347,7 +347,25 @@ typedef struct gb_r3d_params {
                                  independent lines; GB_SMOOTHER_ZEBRA: two colours of lines, the
                                  lines on one-sided boundary rows last within a colour */
     int precision;            /* GB_PRB_FP64 or GB_PRB_MIXED (FP32 V-cycles in FP64 defect correction) */
+    int variant;              /* GB_R3D_VERTICAL (rot3dmg.f) or GB_R3D_HORIZONTAL (rot3dmghor.f) */
 } gb_r3d_params;
+
+/* Which 3D annulus.
+ *   GB_R3D_VERTICAL:   rot3dmg.f, the rotating annulus with a vertical axis.
+ *   GB_R3D_HORIZONTAL: rot3dmghor.f, the annulus with its axis horizontal:
+ *     the only body force in the vorticity updates is gravity across the
+ *     axis, RHS2 = sin(theta) Gr Ptl thz (A, :477-479), cos(theta) Gr Ptl thz
+ *     (B, :604-606), -(1/r) Gr Ptl cos(theta) thh - Gr Ptl sin(theta) thr
+ *     (C, :747-749), theta = 6.283185307/np k with libm's sin and cos; the
+ *     inner cylinder is hot (T = 1 at i = 0, 0 at i = nr+1, :1042-1043);
+ *     heat gives both cylinders' fluxes over the band j = nz/2-3 .. nz/2+3
+ *     (:913-945; nz >= 6); the V-cycles run without the whole-cycle
+ *     over-relaxation and without the psip copies (:1287-1315; sor is
+ *     ignored); the reference's tolerance is 1e-6 (:1599, :1798, :2051; set
+ *     tolcon); Nusselt numbers nz/6 r0 ln(r0/rmax) trans1 / (zmax 2 pi) and
+ *     nz/6 rmax ln(r0/rmax) trans2 / (zmax 2 pi) (:264-267). */
+#define GB_R3D_VERTICAL   0
+#define GB_R3D_HORIZONTAL 1
 
 typedef struct gb_r3d gb_r3d;
 
@@ -370,6 +388,9 @@ int gb_r3d_bvorticity(gb_r3d *h);     /* rot3dmg.f:477-593 */
 int gb_r3d_cvorticity(gb_r3d *h);     /* rot3dmg.f:601-728 */
 int gb_r3d_temperature(gb_r3d *h);    /* rot3dmg.f:736-873 */
 int gb_r3d_heat(gb_r3d *h, double *trans1);   /* rot3dmg.f:882-909 */
+/* heat(trans1, trans2) of rot3dmghor.f:913-945 (GB_R3D_HORIZONTAL; the
+ * vertical annulus gives trans2 = 0). */
+int gb_r3d_heat2(gb_r3d *h, double *trans1, double *trans2);
 int gb_r3d_rhsw(gb_r3d *h);           /* rot3dmg.f:1026-1060 */
 int gb_r3d_rhsv(gb_r3d *h);           /* rot3dmg.f:1063-1104 */
 int gb_r3d_rhsu(gb_r3d *h);           /* rot3dmg.f:1107-1150 */
@@ -384,6 +405,10 @@ int gb_r3d_update(gb_r3d *h);         /* rot3dmg.f:964-1023 */
  * failing solve ends the run (the reference STOPs); *steps_done (may be
  * NULL) receives the steps completed and the return value the status. */
 int gb_r3d_step(gb_r3d *h, int nsteps, double *nu, int *sweeps, int *steps_done);
+/* httrans2 of each step of the last gb_r3d_step run (GB_R3D_HORIZONTAL's
+ * outer-cylinder Nusselt number, rot3dmghor.f:266-267; zero for the
+ * vertical annulus); nu is the step run's httrans1 there. */
+int gb_r3d_nu2(gb_r3d *h, int nsteps, double *nu2);
 void *gb_r3d_stream(gb_r3d *h);
 
 /* ------------------------- stretched-grid streamfunction solve (rcsc.f) */

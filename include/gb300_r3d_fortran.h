@@ -42,7 +42,9 @@ void avorticity_(void);               /* rot3dmg.f:341-469 */
 void bvorticity_(void);               /* rot3dmg.f:477-593 */
 void cvorticity_(void);               /* rot3dmg.f:601-728 */
 void temperature_(void);              /* rot3dmg.f:736-873 */
-void heat_(double *trans1);           /* rot3dmg.f:882-909 */
+/* rot3dmg.f:882-909 heat(trans1); with the horizontal variant bound,
+ * rot3dmghor.f:913-945 heat(trans1, trans2) (only then is trans2 read). */
+void heat_(double *trans1, double *trans2);
 void update_(void);                   /* rot3dmg.f:964-1023 */
 void rhsw_(double *wrh);              /* rot3dmg.f:1026-1060 */
 void rhsv_(double *vrh);              /* rot3dmg.f:1063-1104 */
@@ -57,6 +59,10 @@ void gb_r3d_bind_common(double *sol1, double *sol2, double *sol3, void *num, dou
 void gb_r3d_bind_smoother(int smoother);
 /* GB_PRB_FP64 (default) or GB_PRB_MIXED. */
 void gb_r3d_bind_precision(int precision);
+/* GB_R3D_VERTICAL (default, rot3dmg.f) or GB_R3D_HORIZONTAL (rot3dmghor.f,
+ * same subroutine names; also GB300_R3D_VARIANT=horizontal): its tolerance
+ * defaults to 1e-6. */
+void gb_r3d_bind_variant(int variant);
 /* tolcon (1e-5) and the sweep limit (500) of the solves. */
 void gb_r3d_bind_tolerance(double tolcon, int maxsweeps);
 /* Status of the last call (GB_OK, GB_MAXSWEEPS, GB_NAN, GB_TIMEOUT, GB_ERR_*)

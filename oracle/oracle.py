@@ -91,7 +91,8 @@ class R3D(C.Structure):
                 [(n, C.c_double * R3D_MAXLEV) for n in ("hr", "hz", "hp", "hhr", "hhz", "hhp")] +
                 [(n, _dp * R3D_MAXLEV) for n in ("v", "f", "res")] +
                 [("tolcon", C.c_double), ("sor", C.c_double), ("nrel", C.c_int), ("maxsweeps", C.c_int),
-                 ("mode", C.c_int), ("last_resmax", C.c_double), ("last_sweeps", C.c_int)])
+                 ("mode", C.c_int), ("last_resmax", C.c_double), ("last_sweeps", C.c_int),
+                 ("horizontal", C.c_int), ("sinth", _dp), ("costh", _dp), ("nu2", C.c_double)])
 
 
 STR_MAXLEV = 8
@@ -179,6 +180,10 @@ def lib():
             getattr(L, "orc_r3d_" + nm).argtypes = [C.POINTER(R3D)]
         L.orc_r3d_heat.argtypes = [C.POINTER(R3D)]
         L.orc_r3d_heat.restype = C.c_double
+        L.orc_r3d_heat2.argtypes = [C.POINTER(R3D), _dp]
+        L.orc_r3d_heat2.restype = C.c_double
+        L.orc_r3d_set_horizontal.argtypes = [C.POINTER(R3D)]
+        L.orc_r3d_set_horizontal.restype = C.c_int
         L.orc_r3d_poisson.argtypes = [C.POINTER(R3D), C.c_int, _ip]
         L.orc_r3d_poisson.restype = C.c_int
         L.orc_r3d_relax.argtypes = [C.POINTER(R3D), C.c_int, C.c_int, C.c_int, _ip]
@@ -387,12 +392,17 @@ class OracleR3D:
     Fields are (nr+2, nz+2, np+1) Fortran-ordered views (i fastest)."""
 
     def __init__(self, nr, nz, np_, dt, r0, rmax, zmax, Ra, Re, Pr, Gr=0.0, mode=ORC_LEX, tolcon=None,
-                 maxsweeps=None):
+                 maxsweeps=None, horizontal=False):
+        """horizontal: rot3dmghor.f, the annulus with its axis horizontal
+        (gravity Gr Ptl across the axis, both walls' heat flux, the inner
+        wall hot, plain V-cycle, tolcon 1e-6)."""
         L = lib()
         self.s = R3D()
         if L.orc_r3d_init(C.byref(self.s), nr, nz, np_, dt, r0, rmax, zmax, Ra, Re, Gr, Pr) != 0:
             L.orc_r3d_free(C.byref(self.s))
             raise ValueError("invalid R3D size nr=%d nz=%d np=%d" % (nr, nz, np_))
+        if horizontal:
+            assert L.orc_r3d_set_horizontal(C.byref(self.s)) == 0
         self.s.mode = mode
         if tolcon is not None:
             self.s.tolcon = tolcon
@@ -427,10 +437,16 @@ class OracleR3D:
         return st, sw.value
 
     def step(self):
+        """(status, nu, sweeps[3]); the horizontal annulus's outer-wall
+        Nusselt number httrans2 is in self.nu2."""
         nu = C.c_double()
         sw = np.zeros(3, dtype=np.int32)
         st = lib().orc_r3d_step(C.byref(self.s), C.byref(nu), iptr(sw))
         return st, nu.value, sw
+
+    @property
+    def nu2(self):
+        return self.s.nu2
 
     def close(self):
         if self.s.th:

@@ -118,7 +118,26 @@ void orc_r3d_free(orc_r3d_t *s)
         free(s->f[l]);
         free(s->res[l]);
     }
+    free(s->sinth);
+    free(s->costh);
     memset(s, 0, sizeof(*s));
+}
+
+int orc_r3d_set_horizontal(orc_r3d_t *s)
+{
+    s->horizontal = 1;
+    s->tolcon = 1e-6;
+    free(s->sinth);
+    free(s->costh);
+    s->sinth = (double *)calloc((size_t)s->np + 1, sizeof(double));
+    s->costh = (double *)calloc((size_t)s->np + 1, sizeof(double));
+    if (!s->sinth || !s->costh) return R3D_INVALID;
+    for (int k = 0; k <= s->np; ++k) {
+        const double theta = 6.283185307 / (double)s->np * (double)k;
+        s->sinth[k] = sin(theta);
+        s->costh[k] = cos(theta);
+    }
+    return R3D_OK;
 }
 
 void orc_r3d_initial(orc_r3d_t *s, int nval, double amp)
@@ -135,11 +154,12 @@ void orc_r3d_initial(orc_r3d_t *s, int nval, double amp)
         for (int j = 0; j <= nz + 1; ++j)
             for (int k = 0; k <= np; ++k) {
                 const double phi = 8.0 * atan(1.0) * (double)k / (double)np;
-                FX(s->th, i, j, k) = 1.0 - log(r) / log(s->r0) +
-                                     amp * (s->rmax - r) * (r - s->r0) * cos((double)nval * phi);
+                const double base = s->horizontal ? log(r) / log(s->r0) : 1.0 - log(r) / log(s->r0);
+                FX(s->th, i, j, k) = base + amp * (s->rmax - r) * (r - s->r0) * cos((double)nval * phi);
             }
     }
-    FX(s->th, nr / 4, nz / 4, np / 2) = FX(s->th, nr / 4, nz / 4, np / 2) - 0.5 * FX(s->th, nr / 4, nz / 4, np / 2);
+    const int ic = s->horizontal ? nr / 2 : nr / 4, jc = s->horizontal ? nz / 2 : nz / 4;
+    FX(s->th, ic, jc, np / 2) = FX(s->th, ic, jc, np / 2) - 0.5 * FX(s->th, ic, jc, np / 2);
     memcpy(s->Ap, s->A, nf * sizeof(double));
     memcpy(s->Bp, s->B, nf * sizeof(double));
     memcpy(s->Cp, s->C, nf * sizeof(double));
@@ -236,7 +256,9 @@ void orc_r3d_avorticity(orc_r3d_t *s)
                 const double cnh = -1.0 / (dp * dp) / (r * r);
                 const double RHS1 = Arra + Ara / r + Ahha / (r * r) + Azza - 2.0 * Bh / (r * r) + FX(A, i, j, k) / (Ptl * dt);
                 const double ULT = (u * Ar + v * Ah / r + w * Az - uelh * BB / r - uelz * CC) / Ptl;
-                const double RHS2 = -2.0 * Re * uelz + 2.0 * Ra * (tem * uelz + thz * u) / Re / Ptl - Gr * Ptl / r * thh;
+                const double RHS2 = s->horizontal ? s->sinth[k] * Gr * Ptl * thz
+                                                  : -2.0 * Re * uelz + 2.0 * Ra * (tem * uelz + thz * u) / Re / Ptl -
+                                                        Gr * Ptl / r * thh;
                 const double cf1 = 1.0 / (Ptl * dt) - uelr / (2.0 * Ptl) + 1.0 / (2.0 * (r * r)) - cnr - cnz - cnh;
                 const double cf2 = uelr / (2.0 * Ptl) - 1.0 / (2.0 * (r * r)) + cnr + cnz + cnh;
                 FX(An, i, j, k) = (cf2 * FX(Ap, i, j, k) - ULT - RHS2 + RHS1) / cf1;
@@ -315,7 +337,9 @@ void orc_r3d_bvorticity(orc_r3d_t *s)
                 const double RHS1 = Brra + Bra / r + Bhha / (r * r) + Bzza + 2.0 * Ah / (r * r) + FX(B, i, j, k) / (Ptl * dt);
                 const double ULT = (u * Br + v * Bh / r + w * Bz - (velr - v / r) * AA - velz * CC) / Ptl;
                 const double RHS2 =
-                    -2.0 * Re * velz + r * Ra * thz + 2.0 * Ra * (tem * velz + thz * v) / Re / Ptl + Gr * Ptl * thr;
+                    s->horizontal ? s->costh[k] * Gr * Ptl * thz
+                                  : -2.0 * Re * velz + r * Ra * thz + 2.0 * Ra * (tem * velz + thz * v) / Re / Ptl +
+                                        Gr * Ptl * thr;
                 const double cf1 = 1.0 / (Ptl * dt) - (u / r + velh / r) / (2.0 * Ptl) + 1.0 / (2.0 * (r * r)) - cnr - cnz - cnh;
                 const double cf2 = (u / r + velh / r) / (2.0 * Ptl) - 1.0 / (2.0 * (r * r)) + cnr + cnz + cnh;
                 FX(Bn, i, j, k) = (cf2 * FX(Bp, i, j, k) - ULT - RHS2 + RHS1) / cf1;
@@ -404,7 +428,9 @@ void orc_r3d_cvorticity(orc_r3d_t *s)
                 const double cnh = -1.0 / (dp * dp) / (r * r);
                 const double RHS1 = Crra + Cra / r + Chha / (r * r) + Czza + FX(C, i, j, k) / (Ptl * dt);
                 const double ULT = (u * Cr + v * Ch / r + w * Cz - welr * AA - welh * BB / r) / Ptl;
-                const double RHS2 = -2.0 * Re * welz - Ra * thh + 2.0 * Ra * (tem * welz - thr * u - thh * v / r) / Re / Ptl;
+                const double RHS2 =
+                    s->horizontal ? -(1.0 / r * s->Gr * Ptl * s->costh[k] * thh) - s->Gr * Ptl * s->sinth[k] * thr
+                                  : -2.0 * Re * welz - Ra * thh + 2.0 * Ra * (tem * welz - thr * u - thh * v / r) / Re / Ptl;
                 const double cf1 = 1.0 / (Ptl * dt) - welz / (2.0 * Ptl) - cnr - cnz - cnh;
                 const double cf2 = welz / (2.0 * Ptl) + cnr + cnz + cnh;
                 FX(Cn, i, j, k) = (cf2 * FX(Cp, i, j, k) - ULT - RHS2 + RHS1) / cf1;
@@ -526,8 +552,40 @@ double orc_r3d_heat(const orc_r3d_t *s)
     return trans1;
 }
 
+/* heat(trans1, trans2), rot3dmghor.f:913-945: both cylinders' fluxes over
+ * the band j = nz/2-3 .. nz/2+3, weights 1/120 at its ends and 1/60 inside,
+ * summed over k = 1..np. */
+double orc_r3d_heat2(const orc_r3d_t *s, double *trans2)
+{
+    const int nr = s->nr, nz = s->nz, np = s->np;
+    const double dr = s->dr, dz = s->dz, dp = s->dp;
+    const double *th = s->th;
+    const int nza = nz / 2 - 3, nzb = nz / 2 + 3;
+    double trans1 = 0.0, t2 = 0.0;
+#define HA(j, k) ((-184.0 * FX(th, 0, j, k) + 225.0 * FX(th, 1, j, k) - 50.0 * FX(th, 2, j, k) + 9.0 * FX(th, 3, j, k)))
+#define HB(j, k) ((184.0 * FX(th, nr + 1, j, k) - 225.0 * FX(th, nr, j, k) + 50.0 * FX(th, nr - 1, j, k) - \
+                   9.0 * FX(th, nr - 2, j, k)))
+    for (int k = 1; k <= np; ++k) {
+        double ta = dz * HA(nza, k) / (120.0 * dr);
+        double tb = dz * HB(nza, k) / (120.0 * dr);
+        ta = ta + dz * HA(nzb, k) / (120.0 * dr);
+        tb = tb + dz * HB(nzb, k) / (120.0 * dr);
+        for (int j = nza + 1; j <= nzb - 1; ++j) {
+            ta = ta + dz * HA(j, k) / (60.0 * dr);
+            tb = tb + dz * HB(j, k) / (60.0 * dr);
+        }
+        trans1 = trans1 + ta * dp;
+        t2 = t2 + tb * dp;
+    }
+#undef HA
+#undef HB
+    if (trans2) *trans2 = t2;
+    return trans1;
+}
+
 /* update, rot3dmg.f:964-1023: wall vorticities from the new velocities,
- * wall temperatures 0 (inner) and 1 (outer), then the time levels move. */
+ * wall temperatures 0 (inner) and 1 (outer; reversed in rot3dmghor.f:1042),
+ * then the time levels move. */
 void orc_r3d_update(orc_r3d_t *s)
 {
     const int nr = s->nr, nz = s->nz, np = s->np;
@@ -555,8 +613,8 @@ void orc_r3d_update(orc_r3d_t *s)
         }
     for (int j = 0; j <= nz + 1; ++j)
         for (int k = 0; k <= np; ++k) {
-            FX(s->thn, 0, j, k) = 0.0;
-            FX(s->thn, nr + 1, j, k) = 1.0;
+            FX(s->thn, 0, j, k) = s->horizontal ? 1.0 : 0.0;
+            FX(s->thn, nr + 1, j, k) = s->horizontal ? 0.0 : 1.0;
         }
     const size_t n = field_size(s) * sizeof(double);
     memcpy(s->Ap, s->A, n);
@@ -1260,7 +1318,7 @@ int orc_r3d_poisson(orc_r3d_t *s, int which, int *sweeps)
             s->last_sweeps = sweep - 1;
             return R3D_MAXSWEEPS;
         }
-        if (sweep != 1) {
+        if (sweep != 1 && !s->horizontal) {
             for (int k = 0; k <= np; ++k)
                 for (int j = 0; j <= n2; ++j)
                     for (int i = 0; i <= n1; ++i) {
@@ -1270,9 +1328,10 @@ int orc_r3d_poisson(orc_r3d_t *s, int which, int *sweeps)
         }
         if (sweep == 1 || nlev == 1) {
             orc_r3d_relax(s, which, s->nrel, 1, &nconv);
-            for (int k = 0; k <= np; ++k)
-                for (int j = 0; j <= n2; ++j)
-                    for (int i = 0; i <= n1; ++i) FX(psip, i, j, k) = V1(i, j, k);
+            if (!s->horizontal)
+                for (int k = 0; k <= np; ++k)
+                    for (int j = 0; j <= n2; ++j)
+                        for (int i = 0; i <= n1; ++i) FX(psip, i, j, k) = V1(i, j, k);
         }
         if (nlev > 1) {
             for (int l = 1; l <= nlev - 1; ++l) {
@@ -1324,7 +1383,8 @@ int orc_r3d_step(orc_r3d_t *s, double *nu, int *sweeps)
     orc_r3d_bvorticity(s);
     orc_r3d_cvorticity(s);
     orc_r3d_temperature(s);
-    const double trans1 = orc_r3d_heat(s);
+    double trans2 = 0.0;
+    const double trans1 = s->horizontal ? orc_r3d_heat2(s, &trans2) : orc_r3d_heat(s);
     orc_r3d_rhsw(s);
     int st = orc_r3d_poisson(s, 1, &sw[0]);
     if (st == R3D_OK) {
@@ -1342,6 +1402,13 @@ int orc_r3d_step(orc_r3d_t *s, double *nu, int *sweeps)
     }
     if (st != R3D_OK) return st;
     orc_r3d_update(s);
-    if (nu) *nu = -s->r0 * log(s->r0 / s->rmax) * trans1 / (s->zmax * 2.0 * s->pi);
+    if (s->horizontal) {
+        /* httrans1, httrans2 of rot3dmghor.f:264-267 */
+        const double L = log(s->r0 / s->rmax);
+        if (nu) *nu = (double)s->nz / 6.0 * s->r0 * L * trans1 / (s->zmax * 2.0 * s->pi);
+        s->nu2 = (double)s->nz / 6.0 * s->rmax * L * trans2 / (s->zmax * 2.0 * s->pi);
+    } else if (nu) {
+        *nu = -s->r0 * log(s->r0 / s->rmax) * trans1 / (s->zmax * 2.0 * s->pi);
+    }
     return R3D_OK;
 }

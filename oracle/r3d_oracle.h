@@ -67,6 +67,21 @@ typedef struct {
     int mode;                       /* R3D_LEX or R3D_ZEBRA */
     double last_resmax;
     int last_sweeps;
+    /* rot3dmghor.f, the annulus with its axis horizontal (set by
+     * orc_r3d_set_horizontal): gravity Gr Ptl across the axis as the only
+     * body force in the three vorticity updates (:477-479, :604-606,
+     * :747-749) with sin and cos of theta = 6.283185307/np k (libm, per
+     * k = 0..np); the heat flux of both cylinders over the band
+     * j = nz/2-3 .. nz/2+3 (:913-945); the inner cylinder hot (thn = 1 at
+     * i = 0, 0 at i = nr+1, :1042-1043); a plain V-cycle without the
+     * whole-cycle over-relaxation and without the psip copies (:1287-1315,
+     * commented out there); tolcon 1e-6 (:1599, :1798, :2051); the start
+     * T = ln r / ln r0 + ... with the point (nr/2, nz/2, np/2) halved
+     * (:133-141); Nusselt numbers nz/6 r0 ln(r0/rmax) trans1 / (zmax 2 pi)
+     * and the same with rmax and trans2 (:264-267). */
+    int horizontal;
+    double *sinth, *costh;
+    double nu2;                     /* httrans2 of the last step */
 } orc_r3d_t;
 
 /* Sets sizes, constants (rot3dmg.f:92-96) and the multigrid levels; all
@@ -80,12 +95,16 @@ void orc_r3d_free(orc_r3d_t *s);
  * (nr/4, nz/4, np/2) halved, and the previous time level copied
  * (rot3dmg.f:220-230). */
 void orc_r3d_initial(orc_r3d_t *s, int nval, double amp);
+/* Switches s to rot3dmghor.f (see the horizontal field); call after init. */
+int  orc_r3d_set_horizontal(orc_r3d_t *s);
 
 void orc_r3d_avorticity(orc_r3d_t *s);
 void orc_r3d_bvorticity(orc_r3d_t *s);
 void orc_r3d_cvorticity(orc_r3d_t *s);
 void orc_r3d_temperature(orc_r3d_t *s);
 double orc_r3d_heat(const orc_r3d_t *s);
+/* heat(trans1, trans2) of rot3dmghor.f:913-945 (both cylinders). */
+double orc_r3d_heat2(const orc_r3d_t *s, double *trans2);
 void orc_r3d_update(orc_r3d_t *s);
 void orc_r3d_rhsw(orc_r3d_t *s);
 void orc_r3d_rhsv(orc_r3d_t *s);

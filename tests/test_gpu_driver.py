@@ -88,3 +88,27 @@ def test_r3d_driver_matches_oracle_and_restarts(oracle, gblib, tmp_path):
         np.testing.assert_array_equal(g2.get(name), np.array(o.field(name)), err_msg=name)
     _, _, t2 = fortio.read_r3d_field(str(tmp_path / "t2.dat"), "th")
     np.testing.assert_array_equal(t2, np.array(o.field("th")))
+
+
+def test_r3d_horizontal_driver_matches_oracle(oracle, gblib, tmp_path):
+    """The same deck through rot3dmghor.f's main program (--horizontal):
+    httrans1 and the fields equal the oracle's, and the Nusselt history has
+    rot3dmghor.f's three columns (time, inner, outer cylinder)."""
+    from codesthesis_dir_gb300 import driver_r3d, fortio
+    from test_formats import R3D_DECK
+    deck = R3D_DECK.replace("1.d5\n100.\n0.\n0.7\n", "0.\n0.\n1.d4\n7.\n")
+    g, ht = driver_r3d.run(deck, outdir=str(tmp_path), log=lambda *a: None, horizontal=True)
+    o = oracle.OracleR3D(8, 8, 16, 1e-5, 0.5, 1.0, 0.5, 0.0, 0.0, 7.0, Gr=1e4, horizontal=True)
+    o.initial(3, 5e-2)
+    want, want2 = [], []
+    for _ in range(5):
+        st, nu, sw = o.step()
+        assert st == 0
+        want.append(nu)
+        want2.append(o.nu2)
+    np.testing.assert_array_equal(ht, np.array(want))
+    for name in ("A", "B", "C", "th", "uel", "vel", "wel"):
+        np.testing.assert_array_equal(g.get(name), np.array(o.field(name)), err_msg=name)
+    rows = [[fortio.fortran_real(x) for x in ln.split()] for ln in open(tmp_path / "nu.dat").read().splitlines()]
+    assert len(rows) == 5 and all(len(r) == 3 for r in rows)
+    np.testing.assert_allclose([r[2] for r in rows], want2, rtol=5.1e-8)

@@ -34,12 +34,18 @@ def _ptr(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
-@pytest.mark.parametrize("mode", [0, 1], ids=["lex", "zebra"])
-def test_main_loop_through_dropin(oracle, D, mode):
+@pytest.mark.parametrize("mode,horizontal", [(0, False), (1, False), (1, True)],
+                         ids=["lex", "zebra", "horizontal-zebra"])
+def test_main_loop_through_dropin(oracle, D, mode, horizontal):
+    """horizontal: rot3dmghor.f's main loop through the same symbols with
+    gb_r3d_bind_variant(GB_R3D_HORIZONTAL): heat(trans1, trans2) and both
+    Nusselt numbers (rot3dmghor.f:255-267)."""
     nr, nz, np_ = 8, 8, 16
-    prm = dict(dt=1e-5, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e5, Re=100.0, Pr=0.7)
+    prm = dict(dt=1e-5, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e5, Re=100.0, Pr=0.7, Gr=0.0)
+    if horizontal:
+        prm.update(Ra=0.0, Re=0.0, Pr=7.0, Gr=1e4)
     o = oracle.OracleR3D(nr, nz, np_, prm["dt"], prm["r0"], prm["rmax"], prm["zmax"], prm["Ra"], prm["Re"],
-                         prm["Pr"], mode=mode)
+                         prm["Pr"], Gr=prm["Gr"], mode=mode, horizontal=horizontal)
     o.initial(3, 5e-2)
     shp = (KR + 1, KZ + 1, KP + 1)
     S = int(np.prod(shp))
@@ -57,7 +63,7 @@ def test_main_loop_through_dropin(oracle, D, mode):
     for name in SOL1 + SOL2 + SOL3:
         view(name)[:ni, :nj, :nk] = np.array(o.field(name))
     num = Num(prm["dt"], o.s.dr, o.s.dz, o.s.dp, nr, nz, np_)
-    val = np.array([prm["Ra"], prm["Re"], prm["Pr"], 0.0])
+    val = np.array([prm["Ra"], prm["Re"], prm["Pr"], prm["Gr"]])
     radius = np.array([prm["r0"], prm["rmax"]])
     rh = {n: np.full(S, SENTINEL) for n in ("wrh", "vrh", "urh")}
     for n in rh:
@@ -66,6 +72,7 @@ def test_main_loop_through_dropin(oracle, D, mode):
     D.gb_r3d_bind_common(_ptr(blocks["sol1"][1]), _ptr(blocks["sol2"][1]), _ptr(blocks["sol3"][1]),
                          C.cast(C.byref(num), C.c_void_p), _ptr(val), _ptr(radius))
     D.gb_r3d_bind_smoother(mode)
+    D.gb_r3d_bind_variant(1 if horizontal else 0)
     ci = lambda v: C.byref(C.c_int(v))  # noqa: E731
     cd = lambda v: C.byref(C.c_double(v))  # noqa: E731
     nlev = C.c_int(0)
@@ -86,8 +93,11 @@ def test_main_loop_through_dropin(oracle, D, mode):
         D.bvorticity_()
         D.cvorticity_()
         D.temperature_()
-        trans1 = C.c_double()
-        D.heat_(C.byref(trans1))
+        trans1, trans2 = C.c_double(), C.c_double()
+        if horizontal:
+            D.heat_(C.byref(trans1), C.byref(trans2))
+        else:
+            D.heat_(C.byref(trans1), None)   # rot3dmg.f's one-argument call: trans2 is not read
         sweeps = []
         for which, rhsn, fn, fnp, rfn in ((1, "wrh", "wel", "welp", D.rhsw_), (2, "vrh", "vel", "velp", D.rhsv_),
                                           (3, "urh", "uel", "uelp", D.rhsu_)):
@@ -97,7 +107,13 @@ def test_main_loop_through_dropin(oracle, D, mode):
             sweeps.append(D.gb_r3d_last_sweeps())
         D.update_()
         assert D.gb_r3d_last_status() == 0
-        nu = -prm["r0"] * math.log(prm["r0"] / prm["rmax"]) * trans1.value / (prm["zmax"] * 2.0 * pi)
+        if horizontal:
+            L = math.log(prm["r0"] / prm["rmax"])
+            nu = nz / 6.0 * prm["r0"] * L * trans1.value / (prm["zmax"] * 2.0 * pi)
+            nu2 = nz / 6.0 * prm["rmax"] * L * trans2.value / (prm["zmax"] * 2.0 * pi)
+            assert nu2 == o.nu2, (step, nu2, o.nu2)
+        else:
+            nu = -prm["r0"] * math.log(prm["r0"] / prm["rmax"]) * trans1.value / (prm["zmax"] * 2.0 * pi)
         assert nu == nu_o, (step, nu, nu_o)
         assert sweeps == list(sw_o), (step, sweeps, sw_o)
         for name in SOL1 + SOL2 + SOL3:
@@ -109,3 +125,4 @@ def test_main_loop_through_dropin(oracle, D, mode):
         a[:ni, :nj, :nk] = SENTINEL
         assert np.all(a == SENTINEL), name
     D.gb_r3d_bind_common(None, None, None, None, None, None)
+    D.gb_r3d_bind_variant(0)

@@ -145,3 +145,52 @@ def test_sweep_limit_stops(oracle, R):
         g.step(2)
     assert ei.value.status == lib.GB_MAXSWEEPS
     assert g.steps_done == 0 and g.last_sweeps[0][0] == 3
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["lex", "zebra"])
+def test_horizontal_annulus_steps(oracle, R, mode):
+    """rot3dmghor.f (GB_R3D_HORIZONTAL) from its own start: gravity across
+    the axis, both cylinders' Nusselt numbers, the plain V-cycle at tolcon
+    1e-6; fields, httrans1, httrans2 and sweep counts equal the oracle's bit
+    for bit, step by step and through the routines."""
+    from codesthesis_dir_gb300 import lib
+    prm = dict(dt=1e-5, r0=0.5, rmax=1.0, zmax=0.5, Ra=0.0, Re=0.0, Pr=7.0, Gr=1e4)
+    o = oracle.OracleR3D(8, 8, 16, prm["dt"], prm["r0"], prm["rmax"], prm["zmax"], prm["Ra"], prm["Re"], prm["Pr"],
+                         Gr=prm["Gr"], mode=mode, horizontal=True)
+    o.initial(3, 5e-2)
+    g = R.R3D(8, 8, 16, smoother=mode, variant=lib.R3D_HORIZONTAL, **prm)
+    assert g.params.tolcon == 1e-6 and g.nlev == o.s.nlev
+    for n in FIELDS:
+        g.set(n, np.array(o.field(n)))
+    nus, nu2s, sws = [], [], []
+    for _ in range(3):
+        st, nu, sw = o.step()
+        assert st == 0
+        nus.append(nu)
+        nu2s.append(o.nu2)
+        sws.append(sw.copy())
+    nu_g, sw_g = g.step(3)
+    assert list(nu_g) == nus and list(g.nu2) == nu2s
+    np.testing.assert_array_equal(sw_g, np.array(sws))
+    assert diff(o, g) == {}
+    # one more step routine by routine, heat(trans1, trans2) included
+    import ctypes as C
+    o.call("avorticity")
+    o.call("bvorticity")
+    o.call("cvorticity")
+    o.call("temperature")
+    t2 = C.c_double()
+    t1 = oracle.lib().orc_r3d_heat2(C.byref(o.s), C.byref(t2))
+    g.avorticity()
+    g.bvorticity()
+    g.cvorticity()
+    g.temperature()
+    assert g.heat2() == (t1, t2.value)
+    for which, rhs in ((1, "rhsw"), (2, "rhsv"), (3, "rhsu")):
+        o.call(rhs)
+        getattr(g, rhs)()
+        st, sw = o.poisson(which)
+        assert st == 0 and g.poisson(which) == sw
+    o.call("update")
+    g.update()
+    assert diff(o, g) == {}

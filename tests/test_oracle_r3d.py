@@ -219,3 +219,63 @@ def test_sweep_limit(oracle):
     o.field("wrh")[...] = f
     st, sw = o.poisson(1)
     assert st == 1 and sw == 3
+
+
+# ---------------------------------------------------------------------------
+# rot3dmghor.f: the annulus with its axis horizontal
+# ---------------------------------------------------------------------------
+def _hor(oracle, Gr, nr=8, nz=8, np_=16, tolcon=None):
+    o = oracle.OracleR3D(nr, nz, np_, 1e-5, 0.5, 1.0, 0.5, 0.0, 0.0, 7.0, Gr=Gr, mode=1, horizontal=True,
+                         tolcon=tolcon)
+    return o
+
+
+def test_horizontal_initial_state_matches_host(oracle):
+    from codesthesis_dir_gb300 import initial
+    o = _hor(oracle, 1e4)
+    o.initial(3, 5e-2)
+    np.testing.assert_array_equal(np.array(o.field("th")),
+                                  initial.r3d_reference(8, 8, 16, 0.5, 1.0, 3, 5e-2, horizontal=True))
+    th = np.array(o.field("th"))
+    assert th[0, 3, 0] == 1.0 and th[9, 3, 0] == 0.0   # the inner cylinder hot
+
+
+def test_horizontal_without_gravity_stays_at_rest(oracle):
+    """With Gr = 0 the horizontal annulus has no body force: the flow stays
+    exactly at rest while T diffuses; with Gr > 0 it moves."""
+    for Gr, moving in ((0.0, False), (1e4, True)):
+        o = _hor(oracle, Gr)
+        o.initial(3, 5e-2)
+        for _ in range(3):
+            st, nu, sw = o.step()
+            assert st == 0, sw
+        vmax = max(np.abs(np.array(o.field(n))).max() for n in ("uel", "vel", "wel"))
+        assert (vmax > 1e-6) == moving, (Gr, vmax)
+
+
+def test_horizontal_heat_of_the_conduction_profile(oracle):
+    """For T = ln r / ln r0 (the conduction state, inner wall 1 at r0, outer
+    0 at rmax = 1) both Nusselt numbers of rot3dmghor.f:264-267 are 1 to
+    the one-sided derivative's accuracy."""
+    import ctypes as C
+    for nr in (16, 32):
+        o = _hor(oracle, 0.0, nr=nr, nz=16, np_=16)
+        s = o.s
+        i = np.arange(nr + 2)
+        r = np.where(i == 0, s.r0, np.where(i == nr + 1, s.rmax, s.r0 + (i - 0.5) * s.dr))
+        o.field("th")[...] = (np.log(r) / math.log(s.r0))[:, None, None]
+        t2 = C.c_double()
+        t1 = oracle.lib().orc_r3d_heat2(C.byref(s), C.byref(t2))
+        L = math.log(s.r0 / s.rmax)
+        nu1 = s.nz / 6.0 * s.r0 * L * t1 / (s.zmax * 2.0 * math.pi)
+        nu2 = s.nz / 6.0 * s.rmax * L * t2.value / (s.zmax * 2.0 * math.pi)
+        assert abs(nu1 - 1.0) < 40.0 / nr ** 2 and abs(nu2 - 1.0) < 40.0 / nr ** 2, (nr, nu1, nu2)
+
+
+def test_horizontal_plain_cycle_converges_at_the_reference_tolerance(oracle):
+    o = _hor(oracle, 1e4)
+    assert o.s.tolcon == 1e-6
+    o.initial(3, 5e-2)
+    st, nu, sw = o.step()
+    assert st == 0 and all(0 < x < 100 for x in sw)
+    assert abs(nu - 1.0) < 0.01 and abs(o.nu2 - 1.0) < 0.01
