@@ -172,7 +172,7 @@ __global__ void k_robert(PrbDev d, int fx, int fxn, int fxp, int imax)
     if (t >= imax * (d.np + 1) || *d.abort) return;
     const int i = t % imax + 1, k = t / imax;
     const size_t c = GIX(i, k, d.ld);
-    const double gamma = d.polar ? 0.05 : 0.02;
+    const double gamma = d.robert;
     double *X = d.f[fx];
     X[c] = X[c] + gamma * (d.f[fxn][c] - 2.0 * X[c] + d.f[fxp][c]);
 }
@@ -322,7 +322,16 @@ __global__ void k_rhs(PrbDev d, int do_v, int do_u)
         if (d.polar) {
             const double r = d.r0 + ((double)i - 0.5) * d.dr;
             if (i == 1) v = Cn[GIX(1, k, ld)] / d.dr + Cn[GIX(1, k, ld)] / r;
-            else if (i == nr) v = -Cn[GIX(nr - 1, k, ld)] / d.dr + Cn[GIX(nr - 1, k, ld)] / r;
+            else if (i == nr) {
+                v = -Cn[GIX(nr - 1, k, ld)] / d.dr + Cn[GIX(nr - 1, k, ld)] / r;
+                if (d.taycou) {
+                    // the moving wall's term, velvor2dtaycouheat.f:1668-1670
+                    const double velo = d.velo, rvali = 1.0 / d.rmax, hri = 1.0 / d.dr;
+                    const double hhri = hri * hri;
+                    v = v - 8.0 / 15.0 * velo * hhri + rvali * hri * velo - 4.0 / 3.0 * velo * hri * rvali +
+                        velo * (rvali * rvali);
+                }
+            }
             else v = Cr + (Cn[GIX(i, k, ld)] + Cn[GIX(i - 1, k, ld)]) / r;
         } else if (i == 1) v = Cn[GIX(1, k, ld)] / d.dr;
         else if (i == nr) v = -Cn[GIX(nr - 1, k, ld)] / d.dr;
@@ -379,9 +388,16 @@ __global__ void k_update(PrbDev d)
             f[GB_F_thn][c] = 0.0;
         } else if (i == nr) {
             f[GB_F_Bn][c] = -(f[GB_F_wel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_wel][GIX(nr, k, ld)]) / dr;
-            f[GB_F_Cn][c] = (f[GB_F_vel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_vel][GIX(nr, k, ld)]) / dr;
+            if (d.taycou)
+                // velvor2dtaycouheat.f:1587-1590; v(nr+1) is the wall speed the
+                // i = nr+1 thread stores
+                f[GB_F_Cn][c] = (8.0 / 3.0 * d.velo + f[GB_F_vel][GIX(nr - 1, k, ld)] / 3.0 -
+                                 3.0 * f[GB_F_vel][GIX(nr, k, ld)]) / dr + d.velo / d.rmax;
+            else
+                f[GB_F_Cn][c] = (f[GB_F_vel][GIX(nr - 1, k, ld)] / 3.0 - 3.0 * f[GB_F_vel][GIX(nr, k, ld)]) / dr;
         } else if (i == nr + 1) {
             f[GB_F_thn][c] = 1.0;
+            if (d.taycou) f[GB_F_vel][c] = d.velo;
         }
         f[GB_F_Cp][c] = f[GB_F_C][c];
         f[GB_F_C][c] = f[GB_F_Cn][c];
@@ -525,7 +541,7 @@ int prb_launch_update(gb_prb *h, cudaStream_t s, bool diag)
 int prb_launch_record(gb_prb *h, cudaStream_t s)
 {
     double c1 = h->p.rmax - h->p.r0, c2 = c1, div = h->p.xx;
-    if (h->p.variant == GB_PRB_ANNULUS) {
+    if (h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU) {
         const double L = log(h->p.r0 / h->p.rmax);
         c1 = -h->p.r0 * L;
         c2 = -h->p.rmax * L;
@@ -570,6 +586,17 @@ extern "C" void gb_prb_default_params_annulus(gb_prb_params *p, int nr, int np)
     p->maxsweeps = 10000;
 }
 
+extern "C" void gb_prb_default_params_taycou(gb_prb_params *p, int nr, int np)
+{
+    gb_prb_default_params_annulus(p, nr, np);
+    p->variant = GB_PRB_TAYCOU;
+    p->Ra = 6e8;
+    p->Re = 91927.0;
+    p->Ta = 0.0;
+    p->tolcon = 1e-5;
+    p->maxsweeps = 500;
+}
+
 // Level count of poissoninit (PRB:1744-1767; the annulus caps at 5,
 // velvor2dnewsch3.4.f:1778).
 int prb_mg_levels(int nr, int variant)
@@ -598,8 +625,12 @@ int prb_refresh_scalars(gb_prb *h)
     d.dt = h->p.dt;
     d.Ra = h->p.Ra;
     d.Pr = h->p.Pr;
-    d.polar = h->p.variant == GB_PRB_ANNULUS;
+    d.polar = h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU;
     d.oblique = h->p.variant == GB_PRB_OBLIQUE;
+    d.taycou = h->p.variant == GB_PRB_TAYCOU;
+    d.rmax = h->p.rmax;
+    d.velo = d.taycou ? -(pow(h->p.Ta, 0.5) * h->p.Pr * 0.5 * h->p.rmax) : 0.0;
+    d.robert = h->p.variant == GB_PRB_ANNULUS ? 0.05 : d.taycou ? 0.01 : 0.02;
     d.r0 = h->p.r0;
     d.Re = h->p.Re;
     d.dr = h->dr_set != 0.0 ? h->dr_set : (h->p.rmax - h->p.r0) / (double)h->p.nr;
@@ -620,11 +651,13 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     const int nr = p->nr, np = p->np;
     const int nlev = prb_mg_levels(nr, p->variant);
     if (nlev_out) *nlev_out = nlev;
-    if (p->variant != GB_PRB_LAYER && p->variant != GB_PRB_ANNULUS && p->variant != GB_PRB_OBLIQUE) {
+    if (p->variant != GB_PRB_LAYER && p->variant != GB_PRB_ANNULUS && p->variant != GB_PRB_OBLIQUE &&
+        p->variant != GB_PRB_TAYCOU) {
         gb_set_error("gb_prb_create: unknown variant %d", p->variant);
         return GB_ERR_INVALID;
     }
-    if (p->variant == GB_PRB_ANNULUS && !(p->r0 > 0.0 && p->rmax > p->r0 && p->Re != 0.0)) {
+    if ((p->variant == GB_PRB_ANNULUS || p->variant == GB_PRB_TAYCOU) &&
+        !(p->r0 > 0.0 && p->rmax > p->r0 && p->Re != 0.0 && p->Ta >= 0.0)) {
         gb_set_error("gb_prb_create: the annulus needs 0 < r0 < rmax and Re != 0 (r0=%g rmax=%g Re=%g)", p->r0, p->rmax, p->Re);
         return GB_ERR_INVALID;
     }

@@ -80,6 +80,7 @@ DropIn &g()
         {
             if (strcmp(s, "annulus") == 0 || strcmp(s, "1") == 0) d.variant = GB_PRB_ANNULUS;
             if (strcmp(s, "oblique") == 0 || strcmp(s, "2") == 0) d.variant = GB_PRB_OBLIQUE;
+            if (strcmp(s, "taycou") == 0 || strcmp(s, "3") == 0) d.variant = GB_PRB_TAYCOU;
         }
     }
     return d;
@@ -117,7 +118,7 @@ int ensure(int nr, int np, double dr, double dp)
         gb_set_error("grid nr=%d np=%d exceeds the COMMON bounds kr=%d kp=%d", nr, np, d.kr, d.kp);
         return GB_ERR_INVALID;
     }
-    const bool ann = d.variant == GB_PRB_ANNULUS;
+    const bool ann = d.variant == GB_PRB_ANNULUS || d.variant == GB_PRB_TAYCOU;
     double r0 = 0.5, rmax = 1.0, Re = 1.0;
     if (ann) {
         // the annulus multigrid coefficients depend on r0 (COMMON /radius/)
@@ -136,7 +137,8 @@ int ensure(int nr, int np, double dr, double dp)
     d.ctx = nullptr;
     gb_prb_params p;
     if (ann) {
-        gb_prb_default_params_annulus(&p, nr, np);
+        if (d.variant == GB_PRB_TAYCOU) gb_prb_default_params_taycou(&p, nr, np);
+        else gb_prb_default_params_annulus(&p, nr, np);
         p.r0 = r0;
         p.rmax = rmax;
         p.Re = Re;
@@ -165,7 +167,8 @@ int ensure_from_common()
     h->p.dt = n->dt;
     h->p.Ra = valp()->Ra;
     h->p.Pr = valp()->Ptl;
-    if (h->p.variant == GB_PRB_ANNULUS) {
+    if (h->p.variant == GB_PRB_TAYCOU) h->p.Ta = valp()->Gr;   // velvor2dtaycouheat.f:106-109: Gr holds Ta
+    if (h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU) {
         h->p.Re = valp()->Re;
         h->p.r0 = radiusp()[0];
         h->p.rmax = radiusp()[1];
@@ -283,7 +286,8 @@ void gb_prb_bind_common(double *sol1, double *sol2, double *sol3, void *num, dou
 void gb_prb_bind_variant(int variant)
 {
     std::lock_guard<std::mutex> lk(g().mu);
-    g().variant = (variant == GB_PRB_ANNULUS || variant == GB_PRB_OBLIQUE) ? variant : GB_PRB_LAYER;
+    g().variant = (variant == GB_PRB_ANNULUS || variant == GB_PRB_OBLIQUE || variant == GB_PRB_TAYCOU) ? variant
+                                                                                                   : GB_PRB_LAYER;
 }
 
 void gb_prb_bind_radius(double *radius)
@@ -343,6 +347,8 @@ void update_(void)
     long long clamps = 0;
     if (st == GB_OK) st = gb_prb_update(g().ctx, &clamps);
     if (st == GB_OK) st = down({GB_F_Bn, GB_F_Cn, GB_F_Cp, GB_F_C, GB_F_thp, GB_F_thn, GB_F_th});
+    // the Taylor-Couette update also sets the moving wall's v (velvor2dtaycouheat.f:1587)
+    if (st == GB_OK && g().ctx->p.variant == GB_PRB_TAYCOU) st = down({GB_F_vel});
     for (long long i = 0; i < clamps && i < 16; ++i) printf(" WARNING! Temp damped\n");
     fail(st);
 }

@@ -29,7 +29,9 @@ struct MgLevel {
 struct MgEq {
     int which;           // 2: v (cell centred, pentadiagonal), 3: u (face, tridiagonal)
     int nr, np, ld, nlev, mode, maxsweeps;
-    int polar;           // annulus operator, three relaxations per visit, seam residual kept
+    int polar;           // the (r, phi) operator (annulus and Taylor-Couette)
+    int nrelax;          // relaxations per relax call: 3 in the annulus, else 1
+    int seam_keep;       // the annulus's corser keeps the coarse seam residual
     int stop_on_max;     // the sweep limit fails the step (PRB's STOP) or only is reported
     double r0;
     double tolcon, sor;
@@ -45,8 +47,12 @@ struct MgEq {
 
 struct PrbDev {
     int nr, np, ld;
-    int polar;           // GB_PRB_ANNULUS
+    int polar;           // GB_PRB_ANNULUS or GB_PRB_TAYCOU: the (r, phi) plane
     int oblique;         // GB_PRB_OBLIQUE
+    int taycou;          // GB_PRB_TAYCOU: the moving outer wall
+    double velo;         // its speed -(Ta**0.5) Ptl rmax / 2 (host libm pow)
+    double rmax;
+    double robert;       // Robert filter coefficient: 0.02 layer, 0.05 annulus, 0.01 Taylor-Couette
     double dt, Ra, Pr, dr, dp, dri, dpi;
     double r0, Re;
     double *f[GB_F_COUNT];

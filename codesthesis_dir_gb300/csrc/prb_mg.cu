@@ -16,13 +16,16 @@
 // bit-identical to the reference algorithm and ZEBRA results to the same
 // algorithm under zebra ordering.
 //
-// The rotating-annulus variant (E.polar; relax2/relax3/corser of
+// The rotating-annulus variant (relax2/relax3/corser of
 // velvor2dnewsch3.4.f:2071-2716) uses the same kernel: its line matrices
 // depend on the radius of row i but not on the line k, so they are still
 // factored once per level; the line right-hand sides and residuals gain the
-// polar terms, every level visit runs three relaxations (:2134, :2410), and
-// the coarse right-hand side of seam line n3c keeps the fine residual stored
-// there because that corser does not clear it (:2696-2704).
+// polar terms (E.polar), every level visit runs three relaxations (E.nrelax,
+// :2134, :2410), and the coarse right-hand side of seam line n3c keeps the
+// fine residual stored there because that corser does not clear it
+// (E.seam_keep, :2696-2704).  The Taylor-Couette driver
+// (velvor2dtaycouheat.f) has the polar operator with PRB's single
+// relaxation and seam reset.
 //
 // Storage differs from the reference only in scratch that no output depends
 // on: the right-hand sides are read from the packed per-level arrays instead
@@ -143,7 +146,7 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
     const double *rvi = L.rvi, *rvq = L.rvq;
     double *psif = E.psif, *rc = E.rc;
     const double *f = L.f;
-    const int nrel = E.polar ? 3 : 1;
+    const int nrel = E.nrelax;
     for (int irel = 0; irel < nrel; ++irel) {
         if (E.mode == GB_SMOOTHER_LEX) {
             if (threadIdx.x == 0)
@@ -230,7 +233,7 @@ __device__ void mg_corser(const MgEq &E, int klev)
             t = t + rf[GIX(iim, kkp, ld)];
             t = t + rf[GIX(iim, kkm, ld)];
             t = t * 0.015625;
-        } else if (E.polar && i >= 1 && i <= n1c - 1) {
+        } else if (E.seam_keep && i >= 1 && i <= n1c - 1) {
             t = rf[GIX(i, k, ld)];   // seam lines k = 0, n3c keep rc (k = 0 is never written)
         }
         fc[idx] = t;
@@ -541,7 +544,7 @@ __device__ void mg_relax32(const MgEq &E, int klev)
     const int ld = E.ld, n1 = L.n1, n3 = L.n3;
     const float hhri = (float)L.hhri, hhpi = (float)L.hhpi, hri = (float)L.hri;
     float *psif = E.psif32, *rc = E.rc32;
-    const int nrel = E.polar ? 3 : 1;
+    const int nrel = E.nrelax;
     for (int irel = 0; irel < nrel; ++irel) {
         if (E.mode == GB_SMOOTHER_LEX) {
             if (threadIdx.x == 0)
@@ -590,7 +593,7 @@ __device__ void mg_corser32(const MgEq &E, int klev)
                           rf[GIX(ii, kk - 1, ld)]) +
                 0.0625f * (rf[GIX(ii + 1, kk + 1, ld)] + rf[GIX(ii + 1, kk - 1, ld)] + rf[GIX(ii - 1, kk + 1, ld)] +
                            rf[GIX(ii - 1, kk - 1, ld)]);
-        } else if (E.polar && i >= 1 && i <= n1c - 1 && k == n3c) {
+        } else if (E.seam_keep && i >= 1 && i <= n1c - 1 && k == n3c) {
             t = rf[GIX(i, k, ld)];
         }
         fc[idx] = t;
@@ -874,8 +877,10 @@ int prb_mg_create(gb_prb *h)
         E.which = q == 0 ? 2 : 3;
         E.nr = nr; E.np = np; E.ld = ld; E.nlev = nlev;
         E.mode = p.smoother; E.maxsweeps = p.maxsweeps; E.tolcon = p.tolcon; E.sor = p.sor;
-        E.polar = p.variant == GB_PRB_ANNULUS;
-        E.stop_on_max = !E.polar;
+        E.polar = p.variant == GB_PRB_ANNULUS || p.variant == GB_PRB_TAYCOU;
+        E.nrelax = p.variant == GB_PRB_ANNULUS ? 3 : 1;
+        E.seam_keep = p.variant == GB_PRB_ANNULUS;
+        E.stop_on_max = p.variant != GB_PRB_ANNULUS;
         E.r0 = p.r0;
         double *base = h->mg_pool + q * per_eq;
         E.psif = base; base += (size_t)ld * (np + 1);

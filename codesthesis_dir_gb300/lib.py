@@ -34,6 +34,7 @@ SMOOTHER_ZEBRA = 1
 PRB_LAYER = 0
 PRB_ANNULUS = 1
 PRB_OBLIQUE = 2   # mpkoks.f: the layer with gravity along the diagonal
+PRB_TAYCOU = 3    # velvor2dtaycouheat.f: the annulus with a moving outer cylinder
 PRB_FP64 = 0
 PRB_MIXED = 1
 BATCH_FP64 = 0
@@ -86,7 +87,7 @@ class PrbParams(C.Structure):
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
                 ("Ra", C.c_double), ("Pr", C.c_double), ("tolcon", C.c_double), ("sor", C.c_double),
                 ("maxsweeps", C.c_int), ("smoother", C.c_int), ("variant", C.c_int), ("Re", C.c_double),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("Ta", C.c_double)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -100,6 +101,7 @@ SIGNATURES = [
     ("gb_version", C.c_char_p, []),
     ("gb_prb_default_params", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
     ("gb_prb_default_params_annulus", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
+    ("gb_prb_default_params_taycou", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
     ("gb_prb_create", C.c_int, [C.POINTER(PrbParams), C.POINTER(_vp), _ip]),
     ("gb_prb_destroy", C.c_int, [_vp]),
     ("gb_prb_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),

@@ -11,7 +11,11 @@ out as Fortran-ordered (ld, np+1) float64 arrays with ld >= nr+2.
 variant=PRB_ANNULUS gives the rotating-annulus (r, phi) plane driver
 (iarchomedir_groke_storage_users_mpking_rotannconvvelvorplane_continueddir/
 velvor2dnewsch3.4.f), whose routines have the same names; tolcon and
-maxsweeps then default to its 1e-5 and 10000.
+maxsweeps then default to its 1e-5 and 10000.  variant=PRB_OBLIQUE is
+mpkoks.f (the layer with gravity along the diagonal) and variant=PRB_TAYCOU
+the Taylor-Couette driver (monashubuntudir_velvor2dtaycouheatdir/
+velvor2dtaycouheat.f: the annulus with its outer cylinder moving at
+-(Ta**0.5) Ptl rmax / 2, Taylor number Ta).
 
 Error behaviour: where the reference STOPs after 500 multigrid sweeps
 (PRB:1843), poisson2/poisson3 raise GBError with status GB_MAXSWEEPS.  The
@@ -30,13 +34,16 @@ from . import lib as _L
 class PRB:
     def __init__(self, nr, np_, dt=1e-7, r0=0.5, rmax=1.0, xx=3.0, Ra=1e7, Pr=0.71,
                  tolcon=None, sor=1.2, maxsweeps=None, smoother=_L.SMOOTHER_LEX,
-                 variant=_L.PRB_LAYER, Re=0.0, precision=_L.PRB_FP64):
+                 variant=_L.PRB_LAYER, Re=0.0, precision=_L.PRB_FP64, Ta=0.0):
         L = _L.load()
         p = _L.PrbParams()
         if variant == _L.PRB_ANNULUS:
             L.gb_prb_default_params_annulus(C.byref(p), nr, np_)
+        elif variant == _L.PRB_TAYCOU:
+            L.gb_prb_default_params_taycou(C.byref(p), nr, np_)
         else:
             L.gb_prb_default_params(C.byref(p), nr, np_)
+        p.Ta = Ta
         p.dt, p.r0, p.rmax, p.xx, p.Ra, p.Pr = dt, r0, rmax, xx, Ra, Pr
         p.sor, p.smoother, p.Re, p.precision, p.variant = sor, smoother, Re, precision, variant
         if tolcon is not None:

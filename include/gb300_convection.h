@@ -82,6 +82,7 @@ typedef struct gb_prb_params {
     int variant;     /* GB_PRB_LAYER, GB_PRB_ANNULUS or GB_PRB_OBLIQUE */
     double Re;       /* rotational Reynolds number (COMMON /val/ Re; annulus only) */
     int precision;   /* GB_PRB_FP64 (bit-exact) or GB_PRB_MIXED (FP32 cycles inside FP64 defect correction) */
+    double Ta;       /* Taylor number (GB_PRB_TAYCOU; read into COMMON /val/ Gr there) */
 } gb_prb_params;
 
 /* Precision of the velocity multigrid solves.
@@ -116,10 +117,23 @@ typedef struct gb_prb_params {
  *                   monashubuntudir_velvor2dperiodicrbconvdir/mpkoks.f: the
  *                   buoyancy term of both vorticity updates is
  *                   RHS2 = -Ra thr 0.707106781 (REAL*4 literal; :769-770,
- *                   :974-975) instead of -Ra thh; all else is the layer's. */
+ *                   :974-975) instead of -Ra thh; all else is the layer's.
+ *   GB_PRB_TAYCOU:  the annulus with a moving outer cylinder,
+ *                   monashubuntudir_velvor2dtaycouheatdir/velvor2dtaycouheat.f:
+ *                   the annulus's geometry and transport with Robert filter
+ *                   0.01 (:605, :837); the outer wall moves at
+ *                   v = -(Ta**0.5) Ptl rmax / 2 (the start :177 and every
+ *                   update :1587, libm pow), its wall vorticity is
+ *                   (8/3 v(nr+1) + v(nr-1)/3 - 3 v(nr))/dr + v(nr+1)/rmax
+ *                   (:1589-1590) and rhsv adds its term at i = nr
+ *                   (:1668-1670); the multigrid is PRB's (one relaxation
+ *                   per visit, coarse seam reset, STOP after 500 sweeps,
+ *                   at most 4 levels) with the polar operator and tolcon
+ *                   1e-5 (:1234, :1345); Nu as the annulus's. */
 #define GB_PRB_LAYER   0
 #define GB_PRB_ANNULUS 1
 #define GB_PRB_OBLIQUE 2
+#define GB_PRB_TAYCOU  3
 
 /* Fills *p with the reference defaults for an nr x np grid
  * (dt 1e-7, r0 0.5, rmax 1, xx 3, Ra 1e7, Pr 0.71: the PRB input deck). */
@@ -128,6 +142,10 @@ void gb_prb_default_params(gb_prb_params *p, int nr, int np);
  * r0 0.5, rmax 1, Ra 8e8, Re 1.06148e5, Pr 0.71; tolcon 1e-5 (:2093),
  * sweep limit 10000 (:1829)). */
 void gb_prb_default_params_annulus(gb_prb_params *p, int nr, int np);
+/* The Taylor-Couette defaults (velvor2dtaycouheat.f with its input.s: dt
+ * 2e-8, r0 0.5, rmax 1, Ra 6e8, Re 91927, Ta 0, Pr 0.71; tolcon 1e-5, sweep
+ * limit 500). */
+void gb_prb_default_params_taycou(gb_prb_params *p, int nr, int np);
 
 typedef struct gb_prb gb_prb;
 

@@ -22,6 +22,7 @@ ORC_ZEBRA = 1
 ORC_PRB = 0
 ORC_ANNULUS = 1
 ORC_OBLIQUE = 2   # mpkoks.f: the layer with gravity along the diagonal
+ORC_TAYCOU = 3    # velvor2dtaycouheat.f: the annulus with a moving outer cylinder
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -57,7 +58,7 @@ class PRB(C.Structure):
     _fields_ = ([("nr", C.c_int), ("np", C.c_int), ("ld", C.c_int)] +
                 [(n, C.c_double) for n in ("dt", "dr", "dp", "Ra", "Pr", "r0", "rmax", "xx")] +
                 [(n, _dp) for n in _PRB_FIELDS] +
-                [("clamp_count", C.c_long), ("variant", C.c_int), ("Re", C.c_double)])
+                [("clamp_count", C.c_long), ("variant", C.c_int), ("Re", C.c_double), ("Ta", C.c_double)])
 
 
 _AXI_FIELDS = ["phi", "omegn", "omeg", "omegp", "veln", "vel", "velp", "thetan", "theta", "thetap"]
@@ -254,15 +255,15 @@ class OraclePRB:
     and maxsweeps default to each driver's own values."""
 
     def __init__(self, nr, np_, dt, Ra, Pr, r0=0.5, rmax=1.0, xx=3.0, mode=ORC_LEX,
-                 tolcon=None, maxsweeps=None, sor=1.2, variant=ORC_PRB, Re=0.0):
+                 tolcon=None, maxsweeps=None, sor=1.2, variant=ORC_PRB, Re=0.0, Ta=0.0):
         L = lib()
         self.s = PRB()
         assert L.orc_prb_alloc(C.byref(self.s), nr, np_, nr + 2) == 0
         s = self.s
         s.dt, s.Ra, s.Pr, s.r0, s.rmax, s.xx = dt, Ra, Pr, r0, rmax, xx
-        s.variant, s.Re = variant, Re
+        s.variant, s.Re, s.Ta = variant, Re, Ta
         s.dr = (rmax - r0) / nr
-        s.dp = 2.0 * math.acos(-1.0) / np_ if variant == ORC_ANNULUS else xx / np_
+        s.dp = 2.0 * math.acos(-1.0) / np_ if variant in (ORC_ANNULUS, ORC_TAYCOU) else xx / np_
         self.mgv, self.mgu = MG(), MG()
         for mg in (self.mgv, self.mgu):
             st = L.orc_mg_init_variant(C.byref(mg), nr, np_, s.dr, s.dp, variant, r0)

@@ -165,6 +165,7 @@ int orc_mg_init_variant(orc_mg_t *mg, int nr, int np, double dr, double dp, int 
         mg->maxsweeps = 10000;
         mg->mgen = 2000000;
     }
+    if (variant == ORC_TAYCOU) mg->tolcon = 1.0e-5;   /* velvor2dtaycouheat.f:1234, :1345 */
     return ORC_OK;
 }
 
@@ -259,14 +260,14 @@ static void relax3_line(orc_mg_t *mg, int klev, int k, const double *ca,
 void orc_relax(orc_mg_t *mg, int which, int nrel, int klev, int *nconv)
 {
     const int ld = mg->ld, n1 = mg->n1[klev], n3 = mg->n3[klev];
-    const int polar = (mg->variant == ORC_ANNULUS);
+    const int polar = (mg->variant == ORC_ANNULUS || mg->variant == ORC_TAYCOU);
     double *psif = mg->psif, *rc = mg->rc, *rf = mg->rf;
     *nconv = 0;
     trans2(mg, mg->f[klev], rf, klev);
     const double hhri = 1.0 / mg->hhr[klev];
     const double hri = 1.0 / mg->hr[klev];
     const double hhpi = 1.0 / mg->hhp[klev];
-    if (polar) nrel = 3;
+    if (mg->variant == ORC_ANNULUS) nrel = 3;
 
     const int nmax = n1 + 2;
     double *buf = (double *)malloc(sizeof(double) * (size_t)nmax * 14);
@@ -660,6 +661,15 @@ void orc_prb_free(orc_prb_t *s)
     memset(s, 0, sizeof(*s));
 }
 
+/* The (r, phi) plane of the annulus drivers (velvor2dnewsch3.4.f and the
+ * Taylor-Couette velvor2dtaycouheat.f): radius terms everywhere. */
+static int prb_polar(const orc_prb_t *s) { return s->variant == ORC_ANNULUS || s->variant == ORC_TAYCOU; }
+
+/* The Taylor-Couette outer wall speed -(Ta**0.5) Ptl 0.5 rmax
+ * (velvor2dtaycouheat.f:177, :1587, :1668); ** 0.5d0 through libm pow as
+ * the compiled Fortran calls it. */
+static double taycou_wall(const orc_prb_t *s) { return -(pow(s->Ta, 0.5) * s->Pr * 0.5 * s->rmax); }
+
 /* REAL*4 constants of the reference's wall closures (PRB:865-872). */
 static const double F23 = (double)(2.0f / 3.0f);
 static const double F16 = (double)(1.0f / 6.0f);
@@ -747,7 +757,7 @@ static void cvort_derivatives(orc_prb_t *s, double *wa, double *wb, double *wc,
 static void cvort_update(orc_prb_t *s, int first)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
-    const int polar = (s->variant == ORC_ANNULUS);
+    const int polar = prb_polar(s);
     const double dri = 1.0 / s->dr, dpi = 1.0 / s->dp;
     const double Ptl = s->Pr, dt = s->dt, Ra = s->Ra, Re = s->Re;
     const double *C = s->C, *Cp = s->Cp, *uel = s->uel, *vel = s->vel;
@@ -799,7 +809,10 @@ static void cvort_update(orc_prb_t *s, int first)
 
 /* Robert filter coefficient: 0.02 in PRB (PRB:1041-1045), 0.05 in the
  * annulus driver (velvor2dnewsch3.4.f:1055, :1454). */
-static double robert(const orc_prb_t *s) { return s->variant == ORC_ANNULUS ? 0.05 : 0.02; }
+static double robert(const orc_prb_t *s)
+{
+    return s->variant == ORC_ANNULUS ? 0.05 : s->variant == ORC_TAYCOU ? 0.01 : 0.02;
+}
 
 static void *wbuf(int n, double **wa, double **wb, double **wc, double **wr, double **ws)
 {
@@ -880,7 +893,7 @@ static void temp_derivatives(orc_prb_t *s, double *wa, double *wb, double *wc,
 static void temp_update(orc_prb_t *s, int first)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
-    const int polar = (s->variant == ORC_ANNULUS);
+    const int polar = prb_polar(s);
     const double dri = 1.0 / s->dr, dpi = 1.0 / s->dp, dt = s->dt;
     const double *th = s->th, *thp = s->thp, *uel = s->uel, *vel = s->vel;
     for (int i = 1; i <= nr; ++i) {
@@ -993,6 +1006,14 @@ void orc_update(orc_prb_t *s)
         s->Bn[IX(nr, k)] = -(s->wel[IX(nr - 1, k)] / 3.0 - 3.0 * s->wel[IX(nr, k)]) / dr;
     }
     for (int k = 0; k <= np; ++k) {
+        if (s->variant == ORC_TAYCOU) {
+            /* velvor2dtaycouheat.f:1587-1590: the moving outer wall */
+            s->vel[IX(nr + 1, k)] = taycou_wall(s);
+            s->Cn[IX(0, k)] = (3.0 * s->vel[IX(1, k)] - s->vel[IX(2, k)] / 3.0) / dr;
+            s->Cn[IX(nr, k)] = (8.0 / 3.0 * s->vel[IX(nr + 1, k)] + s->vel[IX(nr - 1, k)] / 3.0 -
+                                3.0 * s->vel[IX(nr, k)]) / dr + s->vel[IX(nr + 1, k)] / s->rmax;
+            continue;
+        }
         s->Cn[IX(0, k)] = (3.0 * s->vel[IX(1, k)] - s->vel[IX(2, k)] / 3.0) / dr;
         s->Cn[IX(nr, k)] = (s->vel[IX(nr - 1, k)] / 3.0 - 3.0 * s->vel[IX(nr, k)]) / dr;
     }
@@ -1020,14 +1041,23 @@ void orc_rhsv(orc_prb_t *s)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
     const double dr = s->dr;
-    const int polar = (s->variant == ORC_ANNULUS);
+    const int polar = prb_polar(s);
     for (int i = 1; i <= nr; ++i) {
         for (int k = 0; k <= np; ++k) {
             const double Cr = (s->Cn[IX(i, k)] - s->Cn[IX(i - 1, k)]) / dr;
             if (polar) {
                 const double r = s->r0 + ((double)i - 0.5) * dr;
                 if (i == 1) s->vrh[IX(i, k)] = s->Cn[IX(1, k)] / dr + s->Cn[IX(1, k)] / r;
-                else if (i == nr) s->vrh[IX(i, k)] = -s->Cn[IX(nr - 1, k)] / dr + s->Cn[IX(nr - 1, k)] / r;
+                else if (i == nr) {
+                    s->vrh[IX(i, k)] = -s->Cn[IX(nr - 1, k)] / dr + s->Cn[IX(nr - 1, k)] / r;
+                    if (s->variant == ORC_TAYCOU) {
+                        /* velvor2dtaycouheat.f:1668-1670, hhri = hri**2.d0, rvali**2.d0 */
+                        const double velo = taycou_wall(s), rvali = 1.0 / s->rmax, hri = 1.0 / dr;
+                        const double hhri = hri * hri;
+                        s->vrh[IX(i, k)] = s->vrh[IX(i, k)] - 8.0 / 15.0 * velo * hhri + rvali * hri * velo -
+                                           4.0 / 3.0 * velo * hri * rvali + velo * (rvali * rvali);
+                    }
+                }
                 else s->vrh[IX(i, k)] = Cr + (s->Cn[IX(i, k)] + s->Cn[IX(i - 1, k)]) / r;
             } else if (i == 1) s->vrh[IX(i, k)] = s->Cn[IX(1, k)] / dr;
             else if (i == nr) s->vrh[IX(i, k)] = -s->Cn[IX(nr - 1, k)] / dr;
@@ -1042,7 +1072,7 @@ void orc_rhsv(orc_prb_t *s)
 void orc_rhsu(orc_prb_t *s)
 {
     const int ld = s->ld, nr = s->nr, np = s->np;
-    const int polar = (s->variant == ORC_ANNULUS);
+    const int polar = prb_polar(s);
     for (int i = 1; i <= nr - 1; ++i) {
         for (int k = 0; k <= np; ++k) {
             int km = k - 1;
@@ -1082,8 +1112,8 @@ int orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double *nu,
     if (solve_failed(s, st)) { if (sweeps) { sweeps[0] = sv; sweeps[1] = su; } return st; }
     orc_update(s);
     if (nu) {
-        if (s->variant == ORC_ANNULUS) {
-            /* httrans, httrans2 of velvor2dnewsch3.4.f:386-387 */
+        if (prb_polar(s)) {
+            /* httrans, httrans2 of velvor2dnewsch3.4.f:386-387 (velvor2dtaycouheat.f alike) */
             const double pi = acos(-1.0), L = log(s->r0 / s->rmax);
             nu[0] = -s->r0 * L * t1 / (2.0 * pi);
             nu[1] = -s->rmax * L * t2 / (2.0 * pi);
@@ -1127,7 +1157,7 @@ void orc_prb_cfl(const orc_prb_t *s, double *cflu, double *cflv)
             if (cfl > mu) mu = cfl;
         }
     for (int i = 1; i <= s->nr - 1; ++i) {
-        const double r = s->variant == ORC_ANNULUS ? s->r0 + ((double)i - 0.5) * s->dr : 1.0;
+        const double r = prb_polar(s) ? s->r0 + ((double)i - 0.5) * s->dr : 1.0;
         for (int k = 0; k <= s->np; ++k) {
             const double cfl = fabs(s->vel[(size_t)i + (size_t)ld * (size_t)k] * s->dt / (r * s->dp));
             if (cfl > mv) mv = cfl;
@@ -1181,7 +1211,7 @@ void orc_prb_initial(orc_prb_t *s, int kind, unsigned long long seed, double amp
             s->An[IX(i, k)] = s->Bn[IX(i, k)] = s->Cn[IX(i, k)] = 0.0;
             s->A[IX(i, k)] = s->B[IX(i, k)] = s->C[IX(i, k)] = 0.0;
             s->uel[IX(i, k)] = s->vel[IX(i, k)] = s->wel[IX(i, k)] = 0.0;
-            if (kind == 0 && s->variant == ORC_ANNULUS) {
+            if (kind == 0 && prb_polar(s)) {
                 /* velvor2dnewsch3.4.f:130-178: conduction profile 1 - ln r / ln r0
                  * with walls 0 and 1 and the ripple 0.7 T (r-rmax)/rmax (2 randno - 1),
                  * randno = 1/2 + sin(2 pi k/150)/2.  The blobs of :185-220 have
@@ -1220,13 +1250,15 @@ void orc_prb_initial(orc_prb_t *s, int kind, unsigned long long seed, double amp
                 else if (k == np) t = s->th[IX(i, 0)];
                 else {
                     double u = (double)(splitmix64(&st) >> 11) * (1.0 / 9007199254740992.0);
-                    if (s->variant == ORC_ANNULUS) t = 1.0 - log(r) / log(r0) + amp * (2.0 * u - 1.0);
+                    if (prb_polar(s)) t = 1.0 - log(r) / log(r0) + amp * (2.0 * u - 1.0);
                     else t = (r - r0) / (rmax - r0) + amp * (2.0 * u - 1.0);
                 }
                 s->th[IX(i, k)] = t;
             }
         }
     }
+    if (s->variant == ORC_TAYCOU)   /* the moving outer wall of the start, velvor2dtaycouheat.f:177 */
+        for (int k = 0; k <= np; ++k) s->vel[IX(nr + 1, k)] = taycou_wall(s);
     for (int k = 0; k <= np; ++k) {
         for (int i = 0; i <= nr + 1; ++i) {
             s->Ap[IX(i, k)] = s->A[IX(i, k)];

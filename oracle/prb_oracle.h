@@ -73,6 +73,14 @@ typedef struct {
 #define ORC_PRB     0
 #define ORC_ANNULUS 1
 #define ORC_OBLIQUE 2   /* the layer with gravity at 45 degrees (mpkoks.f:769-770, :974-975) */
+/* the annulus with a moving outer cylinder, velvor2dtaycouheat.f: the
+ * annulus's transport with Robert filter 0.01 (:605, :837), the outer wall
+ * v = -(Ta**0.5) Ptl rmax / 2 (the start :177, update :1587), its wall
+ * vorticity (8/3 v(nr+1) + v(nr-1)/3 - 3 v(nr))/dr + v(nr+1)/rmax (:1589-1590)
+ * and its term in rhsv at i = nr (:1668-1670); the multigrid of PRB (one
+ * relaxation per visit, the coarse seam reset, STOP after 500 sweeps, at
+ * most 4 levels) with the polar operator and tolcon 1e-5 (:1234, :1345). */
+#define ORC_TAYCOU  3
 
 int  orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp);
 /* Same with the variant and inner radius of the annulus driver. */
@@ -99,8 +107,9 @@ typedef struct {
     double *uel, *vel, *wel, *uelp, *velp, *welp;
     double *urh, *vrh;
     long clamp_count;                    /* "WARNING! Temp damped" count */
-    int variant;                         /* ORC_PRB or ORC_ANNULUS */
+    int variant;                         /* ORC_PRB, ORC_ANNULUS, ORC_OBLIQUE or ORC_TAYCOU */
     double Re;                           /* rotational Reynolds number (annulus) */
+    double Ta;                           /* Taylor number (ORC_TAYCOU; COMMON /val/ Gr there) */
 } orc_prb_t;
 
 int  orc_prb_alloc(orc_prb_t *s, int nr, int np, int ld);

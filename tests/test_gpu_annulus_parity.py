@@ -112,3 +112,65 @@ def test_fields_unchanged_by_layer_entry_points(oracle, P):
         o2.step()
     g2.step(2)
     assert diff_fields(o2, g2, COMPARED) == {}
+
+
+def make_taycou(O, P, nr, np_, dt, Ra, Ta, smoother, kind=0, seed=0, amp=1e-2, tolcon=None, maxsweeps=None):
+    o = O.OraclePRB(nr, np_, dt, Ra, ANN["Pr"], r0=ANN["r0"], rmax=ANN["rmax"], mode=smoother, tolcon=tolcon,
+                    maxsweeps=maxsweeps, variant=O.ORC_TAYCOU, Re=9.1927e4, Ta=Ta)
+    o.initial(kind, seed, amp)
+    from codesthesis_dir_gb300 import lib
+    g = P.PRB(nr, np_, dt=dt, r0=ANN["r0"], rmax=ANN["rmax"], Ra=Ra, Pr=ANN["Pr"], tolcon=tolcon,
+              maxsweeps=maxsweeps, smoother=smoother, variant=lib.PRB_TAYCOU, Re=9.1927e4, Ta=Ta)
+    assert g.nlev == o.mgv.nlev
+    for name in STATE_FIELDS:
+        g.set(name, np.array(o.field(name), order="F"))
+    return o, g
+
+
+@pytest.mark.parametrize("smoother", [0, 1], ids=["lex", "zebra"])
+def test_taylor_couette_routines_and_steps(oracle, P, smoother):
+    """velvor2dtaycouheat.f (GB_PRB_TAYCOU): the moving outer cylinder, its
+    wall vorticity and rhsv term, Robert filter 0.01, PRB's multigrid with the
+    polar operator; routine by routine and then graph-replayed, every field,
+    Nusselt number and sweep count equal to the oracle's."""
+    o, g = make_taycou(oracle, P, 16, 32, 1e-6, 1e6, 1e4, smoother)
+    for kt in range(1, 4):
+        st, nu, sw = o.step()
+        assert st == 0
+        (g.cvorticity1 if kt == 1 else g.cvorticity)()
+        (g.temperature1 if kt == 1 else g.temperature)()
+        t1, t2 = g.heat()
+        g.rhsv()
+        sv = g.poisson2()
+        g.rhsu()
+        su = g.poisson3()
+        g.update()
+        assert (sv, su) == (int(sw[0]), int(sw[1])), kt
+        assert nu_annulus(o, t1, t2) == (nu[0], nu[1]), kt
+        assert diff_fields(o, g) == {}, kt
+    g.kt = 3
+    nu_o, sw_o = [], []
+    for _ in range(6):
+        st, nu, sw = o.step()
+        assert st == 0
+        nu_o.append(nu.copy())
+        sw_o.append(sw.copy())
+    nu_g, sw_g = g.step(6)
+    np.testing.assert_array_equal(np.array(sw_o), sw_g)
+    np.testing.assert_array_equal(np.array(nu_o), nu_g)
+    assert diff_fields(o, g) == {}
+    assert np.all(g.get("vel")[17] == -(1e4 ** 0.5) * ANN["Pr"] * 0.5 * ANN["rmax"])
+
+
+def test_taylor_couette_four_levels_and_stop(oracle, P):
+    """At most four levels where the annulus has five, and the sweep limit
+    stops the run (the driver STOPs) on the device as in the oracle."""
+    from codesthesis_dir_gb300 import lib
+    o, g = make_taycou(oracle, P, 64, 64, 1e-6, 1e6, 1e4, 1)
+    assert g.nlev == 4
+    o, g = make_taycou(oracle, P, 16, 32, 1e-6, 1e6, 1e4, 0, tolcon=1e-30, maxsweeps=3)
+    st, nu, sw = o.step()
+    assert st == 1 and sw[0] == 3
+    with pytest.raises(lib.GBError) as ei:
+        g.step(2)
+    assert ei.value.status == lib.GB_MAXSWEEPS

@@ -25,20 +25,23 @@ SOL2 = ["thn", "th", "thp"]
 SOL3 = ["uel", "vel", "wel", "uelp", "velp", "welp"]
 
 
-@pytest.mark.parametrize("kr,kp,variant", [(20, 40, 0), (290, 1610, 0), (20, 40, 1), (420, 3600, 1), (20, 40, 2)],
+@pytest.mark.parametrize("kr,kp,variant", [(20, 40, 0), (290, 1610, 0), (20, 40, 1), (420, 3600, 1), (20, 40, 2),
+                                           (20, 40, 3)],
                          ids=["small-bounds", "reference-bounds", "annulus-small-bounds", "annulus-reference-bounds",
-                              "oblique-small-bounds"])
+                              "oblique-small-bounds", "taycou-small-bounds"])
 def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
     """variant 0: PRB; 1: the annulus (velvor2dnewsch3.4.f); 2: mpkoks.f's
-    oblique gravity (the same names, gb_prb_bind_variant(2))."""
+    oblique gravity (the same names, gb_prb_bind_variant(2)); 3: the
+    Taylor-Couette driver (velvor2dtaycouheat.f, Ta in /val/'s Gr slot)."""
     L = gblib
     nr, np_ = 16, 32
     dt, Ra, Pr, r0, rmax, xx, Re = 1e-4, 1e5, 0.71, 0.5, 1.0, 3.0, 1e4
-    ann = variant == 1
+    ann = variant in (1, 3)
+    Ta = 1e4 if variant == 3 else 0.0
     if ann:
         dt, Ra = 1e-6, 1e6
-    tol, maxsw = (10e-6, 10000) if ann else (2e-6, 500)
-    o = oracle.OraclePRB(nr, np_, dt, Ra, Pr, r0=r0, rmax=rmax, xx=xx, variant=variant, Re=Re)
+    tol, maxsw = (10e-6, 10000) if variant == 1 else (1e-5, 500) if variant == 3 else (2e-6, 500)
+    o = oracle.OraclePRB(nr, np_, dt, Ra, Pr, r0=r0, rmax=rmax, xx=xx, variant=variant, Re=Re, Ta=Ta)
     o.initial(0, 0, 0.0)  # the reference's own initial profile (PRB:137-186, annulus :130-178)
     S = (kr + 1) * (kp + 1)
     sol1 = np.zeros(9 * S)
@@ -54,7 +57,7 @@ def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
         for i, nm in enumerate(names):
             view(blk, i)[: nr + 2, : np_ + 1] = np.array(o.field(nm))
     num = Num(dt, o.s.dr, 0.0, o.s.dp, nr, 1, np_)
-    val = np.array([Ra, Re if ann else 0.0, Pr, 0.0])
+    val = np.array([Ra, Re if ann else 0.0, Pr, Ta])
     radius = np.array([r0, rmax])
     L.gb_prb_bind_bounds(kr, kp)
     L.gb_prb_bind_tolerance(tol, maxsw)
