@@ -23,6 +23,7 @@ ORC_PRB = 0
 ORC_ANNULUS = 1
 ORC_OBLIQUE = 2   # mpkoks.f: the layer with gravity along the diagonal
 ORC_TAYCOU = 3    # velvor2dtaycouheat.f: the annulus with a moving outer cylinder
+ORC_TANK = 4      # velvor2dhorconvtank.f: the layer closed by side walls in x
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -46,7 +47,7 @@ class MG(C.Structure):
         ("mgen", C.c_long),
         ("scratch_v", _dp), ("scratch_f", _dp),
         ("last_sweeps", C.c_int), ("last_resmax", C.c_double),
-        ("variant", C.c_int), ("r0", C.c_double),
+        ("variant", C.c_int), ("r0", C.c_double), ("xwall", C.c_int),
     ]
 
 
@@ -145,6 +146,12 @@ def lib():
         L.orc_prb_step.argtypes = [C.POINTER(PRB), C.POINTER(MG), C.POINTER(MG), C.c_int, _dp, _ip]
         L.orc_prb_step.restype = C.c_int
         L.orc_prb_initial.argtypes = [C.POINTER(PRB), C.c_int, C.c_ulonglong, C.c_double]
+        L.orc_tank_initial.argtypes = [C.POINTER(PRB)]
+        for nm in ("orc_tank_update", "orc_tank_rhsv", "orc_tank_rhsu"):
+            getattr(L, nm).argtypes = [C.POINTER(PRB)]
+        for nm in ("orc_tank_cvorticity", "orc_tank_temperature"):
+            getattr(L, nm).argtypes = [C.POINTER(PRB), C.c_int]
+        L.orc_tank_heat.argtypes = [C.POINTER(PRB), _dp, _dp]
         L.orc_prb_diag_accum.argtypes = [C.POINTER(PRB), C.c_int, _dp, _dp, _dp, _dp]
         L.orc_prb_cfl.argtypes = [C.POINTER(PRB), _dp, _dp]
         L.orc_prb_zmtm.argtypes = [C.POINTER(PRB), _dp, _dp, _dp, _dp, _dp]
@@ -309,15 +316,25 @@ class OraclePRB:
     def np(self):
         return self.s.np
 
+    @property
+    def ncol(self):
+        """Columns of a field: np+1, or np+2 in the tank (ghost column np+1)."""
+        return self.s.np + (2 if self.s.variant == ORC_TANK else 1)
+
     def field(self, name) -> np.ndarray:
-        """A (ld, np+1) Fortran-ordered view of a state field (i fastest)."""
+        """A (ld, ncol) Fortran-ordered view of a state field (i fastest)."""
         p = getattr(self.s, name)
-        n = self.s.ld * (self.s.np + 1)
+        n = self.s.ld * self.ncol
         flat = np.ctypeslib.as_array(p, shape=(n,))
-        return flat.reshape((self.s.np + 1, self.s.ld)).T
+        return flat.reshape((self.ncol, self.s.ld)).T
 
     def initial(self, kind=1, seed=0, amp=1e-3):
-        lib().orc_prb_initial(C.byref(self.s), kind, seed, amp)
+        """kind 0: the driver's own start; 1: conduction plus seeded noise.
+        The tank has only its own start (velvor2dhorconvtank.f:70-140)."""
+        if self.s.variant == ORC_TANK:
+            lib().orc_tank_initial(C.byref(self.s))
+        else:
+            lib().orc_prb_initial(C.byref(self.s), kind, seed, amp)
         self.kt = 0
 
     def step(self):

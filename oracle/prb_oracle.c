@@ -166,6 +166,10 @@ int orc_mg_init_variant(orc_mg_t *mg, int nr, int np, double dr, double dp, int 
         mg->mgen = 2000000;
     }
     if (variant == ORC_TAYCOU) mg->tolcon = 1.0e-5;   /* velvor2dtaycouheat.f:1234, :1345 */
+    if (variant == ORC_TANK) {                          /* velvor2dhorconvtank.f:1163, :1264 */
+        mg->tolcon = 5.0e-6;
+        mg->xwall = 1;
+    }
     return ORC_OK;
 }
 
@@ -234,7 +238,7 @@ static void relax3_line(orc_mg_t *mg, int klev, int k, const double *ca,
     double *psif = mg->psif;
     const double *rf = mg->rf;
     int ka = k + 1, km = k - 1;
-    if (k == n3) ka = 1;
+    if (k == n3) ka = mg->xwall ? 0 : 1;
     for (int i = 1; i <= n1 - 1; ++i) {
         wa[i - 1] = ca[i];
         wb[i - 1] = cb[i];
@@ -244,7 +248,7 @@ static void relax3_line(orc_mg_t *mg, int klev, int k, const double *ca,
     orc_tdma(wa, wb, wc, ws, wr, n1 - 1);
     for (int i = 1; i <= n1 - 1; ++i) {
         psif[IX(i, k)] = ws[i - 1];
-        if (k == n3) psif[IX(i, 0)] = psif[IX(i, k)];
+        if (k == n3) psif[IX(i, 0)] = mg->xwall ? 0.0 : psif[IX(i, k)];
     }
 }
 
@@ -344,15 +348,16 @@ void orc_relax(orc_mg_t *mg, int which, int nrel, int klev, int *nconv)
 
     double resmax = 0.0;
     int anynan = 0;
+    const int klast = (mg->xwall && which == 2) ? n3 - 1 : n3;   /* the tank's v walls k = 0, n3 */
     for (int irel = 1; irel <= nrel; ++irel) {
         if (mg->mode == ORC_LEX) {
-            for (int k = 1; k <= n3; ++k) {
+            for (int k = 1; k <= klast; ++k) {
                 if (which == 2) relax2_line(mg, klev, k, ca, cb, cc, cd, ce, rvq, hhpi, wa, wb, wc, wd, we, wr, ws);
                 else relax3_line(mg, klev, k, ca, cb, cc, rvq, hhpi, wa, wb, wc, wr, ws);
             }
         } else {
             for (int parity = 1; parity >= 0; --parity) {
-                for (int k = 1; k <= n3; ++k) {
+                for (int k = 1; k <= klast; ++k) {
                     if ((k & 1) != parity) continue;
                     if (which == 2) relax2_line(mg, klev, k, ca, cb, cc, cd, ce, rvq, hhpi, wa, wb, wc, wd, we, wr, ws);
                     else relax3_line(mg, klev, k, ca, cb, cc, rvq, hhpi, wa, wb, wc, wr, ws);
@@ -362,9 +367,9 @@ void orc_relax(orc_mg_t *mg, int which, int nrel, int klev, int *nconv)
         /* residual and its max norm, PRB:2306-2357 / PRB:2553-2587
          * (annulus velvor2dnewsch3.4.f:2300-2346 / :2546-2579) */
         resmax = 0.0;
-        for (int k = 1; k <= n3; ++k) {
+        for (int k = 1; k <= klast; ++k) {
             int ka = k + 1, km = k - 1;
-            if (k == n3) ka = 1;
+            if (k == n3) ka = mg->xwall ? 0 : 1;
             if (which == 2) {
                 for (int i = 1; i <= n1; ++i) {
                     double temp;
@@ -613,12 +618,19 @@ int orc_poisson(orc_mg_t *mg, int which, double *psi, double *psip,
         if (nconv == 1) {
             for (int i = 0; i <= imax; ++i)
                 for (int k = 0; k <= np; ++k) psip[IO(i, k)] = psi[IO(i, k)];
+            /* the tank: v on k = 1..np-1, u on k = 1..np (velvor2dhorconvtank.f:1032, :1129) */
+            const int k0 = mg->xwall ? 1 : 0, k1 = mg->xwall ? (which == 2 ? np - 1 : np) : np;
             for (int i = 1; i <= imax - 1; ++i)
-                for (int k = 0; k <= np; ++k) psi[IO(i, k)] = psif[IX(i, k)];
+                for (int k = k0; k <= k1; ++k) psi[IO(i, k)] = psif[IX(i, k)];
             for (int k = 0; k <= np; ++k) {
                 psi[IO(0, k)] = 0.0;
                 psi[IO(imax, k)] = 0.0;
             }
+            if (mg->xwall)
+                for (int i = 0; i <= imax; ++i) {
+                    psi[IO(i, 0)] = 0.0;
+                    psi[IO(i, which == 2 ? np : np + 1)] = 0.0;
+                }
             if (sweeps) *sweeps = sweep;
             mg->last_sweeps = sweep;
             return ORC_OK;
@@ -638,7 +650,7 @@ int orc_prb_alloc(orc_prb_t *s, int nr, int np, int ld)
     s->nr = nr;
     s->np = np;
     s->ld = ld;
-    size_t sz = (size_t)ld * (size_t)(np + 1);
+    size_t sz = (size_t)ld * (size_t)(np + 2);   /* the tank's T and u have a ghost column np+1 */
     double **f[] = {&s->An, &s->A, &s->Ap, &s->Bn, &s->B, &s->Bp, &s->Cn, &s->C, &s->Cp,
                     &s->thn, &s->th, &s->thp, &s->uel, &s->vel, &s->wel, &s->uelp,
                     &s->velp, &s->welp, &s->urh, &s->vrh};
@@ -1092,10 +1104,40 @@ static int solve_failed(const orc_prb_t *s, int st)
     return st != ORC_OK && !(s->variant == ORC_ANNULUS && st == ORC_MAXSWEEPS);
 }
 
+static int tank_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double *nu, int *sweeps)
+{
+    double t1, t2;
+    int sv = 0, su = 0, st;
+    orc_tank_cvorticity(s, kt == 1);
+    orc_tank_temperature(s, kt == 1);
+    orc_tank_heat(s, &t1, &t2);
+    orc_tank_rhsv(s);
+    st = orc_poisson(mgv, 2, s->vel, s->velp, s->vrh, s->ld, &sv);
+    if (st != ORC_OK) { if (sweeps) { sweeps[0] = sv; sweeps[1] = 0; } return st; }
+    orc_tank_rhsu(s);
+    st = orc_poisson(mgu, 3, s->uel, s->uelp, s->urh, s->ld, &su);
+    if (st != ORC_OK) { if (sweeps) { sweeps[0] = sv; sweeps[1] = su; } return st; }
+    orc_tank_update(s);
+    if (nu) {
+        /* velvor2dhorconvtank.f:197-198, :209-210: the first step overwrites
+         * httrans with 2 trans2 and leaves httrans2 at zero */
+        if (kt == 1) {
+            nu[0] = t2 * 2.0;
+            nu[1] = 0.0;
+        } else {
+            nu[0] = t1 * 2.0;
+            nu[1] = t2 * 2.0;
+        }
+    }
+    if (sweeps) { sweeps[0] = sv; sweeps[1] = su; }
+    return ORC_OK;
+}
+
 int orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double *nu, int *sweeps)
 {
     double t1, t2;
     int sv = 0, su = 0, st;
+    if (s->variant == ORC_TANK) return tank_step(s, mgv, mgu, kt, nu, sweeps);
     if (kt == 1) {
         orc_cvorticity1(s);
         orc_temperature1(s);

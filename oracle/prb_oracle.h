@@ -68,6 +68,13 @@ typedef struct {
      * relaxations per call, no reset of the coarse seam of rc, level cap 5 */
     int variant;
     double r0;
+    /* ORC_TANK (velvor2dhorconvtank.f:1163-1303): side walls in x.  relax2
+     * runs and measures lines k = 1..n3-1 (the v walls k = 0, n3 are not
+     * relaxed); relax3's last line k = n3 takes k = 0 (zero) as its k+1
+     * neighbour and resets psif(0) to zero instead of copying the seam;
+     * tolcon 5e-6; the final update writes v on k = 1..np-1 and zeroes
+     * k = 0, np, u on k = 1..np and zeroes k = 0, np+1. */
+    int xwall;
 } orc_mg_t;
 
 #define ORC_PRB     0
@@ -81,6 +88,9 @@ typedef struct {
  * relaxation per visit, the coarse seam reset, STOP after 500 sweeps, at
  * most 4 levels) with the polar operator and tolcon 1e-5 (:1234, :1345). */
 #define ORC_TAYCOU  3
+/* the horizontal-convection tank, velvor2dhorconvtank.f (tank_oracle.c):
+ * the layer closed by side walls in x */
+#define ORC_TANK    4
 
 int  orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp);
 /* Same with the variant and inner radius of the annulus driver. */
@@ -150,6 +160,15 @@ void orc_prb_diag_accum(const orc_prb_t *s, int kt, double *msqT, double *mT, do
 void orc_prb_cfl(const orc_prb_t *s, double *cflu, double *cflv);
 void orc_prb_zmtm(const orc_prb_t *s, const double *msqT, const double *mT, const double *msqU,
                   const double *msqV, double *out);
+
+/* The tank (tank_oracle.c); the state's fields have np+2 columns. */
+void orc_tank_cvorticity(orc_prb_t *s, int first);
+void orc_tank_temperature(orc_prb_t *s, int first);
+void orc_tank_heat(const orc_prb_t *s, double *trans1, double *trans2);
+void orc_tank_update(orc_prb_t *s);
+void orc_tank_rhsv(orc_prb_t *s);
+void orc_tank_rhsu(orc_prb_t *s);
+void orc_tank_initial(orc_prb_t *s);
 
 /* Initial conditions.  kind 0: the reference's own deterministic profile
  * (PRB:137-186; for ORC_ANNULUS the conduction profile 1 - ln r / ln r0
