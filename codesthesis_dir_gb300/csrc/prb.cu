@@ -26,7 +26,7 @@
 // Matrix factors of the compact-derivative line solves (one thread).
 // ---------------------------------------------------------------------------
 __global__ void k_transport_factors(int nr, int np, double *fac_r1, double *fac_x,
-                                    double *fac_rT, double *work)
+                                    double *fac_rT, double *work, double *fac_xw1, double *fac_xw2)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int nmax = (nr > np ? nr : np) + 2;
@@ -42,6 +42,13 @@ __global__ void k_transport_factors(int nr, int np, double *fac_r1, double *fac_
     b[0] = 1.0; c[0] = 2.0;
     a[nr - 1] = 2.0; b[nr - 1] = 1.0;
     factor_tdma(a, b, c, nr, fac_rT);
+    if (fac_xw1) {
+        // the tank's x-lines: (1,4,1) over k = 1..np-1 (C points) and over the
+        // cells k = 1..np (T), velvor2dhorconvtank.f:355-369, :616-624
+        for (int j = 0; j < np; ++j) { a[j] = 1.0; b[j] = 4.0; c[j] = 1.0; }
+        factor_tdma(a, b, c, np - 1, fac_xw1);
+        factor_tdma(a, b, c, np, fac_xw2);
+    }
 }
 
 // REAL*4 literals 2./3. and 1./6. of PRB:865-872, as the doubles they widen to.
@@ -277,7 +284,7 @@ __global__ void k_temp_update(PrbDev d, int first)
 
 // Wall heat fluxes, PRB:1452-1500.  The per-column five-point derivatives are
 // formed in parallel; one thread then sums them in the reference's order.
-__global__ void k_heat(PrbDev d)
+__global__ void k_heat(PrbDev d, int k0, int k1)
 {
     extern __shared__ double sh[];
     if (*d.abort) return;
@@ -296,7 +303,7 @@ __global__ void k_heat(PrbDev d)
     __syncthreads();
     if (threadIdx.x == 0) {
         double t1 = 0.0, t2 = 0.0;
-        for (int k = 1; k <= np; ++k) {
+        for (int k = k0; k <= k1; ++k) {
             const int ka = (k == np) ? 1 : k + 1;
             t1 = t1 + P0[k] + P0[ka];
             t2 = t2 + P1[k] + P1[ka];
@@ -438,13 +445,15 @@ __global__ void k_update(PrbDev d)
 // Nu = heat * c / div: c = rmax - r0, div = xx in PRB (PRB:386-388);
 // c = -r0 ln(r0/rmax) (inner) and -rmax ln(r0/rmax) (outer), div = 2 pi in
 // the annulus (velvor2dnewsch3.4.f:386-387).
-__global__ void k_record(PrbDev d, double c1, double c2, double div)
+// swap: the tank's first step stores 2 trans2 in httrans and leaves httrans2
+// at zero (velvor2dhorconvtank.f:197-198).
+__global__ void k_record(PrbDev d, double c1, double c2, double div, int swap)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int s = *d.step_index;
     if (s < d.hist_cap) {
-        d.nu_hist[2 * s + 0] = d.heat[0] * c1 / div;
-        d.nu_hist[2 * s + 1] = d.heat[1] * c2 / div;
+        d.nu_hist[2 * s + 0] = swap ? d.heat[1] * c2 / div : d.heat[0] * c1 / div;
+        d.nu_hist[2 * s + 1] = swap ? 0.0 : d.heat[1] * c2 / div;
         d.sweep_hist[2 * s + 0] = d.mg_status[1];
         d.sweep_hist[2 * s + 1] = d.mg_status[3];
     }
@@ -489,6 +498,7 @@ static const int TPB = 256;
 
 int prb_launch_cvorticity(gb_prb *h, int first, cudaStream_t s)
 {
+    if (h->dev.tank) return tank_launch_cvorticity(h, first, s);
     PrbDev &d = h->dev;
     k_cvort_deriv_r<<<gb_ceil_div(d.np + 1, 64), 64, 0, s>>>(d);
     k_cvort_deriv_x<<<gb_ceil_div(d.nr - 1, 64), 64, 0, s>>>(d);
@@ -501,6 +511,7 @@ int prb_launch_cvorticity(gb_prb *h, int first, cudaStream_t s)
 
 int prb_launch_temperature(gb_prb *h, int first, cudaStream_t s)
 {
+    if (h->dev.tank) return tank_launch_temperature(h, first, s);
     PrbDev &d = h->dev;
     k_temp_deriv_r<<<gb_ceil_div(d.np + 1, 64), 64, 0, s>>>(d);
     k_temp_deriv_x<<<gb_ceil_div(d.nr, 64), 64, 0, s>>>(d);
@@ -514,13 +525,16 @@ int prb_launch_temperature(gb_prb *h, int first, cudaStream_t s)
 int prb_launch_heat(gb_prb *h, cudaStream_t s)
 {
     PrbDev &d = h->dev;
-    k_heat<<<1, 256, 2 * (d.np + 1) * sizeof(double), s>>>(d);
+    // the tank integrates over k = np/2..np-1 (velvor2dhorconvtank.f:778)
+    if (d.tank) k_heat<<<1, 256, 2 * (d.np + 1) * sizeof(double), s>>>(d, d.np / 2, d.np - 1);
+    else k_heat<<<1, 256, 2 * (d.np + 1) * sizeof(double), s>>>(d, 1, d.np);
     h->launches += 1;
     return GB_OK;
 }
 
 int prb_launch_rhs(gb_prb *h, int do_v, int do_u, cudaStream_t s)
 {
+    if (h->dev.tank) return tank_launch_rhs(h, do_v, do_u, s);
     PrbDev &d = h->dev;
     k_rhs<<<gb_ceil_div((size_t)d.nr * (d.np + 1), TPB), TPB, 0, s>>>(d, do_v, do_u);
     h->launches += 1;
@@ -529,6 +543,7 @@ int prb_launch_rhs(gb_prb *h, int do_v, int do_u, cudaStream_t s)
 
 int prb_launch_update(gb_prb *h, cudaStream_t s, bool diag)
 {
+    if (h->dev.tank) return tank_launch_update(h, s);
     PrbDev &d = h->dev;
     if (diag && d.diag)
         k_update<true><<<gb_ceil_div((size_t)(d.nr + 2) * (d.np + 1), TPB), TPB, 0, s>>>(d);
@@ -538,16 +553,20 @@ int prb_launch_update(gb_prb *h, cudaStream_t s, bool diag)
     return GB_OK;
 }
 
-int prb_launch_record(gb_prb *h, cudaStream_t s)
+int prb_launch_record(gb_prb *h, cudaStream_t s, int first)
 {
     double c1 = h->p.rmax - h->p.r0, c2 = c1, div = h->p.xx;
+    if (h->p.variant == GB_PRB_TANK) {
+        c1 = c2 = 2.0;   // httrans = 2 trans (velvor2dhorconvtank.f:209-210)
+        div = 1.0;
+    }
     if (h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU) {
         const double L = log(h->p.r0 / h->p.rmax);
         c1 = -h->p.r0 * L;
         c2 = -h->p.rmax * L;
         div = 2.0 * acos(-1.0);
     }
-    k_record<<<1, 32, 0, s>>>(h->dev, c1, c2, div);
+    k_record<<<1, 32, 0, s>>>(h->dev, c1, c2, div, (h->p.variant == GB_PRB_TANK && first) ? 1 : 0);
     h->launches += 1;
     return GB_OK;
 }
@@ -584,6 +603,20 @@ extern "C" void gb_prb_default_params_annulus(gb_prb_params *p, int nr, int np)
     p->Pr = 0.71;
     p->tolcon = 10e-6;
     p->maxsweeps = 10000;
+}
+
+extern "C" void gb_prb_default_params_tank(gb_prb_params *p, int nr, int np)
+{
+    gb_prb_default_params(p, nr, np);
+    p->variant = GB_PRB_TANK;
+    p->dt = 5e-8;
+    p->r0 = 0.5;
+    p->rmax = 1.5;
+    p->xx = 3.1;
+    p->Ra = 8.63e7;
+    p->Pr = 10.0;
+    p->tolcon = 5e-6;
+    p->maxsweeps = 500;
 }
 
 extern "C" void gb_prb_default_params_taycou(gb_prb_params *p, int nr, int np)
@@ -628,6 +661,7 @@ int prb_refresh_scalars(gb_prb *h)
     d.polar = h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU;
     d.oblique = h->p.variant == GB_PRB_OBLIQUE;
     d.taycou = h->p.variant == GB_PRB_TAYCOU;
+    d.tank = h->p.variant == GB_PRB_TANK;
     d.rmax = h->p.rmax;
     d.velo = d.taycou ? -(pow(h->p.Ta, 0.5) * h->p.Pr * 0.5 * h->p.rmax) : 0.0;
     d.robert = h->p.variant == GB_PRB_ANNULUS ? 0.05 : d.taycou ? 0.01 : 0.02;
@@ -652,13 +686,17 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     const int nlev = prb_mg_levels(nr, p->variant);
     if (nlev_out) *nlev_out = nlev;
     if (p->variant != GB_PRB_LAYER && p->variant != GB_PRB_ANNULUS && p->variant != GB_PRB_OBLIQUE &&
-        p->variant != GB_PRB_TAYCOU) {
+        p->variant != GB_PRB_TAYCOU && p->variant != GB_PRB_TANK) {
         gb_set_error("gb_prb_create: unknown variant %d", p->variant);
         return GB_ERR_INVALID;
     }
     if ((p->variant == GB_PRB_ANNULUS || p->variant == GB_PRB_TAYCOU) &&
         !(p->r0 > 0.0 && p->rmax > p->r0 && p->Re != 0.0 && p->Ta >= 0.0)) {
         gb_set_error("gb_prb_create: the annulus needs 0 < r0 < rmax and Re != 0 (r0=%g rmax=%g Re=%g)", p->r0, p->rmax, p->Re);
+        return GB_ERR_INVALID;
+    }
+    if (p->variant == GB_PRB_TANK && p->precision != GB_PRB_FP64) {
+        gb_set_error("gb_prb_create: the tank runs in FP64 only");
         return GB_ERR_INVALID;
     }
     if (nr < 4 || np < 4 || (np & 1) || nlev < 1 || nr > 8192 || np > 65536) {
@@ -672,7 +710,8 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     d.nr = nr;
     d.np = np;
     d.ld = nr + 2;
-    h->fsz = (size_t)d.ld * (size_t)(np + 1);
+    h->ncol = p->variant == GB_PRB_TANK ? np + 2 : np + 1;   // the tank's T and u ghost column np+1
+    h->fsz = (size_t)d.ld * (size_t)h->ncol;
     h->dr_set = dr;
     h->dp_set = dp;
     prb_refresh_scalars(h);
@@ -681,17 +720,22 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     cudaMemset(h->fields, 0, sizeof(double) * h->fsz * GB_F_COUNT);
     for (int f = 0; f < GB_F_COUNT; ++f) d.f[f] = h->fields + (size_t)f * h->fsz;
     // factors + small device state
-    const size_t nfac = 3 * (size_t)nr + (6 * (size_t)(np + 1) + 3) + 3 * (size_t)nr + 3 * ((size_t)(nr > np ? nr : np) + 2);
+    const size_t nfac = 3 * (size_t)nr + (6 * (size_t)(np + 1) + 3) + 3 * (size_t)nr + 3 * ((size_t)(nr > np ? nr : np) + 2) +
+                        6 * ((size_t)np + 1);
     e = cudaMalloc(&h->factors, sizeof(double) * nfac);
     if (e != cudaSuccess) { gb_prb_destroy(h); gb_set_error("gb_prb_create: factor alloc"); return GB_ERR_ALLOC; }
     double *fr1 = h->factors;
     double *fx = fr1 + 3 * (size_t)nr;
     double *frT = fx + 6 * (size_t)(np + 1) + 3;
     double *work = frT + 3 * (size_t)nr;
+    double *fxw1 = work + 3 * ((size_t)(nr > np ? nr : np) + 2);
+    double *fxw2 = fxw1 + 3 * ((size_t)np + 1);
     d.fac_r1 = fr1;
     d.fac_x = fx;
     d.fac_rT = frT;
-    k_transport_factors<<<1, 1>>>(nr, np, fr1, fx, frT, work);
+    d.fac_xw1 = fxw1;
+    d.fac_xw2 = fxw2;
+    k_transport_factors<<<1, 1>>>(nr, np, fr1, fx, frT, work, d.tank ? fxw1 : nullptr, fxw2);
     e = cudaMalloc(&h->small, 4096);
     if (e != cudaSuccess) { gb_prb_destroy(h); gb_set_error("gb_prb_create: small alloc"); return GB_ERR_ALLOC; }
     cudaMemset(h->small, 0, 4096);
@@ -743,7 +787,7 @@ extern "C" int gb_prb_set_field(gb_prb *h, int field, const double *host, int ld
         return GB_ERR_INVALID;
     }
     GB_CUDA_TRY(cudaMemcpy2DAsync(h->dev.f[field], sizeof(double) * h->dev.ld, host, sizeof(double) * (size_t)ld,
-                                  sizeof(double) * (h->dev.nr + 2), h->dev.np + 1, cudaMemcpyHostToDevice, h->stream));
+                                  sizeof(double) * (h->dev.nr + 2), h->ncol, cudaMemcpyHostToDevice, h->stream));
     GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return GB_OK;
 }
@@ -755,7 +799,7 @@ extern "C" int gb_prb_get_field(gb_prb *h, int field, double *host, int ld)
         return GB_ERR_INVALID;
     }
     GB_CUDA_TRY(cudaMemcpy2DAsync(host, sizeof(double) * (size_t)ld, h->dev.f[field], sizeof(double) * h->dev.ld,
-                                  sizeof(double) * (h->dev.nr + 2), h->dev.np + 1, cudaMemcpyDeviceToHost, h->stream));
+                                  sizeof(double) * (h->dev.nr + 2), h->ncol, cudaMemcpyDeviceToHost, h->stream));
     GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return GB_OK;
 }
@@ -867,7 +911,7 @@ static void prb_enqueue_step(gb_prb *h, int first, cudaStream_t s)
     prb_launch_rhs(h, 1, 1, s);
     prb_launch_mg(h, 1, 1, s);
     prb_launch_update(h, s, true);
-    prb_launch_record(h, s);
+    prb_launch_record(h, s, first);
 }
 
 static int prb_build_graph(gb_prb *h, int first, cudaGraphExec_t *exec)
@@ -1032,6 +1076,10 @@ extern "C" int gb_prb_diag_enable(gb_prb *h, int on)
 {
     if (!h) { gb_set_error("gb_prb_diag_enable: null handle"); return GB_ERR_INVALID; }
     PrbDev &d = h->dev;
+    if (on && h->dev.tank) {
+        gb_set_error("gb_prb_diag_enable: the tank has no device diagnostics");
+        return GB_ERR_INVALID;
+    }
     if (!on) {
         if (h->diag_buf) {
             GB_CUDA_TRY(cudaStreamSynchronize(h->stream));

@@ -81,6 +81,7 @@ DropIn &g()
             if (strcmp(s, "annulus") == 0 || strcmp(s, "1") == 0) d.variant = GB_PRB_ANNULUS;
             if (strcmp(s, "oblique") == 0 || strcmp(s, "2") == 0) d.variant = GB_PRB_OBLIQUE;
             if (strcmp(s, "taycou") == 0 || strcmp(s, "3") == 0) d.variant = GB_PRB_TAYCOU;
+            if (strcmp(s, "tank") == 0 || strcmp(s, "4") == 0) d.variant = GB_PRB_TANK;
         }
     }
     return d;
@@ -142,6 +143,8 @@ int ensure(int nr, int np, double dr, double dp)
         p.r0 = r0;
         p.rmax = rmax;
         p.Re = Re;
+    } else if (d.variant == GB_PRB_TANK) {
+        gb_prb_default_params_tank(&p, nr, np);
     } else {
         gb_prb_default_params(&p, nr, np);
         p.variant = d.variant;   // GB_PRB_LAYER or GB_PRB_OBLIQUE
@@ -286,8 +289,10 @@ void gb_prb_bind_common(double *sol1, double *sol2, double *sol3, void *num, dou
 void gb_prb_bind_variant(int variant)
 {
     std::lock_guard<std::mutex> lk(g().mu);
-    g().variant = (variant == GB_PRB_ANNULUS || variant == GB_PRB_OBLIQUE || variant == GB_PRB_TAYCOU) ? variant
-                                                                                                   : GB_PRB_LAYER;
+    g().variant = (variant == GB_PRB_ANNULUS || variant == GB_PRB_OBLIQUE || variant == GB_PRB_TAYCOU ||
+                   variant == GB_PRB_TANK)
+                      ? variant
+                      : GB_PRB_LAYER;
 }
 
 void gb_prb_bind_radius(double *radius)

@@ -32,6 +32,7 @@ struct MgEq {
     int polar;           // the (r, phi) operator (annulus and Taylor-Couette)
     int nrelax;          // relaxations per relax call: 3 in the annulus, else 1
     int seam_keep;       // the annulus's corser keeps the coarse seam residual
+    int xwall;           // the tank: side walls in x (velvor2dhorconvtank.f:1032-1303)
     int stop_on_max;     // the sweep limit fails the step (PRB's STOP) or only is reported
     double r0;
     double tolcon, sor;
@@ -50,6 +51,8 @@ struct PrbDev {
     int polar;           // GB_PRB_ANNULUS or GB_PRB_TAYCOU: the (r, phi) plane
     int oblique;         // GB_PRB_OBLIQUE
     int taycou;          // GB_PRB_TAYCOU: the moving outer wall
+    int tank;            // GB_PRB_TANK: side walls in x, np+2 columns per field
+    const double *fac_xw1, *fac_xw2;   // the tank's tdma factors along x, n = np-1 and np
     double velo;         // its speed -(Ta**0.5) Ptl rmax / 2 (host libm pow)
     double rmax;
     double robert;       // Robert filter coefficient: 0.02 layer, 0.05 annulus, 0.01 Taylor-Couette
@@ -91,6 +94,7 @@ struct gb_prb {
     cudaGraphExec_t graph_exec = nullptr, graph_exec1 = nullptr;
     gb_prb_params graph_scalars;
     long long launches = 0, launches_per_step = 0;
+    int ncol = 0;                 // columns per field: np+1, np+2 in the tank
     double *diag_buf = nullptr;   // 4 running means + kt + CFL history (hist_cap slots)
     int diag_cap = 0;
     int steps_done = 0;
@@ -101,3 +105,8 @@ int prb_mg_create(gb_prb *h);
 void prb_mg_destroy(gb_prb *h);
 int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s);
 int prb_refresh_scalars(gb_prb *h);
+// the tank's transport (tank.cu)
+int tank_launch_cvorticity(gb_prb *h, int first, cudaStream_t s);
+int tank_launch_temperature(gb_prb *h, int first, cudaStream_t s);
+int tank_launch_rhs(gb_prb *h, int do_v, int do_u, cudaStream_t s);
+int tank_launch_update(gb_prb *h, cudaStream_t s);

@@ -116,7 +116,8 @@ __device__ __forceinline__ void mg_line(const MgEq &E, const MgLevel &L, int k)
     double *psif = E.psif;
     const double *f = L.f;
     const double hhpi = L.hhpi;
-    const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
+    // the tank's last u line takes the zero k = 0 as its wall (velvor2dhorconvtank.f:1275)
+    const int ka = (k == n3) ? (E.xwall ? 0 : 1) : k + 1, km = k - 1;
     const bool polar = E.polar;
     const double *rvq = L.rvq;
     auto rhs = [&](int j) -> double {
@@ -129,7 +130,7 @@ __device__ __forceinline__ void mg_line(const MgEq &E, const MgLevel &L, int k)
     if (E.which == 2) apply_pdma_rhs(L.fac, n1, psif + GIX(1, k, ld), 1, rhs);
     else apply_tdma_rhs(L.fac, n1 - 1, psif + GIX(1, k, ld), 1, rhs);
     if (k == n3)
-        for (int i = 1; i <= nrow; ++i) psif[GIX(i, 0, ld)] = psif[GIX(i, k, ld)];
+        for (int i = 1; i <= nrow; ++i) psif[GIX(i, 0, ld)] = E.xwall ? 0.0 : psif[GIX(i, k, ld)];
 }
 
 // relax2 / relax3: line sweeps (one with nrel = 1; three in the annulus),
@@ -147,14 +148,19 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
     double *psif = E.psif, *rc = E.rc;
     const double *f = L.f;
     const int nrel = E.nrelax;
+    // the tank's v lines stop short of its wall k = n3 (velvor2dhorconvtank.f:1170, :1216)
+    const int klast = (E.xwall && E.which == 2) ? n3 - 1 : n3;
     for (int irel = 0; irel < nrel; ++irel) {
         if (E.mode == GB_SMOOTHER_LEX) {
             if (threadIdx.x == 0)
-                for (int k = 1; k <= n3; ++k) mg_line(E, L, k);
+                for (int k = 1; k <= klast; ++k) mg_line(E, L, k);
             __syncthreads();
         } else {
             for (int parity = 1; parity >= 0; --parity) {
-                for (int t = threadIdx.x; t < n3 / 2; t += blockDim.x) mg_line(E, L, 2 * t + 2 - parity);
+                for (int t = threadIdx.x; t < n3 / 2; t += blockDim.x) {
+                    const int k = 2 * t + 2 - parity;
+                    if (k <= klast) mg_line(E, L, k);
+                }
                 __syncthreads();
             }
         }
@@ -163,10 +169,10 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
     double m = 0.0;
     int nan = 0;
     const int nrow = (E.which == 2) ? n1 : n1 - 1;
-    const int tot = nrow * n3;
+    const int tot = nrow * klast;
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
         const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
-        const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
+        const int ka = (k == n3) ? (E.xwall ? 0 : 1) : k + 1, km = k - 1;
         double temp = mg_apply_op<double>(psif, ld, i, k, ka, km, E.which, E.polar, n1, hhri, hhpi, hri, rvi, rvq);
         temp = f[(size_t)k * (n1 + 1) + i] - temp;
         rc[GIX(i, k, ld)] = temp;
@@ -345,13 +351,18 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
             break;
         }
         if (res1 < E.tolcon) {
+            // the tank: v on k = 1..np-1, u on k = 1..np, zero side walls
+            // (velvor2dhorconvtank.f:1032-1043, :1129-1140)
+            const int kend = (E.which == 2) ? np - 1 : np;
             for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
                 const int k = idx / rows, i = idx - k * rows;
                 const size_t c = GIX(i, k, ld);
                 psip[c] = psi[c];
-                if (i == 0 || i == imax) psi[c] = 0.0;
+                if (i == 0 || i == imax || (E.xwall && (k == 0 || k > kend))) psi[c] = 0.0;
                 else psi[c] = psif[c];
             }
+            if (E.xwall && E.which == 3)
+                for (int i = threadIdx.x; i <= imax; i += blockDim.x) psi[GIX(i, np + 1, ld)] = 0.0;
             status = GB_OK;
             break;
         }
@@ -880,6 +891,8 @@ int prb_mg_create(gb_prb *h)
         E.polar = p.variant == GB_PRB_ANNULUS || p.variant == GB_PRB_TAYCOU;
         E.nrelax = p.variant == GB_PRB_ANNULUS ? 3 : 1;
         E.seam_keep = p.variant == GB_PRB_ANNULUS;
+        E.xwall = p.variant == GB_PRB_TANK;
+        if (E.xwall && p.precision != GB_PRB_FP64) return GB_ERR_INVALID;
         E.stop_on_max = p.variant != GB_PRB_ANNULUS;
         E.r0 = p.r0;
         double *base = h->mg_pool + q * per_eq;

@@ -15,7 +15,9 @@ maxsweeps then default to its 1e-5 and 10000.  variant=PRB_OBLIQUE is
 mpkoks.f (the layer with gravity along the diagonal) and variant=PRB_TAYCOU
 the Taylor-Couette driver (monashubuntudir_velvor2dtaycouheatdir/
 velvor2dtaycouheat.f: the annulus with its outer cylinder moving at
--(Ta**0.5) Ptl rmax / 2, Taylor number Ta).
+-(Ta**0.5) Ptl rmax / 2, Taylor number Ta); variant=PRB_TANK the
+horizontal-convection tank (monashubuntudir_velvor2dhorconvtankdir/
+velvor2dhorconvtank.f), whose fields carry np+2 columns.
 
 Error behaviour: where the reference STOPs after 500 multigrid sweeps
 (PRB:1843), poisson2/poisson3 raise GBError with status GB_MAXSWEEPS.  The
@@ -41,6 +43,8 @@ class PRB:
             L.gb_prb_default_params_annulus(C.byref(p), nr, np_)
         elif variant == _L.PRB_TAYCOU:
             L.gb_prb_default_params_taycou(C.byref(p), nr, np_)
+        elif variant == _L.PRB_TANK:
+            L.gb_prb_default_params_tank(C.byref(p), nr, np_)
         else:
             L.gb_prb_default_params(C.byref(p), nr, np_)
         p.Ta = Ta
@@ -59,18 +63,19 @@ class PRB:
         self.nlev = nlev.value
         self.nr, self.np = nr, np_
         self.ld = nr + 2
+        self.ncol = np_ + 2 if variant == _L.PRB_TANK else np_ + 1
         self.kt = 0
 
     # -- fields ------------------------------------------------------------
     def set(self, name, arr):
         a = np.asfortranarray(arr, dtype=np.float64)
-        assert a.shape[0] >= self.nr + 2 and a.shape[1] >= self.np + 1, a.shape
+        assert a.shape[0] >= self.nr + 2 and a.shape[1] >= self.ncol, a.shape
         _L.check(_L.load().gb_prb_set_field(self._h, _L.FIELD_ID[name], a.ctypes.data, a.shape[0]),
                  "set_field " + name)
 
     def get(self, name, ld=None):
         ld = ld or self.ld
-        a = np.zeros((ld, self.np + 1), order="F")
+        a = np.zeros((ld, self.ncol), order="F")
         _L.check(_L.load().gb_prb_get_field(self._h, _L.FIELD_ID[name], a.ctypes.data, ld), "get_field " + name)
         return a
 

@@ -129,11 +129,25 @@ typedef struct gb_prb_params {
  *                   (:1668-1670); the multigrid is PRB's (one relaxation
  *                   per visit, coarse seam reset, STOP after 500 sweeps,
  *                   at most 4 levels) with the polar operator and tolcon
- *                   1e-5 (:1234, :1345); Nu as the annulus's. */
+ *                   1e-5 (:1234, :1345); Nu as the annulus's.
+ *   GB_PRB_TANK:    the horizontal-convection tank,
+ *                   monashubuntudir_velvor2dhorconvtankdir/velvor2dhorconvtank.f:
+ *                   the layer closed by side walls at x = 0 and x = xx; C
+ *                   and v on the faces k = 0..np, T and u on the cells
+ *                   k = 1..np with ghost columns 0 and np+1, so every field
+ *                   has np+2 columns (set/get_field move np+2 columns);
+ *                   plain Thomas x-lines; the top wall T = k/np, an
+ *                   insulated bottom and insulated side walls (:812-845);
+ *                   heat over k = np/2..np-1; Nu = 2 trans, the first step
+ *                   storing 2 trans2 in httrans and zero in httrans2
+ *                   (:197-198); the multigrid with side walls (v lines
+ *                   k = 1..np-1, u lines k = 1..np against the zero wall)
+ *                   and tolcon 5e-6.  FP64 only; no device diagnostics. */
 #define GB_PRB_LAYER   0
 #define GB_PRB_ANNULUS 1
 #define GB_PRB_OBLIQUE 2
 #define GB_PRB_TAYCOU  3
+#define GB_PRB_TANK    4
 
 /* Fills *p with the reference defaults for an nr x np grid
  * (dt 1e-7, r0 0.5, rmax 1, xx 3, Ra 1e7, Pr 0.71: the PRB input deck). */
@@ -146,6 +160,9 @@ void gb_prb_default_params_annulus(gb_prb_params *p, int nr, int np);
  * 2e-8, r0 0.5, rmax 1, Ra 6e8, Re 91927, Ta 0, Pr 0.71; tolcon 1e-5, sweep
  * limit 500). */
 void gb_prb_default_params_taycou(gb_prb_params *p, int nr, int np);
+/* The tank defaults (velvor2dhorconvtank.f with its input.s: dt 5e-8,
+ * r0 0.5, rmax 1.5, xx 3.1, Ra 8.63e7, Pr 10; tolcon 5e-6, sweep limit 500). */
+void gb_prb_default_params_tank(gb_prb_params *p, int nr, int np);
 
 typedef struct gb_prb gb_prb;
 

@@ -26,21 +26,27 @@ SOL3 = ["uel", "vel", "wel", "uelp", "velp", "welp"]
 
 
 @pytest.mark.parametrize("kr,kp,variant", [(20, 40, 0), (290, 1610, 0), (20, 40, 1), (420, 3600, 1), (20, 40, 2),
-                                           (20, 40, 3)],
+                                           (20, 40, 3), (20, 40, 4)],
                          ids=["small-bounds", "reference-bounds", "annulus-small-bounds", "annulus-reference-bounds",
-                              "oblique-small-bounds", "taycou-small-bounds"])
+                              "oblique-small-bounds", "taycou-small-bounds", "tank-small-bounds"])
 def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
     """variant 0: PRB; 1: the annulus (velvor2dnewsch3.4.f); 2: mpkoks.f's
     oblique gravity (the same names, gb_prb_bind_variant(2)); 3: the
-    Taylor-Couette driver (velvor2dtaycouheat.f, Ta in /val/'s Gr slot)."""
+    Taylor-Couette driver (velvor2dtaycouheat.f, Ta in /val/'s Gr slot); 4:
+    the tank (velvor2dhorconvtank.f: np+2 columns, Nu = 2 trans with the
+    first step's swap)."""
     L = gblib
     nr, np_ = 16, 32
     dt, Ra, Pr, r0, rmax, xx, Re = 1e-4, 1e5, 0.71, 0.5, 1.0, 3.0, 1e4
     ann = variant in (1, 3)
+    tank = variant == 4
     Ta = 1e4 if variant == 3 else 0.0
     if ann:
         dt, Ra = 1e-6, 1e6
-    tol, maxsw = (10e-6, 10000) if variant == 1 else (1e-5, 500) if variant == 3 else (2e-6, 500)
+    if tank:
+        dt, Ra, Pr, r0, rmax, xx = 1e-6, 1e6, 10.0, 0.5, 1.5, 3.1
+    tol, maxsw = {1: (10e-6, 10000), 3: (1e-5, 500), 4: (5e-6, 500)}.get(variant, (2e-6, 500))
+    ncol = np_ + 2 if tank else np_ + 1
     o = oracle.OraclePRB(nr, np_, dt, Ra, Pr, r0=r0, rmax=rmax, xx=xx, variant=variant, Re=Re, Ta=Ta)
     o.initial(0, 0, 0.0)  # the reference's own initial profile (PRB:137-186, annulus :130-178)
     S = (kr + 1) * (kp + 1)
@@ -55,7 +61,7 @@ def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
 
     for blk, names in ((sol1, SOL1), (sol2, SOL2), (sol3, SOL3)):
         for i, nm in enumerate(names):
-            view(blk, i)[: nr + 2, : np_ + 1] = np.array(o.field(nm))
+            view(blk, i)[: nr + 2, : ncol] = np.array(o.field(nm))
     num = Num(dt, o.s.dr, 0.0, o.s.dp, nr, 1, np_)
     val = np.array([Ra, Re if ann else 0.0, Pr, Ta])
     radius = np.array([r0, rmax])
@@ -98,13 +104,15 @@ def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
             assert L.gb_prb_last_sweeps() == sw[1]
             L.update_()
             assert L.gb_prb_last_status() == 0
-            if ann:
+            if tank:
+                assert (t2.value * 2.0 if kt == 1 else t1.value * 2.0) == nu[0]
+            elif ann:
                 assert -r0 * math.log(r0 / rmax) * t1.value / (2.0 * math.acos(-1.0)) == nu[0]
             else:
                 assert t1.value * (rmax - r0) / xx == nu[0]
             for blk, names in ((sol1, SOL1), (sol2, SOL2), (sol3, SOL3)):
                 for i, nm in enumerate(names):
-                    np.testing.assert_array_equal(view(blk, i)[: nr + 2, : np_ + 1], np.array(o.field(nm)),
+                    np.testing.assert_array_equal(view(blk, i)[: nr + 2, : ncol], np.array(o.field(nm)),
                                                   err_msg="%s kt=%d" % (nm, kt))
         del vel, velp, uel, uelp
     finally:
