@@ -526,7 +526,7 @@ int prb_launch_heat(gb_prb *h, cudaStream_t s)
 {
     PrbDev &d = h->dev;
     // the tank integrates over k = np/2..np-1 (velvor2dhorconvtank.f:778)
-    if (d.tank) k_heat<<<1, 256, 2 * (d.np + 1) * sizeof(double), s>>>(d, d.np / 2, d.np - 1);
+    if (d.tank) k_heat<<<1, 256, 2 * (d.np + 1) * sizeof(double), s>>>(d, d.dvd ? 2 : d.np / 2, d.np - 1);
     else k_heat<<<1, 256, 2 * (d.np + 1) * sizeof(double), s>>>(d, 1, d.np);
     h->launches += 1;
     return GB_OK;
@@ -556,8 +556,9 @@ int prb_launch_update(gb_prb *h, cudaStream_t s, bool diag)
 int prb_launch_record(gb_prb *h, cudaStream_t s, int first)
 {
     double c1 = h->p.rmax - h->p.r0, c2 = c1, div = h->p.xx;
-    if (h->p.variant == GB_PRB_TANK) {
-        c1 = c2 = 2.0;   // httrans = 2 trans (velvor2dhorconvtank.f:209-210)
+    if (h->p.variant == GB_PRB_TANK || h->p.variant == GB_PRB_DVD) {
+        // httrans = 2 trans (velvor2dhorconvtank.f:209-210), trans in the cavity
+        c1 = c2 = h->p.variant == GB_PRB_DVD ? 1.0 : 2.0;
         div = 1.0;
     }
     if (h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU) {
@@ -566,7 +567,7 @@ int prb_launch_record(gb_prb *h, cudaStream_t s, int first)
         c2 = -h->p.rmax * L;
         div = 2.0 * acos(-1.0);
     }
-    k_record<<<1, 32, 0, s>>>(h->dev, c1, c2, div, (h->p.variant == GB_PRB_TANK && first) ? 1 : 0);
+    k_record<<<1, 32, 0, s>>>(h->dev, c1, c2, div, (h->dev.tank && first) ? 1 : 0);
     h->launches += 1;
     return GB_OK;
 }
@@ -619,6 +620,18 @@ extern "C" void gb_prb_default_params_tank(gb_prb_params *p, int nr, int np)
     p->maxsweeps = 500;
 }
 
+extern "C" void gb_prb_default_params_dvd(gb_prb_params *p, int nr, int np)
+{
+    gb_prb_default_params_tank(p, nr, np);
+    p->variant = GB_PRB_DVD;
+    p->dt = 2e-6;
+    p->r0 = 0.0;
+    p->rmax = 1.0;
+    p->xx = 1.0;
+    p->Ra = 1e6;
+    p->Pr = 0.71;
+}
+
 extern "C" void gb_prb_default_params_taycou(gb_prb_params *p, int nr, int np)
 {
     gb_prb_default_params_annulus(p, nr, np);
@@ -661,7 +674,8 @@ int prb_refresh_scalars(gb_prb *h)
     d.polar = h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU;
     d.oblique = h->p.variant == GB_PRB_OBLIQUE;
     d.taycou = h->p.variant == GB_PRB_TAYCOU;
-    d.tank = h->p.variant == GB_PRB_TANK;
+    d.tank = h->p.variant == GB_PRB_TANK || h->p.variant == GB_PRB_DVD;
+    d.dvd = h->p.variant == GB_PRB_DVD;
     d.rmax = h->p.rmax;
     d.velo = d.taycou ? -(pow(h->p.Ta, 0.5) * h->p.Pr * 0.5 * h->p.rmax) : 0.0;
     d.robert = h->p.variant == GB_PRB_ANNULUS ? 0.05 : d.taycou ? 0.01 : 0.02;
@@ -686,7 +700,7 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     const int nlev = prb_mg_levels(nr, p->variant);
     if (nlev_out) *nlev_out = nlev;
     if (p->variant != GB_PRB_LAYER && p->variant != GB_PRB_ANNULUS && p->variant != GB_PRB_OBLIQUE &&
-        p->variant != GB_PRB_TAYCOU && p->variant != GB_PRB_TANK) {
+        p->variant != GB_PRB_TAYCOU && p->variant != GB_PRB_TANK && p->variant != GB_PRB_DVD) {
         gb_set_error("gb_prb_create: unknown variant %d", p->variant);
         return GB_ERR_INVALID;
     }
@@ -695,8 +709,8 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
         gb_set_error("gb_prb_create: the annulus needs 0 < r0 < rmax and Re != 0 (r0=%g rmax=%g Re=%g)", p->r0, p->rmax, p->Re);
         return GB_ERR_INVALID;
     }
-    if (p->variant == GB_PRB_TANK && p->precision != GB_PRB_FP64) {
-        gb_set_error("gb_prb_create: the tank runs in FP64 only");
+    if ((p->variant == GB_PRB_TANK || p->variant == GB_PRB_DVD) && p->precision != GB_PRB_FP64) {
+        gb_set_error("gb_prb_create: the tank and the cavity run in FP64 only");
         return GB_ERR_INVALID;
     }
     if (nr < 4 || np < 4 || (np & 1) || nlev < 1 || nr > 8192 || np > 65536) {
@@ -710,7 +724,8 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     d.nr = nr;
     d.np = np;
     d.ld = nr + 2;
-    h->ncol = p->variant == GB_PRB_TANK ? np + 2 : np + 1;   // the tank's T and u ghost column np+1
+    // the tank's and the cavity's T and u ghost column np+1
+    h->ncol = (p->variant == GB_PRB_TANK || p->variant == GB_PRB_DVD) ? np + 2 : np + 1;
     h->fsz = (size_t)d.ld * (size_t)h->ncol;
     h->dr_set = dr;
     h->dp_set = dp;

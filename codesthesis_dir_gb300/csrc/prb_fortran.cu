@@ -82,6 +82,7 @@ DropIn &g()
             if (strcmp(s, "oblique") == 0 || strcmp(s, "2") == 0) d.variant = GB_PRB_OBLIQUE;
             if (strcmp(s, "taycou") == 0 || strcmp(s, "3") == 0) d.variant = GB_PRB_TAYCOU;
             if (strcmp(s, "tank") == 0 || strcmp(s, "4") == 0) d.variant = GB_PRB_TANK;
+            if (strcmp(s, "dvd") == 0 || strcmp(s, "5") == 0) d.variant = GB_PRB_DVD;
         }
     }
     return d;
@@ -145,6 +146,8 @@ int ensure(int nr, int np, double dr, double dp)
         p.Re = Re;
     } else if (d.variant == GB_PRB_TANK) {
         gb_prb_default_params_tank(&p, nr, np);
+    } else if (d.variant == GB_PRB_DVD) {
+        gb_prb_default_params_dvd(&p, nr, np);
     } else {
         gb_prb_default_params(&p, nr, np);
         p.variant = d.variant;   // GB_PRB_LAYER or GB_PRB_OBLIQUE
@@ -290,7 +293,7 @@ void gb_prb_bind_variant(int variant)
 {
     std::lock_guard<std::mutex> lk(g().mu);
     g().variant = (variant == GB_PRB_ANNULUS || variant == GB_PRB_OBLIQUE || variant == GB_PRB_TAYCOU ||
-                   variant == GB_PRB_TANK)
+                   variant == GB_PRB_TANK || variant == GB_PRB_DVD)
                       ? variant
                       : GB_PRB_LAYER;
 }

@@ -51,7 +51,8 @@ struct PrbDev {
     int polar;           // GB_PRB_ANNULUS or GB_PRB_TAYCOU: the (r, phi) plane
     int oblique;         // GB_PRB_OBLIQUE
     int taycou;          // GB_PRB_TAYCOU: the moving outer wall
-    int tank;            // GB_PRB_TANK: side walls in x, np+2 columns per field
+    int tank;            // GB_PRB_TANK or GB_PRB_DVD: side walls in x, np+2 columns per field
+    int dvd;             // GB_PRB_DVD: the differentially heated cavity's differences
     const double *fac_xw1, *fac_xw2;   // the tank's tdma factors along x, n = np-1 and np
     double velo;         // its speed -(Ta**0.5) Ptl rmax / 2 (host libm pow)
     double rmax;

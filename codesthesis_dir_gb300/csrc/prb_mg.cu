@@ -891,7 +891,7 @@ int prb_mg_create(gb_prb *h)
         E.polar = p.variant == GB_PRB_ANNULUS || p.variant == GB_PRB_TAYCOU;
         E.nrelax = p.variant == GB_PRB_ANNULUS ? 3 : 1;
         E.seam_keep = p.variant == GB_PRB_ANNULUS;
-        E.xwall = p.variant == GB_PRB_TANK;
+        E.xwall = p.variant == GB_PRB_TANK || p.variant == GB_PRB_DVD;
         if (E.xwall && p.precision != GB_PRB_FP64) return GB_ERR_INVALID;
         E.stop_on_max = p.variant != GB_PRB_ANNULUS;
         E.r0 = p.r0;

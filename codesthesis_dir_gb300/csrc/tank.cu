@@ -7,8 +7,18 @@
 // update and right-hand-side kernels; the multigrid is the layer's with its
 // x-wall switch (MgEq::xwall).
 //
+// The differentially heated cavity benchmark of
+// monashubuntudir_velvor2ddvdbenchmarkdir/velvor2ddvdbenchmark.f (PrbDev::dvd)
+// runs the same kernels with its differences: the wall correction of the
+// C-point dT/dr at i = 1 (:382-383), buoyancy -Ra thr (:437, :560), the T
+// derivative's wall row 0.5333333333 T0 - 3.6 T1 + 2.9666666667 T2 + 0.1 T4
+// (:601, :696), the T Robert filter on i = 1..nr (:763), heat over
+// k = 2..np-1 (:780), side-wall vorticities -u(1)/dp and u(np)/dp
+// (:819-820), T = 0 and 1 on the bottom and top rows with the insulated
+// closure on the side ghosts (:822-830).
+//
 // Numerics: the reference's expressions in its order with -fmad=false; the
-// REAL*4 literals 1./6. and 4./3. of the C-point dT/dr row (:384-386) are
+// REAL*4 literals 1./6. and 4./3. of the C-point dT/dr rows (:384-386) are
 // the floats they round to.
 #include "banded.cuh"
 #include "gbcommon.cuh"
@@ -38,8 +48,13 @@ __global__ void k_tank_cvort_deriv_r(PrbDev d)
     };
     apply_tdma_rhs(d.fac_r1, nr - 1, d.f[GB_F_A] + GIX(1, k, ld), 1, rhsC);
     const int ka = k + 1;
+    const bool dvd = d.dvd;
     auto rhsT = [&](int j) -> double {
         const int i = j + 1;
+        if (i == 1 && dvd)
+            return 3.0 * (th[GIX(2, k, ld)] + th[GIX(2, ka, ld)] - th[GIX(1, k, ld)] - th[GIX(1, ka, ld)]) * dri -
+                   (-TF43 * (th[GIX(0, k, ld)] + th[GIX(0, ka, ld)]) + 1.5 * (th[GIX(1, k, ld)] + th[GIX(1, ka, ld)]) -
+                    TF16 * (th[GIX(2, k, ld)] + th[GIX(2, ka, ld)])) * dri;
         if (i == 1)
             return 3.0 * (th[GIX(2, k, ld)] + th[GIX(2, ka, ld)] - th[GIX(1, k, ld)] - th[GIX(1, ka, ld)]) * dri;
         if (i == nr - 1)
@@ -107,7 +122,7 @@ __global__ void k_tank_cvort_update(PrbDev d, int first)
         cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
     }
     const double ULT = (u * Cr + v * Ch * ri) / Ptl;
-    const double RHS2 = -Ra * thh;
+    const double RHS2 = d.dvd ? -Ra * d.f[GB_F_An][GIX(i, k, ld)] : -Ra * thh;
     const double cf2 = cnr + cnh;
     const double cn = (cf2 * Cp[GIX(i, k, ld)] - ULT - RHS2 + RHS1) / cf1;
     d.f[GB_F_Cn][GIX(i, k, ld)] = cn;
@@ -135,8 +150,12 @@ __global__ void k_tank_temp_deriv_r(PrbDev d)
     const int ld = d.ld, nr = d.nr;
     const double dri = d.dri;
     const double *th = d.f[GB_F_th];
+    const bool dvd = d.dvd;
     auto rhs = [&](int j) -> double {
         const int i = j + 1;
+        if (i == 1 && dvd)
+            return dri * (0.5333333333 * th[GIX(0, k, ld)] - 3.6 * th[GIX(1, k, ld)] + 2.9666666667 * th[GIX(2, k, ld)] +
+                          0.1 * th[GIX(4, k, ld)]);
         if (i == 1)
             return dri * (-8.0 * th[GIX(0, k, ld)] + 6.0 * th[GIX(1, k, ld)] + 1.9 * th[GIX(2, k, ld)] +
                           0.1 * th[GIX(4, k, ld)]);
@@ -227,7 +246,24 @@ __global__ void k_tank_walls(PrbDev d)
         if (i == 0) Cn[GIX(0, k, ld)] = (3.0 * vel[GIX(1, k, ld)] - vel[GIX(2, k, ld)] / 3.0) / dr;
         else if (i == nr) Cn[GIX(nr, k, ld)] = (vel[GIX(nr - 1, k, ld)] / 3.0 - 3.0 * vel[GIX(nr, k, ld)]) / dr;
     }
-    if (i <= nr && (k == 0 || k == np)) Cn[GIX(i, k, ld)] = 0.0;
+    if (i <= nr && (k == 0 || k == np)) {
+        const double *uel = d.f[GB_F_uel];
+        if (d.dvd) Cn[GIX(i, k, ld)] = k == 0 ? -uel[GIX(i, 1, ld)] / d.dp : uel[GIX(i, np, ld)] / d.dp;
+        else Cn[GIX(i, k, ld)] = 0.0;
+    }
+    if (d.dvd) {
+        // T = 0 and 1 on the bottom and top rows (ghost columns included),
+        // the insulated closure on the side ghosts of rows 1..nr
+        if (i == 0) thn[GIX(0, k, ld)] = 0.0;
+        else if (i == nr + 1) thn[GIX(nr + 1, k, ld)] = 1.0;
+        else if (k == 0)
+            thn[GIX(i, 0, ld)] = -30.0 / 92.0 * (-3.75 * thn[GIX(i, 1, ld)] + 5.0 / 6.0 * thn[GIX(i, 2, ld)] -
+                                                 3.0 / 20.0 * thn[GIX(i, 3, ld)]);
+        else if (k == np + 1)
+            thn[GIX(i, np + 1, ld)] = -30.0 / 92.0 * (-3.75 * thn[GIX(i, np, ld)] + 5.0 / 6.0 * thn[GIX(i, np - 1, ld)] -
+                                                      3.0 / 20.0 * thn[GIX(i, np - 2, ld)]);
+        return;
+    }
     // T on row ii of column kk after the wall rows are set (kk = 0..np)
     auto row = [&](int ii, int kk) -> double {
         if (ii == 0)
@@ -315,7 +351,7 @@ int tank_launch_temperature(gb_prb *h, int first, cudaStream_t s)
     k_tank_temp_update<<<gb_ceil_div((size_t)d.nr * d.np, TANK_TPB), TANK_TPB, 0, s>>>(d, first);
     if (!first)
         k_tank_robert<<<gb_ceil_div((size_t)(d.nr + 1) * d.np, TANK_TPB), TANK_TPB, 0, s>>>(
-            d, GB_F_th, GB_F_thn, GB_F_thp, 0, d.nr, 1, d.np);
+            d, GB_F_th, GB_F_thn, GB_F_thp, d.dvd ? 1 : 0, d.nr, 1, d.np);
     h->launches += first ? 3 : 4;
     return GB_OK;
 }

@@ -36,6 +36,7 @@ PRB_ANNULUS = 1
 PRB_OBLIQUE = 2   # mpkoks.f: the layer with gravity along the diagonal
 PRB_TAYCOU = 3    # velvor2dtaycouheat.f: the annulus with a moving outer cylinder
 PRB_TANK = 4      # velvor2dhorconvtank.f: the layer closed by side walls (fields have np+2 columns)
+PRB_DVD = 5       # velvor2ddvdbenchmark.f: the differentially heated cavity (np+2 columns)
 PRB_FP64 = 0
 PRB_MIXED = 1
 BATCH_FP64 = 0
@@ -104,6 +105,7 @@ SIGNATURES = [
     ("gb_prb_default_params_annulus", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
     ("gb_prb_default_params_taycou", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
     ("gb_prb_default_params_tank", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
+    ("gb_prb_default_params_dvd", None, [C.POINTER(PrbParams), C.c_int, C.c_int]),
     ("gb_prb_create", C.c_int, [C.POINTER(PrbParams), C.POINTER(_vp), _ip]),
     ("gb_prb_destroy", C.c_int, [_vp]),
     ("gb_prb_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),

@@ -17,7 +17,9 @@ the Taylor-Couette driver (monashubuntudir_velvor2dtaycouheatdir/
 velvor2dtaycouheat.f: the annulus with its outer cylinder moving at
 -(Ta**0.5) Ptl rmax / 2, Taylor number Ta); variant=PRB_TANK the
 horizontal-convection tank (monashubuntudir_velvor2dhorconvtankdir/
-velvor2dhorconvtank.f), whose fields carry np+2 columns.
+velvor2dhorconvtank.f), whose fields carry np+2 columns, and
+variant=PRB_DVD the differentially heated cavity benchmark
+(monashubuntudir_velvor2ddvdbenchmarkdir/velvor2ddvdbenchmark.f), likewise.
 
 Error behaviour: where the reference STOPs after 500 multigrid sweeps
 (PRB:1843), poisson2/poisson3 raise GBError with status GB_MAXSWEEPS.  The
@@ -45,6 +47,8 @@ class PRB:
             L.gb_prb_default_params_taycou(C.byref(p), nr, np_)
         elif variant == _L.PRB_TANK:
             L.gb_prb_default_params_tank(C.byref(p), nr, np_)
+        elif variant == _L.PRB_DVD:
+            L.gb_prb_default_params_dvd(C.byref(p), nr, np_)
         else:
             L.gb_prb_default_params(C.byref(p), nr, np_)
         p.Ta = Ta
@@ -63,7 +67,7 @@ class PRB:
         self.nlev = nlev.value
         self.nr, self.np = nr, np_
         self.ld = nr + 2
-        self.ncol = np_ + 2 if variant == _L.PRB_TANK else np_ + 1
+        self.ncol = np_ + 2 if variant in (_L.PRB_TANK, _L.PRB_DVD) else np_ + 1
         self.kt = 0
 
     # -- fields ------------------------------------------------------------

@@ -142,12 +142,23 @@ typedef struct gb_prb_params {
  *                   storing 2 trans2 in httrans and zero in httrans2
  *                   (:197-198); the multigrid with side walls (v lines
  *                   k = 1..np-1, u lines k = 1..np against the zero wall)
- *                   and tolcon 5e-6.  FP64 only; no device diagnostics. */
+ *                   and tolcon 5e-6.  FP64 only; no device diagnostics.
+ *   GB_PRB_DVD:     the differentially heated cavity benchmark,
+ *                   monashubuntudir_velvor2ddvdbenchmarkdir/velvor2ddvdbenchmark.f:
+ *                   the tank's scheme (np+2 columns, same multigrid) with
+ *                   xx = 1, T = 0 and 1 on the bottom and top rows and
+ *                   insulated side walls (:822-830), side-wall vorticities
+ *                   -u(1)/dp and u(np)/dp (:819-820), buoyancy -Ra thr
+ *                   (:437, :560), its own wall rows of the T derivatives
+ *                   (:382-383, :601, :696), the T Robert filter on
+ *                   i = 1..nr, heat over k = 2..np-1 and Nu = trans (with
+ *                   the tank's first-step quirk).  FP64 only. */
 #define GB_PRB_LAYER   0
 #define GB_PRB_ANNULUS 1
 #define GB_PRB_OBLIQUE 2
 #define GB_PRB_TAYCOU  3
 #define GB_PRB_TANK    4
+#define GB_PRB_DVD     5
 
 /* Fills *p with the reference defaults for an nr x np grid
  * (dt 1e-7, r0 0.5, rmax 1, xx 3, Ra 1e7, Pr 0.71: the PRB input deck). */
@@ -163,6 +174,9 @@ void gb_prb_default_params_taycou(gb_prb_params *p, int nr, int np);
 /* The tank defaults (velvor2dhorconvtank.f with its input.s: dt 5e-8,
  * r0 0.5, rmax 1.5, xx 3.1, Ra 8.63e7, Pr 10; tolcon 5e-6, sweep limit 500). */
 void gb_prb_default_params_tank(gb_prb_params *p, int nr, int np);
+/* The cavity defaults (velvor2ddvdbenchmark.f with its input.s: dt 2e-6,
+ * r0 0, rmax 1, xx 1, Ra 1e6, Pr 0.71; tolcon 5e-6, sweep limit 500). */
+void gb_prb_default_params_dvd(gb_prb_params *p, int nr, int np);
 
 typedef struct gb_prb gb_prb;
 

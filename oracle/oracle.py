@@ -24,6 +24,7 @@ ORC_ANNULUS = 1
 ORC_OBLIQUE = 2   # mpkoks.f: the layer with gravity along the diagonal
 ORC_TAYCOU = 3    # velvor2dtaycouheat.f: the annulus with a moving outer cylinder
 ORC_TANK = 4      # velvor2dhorconvtank.f: the layer closed by side walls in x
+ORC_DVD = 5       # velvor2ddvdbenchmark.f: the differentially heated cavity
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -319,7 +320,7 @@ class OraclePRB:
     @property
     def ncol(self):
         """Columns of a field: np+1, or np+2 in the tank (ghost column np+1)."""
-        return self.s.np + (2 if self.s.variant == ORC_TANK else 1)
+        return self.s.np + (2 if self.s.variant in (ORC_TANK, ORC_DVD) else 1)
 
     def field(self, name) -> np.ndarray:
         """A (ld, ncol) Fortran-ordered view of a state field (i fastest)."""
@@ -331,7 +332,7 @@ class OraclePRB:
     def initial(self, kind=1, seed=0, amp=1e-3):
         """kind 0: the driver's own start; 1: conduction plus seeded noise.
         The tank has only its own start (velvor2dhorconvtank.f:70-140)."""
-        if self.s.variant == ORC_TANK:
+        if self.s.variant in (ORC_TANK, ORC_DVD):
             lib().orc_tank_initial(C.byref(self.s))
         else:
             lib().orc_prb_initial(C.byref(self.s), kind, seed, amp)

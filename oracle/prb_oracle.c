@@ -166,7 +166,7 @@ int orc_mg_init_variant(orc_mg_t *mg, int nr, int np, double dr, double dp, int 
         mg->mgen = 2000000;
     }
     if (variant == ORC_TAYCOU) mg->tolcon = 1.0e-5;   /* velvor2dtaycouheat.f:1234, :1345 */
-    if (variant == ORC_TANK) {                          /* velvor2dhorconvtank.f:1163, :1264 */
+    if (variant == ORC_TANK || variant == ORC_DVD) {   /* velvor2dhorconvtank.f:1163, :1264 */
         mg->tolcon = 5.0e-6;
         mg->xwall = 1;
     }
@@ -1120,13 +1120,15 @@ static int tank_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double 
     orc_tank_update(s);
     if (nu) {
         /* velvor2dhorconvtank.f:197-198, :209-210: the first step overwrites
-         * httrans with 2 trans2 and leaves httrans2 at zero */
+         * httrans with 2 trans2 and leaves httrans2 at zero; the DVD cavity
+         * (velvor2ddvdbenchmark.f:197-210) the same without the factor 2 */
+        const double c = s->variant == ORC_DVD ? 1.0 : 2.0;
         if (kt == 1) {
-            nu[0] = t2 * 2.0;
+            nu[0] = s->variant == ORC_DVD ? t2 : t2 * c;
             nu[1] = 0.0;
         } else {
-            nu[0] = t1 * 2.0;
-            nu[1] = t2 * 2.0;
+            nu[0] = s->variant == ORC_DVD ? t1 : t1 * c;
+            nu[1] = s->variant == ORC_DVD ? t2 : t2 * c;
         }
     }
     if (sweeps) { sweeps[0] = sv; sweeps[1] = su; }
@@ -1137,7 +1139,7 @@ int orc_prb_step(orc_prb_t *s, orc_mg_t *mgv, orc_mg_t *mgu, int kt, double *nu,
 {
     double t1, t2;
     int sv = 0, su = 0, st;
-    if (s->variant == ORC_TANK) return tank_step(s, mgv, mgu, kt, nu, sweeps);
+    if (s->variant == ORC_TANK || s->variant == ORC_DVD) return tank_step(s, mgv, mgu, kt, nu, sweeps);
     if (kt == 1) {
         orc_cvorticity1(s);
         orc_temperature1(s);

@@ -91,6 +91,9 @@ typedef struct {
 /* the horizontal-convection tank, velvor2dhorconvtank.f (tank_oracle.c):
  * the layer closed by side walls in x */
 #define ORC_TANK    4
+/* the differentially heated cavity benchmark, velvor2ddvdbenchmark.f: the
+ * tank's side-walled scheme with the DVD differences (tank_oracle.c) */
+#define ORC_DVD     5
 
 int  orc_mg_init(orc_mg_t *mg, int nr, int np, double dr, double dp);
 /* Same with the variant and inner radius of the annulus driver. */

@@ -28,6 +28,19 @@
  *   poisson2/poisson3 and relax2/relax3: see the xwall field of orc_mg_t;
  *   main (:188-210): Nu = 2 trans; the first step stores 2 trans2 in
  *     httrans and leaves httrans2 at zero.
+ *
+ * ORC_DVD, the differentially heated cavity of
+ * monashubuntudir_velvor2ddvdbenchmarkdir/velvor2ddvdbenchmark.f, is the
+ * same scheme with: xx = 1; the start T = 0.5 inside, 0 at i = 0, 1 at
+ * i = nr+1; the wall correction -(-4/3 (T0) + 1.5 (T1) - 1/6 (T2)) dr^-1 of
+ * dT/dr at the C points at i = 1 (:382-383, REAL*4 4./3. and 1./6.);
+ * buoyancy RHS2 = -Ra thr (:437, :560); the T derivative's wall row
+ * 0.5333333333 T0 - 3.6 T1 + 2.9666666667 T2 + 0.1 T4 at i = 1 (:601,
+ * :696); the Robert filter of T on i = 1..nr (:763); heat over
+ * k = 2..np-1 (:780); the side-wall vorticities -u(1)/dp and u(np)/dp
+ * (:819-820); T = 0 and 1 on the bottom and top rows including the ghost
+ * columns, and the insulated closure on the side ghosts (:822-830);
+ * Nu = trans.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -39,6 +52,8 @@
 
 static const double F16 = (double)(1.0f / 6.0f);
 static const double F43 = (double)(4.0f / 3.0f);
+
+static int is_dvd(const orc_prb_t *s) { return s->variant == ORC_DVD; }
 
 static double *tank_buf(int n, double **wa, double **wb, double **wc, double **wr, double **ws)
 {
@@ -90,7 +105,11 @@ void orc_tank_cvorticity(orc_prb_t *s, int first)
         const int ka = k + 1;
         for (int i = 1; i <= nr - 1; ++i) {
             wa[i - 1] = 1.0; wb[i - 1] = 4.0; wc[i - 1] = 1.0;
-            if (i == 1)
+            if (i == 1 && is_dvd(s))
+                wr[i - 1] = 3.0 * (th[IX(2, k)] + th[IX(2, ka)] - th[IX(1, k)] - th[IX(1, ka)]) * dri -
+                            (-F43 * (th[IX(0, k)] + th[IX(0, ka)]) + 1.5 * (th[IX(1, k)] + th[IX(1, ka)]) -
+                             F16 * (th[IX(2, k)] + th[IX(2, ka)])) * dri;
+            else if (i == 1)
                 wr[i - 1] = 3.0 * (th[IX(2, k)] + th[IX(2, ka)] - th[IX(1, k)] - th[IX(1, ka)]) * dri;
             else if (i == nr - 1)
                 wr[i - 1] = 3.0 * (th[IX(nr, k)] + th[IX(nr, ka)] - th[IX(nr - 1, k)] - th[IX(nr - 1, ka)]) * dri -
@@ -136,7 +155,7 @@ void orc_tank_cvorticity(orc_prb_t *s, int first)
                 cf1 = 0.5 / (Ptl * dt) - cnr - cnh;
             }
             const double ULT = (u * Cr + v * Ch * ri) / Ptl;
-            const double RHS2 = -Ra * thh;
+            const double RHS2 = is_dvd(s) ? -Ra * s->An[IX(i, k)] : -Ra * thh;
             const double cf2 = cnr + cnh;
             s->Cn[IX(i, k)] = (cf2 * Cp[IX(i, k)] - ULT - RHS2 + RHS1) / cf1;
             if (!first) s->Ap[IX(i, k)] = s->Cn[IX(i, k)];
@@ -162,7 +181,11 @@ void orc_tank_temperature(orc_prb_t *s, int first)
             if (i == 1) {
                 wb[i - 1] = 1.0;
                 wc[i - 1] = 2.0;
-                wr[i - 1] = dri * (-8.0 * th[IX(0, k)] + 6.0 * th[IX(1, k)] + 1.9 * th[IX(2, k)] + 0.1 * th[IX(4, k)]);
+                if (is_dvd(s))
+                    wr[i - 1] = dri * (0.5333333333 * th[IX(0, k)] - 3.6 * th[IX(1, k)] + 2.9666666667 * th[IX(2, k)] +
+                                       0.1 * th[IX(4, k)]);
+                else
+                    wr[i - 1] = dri * (-8.0 * th[IX(0, k)] + 6.0 * th[IX(1, k)] + 1.9 * th[IX(2, k)] + 0.1 * th[IX(4, k)]);
             } else if (i == nr) {
                 wa[i - 1] = 2.0;
                 wb[i - 1] = 1.0;
@@ -221,7 +244,7 @@ void orc_tank_temperature(orc_prb_t *s, int first)
         }
     if (!first)
         for (int k = 1; k <= np; ++k)
-            for (int i = 0; i <= nr; ++i)
+            for (int i = is_dvd(s) ? 1 : 0; i <= nr; ++i)
                 s->th[IX(i, k)] = s->th[IX(i, k)] + 0.02 * (s->thn[IX(i, k)] - 2.0 * s->th[IX(i, k)] + s->thp[IX(i, k)]);
 }
 
@@ -232,7 +255,7 @@ void orc_tank_heat(const orc_prb_t *s, double *trans1, double *trans2)
     const double dp = s->dp, dri = 1.0 / s->dr;
     const double *th = s->th;
     double t1 = 0.0, t2 = 0.0;
-    for (int k = np / 2; k <= np - 1; ++k) {
+    for (int k = is_dvd(s) ? 2 : np / 2; k <= np - 1; ++k) {
         const int ka = k + 1;
         t1 = t1 + 0.5 * dp *
                       (-3.35238095 * th[IX(0, k)] + 4.375 * th[IX(1, k)] - 1.45833333 * th[IX(2, k)] +
@@ -261,18 +284,30 @@ void orc_tank_update(orc_prb_t *s)
         s->Cn[IX(nr, k)] = (s->vel[IX(nr - 1, k)] / 3.0 - 3.0 * s->vel[IX(nr, k)]) / dr;
     }
     for (int i = 0; i <= nr; ++i) {
-        s->Cn[IX(i, 0)] = 0.0;
-        s->Cn[IX(i, np)] = 0.0;
+        s->Cn[IX(i, 0)] = is_dvd(s) ? -s->uel[IX(i, 1)] / s->dp : 0.0;
+        s->Cn[IX(i, np)] = is_dvd(s) ? s->uel[IX(i, np)] / s->dp : 0.0;
     }
-    for (int k = 0; k <= np; ++k) {
+    if (is_dvd(s)) {
+        for (int k = 0; k <= np + 1; ++k) {
+            s->thn[IX(0, k)] = 0.0;
+            s->thn[IX(nr + 1, k)] = 1.0;
+        }
+        for (int i = 1; i <= nr; ++i) {
+            s->thn[IX(i, 0)] = -30.0 / 92.0 * (-3.75 * s->thn[IX(i, 1)] + 5.0 / 6.0 * s->thn[IX(i, 2)] -
+                                               3.0 / 20.0 * s->thn[IX(i, 3)]);
+            s->thn[IX(i, np + 1)] = -30.0 / 92.0 * (-3.75 * s->thn[IX(i, np)] + 5.0 / 6.0 * s->thn[IX(i, np - 1)] -
+                                                    3.0 / 20.0 * s->thn[IX(i, np - 2)]);
+        }
+    } else for (int k = 0; k <= np; ++k) {
         s->thn[IX(0, k)] = -30.0 / 92.0 * (-3.75 * s->thn[IX(1, k)] + 5.0 / 6.0 * s->thn[IX(2, k)] -
                                            3.0 / 20.0 * s->thn[IX(3, k)]);
         s->thn[IX(nr + 1, k)] = (double)k / (double)np * 1.0;
     }
-    for (int i = 0; i <= nr + 1; ++i) {
-        s->thn[IX(i, 0)] = 2.0 / 1.5 * s->thn[IX(i, 1)] - 1.0 / 3.0 * s->thn[IX(i, 2)];
-        s->thn[IX(i, np + 1)] = 2.0 / 1.5 * s->thn[IX(i, np)] - 1.0 / 3.0 * s->thn[IX(i, np - 1)];
-    }
+    if (!is_dvd(s))
+        for (int i = 0; i <= nr + 1; ++i) {
+            s->thn[IX(i, 0)] = 2.0 / 1.5 * s->thn[IX(i, 1)] - 1.0 / 3.0 * s->thn[IX(i, 2)];
+            s->thn[IX(i, np + 1)] = 2.0 / 1.5 * s->thn[IX(i, np)] - 1.0 / 3.0 * s->thn[IX(i, np - 1)];
+        }
     for (int i = 0; i <= nr + 1; ++i) {
         s->thp[IX(i, np + 1)] = s->th[IX(i, np + 1)];
         s->th[IX(i, np + 1)] = s->thn[IX(i, np + 1)];
@@ -324,7 +359,10 @@ void orc_tank_initial(orc_prb_t *s)
             s->An[IX(i, k)] = s->Bn[IX(i, k)] = s->Cn[IX(i, k)] = 0.0;
             s->A[IX(i, k)] = s->B[IX(i, k)] = s->C[IX(i, k)] = 0.0;
             s->uel[IX(i, k)] = s->vel[IX(i, k)] = s->wel[IX(i, k)] = 0.0;
-            s->th[IX(i, k)] = i == nr + 1 ? (double)k / (double)np * 1.0 : 0.5;
+            if (is_dvd(s))   /* velvor2ddvdbenchmark.f:92-96 */
+                s->th[IX(i, k)] = i == 0 ? 0.0 : i == nr + 1 ? 1.0 : 0.5;
+            else
+                s->th[IX(i, k)] = i == nr + 1 ? (double)k / (double)np * 1.0 : 0.5;
         }
     }
     for (int i = 0; i <= nr + 1; ++i)

@@ -26,9 +26,9 @@ SOL3 = ["uel", "vel", "wel", "uelp", "velp", "welp"]
 
 
 @pytest.mark.parametrize("kr,kp,variant", [(20, 40, 0), (290, 1610, 0), (20, 40, 1), (420, 3600, 1), (20, 40, 2),
-                                           (20, 40, 3), (20, 40, 4)],
+                                           (20, 40, 3), (20, 40, 4), (20, 40, 5)],
                          ids=["small-bounds", "reference-bounds", "annulus-small-bounds", "annulus-reference-bounds",
-                              "oblique-small-bounds", "taycou-small-bounds", "tank-small-bounds"])
+                              "oblique-small-bounds", "taycou-small-bounds", "tank-small-bounds", "dvd-small-bounds"])
 def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
     """variant 0: PRB; 1: the annulus (velvor2dnewsch3.4.f); 2: mpkoks.f's
     oblique gravity (the same names, gb_prb_bind_variant(2)); 3: the
@@ -39,13 +39,15 @@ def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
     nr, np_ = 16, 32
     dt, Ra, Pr, r0, rmax, xx, Re = 1e-4, 1e5, 0.71, 0.5, 1.0, 3.0, 1e4
     ann = variant in (1, 3)
-    tank = variant == 4
+    tank = variant in (4, 5)
     Ta = 1e4 if variant == 3 else 0.0
     if ann:
         dt, Ra = 1e-6, 1e6
-    if tank:
+    if variant == 4:
         dt, Ra, Pr, r0, rmax, xx = 1e-6, 1e6, 10.0, 0.5, 1.5, 3.1
-    tol, maxsw = {1: (10e-6, 10000), 3: (1e-5, 500), 4: (5e-6, 500)}.get(variant, (2e-6, 500))
+    if variant == 5:
+        dt, Ra, Pr, r0, rmax, xx = 2e-5, 1e5, 0.71, 0.0, 1.0, 1.0
+    tol, maxsw = {1: (10e-6, 10000), 3: (1e-5, 500), 4: (5e-6, 500), 5: (5e-6, 500)}.get(variant, (2e-6, 500))
     ncol = np_ + 2 if tank else np_ + 1
     o = oracle.OraclePRB(nr, np_, dt, Ra, Pr, r0=r0, rmax=rmax, xx=xx, variant=variant, Re=Re, Ta=Ta)
     o.initial(0, 0, 0.0)  # the reference's own initial profile (PRB:137-186, annulus :130-178)
@@ -105,7 +107,8 @@ def test_dropin_main_loop(oracle, gblib, kr, kp, variant):
             L.update_()
             assert L.gb_prb_last_status() == 0
             if tank:
-                assert (t2.value * 2.0 if kt == 1 else t1.value * 2.0) == nu[0]
+                c = 1.0 if variant == 5 else 2.0
+                assert (t2.value * c if kt == 1 else t1.value * c) == nu[0]
             elif ann:
                 assert -r0 * math.log(r0 / rmax) * t1.value / (2.0 * math.acos(-1.0)) == nu[0]
             else:

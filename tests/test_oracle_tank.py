@@ -89,3 +89,28 @@ def test_tank_steps_walls_and_ghosts(oracle):
     np.testing.assert_array_equal(th[NR + 1, 1:NP + 1], k / NP * 1.0)
     np.testing.assert_array_equal(th[:, 0], 2.0 / 1.5 * th[:, 1] - 1.0 / 3.0 * th[:, 2])
     np.testing.assert_array_equal(th[:, NP + 1], 2.0 / 1.5 * th[:, NP] - 1.0 / 3.0 * th[:, NP - 1])
+
+
+def test_dvd_cavity_walls(oracle):
+    """The differentially heated cavity (velvor2ddvdbenchmark.f): T = 0 and
+    1 on the bottom and top rows including the ghost columns, the insulated
+    closure on the side ghosts, side-wall vorticities -u(1)/dp and u(np)/dp
+    (:819-830), and Nu = trans (the first step storing trans2)."""
+    n = 16
+    o = oracle.OraclePRB(n, n, 2e-5, 1e5, 0.71, r0=0.0, rmax=1.0, xx=1.0, mode=1, variant=oracle.ORC_DVD)
+    o.initial()
+    th0 = np.array(o.field("th"))
+    assert np.all(th0[0, :n + 1] == 0.0) and np.all(th0[n + 1, :n + 1] == 1.0) and np.all(th0[:, n + 1] == 0.5)
+    st, nu, sw = o.step()
+    assert st == 0 and nu[1] == 0.0
+    for _ in range(4):
+        st, nu, sw = o.step()
+        assert st == 0
+    th, C, u = (np.array(o.field(x)) for x in ("th", "C", "uel"))
+    assert np.all(th[0] == 0.0) and np.all(th[n + 1] == 1.0)
+    i = np.arange(1, n + 1)
+    want0 = -30.0 / 92.0 * (-3.75 * th[i, 1] + 5.0 / 6.0 * th[i, 2] - 3.0 / 20.0 * th[i, 3])
+    np.testing.assert_array_equal(th[i, 0], want0)
+    np.testing.assert_array_equal(C[:n + 1, 0], -u[:n + 1, 1] / o.s.dp)
+    np.testing.assert_array_equal(C[:n + 1, n], u[:n + 1, n] / o.s.dp)
+    assert np.abs(u).max() > 1e-6
