@@ -25,6 +25,11 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgb300conv.so")
 DROPIN_SRC = os.path.join(HERE, "csrc_dropin", "r3d_fortran.cpp")
 R3D_LIB = os.path.join(OUT, "libgb300r3d.so")
+AXI_DROPIN_SRC = os.path.join(HERE, "csrc_dropin", "axi_fortran.cpp")
+AXI_LIB = os.path.join(OUT, "libgb300axi.so")
+# (source, library) of the drop-in libraries whose Fortran names clash with
+# the main library's: rot3dmg.f's and rotann2.f's subroutines
+DROPINS = [(DROPIN_SRC, R3D_LIB), (AXI_DROPIN_SRC, AXI_LIB)]
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -69,21 +74,26 @@ def needs_build() -> bool:
     return any(os.path.getmtime(f) > t for f in _sources() + _headers())
 
 
-def _build_dropin(force: bool) -> str:
-    deps = [DROPIN_SRC, LIB] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
-    if not force and os.path.exists(R3D_LIB) and os.path.getmtime(R3D_LIB) >= max(os.path.getmtime(f) for f in deps):
-        return R3D_LIB
+def _build_one_dropin(src: str, lib: str, force: bool) -> str:
+    deps = [src, LIB] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(f) for f in deps):
+        return lib
     cxx = shutil.which("g++") or shutil.which("c++")
     if not cxx:
         raise RuntimeError("no C++ compiler found for the drop-in library")
-    tmp = R3D_LIB + ".tmp"
-    cmd = [cxx, "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", INCLUDE, DROPIN_SRC,
+    tmp = lib + ".tmp"
+    cmd = [cxx, "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", INCLUDE, src,
            "-L", OUT, "-lgb300conv", "-Wl,-rpath,$ORIGIN", "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("drop-in build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
-    os.replace(tmp, R3D_LIB)
-    return R3D_LIB
+    os.replace(tmp, lib)
+    return lib
+
+
+def _build_dropin(force: bool) -> None:
+    for src, lib in DROPINS:
+        _build_one_dropin(src, lib, force)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:

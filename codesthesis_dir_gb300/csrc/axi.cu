@@ -812,6 +812,7 @@ struct gb_axi {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     gb_axi_params graph_params;
+    double dr_set = 0.0, dz_set = 0.0;   // a Fortran caller's /num/ spacings, 0 = derived
 };
 
 static int axi_levels(int nr, int nz)
@@ -862,8 +863,8 @@ static void axi_scalars(gb_axi *h)
     d.Ra = p.Ra;
     d.Re = p.Re;
     d.Ptl = p.Pr;
-    d.dr = (p.rmax - p.r0) / (double)p.nr;
-    d.dz = p.zmax / (double)p.nz;
+    d.dr = h->dr_set != 0.0 ? h->dr_set : (p.rmax - p.r0) / (double)p.nr;
+    d.dz = h->dz_set != 0.0 ? h->dz_set : p.zmax / (double)p.nz;
     const double dr = d.dr, dz = d.dz, Ptl = p.Pr, dt = p.dt;
     d.cf1 = 1.0 / (2.0 * Ptl * dt) + 1.0 / (dr * dr) + 1.0 / (dz * dz);
     d.cf2 = 1.0 / (2.0 * Ptl * dt) - 1.0 / (dr * dr) - 1.0 / (dz * dz);
@@ -890,7 +891,23 @@ extern "C" int gb_axi_destroy(gb_axi *h)
     return GB_OK;
 }
 
+static int axi_create(const gb_axi_params *p, double dr, double dz, gb_axi **out, int *nlev_out);
+
 extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out)
+{
+    return axi_create(p, 0.0, 0.0, out, nlev_out);
+}
+
+extern "C" int gb_axi_create_spacing(const gb_axi_params *p, double dr, double dz, gb_axi **out, int *nlev_out)
+{
+    if (!(dr > 0.0 && dz > 0.0)) {
+        gb_set_error("gb_axi_create_spacing: spacings must be positive");
+        return GB_ERR_INVALID;
+    }
+    return axi_create(p, dr, dz, out, nlev_out);
+}
+
+static int axi_create(const gb_axi_params *p, double dr, double dz, gb_axi **out, int *nlev_out)
 {
     if (!p || !out) { gb_set_error("gb_axi_create: null argument"); return GB_ERR_INVALID; }
     *out = nullptr;
@@ -913,6 +930,8 @@ extern "C" int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out
     }
     gb_axi *h = new gb_axi();
     h->p = *p;
+    h->dr_set = dr;
+    h->dz_set = dz;
     AxiDev &d = h->dev;
     memset(&d, 0, sizeof(d));
     d.nr = nr;

@@ -130,6 +130,7 @@ SIGNATURES = [
     ("gb_prb_diag_cfl", C.c_int, [_vp, C.c_int, _vp]),
     ("gb_axi_default_params", None, [C.POINTER(AxiParams), C.c_int, C.c_int]),
     ("gb_axi_create", C.c_int, [C.POINTER(AxiParams), C.POINTER(_vp), _ip]),
+    ("gb_axi_create_spacing", C.c_int, [C.POINTER(AxiParams), C.c_double, C.c_double, C.POINTER(_vp), _ip]),
     ("gb_axi_destroy", C.c_int, [_vp]),
     ("gb_axi_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
     ("gb_axi_get_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
@@ -235,6 +236,44 @@ R3D_DROPIN_SIGNATURES = [
     ("gb_r3d_last_sweeps", C.c_int, []),
 ]
 _r3d_dropin = None
+
+AXI_DROPIN_PATH = os.path.join(HERE, "_build", "libgb300axi.so")
+# (name, restype, argtypes) of libgb300axi.so (include/gb300_axi_fortran.h).
+AXI_DROPIN_SIGNATURES = [
+    ("poissoninit_", None, [_ip, _ip, _dp, _dp]),
+    ("vorticity_", None, []),
+    ("velocity_", None, []),
+    ("temperature_", None, []),
+    ("poisson_", None, [_vp, _vp]),
+    ("update_", None, []),
+    ("heat_", None, [_dp]),
+    ("gb_axi_bind_bounds", None, [C.c_int, C.c_int]),
+    ("gb_axi_bind_common", None, [_vp, _vp, _vp, _vp, _vp]),
+    ("gb_axi_bind_smoother", None, [C.c_int]),
+    ("gb_axi_bind_precision", None, [C.c_int]),
+    ("gb_axi_bind_tolerance", None, [C.c_double, C.c_int]),
+    ("gb_axi_last_status", C.c_int, []),
+    ("gb_axi_last_sweeps", C.c_int, []),
+]
+_axi_dropin = None
+
+
+def load_axi_dropin(path: str = AXI_DROPIN_PATH):
+    """Loads the rotann2.f drop-in library (its own handle: its symbols share
+    names with the other drop-ins)."""
+    global _axi_dropin
+    if _axi_dropin is not None:
+        return _axi_dropin
+    load()
+    if not os.path.exists(path):
+        raise RuntimeError("libgb300axi.so not found at %s; run __graft_entry__.build() first" % path)
+    L = C.CDLL(path, mode=C.RTLD_LOCAL)
+    for name, res, args in AXI_DROPIN_SIGNATURES:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _axi_dropin = L
+    return L
 
 
 def load_r3d_dropin(path: str = R3D_DROPIN_PATH):

@@ -342,6 +342,9 @@ void gb_axi_default_params(gb_axi_params *p, int nr, int nz);
  * (may be NULL) receives the level count (halvings while nr and nz stay
  * even, capped at 6). */
 int gb_axi_create(const gb_axi_params *p, gb_axi **out, int *nlev_out);
+/* As gb_axi_create with the grid spacings given: a Fortran driver's own dr,
+ * dz from COMMON /num/ (rotann2.f:22), used verbatim. */
+int gb_axi_create_spacing(const gb_axi_params *p, double dr, double dz, gb_axi **out, int *nlev_out);
 int gb_axi_destroy(gb_axi *h);
 int gb_axi_set_field(gb_axi *h, int field, const double *host, int ld);
 int gb_axi_get_field(gb_axi *h, int field, double *host, int ld);

@@ -83,3 +83,17 @@ def test_r3d_dropin_exports_its_header():
     assert {"avorticity_", "bvorticity_", "poisson1_", "rhsw_", "heat_", "update_"} <= declared
     assert not sorted(declared - exported), sorted(declared - exported)
     assert declared == {n for n, _, _ in lib.R3D_DROPIN_SIGNATURES}
+
+
+def test_axi_dropin_exports_its_header():
+    """libgb300axi.so (the rotann2.f drop-ins) exports every symbol its header
+    declares, and the binding table covers the same set."""
+    from codesthesis_dir_gb300 import _build, lib
+    _build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", lib.AXI_DROPIN_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    declared = declared_functions(os.path.join(ROOT, "include", "gb300_axi_fortran.h"))
+    assert {"vorticity_", "velocity_", "temperature_", "poisson_", "update_", "heat_", "poissoninit_"} <= declared
+    assert not sorted(declared - exported), sorted(declared - exported)
+    assert declared == {n for n, _, _ in lib.AXI_DROPIN_SIGNATURES}
