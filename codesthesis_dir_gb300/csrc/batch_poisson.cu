@@ -121,35 +121,58 @@ template <class T> __device__ __forceinline__ T *RP(const BatchDev &B, int p, in
 #define ST_R (TY / 8)    // rows a thread stores: TILE_THREADS / 32 warps step through TY rows
 #define ST_C (TX / 32)   // columns a thread stores
 
+// Colour-split shared layout of a tile staged with halo H: the points of
+// one parity of (row + column) in one half, those of the other in the other
+// half, each half row-major with SX/2 points per row.  A red-black phase then
+// walks consecutive words of one half (its neighbours are consecutive words
+// of the other), where the plain layout would walk every other word and
+// serialise half of each warp's accesses into a second wavefront.  The halves
+// are 16 banks apart, so accesses that alternate colour (loads, stores,
+// residual) stay conflict-free too.  The tile origin is even in both
+// directions (tiles are TX x TY apart and H is even), so the layout parity
+// is the grid parity (gx + gy) & 1.
+template <class T, int H> struct TileLayout {
+    static constexpr int SX = TX + 2 * H, SY = TY + 2 * H, SXH = SX / 2;
+    static constexpr int W = 128 / (int)sizeof(T);                     // words in 32 banks
+    static constexpr int HALF = ((SY * SXH + W - 1) / W) * W + W / 2;  // plus 16 banks
+    __device__ static __forceinline__ int at(int r, int c) { return ((r + c) & 1) * HALF + r * SXH + (c >> 1); }
+};
+
 // One red (color 0) or black (color 1) phase on ring rho around the tile.
-// The smem array has origin (ox, oy) in grid coordinates and row stride SX.
-template <class T>
-__device__ __forceinline__ void tile_phase(T *sx, const T *sf, int SX, int ox, int oy, int x0, int y0, int n,
-                                           T h2, int rho, int color)
+// The smem tile has origin (ox, oy) in grid coordinates, colour-split.
+template <class T, int H>
+__device__ __forceinline__ void tile_phase(T *sx, const T *sf, int ox, int oy, int x0, int y0, int n, T h2,
+                                           int rho, int color)
 {
+    using LY = TileLayout<T, H>;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int gxa = max(x0 - rho, 1), gxb = min(x0 + TX + rho, n - 1);
     const int gya = max(y0 - rho, 1), gyb = min(y0 + TY + rho, n - 1);
     for (int gy = gya + warp; gy < gyb; gy += nw) {
-        const int base = (gy - oy) * SX - ox;
+        const int r = gy - oy, row = r * LY::SXH;
         const int first = gxa + ((gxa + gy + color) & 1);
-        for (int gx = first + 2 * lane; gx < gxb; gx += 64) {
-            const int c = base + gx;
-            const T s = (sx[c - 1] + sx[c + 1]) + (sx[c - SX] + sx[c + SX]);
-            sx[c] = fmaT<T>(-h2, sf[c], s) * (T)0.25;
+        // points c = 2k + odd of this row; their row neighbours c -+ 1 are
+        // k - 1 + odd and k + odd of the other half
+        const int c0 = first - ox, odd = c0 & 1, kend = (gxb - ox - odd + 1) >> 1;
+        T *X = sx + color * LY::HALF + row;
+        const T *F = sf + color * LY::HALF + row;
+        const T *N = sx + (color ^ 1) * LY::HALF + row;
+        const T *Nu = N - LY::SXH, *Nd = N + LY::SXH;
+        for (int k = (c0 >> 1) + lane; k < kend; k += 32) {
+            const T s = (N[k - 1 + odd] + N[k + odd]) + (Nu[k] + Nd[k]);
+            X[k] = fmaT<T>(-h2, F[k], s) * (T)0.25;
         }
     }
     __syncthreads();
 }
 
-template <class T>
-__device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int SX, int ox, int oy, int x0, int y0, int n,
-                                            int nu, int H)
+template <class T, int H>
+__device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int ox, int oy, int x0, int y0, int n, int nu)
 {
     const T h = (T)1 / (T)(n - 1), h2 = h * h;
     for (int s = 0; s < nu; ++s) {
-        tile_phase<T>(sx, sf, SX, ox, oy, x0, y0, n, h2, H - 1 - 2 * s, 0);
-        tile_phase<T>(sx, sf, SX, ox, oy, x0, y0, n, h2, H - 2 - 2 * s, 1);
+        tile_phase<T, H>(sx, sf, ox, oy, x0, y0, n, h2, H - 1 - 2 * s, 0);
+        tile_phase<T, H>(sx, sf, ox, oy, x0, y0, n, h2, H - 2 - 2 * s, 1);
     }
 }
 
@@ -172,8 +195,8 @@ __device__ __forceinline__ void psi_prefetch(const double *psi, int x0, int y0, 
 // Stores the tile's interior points into x, or (CORRECT) adds them to the
 // FP64 solution: the last level-0 operation of an inner cycle applies the
 // defect correction psi += e point by point.
-template <class T, bool CORRECT>
-__device__ __forceinline__ void tile_store(const T *sx, int SX, int ox, int oy, int x0, int y0, int n, T *x,
+template <class T, int H, bool CORRECT>
+__device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, int y0, int n, T *x,
                                            double *psi, const double (&pv)[ST_R * ST_C])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -184,7 +207,7 @@ __device__ __forceinline__ void tile_store(const T *sx, int SX, int ox, int oy, 
             const int gy = y0 + warp + 8 * rr, gx = x0 + lane + 32 * cc;
             if (gx < 1 || gx > n - 2 || gy < 1 || gy > n - 2) continue;
             const size_t g = (size_t)gy * n + gx;
-            const T v = sx[(gy - oy) * SX + gx - ox];
+            const T v = sx[TileLayout<T, H>::at(gy - oy, gx - ox)];
             if (CORRECT) psi[g] = pv[rr * ST_C + cc] + to_double(v);
             else x[g] = v;
         }
@@ -206,8 +229,9 @@ __device__ __forceinline__ void tile_load(T *sx, T *sf, const T *x, const T *f, 
             if (load_f) fv = f[g];
             if (!zero_x) v = x[g];
         }
-        sx[i] = v;
-        if (load_f) sf[i] = fv;
+        const int q = TileLayout<T, H>::at(r, c);
+        sx[q] = v;
+        if (load_f) sf[q] = fv;
     }
 }
 
@@ -221,45 +245,62 @@ template <class T, int NU, bool CORR, bool RESTRICT>
 __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, int src, int dst,
                           unsigned char *smem)
 {
-    constexpr int H = 2 * NU + (RESTRICT ? 2 : 0), SX = TX + 2 * H, SY = TY + 2 * H;
-    T *sx = (T *)smem, *sf = sx + SX * SY;
+    constexpr int H = 2 * NU + (RESTRICT ? 2 : 0);
+    using LY = TileLayout<T, H>;
+    T *sx = (T *)smem, *sf = sx + 2 * LY::HALF;
     const int n = B.n_of[e.p * BP_MAXL + l];
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
     double pv[ST_R * ST_C];
     if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
     tile_load<T, H>(sx, sf, XS<T>(B, e.p, l, src), FP<T>(B, e.p, l), ox, oy, n, zero_init != 0, true);
     __syncthreads();
-    tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
-    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
+    tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, NU);
+    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     if (RESTRICT) {
-        // residual on the tile plus one ring, in place of f
+        // residual on the tile plus one ring, in place of f, one colour at a
+        // time (each point reads f only at itself and x, which stays put)
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         const T h = (T)1 / (T)(n - 1), ih2 = (T)1 / (h * h);
-        for (int gy = y0 - 1 + warp; gy <= y0 + TY; gy += nw) {
-            for (int gx = x0 - 1 + lane; gx <= x0 + TX; gx += 32) {
-                const int q = (gy - oy) * SX + gx - ox;
-                T rv = (T)0;
-                if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
-                    const T s = (sx[q - 1] + sx[q + 1]) + (sx[q - SX] + sx[q + SX]);
-                    const T lap = fmaT<T>((T)-4, sx[q], s);
-                    rv = fmaT<T>(-ih2, lap, sf[q]);
+        for (int q = 0; q < 2; ++q)
+            for (int gy = y0 - 1 + warp; gy <= y0 + TY; gy += nw) {
+                const int r = gy - oy, row = r * LY::SXH;
+                const int first = (x0 - 1) + ((x0 - 1 + gy + q) & 1);
+                const int c0 = first - ox, odd = c0 & 1, kend = (x0 + TX + 1 - ox - odd + 1) >> 1;
+                const T *X = sx + q * LY::HALF + row;
+                T *F = sf + q * LY::HALF + row;
+                const T *N = sx + (q ^ 1) * LY::HALF + row;
+                const T *Nu = N - LY::SXH, *Nd = N + LY::SXH;
+                const bool rin = gy >= 1 && gy <= n - 2;
+                for (int k = (c0 >> 1) + lane; k < kend; k += 32) {
+                    const int gx = 2 * k + odd + ox;
+                    T rv = (T)0;
+                    if (rin && gx >= 1 && gx <= n - 2) {
+                        const T s = (N[k - 1 + odd] + N[k + odd]) + (Nu[k] + Nd[k]);
+                        const T lap = fmaT<T>((T)-4, X[k], s);
+                        rv = fmaT<T>(-ih2, lap, F[k]);
+                    }
+                    F[k] = rv;
                 }
-                sf[q] = rv;
             }
-        }
         __syncthreads();
         const int nc = B.n_of[e.p * BP_MAXL + l + 1];
         T *fc = FP<T>(B, e.p, l + 1);
         const int Ia = max(x0 / 2, 1), Ib = min(x0 / 2 + TX / 2, nc - 1);
         const int Ja = max(y0 / 2, 1), Jb = min(y0 / 2 + TY / 2, nc - 1);
         for (int J = Ja + warp; J < Jb; J += nw) {
+            // the fine point (2J, 2I) has even row and column (the tile origin
+            // is even): colour 0 at k = I - ox/2; its row and column neighbours
+            // are colour 1 at k and k - 1, its diagonals colour 0 at k, k - 1
+            const int row = (2 * J - oy) * LY::SXH;
+            const T *F0 = sf + row, *F1 = sf + LY::HALF + row;
+            const T *F0u = F0 - LY::SXH, *F0d = F0 + LY::SXH, *F1u = F1 - LY::SXH, *F1d = F1 + LY::SXH;
             for (int I = Ia + lane; I < Ib; I += 32) {
-                const int q = (2 * J - oy) * SX + 2 * I - ox;
-                T t = sf[q];
-                t = t * (T)2 + sf[q + 1] + sf[q - 1];
-                t = t + sf[q + SX] + sf[q - SX];
-                t = t * (T)2 + sf[q + 1 + SX] + sf[q - 1 - SX];
-                t = t + sf[q + 1 - SX] + sf[q - 1 + SX];
+                const int k = I - ox / 2;
+                T t = F0[k];
+                t = t * (T)2 + F1[k] + F1[k - 1];
+                t = t + F1d[k] + F1u[k];
+                t = t * (T)2 + F0d[k] + F0u[k - 1];
+                t = t + F0u[k] + F0d[k - 1];
                 fc[(size_t)J * nc + I] = t * (T)0.0625;
             }
         }
@@ -274,7 +315,8 @@ template <class T, int NU, bool CORR>
 __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int dst, unsigned char *smem)
 {
     constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
-    T *sx = (T *)smem, *sf = sx + SX * SY;
+    using LY = TileLayout<T, H>;
+    T *sx = (T *)smem, *sf = sx + 2 * LY::HALF;
     const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1];
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
     double pv[ST_R * ST_C];
@@ -308,12 +350,13 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
                 v = v + pr;
             }
         }
-        sx[i] = v;
-        if (NU > 0) sf[i] = fv;
+        const int q = LY::at(r, c);
+        sx[q] = v;
+        if (NU > 0) sf[q] = fv;
     }
     __syncthreads();
-    if (NU > 0) tile_sweeps<T>(sx, sf, SX, ox, oy, x0, y0, n, NU, H);
-    tile_store<T, CORR>(sx, SX, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
+    if (NU > 0) tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, NU);
+    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     __syncthreads();
 }
 
@@ -679,6 +722,7 @@ struct gb_batch {
     std::vector<void *> hx, hf;
     size_t local_smem = 0;
     int *h_pinned = nullptr;
+    double *host_stage = nullptr;       // f and psi of gb_batch_solve_host, allocated on first use
     cudaStream_t stream = nullptr;
     // operation lists (first iteration, later iterations) and their device copies
     std::vector<Op> ops0, ops;
@@ -714,7 +758,13 @@ static int levels_of(int n, int *nl)
     return L;
 }
 
-template <class T> static size_t smem_tile(int H) { return 2 * sizeof(T) * (size_t)(TX + 2 * H) * (TY + 2 * H); }
+// Two colour-split arrays (x and f) of a tile with halo H (TileLayout).
+template <class T> static size_t smem_tile(int H)
+{
+    const int SXH = (TX + 2 * H) / 2, SY = TY + 2 * H, W = 128 / (int)sizeof(T);
+    const size_t half = (size_t)((SY * SXH + W - 1) / W) * W + W / 2;
+    return 2 * sizeof(T) * 2 * half;
+}
 static size_t smem_outer() { return sizeof(double) * ((size_t)(TX + 2) * (TY + 2) + 32); }
 
 template <class T> static size_t smem_of(const gb_batch *b, const Op &op)
@@ -1123,6 +1173,7 @@ extern "C" int gb_batch_destroy(gb_batch *b)
     cudaFree(b->d_tiles);
     cudaFree(b->d_ops);
     cudaFree(b->d_sync);
+    cudaFree(b->host_stage);
     if (b->h_pinned) cudaFreeHost(b->h_pinned);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -1448,12 +1499,21 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
 extern "C" int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi, int *cycles, double *relres)
 {
     if (!b || !h_f || !h_psi) { gb_set_error("gb_batch_solve_host: null argument"); return GB_ERR_INVALID; }
-    double *d = nullptr;
-    GB_CUDA_TRY(cudaMallocAsync((void **)&d, sizeof(double) * 2 * (size_t)b->total, b->stream));
+    // the staging buffer stays with the handle: an allocation of 2 x total
+    // doubles per call costs as much as a third of a copy (the stream-ordered
+    // pool hands the memory back at every synchronisation)
+    if (!b->host_stage) {
+        const cudaError_t e = cudaMalloc((void **)&b->host_stage, sizeof(double) * 2 * (size_t)b->total);
+        if (e != cudaSuccess) {
+            b->host_stage = nullptr;
+            gb_set_error("gb_batch_solve_host: staging buffer: %s", cudaGetErrorString(e));
+            return GB_ERR_ALLOC;
+        }
+    }
+    double *d = b->host_stage;
     GB_CUDA_TRY(cudaMemcpyAsync(d, h_f, sizeof(double) * (size_t)b->total, cudaMemcpyHostToDevice, b->stream));
     int st = gb_batch_solve_device(b, d, d + b->total, cycles, relres, b->stream);
     cudaMemcpyAsync(h_psi, d + b->total, sizeof(double) * (size_t)b->total, cudaMemcpyDeviceToHost, b->stream);
-    cudaFreeAsync(d, b->stream);
     GB_CUDA_TRY(cudaStreamSynchronize(b->stream));
     return st;
 }

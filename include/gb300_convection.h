@@ -566,7 +566,9 @@ long long gb_batch_total_points(const gb_batch *b);
  * and final relative residuals.  Returns GB_OK or GB_MAXSWEEPS. */
 int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_psi, int *cycles,
                           double *relres, void *stream);
-/* Host-buffer solve (copies in and out inside the call). */
+/* Host-buffer solve (copies in and out inside the call).  The first call
+ * allocates a device staging buffer of 2 x total doubles that the handle
+ * keeps until gb_batch_destroy. */
 int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi, int *cycles,
                         double *relres);
 /* Number of kernel launches the last solve issued. */
