@@ -36,34 +36,67 @@ template <> __device__ __forceinline__ float fmaT<float>(float a, float b, float
 // Conversions between float and double on the integer pipe.  GB300 issues
 // FP64 instructions (conversions included) at about 1/64 of the FP32 rate,
 // and the defect-correction loop converts every point twice per outer
-// iteration.  Both functions round exactly as the hardware conversions
-// (round to nearest even; float -> double is exact); values outside the
-// normal float range take the hardware path.
+// iteration.  Both functions round as IEEE 754 binary conversion does
+// (round to nearest, ties to even; float -> double is exact) over the whole
+// range, denormals, infinities and overflow included, with integer
+// operations only, so that no FP64 instruction is issued even on a
+// predicated path.  A NaN converts to a quiet NaN of the same sign.
+// gb_check_conversions compares both with the hardware conversions.
 __device__ __forceinline__ float d2f_rn(double x)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned int hi = (unsigned int)(b >> 32);
-    const int e = (int)((hi >> 20) & 0x7ffu);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ffu);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    unsigned int r;
     if (e >= 897 && e <= 1150) {
-        const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-        unsigned int r = (hi & 0x80000000u) | ((unsigned int)(e - 896) << 23) | (unsigned int)(m >> 29);
+        // normal float range: keep the top 23 fraction bits, round on the
+        // 29 dropped (a carry into the exponent rounds up to the next
+        // binade, or to infinity past the largest float)
+        r = ((unsigned int)(e - 896) << 23) | (unsigned int)(m >> 29);
         const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull);
         r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
-        return __uint_as_float(r);
+    } else if (e == 0x7ff) {
+        r = m ? 0x7fc00000u : 0x7f800000u;
+    } else if (e > 1150) {
+        r = 0x7f800000u;   // at or above 2^128: overflows to infinity
+    } else if (e == 0) {
+        r = 0u;            // double denormals are far below the float range
+    } else {
+        // float denormal range: the result counts units of 2^-149, the
+        // significand (with its hidden bit) shifted right by 926 - e >= 30
+        const int sh = 926 - e;
+        if (sh > 53) {
+            r = 0u;        // below half the smallest denormal
+        } else {
+            const unsigned long long full = m | (1ull << 52);
+            r = (unsigned int)(full >> sh);
+            const unsigned long long rem = full & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+            r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;
+        }
     }
-    return __double2float_rn(x);
+    return __uint_as_float(sign | r);
 }
 
 __device__ __forceinline__ double f2d(float v)
 {
     const unsigned int u = __float_as_uint(v);
-    const unsigned int e = (u >> 23) & 0xffu;
-    if (e != 0u && e != 255u)
-        return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
-                                                ((unsigned long long)(e + 896u) << 52) |
-                                                ((unsigned long long)(u & 0x7FFFFFu) << 29)));
-    if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(u & 0x80000000u) << 32));
-    return (double)v;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned int e = (u >> 23) & 0xffu, m = u & 0x7FFFFFu;
+    unsigned long long r;
+    if (e != 0u && e != 255u) {
+        r = ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    } else if (e == 255u) {
+        r = m ? 0x7ff8000000000000ull | ((unsigned long long)m << 29) : 0x7ff0000000000000ull;
+    } else if (m == 0u) {
+        r = 0ull;
+    } else {
+        // float denormal m * 2^-149: normalise so that the leading bit of m
+        // becomes the hidden bit
+        const int lz = __clz(m) - 8;   // m < 2^23: 9 or more leading zeros
+        r = ((unsigned long long)(897 - lz) << 52) | ((unsigned long long)((m << lz) & 0x7FFFFFu) << 29);
+    }
+    return __longlong_as_double((long long)(sign | r));
 }
 
 __device__ __forceinline__ double to_double(float v) { return f2d(v); }
@@ -89,6 +122,11 @@ struct BatchDev {
     double *partial;          // per level-0 block
     const int *p_blk0, *p_nblk0;  // level-0 table range of each problem
     double *const *psi;       // [p] the caller's FP64 solution of level 0
+    // [p*BP_MAXL + l] h^2 and 1/h^2 of level l, h = 1/(n-1), rounded in the
+    // precision of use; formed once on the host (IEEE division there as
+    // here) so that no thread spends FP64 divisions on them
+    const double *h2d, *ih2d;
+    const float *h2f, *ih2f;
     int *num_active;
     int max_cycles;
     int inner;                // V-cycles per outer iteration (defect correction)
@@ -101,6 +139,12 @@ template <class T> __device__ __forceinline__ T *XS(const BatchDev &B, int p, in
 }
 template <class T> __device__ __forceinline__ T *FP(const BatchDev &B, int p, int l) { return (T *)B.f[p * BP_MAXL + l]; }
 template <class T> __device__ __forceinline__ T *RP(const BatchDev &B, int p, int l) { return (T *)B.r[p * BP_MAXL + l]; }
+template <class T> __device__ __forceinline__ T H2(const BatchDev &B, int p, int l);
+template <> __device__ __forceinline__ double H2<double>(const BatchDev &B, int p, int l) { return B.h2d[p * BP_MAXL + l]; }
+template <> __device__ __forceinline__ float H2<float>(const BatchDev &B, int p, int l) { return B.h2f[p * BP_MAXL + l]; }
+template <class T> __device__ __forceinline__ T IH2(const BatchDev &B, int p, int l);
+template <> __device__ __forceinline__ double IH2<double>(const BatchDev &B, int p, int l) { return B.ih2d[p * BP_MAXL + l]; }
+template <> __device__ __forceinline__ float IH2<float>(const BatchDev &B, int p, int l) { return B.ih2f[p * BP_MAXL + l]; }
 
 // ---------------------------------------------------------------------------
 // Tile operations
@@ -167,9 +211,8 @@ __device__ __forceinline__ void tile_phase(T *sx, const T *sf, int ox, int oy, i
 }
 
 template <class T, int H>
-__device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int ox, int oy, int x0, int y0, int n, int nu)
+__device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int ox, int oy, int x0, int y0, int n, T h2, int nu)
 {
-    const T h = (T)1 / (T)(n - 1), h2 = h * h;
     for (int s = 0; s < nu; ++s) {
         tile_phase<T, H>(sx, sf, ox, oy, x0, y0, n, h2, H - 1 - 2 * s, 0);
         tile_phase<T, H>(sx, sf, ox, oy, x0, y0, n, h2, H - 2 - 2 * s, 1);
@@ -254,13 +297,13 @@ __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, 
     if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
     tile_load<T, H>(sx, sf, XS<T>(B, e.p, l, src), FP<T>(B, e.p, l), ox, oy, n, zero_init != 0, true);
     __syncthreads();
-    tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, NU);
+    tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
     tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     if (RESTRICT) {
         // residual on the tile plus one ring, in place of f, one colour at a
         // time (each point reads f only at itself and x, which stays put)
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        const T h = (T)1 / (T)(n - 1), ih2 = (T)1 / (h * h);
+        const T ih2 = IH2<T>(B, e.p, l);
         for (int q = 0; q < 2; ++q)
             for (int gy = y0 - 1 + warp; gy <= y0 + TY; gy += nw) {
                 const int r = gy - oy, row = r * LY::SXH;
@@ -355,7 +398,7 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
         if (NU > 0) sf[q] = fv;
     }
     __syncthreads();
-    if (NU > 0) tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, NU);
+    if (NU > 0) tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
     tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     __syncthreads();
 }
@@ -419,7 +462,7 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
     for (int l = d0; l < L - 1; ++l) {
         const int n = B.n_of[p * BP_MAXL + l], nc = B.n_of[p * BP_MAXL + l + 1];
         T *x = X + off[l], *f = F + off[l];
-        const T h = (T)1 / (T)(n - 1), h2 = h * h, ih2 = (T)1 / h2;
+        const T h2 = H2<T>(B, p, l), ih2 = IH2<T>(B, p, l);
         for (int s = 0; s < nu1; ++s) { loc_rb_half(x, f, n, h2, 0); loc_rb_half(x, f, n, h2, 1); }
         T *fc = F + off[l + 1];
         const int mc = nc - 2;
@@ -437,8 +480,7 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
     }
     {
         const int n = B.n_of[p * BP_MAXL + L - 1];
-        const T h = (T)1 / (T)(n - 1);
-        loc_rb_half(X + off[L - 1], F + off[L - 1], n, h * h, 0);
+        loc_rb_half(X + off[L - 1], F + off[L - 1], n, H2<T>(B, p, L - 1), 0);
     }
     for (int l = L - 2; l >= d0; --l) {
         const int n = B.n_of[p * BP_MAXL + l], nc = B.n_of[p * BP_MAXL + l + 1], m = n - 2;
@@ -463,7 +505,7 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
             x[c] = x[c] + v;
         }
         __syncthreads();
-        const T h = (T)1 / (T)(n - 1), h2 = h * h;
+        const T h2 = H2<T>(B, p, l);
         for (int s = 0; s < nu2; ++s) { loc_rb_half(x, f, n, h2, 0); loc_rb_half(x, f, n, h2, 1); }
     }
     {
@@ -508,22 +550,32 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const double 
         sp[i] = (gy >= 0 && gy < n && gx >= 0 && gx < n) ? psi[(size_t)gy * n + gx] : 0.0;
     }
     __syncthreads();
-    const double h = 1.0 / (double)(n - 1), ih2 = 1.0 / (h * h);
+    const double ih2 = B.ih2d[e.p * BP_MAXL];
     float *f32 = store_r ? FP<float>(B, e.p, 0) : nullptr;
-    double acc = 0.0;
+    // one accumulator per column group: the sum of squares is a dependent
+    // FP64 chain, and TX / 32 independent chains let the points overlap
+    double accs[TX / 32];
+#pragma unroll
+    for (int a = 0; a < TX / 32; ++a) accs[a] = 0.0;
     const int gxa = max(x0, 1), gxb = min(x0 + TX, n - 1);
     const int gya = max(y0, 1), gyb = min(y0 + TY, n - 1);
     for (int gy = gya + warp; gy < gyb; gy += nw) {
-        for (int gx = gxa + lane; gx < gxb; gx += 32) {
+#pragma unroll
+        for (int a = 0; a < TX / 32; ++a) {
+            const int gx = x0 + lane + 32 * a;
+            if (gx < gxa || gx >= gxb) continue;
             const int q = (gy - oy) * SX + gx - ox;
             const size_t g = (size_t)gy * n + gx;
             const double s = (sp[q - 1] + sp[q + 1]) + (sp[q - SX] + sp[q + SX]);
             const double lap = __fma_rn(-4.0, sp[q], s);
             const double r = __fma_rn(-ih2, lap, f[g]);
-            acc = __fma_rn(r, r, acc);
+            accs[a] = __fma_rn(r, r, accs[a]);
             if (store_r) f32[g] = d2f_rn(r);
         }
     }
+    double acc = 0.0;
+#pragma unroll
+    for (int a = 0; a < TX / 32; ++a) acc += accs[a];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) s_red[warp] = acc;
     __syncthreads();
@@ -713,6 +765,7 @@ struct gb_batch {
     size_t pool_bytes = 0;
     int *d_int = nullptr;
     double *d_dbl = nullptr;
+    void *d_spacing = nullptr;          // h^2 and 1/h^2 per (problem, level): FP64 then FP32
     void **d_ptrs = nullptr;
     TileEntry *d_tiles = nullptr;
     std::vector<int> ft_off, ft_cnt;    // per level: tiles of problems with l < dloc
@@ -1065,6 +1118,25 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     BTRY(cudaMalloc(&b->d_int, sizeof(int) * nint));
     BTRY(cudaMemset(b->d_int, 0, sizeof(int) * nint));
     BTRY(cudaMalloc(&b->d_dbl, sizeof(double) * (2 * (size_t)nprob + (size_t)b->ot_cnt)));
+    const size_t nsp = (size_t)nprob * BP_MAXL;
+    BTRY(cudaMalloc(&b->d_spacing, (sizeof(double) + sizeof(float)) * 2 * nsp));
+    {
+        std::vector<double> hd(2 * nsp, 0.0);
+        std::vector<float> hf(2 * nsp, 0.0f);
+        for (size_t k = 0; k < nsp; ++k) {
+            const int m = nof[k];
+            if (m < 2) continue;
+            const double h = 1.0 / (double)(m - 1);
+            hd[k] = h * h;
+            hd[nsp + k] = 1.0 / hd[k];
+            const float hs = 1.0f / (float)(m - 1);
+            hf[k] = hs * hs;
+            hf[nsp + k] = 1.0f / hf[k];
+        }
+        BTRY(cudaMemcpy(b->d_spacing, hd.data(), sizeof(double) * 2 * nsp, cudaMemcpyHostToDevice));
+        BTRY(cudaMemcpy((char *)b->d_spacing + sizeof(double) * 2 * nsp, hf.data(), sizeof(float) * 2 * nsp,
+                        cudaMemcpyHostToDevice));
+    }
     // pointer tables: x (two buffers per level), f (one per level), psi and f of level 0
     const size_t nptr = 2 * (size_t)nprob * BP_MAXL + (size_t)nprob * BP_MAXL + 2 * (size_t)nprob;
     BTRY(cudaMalloc(&b->d_ptrs, sizeof(void *) * nptr));
@@ -1125,6 +1197,10 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     D.f = dp + b->hx.size();
     D.r = nullptr;
     D.psi = b->d_psi_tab;
+    D.h2d = (const double *)b->d_spacing;
+    D.ih2d = D.h2d + nsp;
+    D.h2f = (const float *)(D.h2d + 2 * nsp);
+    D.ih2f = D.h2f + nsp;
     D.active = d_active;
     D.cycles = d_cycles;
     D.failed = d_failed;
@@ -1169,6 +1245,7 @@ extern "C" int gb_batch_destroy(gb_batch *b)
     cudaFree(b->pool);
     cudaFree(b->d_int);
     cudaFree(b->d_dbl);
+    cudaFree(b->d_spacing);
     cudaFree(b->d_ptrs);
     cudaFree(b->d_tiles);
     cudaFree(b->d_ops);
@@ -1516,4 +1593,94 @@ extern "C" int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi
     cudaMemcpyAsync(h_psi, d + b->total, sizeof(double) * (size_t)b->total, cudaMemcpyDeviceToHost, b->stream);
     GB_CUDA_TRY(cudaStreamSynchronize(b->stream));
     return st;
+}
+
+// ---------------------------------------------------------------------------
+// Self-check of the integer-pipe conversions against the hardware ones.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long cvt_mix(unsigned long long z)
+{
+    // splitmix64 finaliser (Steele, Lea and Flood, 2014)
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ bool cvt_same_f(float a, float b)
+{
+    return __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
+}
+__device__ __forceinline__ bool cvt_same_d(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
+}
+
+// Every float bit pattern through f2d.
+__global__ void k_cvt_check_f2d(unsigned long long *bad)
+{
+    unsigned long long cnt = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < (1ull << 32); i += stride) {
+        const float v = __uint_as_float((unsigned int)i);
+        if (!cvt_same_d(f2d(v), (double)v)) ++cnt;
+    }
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+// n seeded double bit patterns through d2f_rn: exponents drawn over the
+// whole range or around the float range, fractions random or with the
+// dropped bits set to a tie or one unit either side of it.
+__global__ void k_cvt_check_d2f(unsigned long long n, unsigned long long seed, unsigned long long *bad)
+{
+    unsigned long long cnt = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long h = cvt_mix(seed ^ cvt_mix(i)), h2 = cvt_mix(h);
+        unsigned long long bits = h;
+        const unsigned int kind = (unsigned int)(h2 & 7u);
+        if (kind != 0u) {
+            const unsigned long long e = (kind == 1u) ? (h2 >> 8) & 0x7ffull : 850ull + ((h2 >> 8) % 310ull);
+            unsigned long long m = h & 0xFFFFFFFFFFFFFull;
+            // bits dropped by the rounding: 29 in the normal range, more below
+            const int sh = (e >= 897ull) ? 29 : (int)min(52ull, 926ull - e);
+            const unsigned long long low = (1ull << sh) - 1ull, half = 1ull << (sh - 1);
+            const unsigned int tie = (unsigned int)((h2 >> 24) & 7u);
+            if (tie == 0u) m = (m & ~low) | half;
+            else if (tie == 1u) m = (m & ~low) | (half - 1ull);
+            else if (tie == 2u) m = (m & ~low) | (half + 1ull);
+            else if (tie == 3u) m = (m & ~low) | low;
+            bits = (h & 0x8000000000000000ull) | (e << 52) | m;
+        }
+        const double x = __longlong_as_double((long long)bits);
+        if (!cvt_same_f(d2f_rn(x), __double2float_rn(x))) ++cnt;
+    }
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+extern "C" int gb_check_conversions(long long n_random, unsigned long long seed, long long *mismatches_f2d,
+                                    long long *mismatches_d2f)
+{
+    if (n_random < 0 || !mismatches_f2d || !mismatches_d2f) {
+        gb_set_error("gb_check_conversions: invalid arguments");
+        return GB_ERR_INVALID;
+    }
+    unsigned long long *d = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+    cudaError_t e = cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        k_cvt_check_f2d<<<152 * 8, 256>>>(d);
+        if (n_random > 0) k_cvt_check_d2f<<<152 * 8, 256>>>((unsigned long long)n_random, seed, d + 1);
+        e = cudaGetLastError();
+    }
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        gb_set_error("gb_check_conversions: %s", cudaGetErrorString(e));
+        return GB_ERR_CUDA;
+    }
+    *mismatches_f2d = (long long)h[0];
+    *mismatches_d2f = (long long)h[1];
+    return GB_OK;
 }

@@ -207,6 +207,7 @@ SIGNATURES = [
     ("gb_batch_profile_read", C.c_int, [_vp, _dp, C.POINTER(C.c_longlong), _dp, C.c_int]),
     ("gb_batch_profile_read_kind", C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp]),
     ("gb_measure_issue_rates", C.c_int, [_dp, _dp]),
+    ("gb_check_conversions", C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
 ]
 
 

@@ -595,6 +595,14 @@ int gb_batch_profile_read_kind(gb_batch *b, int kind, double *ms, long long *lau
  * (instructions per second, every SM busy); the FP64 figure is the peak the
  * FP64-bound kernels are measured against. */
 int gb_measure_issue_rates(double *fp64_fma_per_s, double *fp32_fma_per_s);
+/* Compares the batched solver's integer-pipe float <-> double conversions
+ * with the hardware conversions on the current device: every float bit
+ * pattern through float -> double, and n_random seeded double bit patterns
+ * (whole exponent range, the float range and its edges, rounding ties and
+ * their neighbours) through double -> float.  The counts of differing
+ * results go to *mismatches_f2d and *mismatches_d2f (two NaNs agree). */
+int gb_check_conversions(long long n_random, unsigned long long seed, long long *mismatches_f2d,
+                         long long *mismatches_d2f);
 
 #ifdef __cplusplus
 }

@@ -113,3 +113,14 @@ def test_graph_and_persistent_agree_on_workload_sizes(gblib):
         out.append((psi, cyc))
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+def test_integer_conversions_match_hardware(gblib):
+    """The mixed solve converts the defect to FP32 and the correction back
+    to FP64 with integer operations; over every float bit pattern and 2^26
+    seeded double patterns (ties, denormals, overflow, NaN and infinity
+    included) they equal the hardware conversions."""
+    import ctypes as C
+    f2d, d2f = C.c_longlong(-1), C.c_longlong(-1)
+    assert gblib.gb_check_conversions(1 << 26, 20261203, C.byref(f2d), C.byref(d2f)) == 0
+    assert (f2d.value, d2f.value) == (0, 0)
