@@ -256,25 +256,44 @@ __device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, 
         }
 }
 
-// Loads x (or zeros) and f over the tile plus an H halo.
+// Loads x (or zeros) and f over the tile plus an H halo: warps step
+// through the rows, lanes through the columns (coalesced in global memory;
+// no division and one row base per row).
 template <class T, int H>
 __device__ __forceinline__ void tile_load(T *sx, T *sf, const T *x, const T *f, int ox, int oy, int n,
                                           bool zero_x, bool load_f)
 {
-    constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
-#pragma unroll 4
-    for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
-        const int r = i / SX, c = i - r * SX;
-        const int gy = oy + r, gx = ox + c;
-        T v = (T)0, fv = (T)0;
-        if (gy >= 0 && gy < n && gx >= 0 && gx < n) {
-            const size_t g = (size_t)gy * n + gx;
-            if (load_f) fv = f[g];
-            if (!zero_x) v = x[g];
+    using LY = TileLayout<T, H>;
+    constexpr int SX = LY::SX, SY = LY::SY;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = warp; r < SY; r += TILE_THREADS / 32) {
+        const int gy = oy + r;
+        const bool rin = gy >= 0 && gy < n;
+        const size_t base = rin ? (size_t)gy * n : 0;
+        const T *xr = x + base, *fr = f + base;
+        T *xs = sx + r * LY::SXH, *fs = sf + r * LY::SXH;
+        constexpr int NJ = (SX + 31) / 32;
+        T v[NJ], fv[NJ];
+        // all loads of the row first, then the shared stores
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int c = lane + 32 * j, gx = ox + c;
+            v[j] = (T)0;
+            fv[j] = (T)0;
+            if (c < SX && rin && gx >= 0 && gx < n) {
+                if (load_f) fv[j] = fr[gx];
+                if (!zero_x) v[j] = xr[gx];
+            }
         }
-        const int q = TileLayout<T, H>::at(r, c);
-        sx[q] = v;
-        if (load_f) sf[q] = fv;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int c = lane + 32 * j;
+            if (c < SX) {
+                const int q = ((r + c) & 1) * LY::HALF + (c >> 1);
+                xs[q] = v[j];
+                if (load_f) fs[q] = fv[j];
+            }
+        }
     }
 }
 
