@@ -9,9 +9,11 @@ One step = one solve of the whole batch.  value = cell-updates/s (interior
 points x V-cycles / second) of the FP32-inner / FP64-defect-correction path,
 with inputs resident in HBM; the plain FP64 path is timed the same way and
 reported beside it; e2e repeats the mixed solve through the C ABI's host-
-buffer entry point (gb_batch_solve_host) with pinned host arrays, so the
-host->device copy of f and the device->host copy of psi are inside the
-timed region.
+buffer entry points with pinned host arrays, so every step's host->device
+copy of f and device->host copy of psi are inside the timed region: as a
+stream of steps (gb_batch_submit_host / gb_batch_drain, each step's copies
+overlapping the neighbouring steps' solves) for e2e.value, and one call per
+step (gb_batch_solve_host: copy in, solve, copy out) for e2e.serial_value.
 
 --impl reference times the CPU restatement of the same algorithm (oracle/,
 OpenMP over problems, all host threads) on a bounded sample of problems.
@@ -767,20 +769,38 @@ def main():
         L.gb_batch_solve_host(mixed._h, h_f.data_ptr(), h_psi.data_ptr(), cycp.ctypes.data, rrp.ctypes.data)
     barrier()
     t0 = time.perf_counter()
-    e2e_cu = 0.0
+    serial_cu = 0.0
     for _ in range(args.steps):
         st = L.gb_batch_solve_host(mixed._h, h_f.data_ptr(), h_psi.data_ptr(), cycp.ctypes.data, rrp.ctypes.data)
         assert st == 0, lib.last_error()
-        e2e_cu += float(np.sum(cu_per_cycle * cycp))
+        serial_cu += float(np.sum(cu_per_cycle * cycp))
+    barrier()
+    serial_s = time.perf_counter() - t0
+    # the same steps as a stream of calls (gb_batch_submit_host): each step
+    # still uploads its f and downloads its psi, the copies overlapping the
+    # neighbouring steps' solves; two psi buffers, cycle counts per step
+    h_psi2 = [h_psi, torch.zeros(total, dtype=torch.float64).pin_memory()]
+    cyc_k = [np.zeros(len(sizes), dtype=np.int32) for _ in range(args.steps)]
+    rr_k = [np.zeros(len(sizes)) for _ in range(args.steps)]
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        st = L.gb_batch_submit_host(mixed._h, h_f.data_ptr(), h_psi2[k & 1].data_ptr(), cyc_k[k].ctypes.data,
+                                    rr_k[k].ctypes.data)
+        assert st == 0, lib.last_error()
+    st = L.gb_batch_drain(mixed._h)
+    assert st == 0, lib.last_error()
     barrier()
     e2e_s = time.perf_counter() - t0
+    e2e_cu = float(sum(np.sum(cu_per_cycle * c) for c in cyc_k))
+    assert np.array_equal(h_psi2[0].numpy(), h_psi2[1].numpy()) or args.steps < 2
     if ws > 1:
         import torch.distributed as dist
-        t = torch.tensor([e2e_s, e2e_cu], dtype=torch.float64, device="cuda")
+        t = torch.tensor([e2e_s, e2e_cu, serial_s, serial_cu], dtype=torch.float64, device="cuda")
         mx = t.clone()
         dist.all_reduce(mx, op=dist.ReduceOp.MAX)
         dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        e2e_s, e2e_cu = float(mx[0]), float(t[1])
+        e2e_s, e2e_cu, serial_s, serial_cu = float(mx[0]), float(t[1]), float(mx[2]), float(t[3])
 
     if rank != 0:
         if ws > 1:
@@ -823,7 +843,11 @@ def main():
         "persistent_single_launch": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / max(3, args.steps // 4),
                                      "identical_to_graph_mode": pers_same},
         "e2e": {"value": e2e_cu / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": total * 8,
-                "d2h_bytes_per_step": total * 8},
+                "d2h_bytes_per_step": total * 8,
+                "api": "gb_batch_submit_host/gb_batch_drain (a stream of steps; copies overlap the neighbouring "
+                       "steps' solves)",
+                "serial_value": serial_cu / serial_s,
+                "serial_api": "gb_batch_solve_host (one step per call: copy in, solve, copy out)"},
         "roofline": {"bound": "hbm",
                      "kernel": "k_op<float,OP_SMOOTH_R,2> (finest level: two red-black sweeps + residual + restriction)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -51,6 +51,27 @@ class BatchPoisson:
                                            rr.ctypes.data)
         return st, psi, cyc, rr
 
+    def solve_stream(self, fs):
+        """Solves a sequence of right-hand sides through the pipelined
+        host-buffer calls (gb_batch_submit_host / gb_batch_drain): each
+        upload and download overlaps a neighbouring call's solve.  Returns
+        one (status, psi, cycles, relres) per right-hand side."""
+        L = _L.load()
+        keep, out, sts = [], [], []
+        for f in fs:
+            f = np.ascontiguousarray(f, dtype=np.float64)
+            assert f.size == self.total
+            psi = np.zeros(self.total)
+            cyc = np.zeros(self.nprob, dtype=np.int32)
+            rr = np.zeros(self.nprob)
+            keep.append(f)
+            out.append((psi, cyc, rr))
+            sts.append(L.gb_batch_submit_host(self._h, f.ctypes.data, psi.ctypes.data, cyc.ctypes.data,
+                                              rr.ctypes.data))
+        sts.append(L.gb_batch_drain(self._h))
+        # a submit returns the status of the solve submitted before it
+        return [(sts[i + 1],) + out[i] for i in range(len(out))]
+
     def last_launches(self):
         return int(_L.load().gb_batch_last_launches(self._h))
 

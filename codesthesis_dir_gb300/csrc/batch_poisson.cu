@@ -795,6 +795,17 @@ struct gb_batch {
     size_t local_smem = 0;
     int *h_pinned = nullptr;
     double *host_stage = nullptr;       // f and psi of gb_batch_solve_host, allocated on first use
+    // pipelined host-buffer solves (gb_batch_submit_host): two slots of f and
+    // psi, an upload and a download stream, and the one submitted call whose
+    // solve has not run yet
+    double *pipe_buf = nullptr;
+    cudaStream_t up = nullptr, down = nullptr;
+    cudaEvent_t ev_up[2] = {nullptr, nullptr}, ev_solved[2] = {nullptr, nullptr}, ev_down[2] = {nullptr, nullptr};
+    int pipe_next = 0;
+    bool pend = false;
+    int pend_slot = 0;
+    double *pend_psi = nullptr, *pend_relres = nullptr;
+    int *pend_cycles = nullptr;
     cudaStream_t stream = nullptr;
     // operation lists (first iteration, later iterations) and their device copies
     std::vector<Op> ops0, ops;
@@ -1270,6 +1281,16 @@ extern "C" int gb_batch_destroy(gb_batch *b)
     cudaFree(b->d_ops);
     cudaFree(b->d_sync);
     cudaFree(b->host_stage);
+    if (b->up) cudaStreamSynchronize(b->up);
+    if (b->down) cudaStreamSynchronize(b->down);
+    for (int i = 0; i < 2; ++i) {
+        if (b->ev_up[i]) cudaEventDestroy(b->ev_up[i]);
+        if (b->ev_solved[i]) cudaEventDestroy(b->ev_solved[i]);
+        if (b->ev_down[i]) cudaEventDestroy(b->ev_down[i]);
+    }
+    if (b->up) cudaStreamDestroy(b->up);
+    if (b->down) cudaStreamDestroy(b->down);
+    cudaFree(b->pipe_buf);
     if (b->h_pinned) cudaFreeHost(b->h_pinned);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -1611,6 +1632,77 @@ extern "C" int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi
     int st = gb_batch_solve_device(b, d, d + b->total, cycles, relres, b->stream);
     cudaMemcpyAsync(h_psi, d + b->total, sizeof(double) * (size_t)b->total, cudaMemcpyDeviceToHost, b->stream);
     GB_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    return st;
+}
+
+// Pipelined host-buffer solves.  Call k's right-hand side goes up on the
+// upload stream while call k-1 solves on the solve stream, and call k-1's
+// solution comes down on the download stream while call k solves: the
+// copies of a stream of calls hide behind the solves.
+static int pipe_alloc(gb_batch *b)
+{
+    if (b->pipe_buf) return GB_OK;
+    cudaError_t e = cudaMalloc((void **)&b->pipe_buf, sizeof(double) * 4 * (size_t)b->total);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->down, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaEventCreateWithFlags(&b->ev_up[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_solved[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_down[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        gb_set_error("gb_batch_submit_host: pipeline buffers: %s", cudaGetErrorString(e));
+        return GB_ERR_ALLOC;
+    }
+    return GB_OK;
+}
+
+// Runs the solve of the submitted call and queues its solution's download.
+static int pipe_finish(gb_batch *b)
+{
+    b->pend = false;
+    const int slot = b->pend_slot;
+    double *f = b->pipe_buf + (size_t)slot * 2 * (size_t)b->total, *psi = f + b->total;
+    GB_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_up[slot], 0));
+    GB_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_down[slot], 0));   // the slot's previous download
+    const int st = gb_batch_solve_device(b, f, psi, b->pend_cycles, b->pend_relres, b->stream);
+    GB_CUDA_TRY(cudaEventRecord(b->ev_solved[slot], b->stream));
+    GB_CUDA_TRY(cudaStreamWaitEvent(b->down, b->ev_solved[slot], 0));
+    GB_CUDA_TRY(cudaMemcpyAsync(b->pend_psi, psi, sizeof(double) * (size_t)b->total, cudaMemcpyDeviceToHost, b->down));
+    GB_CUDA_TRY(cudaEventRecord(b->ev_down[slot], b->down));
+    return st;
+}
+
+extern "C" int gb_batch_submit_host(gb_batch *b, const double *h_f, double *h_psi, int *cycles, double *relres)
+{
+    if (!b || !h_f || !h_psi) { gb_set_error("gb_batch_submit_host: null argument"); return GB_ERR_INVALID; }
+    int st = pipe_alloc(b);
+    if (st != GB_OK) return st;
+    const int slot = b->pipe_next;
+    b->pipe_next ^= 1;
+    double *f = b->pipe_buf + (size_t)slot * 2 * (size_t)b->total;
+    // the slot's f was last read by a solve that has returned (solves run
+    // on this thread, one call behind)
+    GB_CUDA_TRY(cudaMemcpyAsync(f, h_f, sizeof(double) * (size_t)b->total, cudaMemcpyHostToDevice, b->up));
+    GB_CUDA_TRY(cudaEventRecord(b->ev_up[slot], b->up));
+    st = b->pend ? pipe_finish(b) : GB_OK;
+    // call k-2 (this slot's last user) has its solution on the host when
+    // this returns
+    GB_CUDA_TRY(cudaEventSynchronize(b->ev_down[slot]));
+    b->pend = true;
+    b->pend_slot = slot;
+    b->pend_psi = h_psi;
+    b->pend_cycles = cycles;
+    b->pend_relres = relres;
+    return st;
+}
+
+extern "C" int gb_batch_drain(gb_batch *b)
+{
+    if (!b) { gb_set_error("gb_batch_drain: null handle"); return GB_ERR_INVALID; }
+    const int st = b->pend ? pipe_finish(b) : GB_OK;
+    if (b->down) GB_CUDA_TRY(cudaStreamSynchronize(b->down));
+    if (b->up) GB_CUDA_TRY(cudaStreamSynchronize(b->up));
     return st;
 }
 

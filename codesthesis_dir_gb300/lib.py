@@ -202,6 +202,8 @@ SIGNATURES = [
     ("gb_batch_set_exec", C.c_int, [_vp, C.c_int]),
     ("gb_batch_solve_device", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("gb_batch_solve_host", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("gb_batch_submit_host", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("gb_batch_drain", C.c_int, [_vp]),
     ("gb_batch_last_launches", C.c_longlong, [_vp]),
     ("gb_batch_profile", C.c_int, [_vp, C.c_int]),
     ("gb_batch_profile_read", C.c_int, [_vp, _dp, C.POINTER(C.c_longlong), _dp, C.c_int]),

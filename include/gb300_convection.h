@@ -571,6 +571,19 @@ int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_psi, int *cy
  * keeps until gb_batch_destroy. */
 int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi, int *cycles,
                         double *relres);
+/* Pipelined host-buffer solves for a stream of calls: call k's h_f is
+ * uploaded on its own stream while call k-1 solves, and call k-1's solution
+ * is downloaded on another while call k solves.  A submit queues call k's
+ * upload, then runs the solve of the call submitted before it and returns
+ * that solve's status (GB_OK when there was none); gb_batch_drain runs the
+ * last submitted solve, waits for every download and returns its status.
+ * Call k's cycles and relres are written when call k+1's submit (or the
+ * drain) returns, its h_psi when the drain returns or call k+2's submit
+ * has; h_f must stay unchanged until call k+1's submit returns.  Host
+ * buffers should be page-locked for the copies to overlap.  The first
+ * submit allocates 4 x total doubles that the handle keeps. */
+int gb_batch_submit_host(gb_batch *b, const double *h_f, double *h_psi, int *cycles, double *relres);
+int gb_batch_drain(gb_batch *b);
 /* Number of kernel launches the last solve issued. */
 long long gb_batch_last_launches(const gb_batch *b);
 /* Times every launch of the finest-level smoothing kernel with CUDA events

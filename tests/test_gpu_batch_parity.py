@@ -124,3 +124,31 @@ def test_integer_conversions_match_hardware(gblib):
     f2d, d2f = C.c_longlong(-1), C.c_longlong(-1)
     assert gblib.gb_check_conversions(1 << 26, 20261203, C.byref(f2d), C.byref(d2f)) == 0
     assert (f2d.value, d2f.value) == (0, 0)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_pipelined_stream_matches_single_calls(gblib, precision):
+    """A stream of different right-hand sides through the pipelined calls
+    (upload of call k and download of call k-1 overlapping the solves) gives
+    each call exactly what a lone host-buffer solve gives, including a
+    maximum-cycle failure in the middle of the stream; the handle solves
+    plainly again after the drain."""
+    from codesthesis_dir_gb300.batch import BatchPoisson
+    sizes = [257, 65, 129, 513, 33]
+    fs = [make_batch(sizes, 40 + i) for i in range(5)]
+    fs[2] = fs[2] * 1e30          # large magnitudes (still inside the FP32 range in the inner cycles)
+    bp = BatchPoisson(sizes, precision=precision)
+    ref = [bp.solve_host(f) for f in fs]
+    got = bp.solve_stream(fs)
+    assert len(got) == len(fs)
+    for (st, psi, cyc, rr), (st0, psi0, cyc0, rr0) in zip(got, ref):
+        assert st == st0 == 0
+        np.testing.assert_array_equal(psi, psi0)
+        np.testing.assert_array_equal(cyc, cyc0)
+        np.testing.assert_array_equal(rr, rr0)
+    assert gblib.gb_batch_drain(bp._h) == 0          # nothing pending
+    st, psi, cyc, rr = bp.solve_host(fs[0])
+    np.testing.assert_array_equal(psi, ref[0][1])
+    short = BatchPoisson(sizes, precision=precision, max_cycles=2, rtol=1e-14)
+    res = short.solve_stream(fs[:3])
+    assert [r[0] for r in res] == [1, 1, 1] and all(np.all(r[2] == 2) for r in res)
