@@ -182,29 +182,75 @@ template <class T, int H> struct TileLayout {
     __device__ static __forceinline__ int at(int r, int c) { return ((r + c) & 1) * HALF + r * SXH + (c >> 1); }
 };
 
+// One row of a red-black phase: the points of one colour between the
+// bounds, as consecutive words of one half (c = 2k + odd; the row neighbours
+// c -+ 1 are k - 1 + odd and k + odd of the other half).
+template <class T> struct PhaseRow {
+    T *X;
+    const T *F, *N;
+    int odd, k0, kend;
+};
+
+template <class T, int H>
+__device__ __forceinline__ PhaseRow<T> phase_row(T *sx, const T *sf, int gy, int oy, int ox, int gxa, int gxb,
+                                                 int color)
+{
+    using LY = TileLayout<T, H>;
+    const int row = (gy - oy) * LY::SXH;
+    const int first = gxa + ((gxa + gy + color) & 1);
+    const int c0 = first - ox, odd = c0 & 1;
+    PhaseRow<T> R;
+    R.X = sx + color * LY::HALF + row;
+    R.F = sf + color * LY::HALF + row;
+    R.N = sx + (color ^ 1) * LY::HALF + row;
+    R.odd = odd;
+    R.k0 = c0 >> 1;
+    R.kend = (gxb - ox - odd + 1) >> 1;
+    return R;
+}
+
+template <class T, int H>
+__device__ __forceinline__ void phase_point(const PhaseRow<T> &R, int k, T h2)
+{
+    using LY = TileLayout<T, H>;
+    const T s = (R.N[k - 1 + R.odd] + R.N[k + R.odd]) + (R.N[k - LY::SXH] + R.N[k + LY::SXH]);
+    R.X[k] = fmaT<T>(-h2, R.F[k], s) * (T)0.25;
+}
+
 // One red (color 0) or black (color 1) phase on ring rho around the tile.
-// The smem tile has origin (ox, oy) in grid coordinates, colour-split.
+// The smem tile has origin (ox, oy) in grid coordinates, colour-split.  A
+// row holds at most SXH = 64 + H points of a colour, so a warp covers the
+// first 64 of each of two rows in two passes per row and the rest of both
+// (at most H each) in one shared pass: half the lanes per row.
 template <class T, int H>
 __device__ __forceinline__ void tile_phase(T *sx, const T *sf, int ox, int oy, int x0, int y0, int n, T h2,
                                            int rho, int color)
 {
-    using LY = TileLayout<T, H>;
+    static_assert(TileLayout<T, H>::SXH <= 64 + 16, "row remainder must fit in half a warp");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int gxa = max(x0 - rho, 1), gxb = min(x0 + TX + rho, n - 1);
     const int gya = max(y0 - rho, 1), gyb = min(y0 + TY + rho, n - 1);
-    for (int gy = gya + warp; gy < gyb; gy += nw) {
-        const int r = gy - oy, row = r * LY::SXH;
-        const int first = gxa + ((gxa + gy + color) & 1);
-        // points c = 2k + odd of this row; their row neighbours c -+ 1 are
-        // k - 1 + odd and k + odd of the other half
-        const int c0 = first - ox, odd = c0 & 1, kend = (gxb - ox - odd + 1) >> 1;
-        T *X = sx + color * LY::HALF + row;
-        const T *F = sf + color * LY::HALF + row;
-        const T *N = sx + (color ^ 1) * LY::HALF + row;
-        const T *Nu = N - LY::SXH, *Nd = N + LY::SXH;
-        for (int k = (c0 >> 1) + lane; k < kend; k += 32) {
-            const T s = (N[k - 1 + odd] + N[k + odd]) + (Nu[k] + Nd[k]);
-            X[k] = fmaT<T>(-h2, F[k], s) * (T)0.25;
+    for (int gy = gya + warp; gy < gyb; gy += 2 * nw) {
+        const PhaseRow<T> A = phase_row<T, H>(sx, sf, gy, oy, ox, gxa, gxb, color);
+        const bool two = gy + nw < gyb;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int k = A.k0 + lane + 32 * j;
+            if (k < A.kend) phase_point<T, H>(A, k, h2);
+        }
+        if (two) {
+            const PhaseRow<T> B = phase_row<T, H>(sx, sf, gy + nw, oy, ox, gxa, gxb, color);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int k = B.k0 + lane + 32 * j;
+                if (k < B.kend) phase_point<T, H>(B, k, h2);
+            }
+            const PhaseRow<T> &R = lane < 16 ? A : B;
+            const int k = R.k0 + 64 + (lane & 15);
+            if (k < R.kend) phase_point<T, H>(R, k, h2);
+        } else if (lane < 16) {
+            const int k = A.k0 + 64 + lane;
+            if (k < A.kend) phase_point<T, H>(A, k, h2);
         }
     }
     __syncthreads();
@@ -721,8 +767,10 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
 }
 
 // One kernel launch per operation (graph path).
+// The correction-store variants hold the prefetched psi values (16 doubles
+// per thread) across the sweeps; four blocks per SM keep them at 64 registers.
 template <class T, int KIND, int NU, bool CORR>
-__global__ void __launch_bounds__(TILE_THREADS) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
+__global__ void __launch_bounds__(TILE_THREADS, CORR ? 4 : 1) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
                                                      Op op, int nu1, int nu2)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
