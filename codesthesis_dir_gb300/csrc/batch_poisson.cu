@@ -365,31 +365,41 @@ __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, 
     tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
     tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     if (RESTRICT) {
-        // residual on the tile plus one ring, in place of f, one colour at a
-        // time (each point reads f only at itself and x, which stays put)
+        // residual on the tile plus one ring, in place of f (each point
+        // reads f only at itself and x, which stays put, so both colours of
+        // a row go in one pass: 65 points each, two full passes per colour
+        // and one shared pass for the last point of each)
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         const T ih2 = IH2<T>(B, e.p, l);
-        for (int q = 0; q < 2; ++q)
-            for (int gy = y0 - 1 + warp; gy <= y0 + TY; gy += nw) {
-                const int r = gy - oy, row = r * LY::SXH;
-                const int first = (x0 - 1) + ((x0 - 1 + gy + q) & 1);
-                const int c0 = first - ox, odd = c0 & 1, kend = (x0 + TX + 1 - ox - odd + 1) >> 1;
-                const T *X = sx + q * LY::HALF + row;
-                T *F = sf + q * LY::HALF + row;
-                const T *N = sx + (q ^ 1) * LY::HALF + row;
-                const T *Nu = N - LY::SXH, *Nd = N + LY::SXH;
-                const bool rin = gy >= 1 && gy <= n - 2;
-                for (int k = (c0 >> 1) + lane; k < kend; k += 32) {
-                    const int gx = 2 * k + odd + ox;
-                    T rv = (T)0;
-                    if (rin && gx >= 1 && gx <= n - 2) {
-                        const T s = (N[k - 1 + odd] + N[k + odd]) + (Nu[k] + Nd[k]);
-                        const T lap = fmaT<T>((T)-4, X[k], s);
-                        rv = fmaT<T>(-ih2, lap, F[k]);
-                    }
-                    F[k] = rv;
+        const int gxa = x0 - 1, gxb = x0 + TX + 1;
+        for (int gy = y0 - 1 + warp; gy <= y0 + TY; gy += nw) {
+            const bool rin = gy >= 1 && gy <= n - 2;
+            const PhaseRow<T> R0 = phase_row<T, H>(sx, sf, gy, oy, ox, gxa, gxb, 0);
+            const PhaseRow<T> R1 = phase_row<T, H>(sx, sf, gy, oy, ox, gxa, gxb, 1);
+            auto res_point = [&](const PhaseRow<T> &R, int k) {
+                const int gx = 2 * k + R.odd + ox;
+                T rv = (T)0;
+                if (rin && gx >= 1 && gx <= n - 2) {
+                    const T s = (R.N[k - 1 + R.odd] + R.N[k + R.odd]) + (R.N[k - LY::SXH] + R.N[k + LY::SXH]);
+                    const T lap = fmaT<T>((T)-4, R.X[k], s);
+                    rv = fmaT<T>(-ih2, lap, R.F[k]);
                 }
+                const_cast<T *>(R.F)[k] = rv;
+            };
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int k = R0.k0 + lane + 32 * j;
+                if (k < R0.kend) res_point(R0, k);
             }
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int k = R1.k0 + lane + 32 * j;
+                if (k < R1.kend) res_point(R1, k);
+            }
+            const PhaseRow<T> &R = lane < 16 ? R0 : R1;
+            const int k = R.k0 + 64 + (lane & 15);
+            if (k < R.kend) res_point(R, k);
+        }
         __syncthreads();
         const int nc = B.n_of[e.p * BP_MAXL + l + 1];
         T *fc = FP<T>(B, e.p, l + 1);
