@@ -442,35 +442,47 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
     const T *x = XS<T>(B, e.p, l, src);
     const T *f = FP<T>(B, e.p, l);
     const T *ec = XS<T>(B, e.p, l + 1, 0);
-#pragma unroll 4
-    for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
-        const int r = i / SX, c = i - r * SX;
-        const int gy = oy + r, gx = ox + c;
-        T v = (T)0, fv = (T)0;
-        if (gy >= 0 && gy < n && gx >= 0 && gx < n) {
-            const size_t g = (size_t)gy * n + gx;
-            v = x[g];
-            if (NU > 0) fv = f[g];
-            if (gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2) {
-                const T *ep = ec + (size_t)(gy / 2) * nc + (gx / 2);
+    // rows by warp, columns by lane.  The row parity is the same for the
+    // whole warp; the column parity alternates between lanes and selects
+    // among the four interpolation forms without a branch.
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = warp; r < SY; r += TILE_THREADS / 32) {
+        const int gy = oy + r;
+        const bool rin = gy >= 0 && gy < n, rint = gy >= 1 && gy <= n - 2, yodd = (gy & 1) != 0;
+        const size_t base = rin ? (size_t)gy * n : 0;
+        const T *xr = x + base, *fr = f + base;
+        const T *er = ec + (rint ? (size_t)(gy / 2) * nc : 0);
+        T *xs = sx + r * LY::SXH, *fs = sf + r * LY::SXH;
+#pragma unroll
+        for (int j = 0; j < (SX + 31) / 32; ++j) {
+            const int c = lane + 32 * j, gx = ox + c;
+            const bool xodd = (gx & 1) != 0;
+            const bool g = c < SX && rin && gx >= 0 && gx < n;
+            const bool in = g && rint && gx >= 1 && gx <= n - 2;
+            T val = g ? xr[gx] : (T)0;
+            const T fv = (NU > 0 && g) ? fr[gx] : (T)0;
+            if (in) {
+                const T *ep = er + (gx / 2);
+                const T e00 = ep[0];
+                const T e01 = xodd ? ep[1] : (T)0;
                 T pr;
-                if ((gx & 1) == 0) {
-                    if ((gy & 1) == 0) pr = ep[0];
-                    else pr = (ep[0] + ep[nc]) * (T)0.5;
+                if (!yodd) {
+                    pr = xodd ? (e00 + e01) * (T)0.5 : e00;
                 } else {
-                    if ((gy & 1) == 0) pr = (ep[0] + ep[1]) * (T)0.5;
-                    else {
-                        T t = ep[0] + ep[nc + 1];
-                        t = t + ep[nc] + ep[1];
-                        pr = t * (T)0.25;
-                    }
+                    const T e10 = ep[nc];
+                    const T e11 = xodd ? ep[nc + 1] : (T)0;
+                    T t = e00 + e11;
+                    t = t + e10 + e01;
+                    pr = xodd ? t * (T)0.25 : (e00 + e10) * (T)0.5;
                 }
-                v = v + pr;
+                val = val + pr;
+            }
+            if (c < SX) {
+                const int q = ((r + c) & 1) * LY::HALF + (c >> 1);
+                xs[q] = val;
+                if (NU > 0) fs[q] = fv;
             }
         }
-        const int q = LY::at(r, c);
-        sx[q] = v;
-        if (NU > 0) sf[q] = fv;
     }
     __syncthreads();
     if (NU > 0) tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
@@ -778,9 +790,11 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
 
 // One kernel launch per operation (graph path).
 // The correction-store variants hold the prefetched psi values (16 doubles
-// per thread) across the sweeps; four blocks per SM keep them at 64 registers.
+// per thread) across the sweeps; four blocks per SM keep them at 64
+// registers.  The other prolongation variants fit five blocks' shared tiles
+// per SM and are held to the registers of five.
 template <class T, int KIND, int NU, bool CORR>
-__global__ void __launch_bounds__(TILE_THREADS, CORR ? 4 : 1) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
+__global__ void __launch_bounds__(TILE_THREADS, CORR ? 4 : (KIND == OP_PROLONG ? 5 : 1)) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
                                                      Op op, int nu1, int nu2)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
