@@ -370,6 +370,32 @@ __device__ __forceinline__ void prb_cfl_reduce(const PrbDev &d, double cu, doubl
     }
 }
 
+// The diagnostics of point (i, k) = c after the step's update: at kt >= 2
+// the running means m = (1/(kt-1)) m (kt-2) + (1/(kt-1)) x of T^2, T, u^2,
+// v^2, and the point's candidates for the CFL maxima (PRB:404-459).
+__device__ __forceinline__ void prb_diag_point(const PrbDev &d, int i, size_t c, double tn, double u, double v,
+                                               double &cu, double &cv)
+{
+    const int kt = *d.diag_kt;
+    if (kt < 2) return;
+    const size_t n = d.diag_stride;
+    double *mT2 = d.diag, *mT = d.diag + n, *mU2 = d.diag + 2 * n, *mV2 = d.diag + 3 * n;
+    const double tkti = 1.0 / (double)(kt - 1), w = (double)(kt - 2);
+    mT2[c] = tkti * mT2[c] * w + tkti * (tn * tn);
+    mT[c] = tkti * mT[c] * w + tkti * tn;
+    mU2[c] = tkti * mU2[c] * w + tkti * (u * u);
+    mV2[c] = tkti * mV2[c] * w + tkti * (v * v);
+    if (i >= 1 && i <= d.nr) {
+        const double x = fabs(u * d.dt / d.dr);
+        if (x > cu) cu = x;
+    }
+    if (i >= 1 && i <= d.nr - 1) {
+        const double r = d.polar ? d.r0 + ((double)i - 0.5) * d.dr : 1.0;
+        const double x = fabs(v * d.dt / (r * d.dp));
+        if (x > cv) cv = x;
+    }
+}
+
 //
 // DIAG: the time loop's diagnostics of the step, fused (PRB:404-459,
 // velvor2dnewsch3.4.f:404-459): at kt >= 2 the running means
@@ -416,28 +442,25 @@ __global__ void k_update(PrbDev d)
         f[GB_F_thn][c] = tn;
         f[GB_F_th][c] = tn;
         if (clamped) atomicAdd(d.clamps, clamped);
-        const int kt = DIAG ? *d.diag_kt : 0;
-        if (DIAG && kt >= 2) {
-            const size_t n = (size_t)ld * (size_t)(np + 1);
-            double *mT2 = d.diag, *mT = d.diag + n, *mU2 = d.diag + 2 * n, *mV2 = d.diag + 3 * n;
-            const double tkti = 1.0 / (double)(kt - 1), w = (double)(kt - 2);
-            const double u = f[GB_F_uel][c], v = f[GB_F_vel][c];
-            mT2[c] = tkti * mT2[c] * w + tkti * (tn * tn);
-            mT[c] = tkti * mT[c] * w + tkti * tn;
-            mU2[c] = tkti * mU2[c] * w + tkti * (u * u);
-            mV2[c] = tkti * mV2[c] * w + tkti * (v * v);
-            if (i >= 1 && i <= nr) {
-                const double x = fabs(u * d.dt / d.dr);
-                if (x > cu) cu = x;
-            }
-            if (i >= 1 && i <= nr - 1) {
-                const double r = d.polar ? d.r0 + ((double)i - 0.5) * dr : 1.0;
-                const double x = fabs(v * d.dt / (r * d.dp));
-                if (x > cv) cv = x;
-            }
-        }
+        if (DIAG) prb_diag_point(d, i, c, tn, f[GB_F_uel][c], f[GB_F_vel][c], cu, cv);
     }
     if (DIAG) prb_cfl_reduce(d, cu, cv);   // every lane of every warp
+}
+
+// The diagnostics alone, after the tank's and the cavity's update: the same
+// running means and CFL scans over the same rows and columns k = 0..np
+// (velvor2dhorconvtank.f:424-479, velvor2ddvdbenchmark.f:434-486).
+__global__ void k_prb_diag(PrbDev d)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (*d.abort) return;   // uniform across the grid
+    double cu = 0.0, cv = 0.0;
+    if (t < (d.nr + 2) * (d.np + 1)) {
+        const int i = t % (d.nr + 2), k = t / (d.nr + 2);
+        const size_t c = GIX(i, k, d.ld);
+        prb_diag_point(d, i, c, d.f[GB_F_th][c], d.f[GB_F_uel][c], d.f[GB_F_vel][c], cu, cv);
+    }
+    prb_cfl_reduce(d, cu, cv);
 }
 
 // Per-step bookkeeping for graph-replayed steps: copies the step's Nusselt
@@ -475,7 +498,7 @@ __global__ void k_prb_zonal(PrbDev d, double *out)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i > d.nr + 1) return;
     const int ld = d.ld, np = d.np;
-    const size_t n = (size_t)ld * (size_t)(np + 1);
+    const size_t n = d.diag_stride;
     const double *mT2 = d.diag, *mT = d.diag + n, *mU2 = d.diag + 2 * n, *mV2 = d.diag + 3 * n;
     double a = 0.0, b = 0.0, cu = 0.0, cv = 0.0;
     for (int k = 0; k <= np; ++k) {
@@ -543,8 +566,14 @@ int prb_launch_rhs(gb_prb *h, int do_v, int do_u, cudaStream_t s)
 
 int prb_launch_update(gb_prb *h, cudaStream_t s, bool diag)
 {
-    if (h->dev.tank) return tank_launch_update(h, s);
     PrbDev &d = h->dev;
+    if (d.tank) {
+        const int st = tank_launch_update(h, s);
+        if (st != GB_OK || !(diag && d.diag)) return st;
+        k_prb_diag<<<gb_ceil_div((size_t)(d.nr + 2) * (d.np + 1), TPB), TPB, 0, s>>>(d);
+        h->launches += 1;
+        return GB_OK;
+    }
     if (diag && d.diag)
         k_update<true><<<gb_ceil_div((size_t)(d.nr + 2) * (d.np + 1), TPB), TPB, 0, s>>>(d);
     else
@@ -1081,6 +1110,7 @@ static int prb_diag_alloc(gb_prb *h, int cap)
     h->diag_buf = buf;
     h->diag_cap = cap;
     d.diag = buf;
+    d.diag_stride = n;
     d.diag_kt = (int *)(buf + 4 * n);
     d.cfl_hist = (unsigned long long *)(buf + 4 * n + 8);
     prb_drop_graphs(h);
@@ -1091,10 +1121,6 @@ extern "C" int gb_prb_diag_enable(gb_prb *h, int on)
 {
     if (!h) { gb_set_error("gb_prb_diag_enable: null handle"); return GB_ERR_INVALID; }
     PrbDev &d = h->dev;
-    if (on && h->dev.tank) {
-        gb_set_error("gb_prb_diag_enable: the tank has no device diagnostics");
-        return GB_ERR_INVALID;
-    }
     if (!on) {
         if (h->diag_buf) {
             GB_CUDA_TRY(cudaStreamSynchronize(h->stream));

@@ -69,9 +69,11 @@ struct PrbDev {
     int *sweep_hist;
     int hist_cap;
     // time-loop diagnostics (PRB:404-459), null when off: running means of
-    // T^2, T, u^2, v^2 (four (ld, np+1) arrays), the kt of the step in
-    // flight, per-step CFL maxima (2 per history slot, bit patterns)
+    // T^2, T, u^2, v^2 (four arrays of diag_stride doubles, columns
+    // k = 0..np of leading dimension ld used), the kt of the step in flight,
+    // per-step CFL maxima (2 per history slot, bit patterns)
     double *diag;
+    size_t diag_stride;
     int *diag_kt;
     unsigned long long *cfl_hist;
 };

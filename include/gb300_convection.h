@@ -142,7 +142,7 @@ typedef struct gb_prb_params {
  *                   storing 2 trans2 in httrans and zero in httrans2
  *                   (:197-198); the multigrid with side walls (v lines
  *                   k = 1..np-1, u lines k = 1..np against the zero wall)
- *                   and tolcon 5e-6.  FP64 only; no device diagnostics.
+ *                   and tolcon 5e-6.  FP64 only.
  *   GB_PRB_DVD:     the differentially heated cavity benchmark,
  *                   monashubuntudir_velvor2ddvdbenchmarkdir/velvor2ddvdbenchmark.f:
  *                   the tank's scheme (np+2 columns, same multigrid) with
@@ -239,7 +239,9 @@ int gb_prb_run_end(gb_prb *h, int nsteps, double *nu, int *sweeps, int *steps_do
 
 /* Time-loop diagnostics on the device (PRB:404-493; velvor2dnewsch3.4.f:
  * 404-493 for the annulus), fused into the step's update kernel so the step
- * reads nothing back.  Enabled, every graph-replayed step with kt >= 2
+ * reads nothing back (a kernel of their own after the tank's and the
+ * cavity's update: velvor2dhorconvtank.f:424-513, velvor2ddvdbenchmark.f:
+ * 434-518, the same means and scans over columns k = 0..np).  Enabled, every graph-replayed step with kt >= 2
  * updates the running means of T^2, T, u^2 and v^2 over the block's steps
  * 2..kt (m = (1/(kt-1)) m (kt-2) + (1/(kt-1)) x; the reference keeps them
  * in weln, welp, Bp and vrms, PRB:408-416), and records the step's CFL

@@ -1,5 +1,7 @@
-"""The time-loop diagnostics fused into the device step (PRB:404-493,
-velvor2dnewsch3.4.f:404-493) against the oracle: the four running means and
+"""The time-loop diagnostics of the device step (PRB:404-493,
+velvor2dnewsch3.4.f:404-493; after the update of the tank and the cavity,
+velvor2dhorconvtank.f:424-513 and velvor2ddvdbenchmark.f:434-518) against
+the oracle: the four running means and
 every step's CFL maxima bit for bit, the zonal T variance bit for bit and the
 zonal rms of u and v to an ulp (sqrt against libm pow), over a first block
 and a "more iterations" block that starts the means again; the step's
@@ -25,11 +27,22 @@ def _pair(O, P, variant, smoother):
                         mode=smoother)
         g = P.PRB(p["nr"], p["np_"], dt=2e-4, r0=p["r0"], rmax=p["rmax"], xx=p["xx"], Ra=1e6, Pr=p["Pr"],
                   smoother=smoother)
-    else:
+    elif variant == "annulus":
         kw = dict(r0=0.5, rmax=1.0, Re=1.06148e5)
         o = O.OraclePRB(16, 32, 1e-6, 1e6, 0.71, mode=smoother, variant=O.ORC_ANNULUS, **kw)
         g = P.PRB(16, 32, dt=1e-6, Ra=1e6, Pr=0.71, smoother=smoother, variant=1, **kw)
-    o.initial(1, 5, 5e-2)
+    else:
+        from codesthesis_dir_gb300 import lib
+        dvd = variant == "dvd"
+        geo = dict(r0=0.0, rmax=1.0, xx=1.0, Pr=0.71) if dvd else dict(r0=0.5, rmax=1.5, xx=3.1, Pr=10.0)
+        dt, Ra = (2e-5, 1e5) if dvd else (1e-5, 1e6)
+        o = O.OraclePRB(16, 32, dt, Ra, geo["Pr"], r0=geo["r0"], rmax=geo["rmax"], xx=geo["xx"], mode=smoother,
+                        variant=O.ORC_DVD if dvd else O.ORC_TANK)
+        g = P.PRB(16, 32, dt=dt, Ra=Ra, smoother=smoother, variant=lib.PRB_DVD if dvd else lib.PRB_TANK, **geo)
+    if variant in ("tank", "dvd"):
+        o.initial()
+    else:
+        o.initial(1, 5, 5e-2)
     for name in STATE_FIELDS:
         g.set(name, np.array(o.field(name), order="F"))
     o.enable_diagnostics()
@@ -46,7 +59,7 @@ def _check(o, g, cfl_o):
     assert diff_fields(o, g, COMPARED) == {}
 
 
-@pytest.mark.parametrize("variant", ["layer", "annulus"])
+@pytest.mark.parametrize("variant", ["layer", "annulus", "tank", "dvd"])
 @pytest.mark.parametrize("smoother", [0, 1], ids=["lex", "zebra"])
 def test_diagnostics_two_blocks(oracle, P, variant, smoother):
     o, g = _pair(oracle, P, variant, smoother)
