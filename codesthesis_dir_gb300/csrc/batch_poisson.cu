@@ -266,8 +266,8 @@ __device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int ox, int oy, 
 }
 
 // psi values of the points this thread stores (fixed assignment: row
-// warp + 8*rr, column lane + 32*cc of the tile), fetched before the sweeps
-// so that the defect correction's read of psi does not wait at the store.
+// warp + 8*rr, column lane + 32*cc of the tile), fetched together after the
+// sweeps so that the defect correction's reads of psi overlap one another.
 __device__ __forceinline__ void psi_prefetch(const double *psi, int x0, int y0, int n, double (&pv)[ST_R * ST_C])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -358,11 +358,11 @@ __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, 
     T *sx = (T *)smem, *sf = sx + 2 * LY::HALF;
     const int n = B.n_of[e.p * BP_MAXL + l];
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
-    double pv[ST_R * ST_C];
-    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
     tile_load<T, H>(sx, sf, XS<T>(B, e.p, l, src), FP<T>(B, e.p, l), ox, oy, n, zero_init != 0, true);
     __syncthreads();
     tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
+    double pv[ST_R * ST_C];
+    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
     tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     if (RESTRICT) {
         // residual on the tile plus one ring, in place of f (each point
@@ -437,8 +437,6 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
     T *sx = (T *)smem, *sf = sx + 2 * LY::HALF;
     const int n = B.n_of[e.p * BP_MAXL + l], nc = B.n_of[e.p * BP_MAXL + l + 1];
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - H, oy = y0 - H;
-    double pv[ST_R * ST_C];
-    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
     const T *x = XS<T>(B, e.p, l, src);
     const T *f = FP<T>(B, e.p, l);
     const T *ec = XS<T>(B, e.p, l + 1, 0);
@@ -486,6 +484,8 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
     }
     __syncthreads();
     if (NU > 0) tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
+    double pv[ST_R * ST_C];
+    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
     tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
     __syncthreads();
 }
@@ -789,12 +789,10 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
 }
 
 // One kernel launch per operation (graph path).
-// The correction-store variants hold the prefetched psi values (16 doubles
-// per thread) across the sweeps; four blocks per SM keep them at 64
-// registers.  The other prolongation variants fit five blocks' shared tiles
-// per SM and are held to the registers of five.
+// The prolongation variants fit five blocks' shared tiles per SM and are
+// held to the registers of five.
 template <class T, int KIND, int NU, bool CORR>
-__global__ void __launch_bounds__(TILE_THREADS, CORR ? 4 : (KIND == OP_PROLONG ? 5 : 1)) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
+__global__ void __launch_bounds__(TILE_THREADS, KIND == OP_PROLONG ? 5 : 1) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
                                                      Op op, int nu1, int nu2)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
