@@ -495,13 +495,16 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
 // the V-cycle below level dloc, solution and right-hand side of every level
 // resident, residuals formed inside the restriction.
 // ---------------------------------------------------------------------------
+// One colour of a red-black sweep over the interior: the points of that
+// colour only, (m + 1) / 2 slots per row (row j starts at i = 1 or 2).
 template <class T>
 __device__ void loc_rb_half(T *x, const T *f, int n, T h2, int color)
 {
-    const int m = n - 2;
-    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
-        const int j = q / m + 1, i = q - (j - 1) * m + 1;
-        if (((i + j) & 1) != color) continue;
+    const int m = n - 2, w = (m + 1) >> 1;
+    for (int q = threadIdx.x; q < m * w; q += blockDim.x) {
+        const int jj = q / w, j = jj + 1;
+        const int i = 1 + ((1 + j + color) & 1) + 2 * (q - jj * w);
+        if (i > m) continue;
         const int c = j * n + i;
         const T s = (x[c - 1] + x[c + 1]) + (x[c - n] + x[c + n]);
         x[c] = fmaT<T>(-h2, f[c], s) * (T)0.25;
@@ -788,6 +791,17 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
     }
 }
 
+// The coarse levels of every problem below its tiled levels (graph path):
+// one block of LOCAL_THREADS per problem.
+#define LOCAL_THREADS 512
+template <class T>
+__global__ void __launch_bounds__(LOCAL_THREADS) k_local(BatchDev B, Op op, int nu1, int nu2)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (!B.active[blockIdx.x]) return;
+    op_local<T>(B, blockIdx.x, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, smem_raw);
+}
+
 // One kernel launch per operation (graph path).
 // The prolongation variants fit five blocks' shared tiles per SM and are
 // held to the registers of five.
@@ -1068,7 +1082,7 @@ template <class T> static cudaError_t set_smem_attrs(size_t local, size_t persis
     SA((k_op<T, OP_PROLONG, 0, true>), smem_tile<T>(0));
     SA((k_op<T, OP_PROLONG, 1, true>), smem_tile<T>(2));
     SA((k_op<T, OP_PROLONG, 2, true>), smem_tile<T>(4));
-    SA((k_op<T, OP_LOCAL, 0, false>), local);
+    SA((k_local<T>), local);
     SA((k_persistent<T>), persistent);
 #undef SA
     return cudaSuccess;
@@ -1105,7 +1119,7 @@ static void launch_op(gb_batch *b, const Op &op, cudaStream_t s)
         else k_op<T, OP_PROLONG, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
         break;
     case OP_LOCAL:
-        k_op<T, OP_LOCAL, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        k_local<T><<<g, LOCAL_THREADS, sm, s>>>(D, op, n1, n2);
         break;
     case OP_OUTER:
         k_op<T, OP_OUTER, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
