@@ -1,8 +1,10 @@
 // Batched Dirichlet Poisson solver: many independent n x n vertex-grid
 // problems of uneven size, V(nu1,nu2) red-black Gauss-Seidel cycles with
 // full-weighting restriction and bilinear prolongation (the transfer
-// operators of rotann2.f:755-854), in plain FP64 or as an FP32 inner
-// V-cycle inside FP64 defect correction.
+// operators of rotann2.f:755-854), in plain FP64 or as FP32 inner V-cycles
+// inside defect correction whose outer residual is formed in float-pair
+// arithmetic (about 48 significand bits) on the FP32 pipe, the solution
+// returned in FP64.
 //
 // Execution: every level of every problem larger than LOCAL_N is processed
 // by level-synchronous kernels whose blocks are drawn from one table over
@@ -20,6 +22,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "gbcommon.cuh"
@@ -100,6 +103,44 @@ __device__ __forceinline__ double f2d(float v)
 }
 
 __device__ __forceinline__ double to_double(float v) { return f2d(v); }
+
+// Float pairs (hi, lo), |lo| <= ulp(hi)/2: about 48 significand bits with
+// FP32 arithmetic only.  two_sum finds the rounding error of a float sum
+// exactly (Knuth, TAOCP vol. 2, 4.2.2); df_add is the accurate pair sum of
+// Dekker (1971) as the QD library's ieee_add arranges it.  The mixed solve
+// keeps psi and f as pairs so that its outer residual runs on the FP32
+// pipe; every multiplication in it is by a power of two (exact).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e)   // |a| >= |b| or a = 0
+{
+    s = a + b;
+    e = b - (s - a);
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b)
+{
+    float s, e, t, f;
+    two_sum(a.x, b.x, s, e);
+    two_sum(a.y, b.y, t, f);
+    e = e + t;
+    fast_two_sum(s, e, s, e);
+    e = e + f;
+    fast_two_sum(s, e, s, e);
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_add_f(float2 a, float b)
+{
+    float s, e;
+    two_sum(a.x, b, s, e);
+    e = e + a.y;
+    fast_two_sum(s, e, s, e);
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_scale(float2 a, float p) { return make_float2(a.x * p, a.y * p); }
 __device__ __forceinline__ double to_double(double v) { return v; }
 
 struct TileEntry {
@@ -268,7 +309,7 @@ __device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int ox, int oy, 
 // psi values of the points this thread stores (fixed assignment: row
 // warp + 8*rr, column lane + 32*cc of the tile), fetched together after the
 // sweeps so that the defect correction's reads of psi overlap one another.
-__device__ __forceinline__ void psi_prefetch(const double *psi, int x0, int y0, int n, double (&pv)[ST_R * ST_C])
+__device__ __forceinline__ void psi_prefetch(const float2 *psi, int x0, int y0, int n, float2 (&pv)[ST_R * ST_C])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -277,7 +318,7 @@ __device__ __forceinline__ void psi_prefetch(const double *psi, int x0, int y0, 
         for (int cc = 0; cc < ST_C; ++cc) {
             const int gy = y0 + warp + 8 * rr, gx = x0 + lane + 32 * cc;
             const bool in = gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2;
-            pv[rr * ST_C + cc] = in ? psi[(size_t)gy * n + gx] : 0.0;
+            pv[rr * ST_C + cc] = in ? psi[(size_t)gy * n + gx] : make_float2(0.f, 0.f);
         }
 }
 
@@ -286,7 +327,7 @@ __device__ __forceinline__ void psi_prefetch(const double *psi, int x0, int y0, 
 // defect correction psi += e point by point.
 template <class T, int H, bool CORRECT>
 __device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, int y0, int n, T *x,
-                                           double *psi, const double (&pv)[ST_R * ST_C])
+                                           float2 *psi, const float2 (&pv)[ST_R * ST_C])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -297,7 +338,7 @@ __device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, 
             if (gx < 1 || gx > n - 2 || gy < 1 || gy > n - 2) continue;
             const size_t g = (size_t)gy * n + gx;
             const T v = sx[TileLayout<T, H>::at(gy - oy, gx - ox)];
-            if (CORRECT) psi[g] = pv[rr * ST_C + cc] + to_double(v);
+            if (CORRECT) psi[g] = df_add_f(pv[rr * ST_C + cc], (float)v);
             else x[g] = v;
         }
 }
@@ -361,9 +402,9 @@ __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, 
     tile_load<T, H>(sx, sf, XS<T>(B, e.p, l, src), FP<T>(B, e.p, l), ox, oy, n, zero_init != 0, true);
     __syncthreads();
     tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
-    double pv[ST_R * ST_C];
-    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
-    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
+    float2 pv[ST_R * ST_C];
+    if (CORR) psi_prefetch((const float2 *)B.psi[e.p], x0, y0, n, pv);
+    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? (float2 *)B.psi[e.p] : nullptr, pv);
     if (RESTRICT) {
         // residual on the tile plus one ring, in place of f (each point
         // reads f only at itself and x, which stays put, so both colours of
@@ -484,9 +525,9 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
     }
     __syncthreads();
     if (NU > 0) tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
-    double pv[ST_R * ST_C];
-    if (CORR) psi_prefetch(B.psi[e.p], x0, y0, n, pv);
-    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? B.psi[e.p] : nullptr, pv);
+    float2 pv[ST_R * ST_C];
+    if (CORR) psi_prefetch((const float2 *)B.psi[e.p], x0, y0, n, pv);
+    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? (float2 *)B.psi[e.p] : nullptr, pv);
     __syncthreads();
 }
 
@@ -601,8 +642,8 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
     {
         const int n = B.n_of[p * BP_MAXL + d0];
         if (d0 == 0 && correct_level0) {
-            double *psi = B.psi[p];
-            for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = psi[q] + to_double(X[q]);
+            float2 *psi = (float2 *)B.psi[p];
+            for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = df_add_f(psi[q], (float)X[q]);
         } else {
             T *gx = XS<T>(B, p, d0, 0);
             for (int q = threadIdx.x; q < n * n; q += blockDim.x) gx[q] = X[q];
@@ -612,18 +653,27 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
 }
 
 // ---------------------------------------------------------------------------
-// FP64 outer pass, convergence bookkeeping
+// Outer pass (residual and norm), convergence bookkeeping
 // ---------------------------------------------------------------------------
 // One TX x TY tile of level 0 (psi, f: the caller's arrays): the FP64
 // residual r = f - A psi, its squared norm (the tile's partial sum) and,
 // when store_r, r rounded to FP32 as the inner cycle's right-hand side.
 // psi is only read here, so neighbouring tiles may overlap freely.
-__device__ void op_outer(const BatchDev &B, TileEntry e, int item, const double *const *f_p, int store_r,
+// T = double (plain FP64 cycles): psi and f are the caller's FP64 arrays
+// and the pass forms only the norm.  T = float (FP32 inner cycles): psi is
+// held as float pairs in the caller's array and f as float pairs split at
+// the start of the solve; the residual is formed in pair arithmetic
+// (rounding error about 2^-48 of the terms) and its high part is both the
+// FP32 right-hand side and, widened exactly, the term of the FP64 norm.
+template <class T>
+__device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *const *f_p, int store_r,
                          unsigned char *smem)
 {
+    constexpr bool PAIR = sizeof(T) == 4;
+    using V = typename std::conditional<PAIR, float2, double>::type;
     constexpr int SX = TX + 2, SY = TY + 2;
-    double *sp = (double *)smem;
-    double *s_red = sp + SX * SY;
+    V *sp = (V *)smem;
+    double *s_red = (double *)(sp + SX * SY);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (!B.active[e.p]) {
         if (threadIdx.x == 0) B.partial[item] = 0.0;
@@ -631,16 +681,18 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const double 
     }
     const int n = B.n_of[e.p * BP_MAXL];
     const int x0 = e.tx * TX, y0 = e.ty * TY, ox = x0 - 1, oy = y0 - 1;
-    const double *psi = B.psi[e.p];
-    const double *f = f_p[e.p];
+    const V *psi = (const V *)B.psi[e.p];
+    const V *f = (const V *)f_p[e.p];
+    V zero;
+    if constexpr (PAIR) zero = make_float2(0.f, 0.f);
+    else zero = 0.0;
 #pragma unroll 4
     for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
         const int r = i / SX, c = i - r * SX;
         const int gy = oy + r, gx = ox + c;
-        sp[i] = (gy >= 0 && gy < n && gx >= 0 && gx < n) ? psi[(size_t)gy * n + gx] : 0.0;
+        sp[i] = (gy >= 0 && gy < n && gx >= 0 && gx < n) ? psi[(size_t)gy * n + gx] : zero;
     }
     __syncthreads();
-    const double ih2 = B.ih2d[e.p * BP_MAXL];
     float *f32 = store_r ? FP<float>(B, e.p, 0) : nullptr;
     // one accumulator per column group: the sum of squares is a dependent
     // FP64 chain, and TX / 32 independent chains let the points overlap
@@ -656,11 +708,21 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const double 
             if (gx < gxa || gx >= gxb) continue;
             const int q = (gy - oy) * SX + gx - ox;
             const size_t g = (size_t)gy * n + gx;
-            const double s = (sp[q - 1] + sp[q + 1]) + (sp[q - SX] + sp[q + SX]);
-            const double lap = __fma_rn(-4.0, sp[q], s);
-            const double r = __fma_rn(-ih2, lap, f[g]);
-            accs[a] = __fma_rn(r, r, accs[a]);
-            if (store_r) f32[g] = d2f_rn(r);
+            double rw;
+            if constexpr (PAIR) {
+                // ih2 = 4^m exactly (n = 2^m + 1): every scaling is exact
+                const float2 sum = df_add(df_add(sp[q - 1], sp[q + 1]), df_add(sp[q - SX], sp[q + SX]));
+                const float2 lap = df_add(sum, df_scale(sp[q], -4.0f));
+                const float2 r = df_add(f[g], df_scale(lap, -B.ih2f[e.p * BP_MAXL]));
+                rw = f2d(r.x);
+                if (store_r) f32[g] = r.x;
+            } else {
+                const double sum = (sp[q - 1] + sp[q + 1]) + (sp[q - SX] + sp[q + SX]);
+                const double lap = __fma_rn(-4.0, sp[q], sum);
+                rw = __fma_rn(-B.ih2d[e.p * BP_MAXL], lap, f[g]);
+                if (store_r) f32[g] = d2f_rn(rw);
+            }
+            accs[a] = __fma_rn(rw, rw, accs[a]);
         }
     }
     double acc = 0.0;
@@ -675,6 +737,29 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const double 
         B.partial[item] = t;
     }
     __syncthreads();
+}
+
+// The right-hand side as float pairs (hi = f rounded to FP32, lo = the
+// remainder rounded), once per mixed solve; and the solution back from
+// pairs to FP64 (hi + lo, exact: the pair spans at most 48 bits) at its end,
+// in place.
+__global__ void k_split_pairs(const double *f, float2 *out, long long total)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const double v = f[q];
+        const float hi = d2f_rn(v);
+        out[q] = make_float2(hi, d2f_rn(v - f2d(hi)));
+    }
+}
+
+__global__ void k_join_pairs(double *psi, long long total)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const float2 v = ((const float2 *)psi)[q];
+        psi[q] = f2d(v.x) + f2d(v.y);
+    }
 }
 
 // Copies buffer 1 of level 0 into the caller's psi (plain FP64 cycles whose
@@ -779,7 +864,7 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
         op_local<T>(B, item, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, smem);
         return;
     case OP_OUTER:
-        op_outer(B, tiles[op.off + item], item, f_p, op.aux, smem);
+        op_outer<T>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
         return;
     case OP_COPYBACK: {
         const TileEntry e = tiles[op.off + item];
@@ -869,6 +954,7 @@ struct gb_batch {
     int *d_int = nullptr;
     double *d_dbl = nullptr;
     void *d_spacing = nullptr;          // h^2 and 1/h^2 per (problem, level): FP64 then FP32
+    float2 *d_fpairs = nullptr;         // mixed: the right-hand side as float pairs (total)
     void **d_ptrs = nullptr;
     TileEntry *d_tiles = nullptr;
     std::vector<int> ft_off, ft_cnt;    // per level: tiles of problems with l < dloc
@@ -1234,6 +1320,7 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     BTRY(cudaMalloc(&b->d_dbl, sizeof(double) * (2 * (size_t)nprob + (size_t)b->ot_cnt)));
     const size_t nsp = (size_t)nprob * BP_MAXL;
     BTRY(cudaMalloc(&b->d_spacing, (sizeof(double) + sizeof(float)) * 2 * nsp));
+    if (precision == GB_BATCH_MIXED) BTRY(cudaMalloc(&b->d_fpairs, sizeof(float2) * (size_t)std::max<long long>(b->total, 1)));
     {
         std::vector<double> hd(2 * nsp, 0.0);
         std::vector<float> hf(2 * nsp, 0.0f);
@@ -1360,6 +1447,7 @@ extern "C" int gb_batch_destroy(gb_batch *b)
     cudaFree(b->d_int);
     cudaFree(b->d_dbl);
     cudaFree(b->d_spacing);
+    cudaFree(b->d_fpairs);
     cudaFree(b->d_ptrs);
     cudaFree(b->d_tiles);
     cudaFree(b->d_ops);
@@ -1451,8 +1539,9 @@ static void enqueue_iteration(gb_batch *b, const std::vector<Op> &v, cudaStream_
 
 // Algorithmic bytes of one V-cycle per interior point (24.7 words: four
 // sweeps of 3 words, residual 3, restriction 1.25, prolongation 2.25, all
-// levels x 4/3) at the inner precision, and of one FP64 outer step (read psi
-// and f, write the FP32 residual; read e, read and write psi).
+// levels x 4/3) at the inner precision, and of one outer step (read psi
+// and f, 8 B each as FP64 or float pairs, write the FP32 residual; read e,
+// read and write psi).
 static double cycle_bytes(const gb_batch *b) { return 24.7 * (b->precision == GB_BATCH_FP64 ? 8.0 : 4.0); }
 static double outer_bytes(const gb_batch *b) { return b->precision == GB_BATCH_FP64 ? 16.0 : 40.0; }
 
@@ -1551,9 +1640,14 @@ extern "C" int gb_batch_profile_read_kind(gb_batch *b, int kind, double *ms, lon
 static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStream_t s)
 {
     std::vector<const void *> pf(b->nprob), pp(b->nprob);
+    const bool mixed = b->precision == GB_BATCH_MIXED;
     for (int p = 0; p < b->nprob; ++p) {
-        pf[p] = d_f + b->off0[p];
+        pf[p] = mixed ? (const void *)(b->d_fpairs + b->off0[p]) : (const void *)(d_f + b->off0[p]);
         pp[p] = d_psi + b->off0[p];
+    }
+    if (mixed && b->total > 0) {
+        k_split_pairs<<<152 * 8, 256, 0, s>>>(d_f, b->d_fpairs, b->total);
+        GB_CUDA_TRY(cudaGetLastError());
     }
     GB_CUDA_TRY(cudaMemcpyAsync(b->d_f_tab, pf.data(), sizeof(void *) * b->nprob, cudaMemcpyHostToDevice, s));
     GB_CUDA_TRY(cudaMemcpyAsync(b->d_psi_tab, pp.data(), sizeof(void *) * b->nprob, cudaMemcpyHostToDevice, s));
@@ -1686,6 +1780,11 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
     GB_CUDA_TRY(cudaMemsetAsync(D.failed, 0, sizeof(int) * b->nprob, s));
     st = b->exec == GB_BATCH_EXEC_PERSISTENT ? solve_persistent(b, s) : solve_graph(b, s);
     if (st != GB_OK) return st;
+    if (b->precision == GB_BATCH_MIXED && b->total > 0) {
+        // the mixed solve held psi as float pairs in place: back to FP64
+        k_join_pairs<<<152 * 8, 256, 0, s>>>(d_psi, b->total);
+        GB_CUDA_TRY(cudaGetLastError());
+    }
     std::vector<int> fl(b->nprob);
     GB_CUDA_TRY(cudaMemcpyAsync(fl.data(), D.failed, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s));
     if (cycles) GB_CUDA_TRY(cudaMemcpyAsync(cycles, D.cycles, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s));

@@ -540,17 +540,20 @@ int gb_pdma_batch_noalloc(const double *a, const double *b, const double *c, con
  * until ||f - A psi||_2 <= rtol ||f||_2.  Problem p occupies n[p]^2
  * doubles, row-major, starting at offset sum_{q<p} n[q]^2. */
 #define GB_BATCH_FP64  0   /* plain FP64 V-cycles */
-#define GB_BATCH_MIXED 1   /* FP32 inner V-cycle inside FP64 defect correction */
+#define GB_BATCH_MIXED 1   /* FP32 inner V-cycles inside defect correction; the
+                              outer residual in float-pair arithmetic (~48-bit
+                              significands: f and psi held as FP32 hi + lo
+                              pairs during the solve), psi returned in FP64 */
 
 typedef struct gb_batch gb_batch;
 
 int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
                     int max_cycles, gb_batch **out);
 int gb_batch_destroy(gb_batch *b);
-/* Mixed solves only: V-cycles per outer (FP64 defect-correction)
- * iteration, 1..16 (default 1).  With k > 1 the FP64 residual, its norm
- * and the FP64 update run once per k inner cycles, and convergence is
- * tested every k cycles. */
+/* Mixed solves only: V-cycles per outer (defect-correction) iteration,
+ * 1..16 (default 1).  With k > 1 the outer residual, its norm and the
+ * update of psi run once per k inner cycles, and convergence is tested
+ * every k cycles. */
 int gb_batch_set_inner_cycles(gb_batch *b, int inner);
 /* How a solve is executed.  GRAPH (the default): one kernel per level
  * operation, one CUDA graph per outer iteration.  PERSISTENT (devices with
@@ -597,7 +600,7 @@ int gb_batch_profile(gb_batch *b, int enable);
  * profile counters. */
 int gb_batch_profile_read(gb_batch *b, double *ms, long long *launches, double *alg_bytes, int reset);
 /* The same per operation kind (graph mode): 0 smoothing, 1 smoothing +
- * residual + restriction, 2 prolongation + smoothing, 4 FP64 outer pass;
+ * residual + restriction, 2 prolongation + smoothing, 4 outer pass;
  * finest level only, except the outer pass. */
 #define GB_BATCH_OP_SMOOTH   0
 #define GB_BATCH_OP_DOWN     1

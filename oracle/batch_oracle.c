@@ -157,6 +157,56 @@ static int levels_of(int n, int *nl)
     return L;
 }
 
+/* Float pairs (hi, lo) for the mixed solve's outer residual, the same
+ * operations in the same order as the device: two_sum (Knuth, TAOCP vol. 2,
+ * 4.2.2), the accurate pair sum of Dekker (1971) as the QD library's ieee_add
+ * arranges it, and scalings by powers of two (exact). */
+typedef struct {
+    float hi, lo;
+} fpair;
+
+static void two_sum(float a, float b, float *s, float *e)
+{
+    *s = a + b;
+    const float bb = *s - a;
+    *e = (a - (*s - bb)) + (b - bb);
+}
+
+static void fast_two_sum(float a, float b, float *s, float *e)
+{
+    *s = a + b;
+    *e = b - (*s - a);
+}
+
+static fpair fp_add(fpair a, fpair b)
+{
+    float s, e, t, f;
+    two_sum(a.hi, b.hi, &s, &e);
+    two_sum(a.lo, b.lo, &t, &f);
+    e = e + t;
+    fast_two_sum(s, e, &s, &e);
+    e = e + f;
+    fast_two_sum(s, e, &s, &e);
+    fpair r = {s, e};
+    return r;
+}
+
+static fpair fp_add_f(fpair a, float b)
+{
+    float s, e;
+    two_sum(a.hi, b, &s, &e);
+    e = e + a.lo;
+    fast_two_sum(s, e, &s, &e);
+    fpair r = {s, e};
+    return r;
+}
+
+static fpair fp_scale(fpair a, float p)
+{
+    fpair r = {a.hi * p, a.lo * p};
+    return r;
+}
+
 static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, double rtol,
                      int max_cycles, int precision, int inner, int *cycles_out, double *relres_out)
 {
@@ -166,7 +216,7 @@ static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, doub
     for (int l = 0; l < L; ++l) tot += (size_t)nl[l] * nl[l];
     const size_t nn = (size_t)n * n;
     memset(psi, 0, sizeof(double) * nn);
-    const double fn = sqrt(sumsq_interior(n, f));
+    double fn = sqrt(sumsq_interior(n, f));
     double *r64 = (double *)calloc(nn, sizeof(double));
     int cycles = 0, status = 0;
     double rn = fn;
@@ -196,31 +246,51 @@ static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, doub
             P[l] = pool + off; F[l] = pool + tot + off; R[l] = pool + 2 * tot + off;
             off += (size_t)nl[l] * nl[l];
         }
-        double h = 1.0 / (double)(n - 1);
-        double ih2 = 1.0 / (h * h);
+        /* f and psi as float pairs; 1/h^2 = 4^m is exact in FP32 (n = 2^m + 1) */
+        fpair *fq = (fpair *)malloc(nn * sizeof(fpair));
+        fpair *pq = (fpair *)calloc(nn, sizeof(fpair));
+        float *r32 = (float *)calloc(nn, sizeof(float));
+        for (size_t c = 0; c < nn; ++c) {
+            fq[c].hi = (float)f[c];
+            fq[c].lo = (float)(f[c] - (double)fq[c].hi);
+        }
+        const float hs = 1.0f / (float)(n - 1);
+        const float ih2 = 1.0f / (hs * hs);
+        int first = 1;
         for (;;) {
-            /* FP64 outer residual r = f - A psi and its norm */
-            residual_64(n, psi, f, r64, ih2);
+            /* outer residual r = f - A psi in pair arithmetic; its high part
+             * is the FP32 right-hand side and, widened, the norm's term */
             double s = 0.0;
             for (int j = 1; j <= n - 2; ++j)
                 for (int i = 1; i <= n - 2; ++i) {
-                    double x = r64[(size_t)j * n + i];
+                    const size_t c = (size_t)j * n + i;
+                    const fpair sum = fp_add(fp_add(pq[c - 1], pq[c + 1]), fp_add(pq[c - n], pq[c + n]));
+                    const fpair lap = fp_add(sum, fp_scale(pq[c], -4.0f));
+                    const fpair r = fp_add(fq[c], fp_scale(lap, -ih2));
+                    r32[c] = r.hi;
+                    const double x = (double)r.hi;
                     s = fma(x, x, s);
                 }
             rn = sqrt(s);
+            if (first) fn = rn;   /* psi = 0: the norm of f's high parts */
+            first = 0;
             if (rn <= rtol * fn) break;
             if (cycles >= max_cycles) { status = 1; break; }
             /* inner FP32 V-cycles on A e = r, e0 = 0 */
-            for (size_t c = 0; c < nn; ++c) F[0][c] = (float)r64[c];
+            memcpy(F[0], r32, sizeof(float) * nn);
             memset(P[0], 0, sizeof(float) * nn);
             for (int k = 0; k < inner; ++k) vcycle_32(L, nl, P, F, R, nu1, nu2, 0);
             for (int j = 1; j <= n - 2; ++j)
                 for (int i = 1; i <= n - 2; ++i) {
                     size_t c = (size_t)j * n + i;
-                    psi[c] = psi[c] + (double)P[0][c];
+                    pq[c] = fp_add_f(pq[c], P[0][c]);
                 }
             cycles += inner;
         }
+        for (size_t c = 0; c < nn; ++c) psi[c] = (double)pq[c].hi + (double)pq[c].lo;
+        free(fq);
+        free(pq);
+        free(r32);
         free(pool);
     }
     free(r64);

@@ -25,11 +25,11 @@ extern "C" {
 #endif
 
 #define ORC_BATCH_FP64  0
-#define ORC_BATCH_MIXED 1   /* FP32 inner V-cycle, FP64 defect correction */
+#define ORC_BATCH_MIXED 1   /* FP32 inner V-cycles, float-pair outer residual */
 
 /* Solve every problem.  psi is overwritten (initial guess zero).  cycles[p]
  * receives the V-cycles taken, relres[p] the final ||f - A psi||_2/||f||_2.
- * inner: FP32 V-cycles per FP64 defect-correction step (mixed only).
+ * inner: FP32 V-cycles per defect-correction step (mixed only).
  * Returns 0, or 1 if any problem hit max_cycles. Uses OpenMP threads over
  * problems when built with -fopenmp. */
 int orc_batch_solve(int nprob, const int *n, const long long *offset,
