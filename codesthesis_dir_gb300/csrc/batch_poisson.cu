@@ -686,11 +686,23 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *c
     V zero;
     if constexpr (PAIR) zero = make_float2(0.f, 0.f);
     else zero = 0.0;
-#pragma unroll 4
-    for (int i = threadIdx.x; i < SX * SY; i += TILE_THREADS) {
-        const int r = i / SX, c = i - r * SX;
-        const int gy = oy + r, gx = ox + c;
-        sp[i] = (gy >= 0 && gy < n && gx >= 0 && gx < n) ? psi[(size_t)gy * n + gx] : zero;
+    // rows by warp, a row's loads issued before its shared stores
+    for (int r = warp; r < SY; r += TILE_THREADS / 32) {
+        const int gy = oy + r;
+        const bool rin = gy >= 0 && gy < n;
+        const V *pr = psi + (rin ? (size_t)gy * n : 0);
+        constexpr int NJ = (SX + 31) / 32;
+        V v[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int c = lane + 32 * j, gx = ox + c;
+            v[j] = (c < SX && rin && gx >= 0 && gx < n) ? pr[gx] : zero;
+        }
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int c = lane + 32 * j;
+            if (c < SX) sp[r * SX + c] = v[j];
+        }
     }
     __syncthreads();
     float *f32 = store_r ? FP<float>(B, e.p, 0) : nullptr;
@@ -701,11 +713,22 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *c
     for (int a = 0; a < TX / 32; ++a) accs[a] = 0.0;
     const int gxa = max(x0, 1), gxb = min(x0 + TX, n - 1);
     const int gya = max(y0, 1), gyb = min(y0 + TY, n - 1);
-    for (int gy = gya + warp; gy < gyb; gy += nw) {
+    for (int gy0 = gya + warp; gy0 < gyb; gy0 += 2 * nw) {
+        // two rows per pass: both rows' f loads are in flight together
+        V fr[2][TX / 32];
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int a = 0; a < TX / 32; ++a) {
+                const int gy = gy0 + h * nw, gx = x0 + lane + 32 * a;
+                fr[h][a] = (gy < gyb && gx >= gxa && gx < gxb) ? f[(size_t)gy * n + gx] : zero;
+            }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
         for (int a = 0; a < TX / 32; ++a) {
-            const int gx = x0 + lane + 32 * a;
-            if (gx < gxa || gx >= gxb) continue;
+            const int gy = gy0 + h * nw, gx = x0 + lane + 32 * a;
+            if (gy >= gyb || gx < gxa || gx >= gxb) continue;
             const int q = (gy - oy) * SX + gx - ox;
             const size_t g = (size_t)gy * n + gx;
             double rw;
@@ -713,13 +736,13 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *c
                 // ih2 = 4^m exactly (n = 2^m + 1): every scaling is exact
                 const float2 sum = df_add(df_add(sp[q - 1], sp[q + 1]), df_add(sp[q - SX], sp[q + SX]));
                 const float2 lap = df_add(sum, df_scale(sp[q], -4.0f));
-                const float2 r = df_add(f[g], df_scale(lap, -B.ih2f[e.p * BP_MAXL]));
+                const float2 r = df_add(fr[h][a], df_scale(lap, -B.ih2f[e.p * BP_MAXL]));
                 rw = f2d(r.x);
                 if (store_r) f32[g] = r.x;
             } else {
                 const double sum = (sp[q - 1] + sp[q + 1]) + (sp[q - SX] + sp[q + SX]);
                 const double lap = __fma_rn(-4.0, sp[q], sum);
-                rw = __fma_rn(-B.ih2d[e.p * BP_MAXL], lap, f[g]);
+                rw = __fma_rn(-B.ih2d[e.p * BP_MAXL], lap, fr[h][a]);
                 if (store_r) f32[g] = d2f_rn(rw);
             }
             accs[a] = __fma_rn(rw, rw, accs[a]);
