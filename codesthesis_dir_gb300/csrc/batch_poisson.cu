@@ -912,9 +912,9 @@ __global__ void __launch_bounds__(LOCAL_THREADS) k_local(BatchDev B, Op op, int 
 
 // One kernel launch per operation (graph path).
 // The prolongation variants fit five blocks' shared tiles per SM and are
-// held to the registers of five.
+// held to the registers of five; the outer pass is held to four.
 template <class T, int KIND, int NU, bool CORR>
-__global__ void __launch_bounds__(TILE_THREADS, KIND == OP_PROLONG ? 5 : 1) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
+__global__ void __launch_bounds__(TILE_THREADS, KIND == OP_PROLONG ? 5 : (KIND == OP_OUTER ? 4 : 1)) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
                                                      Op op, int nu1, int nu2)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
