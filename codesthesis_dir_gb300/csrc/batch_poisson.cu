@@ -1020,7 +1020,7 @@ struct gb_batch {
     long long prof_launches = 0;
     double kind_ms[8] = {0}, kind_bytes[8] = {0};
     long long kind_launches[8] = {0};
-    std::vector<int> h_active;
+    int *h_active = nullptr;            // page-locked: the active flags after a profiled iteration
 };
 
 static int levels_of(int n, int *nl)
@@ -1368,6 +1368,7 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     BTRY(cudaMalloc(&b->d_sync, sizeof(unsigned) * 4));
     BTRY(cudaMemset(b->d_sync, 0, sizeof(unsigned) * 4));
     BTRY(cudaMallocHost(&b->h_pinned, sizeof(int) * 16));
+    BTRY(cudaMallocHost(&b->h_active, sizeof(int) * (size_t)nprob));
     BTRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     b->hx.assign(2 * (size_t)nprob * BP_MAXL, nullptr);
     b->hf.assign((size_t)nprob * BP_MAXL, nullptr);
@@ -1487,6 +1488,7 @@ extern "C" int gb_batch_destroy(gb_batch *b)
     if (b->down) cudaStreamDestroy(b->down);
     cudaFree(b->pipe_buf);
     if (b->h_pinned) cudaFreeHost(b->h_pinned);
+    if (b->h_active) cudaFreeHost(b->h_active);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return GB_OK;
@@ -1558,6 +1560,9 @@ static void enqueue_iteration(gb_batch *b, const std::vector<Op> &v, cudaStream_
         }
     }
     cudaMemcpyAsync(b->h_pinned, b->dev.num_active, sizeof(int), cudaMemcpyDeviceToHost, s);
+    // profiled iterations also bring back the active flags (part of the
+    // graph: read after the iteration's own synchronisation)
+    if (b->profile) cudaMemcpyAsync(b->h_active, b->dev.active, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s);
 }
 
 // Algorithmic bytes of one V-cycle per interior point (24.7 words: four
@@ -1580,9 +1585,7 @@ static double outer_bytes(const gb_batch *b) { return b->precision == GB_BATCH_F
 static void batch_profile_collect(gb_batch *b, cudaStream_t s)
 {
     if (!b->profile || b->ev_used == 0) return;
-    b->h_active.resize(b->nprob);
-    cudaMemcpyAsync(b->h_active.data(), b->dev.active, sizeof(int) * b->nprob, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
+    cudaStreamSynchronize(s);   // a no-op after the iteration's own synchronisation
     double pts_tile = 0.0, pts_all = 0.0;
     for (int p = 0; p < b->nprob; ++p) {
         if (!b->h_active[p]) continue;
