@@ -568,7 +568,9 @@ int gb_batch_set_exec(gb_batch *b, int mode);
 long long gb_batch_total_points(const gb_batch *b);
 /* Device-resident solve: d_f, d_psi device pointers (packed).  cycles and
  * relres (host, nprob each, may be NULL) receive per-problem V-cycle counts
- * and final relative residuals.  Returns GB_OK or GB_MAXSWEEPS. */
+ * and final relative residuals.  Returns GB_OK or GB_MAXSWEEPS.  A mixed
+ * solve keeps psi as float pairs in d_psi's own memory while it runs; d_psi
+ * holds FP64 values again when the call returns (it synchronises stream). */
 int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_psi, int *cycles,
                           double *relres, void *stream);
 /* Host-buffer solve (copies in and out inside the call).  The first call
