@@ -6,9 +6,11 @@ random field with squared-exponential correlation length 0.05 of the domain
 relative residual 1e-10.
 
 One step = one solve of the whole batch.  value = cell-updates/s (interior
-points x V-cycles / second) of the FP32-inner / FP64-defect-correction path,
-with inputs resident in HBM; the plain FP64 path is timed the same way and
-reported beside it; e2e repeats the mixed solve through the C ABI's host-
+points x V-cycles / second) of the FP32-inner / FP64-defect-correction path
+(GB_BATCH_MIXED_F64OUTER: outer residual, norm and update in FP64), with
+inputs resident in HBM; the plain FP64 path and the float-pair defect
+correction (GB_BATCH_MIXED) are timed the same way and reported beside it,
+each with its field error; e2e repeats the mixed solve through the C ABI's host-
 buffer entry points with pinned host arrays, so every step's host->device
 copy of f and device->host copy of psi are inside the timed region: as a
 stream of steps (gb_batch_submit_host / gb_batch_drain, each step's copies
@@ -69,6 +71,38 @@ def workload_rhs(sizes, seed):
 def interior(sizes):
     s = np.asarray(sizes, dtype=np.int64)
     return (s - 2) ** 2
+
+
+def cpu_model():
+    """The host CPU's model as /proc/cpuinfo names it (x86: 'model name';
+    Arm: implementer and part numbers, Neoverse V2 for Grace), and nproc."""
+    name, impl, part = None, None, None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                k, v = k.strip(), v.strip()
+                if k == "model name" and not name:
+                    name = v
+                elif k == "CPU implementer" and not impl:
+                    impl = v
+                elif k == "CPU part" and not part:
+                    part = v
+    except OSError:
+        pass
+    if not name and impl:
+        known = {("0x41", "0xd4f"): "Arm Neoverse V2 (NVIDIA Grace)"}
+        name = known.get((impl, part), "Arm implementer %s part %s" % (impl, part))
+    return "%s, %d logical CPUs" % (name or "unknown CPU", os.cpu_count() or 0)
+
+
+def batch_config(total, interior_pts, ws):
+    """The workload description both arms print (same keys, same values)."""
+    return {"workload": "batched Poisson: 256 problems, n in {65,129,257,513}, V(2,2) RB-GS, rtol 1e-10",
+            "nprob": NPROB, "sizes": list(SIZES), "seed": 0, "points": int(total),
+            "interior_points": int(interior_pts), "rtol": RTOL,
+            "l2": "inputs larger than L2 (f and psi 2 x %.0f MB)" % (total * 8 / 1e6),
+            "parallelism": "replicas x%d" % ws}
 
 
 def measured_peaks():
@@ -142,11 +176,13 @@ def dist_setup():
     return ws, rank, local
 
 
-def cpu_reference(sizes_all, seed, budget_s=20.0, threads=None):
+def cpu_reference(sizes_all, seed, budget_s=20.0, threads=None, reps=1):
     """The oracle (CPU restatement, OpenMP over problems) on a bounded
     sample of the workload: problems are added until about budget_s of work
-    is measured.  Returns (cell-updates/s, sample description, threads,
-    per-problem psi for the sample, sample sizes, sample rhs)."""
+    is measured (the whole batch when it fits), then the same sample is
+    solved again until reps timings exist.  Returns (median cell-updates/s
+    over the reps, sample description, threads, problems used, psi of the
+    sample)."""
     from oracle import oracle as O
     O.build()
     threads = threads or os.cpu_count()
@@ -157,7 +193,7 @@ def cpu_reference(sizes_all, seed, budget_s=20.0, threads=None):
         order.append(int(np.nonzero(sizes_all == n)[0][0]))
     order += [i for i in range(len(sizes_all)) if i not in order]
     done_cu, done_t, used = 0.0, 0.0, []
-    psi_s, f_s = [], []
+    psi_s, chunks = [], []
     rng_f = workload_rhs(sizes_all, seed)
     offs = np.concatenate([[0], np.cumsum(sizes_all.astype(np.int64) ** 2)])
     i = 0
@@ -173,10 +209,17 @@ def cpu_reference(sizes_all, seed, budget_s=20.0, threads=None):
         done_cu += float(np.sum(interior(sz) * cyc))
         used += chunk
         psi_s.append(psi)
-        f_s.append(f)
-    sample = "%d of the %d problems (sizes %s), FP64 oracle, %d OpenMP threads, %.1f s" % (
-        len(used), len(sizes_all), sorted(set(int(sizes_all[j]) for j in used)), threads, done_t)
-    return done_cu / done_t, sample, threads, used, np.concatenate(psi_s)
+        chunks.append((sz, f))
+    rates = [done_cu / done_t]
+    while len(rates) < reps:
+        t0 = time.perf_counter()
+        for sz, f in chunks:
+            O.batch_solve(sz, f, precision=0, rtol=RTOL)
+        rates.append(done_cu / (time.perf_counter() - t0))
+    sample = "%d of the %d problems (sizes %s), FP64 oracle, %d OpenMP threads, %.1f s per run, median of %d " \
+             "run(s); %s" % (len(used), len(sizes_all), sorted(set(int(sizes_all[j]) for j in used)), threads,
+                             done_t, len(rates), cpu_model())
+    return float(np.median(rates)), sample, threads, used, np.concatenate(psi_s)
 
 
 # ---------------------------------------------------------------------------
@@ -602,12 +645,12 @@ def run_reference(args):
         if s >= args.warmup:
             vals.append(v)
     value = float(np.median(vals))
+    total = int(np.sum(sizes.astype(np.int64) ** 2))
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batched Poisson: 256 problems, n in {65,129,257,513}, V(2,2) RB-GS, rtol 1e-10",
-                   "nprob": NPROB, "sizes": list(SIZES), "rtol": RTOL},
+        "config": batch_config(total, int(np.sum(interior(sizes))), ws),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
                          "sample": sample},
@@ -625,6 +668,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-budget", type=float, default=20.0)
     ap.add_argument("--inner", type=int, default=3, help="FP32 V-cycles per defect-correction step")
+    ap.add_argument("--pair-outer", action="store_true",
+                    help="headline the float-pair defect correction (GB_BATCH_MIXED) instead of the FP64 one")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-only", action="store_true",
                     help="time only the mixed solve (for profiler launch lists); prints no JSON line")
@@ -701,7 +746,8 @@ def main():
             ms, cu = float(mx[0]), float(t[1])
         return ms, cu, cyc, rr, launches
 
-    mixed = BatchPoisson(sizes, precision=lib.BATCH_MIXED, rtol=RTOL, inner=args.inner)
+    prec_head = lib.BATCH_MIXED if args.pair_outer else lib.BATCH_MIXED_F64OUTER
+    mixed = BatchPoisson(sizes, precision=prec_head, rtol=RTOL, inner=args.inner)
     if args.mixed_only:
         ms, cu, cyc, rr, launches = timed(mixed, d_psi, args.steps, args.warmup)
         if rank == 0:
@@ -712,7 +758,8 @@ def main():
 
     # plain FP64 arm
     ms64, cu64, cyc64, rr64, _ = timed(fp64, d_psi64, args.steps, args.warmup)
-    # mixed arm (headline), clocks sampled during it, smoothing kernel profiled
+    # mixed arm (headline: FP64 defect correction), clocks sampled during
+    # it, its level-0 operations timed with CUDA events on the solve stream
     L = lib.load()
     L.gb_batch_profile(mixed._h, 1)
     timed(mixed, d_psi, 0, args.warmup)
@@ -736,18 +783,40 @@ def main():
     L.gb_measure_issue_rates(C.byref(r64), C.byref(r32))
     outer_pass = None
     if "outer" in kinds:
-        # per interior point: 4 float-pair sums (about 80 FP32 adds) for the
-        # residual, 1 FP64 fused multiply-add for the norm; 16 B read, 4 B written
+        # per interior point, FP64 defect correction: 3 adds and 2 fused
+        # multiply-adds for the residual, 1 fused multiply-add for the norm;
+        # 16 B read (psi, f), 4 B written (the FP32 right-hand side)
         k = kinds["outer"]
         pts_per_launch = k["alg_bytes_per_launch"] / 20.0
-        outer_pass = {"kernel": "k_op<float,OP_OUTER> (float-pair residual, FP64 norm, FP32 copy)",
+        f64ops = 3 + 2 + 1 if prec_head == lib.BATCH_MIXED_F64OUTER else 1
+        outer_pass = {"kernel": "k_op<float,OP_OUTER,0,%s> (%s)" % (
+                          "CM_F64" if prec_head == lib.BATCH_MIXED_F64OUTER else "CM_PAIR",
+                          "FP64 residual and norm, FP32 copy" if prec_head == lib.BATCH_MIXED_F64OUTER
+                          else "float-pair residual, FP64 norm, FP32 copy"),
                       "points_per_s": pts_per_launch / (k["avg_ms"] / 1e3), "avg_launch_ms": k["avg_ms"],
-                      "fp64_fma_per_point": 1,
+                      "fp64_instr_per_point": f64ops,
+                      "fp64_pipe_frac": f64ops * pts_per_launch / (k["avg_ms"] / 1e3) / r64.value,
                       "fp64_fma_peak_per_s": r64.value, "fp32_fma_peak_per_s": r32.value,
                       "peak_kind": "measured (FMA issue probe, gb_measure_issue_rates)"}
 
+    # the float-pair defect correction (outer residual in ~48-bit float
+    # pairs on the FP32 pipe) beside the headline, on the same inputs
+    pair = None
+    if prec_head != lib.BATCH_MIXED:
+        pr = BatchPoisson(sizes, precision=lib.BATCH_MIXED, rtol=RTOL, inner=args.inner)
+        d_psi_q = torch.zeros_like(d_psi)
+        ms_q, cu_q, cyc_q, rr_q, _ = timed(pr, d_psi_q, args.steps, args.warmup)
+        pair = {"value": cu_q / (ms_q / 1e3), "ms_per_step": ms_q / args.steps, "cycles_mean": float(np.mean(cyc_q)),
+                "relres_max": float(np.max(rr_q)),
+                "field_rel_l2_vs_fp64": float((torch.linalg.vector_norm(d_psi_q - d_psi64) /
+                                               torch.linalg.vector_norm(d_psi64)).item()),
+                "dtype": "f32-inner/f32-pair-outer (f64 result)",
+                "note": "outer residual in float-pair arithmetic (about 48 significand bits), not FP64"}
+        pr.close()
+        del d_psi_q
+
     # the same mixed solve as one persistent launch per solve
-    pers = BatchPoisson(sizes, precision=lib.BATCH_MIXED, rtol=RTOL, inner=args.inner,
+    pers = BatchPoisson(sizes, precision=prec_head, rtol=RTOL, inner=args.inner,
                         exec_mode=lib.BATCH_EXEC_PERSISTENT)
     d_psi_p = torch.zeros_like(d_psi)
     ms_p, cu_p, _, _, _ = timed(pers, d_psi_p, max(3, args.steps // 4), 1)
@@ -809,13 +878,19 @@ def main():
 
     peak, peak_kind = measured_peaks()
     achieved = (pb.value / (pms.value / 1e3)) / 1e9 if pms.value > 0 else None
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "batch_smooth_fp32_traffic.json")
+    # DRAM bytes per launch of the same kernel from one ncu capture (the
+    # profile summary named below); ncu cannot run inside a timed bench
+    traffic, traffic_src = None, None
+    tp = os.path.join(ROOT, "profiles", "batch_down_finest_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
-        if pl.value > 0:
-            traffic = tj.get("bytes_per_launch_full_scale")
+        traffic = tj.get("dram_bytes_per_launch")
+        traffic_src = "%s (%s)" % (tj.get("summary"), tj.get("captured"))
+    # whole-solve algorithmic bandwidth: 24.7 words of the inner precision
+    # per interior point per V-cycle (every level's sweeps, residuals and
+    # transfers) plus the outer passes
+    solve_gbs = cu * 24.7 * 4.0 / (ms / 1e3) / 1e9
     line = {
         "metric": METRIC,
         "value": cu / (ms / 1e3),
@@ -827,18 +902,21 @@ def main():
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32-inner/f32-pair-outer (f64 result)",
+        "dtype": "f32-inner/f64-outer" if prec_head == lib.BATCH_MIXED_F64OUTER
+                 else "f32-inner/f32-pair-outer (f64 result)",
         "data": "synthetic",
-        "config": {"workload": "batched Poisson: 256 problems, n in {65,129,257,513}, V(2,2) RB-GS, rtol 1e-10",
-                   "nprob": NPROB, "points": total, "interior_points": int(np.sum(cu_per_cycle)),
-                   "rtol": RTOL, "l2": "inputs larger than L2 (f and psi 2 x %.0f MB)" % (total * 8 / 1e6),
-                   "parallelism": "replicas x%d" % ws},
+        "config": batch_config(total, int(np.sum(cu_per_cycle)), ws),
         "fp64": {"value": cu64 / (ms64 / 1e3), "ms_per_step": ms64 / args.steps,
-                 "cycles_mean": float(np.mean(cyc64)), "relres_max": float(np.max(rr64))},
-        "mixed": {"cycles_mean": float(np.mean(cyc)), "relres_max": float(np.max(rr)),
+                 "cycles_mean": float(np.mean(cyc64)), "relres_max": float(np.max(rr64)),
+                 "achieved_GBs_alg": cu64 * 24.7 * 8.0 / (ms64 / 1e3) / 1e9,
+                 "hbm_frac_alg": cu64 * 24.7 * 8.0 / (ms64 / 1e3) / 1e9 / peak},
+        "mixed": {"precision": "GB_BATCH_MIXED_F64OUTER" if prec_head == lib.BATCH_MIXED_F64OUTER
+                  else "GB_BATCH_MIXED",
+                  "cycles_mean": float(np.mean(cyc)), "relres_max": float(np.max(rr)),
                   "inner_cycles_per_fp64_step": args.inner,
                   "field_rel_l2_vs_fp64": field_err, "speedup_vs_fp64": (cu / ms) / (cu64 / ms64),
                   "time_to_solution_speedup_vs_fp64": ms64 / ms},
+        "mixed_pair_outer": pair,
         "persistent_single_launch": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / max(3, args.steps // 4),
                                      "identical_to_graph_mode": pers_same},
         "e2e": {"value": e2e_cu / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": total * 8,
@@ -851,15 +929,20 @@ def main():
                      "kernel": "k_op<float,OP_SMOOTH_R,2> (finest level: two red-black sweeps + residual + restriction)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "traffic_unit": "bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "traffic_source": traffic_src,
                      "peak_kind": peak_kind, "launches": pl.value,
-                     "avg_launch_ms": (pms.value / pl.value) if pl.value else None},
+                     "avg_launch_ms": (pms.value / pl.value) if pl.value else None,
+                     "alg_bytes_per_launch": (pb.value / pl.value) if pl.value else None,
+                     "whole_solve": {"achieved": solve_gbs, "frac": solve_gbs / peak, "unit": "GB/s",
+                                     "basis": "24.7 FP32 words per interior point per V-cycle"}},
         "outer_pass": outer_pass,
         "kernels_mixed_graph": kinds,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        v, sample, threads, used, psi_ref = cpu_reference(sizes, rank, budget_s=args.ref_budget)
+        v, sample, threads, used, psi_ref = cpu_reference(sizes, rank, budget_s=args.ref_budget, reps=5)
         offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
         got = np.concatenate([a[offs[j]:offs[j + 1]] for j in used])
         line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",

@@ -172,9 +172,12 @@ extern "C" int gb_pdma_batch(const double *a, const double *b, const double *c, 
 // library holds until the process exits.  Host code may not pass the
 // array's name to a kernel (on the host it is only a stand-in for the
 // device symbol), so its device address is looked up once per device, with
-// that device current, and cached.  The kernel writes every scratch element
-// it reads, so nothing needs clearing between calls; calls that overlap on
-// the GPU share the array and race.
+// that device current, and cached for the life of the process (a
+// cudaDeviceReset after the first call would leave a stale address: not
+// supported).  The kernel writes every scratch element it reads, so nothing
+// needs clearing between calls.  Each call waits for its stream before it
+// returns, so one host thread's calls never overlap; calls from different
+// host threads that overlap on the GPU share the array and race.
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) double g_pdma_noalloc_scratch[GB_PDMA_NOALLOC_MAX_DOUBLES];
 

@@ -2,9 +2,10 @@
 // problems of uneven size, V(nu1,nu2) red-black Gauss-Seidel cycles with
 // full-weighting restriction and bilinear prolongation (the transfer
 // operators of rotann2.f:755-854), in plain FP64 or as FP32 inner V-cycles
-// inside defect correction whose outer residual is formed in float-pair
-// arithmetic (about 48 significand bits) on the FP32 pipe, the solution
-// returned in FP64.
+// inside defect correction.  The defect correction's outer residual, its
+// norm and the update of psi run either in FP64 (GB_BATCH_MIXED_F64OUTER)
+// or in float-pair arithmetic (about 48 significand bits) on the FP32 pipe
+// (GB_BATCH_MIXED); the solution is returned in FP64 either way.
 //
 // Execution: every level of every problem larger than LOCAL_N is processed
 // by level-synchronous kernels whose blocks are drawn from one table over
@@ -162,7 +163,7 @@ struct BatchDev {
     double *fnorm, *relres;   // [p]
     double *partial;          // per level-0 block
     const int *p_blk0, *p_nblk0;  // level-0 table range of each problem
-    double *const *psi;       // [p] the caller's FP64 solution of level 0
+    double *const *psi;       // [p] the caller's solution of level 0 (FP64, or float pairs in place)
     // [p*BP_MAXL + l] h^2 and 1/h^2 of level l, h = 1/(n-1), rounded in the
     // precision of use; formed once on the host (IEEE division there as
     // here) so that no thread spends FP64 divisions on them
@@ -306,10 +307,20 @@ __device__ __forceinline__ void tile_sweeps(T *sx, const T *sf, int ox, int oy, 
     }
 }
 
+// Correction modes of the last level-0 operation of an inner cycle:
+// CM_NONE stores the tile into x; CM_PAIR adds it to psi held as float
+// pairs (GB_BATCH_MIXED); CM_F64 adds it, widened exactly, to the FP64 psi
+// (GB_BATCH_MIXED_F64OUTER).
+#define CM_NONE 0
+#define CM_PAIR 1
+#define CM_F64 2
+
 // psi values of the points this thread stores (fixed assignment: row
 // warp + 8*rr, column lane + 32*cc of the tile), fetched together after the
 // sweeps so that the defect correction's reads of psi overlap one another.
-__device__ __forceinline__ void psi_prefetch(const float2 *psi, int x0, int y0, int n, float2 (&pv)[ST_R * ST_C])
+// Both correction modes hold 8 bytes per point (a float pair or a double).
+template <class V>
+__device__ __forceinline__ void psi_prefetch(const V *psi, int x0, int y0, int n, V (&pv)[ST_R * ST_C])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -318,16 +329,22 @@ __device__ __forceinline__ void psi_prefetch(const float2 *psi, int x0, int y0, 
         for (int cc = 0; cc < ST_C; ++cc) {
             const int gy = y0 + warp + 8 * rr, gx = x0 + lane + 32 * cc;
             const bool in = gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2;
-            pv[rr * ST_C + cc] = in ? psi[(size_t)gy * n + gx] : make_float2(0.f, 0.f);
+            V z;
+            if constexpr (std::is_same<V, float2>::value) z = make_float2(0.f, 0.f);
+            else z = (V)0;
+            pv[rr * ST_C + cc] = in ? psi[(size_t)gy * n + gx] : z;
         }
 }
 
-// Stores the tile's interior points into x, or (CORRECT) adds them to the
-// FP64 solution: the last level-0 operation of an inner cycle applies the
+template <int CM> struct CorrVal { typedef float2 type; };
+template <> struct CorrVal<CM_F64> { typedef double type; };
+
+// Stores the tile's interior points into x, or (CM != CM_NONE) adds them to
+// the solution: the last level-0 operation of an inner cycle applies the
 // defect correction psi += e point by point.
-template <class T, int H, bool CORRECT>
-__device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, int y0, int n, T *x,
-                                           float2 *psi, const float2 (&pv)[ST_R * ST_C])
+template <class T, int H, int CM>
+__device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, int y0, int n, T *x, void *psi,
+                                           const typename CorrVal<CM>::type (&pv)[ST_R * ST_C])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -338,7 +355,8 @@ __device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, 
             if (gx < 1 || gx > n - 2 || gy < 1 || gy > n - 2) continue;
             const size_t g = (size_t)gy * n + gx;
             const T v = sx[TileLayout<T, H>::at(gy - oy, gx - ox)];
-            if (CORRECT) psi[g] = df_add_f(pv[rr * ST_C + cc], (float)v);
+            if constexpr (CM == CM_PAIR) ((float2 *)psi)[g] = df_add_f(pv[rr * ST_C + cc], (float)v);
+            else if constexpr (CM == CM_F64) ((double *)psi)[g] = pv[rr * ST_C + cc] + f2d((float)v);
             else x[g] = v;
         }
 }
@@ -390,7 +408,7 @@ __device__ __forceinline__ void tile_load(T *sx, T *sf, const T *x, const T *f, 
 // not read.  RESTRICT: also form the residual on the tile plus one ring and
 // its full weighting (rotann2.f:773-785 summation order) onto the coarse
 // points of the tile, which the halo of 2*NU + 2 makes exact.
-template <class T, int NU, bool CORR, bool RESTRICT>
+template <class T, int NU, int CM, bool RESTRICT>
 __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, int src, int dst,
                           unsigned char *smem)
 {
@@ -402,9 +420,9 @@ __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, 
     tile_load<T, H>(sx, sf, XS<T>(B, e.p, l, src), FP<T>(B, e.p, l), ox, oy, n, zero_init != 0, true);
     __syncthreads();
     tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
-    float2 pv[ST_R * ST_C];
-    if (CORR) psi_prefetch((const float2 *)B.psi[e.p], x0, y0, n, pv);
-    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? (float2 *)B.psi[e.p] : nullptr, pv);
+    typename CorrVal<CM>::type pv[ST_R * ST_C];
+    if (CM != CM_NONE) psi_prefetch((const typename CorrVal<CM>::type *)B.psi[e.p], x0, y0, n, pv);
+    tile_store<T, H, CM>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CM != CM_NONE ? (void *)B.psi[e.p] : nullptr, pv);
     if (RESTRICT) {
         // residual on the tile plus one ring, in place of f (each point
         // reads f only at itself and x, which stays put, so both colours of
@@ -469,8 +487,8 @@ __device__ void op_smooth(const BatchDev &B, TileEntry e, int l, int zero_init, 
 
 // Bilinear prolongation of level l+1 (buffer 0) added into level l (buffer
 // src) over the tile and its halo (rotann2.f:821-858), then NU
-// post-smoothing sweeps, stored into buffer dst (or added to psi: CORR).
-template <class T, int NU, bool CORR>
+// post-smoothing sweeps, stored into buffer dst (or added to psi: CM).
+template <class T, int NU, int CM>
 __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int dst, unsigned char *smem)
 {
     constexpr int H = 2 * NU, SX = TX + 2 * H, SY = TY + 2 * H;
@@ -525,9 +543,9 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
     }
     __syncthreads();
     if (NU > 0) tile_sweeps<T, H>(sx, sf, ox, oy, x0, y0, n, H2<T>(B, e.p, l), NU);
-    float2 pv[ST_R * ST_C];
-    if (CORR) psi_prefetch((const float2 *)B.psi[e.p], x0, y0, n, pv);
-    tile_store<T, H, CORR>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CORR ? (float2 *)B.psi[e.p] : nullptr, pv);
+    typename CorrVal<CM>::type pv[ST_R * ST_C];
+    if (CM != CM_NONE) psi_prefetch((const typename CorrVal<CM>::type *)B.psi[e.p], x0, y0, n, pv);
+    tile_store<T, H, CM>(sx, ox, oy, x0, y0, n, XS<T>(B, e.p, l, dst), CM != CM_NONE ? (void *)B.psi[e.p] : nullptr, pv);
     __syncthreads();
 }
 
@@ -563,10 +581,11 @@ __device__ __forceinline__ T loc_residual(const T *x, const T *f, int n, int c, 
 
 // zero0: the level-dloc solution starts at zero (a coarse correction, or the
 // first inner cycle of a mixed solve); corr0 (dloc == 0 only): add the
-// result to the FP64 solution instead of storing it.
+// result to the solution instead of storing it, as float pairs or (f64) to
+// the FP64 solution.
 template <class T>
 __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_level0, int correct_level0,
-                         unsigned char *smem)
+                         int f64, unsigned char *smem)
 {
     T *sm = (T *)smem;
     const int L = B.nlev[p], d0 = B.dloc[p];
@@ -641,7 +660,10 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
     }
     {
         const int n = B.n_of[p * BP_MAXL + d0];
-        if (d0 == 0 && correct_level0) {
+        if (d0 == 0 && correct_level0 && f64) {
+            double *psi = (double *)B.psi[p];
+            for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = psi[q] + f2d((float)X[q]);
+        } else if (d0 == 0 && correct_level0) {
             float2 *psi = (float2 *)B.psi[p];
             for (int q = threadIdx.x; q < n * n; q += blockDim.x) psi[q] = df_add_f(psi[q], (float)X[q]);
         } else {
@@ -659,17 +681,19 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
 // residual r = f - A psi, its squared norm (the tile's partial sum) and,
 // when store_r, r rounded to FP32 as the inner cycle's right-hand side.
 // psi is only read here, so neighbouring tiles may overlap freely.
-// T = double (plain FP64 cycles): psi and f are the caller's FP64 arrays
-// and the pass forms only the norm.  T = float (FP32 inner cycles): psi is
-// held as float pairs in the caller's array and f as float pairs split at
-// the start of the solve; the residual is formed in pair arithmetic
-// (rounding error about 2^-48 of the terms) and its high part is both the
-// FP32 right-hand side and, widened exactly, the term of the FP64 norm.
-template <class T>
+// OM = CM_NONE (plain FP64 cycles): psi and f are the caller's FP64 arrays
+// and the pass forms only the norm.  OM = CM_F64 (FP32 inner cycles, FP64
+// defect correction): the same FP64 residual, also stored rounded to FP32
+// as the inner cycles' right-hand side.  OM = CM_PAIR: psi is held as float
+// pairs in the caller's array and f as float pairs split at the start of
+// the solve; the residual is formed in pair arithmetic (rounding error
+// about 2^-48 of the terms) and its high part is both the FP32 right-hand
+// side and, widened exactly, the term of the FP64 norm.
+template <class T, int OM>
 __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *const *f_p, int store_r,
                          unsigned char *smem)
 {
-    constexpr bool PAIR = sizeof(T) == 4;
+    constexpr bool PAIR = OM == CM_PAIR;
     using V = typename std::conditional<PAIR, float2, double>::type;
     constexpr int SX = TX + 2, SY = TY + 2;
     V *sp = (V *)smem;
@@ -802,6 +826,7 @@ __device__ void op_copyback(const BatchDev &B, TileEntry e)
 
 // One warp per problem: sums the problem's tile partials in a fixed order
 // and decides whether it keeps cycling.  first != 0 records ||f|| (psi = 0).
+// A residual norm that is not finite stops the problem as failed (2).
 __device__ void op_finalize(const BatchDev &B, int p, int first)
 {
     const int lane = threadIdx.x & 31;
@@ -815,7 +840,11 @@ __device__ void op_finalize(const BatchDev &B, int p, int first)
     if (first) B.fnorm[p] = rn;
     const double fn = B.fnorm[p];
     B.relres[p] = fn > 0.0 ? rn / fn : 0.0;
-    if (rn <= B.rtol * fn) {
+    if (!(rn <= 1.79769313486231570815e308)) {
+        // a NaN or an infinity in the residual (or in f): the problem stops
+        B.active[p] = 0;
+        B.failed[p] = 2;
+    } else if (rn <= B.rtol * fn) {
         B.active[p] = 0;
     } else if (B.cycles[p] >= B.max_cycles) {
         B.active[p] = 0;
@@ -842,7 +871,26 @@ struct Op {
     int aux;          // OP_LOCAL: zero0 | corr0 << 1; OP_OUTER: store_r; OP_FINALIZE: first
 };
 
-// Runs work item `item` of op on this block.
+// Runs work item `item` of op on this block.  op.corr is the correction
+// mode (CM_*) of the operation that applies the defect correction, and of
+// the outer pass.
+template <class T, int NU, bool RESTRICT>
+__device__ __forceinline__ void run_smooth(const BatchDev &B, TileEntry e, const Op &op, unsigned char *smem)
+{
+    if constexpr (sizeof(T) == 8) op_smooth<T, NU, CM_NONE, RESTRICT>(B, e, op.l, op.zero, op.src, op.dst, smem);
+    else if (op.corr == CM_PAIR) op_smooth<T, NU, CM_PAIR, RESTRICT>(B, e, op.l, op.zero, op.src, op.dst, smem);
+    else if (op.corr == CM_F64) op_smooth<T, NU, CM_F64, RESTRICT>(B, e, op.l, op.zero, op.src, op.dst, smem);
+    else op_smooth<T, NU, CM_NONE, RESTRICT>(B, e, op.l, op.zero, op.src, op.dst, smem);
+}
+template <class T, int NU>
+__device__ __forceinline__ void run_prolong(const BatchDev &B, TileEntry e, const Op &op, unsigned char *smem)
+{
+    if constexpr (sizeof(T) == 8) op_prolong<T, NU, CM_NONE>(B, e, op.l, op.src, op.dst, smem);
+    else if (op.corr == CM_PAIR) op_prolong<T, NU, CM_PAIR>(B, e, op.l, op.src, op.dst, smem);
+    else if (op.corr == CM_F64) op_prolong<T, NU, CM_F64>(B, e, op.l, op.src, op.dst, smem);
+    else op_prolong<T, NU, CM_NONE>(B, e, op.l, op.src, op.dst, smem);
+}
+
 template <class T>
 __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *tiles, const double *const *f_p,
                                          const Op &op, int item, int nu1, int nu2, unsigned char *smem)
@@ -851,43 +899,34 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
     case OP_SMOOTH: {
         const TileEntry e = tiles[op.off + item];
         if (!B.active[e.p]) return;
-        if (op.nu == 2) {
-            if (op.corr) op_smooth<T, 2, true, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
-            else op_smooth<T, 2, false, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
-        } else {
-            if (op.corr) op_smooth<T, 1, true, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
-            else op_smooth<T, 1, false, false>(B, e, op.l, op.zero, op.src, op.dst, smem);
-        }
+        if (op.nu == 2) run_smooth<T, 2, false>(B, e, op, smem);
+        else run_smooth<T, 1, false>(B, e, op, smem);
         return;
     }
     case OP_SMOOTH_R: {
         const TileEntry e = tiles[op.off + item];
         if (!B.active[e.p]) return;
-        if (op.nu == 2) op_smooth<T, 2, false, true>(B, e, op.l, op.zero, op.src, op.dst, smem);
-        else op_smooth<T, 1, false, true>(B, e, op.l, op.zero, op.src, op.dst, smem);
+        if (op.nu == 2) op_smooth<T, 2, CM_NONE, true>(B, e, op.l, op.zero, op.src, op.dst, smem);
+        else op_smooth<T, 1, CM_NONE, true>(B, e, op.l, op.zero, op.src, op.dst, smem);
         return;
     }
     case OP_PROLONG: {
         const TileEntry e = tiles[op.off + item];
         if (!B.active[e.p]) return;
-        if (op.nu == 2) {
-            if (op.corr) op_prolong<T, 2, true>(B, e, op.l, op.src, op.dst, smem);
-            else op_prolong<T, 2, false>(B, e, op.l, op.src, op.dst, smem);
-        } else if (op.nu == 1) {
-            if (op.corr) op_prolong<T, 1, true>(B, e, op.l, op.src, op.dst, smem);
-            else op_prolong<T, 1, false>(B, e, op.l, op.src, op.dst, smem);
-        } else {
-            if (op.corr) op_prolong<T, 0, true>(B, e, op.l, op.src, op.dst, smem);
-            else op_prolong<T, 0, false>(B, e, op.l, op.src, op.dst, smem);
-        }
+        if (op.nu == 2) run_prolong<T, 2>(B, e, op, smem);
+        else if (op.nu == 1) run_prolong<T, 1>(B, e, op, smem);
+        else run_prolong<T, 0>(B, e, op, smem);
         return;
     }
     case OP_LOCAL:
         if (!B.active[item]) return;
-        op_local<T>(B, item, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, smem);
+        op_local<T>(B, item, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, (op.aux >> 2) & 1, smem);
         return;
     case OP_OUTER:
-        op_outer<T>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
+        if constexpr (sizeof(T) == 8) op_outer<T, CM_NONE>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
+        else if (op.corr == CM_PAIR) op_outer<T, CM_PAIR>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
+        else if (op.corr == CM_F64) op_outer<T, CM_F64>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
+        else op_outer<T, CM_NONE>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
         return;
     case OP_COPYBACK: {
         const TileEntry e = tiles[op.off + item];
@@ -907,14 +946,19 @@ __global__ void __launch_bounds__(LOCAL_THREADS) k_local(BatchDev B, Op op, int 
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (!B.active[blockIdx.x]) return;
-    op_local<T>(B, blockIdx.x, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, smem_raw);
+    op_local<T>(B, blockIdx.x, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, (op.aux >> 2) & 1, smem_raw);
 }
 
 // One kernel launch per operation (graph path).
 // The prolongation variants fit five blocks' shared tiles per SM and are
-// held to the registers of five; the outer pass is held to four.
-template <class T, int KIND, int NU, bool CORR>
-__global__ void __launch_bounds__(TILE_THREADS, KIND == OP_PROLONG ? 5 : (KIND == OP_OUTER ? 4 : 1)) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
+// held to the registers of five, except those that also apply the defect
+// correction (eight more values per thread: held to four, where they need no
+// spills); the outer pass is held to four.
+template <int KIND, int CM> struct OpMinBlocks {
+    static constexpr int value = KIND == OP_PROLONG ? (CM == CM_NONE ? 5 : 4) : (KIND == OP_OUTER ? 4 : 1);
+};
+template <class T, int KIND, int NU, int CM>
+__global__ void __launch_bounds__(TILE_THREADS, (OpMinBlocks<KIND, CM>::value)) k_op(BatchDev B, const TileEntry *tiles, const double *const *f_p,
                                                      Op op, int nu1, int nu2)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -926,7 +970,7 @@ __global__ void __launch_bounds__(TILE_THREADS, KIND == OP_PROLONG ? 5 : (KIND =
     Op o = op;
     o.kind = KIND;
     o.nu = NU;
-    o.corr = CORR ? 1 : 0;
+    o.corr = CM;
     run_item<T>(B, tiles, f_p, o, blockIdx.x, nu1, nu2, smem_raw);
 }
 
@@ -1006,6 +1050,7 @@ struct gb_batch {
     int plan_inner = -1;
     // persistent launch
     unsigned *d_sync = nullptr;         // count, gen, err
+    long long wait_limit = GB_GRID_WAIT_LIMIT_DEFAULT;   // polls a barrier wait may take
     int pgrid = 0;
     size_t psmem = 0;
     // graph path
@@ -1032,6 +1077,14 @@ static int levels_of(int n, int *nl)
         n = (n - 1) / 2 + 1;
     }
     return L;
+}
+
+// Inner cycles in FP32 (either mixed mode), and the correction mode the
+// defect correction applies psi's updates and forms its residual with.
+static bool inner32(const gb_batch *b) { return b->precision != GB_BATCH_FP64; }
+static int corr_mode(const gb_batch *b)
+{
+    return b->precision == GB_BATCH_MIXED ? CM_PAIR : b->precision == GB_BATCH_MIXED_F64OUTER ? CM_F64 : CM_NONE;
 }
 
 // Two colour-split arrays (x and f) of a tile with halo H (TileLayout).
@@ -1076,7 +1129,8 @@ template <class T> static int ops_for(int nu)
 template <class T>
 static void plan_vcycle(gb_batch *b, std::vector<Op> &v, bool zero0, bool corr0, int *cur0)
 {
-    const bool mixed = b->precision == GB_BATCH_MIXED;
+    const bool mixed = inner32(b);
+    const int cm = corr_mode(b);
     int cur[BP_MAXL] = {0};
     const int k1 = ops_for<T>(b->nu1);
     const int pro = std::min(b->nu2, sizeof(T) == 4 ? 2 : 1);  // sweeps fused into the prolongation
@@ -1107,16 +1161,16 @@ static void plan_vcycle(gb_batch *b, std::vector<Op> &v, bool zero0, bool corr0,
         Op o{};
         o.kind = OP_LOCAL;
         o.cnt = b->nprob;
-        o.aux = ((mixed && zero0) ? 1 : 0) | ((mixed && corr0) ? 2 : 0);
+        o.aux = ((mixed && zero0) ? 1 : 0) | ((mixed && corr0) ? 2 : 0) | (cm == CM_F64 ? 4 : 0);
         v.push_back(o);
     }
     for (int l = b->maxdepth_global - 1; l >= 0; --l) {
         if (b->ft_cnt[l] == 0) continue;
-        const int correct_last = (mixed && l == 0 && corr0) ? 1 : 0;
+        const int correct_last = (mixed && l == 0 && corr0) ? cm : CM_NONE;
         int src = cur[l], dst = 1 - cur[l];
         Op o{};
         o.kind = OP_PROLONG; o.l = l; o.nu = pro; o.src = src; o.dst = dst;
-        o.corr = k2 == 0 ? correct_last : 0;
+        o.corr = k2 == 0 ? correct_last : CM_NONE;
         o.off = b->ft_off[l]; o.cnt = b->ft_cnt[l];
         v.push_back(o);
         src = dst;
@@ -1126,7 +1180,7 @@ static void plan_vcycle(gb_batch *b, std::vector<Op> &v, bool zero0, bool corr0,
             const int k = sweeps_per_op<T>(nu);
             Op q{};
             q.kind = OP_SMOOTH; q.l = l; q.nu = k; q.zero = 0; q.src = src; q.dst = dst;
-            q.corr = (i == k2 - 1) ? correct_last : 0;
+            q.corr = (i == k2 - 1) ? correct_last : CM_NONE;
             q.off = b->ft_off[l]; q.cnt = b->ft_cnt[l];
             v.push_back(q);
             nu -= k;
@@ -1151,9 +1205,9 @@ template <class T>
 static void plan_iteration(gb_batch *b, std::vector<Op> &v, int first)
 {
     v.clear();
-    const bool mixed = b->precision == GB_BATCH_MIXED;
+    const bool mixed = inner32(b);
     Op o{};
-    o.kind = OP_OUTER; o.off = b->ot_off; o.cnt = b->ot_cnt; o.aux = mixed ? 1 : 0;
+    o.kind = OP_OUTER; o.off = b->ot_off; o.cnt = b->ot_cnt; o.aux = mixed ? 1 : 0; o.corr = corr_mode(b);
     v.push_back(o);
     Op f{};
     f.kind = OP_FINALIZE; f.cnt = b->nprob; f.aux = first;
@@ -1165,7 +1219,7 @@ static void plan_iteration(gb_batch *b, std::vector<Op> &v, int first)
 
 static void build_plans(gb_batch *b)
 {
-    if (b->precision == GB_BATCH_MIXED) {
+    if (inner32(b)) {
         plan_iteration<float>(b, b->ops0, 1);
         plan_iteration<float>(b, b->ops, 0);
     } else {
@@ -1175,69 +1229,85 @@ static void build_plans(gb_batch *b)
     b->plan_inner = b->inner;
 }
 
+// Correction modes a kernel of inner precision T is built for: the plain
+// FP64 solve never corrects; the FP32 inner cycles correct psi as float
+// pairs or in FP64.
+template <class T, int KIND, int NU>
+static cudaError_t smem_attr_cm(size_t sz)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_op<T, KIND, NU, CM_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
+    if constexpr (sizeof(T) == 4) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_op<T, KIND, NU, CM_PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_op<T, KIND, NU, CM_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
+    }
+    return e;
+}
+
 template <class T> static cudaError_t set_smem_attrs(size_t local, size_t persistent)
 {
     cudaError_t e;
-#define SA(k, sz) if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sz))) != cudaSuccess) return e
-    SA((k_op<T, OP_SMOOTH, 1, false>), smem_tile<T>(2));
-    SA((k_op<T, OP_SMOOTH, 2, false>), smem_tile<T>(4));
-    SA((k_op<T, OP_SMOOTH, 1, true>), smem_tile<T>(2));
-    SA((k_op<T, OP_SMOOTH, 2, true>), smem_tile<T>(4));
-    SA((k_op<T, OP_SMOOTH_R, 1, false>), smem_tile<T>(4));
-    SA((k_op<T, OP_SMOOTH_R, 2, false>), smem_tile<T>(6));
-    SA((k_op<T, OP_PROLONG, 0, false>), smem_tile<T>(0));
-    SA((k_op<T, OP_PROLONG, 1, false>), smem_tile<T>(2));
-    SA((k_op<T, OP_PROLONG, 2, false>), smem_tile<T>(4));
-    SA((k_op<T, OP_PROLONG, 0, true>), smem_tile<T>(0));
-    SA((k_op<T, OP_PROLONG, 1, true>), smem_tile<T>(2));
-    SA((k_op<T, OP_PROLONG, 2, true>), smem_tile<T>(4));
-    SA((k_local<T>), local);
-    SA((k_persistent<T>), persistent);
+#define SA(call) if ((e = (call)) != cudaSuccess) return e
+    SA((smem_attr_cm<T, OP_SMOOTH, 1>(smem_tile<T>(2))));
+    SA((smem_attr_cm<T, OP_SMOOTH, 2>(smem_tile<T>(4))));
+    SA((cudaFuncSetAttribute(k_op<T, OP_SMOOTH_R, 1, CM_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tile<T>(4))));
+    SA((cudaFuncSetAttribute(k_op<T, OP_SMOOTH_R, 2, CM_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tile<T>(6))));
+    SA((smem_attr_cm<T, OP_PROLONG, 0>(smem_tile<T>(0))));
+    SA((smem_attr_cm<T, OP_PROLONG, 1>(smem_tile<T>(2))));
+    SA((smem_attr_cm<T, OP_PROLONG, 2>(smem_tile<T>(4))));
+    SA((cudaFuncSetAttribute(k_local<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)local)));
+    SA((cudaFuncSetAttribute(k_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)persistent)));
 #undef SA
     return cudaSuccess;
+}
+
+// Launches k_op<T, KIND, NU, cm> (graph path).
+template <class T, int KIND, int NU>
+static void launch_k(const gb_batch *b, int cm, int g, size_t sm, cudaStream_t s, const Op &op)
+{
+    const TileEntry *t = b->d_tiles;
+    const double *const *fp = (const double *const *)b->d_f_tab;
+    const int n1 = b->nu1, n2 = b->nu2;
+    if constexpr (sizeof(T) == 4) {
+        if (cm == CM_PAIR) { k_op<T, KIND, NU, CM_PAIR><<<g, TILE_THREADS, sm, s>>>(b->dev, t, fp, op, n1, n2); return; }
+        if (cm == CM_F64) { k_op<T, KIND, NU, CM_F64><<<g, TILE_THREADS, sm, s>>>(b->dev, t, fp, op, n1, n2); return; }
+    }
+    k_op<T, KIND, NU, CM_NONE><<<g, TILE_THREADS, sm, s>>>(b->dev, t, fp, op, n1, n2);
 }
 
 // Launches one operation as its own kernel (graph path).
 template <class T>
 static void launch_op(gb_batch *b, const Op &op, cudaStream_t s)
 {
-    const BatchDev &D = b->dev;
-    const TileEntry *t = b->d_tiles;
-    const double *const *fp = (const double *const *)b->d_f_tab;
     const size_t sm = smem_of<T>(b, op);
     const int g = op.cnt;
     if (g <= 0) return;
-    const int n1 = b->nu1, n2 = b->nu2;
     switch (op.kind) {
     case OP_SMOOTH:
-        if (op.nu == 2 && op.corr) k_op<T, OP_SMOOTH, 2, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else if (op.nu == 2) k_op<T, OP_SMOOTH, 2, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else if (op.corr) k_op<T, OP_SMOOTH, 1, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else k_op<T, OP_SMOOTH, 1, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        if (op.nu == 2) launch_k<T, OP_SMOOTH, 2>(b, op.corr, g, sm, s, op);
+        else launch_k<T, OP_SMOOTH, 1>(b, op.corr, g, sm, s, op);
         break;
     case OP_SMOOTH_R:
-        if (op.nu == 2) k_op<T, OP_SMOOTH_R, 2, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else k_op<T, OP_SMOOTH_R, 1, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        if (op.nu == 2) launch_k<T, OP_SMOOTH_R, 2>(b, CM_NONE, g, sm, s, op);
+        else launch_k<T, OP_SMOOTH_R, 1>(b, CM_NONE, g, sm, s, op);
         break;
     case OP_PROLONG:
-        if (op.nu == 2 && op.corr) k_op<T, OP_PROLONG, 2, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else if (op.nu == 2) k_op<T, OP_PROLONG, 2, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else if (op.nu == 1 && op.corr) k_op<T, OP_PROLONG, 1, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else if (op.nu == 1) k_op<T, OP_PROLONG, 1, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else if (op.corr) k_op<T, OP_PROLONG, 0, true><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
-        else k_op<T, OP_PROLONG, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        if (op.nu == 2) launch_k<T, OP_PROLONG, 2>(b, op.corr, g, sm, s, op);
+        else if (op.nu == 1) launch_k<T, OP_PROLONG, 1>(b, op.corr, g, sm, s, op);
+        else launch_k<T, OP_PROLONG, 0>(b, op.corr, g, sm, s, op);
         break;
     case OP_LOCAL:
-        k_local<T><<<g, LOCAL_THREADS, sm, s>>>(D, op, n1, n2);
+        k_local<T><<<g, LOCAL_THREADS, sm, s>>>(b->dev, op, b->nu1, b->nu2);
         break;
     case OP_OUTER:
-        k_op<T, OP_OUTER, 0, false><<<g, TILE_THREADS, sm, s>>>(D, t, fp, op, n1, n2);
+        launch_k<T, OP_OUTER, 0>(b, op.corr, g, sm, s, op);
         break;
     case OP_FINALIZE:
-        k_op<T, OP_FINALIZE, 0, false><<<gb_ceil_div(b->nprob, TILE_THREADS / 32), TILE_THREADS, 0, s>>>(D, t, fp, op, n1, n2);
+        launch_k<T, OP_FINALIZE, 0>(b, CM_NONE, gb_ceil_div(b->nprob, TILE_THREADS / 32), 0, s, op);
         break;
     case OP_COPYBACK:
-        k_op<T, OP_COPYBACK, 0, false><<<g, TILE_THREADS, 0, s>>>(D, t, fp, op, n1, n2);
+        launch_k<T, OP_COPYBACK, 0>(b, CM_NONE, g, 0, s, op);
         break;
     }
     b->launches += 1;
@@ -1246,7 +1316,8 @@ static void launch_op(gb_batch *b, const Op &op, cudaStream_t s)
 extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
                                int max_cycles, gb_batch **out)
 {
-    if (!out || !n || nprob <= 0 || (precision != GB_BATCH_FP64 && precision != GB_BATCH_MIXED) || nu1 < 1 ||
+    if (!out || !n || nprob <= 0 ||
+        (precision != GB_BATCH_FP64 && precision != GB_BATCH_MIXED && precision != GB_BATCH_MIXED_F64OUTER) || nu1 < 1 ||
         nu1 > 8 || nu2 < 0 || nu2 > 8 || max_cycles < 0 || !(rtol >= 0.0)) {
         gb_set_error("gb_batch_create: invalid argument (need nprob > 0, 1 <= nu1 <= 8, 0 <= nu2 <= 8)");
         return GB_ERR_INVALID;
@@ -1517,6 +1588,16 @@ extern "C" int gb_batch_set_inner_cycles(gb_batch *b, int inner)
     return GB_OK;
 }
 
+extern "C" int gb_batch_set_wait_limit(gb_batch *b, long long polls)
+{
+    if (!b || polls < 0) {
+        gb_set_error("gb_batch_set_wait_limit: need a handle and polls >= 0");
+        return GB_ERR_INVALID;
+    }
+    b->wait_limit = polls;
+    return GB_OK;
+}
+
 extern "C" int gb_batch_set_exec(gb_batch *b, int mode)
 {
     if (!b || (mode != GB_BATCH_EXEC_GRAPH && mode != GB_BATCH_EXEC_PERSISTENT)) {
@@ -1551,7 +1632,7 @@ static void enqueue_iteration(gb_batch *b, const std::vector<Op> &v, cudaStream_
         const bool timed = (op.l == 0 && op.kind != OP_FINALIZE && op.kind != OP_LOCAL) || op.kind == OP_OUTER;
         const bool ev = b->profile && timed && b->ev_used + 2 <= (int)b->ev.size();
         if (ev) prof_record(b->ev[b->ev_used], s);
-        if (b->precision == GB_BATCH_MIXED) launch_op<float>(b, op, s);
+        if (inner32(b)) launch_op<float>(b, op, s);
         else launch_op<double>(b, op, s);
         if (ev) {
             prof_record(b->ev[b->ev_used + 1], s);
@@ -1594,7 +1675,7 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
         if (b->dloc[p] > 0) pts_tile += pts;
     }
     const double esz = b->precision == GB_BATCH_FP64 ? 8.0 : 4.0;
-    const bool mixed = b->precision == GB_BATCH_MIXED;
+    const bool mixed = inner32(b);
     const int pre = (mixed && b->nu1 >= 2) ? 2 : 1;
     const int post = std::min(b->nu2, mixed ? 2 : 1);
     for (int i = 0; i + 1 < b->ev_used; i += 2) {
@@ -1666,7 +1747,7 @@ extern "C" int gb_batch_profile_read_kind(gb_batch *b, int kind, double *ms, lon
 static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStream_t s)
 {
     std::vector<const void *> pf(b->nprob), pp(b->nprob);
-    const bool mixed = b->precision == GB_BATCH_MIXED;
+    const bool mixed = b->precision == GB_BATCH_MIXED;   // float-pair right-hand side
     for (int p = 0; p < b->nprob; ++p) {
         pf[p] = mixed ? (const void *)(b->d_fpairs + b->off0[p]) : (const void *)(d_f + b->off0[p]);
         pp[p] = d_psi + b->off0[p];
@@ -1736,7 +1817,7 @@ static int solve_persistent(gb_batch *b, cudaStream_t s)
     gs.count = b->d_sync;
     gs.gen = b->d_sync + 1;
     gs.err = (int *)(b->d_sync + 2);
-    gs.limit = 1LL << 24;   // ~1-2 s of polling at 64 ns per poll
+    gs.limit = b->wait_limit;
     const Op *ops0 = b->d_ops, *ops = b->d_ops + n0;
     const TileEntry *tiles = b->d_tiles;
     const double *const *fp = (const double *const *)b->d_f_tab;
@@ -1817,9 +1898,16 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
     if (relres) GB_CUDA_TRY(cudaMemcpyAsync(relres, D.relres, sizeof(double) * b->nprob, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     GB_CUDA_TRY(cudaGetLastError());
-    for (int p = 0; p < b->nprob; ++p)
-        if (fl[p]) return GB_MAXSWEEPS;
-    return GB_OK;
+    int st_out = GB_OK;
+    for (int p = 0; p < b->nprob; ++p) {
+        if (fl[p] == 2) {
+            gb_set_error("gb_batch_solve: problem %d has a residual norm that is not finite (NaN or infinity in "
+                         "f or in the iterates)", p);
+            return GB_NAN;
+        }
+        if (fl[p]) st_out = GB_MAXSWEEPS;
+    }
+    return st_out;
 }
 
 extern "C" int gb_batch_solve_host(gb_batch *b, const double *h_f, double *h_psi, int *cycles, double *relres)

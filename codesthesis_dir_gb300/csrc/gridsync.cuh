@@ -6,7 +6,9 @@
 // Grid-wide barrier of a persistent (cooperatively launched) kernel.  Every wait is bounded: a
 // block that waits longer than `limit` polls sets the error flag and every
 // block leaves the kernel at its next barrier, so a lost block cannot hang
-// the GPU.
+// the GPU.  The outcome is read once per block (by the thread that waited)
+// and handed to the whole block through shared memory, so all threads of a
+// block leave together even when another block raises the flag meanwhile.
 struct GridSync {
     unsigned *count;
     unsigned *gen;
@@ -14,8 +16,12 @@ struct GridSync {
     long long limit;
 };
 
+// Default wait limit: about 1-2 s of polling at 64 ns per poll.
+#define GB_GRID_WAIT_LIMIT_DEFAULT (1LL << 24)
+
 __device__ __forceinline__ bool grid_sync(const GridSync &gs)
 {
+    __shared__ int s_grid_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *vgen = gs.gen;
@@ -37,8 +43,9 @@ __device__ __forceinline__ bool grid_sync(const GridSync &gs)
             }
         }
         __threadfence();
+        s_grid_ok = *(volatile int *)gs.err == 0;
     }
     __syncthreads();
-    return *(volatile int *)gs.err == 0;
+    return s_grid_ok != 0;
 }
 

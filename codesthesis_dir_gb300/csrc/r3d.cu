@@ -2254,7 +2254,7 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
         d.gs[c].count = h->sync + R3_SYNC_STRIDE * c;
         d.gs[c].gen = h->sync + R3_SYNC_STRIDE * c + 1;
         d.gs[c].err = (int *)(h->sync + R3_SYNC_STRIDE * c + 2);
-        d.gs[c].limit = 1LL << 24;
+        d.gs[c].limit = GB_GRID_WAIT_LIMIT_DEFAULT;
     }
     // factor tables
     FacJob *djobs = nullptr;
@@ -2311,6 +2311,16 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
 }
 
 extern "C" void *gb_r3d_stream(gb_r3d *h) { return h ? (void *)h->stream : nullptr; }
+
+extern "C" int gb_r3d_set_wait_limit(gb_r3d *h, long long polls)
+{
+    if (!h || polls < 0) {
+        gb_set_error("gb_r3d_set_wait_limit: need a context and polls >= 0");
+        return GB_ERR_INVALID;
+    }
+    for (int c = 0; c < 4; ++c) h->dev.gs[c].limit = polls;
+    return GB_OK;
+}
 
 static int r3_io(gb_r3d *h, int field, double *host, int ld1, int ld2, bool to_dev)
 {

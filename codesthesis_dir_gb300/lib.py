@@ -40,7 +40,8 @@ PRB_DVD = 5       # velvor2ddvdbenchmark.f: the differentially heated cavity (np
 PRB_FP64 = 0
 PRB_MIXED = 1
 BATCH_FP64 = 0
-BATCH_MIXED = 1
+BATCH_MIXED = 1            # float-pair outer residual
+BATCH_MIXED_F64OUTER = 2   # FP64 outer residual, norm and update
 BATCH_EXEC_GRAPH = 0
 BATCH_EXEC_PERSISTENT = 1
 
@@ -167,6 +168,7 @@ SIGNATURES = [
     ("gb_r3d_update", C.c_int, [_vp]),
     ("gb_r3d_step", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
     ("gb_r3d_stream", _vp, [_vp]),
+    ("gb_r3d_set_wait_limit", C.c_int, [_vp, C.c_longlong]),
     ("gb_prb_bind_bounds", None, [C.c_int, C.c_int]),
     ("gb_prb_bind_smoother", None, [C.c_int]),
     ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),
@@ -200,6 +202,7 @@ SIGNATURES = [
     ("gb_batch_total_points", C.c_longlong, [_vp]),
     ("gb_batch_set_inner_cycles", C.c_int, [_vp, C.c_int]),
     ("gb_batch_set_exec", C.c_int, [_vp, C.c_int]),
+    ("gb_batch_set_wait_limit", C.c_int, [_vp, C.c_longlong]),
     ("gb_batch_solve_device", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("gb_batch_solve_host", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     ("gb_batch_submit_host", C.c_int, [_vp, _vp, _vp, _vp, _vp]),

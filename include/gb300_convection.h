@@ -464,6 +464,13 @@ int gb_r3d_step(gb_r3d *h, int nsteps, double *nu, int *sweeps, int *steps_done)
  * vertical annulus); nu is the step run's httrans1 there. */
 int gb_r3d_nu2(gb_r3d *h, int nsteps, double *nu2);
 void *gb_r3d_stream(gb_r3d *h);
+/* Polls a grid-wide barrier wait of the cooperative multigrid launches may
+ * take before the solve gives up with GB_TIMEOUT (default 2^24, about
+ * 1-2 s); 0 gives up at the first wait that is not already released.  The
+ * reference has no counterpart (its solves run on host threads); the
+ * context stays usable after a timeout, its fields hold whatever the
+ * interrupted step left. */
+int gb_r3d_set_wait_limit(gb_r3d *h, long long polls);
 
 /* ------------------------- stretched-grid streamfunction solve (rcsc.f) */
 /* The multigrid of rcsc.f:1118-1444 on a non-uniform (r, z) grid: operator
@@ -525,8 +532,12 @@ int gb_pdma_batch(const double *a, const double *b, const double *c, const doubl
  * every GPU loading the library holds until exit); larger requests return
  * GB_ERR_INVALID without launching.  The first call on each device looks up
  * the scratch array's device address (make that first call before any
- * stream capture).  All calls share the scratch: calls that overlap on the
- * GPU race.  Results are identical to gb_pdma_batch. */
+ * stream capture); the address is kept for the life of the process, so a
+ * cudaDeviceReset after that first call is not supported.  Each call waits
+ * for its stream before it returns (its status covers the kernel), so the
+ * calls of one host thread never overlap one another; all calls share the
+ * scratch, so calls from different host threads that overlap on the GPU
+ * race.  Results are identical to gb_pdma_batch. */
 #define GB_PDMA_NOALLOC_MAX_DOUBLES 524288u
 int gb_pdma_batch_noalloc(const double *a, const double *b, const double *c, const double *d,
                           const double *e, const double *r, double *x, int n, int nlines,
@@ -544,6 +555,11 @@ int gb_pdma_batch_noalloc(const double *a, const double *b, const double *c, con
                               outer residual in float-pair arithmetic (~48-bit
                               significands: f and psi held as FP32 hi + lo
                               pairs during the solve), psi returned in FP64 */
+#define GB_BATCH_MIXED_F64OUTER 2  /* FP32 inner V-cycles inside FP64 defect
+                              correction: the outer residual r = f - A psi, its
+                              norm and the update psi += e in FP64 on the
+                              caller's arrays; r rounded to FP32 is the inner
+                              cycles' right-hand side */
 
 typedef struct gb_batch gb_batch;
 
@@ -566,9 +582,16 @@ int gb_batch_set_inner_cycles(gb_batch *b, int inner);
 int gb_batch_set_exec(gb_batch *b, int mode);
 /* Total doubles of the packed f / psi arrays. */
 long long gb_batch_total_points(const gb_batch *b);
+/* Polls a grid-wide barrier wait of the persistent execution mode may take
+ * before the solve gives up with GB_TIMEOUT (default 2^24, about 1-2 s);
+ * 0 gives up at the first wait that is not already released.  The handle
+ * stays usable after a timeout. */
+int gb_batch_set_wait_limit(gb_batch *b, long long polls);
 /* Device-resident solve: d_f, d_psi device pointers (packed).  cycles and
  * relres (host, nprob each, may be NULL) receive per-problem V-cycle counts
- * and final relative residuals.  Returns GB_OK or GB_MAXSWEEPS.  A mixed
+ * and final relative residuals.  Returns GB_OK, GB_MAXSWEEPS, GB_NAN (a
+ * problem's residual norm is a NaN or infinite: that problem stops at once)
+ * or, in persistent mode, GB_TIMEOUT.  A mixed
  * solve keeps psi as float pairs in d_psi's own memory while it runs; d_psi
  * holds FP64 values again when the call returns (it synchronises stream). */
 int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_psi, int *cycles,

@@ -232,10 +232,49 @@ static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, doub
         memcpy(F[0], f, sizeof(double) * nn);
         for (;;) {
             if (cycles > 0) rn = orc_resnorm64(n, psi, f);
+            if (!isfinite(rn)) { status = 2; break; }
             if (rn <= rtol * fn) break;
             if (cycles >= max_cycles) { status = 1; break; }
             vcycle_64(L, nl, P, F, R, nu1, nu2, 0);
             ++cycles;
+        }
+        free(pool);
+    } else if (precision == ORC_BATCH_MIXED_F64OUTER) {
+        /* FP64 defect correction around FP32 inner V-cycles: the outer
+         * residual in FP64 (the plain solve's operations), rounded to FP32 as
+         * the inner right-hand side; psi += e in FP64, e widened exactly */
+        float *pool = (float *)calloc(tot * 3, sizeof(float));
+        float *P[32], *F[32], *R[32];
+        size_t off = 0;
+        for (int l = 0; l < L; ++l) {
+            P[l] = pool + off; F[l] = pool + tot + off; R[l] = pool + 2 * tot + off;
+            off += (size_t)nl[l] * nl[l];
+        }
+        const double h = 1.0 / (double)(n - 1);
+        const double ih2 = 1.0 / (h * h);
+        for (;;) {
+            double s = 0.0;
+            for (int j = 1; j <= n - 2; ++j)
+                for (int i = 1; i <= n - 2; ++i) {
+                    const size_t c = (size_t)j * n + i;
+                    const double sum = (psi[c - 1] + psi[c + 1]) + (psi[c - n] + psi[c + n]);
+                    const double lap = fma(-4.0, psi[c], sum);
+                    const double r = fma(-ih2, lap, f[c]);
+                    F[0][c] = (float)r;
+                    s = fma(r, r, s);
+                }
+            rn = sqrt(s);
+            if (!isfinite(rn)) { status = 2; break; }
+            if (rn <= rtol * fn) break;
+            if (cycles >= max_cycles) { status = 1; break; }
+            memset(P[0], 0, sizeof(float) * nn);
+            for (int k = 0; k < inner; ++k) vcycle_32(L, nl, P, F, R, nu1, nu2, 0);
+            for (int j = 1; j <= n - 2; ++j)
+                for (int i = 1; i <= n - 2; ++i) {
+                    const size_t c = (size_t)j * n + i;
+                    psi[c] = psi[c] + (double)P[0][c];
+                }
+            cycles += inner;
         }
         free(pool);
     } else {
@@ -274,6 +313,7 @@ static int solve_one(int n, const double *f, double *psi, int nu1, int nu2, doub
             rn = sqrt(s);
             if (first) fn = rn;   /* psi = 0: the norm of f's high parts */
             first = 0;
+            if (!isfinite(rn)) { status = 2; break; }
             if (rn <= rtol * fn) break;
             if (cycles >= max_cycles) { status = 1; break; }
             /* inner FP32 V-cycles on A e = r, e0 = 0 */
@@ -305,10 +345,11 @@ int orc_batch_solve(int nprob, const int *n, const long long *offset, const doub
 {
     if (inner < 1) inner = 1;
     int status = 0;
-#pragma omp parallel for schedule(dynamic, 1) reduction(| : status)
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : status)
     for (int p = 0; p < nprob; ++p) {
-        status |= solve_one(n[p], f + offset[p], psi + offset[p], nu1, nu2, rtol, max_cycles,
+        const int st = solve_one(n[p], f + offset[p], psi + offset[p], nu1, nu2, rtol, max_cycles,
                             precision, inner, &cycles[p], &relres[p]);
+        if (st > status) status = st;
     }
     return status;
 }

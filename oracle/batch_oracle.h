@@ -26,12 +26,14 @@ extern "C" {
 
 #define ORC_BATCH_FP64  0
 #define ORC_BATCH_MIXED 1   /* FP32 inner V-cycles, float-pair outer residual */
+#define ORC_BATCH_MIXED_F64OUTER 2   /* FP32 inner V-cycles, FP64 outer residual, norm and update */
 
 /* Solve every problem.  psi is overwritten (initial guess zero).  cycles[p]
  * receives the V-cycles taken, relres[p] the final ||f - A psi||_2/||f||_2.
  * inner: FP32 V-cycles per defect-correction step (mixed only).
- * Returns 0, or 1 if any problem hit max_cycles. Uses OpenMP threads over
- * problems when built with -fopenmp. */
+ * Returns 0; 1 if any problem hit max_cycles; 2 if any problem's residual
+ * norm was not finite (that problem stops at once).  Uses OpenMP threads
+ * over problems when built with -fopenmp. */
 int orc_batch_solve(int nprob, const int *n, const long long *offset,
                     const double *f, double *psi, int nu1, int nu2,
                     double rtol, int max_cycles, int precision, int inner,

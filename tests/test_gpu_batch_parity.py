@@ -47,8 +47,9 @@ SMALL = [3, 5, 9, 17, 33, 65, 129, 257, 65, 129, 3, 33, 513]
 
 
 @pytest.mark.parametrize("exec_mode", [0, 1], ids=["graph", "persistent"])
-@pytest.mark.parametrize("precision,inner", [(0, 1), (1, 1), (1, 2), (1, 3)],
-                         ids=["fp64", "mixed", "mixed-inner2", "mixed-inner3"])
+@pytest.mark.parametrize("precision,inner", [(0, 1), (1, 1), (1, 2), (1, 3), (2, 1), (2, 3), (2, 4)],
+                         ids=["fp64", "mixed", "mixed-inner2", "mixed-inner3", "f64outer", "f64outer-inner3",
+                              "f64outer-inner4"])
 def test_batch_matches_oracle(oracle, gblib, precision, inner, exec_mode):
     from codesthesis_dir_gb300.batch import BatchPoisson
     f = make_batch(SMALL, 7)
@@ -70,9 +71,10 @@ def test_batch_fp64_vs_mixed(gblib):
     sizes = [513, 257, 129, 65, 257, 513]
     f = make_batch(sizes, 11)
     _, p64, c64, r64 = BatchPoisson(sizes, precision=0).solve_host(f)
-    _, pmx, cmx, rmx = BatchPoisson(sizes, precision=1).solve_host(f)
-    assert np.all(r64 <= 1e-10) and np.all(rmx <= 1e-10)
-    assert np.linalg.norm(pmx - p64) / np.linalg.norm(p64) <= 1e-9
+    for prec in (1, 2):
+        _, pmx, cmx, rmx = BatchPoisson(sizes, precision=prec, inner=3).solve_host(f)
+        assert np.all(r64 <= 1e-10) and np.all(rmx <= 1e-10)
+        assert np.linalg.norm(pmx - p64) / np.linalg.norm(p64) <= 1e-9
 
 
 def test_batch_edge_cases(oracle, gblib):
@@ -106,13 +108,14 @@ def test_graph_and_persistent_agree_on_workload_sizes(gblib):
     from codesthesis_dir_gb300.batch import BatchPoisson
     sizes = [513, 65, 257, 129, 513, 129, 65, 257, 3, 17]
     f = make_batch(sizes, 21)
-    out = []
-    for mode in (0, 1):
-        st, psi, cyc, rr = BatchPoisson(sizes, precision=1, inner=3, exec_mode=mode).solve_host(f)
-        assert st == 0
-        out.append((psi, cyc))
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    np.testing.assert_array_equal(out[0][1], out[1][1])
+    for prec in (1, 2):
+        out = []
+        for mode in (0, 1):
+            st, psi, cyc, rr = BatchPoisson(sizes, precision=prec, inner=3, exec_mode=mode).solve_host(f)
+            assert st == 0
+            out.append((psi, cyc))
+        np.testing.assert_array_equal(out[0][0], out[1][0])
+        np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
 def test_integer_conversions_match_hardware(gblib):
@@ -126,7 +129,7 @@ def test_integer_conversions_match_hardware(gblib):
     assert (f2d.value, d2f.value) == (0, 0)
 
 
-@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("precision", [0, 1, 2], ids=["fp64", "mixed", "f64outer"])
 def test_pipelined_stream_matches_single_calls(gblib, precision):
     """A stream of different right-hand sides through the pipelined calls
     (upload of call k and download of call k-1 overlapping the solves) gives

@@ -51,3 +51,63 @@ def test_noalloc_rejects_requests_beyond_its_scratch(gblib):
     assert st == lib.GB_ERR_INVALID
     assert "exceeds the fixed scratch" in lib.last_error()
     assert np.all(np.isnan(out))        # nothing was launched
+
+
+def _cudart():
+    """The CUDA runtime as a shared library (the toolkit's, else none): the
+    default memory pool it reports is the device's own, shared with the
+    library's statically linked runtime."""
+    import ctypes
+    import ctypes.util
+    for name in (ctypes.util.find_library("cudart"), "/usr/local/cuda/lib64/libcudart.so",
+                 "libcudart.so.13", "libcudart.so"):
+        if not name:
+            continue
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    return None
+
+
+def test_noalloc_draws_nothing_from_the_device_memory_pool(gblib):
+    """The defining property: a call takes no memory from the device's
+    stream-ordered pool (which gb_pdma_batch's scratch comes from).  The
+    pool's high-water mark is reset before each call and read after it: the
+    allocating entry point raises it, the no-allocation one leaves it and
+    the pool's reserved memory untouched."""
+    import ctypes as C
+    import torch
+    rt = _cudart()
+    if rt is None:
+        pytest.skip("no shared CUDA runtime library to read the memory pool from")
+    dev = torch.cuda.current_device()
+    pool = C.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), dev) == 0
+    USED_HIGH, RESERVED_CUR = 0x8, 0x5
+
+    def attr(a):
+        v = C.c_uint64()
+        assert rt.cudaMemPoolGetAttribute(pool, a, C.byref(v)) == 0
+        return v.value
+
+    def reset_high():
+        z = C.c_uint64(0)
+        assert rt.cudaMemPoolSetAttribute(pool, USED_HIGH, C.byref(z)) == 0
+
+    from codesthesis_dir_gb300 import lib
+    rng = np.random.default_rng(99)
+    n, nl = 64, 512
+    arrs = _lines(rng, nl, n)
+    torch.cuda.synchronize()
+    reset_high()
+    st, _ = _solve(gblib.gb_pdma_batch, arrs, n, nl)
+    assert st == lib.GB_OK
+    assert attr(USED_HIGH) >= 5 * n * nl * 8          # the control: its scratch came from the pool
+    torch.cuda.synchronize()
+    reserved = attr(RESERVED_CUR)
+    reset_high()
+    st, _ = _solve(gblib.gb_pdma_batch_noalloc, arrs, n, nl)
+    assert st == lib.GB_OK
+    assert attr(USED_HIGH) == 0
+    assert attr(RESERVED_CUR) == reserved
