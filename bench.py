@@ -668,11 +668,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-budget", type=float, default=20.0)
     ap.add_argument("--inner", type=int, default=3, help="FP32 V-cycles per defect-correction step")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner: default tunables, --inner")
     ap.add_argument("--pair-outer", action="store_true",
                     help="headline the float-pair defect correction (GB_BATCH_MIXED) instead of the FP64 one")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-only", action="store_true",
                     help="time only the mixed solve (for profiler launch lists); prints no JSON line")
+    ap.add_argument("--fp64-only", action="store_true",
+                    help="time only the plain FP64 solve (for profiler captures); prints no JSON line")
     ap.add_argument("--no-layer", action="store_true", help="skip the 2D layer step measurement of the default run")
     ap.add_argument("--requests", type=int, default=96, help="serve workload: number of requests")
     ap.add_argument("--serve-steps", default="20,200", help="serve workload: step range lo,hi")
@@ -747,38 +750,66 @@ def main():
         return ms, cu, cyc, rr, launches
 
     prec_head = lib.BATCH_MIXED if args.pair_outer else lib.BATCH_MIXED_F64OUTER
-    mixed = BatchPoisson(sizes, precision=prec_head, rtol=RTOL, inner=args.inner)
+    # autotuned tunables of each arm (outside the timed region; V(2,2) kept)
+    tuning = {"mixed": None, "fp64": None}
+    if not args.no_tune:
+        from codesthesis_dir_gb300.batch import autotune
+        t0 = time.perf_counter()
+        best, table, hit = autotune(sizes, prec_head, d_f.data_ptr(), d_psi.data_ptr(), rtol=RTOL, reps=2)
+        tuning["mixed"] = dict(best, candidates=len(table), from_cache=hit,
+                               top5=sorted(table, key=lambda t: t["ms"])[:5])
+        best64, table64, hit64 = autotune(sizes, lib.BATCH_FP64, d_f.data_ptr(), d_psi64.data_ptr(), rtol=RTOL, reps=2)
+        tuning["fp64"] = dict(best64, candidates=len(table64), from_cache=hit64)
+        tuning["tuning_s"] = time.perf_counter() - t0
+    tm = {k: tuning["mixed"][k] for k in ("nu1", "nu2", "inner", "local_n", "fuse", "exec")} if tuning["mixed"] \
+        else dict(nu1=2, nu2=2, inner=args.inner, local_n=65, fuse=2, exec=lib.BATCH_EXEC_GRAPH)
+    t64 = {k: tuning["fp64"][k] for k in ("nu1", "nu2", "inner", "local_n", "fuse", "exec")} if tuning["fp64"] \
+        else dict(nu1=2, nu2=2, inner=1, local_n=65, fuse=1, exec=lib.BATCH_EXEC_GRAPH)
+    mixed = BatchPoisson(sizes, precision=prec_head, rtol=RTOL, tuning=tm)
+    if args.fp64_only:
+        fp64 = BatchPoisson(sizes, precision=lib.BATCH_FP64, rtol=RTOL, tuning=t64)
+        ms, cu, cyc, rr, launches = timed(fp64, d_psi64, args.steps, args.warmup)
+        if rank == 0:
+            print("fp64-only: %.3f ms/step, %.4g cell-updates/s, cycles %s, launches %d" % (
+                ms / max(1, args.steps), cu / (ms / 1e3) if ms > 0 else 0.0, np.bincount(cyc), launches))
+        return 0
     if args.mixed_only:
         ms, cu, cyc, rr, launches = timed(mixed, d_psi, args.steps, args.warmup)
         if rank == 0:
             print("mixed-only: %.3f ms/step, %.4g cell-updates/s, cycles %s, launches %d" % (
                 ms / max(1, args.steps), cu / (ms / 1e3) if ms > 0 else 0.0, np.bincount(cyc), launches))
         return 0
-    fp64 = BatchPoisson(sizes, precision=lib.BATCH_FP64, rtol=RTOL)
+    fp64 = BatchPoisson(sizes, precision=lib.BATCH_FP64, rtol=RTOL, tuning=t64)
 
     # plain FP64 arm
     ms64, cu64, cyc64, rr64, _ = timed(fp64, d_psi64, args.steps, args.warmup)
     # mixed arm (headline: FP64 defect correction), clocks sampled during
     # it, its level-0 operations timed with CUDA events on the solve stream
     L = lib.load()
-    L.gb_batch_profile(mixed._h, 1)
-    timed(mixed, d_psi, 0, args.warmup)
-    L.gb_batch_profile_read(mixed._h, None, None, None, 1)
+    # per-kernel CUDA events exist in the graph execution mode: a persistent
+    # winner is profiled by a graph-mode twin timed after it
+    prof = mixed if tm["exec"] == lib.BATCH_EXEC_GRAPH else \
+        BatchPoisson(sizes, precision=prec_head, rtol=RTOL, tuning=dict(tm, exec=lib.BATCH_EXEC_GRAPH))
+    L.gb_batch_profile(prof._h, 1)
+    timed(prof, d_psi, 0, args.warmup)
+    L.gb_batch_profile_read(prof._h, None, None, None, 1)
     with ClockSampler(local) as clk:
         ms, cu, cyc, rr, launches = timed(mixed, d_psi, args.steps, 0)
+        if prof is not mixed:
+            timed(prof, d_psi, args.steps, 0)
     import ctypes as C
     pms, pl, pb = C.c_double(), C.c_longlong(), C.c_double()
-    L.gb_batch_profile_read(mixed._h, C.byref(pms), C.byref(pl), C.byref(pb), 0)
+    L.gb_batch_profile_read(prof._h, C.byref(pms), C.byref(pl), C.byref(pb), 0)
     kinds = {}
     for kname, kid in (("down_finest", 1), ("up_finest", 2), ("outer", 4)):
         kms, kl, kb = C.c_double(), C.c_longlong(), C.c_double()
-        L.gb_batch_profile_read_kind(mixed._h, kid, C.byref(kms), C.byref(kl), C.byref(kb))
+        L.gb_batch_profile_read_kind(prof._h, kid, C.byref(kms), C.byref(kl), C.byref(kb))
         if kl.value:
             kinds[kname] = {"launches": kl.value, "avg_ms": kms.value / kl.value,
                             "alg_bytes_per_launch": kb.value / kl.value,
                             "achieved_GBs": kb.value / (kms.value / 1e3) / 1e9 if kms.value > 0 else None}
-    L.gb_batch_profile_read(mixed._h, None, None, None, 1)
-    L.gb_batch_profile(mixed._h, 0)
+    L.gb_batch_profile_read(prof._h, None, None, None, 1)
+    L.gb_batch_profile(prof._h, 0)
     r64, r32 = C.c_double(), C.c_double()
     L.gb_measure_issue_rates(C.byref(r64), C.byref(r32))
     outer_pass = None
@@ -803,7 +834,7 @@ def main():
     # pairs on the FP32 pipe) beside the headline, on the same inputs
     pair = None
     if prec_head != lib.BATCH_MIXED:
-        pr = BatchPoisson(sizes, precision=lib.BATCH_MIXED, rtol=RTOL, inner=args.inner)
+        pr = BatchPoisson(sizes, precision=lib.BATCH_MIXED, rtol=RTOL, tuning=tm)
         d_psi_q = torch.zeros_like(d_psi)
         ms_q, cu_q, cyc_q, rr_q, _ = timed(pr, d_psi_q, args.steps, args.warmup)
         pair = {"value": cu_q / (ms_q / 1e3), "ms_per_step": ms_q / args.steps, "cycles_mean": float(np.mean(cyc_q)),
@@ -816,8 +847,7 @@ def main():
         del d_psi_q
 
     # the same mixed solve as one persistent launch per solve
-    pers = BatchPoisson(sizes, precision=prec_head, rtol=RTOL, inner=args.inner,
-                        exec_mode=lib.BATCH_EXEC_PERSISTENT)
+    pers = BatchPoisson(sizes, precision=prec_head, rtol=RTOL, tuning=dict(tm, exec=lib.BATCH_EXEC_PERSISTENT))
     d_psi_p = torch.zeros_like(d_psi)
     ms_p, cu_p, _, _, _ = timed(pers, d_psi_p, max(3, args.steps // 4), 1)
     pers_same = bool(torch.equal(d_psi_p, d_psi))
@@ -913,10 +943,14 @@ def main():
         "mixed": {"precision": "GB_BATCH_MIXED_F64OUTER" if prec_head == lib.BATCH_MIXED_F64OUTER
                   else "GB_BATCH_MIXED",
                   "cycles_mean": float(np.mean(cyc)), "relres_max": float(np.max(rr)),
-                  "inner_cycles_per_fp64_step": args.inner,
+                  "inner_cycles_per_fp64_step": tm["inner"],
                   "field_rel_l2_vs_fp64": field_err, "speedup_vs_fp64": (cu / ms) / (cu64 / ms64),
                   "time_to_solution_speedup_vs_fp64": ms64 / ms},
         "mixed_pair_outer": pair,
+        "tuning": dict(tuning, used_mixed=tm, used_fp64=t64,
+                       search="gb_batch_autotune: inner 2..5 x local_n {33,65,129} x fuse {1,2} x graph/persistent "
+                              "(FP64: local_n {33,65} x fuse {1,2} x graph/persistent), V(2,2), time to solution "
+                              "by CUDA events"),
         "persistent_single_launch": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / max(3, args.steps // 4),
                                      "identical_to_graph_mode": pers_same},
         "e2e": {"value": e2e_cu / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": total * 8,

@@ -18,15 +18,42 @@ def offsets(sizes):
     return off, int(np.sum(sizes ** 2))
 
 
+def autotune(sizes, precision, d_f, d_psi, nu1=2, nu2=2, tune_nu=False, rtol=1e-10, max_cycles=100, reps=3,
+             cache_path=None):
+    """gb_batch_autotune: times the candidate configurations of this size
+    mix on the device with the right-hand side at device address d_f (d_psi:
+    device scratch of the same size) and returns (winner, table of every
+    candidate timed, from_cache), each a dict of gb_batch_tuning's fields."""
+    L = _L.load()
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    best = _L.BatchTuning()
+    table = (_L.BatchTuning * 512)()
+    nt, hit = C.c_int(), C.c_int()
+    _L.check(L.gb_batch_autotune(len(sizes), sizes.ctypes.data_as(C.POINTER(C.c_int)), precision, nu1, nu2,
+                                 1 if tune_nu else 0, rtol, max_cycles, d_f, d_psi, reps,
+                                 cache_path.encode() if cache_path else None, C.byref(best), table, 512,
+                                 C.byref(nt), C.byref(hit)), "gb_batch_autotune")
+    return best.as_dict(), [table[i].as_dict() for i in range(nt.value)], bool(hit.value)
+
+
 class BatchPoisson:
     def __init__(self, sizes, precision=_L.BATCH_FP64, nu1=2, nu2=2, rtol=1e-10, max_cycles=100, inner=1,
-                 exec_mode=None):
+                 exec_mode=None, tuning=None):
+        """tuning: a dict of gb_batch_tuning's fields (e.g. autotune()'s
+        winner); it replaces nu1, nu2, inner and exec_mode."""
         L = _L.load()
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
         self.offsets, self.total = offsets(self.sizes)
         h = C.c_void_p()
-        _L.check(L.gb_batch_create(len(self.sizes), self.sizes.ctypes.data_as(C.POINTER(C.c_int)), precision,
-                                   nu1, nu2, rtol, max_cycles, C.byref(h)), "gb_batch_create")
+        if tuning is not None:
+            t = _L.BatchTuning(**{k: tuning[k] for k in ("nu1", "nu2", "inner", "local_n", "fuse", "exec")})
+            _L.check(L.gb_batch_create_tuned(len(self.sizes), self.sizes.ctypes.data_as(C.POINTER(C.c_int)),
+                                             precision, rtol, max_cycles, C.byref(t), C.byref(h)),
+                     "gb_batch_create_tuned")
+            inner, exec_mode = 1, None
+        else:
+            _L.check(L.gb_batch_create(len(self.sizes), self.sizes.ctypes.data_as(C.POINTER(C.c_int)), precision,
+                                       nu1, nu2, rtol, max_cycles, C.byref(h)), "gb_batch_create")
         self._h = h
         self.nprob = len(self.sizes)
         if inner != 1:

@@ -30,7 +30,7 @@
 #include "gridsync.cuh"
 
 #define BP_MAXL 16
-#define LOCAL_N 65
+#define LOCAL_N 65        // default: levels with n <= 65 run in one block per problem
 #define BP_THREADS 256
 
 template <class T> __device__ __forceinline__ T fmaT(T a, T b, T c);
@@ -689,7 +689,10 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
 // the solve; the residual is formed in pair arithmetic (rounding error
 // about 2^-48 of the terms) and its high part is both the FP32 right-hand
 // side and, widened exactly, the term of the FP64 norm.
-template <class T, int OM>
+// FIRST: the first pass of a solve, where psi is zero, so r = f exactly
+// (fma(-ih2, 0, f) = f, the pair sum of f and zero keeps f's high part):
+// the pass reads f alone and skips the stencil, with the same bits.
+template <class T, int OM, bool FIRST>
 __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *const *f_p, int store_r,
                          unsigned char *smem)
 {
@@ -711,24 +714,26 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *c
     if constexpr (PAIR) zero = make_float2(0.f, 0.f);
     else zero = 0.0;
     // rows by warp, a row's loads issued before its shared stores
-    for (int r = warp; r < SY; r += TILE_THREADS / 32) {
-        const int gy = oy + r;
-        const bool rin = gy >= 0 && gy < n;
-        const V *pr = psi + (rin ? (size_t)gy * n : 0);
-        constexpr int NJ = (SX + 31) / 32;
-        V v[NJ];
+    if (!FIRST) {
+        for (int r = warp; r < SY; r += TILE_THREADS / 32) {
+            const int gy = oy + r;
+            const bool rin = gy >= 0 && gy < n;
+            const V *pr = psi + (rin ? (size_t)gy * n : 0);
+            constexpr int NJ = (SX + 31) / 32;
+            V v[NJ];
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-            const int c = lane + 32 * j, gx = ox + c;
-            v[j] = (c < SX && rin && gx >= 0 && gx < n) ? pr[gx] : zero;
-        }
+            for (int j = 0; j < NJ; ++j) {
+                const int c = lane + 32 * j, gx = ox + c;
+                v[j] = (c < SX && rin && gx >= 0 && gx < n) ? pr[gx] : zero;
+            }
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-            const int c = lane + 32 * j;
-            if (c < SX) sp[r * SX + c] = v[j];
+            for (int j = 0; j < NJ; ++j) {
+                const int c = lane + 32 * j;
+                if (c < SX) sp[r * SX + c] = v[j];
+            }
         }
+        __syncthreads();
     }
-    __syncthreads();
     float *f32 = store_r ? FP<float>(B, e.p, 0) : nullptr;
     // one accumulator per column group: the sum of squares is a dependent
     // FP64 chain, and TX / 32 independent chains let the points overlap
@@ -756,7 +761,15 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *c
             const int q = (gy - oy) * SX + gx - ox;
             const size_t g = (size_t)gy * n + gx;
             double rw;
-            if constexpr (PAIR) {
+            if constexpr (FIRST) {
+                if constexpr (PAIR) {
+                    rw = f2d(fr[h][a].x);
+                    if (store_r) f32[g] = fr[h][a].x;
+                } else {
+                    rw = fr[h][a];
+                    if (store_r) f32[g] = d2f_rn(rw);
+                }
+            } else if constexpr (PAIR) {
                 // ih2 = 4^m exactly (n = 2^m + 1): every scaling is exact
                 const float2 sum = df_add(df_add(sp[q - 1], sp[q + 1]), df_add(sp[q - SX], sp[q + SX]));
                 const float2 lap = df_add(sum, df_scale(sp[q], -4.0f));
@@ -891,6 +904,17 @@ __device__ __forceinline__ void run_prolong(const BatchDev &B, TileEntry e, cons
     else op_prolong<T, NU, CM_NONE>(B, e, op.l, op.src, op.dst, smem);
 }
 
+template <class T, bool FIRST>
+__device__ __forceinline__ void run_outer(const BatchDev &B, TileEntry e, int item, const double *const *f_p,
+                                          const Op &op, unsigned char *smem)
+{
+    const void *const *fp = (const void *const *)f_p;
+    if constexpr (sizeof(T) == 8) op_outer<T, CM_NONE, FIRST>(B, e, item, fp, op.aux, smem);
+    else if (op.corr == CM_PAIR) op_outer<T, CM_PAIR, FIRST>(B, e, item, fp, op.aux, smem);
+    else if (op.corr == CM_F64) op_outer<T, CM_F64, FIRST>(B, e, item, fp, op.aux, smem);
+    else op_outer<T, CM_NONE, FIRST>(B, e, item, fp, op.aux, smem);
+}
+
 template <class T>
 __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *tiles, const double *const *f_p,
                                          const Op &op, int item, int nu1, int nu2, unsigned char *smem)
@@ -923,10 +947,8 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
         op_local<T>(B, item, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, (op.aux >> 2) & 1, smem);
         return;
     case OP_OUTER:
-        if constexpr (sizeof(T) == 8) op_outer<T, CM_NONE>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
-        else if (op.corr == CM_PAIR) op_outer<T, CM_PAIR>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
-        else if (op.corr == CM_F64) op_outer<T, CM_F64>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
-        else op_outer<T, CM_NONE>(B, tiles[op.off + item], item, (const void *const *)f_p, op.aux, smem);
+        if (op.nu) run_outer<T, true>(B, tiles[op.off + item], item, f_p, op, smem);
+        else run_outer<T, false>(B, tiles[op.off + item], item, f_p, op, smem);
         return;
     case OP_COPYBACK: {
         const TileEntry e = tiles[op.off + item];
@@ -1010,6 +1032,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) k_persistent(BatchDev B, cons
 struct gb_batch {
     int nprob = 0, precision = 0, nu1 = 2, nu2 = 2, max_cycles = 100;
     int inner = 1;                      // V-cycles per outer iteration (mixed)
+    int local_n = LOCAL_N;              // levels with n <= local_n run in one block per problem
+    int fuse = 1;                       // red-black sweeps fused into one tile operation (1 or 2)
     int exec = GB_BATCH_EXEC_GRAPH;
     double rtol = 1e-10;
     std::vector<int> n, L, dloc;
@@ -1047,6 +1071,7 @@ struct gb_batch {
     // operation lists (first iteration, later iterations) and their device copies
     std::vector<Op> ops0, ops;
     Op *d_ops = nullptr;
+    size_t nops_max = 0;
     int plan_inner = -1;
     // persistent launch
     unsigned *d_sync = nullptr;         // count, gen, err
@@ -1108,14 +1133,21 @@ template <class T> static size_t smem_of(const gb_batch *b, const Op &op)
     }
 }
 
-// Sweeps fused into one smoothing operation: two in FP32; one in FP64,
-// whose pipe is the bottleneck and would pay for the wider halo's
-// redundant updates.
-template <class T> static int sweeps_per_op(int nu) { return (sizeof(T) == 4 && nu >= 2) ? 2 : 1; }
-template <class T> static int ops_for(int nu)
+// Sweeps fused into one smoothing operation (b->fuse, at most 2): by
+// default two in FP32; one in FP64, whose pipe is the bottleneck and would
+// pay for the wider halo's redundant updates.
+static int sweeps_per_op(const gb_batch *b, int nu) { return std::max(1, std::min(nu, b->fuse)); }
+static int ops_for(const gb_batch *b, int nu)
 {
     int k = 0;
-    while (nu > 0) { nu -= sweeps_per_op<T>(nu); ++k; }
+    while (nu > 0) { nu -= sweeps_per_op(b, nu); ++k; }
+    return k;
+}
+// Sweeps of the last pre-smoothing operation (the one that also restricts).
+static int sweeps_of_last_pre(const gb_batch *b)
+{
+    int nu = b->nu1, k = 1;
+    while (nu > 0) { k = sweeps_per_op(b, nu); nu -= k; }
     return k;
 }
 
@@ -1132,9 +1164,9 @@ static void plan_vcycle(gb_batch *b, std::vector<Op> &v, bool zero0, bool corr0,
     const bool mixed = inner32(b);
     const int cm = corr_mode(b);
     int cur[BP_MAXL] = {0};
-    const int k1 = ops_for<T>(b->nu1);
-    const int pro = std::min(b->nu2, sizeof(T) == 4 ? 2 : 1);  // sweeps fused into the prolongation
-    const int k2 = ops_for<T>(b->nu2 - pro);
+    const int k1 = ops_for(b, b->nu1);
+    const int pro = std::min(b->nu2, b->fuse);  // sweeps fused into the prolongation
+    const int k2 = ops_for(b, b->nu2 - pro);
     for (int l = 0; l < b->maxdepth_global; ++l) {
         if (b->ft_cnt[l] == 0) continue;
         const bool zero = l > 0 || (mixed && zero0);
@@ -1145,7 +1177,7 @@ static void plan_vcycle(gb_batch *b, std::vector<Op> &v, bool zero0, bool corr0,
         else { src = 0; dst = 1; }                         // level 0 of the plain solve: psi
         int nu = b->nu1;
         for (int i = 0; i < k1; ++i) {
-            const int k = sweeps_per_op<T>(nu);
+            const int k = sweeps_per_op(b, nu);
             Op o{};
             o.kind = (i == k1 - 1) ? OP_SMOOTH_R : OP_SMOOTH;
             o.l = l; o.nu = k; o.zero = (zero && i == 0) ? 1 : 0; o.src = src; o.dst = dst; o.corr = 0;
@@ -1177,7 +1209,7 @@ static void plan_vcycle(gb_batch *b, std::vector<Op> &v, bool zero0, bool corr0,
         dst = 1 - dst;
         int nu = b->nu2 - pro;
         for (int i = 0; i < k2; ++i) {
-            const int k = sweeps_per_op<T>(nu);
+            const int k = sweeps_per_op(b, nu);
             Op q{};
             q.kind = OP_SMOOTH; q.l = l; q.nu = k; q.zero = 0; q.src = src; q.dst = dst;
             q.corr = (i == k2 - 1) ? correct_last : CM_NONE;
@@ -1208,6 +1240,7 @@ static void plan_iteration(gb_batch *b, std::vector<Op> &v, int first)
     const bool mixed = inner32(b);
     Op o{};
     o.kind = OP_OUTER; o.off = b->ot_off; o.cnt = b->ot_cnt; o.aux = mixed ? 1 : 0; o.corr = corr_mode(b);
+    o.nu = first ? 1 : 0;   // the first pass of a solve: psi = 0
     v.push_back(o);
     Op f{};
     f.kind = OP_FINALIZE; f.cnt = b->nprob; f.aux = first;
@@ -1301,7 +1334,8 @@ static void launch_op(gb_batch *b, const Op &op, cudaStream_t s)
         k_local<T><<<g, LOCAL_THREADS, sm, s>>>(b->dev, op, b->nu1, b->nu2);
         break;
     case OP_OUTER:
-        launch_k<T, OP_OUTER, 0>(b, op.corr, g, sm, s, op);
+        if (op.nu) launch_k<T, OP_OUTER, 1>(b, op.corr, g, sm, s, op);
+        else launch_k<T, OP_OUTER, 0>(b, op.corr, g, sm, s, op);
         break;
     case OP_FINALIZE:
         launch_k<T, OP_FINALIZE, 0>(b, CM_NONE, gb_ceil_div(b->nprob, TILE_THREADS / 32), 0, s, op);
@@ -1313,13 +1347,23 @@ static void launch_op(gb_batch *b, const Op &op, cudaStream_t s)
     b->launches += 1;
 }
 
-extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
-                               int max_cycles, gb_batch **out)
+// Creates a handle with every tunable given (gb_batch_create passes the
+// defaults, gb_batch_create_tuned an autotuner's choice).
+static int batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol, int max_cycles,
+                        int local_n, int fuse, int inner, int exec, gb_batch **out)
 {
     if (!out || !n || nprob <= 0 ||
         (precision != GB_BATCH_FP64 && precision != GB_BATCH_MIXED && precision != GB_BATCH_MIXED_F64OUTER) || nu1 < 1 ||
         nu1 > 8 || nu2 < 0 || nu2 > 8 || max_cycles < 0 || !(rtol >= 0.0)) {
         gb_set_error("gb_batch_create: invalid argument (need nprob > 0, 1 <= nu1 <= 8, 0 <= nu2 <= 8)");
+        return GB_ERR_INVALID;
+    }
+    const int local_max = precision == GB_BATCH_FP64 ? 65 : 129;
+    if ((local_n != 33 && local_n != 65 && local_n != 129) || local_n > local_max || fuse < 1 || fuse > 2 ||
+        inner < 1 || inner > 16 || (precision == GB_BATCH_FP64 && inner != 1) ||
+        (exec != GB_BATCH_EXEC_GRAPH && exec != GB_BATCH_EXEC_PERSISTENT)) {
+        gb_set_error("gb_batch_create: invalid tuning (local_n 33, 65 or 129 (65 at most in FP64), fuse 1..2, "
+                     "inner 1..16 (1 in FP64), exec GRAPH or PERSISTENT)");
         return GB_ERR_INVALID;
     }
     *out = nullptr;
@@ -1328,6 +1372,9 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     b->precision = precision;
     b->nu1 = nu1;
     b->nu2 = nu2;
+    b->local_n = local_n;
+    b->fuse = fuse;
+    b->inner = inner;
     b->rtol = rtol;
     b->max_cycles = max_cycles;
     b->n.assign(n, n + nprob);
@@ -1350,7 +1397,7 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
         const int L = levels_of(np_, nl);
         b->L[p] = L;
         int d = 0;
-        while (nl[d] > LOCAL_N) ++d;
+        while (nl[d] > b->local_n) ++d;
         b->dloc[p] = d;
         maxd = std::max(maxd, d);
         for (int l = 0; l < L; ++l) {
@@ -1507,12 +1554,12 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     D.p_nblk0 = d_pnb0;
     D.num_active = d_numact;
     D.max_cycles = max_cycles;
-    D.inner = 1;
+    D.inner = b->inner;
     D.rtol = rtol;
     // persistent launch: shared memory of the largest operation, grid of
     // every block that can be resident at once
     build_plans(b);
-    size_t ps = 0;
+    size_t ps = b->local_smem;
     for (const Op &o : b->ops)
         ps = std::max(ps, precision == GB_BATCH_FP64 ? smem_of<double>(b, o) : smem_of<float>(b, o));
     b->psmem = ps;
@@ -1526,11 +1573,37 @@ extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, 
     else BTRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persistent<float>, TILE_THREADS, b->psmem));
     b->pgrid = nsm * per;
     if (!coop) b->pgrid = 0;
-    const size_t nops_max = 4 * (b->ops.size() + 8);
+    // room for the operation lists of any inner count (set_inner_cycles)
+    const size_t nops_max = 4 * (b->ops.size() + 8) * 16;
     BTRY(cudaMalloc(&b->d_ops, sizeof(Op) * nops_max));
+    b->nops_max = nops_max;
 #undef BTRY
+    if (exec == GB_BATCH_EXEC_PERSISTENT && b->pgrid <= 0) {
+        gb_set_error("gb_batch_create: cooperative launch unavailable on this device");
+        gb_batch_destroy(b);
+        return GB_ERR_INVALID;
+    }
+    b->exec = exec;
     *out = b;
     return GB_OK;
+}
+
+extern "C" int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
+                               int max_cycles, gb_batch **out)
+{
+    return batch_create(nprob, n, precision, nu1, nu2, rtol, max_cycles, LOCAL_N,
+                        precision == GB_BATCH_FP64 ? 1 : 2, 1, GB_BATCH_EXEC_GRAPH, out);
+}
+
+extern "C" int gb_batch_create_tuned(int nprob, const int *n, int precision, double rtol, int max_cycles,
+                                     const gb_batch_tuning *t, gb_batch **out)
+{
+    if (!t) {
+        gb_set_error("gb_batch_create_tuned: null tuning");
+        return GB_ERR_INVALID;
+    }
+    return batch_create(nprob, n, precision, t->nu1, t->nu2, rtol, max_cycles, t->local_n, t->fuse, t->inner,
+                        t->exec, out);
 }
 
 extern "C" int gb_batch_destroy(gb_batch *b)
@@ -1581,7 +1654,7 @@ extern "C" int gb_batch_set_inner_cycles(gb_batch *b, int inner)
     b->inner = inner;
     b->dev.inner = inner;
     build_plans(b);
-    if (4 * (b->ops.size() + 8) < b->ops0.size() + b->ops.size()) {
+    if (b->nops_max < b->ops0.size() + b->ops.size()) {
         gb_set_error("gb_batch_set_inner_cycles: operation list too long");
         return GB_ERR_INVALID;
     }
@@ -1636,7 +1709,7 @@ static void enqueue_iteration(gb_batch *b, const std::vector<Op> &v, cudaStream_
         else launch_op<double>(b, op, s);
         if (ev) {
             prof_record(b->ev[b->ev_used + 1], s);
-            b->ev_kind[b->ev_used / 2] = op.kind;
+            b->ev_kind[b->ev_used / 2] = op.kind | (op.kind == OP_OUTER && op.nu ? 0x100 : 0);
             b->ev_used += 2;
         }
     }
@@ -1662,7 +1735,8 @@ static double outer_bytes(const gb_batch *b) { return b->precision == GB_BATCH_F
 //   OP_PROLONG   prolongation 2.25 + sweeps x 3 (+ 16 B of psi when it
 //                applies the correction);
 //   OP_SMOOTH    sweeps x 3;
-//   OP_OUTER     FP64 psi and f read (16 B) + FP32 residual written (4 B).
+//   OP_OUTER     FP64 psi and f read (16 B) + FP32 residual written (4 B);
+//                the first pass of a solve reads f alone (12 B).
 static void batch_profile_collect(gb_batch *b, cudaStream_t s)
 {
     if (!b->profile || b->ev_used == 0) return;
@@ -1676,21 +1750,22 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
     }
     const double esz = b->precision == GB_BATCH_FP64 ? 8.0 : 4.0;
     const bool mixed = inner32(b);
-    const int pre = (mixed && b->nu1 >= 2) ? 2 : 1;
-    const int post = std::min(b->nu2, mixed ? 2 : 1);
+    const int pre = sweeps_of_last_pre(b);
+    const int post = std::min(b->nu2, b->fuse);
     for (int i = 0; i + 1 < b->ev_used; i += 2) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]) != cudaSuccess) {
             cudaGetLastError();  // timing is advisory: never let it fail a solve
             continue;
         }
-        const int k = b->ev_kind[i / 2];
+        const int k = b->ev_kind[i / 2] & 0xff;
+        const bool first_outer = (b->ev_kind[i / 2] & 0x100) != 0;
         double bytes = 0.0;
         switch (k) {
         case OP_SMOOTH_R: bytes = (3.0 * pre + 3.0 + 1.25) * esz * pts_tile; break;
         case OP_PROLONG: bytes = ((2.25 + 3.0 * post) * esz + (mixed ? 16.0 : 0.0)) * pts_tile; break;
         case OP_SMOOTH: bytes = 3.0 * esz * pts_tile; break;
-        case OP_OUTER: bytes = 20.0 * pts_all; break;
+        case OP_OUTER: bytes = (first_outer ? 12.0 : 20.0) * pts_all; break;   // the first reads f alone
         default: break;
         }
         b->kind_ms[k] += ms;

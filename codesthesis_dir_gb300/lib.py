@@ -56,6 +56,16 @@ AXI_FIELDS = ["phi", "omegn", "omeg", "omegp", "veln", "vel", "velp", "thetan", 
 AXI_FIELD_ID = {n: i for i, n in enumerate(AXI_FIELDS)}
 
 
+class BatchTuning(C.Structure):
+    """gb_batch_tuning: the tunables of a batched solve and, from the
+    autotuner, the measured milliseconds per solve."""
+    _fields_ = [("nu1", C.c_int), ("nu2", C.c_int), ("inner", C.c_int), ("local_n", C.c_int), ("fuse", C.c_int),
+                ("exec", C.c_int), ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class AxiParams(C.Structure):
     _fields_ = [("nr", C.c_int), ("nz", C.c_int),
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("zmax", C.c_double),
@@ -198,6 +208,11 @@ SIGNATURES = [
     ("gb_pdma_batch_noalloc", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong,
                                        C.c_longlong, _vp]),
     ("gb_batch_create", C.c_int, [C.c_int, _ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(_vp)]),
+    ("gb_batch_create_tuned", C.c_int, [C.c_int, _ip, C.c_int, C.c_double, C.c_int, C.POINTER(BatchTuning),
+                                        C.POINTER(_vp)]),
+    ("gb_batch_autotune", C.c_int, [C.c_int, _ip, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp,
+                                    C.c_int, C.c_char_p, C.POINTER(BatchTuning), C.POINTER(BatchTuning), C.c_int,
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("gb_batch_destroy", C.c_int, [_vp]),
     ("gb_batch_total_points", C.c_longlong, [_vp]),
     ("gb_batch_set_inner_cycles", C.c_int, [_vp, C.c_int]),

@@ -565,6 +565,47 @@ typedef struct gb_batch gb_batch;
 
 int gb_batch_create(int nprob, const int *n, int precision, int nu1, int nu2, double rtol,
                     int max_cycles, gb_batch **out);
+
+/* The tunables of a batched solve.  gb_batch_create uses local_n 65, fuse 2
+ * (1 for GB_BATCH_FP64), inner 1 and the graph execution mode.  local_n,
+ * fuse and exec change only the speed (every combination gives the same
+ * bits); nu1, nu2 and inner change the iteration itself. */
+typedef struct {
+    int nu1, nu2;     /* red-black sweeps before / after the coarse correction */
+    int inner;        /* FP32 V-cycles per defect-correction step (1 for GB_BATCH_FP64) */
+    int local_n;      /* levels with n <= local_n are solved by one block per problem in
+                         shared memory: 33, 65 or 129 (at most 65 for GB_BATCH_FP64) */
+    int fuse;         /* red-black sweeps fused into one tile pass: 1 or 2 (halo 2*fuse,
+                         two more where the pass also restricts) */
+    int exec;         /* GB_BATCH_EXEC_GRAPH or GB_BATCH_EXEC_PERSISTENT */
+    double ms;        /* autotuner output: measured milliseconds per solve */
+} gb_batch_tuning;
+
+/* Creates a handle with the given tunables (t->ms is ignored). */
+int gb_batch_create_tuned(int nprob, const int *n, int precision, double rtol, int max_cycles,
+                          const gb_batch_tuning *t, gb_batch **out);
+
+/* Autotuner (no counterpart in the reference, whose multigrid has no
+ * tunables beyond PARAMETERs).  Times every candidate configuration of a
+ * size mix on the current device with CUDA events on a stream of its own:
+ * one untimed solve, then `reps` timed solves of d_f (device, packed, the
+ * caller's right-hand side: convergence depends on it) into d_psi (device
+ * scratch of the same size), and keeps the fastest time to solution.
+ * Candidates: inner 2..5 (mixed; 1 for GB_BATCH_FP64) x local_n 33, 65, 129
+ * x fuse 1, 2 x graph / persistent execution, at the given nu1, nu2; with
+ * tune_nu != 0 also nu in (1,1), (1,2), (2,1), (2,2), (3,3).  A candidate
+ * whose solve does not return GB_OK is skipped.  The winner goes to *best;
+ * table (table_cap entries, may be NULL) receives every candidate timed and
+ * *table_len (may be NULL) their number.  cache_path (may be NULL: then the
+ * environment variable GB300_BATCH_TUNE_CACHE, else no file) names a text
+ * file of earlier winners keyed by device name, SM count, precision, nu,
+ * rtol, max_cycles and the multiset of sizes; a hit returns the cached
+ * winner without timing (*from_cache = 1, may be NULL) and a miss appends
+ * the new winner.  Also answers repeated calls within a process from memory. */
+int gb_batch_autotune(int nprob, const int *n, int precision, int nu1, int nu2, int tune_nu, double rtol,
+                      int max_cycles, const double *d_f, double *d_psi, int reps, const char *cache_path,
+                      gb_batch_tuning *best, gb_batch_tuning *table, int table_cap, int *table_len,
+                      int *from_cache);
 int gb_batch_destroy(gb_batch *b);
 /* Mixed solves only: V-cycles per outer (defect-correction) iteration,
  * 1..16 (default 1).  With k > 1 the outer residual, its norm and the
