@@ -689,9 +689,12 @@ __device__ void op_local(const BatchDev &B, int p, int nu1, int nu2, int zero_le
 // the solve; the residual is formed in pair arithmetic (rounding error
 // about 2^-48 of the terms) and its high part is both the FP32 right-hand
 // side and, widened exactly, the term of the FP64 norm.
-// FIRST: the first pass of a solve, where psi is zero, so r = f exactly
-// (fma(-ih2, 0, f) = f, the pair sum of f and zero keeps f's high part):
-// the pass reads f alone and skips the stencil, with the same bits.
+// FIRST: the first pass of a solve, where psi is zero: the pass reads f
+// alone and skips the stencil, with the same bits.  In FP64 the stencil of
+// zeros gives lap = +0 and r = fma(-ih2, +0, f) = f exactly.  In pairs it
+// gives lap = (+0, +0) and r = f + (-0, -0), which is not always f itself
+// (when the low half is exactly half an ulp of the high half the pair sum
+// may round the tie the other way), so that sum is still formed.
 template <class T, int OM, bool FIRST>
 __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *const *f_p, int store_r,
                          unsigned char *smem)
@@ -763,8 +766,9 @@ __device__ void op_outer(const BatchDev &B, TileEntry e, int item, const void *c
             double rw;
             if constexpr (FIRST) {
                 if constexpr (PAIR) {
-                    rw = f2d(fr[h][a].x);
-                    if (store_r) f32[g] = fr[h][a].x;
+                    const float2 r = df_add(fr[h][a], make_float2(-0.0f, -0.0f));
+                    rw = f2d(r.x);
+                    if (store_r) f32[g] = r.x;
                 } else {
                     rw = fr[h][a];
                     if (store_r) f32[g] = d2f_rn(rw);

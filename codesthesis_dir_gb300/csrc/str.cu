@@ -32,15 +32,20 @@ struct StrLevel {
     double *r, *cr, *crr, *czz;
     double *v, *f;            // packed (n1+1)*(n2+1)
     double *fac_r, *fac_z;    // per r-line j (5(n1-1)+1 each), per z-line i (5(n2-1)+1 each)
+    // mixed precision: FP32 copies (pivots of the factors as reciprocals)
+    float *r32, *cr32, *crr32, *czz32, *v32, *f32, *fac_r32, *fac_z32;
 };
 
 struct StrDev {
     int nlev, ld, nrel, maxsweeps, mode;
     double tolcon;
     double *psif, *rc;        // ld x ld, ld = max(n1, n2) + 1
+    float *psif32, *rc32;     // the same for the FP32 correction cycles
     double *io_psi, *io_rhs;  // level-1 (n1+1) x (n2+1) staging of the caller's arrays
     StrLevel lev[STR_MAXLEV];
     int *status;              // [0] status, [1] sweeps
+    int *abort;               // optional (a time loop's flag): the solve is skipped while it is set and
+                              // sets it to 1 when the residual is a NaN
 };
 
 #define PS(i, j) d.psif[(size_t)(i) + (size_t)d.ld * (size_t)(j)]
@@ -312,6 +317,7 @@ __device__ void str_finer(const StrDev &d, int klev)
 __global__ void __launch_bounds__(STR_THREADS) k_str_solve(const __grid_constant__ StrDev d)
 {
     __shared__ double s_red[33];
+    if (d.abort && *d.abort) return;   // uniform over the block
     const int nlev = d.nlev;
     const StrLevel &L1 = d.lev[1];
     const int n1 = L1.n1, n2 = L1.n2;
@@ -358,9 +364,318 @@ __global__ void __launch_bounds__(STR_THREADS) k_str_solve(const __grid_constant
     if (threadIdx.x == 0) {
         d.status[0] = status;
         d.status[1] = sweeps;
+        if (status == GB_NAN && d.abort) *d.abort = 1;
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision (FP32 V-cycles inside FP64 defect correction): each outer
+// iteration forms the FP64 residual r = f - L psi of the level-1 iterate
+// (relax's own residual expression), stops when max |r| < tolcon, else runs
+// one FP32 V-cycle of the same schedule on L e = r from e = 0 and updates
+// psi += e in FP64 (rcsc.f's solve has no over-relaxation).  The FP32 line
+// eliminations multiply by stored reciprocal pivots.
+// ---------------------------------------------------------------------------
+#define STR32_SMEM_BYTES 0
+#define PS32(i, j) d.psif32[(size_t)(i) + (size_t)d.ld * (size_t)(j)]
+#define CR32(i, k) L.cr32[3 * ((i) - 1) + (k) - 1]
+#define CRR32(i, k) L.crr32[4 * ((i) - 1) + (k) - 1]
+#define CZZ32(j, k) L.czz32[4 * ((j) - 1) + (k) - 1]
+
+template <class Rhs>
+__device__ inline void apply_pdma_rhs32(const float *fac, int n, float *x, int stride, Rhs rhs)
+{
+    const float *icdiv = fac, *bk1 = fac + n, *aa = fac + 2 * n, *dn = fac + 3 * n, *en = fac + 4 * n;
+    const float icN = fac[5 * n];
+    float rk = rhs(0);
+    float rk1 = rhs(1);
+    for (int k = 0; k <= n - 2; ++k) {
+        rk = rk * icdiv[k];
+        x[(size_t)k * stride] = rk;
+        rk1 = rk1 - bk1[k] * rk;
+        float rk2 = 0.f;
+        if (k != n - 2) rk2 = rhs(k + 2) - aa[k + 2] * rk;
+        rk = rk1;
+        rk1 = rk2;
+    }
+    float x1 = rk * icN;
+    x[(size_t)(n - 1) * stride] = x1;
+    float x0 = x[(size_t)(n - 2) * stride] - dn[n - 2] * x1;
+    x[(size_t)(n - 2) * stride] = x0;
+    for (int j = n - 3; j >= 0; --j) {
+        const float xj = x[(size_t)j * stride] - dn[j] * x0 - en[j] * x1;
+        x[(size_t)j * stride] = xj;
+        x1 = x0;
+        x0 = xj;
+    }
+}
+
+__device__ __forceinline__ void str_rline32(const StrDev &d, const StrLevel &L, int j)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const float *f = L.f32;
+    auto rhs = [&](int q) -> float {
+        const int i = q + 1;
+        if (j <= n2 / 2)
+            return -(CZZ32(j, 1) * PS32(i, j - 1) + CZZ32(j, 3) * PS32(i, j + 1) + CZZ32(j, 4) * PS32(i, j + 2)) +
+                   f[(size_t)i + (size_t)(n1 + 1) * j];
+        return -(CZZ32(j, 1) * PS32(i, j - 2) + CZZ32(j, 2) * PS32(i, j - 1) + CZZ32(j, 4) * PS32(i, j + 1)) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    };
+    const int n = n1 - 1;
+    apply_pdma_rhs32(L.fac_r32 + (size_t)(j - 1) * (5 * n + 1), n, &PS32(1, j), 1, rhs);
+}
+
+__device__ __forceinline__ void str_zline32(const StrDev &d, const StrLevel &L, int i)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const float *f = L.f32;
+    const float ir = 1.0f / L.r32[i];
+    auto rhs = [&](int q) -> float {
+        const int j = q + 1;
+        if (i <= n1 / 2)
+            return -(CRR32(i, 1) * PS32(i - 1, j) + CRR32(i, 3) * PS32(i + 1, j) + CRR32(i, 4) * PS32(i + 2, j) +
+                     (CR32(i, 1) * PS32(i - 1, j) + CR32(i, 3) * PS32(i + 1, j)) * ir) +
+                   f[(size_t)i + (size_t)(n1 + 1) * j];
+        return -(CRR32(i, 1) * PS32(i - 2, j) + CRR32(i, 2) * PS32(i - 1, j) + CRR32(i, 4) * PS32(i + 1, j) +
+                 (CR32(i, 1) * PS32(i - 1, j) + CR32(i, 3) * PS32(i + 1, j)) * ir) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    };
+    const int n = n2 - 1;
+    apply_pdma_rhs32(L.fac_z32 + (size_t)(i - 1) * (5 * n + 1), n, &PS32(i, 1), d.ld, rhs);
+}
+
+// nrel sweeps of both line directions on level klev, then the residual of
+// the correction into rc32 (for the restriction that follows).
+__device__ void str_relax32(const StrDev &d, int klev)
+{
+    const StrLevel &L = d.lev[klev];
+    const int n1 = L.n1, n2 = L.n2;
+    const int tp = (n1 + 1) * (n2 + 1);
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        PS32(i, j) = L.v32[idx];
+    }
+    __syncthreads();
+    for (int irel = 0; irel < d.nrel; ++irel) {
+        if (d.mode == GB_SMOOTHER_LEX) {
+            if (threadIdx.x == 0) {
+                for (int j = 1; j <= n2 - 1; ++j) str_rline32(d, L, j);
+                for (int i = 1; i <= n1 - 1; ++i) str_zline32(d, L, i);
+            }
+            __syncthreads();
+        } else {
+            for (int c = 1; c <= 4; ++c) {
+                const int first = (c & 3) == 0 ? 4 : (c & 3);
+                for (int j = first + 4 * threadIdx.x; j <= n2 - 1; j += 4 * blockDim.x) str_rline32(d, L, j);
+                __syncthreads();
+            }
+            for (int c = 1; c <= 4; ++c) {
+                const int first = (c & 3) == 0 ? 4 : (c & 3);
+                for (int i = first + 4 * threadIdx.x; i <= n1 - 1; i += 4 * blockDim.x) str_zline32(d, L, i);
+                __syncthreads();
+            }
+        }
+    }
+    const int ni = n1 - 1, tot = ni * (n2 - 1);
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / ni + 1, i = idx - (j - 1) * ni + 1;
+        const float ir = 1.0f / L.r32[i];
+        float temp;
+        if (i <= n1 / 2)
+            temp = CRR32(i, 1) * PS32(i - 1, j) + CRR32(i, 2) * PS32(i, j) + CRR32(i, 3) * PS32(i + 1, j) +
+                   CRR32(i, 4) * PS32(i + 2, j) +
+                   (CR32(i, 1) * PS32(i - 1, j) + CR32(i, 2) * PS32(i, j) + CR32(i, 3) * PS32(i + 1, j)) * ir -
+                   PS32(i, j) * (ir * ir);
+        else
+            temp = CRR32(i, 1) * PS32(i - 2, j) + CRR32(i, 2) * PS32(i - 1, j) + CRR32(i, 3) * PS32(i, j) +
+                   CRR32(i, 4) * PS32(i + 1, j) +
+                   (CR32(i, 1) * PS32(i - 1, j) + CR32(i, 2) * PS32(i, j) + CR32(i, 3) * PS32(i + 1, j)) * ir -
+                   PS32(i, j) * (ir * ir);
+        if (j <= n2 / 2)
+            temp = temp + CZZ32(j, 1) * PS32(i, j - 1) + CZZ32(j, 2) * PS32(i, j) + CZZ32(j, 3) * PS32(i, j + 1) +
+                   CZZ32(j, 4) * PS32(i, j + 2);
+        else
+            temp = temp + CZZ32(j, 1) * PS32(i, j - 2) + CZZ32(j, 2) * PS32(i, j - 1) + CZZ32(j, 3) * PS32(i, j) +
+                   CZZ32(j, 4) * PS32(i, j + 1);
+        d.rc32[(size_t)i + (size_t)d.ld * j] = L.f32[(size_t)i + (size_t)(n1 + 1) * j] - temp;
+    }
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        L.v32[idx] = PS32(i, j);
+    }
+    __syncthreads();
+}
+
+// corser (rcsc.f:1343-1390) in FP32, with its clearing of rows and columns 0
+// and n1c in both directions
+__device__ void str_corser32(const StrDev &d, int klev)
+{
+    const int ld = d.ld;
+    const int n1c = d.lev[klev + 1].n1, n2c = d.lev[klev + 1].n2;
+    const float *rf = d.rc32;
+    float *fc = d.lev[klev + 1].f32, *vc = d.lev[klev + 1].v32;
+    const int tot = (n1c + 1) * (n2c + 1);
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1c + 1), i = idx - j * (n1c + 1);
+        float temp = 0.f;
+        if (i >= 1 && i <= n1c - 1 && j >= 1 && j <= n2c - 1 && j != n1c) {
+            const int ii = i + i, jj = j + j;
+            temp = rf[(size_t)ii + (size_t)ld * jj];
+            temp = temp * 2.f + rf[(size_t)(ii + 1) + (size_t)ld * jj] + rf[(size_t)(ii - 1) + (size_t)ld * jj];
+            temp = temp + rf[(size_t)ii + (size_t)ld * (jj + 1)] + rf[(size_t)ii + (size_t)ld * (jj - 1)];
+            temp = temp * 2.f + rf[(size_t)(ii + 1) + (size_t)ld * (jj + 1)] + rf[(size_t)(ii - 1) + (size_t)ld * (jj - 1)];
+            temp = temp + rf[(size_t)(ii + 1) + (size_t)ld * (jj - 1)] + rf[(size_t)(ii - 1) + (size_t)ld * (jj + 1)];
+            temp = temp * 0.0625f;
+        }
+        fc[idx] = temp;
+        vc[idx] = 0.f;
+    }
+    __syncthreads();
+}
+
+// finer (rcsc.f:1392-1444) in FP32
+__device__ void str_finer32(const StrDev &d, int klev)
+{
+    const int n1c = d.lev[klev].n1;
+    const int n1f = d.lev[klev - 1].n1, n2f = d.lev[klev - 1].n2;
+    const float *vc = d.lev[klev].v32;
+    float *vf = d.lev[klev - 1].v32;
+    const int tot = (n1f + 1) * (n2f + 1);
+#define PC32(ii, jj) vc[(size_t)(jj) * (n1c + 1) + (ii)]
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1f + 1), i = idx - j * (n1f + 1);
+        const int i1 = i / 2, j1 = j / 2;
+        float p;
+        if (i1 * 2 == i) p = (j1 * 2 == j) ? PC32(i1, j1) : (PC32(i1, j1) + PC32(i1, j1 + 1)) * 0.5f;
+        else if (j1 * 2 == j) p = (PC32(i1, j1) + PC32(i1 + 1, j1)) * 0.5f;
+        else p = (PC32(i1, j1) + PC32(i1 + 1, j1 + 1) + PC32(i1, j1 + 1) + PC32(i1 + 1, j1)) * 0.25f;
+        PS32(i, j) = p + vf[idx];
+    }
+#undef PC32
+    __syncthreads();
+    const int tc = (n1c + 1) * (d.lev[klev].n2 + 1);
+    for (int idx = threadIdx.x; idx < tc; idx += blockDim.x) d.lev[klev].v32[idx] = 0.f;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int j = idx / (n1f + 1), i = idx - j * (n1f + 1);
+        vf[idx] = PS32(i, j);
+    }
+    __syncthreads();
+}
+
+// FP64 residual of level 1 (relax's expression, rcsc.f:1300-1330)
+__device__ __forceinline__ double str_resid64(const StrDev &d, const StrLevel &L, int i, int j)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const double r = L.r[i];
+    double temp;
+    if (i <= n1 / 2)
+        temp = CRR(i, 1) * PS(i - 1, j) + CRR(i, 2) * PS(i, j) + CRR(i, 3) * PS(i + 1, j) + CRR(i, 4) * PS(i + 2, j) +
+               (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r - PS(i, j) / (r * r);
+    else
+        temp = CRR(i, 1) * PS(i - 2, j) + CRR(i, 2) * PS(i - 1, j) + CRR(i, 3) * PS(i, j) + CRR(i, 4) * PS(i + 1, j) +
+               (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r - PS(i, j) / (r * r);
+    if (j <= n2 / 2)
+        temp = temp + CZZ(j, 1) * PS(i, j - 1) + CZZ(j, 2) * PS(i, j) + CZZ(j, 3) * PS(i, j + 1) + CZZ(j, 4) * PS(i, j + 2);
+    else
+        temp = temp + CZZ(j, 1) * PS(i, j - 2) + CZZ(j, 2) * PS(i, j - 1) + CZZ(j, 3) * PS(i, j) + CZZ(j, 4) * PS(i, j + 1);
+    return L.f[(size_t)i + (size_t)(n1 + 1) * j] - temp;
+}
+
+__global__ void __launch_bounds__(STR_THREADS) k_str_solve_mixed(const __grid_constant__ StrDev d)
+{
+    __shared__ double s_red[33];
+    if (d.abort && *d.abort) return;
+    const int nlev = d.nlev;
+    const StrLevel &L1 = d.lev[1];
+    const int n1 = L1.n1, n2 = L1.n2;
+    const int tp = (n1 + 1) * (n2 + 1);
+    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+        const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+        L1.f[idx] = d.io_rhs[idx];
+        PS(i, j) = d.io_psi[idx];
+        L1.f32[idx] = 0.f;
+    }
+    for (int idx = threadIdx.x; idx < d.ld * d.ld; idx += blockDim.x) d.rc32[idx] = 0.f;
+    __syncthreads();
+    const int ni = n1 - 1, tot = ni * (n2 - 1);
+    int status = GB_MAXSWEEPS, cycles = 0;
+    for (int it = 0;; ++it) {
+        double m = 0.0;
+        int nan = 0;
+        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            const int j = idx / ni + 1, i = idx - (j - 1) * ni + 1;
+            const double rr = str_resid64(d, L1, i, j);
+            L1.f32[(size_t)i + (size_t)(n1 + 1) * j] = (float)rr;
+            const double a = fabs(rr);
+            if (a != a) nan = 1;
+            if (a > m) m = a;
+        }
+        nan = __syncthreads_or(nan);
+        const double res = str_blk_max(m, s_red);
+        if (nan) { status = GB_NAN; break; }
+        if (res < d.tolcon) { status = GB_OK; break; }
+        if (it == d.maxsweeps) break;
+        for (int q = threadIdx.x; q < tp; q += blockDim.x) L1.v32[q] = 0.f;
+        __syncthreads();
+        str_relax32(d, 1);
+        if (nlev > 1) {
+            for (int l = 1; l <= nlev - 1; ++l) {
+                str_corser32(d, l);
+                str_relax32(d, l + 1);
+            }
+            for (int l = nlev; l >= 2; --l) {
+                str_finer32(d, l);
+                str_relax32(d, l - 1);
+            }
+        }
+        for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            const int j = idx / ni + 1, i = idx - (j - 1) * ni + 1;
+            PS(i, j) += (double)L1.v32[(size_t)i + (size_t)(n1 + 1) * j];
+        }
+        __syncthreads();
+        cycles = it + 1;
+    }
+    if (status == GB_OK)
+        for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+            const int j = idx / (n1 + 1), i = idx - j * (n1 + 1);
+            d.io_psi[idx] = PS(i, j);
+        }
+    if (threadIdx.x == 0) {
+        d.status[0] = status;
+        d.status[1] = cycles;
+        if (status == GB_NAN && d.abort) *d.abort = 1;
+    }
+}
+
+// FP32 copies of a level's tables and factors (pivots as reciprocals), one
+// thread per level.
+__global__ void k_str_factors32(const __grid_constant__ StrDev d)
+{
+    const int l = 1 + blockIdx.x;
+    if (threadIdx.x != 0 || l > d.nlev) return;
+    const StrLevel &L = d.lev[l];
+    const int a = L.n1, b = L.n2;
+    for (int i = 0; i <= a; ++i) L.r32[i] = (float)L.r[i];
+    for (int q = 0; q < 3 * (a - 1); ++q) L.cr32[q] = (float)L.cr[q];
+    for (int q = 0; q < 4 * (a - 1); ++q) L.crr32[q] = (float)L.crr[q];
+    for (int q = 0; q < 4 * (b - 1); ++q) L.czz32[q] = (float)L.czz[q];
+    auto conv = [](const double *fac, float *g, int n) {
+        for (int k = 0; k < n; ++k) g[k] = (float)(1.0 / fac[k]);   // cdiv as reciprocals
+        for (int k = n; k < 5 * n; ++k) g[k] = (float)fac[k];
+        g[5 * n] = (float)(1.0 / fac[5 * n]);
+    };
+    const int nr = a - 1, nz = b - 1;
+    for (int j = 1; j <= b - 1; ++j)
+        conv(L.fac_r + (size_t)(j - 1) * (5 * nr + 1), L.fac_r32 + (size_t)(j - 1) * (5 * nr + 1), nr);
+    for (int i = 1; i <= a - 1; ++i)
+        conv(L.fac_z + (size_t)(i - 1) * (5 * nz + 1), L.fac_z32 + (size_t)(i - 1) * (5 * nz + 1), nz);
+}
+
+#undef PS32
+#undef CR32
+#undef CRR32
+#undef CZZ32
 #undef PS
 #undef CR
 #undef CRR
@@ -423,6 +738,15 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
         need += (a + 1) + 3 * (a - 1) + 4 * (a - 1) + 4 * (b - 1) + 2 * (a + 1) * (b + 1);
         need += (b - 1) * (5 * (a - 1) + 1) + (a - 1) * (5 * (b - 1) + 1);
     }
+    // FP32 copies: psif32, rc32 and every level's tables (half a double each, rounded up per array)
+    size_t need32 = 2 * (size_t)d.ld * d.ld + 16;
+    for (int l = 0; l < nlev; ++l) {
+        const size_t a = lv[l].n1, b = lv[l].n2;
+        need32 += (a + 1) + 3 * (a - 1) + 4 * (a - 1) + 4 * (b - 1) + 2 * (a + 1) * (b + 1);
+        need32 += (b - 1) * (5 * (a - 1) + 1) + (a - 1) * (5 * (b - 1) + 1) + 16;
+    }
+    const size_t need64 = need;
+    need += (need32 + 1) / 2;
     cudaError_t e = cudaMalloc(&h->pool, sizeof(double) * need);
     if (e != cudaSuccess) { delete h; gb_set_error("gb_str_create: %s", cudaGetErrorString(e)); return GB_ERR_ALLOC; }
     cudaMemset(h->pool, 0, sizeof(double) * need);
@@ -454,10 +778,33 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
         for (int i = 1; i <= a - 1; ++i) jobs.push_back({l + 1, 1, i});
         wmax = std::max(wmax, std::max(a, bb));
     }
-    if ((size_t)(b - h->pool) != need) {
+    if ((size_t)(b - h->pool) != need64) {
         gb_str_destroy(h);
         gb_set_error("gb_str_create: pool layout mismatch");
         return GB_ERR_CUDA;
+    }
+    {
+        float *fb = (float *)b;
+        float *fend = (float *)(h->pool + need);
+        d.psif32 = fb; fb += (size_t)d.ld * d.ld;
+        d.rc32 = fb; fb += (size_t)d.ld * d.ld;
+        for (int l = 1; l <= nlev; ++l) {
+            StrLevel &L = d.lev[l];
+            const size_t a = L.n1, bb = L.n2;
+            L.r32 = fb; fb += a + 1;
+            L.cr32 = fb; fb += 3 * (a - 1);
+            L.crr32 = fb; fb += 4 * (a - 1);
+            L.czz32 = fb; fb += 4 * (bb - 1);
+            L.v32 = fb; fb += (a + 1) * (bb + 1);
+            L.f32 = fb; fb += (a + 1) * (bb + 1);
+            L.fac_r32 = fb; fb += (bb - 1) * (5 * (a - 1) + 1);
+            L.fac_z32 = fb; fb += (a - 1) * (5 * (bb - 1) + 1);
+        }
+        if (fb > fend) {
+            gb_str_destroy(h);
+            gb_set_error("gb_str_create: FP32 pool layout overflow");
+            return GB_ERR_CUDA;
+        }
     }
     const int wstride = 7 * wmax;
     StrJob *djobs = nullptr;
@@ -475,6 +822,10 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
     e = cudaDeviceSynchronize();
     cudaFree(djobs);
     cudaFree(work);
+    if (e == cudaSuccess) {
+        k_str_factors32<<<nlev, 32>>>(d);
+        e = cudaDeviceSynchronize();
+    }
     if (e != cudaSuccess) { gb_set_error("gb_str_create: factors: %s", cudaGetErrorString(e)); gb_str_destroy(h); return GB_ERR_CUDA; }
     e = cudaMalloc(&h->status, 64);
     if (e != cudaSuccess) { gb_str_destroy(h); gb_set_error("gb_str_create: status"); return GB_ERR_ALLOC; }
@@ -483,6 +834,22 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
     if (e != cudaSuccess) { gb_str_destroy(h); gb_set_error("gb_str_create: stream"); return GB_ERR_CUDA; }
     *out = h;
     return GB_OK;
+}
+
+// The solve on device arrays (0:n1, 0:n2) with leading dimension n1 + 1,
+// queued on stream s: psi is read and, on convergence, written in place;
+// the status and sweep count go to status[0..1]; abort as in StrDev.
+cudaError_t gb_str_launch_device(const gb_str *h, double *psi, const double *rhs, int *status, int *abort, int mixed,
+                                 cudaStream_t s)
+{
+    StrDev d = h->dev;
+    d.io_psi = psi;
+    d.io_rhs = const_cast<double *>(rhs);
+    d.status = status;
+    d.abort = abort;
+    if (mixed) k_str_solve_mixed<<<1, STR_THREADS, STR32_SMEM_BYTES, s>>>(d);
+    else k_str_solve<<<1, STR_THREADS, 0, s>>>(d);
+    return cudaGetLastError();
 }
 
 extern "C" int gb_str_poisson(gb_str *h, double *psi, const double *rhs, int ld, int *sweeps)

@@ -16,6 +16,13 @@
 
 static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
 
+/* the stretched-grid forms (end of this file) */
+static void axs_vort_vel(orc_axi_t *s, int what);
+static void axs_temperature(orc_axi_t *s);
+static double axs_heat(const orc_axi_t *s);
+static void axs_update(orc_axi_t *s);
+static int axs_poisson(orc_axi_t *s, int *sweeps);
+
 int orc_axi_init(orc_axi_t *s, int nr, int nz, double dt, double r0, double rmax, double zmax,
                  double Ra, double Re, double Ptl)
 {
@@ -105,7 +112,7 @@ void orc_axi_initial(orc_axi_t *s, int kind, unsigned long long seed, double amp
     unsigned long long st = seed;
     for (int j = 0; j <= nz; ++j) {
         for (int i = 0; i <= nr; ++i) {
-            const double r = s->r0 + (double)i * s->dr;
+            const double r = s->sg ? s->sg->r[1][i] : s->r0 + (double)i * s->dr;
             s->omeg[AX(i, j)] = 0.0;
             s->phi[AX(i, j)] = 0.0;
             s->vel[AX(i, j)] = 0.0;
@@ -152,6 +159,10 @@ void orc_axi_arakawa(const orc_axi_t *s, double *arak, const double *psi, const 
 /* vorticity, rotann2.f:268-316 */
 void orc_axi_vorticity(orc_axi_t *s)
 {
+    if (s->sg) {
+        axs_vort_vel(s, 1);
+        return;
+    }
     const int ld = s->ld, nr = s->nr, nz = s->nz;
     const double dr = s->dr, dz = s->dz, Ptl = s->Ptl, Ra = s->Ra, Re = s->Re;
     const double *omeg = s->omeg, *omegp = s->omegp, *phi = s->phi, *vel = s->vel, *theta = s->theta;
@@ -184,6 +195,10 @@ void orc_axi_vorticity(orc_axi_t *s)
 /* velocity, rotann2.f:324-370 */
 void orc_axi_velocity(orc_axi_t *s)
 {
+    if (s->sg) {
+        axs_vort_vel(s, 2);
+        return;
+    }
     const int ld = s->ld, nr = s->nr, nz = s->nz;
     const double dr = s->dr, dz = s->dz, Ptl = s->Ptl, Ra = s->Ra, Re = s->Re;
     const double *phi = s->phi, *vel = s->vel, *velp = s->velp, *theta = s->theta;
@@ -214,6 +229,10 @@ void orc_axi_velocity(orc_axi_t *s)
  * (adiabatic top and bottom) and take no Jacobian. */
 void orc_axi_temperature(orc_axi_t *s)
 {
+    if (s->sg) {
+        axs_temperature(s);
+        return;
+    }
     const int ld = s->ld, nr = s->nr, nz = s->nz;
     const double dr = s->dr, dz = s->dz;
     const double *phi = s->phi, *theta = s->theta, *thetap = s->thetap;
@@ -246,6 +265,7 @@ void orc_axi_temperature(orc_axi_t *s)
  * trapezoid in z. */
 double orc_axi_heat(const orc_axi_t *s)
 {
+    if (s->sg) return axs_heat(s);
     const int ld = s->ld, nz = s->nz;
     const double dr = s->dr, dz = s->dz;
     const double *th = s->theta;
@@ -263,6 +283,10 @@ double orc_axi_heat(const orc_axi_t *s)
  * written last, so they own the corners), walls of v and T, time levels. */
 void orc_axi_update(orc_axi_t *s)
 {
+    if (s->sg) {
+        axs_update(s);
+        return;
+    }
     const int ld = s->ld, nr = s->nr, nz = s->nz;
     const double dr = s->dr, dz = s->dz;
     for (int i = 0; i <= nr; ++i) {
@@ -461,6 +485,11 @@ void orc_axi_finer(orc_axi_t *s, int klev)
 /* poisson, rotann2.f:598-666 */
 int orc_axi_poisson(orc_axi_t *s, double *psi, const double *rhs, int *sweeps)
 {
+    if (s->sg) {
+        /* the stretched solve works on the state's phi and omegn */
+        if (psi != s->phi || rhs != s->omegn) return ORC_INVALID;
+        return axs_poisson(s, sweeps);
+    }
     const int ld = s->ld, nlev = s->nlev, n1 = s->n1[1], n2 = s->n2[1];
     int nconv = 0;
     for (int i = 0; i <= n1; ++i) {
@@ -524,5 +553,205 @@ int orc_axi_step(orc_axi_t *s, double *nu, int *sweeps, int *converged)
         const double tol = (double)1e-6f;   /* REAL*4 literal of rotann2.f:191 */
         *converged = (e1 < tol && e2 < tol && e3 < tol);
     }
+    return st;
+}
+
+/* ------------------------------------------------------------------------
+ * Stretched grid (see axi_oracle.h): rotann2.f's physics with grid.f's
+ * level-1 weights and rcsc.f's stretched multigrid.  Every expression is
+ * evaluated in the order written here, which the device kernels follow.
+ * ------------------------------------------------------------------------ */
+#define SR(i) (g->r[1][(i)])
+#define SZ(j) (g->z[1][(j)])
+#define SCR(i, k) (g->cr[1][3 * ((i) - 1) + (k) - 1])
+#define SCRR(i, k) (g->crr[1][4 * ((i) - 1) + (k) - 1])
+#define SCZ(j, k) (g->cz[1][3 * ((j) - 1) + (k) - 1])
+#define SCZZ(j, k) (g->czz[1][4 * ((j) - 1) + (k) - 1])
+
+int orc_axi_set_stretched(orc_axi_t *s, const orc_str_grid_t *g, orc_str_mg_t *m)
+{
+    if (!g || !m || g->nlev < 1 || g->n1[1] != s->nr || g->n2[1] != s->nz || s->nr < 4) return ORC_INVALID;
+    double w[25];
+    if (orc_str_fdif(5, 1, 0, g->r[1], w)) return ORC_INVALID;
+    for (int q = 0; q < 5; ++q) s->hw[q] = w[5 + q];
+    s->sg = g;
+    s->smg = m;
+    return ORC_OK;
+}
+
+static double axs_dr_off(const orc_str_grid_t *g, const double *x, int ld, int i, int j)
+{
+    return SCR(i, 1) * x[AX(i - 1, j)] + SCR(i, 3) * x[AX(i + 1, j)];
+}
+static double axs_drr_off(const orc_str_grid_t *g, const double *x, int ld, int i, int j, int nr)
+{
+    if (i <= nr / 2) return SCRR(i, 1) * x[AX(i - 1, j)] + SCRR(i, 3) * x[AX(i + 1, j)] + SCRR(i, 4) * x[AX(i + 2, j)];
+    return SCRR(i, 1) * x[AX(i - 2, j)] + SCRR(i, 2) * x[AX(i - 1, j)] + SCRR(i, 4) * x[AX(i + 1, j)];
+}
+static double axs_crrc(const orc_str_grid_t *g, int i, int nr) { return i <= nr / 2 ? SCRR(i, 2) : SCRR(i, 3); }
+static double axs_dz(const orc_str_grid_t *g, const double *x, int ld, int i, int j)
+{
+    return SCZ(j, 1) * x[AX(i, j - 1)] + SCZ(j, 2) * x[AX(i, j)] + SCZ(j, 3) * x[AX(i, j + 1)];
+}
+static double axs_dzz_off(const orc_str_grid_t *g, const double *x, int ld, int i, int j, int nz)
+{
+    if (j <= nz / 2) return SCZZ(j, 1) * x[AX(i, j - 1)] + SCZZ(j, 3) * x[AX(i, j + 1)] + SCZZ(j, 4) * x[AX(i, j + 2)];
+    return SCZZ(j, 1) * x[AX(i, j - 2)] + SCZZ(j, 2) * x[AX(i, j - 1)] + SCZZ(j, 4) * x[AX(i, j + 1)];
+}
+static double axs_czzc(const orc_str_grid_t *g, int j, int nz) { return j <= nz / 2 ? SCZZ(j, 2) : SCZZ(j, 3); }
+
+/* the Arakawa sum of rotann2.f:432-459 over the local metric */
+static double axs_arakawa(const orc_str_grid_t *g, const double *psi, const double *th, int ld, int i, int j)
+{
+    const int ip = i + 1, im = i - 1;
+    const double a = (psi[AX(ip, j)] - psi[AX(im, j)]) * (th[AX(i, j + 1)] - th[AX(i, j - 1)]) -
+                     (psi[AX(i, j + 1)] - psi[AX(i, j - 1)]) * (th[AX(ip, j)] - th[AX(im, j)]) +
+                     psi[AX(ip, j)] * (th[AX(ip, j + 1)] - th[AX(ip, j - 1)]) -
+                     psi[AX(im, j)] * (th[AX(im, j + 1)] - th[AX(im, j - 1)]) -
+                     psi[AX(i, j + 1)] * (th[AX(ip, j + 1)] - th[AX(im, j + 1)]) +
+                     psi[AX(i, j - 1)] * (th[AX(ip, j - 1)] - th[AX(im, j - 1)]) +
+                     th[AX(i, j + 1)] * (psi[AX(ip, j + 1)] - psi[AX(im, j + 1)]) -
+                     th[AX(i, j - 1)] * (psi[AX(ip, j - 1)] - psi[AX(im, j - 1)]) -
+                     th[AX(ip, j)] * (psi[AX(ip, j + 1)] - psi[AX(ip, j - 1)]) +
+                     th[AX(im, j)] * (psi[AX(im, j + 1)] - psi[AX(im, j - 1)]);
+    return a / (3.0 * (SR(ip) - SR(im)) * (SZ(j + 1) - SZ(j - 1)));
+}
+
+static void axs_vort_vel(orc_axi_t *s, int what)
+{
+    const orc_str_grid_t *g = s->sg;
+    const int ld = s->ld, nr = s->nr, nz = s->nz;
+    const double Ptl = s->Ptl, Ra = s->Ra, Re = s->Re, dt = s->dt;
+    const double *omeg = s->omeg, *phi = s->phi, *vel = s->vel, *theta = s->theta;
+    const double RRP = Ra / Re / Ptl;
+    for (int i = 1; i <= nr - 1; ++i) {
+        for (int j = 1; j <= nz - 1; ++j) {
+            const double r = SR(i);
+            const double sigma = axs_crrc(g, i, nr) + SCR(i, 2) / r + axs_czzc(g, j, nz);
+            const double A = 1.0 / (2.0 * Ptl * dt) - sigma / 2.0 + 1.0 / (2.0 * (r * r));
+            const double AA = 1.0 / (2.0 * Ptl * dt) + sigma / 2.0 - 1.0 / (2.0 * (r * r));
+            const double dz_phi = axs_dz(g, phi, ld, i, j), dz_v = axs_dz(g, vel, ld, i, j);
+            if (what & 1) {
+                const double arak = axs_arakawa(g, phi, omeg, ld, i, j);
+                const double dz_om = axs_dz(g, omeg, ld, i, j), dz_th = axs_dz(g, theta, ld, i, j);
+                const double B = (phi[AX(i, j)] * dz_om + omeg[AX(i, j)] * dz_phi) / (Ptl * r);
+                const double C = 2.0 * vel[AX(i, j)] * dz_v / (Ptl * r);
+                const double D = 2.0 * Re * dz_v;
+                const double E = r * Ra * dz_th;
+                const double EE = 2.0 * RRP * vel[AX(i, j)] * dz_th + 2.0 * RRP * theta[AX(i, j)] * dz_v;
+                const double F = axs_drr_off(g, omeg, ld, i, j, nr);
+                const double G = axs_dr_off(g, omeg, ld, i, j) / r;
+                const double H = axs_dzz_off(g, omeg, ld, i, j, nz);
+                s->omegn[AX(i, j)] = (AA * s->omegp[AX(i, j)] + arak / Ptl + B + C + D - E - EE + F + G + H) / A;
+            }
+            if (what & 2) {
+                const double arak = axs_arakawa(g, phi, vel, ld, i, j);
+                const double B = (vel[AX(i, j)] * dz_phi - phi[AX(i, j)] * dz_v) / (Ptl * r);
+                const double C = 2.0 * Re * dz_phi;
+                const double CC = -2.0 * RRP * theta[AX(i, j)] * dz_phi;
+                const double D = axs_drr_off(g, vel, ld, i, j, nr);
+                const double E = axs_dr_off(g, vel, ld, i, j) / r;
+                const double F = axs_dzz_off(g, vel, ld, i, j, nz);
+                s->veln[AX(i, j)] = (AA * s->velp[AX(i, j)] + arak / Ptl - B - C - CC + D + E + F) / A;
+            }
+        }
+    }
+}
+
+static void axs_temperature(orc_axi_t *s)
+{
+    const orc_str_grid_t *g = s->sg;
+    const int ld = s->ld, nr = s->nr, nz = s->nz;
+    const double dt = s->dt;
+    const double *phi = s->phi, *theta = s->theta;
+    const double h1 = SZ(1) - SZ(0), hn = SZ(nz) - SZ(nz - 1);
+    for (int i = 1; i <= nr - 1; ++i) {
+        for (int j = 0; j <= nz; ++j) {
+            const double r = SR(i);
+            double arak, B, E, czzc;
+            if (j == 0) {
+                arak = 0.0;
+                B = 0.0;
+                E = 2.0 * theta[AX(i, 1)] / (h1 * h1);
+                czzc = -2.0 / (h1 * h1);
+            } else if (j == nz) {
+                arak = 0.0;
+                B = 0.0;
+                E = 2.0 * theta[AX(i, nz - 1)] / (hn * hn);
+                czzc = -2.0 / (hn * hn);
+            } else {
+                arak = axs_arakawa(g, phi, theta, ld, i, j);
+                B = phi[AX(i, j)] * axs_dz(g, theta, ld, i, j) / r;
+                E = axs_dzz_off(g, theta, ld, i, j, nz);
+                czzc = axs_czzc(g, j, nz);
+            }
+            const double sigma = axs_crrc(g, i, nr) + SCR(i, 2) / r + czzc;
+            const double cf3 = 1.0 / (2.0 * dt) - sigma / 2.0;
+            const double cf4 = 1.0 / (2.0 * dt) + sigma / 2.0;
+            const double C = axs_drr_off(g, theta, ld, i, j, nr);
+            const double D = axs_dr_off(g, theta, ld, i, j) / r;
+            s->thetan[AX(i, j)] = (cf4 * s->thetap[AX(i, j)] + arak + B + C + D + E) / cf3;
+        }
+    }
+}
+
+static double axs_heat(const orc_axi_t *s)
+{
+    const orc_str_grid_t *g = s->sg;
+    const int ld = s->ld, nz = s->nz;
+    const double *th = s->theta;
+    const double *w = s->hw;
+#define AXS_DTDR(j) (w[0] * th[AX(0, j)] + w[1] * th[AX(1, j)] + w[2] * th[AX(2, j)] + w[3] * th[AX(3, j)] + \
+                     w[4] * th[AX(4, j)])
+    double trans = (SZ(1) - SZ(0)) / 2.0 * AXS_DTDR(0);
+    trans = trans + (SZ(nz) - SZ(nz - 1)) / 2.0 * AXS_DTDR(nz);
+    for (int j = 1; j <= nz - 1; ++j) trans = trans + (SZ(j + 1) - SZ(j - 1)) / 2.0 * AXS_DTDR(j);
+#undef AXS_DTDR
+    return trans;
+}
+
+static void axs_update(orc_axi_t *s)
+{
+    const orc_str_grid_t *g = s->sg;
+    const int ld = s->ld, nr = s->nr, nz = s->nz;
+    const double hz1 = SZ(1) - SZ(0), hzn = SZ(nz) - SZ(nz - 1);
+    const double hr1 = SR(1) - SR(0), hrn = SR(nr) - SR(nr - 1);
+    for (int i = 0; i <= nr; ++i) {
+        s->omegn[AX(i, 0)] = 2.0 * s->phi[AX(i, 1)] / (hz1 * hz1);
+        s->veln[AX(i, 0)] = 0.0;
+        s->omegn[AX(i, nz)] = 2.0 * s->phi[AX(i, nz - 1)] / (hzn * hzn);
+        s->veln[AX(i, nz)] = 0.0;
+    }
+    for (int j = 0; j <= nz; ++j) {
+        s->omegn[AX(0, j)] = 2.0 * s->phi[AX(1, j)] / (hr1 * hr1);
+        s->veln[AX(0, j)] = 0.0;
+        s->thetan[AX(0, j)] = 0.0;
+        s->omegn[AX(nr, j)] = 2.0 * s->phi[AX(nr - 1, j)] / (hrn * hrn);
+        s->veln[AX(nr, j)] = 0.0;
+        s->thetan[AX(nr, j)] = 1.0;
+    }
+    for (size_t q = 0; q < (size_t)ld * (size_t)(nz + 1); ++q) {
+        s->omegp[q] = s->omeg[q];
+        s->omeg[q] = s->omegn[q];
+        s->velp[q] = s->vel[q];
+        s->vel[q] = s->veln[q];
+        s->thetap[q] = s->theta[q];
+        s->theta[q] = s->thetan[q];
+    }
+}
+
+/* the stretched multigrid with the AXI state's tolerance, relaxation count,
+ * sweep limit and line order (AXI_ZEBRA: rcsc.f's four colours) */
+static int axs_poisson(orc_axi_t *s, int *sweeps)
+{
+    orc_str_mg_t *m = s->smg;
+    m->tolcon = s->tolcon;
+    m->nrel = s->nrel;
+    m->maxsweeps = s->maxsweeps;
+    m->mode = s->mode;
+    int sw = 0;
+    const int st = orc_str_poisson(m, s->phi, s->omegn, &sw);
+    s->last_sweeps = sw;
+    if (sweeps) *sweeps = sw;
     return st;
 }

@@ -16,6 +16,8 @@
 #ifndef AXI_ORACLE_H
 #define AXI_ORACLE_H
 
+#include "str_oracle.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -41,7 +43,40 @@ typedef struct {
     int mode;                                /* AXI_LEX or AXI_ZEBRA */
     int last_sweeps;
     double last_resmax;
+    /* stretched grid (NULL: rotann2.f's uniform grid); see orc_axi_set_stretched */
+    const orc_str_grid_t *sg;
+    orc_str_mg_t *smg;
+    double hw[5];                            /* stretched: inner-wall d/dr weights on r(0..4) */
 } orc_axi_t;
+
+/* The same physics on a non-uniform (r, z) grid: grid.f's level-1 positions
+ * and finite-difference weights (orc_str_levels + orc_str_coefficients) and
+ * rcsc.f's stretched multigrid for the streamfunction (orc_str_poisson; its
+ * operator psi_rr + psi_r/r - psi/r^2 + psi_zz is rotann2.f's).  rotann2.f
+ * has no such mode: the reference's only stretched-grid driver is rcsc.f,
+ * whose transport this follows for the derivative weights.  At a point
+ * (i, j) of the stretched transport:
+ *   d/dr x    = cr1 x(i-1) + cr2 x(i) + cr3 x(i+1)            (rcsc.f dum2)
+ *   d2/dr2 x  = the 4-point crr weights, orientation switching at nr/2
+ *               (rcsc.f dum1a / dum3a off the centre), centre crr_c
+ *   the same in z with cz, czz and nz/2;
+ *   every central difference (x(j+1) - x(j-1)) / (2 dz) of rotann2.f's
+ *   vorticity, velocity and temperature becomes d/dz x, every
+ *   (x(i+1) + x(i-1)) / dr^2 the off-centre part of d2/dr2 x, every
+ *   (x(i+1) - x(i-1)) / (2 r dr) the off-centre part of (d/dr x) / r;
+ *   the Dufort-Frankel centre: sigma = crr_c + cr2 / r + czz_c replaces
+ *   -2/dr^2 - 2/dz^2 (rcsc.f's cnr + cnz, doubled), so cf1 becomes
+ *   1/(2 Ptl dt) - sigma/2 and cf2 1/(2 Ptl dt) + sigma/2 (cf3, cf4 with dt);
+ *   the Arakawa sum is divided by 3 (r(i+1) - r(i-1)) (z(j+1) - z(j-1))
+ *   (12 hr hz on the uniform grid: the Jacobian in index space over the
+ *   local metric);
+ *   the temperature's mirrored wall rows j = 0, nz: d/dz = 0,
+ *   d2/dz2 x = 2 (x(i, 1) - x(i, 0)) / h^2 with h the wall spacing;
+ *   Thom wall vorticity 2 psi(next) / h^2 with the wall spacing (rcsc.f
+ *   update, :706-751); the heat flux with the five-point one-sided d/dr
+ *   weights at the inner wall on r(0..4) (grid.f's fdif, grid.f:917-1032,
+ *   fourth order as rotann2.f's heat stencil) and the trapezoid rule in z. */
+int  orc_axi_set_stretched(orc_axi_t *s, const orc_str_grid_t *g, orc_str_mg_t *m);
 
 int  orc_axi_init(orc_axi_t *s, int nr, int nz, double dt, double r0, double rmax, double zmax,
                   double Ra, double Re, double Ptl);

@@ -76,7 +76,8 @@ class AXI(C.Structure):
                  ("rval", _dp), ("v", _dp * 8), ("f", _dp * 8),
                  ("psic", _dp), ("psif", _dp), ("rc", _dp), ("rf", _dp), ("tempa", _dp),
                  ("tolcon", C.c_double), ("nrel", C.c_int), ("maxsweeps", C.c_int), ("mode", C.c_int),
-                 ("last_sweeps", C.c_int), ("last_resmax", C.c_double)])
+                 ("last_sweeps", C.c_int), ("last_resmax", C.c_double), ("sg", C.c_void_p), ("smg", C.c_void_p),
+                 ("hw", C.c_double * 5)])
 
 
 R3D_FIELDS = ["An", "A", "Ap", "Bn", "B", "Bp", "Cn", "C", "Cp", "thn", "th", "thp",
@@ -167,6 +168,8 @@ def lib():
         L.orc_axi_poisson.argtypes = [C.POINTER(AXI), _dp, _dp, _ip]
         L.orc_axi_poisson.restype = C.c_int
         L.orc_axi_step.argtypes = [C.POINTER(AXI), _dp, _ip, _ip]
+        L.orc_axi_set_stretched.argtypes = [C.POINTER(AXI), C.POINTER(STRGrid), C.POINTER(STRMG)]
+        L.orc_axi_set_stretched.restype = C.c_int
         L.orc_axi_step.restype = C.c_int
         L.orc_axi_relax.argtypes = [C.POINTER(AXI), C.c_int, C.c_int, _ip]
         L.orc_axi_corser.argtypes = [C.POINTER(AXI), C.c_int]
@@ -386,6 +389,17 @@ class OracleAXI:
 
     def initial(self, kind=1, seed=0, amp=1e-3):
         lib().orc_axi_initial(C.byref(self.s), kind, seed, amp)
+
+    def stretch(self, hr1, hz1):
+        """Puts the state on the non-uniform grid of level-1 spacings hr1,
+        hz1 (1-based, index 0 unused; r from r0, z from 0): grid.f's levels
+        and weights, rcsc.f's multigrid for the streamfunction.  Call before
+        initial().  Returns the OracleSTR holding the grid."""
+        st = OracleSTR(hr1, hz1, self.s.r0, 0.0, mode=self.s.mode)
+        if lib().orc_axi_set_stretched(C.byref(self.s), C.byref(st.g), C.byref(st.m)) != 0:
+            raise ValueError("stretched grid does not match nr x nz")
+        self._str = st
+        return st
 
     def step(self):
         nu = C.c_double()
