@@ -20,9 +20,19 @@ import numpy as np
 from . import lib as _L
 
 
+def stretched_grid(nr, nz, r0, rmax, zmax, factor):
+    """grid.f's levels and weights for the tanh grid clustered toward all
+    four walls with the given stretch factor (grid.spacing_tanh)."""
+    from . import grid
+    return grid.build(grid.spacing_tanh(nr, r0, rmax, factor), grid.spacing_tanh(nz, 0.0, zmax, factor), r0)
+
+
 class AXI:
     def __init__(self, nr, nz, dt=1e-5, r0=0.5, rmax=1.0, zmax=0.5, Ra=1e5, Re=1e2, Pr=1.0,
-                 tolcon=None, maxsweeps=None, nrel=None, smoother=_L.SMOOTHER_LEX, precision=_L.PRB_FP64):
+                 tolcon=None, maxsweeps=None, nrel=None, smoother=_L.SMOOTHER_LEX, precision=_L.PRB_FP64,
+                 grid=None):
+        """grid: a grid.Levels (grid.build) for the stretched-grid mode
+        (gb_axi_create_stretched); None for rotann2.f's uniform grid."""
         L = _L.load()
         p = _L.AxiParams()
         L.gb_axi_default_params(C.byref(p), nr, nz)
@@ -37,7 +47,24 @@ class AXI:
         self.params = p
         h = C.c_void_p()
         nlev = C.c_int(0)
-        _L.check(L.gb_axi_create(C.byref(p), C.byref(h), C.byref(nlev)), "gb_axi_create")
+        if grid is None:
+            _L.check(L.gb_axi_create(C.byref(p), C.byref(h), C.byref(nlev)), "gb_axi_create")
+        else:
+            from . import grid as G
+            self._keep = []
+            arr = (_L.StrLevel * grid.nlev)()
+            for l in range(1, grid.nlev + 1):
+                tabs = [np.ascontiguousarray(x, dtype=np.float64).ravel() for x in
+                        (grid.r[l], grid.cr[l], grid.crr[l], grid.czz[l])]
+                self._keep += tabs
+                arr[l - 1] = _L.StrLevel(grid.n1[l], grid.n2[l], *(t.ctypes.data for t in tabs))
+            z = np.ascontiguousarray(grid.z[1], dtype=np.float64)
+            cz = np.ascontiguousarray(grid.cz[1], dtype=np.float64).ravel()
+            hw = np.ascontiguousarray(G.fdif(5, 1, 0, grid.r[1])[1], dtype=np.float64)
+            self._keep += [arr, z, cz, hw]
+            g = _L.AxiGrid(grid.nlev, arr, z.ctypes.data, cz.ctypes.data, hw.ctypes.data)
+            _L.check(L.gb_axi_create_stretched(C.byref(p), C.byref(g), C.byref(h), C.byref(nlev)),
+                     "gb_axi_create_stretched")
         self._h = h
         self.nlev = nlev.value
         self.nr, self.nz = nr, nz

@@ -26,6 +26,7 @@
 
 #include "banded.cuh"
 #include "gbcommon.cuh"
+#include "str_internal.cuh"
 
 #define AXI_THREADS 512
 #define AXI_MAXLEV 8
@@ -41,8 +42,19 @@ struct AxiLevel {
     float *v32, *f32, *fac_r32, *fac_z32;
 };
 
+// Stretched grid (gb_axi_create_stretched): level-1 positions, grid.f's
+// finite-difference weights and the inner-wall d/dr weights of the heat flux.
+struct AxsTab {
+    const double *r, *z;      // r(0..nr), z(0..nz)
+    const double *cr, *crr;   // rows i = 1..nr-1: [3(i-1) + k], [4(i-1) + k]
+    const double *cz, *czz;   // rows j = 1..nz-1: [3(j-1) + k], [4(j-1) + k]
+    double hw[5];             // d/dr at r(0) on r(0..4)
+};
+
 struct AxiDev {
     int nr, nz, ld, nlev, mode, maxsweeps, nrel;
+    int stretched;            // 1: the transport uses st (and the stretched multigrid)
+    AxsTab st;
     double dt, dr, dz, r0, rmax, zmax, Ra, Re, Ptl;
     double cf1, cf2, cf3, cf4, tolcon;
     double *f[GB_A_COUNT];
@@ -83,14 +95,146 @@ __device__ __forceinline__ double arakawa_at(const double *psi, const double *th
     return a / (12.0 * hx * hy);
 }
 
+// ---------------------------------------------------------------------------
+// Stretched-grid forms: every derivative of rotann2.f's transport taken with
+// grid.f's weights, each sum in the order written here (the oracle's
+// orc_axi_set_stretched states them and performs the same operations).
+// ---------------------------------------------------------------------------
+#define SCR(i, k) T.cr[3 * ((i) - 1) + (k) - 1]
+#define SCRR(i, k) T.crr[4 * ((i) - 1) + (k) - 1]
+#define SCZ(j, k) T.cz[3 * ((j) - 1) + (k) - 1]
+#define SCZZ(j, k) T.czz[4 * ((j) - 1) + (k) - 1]
+
+__device__ __forceinline__ double axs_dr_off(const AxsTab &T, const double *x, int ld, int i, int j)
+{
+    return SCR(i, 1) * x[AX(i - 1, j)] + SCR(i, 3) * x[AX(i + 1, j)];
+}
+__device__ __forceinline__ double axs_drr_off(const AxsTab &T, const double *x, int ld, int i, int j, int nr)
+{
+    if (i <= nr / 2) return SCRR(i, 1) * x[AX(i - 1, j)] + SCRR(i, 3) * x[AX(i + 1, j)] + SCRR(i, 4) * x[AX(i + 2, j)];
+    return SCRR(i, 1) * x[AX(i - 2, j)] + SCRR(i, 2) * x[AX(i - 1, j)] + SCRR(i, 4) * x[AX(i + 1, j)];
+}
+__device__ __forceinline__ double axs_crrc(const AxsTab &T, int i, int nr) { return i <= nr / 2 ? SCRR(i, 2) : SCRR(i, 3); }
+__device__ __forceinline__ double axs_dz(const AxsTab &T, const double *x, int ld, int i, int j)
+{
+    return SCZ(j, 1) * x[AX(i, j - 1)] + SCZ(j, 2) * x[AX(i, j)] + SCZ(j, 3) * x[AX(i, j + 1)];
+}
+__device__ __forceinline__ double axs_dzz_off(const AxsTab &T, const double *x, int ld, int i, int j, int nz)
+{
+    if (j <= nz / 2) return SCZZ(j, 1) * x[AX(i, j - 1)] + SCZZ(j, 3) * x[AX(i, j + 1)] + SCZZ(j, 4) * x[AX(i, j + 2)];
+    return SCZZ(j, 1) * x[AX(i, j - 2)] + SCZZ(j, 2) * x[AX(i, j - 1)] + SCZZ(j, 4) * x[AX(i, j + 1)];
+}
+__device__ __forceinline__ double axs_czzc(const AxsTab &T, int j, int nz) { return j <= nz / 2 ? SCZZ(j, 2) : SCZZ(j, 3); }
+
+// the Arakawa sum over the local metric 3 (r(i+1) - r(i-1)) (z(j+1) - z(j-1))
+__device__ __forceinline__ double axs_arakawa(const AxsTab &T, const double *psi, const double *th, int ld, int i, int j)
+{
+    const int ip = i + 1, im = i - 1;
+    const double a = (psi[AX(ip, j)] - psi[AX(im, j)]) * (th[AX(i, j + 1)] - th[AX(i, j - 1)]) -
+                     (psi[AX(i, j + 1)] - psi[AX(i, j - 1)]) * (th[AX(ip, j)] - th[AX(im, j)]) +
+                     psi[AX(ip, j)] * (th[AX(ip, j + 1)] - th[AX(ip, j - 1)]) -
+                     psi[AX(im, j)] * (th[AX(im, j + 1)] - th[AX(im, j - 1)]) -
+                     psi[AX(i, j + 1)] * (th[AX(ip, j + 1)] - th[AX(im, j + 1)]) +
+                     psi[AX(i, j - 1)] * (th[AX(ip, j - 1)] - th[AX(im, j - 1)]) +
+                     th[AX(i, j + 1)] * (psi[AX(ip, j + 1)] - psi[AX(im, j + 1)]) -
+                     th[AX(i, j - 1)] * (psi[AX(ip, j - 1)] - psi[AX(im, j - 1)]) -
+                     th[AX(ip, j)] * (psi[AX(ip, j + 1)] - psi[AX(ip, j - 1)]) +
+                     th[AX(im, j)] * (psi[AX(im, j + 1)] - psi[AX(im, j - 1)]);
+    return a / (3.0 * (T.r[ip] - T.r[im]) * (T.z[j + 1] - T.z[j - 1]));
+}
+
+// vorticity and velocity of the stretched state at interior point (i, j)
+__device__ __forceinline__ void axs_vort_vel_at(const AxiDev &d, int what, int i, int j)
+{
+    const AxsTab &T = d.st;
+    const int ld = d.ld, nr = d.nr, nz = d.nz;
+    const double Ptl = d.Ptl, Ra = d.Ra, Re = d.Re, dt = d.dt;
+    const double *phi = d.f[GB_A_phi], *omeg = d.f[GB_A_omeg], *vel = d.f[GB_A_vel], *theta = d.f[GB_A_theta];
+    const double RRP = Ra / Re / Ptl;
+    const double r = T.r[i];
+    const double sigma = axs_crrc(T, i, nr) + SCR(i, 2) / r + axs_czzc(T, j, nz);
+    const double A = 1.0 / (2.0 * Ptl * dt) - sigma / 2.0 + 1.0 / (2.0 * (r * r));
+    const double AA = 1.0 / (2.0 * Ptl * dt) + sigma / 2.0 - 1.0 / (2.0 * (r * r));
+    const double dz_phi = axs_dz(T, phi, ld, i, j), dz_v = axs_dz(T, vel, ld, i, j);
+    if (what & 1) {
+        const double arak = axs_arakawa(T, phi, omeg, ld, i, j);
+        const double dz_om = axs_dz(T, omeg, ld, i, j), dz_th = axs_dz(T, theta, ld, i, j);
+        const double B = (phi[AX(i, j)] * dz_om + omeg[AX(i, j)] * dz_phi) / (Ptl * r);
+        const double C = 2.0 * vel[AX(i, j)] * dz_v / (Ptl * r);
+        const double D = 2.0 * Re * dz_v;
+        const double E = r * Ra * dz_th;
+        const double EE = 2.0 * RRP * vel[AX(i, j)] * dz_th + 2.0 * RRP * theta[AX(i, j)] * dz_v;
+        const double F = axs_drr_off(T, omeg, ld, i, j, nr);
+        const double G = axs_dr_off(T, omeg, ld, i, j) / r;
+        const double H = axs_dzz_off(T, omeg, ld, i, j, nz);
+        d.f[GB_A_omegn][AX(i, j)] = (AA * d.f[GB_A_omegp][AX(i, j)] + arak / Ptl + B + C + D - E - EE + F + G + H) / A;
+    }
+    if (what & 2) {
+        const double arak = axs_arakawa(T, phi, vel, ld, i, j);
+        const double B = (vel[AX(i, j)] * dz_phi - phi[AX(i, j)] * dz_v) / (Ptl * r);
+        const double C = 2.0 * Re * dz_phi;
+        const double CC = -2.0 * RRP * theta[AX(i, j)] * dz_phi;
+        const double D = axs_drr_off(T, vel, ld, i, j, nr);
+        const double E = axs_dr_off(T, vel, ld, i, j) / r;
+        const double F = axs_dzz_off(T, vel, ld, i, j, nz);
+        d.f[GB_A_veln][AX(i, j)] = (AA * d.f[GB_A_velp][AX(i, j)] + arak / Ptl - B - C - CC + D + E + F) / A;
+    }
+}
+
+// temperature of the stretched state at (i, j), j = 0..nz (rows 0 and nz
+// mirrored: d/dz = 0, d2/dz2 from the wall spacing)
+__device__ __forceinline__ void axs_temperature_at(const AxiDev &d, int i, int j)
+{
+    const AxsTab &T = d.st;
+    const int ld = d.ld, nr = d.nr, nz = d.nz;
+    const double dt = d.dt;
+    const double *phi = d.f[GB_A_phi], *theta = d.f[GB_A_theta];
+    const double r = T.r[i];
+    double arak, B, E, czzc;
+    if (j == 0) {
+        const double h1 = T.z[1] - T.z[0];
+        arak = 0.0;
+        B = 0.0;
+        E = 2.0 * theta[AX(i, 1)] / (h1 * h1);
+        czzc = -2.0 / (h1 * h1);
+    } else if (j == nz) {
+        const double hn = T.z[nz] - T.z[nz - 1];
+        arak = 0.0;
+        B = 0.0;
+        E = 2.0 * theta[AX(i, nz - 1)] / (hn * hn);
+        czzc = -2.0 / (hn * hn);
+    } else {
+        arak = axs_arakawa(T, phi, theta, ld, i, j);
+        B = phi[AX(i, j)] * axs_dz(T, theta, ld, i, j) / r;
+        E = axs_dzz_off(T, theta, ld, i, j, nz);
+        czzc = axs_czzc(T, j, nz);
+    }
+    const double sigma = axs_crrc(T, i, nr) + SCR(i, 2) / r + czzc;
+    const double cf3 = 1.0 / (2.0 * dt) - sigma / 2.0;
+    const double cf4 = 1.0 / (2.0 * dt) + sigma / 2.0;
+    const double C = axs_drr_off(T, theta, ld, i, j, nr);
+    const double D = axs_dr_off(T, theta, ld, i, j) / r;
+    d.f[GB_A_thetan][AX(i, j)] = (cf4 * d.f[GB_A_thetap][AX(i, j)] + arak + B + C + D + E) / cf3;
+}
+
+#undef SCR
+#undef SCRR
+#undef SCZ
+#undef SCZZ
+
 // vorticity (rotann2.f:268-316, what & 1) and velocity (rotann2.f:324-370,
-// what & 2) on the interior, one thread per point.
+// what & 2) on the interior, one thread per point (S: the stretched forms).
+template <bool S>
 __global__ void k_axi_vort_vel(AxiDev d, int what)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int ni = d.nr - 1, nj = d.nz - 1;
     if (t >= ni * nj || *d.abort) return;
     const int i = t % ni + 1, j = t / ni + 1;
+    if constexpr (S) {
+        axs_vort_vel_at(d, what, i, j);
+        return;
+    }
     const int ld = d.ld;
     const int ip = i + 1, im = i - 1, jp = j + 1, jm = j - 1;
     const double dr = d.dr, dz = d.dz, Ptl = d.Ptl;
@@ -131,12 +275,17 @@ __global__ void k_axi_vort_vel(AxiDev d, int what)
 
 // temperature, rotann2.f:379-424: rows j = 0 and nz mirror their neighbour
 // and take no Jacobian.
+template <bool S>
 __global__ void k_axi_temperature(AxiDev d)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int ni = d.nr - 1, nj = d.nz + 1;
     if (t >= ni * nj || *d.abort) return;
     const int i = t % ni + 1, j = t / ni;
+    if constexpr (S) {
+        axs_temperature_at(d, i, j);
+        return;
+    }
     const int ld = d.ld, nz = d.nz;
     const double dr = d.dr, dz = d.dz;
     const double *phi = d.f[GB_A_phi], *theta = d.f[GB_A_theta];
@@ -164,6 +313,9 @@ __global__ void k_axi_temperature(AxiDev d)
 // r-walls written last own the corners), v = 0 on the walls, T = 0 / 1 on
 // the inner / outer wall, then the time levels rotate.  The steady-state
 // test's maxima of |x - x_p| (rotann2.f:162-180) are gathered here.
+// S: the stretched grid's wall spacings in the Thom wall vorticity (rcsc.f
+// update, :706-751).
+template <bool S>
 __global__ void k_axi_update(AxiDev d)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -176,20 +328,27 @@ __global__ void k_axi_update(AxiDev d)
         const size_t c = AX(i, j);
         double *const *f = d.f;
         const double *phi = f[GB_A_phi];
+        double hr0 = d.dr, hrn = d.dr, hz0 = d.dz, hzn = d.dz;
+        if constexpr (S) {
+            hr0 = d.st.r[1] - d.st.r[0];
+            hrn = d.st.r[nr] - d.st.r[nr - 1];
+            hz0 = d.st.z[1] - d.st.z[0];
+            hzn = d.st.z[nz] - d.st.z[nz - 1];
+        }
         double on = f[GB_A_omegn][c], vn = f[GB_A_veln][c], tn = f[GB_A_thetan][c];
         if (i == 0) {
-            on = 2.0 * phi[AX(1, j)] / (d.dr * d.dr);
+            on = 2.0 * phi[AX(1, j)] / (hr0 * hr0);
             vn = 0.0;
             tn = 0.0;
         } else if (i == nr) {
-            on = 2.0 * phi[AX(nr - 1, j)] / (d.dr * d.dr);
+            on = 2.0 * phi[AX(nr - 1, j)] / (hrn * hrn);
             vn = 0.0;
             tn = 1.0;
         } else if (j == 0) {
-            on = 2.0 * phi[AX(i, 1)] / (d.dz * d.dz);
+            on = 2.0 * phi[AX(i, 1)] / (hz0 * hz0);
             vn = 0.0;
         } else if (j == nz) {
-            on = 2.0 * phi[AX(i, nz - 1)] / (d.dz * d.dz);
+            on = 2.0 * phi[AX(i, nz - 1)] / (hzn * hzn);
             vn = 0.0;
         }
         f[GB_A_omegn][c] = on;
@@ -220,6 +379,9 @@ __global__ void k_axi_update(AxiDev d)
 
 // heat, rotann2.f:468-487: the per-row terms in parallel, summed by one
 // thread in the reference's order.
+// S: the five-point one-sided weights of the stretched grid and the
+// trapezoid rule on its z positions.
+template <bool S>
 __global__ void k_axi_heat(AxiDev d)
 {
     extern __shared__ double sh[];
@@ -228,9 +390,18 @@ __global__ void k_axi_heat(AxiDev d)
     const double dr = d.dr, dz = d.dz;
     const double *th = d.f[GB_A_theta];
     for (int j = threadIdx.x; j <= nz; j += blockDim.x) {
-        const double div = (j == 0 || j == nz) ? 24.0 * dr : 12.0 * dr;
-        sh[j] = dz * (-25.0 * th[AX(0, j)] + 48.0 * th[AX(1, j)] - 36.0 * th[AX(2, j)] + 16.0 * th[AX(3, j)] -
-                      3.0 * th[AX(4, j)]) / div;
+        if constexpr (S) {
+            const AxsTab &T = d.st;
+            const double *w = T.hw;
+            const double wz = j == 0 ? (T.z[1] - T.z[0]) / 2.0
+                                     : (j == nz ? (T.z[nz] - T.z[nz - 1]) / 2.0 : (T.z[j + 1] - T.z[j - 1]) / 2.0);
+            sh[j] = wz * (w[0] * th[AX(0, j)] + w[1] * th[AX(1, j)] + w[2] * th[AX(2, j)] + w[3] * th[AX(3, j)] +
+                          w[4] * th[AX(4, j)]);
+        } else {
+            const double div = (j == 0 || j == nz) ? 24.0 * dr : 12.0 * dr;
+            sh[j] = dz * (-25.0 * th[AX(0, j)] + 48.0 * th[AX(1, j)] - 36.0 * th[AX(2, j)] + 16.0 * th[AX(3, j)] -
+                          3.0 * th[AX(4, j)]) / div;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -806,6 +977,8 @@ __global__ void k_axi_factors(AxiDev d, double *work)
 struct gb_axi {
     gb_axi_params p;
     AxiDev dev;
+    gb_str *str = nullptr;              // stretched grid: rcsc.f's multigrid for the streamfunction
+    double *stab = nullptr;             // stretched grid: the transport's tables (AxsTab)
     double *fields = nullptr, *pool = nullptr;
     void *small = nullptr, *hist = nullptr;
     int hist_cap = 0;
@@ -882,6 +1055,8 @@ extern "C" int gb_axi_destroy(gb_axi *h)
 {
     if (!h) return GB_OK;
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->str) gb_str_destroy(h->str);
+    cudaFree(h->stab);
     cudaFree(h->fields);
     cudaFree(h->pool);
     cudaFree(h->small);
@@ -1014,6 +1189,76 @@ static int axi_create(const gb_axi_params *p, double dr, double dz, gb_axi **out
     return GB_OK;
 }
 
+// The annulus on a stretched grid: the state, its transport tables and the
+// stretched multigrid; no uniform multigrid.
+extern "C" int gb_axi_create_stretched(const gb_axi_params *p, const gb_axi_grid *g, gb_axi **out, int *nlev_out)
+{
+    if (!p || !g || !out || !g->levels || !g->z || !g->cz || !g->hw) {
+        gb_set_error("gb_axi_create_stretched: null argument");
+        return GB_ERR_INVALID;
+    }
+    *out = nullptr;
+    const int nr = p->nr, nz = p->nz;
+    const gb_str_level &L1 = g->levels[0];
+    if (g->nlev < 1 || L1.n1 != nr || L1.n2 != nz || nr < 4 || nz < 4 || !L1.r || !L1.cr || !L1.crr || !L1.czz ||
+        !(p->zmax > 0.0) || p->nrel < 1 || p->maxsweeps < 1 || p->Re == 0.0 ||
+        (p->precision != GB_PRB_FP64 && p->precision != GB_PRB_MIXED)) {
+        gb_set_error("gb_axi_create_stretched: level 1 must be %d x %d with all tables (nr, nz >= 4, zmax > 0, "
+                     "Re != 0, FP64 or mixed)", nr, nz);
+        return GB_ERR_INVALID;
+    }
+    gb_axi *h = new gb_axi();
+    h->p = *p;
+    AxiDev &d = h->dev;
+    memset(&d, 0, sizeof(d));
+    d.nr = nr;
+    d.nz = nz;
+    d.ld = nr + 1;
+    d.nlev = g->nlev;
+    d.stretched = 1;
+    axi_scalars(h);
+    int st = gb_str_create(g->nlev, g->levels, p->tolcon, p->maxsweeps, p->nrel, p->smoother, &h->str);
+    if (st != GB_OK) { delete h; return st; }
+    const size_t fsz = (size_t)d.ld * (size_t)(nz + 1);
+    cudaError_t e = cudaMalloc(&h->fields, sizeof(double) * fsz * GB_A_COUNT);
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create_stretched: %s", cudaGetErrorString(e)); return GB_ERR_ALLOC; }
+    cudaMemset(h->fields, 0, sizeof(double) * fsz * GB_A_COUNT);
+    for (int q = 0; q < GB_A_COUNT; ++q) d.f[q] = h->fields + (size_t)q * fsz;
+    const size_t ntab = (size_t)(nr + 1) + (nz + 1) + 3 * (size_t)(nr - 1) + 4 * (size_t)(nr - 1) + 3 * (size_t)(nz - 1) +
+                        4 * (size_t)(nz - 1);
+    e = cudaMalloc(&h->stab, sizeof(double) * ntab);
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create_stretched: tables"); return GB_ERR_ALLOC; }
+    double *b = h->stab;
+    auto put = [&](const double *src, size_t n) {
+        double *dst = b;
+        cudaMemcpy(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice);
+        b += n;
+        return (const double *)dst;
+    };
+    d.st.r = put(L1.r, (size_t)nr + 1);
+    d.st.z = put(g->z, (size_t)nz + 1);
+    d.st.cr = put(L1.cr, 3 * (size_t)(nr - 1));
+    d.st.crr = put(L1.crr, 4 * (size_t)(nr - 1));
+    d.st.cz = put(g->cz, 3 * (size_t)(nz - 1));
+    d.st.czz = put(L1.czz, 4 * (size_t)(nz - 1));
+    for (int q = 0; q < 5; ++q) d.st.hw[q] = g->hw[q];
+    e = cudaMalloc(&h->small, 4096);
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create_stretched: state"); return GB_ERR_ALLOC; }
+    cudaMemset(h->small, 0, 4096);
+    char *sm = (char *)h->small;
+    d.heat = (double *)(sm + 0);
+    d.errmax = (unsigned long long *)(sm + 64);
+    d.abort = (int *)(sm + 128);
+    d.status = (int *)(sm + 192);
+    d.step_index = (int *)(sm + 256);
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create_stretched: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
+    if (nlev_out) *nlev_out = g->nlev;
+    *out = h;
+    return GB_OK;
+}
+
 extern "C" int gb_axi_set_field(gb_axi *h, int field, const double *host, int ld)
 {
     if (!h || !host || field < 0 || field >= GB_A_COUNT || ld < h->dev.nr + 1) {
@@ -1045,28 +1290,38 @@ static const int AXI_TPB = 256;
 static void axi_launch_vort_vel(gb_axi *h, int what, cudaStream_t s)
 {
     const int n = (h->dev.nr - 1) * (h->dev.nz - 1);
-    k_axi_vort_vel<<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev, what);
+    if (h->dev.stretched) k_axi_vort_vel<true><<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev, what);
+    else k_axi_vort_vel<false><<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev, what);
 }
 
 static void axi_launch_temperature(gb_axi *h, cudaStream_t s)
 {
     const int n = (h->dev.nr - 1) * (h->dev.nz + 1);
-    k_axi_temperature<<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
+    if (h->dev.stretched) k_axi_temperature<true><<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
+    else k_axi_temperature<false><<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
 }
 
 static void axi_launch_update(gb_axi *h, cudaStream_t s)
 {
     const int n = (h->dev.nr + 1) * (h->dev.nz + 1);
-    k_axi_update<<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
+    if (h->dev.stretched) k_axi_update<true><<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
+    else k_axi_update<false><<<gb_ceil_div(n, AXI_TPB), AXI_TPB, 0, s>>>(h->dev);
 }
 
 static void axi_launch_heat(gb_axi *h, cudaStream_t s)
 {
-    k_axi_heat<<<1, 256, sizeof(double) * (h->dev.nz + 1), s>>>(h->dev);
+    if (h->dev.stretched) k_axi_heat<true><<<1, 256, sizeof(double) * (h->dev.nz + 1), s>>>(h->dev);
+    else k_axi_heat<false><<<1, 256, sizeof(double) * (h->dev.nz + 1), s>>>(h->dev);
 }
 
 static void axi_launch_mg(gb_axi *h, cudaStream_t s)
 {
+    const AxiDev &d = h->dev;
+    if (d.stretched) {
+        gb_str_launch_device(h->str, d.f[GB_A_phi], d.f[GB_A_omegn], d.status, d.abort,
+                             h->p.precision == GB_PRB_MIXED, d.tolcon, d.maxsweeps, d.nrel, d.mode, s);
+        return;
+    }
     if (h->p.precision == GB_PRB_MIXED) k_axi_mg_solve_mixed<<<1, AXI_THREADS, AX32_SMEM_BYTES, s>>>(h->dev);
     else k_axi_mg_solve<<<1, AXI_THREADS, 0, s>>>(h->dev);
 }

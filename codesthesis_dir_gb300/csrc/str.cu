@@ -17,6 +17,7 @@
 // parallel.
 #include "gbcommon.cuh"
 #include "banded.cuh"
+#include "str_internal.cuh"
 
 #include <stdlib.h>
 #include <string.h>
@@ -837,12 +838,18 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
 }
 
 // The solve on device arrays (0:n1, 0:n2) with leading dimension n1 + 1,
-// queued on stream s: psi is read and, on convergence, written in place;
-// the status and sweep count go to status[0..1]; abort as in StrDev.
+// queued on stream s with the given tolerance, sweep limit, relaxation count
+// and line order: psi is read and, on convergence, written in place; the
+// status and sweep (mixed: outer iteration) count go to status[0..1]; abort
+// as in StrDev.  mixed != 0 runs the FP32-inner / FP64-outer solve.
 cudaError_t gb_str_launch_device(const gb_str *h, double *psi, const double *rhs, int *status, int *abort, int mixed,
-                                 cudaStream_t s)
+                                 double tolcon, int maxsweeps, int nrel, int mode, cudaStream_t s)
 {
     StrDev d = h->dev;
+    d.tolcon = tolcon;
+    d.maxsweeps = maxsweeps;
+    d.nrel = nrel;
+    d.mode = mode;
     d.io_psi = psi;
     d.io_rhs = const_cast<double *>(rhs);
     d.status = status;

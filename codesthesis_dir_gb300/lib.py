@@ -95,6 +95,12 @@ class StrLevel(C.Structure):
                 ("czz", C.c_void_p)]
 
 
+class AxiGrid(C.Structure):
+    """gb_axi_grid: the stretched grid of gb_axi_create_stretched."""
+    _fields_ = [("nlev", C.c_int), ("levels", C.POINTER(StrLevel)), ("z", C.c_void_p), ("cz", C.c_void_p),
+                ("hw", C.c_void_p)]
+
+
 class PrbParams(C.Structure):
     _fields_ = [("nr", C.c_int), ("np", C.c_int),
                 ("dt", C.c_double), ("r0", C.c_double), ("rmax", C.c_double), ("xx", C.c_double),
@@ -142,6 +148,7 @@ SIGNATURES = [
     ("gb_axi_default_params", None, [C.POINTER(AxiParams), C.c_int, C.c_int]),
     ("gb_axi_create", C.c_int, [C.POINTER(AxiParams), C.POINTER(_vp), _ip]),
     ("gb_axi_create_spacing", C.c_int, [C.POINTER(AxiParams), C.c_double, C.c_double, C.POINTER(_vp), _ip]),
+    ("gb_axi_create_stretched", C.c_int, [C.POINTER(AxiParams), C.POINTER(AxiGrid), C.POINTER(_vp), _ip]),
     ("gb_axi_destroy", C.c_int, [_vp]),
     ("gb_axi_set_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),
     ("gb_axi_get_field", C.c_int, [_vp, C.c_int, _vp, C.c_int]),

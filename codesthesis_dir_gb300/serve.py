@@ -120,13 +120,15 @@ def sweep_requests(n=512, rate=50.0, seed=0, steps=(500, 5000), grids=SWEEP_GRID
     return out
 
 
-def axi_initial(nr, nz, r0, rmax, seed, amp):
+def axi_initial(nr, nz, r0, rmax, seed, amp, r=None):
     """The annulus start: conduction profile 1 - ln(r/rmax)/ln(r0/rmax) plus
     seeded splitmix64 noise over rows i = 1..nr-1 (j-major), every other
-    field zero."""
+    field zero.  r: the radii r(0..nr) of a stretched grid (default:
+    uniform)."""
     from .initial import _splitmix64
-    dr = (rmax - r0) / nr
-    r = r0 + np.arange(nr + 1) * dr
+    if r is None:
+        dr = (rmax - r0) / nr
+        r = r0 + np.arange(nr + 1) * dr
     base = np.array([1.0 - math.log(float(x) / rmax) / math.log(r0 / rmax) for x in r])
     u = (_splitmix64(seed, (nr - 1) * (nz + 1)) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
     th = np.asfortranarray(np.repeat(base[:, None], nz + 1, axis=1))

@@ -502,6 +502,33 @@ int gb_str_create(int nlev, const gb_str_level *levels, double tolcon, int maxsw
 int gb_str_poisson(gb_str *h, double *psi, const double *rhs, int ld, int *sweeps);
 int gb_str_destroy(gb_str *h);
 
+/* ------------------------- axisymmetric annulus on a stretched grid */
+/* rotann2.f's annulus (the gb_axi_* entry points above, same fields and
+ * time loop) on a non-uniform (r, z) grid.  rotann2.f itself is uniform;
+ * the reference's stretched-grid method is rcsc.f's (weights from grid.f),
+ * and this mode takes from it: every derivative of rotann2.f's vorticity,
+ * velocity and temperature with grid.f's level-1 weights (first
+ * derivatives on (i-1, i, i+1), second derivatives on four points switching
+ * orientation at n/2, rcsc.f's dum* functions), the Dufort-Frankel centre
+ * crr_c + cr_2/r + czz_c in place of -2/dr^2 - 2/dz^2 (rcsc.f's cnr, cnz),
+ * the Arakawa sum over the local metric 3 (r(i+1) - r(i-1)) (z(j+1) -
+ * z(j-1)), the temperature's mirrored top and bottom rows with their wall
+ * spacing, Thom wall vorticity with the wall spacings (rcsc.f update,
+ * :706-751), the heat flux with five-point one-sided d/dr weights at the
+ * inner wall (hw, from grid.f's fdif on r(0..4)) and the trapezoid rule in
+ * z, and rcsc.f's stretched multigrid (gb_str above, whose operator is
+ * rotann2.f's) for the streamfunction, in FP64 or mixed precision (FP32
+ * V-cycles inside FP64 defect correction).  On a uniform grid the transport
+ * equals rotann2.f's to rounding. */
+typedef struct gb_axi_grid {
+    int nlev;                       /* multigrid levels */
+    const gb_str_level *levels;     /* grid.f's levels (level 1 first: r, cr, crr, czz) */
+    const double *z;                /* level-1 z(0..nz) */
+    const double *cz;               /* level-1 d/dz weights of rows j = 1..nz-1 on (j-1, j, j+1): [3*(j-1) + k] */
+    const double *hw;               /* 5 weights of d/dr at r(0) on r(0..4) */
+} gb_axi_grid;
+int gb_axi_create_stretched(const gb_axi_params *p, const gb_axi_grid *g, gb_axi **out, int *nlev_out);
+
 /* ------------------------------------------------ batched banded solvers */
 /* nlines independent systems with the same n; line l's element j sits at
  * base + l*line_stride + j*elem_stride in each array.  Device pointers.

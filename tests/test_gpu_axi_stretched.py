@@ -1,0 +1,100 @@
+"""The axisymmetric annulus on a stretched grid (gb_axi_create_stretched)
+against the oracle, bit for bit: every routine (the drop-in granularity)
+from random fields, and graph-replayed steps in both line orders, on tanh
+grids clustered toward all walls with nr != nz; the mixed-precision solve
+(FP32 V-cycles inside FP64 defect correction of rcsc.f's stretched
+multigrid) within the 1e-6 field and Nusselt bar of the FP64 oracle."""
+import numpy as np
+import pytest
+
+from codesthesis_dir_gb300 import grid
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["phi", "omegn", "omeg", "omegp", "veln", "vel", "velp", "thetan", "theta", "thetap"]
+
+
+def make(O, nr, nz, mode, factor=1.5, tolcon=1e-9, Ra=1e5, Re=1e2, dt=1e-5, seed=0, amp=1e-2, precision=0):
+    from codesthesis_dir_gb300 import axi
+    hr = grid.spacing_tanh(nr, 0.5, 1.0, factor)
+    hz = grid.spacing_tanh(nz, 0.0, 0.5, factor)
+    o = O.OracleAXI(nr, nz, dt, 0.5, 1.0, 0.5, Ra, Re, 1.0, mode=mode, tolcon=tolcon)
+    o.stretch(hr, hz)
+    o.initial(1, seed, amp)
+    g = axi.AXI(nr, nz, dt=dt, r0=0.5, rmax=1.0, zmax=0.5, Ra=Ra, Re=Re, Pr=1.0, tolcon=tolcon, smoother=mode,
+                precision=precision, grid=grid.build(hr, hz, 0.5))
+    assert g.nlev == o._str.nlev
+    for n in FIELDS:
+        g.set(n, np.array(o.field(n)))
+    return o, g
+
+
+def diff(o, g):
+    bad = {}
+    for n in FIELDS:
+        a, b = np.array(o.field(n)), g.get(n)
+        if not np.array_equal(a, b):
+            bad[n] = float(np.max(np.abs(a - b)))
+    return bad
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["lex", "colours"])
+@pytest.mark.parametrize("nr,nz", [(32, 48), (64, 32)])
+def test_routines_from_random_fields(oracle, gblib, mode, nr, nz):
+    import ctypes as C
+    o, g = make(oracle, nr, nz, mode)
+    rng = np.random.default_rng(nr + nz + mode)
+    for n in ("omeg", "omegp", "vel", "velp", "phi"):
+        a = 0.1 * rng.standard_normal((nr + 1, nz + 1))
+        o.field(n)[...] = a
+        g.set(n, a)
+    for n in ("theta", "thetap"):
+        a = np.array(o.field(n)) + 0.01 * rng.standard_normal((nr + 1, nz + 1))
+        o.field(n)[...] = a
+        g.set(n, a)
+    L = oracle.lib()
+    for step in range(3):
+        L.orc_axi_vorticity(C.byref(o.s))
+        L.orc_axi_velocity(C.byref(o.s))
+        L.orc_axi_temperature(C.byref(o.s))
+        g.vorticity()
+        g.velocity()
+        g.temperature()
+        assert diff(o, g) == {}, step
+        sw = C.c_int()
+        st = L.orc_axi_poisson(C.byref(o.s), o.s.phi, o.s.omegn, C.byref(sw))
+        sw_g = g.poisson()
+        assert st == 0 and sw.value == sw_g, (st, sw.value, sw_g)
+        L.orc_axi_update(C.byref(o.s))
+        g.update()
+        t_o = L.orc_axi_heat(C.byref(o.s))
+        assert g.heat() == t_o
+        assert diff(o, g) == {}, step
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["lex", "colours"])
+def test_graph_steps(oracle, gblib, mode):
+    o, g = make(oracle, 64, 32, mode, amp=1e-3)
+    nsteps = 6
+    nu_o, sw_o = [], []
+    for _ in range(nsteps):
+        st, nu, sw, conv = o.step()
+        assert st == 0 and not conv
+        nu_o.append(nu)
+        sw_o.append(sw)
+    nu_g, sw_g = g.step(nsteps)
+    np.testing.assert_array_equal(np.array(sw_o), sw_g)
+    np.testing.assert_array_equal(np.array(nu_o), nu_g)
+    assert diff(o, g) == {}
+
+
+def test_mixed_within_1e6_of_fp64_oracle(oracle, gblib):
+    o, g = make(oracle, 64, 64, 1, amp=1e-3, precision=1)
+    nsteps = 20
+    nu_o = np.array([o.step()[1] for _ in range(nsteps)])
+    nu_g, cyc = g.step(nsteps)
+    assert np.all(cyc > 0)
+    assert np.max(np.abs(nu_g - nu_o) / np.abs(nu_o)) <= 1e-6
+    for n in ("phi", "omeg", "vel", "theta"):
+        a, b = np.array(o.field(n)), g.get(n)
+        assert np.linalg.norm(a - b) / np.linalg.norm(a) <= 1e-6, n

@@ -9,8 +9,9 @@
 * The 256-problem batched Poisson workload (sizes and right-hand sides of
   the benchmark, seed 0): plain FP64 and both mixed defect corrections,
   psi bit for bit and the V-cycle counts equal.
-* The axisymmetric annulus at 257 x 257 (Ra 1e8, Re 158.1, Pr 1, dt 2e-7):
-  20 steps in the two-colour order, bit for bit.
+* The axisymmetric annulus at 257 x 257 (Ra 1e8, Re 158.1, Pr 1, dt 2e-7)
+  on the tanh grid stretched toward all walls (factor 1.5) and on the
+  uniform grid: 20 steps in the parallel line order, bit for bit.
 * The 3D annulus at 64 x 64 x 128 (Ra 1e6, Re 500, Pr 7, dt 4e-6): two
   steps in the two-colour order, bit for bit, sweep counts equal.
 
@@ -75,11 +76,16 @@ def test_batch_workload_256_problems(oracle, gblib, precision, inner):
     assert np.all(rr <= 1e-10)
 
 
-def test_axi_257_config_scale(oracle, gblib):
+@pytest.mark.parametrize("stretched", [True, False], ids=["tanh1.5", "uniform"])
+def test_axi_257_config_scale(oracle, gblib, stretched):
     from codesthesis_dir_gb300 import axi
-    from test_gpu_axi_parity import diff, make
-    o, g = make(oracle, axi, 256, 256, 1, kind=1, seed=0, amp=1e-4, tolcon=1e-9, Ra=1e8, Re=(1e5 ** 0.5) / 2.0,
-                dt=2e-7)
+    if stretched:
+        from test_gpu_axi_stretched import diff, make
+        o, g = make(oracle, 256, 256, 1, factor=1.5, tolcon=1e-9, Ra=1e8, Re=(1e5 ** 0.5) / 2.0, dt=2e-7, amp=1e-4)
+    else:
+        from test_gpu_axi_parity import diff, make
+        o, g = make(oracle, axi, 256, 256, 1, kind=1, seed=0, amp=1e-4, tolcon=1e-9, Ra=1e8, Re=(1e5 ** 0.5) / 2.0,
+                    dt=2e-7)
     nsteps = 20
     nu_o, sw_o = [], []
     for _ in range(nsteps):
