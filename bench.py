@@ -604,24 +604,36 @@ def run_r3d_workload(args):
 
 
 def run_serve_workload(args):
-    """--workload serve: the parameter sweep served by the continuous-batching
-    loop, FP64 and mixed precision on the same arrivals.  The sweep is a
-    bounded sample of the 512-request one: --requests requests with steps
-    drawn from --serve-steps instead of 500-5000; the four grids, the Ra, Pr
-    and Ta distributions and the Poisson arrivals at 50/s are as stated."""
+    """--workload serve: the parameter sweep served by continuous batching,
+    FP64 and mixed precision on the same arrivals.  512 requests (layer or
+    annulus), the four grids, Ra, Pr and Ta drawn as stated, Poisson
+    arrivals at 50/s, 120 GB budget; --serve-steps bounds the per-request
+    step range (500-5000 as stated by default).  --serve-mode gang (default)
+    steps all active requests of a kind as one gang (one launch per phase
+    across their grids); --serve-mode streams runs each request on its own
+    stream (the per-instance loop) for comparison."""
     from codesthesis_dir_gb300 import lib, serve
     lib.load()
     lo, hi = (int(x) for x in args.serve_steps.split(","))
     reqs = serve.sweep_requests(n=args.requests, rate=50.0, seed=0, steps=(lo, hi))
     out, res_by = {}, {}
     with ClockSampler() as clk:
-        for name, prec in (("fp64", lib.PRB_FP64), ("mixed", lib.PRB_MIXED)):
-            srv = serve.Server(budget_bytes=120e9, max_active=args.max_active, chunk=16, precision=prec)
+        for name, prec in (("mixed", lib.PRB_MIXED), ("fp64", lib.PRB_FP64)):
+            if args.serve_mode == "gang":
+                srv = serve.GangServer(budget_bytes=120e9, max_active=args.max_active, chunk=args.serve_chunk,
+                                       precision=prec)
+            else:
+                srv = serve.Server(budget_bytes=120e9, max_active=args.max_active, chunk=16, precision=prec)
+            t0 = time.perf_counter()
             res = srv.run(reqs)
             res_by[name] = res
             out[name] = serve.summarize(reqs, res)
+            out[name]["wall_s"] = time.perf_counter() - t0
             out[name]["peak_active"] = srv.peak_active
             out[name]["peak_device_bytes_estimate"] = srv.peak_bytes
+            if args.serve_mode == "gang":
+                out[name]["gang_rebuilds"] = srv.rebuilds
+                out[name]["gang_chunks"] = srv.chunks
     errs = []
     for a, b in zip(res_by["fp64"], res_by["mixed"]):
         if a.status == 0 and b.status == 0 and len(a.nu) and len(b.nu) == len(a.nu):
@@ -635,7 +647,8 @@ def run_serve_workload(args):
         "config": {"workload": "served sweep: %d requests (layer or annulus), grids 65x33..513x257, Ra 1e4-1e8, "
                                "Pr {0.7,1,7}, Ta 1-1e6, %d-%d steps, Poisson arrivals 50/s, 120 GB budget" % (
                                    len(reqs), lo, hi),
-                   "max_active": args.max_active, "chunk_steps": 16},
+                   "mode": args.serve_mode, "max_active": args.max_active,
+                   "chunk_steps": args.serve_chunk if args.serve_mode == "gang" else 16},
         "served": out,
         "mixed_vs_fp64": {"solves_per_s_ratio": m["solves_per_s"] / f["solves_per_s"],
                           "cell_updates_ratio": m["cell_updates_per_s"] / f["cell_updates_per_s"],
@@ -692,9 +705,12 @@ def main():
     ap.add_argument("--fp64-only", action="store_true",
                     help="time only the plain FP64 solve (for profiler captures); prints no JSON line")
     ap.add_argument("--no-layer", action="store_true", help="skip the 2D layer step measurement of the default run")
-    ap.add_argument("--requests", type=int, default=96, help="serve workload: number of requests")
-    ap.add_argument("--serve-steps", default="20,200", help="serve workload: step range lo,hi")
-    ap.add_argument("--max-active", type=int, default=128, help="serve workload: active slots")
+    ap.add_argument("--requests", type=int, default=512, help="serve workload: number of requests")
+    ap.add_argument("--serve-steps", default="500,5000", help="serve workload: step range lo,hi")
+    ap.add_argument("--max-active", type=int, default=1024, help="serve workload: active slots")
+    ap.add_argument("--serve-mode", default="gang", choices=["gang", "streams"],
+                    help="serve workload: one gang per kind (batched across sizes) or one stream per request")
+    ap.add_argument("--serve-chunk", type=int, default=32, help="serve workload: gang steps between re-gangings")
     ap.add_argument("--r3d-fp64-steps", type=int, default=10, help="r3d workload: FP64 comparison steps")
     ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus", "axi", "serve", "r3d"],
                     help="batch: 256 batched Poisson problems (the headline); layer / annulus: the 2D driver step")

@@ -225,9 +225,9 @@ __device__ __forceinline__ void axs_temperature_at(const AxiDev &d, int i, int j
 // vorticity (rotann2.f:268-316, what & 1) and velocity (rotann2.f:324-370,
 // what & 2) on the interior, one thread per point (S: the stretched forms).
 template <bool S>
-__global__ void k_axi_vort_vel(AxiDev d, int what)
+__device__ __forceinline__ void k_axi_vort_vel_body(const AxiDev &d, int what, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     const int ni = d.nr - 1, nj = d.nz - 1;
     if (t >= ni * nj || *d.abort) return;
     const int i = t % ni + 1, j = t / ni + 1;
@@ -273,12 +273,15 @@ __global__ void k_axi_vort_vel(AxiDev d, int what)
     }
 }
 
+template <bool S>
+__global__ void k_axi_vort_vel(AxiDev d, int what) { k_axi_vort_vel_body<S>(d, what, blockIdx.x); }
+
 // temperature, rotann2.f:379-424: rows j = 0 and nz mirror their neighbour
 // and take no Jacobian.
 template <bool S>
-__global__ void k_axi_temperature(AxiDev d)
+__device__ __forceinline__ void k_axi_temperature_body(const AxiDev &d, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     const int ni = d.nr - 1, nj = d.nz + 1;
     if (t >= ni * nj || *d.abort) return;
     const int i = t % ni + 1, j = t / ni;
@@ -309,6 +312,9 @@ __global__ void k_axi_temperature(AxiDev d)
     d.f[GB_A_thetan][AX(i, j)] = (d.cf4 * d.f[GB_A_thetap][AX(i, j)] + arak + B + C + D + E) / d.cf3;
 }
 
+template <bool S>
+__global__ void k_axi_temperature(AxiDev d) { k_axi_temperature_body<S>(d, blockIdx.x); }
+
 // update, rotann2.f:497-539, one thread per point: Thom wall vorticity (the
 // r-walls written last own the corners), v = 0 on the walls, T = 0 / 1 on
 // the inner / outer wall, then the time levels rotate.  The steady-state
@@ -316,9 +322,9 @@ __global__ void k_axi_temperature(AxiDev d)
 // S: the stretched grid's wall spacings in the Thom wall vorticity (rcsc.f
 // update, :706-751).
 template <bool S>
-__global__ void k_axi_update(AxiDev d)
+__device__ __forceinline__ void k_axi_update_body(const AxiDev &d, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     const int nr = d.nr, nz = d.nz, ld = d.ld;
     if (*d.abort) return;   // uniform over the grid
     const bool live = t < (nr + 1) * (nz + 1);
@@ -377,12 +383,15 @@ __global__ void k_axi_update(AxiDev d)
     }
 }
 
+template <bool S>
+__global__ void k_axi_update(AxiDev d) { k_axi_update_body<S>(d, blockIdx.x); }
+
 // heat, rotann2.f:468-487: the per-row terms in parallel, summed by one
 // thread in the reference's order.
 // S: the five-point one-sided weights of the stretched grid and the
 // trapezoid rule on its z positions.
 template <bool S>
-__global__ void k_axi_heat(AxiDev d)
+__device__ __forceinline__ void k_axi_heat_body(const AxiDev &d, int bidx)
 {
     extern __shared__ double sh[];
     if (*d.abort == 1) return;
@@ -412,11 +421,14 @@ __global__ void k_axi_heat(AxiDev d)
     }
 }
 
+template <bool S>
+__global__ void k_axi_heat(AxiDev d) { k_axi_heat_body<S>(d, blockIdx.x); }
+
 // Per-step bookkeeping: Nu and sweeps into the history, the steady-state
 // test (REAL*4 threshold 1e-6, rotann2.f:191) and its reset.
-__global__ void k_axi_record(AxiDev d)
+__device__ __forceinline__ void k_axi_record_body(const AxiDev &d, int bidx)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (threadIdx.x != 0 || bidx != 0) return;
     if (*d.abort) return;
     const int s = *d.step_index;
     if (s < d.hist_cap) {
@@ -430,6 +442,8 @@ __global__ void k_axi_record(AxiDev d)
     if (e1 < tol && e2 < tol && e3 < tol) *d.abort = 2;
     d.errmax[0] = d.errmax[1] = d.errmax[2] = 0ull;
 }
+
+__global__ void k_axi_record(AxiDev d) { k_axi_record_body(d, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // Streamfunction multigrid (rotann2.f:543-854)
@@ -615,7 +629,7 @@ __device__ void axi_finer(const AxiDev &d, int klev)
 }
 
 // poisson (rotann2.f:598-666): phi from omegn.
-__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve(AxiDev d)
+__device__ __forceinline__ void k_axi_mg_solve_body(const AxiDev &d, int bidx)
 {
     __shared__ double s_red[33];
     if (*d.abort) return;
@@ -664,6 +678,8 @@ __global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve(AxiDev d)
         if (status == GB_NAN) *d.abort = 1;
     }
 }
+
+__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve(AxiDev d) { k_axi_mg_solve_body(d, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP64 defect correction around one FP32 V-cycle of the
@@ -847,7 +863,7 @@ __device__ void axi_finer32(const AxiDev &d, int klev)
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve_mixed(AxiDev d)
+__device__ __forceinline__ void k_axi_mg_solve_mixed_body(const AxiDev &d, int bidx)
 {
     __shared__ double s_red[33];
     if (*d.abort) return;
@@ -918,6 +934,8 @@ __global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve_mixed(AxiDev d)
         if (status == GB_NAN) *d.abort = 1;
     }
 }
+
+__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve_mixed(AxiDev d) { k_axi_mg_solve_mixed_body(d, blockIdx.x); }
 
 // FP32 copies of rval and the factors (pivots as reciprocals).
 __global__ void k_axi_factors32(AxiDev d)
@@ -1495,4 +1513,186 @@ extern "C" int gb_axi_step(gb_axi *h, int nsteps, double *nu, int *sweeps, int *
     if (st == GB_OK) st = gb_axi_run_enqueue(h, nsteps);
     if (st != GB_OK) return st;
     return gb_axi_run_end(h, nsteps, nu, sweeps, steps_done);
+}
+
+// ---------------------------------------------------------------------------
+// Gangs of annulus instances of different grid sizes stepped together (as
+// the PRB gangs in prb.cu): each phase of a step is one launch over all
+// members' blocks, the streamfunction solves one launch of one block per
+// member; every member runs its own kernel bodies, so its results are
+// bit-identical to stepping it alone.  A member whose step index reaches
+// its step count sets its abort flag to GB_RUN_DONE.
+// ---------------------------------------------------------------------------
+enum AxiGangPhase { AG_VV, AG_T, AG_MG, AG_UPD, AG_HEAT, AG_REC, AG_COUNT };
+
+struct AxiGangTab {
+    const AxiDev *dev;    // [n]
+    const int *off;       // [AG_COUNT][n + 1]
+    const int *limit;     // [n]
+    int n;
+};
+
+__device__ __forceinline__ int axi_gang_member(const int *off, int n, int b)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int PH>
+__global__ void k_axi_gang(AxiGangTab g)
+{
+    const int *off = g.off + (size_t)PH * (g.n + 1);
+    const int m = axi_gang_member(off, g.n, blockIdx.x);
+    const AxiDev &d = g.dev[m];
+    const int b = blockIdx.x - off[m];
+    switch (PH) {
+    case AG_VV: k_axi_vort_vel_body<false>(d, 3, b); break;
+    case AG_T: k_axi_temperature_body<false>(d, b); break;
+    case AG_UPD: k_axi_update_body<false>(d, b); break;
+    case AG_HEAT: k_axi_heat_body<false>(d, b); break;
+    case AG_REC:
+        k_axi_record_body(d, b);
+        if (threadIdx.x == 0 && b == 0 && *d.abort == 0 && *d.step_index >= g.limit[m]) *d.abort = GB_RUN_DONE;
+        break;
+    default: break;
+    }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(AXI_THREADS) k_axi_gang_mg(AxiGangTab g)
+{
+    const AxiDev &d = g.dev[blockIdx.x];
+    if (MIXED) k_axi_mg_solve_mixed_body(d, 0);
+    else k_axi_mg_solve_body(d, 0);
+}
+
+struct gb_axi_gang {
+    int n = 0, mixed = 0;
+    AxiDev *d_dev = nullptr;
+    int *d_off = nullptr, *d_limit = nullptr;
+    int blocks[AG_COUNT], threads[AG_COUNT];
+    size_t heat_smem = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+};
+
+extern "C" int gb_axi_gang_destroy(gb_axi_gang *g)
+{
+    if (!g) return GB_OK;
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    cudaFree(g->d_dev);
+    cudaFree(g->d_off);
+    cudaFree(g->d_limit);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return GB_OK;
+}
+
+extern "C" int gb_axi_gang_create(gb_axi *const *members, const int *nsteps_total, int n, gb_axi_gang **out)
+{
+    if (!members || !nsteps_total || n < 1 || !out) {
+        gb_set_error("gb_axi_gang_create: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    *out = nullptr;
+    const int mixed = members[0]->p.precision == GB_PRB_MIXED;
+    for (int q = 0; q < n; ++q) {
+        const gb_axi *h = members[q];
+        if (!h || h->dev.stretched || (h->p.precision == GB_PRB_MIXED) != (mixed != 0) || nsteps_total[q] < 0 ||
+            nsteps_total[q] > h->hist_cap) {
+            gb_set_error("gb_axi_gang_create: member %d must be a uniform-grid instance of the gang's precision, after "
+                         "gb_axi_run_begin with at least its step count", q);
+            return GB_ERR_INVALID;
+        }
+    }
+    gb_axi_gang *g = new gb_axi_gang();
+    g->n = n;
+    g->mixed = mixed;
+    const int tpb[AG_COUNT] = {AXI_TPB, AXI_TPB, AXI_THREADS, AXI_TPB, 256, 32};
+    std::vector<int> off((size_t)AG_COUNT * (n + 1));
+    std::vector<AxiDev> devs(n);
+    for (int ph = 0; ph < AG_COUNT; ++ph) {
+        g->threads[ph] = tpb[ph];
+        g->blocks[ph] = 0;
+    }
+    for (int q = 0; q < n; ++q) {
+        gb_axi *h = members[q];
+        axi_scalars(h);
+        devs[q] = h->dev;
+        const size_t nr = h->dev.nr, nz = h->dev.nz;
+        const int nb[AG_COUNT] = {(int)gb_ceil_div((nr - 1) * (nz - 1), AXI_TPB), (int)gb_ceil_div((nr - 1) * (nz + 1), AXI_TPB),
+                                  1, (int)gb_ceil_div((nr + 1) * (nz + 1), AXI_TPB), 1, 1};
+        for (int ph = 0; ph < AG_COUNT; ++ph) {
+            off[(size_t)ph * (n + 1) + q] = g->blocks[ph];
+            g->blocks[ph] += nb[ph];
+        }
+        g->heat_smem = std::max(g->heat_smem, sizeof(double) * (nz + 1));
+    }
+    for (int ph = 0; ph < AG_COUNT; ++ph) off[(size_t)ph * (n + 1) + n] = g->blocks[ph];
+#define GTRY(x)                                                                   \
+    do {                                                                          \
+        cudaError_t _e = (x);                                                     \
+        if (_e != cudaSuccess) {                                                  \
+            gb_set_error("gb_axi_gang_create: %s: %s", #x, cudaGetErrorString(_e)); \
+            gb_axi_gang_destroy(g);                                               \
+            return GB_ERR_CUDA;                                                   \
+        }                                                                         \
+    } while (0)
+    GTRY(cudaMalloc(&g->d_dev, sizeof(AxiDev) * n));
+    GTRY(cudaMalloc(&g->d_off, sizeof(int) * off.size()));
+    GTRY(cudaMalloc(&g->d_limit, sizeof(int) * n));
+    GTRY(cudaMemcpy(g->d_dev, devs.data(), sizeof(AxiDev) * n, cudaMemcpyHostToDevice));
+    GTRY(cudaMemcpy(g->d_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    GTRY(cudaMemcpy(g->d_limit, nsteps_total, sizeof(int) * n, cudaMemcpyHostToDevice));
+    for (int q = 0; q < n; ++q) GTRY(cudaStreamSynchronize(members[q]->stream));
+    GTRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    GTRY(cudaFuncSetAttribute(k_axi_gang_mg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AX32_SMEM_BYTES));
+    if (g->heat_smem > 48 * 1024)
+        GTRY(cudaFuncSetAttribute(k_axi_gang<AG_HEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g->heat_smem));
+#undef GTRY
+    *out = g;
+    return GB_OK;
+}
+
+// Queues nsteps steps of every member (one CUDA graph launch per step) on
+// `stream` (NULL: the gang's own).
+extern "C" int gb_axi_gang_enqueue(gb_axi_gang *g, int nsteps, void *stream)
+{
+    if (!g || nsteps < 0) { gb_set_error("gb_axi_gang_enqueue: invalid argument"); return GB_ERR_INVALID; }
+    cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+    if (!g->graph) {
+        AxiGangTab t{g->d_dev, g->d_off, g->d_limit, g->n};
+        cudaGraph_t gr;
+        cudaStream_t cs = g->stream;
+        GB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        k_axi_gang<AG_VV><<<g->blocks[AG_VV], g->threads[AG_VV], 0, cs>>>(t);
+        k_axi_gang<AG_T><<<g->blocks[AG_T], g->threads[AG_T], 0, cs>>>(t);
+        if (g->mixed) k_axi_gang_mg<true><<<g->n, AXI_THREADS, AX32_SMEM_BYTES, cs>>>(t);
+        else k_axi_gang_mg<false><<<g->n, AXI_THREADS, 0, cs>>>(t);
+        k_axi_gang<AG_UPD><<<g->blocks[AG_UPD], g->threads[AG_UPD], 0, cs>>>(t);
+        k_axi_gang<AG_HEAT><<<g->blocks[AG_HEAT], g->threads[AG_HEAT], g->heat_smem, cs>>>(t);
+        k_axi_gang<AG_REC><<<g->blocks[AG_REC], g->threads[AG_REC], 0, cs>>>(t);
+        GB_CUDA_TRY(cudaStreamEndCapture(cs, &gr));
+        GB_CUDA_TRY(cudaGraphInstantiate(&g->graph, gr, 0));
+        cudaGraphDestroy(gr);
+    }
+    for (int k = 0; k < nsteps; ++k) GB_CUDA_TRY(cudaGraphLaunch(g->graph, s));
+    return GB_OK;
+}
+
+extern "C" void *gb_axi_gang_stream(gb_axi_gang *g) { return g ? (void *)g->stream : nullptr; }
+
+extern "C" int gb_axi_gang_query(gb_axi_gang *g)
+{
+    if (!g) return -GB_ERR_INVALID;
+    const cudaError_t e = cudaStreamQuery(g->stream);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) { cudaGetLastError(); return 0; }
+    gb_set_error("gb_axi_gang_query: %s", cudaGetErrorString(e));
+    return -GB_ERR_CUDA;
 }

@@ -17,6 +17,11 @@
         }                                                                        \
     } while (0)
 
+// Value of an instance's abort flag once a gang run has taken all of its
+// steps (gb_prb_gang_*, gb_axi_gang_*): the instance's kernels skip their
+// work from then on, and its run_end reports success.
+#define GB_RUN_DONE 4
+
 // Records the last error message (thread-local) returned by gb_last_error().
 void gb_set_error(const char *fmt, ...);
 

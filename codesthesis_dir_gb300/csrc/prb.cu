@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "banded.cuh"
 #include "gbcommon.cuh"
@@ -57,9 +58,9 @@ __global__ void k_transport_factors(int nr, int np, double *fac_r1, double *fac_
 
 // Cr (tdma along r) -> A and thr at C points (tdma along r) -> An, one thread
 // per column k.  PRB:810-830 and PRB:854-880.
-__global__ void k_cvort_deriv_r(PrbDev d)
+__device__ __forceinline__ void k_cvort_deriv_r_body(const PrbDev &d, int bidx)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = bidx * blockDim.x + threadIdx.x;
     if (k > d.np || *d.abort) return;
     const int ld = d.ld, nr = d.nr, np = d.np;
     const double dri = d.dri;
@@ -91,11 +92,13 @@ __global__ void k_cvort_deriv_r(PrbDev d)
     apply_tdma_rhs(d.fac_r1, nr - 1, d.f[GB_F_An] + GIX(1, k, ld), 1, rhsT);
 }
 
+__global__ void k_cvort_deriv_r(PrbDev d) { k_cvort_deriv_r_body(d, blockIdx.x); }
+
 // Ch (periodic tdma along x) -> B and thh at C points -> Bn, one thread per
 // row i = 1..nr-1.  PRB:833-851 and PRB:882-897.
-__global__ void k_cvort_deriv_x(PrbDev d)
+__device__ __forceinline__ void k_cvort_deriv_x_body(const PrbDev &d, int bidx)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int i = bidx * blockDim.x + threadIdx.x + 1;
     if (i > d.nr - 1 || *d.abort) return;
     const int ld = d.ld, np = d.np;
     const double dpi = d.dpi;
@@ -112,13 +115,15 @@ __global__ void k_cvort_deriv_x(PrbDev d)
     apply_ptdma_rhs(d.fac_x, np + 1, d.f[GB_F_Bn] + GIX(i, 0, ld), ld, rhsT);
 }
 
+__global__ void k_cvort_deriv_x(PrbDev d) { k_cvort_deriv_x_body(d, blockIdx.x); }
+
 // Vorticity update, PRB:706-776 (first) / PRB:900-982 (leapfrog).  Annulus
 // (velvor2dnewsch3.4.f:710-786 / :911-993): radius r = r0 + i dr, the Cra/r
 // term, 0.5*Cp in the leapfrog RHS1 and the rotational buoyancy in RHS2.
 // Oblique gravity (mpkoks.f): RHS2 = -Ra thr 0.707106781 with thr = An.
-__global__ void k_cvort_update(PrbDev d, int first)
+__device__ __forceinline__ void k_cvort_update_body(const PrbDev &d, int first, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     const int nrow = d.nr - 1;
     if (t >= nrow * (d.np + 1) || *d.abort) return;
     const int i = t % nrow + 1, k = t / nrow;
@@ -170,12 +175,14 @@ __global__ void k_cvort_update(PrbDev d, int first)
     if (!first) d.f[GB_F_Ap][GIX(i, k, ld)] = cn;
 }
 
+__global__ void k_cvort_update(PrbDev d, int first) { k_cvort_update_body(d, first, blockIdx.x); }
+
 // Robert filter X += gamma (Xn - 2X + Xp) on rows 1..imax, gamma = 0.02
 // (PRB:1041-1045, PRB:1435-1440) or 0.05 in the annulus
 // (velvor2dnewsch3.4.f:1055, :1454).
-__global__ void k_robert(PrbDev d, int fx, int fxn, int fxp, int imax)
+__device__ __forceinline__ void k_robert_body(const PrbDev &d, int fx, int fxn, int fxp, int imax, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     if (t >= imax * (d.np + 1) || *d.abort) return;
     const int i = t % imax + 1, k = t / imax;
     const size_t c = GIX(i, k, d.ld);
@@ -184,11 +191,13 @@ __global__ void k_robert(PrbDev d, int fx, int fxn, int fxp, int imax)
     X[c] = X[c] + gamma * (d.f[fxn][c] - 2.0 * X[c] + d.f[fxp][c]);
 }
 
+__global__ void k_robert(PrbDev d, int fx, int fxn, int fxp, int imax) { k_robert_body(d, fx, fxn, fxp, imax, blockIdx.x); }
+
 // thr (tdma along r, third-order wall rows) -> A, one thread per column k
 // (PRB:1244-1268).
-__global__ void k_temp_deriv_r(PrbDev d)
+__device__ __forceinline__ void k_temp_deriv_r_body(const PrbDev &d, int bidx)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = bidx * blockDim.x + threadIdx.x;
     if (k > d.np || *d.abort) return;
     const int ld = d.ld, nr = d.nr;
     const double dri = d.dri;
@@ -206,10 +215,12 @@ __global__ void k_temp_deriv_r(PrbDev d)
     apply_tdma_rhs(d.fac_rT, nr, d.f[GB_F_A] + GIX(1, k, ld), 1, rhs);
 }
 
+__global__ void k_temp_deriv_r(PrbDev d) { k_temp_deriv_r_body(d, blockIdx.x); }
+
 // thh (periodic tdma along x) -> B, one thread per row i = 1..nr (PRB:1271-1289).
-__global__ void k_temp_deriv_x(PrbDev d)
+__device__ __forceinline__ void k_temp_deriv_x_body(const PrbDev &d, int bidx)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int i = bidx * blockDim.x + threadIdx.x + 1;
     if (i > d.nr || *d.abort) return;
     const int ld = d.ld, np = d.np;
     const double dpi = d.dpi;
@@ -221,12 +232,14 @@ __global__ void k_temp_deriv_x(PrbDev d)
     apply_ptdma_rhs(d.fac_x, np + 1, d.f[GB_F_B] + GIX(i, 0, ld), ld, rhs);
 }
 
+__global__ void k_temp_deriv_x(PrbDev d) { k_temp_deriv_x_body(d, blockIdx.x); }
+
 // Temperature update, PRB:1142-1207 (first) / PRB:1292-1377 (Dufort-Frankel).
 // Annulus (velvor2dnewsch3.4.f:1140-1223 / :1308-1393): cell-centre radius
 // r = r0 + (i-1/2) dr and the thra/r term.
-__global__ void k_temp_update(PrbDev d, int first)
+__device__ __forceinline__ void k_temp_update_body(const PrbDev &d, int first, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     const int nr = d.nr;
     if (t >= nr * (d.np + 1) || *d.abort) return;
     const int i = t % nr + 1, k = t / nr;
@@ -282,9 +295,11 @@ __global__ void k_temp_update(PrbDev d, int first)
     if (!first) d.f[GB_F_Ap][GIX(i, k, ld)] = tn;
 }
 
+__global__ void k_temp_update(PrbDev d, int first) { k_temp_update_body(d, first, blockIdx.x); }
+
 // Wall heat fluxes, PRB:1452-1500.  The per-column five-point derivatives are
 // formed in parallel; one thread then sums them in the reference's order.
-__global__ void k_heat(PrbDev d, int k0, int k1)
+__device__ __forceinline__ void k_heat_body(const PrbDev &d, int k0, int k1, int bidx)
 {
     extern __shared__ double sh[];
     if (*d.abort) return;
@@ -313,12 +328,14 @@ __global__ void k_heat(PrbDev d, int k0, int k1)
     }
 }
 
+__global__ void k_heat(PrbDev d, int k0, int k1) { k_heat_body(d, k0, k1, blockIdx.x); }
+
 // rhsv (PRB:1629-1676) and rhsu (PRB:1679-1721) in one pass; the annulus
 // adds the Cn/r terms of velvor2dnewsch3.4.f:1666-1686 and divides the u
 // source by the face radius (:1714-1730).
-__global__ void k_rhs(PrbDev d, int do_v, int do_u)
+__device__ __forceinline__ void k_rhs_body(const PrbDev &d, int do_v, int do_u, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     const int nr = d.nr, np = d.np, ld = d.ld;
     if (t >= nr * (np + 1) || *d.abort) return;
     const int i = t % nr + 1, k = t / nr;
@@ -352,6 +369,8 @@ __global__ void k_rhs(PrbDev d, int do_v, int do_u)
         d.f[GB_F_urh][GIX(i, k, ld)] = -Ch / r;
     }
 }
+
+__global__ void k_rhs(PrbDev d, int do_v, int do_u) { k_rhs_body(d, do_v, do_u, blockIdx.x); }
 
 // update, PRB:1557-1626.  Each thread owns one (i,k) of rows 0..nr+1; the
 // wall values it writes are only read back by the same thread.
@@ -404,9 +423,9 @@ __device__ __forceinline__ void prb_diag_point(const PrbDev &d, int i, size_t c,
 // (rows 1..nr-1; r = 1 in the layer, r0 + (i - 1/2) dr in the annulus) into
 // the step's history slot.  A NaN never wins the reference's comparison.
 template <bool DIAG>
-__global__ void k_update(PrbDev d)
+__device__ __forceinline__ void k_update_body(const PrbDev &d, int bidx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = bidx * blockDim.x + threadIdx.x;
     const int nr = d.nr, np = d.np, ld = d.ld;
     if (*d.abort) return;   // uniform across the grid
     double cu = 0.0, cv = 0.0;
@@ -447,6 +466,9 @@ __global__ void k_update(PrbDev d)
     if (DIAG) prb_cfl_reduce(d, cu, cv);   // every lane of every warp
 }
 
+template <bool DIAG>
+__global__ void k_update(PrbDev d) { k_update_body<DIAG>(d, blockIdx.x); }
+
 // The diagnostics alone, after the tank's and the cavity's update: the same
 // running means and CFL scans over the same rows and columns k = 0..np
 // (velvor2dhorconvtank.f:424-479, velvor2ddvdbenchmark.f:434-486).
@@ -470,9 +492,9 @@ __global__ void k_prb_diag(PrbDev d)
 // the annulus (velvor2dnewsch3.4.f:386-387).
 // swap: the tank's first step stores 2 trans2 in httrans and leaves httrans2
 // at zero (velvor2dhorconvtank.f:197-198).
-__global__ void k_record(PrbDev d, double c1, double c2, double div, int swap)
+__device__ __forceinline__ void k_record_body(const PrbDev &d, double c1, double c2, double div, int swap, int bidx)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (threadIdx.x != 0 || bidx != 0) return;
     const int s = *d.step_index;
     if (s < d.hist_cap) {
         d.nu_hist[2 * s + 0] = swap ? d.heat[1] * c2 / div : d.heat[0] * c1 / div;
@@ -485,6 +507,8 @@ __global__ void k_record(PrbDev d, double c1, double c2, double div, int swap)
         if (d.diag_kt) *d.diag_kt += 1;
     }
 }
+
+__global__ void k_record(PrbDev d, double c1, double c2, double div, int swap) { k_record_body(d, c1, c2, div, swap, blockIdx.x); }
 
 __global__ void k_prb_set_kt(int *kt, int value) { *kt = value; }
 
@@ -1061,7 +1085,7 @@ extern "C" int gb_prb_run_end(gb_prb *h, int nsteps, double *nu, int *sweeps, in
     if (sweeps) memcpy(sweeps, swh.data(), sizeof(int) * 2 * nsteps);
     h->steps_done = info[0];
     if (steps_done) *steps_done = info[0];
-    if (info[1]) {
+    if (info[1] && info[1] != GB_RUN_DONE) {
         gb_set_error("gb_prb_step: multigrid failed at step %d (status v=%d u=%d)", info[0] + 1, stat[0], stat[2]);
         return stat[0] != GB_OK ? stat[0] : stat[2];
     }
@@ -1180,3 +1204,241 @@ extern "C" int gb_prb_diag_cfl(gb_prb *h, int nsteps, double *cfl)
                                 h->stream));
     return prb_sync(h, "gb_prb_diag_cfl");
 }
+
+// ---------------------------------------------------------------------------
+// Gangs: many device-resident instances of different grid sizes stepped
+// together.  Every phase of a step is one launch over the blocks of all
+// members (a block finds its member in the phase's block-offset table and
+// runs that member's kernel body with its local block index), and the two
+// velocity solves of every member are the blocks of one multigrid launch.
+// Each member runs exactly the kernel bodies of its own step, so its fields,
+// Nusselt numbers and sweep counts are bit-identical to stepping it alone.
+// A member whose step index reaches its step count sets its abort flag to
+// GB_RUN_DONE and takes no further part.
+// ---------------------------------------------------------------------------
+enum GangPhase { GP_CDR, GP_CDX, GP_CUPD, GP_CROB, GP_TDR, GP_TDX, GP_TUPD, GP_TROB, GP_HEAT, GP_RHS, GP_UPD, GP_REC,
+                 GP_COUNT };
+
+struct GangRec {
+    double c1, c2, div;   // Nusselt scalings of k_record
+};
+
+struct GangTab {
+    const PrbDev *dev;    // [n]
+    const int *off;       // [GP_COUNT][n + 1]: first block of each member in each phase's launch
+    const GangRec *rec;   // [n]
+    const int *limit;     // [n]: the member's total step count of the run
+    int n;
+};
+
+__device__ __forceinline__ int gang_member(const int *off, int n, int b)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int PH>
+__global__ void k_prb_gang(GangTab g)
+{
+    const int *off = g.off + (size_t)PH * (g.n + 1);
+    const int m = gang_member(off, g.n, blockIdx.x);
+    const PrbDev &d = g.dev[m];
+    const int b = blockIdx.x - off[m];
+    switch (PH) {
+    case GP_CDR: k_cvort_deriv_r_body(d, b); break;
+    case GP_CDX: k_cvort_deriv_x_body(d, b); break;
+    case GP_CUPD: k_cvort_update_body(d, 0, b); break;
+    case GP_CROB: k_robert_body(d, GB_F_C, GB_F_Cn, GB_F_Cp, d.nr - 1, b); break;
+    case GP_TDR: k_temp_deriv_r_body(d, b); break;
+    case GP_TDX: k_temp_deriv_x_body(d, b); break;
+    case GP_TUPD: k_temp_update_body(d, 0, b); break;
+    case GP_TROB: k_robert_body(d, GB_F_th, GB_F_thn, GB_F_thp, d.nr, b); break;
+    case GP_HEAT: k_heat_body(d, 1, d.np, b); break;
+    case GP_RHS: k_rhs_body(d, 1, 1, b); break;
+    case GP_UPD: k_update_body<false>(d, b); break;
+    case GP_REC: {
+        const GangRec r = g.rec[m];
+        k_record_body(d, r.c1, r.c2, r.div, 0, b);
+        if (threadIdx.x == 0 && b == 0 && *d.abort == 0 && *d.step_index >= g.limit[m]) *d.abort = GB_RUN_DONE;
+        break;
+    }
+    default: break;
+    }
+}
+
+struct gb_prb_gang {
+    int n = 0, mixed = 0;
+    PrbDev *d_dev = nullptr;
+    int *d_off = nullptr, *d_limit = nullptr;
+    GangRec *d_rec = nullptr;
+    MgEq *d_eqs = nullptr;
+    std::vector<int> blocks;       // [GP_COUNT] total blocks of each phase
+    int threads[GP_COUNT];
+    size_t heat_smem = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    long long launches_per_step = 0;
+};
+
+extern "C" int gb_prb_gang_destroy(gb_prb_gang *g)
+{
+    if (!g) return GB_OK;
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    cudaFree(g->d_dev);
+    cudaFree(g->d_off);
+    cudaFree(g->d_limit);
+    cudaFree(g->d_rec);
+    cudaFree(g->d_eqs);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return GB_OK;
+}
+
+extern "C" int gb_prb_gang_create(gb_prb *const *members, const int *nsteps_total, int n, gb_prb_gang **out)
+{
+    if (!members || !nsteps_total || n < 1 || !out) {
+        gb_set_error("gb_prb_gang_create: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    *out = nullptr;
+    const int mixed = members[0]->p.precision == GB_PRB_MIXED;
+    for (int q = 0; q < n; ++q) {
+        const gb_prb *h = members[q];
+        if (!h || h->dev.tank || h->dev.diag || (h->p.precision == GB_PRB_MIXED) != (mixed != 0) ||
+            nsteps_total[q] < 0 || nsteps_total[q] > h->hist_cap) {
+            gb_set_error("gb_prb_gang_create: member %d must be a layer or annulus instance without diagnostics, of "
+                         "the gang's precision, after gb_prb_run_begin with at least its step count", q);
+            return GB_ERR_INVALID;
+        }
+    }
+    gb_prb_gang *g = new gb_prb_gang();
+    g->n = n;
+    g->mixed = mixed;
+    // block counts per phase and member (the single-instance launch shapes)
+    const int tpb[GP_COUNT] = {64, 64, TPB, TPB, 64, 64, TPB, TPB, 256, TPB, TPB, 32};
+    for (int q = 0; q < GP_COUNT; ++q) g->threads[q] = tpb[q];
+    std::vector<int> off((size_t)GP_COUNT * (n + 1));
+    std::vector<PrbDev> devs(n);
+    std::vector<GangRec> rec(n);
+    std::vector<MgEq> eqs(2 * (size_t)n);
+    g->blocks.assign(GP_COUNT, 0);
+    for (int q = 0; q < n; ++q) {
+        gb_prb *h = members[q];
+        prb_refresh_scalars(h);
+        const PrbDev &d = h->dev;
+        devs[q] = d;
+        const size_t nr = d.nr, np = d.np;
+        const int nb[GP_COUNT] = {(int)gb_ceil_div(np + 1, 64), (int)gb_ceil_div(nr - 1, 64),
+                                  (int)gb_ceil_div((nr - 1) * (np + 1), TPB), (int)gb_ceil_div((nr - 1) * (np + 1), TPB),
+                                  (int)gb_ceil_div(np + 1, 64), (int)gb_ceil_div(nr, 64),
+                                  (int)gb_ceil_div(nr * (np + 1), TPB), (int)gb_ceil_div(nr * (np + 1), TPB), 1,
+                                  (int)gb_ceil_div(nr * (np + 1), TPB), (int)gb_ceil_div((nr + 2) * (np + 1), TPB), 1};
+        for (int ph = 0; ph < GP_COUNT; ++ph) {
+            off[(size_t)ph * (n + 1) + q] = g->blocks[ph];
+            g->blocks[ph] += nb[ph];
+        }
+        g->heat_smem = std::max(g->heat_smem, 2 * (size_t)(np + 1) * sizeof(double));
+        double c1 = h->p.rmax - h->p.r0, c2 = c1, div = h->p.xx;
+        if (h->p.variant == GB_PRB_ANNULUS || h->p.variant == GB_PRB_TAYCOU) {
+            const double L = log(h->p.r0 / h->p.rmax);
+            c1 = -h->p.r0 * L;
+            c2 = -h->p.rmax * L;
+            div = 2.0 * acos(-1.0);
+        }
+        rec[q] = {c1, c2, div};
+        // the member's current equation descriptors (its settings as prb_launch_mg would use them)
+        for (int e = 0; e < 2; ++e) {
+            MgEq E = h->eq_host[e];
+            E.mode = h->p.smoother;
+            E.maxsweeps = h->p.maxsweeps;
+            E.tolcon = h->p.tolcon;
+            E.sor = h->p.sor;
+            eqs[2 * (size_t)q + e] = E;
+        }
+    }
+    for (int ph = 0; ph < GP_COUNT; ++ph) off[(size_t)ph * (n + 1) + n] = g->blocks[ph];
+#define GTRY(x)                                                                   \
+    do {                                                                          \
+        cudaError_t _e = (x);                                                     \
+        if (_e != cudaSuccess) {                                                  \
+            gb_set_error("gb_prb_gang_create: %s: %s", #x, cudaGetErrorString(_e)); \
+            gb_prb_gang_destroy(g);                                               \
+            return GB_ERR_CUDA;                                                   \
+        }                                                                         \
+    } while (0)
+    GTRY(cudaMalloc(&g->d_dev, sizeof(PrbDev) * n));
+    GTRY(cudaMalloc(&g->d_off, sizeof(int) * off.size()));
+    GTRY(cudaMalloc(&g->d_limit, sizeof(int) * n));
+    GTRY(cudaMalloc(&g->d_rec, sizeof(GangRec) * n));
+    GTRY(cudaMalloc(&g->d_eqs, sizeof(MgEq) * eqs.size()));
+    GTRY(cudaMemcpy(g->d_dev, devs.data(), sizeof(PrbDev) * n, cudaMemcpyHostToDevice));
+    GTRY(cudaMemcpy(g->d_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    GTRY(cudaMemcpy(g->d_limit, nsteps_total, sizeof(int) * n, cudaMemcpyHostToDevice));
+    GTRY(cudaMemcpy(g->d_rec, rec.data(), sizeof(GangRec) * n, cudaMemcpyHostToDevice));
+    GTRY(cudaMemcpy(g->d_eqs, eqs.data(), sizeof(MgEq) * eqs.size(), cudaMemcpyHostToDevice));
+    // the members' own queued work (their first steps) finishes before the gang's
+    for (int q = 0; q < n; ++q) GTRY(cudaStreamSynchronize(members[q]->stream));
+    GTRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    if (g->heat_smem > 48 * 1024)
+        GTRY(cudaFuncSetAttribute(k_prb_gang<GP_HEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g->heat_smem));
+#undef GTRY
+    *out = g;
+    return GB_OK;
+}
+
+static void prb_gang_enqueue_step(gb_prb_gang *g, cudaStream_t s)
+{
+    GangTab t{g->d_dev, g->d_off, g->d_rec, g->d_limit, g->n};
+#define GL(PH) k_prb_gang<PH><<<g->blocks[PH], g->threads[PH], PH == GP_HEAT ? g->heat_smem : 0, s>>>(t)
+    GL(GP_CDR);
+    GL(GP_CDX);
+    GL(GP_CUPD);
+    GL(GP_CROB);
+    GL(GP_TDR);
+    GL(GP_TDX);
+    GL(GP_TUPD);
+    GL(GP_TROB);
+    GL(GP_HEAT);
+    GL(GP_RHS);
+    prb_mg_launch_eqs(g->d_eqs, 2 * g->n, g->mixed, s);
+    GL(GP_UPD);
+    GL(GP_REC);
+#undef GL
+    g->launches_per_step = GP_COUNT + 1;
+}
+
+// Queues nsteps leapfrog steps (not the first step of a run) of every
+// member, one CUDA graph launch per step, on `stream` (NULL: the gang's own).
+extern "C" int gb_prb_gang_enqueue(gb_prb_gang *g, int nsteps, void *stream)
+{
+    if (!g || nsteps < 0) { gb_set_error("gb_prb_gang_enqueue: invalid argument"); return GB_ERR_INVALID; }
+    cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+    if (!g->graph) {
+        cudaGraph_t gr;
+        GB_CUDA_TRY(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+        prb_gang_enqueue_step(g, g->stream);
+        GB_CUDA_TRY(cudaStreamEndCapture(g->stream, &gr));
+        GB_CUDA_TRY(cudaGraphInstantiate(&g->graph, gr, 0));
+        cudaGraphDestroy(gr);
+    }
+    for (int k = 0; k < nsteps; ++k) GB_CUDA_TRY(cudaGraphLaunch(g->graph, s));
+    return GB_OK;
+}
+
+extern "C" void *gb_prb_gang_stream(gb_prb_gang *g) { return g ? (void *)g->stream : nullptr; }
+
+extern "C" int gb_prb_gang_query(gb_prb_gang *g)
+{
+    if (!g) return -GB_ERR_INVALID;
+    const cudaError_t e = cudaStreamQuery(g->stream);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) { cudaGetLastError(); return 0; }
+    gb_set_error("gb_prb_gang_query: %s", cudaGetErrorString(e));
+    return -GB_ERR_CUDA;
+}
+extern "C" long long gb_prb_gang_launches_per_step(const gb_prb_gang *g) { return g ? g->launches_per_step : 0; }

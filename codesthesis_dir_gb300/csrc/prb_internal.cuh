@@ -107,6 +107,7 @@ int prb_mg_levels(int nr, int variant);
 int prb_mg_create(gb_prb *h);
 void prb_mg_destroy(gb_prb *h);
 int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s);
+void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, cudaStream_t s);
 int prb_refresh_scalars(gb_prb *h);
 // the tank's transport (tank.cu)
 int tank_launch_cvorticity(gb_prb *h, int first, cudaStream_t s);

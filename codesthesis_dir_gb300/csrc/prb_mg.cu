@@ -281,6 +281,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
     __shared__ double s_red[33];
     int nan1 = 0, nan_c = 0;
     const MgEq &E = eqs[first_eq + blockIdx.x];
+    if (*E.abort == GB_RUN_DONE) return;   // a gang member past its last step (uniform over the block)
     const int ld = E.ld, np = E.np, nlev = E.nlev;
     const int imax = (E.which == 2) ? E.nr + 1 : E.nr;
     const int n1 = E.lev[1].n1;
@@ -673,6 +674,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve_mixed(const MgEq *eqs, 
 {
     __shared__ double s_red[33];
     const MgEq &E = eqs[first_eq + blockIdx.x];
+    if (*E.abort == GB_RUN_DONE) return;   // a gang member past its last step (uniform over the block)
     const MgLevel &L1 = E.lev[1];
     const int ld = E.ld, np = E.np;
     const int imax = (E.which == 2) ? E.nr + 1 : E.nr;
@@ -954,6 +956,15 @@ void prb_mg_destroy(gb_prb *h)
 
 // Refreshes the solve parameters that a caller may change between calls
 // (tolerance, sweep limit, smoother, SOR factor) and launches the solves.
+// The solves of neq equation descriptors (any instances') in one launch,
+// one block each (the gangs' batched multigrid).
+void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, cudaStream_t s)
+{
+    if (neq <= 0) return;
+    if (mixed) k_mg_solve_mixed<<<neq, MG_THREADS, MG32_SMEM_BYTES, s>>>(d_eqs, 0);
+    else k_mg_solve<<<neq, MG_THREADS, 0, s>>>(d_eqs, 0);
+}
+
 int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s)
 {
     bool changed = false;

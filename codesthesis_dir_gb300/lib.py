@@ -214,6 +214,17 @@ SIGNATURES = [
     ("gb_pdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
     ("gb_pdma_batch_noalloc", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong,
                                        C.c_longlong, _vp]),
+    ("gb_prb_gang_create", C.c_int, [C.POINTER(_vp), _ip, C.c_int, C.POINTER(_vp)]),
+    ("gb_prb_gang_enqueue", C.c_int, [_vp, C.c_int, _vp]),
+    ("gb_prb_gang_query", C.c_int, [_vp]),
+    ("gb_prb_gang_stream", _vp, [_vp]),
+    ("gb_prb_gang_launches_per_step", C.c_longlong, [_vp]),
+    ("gb_prb_gang_destroy", C.c_int, [_vp]),
+    ("gb_axi_gang_create", C.c_int, [C.POINTER(_vp), _ip, C.c_int, C.POINTER(_vp)]),
+    ("gb_axi_gang_enqueue", C.c_int, [_vp, C.c_int, _vp]),
+    ("gb_axi_gang_query", C.c_int, [_vp]),
+    ("gb_axi_gang_stream", _vp, [_vp]),
+    ("gb_axi_gang_destroy", C.c_int, [_vp]),
     ("gb_batch_create", C.c_int, [C.c_int, _ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(_vp)]),
     ("gb_batch_create_tuned", C.c_int, [C.c_int, _ip, C.c_int, C.c_double, C.c_int, C.POINTER(BatchTuning),
                                         C.POINTER(_vp)]),

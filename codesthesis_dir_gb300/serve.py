@@ -274,6 +274,161 @@ class Server:
         return [results[r.rid] for r in sorted(requests, key=lambda r: r.rid)]
 
 
+class _Gang:
+    """One gang (gb_prb_gang or gb_axi_gang) over device instances of one
+    kind; rebuilt whenever its membership changes."""
+
+    def __init__(self, kind):
+        L = _L.load()
+        self.kind = kind
+        if kind == LAYER:
+            self._create, self._enqueue, self._query, self._destroy = (
+                L.gb_prb_gang_create, L.gb_prb_gang_enqueue, L.gb_prb_gang_query, L.gb_prb_gang_destroy)
+        else:
+            self._create, self._enqueue, self._query, self._destroy = (
+                L.gb_axi_gang_create, L.gb_axi_gang_enqueue, L.gb_axi_gang_query, L.gb_axi_gang_destroy)
+        self.h = None
+
+    def build(self, members):
+        import ctypes as C
+        self.close()
+        n = len(members)
+        handles = (C.c_void_p * n)(*[m.inst.g._h.value for m in members])
+        totals = (C.c_int * n)(*[m.req.steps for m in members])
+        h = C.c_void_p()
+        _L.check(self._create(handles, totals, n, C.byref(h)), "gang_create")
+        self.h = h
+
+    def enqueue(self, nsteps):
+        _L.check(self._enqueue(self.h, nsteps, None), "gang_enqueue")
+
+    def query(self) -> int:
+        return self._query(self.h)
+
+    def close(self):
+        if self.h is not None and self.h.value:
+            self._destroy(self.h)
+        self.h = None
+
+
+@dataclass
+class _Member:
+    req: Request
+    inst: object
+    admit: float
+    nbytes: int
+    taken: int = 0       # steps the device has run (host accounting, chunk-granular)
+
+
+class GangServer:
+    """Continuous batching across sizes: the active requests of each kind
+    (layer, annulus) form one gang whose every step is a handful of launches
+    over all members, whatever their grids.  Requests are admitted in arrival
+    order while the device-memory budget and the slot cap allow; between
+    chunks of `chunk` steps the server retires the members that finished,
+    admits arrivals and rebuilds the gang; a layer request's first step
+    (the forward step) runs on its own stream before it joins.  Each member
+    runs its own kernel bodies, so its result is bit-identical to the same
+    request served alone."""
+
+    def __init__(self, budget_bytes: float = 120e9, max_active: int = 1024, chunk: int = 32,
+                 keep_fields: bool = False, clock: Callable[[], float] = time.perf_counter,
+                 sleep: Callable[[float], None] = time.sleep, precision=_L.PRB_FP64, smoother=_L.SMOOTHER_ZEBRA):
+        self.budget = budget_bytes
+        self.max_active = max_active
+        self.chunk = chunk
+        self.keep_fields = keep_fields
+        self.clock = clock
+        self.sleep = sleep
+        self.precision = precision
+        self.smoother = smoother
+        self.peak_active = 0
+        self.peak_bytes = 0
+        self.rebuilds = 0
+        self.chunks = 0
+
+    def run(self, requests: List[Request]) -> List[Result]:
+        pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
+        groups = {LAYER: {"members": [], "joining": [], "gang": _Gang(LAYER), "busy": False},
+                  AXI: {"members": [], "joining": [], "gang": _Gang(AXI), "busy": False}}
+        results: Dict[int, Result] = {}
+        used, n_active = 0, 0
+        t0 = self.clock()
+
+        def finish(m, now):
+            nonlocal used, n_active
+            st, nu, done = m.inst.end(m.req.steps)
+            flds = m.inst.fields() if self.keep_fields else None
+            results[m.req.rid] = Result(m.req.rid, st, m.admit, now, now - m.req.arrival, done, nu, flds)
+            m.inst.close()
+            used -= m.nbytes
+            n_active -= 1
+
+        while pending or any(g["members"] or g["joining"] for g in groups.values()):
+            now = self.clock() - t0
+            progressed = False
+            while pending and pending[0].arrival <= now and n_active < self.max_active:
+                nb = estimate_bytes(pending[0])
+                if used + nb > self.budget and n_active:
+                    break
+                req = pending.pop(0)
+                inst = DeviceInstance(req, self.precision, self.smoother)
+                inst.begin(req.steps)
+                m = _Member(req, inst, now, nb)
+                if req.kind == LAYER and req.steps > 0:
+                    inst.enqueue(1)           # the forward first step, on the instance's own stream
+                    m.taken = 1
+                groups[req.kind]["joining"].append(m)
+                used += nb
+                n_active += 1
+                progressed = True
+            self.peak_active = max(self.peak_active, n_active)
+            self.peak_bytes = max(self.peak_bytes, used)
+            for kind, g in groups.items():
+                if g["busy"]:
+                    q = g["gang"].query()
+                    if q == 0:
+                        continue
+                    if q < 0:
+                        _L.check(-q, "gang_query")
+                    g["busy"] = False
+                    now = self.clock() - t0
+                    for m in g["members"]:
+                        m.taken = min(m.req.steps, m.taken + self.chunk)
+                    done = [m for m in g["members"] if m.taken >= m.req.steps]
+                    for m in done:
+                        finish(m, now)
+                    g["members"] = [m for m in g["members"] if m.taken < m.req.steps]
+                    if done:
+                        g["gang"].close()
+                    progressed = True
+                if g["busy"]:
+                    continue
+                if g["joining"]:
+                    now = self.clock() - t0
+                    for m in [m for m in g["joining"] if m.taken >= m.req.steps]:
+                        finish(m, now)        # a one-step request: its first step was all of it
+                    g["members"] += [m for m in g["joining"] if m.taken < m.req.steps]
+                    g["joining"] = []
+                    g["gang"].close()
+                if g["members"]:
+                    if g["gang"].h is None:
+                        g["gang"].build(g["members"])
+                        self.rebuilds += 1
+                    g["gang"].enqueue(self.chunk)
+                    g["busy"] = True
+                    self.chunks += 1
+                    progressed = True
+            if not progressed:
+                if pending and not any(g["busy"] for g in groups.values()):
+                    self.sleep(max(0.0, min(0.01, pending[0].arrival - (self.clock() - t0))))
+                else:
+                    self.sleep(0.0002)
+        for g in groups.values():
+            g["gang"].close()
+        return [results[r.rid] for r in sorted(requests, key=lambda r: r.rid)]
+
+
 def summarize(requests: List[Request], results: List[Result]) -> dict:
     """solves/s over the makespan (first arrival to last finish), p50 / p99
     time to solution, served cell-updates/s."""

@@ -372,6 +372,45 @@ int gb_axi_run_enqueue(gb_axi *h, int nsteps);
 int gb_axi_run_query(gb_axi *h);
 int gb_axi_run_end(gb_axi *h, int nsteps, double *nu, int *sweeps, int *steps_done);
 
+/* ------------------------------------------------------ instance gangs */
+/* Many device-resident instances of different grid sizes stepped together
+ * (the served parameter sweep's continuous batching).  No counterpart in the
+ * reference: its runs are separate processes chained by job scripts
+ * (monashubuntudir_velvor2dhorconvtankdir/sleeprun.s:1-8).  Every phase of
+ * a step (each transport routine, the heat flux, the right-hand sides, the
+ * update, the bookkeeping) is one launch over the blocks of all members; the
+ * multigrid solves of all members are one launch of one block per equation.
+ * Each member runs exactly its own routines, so its fields, Nusselt history
+ * and sweep counts are bit-identical to stepping it alone.
+ *
+ * Members: instances after gb_*_run_begin(h, total); nsteps_total[q] is
+ * member q's total step count of the run: the gang stops a member whose
+ * step index reaches it (its abort flag becomes 4, which gb_*_run_end
+ * reports as success), so members of different lengths share the gang's
+ * launches.  All members have the same precision.  A PRB gang runs leapfrog
+ * steps only: enqueue each member's first step (kt = 1) on its own stream
+ * first (gb_prb_run_enqueue); layer and annulus variants without
+ * diagnostics.  An AXI gang takes uniform-grid annulus instances and all
+ * of their steps.  Create waits for the members' own streams; enqueue queues
+ * nsteps steps of every member (one CUDA graph launch per step) on `stream`
+ * (NULL: the gang's own stream); query reports 1 when the gang's stream is
+ * idle, 0 while it works, -status on error; collect each member with
+ * gb_*_run_end once the gang is idle.  Destroy the gang (not the members)
+ * when the membership changes. */
+typedef struct gb_prb_gang gb_prb_gang;
+int gb_prb_gang_create(gb_prb *const *members, const int *nsteps_total, int n, gb_prb_gang **out);
+int gb_prb_gang_enqueue(gb_prb_gang *g, int nsteps, void *stream);
+int gb_prb_gang_query(gb_prb_gang *g);
+void *gb_prb_gang_stream(gb_prb_gang *g);
+long long gb_prb_gang_launches_per_step(const gb_prb_gang *g);
+int gb_prb_gang_destroy(gb_prb_gang *g);
+typedef struct gb_axi_gang gb_axi_gang;
+int gb_axi_gang_create(gb_axi *const *members, const int *nsteps_total, int n, gb_axi_gang **out);
+int gb_axi_gang_enqueue(gb_axi_gang *g, int nsteps, void *stream);
+int gb_axi_gang_query(gb_axi_gang *g);
+void *gb_axi_gang_stream(gb_axi_gang *g);
+int gb_axi_gang_destroy(gb_axi_gang *g);
+
 /* ---------------------------------------- 3D rotating annulus (rot3dmg.f) */
 /* The 3D rotating annulus of rot3dmg.f ("R3D"): vorticity components A, B,
  * C and temperature by Dufort-Frankel with hybrid upwinding (:341-873), the

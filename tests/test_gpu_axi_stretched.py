@@ -14,15 +14,16 @@ pytestmark = pytest.mark.gpu
 FIELDS = ["phi", "omegn", "omeg", "omegp", "veln", "vel", "velp", "thetan", "theta", "thetap"]
 
 
-def make(O, nr, nz, mode, factor=1.5, tolcon=1e-9, Ra=1e5, Re=1e2, dt=1e-5, seed=0, amp=1e-2, precision=0):
+def make(O, nr, nz, mode, factor=1.5, tolcon=1e-9, Ra=1e5, Re=1e2, dt=1e-5, seed=0, amp=1e-2, precision=0,
+         maxsweeps=None):
     from codesthesis_dir_gb300 import axi
     hr = grid.spacing_tanh(nr, 0.5, 1.0, factor)
     hz = grid.spacing_tanh(nz, 0.0, 0.5, factor)
-    o = O.OracleAXI(nr, nz, dt, 0.5, 1.0, 0.5, Ra, Re, 1.0, mode=mode, tolcon=tolcon)
+    o = O.OracleAXI(nr, nz, dt, 0.5, 1.0, 0.5, Ra, Re, 1.0, mode=mode, tolcon=tolcon, maxsweeps=maxsweeps)
     o.stretch(hr, hz)
     o.initial(1, seed, amp)
     g = axi.AXI(nr, nz, dt=dt, r0=0.5, rmax=1.0, zmax=0.5, Ra=Ra, Re=Re, Pr=1.0, tolcon=tolcon, smoother=mode,
-                precision=precision, grid=grid.build(hr, hz, 0.5))
+                precision=precision, grid=grid.build(hr, hz, 0.5), maxsweeps=maxsweeps)
     assert g.nlev == o._str.nlev
     for n in FIELDS:
         g.set(n, np.array(o.field(n)))
@@ -41,8 +42,11 @@ def diff(o, g):
 @pytest.mark.parametrize("mode", [0, 1], ids=["lex", "colours"])
 @pytest.mark.parametrize("nr,nz", [(32, 48), (64, 32)])
 def test_routines_from_random_fields(oracle, gblib, mode, nr, nz):
+    """Random fields: the solve may stop at its sweep limit (nr < nz makes
+    rcsc.f's corser clear an interior coarse row, which slows it), and the
+    device must then stop exactly as the oracle does, psi untouched."""
     import ctypes as C
-    o, g = make(oracle, nr, nz, mode)
+    o, g = make(oracle, nr, nz, mode, tolcon=1e-8, maxsweeps=60)
     rng = np.random.default_rng(nr + nz + mode)
     for n in ("omeg", "omegp", "vel", "velp", "phi"):
         a = 0.1 * rng.standard_normal((nr + 1, nz + 1))
@@ -64,7 +68,7 @@ def test_routines_from_random_fields(oracle, gblib, mode, nr, nz):
         sw = C.c_int()
         st = L.orc_axi_poisson(C.byref(o.s), o.s.phi, o.s.omegn, C.byref(sw))
         sw_g = g.poisson()
-        assert st == 0 and sw.value == sw_g, (st, sw.value, sw_g)
+        assert sw.value == sw_g and st in (0, 1), (st, sw.value, sw_g)
         L.orc_axi_update(C.byref(o.s))
         g.update()
         t_o = L.orc_axi_heat(C.byref(o.s))
