@@ -621,7 +621,7 @@ def run_serve_workload(args):
         for name, prec in (("mixed", lib.PRB_MIXED), ("fp64", lib.PRB_FP64)):
             if args.serve_mode == "gang":
                 srv = serve.GangServer(budget_bytes=120e9, max_active=args.max_active, chunk=args.serve_chunk,
-                                       precision=prec)
+                                       precision=prec, group_by=args.serve_group)
             else:
                 srv = serve.Server(budget_bytes=120e9, max_active=args.max_active, chunk=16, precision=prec)
             t0 = time.perf_counter()
@@ -647,7 +647,7 @@ def run_serve_workload(args):
         "config": {"workload": "served sweep: %d requests (layer or annulus), grids 65x33..513x257, Ra 1e4-1e8, "
                                "Pr {0.7,1,7}, Ta 1-1e6, %d-%d steps, Poisson arrivals 50/s, 120 GB budget" % (
                                    len(reqs), lo, hi),
-                   "mode": args.serve_mode, "max_active": args.max_active,
+                   "mode": args.serve_mode, "group_by": args.serve_group, "max_active": args.max_active,
                    "chunk_steps": args.serve_chunk if args.serve_mode == "gang" else 16},
         "served": out,
         "mixed_vs_fp64": {"solves_per_s_ratio": m["solves_per_s"] / f["solves_per_s"],
@@ -711,6 +711,8 @@ def main():
     ap.add_argument("--serve-mode", default="gang", choices=["gang", "streams"],
                     help="serve workload: one gang per kind (batched across sizes) or one stream per request")
     ap.add_argument("--serve-chunk", type=int, default=32, help="serve workload: gang steps between re-gangings")
+    ap.add_argument("--serve-group", default="kind", choices=["kind", "shape"],
+                    help="serve workload: one gang per kind (across sizes) or per kind and grid")
     ap.add_argument("--r3d-fp64-steps", type=int, default=10, help="r3d workload: FP64 comparison steps")
     ap.add_argument("--workload", default="batch", choices=["batch", "layer", "annulus", "axi", "serve", "r3d"],
                     help="batch: 256 batched Poisson problems (the headline); layer / annulus: the 2D driver step")

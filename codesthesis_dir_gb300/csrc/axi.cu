@@ -679,7 +679,7 @@ __device__ __forceinline__ void k_axi_mg_solve_body(const AxiDev &d, int bidx)
     }
 }
 
-__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve(AxiDev d) { k_axi_mg_solve_body(d, blockIdx.x); }
+__global__ void __maxnreg__(128) k_axi_mg_solve(AxiDev d) { k_axi_mg_solve_body(d, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP64 defect correction around one FP32 V-cycle of the
@@ -935,7 +935,7 @@ __device__ __forceinline__ void k_axi_mg_solve_mixed_body(const AxiDev &d, int b
     }
 }
 
-__global__ void __launch_bounds__(AXI_THREADS) k_axi_mg_solve_mixed(AxiDev d) { k_axi_mg_solve_mixed_body(d, blockIdx.x); }
+__global__ void __maxnreg__(128) k_axi_mg_solve_mixed(AxiDev d) { k_axi_mg_solve_mixed_body(d, blockIdx.x); }
 
 // FP32 copies of rval and the factors (pivots as reciprocals).
 __global__ void k_axi_factors32(AxiDev d)
@@ -1563,8 +1563,10 @@ __global__ void k_axi_gang(AxiGangTab g)
     }
 }
 
+// Launched with AXI_THREADS (512) threads; 128 registers keep the solve
+// free of spills (a launch bound of 512 threads left it at 40-64 with spills).
 template <bool MIXED>
-__global__ void __launch_bounds__(AXI_THREADS) k_axi_gang_mg(AxiGangTab g)
+__global__ void __maxnreg__(128) k_axi_gang_mg(AxiGangTab g)
 {
     const AxiDev &d = g.dev[blockIdx.x];
     if (MIXED) k_axi_mg_solve_mixed_body(d, 0);

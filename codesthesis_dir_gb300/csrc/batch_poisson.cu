@@ -362,14 +362,16 @@ __device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, 
 }
 
 // Loads x (or zeros) and f over the tile plus an H halo: warps step
-// through the rows, lanes through the columns (coalesced in global memory;
-// no division and one row base per row).
+// through the rows, each lane through pairs of columns (2P, 2P + 1: even
+// and odd, the tile origin being even), whose points go to the same word
+// of the two colour halves (coalesced in global memory, conflict-free in
+// shared memory; no division and one row base per row).
 template <class T, int H>
 __device__ __forceinline__ void tile_load(T *sx, T *sf, const T *x, const T *f, int ox, int oy, int n,
                                           bool zero_x, bool load_f)
 {
     using LY = TileLayout<T, H>;
-    constexpr int SX = LY::SX, SY = LY::SY;
+    constexpr int SX = LY::SX, SY = LY::SY, NP = SX / 2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int r = warp; r < SY; r += TILE_THREADS / 32) {
         const int gy = oy + r;
@@ -377,26 +379,35 @@ __device__ __forceinline__ void tile_load(T *sx, T *sf, const T *x, const T *f, 
         const size_t base = rin ? (size_t)gy * n : 0;
         const T *xr = x + base, *fr = f + base;
         T *xs = sx + r * LY::SXH, *fs = sf + r * LY::SXH;
-        constexpr int NJ = (SX + 31) / 32;
-        T v[NJ], fv[NJ];
+        const int he = (r & 1) * LY::HALF, ho = ((r + 1) & 1) * LY::HALF;
+        constexpr int NJ = (NP + 31) / 32;
+        T ve[NJ], vo[NJ], fe[NJ], fo[NJ];
         // all loads of the row first, then the shared stores
 #pragma unroll
         for (int j = 0; j < NJ; ++j) {
-            const int c = lane + 32 * j, gx = ox + c;
-            v[j] = (T)0;
-            fv[j] = (T)0;
-            if (c < SX && rin && gx >= 0 && gx < n) {
-                if (load_f) fv[j] = fr[gx];
-                if (!zero_x) v[j] = xr[gx];
+            const int P = lane + 32 * j, gx = ox + 2 * P;
+            ve[j] = vo[j] = fe[j] = fo[j] = (T)0;
+            if (P < NP && rin) {
+                if (gx >= 0 && gx < n) {
+                    if (load_f) fe[j] = fr[gx];
+                    if (!zero_x) ve[j] = xr[gx];
+                }
+                if (gx + 1 >= 0 && gx + 1 < n) {
+                    if (load_f) fo[j] = fr[gx + 1];
+                    if (!zero_x) vo[j] = xr[gx + 1];
+                }
             }
         }
 #pragma unroll
         for (int j = 0; j < NJ; ++j) {
-            const int c = lane + 32 * j;
-            if (c < SX) {
-                const int q = ((r + c) & 1) * LY::HALF + (c >> 1);
-                xs[q] = v[j];
-                if (load_f) fs[q] = fv[j];
+            const int P = lane + 32 * j;
+            if (P < NP) {
+                xs[he + P] = ve[j];
+                xs[ho + P] = vo[j];
+                if (load_f) {
+                    fs[he + P] = fe[j];
+                    fs[ho + P] = fo[j];
+                }
             }
         }
     }
@@ -499,10 +510,13 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
     const T *x = XS<T>(B, e.p, l, src);
     const T *f = FP<T>(B, e.p, l);
     const T *ec = XS<T>(B, e.p, l + 1, 0);
-    // rows by warp, columns by lane.  The row parity is the same for the
-    // whole warp; the column parity alternates between lanes and selects
-    // among the four interpolation forms without a branch.
+    // rows by warp; each lane takes one coarse column and the two fine
+    // columns it feeds (the tile origin ox is even, so fine column 2P is
+    // even and 2P + 1 odd): one coarse load serves both on an even row, two
+    // on an odd row, and the interpolation forms need no parity select.
+    // The sums are those of rotann2.f:821-850 in its order.
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NP = SX / 2;   // coarse columns over the tile and its halo
     for (int r = warp; r < SY; r += TILE_THREADS / 32) {
         const int gy = oy + r;
         const bool rin = gy >= 0 && gy < n, rint = gy >= 1 && gy <= n - 2, yodd = (gy & 1) != 0;
@@ -510,34 +524,39 @@ __device__ void op_prolong(const BatchDev &B, TileEntry e, int l, int src, int d
         const T *xr = x + base, *fr = f + base;
         const T *er = ec + (rint ? (size_t)(gy / 2) * nc : 0);
         T *xs = sx + r * LY::SXH, *fs = sf + r * LY::SXH;
+        const int he = (r & 1) * LY::HALF, ho = ((r + 1) & 1) * LY::HALF;   // colour halves of columns 2P, 2P+1
 #pragma unroll
-        for (int j = 0; j < (SX + 31) / 32; ++j) {
-            const int c = lane + 32 * j, gx = ox + c;
-            const bool xodd = (gx & 1) != 0;
-            const bool g = c < SX && rin && gx >= 0 && gx < n;
-            const bool in = g && rint && gx >= 1 && gx <= n - 2;
-            T val = g ? xr[gx] : (T)0;
-            const T fv = (NU > 0 && g) ? fr[gx] : (T)0;
-            if (in) {
+        for (int j = 0; j < (NP + 31) / 32; ++j) {
+            const int P = lane + 32 * j;
+            if (P >= NP) continue;
+            const int gx = ox + 2 * P;   // even
+            const bool ge = rin && gx >= 0 && gx < n, go = rin && gx + 1 >= 0 && gx + 1 < n;
+            const bool ie = ge && rint && gx >= 1 && gx <= n - 2, io = go && rint && gx + 1 >= 1 && gx + 1 <= n - 2;
+            T ve = ge ? xr[gx] : (T)0, vo = go ? xr[gx + 1] : (T)0;
+            const T fe = (NU > 0 && ge) ? fr[gx] : (T)0, fo = (NU > 0 && go) ? fr[gx + 1] : (T)0;
+            if (ie || io) {
                 const T *ep = er + (gx / 2);
                 const T e00 = ep[0];
-                const T e01 = xodd ? ep[1] : (T)0;
-                T pr;
+                const T e01 = io ? ep[1] : (T)0;
                 if (!yodd) {
-                    pr = xodd ? (e00 + e01) * (T)0.5 : e00;
+                    if (ie) ve = ve + e00;
+                    if (io) vo = vo + (e00 + e01) * (T)0.5;
                 } else {
                     const T e10 = ep[nc];
-                    const T e11 = xodd ? ep[nc + 1] : (T)0;
-                    T t = e00 + e11;
-                    t = t + e10 + e01;
-                    pr = xodd ? t * (T)0.25 : (e00 + e10) * (T)0.5;
+                    const T e11 = io ? ep[nc + 1] : (T)0;
+                    if (ie) ve = ve + (e00 + e10) * (T)0.5;
+                    if (io) {
+                        T t = e00 + e11;
+                        t = t + e10 + e01;
+                        vo = vo + t * (T)0.25;
+                    }
                 }
-                val = val + pr;
             }
-            if (c < SX) {
-                const int q = ((r + c) & 1) * LY::HALF + (c >> 1);
-                xs[q] = val;
-                if (NU > 0) fs[q] = fv;
+            xs[he + P] = ve;
+            xs[ho + P] = vo;
+            if (NU > 0) {
+                fs[he + P] = fe;
+                fs[ho + P] = fo;
             }
         }
     }

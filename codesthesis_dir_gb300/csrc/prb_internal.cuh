@@ -101,6 +101,7 @@ struct gb_prb {
     double *diag_buf = nullptr;   // 4 running means + kt + CFL history (hist_cap slots)
     int diag_cap = 0;
     int steps_done = 0;
+    int mg_spread = 8;            // CTAs per FP64 zebra solve (gb_prb_set_solve_spread): 1 or 8
 };
 
 int prb_mg_levels(int nr, int variant);

@@ -36,11 +36,16 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <cooperative_groups.h>
+
 #include "banded.cuh"
 #include "gbcommon.cuh"
 #include "prb_internal.cuh"
 
+namespace cg = cooperative_groups;
+
 #define MG_THREADS 512
+#define MG_CLUSTER 8   // CTAs sharing one FP64 zebra solve (gb_prb_step's single-instance path)
 
 __device__ __forceinline__ double blk_max(double v, double *s_red)
 {
@@ -57,6 +62,58 @@ __device__ __forceinline__ double blk_max(double v, double *s_red)
     const double r = s_red[32];
     __syncthreads();
     return r;
+}
+
+// The threads that share one equation's solve: one CTA (MgBlock), or the
+// CTAs of a thread-block cluster (MgCluster), which meet at the hardware
+// cluster barrier (arrive with release, wait with acquire at cluster scope:
+// what any CTA of the cluster wrote to global memory before it is seen by
+// every CTA after it) and reduce through distributed shared memory.  A
+// cluster spreads a solve's lines over several SMs' FP64 units; the work of
+// each line is unchanged, so both give the same bits.
+struct MgBlock {
+    static constexpr int C = 1;
+    __device__ static int tid() { return threadIdx.x; }
+    __device__ static int nthr() { return blockDim.x; }
+    __device__ static void sync() { __syncthreads(); }
+};
+template <int CS> struct MgCluster {
+    static constexpr int C = CS;
+    __device__ static int tid() { return (int)cg::this_cluster().block_rank() * blockDim.x + threadIdx.x; }
+    __device__ static int nthr() { return CS * blockDim.x; }
+    __device__ static void sync() { cg::this_cluster().sync(); }
+};
+
+// Maximum (NaNs ignored, as blk_max) and logical or over the group.
+template <class G> __device__ __forceinline__ double grp_max(double v, double *s_red)
+{
+    v = blk_max(v, s_red);
+    if constexpr (G::C > 1) {
+        __shared__ double s_pub;
+        if (threadIdx.x == 0) s_pub = v;
+        G::sync();
+        cg::cluster_group cl = cg::this_cluster();
+        double m = 0.0;
+        for (int r = 0; r < G::C; ++r) m = fmax(m, *cl.map_shared_rank(&s_pub, r));
+        G::sync();   // every CTA has read every slot before the next reduction writes it
+        v = m;
+    }
+    return v;
+}
+template <class G> __device__ __forceinline__ int grp_or(int x)
+{
+    x = __syncthreads_or(x);
+    if constexpr (G::C > 1) {
+        __shared__ int s_or;
+        if (threadIdx.x == 0) s_or = x;
+        G::sync();
+        cg::cluster_group cl = cg::this_cluster();
+        int o = 0;
+        for (int r = 0; r < G::C; ++r) o |= *cl.map_shared_rank(&s_or, r);
+        G::sync();
+        x = o;
+    }
+    return x;
 }
 
 // The level operator applied at (i, k) (the part of relax2/relax3's
@@ -139,6 +196,7 @@ __device__ __forceinline__ void mg_line(const MgEq &E, const MgLevel &L, int k)
 // resmax after every sweep and keeps the last.  Returns the level's
 // residual max norm (NaNs ignored as in the reference's comparison);
 // *nan_out (uniform over the block) is set when a NaN residual appears.
+template <class G>
 __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
 {
     const MgLevel &L = E.lev[klev];
@@ -152,16 +210,16 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
     const int klast = (E.xwall && E.which == 2) ? n3 - 1 : n3;
     for (int irel = 0; irel < nrel; ++irel) {
         if (E.mode == GB_SMOOTHER_LEX) {
-            if (threadIdx.x == 0)
+            if (G::tid() == 0)
                 for (int k = 1; k <= klast; ++k) mg_line(E, L, k);
-            __syncthreads();
+            G::sync();
         } else {
             for (int parity = 1; parity >= 0; --parity) {
-                for (int t = threadIdx.x; t < n3 / 2; t += blockDim.x) {
+                for (int t = G::tid(); t < n3 / 2; t += G::nthr()) {
                     const int k = 2 * t + 2 - parity;
                     if (k <= klast) mg_line(E, L, k);
                 }
-                __syncthreads();
+                G::sync();
             }
         }
     }
@@ -170,7 +228,7 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
     int nan = 0;
     const int nrow = (E.which == 2) ? n1 : n1 - 1;
     const int tot = nrow * klast;
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    for (int idx = G::tid(); idx < tot; idx += G::nthr()) {
         const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
         const int ka = (k == n3) ? (E.xwall ? 0 : 1) : k + 1, km = k - 1;
         double temp = mg_apply_op<double>(psif, ld, i, k, ka, km, E.which, E.polar, n1, hhri, hhpi, hri, rvi, rvq);
@@ -180,20 +238,21 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
         if (temp != temp) nan = 1;
         if (temp > m) m = temp;
     }
-    *nan_out = __syncthreads_or(nan);
-    m = blk_max(m, s_red);
+    *nan_out = grp_or<G>(nan);
+    m = grp_max<G>(m, s_red);
     // trans1(psif -> v)
     const int tp = (n1 + 1) * (n3 + 1);
-    for (int idx = threadIdx.x; idx < tp; idx += blockDim.x) {
+    for (int idx = G::tid(); idx < tp; idx += G::nthr()) {
         const int k = idx / (n1 + 1), i = idx - k * (n1 + 1);
         L.v[idx] = psif[GIX(i, k, ld)];
     }
-    __syncthreads();
+    G::sync();
     return m;
 }
 
 // corser (PRB:2603-2718): full weighting of rc onto the packed coarse
 // right-hand side; psif zeroed over the coarse region.
+template <class G>
 __device__ void mg_corser(const MgEq &E, int klev)
 {
     const int ld = E.ld;
@@ -201,7 +260,7 @@ __device__ void mg_corser(const MgEq &E, int klev)
     const double *rf = E.rc;
     double *psif = E.psif, *fc = E.lev[klev + 1].f;
     const int tot = (n1c + 1) * (n3c + 1);
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    for (int idx = G::tid(); idx < tot; idx += G::nthr()) {
         const int k = idx / (n1c + 1), i = idx - k * (n1c + 1);
         psif[GIX(i, k, ld)] = 0.0;
         double t = 0.0;
@@ -244,11 +303,12 @@ __device__ void mg_corser(const MgEq &E, int klev)
         }
         fc[idx] = t;
     }
-    __syncthreads();
+    G::sync();
 }
 
 // finer (PRB:2721-2803): bilinear prolongation of the coarse correction plus
 // the saved fine solution.
+template <class G>
 __device__ void mg_finer(const MgEq &E, int klev)
 {
     const int ld = E.ld;
@@ -258,7 +318,7 @@ __device__ void mg_finer(const MgEq &E, int klev)
     double *psif = E.psif;
     const int tot = (n1f + 1) * (n3f + 1);
 #define PC(ii, kk) vc[(size_t)(kk) * (n1c + 1) + (ii)]
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    for (int idx = G::tid(); idx < tot; idx += G::nthr()) {
         const int k = idx / (n1f + 1), i = idx - k * (n1f + 1);
         const int i1 = i / 2, k1 = k / 2;
         double p;
@@ -272,15 +332,16 @@ __device__ void mg_finer(const MgEq &E, int klev)
         psif[GIX(i, k, ld)] = p + vf[idx];
     }
 #undef PC
-    __syncthreads();
+    G::sync();
 }
 
 // poisson2 / poisson3 (PRB:1796-1927 / PRB:1930-2059).
-__global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int first_eq)
+template <class G>
+__device__ __forceinline__ void mg_solve(const MgEq *eqs, int first_eq)
 {
     __shared__ double s_red[33];
     int nan1 = 0, nan_c = 0;
-    const MgEq &E = eqs[first_eq + blockIdx.x];
+    const MgEq &E = eqs[first_eq + blockIdx.x / G::C];
     if (*E.abort == GB_RUN_DONE) return;   // a gang member past its last step (uniform over the block)
     const int ld = E.ld, np = E.np, nlev = E.nlev;
     const int imax = (E.which == 2) ? E.nr + 1 : E.nr;
@@ -288,7 +349,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
     double *psif = E.psif, *psi = E.psi, *psip = E.psip;
     const int rows = imax + 1, tot = rows * (np + 1);
     // initial guess 2 psi - psip; level-1 right-hand side and solution packed
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    for (int idx = G::tid(); idx < tot; idx += G::nthr()) {
         const int k = idx / rows, i = idx - k * rows;
         const size_t c = GIX(i, k, ld);
         const double pf = 2.0 * psi[c] - psip[c];
@@ -298,13 +359,13 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
             E.lev[1].v[(size_t)k * (n1 + 1) + i] = pf;
         }
     }
-    __syncthreads();
+    G::sync();
     int status = GB_MAXSWEEPS, sweeps = 0;
     double res1 = 0.0;
     for (int sweep = 1; sweep <= E.maxsweeps; ++sweep) {
         sweeps = sweep;
         if (sweep != 1) {
-            for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            for (int idx = G::tid(); idx < tot; idx += G::nthr()) {
                 const int k = idx / rows, i = idx - k * rows;
                 const size_t c = GIX(i, k, ld);
                 const double pf = psip[c] + E.sor * (psif[c] - psip[c]);
@@ -312,37 +373,37 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
                 psip[c] = pf;
                 if (i <= n1) E.lev[1].v[(size_t)k * (n1 + 1) + i] = pf;
             }
-            __syncthreads();
+            G::sync();
         }
         if (sweep == 1 || nlev == 1) {
-            res1 = mg_relax(E, 1, s_red, &nan1);
-            for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            res1 = mg_relax<G>(E, 1, s_red, &nan1);
+            for (int idx = G::tid(); idx < tot; idx += G::nthr()) {
                 const int k = idx / rows, i = idx - k * rows;
                 psip[GIX(i, k, ld)] = psif[GIX(i, k, ld)];
             }
-            __syncthreads();
+            G::sync();
         }
         if (nlev > 1) {
             for (int l = 1; l <= nlev - 1; ++l) {
-                mg_corser(E, l);
-                mg_relax(E, l + 1, s_red, &nan_c);
+                mg_corser<G>(E, l);
+                mg_relax<G>(E, l + 1, s_red, &nan_c);
             }
             for (int ifmg = 0; ifmg <= nlev - 2; ++ifmg) {
                 for (int l = nlev; l >= nlev - ifmg; --l) {
-                    mg_finer(E, l);
+                    mg_finer<G>(E, l);
                     int nn = 0;
-                    double r = mg_relax(E, l - 1, s_red, &nn);
+                    double r = mg_relax<G>(E, l - 1, s_red, &nn);
                     if (l - 1 == 1) { res1 = r; nan1 = nn; }
                 }
                 for (int l = nlev - ifmg - 1; l <= nlev - 1; ++l) {
-                    mg_corser(E, l);
-                    mg_relax(E, l + 1, s_red, &nan_c);
+                    mg_corser<G>(E, l);
+                    mg_relax<G>(E, l + 1, s_red, &nan_c);
                 }
             }
             for (int l = nlev; l >= 2; --l) {
-                mg_finer(E, l);
+                mg_finer<G>(E, l);
                 int nn = 0;
-                double r = mg_relax(E, l - 1, s_red, &nn);
+                double r = mg_relax<G>(E, l - 1, s_red, &nn);
                 if (l - 1 == 1) { res1 = r; nan1 = nn; }
             }
         }
@@ -355,7 +416,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
             // the tank: v on k = 1..np-1, u on k = 1..np, zero side walls
             // (velvor2dhorconvtank.f:1032-1043, :1129-1140)
             const int kend = (E.which == 2) ? np - 1 : np;
-            for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+            for (int idx = G::tid(); idx < tot; idx += G::nthr()) {
                 const int k = idx / rows, i = idx - k * rows;
                 const size_t c = GIX(i, k, ld);
                 psip[c] = psi[c];
@@ -363,17 +424,34 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_solve(const MgEq *eqs, int fi
                 else psi[c] = psif[c];
             }
             if (E.xwall && E.which == 3)
-                for (int i = threadIdx.x; i <= imax; i += blockDim.x) psi[GIX(i, np + 1, ld)] = 0.0;
+                for (int i = G::tid(); i <= imax; i += G::nthr()) psi[GIX(i, np + 1, ld)] = 0.0;
             status = GB_OK;
             break;
         }
     }
-    if (threadIdx.x == 0) {
+    if (G::tid() == 0) {
         E.status[0] = status;
         E.status[1] = sweeps;
         *E.resmax = res1;
         if (status == GB_NAN || (status == GB_MAXSWEEPS && E.stop_on_max)) *E.abort = 1;
     }
+}
+
+// Launched with MG_THREADS (512) threads per block.  With a launch bound of
+// 512 threads ptxas held the solve to 64 registers and spilled 604 / 1456
+// bytes; allowing 128 (a whole SM's register file per block) removes every
+// spill, and the bound that matters, the SM's FP64 pipe, is the same with
+// one block per SM as with two.
+__global__ void __maxnreg__(128) k_mg_solve(const MgEq *eqs, int first_eq)
+{
+    mg_solve<MgBlock>(eqs, first_eq);
+}
+
+// The same solve with each equation on a cluster of MG_CLUSTER CTAs
+// (launch MG_CLUSTER blocks of MG_THREADS per equation).
+__global__ void __cluster_dims__(MG_CLUSTER, 1, 1) __maxnreg__(128) k_mg_solve_cluster(const MgEq *eqs, int first_eq)
+{
+    mg_solve<MgCluster<MG_CLUSTER>>(eqs, first_eq);
 }
 
 // ---------------------------------------------------------------------------
@@ -670,7 +748,7 @@ __device__ void mg_cycle32(const MgEq &E)
 }
 
 // poisson2 / poisson3 in mixed precision.  psif holds the FP64 iterate.
-__global__ void __launch_bounds__(MG_THREADS) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
+__global__ void __maxnreg__(128) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
 {
     __shared__ double s_red[33];
     const MgEq &E = eqs[first_eq + blockIdx.x];
@@ -980,7 +1058,23 @@ int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s)
     const int n = (do_v ? 1 : 0) + (do_u ? 1 : 0);
     if (n == 0) return GB_OK;
     if (h->p.precision == GB_PRB_MIXED) k_mg_solve_mixed<<<n, MG_THREADS, MG32_SMEM_BYTES, s>>>(h->eq_dev, first);
+    else if (h->mg_spread > 1 && h->p.smoother == GB_SMOOTHER_ZEBRA)
+        k_mg_solve_cluster<<<n * MG_CLUSTER, MG_THREADS, 0, s>>>(h->eq_dev, first);
     else k_mg_solve<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
     h->launches += 1;
+    return GB_OK;
+}
+
+extern "C" int gb_prb_set_solve_spread(gb_prb *h, int ctas)
+{
+    if (!h || (ctas != 1 && ctas != MG_CLUSTER)) {
+        gb_set_error("gb_prb_set_solve_spread: ctas must be 1 or %d", MG_CLUSTER);
+        return GB_ERR_INVALID;
+    }
+    if (h->mg_spread != ctas) {
+        h->mg_spread = ctas;
+        if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+        if (h->graph_exec1) { cudaGraphExecDestroy(h->graph_exec1); h->graph_exec1 = nullptr; }
+    }
     return GB_OK;
 }

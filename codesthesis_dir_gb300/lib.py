@@ -214,6 +214,7 @@ SIGNATURES = [
     ("gb_pdma_batch", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp]),
     ("gb_pdma_batch_noalloc", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_longlong,
                                        C.c_longlong, _vp]),
+    ("gb_prb_set_solve_spread", C.c_int, [_vp, C.c_int]),
     ("gb_prb_gang_create", C.c_int, [C.POINTER(_vp), _ip, C.c_int, C.POINTER(_vp)]),
     ("gb_prb_gang_enqueue", C.c_int, [_vp, C.c_int, _vp]),
     ("gb_prb_gang_query", C.c_int, [_vp]),

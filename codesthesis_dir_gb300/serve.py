@@ -305,6 +305,9 @@ class _Gang:
     def query(self) -> int:
         return self._query(self.h)
 
+    def built(self) -> bool:
+        return self.h is not None
+
     def close(self):
         if self.h is not None and self.h.value:
             self._destroy(self.h)
@@ -333,7 +336,18 @@ class GangServer:
 
     def __init__(self, budget_bytes: float = 120e9, max_active: int = 1024, chunk: int = 32,
                  keep_fields: bool = False, clock: Callable[[], float] = time.perf_counter,
-                 sleep: Callable[[float], None] = time.sleep, precision=_L.PRB_FP64, smoother=_L.SMOOTHER_ZEBRA):
+                 sleep: Callable[[float], None] = time.sleep, precision=_L.PRB_FP64, smoother=_L.SMOOTHER_ZEBRA,
+                 group_by: str = "kind", factory: Optional[Callable[[Request], object]] = None,
+                 gang_factory: Optional[Callable[[str], object]] = None):
+        """group_by: "kind" (one gang per kind, batched across grid sizes:
+        every member steps at the pace of the largest) or "shape" (one gang
+        per kind and grid; the gangs run side by side on their own streams).
+        factory / gang_factory: stand-ins for the device instance and gang
+        (the host logic's tests)."""
+        assert group_by in ("kind", "shape")
+        self.group_by = group_by
+        self.factory = factory or (lambda r: DeviceInstance(r, precision, smoother))
+        self.gang_factory = gang_factory or _Gang
         self.budget = budget_bytes
         self.max_active = max_active
         self.chunk = chunk
@@ -349,8 +363,13 @@ class GangServer:
 
     def run(self, requests: List[Request]) -> List[Result]:
         pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
-        groups = {LAYER: {"members": [], "joining": [], "gang": _Gang(LAYER), "busy": False},
-                  AXI: {"members": [], "joining": [], "gang": _Gang(AXI), "busy": False}}
+        groups: Dict[tuple, dict] = {}
+
+        def group_of(req):
+            key = (req.kind,) if self.group_by == "kind" else (req.kind, req.nx, req.nz)
+            if key not in groups:
+                groups[key] = {"members": [], "joining": [], "gang": self.gang_factory(req.kind), "busy": False}
+            return groups[key]
         results: Dict[int, Result] = {}
         used, n_active = 0, 0
         t0 = self.clock()
@@ -364,7 +383,7 @@ class GangServer:
             used -= m.nbytes
             n_active -= 1
 
-        while pending or any(g["members"] or g["joining"] for g in groups.values()):
+        while pending or any(g["members"] or g["joining"] for g in list(groups.values())):
             now = self.clock() - t0
             progressed = False
             while pending and pending[0].arrival <= now and n_active < self.max_active:
@@ -372,19 +391,19 @@ class GangServer:
                 if used + nb > self.budget and n_active:
                     break
                 req = pending.pop(0)
-                inst = DeviceInstance(req, self.precision, self.smoother)
+                inst = self.factory(req)
                 inst.begin(req.steps)
                 m = _Member(req, inst, now, nb)
                 if req.kind == LAYER and req.steps > 0:
                     inst.enqueue(1)           # the forward first step, on the instance's own stream
                     m.taken = 1
-                groups[req.kind]["joining"].append(m)
+                group_of(req)["joining"].append(m)
                 used += nb
                 n_active += 1
                 progressed = True
             self.peak_active = max(self.peak_active, n_active)
             self.peak_bytes = max(self.peak_bytes, used)
-            for kind, g in groups.items():
+            for g in list(groups.values()):
                 if g["busy"]:
                     q = g["gang"].query()
                     if q == 0:
@@ -412,7 +431,7 @@ class GangServer:
                     g["joining"] = []
                     g["gang"].close()
                 if g["members"]:
-                    if g["gang"].h is None:
+                    if not g["gang"].built():
                         g["gang"].build(g["members"])
                         self.rebuilds += 1
                     g["gang"].enqueue(self.chunk)

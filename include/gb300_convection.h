@@ -208,6 +208,14 @@ int gb_prb_rhsu(gb_prb *h);                         /* PRB:1679-1721 */
  * which = 3: poisson3 on uel/uelp/urh (PRB:1930-2059).
  * Returns GB_OK, GB_MAXSWEEPS or GB_NAN; *sweeps gets the sweep count. */
 int gb_prb_poisson(gb_prb *h, int which, int *sweeps);
+/* CTAs that share one FP64 two-colour solve of this instance: 8 (the
+ * default: the lines of a colour, the residual and the transfers of each
+ * level are spread over a cluster of 8 CTAs that meet at the hardware
+ * cluster barrier and reduce through distributed shared memory, so the
+ * solve uses eight SMs' FP64 units) or 1 (one CTA per equation).  Both give
+ * the same bits; the reference's line order and the mixed solve always use
+ * one CTA.  No counterpart in the reference (its solves are serial). */
+int gb_prb_set_solve_spread(gb_prb *h, int ctas);
 /* update (PRB:1557-1626); *clamps (may be NULL) gets the number of
  * temperatures clamped, each of which the reference reports with
  * 'WARNING! Temp damped'. */

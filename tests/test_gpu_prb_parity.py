@@ -119,3 +119,34 @@ def test_graph_steps_oblique(oracle, P, smoother):
     np.testing.assert_array_equal(np.array(sw_o), sw_g)
     np.testing.assert_array_equal(np.array(nu_o), nu_g)
     assert diff_fields(o, g) == {}
+
+
+@pytest.mark.parametrize("nr,np_", [(64, 128), (32, 64)])
+def test_cluster_spread_solve_equals_one_cta(oracle, P, nr, np_):
+    """The FP64 two-colour solve spread over a cluster of 8 CTAs (the
+    default) gives exactly the bits of the one-CTA solve and of the oracle:
+    fields, Nusselt numbers and sweep counts."""
+    from codesthesis_dir_gb300 import lib
+    L = lib.load()
+    prm = config0_params(nr, np_)
+    o, g8 = make_pair(oracle, P, smoother=1, tolcon=1e-10, **prm)
+    _, g1 = make_pair(oracle, P, smoother=1, tolcon=1e-10, **prm)
+    assert L.gb_prb_set_solve_spread(g1._h, 1) == 0
+    assert L.gb_prb_set_solve_spread(g8._h, 8) == 0
+    assert L.gb_prb_set_solve_spread(g8._h, 3) == lib.GB_ERR_INVALID
+    nsteps = 8
+    nu8, sw8 = g8.step(nsteps)
+    nu1, sw1 = g1.step(nsteps)
+    nu_o, sw_o = [], []
+    for _ in range(nsteps):
+        st, nu, sw = o.step()
+        assert st == 0
+        nu_o.append(nu.copy())
+        sw_o.append(sw.copy())
+    np.testing.assert_array_equal(sw8, sw1)
+    np.testing.assert_array_equal(nu8, nu1)
+    np.testing.assert_array_equal(np.array(sw_o), sw8)
+    np.testing.assert_array_equal(np.array(nu_o), nu8)
+    assert diff_fields(o, g8) == {}
+    for name in ("C", "th", "vel", "uel"):
+        np.testing.assert_array_equal(g8.get(name), g1.get(name))

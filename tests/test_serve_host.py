@@ -87,3 +87,60 @@ def test_sweep_draws():
     assert all((q.Ta == 0.0) == (q.kind == serve.LAYER) for q in reqs)
     assert all(1.0 <= q.Ta <= 1e6 for q in reqs if q.kind == serve.AXI)
     assert all(serve.default_dt(q) > 0 for q in reqs)
+
+
+class FakeGang:
+    """Stands in for gb_*_gang: a chunk of n steps advances every member by
+    n steps, stopping each at its own step count, and takes 1 ms of virtual
+    time per step."""
+    log = []
+
+    def __init__(self, kind, clock):
+        self.kind, self.clock = kind, clock
+        self.members = None
+        self.busy_until = 0.0
+
+    def build(self, members):
+        self.members = list(members)
+        FakeGang.log.append(("build", self.kind, sorted(m.req.rid for m in members), self.clock.t))
+
+    def built(self):
+        return self.members is not None
+
+    def enqueue(self, n):
+        for m in self.members:
+            m.inst.done = min(m.req.steps, m.inst.done + n)
+        self.busy_until = max(self.busy_until, self.clock.t) + 1e-3 * n
+
+    def query(self):
+        return 1 if self.clock.t >= self.busy_until else 0
+
+    def close(self):
+        self.members = None
+
+
+def test_gang_server_host_logic():
+    """Every request gets exactly its steps (the layer's first step on its
+    own, the rest in chunks of its gang), members join and leave only between
+    chunks, gangs hold one kind (or one kind and grid), the budget and slot
+    cap hold, and each result is reported once."""
+    for group_by in ("kind", "shape"):
+        clock = Clock()
+        FakeInstance.log, FakeGang.log = [], []
+        reqs = serve.sweep_requests(n=60, rate=300.0, seed=5, steps=(3, 90), grids=((64, 32), (128, 64)))
+        srv = serve.GangServer(budget_bytes=12 * serve.estimate_bytes(reqs[0]), max_active=9, chunk=8,
+                               factory=lambda r: FakeInstance(r, clock), gang_factory=lambda k: FakeGang(k, clock),
+                               clock=clock.now, sleep=clock.sleep, group_by=group_by)
+        res = srv.run(reqs)
+        assert [r.rid for r in res] == [q.rid for q in reqs]
+        by = {q.rid: q for q in reqs}
+        for r in res:
+            assert r.status == 0 and r.steps_done == by[r.rid].steps
+            assert r.finish >= r.admit >= by[r.rid].arrival
+        assert srv.peak_active <= 9 and srv.peak_bytes <= srv.budget
+        for ev, kind, rids, _ in FakeGang.log:
+            assert {by[i].kind for i in rids} == {kind}
+            if group_by == "shape":
+                assert len({(by[i].nx, by[i].nz) for i in rids}) == 1
+        closes = [e for e in FakeInstance.log if e[0] == "close"]
+        assert sorted(e[1] for e in closes) == sorted(q.rid for q in reqs)
