@@ -452,13 +452,16 @@ def summarize(requests: List[Request], results: List[Result]) -> dict:
     """solves/s over the makespan (first arrival to last finish), p50 / p99
     time to solution, served cell-updates/s."""
     ok = [r for r in results if r.status == 0]
+    by = {q.rid: q for q in requests}
     tts = np.array([r.tts for r in ok]) if ok else np.zeros(1)
     t_first = min(q.arrival for q in requests)
     t_last = max(r.finish for r in results)
     span = max(t_last - t_first, 1e-9)
-    by = {q.rid: q for q in requests}
     cu = sum(by[r.rid].cells() * r.steps_done for r in ok)
-    return {"requests": len(requests), "completed": len(ok), "failed": len(results) - len(ok),
+    failed = [{"rid": r.rid, "status": r.status, "kind": by[r.rid].kind, "grid": [by[r.rid].nx, by[r.rid].nz],
+               "Ra": by[r.rid].Ra, "Pr": by[r.rid].Pr, "Ta": by[r.rid].Ta, "steps_done": r.steps_done,
+               "steps": by[r.rid].steps} for r in results if r.status != 0]
+    return {"requests": len(requests), "completed": len(ok), "failed": len(results) - len(ok), "failures": failed,
             "makespan_s": span, "solves_per_s": len(ok) / span, "cell_updates_per_s": cu / span,
             "tts_p50_s": float(np.percentile(tts, 50)), "tts_p99_s": float(np.percentile(tts, 99)),
             "tts_mean_s": float(np.mean(tts))}
