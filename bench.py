@@ -289,6 +289,72 @@ def _prb_mixed_instance(cfg, smoother):
     return g
 
 
+def prb_latency_model(cfg, precision, warmup=20, reps=5):
+    """Where a 2D driver step's time goes: after `warmup` graph steps, `reps`
+    steps run routine by routine (the reference's loop order, PRB:363-388),
+    each routine timed with CUDA events on the instance's stream.  The step
+    graph runs the v and u solves side by side, so its critical path is the
+    transport routines plus the longer solve; what the graph step takes
+    beyond that is launch and dependency latency between its nodes.  For
+    the FP64 path the solves are timed again from the same right-hand sides
+    on a cluster of 8 CTAs per equation instead of one CTA (both
+    precisions), and the two results compared bit for bit."""
+    import torch
+    from codesthesis_dir_gb300 import lib
+    g = prb_instance(cfg, 1) if precision == 0 else _prb_mixed_instance(cfg, 1)
+    L = lib.load()
+    s = torch.cuda.ExternalStream(L.gb_prb_stream(g._h))
+    g.step(warmup)
+    torch.cuda.synchronize()
+    names = ("cvorticity", "temperature", "heat", "rhsv", "rhsu", "poisson2", "poisson3", "update")
+    tot = {n: 0.0 for n in names}
+    sweeps = {"poisson2": 0, "poisson3": 0}
+    one = {"poisson2": 0.0, "poisson3": 0.0}
+    same = True
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        r = fn()
+        e1.record(s)
+        e1.synchronize()
+        return e0.elapsed_time(e1), r
+
+    for _ in range(reps):
+        for n in names[:5]:
+            tot[n] += timed(getattr(g, n))[0]
+        snap = {n: g.get(n) for n in ("vel", "velp", "uel", "uelp")}
+        for n in ("poisson2", "poisson3"):
+            ms, sw = timed(getattr(g, n))
+            tot[n] += ms
+            sweeps[n] += sw
+        res = {n: g.get(n) for n in ("vel", "uel")}
+        for n, a in snap.items():
+            g.set(n, a)
+        g.set_solve_spread(8)
+        for n in ("poisson2", "poisson3"):
+            one[n] += timed(getattr(g, n))[0]
+        g.set_solve_spread(1)
+        same = same and all(np.array_equal(res[n], g.get(n)) for n in res)
+        tot["update"] += timed(g.update)[0]
+    g.close()
+    ms = {n: tot[n] / reps for n in names}
+    transport = sum(ms[n] for n in names if not n.startswith("poisson"))
+    out = {"routine_ms": ms, "transport_ms": transport,
+           "solve_ms": {"v": ms["poisson2"], "u": ms["poisson3"]},
+           "sweeps_per_solve": {"v": sweeps["poisson2"] / reps, "u": sweeps["poisson3"] / reps},
+           "us_per_sweep": {"v": 1e3 * ms["poisson2"] / max(sweeps["poisson2"] / reps, 1),
+                            "u": 1e3 * ms["poisson3"] / max(sweeps["poisson3"] / reps, 1)},
+           "critical_ms": transport + max(ms["poisson2"], ms["poisson3"]),
+           "solve_share_of_critical": max(ms["poisson2"], ms["poisson3"]) / (
+               transport + max(ms["poisson2"], ms["poisson3"])),
+           "steps_measured": reps, "after_steps": warmup}
+    out["cluster8_solve_ms"] = {"v": one["poisson2"] / reps, "u": one["poisson3"] / reps}
+    out["cluster8_speedup"] = {k: out["solve_ms"][k] / out["cluster8_solve_ms"][k] for k in ("v", "u")}
+    out["cluster8_bits_equal_one_cta"] = bool(same)
+    return out
+
+
 def time_prb_cpu(cfg, smoother, budget_s=3.0, max_steps=200):
     """The oracle (one core: the reference's loop is serial) on the same
     instance for a bounded number of steps."""
@@ -367,6 +433,16 @@ def run_prb_workload(args, cfg):
         "detail": summ,
         "clocks": clk.summary(),
     }
+    if args.workload == "layer":
+        lm = {"mixed": prb_latency_model(cfg, 1), "fp64": prb_latency_model(cfg, 0)}
+        lm["mixed"]["graph_step_ms"] = mx["ms_per_step"]
+        lm["fp64"]["graph_step_ms"] = z["ms_per_step"]
+        for v in lm.values():
+            v["graph_overhead_ms"] = v["graph_step_ms"] - v["critical_ms"]
+        line["roofline"]["bound"] = "latency"
+        line["roofline"]["note"] = ("8 192 cells: HBM is idle; the step is the transport routines plus the longer "
+                                    "of the two side-by-side solves, each a chain of line eliminations")
+        line["roofline"]["latency_model"] = lm
     if "cpu_baseline" in summ:
         line["cpu_baseline"] = summ["cpu_baseline"]
     print(json.dumps(line))
@@ -516,6 +592,7 @@ def time_r3d_gpu(cfg, smoother, steps, warmup, precision=0):
     if warmup:
         nu_w, _ = g.step(warmup)
     torch.cuda.synchronize()
+    g.barrier_counts(reset=True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
     nu, sw = g.step(steps)
@@ -523,11 +600,44 @@ def time_r3d_gpu(cfg, smoother, steps, warmup, precision=0):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     done = len(nu)
+    bars, blocks = g.barrier_counts()
     fields = {n: g.get(n) for n in ("uel", "vel", "wel", "A", "B", "C", "th")}
     g.close()
     cells = cfg["nr"] * cfg["nz"] * cfg["np"]
+    time_r3d_gpu.last_barriers = {"w": bars[0] / max(done, 1), "v": bars[1] / max(done, 1),
+                                  "u": bars[2] / max(done, 1), "blocks": blocks}
     return cells * done / (ms / 1e3), ms / max(done, 1), sw.sum(axis=1).mean() if done else 0.0, \
         np.concatenate([nu_w, nu]), fields
+
+
+def r3d_latency_model(ms_per_step, barriers, threads=256, reps=2000):
+    """Barrier term of the 3D step: grid barriers per step (counted on the
+    device) times the time of one barrier at the solves' launch shapes
+    (measured by a barrier-only cooperative launch).  The w and v solves run
+    side by side on half the blocks each, the u solve after them on all, so
+    the critical path holds max(w, v) half-grid barriers and the u solve's
+    full-grid ones.  What is left of the step is the phases' own work: the
+    line elimination chains, the residual passes and the transfers."""
+    import ctypes as C
+    from codesthesis_dir_gb300 import lib
+    L = lib.load()
+    full = barriers["blocks"]
+    half = max(1, full // 2)
+    us = {}
+    for nb in (half, full):
+        t = C.c_double()
+        lib.check(L.gb_measure_grid_barrier(nb, threads, reps, C.byref(t)), "gb_measure_grid_barrier")
+        us[nb] = t.value
+    crit = max(barriers["w"], barriers["v"]) * us[half] + barriers["u"] * us[full]
+    return {"barriers_per_step": {k: barriers[k] for k in ("w", "v", "u")},
+            "blocks": {"w_v_side_by_side": half, "u": full},
+            "us_per_barrier": {str(half): us[half], str(full): us[full]},
+            "barrier_ms_per_step": crit / 1e3, "step_ms": ms_per_step,
+            "barrier_share": crit / 1e3 / ms_per_step,
+            "rest_ms_per_step": ms_per_step - crit / 1e3,
+            "model": "step = max(w, v) x barrier(half grid) + u x barrier(full grid) + phase work "
+                     "(elimination chains, residual passes, transfers); barrier counts from the device, barrier "
+                     "time from a barrier-only cooperative launch of the same shape"}
 
 
 def r3d_summary(cfg, steps, steps_fp64, warmup, cpu_budget):
@@ -546,6 +656,8 @@ def r3d_summary(cfg, steps, steps_fp64, warmup, cpu_budget):
         out[nm] = {"value": v, "unit": "cell-updates/s", "ms_per_step": ms, "steps": st, "warmup": wu,
                    ("sweeps_per_step" if prec == 0 else "fp32_cycles_per_step"): float(sw),
                    "nu_last": float(nu[-1])}
+        if nm in ("mixed_zebra", "fp64_zebra"):
+            out[nm]["latency_model"] = r3d_latency_model(ms, time_r3d_gpu.last_barriers)
     if "mixed_zebra_short" in runs and "fp64_zebra" in runs:
         nu_m, f_m = runs["mixed_zebra_short"]
         nu_d, f_d = runs["fp64_zebra"]
@@ -571,7 +683,7 @@ def r3d_summary(cfg, steps, steps_fp64, warmup, cpu_budget):
         out["cpu_baseline"] = {"value": cfg["nr"] * cfg["nz"] * cfg["np"] * n / dt, "unit": "cell-updates/s",
                                "cores": 1, "kind": "port",
                                "sample": "%d step(s) of the same instance from the same start, oracle in the "
-                                         "reference's line order, 1 thread, %.1f s" % (n, dt)}
+                                         "reference's line order, 1 thread, %.1f s; %s" % (n, dt, cpu_model())}
     return out
 
 
@@ -594,7 +706,8 @@ def run_r3d_workload(args):
                    "l2": "working set (~120 MB) fits in L2; the solves are phase-latency bound"},
         "roofline": {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
                      "note": "each relaxation phase costs the elimination chain of its longest line plus one grid "
-                             "barrier; HBM and the FP64 pipe are far from busy"},
+                             "barrier; HBM and the FP64 pipe are far from busy",
+                     "latency_model": mx.get("latency_model")},
         "detail": summ, "clocks": clk.summary(),
     }
     if "cpu_baseline" in summ:
@@ -621,7 +734,8 @@ def run_serve_workload(args):
         for name, prec in (("mixed", lib.PRB_MIXED), ("fp64", lib.PRB_FP64)):
             if args.serve_mode == "gang":
                 srv = serve.GangServer(budget_bytes=120e9, max_active=args.max_active, chunk=args.serve_chunk,
-                                       precision=prec, group_by=args.serve_group)
+                                       precision=prec, group_by=args.serve_group,
+                                       solve_spread=args.serve_spread)
             else:
                 srv = serve.Server(budget_bytes=120e9, max_active=args.max_active, chunk=16, precision=prec)
             t0 = time.perf_counter()
@@ -647,7 +761,8 @@ def run_serve_workload(args):
         "config": {"workload": "served sweep: %d requests (layer or annulus), grids 65x33..513x257, Ra 1e4-1e8, "
                                "Pr {0.7,1,7}, Ta 1-1e6, %d-%d steps, Poisson arrivals 50/s, 120 GB budget" % (
                                    len(reqs), lo, hi),
-                   "mode": args.serve_mode, "group_by": args.serve_group, "max_active": args.max_active,
+                   "mode": args.serve_mode, "group_by": args.serve_group, "solve_spread": args.serve_spread,
+                   "max_active": args.max_active,
                    "chunk_steps": args.serve_chunk if args.serve_mode == "gang" else 16},
         "served": out,
         "mixed_vs_fp64": {"solves_per_s_ratio": m["solves_per_s"] / f["solves_per_s"],
@@ -711,6 +826,8 @@ def main():
     ap.add_argument("--serve-mode", default="gang", choices=["gang", "streams"],
                     help="serve workload: one gang per kind (batched across sizes) or one stream per request")
     ap.add_argument("--serve-chunk", type=int, default=32, help="serve workload: gang steps between re-gangings")
+    ap.add_argument("--serve-spread", type=int, default=1, choices=[1, 8],
+                    help="serve workload: CTAs per velocity solve of the layer gangs")
     ap.add_argument("--serve-group", default="kind", choices=["kind", "shape"],
                     help="serve workload: one gang per kind (across sizes) or per kind and grid")
     ap.add_argument("--r3d-fp64-steps", type=int, default=10, help="r3d workload: FP64 comparison steps")
@@ -1019,6 +1136,13 @@ def main():
     if not args.no_layer:
         # the 129 x 65 layer workload's step (FP64 device path) beside the CPU oracle
         line["layer_config0"] = prb_summary(LAYER, 60, 3, 3, 0.0 if args.no_cpu_baseline else 3.0)
+        line["layer_config0"]["latency_model"] = {"mixed": prb_latency_model(LAYER, 1),
+                                                  "fp64": prb_latency_model(LAYER, 0)}
+        # the 3D annulus step (mixed path, 20 steps after 3 of warm-up) with its barrier model
+        v, ms, sw, _, _ = time_r3d_gpu(R3DWL, 1, 20, 3, 1)
+        line["r3d_config4"] = {"workload": R3DWL["name"], "value": v, "unit": "cell-updates/s", "ms_per_step": ms,
+                               "steps": 20, "warmup": 3, "fp32_cycles_per_step": float(sw),
+                               "latency_model": r3d_latency_model(ms, time_r3d_gpu.last_barriers)}
     print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist

@@ -1916,6 +1916,7 @@ static int solve_persistent(gb_batch *b, cudaStream_t s)
     gs.gen = b->d_sync + 1;
     gs.err = (int *)(b->d_sync + 2);
     gs.limit = b->wait_limit;
+    gs.tally = nullptr;
     const Op *ops0 = b->d_ops, *ops = b->d_ops + n0;
     const TileEntry *tiles = b->d_tiles;
     const double *const *fp = (const double *const *)b->d_f_tab;

@@ -2,6 +2,7 @@
 #include <stdarg.h>
 
 #include "gbcommon.cuh"
+#include "gridsync.cuh"
 
 static thread_local char g_err[512] = "";
 
@@ -76,5 +77,72 @@ extern "C" int gb_measure_issue_rates(double *fp64_fma_per_s, double *fp32_fma_p
     if (st != GB_OK) return st;
     if (fp64_fma_per_s) *fp64_fma_per_s = r64;
     if (fp32_fma_per_s) *fp32_fma_per_s = r32;
+    return GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Grid-barrier probe: one cooperative launch of `blocks` x `threads` that
+// does nothing but pass `nbarriers` bounded grid barriers.  The time per
+// barrier is what a persistent solve launched with that shape pays for each
+// of its phases on top of the phase's own work.
+// ---------------------------------------------------------------------------
+__global__ void k_barrier_probe(GridSync gs, int nbarriers)
+{
+    for (int i = 0; i < nbarriers; ++i)
+        if (!grid_sync(gs)) return;
+}
+
+extern "C" int gb_measure_grid_barrier(int blocks, int threads, int nbarriers, double *us_per_barrier)
+{
+    if (blocks < 1 || threads < 32 || threads > 1024 || (threads & 31) || nbarriers < 1 || !us_per_barrier) {
+        gb_set_error("gb_measure_grid_barrier: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    int dev = 0, coop = 0, per = 0, sms = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_barrier_probe, threads, 0));
+    if (!coop || blocks > per * sms) {
+        gb_set_error("gb_measure_grid_barrier: %d blocks of %d threads cannot all be resident (%d per SM x %d SMs)",
+                     blocks, threads, per, sms);
+        return GB_ERR_INVALID;
+    }
+    unsigned *sync = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&sync, 4 * sizeof(unsigned)));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float ms = 0.f;
+    unsigned hs[4] = {0, 0, 0, 0};
+    for (int rep = 0; rep < 2 && e == cudaSuccess && hs[2] == 0; ++rep) {   // the first launch warms up
+        e = cudaMemset(sync, 0, 4 * sizeof(unsigned));
+        GridSync gs;
+        gs.count = sync;
+        gs.gen = sync + 1;
+        gs.err = (int *)(sync + 2);
+        gs.limit = GB_GRID_WAIT_LIMIT_DEFAULT;
+        gs.tally = nullptr;
+        int nb = nbarriers;
+        void *args[] = {&gs, &nb};
+        if (e == cudaSuccess) e = cudaEventRecord(e0);
+        if (e == cudaSuccess) e = cudaLaunchCooperativeKernel((void *)k_barrier_probe, blocks, threads, args, 0, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(e1);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess) e = cudaMemcpy(hs, sync, sizeof(hs), cudaMemcpyDeviceToHost);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(sync);
+    if (e != cudaSuccess) {
+        gb_set_error("gb_measure_grid_barrier: %s", cudaGetErrorString(e));
+        return GB_ERR_CUDA;
+    }
+    if (hs[2]) {
+        gb_set_error("gb_measure_grid_barrier: a barrier wait reached its limit");
+        return GB_TIMEOUT;
+    }
+    *us_per_barrier = 1e3 * (double)ms / (double)nbarriers;
     return GB_OK;
 }

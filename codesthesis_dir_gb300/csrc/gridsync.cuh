@@ -14,6 +14,7 @@ struct GridSync {
     unsigned *gen;
     int *err;
     long long limit;
+    unsigned long long *tally;   // optional (may be null): barriers passed, counted once per barrier by block 0
 };
 
 // Default wait limit: about 1-2 s of polling at 64 ns per poll.
@@ -44,6 +45,7 @@ __device__ __forceinline__ bool grid_sync(const GridSync &gs)
         }
         __threadfence();
         s_grid_ok = *(volatile int *)gs.err == 0;
+        if (gs.tally && blockIdx.x == 0) atomicAdd(gs.tally, 1ull);
     }
     __syncthreads();
     return s_grid_ok != 0;

@@ -1273,6 +1273,7 @@ __global__ void k_prb_gang(GangTab g)
 
 struct gb_prb_gang {
     int n = 0, mixed = 0;
+    int spread = 1;                // CTAs per equation of the batched multigrid (1 or a cluster)
     PrbDev *d_dev = nullptr;
     int *d_off = nullptr, *d_limit = nullptr;
     GangRec *d_rec = nullptr;
@@ -1405,7 +1406,7 @@ static void prb_gang_enqueue_step(gb_prb_gang *g, cudaStream_t s)
     GL(GP_TROB);
     GL(GP_HEAT);
     GL(GP_RHS);
-    prb_mg_launch_eqs(g->d_eqs, 2 * g->n, g->mixed, s);
+    prb_mg_launch_eqs(g->d_eqs, 2 * g->n, g->mixed, g->spread, s);
     GL(GP_UPD);
     GL(GP_REC);
 #undef GL
@@ -1427,6 +1428,19 @@ extern "C" int gb_prb_gang_enqueue(gb_prb_gang *g, int nsteps, void *stream)
         cudaGraphDestroy(gr);
     }
     for (int k = 0; k < nsteps; ++k) GB_CUDA_TRY(cudaGraphLaunch(g->graph, s));
+    return GB_OK;
+}
+
+extern "C" int gb_prb_gang_set_solve_spread(gb_prb_gang *g, int ctas)
+{
+    if (!g || (ctas != 1 && ctas != prb_mg_cluster_ctas())) {
+        gb_set_error("gb_prb_gang_set_solve_spread: ctas must be 1 or %d", prb_mg_cluster_ctas());
+        return GB_ERR_INVALID;
+    }
+    if (g->spread != ctas) {
+        g->spread = ctas;
+        if (g->graph) { cudaGraphExecDestroy(g->graph); g->graph = nullptr; }
+    }
     return GB_OK;
 }
 

@@ -101,14 +101,15 @@ struct gb_prb {
     double *diag_buf = nullptr;   // 4 running means + kt + CFL history (hist_cap slots)
     int diag_cap = 0;
     int steps_done = 0;
-    int mg_spread = 8;            // CTAs per FP64 zebra solve (gb_prb_set_solve_spread): 1 or 8
+    int mg_spread = 1;            // CTAs per zebra solve (gb_prb_set_solve_spread): 1 or 8
 };
 
 int prb_mg_levels(int nr, int variant);
 int prb_mg_create(gb_prb *h);
 void prb_mg_destroy(gb_prb *h);
 int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s);
-void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, cudaStream_t s);
+void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, int spread, cudaStream_t s);
+int prb_mg_cluster_ctas();
 int prb_refresh_scalars(gb_prb *h);
 // the tank's transport (tank.cu)
 int tank_launch_cvorticity(gb_prb *h, int first, cudaStream_t s);

@@ -582,6 +582,7 @@ __device__ __forceinline__ void tdma32_smem(const float *fac, int n, float *x, i
 // correction cycle, in batches of lines staged in shared memory: right-hand
 // sides in (coalesced along rows), one thread per line eliminates, solutions
 // out.
+template <class G>
 __device__ void mg_colour32_smem(const MgEq &E, const MgLevel &L, int parity)
 {
     extern __shared__ float s_mg32[];
@@ -596,7 +597,11 @@ __device__ void mg_colour32_smem(const MgEq &E, const MgLevel &L, int parity)
     const int nlines = n3 / 2;
     int B = MG32_LINE_FLOATS / nrow - 1;
     if (B > nlines) B = nlines;
-    for (int b0 = 0; b0 < nlines; b0 += B) {
+    // batches of lines in turn over the group's CTAs; within a batch only
+    // this CTA's threads meet
+    int rank = 0;
+    if constexpr (G::C > 1) rank = (int)cg::this_cluster().block_rank();
+    for (int b0 = rank * B; b0 < nlines; b0 += G::C * B) {
         const int nb = (nlines - b0 < B) ? nlines - b0 : B;
         const int pitch = nb | 1;
         for (int j = threadIdx.x >> 5; j < nb; j += blockDim.x >> 5) {
@@ -624,10 +629,12 @@ __device__ void mg_colour32_smem(const MgEq &E, const MgLevel &L, int parity)
         }
         __syncthreads();
     }
+    if constexpr (G::C > 1) G::sync();
 }
 
 // relax2/relax3 of the correction cycle: line sweeps, residual into rc32,
 // psif32 packed into v32.
+template <class G>
 __device__ void mg_relax32(const MgEq &E, int klev)
 {
     const MgLevel &L = E.lev[klev];
@@ -637,32 +644,33 @@ __device__ void mg_relax32(const MgEq &E, int klev)
     const int nrel = E.nrelax;
     for (int irel = 0; irel < nrel; ++irel) {
         if (E.mode == GB_SMOOTHER_LEX) {
-            if (threadIdx.x == 0)
+            if (G::tid() == 0)
                 for (int k = 1; k <= n3; ++k) mg_line32(E, L, k);
-            __syncthreads();
+            G::sync();
         } else {
-            for (int parity = 1; parity >= 0; --parity) mg_colour32_smem(E, L, parity);
+            for (int parity = 1; parity >= 0; --parity) mg_colour32_smem<G>(E, L, parity);
         }
     }
     const int nrow = (E.which == 2) ? n1 : n1 - 1;
     const int tot = nrow * n3;
-    for (int k = 1 + (threadIdx.x >> 5); k <= n3; k += blockDim.x >> 5)
+    for (int k = 1 + (G::tid() >> 5); k <= n3; k += (G::nthr() >> 5))
         for (int i = 1 + (threadIdx.x & 31); i <= nrow; i += 32) {
         const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
         const float a = mg_apply_op<float>(psif, ld, i, k, ka, km, E.which, E.polar, n1, hhri, hhpi, hri, L.rvi32,
                                            L.rvq32);
         rc[GIX(i, k, ld)] = L.f32[(size_t)k * (n1 + 1) + i] - a;
     }
-    __syncthreads();
+    G::sync();
     const int tp = (n1 + 1) * (n3 + 1);
-    for (int k = threadIdx.x >> 5; k < (tp) / ((n1 + 1)); k += blockDim.x >> 5)
+    for (int k = (G::tid() >> 5); k < (tp) / ((n1 + 1)); k += (G::nthr() >> 5))
         for (int i = threadIdx.x & 31; i < (n1 + 1); i += 32) {
             const int idx = k * (n1 + 1) + i;
         L.v32[idx] = psif[GIX(i, k, ld)];
     }
-    __syncthreads();
+    G::sync();
 }
 
+template <class G>
 __device__ void mg_corser32(const MgEq &E, int klev)
 {
     const int ld = E.ld;
@@ -670,7 +678,7 @@ __device__ void mg_corser32(const MgEq &E, int klev)
     const float *rf = E.rc32;
     float *psif = E.psif32, *fc = E.lev[klev + 1].f32;
     const int tot = (n1c + 1) * (n3c + 1);
-    for (int k = threadIdx.x >> 5; k < (tot) / ((n1c + 1)); k += blockDim.x >> 5)
+    for (int k = (G::tid() >> 5); k < (tot) / ((n1c + 1)); k += (G::nthr() >> 5))
         for (int i = threadIdx.x & 31; i < (n1c + 1); i += 32) {
             const int idx = k * (n1c + 1) + i;
         psif[GIX(i, k, ld)] = 0.f;
@@ -688,9 +696,10 @@ __device__ void mg_corser32(const MgEq &E, int klev)
         }
         fc[idx] = t;
     }
-    __syncthreads();
+    G::sync();
 }
 
+template <class G>
 __device__ void mg_finer32(const MgEq &E, int klev)
 {
     const int ld = E.ld;
@@ -700,7 +709,7 @@ __device__ void mg_finer32(const MgEq &E, int klev)
     float *psif = E.psif32;
     const int tot = (n1f + 1) * (n3f + 1);
 #define PC(ii, kk) vc[(size_t)(kk) * (n1c + 1) + (ii)]
-    for (int k = threadIdx.x >> 5; k < (tot) / ((n1f + 1)); k += blockDim.x >> 5)
+    for (int k = (G::tid() >> 5); k < (tot) / ((n1f + 1)); k += (G::nthr() >> 5))
         for (int i = threadIdx.x & 31; i < (n1f + 1); i += 32) {
             const int idx = k * (n1f + 1) + i;
         const int i1 = i / 2, k1 = k / 2;
@@ -715,43 +724,45 @@ __device__ void mg_finer32(const MgEq &E, int klev)
         psif[GIX(i, k, ld)] = p + vf[idx];
     }
 #undef PC
-    __syncthreads();
+    G::sync();
 }
 
 // One FP32 cycle of the reference's sweep schedule (relax on the finest
 // level, the FMG-flavoured down and up legs of PRB:1869-1893) on A e = r
 // from e = 0.
+template <class G>
 __device__ void mg_cycle32(const MgEq &E)
 {
     const int nlev = E.nlev;
-    mg_relax32(E, 1);
+    mg_relax32<G>(E, 1);
     if (nlev > 1) {
         for (int l = 1; l <= nlev - 1; ++l) {
-            mg_corser32(E, l);
-            mg_relax32(E, l + 1);
+            mg_corser32<G>(E, l);
+            mg_relax32<G>(E, l + 1);
         }
         for (int ifmg = 0; ifmg <= nlev - 2; ++ifmg) {
             for (int l = nlev; l >= nlev - ifmg; --l) {
-                mg_finer32(E, l);
-                mg_relax32(E, l - 1);
+                mg_finer32<G>(E, l);
+                mg_relax32<G>(E, l - 1);
             }
             for (int l = nlev - ifmg - 1; l <= nlev - 1; ++l) {
-                mg_corser32(E, l);
-                mg_relax32(E, l + 1);
+                mg_corser32<G>(E, l);
+                mg_relax32<G>(E, l + 1);
             }
         }
         for (int l = nlev; l >= 2; --l) {
-            mg_finer32(E, l);
-            mg_relax32(E, l - 1);
+            mg_finer32<G>(E, l);
+            mg_relax32<G>(E, l - 1);
         }
     }
 }
 
 // poisson2 / poisson3 in mixed precision.  psif holds the FP64 iterate.
-__global__ void __maxnreg__(128) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
+template <class G>
+__device__ __forceinline__ void mg_solve_mixed(const MgEq *eqs, int first_eq)
 {
     __shared__ double s_red[33];
-    const MgEq &E = eqs[first_eq + blockIdx.x];
+    const MgEq &E = eqs[first_eq + blockIdx.x / G::C];
     if (*E.abort == GB_RUN_DONE) return;   // a gang member past its last step (uniform over the block)
     const MgLevel &L1 = E.lev[1];
     const int ld = E.ld, np = E.np;
@@ -759,14 +770,14 @@ __global__ void __maxnreg__(128) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
     const int n1 = L1.n1, n3 = L1.n3;
     double *psif = E.psif, *psi = E.psi, *psip = E.psip;
     const int rows = imax + 1, tot = rows * (np + 1);
-    for (int k = threadIdx.x >> 5; k < (tot) / (rows); k += blockDim.x >> 5)
+    for (int k = (G::tid() >> 5); k < (tot) / (rows); k += (G::nthr() >> 5))
         for (int i = threadIdx.x & 31; i < rows; i += 32) {
             const int idx = k * rows + i;
         const size_t c = GIX(i, k, ld);
         psif[c] = 2.0 * psi[c] - psip[c];
         if (i <= n1) L1.f[(size_t)k * (n1 + 1) + i] = E.rhs[c];
     }
-    __syncthreads();
+    G::sync();
     const int nrow = (E.which == 2) ? n1 : n1 - 1;
     int status = GB_MAXSWEEPS, cycles = 0;
     double res = 0.0;
@@ -775,7 +786,7 @@ __global__ void __maxnreg__(128) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
         double m = 0.0;
         int nan = 0;
         // packed 1D mapping: partly filled warps cost a full FP64 issue slot
-        for (int idx = threadIdx.x; idx < nrow * n3; idx += blockDim.x) {
+        for (int idx = G::tid(); idx < nrow * n3; idx += G::nthr()) {
             const int k = idx / nrow + 1, i = idx - (k - 1) * nrow + 1;
             const int ka = (k == n3) ? 1 : k + 1, km = k - 1;
             const double a = mg_apply_op<double>(psif, ld, i, k, ka, km, E.which, E.polar, n1, L1.hhri, L1.hhpi,
@@ -786,29 +797,29 @@ __global__ void __maxnreg__(128) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
             if (ar != ar) nan = 1;
             if (ar > m) m = ar;
         }
-        nan = __syncthreads_or(nan);
-        res = blk_max(m, s_red);
+        nan = grp_or<G>(nan);
+        res = grp_max<G>(m, s_red);
         if (nan) { status = GB_NAN; break; }
         if (res < E.tolcon) { status = GB_OK; break; }
         if (it == E.maxsweeps) break;
         // e = 0 on the finest level, then one FP32 cycle
-        for (int k = threadIdx.x >> 5; k < (n3 + 1); k += blockDim.x >> 5)
+        for (int k = (G::tid() >> 5); k < (n3 + 1); k += (G::nthr() >> 5))
             for (int i = threadIdx.x & 31; i < (n1 + 2); i += 32) {
                 const int idx = k * (n1 + 2) + i;
             E.psif32[GIX(i, k, ld)] = 0.f;
         }
-        __syncthreads();
-        mg_cycle32(E);
+        G::sync();
+        mg_cycle32<G>(E);
         const double w = (it == 0) ? 1.0 : E.sor;
-        for (int idx = threadIdx.x; idx < nrow * (n3 + 1); idx += blockDim.x) {
+        for (int idx = G::tid(); idx < nrow * (n3 + 1); idx += G::nthr()) {
             const int k = idx / nrow, i = idx - k * nrow + 1;
             psif[GIX(i, k, ld)] += w * (double)E.psif32[GIX(i, k, ld)];
         }
-        __syncthreads();
+        G::sync();
         cycles = it + 1;
     }
     if (status == GB_OK) {
-        for (int k = threadIdx.x >> 5; k < (tot) / (rows); k += blockDim.x >> 5)
+        for (int k = (G::tid() >> 5); k < (tot) / (rows); k += (G::nthr() >> 5))
             for (int i = threadIdx.x & 31; i < rows; i += 32) {
                 const int idx = k * rows + i;
             const size_t c = GIX(i, k, ld);
@@ -816,12 +827,26 @@ __global__ void __maxnreg__(128) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
             psi[c] = (i == 0 || i == imax) ? 0.0 : psif[c];
         }
     }
-    if (threadIdx.x == 0) {
+    if (G::tid() == 0) {
         E.status[0] = status;
         E.status[1] = cycles;
         *E.resmax = res;
         if (status == GB_NAN || (status == GB_MAXSWEEPS && E.stop_on_max)) *E.abort = 1;
     }
+}
+
+__global__ void __maxnreg__(128) k_mg_solve_mixed(const MgEq *eqs, int first_eq)
+{
+    mg_solve_mixed<MgBlock>(eqs, first_eq);
+}
+
+// The mixed solve with each equation on a cluster of MG_CLUSTER CTAs: the
+// FP64 residual passes, the FP32 residual and transfer passes and the
+// batches of each colour's lines are spread over the cluster's SMs.
+__global__ void __cluster_dims__(MG_CLUSTER, 1, 1) __maxnreg__(128) k_mg_solve_mixed_cluster(const MgEq *eqs,
+                                                                                              int first_eq)
+{
+    mg_solve_mixed<MgCluster<MG_CLUSTER>>(eqs, first_eq);
 }
 
 // FP32 copies of the factors (pivots as reciprocals) and radii.
@@ -1017,6 +1042,8 @@ int prb_mg_create(gb_prb *h)
         k_mg_factors32<<<1, 1>>>(E);
     }
     e = cudaFuncSetAttribute(k_mg_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, MG32_SMEM_BYTES);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mg_solve_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, MG32_SMEM_BYTES);
     if (e != cudaSuccess) { gb_set_error("multigrid shared memory: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
     e = cudaMalloc(&h->eq_dev, sizeof(MgEq) * 2);
     if (e != cudaSuccess) { gb_set_error("multigrid descriptors: %s", cudaGetErrorString(e)); return GB_ERR_ALLOC; }
@@ -1035,13 +1062,22 @@ void prb_mg_destroy(gb_prb *h)
 // Refreshes the solve parameters that a caller may change between calls
 // (tolerance, sweep limit, smoother, SOR factor) and launches the solves.
 // The solves of neq equation descriptors (any instances') in one launch,
-// one block each (the gangs' batched multigrid).
-void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, cudaStream_t s)
+// one block or one cluster of MG_CLUSTER blocks each (the gangs' batched
+// multigrid).
+void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, int spread, cudaStream_t s)
 {
     if (neq <= 0) return;
-    if (mixed) k_mg_solve_mixed<<<neq, MG_THREADS, MG32_SMEM_BYTES, s>>>(d_eqs, 0);
-    else k_mg_solve<<<neq, MG_THREADS, 0, s>>>(d_eqs, 0);
+    if (spread > 1) {
+        if (mixed) k_mg_solve_mixed_cluster<<<neq * MG_CLUSTER, MG_THREADS, MG32_SMEM_BYTES, s>>>(d_eqs, 0);
+        else k_mg_solve_cluster<<<neq * MG_CLUSTER, MG_THREADS, 0, s>>>(d_eqs, 0);
+    } else if (mixed) {
+        k_mg_solve_mixed<<<neq, MG_THREADS, MG32_SMEM_BYTES, s>>>(d_eqs, 0);
+    } else {
+        k_mg_solve<<<neq, MG_THREADS, 0, s>>>(d_eqs, 0);
+    }
 }
+
+int prb_mg_cluster_ctas() { return MG_CLUSTER; }
 
 int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s)
 {
@@ -1057,10 +1093,15 @@ int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s)
     const int first = do_v ? 0 : 1;
     const int n = (do_v ? 1 : 0) + (do_u ? 1 : 0);
     if (n == 0) return GB_OK;
-    if (h->p.precision == GB_PRB_MIXED) k_mg_solve_mixed<<<n, MG_THREADS, MG32_SMEM_BYTES, s>>>(h->eq_dev, first);
-    else if (h->mg_spread > 1 && h->p.smoother == GB_SMOOTHER_ZEBRA)
+    const bool spread = h->mg_spread > 1 && h->p.smoother == GB_SMOOTHER_ZEBRA;
+    if (h->p.precision == GB_PRB_MIXED) {
+        if (spread) k_mg_solve_mixed_cluster<<<n * MG_CLUSTER, MG_THREADS, MG32_SMEM_BYTES, s>>>(h->eq_dev, first);
+        else k_mg_solve_mixed<<<n, MG_THREADS, MG32_SMEM_BYTES, s>>>(h->eq_dev, first);
+    } else if (spread) {
         k_mg_solve_cluster<<<n * MG_CLUSTER, MG_THREADS, 0, s>>>(h->eq_dev, first);
-    else k_mg_solve<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
+    } else {
+        k_mg_solve<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
+    }
     h->launches += 1;
     return GB_OK;
 }

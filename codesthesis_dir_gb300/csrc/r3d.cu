@@ -31,6 +31,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <vector>
 
 #define R3_MAXLEV 8
@@ -1075,28 +1076,50 @@ __device__ void r3_line(const R3Lev &L, const R3Work &W, int dir, int p, int q, 
 // contiguous share, forms the right-hand sides of a chunk of its lines with
 // all its threads (every element independently, so the loads and divisions
 // overlap), then one thread per line runs the elimination.
+// A block's share of a phase's entries [a, b) starts at x moved forward
+// past the rest of a group that x would split (entries marked as continued
+// belong with the next one); every block moves its two ends the same way,
+// so the shares still partition [a, b).
+__device__ __forceinline__ int r3_group_start(const int *lines, int a, int b, int x)
+{
+    if (x >= b) return b;
+    while (x > a && (lines[x - 1] & 0x80000000)) ++x;
+    return x;
+}
+
+// End of a chunk [c0, c1): moved back to the end of the last whole group
+// (groups never exceed a chunk; the phase lists are built so).
+__device__ __forceinline__ int r3_chunk_end(const int *lines, int c0, int c1)
+{
+    int e = c1;
+    while (e > c0 + 1 && (lines[e - 1] & 0x80000000)) --e;
+    return e;
+}
+
 template <int COMP>
 __device__ void r3_phase(const R3Lev &L, const R3Work &W, int dir, const int *lines, int a, int b, double *sm)
 {
     const int n = r3_len(COMP, dir, L.n1, L.n2, L.n3);
     const int pitch = n | 1;
     const int per = (b - a + (int)gridDim.x - 1) / (int)gridDim.x;
-    const int my0 = a + (int)blockIdx.x * per;
-    const int my1 = min(b, my0 + per);
+    const int my0 = r3_group_start(lines, a, b, a + (int)blockIdx.x * per);
+    const int my1 = r3_group_start(lines, a, b, a + ((int)blockIdx.x + 1) * per);
     const int chunk = max(1, min((int)blockDim.x, R3_SMEM_DOUBLES / pitch));
-    for (int c0 = my0; c0 < my1; c0 += chunk) {
-        const int nl = min(chunk, my1 - c0);
+    for (int c0 = my0; c0 < my1;) {
+        const int c1 = r3_chunk_end(lines, c0, min(my1, c0 + chunk));
+        const int nl = c1 - c0;
         for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
             const int li = t / n, e = t - li * n;
-            const int pk = lines[c0 + li];
+            const int pk = lines[c0 + li] & 0x7fffffff;
             sm[li * pitch + e] = r3_rhs<COMP>(L, W, dir, pk & 0xffff, pk >> 16, e);
         }
         __syncthreads();
         if ((int)threadIdx.x < nl) {
-            const int pk = lines[c0 + threadIdx.x];
+            const int pk = lines[c0 + threadIdx.x] & 0x7fffffff;
             r3_line<COMP>(L, W, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
         }
         __syncthreads();
+        c0 = c1;
     }
 }
 
@@ -1645,22 +1668,24 @@ __device__ void r3_phase32(const R3Lev &L, const R3Work &W, int dir, const int *
     const int n = r3_len(COMP, dir, L.n1, L.n2, L.n3);
     const int pitch = n | 1;
     const int per = (b - a + (int)gridDim.x - 1) / (int)gridDim.x;
-    const int my0 = a + (int)blockIdx.x * per;
-    const int my1 = min(b, my0 + per);
+    const int my0 = r3_group_start(lines, a, b, a + (int)blockIdx.x * per);
+    const int my1 = r3_group_start(lines, a, b, a + ((int)blockIdx.x + 1) * per);
     const int chunk = max(1, min((int)blockDim.x, (2 * R3_SMEM_DOUBLES) / pitch));
-    for (int c0 = my0; c0 < my1; c0 += chunk) {
-        const int nl = min(chunk, my1 - c0);
+    for (int c0 = my0; c0 < my1;) {
+        const int c1 = r3_chunk_end(lines, c0, min(my1, c0 + chunk));
+        const int nl = c1 - c0;
         for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
             const int li = t / n, e = t - li * n;
-            const int pk = lines[c0 + li];
+            const int pk = lines[c0 + li] & 0x7fffffff;
             sm[li * pitch + e] = r3_rhs32<COMP>(L, W, dir, pk & 0xffff, pk >> 16, e);
         }
         __syncthreads();
         if ((int)threadIdx.x < nl) {
-            const int pk = lines[c0 + threadIdx.x];
+            const int pk = lines[c0 + threadIdx.x] & 0x7fffffff;
             r3_line32<COMP>(L, W, dir, pk & 0xffff, pk >> 16, sm + threadIdx.x * pitch);
         }
         __syncthreads();
+        c0 = c1;
     }
 }
 
@@ -1957,7 +1982,27 @@ extern "C" int gb_r3d_destroy(gb_r3d *h)
     return GB_OK;
 }
 
-// Phase lists of one (level, component, direction), as packed (p, q).
+// Phase lists of one (level, component, direction), as packed (p, q);
+// R3_CONT marks an entry whose line must be solved in the same chunk as the
+// next entry's.
+//
+// LEX: the anti-diagonals p + q, in the reference's order.
+//
+// ZEBRA: lines with even p + q, then odd.  A line on a one-sided row (p = 1
+// or P where p is one-sided, likewise q) also reads the line two over, of
+// its own colour; within a colour such lines are solved before the lines
+// they read (corners, then the other one-sided lines, then the rest), so
+// every read two lines over sees the value from before the colour's pass.
+// On the device a colour is one phase: a line and the lines that read it
+// two over form a group of consecutive entries that one block solves in
+// one chunk, whose right-hand sides are all formed before any of its
+// eliminations writes.  A group larger than a chunk (only on grids far from
+// the sizes the solver is built for) makes the classes separate phases in
+// the same order.
+#define R3_CONT 0x80000000u
+
+static int r3_chunk_lines(int n) { return std::max(1, std::min(R3_THREADS, R3_SMEM_DOUBLES / (n | 1))); }
+
 static void r3_phases(int mode, int comp, int dir, int n1, int n2, int n3, std::vector<int> &lines, std::vector<int> &off)
 {
     const int im = r3_imax(comp, n1), jm = r3_jmax(comp, n2);
@@ -1986,17 +2031,51 @@ static void r3_phases(int mode, int comp, int dir, int n1, int n2, int n3, std::
             for (int p = std::max(1, dsum - Q); p <= std::min(P, dsum - 1); ++p) lines.push_back(p | ((dsum - p) << 16));
             off.push_back((int)lines.size());
         }
-    } else {
-        for (int colour = 0; colour < 2; ++colour)
-            for (int cls = 0; cls < 3; ++cls) {
+        return;
+    }
+    const int chunk = r3_chunk_lines(r3_len(comp, dir, n1, n2, n3));
+    auto cls_of = [&](int p, int q) { return (p_os && (p == 1 || p == P)) + (q_os && (q == 1 || q == Q)); };
+    auto id = [&](int p, int q) { return (q - 1) * P + (p - 1); };
+    for (int colour = 0; colour < 2; ++colour) {
+        // groups: union of each one-sided line with the line it reads two over
+        std::vector<int> parent((size_t)P * Q);
+        for (size_t t = 0; t < parent.size(); ++t) parent[t] = (int)t;
+        std::function<int(int)> root = [&](int x) { return parent[x] == x ? x : (parent[x] = root(parent[x])); };
+        auto join = [&](int a, int b) { parent[root(a)] = root(b); };
+        for (int q = 1; q <= Q; ++q)
+            for (int p = 1; p <= P; ++p) {
+                if (((p + q) & 1) != colour) continue;
+                if (p_os && p == 1 && P >= 3) join(id(p, q), id(3, q));
+                if (p_os && p == P && P >= 3) join(id(p, q), id(P - 2, q));
+                if (q_os && q == 1 && Q >= 3) join(id(p, q), id(p, 3));
+                if (q_os && q == Q && Q >= 3) join(id(p, q), id(p, Q - 2));
+            }
+        // members of each group, the group ordered by class (highest first)
+        std::vector<std::vector<int>> groups((size_t)P * Q);
+        for (int cls = 2; cls >= 0; --cls)
+            for (int q = 1; q <= Q; ++q)
+                for (int p = 1; p <= P; ++p)
+                    if (((p + q) & 1) == colour && cls_of(p, q) == cls) groups[root(id(p, q))].push_back(p | (q << 16));
+        size_t biggest = 0;
+        for (const auto &g : groups) biggest = std::max(biggest, g.size());
+        if ((int)biggest <= chunk) {
+            const size_t before = lines.size();
+            for (int multi = 1; multi >= 0; --multi)   // groups of several lines first, then single lines
+                for (const auto &g : groups) {
+                    if (g.empty() || (g.size() > 1) != (multi == 1)) continue;
+                    for (size_t t = 0; t < g.size(); ++t)
+                        lines.push_back((int)((unsigned)g[t] | (t + 1 < g.size() ? R3_CONT : 0u)));
+                }
+            if (lines.size() != before) off.push_back((int)lines.size());
+        } else {
+            for (int cls = 2; cls >= 0; --cls) {
                 const size_t before = lines.size();
                 for (int q = 1; q <= Q; ++q)
-                    for (int p = 1; p <= P; ++p) {
-                        const int c = (p_os && (p == 1 || p == P)) + (q_os && (q == 1 || q == Q));
-                        if (((p + q) & 1) == colour && c == cls) lines.push_back(p | (q << 16));
-                    }
+                    for (int p = 1; p <= P; ++p)
+                        if (((p + q) & 1) == colour && cls_of(p, q) == cls) lines.push_back(p | (q << 16));
                 if (lines.size() != before) off.push_back((int)lines.size());
             }
+        }
     }
 }
 
@@ -2255,6 +2334,7 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
         d.gs[c].gen = h->sync + R3_SYNC_STRIDE * c + 1;
         d.gs[c].err = (int *)(h->sync + R3_SYNC_STRIDE * c + 2);
         d.gs[c].limit = GB_GRID_WAIT_LIMIT_DEFAULT;
+        d.gs[c].tally = (unsigned long long *)(sm + 448) + c;   // 4 counters, one per component
     }
     // factor tables
     FacJob *djobs = nullptr;
@@ -2311,6 +2391,20 @@ static int r3_create(const gb_r3d_params *p, const double *spacing, gb_r3d **out
 }
 
 extern "C" void *gb_r3d_stream(gb_r3d *h) { return h ? (void *)h->stream : nullptr; }
+
+extern "C" int gb_r3d_barrier_counts(gb_r3d *h, unsigned long long *counts, int *blocks, int reset)
+{
+    if (!h) { gb_set_error("gb_r3d_barrier_counts: null context"); return GB_ERR_INVALID; }
+    GB_CUDA_TRY(cudaStreamSynchronize(h->side));
+    GB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    unsigned long long c[4] = {0, 0, 0, 0};
+    GB_CUDA_TRY(cudaMemcpy(c, h->dev.gs[0].tally, sizeof(c), cudaMemcpyDeviceToHost));
+    if (counts)
+        for (int i = 0; i < 3; ++i) counts[i] = c[i + 1];
+    if (blocks) *blocks = h->grid;
+    if (reset) GB_CUDA_TRY(cudaMemset(h->dev.gs[0].tally, 0, sizeof(c)));
+    return GB_OK;
+}
 
 extern "C" int gb_r3d_set_wait_limit(gb_r3d *h, long long polls)
 {

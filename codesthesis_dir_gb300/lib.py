@@ -186,6 +186,7 @@ SIGNATURES = [
     ("gb_r3d_step", C.c_int, [_vp, C.c_int, _vp, _vp, _ip]),
     ("gb_r3d_stream", _vp, [_vp]),
     ("gb_r3d_set_wait_limit", C.c_int, [_vp, C.c_longlong]),
+    ("gb_r3d_barrier_counts", C.c_int, [_vp, C.POINTER(C.c_ulonglong), C.POINTER(C.c_int), C.c_int]),
     ("gb_prb_bind_bounds", None, [C.c_int, C.c_int]),
     ("gb_prb_bind_smoother", None, [C.c_int]),
     ("gb_prb_bind_tolerance", None, [C.c_double, C.c_int]),
@@ -220,6 +221,7 @@ SIGNATURES = [
     ("gb_prb_gang_query", C.c_int, [_vp]),
     ("gb_prb_gang_stream", _vp, [_vp]),
     ("gb_prb_gang_launches_per_step", C.c_longlong, [_vp]),
+    ("gb_prb_gang_set_solve_spread", C.c_int, [_vp, C.c_int]),
     ("gb_prb_gang_destroy", C.c_int, [_vp]),
     ("gb_axi_gang_create", C.c_int, [C.POINTER(_vp), _ip, C.c_int, C.POINTER(_vp)]),
     ("gb_axi_gang_enqueue", C.c_int, [_vp, C.c_int, _vp]),
@@ -246,6 +248,7 @@ SIGNATURES = [
     ("gb_batch_profile_read", C.c_int, [_vp, _dp, C.POINTER(C.c_longlong), _dp, C.c_int]),
     ("gb_batch_profile_read_kind", C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp]),
     ("gb_measure_issue_rates", C.c_int, [_dp, _dp]),
+    ("gb_measure_grid_barrier", C.c_int, [C.c_int, C.c_int, C.c_int, _dp]),
     ("gb_check_conversions", C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
 ]
 

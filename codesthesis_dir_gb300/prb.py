@@ -126,6 +126,11 @@ class PRB:
     def poisson3(self):
         return self._poisson(3)
 
+    def set_solve_spread(self, ctas):
+        """CTAs sharing one FP64 two-colour solve: 8 (a cluster, the
+        default) or 1.  Both give the same bits."""
+        _L.check(_L.load().gb_prb_set_solve_spread(self._h, ctas), "set_solve_spread")
+
     def update(self):
         c = C.c_longlong()
         _L.check(_L.load().gb_prb_update(self._h, C.byref(c)), "update")

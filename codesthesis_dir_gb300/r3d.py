@@ -132,6 +132,14 @@ class R3D:
     def stream(self):
         return _L.load().gb_r3d_stream(self._h)
 
+    def barrier_counts(self, reset=False):
+        """Grid barriers passed by the w, v and u solves since creation or
+        the last reset, and the block count of a solve launch."""
+        c = (C.c_ulonglong * 3)()
+        nb = C.c_int()
+        _L.check(_L.load().gb_r3d_barrier_counts(self._h, c, C.byref(nb), 1 if reset else 0), "barrier_counts")
+        return [int(x) for x in c], nb.value
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             _L.load().gb_r3d_destroy(self._h)

@@ -278,9 +278,10 @@ class _Gang:
     """One gang (gb_prb_gang or gb_axi_gang) over device instances of one
     kind; rebuilt whenever its membership changes."""
 
-    def __init__(self, kind):
+    def __init__(self, kind, solve_spread=1):
         L = _L.load()
         self.kind = kind
+        self.solve_spread = solve_spread
         if kind == LAYER:
             self._create, self._enqueue, self._query, self._destroy = (
                 L.gb_prb_gang_create, L.gb_prb_gang_enqueue, L.gb_prb_gang_query, L.gb_prb_gang_destroy)
@@ -298,6 +299,8 @@ class _Gang:
         h = C.c_void_p()
         _L.check(self._create(handles, totals, n, C.byref(h)), "gang_create")
         self.h = h
+        if self.kind == LAYER and self.solve_spread != 1:
+            _L.check(_L.load().gb_prb_gang_set_solve_spread(h, self.solve_spread), "gang_set_solve_spread")
 
     def enqueue(self, nsteps):
         _L.check(self._enqueue(self.h, nsteps, None), "gang_enqueue")
@@ -338,16 +341,17 @@ class GangServer:
                  keep_fields: bool = False, clock: Callable[[], float] = time.perf_counter,
                  sleep: Callable[[float], None] = time.sleep, precision=_L.PRB_FP64, smoother=_L.SMOOTHER_ZEBRA,
                  group_by: str = "kind", factory: Optional[Callable[[Request], object]] = None,
-                 gang_factory: Optional[Callable[[str], object]] = None):
+                 gang_factory: Optional[Callable[[str], object]] = None, solve_spread: int = 1):
         """group_by: "kind" (one gang per kind, batched across grid sizes:
         every member steps at the pace of the largest) or "shape" (one gang
         per kind and grid; the gangs run side by side on their own streams).
+        solve_spread: CTAs per velocity solve of the layer gangs (1 or 8).
         factory / gang_factory: stand-ins for the device instance and gang
         (the host logic's tests)."""
         assert group_by in ("kind", "shape")
         self.group_by = group_by
         self.factory = factory or (lambda r: DeviceInstance(r, precision, smoother))
-        self.gang_factory = gang_factory or _Gang
+        self.gang_factory = gang_factory or (lambda kind: _Gang(kind, solve_spread))
         self.budget = budget_bytes
         self.max_active = max_active
         self.chunk = chunk

@@ -208,13 +208,15 @@ int gb_prb_rhsu(gb_prb *h);                         /* PRB:1679-1721 */
  * which = 3: poisson3 on uel/uelp/urh (PRB:1930-2059).
  * Returns GB_OK, GB_MAXSWEEPS or GB_NAN; *sweeps gets the sweep count. */
 int gb_prb_poisson(gb_prb *h, int which, int *sweeps);
-/* CTAs that share one FP64 two-colour solve of this instance: 8 (the
- * default: the lines of a colour, the residual and the transfers of each
- * level are spread over a cluster of 8 CTAs that meet at the hardware
- * cluster barrier and reduce through distributed shared memory, so the
- * solve uses eight SMs' FP64 units) or 1 (one CTA per equation).  Both give
- * the same bits; the reference's line order and the mixed solve always use
- * one CTA.  No counterpart in the reference (its solves are serial). */
+/* CTAs that share one two-colour solve of this instance (FP64 or mixed):
+ * 1 (the default: one CTA per equation) or 8 (the lines of a colour, the
+ * residuals and the transfers of each level are spread over a cluster of 8
+ * CTAs that meet at the hardware cluster barrier and reduce through
+ * distributed shared memory).  Both give the same bits; the reference's
+ * line order always uses one CTA.  The solve of a line is a dependent
+ * chain that a cluster does not shorten: on the 129 x 65 layer the cluster
+ * takes 0.95-1.02x the time of one CTA.  No counterpart in the reference
+ * (its solves are serial). */
 int gb_prb_set_solve_spread(gb_prb *h, int ctas);
 /* update (PRB:1557-1626); *clamps (may be NULL) gets the number of
  * temperatures clamped, each of which the reference reports with
@@ -411,6 +413,10 @@ int gb_prb_gang_enqueue(gb_prb_gang *g, int nsteps, void *stream);
 int gb_prb_gang_query(gb_prb_gang *g);
 void *gb_prb_gang_stream(gb_prb_gang *g);
 long long gb_prb_gang_launches_per_step(const gb_prb_gang *g);
+/* CTAs per equation of a PRB gang's batched multigrid: 1 (the default) or
+ * 8 (a cluster per equation, as gb_prb_set_solve_spread); the same bits
+ * either way.  Takes effect at the next enqueue. */
+int gb_prb_gang_set_solve_spread(gb_prb_gang *g, int ctas);
 int gb_prb_gang_destroy(gb_prb_gang *g);
 typedef struct gb_axi_gang gb_axi_gang;
 int gb_axi_gang_create(gb_axi *const *members, const int *nsteps_total, int n, gb_axi_gang **out);
@@ -446,7 +452,8 @@ typedef struct gb_r3d_params {
     int nrel;                 /* relaxations per level visit (2, rot3dmg.f:1237-1238) */
     int smoother;             /* GB_SMOOTHER_LEX: the reference's line order, run as wavefronts of
                                  independent lines; GB_SMOOTHER_ZEBRA: two colours of lines, the
-                                 lines on one-sided boundary rows last within a colour */
+                                 lines on one-sided boundary rows first within a colour (each
+                                 colour one phase of the device solve) */
     int precision;            /* GB_PRB_FP64 or GB_PRB_MIXED (FP32 V-cycles in FP64 defect correction) */
     int variant;              /* GB_R3D_VERTICAL (rot3dmg.f) or GB_R3D_HORIZONTAL (rot3dmghor.f) */
 } gb_r3d_params;
@@ -518,6 +525,13 @@ void *gb_r3d_stream(gb_r3d *h);
  * context stays usable after a timeout, its fields hold whatever the
  * interrupted step left. */
 int gb_r3d_set_wait_limit(gb_r3d *h, long long polls);
+/* Grid barriers passed by the w, v and u solves (counts[0..2]) since the
+ * context was created or last reset (reset != 0 clears them after reading),
+ * and the number of blocks the solves launch with (*blocks, may be NULL; the
+ * w and v solves of a step run side by side on half of them each).  With
+ * gb_measure_grid_barrier this gives the barrier term of a step's latency.
+ * No counterpart in the reference (its solves have no barriers). */
+int gb_r3d_barrier_counts(gb_r3d *h, unsigned long long *counts, int *blocks, int reset);
 
 /* ------------------------- stretched-grid streamfunction solve (rcsc.f) */
 /* The multigrid of rcsc.f:1118-1444 on a non-uniform (r, z) grid: operator
@@ -753,6 +767,13 @@ int gb_batch_profile_read_kind(gb_batch *b, int kind, double *ms, long long *lau
  * (instructions per second, every SM busy); the FP64 figure is the peak the
  * FP64-bound kernels are measured against. */
 int gb_measure_issue_rates(double *fp64_fma_per_s, double *fp32_fma_per_s);
+/* Time of one bounded grid barrier (microseconds) in a cooperative launch of
+ * `blocks` x `threads` that does nothing else, averaged over `nbarriers`
+ * barriers after one warm-up launch: the per-phase cost a persistent solve of
+ * that launch shape pays on top of its work.  GB_ERR_INVALID when the blocks
+ * cannot all be resident.  No counterpart in the reference (a latency probe
+ * of this library's own barrier). */
+int gb_measure_grid_barrier(int blocks, int threads, int nbarriers, double *us_per_barrier);
 /* Compares the batched solver's integer-pipe float <-> double conversions
  * with the hardware conversions on the current device: every float bit
  * pattern through float -> double, and n_random seeded double bit patterns

@@ -1123,7 +1123,7 @@ static void pass(lev_t *L, int dir, int mode)
         q_os = onesided_j(w);
     }
     for (int colour = 0; colour < (mode == R3D_LEX ? 1 : 2); ++colour)
-        for (int cls = 0; cls < (mode == R3D_LEX ? 1 : 3); ++cls)
+        for (int cls = (mode == R3D_LEX ? 0 : 2); cls >= 0; --cls)
             for (int q = 1; q <= Q; ++q)
                 for (int p = 1; p <= P; ++p) {
                     if (mode != R3D_LEX && (((p + q) & 1) != colour || line_class(p, P, p_os, q, Q, q_os) != cls))

@@ -30,10 +30,13 @@ extern "C" {
  * (:1609-1610), phi-lines j outer and i inner (:1649-1650).  R3D_ZEBRA is
  * the parallel ordering: in each direction, the lines whose two transverse
  * indices have an even sum, then those with an odd sum; within a colour,
- * first the lines away from the one-sided boundary rows (the rows whose
- * stencils reach two lines over, e.g. i = 1 reading i + 2), then the lines
- * on one such row, then those on two.  No line of a phase reads another
- * line of the same phase. */
+ * first the lines on two one-sided boundary rows (the rows whose stencils
+ * reach two lines over, e.g. i = 1 reading i + 2), then those on one such
+ * row, then the rest.  A line reads only lines of the other colour and,
+ * on a one-sided row, the line two over of its own colour on fewer
+ * one-sided rows, which comes later: every line of a colour sees the
+ * colour's lines as they were before the colour's pass, so the lines of a
+ * colour can be solved all at once. */
 #define R3D_LEX   0
 #define R3D_ZEBRA 1
 

@@ -97,3 +97,14 @@ def test_axi_dropin_exports_its_header():
     assert {"vorticity_", "velocity_", "temperature_", "poisson_", "update_", "heat_", "poissoninit_"} <= declared
     assert not sorted(declared - exported), sorted(declared - exported)
     assert declared == {n for n, _, _ in lib.AXI_DROPIN_SIGNATURES}
+
+
+def test_barrier_probe_checks_arguments_before_touching_the_device(gblib):
+    """Argument errors come back without a device call (this runs without a GPU)."""
+    import ctypes as C
+    from codesthesis_dir_gb300 import lib
+    t = C.c_double(-1.0)
+    assert gblib.gb_measure_grid_barrier(0, 256, 10, C.byref(t)) == lib.GB_ERR_INVALID
+    assert gblib.gb_measure_grid_barrier(8, 100, 10, C.byref(t)) == lib.GB_ERR_INVALID
+    assert gblib.gb_measure_grid_barrier(8, 256, 0, C.byref(t)) == lib.GB_ERR_INVALID
+    assert t.value == -1.0

@@ -83,3 +83,28 @@ def test_mixed_solve_meets_fp64_tolerance(oracle, P):
     v_mixed = g.get("vel")
     v_fp64 = np.array(o.field("vel"))
     assert rel_l2(v_fp64, v_mixed) <= 1e-7
+
+
+@pytest.mark.parametrize("variant", [0, 1], ids=["layer", "annulus"])
+def test_mixed_cluster_spread_equals_one_cta(oracle, P, variant):
+    """The mixed solve spread over a cluster of 8 CTAs gives exactly the
+    bits of the one-CTA mixed solve (the default):
+    fields, Nusselt numbers and cycle counts, on the layer and on the annulus
+    (polar operators, three relaxations per visit)."""
+    from codesthesis_dir_gb300 import lib
+    L = lib.load()
+    if variant == 0:
+        prm, tol, kw = config0_params(), 1e-10, {}
+    else:
+        prm, tol, kw = dict(nr=32, np_=64, dt=2e-7, Ra=8e7, Pr=0.71, r0=0.5, rmax=1.0), 1e-8, \
+            dict(variant=1, Re=1.06148e5, kind=0)
+    _, g8 = _pair(oracle, P, prm, 1, tol, **kw)
+    _, g1 = _pair(oracle, P, prm, 1, tol, **kw)
+    assert L.gb_prb_set_solve_spread(g8._h, 8) == 0
+    assert L.gb_prb_set_solve_spread(g1._h, 1) == 0
+    nu8, sw8 = g8.step(12)
+    nu1, sw1 = g1.step(12)
+    np.testing.assert_array_equal(sw8, sw1)
+    np.testing.assert_array_equal(nu8, nu1)
+    for name in ("vel", "uel", "C", "th"):
+        np.testing.assert_array_equal(g8.get(name), g1.get(name))

@@ -123,8 +123,8 @@ def test_graph_steps_oblique(oracle, P, smoother):
 
 @pytest.mark.parametrize("nr,np_", [(64, 128), (32, 64)])
 def test_cluster_spread_solve_equals_one_cta(oracle, P, nr, np_):
-    """The FP64 two-colour solve spread over a cluster of 8 CTAs (the
-    default) gives exactly the bits of the one-CTA solve and of the oracle:
+    """The FP64 two-colour solve spread over a cluster of 8 CTAs gives
+    exactly the bits of the one-CTA solve (the default) and of the oracle:
     fields, Nusselt numbers and sweep counts."""
     from codesthesis_dir_gb300 import lib
     L = lib.load()

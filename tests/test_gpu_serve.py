@@ -35,16 +35,18 @@ def test_mix_equals_alone(gblib, precision):
     assert s["completed"] == len(reqs) and s["tts_p99_s"] >= s["tts_p50_s"] > 0
 
 
+@pytest.mark.parametrize("spread", [1, 8], ids=["cta", "cluster"])
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
-def test_gang_server_mix_equals_alone(gblib, precision):
+def test_gang_server_mix_equals_alone(gblib, precision, spread):
     """The gang server batches the active requests of each kind into one
     set of launches per step across their different grids; every request
     still gets exactly the fields and Nusselt history it gets alone, also
     when its step count is not a multiple of the chunk (the gang stops it at
-    its own count) and when members join and leave between chunks."""
+    its own count) and when members join and leave between chunks; the
+    layer gangs' solves on one CTA or a cluster of 8 per equation."""
     from codesthesis_dir_gb300 import serve
     reqs = _requests()
-    srv = serve.GangServer(max_active=4, chunk=5, keep_fields=True, precision=precision)
+    srv = serve.GangServer(max_active=4, chunk=5, keep_fields=True, precision=precision, solve_spread=spread)
     mix = srv.run(reqs)
     assert all(r.status == 0 for r in mix), [(r.rid, r.status) for r in mix]
     assert srv.rebuilds >= 2
