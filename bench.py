@@ -826,7 +826,7 @@ def main():
     ap.add_argument("--serve-mode", default="gang", choices=["gang", "streams"],
                     help="serve workload: one gang per kind (batched across sizes) or one stream per request")
     ap.add_argument("--serve-chunk", type=int, default=32, help="serve workload: gang steps between re-gangings")
-    ap.add_argument("--serve-spread", type=int, default=1, choices=[1, 8],
+    ap.add_argument("--serve-spread", type=int, default=8, choices=[1, 8],
                     help="serve workload: CTAs per velocity solve of the layer gangs")
     ap.add_argument("--serve-group", default="kind", choices=["kind", "shape"],
                     help="serve workload: one gang per kind (across sizes) or per kind and grid")
@@ -1030,6 +1030,12 @@ def main():
     h_psi2 = [h_psi, torch.zeros(total, dtype=torch.float64).pin_memory()]
     cyc_k = [np.zeros(len(sizes), dtype=np.int32) for _ in range(args.steps)]
     rr_k = [np.zeros(len(sizes)) for _ in range(args.steps)]
+    # warm-up of the stream path (its first call sets up the staging buffers)
+    for k in range(2):
+        st = L.gb_batch_submit_host(mixed._h, h_f.data_ptr(), h_psi2[k & 1].data_ptr(), cyc_k[k].ctypes.data,
+                                    rr_k[k].ctypes.data)
+        assert st == 0, lib.last_error()
+    assert L.gb_batch_drain(mixed._h) == 0, lib.last_error()
     barrier()
     t0 = time.perf_counter()
     for k in range(args.steps):

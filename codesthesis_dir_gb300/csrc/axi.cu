@@ -491,7 +491,7 @@ __device__ __forceinline__ void axi_zline(const AxiDev &d, const AxiLevel &L, in
         return -(psif[AX(i + 1, j)] + psif[AX(i - 1, j)]) / hhr + f[(size_t)j * (n1 + 1) + i] -
                (psif[AX(i + 1, j)] - psif[AX(i - 1, j)]) * 0.5 / rv / hr;
     };
-    apply_tdma_rhs(L.fac_z + (size_t)(i - 1) * 3 * (n2 - 1), n2 - 1, psif + AX(i, 1), ld, rhs);
+    apply_tdma_rhs(L.fac_z + (size_t)(i - 1) * tdma_fac_len(n2 - 1), n2 - 1, psif + AX(i, 1), ld, rhs);
 }
 
 // relax (rotann2.f:668-753): psif from v, nrel sweeps of r-lines then
@@ -694,12 +694,14 @@ __device__ __forceinline__ void tdma32_pitch(const float *fac, int n, float *x, 
 {
     const float *fact = fac, *ibp = fac + n, *c = fac + 2 * n;
     float prev = x[0];
+#pragma unroll 4
     for (int j = 1; j < n; ++j) {
         prev = x[j * pitch] - fact[j] * prev;
         x[j * pitch] = prev;
     }
     float y = prev * ibp[n - 1];
     x[(n - 1) * pitch] = y;
+#pragma unroll 4
     for (int j = n - 2; j >= 0; --j) {
         y = (x[j * pitch] - c[j] * y) * ibp[j];
         x[j * pitch] = y;
@@ -954,7 +956,8 @@ __global__ void k_axi_factors32(AxiDev d)
         if (L.n1 - 1 >= 1) conv(L.fac_r, L.fac_r32, L.n1 - 1);
         if (L.n2 - 1 >= 1)
             for (int i = 1; i <= L.n1 - 1; ++i)
-                conv(L.fac_z + (size_t)(i - 1) * 3 * (L.n2 - 1), L.fac_z32 + (size_t)(i - 1) * 3 * (L.n2 - 1), L.n2 - 1);
+                conv(L.fac_z + (size_t)(i - 1) * tdma_fac_len(L.n2 - 1), L.fac_z32 + (size_t)(i - 1) * 3 * (L.n2 - 1),
+                     L.n2 - 1);
     }
 }
 
@@ -984,7 +987,7 @@ __global__ void k_axi_factors(AxiDev d, double *work)
                 c[j - 1] = 1.0 / hhz;
                 b[j - 1] = -2.0 / hhr - 2.0 / hhz - 1.0 / (rv * rv);
             }
-            if (n2 - 1 >= 1) factor_tdma(a, b, c, n2 - 1, L.fac_z + (size_t)(i - 1) * 3 * (n2 - 1));
+            if (n2 - 1 >= 1) factor_tdma(a, b, c, n2 - 1, L.fac_z + (size_t)(i - 1) * tdma_fac_len(n2 - 1));
         }
     }
 }
@@ -1141,7 +1144,7 @@ static int axi_create(const gb_axi_params *p, double dr, double dz, gb_axi **out
     size_t need = (size_t)(nr + 2) + 2 * fsz + fsz + (size_t)(nr + 2) / 2 + 8;   // + psif32, rc32, rval32
     for (int l = 1; l <= nlev; ++l) {
         const size_t n1 = (size_t)nr * 2 / ((size_t)1 << l), n2 = (size_t)nz * 2 / ((size_t)1 << l);
-        const size_t lv = 2 * (n1 + 1) * (n2 + 1) + 3 * n1 + n1 * 3 * (n2 + 1);
+        const size_t lv = 2 * (n1 + 1) * (n2 + 1) + 4 * n1 + n1 * 4 * (n2 + 1);
         need += lv + (lv + 1) / 2 + 4;   // FP64 slots, then their FP32 copies
     }
     const size_t work = 3 * (size_t)((nr > nz ? nr : nz) + 2);
@@ -1171,8 +1174,8 @@ static int axi_create(const gb_axi_params *p, double dr, double dz, gb_axi **out
         const size_t sz = (size_t)(L.n1 + 1) * (L.n2 + 1);
         L.v = b; b += sz;
         L.f = b; b += sz;
-        L.fac_r = b; b += 3 * (size_t)L.n1;
-        L.fac_z = b; b += (size_t)L.n1 * 3 * (size_t)(L.n2 + 1);
+        L.fac_r = b; b += 4 * (size_t)L.n1;                          // tdma_fac_len(n1 - 1) and more
+        L.fac_z = b; b += (size_t)L.n1 * 4 * (size_t)(L.n2 + 1);
         float *fb = (float *)b;
         L.v32 = fb; fb += sz;
         L.f32 = fb; fb += sz;

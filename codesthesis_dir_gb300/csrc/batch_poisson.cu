@@ -201,11 +201,16 @@ template <> __device__ __forceinline__ float IH2<float>(const BatchDev &B, int p
 // halo while they run.  Each operation ends with a block barrier so that a
 // block may run the next operation in the same shared memory.
 // ---------------------------------------------------------------------------
+// 128 x 32 tiles of 256 threads.  128 x 64 tiles of 512 threads (halo
+// rings adding 17% instead of 29% to a down operation's sweeps, the same
+// warps per SM) measured 5% slower per solve of the 256-problem workload
+// (5.96 against 5.67 ms); updating two points per lane with paired shared
+// loads measured no faster (5.63 ms either way).
 #define TX 128
 #define TY 32
-#define TILE_THREADS 256
-#define ST_R (TY / 8)    // rows a thread stores: TILE_THREADS / 32 warps step through TY rows
-#define ST_C (TX / 32)   // columns a thread stores
+#define TILE_THREADS (8 * TY)   // 256
+#define ST_R (TY / (TILE_THREADS / 32))   // rows a thread stores: the block's warps step through TY rows
+#define ST_C (TX / 32)                    // columns a thread stores
 
 // Colour-split shared layout of a tile staged with halo H: the points of
 // one parity of (row + column) in one half, those of the other in the other
@@ -327,7 +332,7 @@ __device__ __forceinline__ void psi_prefetch(const V *psi, int x0, int y0, int n
     for (int rr = 0; rr < ST_R; ++rr)
 #pragma unroll
         for (int cc = 0; cc < ST_C; ++cc) {
-            const int gy = y0 + warp + 8 * rr, gx = x0 + lane + 32 * cc;
+            const int gy = y0 + warp + (TILE_THREADS / 32) * rr, gx = x0 + lane + 32 * cc;
             const bool in = gx >= 1 && gx <= n - 2 && gy >= 1 && gy <= n - 2;
             V z;
             if constexpr (std::is_same<V, float2>::value) z = make_float2(0.f, 0.f);
@@ -351,7 +356,7 @@ __device__ __forceinline__ void tile_store(const T *sx, int ox, int oy, int x0, 
     for (int rr = 0; rr < ST_R; ++rr)
 #pragma unroll
         for (int cc = 0; cc < ST_C; ++cc) {
-            const int gy = y0 + warp + 8 * rr, gx = x0 + lane + 32 * cc;
+            const int gy = y0 + warp + (TILE_THREADS / 32) * rr, gx = x0 + lane + 32 * cc;
             if (gx < 1 || gx > n - 2 || gy < 1 || gy > n - 2) continue;
             const size_t g = (size_t)gy * n + gx;
             const T v = sx[TileLayout<T, H>::at(gy - oy, gx - ox)];
@@ -986,10 +991,23 @@ __device__ __forceinline__ void run_item(const BatchDev &B, const TileEntry *til
 // The coarse levels of every problem below its tiled levels (graph path):
 // one block of LOCAL_THREADS per problem.
 #define LOCAL_THREADS 512
+// Programmatic dependent launch (the graph path's kernels are launched with
+// programmatic stream serialization): a kernel may be scheduled while its
+// predecessor's last blocks still run, and waits here until that
+// predecessor has completed and its writes are visible; it then lets its own
+// successor be scheduled.  This hides the launch gap between the
+// level-synchronous operations.  Without the attribute both return at once.
+__device__ __forceinline__ void grid_dependency_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <class T>
 __global__ void __launch_bounds__(LOCAL_THREADS) k_local(BatchDev B, Op op, int nu1, int nu2)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    grid_dependency_wait();
     if (!B.active[blockIdx.x]) return;
     op_local<T>(B, blockIdx.x, nu1, nu2, op.aux & 1, (op.aux >> 1) & 1, (op.aux >> 2) & 1, smem_raw);
 }
@@ -1007,6 +1025,7 @@ __global__ void __launch_bounds__(TILE_THREADS, (OpMinBlocks<KIND, CM>::value)) 
                                                      Op op, int nu1, int nu2)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    grid_dependency_wait();
     if (KIND == OP_FINALIZE) {
         const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
         if (p < B.nprob) op_finalize(B, p, op.aux);
@@ -1312,10 +1331,30 @@ template <class T> static cudaError_t set_smem_attrs(size_t local, size_t persis
     SA((smem_attr_cm<T, OP_PROLONG, 0>(smem_tile<T>(0))));
     SA((smem_attr_cm<T, OP_PROLONG, 1>(smem_tile<T>(2))));
     SA((smem_attr_cm<T, OP_PROLONG, 2>(smem_tile<T>(4))));
+    SA((smem_attr_cm<T, OP_OUTER, 0>(smem_outer())));
+    SA((smem_attr_cm<T, OP_OUTER, 1>(smem_outer())));
     SA((cudaFuncSetAttribute(k_local<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)local)));
     SA((cudaFuncSetAttribute(k_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)persistent)));
 #undef SA
     return cudaSuccess;
+}
+
+// A kernel launch with programmatic stream serialization (see
+// grid_dependency_wait).
+template <typename... P, typename... A>
+static void launch_pdl(void (*k)(P...), int grid, int block, size_t sm, cudaStream_t s, A... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = sm;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, ((P)args)...);
 }
 
 // Launches k_op<T, KIND, NU, cm> (graph path).
@@ -1326,10 +1365,10 @@ static void launch_k(const gb_batch *b, int cm, int g, size_t sm, cudaStream_t s
     const double *const *fp = (const double *const *)b->d_f_tab;
     const int n1 = b->nu1, n2 = b->nu2;
     if constexpr (sizeof(T) == 4) {
-        if (cm == CM_PAIR) { k_op<T, KIND, NU, CM_PAIR><<<g, TILE_THREADS, sm, s>>>(b->dev, t, fp, op, n1, n2); return; }
-        if (cm == CM_F64) { k_op<T, KIND, NU, CM_F64><<<g, TILE_THREADS, sm, s>>>(b->dev, t, fp, op, n1, n2); return; }
+        if (cm == CM_PAIR) { launch_pdl(k_op<T, KIND, NU, CM_PAIR>, g, TILE_THREADS, sm, s, b->dev, t, fp, op, n1, n2); return; }
+        if (cm == CM_F64) { launch_pdl(k_op<T, KIND, NU, CM_F64>, g, TILE_THREADS, sm, s, b->dev, t, fp, op, n1, n2); return; }
     }
-    k_op<T, KIND, NU, CM_NONE><<<g, TILE_THREADS, sm, s>>>(b->dev, t, fp, op, n1, n2);
+    launch_pdl(k_op<T, KIND, NU, CM_NONE>, g, TILE_THREADS, sm, s, b->dev, t, fp, op, n1, n2);
 }
 
 // Launches one operation as its own kernel (graph path).
@@ -1354,7 +1393,7 @@ static void launch_op(gb_batch *b, const Op &op, cudaStream_t s)
         else launch_k<T, OP_PROLONG, 0>(b, op.corr, g, sm, s, op);
         break;
     case OP_LOCAL:
-        k_local<T><<<g, LOCAL_THREADS, sm, s>>>(b->dev, op, b->nu1, b->nu2);
+        launch_pdl(k_local<T>, g, LOCAL_THREADS, sm, s, b->dev, op, b->nu1, b->nu2);
         break;
     case OP_OUTER:
         if (op.nu) launch_k<T, OP_OUTER, 1>(b, op.corr, g, sm, s, op);

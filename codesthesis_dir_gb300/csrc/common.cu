@@ -3,6 +3,7 @@
 
 #include "gbcommon.cuh"
 #include "gridsync.cuh"
+#include "divrn.cuh"
 
 static thread_local char g_err[512] = "";
 
@@ -144,5 +145,85 @@ extern "C" int gb_measure_grid_barrier(int blocks, int threads, int nbarriers, d
         return GB_TIMEOUT;
     }
     *us_per_barrier = 1e3 * (double)ms / (double)nbarriers;
+    return GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Division check: the correctly rounded quotient from a stored reciprocal
+// (divrn.cuh) against the hardware division, on seeded operands: random
+// significands and signs with exponents in [-300, 300] (quotients well inside
+// the normal range), products b q rounded (quotients at or next to a
+// representable value), small integers, and zero dividends of either sign.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x)
+{
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double make_double(unsigned long long h, int e)
+{
+    const unsigned long long bits = (h & 0x800fffffffffffffull) | ((unsigned long long)(e + 1023) << 52);
+    return __longlong_as_double((long long)bits);
+}
+
+__global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long *bad)
+{
+    unsigned long long cnt = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long h1 = mix64(seed ^ (2 * i)), h2 = mix64(seed ^ (2 * i + 1)), h3 = mix64(h1 ^ h2);
+        const int ea = (int)((h1 >> 52) % 601) - 300, eb = (int)((h2 >> 52) % 601) - 300;
+        double a, b;
+        switch ((int)(h3 & 3)) {
+        case 0:
+            a = make_double(h1, ea);
+            b = make_double(h2, eb);
+            break;
+        case 1:
+            b = make_double(h2, eb / 2);
+            a = __dmul_rn(b, make_double(h1, ea / 2));
+            break;
+        case 2:
+            a = (double)((long long)(h1 % 2000001ull) - 1000000);
+            b = (double)((long long)(h2 % 1999ull) - 999);
+            if (b == 0.0) b = 7.0;
+            break;
+        default:
+            a = (h1 & 1) ? -0.0 : 0.0;
+            b = make_double(h2, eb);
+            break;
+        }
+        const double y = 1.0 / b;
+        const double q = div_by_rcp(a, b, y);
+        const double ref = a / b;
+        if (__double_as_longlong(q) != __double_as_longlong(ref)) ++cnt;
+    }
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+extern "C" int gb_check_division(long long n_random, unsigned long long seed, long long *mismatches)
+{
+    if (n_random < 1 || !mismatches) {
+        gb_set_error("gb_check_division: invalid argument");
+        return GB_ERR_INVALID;
+    }
+    unsigned long long *d = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long)));
+    cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        k_check_division<<<152 * 8, 256>>>((unsigned long long)n_random, seed, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        gb_set_error("gb_check_division: %s", cudaGetErrorString(e));
+        return GB_ERR_CUDA;
+    }
+    *mismatches = (long long)h;
     return GB_OK;
 }

@@ -788,16 +788,16 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     cudaMemset(h->fields, 0, sizeof(double) * h->fsz * GB_F_COUNT);
     for (int f = 0; f < GB_F_COUNT; ++f) d.f[f] = h->fields + (size_t)f * h->fsz;
     // factors + small device state
-    const size_t nfac = 3 * (size_t)nr + (6 * (size_t)(np + 1) + 3) + 3 * (size_t)nr + 3 * ((size_t)(nr > np ? nr : np) + 2) +
-                        6 * ((size_t)np + 1);
+    const size_t nwork = 3 * ((size_t)(nr > np ? nr : np) + 2);
+    const size_t nfac = tdma_fac_len(nr) + ptdma_fac_len(np + 1) + tdma_fac_len(nr) + nwork + 2 * tdma_fac_len(np + 1);
     e = cudaMalloc(&h->factors, sizeof(double) * nfac);
     if (e != cudaSuccess) { gb_prb_destroy(h); gb_set_error("gb_prb_create: factor alloc"); return GB_ERR_ALLOC; }
     double *fr1 = h->factors;
-    double *fx = fr1 + 3 * (size_t)nr;
-    double *frT = fx + 6 * (size_t)(np + 1) + 3;
-    double *work = frT + 3 * (size_t)nr;
-    double *fxw1 = work + 3 * ((size_t)(nr > np ? nr : np) + 2);
-    double *fxw2 = fxw1 + 3 * ((size_t)np + 1);
+    double *fx = fr1 + tdma_fac_len(nr);
+    double *frT = fx + ptdma_fac_len(np + 1);
+    double *work = frT + tdma_fac_len(nr);
+    double *fxw1 = work + nwork;
+    double *fxw2 = fxw1 + tdma_fac_len(np + 1);
     d.fac_r1 = fr1;
     d.fac_x = fx;
     d.fac_rT = frT;
@@ -1274,6 +1274,7 @@ __global__ void k_prb_gang(GangTab g)
 struct gb_prb_gang {
     int n = 0, mixed = 0;
     int spread = 1;                // CTAs per equation of the batched multigrid (1 or a cluster)
+    size_t mg_smem = 0;            // shared memory of the mixed solves: the largest member's
     PrbDev *d_dev = nullptr;
     int *d_off = nullptr, *d_limit = nullptr;
     GangRec *d_rec = nullptr;
@@ -1333,6 +1334,7 @@ extern "C" int gb_prb_gang_create(gb_prb *const *members, const int *nsteps_tota
         prb_refresh_scalars(h);
         const PrbDev &d = h->dev;
         devs[q] = d;
+        g->mg_smem = std::max(g->mg_smem, prb_mg_smem(h));
         const size_t nr = d.nr, np = d.np;
         const int nb[GP_COUNT] = {(int)gb_ceil_div(np + 1, 64), (int)gb_ceil_div(nr - 1, 64),
                                   (int)gb_ceil_div((nr - 1) * (np + 1), TPB), (int)gb_ceil_div((nr - 1) * (np + 1), TPB),
@@ -1406,7 +1408,7 @@ static void prb_gang_enqueue_step(gb_prb_gang *g, cudaStream_t s)
     GL(GP_TROB);
     GL(GP_HEAT);
     GL(GP_RHS);
-    prb_mg_launch_eqs(g->d_eqs, 2 * g->n, g->mixed, g->spread, s);
+    prb_mg_launch_eqs(g->d_eqs, 2 * g->n, g->mixed, g->spread, g->mg_smem, s);
     GL(GP_UPD);
     GL(GP_REC);
 #undef GL

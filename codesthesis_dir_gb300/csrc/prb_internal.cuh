@@ -34,6 +34,7 @@ struct MgEq {
     int seam_keep;       // the annulus's corser keeps the coarse seam residual
     int xwall;           // the tank: side walls in x (velvor2dhorconvtank.f:1032-1303)
     int stop_on_max;     // the sweep limit fails the step (PRB's STOP) or only is reported
+    int smem_fac;        // mixed solve: floats of shared memory before its line buffer (>= the level-1 factors)
     double r0;
     double tolcon, sor;
     MgLevel lev[PRB_MAXLEV];
@@ -108,7 +109,8 @@ int prb_mg_levels(int nr, int variant);
 int prb_mg_create(gb_prb *h);
 void prb_mg_destroy(gb_prb *h);
 int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s);
-void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, int spread, cudaStream_t s);
+void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, int spread, size_t smem, cudaStream_t s);
+size_t prb_mg_smem(const gb_prb *h);
 int prb_mg_cluster_ctas();
 int prb_refresh_scalars(gb_prb *h);
 // the tank's transport (tank.cu)

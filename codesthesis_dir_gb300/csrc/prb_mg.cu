@@ -190,6 +190,70 @@ __device__ __forceinline__ void mg_line(const MgEq &E, const MgLevel &L, int k)
         for (int i = 1; i <= nrow; ++i) psif[GIX(i, 0, ld)] = E.xwall ? 0.0 : psif[GIX(i, k, ld)];
 }
 
+// Shared memory of the FP64 solves: the line buffer of the staged colour
+// sweeps (96 KB).
+#define MG64_LINE_DOUBLES 12288
+#define MG64_SMEM_BYTES (MG64_LINE_DOUBLES * 8)
+
+// One colour (lines k = 2t + 2 - parity, up to klast) of the zebra sweep, in
+// batches of lines staged in shared memory: the right-hand sides of mg_line
+// go in as [row][line] with an odd pitch (coalesced along rows), one thread
+// per line eliminates in place with the level's factors, the solutions go
+// back (with mg_line's seam copy).  The lines of a colour read only lines of
+// the other colour, so the values are mg_line's.  On a cluster the batches
+// go round the CTAs.
+template <class G>
+__device__ void mg_colour_smem(const MgEq &E, const MgLevel &L, int parity, int klast)
+{
+    extern __shared__ double s_mg64[];
+    const int ld = E.ld, n1 = L.n1, n3 = L.n3;
+    const int nrow = (E.which == 2) ? n1 : n1 - 1;
+    double *psif = E.psif;
+    const double *f = L.f, *rvq = L.rvq;
+    const double hhpi = L.hhpi;
+    const bool polar = E.polar;
+    const int nlines = n3 / 2;
+    int B = MG64_LINE_DOUBLES / nrow - 1;
+    if (B > nlines) B = nlines;
+    int rank = 0;
+    if constexpr (G::C > 1) rank = (int)cg::this_cluster().block_rank();
+    for (int b0 = rank * B; b0 < nlines; b0 += G::C * B) {
+        const int nb = (nlines - b0 < B) ? nlines - b0 : B;
+        const int pitch = nb | 1;
+        for (int j = threadIdx.x >> 5; j < nb; j += blockDim.x >> 5) {
+            const int k = 2 * (b0 + j) + 2 - parity;
+            if (k > klast) continue;
+            const int ka = (k == n3) ? (E.xwall ? 0 : 1) : k + 1, km = k - 1;
+            for (int i = 1 + (threadIdx.x & 31); i <= nrow; i += 32) {
+                double t = -(psif[GIX(i, ka, ld)] + psif[GIX(i, km, ld)]) * hhpi;
+                if (polar) t = t * rvq[i];
+                s_mg64[(i - 1) * pitch + j] = t + f[(size_t)k * (n1 + 1) + i];
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+            const int k = 2 * (b0 + j) + 2 - parity;
+            if (k > klast) continue;
+            double *x = s_mg64 + j;
+            auto in = [&](int q) -> double { return x[q * pitch]; };
+            if (E.which == 2) apply_pdma_rhs(L.fac, n1, x, pitch, in);
+            else apply_tdma_rhs(L.fac, n1 - 1, x, pitch, in);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x >> 5; j < nb; j += blockDim.x >> 5) {
+            const int k = 2 * (b0 + j) + 2 - parity;
+            if (k > klast) continue;
+            for (int i = 1 + (threadIdx.x & 31); i <= nrow; i += 32) {
+                const double v = s_mg64[(i - 1) * pitch + j];
+                psif[GIX(i, k, ld)] = v;
+                if (k == n3) psif[GIX(i, 0, ld)] = E.xwall ? 0.0 : v;
+            }
+        }
+        __syncthreads();
+    }
+    if constexpr (G::C > 1) G::sync();
+}
+
 // relax2 / relax3: line sweeps (one with nrel = 1; three in the annulus),
 // then the residual into rc, its max norm, and psif packed into v.  Only
 // the last sweep's residual is formed: the reference recomputes rc and
@@ -214,13 +278,7 @@ __device__ double mg_relax(const MgEq &E, int klev, double *s_red, int *nan_out)
                 for (int k = 1; k <= klast; ++k) mg_line(E, L, k);
             G::sync();
         } else {
-            for (int parity = 1; parity >= 0; --parity) {
-                for (int t = G::tid(); t < n3 / 2; t += G::nthr()) {
-                    const int k = 2 * t + 2 - parity;
-                    if (k <= klast) mg_line(E, L, k);
-                }
-                G::sync();
-            }
+            for (int parity = 1; parity >= 0; --parity) mg_colour_smem<G>(E, L, parity, klast);
         }
     }
     // residual, PRB:2306-2357 (v) and PRB:2553-2587 (u)
@@ -468,6 +526,7 @@ __device__ __forceinline__ void apply_pdma32(const float *fac, int n, float *x, 
     const float *icdiv = fac, *bk1 = fac + n, *aa = fac + 2 * n, *dn = fac + 3 * n, *en = fac + 4 * n;
     const float icN = fac[5 * n];
     float rk = rhs(0), rk1 = rhs(1);
+#pragma unroll 4
     for (int k = 0; k <= n - 2; ++k) {
         rk = rk * icdiv[k];
         x[k] = rk;
@@ -481,6 +540,7 @@ __device__ __forceinline__ void apply_pdma32(const float *fac, int n, float *x, 
     x[n - 1] = x1;
     float x0 = x[n - 2] - dn[n - 2] * x1;
     x[n - 2] = x0;
+#pragma unroll 4
     for (int j = n - 3; j >= 0; --j) {
         const float xj = x[j] - dn[j] * x0 - en[j] * x1;
         x[j] = xj;
@@ -495,6 +555,7 @@ __device__ __forceinline__ void apply_tdma32(const float *fac, int n, float *x, 
     const float *fact = fac, *ibp = fac + n, *c = fac + 2 * n;
     float prev = rhs(0);
     x[0] = prev;
+#pragma unroll 4
     for (int j = 1; j < n; ++j) {
         const float rj = rhs(j) - fact[j] * prev;
         x[j] = rj;
@@ -502,6 +563,7 @@ __device__ __forceinline__ void apply_tdma32(const float *fac, int n, float *x, 
     }
     float y = prev * ibp[n - 1];
     x[n - 1] = y;
+#pragma unroll 4
     for (int j = n - 2; j >= 0; --j) {
         y = (x[j] - c[j] * y) * ibp[j];
         x[j] = y;
@@ -537,47 +599,6 @@ __device__ __forceinline__ void mg_line32(const MgEq &E, const MgLevel &L, int k
 #define MG32_LINE_FLOATS 24576                // 96 KB of lines
 #define MG32_SMEM_BYTES ((MG32_FAC_FLOATS + MG32_LINE_FLOATS) * 4)
 
-__device__ __forceinline__ void pdma32_smem(const float *fac, int n, float *x, int pitch)
-{
-    const float *icdiv = fac, *bk1 = fac + n, *aa = fac + 2 * n, *dn = fac + 3 * n, *en = fac + 4 * n;
-    float rk = x[0], rk1 = x[pitch];
-    for (int k = 0; k <= n - 2; ++k) {
-        const float xr = (k + 2 < n) ? x[(k + 2) * pitch] : 0.f;
-        rk = rk * icdiv[k];
-        x[k * pitch] = rk;
-        rk1 = rk1 - bk1[k] * rk;
-        const float rk2 = (k != n - 2) ? xr - aa[k + 2] * rk : 0.f;
-        rk = rk1;
-        rk1 = rk2;
-    }
-    float x1 = rk * fac[5 * n];
-    x[(n - 1) * pitch] = x1;
-    float x0 = x[(n - 2) * pitch] - dn[n - 2] * x1;
-    x[(n - 2) * pitch] = x0;
-    for (int j = n - 3; j >= 0; --j) {
-        const float xj = x[j * pitch] - dn[j] * x0 - en[j] * x1;
-        x[j * pitch] = xj;
-        x1 = x0;
-        x0 = xj;
-    }
-}
-
-__device__ __forceinline__ void tdma32_smem(const float *fac, int n, float *x, int pitch)
-{
-    const float *fact = fac, *ibp = fac + n, *c = fac + 2 * n;
-    float prev = x[0];
-    for (int j = 1; j < n; ++j) {
-        prev = x[j * pitch] - fact[j] * prev;
-        x[j * pitch] = prev;
-    }
-    float y = prev * ibp[n - 1];
-    x[(n - 1) * pitch] = y;
-    for (int j = n - 2; j >= 0; --j) {
-        y = (x[j * pitch] - c[j] * y) * ibp[j];
-        x[j * pitch] = y;
-    }
-}
-
 // One colour (lines k = 2t + 2 - parity) of the zebra line sweep of the
 // correction cycle, in batches of lines staged in shared memory: right-hand
 // sides in (coalesced along rows), one thread per line eliminates, solutions
@@ -586,7 +607,7 @@ template <class G>
 __device__ void mg_colour32_smem(const MgEq &E, const MgLevel &L, int parity)
 {
     extern __shared__ float s_mg32[];
-    float *sfac = s_mg32, *sline = s_mg32 + MG32_FAC_FLOATS;
+    float *sfac = s_mg32, *sline = s_mg32 + E.smem_fac;
     const int ld = E.ld, n1 = L.n1, n3 = L.n3;
     const int nrow = (E.which == 2) ? n1 : n1 - 1;
     const int nfac = (E.which == 2) ? 5 * n1 + 1 : 3 * (n1 - 1);
@@ -978,7 +999,7 @@ int prb_mg_create(gb_prb *h)
     size_t per_eq = 2 * (size_t)ld * (np + 1) + (size_t)ld * (np + 1) + 8;   // psif, rc; psif32 + rc32
     for (int l = 1; l <= nlev; ++l) {
         const int n1 = nr * 2 / (1 << l), n3 = np * 2 / (1 << l);
-        per_eq += 2 * (size_t)(n1 + 1) * (n3 + 1) + 5 * (size_t)(n1 + 2) + 1 + 2 * (size_t)(n1 + 2);
+        per_eq += 2 * (size_t)(n1 + 1) * (n3 + 1) + pdma_fac_len(n1 + 2) + 2 * (size_t)(n1 + 2);
         // FP32: v32, f32, fac32, rvi32, rvq32 (counted in doubles, rounded up)
         per_eq += ((2 * (size_t)(n1 + 1) * (n3 + 1) + 5 * (size_t)(n1 + 2) + 1 + 2 * (size_t)(n1 + 2)) + 1) / 2 + 4;
     }
@@ -999,6 +1020,7 @@ int prb_mg_create(gb_prb *h)
         E.xwall = p.variant == GB_PRB_TANK || p.variant == GB_PRB_DVD;
         if (E.xwall && p.precision != GB_PRB_FP64) return GB_ERR_INVALID;
         E.stop_on_max = p.variant != GB_PRB_ANNULUS;
+        E.smem_fac = ((5 * nr + 1 + 31) / 32) * 32;   // the level-1 pentadiagonal factors, rounded to 128 B
         E.r0 = p.r0;
         double *base = h->mg_pool + q * per_eq;
         E.psif = base; base += (size_t)ld * (np + 1);
@@ -1021,7 +1043,7 @@ int prb_mg_create(gb_prb *h)
             const size_t sz = (size_t)(L.n1 + 1) * (L.n3 + 1);
             L.v = base; base += sz;
             L.f = base; base += sz;
-            L.fac = base; base += 5 * (size_t)(L.n1 + 2) + 1;
+            L.fac = base; base += pdma_fac_len(L.n1 + 2);   // >= tdma_fac_len(n1 - 1)
             L.rvi = base; base += (size_t)(L.n1 + 2);
             L.rvq = base; base += (size_t)(L.n1 + 2);
             float *fb = (float *)base;
@@ -1042,6 +1064,9 @@ int prb_mg_create(gb_prb *h)
         k_mg_factors32<<<1, 1>>>(E);
     }
     e = cudaFuncSetAttribute(k_mg_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, MG32_SMEM_BYTES);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mg_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, MG64_SMEM_BYTES);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mg_solve_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, MG64_SMEM_BYTES);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_mg_solve_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, MG32_SMEM_BYTES);
     if (e != cudaSuccess) { gb_set_error("multigrid shared memory: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
@@ -1061,19 +1086,29 @@ void prb_mg_destroy(gb_prb *h)
 
 // Refreshes the solve parameters that a caller may change between calls
 // (tolerance, sweep limit, smoother, SOR factor) and launches the solves.
+// Shared memory of one instance's mixed solve: its factors, then the line
+// buffer.
+size_t prb_mg_smem(const gb_prb *h)
+{
+    return sizeof(float) * ((size_t)h->eq_host[0].smem_fac + MG32_LINE_FLOATS);
+}
+
 // The solves of neq equation descriptors (any instances') in one launch,
 // one block or one cluster of MG_CLUSTER blocks each (the gangs' batched
-// multigrid).
-void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, int spread, cudaStream_t s)
+// multigrid); smem: the largest member's prb_mg_smem.  A gang step waits
+// for its slowest solve, so the solves keep the single-instance block of
+// MG_THREADS: with half-size blocks, two per SM, the served sweep's mixed
+// arm ran 1.5 instead of 2.25 solves/s.
+void prb_mg_launch_eqs(const MgEq *d_eqs, int neq, int mixed, int spread, size_t smem, cudaStream_t s)
 {
     if (neq <= 0) return;
     if (spread > 1) {
-        if (mixed) k_mg_solve_mixed_cluster<<<neq * MG_CLUSTER, MG_THREADS, MG32_SMEM_BYTES, s>>>(d_eqs, 0);
-        else k_mg_solve_cluster<<<neq * MG_CLUSTER, MG_THREADS, 0, s>>>(d_eqs, 0);
+        if (mixed) k_mg_solve_mixed_cluster<<<neq * MG_CLUSTER, MG_THREADS, smem, s>>>(d_eqs, 0);
+        else k_mg_solve_cluster<<<neq * MG_CLUSTER, MG_THREADS, MG64_SMEM_BYTES, s>>>(d_eqs, 0);
     } else if (mixed) {
-        k_mg_solve_mixed<<<neq, MG_THREADS, MG32_SMEM_BYTES, s>>>(d_eqs, 0);
+        k_mg_solve_mixed<<<neq, MG_THREADS, smem, s>>>(d_eqs, 0);
     } else {
-        k_mg_solve<<<neq, MG_THREADS, 0, s>>>(d_eqs, 0);
+        k_mg_solve<<<neq, MG_THREADS, MG64_SMEM_BYTES, s>>>(d_eqs, 0);
     }
 }
 
@@ -1095,12 +1130,12 @@ int prb_launch_mg(gb_prb *h, int do_v, int do_u, cudaStream_t s)
     if (n == 0) return GB_OK;
     const bool spread = h->mg_spread > 1 && h->p.smoother == GB_SMOOTHER_ZEBRA;
     if (h->p.precision == GB_PRB_MIXED) {
-        if (spread) k_mg_solve_mixed_cluster<<<n * MG_CLUSTER, MG_THREADS, MG32_SMEM_BYTES, s>>>(h->eq_dev, first);
-        else k_mg_solve_mixed<<<n, MG_THREADS, MG32_SMEM_BYTES, s>>>(h->eq_dev, first);
+        if (spread) k_mg_solve_mixed_cluster<<<n * MG_CLUSTER, MG_THREADS, prb_mg_smem(h), s>>>(h->eq_dev, first);
+        else k_mg_solve_mixed<<<n, MG_THREADS, prb_mg_smem(h), s>>>(h->eq_dev, first);
     } else if (spread) {
-        k_mg_solve_cluster<<<n * MG_CLUSTER, MG_THREADS, 0, s>>>(h->eq_dev, first);
+        k_mg_solve_cluster<<<n * MG_CLUSTER, MG_THREADS, MG64_SMEM_BYTES, s>>>(h->eq_dev, first);
     } else {
-        k_mg_solve<<<n, MG_THREADS, 0, s>>>(h->eq_dev, first);
+        k_mg_solve<<<n, MG_THREADS, MG64_SMEM_BYTES, s>>>(h->eq_dev, first);
     }
     h->launches += 1;
     return GB_OK;

@@ -25,6 +25,7 @@
 // one-sided boundary rows last.
 #include "gbcommon.cuh"
 #include "gridsync.cuh"
+#include "divrn.cuh"
 
 #include <math.h>
 #include <stdlib.h>
@@ -632,7 +633,7 @@ __host__ __device__ __forceinline__ int r3_len(int comp, int dir, int n1, int n2
 }
 __host__ __device__ __forceinline__ int r3_tabsize(int kind, int n)
 {
-    return kind == 0 ? 5 * n : kind == 1 ? 3 * n : 6 * n;
+    return kind == 0 ? 6 * n : kind == 1 ? 4 * n : 7 * n;   // the last n: reciprocals of the pivots
 }
 __host__ __device__ __forceinline__ int r3_imax(int comp, int n1) { return comp == 3 ? n1 - 1 : n1; }
 __host__ __device__ __forceinline__ int r3_jmax(int comp, int n2) { return comp == 1 ? n2 - 1 : n2; }
@@ -810,6 +811,7 @@ __global__ void k_r3d_factors(const __grid_constant__ R3Dev d, const FacJob *job
                 Cc[k + 2] = Cc[k + 2] - Aa[k + 2] * Ee[k];
             }
         }
+        for (int k = 0; k < n; ++k) T[5 * n + k] = 1.0 / Cc[k];
     } else if (kind == 1) {
         double *F = T, *Bb = T + n, *Cc = T + 2 * n;
         double dummy_d, dummy_e;
@@ -820,6 +822,7 @@ __global__ void k_r3d_factors(const __grid_constant__ R3Dev d, const FacJob *job
             Bb[j] = Bb[j] - fact * Cc[j - 1];
             F[j] = fact;
         }
+        for (int j = 0; j < n; ++j) T[3 * n + j] = 1.0 / Bb[j];
     } else {
         double *a = T, *b = T + n, *c = T + 2 * n, *F1 = T + 3 * n, *F2 = T + 4 * n, *F3 = T + 5 * n;
         double dummy_d, dummy_e;
@@ -851,6 +854,7 @@ __global__ void k_r3d_factors(const __grid_constant__ R3Dev d, const FacJob *job
         fact = a[N] / b[n - 2];
         b[N] = b[N] - fact * c[n - 2];
         F3[0] = fact;
+        for (int j = 0; j < n; ++j) T[6 * n + j] = 1.0 / b[j];
     }
 }
 
@@ -998,11 +1002,11 @@ __device__ void r3_line(const R3Lev &L, const R3Work &W, int dir, int p, int q, 
         if (seam) v[base + (size_t)((long long)(e) * step) - plane] = _x;             \
     } while (0)
     if (kind == 0) {
-        const double *Cc = T, *Bb = T + n, *Aa = T + 2 * n, *Dd = T + 3 * n, *Ee = T + 4 * n;
+        const double *Cc = T, *Bb = T + n, *Aa = T + 2 * n, *Dd = T + 3 * n, *Ee = T + 4 * n, *iC = T + 5 * n;
         double r0 = s[0], r1 = s[1];
 #pragma unroll 4
         for (int k = 0; k <= n - 2; ++k) {
-            const double rk = r0 / Cc[k];
+            const double rk = div_by_rcp(r0, Cc[k], iC[k]);
             s[k] = rk;
             const double rk1 = r1 - Bb[k + 1] * rk;
             double rk2 = 0.0;
@@ -1010,7 +1014,7 @@ __device__ void r3_line(const R3Lev &L, const R3Work &W, int dir, int p, int q, 
             r0 = rk1;
             r1 = rk2;
         }
-        double x1 = r0 / Cc[n - 1];
+        double x1 = div_by_rcp(r0, Cc[n - 1], iC[n - 1]);
         PUT(n - 1, x1);
         double x0 = s[n - 2] - Dd[n - 2] * x1;
         PUT(n - 2, x0);
@@ -1024,7 +1028,7 @@ __device__ void r3_line(const R3Lev &L, const R3Work &W, int dir, int p, int q, 
             x1 = x;
         }
     } else if (kind == 1) {
-        const double *F = T, *Bb = T + n, *Cc = T + 2 * n;
+        const double *F = T, *Bb = T + n, *Cc = T + 2 * n, *iB = T + 3 * n;
         double rprev = s[0];
 #pragma unroll 4
         for (int j = 1; j < n; ++j) {
@@ -1032,15 +1036,16 @@ __device__ void r3_line(const R3Lev &L, const R3Work &W, int dir, int p, int q, 
             s[j] = rj;
             rprev = rj;
         }
-        double y = rprev / Bb[n - 1];
+        double y = div_by_rcp(rprev, Bb[n - 1], iB[n - 1]);
         PUT(n - 1, y);
 #pragma unroll 4
         for (int j = n - 2; j >= 0; --j) {
-            y = (s[j] - Cc[j] * y) / Bb[j];
+            y = div_by_rcp(s[j] - Cc[j] * y, Bb[j], iB[j]);
             PUT(j, y);
         }
     } else {
         const double *Aa = T, *Bb = T + n, *Cc = T + 2 * n, *F1 = T + 3 * n, *F2 = T + 4 * n, *F3 = T + 5 * n;
+        const double *iB = T + 6 * n;
         const int N = n - 1;
         double rN = s[N];
         double rprev = s[0];
@@ -1054,13 +1059,13 @@ __device__ void r3_line(const R3Lev &L, const R3Work &W, int dir, int p, int q, 
         const double rn2 = s[n - 2] - F1[n - 2] * rprev;
         rN = rN - F2[n - 2] * rprev;
         rN = rN - F3[0] * rn2;
-        const double yN = rN / Bb[N];
+        const double yN = div_by_rcp(rN, Bb[N], iB[N]);
         PUT(N, yN);
-        double y = (rn2 - Cc[n - 2] * yN) / Bb[n - 2];
+        double y = div_by_rcp(rn2 - Cc[n - 2] * yN, Bb[n - 2], iB[n - 2]);
         PUT(n - 2, y);
 #pragma unroll 4
         for (int j = n - 3; j >= 0; --j) {
-            y = (s[j] - Cc[j] * y - Aa[j] * yN) / Bb[j];
+            y = div_by_rcp(s[j] - Cc[j] * y - Aa[j] * yN, Bb[j], iB[j]);
             PUT(j, y);
         }
         v[base - (size_t)step] = yN;   // plane 0 = plane n3
@@ -1600,6 +1605,7 @@ __device__ void r3_line32(const R3Lev &L, const R3Work &W, int dir, int p, int q
     if (kind == 0) {
         const float *Ci = T, *Bb = T + n, *Aa = T + 2 * n, *Dd = T + 3 * n, *Ee = T + 4 * n;
         float r0 = s[0], r1 = s[1];
+#pragma unroll 4
         for (int k = 0; k <= n - 2; ++k) {
             const float rk = r0 * Ci[k];
             s[k] = rk;
@@ -1615,6 +1621,7 @@ __device__ void r3_line32(const R3Lev &L, const R3Work &W, int dir, int p, int q
         PUT(n - 2, x0);
         float x2 = x1;
         x1 = x0;
+#pragma unroll 4
         for (int j = n - 3; j >= 0; --j) {
             const float x = __fmaf_rn(-Ee[j], x2, __fmaf_rn(-Dd[j], x1, s[j]));
             PUT(j, x);
@@ -1624,6 +1631,7 @@ __device__ void r3_line32(const R3Lev &L, const R3Work &W, int dir, int p, int q
     } else if (kind == 1) {
         const float *F = T, *Bi = T + n, *Cc = T + 2 * n;
         float rprev = s[0];
+#pragma unroll 4
         for (int j = 1; j < n; ++j) {
             const float rj = __fmaf_rn(-F[j], rprev, s[j]);
             s[j] = rj;
@@ -1631,6 +1639,7 @@ __device__ void r3_line32(const R3Lev &L, const R3Work &W, int dir, int p, int q
         }
         float y = rprev * Bi[n - 1];
         PUT(n - 1, y);
+#pragma unroll 4
         for (int j = n - 2; j >= 0; --j) {
             y = __fmaf_rn(-Cc[j], y, s[j]) * Bi[j];
             PUT(j, y);
@@ -1640,6 +1649,7 @@ __device__ void r3_line32(const R3Lev &L, const R3Work &W, int dir, int p, int q
         const int N = n - 1;
         float rN = s[N];
         float rprev = s[0];
+#pragma unroll 4
         for (int j = 1; j <= n - 3; ++j) {
             const float rj = __fmaf_rn(-F1[j], rprev, s[j]);
             rN = __fmaf_rn(-F2[j], rprev, rN);
@@ -1653,6 +1663,7 @@ __device__ void r3_line32(const R3Lev &L, const R3Work &W, int dir, int p, int q
         PUT(N, yN);
         float y = __fmaf_rn(-Cc[n - 2], yN, rn2) * Bi[n - 2];
         PUT(n - 2, y);
+#pragma unroll 4
         for (int j = n - 3; j >= 0; --j) {
             y = __fmaf_rn(-Aa[j], yN, __fmaf_rn(-Cc[j], y, s[j])) * Bi[j];
             PUT(j, y);

@@ -31,6 +31,7 @@
 struct StrLevel {
     int n1, n2;
     double *r, *cr, *crr, *czz;
+    double *ir, *irr;         // 1/r and 1/(r*r) per row (IEEE, host): the divisors' reciprocals
     double *v, *f;            // packed (n1+1)*(n2+1)
     double *fac_r, *fac_z;    // per r-line j (5(n1-1)+1 each), per z-line i (5(n2-1)+1 each)
     // mixed precision: FP32 copies (pivots of the factors as reciprocals)
@@ -118,7 +119,7 @@ __global__ void k_str_factors(const __grid_constant__ StrDev d, const StrJob *jo
     double *w = work + (size_t)q * wstride;
     double *a = w, *b = w + n, *c = w + 2 * n, *dd = w + 3 * n, *e = w + 4 * n, *scratch = w + 5 * n;
     str_line_matrix(L, J.dir, J.line, a, b, c, dd, e);
-    double *fac = J.dir == 0 ? L.fac_r + (size_t)(J.line - 1) * (5 * n + 1) : L.fac_z + (size_t)(J.line - 1) * (5 * n + 1);
+    double *fac = J.dir == 0 ? L.fac_r + (size_t)(J.line - 1) * pdma_fac_len(n) : L.fac_z + (size_t)(J.line - 1) * pdma_fac_len(n);
     factor_pdma(a, b, c, dd, e, n, fac, scratch);
 }
 
@@ -136,7 +137,7 @@ __device__ __forceinline__ void str_rline(const StrDev &d, const StrLevel &L, in
                f[(size_t)i + (size_t)(n1 + 1) * j];
     };
     const int n = n1 - 1;
-    apply_pdma_rhs(L.fac_r + (size_t)(j - 1) * (5 * n + 1), n, &PS(1, j), 1, rhs);
+    apply_pdma_rhs(L.fac_r + (size_t)(j - 1) * pdma_fac_len(n), n, &PS(1, j), 1, rhs);
 }
 
 // z-line i: right-hand side of row j (rcsc.f:1279-1290)
@@ -149,14 +150,97 @@ __device__ __forceinline__ void str_zline(const StrDev &d, const StrLevel &L, in
         const int j = q + 1;
         if (i <= n1 / 2)
             return -(CRR(i, 1) * PS(i - 1, j) + CRR(i, 3) * PS(i + 1, j) + CRR(i, 4) * PS(i + 2, j) +
-                     (CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j)) / r) +
+                     div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i])) +
                    f[(size_t)i + (size_t)(n1 + 1) * j];
         return -(CRR(i, 1) * PS(i - 2, j) + CRR(i, 2) * PS(i - 1, j) + CRR(i, 4) * PS(i + 1, j) +
-                 (CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j)) / r) +
+                 div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i])) +
                f[(size_t)i + (size_t)(n1 + 1) * j];
     };
     const int n = n2 - 1;
-    apply_pdma_rhs(L.fac_z + (size_t)(i - 1) * (5 * n + 1), n, &PS(i, 1), d.ld, rhs);
+    apply_pdma_rhs(L.fac_z + (size_t)(i - 1) * pdma_fac_len(n), n, &PS(i, 1), d.ld, rhs);
+}
+
+// Shared memory of a solve: the line buffer of the staged two-direction
+// sweeps (96 KB: 12288 doubles or 24576 floats).
+#define STR_LINE_BYTES (96 * 1024)
+
+// Right-hand sides of r-line j at row i and of z-line i at row j, as
+// str_rline and str_zline form them.
+__device__ __forceinline__ double str_rhs_r(const StrDev &d, const StrLevel &L, int j, int i)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const double *f = L.f;
+    if (j <= n2 / 2)
+        return -(CZZ(j, 1) * PS(i, j - 1) + CZZ(j, 3) * PS(i, j + 1) + CZZ(j, 4) * PS(i, j + 2)) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    return -(CZZ(j, 1) * PS(i, j - 2) + CZZ(j, 2) * PS(i, j - 1) + CZZ(j, 4) * PS(i, j + 1)) +
+           f[(size_t)i + (size_t)(n1 + 1) * j];
+}
+
+__device__ __forceinline__ double str_rhs_z(const StrDev &d, const StrLevel &L, int i, int j)
+{
+    const int n1 = L.n1;
+    const double *f = L.f;
+    const double r = L.r[i];
+    if (i <= n1 / 2)
+        return -(CRR(i, 1) * PS(i - 1, j) + CRR(i, 3) * PS(i + 1, j) + CRR(i, 4) * PS(i + 2, j) +
+                 div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i])) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    return -(CRR(i, 1) * PS(i - 2, j) + CRR(i, 2) * PS(i - 1, j) + CRR(i, 4) * PS(i + 1, j) +
+             div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i])) +
+           f[(size_t)i + (size_t)(n1 + 1) * j];
+}
+
+// One colour (every fourth line from `first`) of one direction (DIR 0:
+// r-lines j, DIR 1: z-lines i) in batches staged in shared memory: the
+// right-hand sides go in as [row][line] with an odd pitch (coalesced along
+// the grid's rows, conflict-free for the per-line elimination), one thread
+// per line eliminates in place, the solutions go back.  The lines of a
+// colour read only lines of the other colours, so staging changes no value.
+template <int DIR>
+__device__ void str_colour_smem(const StrDev &d, const StrLevel &L, int first, double *sline)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const int lines = DIR == 0 ? n2 - 1 : n1 - 1, n = DIR == 0 ? n1 - 1 : n2 - 1;
+    if (first > lines) return;
+    const int nl = (lines - first) / 4 + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int B = (int)(STR_LINE_BYTES / sizeof(double)) / n - 1;
+    if (B < 1) {   // lines too long to stage: one thread per line on the level's arrays
+        for (int t = threadIdx.x; t < nl; t += blockDim.x) {
+            if (DIR == 0) str_rline(d, L, first + 4 * t);
+            else str_zline(d, L, first + 4 * t);
+        }
+        __syncthreads();
+        return;
+    }
+    if (B > nl) B = nl;
+    for (int b0 = 0; b0 < nl; b0 += B) {
+        const int nb = min(B, nl - b0), pitch = nb | 1;
+        if (DIR == 0) {
+            for (int t = warp; t < nb; t += nw)
+                for (int q = lane; q < n; q += 32) sline[q * pitch + t] = str_rhs_r(d, L, first + 4 * (b0 + t), q + 1);
+        } else {
+            for (int q = warp; q < n; q += nw)
+                for (int t = lane; t < nb; t += 32) sline[q * pitch + t] = str_rhs_z(d, L, first + 4 * (b0 + t), q + 1);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+            const int line = first + 4 * (b0 + t);
+            double *x = sline + t;
+            const double *fac = (DIR == 0 ? L.fac_r : L.fac_z) + (size_t)(line - 1) * pdma_fac_len(n);
+            apply_pdma_rhs(fac, n, x, pitch, [&](int q) -> double { return x[q * pitch]; });
+        }
+        __syncthreads();
+        if (DIR == 0) {
+            for (int t = warp; t < nb; t += nw)
+                for (int q = lane; q < n; q += 32) PS(q + 1, first + 4 * (b0 + t)) = sline[q * pitch + t];
+        } else {
+            for (int q = warp; q < n; q += nw)
+                for (int t = lane; t < nb; t += 32) PS(first + 4 * (b0 + t), q + 1) = sline[q * pitch + t];
+        }
+        __syncthreads();
+    }
 }
 
 __device__ __forceinline__ double str_blk_max(double v, double *s_red)
@@ -197,16 +281,9 @@ __device__ double str_relax(const StrDev &d, int klev, double *s_red, int *nan_o
             }
             __syncthreads();
         } else {
-            for (int c = 1; c <= 4; ++c) {
-                const int first = (c & 3) == 0 ? 4 : (c & 3);
-                for (int j = first + 4 * threadIdx.x; j <= n2 - 1; j += 4 * blockDim.x) str_rline(d, L, j);
-                __syncthreads();
-            }
-            for (int c = 1; c <= 4; ++c) {
-                const int first = (c & 3) == 0 ? 4 : (c & 3);
-                for (int i = first + 4 * threadIdx.x; i <= n1 - 1; i += 4 * blockDim.x) str_zline(d, L, i);
-                __syncthreads();
-            }
+            extern __shared__ double s_str_line[];
+            for (int c = 1; c <= 4; ++c) str_colour_smem<0>(d, L, (c & 3) == 0 ? 4 : (c & 3), s_str_line);
+            for (int c = 1; c <= 4; ++c) str_colour_smem<1>(d, L, (c & 3) == 0 ? 4 : (c & 3), s_str_line);
         }
         m = 0.0;
         nan = 0;
@@ -217,12 +294,12 @@ __device__ double str_relax(const StrDev &d, int klev, double *s_red, int *nan_o
             double temp;
             if (i <= n1 / 2)
                 temp = CRR(i, 1) * PS(i - 1, j) + CRR(i, 2) * PS(i, j) + CRR(i, 3) * PS(i + 1, j) +
-                       CRR(i, 4) * PS(i + 2, j) + (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r -
-                       PS(i, j) / (r * r);
+                       CRR(i, 4) * PS(i + 2, j) + div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i]) -
+                       div_by_rcp(PS(i, j), r * r, L.irr[i]);
             else
                 temp = CRR(i, 1) * PS(i - 2, j) + CRR(i, 2) * PS(i - 1, j) + CRR(i, 3) * PS(i, j) +
-                       CRR(i, 4) * PS(i + 1, j) + (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r -
-                       PS(i, j) / (r * r);
+                       CRR(i, 4) * PS(i + 1, j) + div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i]) -
+                       div_by_rcp(PS(i, j), r * r, L.irr[i]);
             if (j <= n2 / 2)
                 temp = temp + CZZ(j, 1) * PS(i, j - 1) + CZZ(j, 2) * PS(i, j) + CZZ(j, 3) * PS(i, j + 1) +
                        CZZ(j, 4) * PS(i, j + 2);
@@ -377,7 +454,6 @@ __global__ void __launch_bounds__(STR_THREADS) k_str_solve(const __grid_constant
 // psi += e in FP64 (rcsc.f's solve has no over-relaxation).  The FP32 line
 // eliminations multiply by stored reciprocal pivots.
 // ---------------------------------------------------------------------------
-#define STR32_SMEM_BYTES 0
 #define PS32(i, j) d.psif32[(size_t)(i) + (size_t)d.ld * (size_t)(j)]
 #define CR32(i, k) L.cr32[3 * ((i) - 1) + (k) - 1]
 #define CRR32(i, k) L.crr32[4 * ((i) - 1) + (k) - 1]
@@ -390,6 +466,7 @@ __device__ inline void apply_pdma_rhs32(const float *fac, int n, float *x, int s
     const float icN = fac[5 * n];
     float rk = rhs(0);
     float rk1 = rhs(1);
+#pragma unroll 4
     for (int k = 0; k <= n - 2; ++k) {
         rk = rk * icdiv[k];
         x[(size_t)k * stride] = rk;
@@ -403,6 +480,7 @@ __device__ inline void apply_pdma_rhs32(const float *fac, int n, float *x, int s
     x[(size_t)(n - 1) * stride] = x1;
     float x0 = x[(size_t)(n - 2) * stride] - dn[n - 2] * x1;
     x[(size_t)(n - 2) * stride] = x0;
+#pragma unroll 4
     for (int j = n - 3; j >= 0; --j) {
         const float xj = x[(size_t)j * stride] - dn[j] * x0 - en[j] * x1;
         x[(size_t)j * stride] = xj;
@@ -446,6 +524,77 @@ __device__ __forceinline__ void str_zline32(const StrDev &d, const StrLevel &L, 
     apply_pdma_rhs32(L.fac_z32 + (size_t)(i - 1) * (5 * n + 1), n, &PS32(i, 1), d.ld, rhs);
 }
 
+__device__ __forceinline__ float str_rhs_r32(const StrDev &d, const StrLevel &L, int j, int i)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const float *f = L.f32;
+    if (j <= n2 / 2)
+        return -(CZZ32(j, 1) * PS32(i, j - 1) + CZZ32(j, 3) * PS32(i, j + 1) + CZZ32(j, 4) * PS32(i, j + 2)) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    return -(CZZ32(j, 1) * PS32(i, j - 2) + CZZ32(j, 2) * PS32(i, j - 1) + CZZ32(j, 4) * PS32(i, j + 1)) +
+           f[(size_t)i + (size_t)(n1 + 1) * j];
+}
+
+__device__ __forceinline__ float str_rhs_z32(const StrDev &d, const StrLevel &L, int i, int j)
+{
+    const int n1 = L.n1;
+    const float *f = L.f32;
+    const float ir = 1.0f / L.r32[i];
+    if (i <= n1 / 2)
+        return -(CRR32(i, 1) * PS32(i - 1, j) + CRR32(i, 3) * PS32(i + 1, j) + CRR32(i, 4) * PS32(i + 2, j) +
+                 (CR32(i, 1) * PS32(i - 1, j) + CR32(i, 3) * PS32(i + 1, j)) * ir) +
+               f[(size_t)i + (size_t)(n1 + 1) * j];
+    return -(CRR32(i, 1) * PS32(i - 2, j) + CRR32(i, 2) * PS32(i - 1, j) + CRR32(i, 4) * PS32(i + 1, j) +
+             (CR32(i, 1) * PS32(i - 1, j) + CR32(i, 3) * PS32(i + 1, j)) * ir) +
+           f[(size_t)i + (size_t)(n1 + 1) * j];
+}
+
+// str_colour_smem in FP32 (the correction cycle).
+template <int DIR>
+__device__ void str_colour_smem32(const StrDev &d, const StrLevel &L, int first, float *sline)
+{
+    const int n1 = L.n1, n2 = L.n2;
+    const int lines = DIR == 0 ? n2 - 1 : n1 - 1, n = DIR == 0 ? n1 - 1 : n2 - 1;
+    if (first > lines) return;
+    const int nl = (lines - first) / 4 + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int B = (int)(STR_LINE_BYTES / sizeof(float)) / n - 1;
+    if (B < 1) {
+        for (int t = threadIdx.x; t < nl; t += blockDim.x) {
+            if (DIR == 0) str_rline32(d, L, first + 4 * t);
+            else str_zline32(d, L, first + 4 * t);
+        }
+        __syncthreads();
+        return;
+    }
+    if (B > nl) B = nl;
+    for (int b0 = 0; b0 < nl; b0 += B) {
+        const int nb = min(B, nl - b0), pitch = nb | 1;
+        if (DIR == 0) {
+            for (int t = warp; t < nb; t += nw)
+                for (int q = lane; q < n; q += 32) sline[q * pitch + t] = str_rhs_r32(d, L, first + 4 * (b0 + t), q + 1);
+        } else {
+            for (int q = warp; q < n; q += nw)
+                for (int t = lane; t < nb; t += 32) sline[q * pitch + t] = str_rhs_z32(d, L, first + 4 * (b0 + t), q + 1);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+            const int line = first + 4 * (b0 + t);
+            const float *fac = (DIR == 0 ? L.fac_r32 : L.fac_z32) + (size_t)(line - 1) * (5 * n + 1);
+            pdma32_smem(fac, n, sline + t, pitch);
+        }
+        __syncthreads();
+        if (DIR == 0) {
+            for (int t = warp; t < nb; t += nw)
+                for (int q = lane; q < n; q += 32) PS32(q + 1, first + 4 * (b0 + t)) = sline[q * pitch + t];
+        } else {
+            for (int q = warp; q < n; q += nw)
+                for (int t = lane; t < nb; t += 32) PS32(first + 4 * (b0 + t), q + 1) = sline[q * pitch + t];
+        }
+        __syncthreads();
+    }
+}
+
 // nrel sweeps of both line directions on level klev, then the residual of
 // the correction into rc32 (for the restriction that follows).
 __device__ void str_relax32(const StrDev &d, int klev)
@@ -466,16 +615,9 @@ __device__ void str_relax32(const StrDev &d, int klev)
             }
             __syncthreads();
         } else {
-            for (int c = 1; c <= 4; ++c) {
-                const int first = (c & 3) == 0 ? 4 : (c & 3);
-                for (int j = first + 4 * threadIdx.x; j <= n2 - 1; j += 4 * blockDim.x) str_rline32(d, L, j);
-                __syncthreads();
-            }
-            for (int c = 1; c <= 4; ++c) {
-                const int first = (c & 3) == 0 ? 4 : (c & 3);
-                for (int i = first + 4 * threadIdx.x; i <= n1 - 1; i += 4 * blockDim.x) str_zline32(d, L, i);
-                __syncthreads();
-            }
+            extern __shared__ float s_str_line32[];
+            for (int c = 1; c <= 4; ++c) str_colour_smem32<0>(d, L, (c & 3) == 0 ? 4 : (c & 3), s_str_line32);
+            for (int c = 1; c <= 4; ++c) str_colour_smem32<1>(d, L, (c & 3) == 0 ? 4 : (c & 3), s_str_line32);
         }
     }
     const int ni = n1 - 1, tot = ni * (n2 - 1);
@@ -572,10 +714,10 @@ __device__ __forceinline__ double str_resid64(const StrDev &d, const StrLevel &L
     double temp;
     if (i <= n1 / 2)
         temp = CRR(i, 1) * PS(i - 1, j) + CRR(i, 2) * PS(i, j) + CRR(i, 3) * PS(i + 1, j) + CRR(i, 4) * PS(i + 2, j) +
-               (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r - PS(i, j) / (r * r);
+               div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i]) - div_by_rcp(PS(i, j), r * r, L.irr[i]);
     else
         temp = CRR(i, 1) * PS(i - 2, j) + CRR(i, 2) * PS(i - 1, j) + CRR(i, 3) * PS(i, j) + CRR(i, 4) * PS(i + 1, j) +
-               (CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j)) / r - PS(i, j) / (r * r);
+               div_by_rcp(CR(i, 1) * PS(i - 1, j) + CR(i, 2) * PS(i, j) + CR(i, 3) * PS(i + 1, j), r, L.ir[i]) - div_by_rcp(PS(i, j), r * r, L.irr[i]);
     if (j <= n2 / 2)
         temp = temp + CZZ(j, 1) * PS(i, j - 1) + CZZ(j, 2) * PS(i, j) + CZZ(j, 3) * PS(i, j + 1) + CZZ(j, 4) * PS(i, j + 2);
     else
@@ -668,9 +810,9 @@ __global__ void k_str_factors32(const __grid_constant__ StrDev d)
     };
     const int nr = a - 1, nz = b - 1;
     for (int j = 1; j <= b - 1; ++j)
-        conv(L.fac_r + (size_t)(j - 1) * (5 * nr + 1), L.fac_r32 + (size_t)(j - 1) * (5 * nr + 1), nr);
+        conv(L.fac_r + (size_t)(j - 1) * pdma_fac_len(nr), L.fac_r32 + (size_t)(j - 1) * (5 * nr + 1), nr);
     for (int i = 1; i <= a - 1; ++i)
-        conv(L.fac_z + (size_t)(i - 1) * (5 * nz + 1), L.fac_z32 + (size_t)(i - 1) * (5 * nz + 1), nz);
+        conv(L.fac_z + (size_t)(i - 1) * pdma_fac_len(nz), L.fac_z32 + (size_t)(i - 1) * (5 * nz + 1), nz);
 }
 
 #undef PS32
@@ -736,8 +878,8 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
     size_t need = 2 * (size_t)d.ld * d.ld + 2 * (size_t)(n1 + 1) * (n2 + 1);
     for (int l = 0; l < nlev; ++l) {
         const size_t a = lv[l].n1, b = lv[l].n2;
-        need += (a + 1) + 3 * (a - 1) + 4 * (a - 1) + 4 * (b - 1) + 2 * (a + 1) * (b + 1);
-        need += (b - 1) * (5 * (a - 1) + 1) + (a - 1) * (5 * (b - 1) + 1);
+        need += 3 * (a + 1) + 3 * (a - 1) + 4 * (a - 1) + 4 * (b - 1) + 2 * (a + 1) * (b + 1);
+        need += (b - 1) * pdma_fac_len((int)a - 1) + (a - 1) * pdma_fac_len((int)b - 1);
     }
     // FP32 copies: psif32, rc32 and every level's tables (half a double each, rounded up per array)
     size_t need32 = 2 * (size_t)d.ld * d.ld + 16;
@@ -764,14 +906,25 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
         L.n1 = a;
         L.n2 = bb;
         L.r = b; b += a + 1;
+        L.ir = b; b += a + 1;
+        L.irr = b; b += a + 1;
         L.cr = b; b += 3 * (size_t)(a - 1);
         L.crr = b; b += 4 * (size_t)(a - 1);
         L.czz = b; b += 4 * (size_t)(bb - 1);
         L.v = b; b += (size_t)(a + 1) * (bb + 1);
         L.f = b; b += (size_t)(a + 1) * (bb + 1);
-        L.fac_r = b; b += (size_t)(bb - 1) * (5 * (a - 1) + 1);
-        L.fac_z = b; b += (size_t)(a - 1) * (5 * (bb - 1) + 1);
+        L.fac_r = b; b += (size_t)(bb - 1) * pdma_fac_len((int)a - 1);
+        L.fac_z = b; b += (size_t)(a - 1) * pdma_fac_len((int)bb - 1);
         cudaMemcpy(L.r, lv[l].r, sizeof(double) * (a + 1), cudaMemcpyHostToDevice);
+        {
+            std::vector<double> inv(2 * (size_t)(a + 1));
+            for (int i = 0; i <= a; ++i) {
+                const double r = lv[l].r[i];
+                inv[i] = 1.0 / r;
+                inv[a + 1 + i] = 1.0 / (r * r);
+            }
+            cudaMemcpy(L.ir, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice);
+        }
         cudaMemcpy(L.cr, lv[l].cr, sizeof(double) * 3 * (a - 1), cudaMemcpyHostToDevice);
         cudaMemcpy(L.crr, lv[l].crr, sizeof(double) * 4 * (a - 1), cudaMemcpyHostToDevice);
         cudaMemcpy(L.czz, lv[l].czz, sizeof(double) * 4 * (bb - 1), cudaMemcpyHostToDevice);
@@ -833,6 +986,9 @@ extern "C" int gb_str_create(int nlev, const gb_str_level *lv, double tolcon, in
     d.status = h->status;
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { gb_str_destroy(h); gb_set_error("gb_str_create: stream"); return GB_ERR_CUDA; }
+    e = cudaFuncSetAttribute(k_str_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, STR_LINE_BYTES);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_str_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, STR_LINE_BYTES);
+    if (e != cudaSuccess) { gb_str_destroy(h); gb_set_error("gb_str_create: shared memory: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
     *out = h;
     return GB_OK;
 }
@@ -854,8 +1010,8 @@ cudaError_t gb_str_launch_device(const gb_str *h, double *psi, const double *rhs
     d.io_rhs = const_cast<double *>(rhs);
     d.status = status;
     d.abort = abort;
-    if (mixed) k_str_solve_mixed<<<1, STR_THREADS, STR32_SMEM_BYTES, s>>>(d);
-    else k_str_solve<<<1, STR_THREADS, 0, s>>>(d);
+    if (mixed) k_str_solve_mixed<<<1, STR_THREADS, STR_LINE_BYTES, s>>>(d);
+    else k_str_solve<<<1, STR_THREADS, STR_LINE_BYTES, s>>>(d);
     return cudaGetLastError();
 }
 
@@ -870,7 +1026,7 @@ extern "C" int gb_str_poisson(gb_str *h, double *psi, const double *rhs, int ld,
                                   h->stream));
     GB_CUDA_TRY(cudaMemcpy2DAsync(d.io_rhs, row, rhs, sizeof(double) * (size_t)ld, row, n2 + 1, cudaMemcpyHostToDevice,
                                   h->stream));
-    k_str_solve<<<1, STR_THREADS, 0, h->stream>>>(d);
+    k_str_solve<<<1, STR_THREADS, STR_LINE_BYTES, h->stream>>>(d);
     GB_CUDA_TRY(cudaGetLastError());
     int st[2] = {0, 0};
     GB_CUDA_TRY(cudaMemcpyAsync(st, d.status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));

@@ -249,6 +249,7 @@ SIGNATURES = [
     ("gb_batch_profile_read_kind", C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp]),
     ("gb_measure_issue_rates", C.c_int, [_dp, _dp]),
     ("gb_measure_grid_barrier", C.c_int, [C.c_int, C.c_int, C.c_int, _dp]),
+    ("gb_check_division", C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]),
     ("gb_check_conversions", C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
 ]
 

@@ -341,11 +341,13 @@ class GangServer:
                  keep_fields: bool = False, clock: Callable[[], float] = time.perf_counter,
                  sleep: Callable[[float], None] = time.sleep, precision=_L.PRB_FP64, smoother=_L.SMOOTHER_ZEBRA,
                  group_by: str = "kind", factory: Optional[Callable[[Request], object]] = None,
-                 gang_factory: Optional[Callable[[str], object]] = None, solve_spread: int = 1):
+                 gang_factory: Optional[Callable[[str], object]] = None, solve_spread: int = 8):
         """group_by: "kind" (one gang per kind, batched across grid sizes:
         every member steps at the pace of the largest) or "shape" (one gang
         per kind and grid; the gangs run side by side on their own streams).
-        solve_spread: CTAs per velocity solve of the layer gangs (1 or 8).
+        solve_spread: CTAs per velocity solve of the layer gangs (8, a cluster:
+        a gang step waits for its slowest member's solve, which a cluster
+        shortens; or 1).
         factory / gang_factory: stand-ins for the device instance and gang
         (the host logic's tests)."""
         assert group_by in ("kind", "shape")

@@ -774,6 +774,13 @@ int gb_measure_issue_rates(double *fp64_fma_per_s, double *fp32_fma_per_s);
  * cannot all be resident.  No counterpart in the reference (a latency probe
  * of this library's own barrier). */
 int gb_measure_grid_barrier(int blocks, int threads, int nbarriers, double *us_per_barrier);
+/* Compares the line solvers' division by a stored reciprocal (a product and
+ * two fused multiply-adds that round to the IEEE quotient) with the hardware
+ * FP64 division on n_random seeded operand pairs over the normal range
+ * (random significands, near-exact quotients, small integers, signed zero
+ * dividends); *mismatches gets the count of differing bit patterns.  No
+ * counterpart in the reference (a check of this library's arithmetic). */
+int gb_check_division(long long n_random, unsigned long long seed, long long *mismatches);
 /* Compares the batched solver's integer-pipe float <-> double conversions
  * with the hardware conversions on the current device: every float bit
  * pattern through float -> double, and n_random seeded double bit patterns

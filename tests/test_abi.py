@@ -108,3 +108,11 @@ def test_barrier_probe_checks_arguments_before_touching_the_device(gblib):
     assert gblib.gb_measure_grid_barrier(8, 100, 10, C.byref(t)) == lib.GB_ERR_INVALID
     assert gblib.gb_measure_grid_barrier(8, 256, 0, C.byref(t)) == lib.GB_ERR_INVALID
     assert t.value == -1.0
+
+
+def test_division_check_rejects_bad_arguments_without_a_device(gblib):
+    import ctypes as C
+    from codesthesis_dir_gb300 import lib
+    bad = C.c_longlong(-1)
+    assert gblib.gb_check_division(0, 1, C.byref(bad)) == lib.GB_ERR_INVALID
+    assert bad.value == -1
