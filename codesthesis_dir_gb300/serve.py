@@ -80,12 +80,15 @@ def annulus_re(Ta: float) -> float:
 
 def default_dt(req: Request) -> float:
     """Time step of a request: the 129 x 65 layer's 1e-5 scaled diffusively
-    with the grid and reduced for strong convection; for the annulus also
-    for slow rotation, whose buoyancy coupling scales with Ra/Re (a rule
-    checked stable on the sweep's grids at the corners of its Ra and Ta
-    ranges)."""
+    with the grid and reduced for strong convection; for the layer also by
+    1/sqrt(Pr) above Pr 1 (without it five Pr-7 layers of the 512-request
+    sweep on the 65 x 33 grid, Ra 2.5e6-3e7, stopped at the sweep limit
+    after 287-418 steps, on the device and in the oracle alike, and finish
+    with it); for the annulus also for slow rotation, whose buoyancy
+    coupling scales with Ra/Re (a rule checked stable on the sweep's grids at
+    the corners of its Ra and Ta ranges)."""
     if req.kind == LAYER:
-        return 1e-5 * (64.0 / req.nz) ** 2 * min(1.0, math.sqrt(1e5 / req.Ra))
+        return 1e-5 * (64.0 / req.nz) ** 2 * min(1.0, math.sqrt(1e5 / req.Ra)) * min(1.0, 1.0 / math.sqrt(req.Pr))
     n = max(req.nx, req.nz)
     return 1e-5 * (64.0 / n) ** 2 * min(1.0, math.sqrt(1e5 / req.Ra)) * min(1.0, annulus_re(req.Ta) / 50.0)
 
