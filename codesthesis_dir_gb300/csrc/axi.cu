@@ -940,55 +940,71 @@ __device__ __forceinline__ void k_axi_mg_solve_mixed_body(const AxiDev &d, int b
 __global__ void __maxnreg__(128) k_axi_mg_solve_mixed(AxiDev d) { k_axi_mg_solve_mixed_body(d, blockIdx.x); }
 
 // FP32 copies of rval and the factors (pivots as reciprocals).
+// FP32 copies of the factors (pivots as reciprocals): block l - 1 converts
+// level l, its threads the level's lines (thread 0 also the r-line table).
 __global__ void k_axi_factors32(AxiDev d)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int i = 0; i <= d.lev[1].n1; ++i) d.rval32[i] = (float)d.rval[i];
-    for (int l = 1; l <= d.nlev; ++l) {
-        const AxiLevel &L = d.lev[l];
-        auto conv = [](const double *f, float *g, int n) {
-            for (int j = 0; j < n; ++j) {
-                g[j] = (float)f[j];
-                g[n + j] = (float)(1.0 / f[n + j]);
-                g[2 * n + j] = (float)f[2 * n + j];
-            }
-        };
-        if (L.n1 - 1 >= 1) conv(L.fac_r, L.fac_r32, L.n1 - 1);
-        if (L.n2 - 1 >= 1)
-            for (int i = 1; i <= L.n1 - 1; ++i)
-                conv(L.fac_z + (size_t)(i - 1) * tdma_fac_len(L.n2 - 1), L.fac_z32 + (size_t)(i - 1) * 3 * (L.n2 - 1),
-                     L.n2 - 1);
-    }
+    const int l = 1 + blockIdx.x;
+    if (l == 1)
+        for (int i = threadIdx.x; i <= d.lev[1].n1; i += blockDim.x) d.rval32[i] = (float)d.rval[i];
+    const AxiLevel &L = d.lev[l];
+    auto conv = [](const double *f, float *g, int n) {
+        for (int j = 0; j < n; ++j) {
+            g[j] = (float)f[j];
+            g[n + j] = (float)(1.0 / f[n + j]);
+            g[2 * n + j] = (float)f[2 * n + j];
+        }
+    };
+    if (threadIdx.x == 0 && L.n1 - 1 >= 1) conv(L.fac_r, L.fac_r32, L.n1 - 1);
+    if (L.n2 - 1 >= 1)
+        for (int i = 1 + threadIdx.x; i <= L.n1 - 1; i += blockDim.x)
+            conv(L.fac_z + (size_t)(i - 1) * tdma_fac_len(L.n2 - 1), L.fac_z32 + (size_t)(i - 1) * 3 * (L.n2 - 1),
+                 L.n2 - 1);
 }
 
-// rval and the factored line matrices of every level (one thread): the
-// coefficients relax forms for each line (rotann2.f:698-721).
+__global__ void k_axi_rval(AxiDev d)
+{
+    for (int i = threadIdx.x; i <= d.lev[1].n1; i += blockDim.x) d.rval[i] = (double)i * d.lev[1].hr + d.r0;
+}
+
+// The factored line matrices of every level, with the coefficients relax
+// forms for each line (rotann2.f:698-721): block l - 1 takes level l; its
+// thread 0 the r-line matrix (work: three arrays per level), every thread
+// the z-line matrices of its rows, whose coefficients are constant along the
+// line (the tdma factorization with scalar a, b, c, the same operations).
 __global__ void k_axi_factors(AxiDev d, double *work)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int i = 0; i <= d.lev[1].n1; ++i) d.rval[i] = (double)i * d.lev[1].hr + d.r0;
-    for (int l = 1; l <= d.nlev; ++l) {
-        const AxiLevel &L = d.lev[l];
-        const int n1 = L.n1, n2 = L.n2;
-        const double hhr = L.hhr, hhz = L.hhz, hr = L.hr;
-        const int nmax = (n1 > n2 ? n1 : n2) + 2;
-        double *a = work, *b = a + nmax, *c = b + nmax;
+    const int l = 1 + blockIdx.x;
+    const AxiLevel &L = d.lev[l];
+    const int n1 = L.n1, n2 = L.n2;
+    const double hhr = L.hhr, hhz = L.hhz, hr = L.hr;
+    const int nmax = (d.lev[1].n1 > d.lev[1].n2 ? d.lev[1].n1 : d.lev[1].n2) + 2;
+    if (threadIdx.x == 0 && n1 - 1 >= 1) {
+        double *a = work + (size_t)blockIdx.x * 3 * nmax, *b = a + nmax, *c = b + nmax;
         for (int i = 1; i <= n1 - 1; ++i) {
             const double rv = d.rval[i * L.lf];
             a[i - 1] = 1.0 / hhr - 0.5 / hr / rv;
             c[i - 1] = 1.0 / hhr + 0.5 / hr / rv;
             b[i - 1] = -2.0 / hhr - 2.0 / hhz - 1.0 / (rv * rv);
         }
-        if (n1 - 1 >= 1) factor_tdma(a, b, c, n1 - 1, L.fac_r);
-        for (int i = 1; i <= n1 - 1; ++i) {
-            const double rv = d.rval[i * L.lf];
-            for (int j = 1; j <= n2 - 1; ++j) {
-                a[j - 1] = 1.0 / hhz;
-                c[j - 1] = 1.0 / hhz;
-                b[j - 1] = -2.0 / hhr - 2.0 / hhz - 1.0 / (rv * rv);
-            }
-            if (n2 - 1 >= 1) factor_tdma(a, b, c, n2 - 1, L.fac_z + (size_t)(i - 1) * tdma_fac_len(n2 - 1));
+        factor_tdma(a, b, c, n1 - 1, L.fac_r);
+    }
+    const int n = n2 - 1;
+    if (n < 1) return;
+    for (int i = 1 + threadIdx.x; i <= n1 - 1; i += blockDim.x) {
+        const double rv = d.rval[i * L.lf];
+        const double av = 1.0 / hhz, cv = 1.0 / hhz;
+        const double bv = -2.0 / hhr - 2.0 / hhz - 1.0 / (rv * rv);
+        double *fac = L.fac_z + (size_t)(i - 1) * tdma_fac_len(n);
+        double *fact = fac, *bp = fac + n, *cc = fac + 2 * n, *ibp = fac + 3 * n;
+        bp[0] = bv;
+        fact[0] = 0.0;
+        for (int j = 0; j < n; ++j) cc[j] = cv;
+        for (int j = 1; j < n; ++j) {
+            fact[j] = av / bp[j - 1];
+            bp[j] = bv - fact[j] * cv;
         }
+        for (int j = 0; j < n; ++j) ibp[j] = 1.0 / bp[j];
     }
 }
 
@@ -1147,7 +1163,7 @@ static int axi_create(const gb_axi_params *p, double dr, double dz, gb_axi **out
         const size_t lv = 2 * (n1 + 1) * (n2 + 1) + 4 * n1 + n1 * 4 * (n2 + 1);
         need += lv + (lv + 1) / 2 + 4;   // FP64 slots, then their FP32 copies
     }
-    const size_t work = 3 * (size_t)((nr > nz ? nr : nz) + 2);
+    const size_t work = 3 * (size_t)((nr > nz ? nr : nz) + 2) * (size_t)nlev;   // r-line coefficients, per level
     e = cudaMalloc(&h->pool, sizeof(double) * (need + work));
     if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: multigrid pool"); return GB_ERR_ALLOC; }
     cudaMemset(h->pool, 0, sizeof(double) * (need + work));
@@ -1198,13 +1214,14 @@ static int axi_create(const gb_axi_params *p, double dr, double dz, gb_axi **out
     d.abort = (int *)(sm + 128);
     d.status = (int *)(sm + 192);
     d.step_index = (int *)(sm + 256);
-    k_axi_factors<<<1, 1>>>(d, wk);
-    k_axi_factors32<<<1, 1>>>(d);
+    k_axi_rval<<<1, 256>>>(d);
+    k_axi_factors<<<d.nlev, 128>>>(d, wk);
+    k_axi_factors32<<<d.nlev, 128>>>(d);
     e = cudaFuncSetAttribute(k_axi_mg_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, AX32_SMEM_BYTES);
     if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create: stream"); return GB_ERR_CUDA; }
-    e = cudaDeviceSynchronize();
+    e = cudaStreamSynchronize(0);   // the creation's kernels and copies, not other instances' streams
     if (e != cudaSuccess) { gb_set_error("gb_axi_create: %s", cudaGetErrorString(e)); gb_axi_destroy(h); return GB_ERR_CUDA; }
     *out = h;
     return GB_OK;
@@ -1273,7 +1290,7 @@ extern "C" int gb_axi_create_stretched(const gb_axi_params *p, const gb_axi_grid
     d.status = (int *)(sm + 192);
     d.step_index = (int *)(sm + 256);
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) { gb_axi_destroy(h); gb_set_error("gb_axi_create_stretched: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
     if (nlev_out) *nlev_out = g->nlev;
     *out = h;

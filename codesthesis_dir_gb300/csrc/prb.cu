@@ -821,7 +821,7 @@ int gb_prb_create_ex(const gb_prb_params *p, double dr, double dp, gb_prb **out,
     if (st != GB_OK) { gb_prb_destroy(h); return st; }
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { gb_prb_destroy(h); gb_set_error("gb_prb_create: stream"); return GB_ERR_CUDA; }
-    e = cudaDeviceSynchronize();
+    e = cudaStreamSynchronize(0);   // the creation's kernels and copies, not other instances' streams
     if (e != cudaSuccess) { gb_set_error("gb_prb_create: %s", cudaGetErrorString(e)); gb_prb_destroy(h); return GB_ERR_CUDA; }
     *out = h;
     return GB_OK;
