@@ -954,7 +954,7 @@ def main():
     pms, pl, pb = C.c_double(), C.c_longlong(), C.c_double()
     L.gb_batch_profile_read(prof._h, C.byref(pms), C.byref(pl), C.byref(pb), 0)
     kinds = {}
-    for kname, kid in (("down_finest", 1), ("up_finest", 2), ("outer", 4)):
+    for kname, kid in (("down_finest", 1), ("up_finest", 2), ("outer", 4), ("outer_first", 7)):
         kms, kl, kb = C.c_double(), C.c_longlong(), C.c_double()
         L.gb_batch_profile_read_kind(prof._h, kid, C.byref(kms), C.byref(kl), C.byref(kb))
         if kl.value:
@@ -967,9 +967,11 @@ def main():
     L.gb_measure_issue_rates(C.byref(r64), C.byref(r32))
     outer_pass = None
     if "outer" in kinds:
-        # per interior point, FP64 defect correction: 3 adds and 2 fused
-        # multiply-adds for the residual, 1 fused multiply-add for the norm;
-        # 16 B read (psi, f), 4 B written (the FP32 right-hand side)
+        # per interior point of an outer pass after a solve's first, FP64
+        # defect correction: 3 adds and 2 fused multiply-adds for the
+        # residual, 1 fused multiply-add for the norm; 16 B read (psi, f),
+        # 4 B written (the FP32 right-hand side).  The first pass of each
+        # solve (f read alone) is profiled apart as "outer_first".
         k = kinds["outer"]
         pts_per_launch = k["alg_bytes_per_launch"] / 20.0
         f64ops = 3 + 2 + 1 if prec_head == lib.BATCH_MIXED_F64OUTER else 1
@@ -977,6 +979,7 @@ def main():
                           "CM_F64" if prec_head == lib.BATCH_MIXED_F64OUTER else "CM_PAIR",
                           "FP64 residual and norm, FP32 copy" if prec_head == lib.BATCH_MIXED_F64OUTER
                           else "float-pair residual, FP64 norm, FP32 copy"),
+                      "points_per_launch": pts_per_launch,
                       "points_per_s": pts_per_launch / (k["avg_ms"] / 1e3), "avg_launch_ms": k["avg_ms"],
                       "fp64_instr_per_point": f64ops,
                       "fp64_pipe_frac": f64ops * pts_per_launch / (k["avg_ms"] / 1e3) / r64.value,

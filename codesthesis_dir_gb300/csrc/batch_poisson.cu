@@ -905,6 +905,9 @@ __device__ void op_finalize(const BatchDev &B, int p, int first)
 // ---------------------------------------------------------------------------
 enum OpKind { OP_SMOOTH = 0, OP_SMOOTH_R = 1, OP_PROLONG = 2, OP_LOCAL = 3, OP_OUTER = 4, OP_FINALIZE = 5,
               OP_COPYBACK = 6 };
+// profile slot of the first outer pass of a solve (reads f alone, no residual
+// arithmetic), kept apart from the later passes filed under OP_OUTER
+constexpr int OP_PROFILE_OUTER_FIRST = 7;
 
 struct Op {
     int kind, l, nu, zero, src, dst, corr;
@@ -1830,9 +1833,10 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
         case OP_OUTER: bytes = (first_outer ? 12.0 : 20.0) * pts_all; break;   // the first reads f alone
         default: break;
         }
-        b->kind_ms[k] += ms;
-        b->kind_bytes[k] += bytes;
-        b->kind_launches[k] += 1;
+        const int slot = first_outer ? OP_PROFILE_OUTER_FIRST : k;   // first passes apart
+        b->kind_ms[slot] += ms;
+        b->kind_bytes[slot] += bytes;
+        b->kind_launches[slot] += 1;
         if (k == OP_SMOOTH_R) {
             b->prof_ms += ms;
             b->prof_launches += 1;

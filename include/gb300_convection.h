@@ -754,12 +754,14 @@ int gb_batch_profile(gb_batch *b, int enable);
  * profile counters. */
 int gb_batch_profile_read(gb_batch *b, double *ms, long long *launches, double *alg_bytes, int reset);
 /* The same per operation kind (graph mode): 0 smoothing, 1 smoothing +
- * residual + restriction, 2 prolongation + smoothing, 4 outer pass;
- * finest level only, except the outer pass. */
-#define GB_BATCH_OP_SMOOTH   0
-#define GB_BATCH_OP_DOWN     1
-#define GB_BATCH_OP_UP       2
-#define GB_BATCH_OP_OUTER    4
+ * residual + restriction, 2 prolongation + smoothing, 4 outer passes after
+ * a solve's first, 7 the first outer pass of each solve (it reads f alone);
+ * finest level only, except the outer passes. */
+#define GB_BATCH_OP_SMOOTH      0
+#define GB_BATCH_OP_DOWN        1
+#define GB_BATCH_OP_UP          2
+#define GB_BATCH_OP_OUTER       4
+#define GB_BATCH_OP_OUTER_FIRST 7
 int gb_batch_profile_read_kind(gb_batch *b, int kind, double *ms, long long *launches, double *alg_bytes);
 
 /* ------------------------------------------------------ device probes */
