@@ -295,10 +295,10 @@ def prb_latency_model(cfg, precision, warmup=20, reps=5):
     each routine timed with CUDA events on the instance's stream.  The step
     graph runs the v and u solves side by side, so its critical path is the
     transport routines plus the longer solve; what the graph step takes
-    beyond that is launch and dependency latency between its nodes.  For
-    the FP64 path the solves are timed again from the same right-hand sides
-    on a cluster of 8 CTAs per equation instead of one CTA (both
-    precisions), and the two results compared bit for bit."""
+    beyond that is launch and dependency latency between its nodes.  The
+    solves are timed again from the same right-hand sides on a cluster of 8
+    CTAs per equation instead of one CTA, and the two results compared bit
+    for bit."""
     import torch
     from codesthesis_dir_gb300 import lib
     g = prb_instance(cfg, 1) if precision == 0 else _prb_mixed_instance(cfg, 1)
@@ -310,6 +310,7 @@ def prb_latency_model(cfg, precision, warmup=20, reps=5):
     tot = {n: 0.0 for n in names}
     sweeps = {"poisson2": 0, "poisson3": 0}
     one = {"poisson2": 0.0, "poisson3": 0.0}
+    each = {"poisson2": [], "poisson3": []}
     same = True
 
     def timed(fn):
@@ -320,28 +321,39 @@ def prb_latency_model(cfg, precision, warmup=20, reps=5):
         e1.synchronize()
         return e0.elapsed_time(e1), r
 
-    for _ in range(reps):
-        for n in names[:5]:
-            tot[n] += timed(getattr(g, n))[0]
-        snap = {n: g.get(n) for n in ("vel", "velp", "uel", "uelp")}
-        for n in ("poisson2", "poisson3"):
-            ms, sw = timed(getattr(g, n))
-            tot[n] += ms
-            sweeps[n] += sw
-        res = {n: g.get(n) for n in ("vel", "uel")}
-        for n, a in snap.items():
-            g.set(n, a)
-        g.set_solve_spread(8)
-        for n in ("poisson2", "poisson3"):
-            one[n] += timed(getattr(g, n))[0]
-        g.set_solve_spread(1)
-        same = same and all(np.array_equal(res[n], g.get(n)) for n in res)
-        tot["update"] += timed(g.update)[0]
+    # each routine's events bracket its host call too (the solves read their
+    # sweep counts back): a garbage collection inside that call would be
+    # counted as routine time, so the collector waits until the loop ends
+    import gc
+    gc.collect()
+    gc.disable()
+    try:
+        for _ in range(reps):
+            for n in names[:5]:
+                tot[n] += timed(getattr(g, n))[0]
+            snap = {n: g.get(n) for n in ("vel", "velp", "uel", "uelp")}
+            for n in ("poisson2", "poisson3"):
+                ms, sw = timed(getattr(g, n))
+                tot[n] += ms
+                each[n].append(ms)
+                sweeps[n] += sw
+            res = {n: g.get(n) for n in ("vel", "uel")}
+            for n, a in snap.items():
+                g.set(n, a)
+            g.set_solve_spread(8)
+            for n in ("poisson2", "poisson3"):
+                one[n] += timed(getattr(g, n))[0]
+            g.set_solve_spread(1)
+            same = same and all(np.array_equal(res[n], g.get(n)) for n in res)
+            tot["update"] += timed(g.update)[0]
+    finally:
+        gc.enable()
     g.close()
     ms = {n: tot[n] / reps for n in names}
     transport = sum(ms[n] for n in names if not n.startswith("poisson"))
     out = {"routine_ms": ms, "transport_ms": transport,
            "solve_ms": {"v": ms["poisson2"], "u": ms["poisson3"]},
+           "solve_ms_each_step": {"v": each["poisson2"], "u": each["poisson3"]},
            "sweeps_per_solve": {"v": sweeps["poisson2"] / reps, "u": sweeps["poisson3"] / reps},
            "us_per_sweep": {"v": 1e3 * ms["poisson2"] / max(sweeps["poisson2"] / reps, 1),
                             "u": 1e3 * ms["poisson3"] / max(sweeps["poisson3"] / reps, 1)},

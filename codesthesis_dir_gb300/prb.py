@@ -127,8 +127,9 @@ class PRB:
         return self._poisson(3)
 
     def set_solve_spread(self, ctas):
-        """CTAs sharing one FP64 two-colour solve: 8 (a cluster, the
-        default) or 1.  Both give the same bits."""
+        """CTAs sharing one two-colour solve (FP64 or mixed): 1 (the
+        default, one CTA per equation) or 8 (a cluster).  Both give the same
+        bits."""
         _L.check(_L.load().gb_prb_set_solve_spread(self._h, ctas), "set_solve_spread")
 
     def update(self):
