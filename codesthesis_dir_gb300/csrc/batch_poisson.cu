@@ -1137,6 +1137,7 @@ struct gb_batch {
     double kind_ms[8] = {0}, kind_bytes[8] = {0};
     long long kind_launches[8] = {0};
     int *h_active = nullptr;            // page-locked: the active flags after a profiled iteration
+    std::vector<int> prof_prev;         // the flags before it: the problems its outer pass covered
 };
 
 static int levels_of(int n, int *nl)
@@ -1807,12 +1808,14 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
 {
     if (!b->profile || b->ev_used == 0) return;
     cudaStreamSynchronize(s);   // a no-op after the iteration's own synchronisation
-    double pts_tile = 0.0, pts_all = 0.0;
+    // the outer pass runs before the iteration's convergence test and covers
+    // the problems active when the iteration began; the cycles after the
+    // test cover those still active when it ends
+    double pts_tile = 0.0, pts_outer = 0.0;
     for (int p = 0; p < b->nprob; ++p) {
-        if (!b->h_active[p]) continue;
         const double pts = (double)(b->n[p] - 2) * (double)(b->n[p] - 2);
-        pts_all += pts;
-        if (b->dloc[p] > 0) pts_tile += pts;
+        if (b->prof_prev[p]) pts_outer += pts;
+        if (b->h_active[p] && b->dloc[p] > 0) pts_tile += pts;
     }
     const double esz = b->precision == GB_BATCH_FP64 ? 8.0 : 4.0;
     const bool mixed = inner32(b);
@@ -1831,7 +1834,7 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
         case OP_SMOOTH_R: bytes = (3.0 * pre + 3.0 + 1.25) * esz * pts_tile; break;
         case OP_PROLONG: bytes = ((2.25 + 3.0 * post) * esz + (mixed ? 16.0 : 0.0)) * pts_tile; break;
         case OP_SMOOTH: bytes = 3.0 * esz * pts_tile; break;
-        case OP_OUTER: bytes = (first_outer ? 12.0 : 20.0) * pts_all; break;   // the first reads f alone
+        case OP_OUTER: bytes = (first_outer ? 12.0 : 20.0) * pts_outer; break;   // the first reads f alone
         default: break;
         }
         const int slot = first_outer ? OP_PROFILE_OUTER_FIRST : k;   // first passes apart
@@ -1844,6 +1847,7 @@ static void batch_profile_collect(gb_batch *b, cudaStream_t s)
             b->prof_bytes += bytes;
         }
     }
+    b->prof_prev.assign(b->h_active, b->h_active + b->nprob);
 }
 
 extern "C" int gb_batch_profile(gb_batch *b, int enable)
@@ -1919,6 +1923,7 @@ static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStre
 static int solve_graph(gb_batch *b, cudaStream_t s)
 {
     b->ev_used = 0;
+    b->prof_prev.assign(b->nprob, 1);   // every problem starts active
     enqueue_iteration(b, b->ops0, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     batch_profile_collect(b, s);
