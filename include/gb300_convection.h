@@ -619,9 +619,9 @@ int gb_pdma_batch(const double *a, const double *b, const double *c, const doubl
  * Limit: 5*n*nlines <= GB_PDMA_NOALLOC_MAX_DOUBLES (4 MiB of scratch that
  * every GPU loading the library holds until exit); larger requests return
  * GB_ERR_INVALID without launching.  The first call on each device looks up
- * the scratch array's device address (make that first call before any
- * stream capture); the address is kept for the life of the process, so a
- * cudaDeviceReset after that first call is not supported.  Each call waits
+ * the scratch array's device address; the address is kept for the life of
+ * the process, so a cudaDeviceReset after that first call is not
+ * supported.  Each call waits
  * for its stream before it returns (its status covers the kernel), so the
  * calls of one host thread never overlap one another; all calls share the
  * scratch, so calls from different host threads that overlap on the GPU
