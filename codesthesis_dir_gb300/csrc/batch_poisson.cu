@@ -1137,6 +1137,7 @@ struct gb_batch {
     double kind_ms[8] = {0}, kind_bytes[8] = {0};
     long long kind_launches[8] = {0};
     int *h_active = nullptr;            // page-locked: the active flags after a profiled iteration
+    int nsm = 0;                        // the device's SMs (grid-stride element-wise launches)
     std::vector<int> prof_prev;         // the flags before it: the problems its outer pass covered
 };
 
@@ -1638,6 +1639,7 @@ static int batch_create(int nprob, const int *n, int precision, int nu1, int nu2
     BTRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (precision == GB_BATCH_FP64) BTRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persistent<double>, TILE_THREADS, b->psmem));
     else BTRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persistent<float>, TILE_THREADS, b->psmem));
+    b->nsm = nsm;
     b->pgrid = nsm * per;
     if (!coop) b->pgrid = 0;
     // room for the operation lists of any inner count (set_inner_cycles)
@@ -1899,7 +1901,7 @@ static int batch_bind_io(gb_batch *b, const double *d_f, double *d_psi, cudaStre
         pp[p] = d_psi + b->off0[p];
     }
     if (mixed && b->total > 0) {
-        k_split_pairs<<<152 * 8, 256, 0, s>>>(d_f, b->d_fpairs, b->total);
+        k_split_pairs<<<b->nsm * 8, 256, 0, s>>>(d_f, b->d_fpairs, b->total);
         GB_CUDA_TRY(cudaGetLastError());
     }
     GB_CUDA_TRY(cudaMemcpyAsync(b->d_f_tab, pf.data(), sizeof(void *) * b->nprob, cudaMemcpyHostToDevice, s));
@@ -2041,7 +2043,7 @@ extern "C" int gb_batch_solve_device(gb_batch *b, const double *d_f, double *d_p
     if (st != GB_OK) return st;
     if (b->precision == GB_BATCH_MIXED && b->total > 0) {
         // the mixed solve held psi as float pairs in place: back to FP64
-        k_join_pairs<<<152 * 8, 256, 0, s>>>(d_psi, b->total);
+        k_join_pairs<<<b->nsm * 8, 256, 0, s>>>(d_psi, b->total);
         GB_CUDA_TRY(cudaGetLastError());
     }
     std::vector<int> fl(b->nprob);
@@ -2225,12 +2227,15 @@ extern "C" int gb_check_conversions(long long n_random, unsigned long long seed,
         gb_set_error("gb_check_conversions: invalid arguments");
         return GB_ERR_INVALID;
     }
+    int dev = 0, sms = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     unsigned long long *d = nullptr;
     GB_CUDA_TRY(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
     cudaError_t e = cudaMemset(d, 0, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) {
-        k_cvt_check_f2d<<<152 * 8, 256>>>(d);
-        if (n_random > 0) k_cvt_check_d2f<<<152 * 8, 256>>>((unsigned long long)n_random, seed, d + 1);
+        k_cvt_check_f2d<<<sms * 8, 256>>>(d);
+        if (n_random > 0) k_cvt_check_d2f<<<sms * 8, 256>>>((unsigned long long)n_random, seed, d + 1);
         e = cudaGetLastError();
     }
     unsigned long long h[2] = {0, 0};

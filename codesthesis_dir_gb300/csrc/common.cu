@@ -210,11 +210,14 @@ extern "C" int gb_check_division(long long n_random, unsigned long long seed, lo
         gb_set_error("gb_check_division: invalid argument");
         return GB_ERR_INVALID;
     }
+    int dev = 0, sms = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     unsigned long long *d = nullptr;
     GB_CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long)));
     cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) {
-        k_check_division<<<152 * 8, 256>>>((unsigned long long)n_random, seed, d);
+        k_check_division<<<sms * 8, 256>>>((unsigned long long)n_random, seed, d);
         e = cudaGetLastError();
     }
     unsigned long long h = 0;
