@@ -8,12 +8,12 @@ coefficient file comes from.
 * ``spacing_tanh``: wall clustering by a tanh map, h_i = L (x_i - x_{i-1}),
   x_i = (1 + tanh(s (2i/n - 1)) / tanh(s)) / 2, stretch factor s (the 257^2
   annulus workload uses s = 1.5; grid.f itself has only the GEF grid);
-* ``levels``: grid.f:859-915 -- coarse spacings are sums of fine pairs,
+* ``levels``: grid.f:859-924 -- coarse spacings are sums of fine pairs,
   positions their running sums, at most 6 levels;
-* ``fdif``: grid.f:917-1114 -- weights of the points of a stencil for the
+* ``fdif``: grid.f:926-1115 -- weights of the points of a stencil for the
   derivatives 0..nx-1, by Gaussian elimination (partial pivoting) of the
   Taylor matrix, in the reference's operation order;
-* ``coefficients``: grid.f:160-231 -- per level, first-derivative weights on
+* ``coefficients``: grid.f:178-243 -- per level, first-derivative weights on
   (i-1, i, i+1) and second-derivative weights on (i-1..i+2) for i <= n/2 and
   on (i-2..i+1) above, in r and in z.
 
@@ -120,7 +120,7 @@ def levels(hr1, hz1, r0, zmin=0.0, maxlev=0):
 
 
 def _gausse(a, b, n):
-    """grid.f:1034-1114: a[i][j] is row i, column j; b[i] the n+2
+    """grid.f:1034-1115: a[i][j] is row i, column j; b[i] the n+2
     right-hand sides of row i.  Returns x[i][k] (unknown i, right-hand side k)."""
     for k in range(n - 1):
         kpvt = k
@@ -154,7 +154,7 @@ def _gausse(a, b, n):
 
 
 def fdif(nx, nref, k, pos):
-    """grid.f:917-1032 (nans = 0): w[d][p] = weight of point pos[k-nref+1+p]
+    """grid.f:926-1032 (nans = 0): w[d][p] = weight of point pos[k-nref+1+p]
     for the d-th derivative.  nref is 1-based, as in the reference."""
     x = [float(pos[k - nref + i]) for i in range(1, nx + 1)]
     # equation (row) i: the Taylor expansion about point nref at point i

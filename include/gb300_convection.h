@@ -499,9 +499,9 @@ int gb_r3d_heat(gb_r3d *h, double *trans1);   /* rot3dmg.f:882-909 */
 /* heat(trans1, trans2) of rot3dmghor.f:913-945 (GB_R3D_HORIZONTAL; the
  * vertical annulus gives trans2 = 0). */
 int gb_r3d_heat2(gb_r3d *h, double *trans1, double *trans2);
-int gb_r3d_rhsw(gb_r3d *h);           /* rot3dmg.f:1026-1060 */
-int gb_r3d_rhsv(gb_r3d *h);           /* rot3dmg.f:1063-1104 */
-int gb_r3d_rhsu(gb_r3d *h);           /* rot3dmg.f:1107-1150 */
+int gb_r3d_rhsw(gb_r3d *h);           /* rot3dmg.f:1026-1063 */
+int gb_r3d_rhsv(gb_r3d *h);           /* rot3dmg.f:1066-1108 */
+int gb_r3d_rhsu(gb_r3d *h);           /* rot3dmg.f:1111-1150 */
 /* poisson1 (which = 1: wel, welp, wrh), poisson2 (2: vel), poisson3 (3: uel),
  * rot3dmg.f:1216-1540: GB_OK, GB_MAXSWEEPS (the reference STOPs), GB_NAN or
  * GB_TIMEOUT; *sweeps (may be NULL) receives the sweep count. */

@@ -46,9 +46,9 @@ void temperature_(void);              /* rot3dmg.f:736-873 */
  * rot3dmghor.f:913-945 heat(trans1, trans2) (only then is trans2 read). */
 void heat_(double *trans1, double *trans2);
 void update_(void);                   /* rot3dmg.f:964-1023 */
-void rhsw_(double *wrh);              /* rot3dmg.f:1026-1060 */
-void rhsv_(double *vrh);              /* rot3dmg.f:1063-1104 */
-void rhsu_(double *urh);              /* rot3dmg.f:1107-1150 */
+void rhsw_(double *wrh);              /* rot3dmg.f:1026-1063 */
+void rhsv_(double *vrh);              /* rot3dmg.f:1066-1108 */
+void rhsu_(double *urh);              /* rot3dmg.f:1111-1150 */
 
 /* Configuration, callable from C before poissoninit_. */
 void gb_r3d_bind_bounds(int kr, int kz, int kp);

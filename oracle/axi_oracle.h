@@ -74,7 +74,7 @@ typedef struct {
  *   d2/dz2 x = 2 (x(i, 1) - x(i, 0)) / h^2 with h the wall spacing;
  *   Thom wall vorticity 2 psi(next) / h^2 with the wall spacing (rcsc.f
  *   update, :706-751); the heat flux with the five-point one-sided d/dr
- *   weights at the inner wall on r(0..4) (grid.f's fdif, grid.f:917-1032,
+ *   weights at the inner wall on r(0..4) (grid.f's fdif, grid.f:926-1032,
  *   fourth order as rotann2.f's heat stencil) and the trapezoid rule in z. */
 int  orc_axi_set_stretched(orc_axi_t *s, const orc_str_grid_t *g, orc_str_mg_t *m);
 

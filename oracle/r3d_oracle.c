@@ -627,7 +627,7 @@ void orc_r3d_update(orc_r3d_t *s)
     memcpy(s->th, s->thn, n);
 }
 
-/* rhsw, rot3dmg.f:1026-1060 */
+/* rhsw, rot3dmg.f:1026-1063 */
 void orc_r3d_rhsw(orc_r3d_t *s)
 {
     const int nr = s->nr, nz = s->nz, np = s->np;
@@ -650,7 +650,7 @@ void orc_r3d_rhsw(orc_r3d_t *s)
             }
 }
 
-/* rhsv, rot3dmg.f:1063-1104 */
+/* rhsv, rot3dmg.f:1066-1108 */
 void orc_r3d_rhsv(orc_r3d_t *s)
 {
     const int nr = s->nr, nz = s->nz, np = s->np;
@@ -677,7 +677,7 @@ void orc_r3d_rhsv(orc_r3d_t *s)
             }
 }
 
-/* rhsu, rot3dmg.f:1107-1150 */
+/* rhsu, rot3dmg.f:1111-1150 */
 void orc_r3d_rhsu(orc_r3d_t *s)
 {
     const int nr = s->nr, nz = s->nz, np = s->np;

@@ -47,7 +47,7 @@ int orc_str_spacing_gef(int n, double lo, double hi, double dist, double gef, do
     return 0;
 }
 
-/* level, grid.f:859-915 (without the interactive change of nlev). */
+/* level, grid.f:859-924 (without the interactive change of nlev). */
 int orc_str_levels(orc_str_grid_t *g, int n1, int n2, const double *hr1, const double *hz1, double r0,
                    double zmin, int maxlev)
 {
@@ -109,7 +109,7 @@ void orc_str_grid_free(orc_str_grid_t *g)
     memset(g, 0, sizeof(*g));
 }
 
-/* gausse, grid.f:1034-1114.  a(j,i) is row i, column j of the system;
+/* gausse, grid.f:1034-1115.  a(j,i) is row i, column j of the system;
  * b(k,i) is right-hand side k of row i (n+2 of them); x(k,i) the solution. */
 #define GA(j, i) a[(size_t)((j) - 1) + (size_t)n * (size_t)((i) - 1)]
 #define GB(k, i) b[(size_t)((k) - 1) + (size_t)(n + 2) * (size_t)((i) - 1)]
@@ -160,7 +160,7 @@ static int gausse(double *a, double *b, double *x, int n)
 #undef GB
 #undef GX
 
-/* fdif, grid.f:917-1032 (nans = 0). */
+/* fdif, grid.f:926-1032 (nans = 0). */
 int orc_str_fdif(int nx, int nref, int k, const double *xr, double *w)
 {
     const int n = nx;
@@ -198,7 +198,7 @@ int orc_str_fdif(int nx, int nref, int k, const double *xr, double *w)
     return 0;
 }
 
-/* grid.f:160-231 */
+/* grid.f:178-243 */
 int orc_str_coefficients(orc_str_grid_t *g)
 {
     double w[16];

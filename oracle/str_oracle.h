@@ -4,12 +4,12 @@
  *
  *   grid.f:723-857  wall-clustered spacings (geometric expansion factor
  *                   near both walls, uniform core), or uniform spacings;
- *   grid.f:859-915  levels: coarse spacings are sums of fine pairs,
+ *   grid.f:859-924  levels: coarse spacings are sums of fine pairs,
  *                   positions their running sums, at most 6 levels;
- *   grid.f:917-1114 finite-difference weights by inverting the Taylor
+ *   grid.f:926-1115 finite-difference weights by inverting the Taylor
  *                   matrix of the stencil points (Gaussian elimination with
  *                   partial pivoting, gausse);
- *   grid.f:160-214  per level: first-derivative weights on (i-1, i, i+1),
+ *   grid.f:178-226  per level: first-derivative weights on (i-1, i, i+1),
  *                   second-derivative weights on (i-1..i+2) for i <= n/2
  *                   and on (i-2..i+1) above;
  *   rcsc.f:1118-1444 the multigrid: psi_rr + psi_r / r - psi / r^2 + psi_zz
@@ -46,7 +46,7 @@ extern "C" {
  * exceeded"). */
 int orc_str_spacing_gef(int n, double lo, double hi, double dist, double gef, double d1, double *h);
 
-/* level (grid.f:859-915) for level-1 spacings hr1[1..n1], hz1[1..n2]
+/* level (grid.f:859-924) for level-1 spacings hr1[1..n1], hz1[1..n2]
  * (1-based, index 0 unused); fills n1[l], n2[l], hr[l][1..], hz[l][1..],
  * r[l][0..], z[l][0..] and returns nlev (halvings while both halve exactly
  * and are >= 4, capped at 6). */
@@ -55,18 +55,18 @@ typedef struct {
     int n1[STR_MAXLEV], n2[STR_MAXLEV];
     double *hr[STR_MAXLEV], *hz[STR_MAXLEV], *r[STR_MAXLEV], *z[STR_MAXLEV];
     double *cr[STR_MAXLEV], *crr[STR_MAXLEV], *cz[STR_MAXLEV], *czz[STR_MAXLEV];
-    double cr0[3], crn[3], cz0[3], czn[3];   /* one-sided wall weights of level 1 (grid.f:216-231) */
+    double cr0[3], crn[3], cz0[3], czn[3];   /* one-sided wall weights of level 1 (grid.f:228-243) */
 } orc_str_grid_t;
 
 int  orc_str_levels(orc_str_grid_t *g, int n1, int n2, const double *hr1, const double *hz1, double r0,
                     double zmin, int maxlev);
 void orc_str_grid_free(orc_str_grid_t *g);
-/* fdif (grid.f:917-1032) with nans = 0: weights of the nx points
+/* fdif (grid.f:926-1032) with nans = 0: weights of the nx points
  * x[k-nref+1 .. k-nref+nx] (x 0-based here) for derivatives 0..nx-1;
  * w[d*nx + p] = weight of point p for derivative d.  Returns -1 on a
  * singular matrix (the reference STOPs). */
 int  orc_str_fdif(int nx, int nref, int k, const double *x, double *w);
-/* The coefficient tables of every level (grid.f:160-231). */
+/* The coefficient tables of every level (grid.f:178-243). */
 int  orc_str_coefficients(orc_str_grid_t *g);
 
 /* Multigrid state (COMMON /backup/ /arrays/ /step/ /ints/ /coeff/). */

@@ -1,7 +1,7 @@
 """The stretched-grid operator (rcsc.f) and its coefficient build (grid.f),
 on the CPU:
 
-* fdif's weights (grid.f:917-1114) differentiate polynomials of degree
+* fdif's weights (grid.f:926-1115) differentiate polynomials of degree
   < nx exactly on arbitrary non-uniform points;
 * the product's host generator (codesthesis_dir_gb300/grid.py) produces the
   oracle's spacings, levels and tables bit for bit, for grid.f's GEF grid,
