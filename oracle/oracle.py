@@ -171,6 +171,7 @@ def lib():
         L.orc_axi_set_stretched.argtypes = [C.POINTER(AXI), C.POINTER(STRGrid), C.POINTER(STRMG)]
         L.orc_axi_set_stretched.restype = C.c_int
         L.orc_axi_step.restype = C.c_int
+        L.orc_axi_arakawa.argtypes = [C.POINTER(AXI), _dp, _dp, _dp]
         L.orc_axi_relax.argtypes = [C.POINTER(AXI), C.c_int, C.c_int, _ip]
         L.orc_axi_corser.argtypes = [C.POINTER(AXI), C.c_int]
         L.orc_axi_finer.argtypes = [C.POINTER(AXI), C.c_int]
@@ -389,6 +390,20 @@ class OracleAXI:
 
     def initial(self, kind=1, seed=0, amp=1e-3):
         lib().orc_axi_initial(C.byref(self.s), kind, seed, amp)
+
+    def arakawa(self, psi, th) -> np.ndarray:
+        """rotann2.f's arakawa(arak, psi, th) on (nr+1, nz+1) arrays indexed
+        [i, j]; the interior points of the result are set, the rest zero."""
+        ld, nz = self.s.ld, self.s.nz
+        def col(a):
+            b = np.zeros((nz + 1, ld))
+            b[:, :a.shape[0]] = np.asarray(a, dtype=np.float64).T
+            return np.ascontiguousarray(b)
+        out = np.zeros((nz + 1, ld))
+        pa, ta = col(psi), col(th)
+        lib().orc_axi_arakawa(C.byref(self.s), out.ctypes.data_as(_dp), pa.ctypes.data_as(_dp),
+                              ta.ctypes.data_as(_dp))
+        return out.T[:self.s.nr + 1, :].copy()
 
     def stretch(self, hr1, hz1):
         """Puts the state on the non-uniform grid of level-1 spacings hr1,

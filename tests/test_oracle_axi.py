@@ -10,7 +10,9 @@ own, on the CPU:
 * the two line orderings converge to the same solution;
 * corser clears row j = n1 of the coarse level (n1 in both directions,
   rotann2.f:787-798): with nr < nz that row is interior and its coarse
-  right-hand side is zero."""
+  right-hand side is zero;
+* the Arakawa Jacobian (rotann2.f:432-459) is antisymmetric, conserves the
+  mean and both fields' squares over the interior, and is second order."""
 import ctypes as C
 import math
 
@@ -79,3 +81,64 @@ def test_corser_clears_row_n1(oracle):
     assert n1c < n2c
     assert np.all(fc[:, n1c] == 0.0)          # the interior row j = n1c
     assert np.all(fc[1:n1c, n1c + 1] != 0.0)  # its neighbour is a restriction
+
+
+# Arakawa's Jacobian (rotann2.f:432-459; A. Arakawa, J. Comput. Phys. 1, 1966,
+# the average J = (J++ + J+x + Jx+) / 3 of three second-order forms).  The
+# restatement must keep the properties the published scheme has by
+# construction, whatever the fields: J(a, b) = -J(b, a) (the terms pair off
+# exactly, so only rounding remains); with both fields zero on the two outer
+# rings of points, the interior sums of J, a J and b J vanish (discrete
+# conservation of the mean, of a^2 and of b^2 under advection); and it
+# approximates a_r b_z - a_z b_r to second order.
+
+def _axi(oracle, nr, nz):
+    return oracle.OracleAXI(nr, nz, 1e-5, 0.5, 1.0, 0.5, 1e5, 1e2, 1.0)
+
+
+def _compact_random(rng, nr, nz):
+    a = np.zeros((nr + 1, nz + 1))
+    a[2:nr - 1, 2:nz - 1] = rng.standard_normal((nr - 3, nz - 3))
+    return a
+
+
+@pytest.mark.parametrize("nr,nz", [(16, 16), (24, 40)])
+def test_arakawa_antisymmetric_and_conservative(oracle, nr, nz):
+    o = _axi(oracle, nr, nz)
+    rng = np.random.default_rng(nr * 100 + nz)
+    a, b = _compact_random(rng, nr, nz), _compact_random(rng, nr, nz)
+    jab, jba = o.arakawa(a, b), o.arakawa(b, a)
+    scale = np.max(np.abs(jab))
+    assert scale > 0
+    np.testing.assert_allclose(jab, -jba, rtol=0, atol=1e-13 * scale)
+    w = np.abs(jab).sum()
+    for weight in (np.ones_like(a), a, b):
+        assert abs((weight * jab).sum()) <= 1e-12 * w * max(1.0, np.max(np.abs(weight)))
+    # an ordinary centred Jacobian of the same fields conserves none of them
+    assert abs((a * jab).sum()) < 1e-6 * abs((a * _centred(a, b, o)).sum())
+    o.close()
+
+
+def _centred(a, b, o):
+    hx, hy = o.s.dr, o.s.dz
+    j = np.zeros_like(a)
+    j[1:-1, 1:-1] = ((a[2:, 1:-1] - a[:-2, 1:-1]) * (b[1:-1, 2:] - b[1:-1, :-2]) -
+                     (a[1:-1, 2:] - a[1:-1, :-2]) * (b[2:, 1:-1] - b[:-2, 1:-1])) / (4 * hx * hy)
+    return j
+
+
+def test_arakawa_second_order(oracle):
+    errs = []
+    for n in (16, 32, 64):
+        o = _axi(oracle, n, n)
+        r = 0.5 + np.arange(n + 1) * (0.5 / n)
+        z = np.arange(n + 1) * (0.5 / n)
+        R, Z = np.meshgrid(r, z, indexing="ij")
+        a = np.sin(3.0 * R) * np.cos(2.0 * Z)
+        b = np.cos(2.0 * R + Z)
+        exact = (3.0 * np.cos(3.0 * R) * np.cos(2.0 * Z)) * (-np.sin(2.0 * R + Z)) - \
+                (-2.0 * np.sin(3.0 * R) * np.sin(2.0 * Z)) * (-2.0 * np.sin(2.0 * R + Z))
+        j = o.arakawa(a, b)
+        errs.append(np.max(np.abs(j[1:-1, 1:-1] - exact[1:-1, 1:-1])))
+        o.close()
+    assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5, errs
