@@ -1,0 +1,244 @@
+"""Runs the reference's own Fortran drivers on the CPU through the translator
+in f77.py and collects what they compute: the final fields, the Nusselt
+number history and the multigrid sweep count of every solve.
+
+Test infrastructure only.  It reads the reference's source files, so only
+the fixture generator beside it (make_reference_golden.py) calls it; the
+fixtures it writes are what the tests read.
+
+Each driver runs as its main program with an input deck in the format the
+program reads (list-directed READ *), answering "no" to "initial
+conditions from file" (the program's own initial state) and to "more
+iterations"; its file output is skipped.  The sweep count of a solve is the
+last value the solve's outer loop variable took (`do 50 i=1,nvs`), read
+through the translator's loop probes.
+"""
+import hashlib
+import os
+
+import numpy as np
+
+import f77
+
+REFERENCE = os.environ.get("GB300_REFERENCE_SOURCE", "/root/reference")
+
+# driver -> (source file within the reference, multigrid units in step order)
+DRIVERS = {
+    "layer": ("monashubuntudir_velvor2dperiodicrbconvdir/velvor2dperiodicrbconv.f", ("poisson2", "poisson3")),
+    "oblique": ("monashubuntudir_velvor2dperiodicrbconvdir/mpkoks.f", ("poisson2", "poisson3")),
+    "annulus": ("iarchomedir_groke_storage_users_mpking_rotannconvvelvorplane_continueddir/velvor2dnewsch3.4.f",
+                ("poisson2", "poisson3")),
+    "tank": ("monashubuntudir_velvor2dhorconvtankdir/velvor2dhorconvtank.f", ("poisson2", "poisson3")),
+    "dvd": ("monashubuntudir_velvor2ddvdbenchmarkdir/velvor2ddvdbenchmark.f", ("poisson2", "poisson3")),
+    "taycou": ("monashubuntudir_velvor2dtaycouheatdir/velvor2dtaycouheat.f", ("poisson2", "poisson3")),
+    "r3d": ("rot3dmg.f", ("poisson1", "poisson2", "poisson3")),
+    "r3d_hor": ("rot3dmghor.f", ("poisson1", "poisson2", "poisson3")),
+    "axi": ("rotann2.f", ("poisson",)),
+}
+
+FIELDS_2D = ["A", "B", "An", "Bn", "Ap", "Cn", "C", "Cp", "thn", "th", "thp", "uel", "vel", "uelp", "velp"]
+FIELDS_3D = ["An", "A", "Ap", "Bn", "B", "Bp", "Cn", "C", "Cp", "thn", "th", "thp",
+             "uel", "vel", "wel", "uelp", "velp", "welp"]
+FIELDS_AXI = ["phi", "omegn", "omeg", "omegp", "veln", "vel", "velp", "thetan", "theta", "thetap"]
+
+
+def source(driver):
+    return os.path.join(REFERENCE, DRIVERS[driver][0])
+
+
+def sha256(path):
+    with open(path, "rb") as fh:
+        return hashlib.sha256(fh.read()).hexdigest()
+
+
+def _solve_loops(prog, unit):
+    """Source lines of the unit's `do ... i=1,nvs` loops (the sweep loop)."""
+    out = []
+
+    def walk(items):
+        for _, node in items:
+            if node[0] == "do":
+                if node[1] == "i" and node[3] == ("name", "nvs"):
+                    out.append(node[6])
+                walk(node[5])
+            elif node[0] == "if":
+                for _, body in node[1]:
+                    walk(body)
+    walk(prog.units[unit].exec)
+    if len(out) != 1:
+        raise ValueError("%s: expected one sweep loop, found %s" % (unit, out))
+    return out[0]
+
+
+def sweeps_per_solve(seq):
+    """Loop-variable values of consecutive solves -> sweeps of each solve."""
+    counts = []
+    for v in seq:
+        if v == 1:
+            counts.append(1)
+        else:
+            counts[-1] = v
+    return counts
+
+
+def sweep_table(prog, units):
+    """Sweeps of each solve, one column per multigrid unit in step order;
+    -1 where a solve did not run (the run stopped before it)."""
+    cols = [sweeps_per_solve(prog.probe[u]) for u in units]
+    n = max(len(c) for c in cols)
+    return np.array([c + [-1] * (n - len(c)) for c in cols], dtype=np.int32).T
+
+
+def program(driver, deck):
+    """The driver's translated program, fed `deck`, with its sweep loops
+    probed."""
+    path = source(driver)
+    plain = f77.Program(path, with_main=True)
+    probes = {(u, _solve_loops(plain, u)): u for u in DRIVERS[driver][1]}
+    return f77.Program(path, probes=probes, with_main=True, stdin=deck)
+
+
+def run_main(prog):
+    """Runs the main program to its STOP.  Returns the unit whose STOP
+    ended it: '_main' for the program's own closing STOP, else the routine
+    that stopped the run (a solve past its sweep limit)."""
+    try:
+        prog.sub("_main")()
+    except f77.FortranStop as e:
+        return str(e)
+    return "end"
+
+
+def extract(prog, name, ranges):
+    """Elements of main-program array `name` over the index ranges
+    [(lo, hi), ...] (inclusive), dimensions of extent 1 dropped."""
+    u = prog.units["_main"]
+    v = u.vars[name.lower()]
+    lo = [u.const_eval(a)[1] for a, _ in v.dims]
+    hi = [u.const_eval(b)[1] for _, b in v.dims]
+    if v.kind == "common":
+        blk, idx = v.common
+        buf = prog.common[blk][idx]
+    else:
+        buf = prog.static[("_main", name.lower())]
+    strides, s = [], 1
+    for a, b in zip(lo, hi):
+        strides.append(s)
+        s *= b - a + 1
+    shape = [b - a + 1 for a, b in ranges]
+    out = np.zeros(shape)
+    for idx in np.ndindex(*shape):
+        off = sum((ranges[d][0] + idx[d] - lo[d]) * strides[d] for d in range(len(idx)))
+        out[idx] = buf[off]
+    return out.reshape([n for n in shape if n != 1])
+
+
+def deck_2d(nr, np_, nts, dt, r0, rmax, Ra, Re, Gr, Pr, zmax=0.1, pert=0.0, amp=1.0, nval=3):
+    """The 2D drivers' deck (velvor2dperiodicrbconv.f:73-117 and alike):
+    file names, dt, nr, np, nts, r0 rmax zmax, Ra, Re, Gr (Ta for the
+    Taylor-Couette driver), Ptl, pert, amp, nval, then the answers."""
+    return ["a.dat", "b.dat", "c.dat", "u.dat", "v.dat", "w.dat", "t.dat", "nu.dat",
+            repr(dt), str(nr), str(np_), str(nts), "%r,%r,%r" % (r0, rmax, zmax), repr(Ra), repr(Re), repr(Gr),
+            repr(Pr), repr(pert), repr(amp), str(nval), "no", "no"]
+
+
+def deck_3d(nr, nz, np_, nts, dt, r0, rmax, zmax, Ra, Re, Gr, Pr, pert=0.0, amp=1e-2, nval=3):
+    """rot3dmg.f:45-86 (rot3dmghor.f alike)."""
+    return ["a.dat", "b.dat", "c.dat", "u.dat", "v.dat", "w.dat", "t.dat", "nu.dat",
+            repr(dt), str(nr), str(nz), str(np_), str(nts), "%r,%r,%r" % (r0, rmax, zmax), repr(Ra), repr(Re),
+            repr(Gr), repr(Pr), repr(pert), repr(amp), str(nval), "no", "no"]
+
+
+def deck_axi(nr, nz, nts, dt, r0, rmax, zmax, Ra, Re, Pr, pert=0.0):
+    """rotann2.f:24-55."""
+    return ["o.dat", "p.dat", "v.dat", "t.dat", "no", "no", "no", repr(dt), str(nr), str(nz), str(nts),
+            "%r,%r,%r" % (r0, rmax, zmax), repr(Ra), repr(Re), repr(Pr), repr(pert), "no"]
+
+
+def run_2d(driver, nr, np_, nts, **kw):
+    """A 2D driver from its own start.  Returns the outputs as a dict."""
+    deck = deck_2d(nr, np_, nts, **kw)
+    prog = program(driver, deck)
+    end = run_main(prog)
+    ncol = np_ + 2 if driver in ("tank", "dvd") else np_ + 1
+    out = {f: extract(prog, f, [(0, nr + 1), (1, 1), (0, ncol - 1)]) for f in FIELDS_2D}
+    nu = np.stack([extract(prog, h, [(1, nts)]) for h in ("httrans", "httrans2")], axis=1)
+    return dict(fields=out, nu=nu, sweeps=sweep_table(prog, DRIVERS[driver][1]), end=end, deck=deck,
+                source=DRIVERS[driver][0], sha256=sha256(source(driver)))
+
+
+def run_3d(driver, nr, nz, np_, nts, **kw):
+    deck = deck_3d(nr, nz, np_, nts, **kw)
+    prog = program(driver, deck)
+    end = run_main(prog)
+    out = {f: extract(prog, f, [(0, nr + 1), (0, nz + 1), (0, np_)]) for f in FIELDS_3D}
+    names = ("httrans1", "httrans2") if driver == "r3d_hor" else ("httrans",)
+    nu = np.stack([extract(prog, h, [(1, nts)]) for h in names], axis=1)
+    return dict(fields=out, nu=nu, sweeps=sweep_table(prog, DRIVERS[driver][1]), end=end, deck=deck,
+                source=DRIVERS[driver][0], sha256=sha256(source(driver)))
+
+
+def run_axi(nr, nz, nts, **kw):
+    deck = deck_axi(nr, nz, nts, **kw)
+    prog = program("axi", deck)
+    end = run_main(prog)
+    out = {f: extract(prog, f, [(0, nr), (0, nz)]) for f in FIELDS_AXI}
+    sw = sweeps_per_solve(prog.probe["poisson"])
+    nu = extract(prog, "httrans", [(1, len(sw))]).reshape(-1)
+    return dict(fields=out, nu=nu, sweeps=np.array(sw, dtype=np.int32), end=end, deck=deck,
+                source=DRIVERS["axi"][0], sha256=sha256(source("axi")))
+
+
+def run_layer_routines(nr, np_, nsteps, init, dt, Ra, Pr, r0, rmax, xx):
+    """The layer's subroutines called in the main loop's order
+    (velvor2dperiodicrbconv.f:341-388) from a given state, with COMMON set
+    as the main program sets it (dr = (rmax-r0)/nr, dp = xx/np, nz = 1,
+    dz = 0, Re = Gr = 0): for states other than the program's own start
+    and for box lengths other than its xx = 3."""
+    prog = program("layer", [])
+    cm = prog.common_member
+    dr = (rmax - r0) / float(nr)
+    dp = xx / float(np_)
+    for blk, name, val in (("num", "dt", dt), ("num", "dr", dr), ("num", "dz", 0.0), ("num", "dp", dp),
+                           ("num", "nr", nr), ("num", "nz", 1), ("num", "np", np_), ("val", "ra", Ra),
+                           ("val", "re", 0.0), ("val", "ptl", Pr), ("val", "gr", 0.0), ("radius", "r0", r0),
+                           ("radius", "rmax", rmax)):
+        cm(blk, name)[0] = val
+    u = prog.units["poisson2"]
+    kr1 = u.const_eval(("name", "kr"))[1] + 1
+    kp1 = u.const_eval(("name", "kp"))[1] + 1
+    sol = {"an": "sol1", "a": "sol1", "ap": "sol1", "bn": "sol1", "b": "sol1", "bp": "sol1", "cn": "sol1",
+           "c": "sol1", "cp": "sol1", "thn": "sol2", "th": "sol2", "thp": "sol2", "uel": "sol3", "vel": "sol3",
+           "wel": "sol3", "uelp": "sol3", "velp": "sol3", "welp": "sol3"}
+    vrh, urh = [0.0] * (kr1 * kp1), [0.0] * (kr1 * kp1)
+    bufs = {n: cm(b, n) for n, b in sol.items()}
+    bufs["vrh"], bufs["urh"] = vrh, urh
+    for name, a in init.items():
+        buf = bufs[name.lower()]
+        for k in range(np_ + 1):
+            for i in range(nr + 2):
+                buf[i + kr1 * k] = float(a[i, k])
+    R, Cl = f77.ref, f77.cell
+    nrc, nzc, npc = Cl(nr), Cl(1), Cl(np_)
+    drc, dzc, dpc = Cl(dr), Cl(0.0), Cl(dp)
+    nlev = Cl(0)
+    prog.sub("poissoninit")(nrc, nzc, npc, drc, dzc, dpc, nlev)
+    nus = []
+    for kt in range(1, nsteps + 1):
+        cm("iteration", "kt")[0] = kt
+        prog.sub("cvorticity1" if kt == 1 else "cvorticity")()
+        prog.sub("temperature1" if kt == 1 else "temperature")()
+        t1, t2 = Cl(0.0), Cl(0.0)
+        prog.sub("heat")(t1, t2)
+        prog.sub("rhsv")(R(vrh))
+        prog.sub("poisson2")(R(bufs["vel"]), R(bufs["velp"]), R(vrh), nrc, nzc, npc, drc, dzc, dpc, nlev)
+        prog.sub("rhsu")(R(urh))
+        prog.sub("poisson3")(R(bufs["uel"]), R(bufs["uelp"]), R(urh), nrc, nzc, npc, drc, dzc, dpc, nlev)
+        prog.sub("update")()
+        nus.append((t1[0][0] * (rmax - r0) / xx, t2[0][0] * (rmax - r0) / xx))
+
+    def grab(buf):
+        return np.array([[buf[i + kr1 * k] for k in range(np_ + 1)] for i in range(nr + 2)])
+    out = {f: grab(bufs[f.lower()]) for f in FIELDS_2D + ["urh", "vrh"]}
+    return dict(fields=out, nu=np.array(nus), sweeps=sweep_table(prog, ("poisson2", "poisson3")), end="return",
+                source=DRIVERS["layer"][0], sha256=sha256(source("layer")))
