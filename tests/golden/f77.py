@@ -1177,7 +1177,10 @@ class Program:
     (subroutine, source line of a DO statement) -> a name under which every
     value the loop variable takes is appended to self.probe[name]."""
 
-    def __init__(self, path, probes=None, with_main=False, stdin=()):
+    def __init__(self, path, probes=None, with_main=False, stdin=(), replace=None):
+        """replace maps a subroutine name to another source file whose
+        subroutine of that name is used instead (to run a program with one
+        routine taken from a sibling version of the file)."""
         self.path = path
         self.input = ListInput(stdin)
         self.probes = dict(probes or {})
@@ -1195,6 +1198,14 @@ class Program:
                 self.units[name] = u
             elif with_main:
                 self.units["_main"] = Unit("_main", [], stmts, self.commons)
+        for name, other in (replace or {}).items():
+            found = [u for u in read_units(other) if u[0] == "subroutine" and u[1] == name]
+            if len(found) != 1 or name not in self.units:
+                raise ValueError("cannot replace %s from %s" % (name, other))
+            kind, _, args, stmts = found[0]
+            for key in list(self.commons):
+                self.commons[key] = [(u, n) for u, n in self.commons[key] if u.name != name]
+            self.units[name] = Unit(name, args, stmts, self.commons)
         self.layout = self._common_layout()
         src = ["import math", ""]
         for u in self.units.values():

@@ -72,6 +72,16 @@ def main():
         meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra,
                     Re=Re, Gr=Gr, Pr=Pr, xx=XX[drv])
         save("ref_%s_%dx%d.npz" % (drv, nr, np_), res, meta)
+    # the Taylor-Couette driver as written STOPs in its first v solve (its
+    # relax2 forms a line's right-hand side only for k = 1); the same
+    # program with relax2 taken from velvor2dtaycouheat_new.f, which forms
+    # every line's, is what the oracle restates
+    drv, nr, np_, nts, dt, r0, rmax, Ra, Re, Gr, Pr = CASES_2D[-1]
+    rep = {"relax2": "monashubuntudir_velvor2dtaycouheatdir/velvor2dtaycouheat_new.f"}
+    res = RR.run_2d(drv, nr, np_, nts, replace=rep, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr)
+    meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re,
+                Gr=Gr, Pr=Pr, xx=XX[drv], replace=rep)
+    save("ref_taycou_relax2new_%dx%d.npz" % (nr, np_), res, meta)
     # the layer at the 129 x 65 grid of the benchmark's layer workload (box
     # length 2, seeded start), routine by routine in the main loop's order
     cfg = dict(nr=64, np_=128, dt=1e-5, Ra=1e5, Pr=1.0, r0=0.0, rmax=1.0, xx=2.0)

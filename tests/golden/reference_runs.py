@@ -89,13 +89,15 @@ def sweep_table(prog, units):
     return np.array([c + [-1] * (n - len(c)) for c in cols], dtype=np.int32).T
 
 
-def program(driver, deck):
+def program(driver, deck, replace=None):
     """The driver's translated program, fed `deck`, with its sweep loops
-    probed."""
+    probed; replace: {subroutine: source file within the reference} takes
+    those subroutines from a sibling version of the driver."""
     path = source(driver)
-    plain = f77.Program(path, with_main=True)
+    rep = {n: os.path.join(REFERENCE, f) for n, f in (replace or {}).items()}
+    plain = f77.Program(path, with_main=True, replace=rep)
     probes = {(u, _solve_loops(plain, u)): u for u in DRIVERS[driver][1]}
-    return f77.Program(path, probes=probes, with_main=True, stdin=deck)
+    return f77.Program(path, probes=probes, with_main=True, stdin=deck, replace=rep)
 
 
 def run_main(prog):
@@ -155,10 +157,10 @@ def deck_axi(nr, nz, nts, dt, r0, rmax, zmax, Ra, Re, Pr, pert=0.0):
             "%r,%r,%r" % (r0, rmax, zmax), repr(Ra), repr(Re), repr(Pr), repr(pert), "no"]
 
 
-def run_2d(driver, nr, np_, nts, **kw):
+def run_2d(driver, nr, np_, nts, replace=None, **kw):
     """A 2D driver from its own start.  Returns the outputs as a dict."""
     deck = deck_2d(nr, np_, nts, **kw)
-    prog = program(driver, deck)
+    prog = program(driver, deck, replace)
     end = run_main(prog)
     ncol = np_ + 2 if driver in ("tank", "dvd") else np_ + 1
     out = {f: extract(prog, f, [(0, nr + 1), (1, 1), (0, ncol - 1)]) for f in FIELDS_2D}

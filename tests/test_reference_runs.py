@@ -17,8 +17,10 @@ side only for k = 1 (the block of :2132-2164 sits inside `if(k.eq.1)then`),
 so every later line solves with the right-hand side the previous line's
 elimination left in pdmar; run as written, its first velocity solve reaches
 the sweep limit and STOPs.  The oracle forms every line's right-hand side,
-as velvor2dtaycouheat_new.f does (:2181-2182, after the block); the last
-test records both facts."""
+as velvor2dtaycouheat_new.f does (:2181-2182, after the block): it
+reproduces velvor2dtaycouheat.f run with that one subroutine taken from
+velvor2dtaycouheat_new.f (ref_taycou_relax2new_*.npz), and the last test
+records that the program as written stops."""
 import json
 import os
 
@@ -27,7 +29,7 @@ import pytest
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = sorted(f for f in os.listdir(GOLD) if f.startswith("ref_") and f.endswith(".npz")
-               and not f.startswith("ref_taycou"))
+               and f != "ref_taycou_16x32.npz")
 F2D = ["A", "B", "An", "Bn", "Ap", "Cn", "C", "Cp", "thn", "th", "thp", "uel", "vel", "uelp", "velp"]
 
 
@@ -54,7 +56,7 @@ def test_oracle_reproduces_reference_run(oracle, case):
     g, m = load(case)
     assert m["end"] in ("_main", "return")     # the run ended at its own end
     drv = m["driver"]
-    if drv in ("layer", "oblique", "annulus", "tank", "dvd", "layer_routines"):
+    if drv in ("layer", "oblique", "annulus", "tank", "dvd", "taycou", "layer_routines"):
         if drv == "layer_routines":
             o, nu, sw = run_2d(oracle, m, 1, m["init"]["seed"], m["init"]["amp"])
             names = F2D + ["urh", "vrh"]
@@ -99,7 +101,8 @@ def test_oracle_reproduces_reference_run(oracle, case):
 
 def test_reference_runs_cover_the_drivers():
     drivers = {load(c)[1]["driver"] for c in CASES}
-    assert drivers >= {"layer", "oblique", "annulus", "tank", "dvd", "layer_routines", "r3d", "r3d_hor", "axi"}
+    assert drivers >= {"layer", "oblique", "annulus", "tank", "dvd", "taycou", "layer_routines", "r3d", "r3d_hor",
+                       "axi"}
     for c in CASES:
         m = load(c)[1]
         assert len(m["sha256"]) == 64 and m["source"].endswith(".f")
