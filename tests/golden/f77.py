@@ -164,6 +164,8 @@ def read_units(path):
             t = {"real*8": "d", "doubleprecision": "d", "real*4": "r", "real": "r", "integer": "i",
                  "logical": "l"}.get(f.group(1))
             res.append(("function:%s" % (t or ""), f.group(2), args, u[1:-1]))
+        elif re.match(r"^program[a-z]\w*$", u[0][1]):
+            res.append(("program", None, [], u[1:-1]))
         else:
             res.append(("program", None, [], u[:-1]))
     return res
@@ -661,7 +663,8 @@ class Unit:
             if s.startswith("common"):
                 self._common(s[6:], lineno)
                 continue
-            if s.startswith(("save", "data", "equivalence", "external", "intrinsic", "entry")):
+            if s.startswith(("save", "data", "equivalence", "external", "intrinsic", "entry")) \
+                    and find_top(s, "=") < 0:
                 raise NotImplementedError("line %d: %r" % (lineno, s))
             if s.startswith("format("):
                 continue
@@ -1177,17 +1180,23 @@ class Program:
     (subroutine, source line of a DO statement) -> a name under which every
     value the loop variable takes is appended to self.probe[name]."""
 
-    def __init__(self, path, probes=None, with_main=False, stdin=(), replace=None):
+    def __init__(self, path, probes=None, with_main=False, stdin=(), replace=None, stubs=()):
         """replace maps a subroutine name to another source file whose
         subroutine of that name is used instead (to run a program with one
-        routine taken from a sibling version of the file)."""
+        routine taken from a sibling version of the file); stubs names
+        subroutines that run as no-ops (graphics calls into a plotting
+        library the image does not have, whether or not the file defines
+        them)."""
         self.path = path
+        self.stubs = set(stubs)
         self.input = ListInput(stdin)
         self.probes = dict(probes or {})
         self.statics = {}
         self.commons = {}
         self.units = {}
         for kind, name, args, stmts in read_units(path):
+            if name in self.stubs:
+                continue
             if kind == "subroutine":
                 self.units[name] = Unit(name, args, stmts, self.commons)
             elif kind.startswith("function:"):
@@ -1208,6 +1217,8 @@ class Program:
             self.units[name] = Unit(name, args, stmts, self.commons)
         self.layout = self._common_layout()
         src = ["import math", ""]
+        for name in sorted(self.stubs):
+            src.append("def F_%s(*args):\n    return None\n" % name)
         for u in self.units.values():
             src.append(Gen(u, self).function())
             src.append("")

@@ -105,6 +105,22 @@ def main():
         res = RR.run_axi(nr, nz, nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Pr=Pr)
         meta = dict(driver="axi", nr=nr, nz=nz, steps=nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Pr=Pr)
         save("ref_axi_%dx%d.npz" % (nr, nz), res, meta)
+    # grid.f's stretched levels and weight tables, and rcsc.f's multigrid on
+    # them (the stretched streamfunction solve of the annulus on a tanh
+    # or GEF grid)
+    g = dict(nr=64, nz=64, r0=0.5, rmax=1.0, zmax=0.5, zmin=0.0, rdist=0.1, rgef=1.1, dr1=0.002, zdist=0.1,
+             zgef=1.1, dz1=0.002)
+    gprog, res = RR.run_grid(**g)
+    rng = np.random.default_rng(5)
+    rhs = rng.standard_normal((g["nr"] + 1, g["nz"] + 1))
+    psi0 = np.zeros_like(rhs)
+    psi, sw, sha_rcsc = RR.run_rcsc_poisson(gprog, res["nlev"], psi0, rhs)
+    meta = dict(driver="grid_rcsc", nlev=res["nlev"], source=res["source"], sha256=res["sha256"], end=res["end"],
+                deck=res["deck"], rcsc_source="rcsc.f", rcsc_sha256=sha_rcsc, **g)
+    np.savez_compressed(os.path.join(HERE, "ref_grid_rcsc_64x64.npz"), meta=np.array(json.dumps(meta)),
+                        rhs=rhs, psi=psi, sweeps=np.array(sw, dtype=np.int32),
+                        **{"t_" + k: v for k, v in res["tables"].items()})
+    print("ref_grid_rcsc_64x64.npz            grid_rcsc  nlev=%d sweeps=%s" % (res["nlev"], sw), flush=True)
     print("fixtures written to %s in %.0f s" % (HERE, time.time() - t0))
 
 

@@ -244,3 +244,71 @@ def run_layer_routines(nr, np_, nsteps, init, dt, Ra, Pr, r0, rmax, xx):
     out = {f: grab(bufs[f.lower()]) for f in FIELDS_2D + ["urh", "vrh"]}
     return dict(fields=out, nu=np.array(nus), sweeps=sweep_table(prog, ("poisson2", "poisson3")), end="return",
                 source=DRIVERS["layer"][0], sha256=sha256(source("layer")))
+
+
+GRID_STUBS = ("contor", "xxxxxx", "j06waf", "j06wcf", "j06wbf", "j06xff", "j06ahf", "j06wzf", "grapol", "gracur",
+              "gramov", "gralin")
+
+
+def run_grid(nr, nz, r0, rmax, zmax, zmin, rdist, rgef, dr1, zdist, zgef, dz1):
+    """grid.f's main program (grid.f:53-270): wall-clustered spacings with
+    geometric expansion (grid, :723-857), the levels (level, :859-924) and
+    the finite-difference weight tables of every level (:178-243, fdif and
+    gausse).  Its plotting calls (the NAG graphics library and its contour
+    routine) run as no-ops; the coefficient file it writes is read from its
+    arrays instead.  Returns the program (its arrays feed run_rcsc_poisson)
+    and the tables."""
+    deck = [str(nr), str(nz), "%r,%r,%r,%r" % (r0, rmax, zmax, zmin), "y", repr(rdist), repr(rgef), repr(dr1),
+            "y", repr(zdist), repr(zgef), repr(dz1), "n", "y", "coef.dat"]
+    path = os.path.join(REFERENCE, "grid.f")
+    prog = f77.Program(path, with_main=True, stdin=deck, stubs=GRID_STUBS)
+    end = run_main(prog)
+    u = prog.units["_main"]
+    nx = u.const_eval(("name", "nx"))[1]
+    st = lambda n: prog.static[("_main", n)]  # noqa: E731
+    n1, n2 = st("n1"), st("n2")
+    nlev = sum(1 for v in n1 if v > 0)
+    tables = {}
+    for L in range(1, nlev + 1):
+        a, b = n1[L - 1], n2[L - 1]
+        tables["hr_%d" % L] = np.array([st("hx")[(i - 1) + nx * (L - 1)] for i in range(1, a + 1)])
+        tables["hz_%d" % L] = np.array([st("hy")[(j - 1) + nx * (L - 1)] for j in range(1, b + 1)])
+        tables["r_%d" % L] = np.array([st("x")[i + (nx + 1) * (L - 1)] for i in range(a + 1)])
+        tables["z_%d" % L] = np.array([st("y")[j + (nx + 1) * (L - 1)] for j in range(b + 1)])
+        for name, n, w in (("cr", a, 3), ("crr", a, 4), ("cz", b, 3), ("czz", b, 4)):
+            tables["%s_%d" % (name, L)] = np.array([[st(name)[(i - 1) + nx * ((k - 1) + w * (L - 1))]
+                                                     for k in range(1, w + 1)] for i in range(1, n)]).ravel()
+    # the wall weights of level 1 at i = n1 and j = n2 (the file's last lines)
+    tables["crn"] = np.array([st("cr")[(n1[0] - 1) + nx * (k - 1)] for k in range(1, 4)])
+    tables["czn"] = np.array([st("cz")[(n2[0] - 1) + nx * (k - 1)] for k in range(1, 4)])
+    return prog, dict(tables=tables, nlev=nlev, end=end, deck=deck, source="grid.f", sha256=sha256(path))
+
+
+def run_rcsc_poisson(grid_prog, nlev, psi, rhs):
+    """rcsc.f's stretched-grid multigrid (poisson, :1118-1190, with relax,
+    corser and finer) on the levels and tables grid.f computed, copied into
+    rcsc.f's COMMON blocks /num/, /ints/ and /coeff/ as rcsc.f's main program
+    reads them from grid.f's coefficient file.  Returns psi and the sweeps."""
+    path = os.path.join(REFERENCE, "rcsc.f")
+    plain = f77.Program(path)
+    prog = f77.Program(path, probes={("poisson", _solve_loops(plain, "poisson")): "poisson"})
+    st = lambda n: grid_prog.static[("_main", n)]  # noqa: E731
+    for blk, name, src in (("num", "hr", "hx"), ("num", "hz", "hy"), ("num", "r", "x"), ("num", "z", "y"),
+                           ("num", "n1", "n1"), ("num", "n2", "n2"), ("ints", "ibeg", "ibeg"),
+                           ("coeff", "cr", "cr"), ("coeff", "crr", "crr"), ("coeff", "cz", "cz"),
+                           ("coeff", "czz", "czz")):
+        dst = prog.common_member(blk, name)
+        if len(dst) != len(st(src)):
+            raise ValueError("grid.f and rcsc.f disagree on the size of " + name)
+        dst[:] = st(src)
+    u = prog.units["poisson"]
+    ld = u.const_eval(("name", "kr"))[1] + 1
+    n1, n2 = psi.shape[0] - 1, psi.shape[1] - 1
+    pb, rb, vb = [0.0] * (ld * ld), [0.0] * (ld * ld), [0.0] * (ld * ld)
+    for j in range(n2 + 1):
+        for i in range(n1 + 1):
+            pb[i + ld * j] = float(psi[i, j])
+            rb[i + ld * j] = float(rhs[i, j])
+    prog.sub("poisson")(f77.ref(pb), f77.ref(rb), f77.cell(nlev), f77.ref(vb))
+    out = np.array([[pb[i + ld * j] for j in range(n2 + 1)] for i in range(n1 + 1)])
+    return out, sweeps_per_solve(prog.probe["poisson"]), sha256(path)

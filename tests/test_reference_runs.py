@@ -29,7 +29,7 @@ import pytest
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = sorted(f for f in os.listdir(GOLD) if f.startswith("ref_") and f.endswith(".npz")
-               and f != "ref_taycou_16x32.npz")
+               and f not in ("ref_taycou_16x32.npz", "ref_grid_rcsc_64x64.npz"))
 F2D = ["A", "B", "An", "Bn", "Ap", "Cn", "C", "Cp", "thn", "th", "thp", "uel", "vel", "uelp", "velp"]
 
 
@@ -128,3 +128,26 @@ def test_taylor_couette_reference_stops_where_the_oracle_converges(oracle):
     o, nu, sw = run_2d(oracle, m)
     assert np.all(sw > 0) and np.all(sw < 100)
     assert np.all(np.isfinite(nu))
+
+
+def test_oracle_reproduces_grid_tables_and_stretched_multigrid(oracle):
+    """grid.f's own main program (spacings with geometric expansion toward
+    both walls, levels, finite-difference weights of every level, wall
+    weights) and rcsc.f's multigrid on those tables: the oracle's grid and
+    its stretched solve equal them bit for bit."""
+    g, m = load("ref_grid_rcsc_64x64.npz")
+    hr1 = oracle.str_spacing_gef(m["nr"], m["r0"], m["rmax"], m["rdist"], m["rgef"], m["dr1"])
+    hz1 = oracle.str_spacing_gef(m["nz"], m["zmin"], m["zmax"], m["zdist"], m["zgef"], m["dz1"])
+    o = oracle.OracleSTR(hr1, hz1, m["r0"], m["zmin"])
+    assert o.nlev == m["nlev"]
+    np.testing.assert_array_equal(hr1[1:], g["t_hr_1"])
+    np.testing.assert_array_equal(hz1[1:], g["t_hz_1"])
+    for L in range(1, o.nlev + 1):
+        for name in ("r", "z", "cr", "crr", "cz", "czz"):
+            np.testing.assert_array_equal(o.table(name, L), g["t_%s_%d" % (name, L)], err_msg="%s %d" % (name, L))
+    np.testing.assert_array_equal(np.array(o.g.crn), g["t_crn"])
+    np.testing.assert_array_equal(np.array(o.g.czn), g["t_czn"])
+    st, sw, psi = o.poisson(np.zeros_like(g["rhs"]), g["rhs"])
+    assert st == 0
+    assert [sw] == list(g["sweeps"])
+    np.testing.assert_array_equal(psi, g["psi"])
