@@ -1,6 +1,6 @@
 /*
  * CPU oracle: restatement of rotann2.f's axisymmetric rotating-annulus step
- * ("AXI").  TEST INFRASTRUCTURE ONLY; PARITY UNPINNED (see axi_oracle.h).
+ * ("AXI").  TEST INFRASTRUCTURE ONLY; parity as in axi_oracle.h.
  * Every expression keeps the reference's left-to-right evaluation order;
  * build with -ffp-contract=off.
  */

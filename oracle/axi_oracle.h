@@ -6,8 +6,12 @@
  * 9-point restriction, bilinear prolongation, plain V-cycle).
  *
  * TEST INFRASTRUCTURE ONLY: the checker of tests/, smoke() and bench.py's
- * CPU legs; never linked into the product.  PARITY UNPINNED: the reference
- * ships no outputs and no Fortran compiler exists where this was written.
+ * CPU legs; never linked into the product.  PARITY PINNED for the uniform
+ * grid: it reproduces bit for bit rotann2.f run as its main program through
+ * the translator tests/golden/f77.py (tests/test_reference_runs.py).  The
+ * stretched mode composes rotann2.f's physics with grid.f's weights and
+ * rcsc.f's multigrid, which are pinned separately; no reference program
+ * runs that composition.
  * Double precision, the reference's left-to-right order, -ffp-contract=off.
  *
  * Arrays are the reference's (0:nr, 0:nz) arrays, column-major with leading

@@ -1,6 +1,6 @@
 /*
  * CPU oracle for the batched Dirichlet Poisson solve.  TEST INFRASTRUCTURE
- * ONLY (see batch_oracle.h).  PARITY UNPINNED.
+ * ONLY (see batch_oracle.h).  No reference program solves this workload.
  *
  * Transfer operators follow rotann2.f: full-weighting restriction summed in
  * the order of corser (rotann2.f:773-785) and bilinear prolongation with the

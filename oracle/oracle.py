@@ -1,9 +1,12 @@
 """ctypes access to the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-the CPU legs of bench.py, never by the product package.  PARITY UNPINNED:
+the CPU legs of bench.py, never by the product package.  PARITY PINNED:
 the oracle restates the reference Fortran, which cannot be compiled here and
-ships no outputs to compare against.
+ships no outputs; its drivers run instead through the translator
+tests/golden/f77.py, and the oracle reproduces those runs bit for bit
+(tests/test_reference_runs.py).  The batched Poisson workload has no
+reference program.
 """
 from __future__ import annotations
 

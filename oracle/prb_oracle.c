@@ -3,9 +3,16 @@
  * monashubuntudir_velvor2dperiodicrbconvdir/velvor2dperiodicrbconv.f (PRB).
  *
  * TEST INFRASTRUCTURE ONLY -- the checker for tests/, smoke() and the CPU
- * legs of bench.py; never linked into the product.  PARITY UNPINNED: the
- * reference has no tests or stored outputs and cannot be compiled here (no
- * Fortran compiler), so this file is validated by its own invariants only.
+ * legs of bench.py; never linked into the product.  PARITY PINNED to the
+ * reference's own source: with no Fortran compiler in the image, the
+ * reference's drivers are run on the CPU by a translator of their Fortran
+ * (tests/golden/f77.py), and this file reproduces those runs bit for bit —
+ * every field, Nusselt number and sweep count of the layer, its oblique
+ * and annulus variants and the Taylor-Couette driver
+ * (tests/test_reference_runs.py).  The one departure: velvor2dtaycouheat.f
+ * forms a relax2 line's right-hand side only for k = 1 (:2132-2164), so its
+ * first solve STOPs; this file forms every line's, as
+ * velvor2dtaycouheat_new.f:2181-2182 does.
  *
  * Every expression keeps the reference's left-to-right evaluation order.
  * Fortran REAL*4 literals that the reference mixes into REAL*8 arithmetic

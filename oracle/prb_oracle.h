@@ -11,12 +11,17 @@
  * reference's left-to-right operation order, compiled with
  * -ffp-contract=off so that no multiply-add is fused.
  *
- * PARITY UNPINNED: the reference ships no tests, no golden vectors and no
- * stored outputs, and no Fortran compiler exists where this was written, so
- * the restatement is checked only by its own invariants (dense-solve
- * agreement of the banded solvers, manufactured solutions, conduction
- * Nusselt number 1, periodic-seam identities) and by golden fixtures it
- * generated itself.
+ * PARITY PINNED to the reference's own source.  The reference ships no
+ * tests, golden vectors or stored outputs and the image has no Fortran
+ * compiler, so the reference's drivers are run on the CPU by a translator
+ * of their Fortran (tests/golden/f77.py: IEEE binary64 / binary32
+ * arithmetic in source order); this restatement reproduces those runs bit
+ * for bit (tests/test_reference_runs.py), the Taylor-Couette driver with
+ * the relax2 of its newer sibling (velvor2dtaycouheat.f forms a line's
+ * right-hand side only for k = 1 and its first solve STOPs).  Its own
+ * invariants (dense-solve agreement of the banded solvers, manufactured
+ * solutions, conduction Nusselt number 1, periodic-seam identities) are
+ * checked too.
  *
  * Array convention: every field is the reference's (0:kr,1,0:kp) array,
  * stored column-major, element (i,k) at index i + ld*k, 0 <= i <= ld-1,

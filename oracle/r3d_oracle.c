@@ -1,11 +1,12 @@
 /*
  * CPU oracle: restatement of the 3D rotating-annulus hot path of rot3dmg.f
  * (R3D).  TEST INFRASTRUCTURE ONLY -- the checker of tests/, smoke() and the
- * CPU legs of bench.py; never linked into the product.  PARITY UNPINNED:
- * no Fortran compiler and no stored reference outputs exist here, so this
- * file is checked by its own invariants (manufactured solutions of the three
- * velocity operators, the conduction state, agreement of the two line
- * orderings) and by fixtures it generated itself.
+ * CPU legs of bench.py; never linked into the product.  PARITY PINNED: it
+ * reproduces bit for bit rot3dmg.f and rot3dmghor.f run as their main
+ * programs through the translator tests/golden/f77.py (every field, Nusselt
+ * number and sweep count; tests/test_reference_runs.py), besides its own
+ * invariants (manufactured solutions of the three velocity operators, the
+ * conduction state, agreement of the two line orderings).
  *
  * Every expression keeps the reference's left-to-right evaluation order;
  * x**2 is x*x as the Fortran compiler expands it.  Build with

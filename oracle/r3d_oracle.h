@@ -8,8 +8,9 @@
  * trilinear prolongation, plain V-cycle with SOR 1.2).
  *
  * TEST INFRASTRUCTURE ONLY: the checker of tests/, smoke() and bench.py's
- * CPU legs; never linked into the product.  PARITY UNPINNED: the reference
- * ships no outputs and no Fortran compiler exists where this was written.
+ * CPU legs; never linked into the product.  PARITY PINNED to rot3dmg.f and
+ * rot3dmghor.f run through the translator tests/golden/f77.py
+ * (tests/test_reference_runs.py).
  * Double precision, the reference's left-to-right order, -ffp-contract=off;
  * the REAL*4 literal 0.2 of relax1/2/3 (rot3dmg.f:1626, 1634, 1664, 1672,
  * 1800, 1805, 2029, 2034, 2106, 2112) is the float it rounds to.

@@ -1,10 +1,13 @@
 /*
  * CPU oracle: restatement of grid.f's coefficient build and rcsc.f's
  * stretched-grid streamfunction multigrid ("STR").  TEST INFRASTRUCTURE
- * ONLY (the checker; never linked into the product).  PARITY UNPINNED: the
- * reference ships no outputs and no Fortran compiler exists here; checked by
- * its own invariants (exact weights on polynomials, second-order convergence
- * on stretched grids, agreement of the two line orders).
+ * ONLY (the checker; never linked into the product).  PARITY PINNED: its
+ * spacings, levels and weight tables equal grid.f's own main program, and
+ * its multigrid equals rcsc.f's poisson on those tables, bit for bit, both
+ * run through the translator tests/golden/f77.py
+ * (tests/test_reference_runs.py); also checked by its own invariants (exact
+ * weights on polynomials, second-order convergence on stretched grids,
+ * agreement of the two line orders).
  *
  * Every expression keeps the reference's left-to-right order; x**2 is x*x.
  * Build with -ffp-contract=off (see Makefile).

@@ -21,8 +21,9 @@
  *                   STOP after nvs = 10000 sweeps.
  *
  * TEST INFRASTRUCTURE ONLY: the checker of tests/ and bench.py's CPU legs;
- * never linked into the product.  PARITY UNPINNED (no Fortran compiler, no
- * stored outputs).  Double precision, the reference's order,
+ * never linked into the product.  PARITY PINNED to grid.f and rcsc.f run
+ * through the translator tests/golden/f77.py.  Double precision, the
+ * reference's order,
  * -ffp-contract=off.
  *
  * Arrays: psi and rhs are (0:n1, 0:n2) column-major with leading dimension

@@ -4,7 +4,9 @@
  * the 2D layer's scheme closed by side walls at x = 0 and x = xx (3.1).
  *
  * TEST INFRASTRUCTURE ONLY: the checker of tests/; never linked into the
- * product.  PARITY UNPINNED (no Fortran compiler, no stored outputs).
+ * product.  PARITY PINNED: reproduces bit for bit velvor2dhorconvtank.f and
+ * velvor2ddvdbenchmark.f run through the translator tests/golden/f77.py
+ * (tests/test_reference_runs.py).
  * Double precision, the reference's order, -ffp-contract=off; REAL*4
  * literals (1./6., 4./3.) are the floats they round to.
  *
