@@ -12,6 +12,7 @@ Each fixture holds the deck, the driver, the parameters the oracle needs, the
 source file's path and SHA-256, the final fields, the Nusselt history and
 the sweep count of every multigrid solve.
 """
+import hashlib
 import json
 import os
 import sys
@@ -40,6 +41,14 @@ CASES_2D = [
     ("dvd", 16, 32, 4, 2e-5, 0.0, 1.0, 1e5, 0.0, 0.0, 0.71),
     ("taycou", 16, 32, 4, 1e-6, 0.5, 1.0, 1e6, 1e4, 1e4, 0.71),
 ]
+# the input decks shipped beside each driver (input.s: dt, nr, np, r0 rmax,
+# Ra, Re, Gr, Ptl), run for a few steps
+DECKS_2D = [
+    ("layer", 96, 336, 3, 1e-7, 0.5, 1.0, 1e7, 0.0, 0.0, 0.71),
+    ("tank", 128, 128, 3, 5e-8, 0.5, 1.5, 8.63e7, 0.0, 0.0, 10.0),
+    ("dvd", 96, 96, 3, 2e-6, 0.0, 1.0, 1e6, 0.0, 0.0, 0.71),
+    ("annulus", 272, 1200, 1, 2e-8, 0.5, 1.0, 8e8, 1.06148e5, 0.0, 0.71),
+]
 CASES_3D = [
     # driver, nr, nz, np, steps, dt, r0, rmax, zmax, Ra, Re, Gr, Pr, amp, nval
     ("r3d", 8, 8, 16, 2, 1e-5, 0.5, 1.0, 0.5, 1e5, 100.0, 0.0, 0.7, 1e-2, 3),
@@ -53,9 +62,18 @@ CASES_AXI = [
 ]
 
 
-def save(name, res, meta, extra=None):
+def field_digest(a):
+    """SHA-256 of a field's binary64 values in C order (large runs keep
+    digests, not the fields)."""
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def save(name, res, meta, extra=None, digests=False):
     meta = dict(meta, source=res["source"], sha256=res["sha256"], end=res["end"], deck=res.get("deck"))
-    arrays = {"f_" + k: v for k, v in res["fields"].items()}
+    if digests:
+        arrays = {"h_" + k: np.array(field_digest(v)) for k, v in res["fields"].items()}
+    else:
+        arrays = {"f_" + k: v for k, v in res["fields"].items()}
     arrays.update(extra or {})
     np.savez_compressed(os.path.join(HERE, name), meta=np.array(json.dumps(meta)), nu=res["nu"],
                         sweeps=res["sweeps"], **arrays)
@@ -72,6 +90,13 @@ def main():
         meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra,
                     Re=Re, Gr=Gr, Pr=Pr, xx=XX[drv])
         save("ref_%s_%dx%d.npz" % (drv, nr, np_), res, meta)
+    # the decks the reference ships (its own grids, time steps and numbers;
+    # a few steps), fields kept as digests
+    for drv, nr, np_, nts, dt, r0, rmax, Ra, Re, Gr, Pr in DECKS_2D:
+        res = RR.run_2d(drv, nr, np_, nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr)
+        meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra,
+                    Re=Re, Gr=Gr, Pr=Pr, xx=XX[drv], deck_of="input.s")
+        save("ref_%s_deck_%dx%d.npz" % (drv, nr, np_), res, meta, digests=True)
     # the Taylor-Couette driver as written STOPs in its first v solve (its
     # relax2 forms a line's right-hand side only for k = 1); the same
     # program with relax2 taken from velvor2dtaycouheat_new.f, which forms

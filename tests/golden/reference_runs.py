@@ -164,7 +164,7 @@ def run_2d(driver, nr, np_, nts, replace=None, **kw):
     end = run_main(prog)
     ncol = np_ + 2 if driver in ("tank", "dvd") else np_ + 1
     out = {f: extract(prog, f, [(0, nr + 1), (1, 1), (0, ncol - 1)]) for f in FIELDS_2D}
-    nu = np.stack([extract(prog, h, [(1, nts)]) for h in ("httrans", "httrans2")], axis=1)
+    nu = np.stack([extract(prog, h, [(1, nts)]).reshape(nts) for h in ("httrans", "httrans2")], axis=1)
     return dict(fields=out, nu=nu, sweeps=sweep_table(prog, DRIVERS[driver][1]), end=end, deck=deck,
                 source=DRIVERS[driver][0], sha256=sha256(source(driver)))
 
@@ -175,7 +175,7 @@ def run_3d(driver, nr, nz, np_, nts, **kw):
     end = run_main(prog)
     out = {f: extract(prog, f, [(0, nr + 1), (0, nz + 1), (0, np_)]) for f in FIELDS_3D}
     names = ("httrans1", "httrans2") if driver == "r3d_hor" else ("httrans",)
-    nu = np.stack([extract(prog, h, [(1, nts)]) for h in names], axis=1)
+    nu = np.stack([extract(prog, h, [(1, nts)]).reshape(nts) for h in names], axis=1)
     return dict(fields=out, nu=nu, sweeps=sweep_table(prog, DRIVERS[driver][1]), end=end, deck=deck,
                 source=DRIVERS[driver][0], sha256=sha256(source(driver)))
 

@@ -21,6 +21,7 @@ as velvor2dtaycouheat_new.f does (:2181-2182, after the block): it
 reproduces velvor2dtaycouheat.f run with that one subroutine taken from
 velvor2dtaycouheat_new.f (ref_taycou_relax2new_*.npz), and the last test
 records that the program as written stops."""
+import hashlib
 import json
 import os
 
@@ -31,6 +32,10 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = sorted(f for f in os.listdir(GOLD) if f.startswith("ref_") and f.endswith(".npz")
                and f not in ("ref_taycou_16x32.npz", "ref_grid_rcsc_64x64.npz"))
 F2D = ["A", "B", "An", "Bn", "Ap", "Cn", "C", "Cp", "thn", "th", "thp", "uel", "vel", "uelp", "velp"]
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
 
 
 def load(name):
@@ -64,7 +69,10 @@ def test_oracle_reproduces_reference_run(oracle, case):
             o, nu, sw = run_2d(oracle, m)
             names = F2D
         for f in names:
-            np.testing.assert_array_equal(np.array(o.field(f)), g["f_" + f], err_msg=f)
+            if "h_" + f in g.files:      # large runs keep SHA-256 digests of the fields
+                assert digest(o.field(f)) == str(g["h_" + f]), f
+            else:
+                np.testing.assert_array_equal(np.array(o.field(f)), g["f_" + f], err_msg=f)
     elif drv in ("r3d", "r3d_hor"):
         o = oracle.OracleR3D(m["nr"], m["nz"], m["np"], m["dt"], m["r0"], m["rmax"], m["zmax"], m["Ra"], m["Re"],
                              m["Pr"], Gr=m["Gr"], horizontal=drv == "r3d_hor")
