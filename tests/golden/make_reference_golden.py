@@ -59,7 +59,11 @@ CASES_AXI = [
     # nr, nz, steps, dt, r0, rmax, zmax, Ra, Re, Pr
     (16, 16, 5, 1e-5, 0.5, 1.0, 0.5, 1e5, 1e2, 1.0),
     (32, 64, 5, 1e-6, 0.5, 1.0, 1.0, 1e6, 1e2, 1.0),
+    (128, 128, 3, 1e-6, 0.5, 1.0, 0.5, 1e6, 1e2, 1.0),   # rotann2.f's largest grid (nrmax = 128)
 ]
+# the 3D annulus at half the benchmark's grid in each direction (one step;
+# the translated program needs about five minutes for it)
+LARGE_3D = [("r3d", 32, 32, 64, 1, 1e-5, 0.5, 1.0, 0.5, 1e6, 500.0, 0.0, 7.0, 1e-3, 3)]
 
 
 def field_digest(a):
@@ -126,10 +130,16 @@ def main():
         meta = dict(driver=drv, nr=nr, nz=nz, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re,
                     Gr=Gr, Pr=Pr, amp=amp, nval=nval)
         save("ref_%s_%dx%dx%d.npz" % (drv, nr, nz, np_), res, meta)
+    for drv, nr, nz, np_, nts, dt, r0, rmax, zmax, Ra, Re, Gr, Pr, amp, nval in LARGE_3D:
+        res = RR.run_3d(drv, nr, nz, np_, nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr,
+                        amp=amp, nval=nval)
+        meta = dict(driver=drv, nr=nr, nz=nz, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re,
+                    Gr=Gr, Pr=Pr, amp=amp, nval=nval)
+        save("ref_%s_%dx%dx%d.npz" % (drv, nr, nz, np_), res, meta, digests=True)
     for nr, nz, nts, dt, r0, rmax, zmax, Ra, Re, Pr in CASES_AXI:
         res = RR.run_axi(nr, nz, nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Pr=Pr)
         meta = dict(driver="axi", nr=nr, nz=nz, steps=nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Pr=Pr)
-        save("ref_axi_%dx%d.npz" % (nr, nz), res, meta)
+        save("ref_axi_%dx%d.npz" % (nr, nz), res, meta, digests=nr * nz > 10000)
     # grid.f's stretched levels and weight tables, and rcsc.f's multigrid on
     # them (the stretched streamfunction solve of the annulus on a tanh
     # or GEF grid)

@@ -38,6 +38,20 @@ def digest(a):
     return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
 
 
+def check_fields(g, field, view=lambda a: a):
+    """Every field the fixture holds, as an array (f_*) or as a SHA-256
+    digest of its binary64 values (h_*, the large runs)."""
+    n = 0
+    for key in g.files:
+        if key.startswith("f_"):
+            np.testing.assert_array_equal(view(np.array(field(key[2:]))), g[key], err_msg=key)
+            n += 1
+        elif key.startswith("h_"):
+            assert digest(view(np.array(field(key[2:])))) == str(g[key]), key
+            n += 1
+    assert n > 0
+
+
 def load(name):
     g = np.load(os.path.join(GOLD, name))
     return g, json.loads(str(g["meta"]))
@@ -64,15 +78,9 @@ def test_oracle_reproduces_reference_run(oracle, case):
     if drv in ("layer", "oblique", "annulus", "tank", "dvd", "taycou", "layer_routines"):
         if drv == "layer_routines":
             o, nu, sw = run_2d(oracle, m, 1, m["init"]["seed"], m["init"]["amp"])
-            names = F2D + ["urh", "vrh"]
         else:
             o, nu, sw = run_2d(oracle, m)
-            names = F2D
-        for f in names:
-            if "h_" + f in g.files:      # large runs keep SHA-256 digests of the fields
-                assert digest(o.field(f)) == str(g["h_" + f]), f
-            else:
-                np.testing.assert_array_equal(np.array(o.field(f)), g["f_" + f], err_msg=f)
+        check_fields(g, o.field)
     elif drv in ("r3d", "r3d_hor"):
         o = oracle.OracleR3D(m["nr"], m["nz"], m["np"], m["dt"], m["r0"], m["rmax"], m["zmax"], m["Ra"], m["Re"],
                              m["Pr"], Gr=m["Gr"], horizontal=drv == "r3d_hor")
@@ -84,9 +92,7 @@ def test_oracle_reproduces_reference_run(oracle, case):
             nus.append([n1, o.nu2] if drv == "r3d_hor" else [n1])
             sws.append(s.copy())
         nu, sw = np.array(nus), np.array(sws)
-        for f in g.files:
-            if f.startswith("f_"):
-                np.testing.assert_array_equal(np.array(o.field(f[2:])), g[f], err_msg=f)
+        check_fields(g, o.field)
     else:
         assert drv == "axi"
         o = oracle.OracleAXI(m["nr"], m["nz"], m["dt"], m["r0"], m["rmax"], m["zmax"], m["Ra"], m["Re"], m["Pr"])
@@ -100,9 +106,7 @@ def test_oracle_reproduces_reference_run(oracle, case):
             if conv:
                 break
         nu, sw = np.array(nus), np.array(sws)
-        for f in g.files:
-            if f.startswith("f_"):
-                np.testing.assert_array_equal(np.array(o.field(f[2:]))[:m["nr"] + 1, :m["nz"] + 1], g[f], err_msg=f)
+        check_fields(g, o.field, lambda a: a[:m["nr"] + 1, :m["nz"] + 1])
     np.testing.assert_array_equal(nu, g["nu"])
     np.testing.assert_array_equal(sw, g["sweeps"])
 
