@@ -7,7 +7,9 @@ the reference's own source.
 
 Reads the reference source tree (GB300_REFERENCE_SOURCE, default
 /root/reference).  Run from the repository root:
-    python tests/golden/make_reference_golden.py
+    python tests/golden/make_reference_golden.py [driver ...]
+(all drivers, or only those named: layer oblique annulus tank dvd taycou
+layer_routines r3d r3d_hor axi grid_rcsc).
 Each fixture holds the deck, the driver, the parameters the oracle needs, the
 source file's path and SHA-256, the final fields, the Nusselt history and
 the sweep count of every multigrid solve.
@@ -60,6 +62,7 @@ CASES_AXI = [
     (16, 16, 5, 1e-5, 0.5, 1.0, 0.5, 1e5, 1e2, 1.0),
     (32, 64, 5, 1e-6, 0.5, 1.0, 1.0, 1e6, 1e2, 1.0),
     (128, 128, 3, 1e-6, 0.5, 1.0, 0.5, 1e6, 1e2, 1.0),   # rotann2.f's largest grid (nrmax = 128)
+    (8, 8, 400, 1e-3, 0.5, 1.0, 0.5, 0.0, 1.0, 1.0),      # runs to the steady-state stop (:182-194)
 ]
 # the 3D annulus at half the benchmark's grid in each direction (one step;
 # the translated program needs about five minutes for it)
@@ -85,11 +88,17 @@ def save(name, res, meta, extra=None, digests=False):
                                                             res["sweeps"][-1]), flush=True)
 
 
-def main():
+def main(only=()):
+    """only: driver names to regenerate (all when empty)."""
     from oracle import oracle as O
     O.build()
     t0 = time.time()
+
+    def want(drv):
+        return not only or drv in only
     for drv, nr, np_, nts, dt, r0, rmax, Ra, Re, Gr, Pr in CASES_2D:
+        if not want(drv):
+            continue
         res = RR.run_2d(drv, nr, np_, nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr)
         meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra,
                     Re=Re, Gr=Gr, Pr=Pr, xx=XX[drv])
@@ -97,6 +106,8 @@ def main():
     # the decks the reference ships (its own grids, time steps and numbers;
     # a few steps), fields kept as digests
     for drv, nr, np_, nts, dt, r0, rmax, Ra, Re, Gr, Pr in DECKS_2D:
+        if not want(drv):
+            continue
         res = RR.run_2d(drv, nr, np_, nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr)
         meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra,
                     Re=Re, Gr=Gr, Pr=Pr, xx=XX[drv], deck_of="input.s")
@@ -107,10 +118,13 @@ def main():
     # every line's, is what the oracle restates
     drv, nr, np_, nts, dt, r0, rmax, Ra, Re, Gr, Pr = CASES_2D[-1]
     rep = {"relax2": "monashubuntudir_velvor2dtaycouheatdir/velvor2dtaycouheat_new.f"}
-    res = RR.run_2d(drv, nr, np_, nts, replace=rep, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr)
-    meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re,
-                Gr=Gr, Pr=Pr, xx=XX[drv], replace=rep)
-    save("ref_taycou_relax2new_%dx%d.npz" % (nr, np_), res, meta)
+    if want(drv):
+        res = RR.run_2d(drv, nr, np_, nts, replace=rep, dt=dt, r0=r0, rmax=rmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr)
+        meta = dict(driver=drv, variant=VARIANT[drv], nr=nr, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, Ra=Ra,
+                    Re=Re, Gr=Gr, Pr=Pr, xx=XX[drv], replace=rep)
+        save("ref_taycou_relax2new_%dx%d.npz" % (nr, np_), res, meta)
+    if not want("layer_routines"):
+        return main_3d(only, want, t0)
     # the layer at the 129 x 65 grid of the benchmark's layer workload (box
     # length 2, seeded start), routine by routine in the main loop's order
     cfg = dict(nr=64, np_=128, dt=1e-5, Ra=1e5, Pr=1.0, r0=0.0, rmax=1.0, xx=2.0)
@@ -124,25 +138,38 @@ def main():
                 r0=cfg["r0"], rmax=cfg["rmax"], Ra=cfg["Ra"], Re=0.0, Gr=0.0, Pr=cfg["Pr"], xx=cfg["xx"],
                 init=dict(kind=1, seed=0, amp=1e-2))
     save("ref_layer_routines_64x128.npz", res, meta)
+    return main_3d(only, want, t0)
+
+
+def main_3d(only, want, t0):
     for drv, nr, nz, np_, nts, dt, r0, rmax, zmax, Ra, Re, Gr, Pr, amp, nval in CASES_3D:
+        if not want(drv):
+            continue
         res = RR.run_3d(drv, nr, nz, np_, nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr,
                         amp=amp, nval=nval)
         meta = dict(driver=drv, nr=nr, nz=nz, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re,
                     Gr=Gr, Pr=Pr, amp=amp, nval=nval)
         save("ref_%s_%dx%dx%d.npz" % (drv, nr, nz, np_), res, meta)
     for drv, nr, nz, np_, nts, dt, r0, rmax, zmax, Ra, Re, Gr, Pr, amp, nval in LARGE_3D:
+        if not want(drv):
+            continue
         res = RR.run_3d(drv, nr, nz, np_, nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Gr=Gr, Pr=Pr,
                         amp=amp, nval=nval)
         meta = dict(driver=drv, nr=nr, nz=nz, np=np_, steps=nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re,
                     Gr=Gr, Pr=Pr, amp=amp, nval=nval)
         save("ref_%s_%dx%dx%d.npz" % (drv, nr, nz, np_), res, meta, digests=True)
     for nr, nz, nts, dt, r0, rmax, zmax, Ra, Re, Pr in CASES_AXI:
+        if not want("axi"):
+            continue
         res = RR.run_axi(nr, nz, nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Pr=Pr)
         meta = dict(driver="axi", nr=nr, nz=nz, steps=nts, dt=dt, r0=r0, rmax=rmax, zmax=zmax, Ra=Ra, Re=Re, Pr=Pr)
         save("ref_axi_%dx%d.npz" % (nr, nz), res, meta, digests=nr * nz > 10000)
     # grid.f's stretched levels and weight tables, and rcsc.f's multigrid on
     # them (the stretched streamfunction solve of the annulus on a tanh
     # or GEF grid)
+    if not want("grid_rcsc"):
+        print("fixtures written to %s in %.0f s" % (HERE, time.time() - t0))
+        return
     g = dict(nr=64, nz=64, r0=0.5, rmax=1.0, zmax=0.5, zmin=0.0, rdist=0.1, rgef=1.1, dr1=0.002, zdist=0.1,
              zgef=1.1, dz1=0.002)
     gprog, res = RR.run_grid(**g)
@@ -160,4 +187,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(set(sys.argv[1:]))

@@ -111,6 +111,11 @@ def test_oracle_reproduces_reference_run(oracle, case):
     np.testing.assert_array_equal(sw, g["sweeps"])
 
 
+def test_axisymmetric_run_reaches_the_steady_state_stop():
+    g, m = load("ref_axi_8x8.npz")
+    assert len(g["nu"]) < m["steps"]       # rotann2.f's convergence exit (:182-194) ended the loop
+
+
 def test_reference_runs_cover_the_drivers():
     drivers = {load(c)[1]["driver"] for c in CASES}
     assert drivers >= {"layer", "oblique", "annulus", "tank", "dvd", "taycou", "layer_routines", "r3d", "r3d_hor",
