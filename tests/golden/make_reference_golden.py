@@ -62,7 +62,7 @@ CASES_AXI = [
     (16, 16, 5, 1e-5, 0.5, 1.0, 0.5, 1e5, 1e2, 1.0),
     (32, 64, 5, 1e-6, 0.5, 1.0, 1.0, 1e6, 1e2, 1.0),
     (128, 128, 3, 1e-6, 0.5, 1.0, 0.5, 1e6, 1e2, 1.0),   # rotann2.f's largest grid (nrmax = 128)
-    (8, 8, 400, 1e-3, 0.5, 1.0, 0.5, 0.0, 1.0, 1.0),      # runs to the steady-state stop (:182-194)
+    (8, 8, 400, 1e-3, 0.5, 1.0, 0.5, 0.0, 1.0, 1.0),      # runs to the steady-state stop (:191-194)
 ]
 # the 3D annulus at half the benchmark's grid in each direction (one step;
 # the translated program needs about five minutes for it)

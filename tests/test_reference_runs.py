@@ -113,7 +113,7 @@ def test_oracle_reproduces_reference_run(oracle, case):
 
 def test_axisymmetric_run_reaches_the_steady_state_stop():
     g, m = load("ref_axi_8x8.npz")
-    assert len(g["nu"]) < m["steps"]       # rotann2.f's convergence exit (:182-194) ended the loop
+    assert len(g["nu"]) < m["steps"]       # rotann2.f's convergence exit (:191-194) ended the loop
 
 
 def test_reference_runs_cover_the_drivers():
