@@ -289,6 +289,12 @@ def _prb_mixed_instance(cfg, smoother):
     return g
 
 
+# the CPU oracle that the layer and 3D baselines time equals the reference's
+# own Fortran, run on the CPU through a translator of it, bit for bit
+PORT_PINNED = ("bit-identical to the reference's Fortran run through a translator of it "
+               "(tests/test_reference_runs.py)")
+
+
 def prb_latency_model(cfg, precision, warmup=20, reps=5):
     """Where a 2D driver step's time goes: after `warmup` graph steps, `reps`
     steps run routine by routine (the reference's loop order, PRB:363-388),
@@ -417,7 +423,7 @@ def prb_summary(cfg, steps_zebra, steps_lex, warmup, cpu_budget):
         v, n, dt = time_prb_cpu(cfg, 0, cpu_budget)
         out["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
                                "sample": "%d steps of the same instance, oracle LEX (the reference schedule), "
-                                         "1 thread, %.1f s" % (n, dt)}
+                                         "1 thread, %.1f s" % (n, dt), "port_fidelity": PORT_PINNED}
     return out
 
 
@@ -555,7 +561,11 @@ def axi_summary(cfg, steps, steps_lex, warmup, cpu_budget):
         out["cpu_baseline"] = {"value": (cfg["nr"] + 1) * (cfg["nz"] + 1) * n / dt, "unit": "cell-updates/s",
                                "cores": 1, "kind": "port",
                                "sample": "%d steps of the same instance, oracle in the reference's line order, "
-                                         "1 thread, %.1f s; %s" % (n, dt, cpu_model())}
+                                         "1 thread, %.1f s; %s" % (n, dt, cpu_model()),
+                               "port_fidelity": "rotann2.f's physics on grid.f's weights with rcsc.f's multigrid: "
+                                                "the parts equal the reference's Fortran bit for bit "
+                                                "(tests/test_reference_runs.py); no reference program runs "
+                                                "the composition"}
     return out
 
 
@@ -695,7 +705,8 @@ def r3d_summary(cfg, steps, steps_fp64, warmup, cpu_budget):
         out["cpu_baseline"] = {"value": cfg["nr"] * cfg["nz"] * cfg["np"] * n / dt, "unit": "cell-updates/s",
                                "cores": 1, "kind": "port",
                                "sample": "%d step(s) of the same instance from the same start, oracle in the "
-                                         "reference's line order, 1 thread, %.1f s; %s" % (n, dt, cpu_model())}
+                                         "reference's line order, 1 thread, %.1f s; %s" % (n, dt, cpu_model()),
+                               "port_fidelity": PORT_PINNED}
     return out
 
 
