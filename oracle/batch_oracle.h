@@ -3,8 +3,10 @@
  * problems of uneven size, V(nu1,nu2) red-black Gauss-Seidel cycles).
  *
  * TEST INFRASTRUCTURE ONLY: the checker of tests/, smoke() and the CPU legs
- * of bench.py.  No reference driver solves this workload, so no run of the
- * reference pins it;
+ * of bench.py.  No reference driver solves this workload; its FP64 grid
+ * transfers equal rotann2.f's corser and finer run through the translator
+ * tests/golden/f77.py (tests/test_reference_runs.py), while the smoother
+ * and residual below have no reference counterpart;
  * the grid transfer operators restate the vertex-centred multigrid of
  * rotann2.f (corser rotann2.f:755-801, finer rotann2.f:803-854) with the
  * radial terms dropped, and the smoother is point red-black Gauss-Seidel.

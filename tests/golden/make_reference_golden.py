@@ -9,7 +9,7 @@ Reads the reference source tree (GB300_REFERENCE_SOURCE, default
 /root/reference).  Run from the repository root:
     python tests/golden/make_reference_golden.py [driver ...]
 (all drivers, or only those named: layer oblique annulus tank dvd taycou
-layer_routines r3d r3d_hor axi grid_rcsc).
+layer_routines r3d r3d_hor axi transfer grid_rcsc).
 Each fixture holds the deck, the driver, the parameters the oracle needs, the
 source file's path and SHA-256, the final fields, the Nusselt history and
 the sweep count of every multigrid solve.
@@ -167,6 +167,22 @@ def main_3d(only, want, t0):
     # grid.f's stretched levels and weight tables, and rcsc.f's multigrid on
     # them (the stretched streamfunction solve of the annulus on a tanh
     # or GEF grid)
+    if want("transfer"):
+        # the batched solve's grid transfers against rotann2.f's corser and
+        # finer (the batched workload has no reference program of its own)
+        n = 33
+        rng = np.random.default_rng(9)
+        r = rng.standard_normal((n, n))
+        nc = (n - 1) // 2 + 1
+        ec = rng.standard_normal((nc, nc))
+        psi = rng.standard_normal((n, n))
+        for a in (r, ec, psi):
+            a[0, :] = a[-1, :] = a[:, 0] = a[:, -1] = 0.0
+        fc, psi2, sha = RR.run_rotann2_transfer(n, r, ec, psi)
+        meta = dict(driver="transfer", n=n, source="rotann2.f", sha256=sha, end="return")
+        np.savez_compressed(os.path.join(HERE, "ref_transfer_rotann2_33.npz"), meta=np.array(json.dumps(meta)),
+                            r=r, ec=ec, psi=psi, fc=fc, psi_out=psi2)
+        print("ref_transfer_rotann2_33.npz        transfer", flush=True)
     if not want("grid_rcsc"):
         print("fixtures written to %s in %.0f s" % (HERE, time.time() - t0))
         return

@@ -312,3 +312,40 @@ def run_rcsc_poisson(grid_prog, nlev, psi, rhs):
     prog.sub("poisson")(f77.ref(pb), f77.ref(rb), f77.cell(nlev), f77.ref(vb))
     out = np.array([[pb[i + ld * j] for j in range(n2 + 1)] for i in range(n1 + 1)])
     return out, sweeps_per_solve(prog.probe["poisson"]), sha256(path)
+
+
+def run_rotann2_transfer(n, r, ec, psi):
+    """rotann2.f's corser (:755-801) and finer (:803-854) between a level of
+    n x n vertices (n - 1 intervals each way) and the next coarser: the
+    residual r restricted to the coarse grid, and the coarse correction ec
+    prolonged and added to psi.  Arrays are indexed [j, i] (i fastest, as
+    the batched oracle stores them); returns (coarse right-hand side, psi)."""
+    path = os.path.join(REFERENCE, "rotann2.f")
+    prog = f77.Program(path)
+    cm = prog.common_member
+    u = prog.units["corser"]
+    ld = u.const_eval(("name", "kr"))[1] + 1
+    m, mc = n - 1, (n - 1) // 2
+    for name, vals in (("n1", (m, mc)), ("n2", (m, mc)), ("ibeg", (1, 1 + n * n + 1))):
+        buf = cm("ints", name)
+        for k, v in enumerate(vals):
+            buf[k] = v
+    cm("ints", "nlev")[0] = 2
+    rc = cm("arrays", "rc")
+    for j in range(n):
+        for i in range(n):
+            rc[i + ld * j] = float(r[j, i])
+    prog.sub("corser")(f77.cell(1))
+    fc = np.array([[rc[i + ld * j] for i in range(mc + 1)] for j in range(mc + 1)])
+    v = cm("backup", "v")
+    nc = mc + 1
+    for j in range(nc):
+        for i in range(nc):
+            v[(1 + n * n + 1) - 1 + i + nc * j] = float(ec[j, i])
+    for j in range(n):
+        for i in range(n):
+            v[1 - 1 + i + n * j] = float(psi[j, i])
+    prog.sub("finer")(f77.cell(2))
+    psif = cm("arrays", "psif")
+    out = np.array([[psif[i + ld * j] for i in range(n)] for j in range(n)])
+    return fc, out, sha256(path)

@@ -30,7 +30,7 @@ import pytest
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = sorted(f for f in os.listdir(GOLD) if f.startswith("ref_") and f.endswith(".npz")
-               and f not in ("ref_taycou_16x32.npz", "ref_grid_rcsc_64x64.npz"))
+               and f not in ("ref_taycou_16x32.npz", "ref_grid_rcsc_64x64.npz", "ref_transfer_rotann2_33.npz"))
 F2D = ["A", "B", "An", "Bn", "Ap", "Cn", "C", "Cp", "thn", "th", "thp", "uel", "vel", "uelp", "velp"]
 
 
@@ -168,3 +168,23 @@ def test_oracle_reproduces_grid_tables_and_stretched_multigrid(oracle):
     assert st == 0
     assert [sw] == list(g["sweeps"])
     np.testing.assert_array_equal(psi, g["psi"])
+
+
+def test_batched_grid_transfers_are_rotann2s(oracle):
+    """The batched solve has no reference program; its grid transfers are
+    rotann2.f's: full weighting in corser's order and bilinear prolongation
+    with finer's corner sum, then the correction added.  The oracle's FP64
+    transfers equal those subroutines run through the translator."""
+    import ctypes as C
+    g, m = load("ref_transfer_rotann2_33.npz")
+    n = m["n"]
+    nc = (n - 1) // 2 + 1
+    dp = C.POINTER(C.c_double)
+    r = np.ascontiguousarray(g["r"])
+    fc = np.zeros((nc, nc))
+    oracle.lib().orc_restrict64(n, r.ctypes.data_as(dp), fc.ctypes.data_as(dp))
+    np.testing.assert_array_equal(fc, g["fc"])
+    psi = np.ascontiguousarray(g["psi"]).copy()
+    ec = np.ascontiguousarray(g["ec"])
+    oracle.lib().orc_prolong_add64(n, ec.ctypes.data_as(dp), psi.ctypes.data_as(dp))
+    np.testing.assert_array_equal(psi, g["psi_out"])
