@@ -188,3 +188,27 @@ def test_batched_grid_transfers_are_rotann2s(oracle):
     ec = np.ascontiguousarray(g["ec"])
     oracle.lib().orc_prolong_add64(n, ec.ctypes.data_as(dp), psi.ctypes.data_as(dp))
     np.testing.assert_array_equal(psi, g["psi_out"])
+
+
+def test_fixtures_regenerate_from_the_reference_source():
+    """Provenance: where the reference source tree is present, the
+    translator run again gives the committed fixtures exactly (the source
+    file's SHA-256 included).  Skipped where the tree is absent."""
+    import sys
+    sys.path.insert(0, GOLD)
+    import reference_runs as RR
+    if not os.path.isdir(RR.REFERENCE):
+        pytest.skip("reference source tree not present")
+    g, m = load("ref_layer_16x48.npz")
+    res = RR.run_2d("layer", m["nr"], m["np"], m["steps"], dt=m["dt"], r0=m["r0"], rmax=m["rmax"], Ra=m["Ra"],
+                    Re=m["Re"], Gr=m["Gr"], Pr=m["Pr"])
+    assert res["sha256"] == m["sha256"] and res["deck"] == m["deck"]
+    np.testing.assert_array_equal(res["nu"], g["nu"])
+    np.testing.assert_array_equal(res["sweeps"], g["sweeps"])
+    for f, a in res["fields"].items():
+        np.testing.assert_array_equal(a, g["f_" + f], err_msg=f)
+    g, m = load("ref_transfer_rotann2_33.npz")
+    fc, psi, sha = RR.run_rotann2_transfer(m["n"], g["r"], g["ec"], g["psi"])
+    assert sha == m["sha256"]
+    np.testing.assert_array_equal(fc, g["fc"])
+    np.testing.assert_array_equal(psi, g["psi_out"])
