@@ -157,3 +157,48 @@ def test_real4_decimal_rounding_ties():
     assert f77.dec_to_r4("0.1") == float(np.float32(0.1))
     assert f77.dec_to_r4("16777217") == 16777216.0        # halfway: to the even neighbour
     assert f77.dec_to_r4("16777219") == 16777220.0
+
+
+def test_functions_nested_loop_exits_and_stubs(tmp_path):
+    src = col6("subroutine s(n, x)",
+               "implicit real*8(a-h,o-z)",
+               "n=0",
+               "do 10 i=1,5",
+               "do 10 j=1,5",
+               "n=n+1",
+               "if(i*j.eq.6)goto 20",
+               ("10", "continue"),
+               "n=-1",
+               ("20", "continue"),
+               "call plot(n)",
+               "x=twice(dble(n))",
+               "return",
+               "end",
+               "double precision function twice(a)",
+               "implicit real*8(a-h,o-z)",
+               "twice=2.d0*a",
+               "return",
+               "end",
+               "subroutine plot(n)",
+               "n=12345",
+               "return",
+               "end")
+    P = prog(tmp_path, src, stubs=("plot",))
+    c = [f77.cell(0), f77.cell(0.0)]
+    P.sub("s")(*c)
+    # (i, j) = (2, 3) is the first product 6 in loop order: 5 + 3 iterations; the
+    # GOTO leaves both loops and skips n=-1; the stubbed plot leaves n alone
+    assert c[0][0][0] == 8
+    assert c[1][0][0] == 16.0
+
+
+def test_replace_takes_a_routine_from_a_sibling_file(tmp_path):
+    a = tmp_path / "a.f"
+    b = tmp_path / "b.f"
+    a.write_text(col6("subroutine top(x)", "real*8 x", "call leaf(x)", "return", "end",
+                      "subroutine leaf(x)", "real*8 x", "x=1.d0", "return", "end"))
+    b.write_text(col6("subroutine leaf(x)", "real*8 x", "x=2.d0", "return", "end"))
+    P = f77.Program(str(a), replace={"leaf": str(b)})
+    c = f77.cell(0.0)
+    P.sub("top")(c)
+    assert c[0][0] == 2.0
