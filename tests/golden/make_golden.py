@@ -1,8 +1,9 @@
 """Regenerates the golden fixtures of tests/golden/ from the CPU oracle.
 
-The reference ships no outputs and cannot be compiled here, so these
-fixtures pin the oracle (and through it the device path) against
-regressions; they are not reference outputs.  Run from the repository root:
+These fixtures pin the oracle (and through it the device path) against
+regressions; they are the oracle's outputs.  The reference's own outputs,
+from its Fortran run through the translator f77.py, are the ref_*.npz
+fixtures that make_reference_golden.py writes.  Run from the repository root:
     python tests/golden/make_golden.py
 """
 import os

@@ -1,6 +1,7 @@
-"""The committed fixtures of tests/golden/ (generated by make_golden.py from
-the oracle) reproduced exactly: by the oracle on the CPU (a regression pin,
-since the reference has no outputs of its own) and by the device path."""
+"""The committed fixtures of tests/golden/ generated by make_golden.py from
+the oracle, reproduced exactly: by the oracle on the CPU (a regression pin)
+and by the device path.  The reference's own runs (ref_*.npz) are checked
+in test_reference_runs.py and test_gpu_reference_runs.py."""
 import os
 
 import numpy as np
