@@ -7,9 +7,12 @@ fixed-form Fortran 77 with IEEE binary64 / binary32 arithmetic in source
 order), written by tests/golden/make_reference_golden.py.  The oracle run
 on the same parameters must reproduce every field, every Nusselt number and
 every multigrid sweep count bit for bit: the 2D layer, its oblique-gravity,
-rotating-annulus, tank and cavity variants, the 3D annulus (vertical and
-horizontal) and the axisymmetric annulus.  The device path is tied to the
-oracle bit for bit by the parity tests, so these fixtures pin it too.
+rotating-annulus, tank and cavity variants (also on the decks the reference
+ships), the 3D annulus (vertical and horizontal), the axisymmetric annulus,
+grid.f's stretched tables with rcsc.f's multigrid on them, and the batched
+solve's grid transfers (rotann2.f's corser and finer).  The device path is
+tied to the oracle bit for bit by the parity tests, so these fixtures pin it
+too; test_gpu_reference_runs.py replays the 2D runs on the device directly.
 
 The Taylor-Couette driver (velvor2dtaycouheat.f) is the one the oracle does
 not follow to the letter: its relax2 forms a line's pentadiagonal right-hand
